@@ -1,0 +1,194 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Loads ``liboracle_f32.so`` / ``liboracle_f64.so`` (built by ``oracle/Makefile``)
+and runs scenes from :mod:`playrho_gb300.scenes` through the restated world step.
+Only tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+CONF_REAL_FIELDS = (
+    "deltaTime", "dtRatio", "minStillTimeToSleep", "linearSlop", "angularSlop",
+    "regResolutionRate", "regMinSeparation", "regMinMomentum", "velocityThreshold",
+    "maxTranslation", "maxRotation", "maxLinearCorrection", "maxAngularCorrection",
+    "linearSleepTolerance", "angularSleepTolerance", "displaceMultiplier", "aabbExtension",
+    "maxCirclesRatio")
+CONF_INT_FIELDS = ("regVelocityIters", "regPositionIters", "doWarmStart", "doBlocksolve")
+STATS_INT_FIELDS = (
+    "preProxiesCreated", "preProxiesMoved", "preContactsDestroyed", "preContactsAdded",
+    "preContactsUpdated", "regIslandsFound", "regIslandsSolved", "regContactsAdded",
+    "regContactsUpdated", "regProxiesMoved", "regBodiesSlept", "regSumPosIters", "regSumVelIters")
+
+
+def build() -> None:
+    """Compiles the oracle libraries in place (gcc, a few seconds)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_LIBS = {}
+
+
+def _lib(double: bool):
+    key = bool(double)
+    if key in _LIBS:
+        return _LIBS[key]
+    path = os.path.join(HERE, "liboracle_f64.so" if double else "liboracle_f32.so")
+    if not os.path.exists(path):
+        build()
+    lib = ctypes.CDLL(path)
+    real = ctypes.c_double if double else ctypes.c_float
+
+    class Conf(ctypes.Structure):
+        _fields_ = [(n, real) for n in CONF_REAL_FIELDS] + [(n, ctypes.c_int) for n in CONF_INT_FIELDS]
+
+    class Stats(ctypes.Structure):
+        _fields_ = [(n, ctypes.c_int) for n in STATS_INT_FIELDS] + [
+            ("regMinSeparation", real), ("regMaxIncImpulse", real)]
+
+    P = ctypes.c_void_p
+    lib.or_world_create.restype = P
+    lib.or_world_destroy.argtypes = [P]
+    lib.or_add_body.argtypes = [P, ctypes.c_int] + [real] * 11 + [ctypes.c_uint]
+    lib.or_add_body.restype = ctypes.c_int
+    lib.or_add_shape.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                 real, real, real, real, ctypes.c_uint, ctypes.c_uint, ctypes.c_int, ctypes.c_int]
+    lib.or_add_shape.restype = ctypes.c_int
+    lib.or_reset_mass.argtypes = [P, ctypes.c_int]
+    lib.or_add_revolute.argtypes = [P, ctypes.c_int, ctypes.c_int] + [real] * 5 + [
+        ctypes.c_int, real, real, ctypes.c_int, real, real, ctypes.c_int]
+    lib.or_add_revolute.restype = ctypes.c_int
+    lib.or_default_conf.argtypes = [ctypes.POINTER(Conf)]
+    lib.or_step.argtypes = [P, ctypes.POINTER(Conf), ctypes.POINTER(Stats)]
+    lib.or_body_count.argtypes = [P]
+    lib.or_body_count.restype = ctypes.c_int
+    lib.or_get_body.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+    lib.or_set_body_state.argtypes = [P, ctypes.c_int] + [real] * 6
+    lib.or_contact_count.argtypes = [P]
+    lib.or_contact_count.restype = ctypes.c_int
+    lib.or_get_contact.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.or_proxy_count.argtypes = [P]
+    lib.or_proxy_count.restype = ctypes.c_int
+    lib.or_get_proxy.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.or_collide.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, real, ctypes.c_void_p,
+                               ctypes.c_int, ctypes.c_int, ctypes.c_void_p, real, ctypes.c_void_p,
+                               real, real, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    _LIBS[key] = (lib, real, Conf, Stats)
+    return _LIBS[key]
+
+
+def default_conf(double: bool = False) -> dict:
+    lib, real, Conf, _ = _lib(double)
+    c = Conf()
+    lib.or_default_conf(ctypes.byref(c))
+    return {n: getattr(c, n) for n in CONF_REAL_FIELDS + CONF_INT_FIELDS}
+
+
+class OracleWorld:
+    """One world of the restated step, built from a :class:`Scene`."""
+
+    def __init__(self, scene, double: bool = False):
+        self.lib, self.real, self.Conf, self.Stats = _lib(double)
+        self.double = double
+        self.np_real = np.float64 if double else np.float32
+        self.h = ctypes.c_void_p(self.lib.or_world_create())
+        lib, h = self.lib, self.h
+        for i in range(scene.n_bodies):
+            p, v, a, d = scene.body_pos[i], scene.body_vel[i], scene.body_acc[i], scene.body_damp[i]
+            lib.or_add_body(h, int(scene.body_type[i]), *(float(x) for x in (*p, *v, *a, *d)),
+                            int(scene.body_flags[i]))
+        for s in range(scene.n_shapes):
+            vo, nv = int(scene.shape_voff[s]), int(scene.shape_nv[s])
+            xy = np.ascontiguousarray(scene.verts[vo:vo + nv].reshape(-1), dtype=self.np_real)
+            f = scene.shape_filter[s]
+            b = int(scene.shape_body[s])
+            lib.or_add_shape(h, b, int(scene.shape_kind[s]), nv, xy.ctypes.data,
+                             float(scene.shape_radius[s]), float(scene.shape_density[s]),
+                             float(scene.shape_friction[s]), float(scene.shape_restitution[s]),
+                             int(f[0]), int(f[1]), int(f[2]), int(f[3]))
+            lib.or_reset_mass(h, b)  # Attach(world, body, shape, resetMassData = true)
+        for j in range(scene.n_joints):
+            a, b = scene.joint_bodies[j]
+            an, pr, fl = scene.joint_anchors[j], scene.joint_params[j], scene.joint_flags[j]
+            lib.or_add_revolute(h, int(a), int(b), *(float(x) for x in an), float(pr[0]), int(fl[0]),
+                                float(pr[1]), float(pr[2]), int(fl[1]), float(pr[3]), float(pr[4]),
+                                int(fl[2]))
+        self.n_bodies = scene.n_bodies
+
+    def __del__(self):
+        try:
+            self.lib.or_world_destroy(self.h)
+        except Exception:
+            pass
+
+    def make_conf(self, **overrides):
+        c = self.Conf()
+        self.lib.or_default_conf(ctypes.byref(c))
+        for k, v in overrides.items():
+            setattr(c, k, v)
+        return c
+
+    def step(self, conf=None, **overrides):
+        c = conf if conf is not None else self.make_conf(**overrides)
+        st = self.Stats()
+        self.lib.or_step(self.h, ctypes.byref(c), ctypes.byref(st))
+        return {n: getattr(st, n) for n, _ in self.Stats._fields_}
+
+    def bodies(self) -> dict:
+        n = self.lib.or_body_count(self.h)
+        out = np.zeros((n, 13), dtype=self.np_real)
+        awake = np.zeros(n, dtype=np.int32)
+        aw = ctypes.c_int()
+        for i in range(n):
+            self.lib.or_get_body(self.h, i, out[i].ctypes.data, ctypes.byref(aw))
+            awake[i] = aw.value
+        return {"pos": out[:, 0:3].copy(), "vel": out[:, 3:6].copy(), "xf": out[:, 6:10].copy(),
+                "inv_mass": out[:, 10].copy(), "inv_rot_inertia": out[:, 11].copy(),
+                "under_active": out[:, 12].copy(), "awake": awake}
+
+    def set_body_state(self, i, pos, vel):
+        self.lib.or_set_body_state(self.h, int(i), *(float(x) for x in (*pos, *vel)))
+
+    def contacts(self) -> dict:
+        n = self.lib.or_contact_count(self.h)
+        io = np.zeros((n, 12), dtype=np.int32)
+        fo = np.zeros((n, 12), dtype=self.np_real)
+        ft = np.zeros((n, 8), dtype=np.int32)
+        for k in range(n):
+            self.lib.or_get_contact(self.h, k, io[k].ctypes.data, fo[k].ctypes.data, ft[k].ctypes.data)
+        return {"id": io[:, 0], "proxy": io[:, 1:3], "bsc_a": io[:, 3:6], "bsc_b": io[:, 6:9],
+                "touching": io[:, 9], "type": io[:, 10], "count": io[:, 11], "local_normal": fo[:, 0:2],
+                "local_point": fo[:, 2:4], "points": fo[:, 4:12].reshape(n, 2, 4), "features": ft.reshape(n, 2, 4)}
+
+    def proxies(self) -> dict:
+        n = self.lib.or_proxy_count(self.h)
+        bsc = np.zeros((n, 3), dtype=np.int32)
+        aabb = np.zeros((n, 4), dtype=self.np_real)
+        for p in range(n):
+            self.lib.or_get_proxy(self.h, p, bsc[p].ctypes.data, aabb[p].ctypes.data)
+        return {"bsc": bsc, "aabb": aabb}
+
+
+def collide(kind_a, verts_a, r_a, xf_a, kind_b, verts_b, r_b, xf_b, linear_slop=0.005,
+            max_circles_ratio=10.0, double=False):
+    """Stand-alone CollideShapes of the oracle for known-answer tests."""
+    lib, real, _, _ = _lib(double)
+    npr = np.float64 if double else np.float32
+    va = np.ascontiguousarray(np.asarray(verts_a, dtype=npr).reshape(-1))
+    vb = np.ascontiguousarray(np.asarray(verts_b, dtype=npr).reshape(-1))
+    xa = np.ascontiguousarray(np.asarray(xf_a, dtype=npr))
+    xb = np.ascontiguousarray(np.asarray(xf_b, dtype=npr))
+    tc = np.zeros(2, dtype=np.int32)
+    ft = np.zeros(8, dtype=np.int32)
+    fo = np.zeros(8, dtype=npr)
+    lib.or_collide(kind_a, va.size // 2, va.ctypes.data, r_a, xa.ctypes.data, kind_b, vb.size // 2,
+                   vb.ctypes.data, r_b, xb.ctypes.data, linear_slop, max_circles_ratio,
+                   tc.ctypes.data, ft.ctypes.data, fo.ctypes.data)
+    return {"type": int(tc[0]), "count": int(tc[1]), "features": ft.reshape(2, 4),
+            "local_normal": fo[0:2], "local_point": fo[2:4], "points": fo[4:8].reshape(2, 2)}

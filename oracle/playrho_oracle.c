@@ -1,0 +1,1878 @@
+/*
+ * playrho_oracle.c -- CPU restatement of the PlayRho 2.0.0 regular-phase world
+ * step (TEST INFRASTRUCTURE ONLY; see playrho_oracle.h).
+ *
+ * Every routine names the reference function it follows (paths are inside the
+ * PlayRho project, Library/...).  The order of floating-point operations follows
+ * the reference so that, compiled with -ffp-contract=off, the FP32 build gives
+ * the reference's FP32 numbers.  Compile with -DOR_DOUBLE for the FP64 oracle.
+ *
+ * Scope: disks, convex polygons and edges (one child per shape), revolute
+ * joints, contact persistence with fattened/displaced proxy AABBs, island
+ * discovery by depth-first search, sequential-impulse Gauss-Seidel velocity
+ * solve with the 2-point block solver, NGS position solve, sleep.  TOI
+ * (StepConf::doToi) is not restated: the callers run with doToi = false.
+ */
+#include "playrho_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef or_real real;
+
+#ifdef OR_DOUBLE
+#define RSQRT sqrt
+#define RCOS cos
+#define RSIN sin
+#define RHYPOT hypot
+#define RNEXT nextafter
+#define RMIN_NORMAL DBL_MIN
+#define RMAXV DBL_MAX
+#else
+#define RSQRT sqrtf
+#define RCOS cosf
+#define RSIN sinf
+#define RHYPOT hypotf
+#define RNEXT nextafterf
+#define RMIN_NORMAL FLT_MIN
+#define RMAXV FLT_MAX
+#endif
+#define R(x) ((real)(x))
+#define RINF ((real)INFINITY)
+
+/* ------------------------------------------------------------------------- */
+/* Small value types: Vector2, UnitVec, Transformation, Position/Velocity.    */
+/* ------------------------------------------------------------------------- */
+typedef struct { real x, y; } v2;
+typedef struct { v2 p; v2 q; } xf_t;       /* q = (cos, sin) as UnitVec */
+typedef struct { v2 lin; real ang; } pos_t; /* Position and Velocity */
+
+static inline v2 V(real x, real y) { v2 r = {x, y}; return r; }
+static inline v2 vadd(v2 a, v2 b) { return V(a.x + b.x, a.y + b.y); }
+static inline v2 vsub(v2 a, v2 b) { return V(a.x - b.x, a.y - b.y); }
+static inline v2 vneg(v2 a) { return V(-a.x, -a.y); }
+/* Vector * scalar (Vector.hpp:497-504): a[i] * s. */
+static inline v2 vmul(v2 a, real s) { return V(a.x * s, a.y * s); }
+/* Vector / scalar (Vector.hpp:511-519): a[i] * (1 / s). */
+static inline v2 vdiv(v2 a, real s) { const real inv = R(1) / s; return V(a.x * inv, a.y * inv); }
+/* Dot (Math.hpp:320-333): accumulates from zero. */
+static inline real dot(v2 a, v2 b) { real r = R(0); r += a.x * b.x; r += a.y * b.y; return r; }
+/* Cross (Math.hpp:365-386). */
+static inline real cross(v2 a, v2 b) { const real m = a.x * b.y; const real s = a.y * b.x; return m - s; }
+/* GetMagnitudeSquared (Math.hpp:274-283). */
+static inline real mag2(v2 a) { real r = R(0); r += a.x * a.x; r += a.y * a.y; return r; }
+/* GetRevPerpendicular (-y, x) and GetFwdPerpendicular (y, -x) (UnitVec.hpp:364-378). */
+static inline v2 revperp(v2 a) { return V(-a.y, a.x); }
+static inline v2 fwdperp(v2 a) { return V(a.y, -a.x); }
+/* Rotate / InverseRotate (d2/Math.hpp, Rotate and InverseRotate templates). */
+static inline v2 rotate(v2 v, v2 q) {
+    const real nx = (q.x * v.x) - (q.y * v.y);
+    const real ny = (q.y * v.x) + (q.x * v.y);
+    return V(nx, ny);
+}
+static inline v2 invrotate(v2 v, v2 q) {
+    const real nx = (q.x * v.x) + (q.y * v.y);
+    const real ny = (q.x * v.y) - (q.y * v.x);
+    return V(nx, ny);
+}
+/* UnitVec::Rotate (UnitVec.hpp:353-358). */
+static inline v2 urotate(v2 u, v2 amount) {
+    return V(u.x * amount.x - u.y * amount.y, u.y * amount.x + u.x * amount.y);
+}
+/* Transform / InverseTransform (d2/Math.hpp). */
+static inline v2 xform(v2 v, xf_t t) { return vadd(rotate(v, t.q), t.p); }
+static inline v2 invxform(v2 v, xf_t t) { return invrotate(vsub(v, t.p), t.q); }
+/* MulT(A, B) (d2/Math.hpp): {InverseRotate(B.p - A.p, A.q), B.q.Rotate(A.q.FlipY())}. */
+static inline xf_t mult(xf_t A, xf_t B) {
+    xf_t r;
+    r.p = invrotate(vsub(B.p, A.p), A.q);
+    r.q = urotate(B.q, V(A.q.x, -A.q.y));
+    return r;
+}
+/* UnitVec::Get(angle) (UnitVec.cpp:27-30). */
+static inline v2 unit_from_angle(real a) { return V(RCOS(a), RSIN(a)); }
+/* UnitVec::Get(x, y, fallback) (UnitVec.hpp:175-235). */
+static inline v2 unit_vector(v2 v, v2 fallback) {
+    const real m2 = v.x * v.x + v.y * v.y;
+    if (isnormal(m2)) {
+        const real m = RSQRT(m2);
+        const real inv = R(1) / m;
+        return V(v.x * inv, v.y * inv);
+    }
+    const real m = RHYPOT(v.x, v.y);
+    if (!isnormal(m)) {
+        return fallback;
+    }
+    return V(v.x / m, v.y / m);
+}
+/* GetTransformation(pos, localCenter) (d2/Math.hpp). */
+static inline xf_t get_xf(pos_t pos, v2 lc) {
+    xf_t t;
+    t.q = unit_from_angle(pos.ang);
+    t.p = vsub(pos.lin, rotate(lc, t.q));
+    return t;
+}
+/* AlmostZero / AlmostEqual (Math.hpp:177-194). */
+static inline int almost_zero(real v) { return fabs(v) < RMIN_NORMAL; }
+static inline int almost_equal(real a, real b) {
+    int ulp = 4;
+    for (; (a != b) && (ulp > 0); --ulp) {
+        a = RNEXT(a, b);
+    }
+    return a == b;
+}
+static inline real clampr(real v, real lo, real hi) { return (v < lo) ? lo : ((hi < v) ? hi : v); }
+static inline real maxr(real a, real b) { return (a < b) ? b : a; }
+static inline real minr(real a, real b) { return (b < a) ? b : a; }
+
+/* ------------------------------------------------------------------------- */
+/* Growable integer vectors.                                                  */
+/* ------------------------------------------------------------------------- */
+typedef struct { int64_t* a; int n, cap; } ivec;
+static void iv_push(ivec* v, int64_t x) {
+    if (v->n == v->cap) {
+        v->cap = v->cap ? v->cap * 2 : 8;
+        v->a = (int64_t*)realloc(v->a, (size_t)v->cap * sizeof(int64_t));
+    }
+    v->a[v->n++] = x;
+}
+static void iv_erase_at(ivec* v, int i) {
+    memmove(v->a + i, v->a + i + 1, (size_t)(v->n - i - 1) * sizeof(int64_t));
+    --v->n;
+}
+static void iv_free(ivec* v) { free(v->a); v->a = NULL; v->n = v->cap = 0; }
+
+/* ------------------------------------------------------------------------- */
+/* Entities.                                                                  */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    v2 lp;
+    unsigned char tA, iA, tB, iB;
+    real ni, ti;
+} mpt;
+enum { M_UNSET = 0, M_CIRCLES = 1, M_FACEA = 2, M_FACEB = 3 };
+typedef struct { int type; v2 ln; v2 lp; int count; mpt p[2]; } manifold;
+
+typedef struct { int count; v2 v[OR_MAXV]; v2 n[OR_MAXV]; real r; } dproxy;
+
+enum { BF_AWAKE = 1u, BF_ALLOW_SLEEP = 2u, BF_FIXED_ROT = 4u, BF_ENABLED = 8u };
+typedef struct {
+    int type;
+    unsigned flags;
+    pos_t pos0, pos1;
+    v2 lc;
+    xf_t xf;
+    pos_t vel;
+    v2 la;
+    real aa, ldamp, adamp, invM, invI, uat;
+    ivec shapes, proxies;
+    ivec ckeys, cids; /* body contact list: (key, contactID), insertion order */
+    ivec jids, jother; /* body joint list: (jointID, other body) */
+} body_t;
+
+typedef struct {
+    int kind;
+    dproxy dp;
+    real density, friction, restitution;
+    unsigned cat, mask;
+    int group, sensor;
+} shape_t;
+
+typedef struct {
+    int bA, bB;
+    v2 laA, laB;
+    real refAngle, lower, upper, motorSpeed, maxMotorTorque;
+    int enableLimit, enableMotor, collideConnected;
+    /* solver state */
+    v2 rA, rB;
+    real mass[3][3];
+    real angularMass, motorImpulse;
+    real imp[3];
+    int limitState;
+} joint_t;
+enum { LS_INACTIVE = 0, LS_LOWER = 1, LS_UPPER = 2, LS_EQUAL = 3 };
+
+typedef struct {
+    int body, shape, child;
+    real aabb[4]; /* minx miny maxx maxy -- the tree (fat) AABB */
+} proxy_t;
+
+typedef struct {
+    int alive;
+    uint64_t key;
+    int pA, pB; /* proxy ids (min, max) */
+    int bA, sA, cA, bB, sB, cB;
+    int touching, sensor, needsUpdate, impenetrable;
+    real friction, restitution, tangentSpeed;
+    manifold m;
+} contact_t;
+
+struct or_world {
+    body_t* b; int nb, capb;
+    shape_t* s; int ns, caps;
+    joint_t* j; int nj, capj;
+    proxy_t* p; int np, capp;
+    contact_t* c; int nc, capc;
+    ivec cfree;
+    ivec wkeys, wcids;      /* m_contacts: (key, contactID) in insertion order */
+    ivec fixturesForProxies; /* pairs (body << 32 | shape) */
+    ivec bodiesForSync;
+    ivec proxiesForContacts;
+    real inv_dt0;
+};
+
+#define GROW(ptr, n, cap, T)                                                   \
+    do {                                                                       \
+        if ((n) == (cap)) {                                                    \
+            (cap) = (cap) ? (cap) * 2 : 16;                                    \
+            (ptr) = (T*)realloc((ptr), (size_t)(cap) * sizeof(T));             \
+        }                                                                      \
+    } while (0)
+
+static inline uint64_t make_key(int a, int b) {
+    const uint32_t lo = (uint32_t)(a < b ? a : b), hi = (uint32_t)(a < b ? b : a);
+    return ((uint64_t)lo << 32) | hi;
+}
+
+static inline int is_speedable(const body_t* b) { return b->type != OR_STATIC; }
+static inline int is_accelerable(const body_t* b) { return b->type == OR_DYNAMIC; }
+static inline int is_impenetrable(const body_t* b) { return b->type != OR_DYNAMIC; }
+
+/* Body::SetAwake (Body.cpp:161-169). */
+static void body_set_awake(body_t* b) {
+    if (is_speedable(b)) { b->flags |= BF_AWAKE; b->uat = R(0); }
+}
+/* Body::UnsetAwake via Unawaken (Body.hpp:1203-1210, Body.cpp:171-180). */
+static int body_unawaken(body_t* b) {
+    if ((b->flags & BF_AWAKE) && (b->flags & BF_ALLOW_SLEEP)) {
+        b->flags &= ~BF_AWAKE;
+        b->uat = R(0);
+        b->vel.lin = V(R(0), R(0));
+        b->vel.ang = R(0);
+        return 1;
+    }
+    return 0;
+}
+/* Body::SetPosition1 keeps m_xf = GetTransform1(sweep) (Body.hpp:701-714). */
+static void body_set_pos1(body_t* b, pos_t p) { b->pos1 = p; b->xf = get_xf(p, b->lc); }
+
+/* ------------------------------------------------------------------------- */
+/* World construction.                                                        */
+/* ------------------------------------------------------------------------- */
+or_world* or_world_create(void) {
+    or_world* w = (or_world*)calloc(1, sizeof(or_world));
+    return w;
+}
+
+void or_world_destroy(or_world* w) {
+    if (!w) return;
+    for (int i = 0; i < w->nb; ++i) {
+        body_t* b = &w->b[i];
+        iv_free(&b->shapes); iv_free(&b->proxies); iv_free(&b->ckeys); iv_free(&b->cids);
+        iv_free(&b->jids); iv_free(&b->jother);
+    }
+    free(w->b); free(w->s); free(w->j); free(w->p); free(w->c);
+    iv_free(&w->cfree); iv_free(&w->wkeys); iv_free(&w->wcids);
+    iv_free(&w->fixturesForProxies); iv_free(&w->bodiesForSync); iv_free(&w->proxiesForContacts);
+    free(w);
+}
+
+/* Body(BodyConf) (Body.cpp:88-109) + flags from Body::GetFlags. */
+int or_add_body(or_world* w, int type, real px, real py, real angle, real vx, real vy,
+                real av, real ax, real ay, real aa, real linDamp, real angDamp, unsigned flags) {
+    GROW(w->b, w->nb, w->capb, body_t);
+    body_t* b = &w->b[w->nb];
+    memset(b, 0, sizeof(*b));
+    b->type = type;
+    b->flags = 0;
+    if (flags & OR_BF_ALLOW_SLEEP) b->flags |= BF_ALLOW_SLEEP;
+    if (flags & OR_BF_FIXED_ROTATION) b->flags |= BF_FIXED_ROT;
+    if (flags & OR_BF_ENABLED) b->flags |= BF_ENABLED;
+    if ((flags & OR_BF_AWAKE) && type != OR_STATIC) b->flags |= BF_AWAKE;
+    b->lc = V(R(0), R(0));
+    b->pos0.lin = V(px, py); b->pos0.ang = angle;
+    body_set_pos1(b, b->pos0);
+    if (type == OR_STATIC) {
+        b->vel.lin = V(R(0), R(0)); b->vel.ang = R(0);
+    } else {
+        b->vel.lin = V(vx, vy); b->vel.ang = av;
+    }
+    if (type == OR_DYNAMIC) { b->la = V(ax, ay); b->aa = aa; }
+    b->ldamp = linDamp; b->adamp = angDamp;
+    /* default inverse mass data (Body.cpp: dynamic bodies start with 1 kg). */
+    b->invM = (type == OR_DYNAMIC) ? R(1) : R(0);
+    b->invI = R(0);
+    b->uat = R(0);
+    return w->nb++;
+}
+
+/* GetFwdNormalsVector (d2/Math.cpp) -- polygon / edge normals. */
+static void make_normals(dproxy* dp) {
+    if (dp->count > 1) {
+        for (int i = 0; i < dp->count; ++i) {
+            const int nx = (i + 1) % dp->count;
+            const v2 e = vsub(dp->v[nx], dp->v[i]);
+            dp->n[i] = unit_vector(fwdperp(e), V(R(0), R(0)));
+        }
+    } else if (dp->count == 1) {
+        dp->n[0] = V(R(0), R(0));
+    }
+}
+
+int or_add_shape(or_world* w, int body, int kind, int nverts, const real* xy, real radius,
+                 real density, real friction, real restitution, unsigned categoryBits,
+                 unsigned maskBits, int groupIndex, int sensor) {
+    GROW(w->s, w->ns, w->caps, shape_t);
+    shape_t* s = &w->s[w->ns];
+    memset(s, 0, sizeof(*s));
+    s->kind = kind;
+    s->dp.count = nverts > OR_MAXV ? OR_MAXV : nverts;
+    for (int i = 0; i < s->dp.count; ++i) s->dp.v[i] = V(xy[2 * i], xy[2 * i + 1]);
+    s->dp.r = radius;
+#ifdef OR_DOUBLE
+    /* Scenes carry float32 values; a 0.01f polygon/edge skin is just under the
+     * Real = double world's minimum vertex radius (0.01 m), which CreateShape
+     * enforces (AabbTreeWorld.cpp:1239-1249), so it is raised to that minimum. */
+    if (kind != OR_SHAPE_DISK && s->dp.r < R(0.01)) s->dp.r = R(0.01);
+#endif
+    make_normals(&s->dp);
+    s->density = density; s->friction = friction; s->restitution = restitution;
+    s->cat = categoryBits; s->mask = maskBits; s->group = groupIndex; s->sensor = sensor;
+    const int sid = w->ns++;
+    /* CreateBody / Attach queue the fixture for proxy creation in the next Step
+     * (AabbTreeWorld.cpp:1041). */
+    iv_push(&w->b[body].shapes, sid);
+    iv_push(&w->fixturesForProxies, ((int64_t)body << 32) | (int64_t)sid);
+    return sid;
+}
+
+/* GetMassData for disk / edge / polygon (MassData.cpp). */
+static void shape_mass(const shape_t* s, real* mass, v2* center, real* I) {
+    const real Pi = R(3.14159265358979323846264338327950288L);
+    const real density = s->density;
+    const dproxy* dp = &s->dp;
+    if (dp->count == 1) {
+        const real r = dp->r;
+        const real r2 = r * r;
+        const real area = r2 * Pi;
+        *mass = density * area;
+        const real Iz = area * ((r2 / R(2)) + mag2(dp->v[0]));
+        *I = Iz * density;
+        *center = dp->v[0];
+        return;
+    }
+    if (dp->count == 2) {
+        const real r = dp->r;
+        const real r2 = r * r;
+        const real circle_area = r2 * Pi;
+        const real circle_mass = density * circle_area;
+        const v2 v0 = dp->v[0], v1 = dp->v[1];
+        const v2 d = vsub(v1, v0);
+        const v2 offset = vmul(revperp(unit_vector(d, V(R(0), R(0)))), r);
+        const real b = RSQRT(mag2(d));
+        const real h = r * R(2);
+        const real rect_mass = density * b * h;
+        *mass = circle_mass + rect_mass;
+        *center = vdiv(vadd(v0, v1), R(2));
+        const real halfCircleArea = circle_area / R(2);
+        const real halfRSquared = r2 / R(2);
+        v2 q[4] = {vadd(v0, offset), vsub(v0, offset), vsub(v1, offset), vadd(v1, offset)};
+        /* GetPolarMoment (Math.cpp:243-275) */
+        real sum_x = R(0), sum_y = R(0);
+        for (int i = 0; i < 4; ++i) {
+            const v2 tv = q[i];
+            const v2 nv = q[(i + 1) % 4];
+            const real fact_b = cross(tv, nv);
+            sum_x += ((tv.y * tv.y) + tv.y * nv.y + (nv.y * nv.y)) * fact_b;
+            sum_y += ((tv.x * tv.x) + tv.x * nv.x + (nv.x * nv.x)) * fact_b;
+        }
+        const real RealInverseOfTwelve = R(1) / R(12);
+        const real Iz = (sum_x + sum_y) * RealInverseOfTwelve;
+        const real I0 = halfCircleArea * (halfRSquared + mag2(v0));
+        const real I1 = halfCircleArea * (halfRSquared + mag2(v1));
+        *I = (I0 + I1 + Iz) * density;
+        return;
+    }
+    /* Polygon (MassData.cpp, GetMassData(vertexRadius, density, vertices)). */
+    const int count = dp->count;
+    v2 ctr = V(R(0), R(0));
+    real area = R(0);
+    real II = R(0);
+    v2 s0 = V(R(0), R(0));
+    for (int i = 0; i < count; ++i) s0 = vadd(s0, dp->v[i]);
+    s0 = vdiv(s0, (real)count); /* Average(vertices) */
+    for (int i = 0; i < count; ++i) {
+        const v2 e1 = vsub(dp->v[i], s0);
+        const v2 e2 = vsub(dp->v[(i + 1) % count], s0);
+        const real D = cross(e1, e2);
+        const real RealReciprocalOfTwo = R(1) / R(2);
+        const real triangleArea = D * RealReciprocalOfTwo;
+        area += triangleArea;
+        const real RealReciprocalOfThree = R(1) / R(3);
+        ctr = vadd(ctr, vmul(vmul(vadd(e1, e2), triangleArea), RealReciprocalOfThree));
+        const real intx2 = (e1.x * e1.x) + e2.x * e1.x + (e2.x * e2.x);
+        const real inty2 = (e1.y * e1.y) + e2.y * e1.y + (e2.y * e2.y);
+        const real RealReciprocalOfTwelve = R(1) / R(3 * 4);
+        const real triangleI = D * (intx2 + inty2) * RealReciprocalOfTwelve;
+        II += triangleI;
+    }
+    const real m = density * area;
+    ctr = ((area > R(0)) && !almost_zero(area)) ? vdiv(ctr, area) : V(R(0), R(0));
+    const v2 massDataCenter = vadd(ctr, s0);
+    const real massCenterOffset = mag2(massDataCenter);
+    const real centerOffset = mag2(ctr);
+    const real inertialLever = massCenterOffset - centerOffset;
+    *mass = m;
+    *center = massDataCenter;
+    *I = ((density * II) + (m * inertialLever));
+}
+
+/* ResetMassData -> ComputeMassData (WorldShape.cpp:160-176) -> SetMassData
+ * (WorldBody.cpp:365-400). */
+void or_reset_mass(or_world* w, int body) {
+    body_t* b = &w->b[body];
+    real mass = R(0), I = R(0);
+    v2 wc = V(R(0), R(0));
+    for (int k = 0; k < b->shapes.n; ++k) {
+        const shape_t* s = &w->s[b->shapes.a[k]];
+        if (s->density > R(0)) {
+            real m, i;
+            v2 c;
+            shape_mass(s, &m, &c, &i);
+            mass += m;
+            wc = vadd(wc, vmul(c, m));
+            I += i;
+        }
+    }
+    const v2 center = (mass > R(0)) ? vdiv(wc, mass) : V(R(0), R(0));
+    if (!is_accelerable(b)) {
+        b->invM = R(0); b->invI = R(0);
+        if (!is_speedable(b)) {
+            /* SetSweep(Sweep{Position{location, angle}}) with zero local center. */
+            const v2 loc = b->xf.p;
+            const real ang = b->pos1.ang;
+            b->lc = V(R(0), R(0));
+            b->pos0.lin = loc; b->pos0.ang = ang;
+            body_set_pos1(b, b->pos0);
+        }
+        return;
+    }
+    const real m = (mass > R(0)) ? mass : R(1);
+    const real invMass = R(1) / m;
+    real invRotI = R(0);
+    if ((I > R(0)) && !(b->flags & BF_FIXED_ROT)) {
+        const real lengthSquared = mag2(center);
+        const real Ic = I - (m * lengthSquared);
+        invRotI = R(1) / Ic;
+    }
+    b->invM = invMass; b->invI = invRotI;
+    const v2 oldCenter = b->pos1.lin;
+    const pos_t np = {xform(center, b->xf), b->pos1.ang};
+    b->lc = center;
+    b->pos0 = np;
+    body_set_pos1(b, np);
+    const v2 newCenter = b->pos1.lin;
+    const v2 dc = vsub(newCenter, oldCenter);
+    b->vel.lin = vadd(b->vel.lin, vmul(revperp(dc), b->vel.ang));
+}
+
+int or_add_revolute(or_world* w, int bodyA, int bodyB, real lax, real lay, real lbx, real lby,
+                    real refAngle, int enableLimit, real lower, real upper, int enableMotor,
+                    real motorSpeed, real maxMotorTorque, int collideConnected) {
+    GROW(w->j, w->nj, w->capj, joint_t);
+    joint_t* j = &w->j[w->nj];
+    memset(j, 0, sizeof(*j));
+    j->bA = bodyA; j->bB = bodyB;
+    j->laA = V(lax, lay); j->laB = V(lbx, lby);
+    j->refAngle = refAngle; j->enableLimit = enableLimit; j->lower = lower; j->upper = upper;
+    j->enableMotor = enableMotor; j->motorSpeed = motorSpeed; j->maxMotorTorque = maxMotorTorque;
+    j->collideConnected = collideConnected;
+    const int jid = w->nj++;
+    /* CreateJoint adds (jointID, other) to both bodies' joint lists (AabbTreeWorld.cpp:1132-1157). */
+    iv_push(&w->b[bodyA].jids, jid); iv_push(&w->b[bodyA].jother, bodyB);
+    if (bodyB != bodyA) { iv_push(&w->b[bodyB].jids, jid); iv_push(&w->b[bodyB].jother, bodyA); }
+    return jid;
+}
+
+/* ------------------------------------------------------------------------- */
+/* AABBs (AABB.cpp:51-62, detail/AABB.hpp, Interval.hpp).                     */
+/* ------------------------------------------------------------------------- */
+static inline void aabb_empty(real* a) { a[0] = RINF; a[1] = RINF; a[2] = -RINF; a[3] = -RINF; }
+static inline void aabb_include(real* a, v2 p) {
+    /* Interval::Include: {min(v, min), max(v, max)} */
+    a[0] = (a[0] < p.x) ? a[0] : p.x;  /* std::min(v, GetMin()) returns v unless GetMin() < v */
+    a[2] = (p.x < a[2]) ? a[2] : p.x;  /* std::max(v, GetMax()) returns v unless v < GetMax() */
+    a[1] = (a[1] < p.y) ? a[1] : p.y;
+    a[3] = (p.y < a[3]) ? a[3] : p.y;
+}
+/* Fatten = ExpandEqually (Interval.hpp:210-222). */
+static inline void aabb_fatten(real* a, real amount) {
+    a[0] = a[0] - amount; a[2] = a[2] + amount;
+    a[1] = a[1] - amount; a[3] = a[3] + amount;
+}
+/* GetDisplacedAABB -> Interval::Expand (Interval.hpp:186-200). */
+static inline void aabb_displace(real* a, v2 d) {
+    if (d.x < R(0)) a[0] += d.x; else a[2] += d.x;
+    if (d.y < R(0)) a[1] += d.y; else a[3] += d.y;
+}
+/* ComputeAABB(proxy, xf0, xf1) (AABB.cpp:51-62). */
+static void compute_aabb2(const dproxy* dp, xf_t x0, xf_t x1, real* out) {
+    aabb_empty(out);
+    for (int i = 0; i < dp->count; ++i) {
+        aabb_include(out, xform(dp->v[i], x0));
+        aabb_include(out, xform(dp->v[i], x1));
+    }
+    aabb_fatten(out, dp->r);
+}
+/* TestOverlap -> IsIntersecting (Interval.hpp:292-298). */
+static inline int aabb_overlap(const real* a, const real* b) {
+    {
+        const real maxOfMins = (a[0] < b[0]) ? b[0] : a[0];
+        const real minOfMaxs = (b[2] < a[2]) ? b[2] : a[2];
+        if (!(minOfMaxs >= maxOfMins)) return 0;
+    }
+    {
+        const real maxOfMins = (a[1] < b[1]) ? b[1] : a[1];
+        const real minOfMaxs = (b[3] < a[3]) ? b[3] : a[3];
+        if (!(minOfMaxs >= maxOfMins)) return 0;
+    }
+    return 1;
+}
+/* Contains -> IsEntirelyEnclosing (Interval.hpp:324-327). */
+static inline int aabb_contains(const real* a, const real* b) {
+    return a[0] <= b[0] && a[2] >= b[2] && a[1] <= b[1] && a[3] >= b[3];
+}
+
+/* ------------------------------------------------------------------------- */
+/* Narrowphase: CollideShapes (Manifold.cpp:393-438) and helpers.             */
+/* ------------------------------------------------------------------------- */
+typedef struct { v2 v; unsigned char tA, iA, tB, iB; } clipv;
+enum { CF_VERTEX = 0, CF_FACE = 1 };
+#define INVALID_V 255
+
+static manifold man_empty(void) { manifold m; memset(&m, 0, sizeof(m)); m.type = M_UNSET; return m; }
+static void set_cf(mpt* p, int tA, int iA, int tB, int iB) {
+    p->tA = (unsigned char)tA; p->iA = (unsigned char)iA; p->tB = (unsigned char)tB; p->iB = (unsigned char)iB;
+}
+/* Manifold::GetForCircles (Manifold.hpp:168-171). */
+static manifold man_circles(v2 vA, int iA, v2 vB, int iB) {
+    manifold m = man_empty();
+    m.type = M_CIRCLES; m.ln = V(R(0), R(0)); m.lp = vA; m.count = 1;
+    m.p[0].lp = vB; set_cf(&m.p[0], CF_VERTEX, iA, CF_VERTEX, iB);
+    return m;
+}
+static manifold man_face(int type, v2 ln, v2 lp) {
+    manifold m = man_empty();
+    m.type = type; m.ln = ln; m.lp = lp; m.count = 0;
+    return m;
+}
+static void man_add(manifold* m, v2 lp, int tA, int iA, int tB, int iB) {
+    mpt* p = &m->p[m->count++];
+    p->lp = lp; set_cf(p, tA, iA, tB, iB); p->ni = R(0); p->ti = R(0);
+}
+
+/* ClipSegmentToLine (Manifold.cpp:61-102). */
+static int clip_segment(const clipv* vin, int nin, v2 normal, real offset, int indexA, clipv* vout) {
+    int n = 0;
+    if (nin == 2) {
+        const real d0 = dot(normal, vin[0].v) - offset;
+        const real d1 = dot(normal, vin[1].v) - offset;
+        if (d0 <= R(0) || almost_zero(d0)) vout[n++] = vin[0];
+        if (d1 <= R(0) || almost_zero(d1)) vout[n++] = vin[1];
+        if (n < 2 && (signbit(d0) != signbit(d1))) {
+            const real interp = d0 / (d0 - d1);
+            const v2 vertex = vadd(vin[0].v, vmul(vsub(vin[1].v, vin[0].v), interp));
+            clipv cv;
+            cv.v = vertex; cv.tA = CF_VERTEX; cv.iA = (unsigned char)indexA; cv.tB = CF_FACE; cv.iB = vin[0].iB;
+            vout[n++] = cv;
+        }
+    }
+    return n;
+}
+
+/* GetMinSeparationInfo (ShapeSeparation.cpp:36-58). */
+static real min_sep_info(v2 origin, v2 dir, const v2* verts, int n, int* first, int* second) {
+    real minSep = RINF;
+    *first = INVALID_V; *second = INVALID_V;
+    for (int i = 0; i < n; ++i) {
+        const real s = dot(dir, vsub(verts[i], origin));
+        if (minSep > s) { minSep = s; *first = i; *second = INVALID_V; }
+        else if (minSep == s) { *second = i; }
+    }
+    return minSep;
+}
+typedef struct { real distance; int firstShape; int second0, second1; } sepinfo;
+/* GetMaxSeparation4x4 (ShapeSeparation.cpp:62-101). */
+static sepinfo max_sep_4x4(const dproxy* p1, xf_t xf1, const dproxy* p2, xf_t xf2) {
+    sepinfo r; r.distance = -RINF; r.firstShape = INVALID_V; r.second0 = INVALID_V; r.second1 = INVALID_V;
+    const xf_t xf = mult(xf1, xf2);
+    v2 verts[4];
+    for (int i = 0; i < 4; ++i) verts[i] = xform(p2->v[i], xf);
+    for (int i = 0; i < 4; ++i) {
+        int f, s;
+        const real d = min_sep_info(p1->v[i], p1->n[i], verts, 4, &f, &s);
+        if (r.distance < d) { r.distance = d; r.second0 = f; r.second1 = s; r.firstShape = i; }
+    }
+    return r;
+}
+/* GetMaxSeparation (ShapeSeparation.cpp:103-124). */
+static sepinfo max_sep(const dproxy* p1, xf_t xf1, const dproxy* p2, xf_t xf2) {
+    sepinfo r; r.distance = -RINF; r.firstShape = INVALID_V; r.second0 = INVALID_V; r.second1 = INVALID_V;
+    const xf_t xf = mult(xf2, xf1);
+    for (int i = 0; i < p1->count; ++i) {
+        const v2 origin = xform(p1->v[i], xf);
+        const v2 normal = rotate(p1->n[i], xf.q);
+        int f, s;
+        const real d = min_sep_info(origin, normal, p2->v, p2->count, &f, &s);
+        if (r.distance < d) { r.distance = d; r.second0 = f; r.second1 = s; r.firstShape = i; }
+    }
+    return r;
+}
+
+/* GetMostAntiParallelEdge (Manifold.cpp:124-141). */
+static void most_anti_parallel_edge(v2 n0, xf_t xf0, const dproxy* s1, xf_t xf1, int first, int second,
+                                    int* e0, int* e1) {
+    if (second == INVALID_V) {
+        const v2 normal = invrotate(rotate(n0, xf0.q), xf1.q);
+        const int count = s1->count;
+        const int prev = (first == 0) ? count - 1 : first - 1;
+        const real prevDot = dot(normal, s1->n[prev]);
+        const real currDot = dot(normal, s1->n[first]);
+        if (prevDot < currDot) { *e0 = prev; *e1 = first; }
+        else { *e0 = first; *e1 = (first + 1) % count; }
+        return;
+    }
+    if ((second > first) && ((first + 1) == second)) { *e0 = first; *e1 = second; }
+    else { *e0 = second; *e1 = first; }
+}
+
+/* GetManifold for two polygons (Manifold.cpp:162-291). */
+static manifold get_manifold_poly(int flipped, const dproxy* s0, xf_t xf0, int idx0,
+                                  const dproxy* s1, xf_t xf1, int sec0, int sec1,
+                                  real maxCirclesRatio) {
+    const real r0 = s0->r, r1 = s1->r;
+    const real totalRadius = r0 + r1;
+    const int idx0Next = (idx0 + 1) % s0->count;
+    const v2 s0_rel_v0 = s0->v[idx0];
+    const v2 s0_rel_v1 = s0->v[idx0Next];
+    const v2 s0_abs_v0 = xform(s0_rel_v0, xf0);
+    const v2 s0_abs_v1 = xform(s0_rel_v1, xf0);
+    const real s0_len_edge0 = mag2(vsub(s0_rel_v1, s0_rel_v0));
+    const v2 s0_rel_n0 = s0->n[idx0];
+    const v2 s0_rel_e0_dir = revperp(s0_rel_n0);
+    int e1f, e1s;
+    most_anti_parallel_edge(s0_rel_n0, xf0, s1, xf1, sec0, sec1, &e1f, &e1s);
+    const v2 s1_rel_v0 = s1->v[e1f];
+    const v2 s1_abs_v0 = xform(s1_rel_v0, xf1);
+    const v2 s1_rel_v1 = s1->v[e1s];
+    const v2 s1_abs_v1 = xform(s1_rel_v1, xf1);
+    {
+        const v2 s0_abs_e0_dir = rotate(s0_rel_e0_dir, xf0.q);
+        /* GetClipPoints (Manifold.cpp:143-158) */
+        clipv ie[2];
+        ie[0].v = s1_abs_v0; ie[0].tA = CF_FACE; ie[0].iA = (unsigned char)idx0; ie[0].tB = CF_VERTEX; ie[0].iB = (unsigned char)e1f;
+        ie[1].v = s1_abs_v1; ie[1].tA = CF_FACE; ie[1].iA = (unsigned char)idx0; ie[1].tB = CF_VERTEX; ie[1].iB = (unsigned char)e1s;
+        const real dp_v0_e0 = -dot(s0_abs_e0_dir, s0_abs_v0);
+        const real dp_v1_e0 = +dot(s0_abs_e0_dir, s0_abs_v1);
+        clipv pts[2], cps[2];
+        const int np = clip_segment(ie, 2, vneg(s0_abs_e0_dir), dp_v0_e0, idx0, pts);
+        const int nc = clip_segment(pts, np, s0_abs_e0_dir, dp_v1_e0, idx0Next, cps);
+        if (nc == 2) {
+            const v2 abs_normal = fwdperp(s0_abs_e0_dir);
+            const v2 rel_midpoint = vdiv(vadd(s0_rel_v0, s0_rel_v1), R(2));
+            const real abs_offset = dot(abs_normal, s0_abs_v0);
+            const v2 normal = fwdperp(s0_rel_e0_dir);
+            manifold m = man_face(flipped ? M_FACEB : M_FACEA, normal, rel_midpoint);
+            for (int k = 0; k < 2; ++k) {
+                if ((dot(abs_normal, cps[k].v) - abs_offset) <= totalRadius) {
+                    const v2 lp = invxform(cps[k].v, xf1);
+                    if (!flipped) man_add(&m, lp, cps[k].tA, cps[k].iA, cps[k].tB, cps[k].iB);
+                    else man_add(&m, lp, cps[k].tB, cps[k].iB, cps[k].tA, cps[k].iA);
+                }
+            }
+            if (m.count > 0) return m;
+        }
+    }
+    const real totalRadiusSquared = totalRadius * totalRadius;
+    const real mcr = maxCirclesRatio * r0;
+    const int mustUseFace = s0_len_edge0 > (mcr * mcr);
+    const v2 fn = fwdperp(s0_rel_e0_dir);
+    /* four vertex-vertex tests in the reference's order */
+    const v2 a_rel[4] = {s0_rel_v0, s0_rel_v1, s0_rel_v0, s0_rel_v1};
+    const v2 a_abs[4] = {s0_abs_v0, s0_abs_v1, s0_abs_v0, s0_abs_v1};
+    const int a_idx[4] = {idx0, idx0Next, idx0, idx0Next};
+    const v2 b_rel[4] = {s1_rel_v0, s1_rel_v1, s1_rel_v1, s1_rel_v0};
+    const v2 b_abs[4] = {s1_abs_v0, s1_abs_v1, s1_abs_v1, s1_abs_v0};
+    const int b_idx[4] = {e1f, e1s, e1s, e1f};
+    for (int k = 0; k < 4; ++k) {
+        if (mag2(vsub(a_abs[k], b_abs[k])) <= totalRadiusSquared) {
+            if (mustUseFace) {
+                manifold m = man_face(flipped ? M_FACEB : M_FACEA, fn, a_rel[k]);
+                if (!flipped) man_add(&m, b_rel[k], CF_FACE, a_idx[k], CF_VERTEX, b_idx[k]);
+                else man_add(&m, b_rel[k], CF_VERTEX, b_idx[k], CF_FACE, a_idx[k]);
+                return m;
+            }
+            return !flipped ? man_circles(a_rel[k], a_idx[k], b_rel[k], b_idx[k])
+                            : man_circles(b_rel[k], b_idx[k], a_rel[k], a_idx[k]);
+        }
+    }
+    return man_empty();
+}
+
+/* GetManifold for polygon vs circle (Manifold.cpp:293-372). */
+static manifold get_manifold_circle(int flipped, real totalRadius, const dproxy* shape, xf_t sxf,
+                                    v2 point, xf_t xfm) {
+    const int vc = shape->count;
+    const v2 cLocal = invxform(xform(point, xfm), sxf);
+    int indexOfMax = 0;
+    real maxSeparation = -RMAXV;
+    for (int i = 0; i < vc; ++i) {
+        const real s = dot(shape->n[i], vsub(cLocal, shape->v[i]));
+        if (s > totalRadius) return man_empty();
+        if (maxSeparation < s) { maxSeparation = s; indexOfMax = i; }
+    }
+    const int indexOfMax2 = (indexOfMax + 1) % vc;
+    const v2 v1 = shape->v[indexOfMax];
+    const v2 v2_ = shape->v[indexOfMax2];
+    if (maxSeparation < R(0)) {
+        const v2 faceCenter = vdiv(vadd(v1, v2_), R(2));
+        manifold m = man_face(flipped ? M_FACEB : M_FACEA, shape->n[indexOfMax], faceCenter);
+        if (!flipped) man_add(&m, point, CF_FACE, indexOfMax, CF_VERTEX, 0);
+        else man_add(&m, point, CF_VERTEX, 0, CF_FACE, indexOfMax);
+        return m;
+    }
+    const v2 cLocalV1 = vsub(cLocal, v1);
+    if (dot(cLocalV1, vsub(v2_, v1)) <= R(0)) {
+        if (mag2(cLocalV1) > totalRadius * totalRadius) return man_empty();
+        return !flipped ? man_circles(v1, indexOfMax, point, 0) : man_circles(point, 0, v1, indexOfMax);
+    }
+    const v2 cLocalV2 = vsub(cLocal, v2_);
+    if (dot(cLocalV2, vsub(v1, v2_)) <= R(0)) {
+        if (mag2(cLocalV2) > totalRadius * totalRadius) return man_empty();
+        return !flipped ? man_circles(v2_, indexOfMax2, point, 0) : man_circles(point, 0, v2_, indexOfMax2);
+    }
+    const v2 faceCenter = vdiv(vadd(v1, v2_), R(2));
+    if (dot(vsub(cLocal, faceCenter), shape->n[indexOfMax]) > totalRadius) return man_empty();
+    manifold m = man_face(flipped ? M_FACEB : M_FACEA, shape->n[indexOfMax], faceCenter);
+    if (!flipped) man_add(&m, point, CF_FACE, indexOfMax, CF_VERTEX, 0);
+    else man_add(&m, point, CF_VERTEX, 0, CF_FACE, indexOfMax);
+    return m;
+}
+
+/* CollideShapes (Manifold.cpp:393-438). */
+static manifold collide_shapes(const dproxy* A, xf_t xfA, const dproxy* B, xf_t xfB,
+                               real linearSlop, real maxCirclesRatio) {
+    const real totalRadius = A->r + B->r;
+    if (A->count == 1 && B->count == 1) {
+        /* GetManifold(locationA, xfA, locationB, xfB, totalRadius) (Manifold.cpp:374-386) */
+        const v2 pA = xform(A->v[0], xfA);
+        const v2 pB = xform(B->v[0], xfB);
+        const real lenSq = mag2(vsub(pB, pA));
+        const real totSq = totalRadius * totalRadius;
+        if (lenSq > totSq) return man_empty();
+        return man_circles(A->v[0], 0, B->v[0], 0);
+    }
+    if (A->count == 1) return get_manifold_circle(1, totalRadius, B, xfB, A->v[0], xfA);
+    if (B->count == 1) return get_manifold_circle(0, totalRadius, A, xfA, B->v[0], xfB);
+    const int do4x4 = (A->count == 4) && (B->count == 4);
+    const sepinfo sa = do4x4 ? max_sep_4x4(A, xfA, B, xfB) : max_sep(A, xfA, B, xfB);
+    if (sa.distance > totalRadius) return man_empty();
+    const sepinfo sb = do4x4 ? max_sep_4x4(B, xfB, A, xfA) : max_sep(B, xfB, A, xfA);
+    if (sb.distance > totalRadius) return man_empty();
+    const real k_tol = linearSlop / R(10);
+    return (sb.distance > (sa.distance + k_tol))
+               ? get_manifold_poly(1, B, xfB, sb.firstShape, A, xfA, sb.second0, sb.second1, maxCirclesRatio)
+               : get_manifold_poly(0, A, xfA, sa.firstShape, B, xfB, sa.second0, sa.second1, maxCirclesRatio);
+}
+
+void or_collide(int kindA, int nA, const real* xyA, real rA, const real* xfA4, int kindB, int nB,
+                const real* xyB, real rB, const real* xfB4, real linearSlop, real maxCirclesRatio,
+                int* type_count2, int* feat8, real* fout8) {
+    (void)kindA; (void)kindB;
+    dproxy a, b;
+    memset(&a, 0, sizeof(a)); memset(&b, 0, sizeof(b));
+    a.count = nA; b.count = nB; a.r = rA; b.r = rB;
+    for (int i = 0; i < nA; ++i) a.v[i] = V(xyA[2 * i], xyA[2 * i + 1]);
+    for (int i = 0; i < nB; ++i) b.v[i] = V(xyB[2 * i], xyB[2 * i + 1]);
+    make_normals(&a); make_normals(&b);
+    xf_t xa, xb;
+    xa.p = V(xfA4[0], xfA4[1]); xa.q = V(xfA4[2], xfA4[3]);
+    xb.p = V(xfB4[0], xfB4[1]); xb.q = V(xfB4[2], xfB4[3]);
+    const manifold m = collide_shapes(&a, xa, &b, xb, linearSlop, maxCirclesRatio);
+    type_count2[0] = m.type; type_count2[1] = m.count;
+    for (int k = 0; k < 2; ++k) {
+        feat8[4 * k + 0] = m.p[k].tA; feat8[4 * k + 1] = m.p[k].iA;
+        feat8[4 * k + 2] = m.p[k].tB; feat8[4 * k + 3] = m.p[k].iB;
+    }
+    fout8[0] = m.ln.x; fout8[1] = m.ln.y; fout8[2] = m.lp.x; fout8[3] = m.lp.y;
+    fout8[4] = m.p[0].lp.x; fout8[5] = m.p[0].lp.y; fout8[6] = m.p[1].lp.x; fout8[7] = m.p[1].lp.y;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Contact maintenance.                                                       */
+/* ------------------------------------------------------------------------- */
+static int kv_find(const ivec* ids, int64_t id) {
+    for (int i = 0; i < ids->n; ++i) if (ids->a[i] == id) return i;
+    return -1;
+}
+
+/* AabbTreeWorld::Update(ContactID) (AabbTreeWorld.cpp:2587-2721). */
+static void contact_update(or_world* w, int cid, const or_stepconf* conf) {
+    contact_t* c = &w->c[cid];
+    const manifold old = c->m;
+    const body_t* bA = &w->b[c->bA];
+    const body_t* bB = &w->b[c->bB];
+    const shape_t* sA = &w->s[c->sA];
+    const shape_t* sB = &w->s[c->sB];
+    int newTouching;
+    if (c->sensor) {
+        /* sensors: TestOverlap via GJK is not restated; configs use no sensors */
+        newTouching = 0;
+        c->m = man_empty();
+    } else {
+        manifold nm = collide_shapes(&sA->dp, bA->xf, &sB->dp, bB->xf, conf->linearSlop, conf->maxCirclesRatio);
+        const int oldn = old.count, newn = nm.count;
+        newTouching = newn > 0;
+        int found[2] = {0, newn < 2};
+        for (int i = 0; i < newn; ++i) {
+            for (int j = 0; j < oldn; ++j) {
+                if (nm.p[i].tA == old.p[j].tA && nm.p[i].iA == old.p[j].iA &&
+                    nm.p[i].tB == old.p[j].tB && nm.p[i].iB == old.p[j].iB) {
+                    found[i] = 1;
+                    nm.p[i].ni = old.p[j].ni; nm.p[i].ti = old.p[j].ti;
+                    break;
+                }
+            }
+        }
+        for (int i = 0; i < newn; ++i) {
+            if (!found[i]) {
+                real least = RINF;
+                for (int j = 0; j < oldn; ++j) {
+                    const real sq = mag2(vsub(old.p[j].lp, nm.p[i].lp));
+                    if (least > sq) { least = sq; nm.p[i].ni = old.p[j].ni; nm.p[i].ti = old.p[j].ti; }
+                }
+            }
+        }
+        c->m = nm;
+    }
+    c->needsUpdate = 0;
+    c->touching = newTouching;
+}
+
+/* InternalDestroy(ContactID) (AabbTreeWorld.cpp:2245-2279). */
+static void contact_destroy(or_world* w, int cid) {
+    contact_t* c = &w->c[cid];
+    body_t* bA = &w->b[c->bA];
+    body_t* bB = &w->b[c->bB];
+    int k = kv_find(&bA->cids, cid);
+    if (k >= 0) { iv_erase_at(&bA->cids, k); iv_erase_at(&bA->ckeys, k); }
+    k = kv_find(&bB->cids, cid);
+    if (k >= 0) { iv_erase_at(&bB->cids, k); iv_erase_at(&bB->ckeys, k); }
+    if (c->m.count > 0 && !c->sensor) { body_set_awake(bA); body_set_awake(bB); }
+    c->alive = 0;
+    iv_push(&w->cfree, cid);
+}
+
+/* DestroyContacts (AabbTreeWorld.cpp:2290-2331), overlap pass only. */
+static int destroy_contacts(or_world* w) {
+    int n = 0, out = 0;
+    for (int i = 0; i < w->wcids.n; ++i) {
+        const int cid = (int)w->wcids.a[i];
+        const contact_t* c = &w->c[cid];
+        if (!aabb_overlap(w->p[c->pA].aabb, w->p[c->pB].aabb)) {
+            contact_destroy(w, cid);
+            ++n;
+        } else {
+            w->wcids.a[out] = w->wcids.a[i];
+            w->wkeys.a[out] = w->wkeys.a[i];
+            ++out;
+        }
+    }
+    w->wcids.n = out; w->wkeys.n = out;
+    return n;
+}
+
+/* UpdateContacts (AabbTreeWorld.cpp:2333-2415). */
+static int update_contacts(or_world* w, const or_stepconf* conf) {
+    int n = 0;
+    for (int i = 0; i < w->wcids.n; ++i) {
+        const int cid = (int)w->wcids.a[i];
+        if (w->c[cid].needsUpdate) { contact_update(w, cid, conf); ++n; }
+    }
+    return n;
+}
+
+/* Static median-split BVH over the fat AABBs: the same query result set as
+ * DynamicTree::Query (DynamicTree.cpp:673-700); FindContacts sorts and
+ * de-duplicates the results, so the traversal order does not matter. */
+typedef struct { real box[4]; int left, right, leaf; } bnode;
+typedef struct { bnode* n; int nn; int* idx; } bvh_t;
+static or_world* g_sort_world;
+static int g_sort_axis;
+static int cmp_proxy_center(const void* a, const void* b) {
+    const proxy_t* pa = &g_sort_world->p[*(const int*)a];
+    const proxy_t* pb = &g_sort_world->p[*(const int*)b];
+    const real ca = pa->aabb[g_sort_axis] + pa->aabb[g_sort_axis + 2];
+    const real cb = pb->aabb[g_sort_axis] + pb->aabb[g_sort_axis + 2];
+    return (ca < cb) ? -1 : (ca > cb) ? 1 : (*(const int*)a - *(const int*)b);
+}
+static int bvh_build(or_world* w, bvh_t* t, int* idx, int n) {
+    const int me = t->nn++;
+    bnode* nd = &t->n[me];
+    aabb_empty(nd->box);
+    for (int i = 0; i < n; ++i) {
+        const real* a = w->p[idx[i]].aabb;
+        nd->box[0] = minr(nd->box[0], a[0]); nd->box[1] = minr(nd->box[1], a[1]);
+        nd->box[2] = maxr(nd->box[2], a[2]); nd->box[3] = maxr(nd->box[3], a[3]);
+    }
+    if (n == 1) { nd->leaf = idx[0]; nd->left = nd->right = -1; return me; }
+    nd->leaf = -1;
+    g_sort_world = w;
+    g_sort_axis = ((nd->box[2] - nd->box[0]) >= (nd->box[3] - nd->box[1])) ? 0 : 1;
+    qsort(idx, (size_t)n, sizeof(int), cmp_proxy_center);
+    const int h = n / 2;
+    const int l = bvh_build(w, t, idx, h);
+    const int r = bvh_build(w, t, idx + h, n - h);
+    t->n[me].left = l; t->n[me].right = r;
+    return me;
+}
+
+typedef struct { uint64_t key; int pmin, pmax; } pkey;
+static int cmp_pkey(const void* a, const void* b) {
+    const uint64_t ka = ((const pkey*)a)->key, kb = ((const pkey*)b)->key;
+    return (ka < kb) ? -1 : (ka > kb) ? 1 : 0;
+}
+
+/* FindContacts (AabbTreeWorld.cpp:709-751) + AddContacts (:2423-2547). */
+static int find_and_add_contacts(or_world* w, const or_stepconf* conf) {
+    if (w->proxiesForContacts.n == 0 || w->np == 0) { iv_free(&w->proxiesForContacts); return 0; }
+    bvh_t t;
+    t.n = (bnode*)malloc(sizeof(bnode) * (size_t)(2 * w->np));
+    t.nn = 0;
+    int* idx = (int*)malloc(sizeof(int) * (size_t)w->np);
+    int live = 0;
+    for (int i = 0; i < w->np; ++i) if (w->p[i].body >= 0) idx[live++] = i;
+    const int root = live ? bvh_build(w, &t, idx, live) : -1;
+    pkey* keys = NULL; int nk = 0, capk = 0;
+    int* stack = (int*)malloc(sizeof(int) * (size_t)(2 * w->np + 8));
+    for (int q = 0; q < w->proxiesForContacts.n; ++q) {
+        const int pid = (int)w->proxiesForContacts.a[q];
+        const proxy_t* pp = &w->p[pid];
+        if (pp->body < 0 || root < 0) continue;
+        int sp = 0;
+        stack[sp++] = root;
+        while (sp) {
+            const bnode* nd = &t.n[stack[--sp]];
+            if (!aabb_overlap(nd->box, pp->aabb)) continue;
+            if (nd->leaf >= 0) {
+                const int other = nd->leaf;
+                if (other != pid && w->p[other].body != pp->body) {
+                    GROW(keys, nk, capk, pkey);
+                    keys[nk].key = make_key(pid, other);
+                    keys[nk].pmin = pid < other ? pid : other;
+                    keys[nk].pmax = pid < other ? other : pid;
+                    ++nk;
+                }
+            } else {
+                stack[sp++] = nd->left;
+                stack[sp++] = nd->right;
+            }
+        }
+    }
+    free(stack); free(idx); free(t.n);
+    iv_free(&w->proxiesForContacts);
+    qsort(keys, (size_t)nk, sizeof(pkey), cmp_pkey);
+    int added = 0;
+    for (int i = 0; i < nk; ++i) {
+        if (i > 0 && keys[i].key == keys[i - 1].key) continue;
+        const proxy_t* pa = &w->p[keys[i].pmin];
+        const proxy_t* pb = &w->p[keys[i].pmax];
+        body_t* bA = &w->b[pa->body];
+        body_t* bB = &w->b[pb->body];
+        const shape_t* sA = &w->s[pa->shape];
+        const shape_t* sB = &w->s[pb->shape];
+        if (!(is_accelerable(bA) || is_accelerable(bB))) continue;
+        /* ShouldCollide(jointBuffer, bodyJoints, A, B) (AabbTreeWorld.cpp:479-490) */
+        int jointBlocks = 0;
+        for (int k = 0; k < bA->jids.n; ++k) {
+            if (bA->jother.a[k] == pb->body && !w->j[bA->jids.a[k]].collideConnected) { jointBlocks = 1; break; }
+        }
+        if (jointBlocks) continue;
+        /* ShouldCollide(Filter, Filter) (Filter.hpp:81-88) */
+        if ((sA->group == sB->group) && (sA->group != 0)) {
+            if (!(sA->group > 0)) continue;
+        } else if (!(((sA->mask & sB->cat) != 0) && ((sB->mask & sA->cat) != 0))) {
+            continue;
+        }
+        /* already exists? search the body with fewer contacts */
+        const ivec* kl = (bA->ckeys.n < bB->ckeys.n) ? &bA->ckeys : &bB->ckeys;
+        int exists = 0;
+        for (int k = 0; k < kl->n; ++k) if ((uint64_t)kl->a[k] == keys[i].key) { exists = 1; break; }
+        if (exists) continue;
+        int cid;
+        if (w->cfree.n) { cid = (int)w->cfree.a[--w->cfree.n]; }
+        else { GROW(w->c, w->nc, w->capc, contact_t); cid = w->nc++; }
+        contact_t* c = &w->c[cid];
+        memset(c, 0, sizeof(*c));
+        c->alive = 1;
+        c->key = keys[i].key;
+        c->pA = keys[i].pmin; c->pB = keys[i].pmax;
+        c->bA = pa->body; c->sA = pa->shape; c->cA = pa->child;
+        c->bB = pb->body; c->sB = pb->shape; c->cB = pb->child;
+        c->impenetrable = is_impenetrable(bA) || is_impenetrable(bB);
+        c->sensor = sA->sensor || sB->sensor;
+        c->friction = RSQRT(sA->friction * sB->friction); /* MixFriction (Contact.hpp:57-60) */
+        c->restitution = (sA->restitution > sB->restitution) ? sA->restitution : sB->restitution;
+        c->tangentSpeed = R(0);
+        c->m = man_empty();
+        c->needsUpdate = 1;
+        iv_push(&w->wkeys, (int64_t)c->key); iv_push(&w->wcids, cid);
+        iv_push(&bA->ckeys, (int64_t)c->key); iv_push(&bA->cids, cid);
+        iv_push(&bB->ckeys, (int64_t)c->key); iv_push(&bB->cids, cid);
+        if (!c->sensor) {
+            if (is_speedable(bA)) bA->flags |= BF_AWAKE;
+            if (is_speedable(bB)) bB->flags |= BF_AWAKE;
+        }
+        contact_update(w, cid, conf);
+        ++added;
+    }
+    free(keys);
+    return added;
+}
+
+/* CreateProxies (AabbTreeWorld.cpp:557-579). */
+static void create_proxies(or_world* w, int body, int shape, const or_stepconf* conf) {
+    body_t* b = &w->b[body];
+    const xf_t x0 = get_xf(b->pos0, b->lc);
+    const xf_t x1 = b->xf;
+    const v2 disp = vmul(vsub(x1.p, x0.p), conf->displaceMultiplier);
+    GROW(w->p, w->np, w->capp, proxy_t);
+    proxy_t* p = &w->p[w->np];
+    p->body = body; p->shape = shape; p->child = 0;
+    compute_aabb2(&w->s[shape].dp, x0, x1, p->aabb);
+    aabb_fatten(p->aabb, conf->aabbExtension);
+    aabb_displace(p->aabb, disp);
+    iv_push(&b->proxies, w->np);
+    iv_push(&w->proxiesForContacts, w->np);
+    w->np++;
+}
+
+/* AabbTreeWorld::Synchronize (AabbTreeWorld.cpp:2564-2585). */
+static int synchronize(or_world* w, int body, const or_stepconf* conf) {
+    body_t* b = &w->b[body];
+    const xf_t x0 = get_xf(b->pos0, b->lc);
+    const xf_t x1 = b->xf;
+    const v2 disp = vmul(vsub(x1.p, x0.p), conf->displaceMultiplier);
+    int n = 0;
+    for (int k = 0; k < b->proxies.n; ++k) {
+        proxy_t* p = &w->p[b->proxies.a[k]];
+        real aabb[4];
+        compute_aabb2(&w->s[p->shape].dp, x0, x1, aabb);
+        if (!aabb_contains(p->aabb, aabb)) {
+            aabb_fatten(aabb, conf->aabbExtension);
+            aabb_displace(aabb, disp);
+            memcpy(p->aabb, aabb, sizeof(aabb));
+            iv_push(&w->proxiesForContacts, b->proxies.a[k]);
+            ++n;
+        }
+    }
+    return n;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Solver (ContactSolver.cpp, VelocityConstraint.cpp, RevoluteJointConf.cpp). */
+/* ------------------------------------------------------------------------- */
+typedef struct { pos_t pos; pos_t vel; v2 lc; real invM, invI; } bc_t;
+typedef struct {
+    v2 rA, rB;
+    real ni, ti, nm, tm, vb;
+} vcp_t;
+typedef struct {
+    int bA, bB;
+    v2 n;
+    real friction, restitution, tangentSpeed;
+    int count;
+    vcp_t p[2];
+    real K[3];  /* k00 k11 k01 */
+    real NM[3]; /* normal mass 2x2: m00 m11 m01 */
+} vc_t;
+
+/* GetContactRelVelocity (d2/Math.cpp). */
+static inline v2 rel_vel(pos_t va, v2 rA, pos_t vb, v2 rB) {
+    const v2 velBrot = vmul(revperp(rB), vb.ang);
+    const v2 velArot = vmul(revperp(rA), va.ang);
+    return vsub(vadd(vb.lin, velBrot), vadd(va.lin, velArot));
+}
+
+/* GetWorldManifold (WorldManifold.cpp:111-132). */
+typedef struct { v2 n; int count; v2 pt[2]; real ni[2], ti[2], sep[2]; } wman_t;
+static wman_t world_manifold(const manifold* m, xf_t xfA, real rA, xf_t xfB, real rB) {
+    wman_t wm; memset(&wm, 0, sizeof(wm));
+    if (m->type == M_CIRCLES) {
+        const v2 pA = xform(m->lp, xfA);
+        const v2 pB = xform(m->p[0].lp, xfB);
+        const v2 n = unit_vector(vsub(pB, pA), V(R(1), R(0)));
+        const v2 cA = vadd(pA, vmul(n, rA));
+        const v2 cB = vsub(pB, vmul(n, rB));
+        wm.n = n; wm.count = 1;
+        wm.pt[0] = vdiv(vadd(cA, cB), R(2));
+        wm.ni[0] = m->p[0].ni; wm.ti[0] = m->p[0].ti;
+        wm.sep[0] = dot(vsub(cB, cA), n);
+    } else if (m->type == M_FACEA) {
+        const v2 n = urotate(m->ln, xfA.q);
+        const v2 planePoint = xform(m->lp, xfA);
+        wm.n = n; wm.count = m->count;
+        for (int i = 0; i < m->count; ++i) {
+            const v2 clip = xform(m->p[i].lp, xfB);
+            const v2 cA = vadd(clip, vmul(n, (rA - dot(vsub(clip, planePoint), n))));
+            const v2 cB = vsub(clip, vmul(n, rB));
+            wm.pt[i] = vdiv(vadd(cA, cB), R(2));
+            wm.ni[i] = m->p[i].ni; wm.ti[i] = m->p[i].ti;
+            wm.sep[i] = dot(vsub(cB, cA), n);
+        }
+    } else if (m->type == M_FACEB) {
+        const v2 n = urotate(m->ln, xfB.q);
+        const v2 planePoint = xform(m->lp, xfB);
+        wm.n = vneg(n); wm.count = m->count;
+        for (int i = 0; i < m->count; ++i) {
+            const v2 clip = xform(m->p[i].lp, xfA);
+            const v2 cB = vadd(clip, vmul(n, (rB - dot(vsub(clip, planePoint), n))));
+            const v2 cA = vsub(clip, vmul(n, rA));
+            wm.pt[i] = vdiv(vadd(cA, cB), R(2));
+            wm.ni[i] = m->p[i].ni; wm.ti[i] = m->p[i].ti;
+            wm.sep[i] = dot(vsub(cA, cB), n);
+        }
+    }
+    return wm;
+}
+
+/* VelocityConstraint ctor + GetPoint + ComputeK (VelocityConstraint.cpp:38-185). */
+static void make_vc(vc_t* vc, const contact_t* c, const wman_t* wm, const bc_t* bcs, const or_stepconf* conf) {
+    memset(vc, 0, sizeof(*vc));
+    vc->bA = c->bA; vc->bB = c->bB;
+    vc->n = wm->n;
+    vc->friction = c->friction; vc->restitution = c->restitution; vc->tangentSpeed = c->tangentSpeed;
+    const bc_t* A = &bcs[c->bA];
+    const bc_t* B = &bcs[c->bB];
+    const real invMass = A->invM + B->invM;
+    const v2 tangent = fwdperp(vc->n);
+    for (int j = 0; j < wm->count; ++j) {
+        vcp_t* p = &vc->p[vc->count];
+        const v2 relA = vsub(wm->pt[j], A->pos.lin);
+        const v2 relB = vsub(wm->pt[j], B->pos.lin);
+        p->ni = wm->ni[j] * conf->dtRatio;
+        p->ti = wm->ti[j] * conf->dtRatio;
+        {
+            const v2 dv = rel_vel(A->vel, relA, B->vel, relB);
+            const real vn = dot(dv, vc->n);
+            p->vb = (vn < -conf->velocityThreshold) ? -vc->restitution * vn : R(0);
+        }
+        p->rA = relA; p->rB = relB;
+        {
+            const real crA = cross(relA, vc->n), crB = cross(relB, vc->n);
+            const real iA = A->invI * (crA * crA);
+            const real iB = B->invI * (crB * crB);
+            const real value = invMass + iA + iB;
+            p->nm = (value != R(0)) ? R(1) / value : R(0);
+        }
+        {
+            const real crA = cross(relA, tangent), crB = cross(relB, tangent);
+            const real iA = A->invI * (crA * crA);
+            const real iB = B->invI * (crB * crB);
+            const real value = invMass + iA + iB;
+            p->tm = (value != R(0)) ? R(1) / value : R(0);
+        }
+        vc->count++;
+    }
+    if (conf->doBlocksolve && vc->count == 2) {
+        const real rnA0 = cross(vc->p[0].rA, vc->n), rnB0 = cross(vc->p[0].rB, vc->n);
+        const real rnA1 = cross(vc->p[1].rA, vc->n), rnB1 = cross(vc->p[1].rB, vc->n);
+        const real iMA0 = A->invI * (rnA0 * rnA0);
+        const real iMA1 = A->invI * (rnA1 * rnA1);
+        const real iMB0 = B->invI * (rnB0 * rnB0);
+        const real iMB1 = B->invI * (rnB1 * rnB1);
+        const real iMA = (A->invI * rnA0 * rnA1);
+        const real iMB = (B->invI * rnB0 * rnB1);
+        const real k00 = invMass + iMA0 + iMB0;
+        const real k11 = invMass + iMA1 + iMB1;
+        const real k01 = invMass + iMA + iMB;
+        const real k00_sq = k00 * k00;
+        const real k00_k11 = k00 * k11;
+        const real k01_sq = k01 * k01;
+        const real k_diff = k00_k11 - k01_sq;
+        const real maxCondNum = R(1000.0f);
+        if (k00_sq < maxCondNum * k_diff) {
+            vc->K[0] = k00; vc->K[1] = k11; vc->K[2] = k01;
+            /* Invert(Matrix22) (Math.hpp:430-442): cp = Cross(row0, row1) */
+            const real cp = cross(V(k00, k01), V(k01, k11));
+            if (!almost_zero(cp)) {
+                const real inv = R(1) / cp;
+                vc->NM[0] = k11 * inv;      /* [0][0] */
+                vc->NM[2] = -k01 * inv;     /* [0][1] */
+                vc->NM[1] = k00 * inv;      /* [1][1] */
+            }
+        } else {
+            memset(&vc->p[1], 0, sizeof(vc->p[1]));
+            vc->count = 1;
+        }
+    }
+}
+
+static inline void apply_imp(bc_t* b, v2 P, real L, int sign) {
+    if (sign < 0) {
+        b->vel.lin = vsub(b->vel.lin, vmul(P, b->invM));
+        b->vel.ang = b->vel.ang - b->invI * L;
+    } else {
+        b->vel.lin = vadd(b->vel.lin, vmul(P, b->invM));
+        b->vel.ang = b->vel.ang + b->invI * L;
+    }
+}
+
+/* CalcWarmStartVelocityDeltas + WarmStartVelocities (AabbTreeWorld.cpp:227-274). */
+static void warm_start(const vc_t* vc, bc_t* bcs) {
+    pos_t dA = {{R(0), R(0)}, R(0)}, dB = {{R(0), R(0)}, R(0)};
+    const v2 n = vc->n, t = fwdperp(vc->n);
+    bc_t* A = &bcs[vc->bA];
+    bc_t* B = &bcs[vc->bB];
+    for (int j = 0; j < vc->count; ++j) {
+        const vcp_t* p = &vc->p[j];
+        const v2 P = vadd(vmul(n, p->ni), vmul(t, p->ti));
+        const real LA = cross(p->rA, P);
+        const real LB = cross(p->rB, P);
+        dA.lin = vsub(dA.lin, vmul(P, A->invM)); dA.ang = dA.ang - A->invI * LA;
+        dB.lin = vadd(dB.lin, vmul(P, B->invM)); dB.ang = dB.ang + B->invI * LB;
+    }
+    A->vel.lin = vadd(A->vel.lin, dA.lin); A->vel.ang = A->vel.ang + dA.ang;
+    B->vel.lin = vadd(B->vel.lin, dB.lin); B->vel.ang = B->vel.ang + dB.ang;
+}
+
+/* BlockSolveUpdate (ContactSolver.cpp:100-111). */
+static real block_update(vc_t* vc, bc_t* bcs, real x0, real x1) {
+    bc_t* A = &bcs[vc->bA];
+    bc_t* B = &bcs[vc->bB];
+    const real d0 = x0 - vc->p[0].ni, d1 = x1 - vc->p[1].ni;
+    /* GetVelocityDelta (ContactSolver.cpp:69-98) */
+    const v2 P0 = vmul(vc->n, d0);
+    const v2 P1 = vmul(vc->n, d1);
+    const v2 P = vadd(P0, P1);
+    const real LA = cross(vc->p[0].rA, P0) + cross(vc->p[1].rA, P1);
+    const real LB = cross(vc->p[0].rB, P0) + cross(vc->p[1].rB, P1);
+    const v2 dvAl = vneg(vmul(P, A->invM)); const real dvAa = -(A->invI * LA);
+    const v2 dvBl = vmul(P, B->invM); const real dvBa = +(B->invI * LB);
+    A->vel.lin = vadd(A->vel.lin, dvAl); A->vel.ang = A->vel.ang + dvAa;
+    B->vel.lin = vadd(B->vel.lin, dvBl); B->vel.ang = B->vel.ang + dvBa;
+    vc->p[0].ni = x0; vc->p[1].ni = x1;
+    return maxr(fabs(x0), fabs(x1));
+}
+
+/* BlockSolveNormalConstraint (ContactSolver.cpp:245-335). */
+static real block_solve(vc_t* vc, bc_t* bcs) {
+    const v2 n = vc->n;
+    const bc_t* A = &bcs[vc->bA];
+    const bc_t* B = &bcs[vc->bB];
+    const v2 dv0 = rel_vel(A->vel, vc->p[0].rA, B->vel, vc->p[0].rB);
+    const v2 dv1 = rel_vel(A->vel, vc->p[1].rA, B->vel, vc->p[1].rB);
+    const real vn0 = dot(dv0, n), vn1 = dot(dv1, n);
+    const real b0 = vn0 - vc->p[0].vb, b1 = vn1 - vc->p[1].vb;
+    /* b - Transform(impulses, K): K * x with rows (k00 k01), (k01 k11) */
+    const real a0 = vc->p[0].ni, a1 = vc->p[1].ni;
+    real Kx0 = R(0); Kx0 += vc->K[0] * a0; Kx0 += vc->K[2] * a1;
+    real Kx1 = R(0); Kx1 += vc->K[2] * a0; Kx1 += vc->K[1] * a1;
+    const real bp0 = b0 - Kx0, bp1 = b1 - Kx1;
+    /* Case 1: x = -NM * b' */
+    {
+        real m0 = R(0); m0 += vc->NM[0] * bp0; m0 += vc->NM[2] * bp1;
+        real m1 = R(0); m1 += vc->NM[2] * bp0; m1 += vc->NM[1] * bp1;
+        const real x0 = -m0, x1 = -m1;
+        if (x0 >= R(0) && x1 >= R(0)) return block_update(vc, bcs, x0, x1);
+    }
+    /* Case 2 */
+    {
+        const real x0 = -vc->p[0].nm * bp0;
+        const real vn2 = vc->K[2] * x0 + bp1;
+        if (x0 >= R(0) && vn2 >= R(0)) return block_update(vc, bcs, x0, R(0));
+    }
+    /* Case 3 */
+    {
+        const real x1 = -vc->p[1].nm * bp1;
+        const real vn1b = vc->K[2] * x1 + bp0;
+        if (x1 >= R(0) && vn1b >= R(0)) return block_update(vc, bcs, R(0), x1);
+    }
+    /* Case 4 */
+    if (bp0 >= R(0) && bp1 >= R(0)) return block_update(vc, bcs, R(0), R(0));
+    return R(0);
+}
+
+/* SeqSolveNormalConstraint (ContactSolver.cpp:337-393) with dir = normal, and
+ * SolveTangentConstraint (:395-454) with dir = tangent. */
+static real seq_solve(vc_t* vc, bc_t* bcs, int tangentPass) {
+    real maxInc = R(0);
+    const v2 dir = tangentPass ? fwdperp(vc->n) : vc->n;
+    bc_t* A = &bcs[vc->bA];
+    bc_t* B = &bcs[vc->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    for (int k = (vc->count == 2) ? 1 : 0; k >= 0; --k) {
+        vcp_t* p = &vc->p[k];
+        const v2 cv = rel_vel(vA, p->rA, vB, p->rB);
+        real newImp, oldImp;
+        if (tangentPass) {
+            const real dvel = vc->tangentSpeed - dot(cv, dir);
+            const real lambda = p->tm * dvel;
+            const real maxImp = vc->friction * p->ni;
+            oldImp = p->ti;
+            newImp = clampr(oldImp + lambda, -maxImp, maxImp);
+        } else {
+            const real dvel = dot(cv, dir);
+            const real lambda = p->nm * (p->vb - dvel);
+            oldImp = p->ni;
+            newImp = maxr(oldImp + lambda, R(0));
+        }
+        const real inc = newImp - oldImp;
+        const v2 P = vmul(dir, inc);
+        const real LA = cross(p->rA, P);
+        const real LB = cross(p->rB, P);
+        vA.lin = vsub(vA.lin, vmul(P, A->invM)); vA.ang = vA.ang - A->invI * LA;
+        vB.lin = vadd(vB.lin, vmul(P, B->invM)); vB.ang = vB.ang + B->invI * LB;
+        maxInc = maxr(maxInc, fabs(inc));
+        if (tangentPass) p->ti = oldImp + inc; else p->ni = oldImp + inc;
+    }
+    A->vel = vA;
+    B->vel = vB;
+    return maxInc;
+}
+
+/* GaussSeidel::SolveVelocityConstraint (ContactSolver.cpp:481-492). */
+static real solve_vc(vc_t* vc, bc_t* bcs) {
+    real m = R(0);
+    m = maxr(m, seq_solve(vc, bcs, 1));
+    const int useSeq = (vc->count == 1) || (vc->K[0] == R(0) && vc->K[1] == R(0) && vc->K[2] == R(0));
+    m = maxr(m, useSeq ? seq_solve(vc, bcs, 0) : block_solve(vc, bcs));
+    return m;
+}
+
+/* GetPSM (PositionSolverManifold.cpp:103-121). */
+typedef struct { v2 n, pt; real sep; } psm_t;
+static psm_t get_psm(const manifold* m, int idx, xf_t xfA, xf_t xfB) {
+    psm_t r;
+    if (m->type == M_CIRCLES) {
+        const v2 pA = xform(m->lp, xfA);
+        const v2 pB = xform(m->p[idx].lp, xfB);
+        const v2 delta = vsub(pB, pA);
+        r.n = unit_vector(delta, V(R(0), R(0)));
+        r.pt = vdiv(vadd(pA, pB), R(2));
+        r.sep = dot(delta, r.n);
+    } else if (m->type == M_FACEA) {
+        const v2 planePoint = xform(m->lp, xfA);
+        r.n = urotate(m->ln, xfA.q);
+        r.pt = xform(m->p[idx].lp, xfB);
+        r.sep = dot(vsub(r.pt, planePoint), r.n);
+    } else {
+        const v2 planePoint = xform(m->lp, xfB);
+        const v2 n = urotate(m->ln, xfB.q);
+        r.pt = xform(m->p[idx].lp, xfA);
+        r.sep = dot(vsub(r.pt, planePoint), n);
+        r.n = vneg(n);
+    }
+    return r;
+}
+
+typedef struct { const manifold* m; int bA, bB; real totalRadius; } pc_t;
+typedef struct { pos_t a, b; real sep; } psol_t;
+
+/* solver_fn lambda of GaussSeidel::SolvePositionConstraint (ContactSolver.cpp:521-551). */
+static psol_t pos_solver_fn(psm_t psm, v2 pA, v2 pB, real invMassA, real invIA, real invMassB, real invIB,
+                            real totalRadius, const or_stepconf* conf) {
+    const real invMassTotal = invMassA + invMassB;
+    const real separation = psm.sep - totalRadius;
+    const v2 rA = vsub(psm.pt, pA);
+    const v2 rB = vsub(psm.pt, pB);
+    const real cA = cross(rA, psm.n), cB = cross(rB, psm.n);
+    const real K = invMassTotal + invIA * (cA * cA) + invIB * (cB * cB);
+    const real C = -clampr(conf->regResolutionRate * (separation + conf->linearSlop), -conf->maxLinearCorrection, R(0));
+    const v2 P = vdiv(vmul(psm.n, C), K);
+    const real LA = cross(rA, P);
+    const real LB = cross(rB, P);
+    psol_t s;
+    s.a.lin = vneg(vmul(P, invMassA)); s.a.ang = -(invIA * LA);
+    s.b.lin = vmul(P, invMassB); s.b.ang = +(invIB * LB);
+    s.sep = separation;
+    return s;
+}
+
+static inline pos_t padd(pos_t a, pos_t b) { pos_t r; r.lin = vadd(a.lin, b.lin); r.ang = a.ang + b.ang; return r; }
+
+/* GaussSeidel::SolvePositionConstraint (ContactSolver.cpp:494-643). */
+static real solve_pc(const pc_t* pc, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[pc->bA];
+    bc_t* B = &bcs[pc->bB];
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    pos_t posA = A->pos, posB = B->pos;
+    real minSep = RINF;
+    const int count = pc->m->count;
+    if (count == 1) {
+        const psm_t psm0 = get_psm(pc->m, 0, get_xf(posA, A->lc), get_xf(posB, B->lc));
+        const psol_t s = pos_solver_fn(psm0, posA.lin, posB.lin, iMA, iIA, iMB, iIB, pc->totalRadius, conf);
+        posA = padd(posA, s.a); posB = padd(posB, s.b);
+        minSep = R(0) + s.sep;
+    } else if (count == 2) {
+        const xf_t xfA = get_xf(posA, A->lc), xfB = get_xf(posB, B->lc);
+        const psm_t psm0 = get_psm(pc->m, 0, xfA, xfB);
+        const psm_t psm1 = get_psm(pc->m, 1, xfA, xfB);
+        if (almost_equal(psm0.sep, psm1.sep)) {
+            const psol_t s0 = pos_solver_fn(psm0, posA.lin, posB.lin, iMA, iIA, iMB, iIB, pc->totalRadius, conf);
+            const psol_t s1 = pos_solver_fn(psm1, posA.lin, posB.lin, iMA, iIA, iMB, iIB, pc->totalRadius, conf);
+            posA = padd(padd(posA, s0.a), s1.a);
+            posB = padd(padd(posB, s0.b), s1.b);
+            minSep = s0.sep;
+        } else if (psm0.sep < psm1.sep) {
+            const psol_t s0 = pos_solver_fn(psm0, posA.lin, posB.lin, iMA, iIA, iMB, iIB, pc->totalRadius, conf);
+            posA = padd(posA, s0.a); posB = padd(posB, s0.b);
+            const psm_t p1 = get_psm(pc->m, 1, get_xf(posA, A->lc), get_xf(posB, B->lc));
+            const psol_t s1 = pos_solver_fn(p1, posA.lin, posB.lin, iMA, iIA, iMB, iIB, pc->totalRadius, conf);
+            posA = padd(posA, s1.a); posB = padd(posB, s1.b);
+            minSep = s0.sep;
+        } else if (psm1.sep < psm0.sep) {
+            const psol_t s1 = pos_solver_fn(psm1, posA.lin, posB.lin, iMA, iIA, iMB, iIB, pc->totalRadius, conf);
+            posA = padd(posA, s1.a); posB = padd(posB, s1.b);
+            const psm_t p0 = get_psm(pc->m, 0, get_xf(posA, A->lc), get_xf(posB, B->lc));
+            const psol_t s0 = pos_solver_fn(p0, posA.lin, posB.lin, iMA, iIA, iMB, iIB, pc->totalRadius, conf);
+            posA = padd(posA, s0.a); posB = padd(posB, s0.b);
+            minSep = s1.sep;
+        }
+    }
+    A->pos = posA;
+    B->pos = posB;
+    return minSep;
+}
+
+/* Revolute joint InitVelocity (RevoluteJointConf.cpp:127-225), no motor/limit
+ * beyond what the reference supports. */
+static void rj_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const real aA = A->pos.ang, aB = B->pos.ang;
+    pos_t vA = A->vel, vB = B->vel;
+    const v2 qA = unit_from_angle(aA), qB = unit_from_angle(aB);
+    j->rA = rotate(vsub(j->laA, A->lc), qA);
+    j->rB = rotate(vsub(j->laB, B->lc), qB);
+    const real totInvI = iIA + iIB;
+    const int fixedRotation = (totInvI == R(0));
+    /* GetMat33 (RevoluteJointConf.cpp:35-63) */
+    {
+        const v2 rA = j->rA, rB = j->rB;
+        const real exx = iMA + ((rA.y * rA.y) * iIA) + iMB + ((rB.y * rB.y) * iIB);
+        const real eyx = (-rA.y * rA.x * iIA) + (-rB.y * rB.x * iIB);
+        const real ezx = (-rA.y * iIA) + (-rB.y * iIB);
+        const real eyy = iMA + ((rA.x * rA.x) * iIA) + iMB + ((rB.x * rB.x) * iIB);
+        const real ezy = (rA.x * iIA) + (rB.x * iIB);
+        j->mass[0][0] = exx; j->mass[1][0] = eyx; j->mass[2][0] = ezx;
+        j->mass[0][1] = eyx; j->mass[1][1] = eyy; j->mass[2][1] = ezy;
+        j->mass[0][2] = ezx; j->mass[1][2] = ezy; j->mass[2][2] = totInvI;
+    }
+    j->angularMass = (totInvI > R(0)) ? R(1) / totInvI : R(0);
+    if (!j->enableMotor || fixedRotation) j->motorImpulse = R(0);
+    if (j->enableLimit && !fixedRotation) {
+        const real jointAngle = aB - aA - j->refAngle;
+        if (fabs(j->upper - j->lower) < (conf->angularSlop * R(2))) j->limitState = LS_EQUAL;
+        else if (jointAngle <= j->lower) { if (j->limitState != LS_LOWER) { j->limitState = LS_LOWER; j->imp[2] = R(0); } }
+        else if (jointAngle >= j->upper) { if (j->limitState != LS_UPPER) { j->limitState = LS_UPPER; j->imp[2] = R(0); } }
+        else { j->limitState = LS_INACTIVE; j->imp[2] = R(0); }
+    } else {
+        j->limitState = LS_INACTIVE;
+    }
+    if (conf->doWarmStart) {
+        j->imp[0] *= conf->dtRatio; j->imp[1] *= conf->dtRatio; j->imp[2] *= conf->dtRatio;
+        j->motorImpulse *= conf->dtRatio;
+        const v2 P = V(j->imp[0], j->imp[1]);
+        const real L = j->motorImpulse + j->imp[2];
+        const real LA = cross(j->rA, P) + L;
+        const real LB = cross(j->rB, P) + L;
+        vA.lin = vsub(vA.lin, vmul(P, iMA)); vA.ang = vA.ang - iIA * LA;
+        vB.lin = vadd(vB.lin, vmul(P, iMB)); vB.ang = vB.ang + iIB * LB;
+    } else {
+        j->imp[0] = j->imp[1] = j->imp[2] = R(0);
+        j->motorImpulse = R(0);
+    }
+    A->vel = vA;
+    B->vel = vB;
+}
+
+/* Solve22 (Math.hpp:462-474) on the upper 2x2 of a Mat33 (column-major here). */
+static v2 solve22(real m[3][3], v2 b) {
+    const real xx = m[0][0], xy = m[1][0], yx = m[0][1], yy = m[1][1];
+    const real cp = xx * yy - xy * yx;
+    const real det = (cp != R(0)) ? (R(1) / cp) : cp;
+    return V(det * (yy * b.x - xy * b.y), det * (xx * b.y - yx * b.x));
+}
+
+/* Revolute SolveVelocity (RevoluteJointConf.cpp:228-330), point constraint and
+ * motor; limits are restated for the inactive state only. */
+static int rj_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    const pos_t oA = A->vel, oB = B->vel;
+    pos_t vA = oA, vB = oB;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const int fixedRotation = (iIA + iIB == R(0));
+    if (j->enableMotor && (j->limitState != LS_EQUAL) && !fixedRotation) {
+        const real impulse = -j->angularMass * (vB.ang - vA.ang - j->motorSpeed);
+        const real oldImpulse = j->motorImpulse;
+        const real maxImpulse = conf->deltaTime * j->maxMotorTorque;
+        j->motorImpulse = clampr(j->motorImpulse + impulse, -maxImpulse, maxImpulse);
+        const real inc = j->motorImpulse - oldImpulse;
+        vA.ang -= iIA * inc;
+        vB.ang += iIB * inc;
+    }
+    const v2 vb = vadd(vB.lin, vmul(revperp(j->rB), vB.ang));
+    const v2 va = vadd(vA.lin, vmul(revperp(j->rA), vA.ang));
+    const v2 vDelta = vsub(vb, va);
+    {
+        const v2 impulse = solve22(j->mass, vneg(vDelta));
+        j->imp[0] += impulse.x;
+        j->imp[1] += impulse.y;
+        const v2 P = impulse;
+        const real LA = cross(j->rA, P);
+        const real LB = cross(j->rB, P);
+        vA.lin = vsub(vA.lin, vmul(P, iMA)); vA.ang = vA.ang - iIA * LA;
+        vB.lin = vadd(vB.lin, vmul(P, iMB)); vB.ang = vB.ang + iIB * LB;
+    }
+    if (vA.lin.x != oA.lin.x || vA.lin.y != oA.lin.y || vA.ang != oA.ang ||
+        vB.lin.x != oB.lin.x || vB.lin.y != oB.lin.y || vB.ang != oB.ang) {
+        A->vel = vA;
+        B->vel = vB;
+        return 0;
+    }
+    return 1;
+}
+
+/* Revolute SolvePosition (RevoluteJointConf.cpp:333-431), point constraint. */
+static int rj_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t posA = A->pos, posB = B->pos;
+    const real iIA = A->invI, iIB = B->invI;
+    const real angularError = R(0);
+    real positionError;
+    {
+        const v2 qA = unit_from_angle(posA.ang), qB = unit_from_angle(posB.ang);
+        const v2 rA = rotate(vsub(j->laA, A->lc), qA);
+        const v2 rB = rotate(vsub(j->laB, B->lc), qB);
+        const v2 C = vsub(vadd(posB.lin, rB), vadd(posA.lin, rA));
+        positionError = mag2(C);
+        const real iMA = A->invM, iMB = B->invM;
+        const real exx = iMA + (iIA * (rA.y * rA.y)) + iMB + (iIB * (rB.y * rB.y));
+        const real exy = (-iIA * rA.x * rA.y) + (-iIB * rB.x * rB.y);
+        const real eyy = iMA + (iIA * (rA.x * rA.x)) + iMB + (iIB * (rB.x * rB.x));
+        /* Solve(K, C) (Math.hpp:410-426): cp = Cross(col0, col1) */
+        const real cp = cross(V(exx, exy), V(exy, eyy));
+        v2 x = V(R(0), R(0));
+        if (!almost_zero(cp)) {
+            const real inv = R(1) / cp;
+            x = V((eyy * C.x - exy * C.y) * inv, (exx * C.y - exy * C.x) * inv);
+        }
+        const v2 P = vneg(x);
+        posA.lin = vsub(posA.lin, vmul(P, iMA)); posA.ang = posA.ang - iIA * cross(rA, P);
+        posB.lin = vadd(posB.lin, vmul(P, iMB)); posB.ang = posB.ang + iIB * cross(rB, P);
+    }
+    A->pos = posA;
+    B->pos = posB;
+    return (positionError <= conf->linearSlop * conf->linearSlop) && (angularError <= conf->angularSlop);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Islands and the regular phase (AabbTreeWorld.cpp:1358-1683).               */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    ivec bodies, contacts, joints;
+} island_t;
+
+static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc_t* bcs,
+                         or_stepstats* st) {
+    const real h = conf->deltaTime;
+    /* pos0 <- pos1 (:1574-1580) */
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        body_t* b = &w->b[isl->bodies.a[i]];
+        b->pos0 = b->pos1;
+    }
+    /* GetBodyConstraints -> GetBodyConstraint: Cap(GetVelocity(body, h)) (Body.cpp:290-309,
+     * Velocity.cpp:26-45). */
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        const int id = (int)isl->bodies.a[i];
+        const body_t* b = &w->b[id];
+        bc_t* bc = &bcs[id];
+        bc->invM = b->invM; bc->invI = b->invI; bc->lc = b->lc; bc->pos = b->pos1;
+        pos_t v = b->vel;
+        if (is_accelerable(b)) {
+            v.lin = vadd(v.lin, vmul(b->la, h));
+            v.ang = v.ang + h * b->aa;
+            v.lin = vdiv(v.lin, R(1) + h * b->ldamp);
+            v.ang = v.ang / (R(1) + h * b->adamp);
+        }
+        {
+            const v2 translation = vmul(v.lin, h);
+            const real lsq = mag2(translation);
+            if (lsq > conf->maxTranslation * conf->maxTranslation) {
+                const real ratio = conf->maxTranslation / RSQRT(lsq);
+                v.lin = vmul(v.lin, ratio);
+            }
+            const real absRot = fabs(h * v.ang);
+            if (absRot > conf->maxRotation) {
+                const real ratio = conf->maxRotation / absRot;
+                v.ang = v.ang * ratio;
+            }
+        }
+        bc->vel = v;
+    }
+    const int nc = isl->contacts.n;
+    pc_t* pcs = (pc_t*)malloc(sizeof(pc_t) * (size_t)(nc + 1));
+    vc_t* vcs = (vc_t*)malloc(sizeof(vc_t) * (size_t)(nc + 1));
+    for (int i = 0; i < nc; ++i) {
+        const contact_t* c = &w->c[isl->contacts.a[i]];
+        const real rA = w->s[c->sA].dp.r, rB = w->s[c->sB].dp.r;
+        pcs[i].m = &c->m; pcs[i].bA = c->bA; pcs[i].bB = c->bB; pcs[i].totalRadius = rA + rB;
+    }
+    for (int i = 0; i < nc; ++i) {
+        const contact_t* c = &w->c[isl->contacts.a[i]];
+        const bc_t* A = &bcs[c->bA];
+        const bc_t* B = &bcs[c->bB];
+        const real rA = w->s[c->sA].dp.r, rB = w->s[c->sB].dp.r;
+        const xf_t xfA = get_xf(A->pos, A->lc), xfB = get_xf(B->pos, B->lc);
+        const wman_t wm = world_manifold(&c->m, xfA, rA, xfB, rB);
+        make_vc(&vcs[i], c, &wm, bcs, conf);
+    }
+    if (conf->doWarmStart) {
+        for (int i = 0; i < nc; ++i) warm_start(&vcs[i], bcs);
+    }
+    for (int i = 0; i < isl->joints.n; ++i) rj_init_velocity(&w->j[isl->joints.a[i]], bcs, conf);
+
+    int velIters = conf->regVelocityIters;
+    real maxInc = R(0);
+    for (int it = 0; it < conf->regVelocityIters; ++it) {
+        int jointsOkay = 1;
+        for (int i = 0; i < isl->joints.n; ++i) jointsOkay &= rj_solve_velocity(&w->j[isl->joints.a[i]], bcs, conf);
+        real newInc = R(0);
+        for (int i = 0; i < nc; ++i) newInc = maxr(newInc, solve_vc(&vcs[i], bcs));
+        maxInc = maxr(maxInc, newInc);
+        if (jointsOkay && (newInc <= conf->regMinMomentum)) { velIters = it + 1; break; }
+    }
+    /* IntegratePositions (:176-188) */
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        bc_t* bc = &bcs[isl->bodies.a[i]];
+        const v2 tr = vmul(bc->vel.lin, h);
+        const real rot = h * bc->vel.ang;
+        bc->pos.lin = vadd(bc->pos.lin, tr);
+        bc->pos.ang = bc->pos.ang + rot;
+    }
+    int solved = 0, posIters = conf->regPositionIters;
+    real minSepIsland = RINF;
+    for (int it = 0; it < conf->regPositionIters; ++it) {
+        real minSep = RINF;
+        for (int i = 0; i < nc; ++i) minSep = minr(minSep, solve_pc(&pcs[i], bcs, conf));
+        minSepIsland = minr(minSepIsland, minSep);
+        const int contactsOkay = (minSep >= conf->regMinSeparation);
+        int jointsOkay = 1;
+        for (int i = 0; i < isl->joints.n; ++i) jointsOkay &= rj_solve_position(&w->j[isl->joints.a[i]], bcs, conf);
+        if (contactsOkay && jointsOkay) { posIters = it + 1; solved = 1; break; }
+    }
+    /* AssignImpulses (:196-220) */
+    for (int i = 0; i < nc; ++i) {
+        contact_t* c = &w->c[isl->contacts.a[i]];
+        for (int k = 0; k < vcs[i].count; ++k) { c->m.p[k].ni = vcs[i].p[k].ni; c->m.p[k].ti = vcs[i].p[k].ti; }
+    }
+    /* write back (:1652-1664) */
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        const int id = (int)isl->bodies.a[i];
+        body_t* b = &w->b[id];
+        const bc_t* bc = &bcs[id];
+        b->vel = bc->vel;
+        if (b->pos1.lin.x != bc->pos.lin.x || b->pos1.lin.y != bc->pos.lin.y || b->pos1.ang != bc->pos.ang) {
+            body_set_pos1(b, bc->pos);
+            for (int k = 0; k < b->cids.n; ++k) w->c[b->cids.a[k]].needsUpdate = 1;
+        }
+    }
+    /* UpdateUnderActiveTimes + Sleepem (:403-429) */
+    real minUat = RINF;
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        body_t* b = &w->b[isl->bodies.a[i]];
+        if (is_speedable(b)) {
+            const real lin2 = mag2(b->vel.lin);
+            const real ang2 = b->vel.ang * b->vel.ang;
+            const int under = (ang2 <= conf->angularSleepTolerance * conf->angularSleepTolerance) &&
+                              (lin2 <= conf->linearSleepTolerance * conf->linearSleepTolerance);
+            const int sleepable = (b->flags & BF_ALLOW_SLEEP) != 0;
+            const real t = (sleepable && under) ? b->uat + conf->deltaTime : R(0);
+            b->uat = t;
+            minUat = minr(minUat, t);
+        }
+    }
+    if ((minUat >= conf->minStillTimeToSleep) && solved) {
+        for (int i = 0; i < isl->bodies.n; ++i) st->regBodiesSlept += body_unawaken(&w->b[isl->bodies.a[i]]);
+    }
+    if (solved) st->regIslandsSolved++;
+    st->regSumPosIters += posIters;
+    st->regSumVelIters += velIters;
+    st->regMinSeparation = minr(st->regMinSeparation, minSepIsland);
+    st->regMaxIncImpulse = maxr(st->regMaxIncImpulse, maxInc);
+    free(pcs); free(vcs);
+}
+
+/* SolveReg (AabbTreeWorld.cpp:1472-1561) with AddToIsland (:1358-1470). */
+static void solve_reg(or_world* w, const or_stepconf* conf, or_stepstats* st) {
+    unsigned char* ib = (unsigned char*)calloc((size_t)w->nb + 1, 1);
+    unsigned char* ic = (unsigned char*)calloc((size_t)w->nc + 1, 1);
+    unsigned char* ij = (unsigned char*)calloc((size_t)w->nj + 1, 1);
+    bc_t* bcs = (bc_t*)calloc((size_t)w->nb + 1, sizeof(bc_t));
+    int* stack = (int*)malloc(sizeof(int) * (size_t)(w->nb + 1));
+    island_t isl;
+    memset(&isl, 0, sizeof(isl));
+    for (int seed = 0; seed < w->nb; ++seed) {
+        body_t* sb = &w->b[seed];
+        if (ib[seed]) continue;
+        if (!((sb->flags & BF_AWAKE) && (sb->flags & BF_ENABLED))) continue;
+        st->regIslandsFound++;
+        isl.bodies.n = isl.contacts.n = isl.joints.n = 0;
+        int sp = 0;
+        stack[sp++] = seed;
+        ib[seed] = 1;
+        while (sp) {
+            const int id = stack[--sp];
+            body_t* b = &w->b[id];
+            iv_push(&isl.bodies, id);
+            if (!is_speedable(b)) continue;
+            b->flags |= BF_AWAKE;
+            for (int k = 0; k < b->cids.n; ++k) {
+                const int cid = (int)b->cids.a[k];
+                if (ic[cid]) continue;
+                const contact_t* c = &w->c[cid];
+                if (c->touching && !c->sensor) {
+                    const int other = (c->bA == id) ? c->bB : c->bA;
+                    iv_push(&isl.contacts, cid);
+                    ic[cid] = 1;
+                    if (!ib[other]) { ib[other] = 1; stack[sp++] = other; }
+                }
+            }
+            for (int k = 0; k < b->jids.n; ++k) {
+                const int jid = (int)b->jids.a[k];
+                if (ij[jid]) continue;
+                const int other = (int)b->jother.a[k];
+                if (w->b[other].flags & BF_ENABLED) {
+                    ij[jid] = 1;
+                    iv_push(&isl.joints, jid);
+                    if (!ib[other]) { ib[other] = 1; stack[sp++] = other; }
+                }
+            }
+        }
+        for (int i = 0; i < isl.bodies.n; ++i) {
+            const int id = (int)isl.bodies.a[i];
+            if (!is_speedable(&w->b[id])) ib[id] = 0;
+        }
+        solve_island(w, conf, &isl, bcs, st);
+    }
+    for (int id = 0; id < w->nb; ++id) {
+        if (ib[id] && is_speedable(&w->b[id])) st->regProxiesMoved += synchronize(w, id, conf);
+    }
+    st->regContactsUpdated += update_contacts(w, conf);
+    st->regContactsAdded += find_and_add_contacts(w, conf);
+    iv_free(&isl.bodies); iv_free(&isl.contacts); iv_free(&isl.joints);
+    free(ib); free(ic); free(ij); free(bcs); free(stack);
+}
+
+/* Step(AabbTreeWorld&, StepConf) (AabbTreeWorld.cpp:2144-2219), doToi = false. */
+void or_step(or_world* w, const or_stepconf* conf, or_stepstats* st) {
+    or_stepstats local;
+    if (!st) st = &local;
+    memset(st, 0, sizeof(*st));
+    st->regMinSeparation = RINF;
+    for (int i = 0; i < w->fixturesForProxies.n; ++i) {
+        const int body = (int)(w->fixturesForProxies.a[i] >> 32);
+        const int shape = (int)(w->fixturesForProxies.a[i] & 0xffffffff);
+        create_proxies(w, body, shape, conf);
+        st->preProxiesCreated++;
+    }
+    w->fixturesForProxies.n = 0;
+    for (int i = 0; i < w->bodiesForSync.n; ++i) st->preProxiesMoved += synchronize(w, (int)w->bodiesForSync.a[i], conf);
+    w->bodiesForSync.n = 0;
+    st->preContactsDestroyed = destroy_contacts(w);
+    st->preContactsUpdated = update_contacts(w, conf);
+    st->preContactsAdded = find_and_add_contacts(w, conf);
+    if (conf->deltaTime != R(0)) {
+        w->inv_dt0 = R(1) / conf->deltaTime;
+        solve_reg(w, conf, st);
+    }
+}
+
+/* StepConf defaults (StepConf.hpp:59-161, Settings.hpp). */
+void or_default_conf(or_stepconf* c) {
+    const real Pi = R(3.14159265358979323846264338327950288L);
+    const real linearSlop = R(0.005);
+    memset(c, 0, sizeof(*c));
+    c->deltaTime = R(1) / R(60);
+    c->dtRatio = R(1);
+    c->minStillTimeToSleep = R(1) / R(2);
+    c->linearSlop = linearSlop;
+    c->angularSlop = (Pi * R(2)) / R(180);
+    c->regResolutionRate = R(2) / R(10);
+    c->regMinSeparation = -linearSlop * R(3);
+    c->regMinMomentum = R(0) / R(100);
+    c->velocityThreshold = R(1);
+    c->maxTranslation = R(2);
+    c->maxRotation = R(179) * ((R(1) * Pi) / R(180));
+    c->maxLinearCorrection = R(0.2);
+    c->maxAngularCorrection = R(8.0f / 180.0f) * Pi;
+    c->linearSleepTolerance = R(0.01);
+    c->angularSleepTolerance = R((Pi * R(2)) / R(180));
+    c->displaceMultiplier = R(2);
+    c->aabbExtension = linearSlop * R(20);
+    c->maxCirclesRatio = R(10);
+    c->regVelocityIters = 8;
+    c->regPositionIters = 3;
+    c->doWarmStart = 1;
+    c->doBlocksolve = 1;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Queries.                                                                   */
+/* ------------------------------------------------------------------------- */
+int or_body_count(const or_world* w) { return w->nb; }
+void or_get_body(const or_world* w, int id, real* o, int* awake) {
+    const body_t* b = &w->b[id];
+    o[0] = b->pos1.lin.x; o[1] = b->pos1.lin.y; o[2] = b->pos1.ang;
+    o[3] = b->vel.lin.x; o[4] = b->vel.lin.y; o[5] = b->vel.ang;
+    o[6] = b->xf.p.x; o[7] = b->xf.p.y; o[8] = b->xf.q.x; o[9] = b->xf.q.y;
+    o[10] = b->invM; o[11] = b->invI; o[12] = b->uat;
+    if (awake) *awake = (b->flags & BF_AWAKE) ? 1 : 0;
+}
+void or_get_local_center(const or_world* w, int id, real* o) { o[0] = w->b[id].lc.x; o[1] = w->b[id].lc.y; }
+/* SetTransformation-like state override used by tests; queues proxy sync. */
+void or_set_body_state(or_world* w, int id, real px, real py, real angle, real vx, real vy, real av) {
+    body_t* b = &w->b[id];
+    pos_t p; p.lin = V(px, py); p.ang = angle;
+    b->pos0 = p;
+    body_set_pos1(b, p);
+    b->vel.lin = V(vx, vy); b->vel.ang = av;
+    for (int k = 0; k < b->cids.n; ++k) w->c[b->cids.a[k]].needsUpdate = 1;
+    iv_push(&w->bodiesForSync, id);
+}
+int or_contact_count(const or_world* w) { return w->wcids.n; }
+void or_get_contact(const or_world* w, int k, int* io, real* fo, int* feat) {
+    const int cid = (int)w->wcids.a[k];
+    const contact_t* c = &w->c[cid];
+    io[0] = cid; io[1] = c->pA; io[2] = c->pB; io[3] = c->bA; io[4] = c->sA; io[5] = c->cA;
+    io[6] = c->bB; io[7] = c->sB; io[8] = c->cB; io[9] = c->touching; io[10] = c->m.type; io[11] = c->m.count;
+    fo[0] = c->m.ln.x; fo[1] = c->m.ln.y; fo[2] = c->m.lp.x; fo[3] = c->m.lp.y;
+    for (int i = 0; i < 2; ++i) {
+        fo[4 + 4 * i] = c->m.p[i].lp.x; fo[5 + 4 * i] = c->m.p[i].lp.y;
+        fo[6 + 4 * i] = c->m.p[i].ni; fo[7 + 4 * i] = c->m.p[i].ti;
+        feat[4 * i + 0] = c->m.p[i].tA; feat[4 * i + 1] = c->m.p[i].iA;
+        feat[4 * i + 2] = c->m.p[i].tB; feat[4 * i + 3] = c->m.p[i].iB;
+    }
+}
+int or_proxy_count(const or_world* w) { return w->np; }
+void or_get_proxy(const or_world* w, int p, int* bsc, real* aabb) {
+    bsc[0] = w->p[p].body; bsc[1] = w->p[p].shape; bsc[2] = w->p[p].child;
+    memcpy(aabb, w->p[p].aabb, 4 * sizeof(real));
+}

@@ -1,0 +1,119 @@
+/*
+ * playrho_oracle.h -- CPU restatement of the PlayRho 2.0.0 world step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA world step is checked
+ * against: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+ * may load it.  Nothing in the shipped library links or calls it.
+ *
+ * It restates, in plain C, the reference's regular-phase Step for disks, convex
+ * polygons, edges and revolute joints (file:line citations are on each function
+ * in playrho_oracle.c).  It follows the reference's operation order closely so
+ * that the FP32 build reproduces the reference's FP32 results, and it builds a
+ * second time with OR_DOUBLE for the FP64 oracle.
+ *
+ * Pinning: tests/test_oracle_kat.py checks it against the known-answer values
+ * transcribed from the reference's own unit tests and HelloWorld expected
+ * output; tests/test_oracle_vs_reference.py checks it against the reference
+ * compiled from source (oracle/ref) whenever that build is available.
+ */
+#ifndef PLAYRHO_ORACLE_H
+#define PLAYRHO_ORACLE_H
+
+#ifdef OR_DOUBLE
+typedef double or_real;
+#else
+typedef float or_real;
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { OR_STATIC = 0, OR_KINEMATIC = 1, OR_DYNAMIC = 2 };
+enum { OR_SHAPE_DISK = 0, OR_SHAPE_POLYGON = 1, OR_SHAPE_EDGE = 2 };
+enum { OR_MAXV = 16 };
+
+/* Body flags accepted by or_add_body (subset of BodyConf booleans). */
+enum {
+    OR_BF_ALLOW_SLEEP = 1u,
+    OR_BF_AWAKE = 2u,
+    OR_BF_FIXED_ROTATION = 4u,
+    OR_BF_ENABLED = 8u,
+};
+
+/* Mirrors the StepConf fields the regular phase reads (StepConf.hpp:165-340). */
+typedef struct or_stepconf {
+    or_real deltaTime, dtRatio, minStillTimeToSleep, linearSlop, angularSlop;
+    or_real regResolutionRate, regMinSeparation, regMinMomentum, velocityThreshold;
+    or_real maxTranslation, maxRotation, maxLinearCorrection, maxAngularCorrection;
+    or_real linearSleepTolerance, angularSleepTolerance, displaceMultiplier;
+    or_real aabbExtension, maxCirclesRatio;
+    int regVelocityIters, regPositionIters, doWarmStart, doBlocksolve;
+} or_stepconf;
+
+/* Subset of StepStats (StepStats.hpp:41-191) the oracle counts. */
+typedef struct or_stepstats {
+    int preProxiesCreated, preProxiesMoved, preContactsDestroyed, preContactsAdded;
+    int preContactsUpdated, regIslandsFound, regIslandsSolved, regContactsAdded;
+    int regContactsUpdated, regProxiesMoved, regBodiesSlept, regSumPosIters, regSumVelIters;
+    or_real regMinSeparation, regMaxIncImpulse;
+} or_stepstats;
+
+typedef struct or_world or_world;
+
+or_world* or_world_create(void);
+void or_world_destroy(or_world* w);
+
+/* Creates a body; returns its BodyID (creation order). */
+int or_add_body(or_world* w, int type, or_real px, or_real py, or_real angle,
+                or_real vx, or_real vy, or_real av, or_real ax, or_real ay, or_real aa,
+                or_real linDamp, or_real angDamp, unsigned flags);
+/* Creates a shape and attaches it to body; verts are already in the order the
+ * reference's shape configuration stores them (hull order for polygons).
+ * Returns the ShapeID. */
+int or_add_shape(or_world* w, int body, int kind, int nverts, const or_real* xy,
+                 or_real radius, or_real density, or_real friction, or_real restitution,
+                 unsigned categoryBits, unsigned maskBits, int groupIndex, int sensor);
+/* ResetMassData (WorldBody.cpp:360-400). */
+void or_reset_mass(or_world* w, int body);
+/* Revolute joint (RevoluteJointConf).  Returns JointID. */
+int or_add_revolute(or_world* w, int bodyA, int bodyB, or_real lax, or_real lay,
+                    or_real lbx, or_real lby, or_real refAngle, int enableLimit,
+                    or_real lower, or_real upper, int enableMotor, or_real motorSpeed,
+                    or_real maxMotorTorque, int collideConnected);
+
+void or_default_conf(or_stepconf* conf);
+void or_step(or_world* w, const or_stepconf* conf, or_stepstats* stats);
+
+/* Body queries. */
+int or_body_count(const or_world* w);
+/* out[0..12] = pos1.x pos1.y pos1.a vel.x vel.y vel.a xf.p.x xf.p.y xf.q.c xf.q.s
+ *              invMass invRotI underActiveTime ; flags -> *awake */
+void or_get_body(const or_world* w, int body, or_real* out13, int* awake);
+void or_set_body_state(or_world* w, int body, or_real px, or_real py, or_real angle,
+                       or_real vx, or_real vy, or_real av);
+void or_get_local_center(const or_world* w, int body, or_real* out2);
+
+/* Contact queries.  Contacts are reported in the world's container order. */
+int or_contact_count(const or_world* w);
+/* iout[0..11]: contactID proxyMin proxyMax bodyA shapeA childA bodyB shapeB childB
+ *              touching manifoldType pointCount
+ * fout[0..11]: ln.x ln.y lp.x lp.y  p0.lx p0.ly p0.ni p0.ti  p1.lx p1.ly p1.ni p1.ti
+ * feat[0..7] : p0.typeA p0.indexA p0.typeB p0.indexB  p1.(same) */
+void or_get_contact(const or_world* w, int k, int* iout12, or_real* fout12, int* feat8);
+/* Fat AABB of proxy p (tree AABB): minx miny maxx maxy. */
+int or_proxy_count(const or_world* w);
+void or_get_proxy(const or_world* w, int p, int* body_shape_child3, or_real* aabb4);
+
+/* Stand-alone narrowphase (CollideShapes, Manifold.cpp:393-438) on two shapes in
+ * the oracle's shape format, for known-answer tests.  iout: type count
+ * feat[8]; fout: ln.x ln.y lp.x lp.y p0.lx p0.ly p1.lx p1.ly */
+void or_collide(int kindA, int nA, const or_real* xyA, or_real rA, const or_real* xfA4,
+                int kindB, int nB, const or_real* xyB, or_real rB, const or_real* xfB4,
+                or_real linearSlop, or_real maxCirclesRatio,
+                int* type_count2, int* feat8, or_real* fout8);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

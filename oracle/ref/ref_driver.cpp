@@ -1,0 +1,276 @@
+// ref_driver.cpp -- runs a scene through the PlayRho reference's public API
+// (World, CreateBody, CreateShape, Attach, CreateJoint, Step, Get*) and prints
+// the resulting state with hexadecimal floats.  Used only as a checker of the
+// oracle in the container where the reference sources are present.
+//
+// Input (stdin), one record per line:
+//   conf <StepConf field> <value> ...        overrides of StepConf defaults
+//   body type px py angle vx vy av ax ay aa linDamp angDamp flags
+//   shape body kind nverts radius density friction restitution cat mask group sensor x0 y0 ...
+//   joint bodyA bodyB lax lay lbx lby refAngle enableLimit lower upper enableMotor
+//         motorSpeed maxMotorTorque collideConnected
+//   step N            (runs N steps; may repeat)
+//   dump              (prints bodies, contacts and proxies)
+//   defaults          (prints the StepConf defaults)
+#include <playrho/d2/World.hpp>
+#include <playrho/d2/WorldBody.hpp>
+#include <playrho/d2/WorldContact.hpp>
+#include <playrho/d2/WorldShape.hpp>
+#include <playrho/d2/WorldJoint.hpp>
+#include <playrho/d2/WorldMisc.hpp>
+#include <playrho/d2/DiskShapeConf.hpp>
+#include <playrho/d2/EdgeShapeConf.hpp>
+#include <playrho/d2/PolygonShapeConf.hpp>
+#include <playrho/d2/RevoluteJointConf.hpp>
+#include <playrho/d2/Joint.hpp>
+#include <playrho/d2/DynamicTree.hpp>
+#include <playrho/StepConf.hpp>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+using namespace playrho;
+using namespace playrho::d2;
+
+namespace {
+
+Real rd(std::istream& in)
+{
+    std::string t;
+    in >> t;
+    return static_cast<Real>(std::strtod(t.c_str(), nullptr));
+}
+
+void hex(double v) { std::printf(" %a", v); }
+
+void setConf(StepConf& c, const std::string& k, Real v)
+{
+    if (k == "deltaTime") c.deltaTime = v * 1_s;
+    else if (k == "dtRatio") c.dtRatio = v;
+    else if (k == "minStillTimeToSleep") c.minStillTimeToSleep = v * 1_s;
+    else if (k == "linearSlop") c.linearSlop = v * 1_m;
+    else if (k == "angularSlop") c.angularSlop = v * 1_rad;
+    else if (k == "regResolutionRate") c.regResolutionRate = v;
+    else if (k == "regMinSeparation") c.regMinSeparation = v * 1_m;
+    else if (k == "regMinMomentum") c.regMinMomentum = v * 1_Ns;
+    else if (k == "velocityThreshold") c.velocityThreshold = v * 1_mps;
+    else if (k == "maxTranslation") c.maxTranslation = v * 1_m;
+    else if (k == "maxRotation") c.maxRotation = v * 1_rad;
+    else if (k == "maxLinearCorrection") c.maxLinearCorrection = v * 1_m;
+    else if (k == "maxAngularCorrection") c.maxAngularCorrection = v * 1_rad;
+    else if (k == "linearSleepTolerance") c.linearSleepTolerance = v * 1_mps;
+    else if (k == "angularSleepTolerance") c.angularSleepTolerance = v * 1_rad / 1_s;
+    else if (k == "displaceMultiplier") c.displaceMultiplier = v;
+    else if (k == "aabbExtension") c.aabbExtension = v * 1_m;
+    else if (k == "maxCirclesRatio") c.maxCirclesRatio = v;
+    else if (k == "regVelocityIters") c.regVelocityIters = static_cast<StepConf::iteration_type>(v);
+    else if (k == "regPositionIters") c.regPositionIters = static_cast<StepConf::iteration_type>(v);
+    else if (k == "doWarmStart") c.doWarmStart = v != 0;
+    else if (k == "doBlocksolve") c.doBlocksolve = v != 0;
+    else if (k == "doToi") c.doToi = v != 0;
+    else { std::fprintf(stderr, "unknown conf key %s\n", k.c_str()); std::exit(2); }
+}
+
+void printDefaults()
+{
+    const auto c = StepConf{};
+    std::printf("defaults");
+    hex(c.deltaTime / 1_s); hex(c.dtRatio); hex(c.minStillTimeToSleep / 1_s); hex(c.linearSlop / 1_m);
+    hex(c.angularSlop / 1_rad); hex(c.regResolutionRate); hex(c.regMinSeparation / 1_m);
+    hex(c.regMinMomentum / 1_Ns); hex(c.velocityThreshold / 1_mps); hex(c.maxTranslation / 1_m);
+    hex(c.maxRotation / 1_rad); hex(c.maxLinearCorrection / 1_m); hex(c.maxAngularCorrection / 1_rad);
+    hex(c.linearSleepTolerance / 1_mps); hex(c.angularSleepTolerance / (1_rad / 1_s));
+    hex(c.displaceMultiplier); hex(c.aabbExtension / 1_m); hex(c.maxCirclesRatio);
+    std::printf(" %d %d %d %d\n", int(c.regVelocityIters), int(c.regPositionIters), int(c.doWarmStart),
+                int(c.doBlocksolve));
+}
+
+void dump(const World& world, const StepStats& st)
+{
+    std::printf("stats %u %u %u %u %u %u %u %u %u",
+                unsigned(st.pre.proxiesCreated), unsigned(st.pre.contactsDestroyed),
+                unsigned(st.pre.contactsAdded), unsigned(st.reg.islandsFound),
+                unsigned(st.reg.islandsSolved), unsigned(st.reg.contactsAdded),
+                unsigned(st.reg.bodiesSlept), unsigned(st.reg.sumPosIters), unsigned(st.reg.sumVelIters));
+    hex(st.reg.minSeparation / 1_m); hex(st.reg.maxIncImpulse / 1_Ns);
+    std::printf("\n");
+    const auto nb = GetBodyRange(world);
+    for (auto i = decltype(nb){0}; i < nb; ++i) {
+        const auto id = BodyID(i);
+        const auto& b = GetBody(world, id);
+        const auto sw = GetSweep(b);
+        const auto v = GetVelocity(b);
+        const auto xf = GetTransformation(b);
+        std::printf("body %u", unsigned(i));
+        hex(GetX(sw.pos1.linear) / 1_m); hex(GetY(sw.pos1.linear) / 1_m); hex(sw.pos1.angular / 1_rad);
+        hex(GetX(v.linear) / 1_mps); hex(GetY(v.linear) / 1_mps); hex(v.angular / (1_rad / 1_s));
+        hex(GetX(xf.p) / 1_m); hex(GetY(xf.p) / 1_m); hex(GetX(xf.q)); hex(GetY(xf.q));
+        hex(StripUnit(GetInvMass(b))); hex(StripUnit(GetInvRotInertia(b)));
+        hex(GetUnderActiveTime(b) / 1_s);
+        std::printf(" %d\n", IsAwake(b) ? 1 : 0);
+    }
+    // Proxies in leaf-ID order; leaf IDs are mapped to their rank (creation order).
+    const auto& tree = GetTree(world);
+    std::map<DynamicTree::Size, int> rank;
+    {
+        int r = 0;
+        for (auto i = DynamicTree::Size{0}; i < tree.GetNodeCapacity(); ++i) {
+            if (DynamicTree::IsLeaf(tree.GetHeight(i))) rank[i] = r++;
+        }
+        for (const auto& e : rank) {
+            const auto leaf = tree.GetLeafData(e.first);
+            const auto aabb = tree.GetAABB(e.first);
+            std::printf("proxy %d %u %u %u", e.second, unsigned(to_underlying(leaf.bodyId)),
+                        unsigned(to_underlying(leaf.shapeId)), unsigned(leaf.childId));
+            hex(aabb.ranges[0].GetMin() / 1_m); hex(aabb.ranges[1].GetMin() / 1_m);
+            hex(aabb.ranges[0].GetMax() / 1_m); hex(aabb.ranges[1].GetMax() / 1_m);
+            std::printf("\n");
+        }
+    }
+    const auto contacts = GetContacts(world);
+    int k = 0;
+    for (const auto& kc : contacts) {
+        const auto key = std::get<ContactKey>(kc);
+        const auto cid = std::get<ContactID>(kc);
+        const auto c = GetContact(world, cid);
+        const auto m = GetManifold(world, cid);
+        std::printf("contact %d %u %d %d %u %u %u %u %u %u %d %d %d", k++, unsigned(to_underlying(cid)),
+                    rank[key.GetMin()], rank[key.GetMax()],
+                    unsigned(to_underlying(GetBodyA(c))), unsigned(to_underlying(GetShapeA(c))),
+                    unsigned(GetChildIndexA(c)), unsigned(to_underlying(GetBodyB(c))),
+                    unsigned(to_underlying(GetShapeB(c))), unsigned(GetChildIndexB(c)),
+                    IsTouching(c) ? 1 : 0, int(m.GetType()), int(m.GetPointCount()));
+        hex(GetX(m.GetLocalNormal())); hex(GetY(m.GetLocalNormal()));
+        hex(GetX(m.GetLocalPoint()) / 1_m); hex(GetY(m.GetLocalPoint()) / 1_m);
+        for (auto i = 0; i < 2; ++i) {
+            const auto p = (i < m.GetPointCount()) ? m.GetPoint(i) : Manifold::Point{};
+            hex(GetX(p.localPoint) / 1_m); hex(GetY(p.localPoint) / 1_m);
+            hex(p.normalImpulse / 1_Ns); hex(p.tangentImpulse / 1_Ns);
+        }
+        for (auto i = 0; i < 2; ++i) {
+            const auto p = (i < m.GetPointCount()) ? m.GetPoint(i) : Manifold::Point{};
+            std::printf(" %d %d %d %d", int(p.contactFeature.typeA), int(p.contactFeature.indexA),
+                        int(p.contactFeature.typeB), int(p.contactFeature.indexB));
+        }
+        std::printf("\n");
+    }
+}
+
+} // namespace
+
+int main()
+{
+    auto world = World{};
+    auto conf = StepConf{};
+    conf.doToi = false;
+    auto stats = StepStats{};
+    std::string line;
+    while (std::getline(std::cin, line)) {
+        std::istringstream in(line);
+        std::string tag;
+        if (!(in >> tag)) continue;
+        if (tag == "defaults") {
+            printDefaults();
+        }
+        else if (tag == "conf") {
+            std::string k;
+            while (in >> k) setConf(conf, k, rd(in));
+        }
+        else if (tag == "body") {
+            int type = 0; in >> type;
+            const auto px = rd(in), py = rd(in), a = rd(in), vx = rd(in), vy = rd(in), av = rd(in);
+            const auto ax = rd(in), ay = rd(in), aa = rd(in), ld = rd(in), ad = rd(in);
+            unsigned flags = 0; in >> flags;
+            auto bc = BodyConf{};
+            bc.Use(type == 2 ? BodyType::Dynamic : type == 1 ? BodyType::Kinematic : BodyType::Static);
+            bc.UseLocation(Length2{px * 1_m, py * 1_m});
+            bc.UseAngle(a * 1_rad);
+            bc.UseLinearVelocity(LinearVelocity2{vx * 1_mps, vy * 1_mps});
+            bc.UseAngularVelocity(av * 1_rad / 1_s);
+            bc.UseLinearAcceleration(LinearAcceleration2{ax * 1_mps2, ay * 1_mps2});
+            bc.UseAngularAcceleration(aa * 1_rad / (1_s * 1_s));
+            bc.UseLinearDamping(ld * 1_Hz);
+            bc.UseAngularDamping(ad * 1_Hz);
+            bc.UseAllowSleep((flags & 1u) != 0);
+            bc.UseAwake((flags & 2u) != 0);
+            bc.UseFixedRotation((flags & 4u) != 0);
+            bc.UseEnabled((flags & 8u) != 0);
+            CreateBody(world, bc);
+        }
+        else if (tag == "shape") {
+            int body = 0, kind = 0, nv = 0;
+            in >> body >> kind >> nv;
+            auto radius = rd(in);
+            const auto density = rd(in), friction = rd(in), restitution = rd(in);
+            // Scenes carry float32 values; in the Real = double build a 0.01f skin is
+            // just under the world's minimum vertex radius, so it is raised to it.
+            const auto minRadius = GetVertexRadiusInterval(world).GetMin() / 1_m;
+            if (kind != 0 && radius < minRadius) radius = static_cast<Real>(minRadius);
+            unsigned cat = 0, mask = 0; int group = 0, sensor = 0;
+            in >> cat >> mask >> group >> sensor;
+            std::vector<Length2> v;
+            for (int i = 0; i < nv; ++i) { const auto x = rd(in); const auto y = rd(in); v.push_back(Length2{x * 1_m, y * 1_m}); }
+            auto filter = Filter{};
+            filter.categoryBits = static_cast<Filter::bits_type>(cat);
+            filter.maskBits = static_cast<Filter::bits_type>(mask);
+            filter.groupIndex = static_cast<Filter::index_type>(group);
+            ShapeID sid;
+            if (kind == 0) {
+                auto c = DiskShapeConf{};
+                c.UseRadius(radius * 1_m).UseLocation(v.at(0));
+                c.UseDensity(density * 1_kgpm2).UseFriction(friction).UseRestitution(restitution);
+                c.UseFilter(filter).UseIsSensor(sensor != 0);
+                sid = CreateShape(world, c);
+            }
+            else if (kind == 1) {
+                auto c = PolygonShapeConf{};
+                c.UseVertices(v);
+                c.UseVertexRadius(radius * 1_m);
+                c.UseDensity(density * 1_kgpm2).UseFriction(friction).UseRestitution(restitution);
+                c.UseFilter(filter).UseIsSensor(sensor != 0);
+                sid = CreateShape(world, c);
+            }
+            else {
+                auto c = EdgeShapeConf{v.at(0), v.at(1)};
+                c.UseVertexRadius(radius * 1_m);
+                c.UseDensity(density * 1_kgpm2).UseFriction(friction).UseRestitution(restitution);
+                c.UseFilter(filter).UseIsSensor(sensor != 0);
+                sid = CreateShape(world, c);
+            }
+            Attach(world, BodyID(static_cast<BodyID::underlying_type>(body)), sid, true);
+        }
+        else if (tag == "joint") {
+            int a = 0, b = 0; in >> a >> b;
+            auto j = RevoluteJointConf{};
+            j.bodyA = BodyID(static_cast<BodyID::underlying_type>(a));
+            j.bodyB = BodyID(static_cast<BodyID::underlying_type>(b));
+            const auto lax = rd(in), lay = rd(in), lbx = rd(in), lby = rd(in), ref = rd(in);
+            j.localAnchorA = Length2{lax * 1_m, lay * 1_m};
+            j.localAnchorB = Length2{lbx * 1_m, lby * 1_m};
+            j.referenceAngle = ref * 1_rad;
+            int en = 0; in >> en; j.enableLimit = en != 0;
+            j.lowerAngle = rd(in) * 1_rad; j.upperAngle = rd(in) * 1_rad;
+            in >> en; j.enableMotor = en != 0;
+            j.motorSpeed = rd(in) * 1_rad / 1_s;
+            j.maxMotorTorque = rd(in) * 1_Nm;
+            in >> en; j.collideConnected = en != 0;
+            CreateJoint(world, Joint{j});
+        }
+        else if (tag == "step") {
+            int n = 0; in >> n;
+            for (int i = 0; i < n; ++i) stats = Step(world, conf);
+        }
+        else if (tag == "dump") {
+            dump(world, stats);
+            std::printf("end\n");
+            std::fflush(stdout);
+        }
+    }
+    return 0;
+}
