@@ -1,0 +1,381 @@
+"""Benchmark of the GB300 PlayRho world step.
+
+Default workload: 4096 independent worlds (body counts log-uniform in [16, 2048],
+half box pyramids, half piles of disks and 3-8-gons, seed 1; ~1.6 M bodies)
+advanced together in one CUDA-graph step (dt 1/60, 8/3 iterations, float32).
+
+  value : body-steps/s of the batched step, inputs resident in HBM, device time
+          from CUDA events the captured step graph records around its phases
+  e2e   : the same metric through the C ABI with host buffers: every step
+          uploads the body states from pinned host memory, steps, and reads them
+          back, all inside the host-timed region
+  roofline : the Gauss-Seidel sweep kernel (the dominant phase), algorithmic
+          bytes per launch over its live CUDA-event duration vs measured HBM peak
+  cpu_baseline : the CPU oracle (a restatement of the reference step, pinned bit
+          for bit to the reference) on one host core, on a bounded sample
+
+``--impl reference`` times the reference's CPU step on the host's cores (the
+oracle port, one process per core) on the same workload and prints the same
+metric.  Multi-GPU (torchrun): each rank advances its own copy of the batch
+(worlds are independent; no collective on the data path), scaling "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "batched body-steps/s"
+UNIT = "body-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--worlds", type=int, default=4096)
+    p.add_argument("--settle", type=int, default=240,
+                   help="untimed steps that bring the scenes to their contact-rich state")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--kernels-only", action="store_true",
+                   help="only the warm-up and timed steps (for a profiler launch list)")
+    return p.parse_args()
+
+
+def workload(n_worlds):
+    from playrho_gb300 import scenes
+
+    return scenes.batched_worlds(n_worlds, seed=1)
+
+
+def dist_setup(args):
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        td.init_process_group(backend, init_method="env://")
+        dist = td
+    return rank, world, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([float(v)], device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = []
+        reasons = set()
+        smax = None
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                smax = float(r[1])
+                names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+                for n, v in zip(names, r[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+            except Exception:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def sweep_bytes(stats, conf, n_bodies_solved):
+    """Algorithmic bytes of one Gauss-Seidel sweep launch (warm start, velocity and
+    position iterations, integration, impulse store) for the active constraints."""
+    nc = stats["activeConstraints"]
+    iv = conf.regVelocityIters
+    ip = stats["sumPosIters"] / max(1, stats["islandsFound"])  # mean position iterations per island
+    per_contact = 160 + 240 * iv + 160 * ip + 32
+    return nc * per_contact + n_bodies_solved * 52
+
+
+def cpu_baseline_sample(worlds, seconds=8.0):
+    """Times the single-threaded oracle on a bounded sample of the workload."""
+    from oracle import oracle
+
+    sample = worlds[: max(1, len(worlds) // 16)]
+    ows = [oracle.OracleWorld(w) for w in sample]
+    for o in ows:
+        o.step()
+    nb = sum(int((w.body_type == 2).sum()) for w in sample)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        for o in ows:
+            o.step()
+        steps += 1
+        if time.perf_counter() - t0 > seconds or steps >= 200:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": nb * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{len(sample)} of {len(worlds)} worlds ({nb} dynamic bodies), {steps} steps after 1 warm-up, "
+                      f"{dt:.1f} s, oracle FP32 (bit-exact restatement of the reference step)"}
+
+
+def _ref_worker(args):
+    """Process-pool worker: builds its share of worlds in the oracle and steps them."""
+    idx, n_worlds, steps, warmup = args
+    sys.path.insert(0, ROOT)
+    from oracle import oracle
+    from playrho_gb300 import scenes
+
+    worlds = scenes.batched_worlds(n_worlds, seed=1)
+    mine = [worlds[i] for i in idx]
+    ows = [oracle.OracleWorld(w) for w in mine]
+    for _ in range(warmup):
+        for o in ows:
+            o.step()
+    nb = sum(int((w.body_type == 2).sum()) for w in mine)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for o in ows:
+            o.step()
+    return nb, time.perf_counter() - t0
+
+
+def run_reference(args, rank):
+    """The reference's CPU step on all host cores (oracle port), same workload and metric."""
+    import multiprocessing as mp
+
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n_worlds = args.worlds
+    # one bounded sample per process: a slice of the worlds, `steps` steps each
+    per = max(1, min(n_worlds // cores, 64))
+    idx_all = list(range(n_worlds))
+    shares = [idx_all[c::cores][:per] for c in range(cores)]
+    steps = max(1, min(args.steps, 5))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_ref_worker, [(s, n_worlds, steps, min(args.warmup, 1)) for s in shares])
+    nb = sum(r[0] for r in res)
+    tmax = max(r[1] for r in res)
+    value = nb * steps / tmax
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": tmax / steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic",
+           "config": {"workload": f"batched worlds: {n_worlds} worlds, log-uniform 16..2048 bodies, seed 1",
+                      "sample": f"{sum(len(s) for s in shares)} worlds on {cores} processes"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"{sum(len(s) for s in shares)} of {n_worlds} worlds, {steps} steps, "
+                                      f"one oracle process per core (reference sources are not on this host)"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args, rank, world_size, local, dist):
+    from playrho_gb300 import build, gpu
+
+    build.build()
+    worlds = workload(args.worlds)
+    n_dyn = sum(int((w.body_type == 2).sum()) for w in worlds)
+    batch = gpu.GpuBatch(worlds, device=local)
+    conf = gpu.default_conf()
+    # Scene preparation: advance the batch `settle` steps (piles land, pyramids take
+    # their load) so the measured steps are the contact-rich middle of the run,
+    # then W warm-up steps.  The first step creates every proxy and contact, as
+    # the reference's does.
+    batch.step_n(args.settle, conf)
+    for _ in range(max(3, args.warmup)):
+        batch.step_n(1, conf)
+    barrier(dist)
+    step_ms, phases = [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            batch.step_async(1, conf)
+            ph = batch.last_step_phase_ms()
+            phases.append(ph)
+            step_ms.append(ph["step"])
+        batch.synchronize()
+    barrier(dist)
+    total_s = max_over_ranks(dist, sum(step_ms) / 1e3)
+    value = world_size * n_dyn * args.steps / total_s
+    # statistics of one more step (outside the timed region) for the roofline bytes
+    _, st = batch.step_profiled(conf)
+    sweeps_ms = statistics.mean(p["sweeps"] for p in phases)
+    n_solved = n_dyn  # every dynamic body of an awake island is integrated
+    bytes_sweep = sweep_bytes(st, conf, n_solved)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_sweep / (sweeps_ms / 1e3) / 1e9
+
+    if args.kernels_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "kernels_only": True,
+                              "ms_per_step": statistics.mean(step_ms),
+                              "phase_ms": {k: statistics.mean(p[k] for p in phases) for k in phases[0]}}))
+        return
+    # e2e through the C ABI with host buffers (pinned), copies inside the timed region
+    import torch
+
+    nb = batch.n_bodies
+    pos_h = torch.empty((nb, 3), dtype=torch.float32, pin_memory=True)
+    vel_h = torch.empty((nb, 3), dtype=torch.float32, pin_memory=True)
+    b0 = batch.bodies()
+    pos_h.numpy()[:] = b0["pos"]
+    vel_h.numpy()[:] = b0["vel"]
+    lib = batch.lib
+    import ctypes
+
+    pp, vp = ctypes.c_void_p(pos_h.data_ptr()), ctypes.c_void_p(vel_h.data_ptr())
+    e2e_steps = max(3, args.steps // 2)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        batch._check(lib.prgpu_upload_body_states(batch.h, 0, nb, pp, vp), "upload")
+        batch._check(lib.prgpu_step_n(batch.h, ctypes.byref(conf), 1), "step")
+        batch._check(lib.prgpu_download_bodies(batch.h, pp, vp, None, None, None, None), "download")
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = world_size * n_dyn * e2e_steps / e2e_s
+
+    # the plain single-world GPU step on a sample of the same worlds (one world per call)
+    plain = None
+    if rank == 0:
+        sample = worlds[:: max(1, len(worlds) // 48)][:48]
+        singles = [gpu.GpuBatch([w], device=local) for w in sample]
+        for s in singles:
+            s.step_n(3, conf)
+        nsb = sum(int((w.body_type == 2).sum()) for w in sample)
+        t0 = time.perf_counter()
+        for _ in range(10):
+            for s in singles:
+                s.step_n(1, conf)
+        plain_dt = time.perf_counter() - t0
+        plain = nsb * 10 / plain_dt
+        for s in singles:
+            s.close()
+
+    if rank != 0:
+        return
+    cpu = None if args.no_cpu_baseline else cpu_baseline_sample(worlds)
+    clocks = clk.summary()
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "sweeps_traffic.json")) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch_scaled")
+    except Exception:
+        pass
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched worlds: {len(worlds)} worlds, log-uniform 16..2048 bodies, "
+                               f"pyramids + piles, seed 1", "worlds": len(worlds), "dynamic_bodies": n_dyn,
+                   "dt": "1/60", "iterations": "8/3", "parallelism": f"replicas x{world_size}",
+                   "settle_steps": args.settle,
+                   "l2": "working set > 129 MB L2 (no flush needed)",
+                   "live_contacts": st["liveContacts"], "active_constraints": st["activeConstraints"],
+                   "colours": st["colours"], "serial_constraints": st["serialConstraints"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "k_solve (Gauss-Seidel colour sweeps)",
+                     "peak_source": peak_kind, "launch_ms": sweeps_ms, "algorithmic_bytes": bytes_sweep},
+        "phase_ms": {k: statistics.mean(p[k] for p in phases) for k in phases[0]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nb * 24, "d2h_bytes_per_step": nb * 24},
+        "plain_single_world_gpu": {"value": plain, "unit": UNIT,
+                                   "batched_over_plain": (value / plain) if plain else None},
+        "gpu_launches": None,
+        "clocks": clocks,
+    }
+    out["gpu_launches"] = launches_per_step(batch) * args.steps
+    print(json.dumps(out), flush=True)
+
+
+def launches_per_step(batch) -> int:
+    """Kernel nodes in the captured step graph (counted from the graph itself)."""
+    import ctypes
+
+    n = ctypes.c_uint32()
+    rc = batch.lib.prgpu_graph_kernel_count(batch.h, ctypes.byref(n))
+    return int(n.value) if rc == 0 else -1
+
+
+def main():
+    args = parse()
+    rank, world_size, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_ours(args, rank, world_size, local, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * prgpu.h -- C ABI of the GB300 world step for PlayRho worlds.
+ *
+ * One handle holds a batch of one or more independent 2-D worlds resident in
+ * GPU memory.  Every entry point returns an int status (PRGPU_OK = 0) and takes
+ * plain pointers and sizes; host buffers belong to the caller, device buffers
+ * to the handle.  The C++ world type of the PlayRho drop-in (GpuWorld) and the
+ * Python bindings sit on top of these calls.
+ *
+ * Reference interfaces each entry point replaces (PlayRho 2.0.0 paths):
+ *   prgpu_default_step_conf     StepConf defaults, Library/include/playrho/StepConf.hpp:59-161
+ *   prgpu_world_create          World{} + CreateBody/CreateShape/Attach/CreateJoint,
+ *                               Library/include/playrho/d2/World.hpp:739-745, :521-526;
+ *                               Library/source/playrho/d2/AabbTreeWorld.cpp:1019-1044, :1132-1157, :1234-1257
+ *   prgpu_step                  Step(World&, const StepConf&), World.hpp:917-920 ->
+ *                               Step(AabbTreeWorld&, const StepConf&), AabbTreeWorld.cpp:2144-2219
+ *   prgpu_step_n                a loop of Step calls (no per-step host synchronisation)
+ *   prgpu_download_bodies       GetBody(World, BodyID) / GetTransformation / GetVelocity,
+ *                               World.hpp (GetBody), AabbTreeWorld.cpp:2850
+ *   prgpu_upload_body_states    SetBody(World, BodyID, Body), AabbTreeWorld.cpp:2723-2795
+ *   prgpu_download_contacts     GetContacts(World) + GetContact + GetManifold,
+ *                               World.hpp:563-591, AabbTreeWorld.cpp:2860-2865
+ *   prgpu_download_proxies      GetTree(World) leaf AABBs, World.hpp:937
+ *   prgpu_convex_hull           PolygonShapeConf::Set -> GetConvexHullAsVector,
+ *                               PolygonShapeConf.cpp:120-133, DistanceProxy.cpp:62-105
+ */
+#ifndef PRGPU_H
+#define PRGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PRGPU_ABI_VERSION 1
+
+enum prgpu_status {
+    PRGPU_OK = 0,
+    PRGPU_EINVAL = 1,      /* invalid argument (reference: InvalidArgument / OutOfRange) */
+    PRGPU_ECUDA = 2,       /* CUDA runtime error (message via prgpu_last_error) */
+    PRGPU_ECAPACITY = 3,   /* a device buffer overflowed (reference: LengthError) */
+    PRGPU_ETIMEOUT = 4,    /* a bounded device wait gave up */
+    PRGPU_ENOTREADY = 5,   /* no GPU or the library was built without one */
+    PRGPU_ESTATE = 6       /* call not valid in the handle's state (reference: WrongState) */
+};
+
+enum prgpu_body_type { PRGPU_STATIC = 0, PRGPU_KINEMATIC = 1, PRGPU_DYNAMIC = 2 };
+enum prgpu_shape_kind { PRGPU_DISK = 0, PRGPU_POLYGON = 1, PRGPU_EDGE = 2 };
+/* body flags (BodyConf booleans) */
+enum {
+    PRGPU_BODY_ALLOW_SLEEP = 1,
+    PRGPU_BODY_AWAKE = 2,
+    PRGPU_BODY_FIXED_ROTATION = 4,
+    PRGPU_BODY_ENABLED = 8
+};
+
+typedef struct prgpu_world prgpu_world;
+
+/* StepConf fields read by the regular phase (StepConf.hpp:165-340).  TOI is not
+ * part of this step: callers use the reference's doToi = false behaviour. */
+typedef struct prgpu_step_conf {
+    float deltaTime, dtRatio, minStillTimeToSleep, linearSlop, angularSlop;
+    float regResolutionRate, regMinSeparation, regMinMomentum, velocityThreshold;
+    float maxTranslation, maxRotation, maxLinearCorrection, maxAngularCorrection;
+    float linearSleepTolerance, angularSleepTolerance, displaceMultiplier;
+    float aabbExtension, maxCirclesRatio;
+    int32_t regVelocityIters, regPositionIters, doWarmStart, doBlocksolve;
+} prgpu_step_conf;
+
+/* Subset of StepStats (StepStats.hpp:41-191), summed over the batch. */
+typedef struct prgpu_step_stats {
+    uint32_t contactsAdded, contactsDestroyed, contactsUpdated;
+    uint32_t islandsFound, islandsSolved, bodiesSlept, proxiesMoved, sumPosIters;
+    uint32_t liveContacts, activeConstraints, colours, serialConstraints;
+    float minSeparation, maxIncImpulse;
+} prgpu_step_stats;
+
+/* A batch of worlds in creation order, flattened world-major.  Body indices in
+ * shape_body / joint_bodies are global (into the flattened body arrays); each
+ * world's bodies, shapes and joints are contiguous.  Polygon vertices must
+ * already be in the order the reference's shape configuration stores them
+ * (prgpu_convex_hull gives that order).  Mass data is derived from the shapes
+ * as Attach(world, body, shape, resetMassData = true) does after each shape. */
+typedef struct prgpu_batch_desc {
+    uint32_t n_worlds;
+    const uint32_t* world_body_count;   /* [n_worlds] */
+    const uint32_t* world_shape_count;  /* [n_worlds] */
+    const uint32_t* world_joint_count;  /* [n_worlds] */
+    uint32_t n_bodies;
+    const int32_t* body_type;           /* [n_bodies] */
+    const float* body_pos;              /* [n_bodies*3] x y angle */
+    const float* body_vel;              /* [n_bodies*3] vx vy w */
+    const float* body_acc;              /* [n_bodies*3] ax ay alpha */
+    const float* body_damp;             /* [n_bodies*2] linear angular */
+    const uint32_t* body_flags;         /* [n_bodies] PRGPU_BODY_* */
+    uint32_t n_shapes;
+    const uint32_t* shape_body;         /* [n_shapes] */
+    const int32_t* shape_kind;          /* [n_shapes] */
+    const uint32_t* shape_voff;         /* [n_shapes] first vertex */
+    const uint32_t* shape_nv;           /* [n_shapes] vertex count (disk 1, edge 2, polygon 3..16) */
+    const float* shape_radius;          /* [n_shapes] vertex radius (disk radius) */
+    const float* shape_density;
+    const float* shape_friction;
+    const float* shape_restitution;
+    const int32_t* shape_filter;        /* [n_shapes*4] category mask group sensor */
+    uint32_t n_verts;
+    const float* verts;                 /* [n_verts*2] */
+    uint32_t n_joints;                  /* revolute joints */
+    const uint32_t* joint_bodies;       /* [n_joints*2] */
+    const float* joint_anchors;         /* [n_joints*4] localAnchorA.xy localAnchorB.xy */
+    const float* joint_params;          /* [n_joints*6] refAngle lower upper motorSpeed maxMotorTorque - */
+    const int32_t* joint_flags;         /* [n_joints*3] enableLimit enableMotor collideConnected */
+    uint32_t contact_capacity;          /* 0: automatic */
+    uint32_t candidate_capacity;        /* 0: automatic */
+} prgpu_batch_desc;
+
+int prgpu_abi_version(void);
+int prgpu_default_step_conf(prgpu_step_conf* out);
+/* Creates the batch on `device` (the first step creates proxies and contacts, as
+ * the reference's first Step does). */
+int prgpu_world_create(const prgpu_batch_desc* desc, int device, prgpu_world** out);
+int prgpu_world_destroy(prgpu_world* w);
+/* One world step of every world in the batch; synchronous like Step(World&).
+ * stats may be NULL. */
+int prgpu_step(prgpu_world* w, const prgpu_step_conf* conf, prgpu_step_stats* stats);
+/* n steps replayed from a captured CUDA graph without host synchronisation;
+ * returns after the last one has finished. */
+int prgpu_step_n(prgpu_world* w, const prgpu_step_conf* conf, int n);
+/* One step launched phase by phase (no graph) with CUDA events between the
+ * phases; phase_ms[k] receives the device time of phase k:
+ *   0 pre-step contact maintenance, 1 islands + colouring, 2 constraint set-up,
+ *   3 Gauss-Seidel sweeps (velocity + position), 4 write-back + sleep,
+ *   5 proxy synchronisation + contact update, 6 new-contact search. */
+int prgpu_step_profiled(prgpu_world* w, const prgpu_step_conf* conf, float* phase_ms, int n_phases,
+                        prgpu_step_stats* stats);
+/* Device times of the phases of the last step replayed from the captured graph
+ * (same phase numbering as prgpu_step_profiled; entry 7 is the whole step),
+ * from CUDA events the graph records between its phases.  Waits for the step. */
+int prgpu_last_step_phase_ms(prgpu_world* w, float* phase_ms, int n_phases);
+/* Number of kernel launches in one captured step. */
+int prgpu_graph_kernel_count(prgpu_world* w, uint32_t* n_kernels);
+/* Enqueues n steps on the handle's stream and returns at once. */
+int prgpu_step_async(prgpu_world* w, const prgpu_step_conf* conf, int n);
+int prgpu_synchronize(prgpu_world* w);
+int prgpu_get_counts(prgpu_world* w, uint32_t* n_worlds, uint32_t* n_bodies, uint32_t* n_shapes,
+                     uint32_t* n_joints, uint32_t* n_contacts);
+/* Body state; any pointer may be NULL.  flags: bit0 awake.  mass: invM invI lcx lcy. */
+int prgpu_download_bodies(prgpu_world* w, float* pos3, float* vel3, float* xf4, float* mass4,
+                          float* under_active, uint32_t* flags);
+/* Sets positions (x y angle of the centre of mass) and velocities of bodies
+ * [first, first+count); unchanged transforms are left alone, changed ones are
+ * re-synchronised before the next step (SetBody semantics). */
+int prgpu_upload_body_states(prgpu_world* w, uint32_t first, uint32_t count, const float* pos3, const float* vel3);
+/* Live contacts in ContactKey order.  Any array may be NULL; n_out receives the count.
+ *   proxies2: proxy min, proxy max (global shape indices)   bodies2: body A, body B
+ *   flags: bit0 touching, bit1 sensor                        meta2: manifold type, point count
+ *   head4: local normal xy, local point xy                   pts8: per point local xy, normal and
+ *   tangent impulse                                          features2: packed ContactFeature of each point
+ *   (typeA | indexA << 8 | typeB << 16 | indexB << 24) */
+int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
+                            uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
+                            uint32_t* features2);
+/* Fat (tree) AABB of every proxy: minx miny maxx maxy. */
+int prgpu_download_proxies(prgpu_world* w, float* aabb4);
+/* Runs the host-side part of prgpu_world_create (validation, mass data as
+ * Attach(..., resetMassData = true) leaves it) without a GPU: centre-of-mass
+ * positions, velocities and invM invI lcx lcy of every body.  Any output may be NULL. */
+int prgpu_prepare_bodies(const prgpu_batch_desc* desc, float* pos3, float* vel3, float* mass4);
+/* Copies the last error message into buf. */
+int prgpu_last_error(prgpu_world* w, char* buf, int len);
+/* Vertex order of PolygonShapeConf::Set (VertexSet de-duplication + gift wrap);
+ * returns the hull vertex count written to out_xy (capacity n). */
+int prgpu_convex_hull(const float* xy, int n, float linear_slop, float* out_xy);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

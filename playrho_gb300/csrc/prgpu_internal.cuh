@@ -1,0 +1,314 @@
+// prgpu_internal.cuh -- device data layout of a batch of worlds and the shared
+// device primitives (bounded grid barrier, ordered float atomics, scans, sort).
+//
+// Layout in HBM: every world of a batch is flattened into one structure of
+// arrays.  Bodies, shapes (one proxy each) and joints of world w occupy the
+// contiguous ranges [body_off[w], body_off[w+1]) etc., in creation order, so a
+// global proxy index orders proxies exactly as the reference's tree leaf IDs
+// order them within a world (leaf k of a tree built without removals has ID
+// 0, 1, 3, 5, ...; the ranks are what ContactKey compares).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "prgpu_math.cuh"
+
+namespace prgpu {
+
+// Status codes of the C ABI (include/prgpu.h).
+enum {
+    PR_OK = 0,
+    PR_EINVAL = 1,
+    PR_ECUDA = 2,
+    PR_ECAPACITY = 3,
+    PR_ETIMEOUT = 4,
+    PR_ENOTREADY = 5,
+    PR_ESTATE = 6,
+};
+
+// Body flags (device).
+enum : uint32_t {
+    BF_TYPE_MASK = 3u,        // 0 static, 1 kinematic, 2 dynamic
+    BF_AWAKE = 1u << 2,
+    BF_ALLOW_SLEEP = 1u << 3,
+    BF_FIXED_ROT = 1u << 4,
+    BF_ENABLED = 1u << 5,
+    BF_SOLVED = 1u << 8,      // in an awake island this step
+    BF_MOVED = 1u << 9,       // pos1 changed in this step's solve
+    BF_DIRTY = 1u << 10,      // state set by the host since the last step
+};
+
+// Contact slot flags.
+enum : uint32_t {
+    CF_TOUCHING = 1u,
+    CF_SENSOR = 2u,
+    CF_NEEDS_UPDATE = 4u,
+    CF_IMPENETRABLE = 8u,
+};
+
+PR_HD uint32_t body_type(uint32_t f) { return f & BF_TYPE_MASK; }
+PR_HD bool is_speedable(uint32_t f) { return (f & BF_TYPE_MASK) != 0u; }
+PR_HD bool is_accelerable(uint32_t f) { return (f & BF_TYPE_MASK) == 2u; }
+
+constexpr int kMaxColours = 64;      // colours 0..63 solved in parallel
+constexpr int kSerialColour = 64;    // leftover constraints solved by one thread
+constexpr int kMaxPosIters = 32;
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr uint32_t kNone = 0xffffffffu;
+
+// Velocity constraint of one contact (VelocityConstraint.hpp), 160 bytes.
+struct __align__(16) VC {
+    float nx, ny, friction, tangentSpeed;
+    float rA0x, rA0y, rB0x, rB0y;
+    float rA1x, rA1y, rB1x, rB1y;
+    float nm0, tm0, nm1, tm1;
+    float vb0, vb1, k00, k11;
+    float k01, m00, m11, m01;
+    float ni0, ti0, ni1, ti1;
+    uint32_t bA, bB, count, island;
+    uint32_t slot, pad0, pad1, pad2;
+};
+
+// Position constraint of one contact (PositionConstraint.hpp), 64 bytes.
+struct __align__(16) PC {
+    float lnx, lny, lpx, lpy;
+    float p0x, p0y, p1x, p1y;
+    float totalRadius;
+    uint32_t type, count, bA;
+    uint32_t bB, island, pad0, pad1;
+};
+
+// Device counters and small per-step state.
+struct Counters {
+    uint32_t n_live;          // live contacts (sorted key list length)
+    uint32_t n_new;           // new contacts found this pass
+    uint32_t n_moved;         // proxies whose fat AABB moved this pass
+    uint32_t n_destroyed;
+    uint32_t free_top;        // entries on the free-slot stack
+    uint32_t high_water;      // slots ever used
+    uint32_t n_active;        // active constraints this step (contacts then joints)
+    uint32_t n_active_c;
+    uint32_t n_active_j;
+    uint32_t n_colours;       // parallel colours used
+    uint32_t colour_off[kSerialColour + 2];
+    uint32_t colour_cnt[kSerialColour + 2];
+    uint32_t colour_remaining;
+    uint32_t err;             // first error status raised on the device
+    uint32_t err_where;
+    uint32_t bar_count;
+    uint32_t bar_gen;
+    uint32_t need_find;
+    // StepStats counters (StepStats.hpp)
+    uint32_t st_contacts_added;
+    uint32_t st_contacts_destroyed;
+    uint32_t st_contacts_updated;
+    uint32_t st_islands_found;
+    uint32_t st_islands_solved;
+    uint32_t st_bodies_slept;
+    uint32_t st_proxies_moved;
+    uint32_t st_sum_pos_iters;
+    float st_min_separation;
+    float st_max_inc_impulse;
+    uint32_t scan_total;
+    uint32_t pad[7];
+};
+
+// Solver / step configuration in device memory (mirrors prgpu_step_conf).
+struct DConf {
+    float deltaTime, dtRatio, minStillTimeToSleep, linearSlop, angularSlop;
+    float regResolutionRate, regMinSeparation, regMinMomentum, velocityThreshold;
+    float maxTranslation, maxRotation, maxLinearCorrection, maxAngularCorrection;
+    float linearSleepTolerance, angularSleepTolerance, displaceMultiplier;
+    float aabbExtension, maxCirclesRatio;
+    int regVelocityIters, regPositionIters, doWarmStart, doBlocksolve;
+};
+
+// All device pointers of one batch.  Passed to kernels by value.
+struct DW {
+    uint32_t n_worlds, n_bodies, n_shapes, n_joints, n_verts;
+    uint32_t contact_cap, cand_cap, key_bits, world_bits;
+    // worlds
+    const uint32_t* w_body_off;
+    const uint32_t* w_shape_off;
+    uint32_t* w_root;        // LBVH root of each world (internal index or leaf | kLeafBit)
+    float4* w_bounds;        // centroid bounds for Morton codes (ordered-int encoded)
+    // bodies
+    float4* b_pos1;          // cx cy angle -
+    float4* b_pos0;
+    float4* b_vel;           // vx vy w -
+    float4* b_xf;            // px py c s
+    float4* b_mass;          // invM invI lcx lcy
+    float4* b_acc;           // ax ay aa -
+    float2* b_damp;
+    uint32_t* b_flags;
+    float* b_uat;
+    uint32_t* b_world;
+    uint32_t* b_island;      // union-find parent / island root
+    uint32_t* b_jnt_off;     // body -> joints CSR (for joint collision filtering)
+    uint32_t* b_jnt_other;
+    uint32_t* b_jnt_cc;      // collideConnected of that joint
+    // per-island data, indexed by the island's root body
+    uint32_t* isl_awake;
+    float* isl_sep;          // [n_bodies * kMaxPosIters] min separation per position iteration
+    uint32_t* isl_jok;       // [n_bodies * kMaxPosIters] joints within tolerance
+    float* isl_uat;          // min under-active time
+    // shapes / proxies
+    uint32_t* s_body;
+    uint32_t* s_meta;        // kind | nverts << 8
+    uint32_t* s_voff;
+    float* s_radius;
+    float2* s_mat;           // friction restitution
+    uint32_t* s_filter;      // category | mask << 16
+    int32_t* s_group;        // group index; bit 30 = sensor
+    float4* verts;           // vx vy nx ny
+    float4* p_aabb;          // fat AABB: minx miny maxx maxy
+    uint32_t* p_moved;       // 1 if the proxy's fat AABB moved this pass
+    uint32_t* moved_list;
+    // joints
+    uint32_t* j_bodies;      // [2*J]
+    float4* j_anchor;        // laA.xy laB.xy
+    float4* j_param;         // ref lower upper motorSpeed
+    float* j_maxtorque;
+    uint32_t* j_flags;       // enableLimit | enableMotor << 1 | collideConnected << 2
+    float4* j_r;             // rA.xy rB.xy
+    float4* j_m0;            // mass ex.x ex.y ex.z ey.y
+    float4* j_m1;            // ey.z ez.z angularMass motorImpulse
+    float4* j_imp;           // impulse xyz, limitState
+    // contacts (slot storage)
+    uint64_t* c_key;         // sorted live keys
+    uint32_t* c_slot;
+    uint64_t* c_key_alt;     // ping-pong buffers
+    uint32_t* c_slot_alt;
+    uint32_t* free_stack;
+    uint2* cs_proxy;         // proxy min, proxy max
+    uint2* cs_body;
+    uint32_t* cs_flags;
+    float2* cs_mat;          // friction restitution
+    float4* m_head;          // ln.xy lp.xy
+    float4* m_p0;            // lp.xy ni ti
+    float4* m_p1;
+    uint32_t* m_meta;        // type | count << 4
+    uint2* m_cf;             // contact features of the two points
+    // new-contact scratch
+    uint64_t* n_key;
+    uint64_t* n_key_alt;
+    uint32_t* n_val;
+    uint32_t* n_val_alt;
+    // LBVH
+    uint64_t* l_key;
+    uint64_t* l_key_alt;
+    uint32_t* l_idx;
+    uint32_t* l_idx_alt;
+    float4* l_leaf_box;
+    float4* l_node_box;
+    uint32_t* l_left;
+    uint32_t* l_right;
+    uint32_t* l_parent;      // [2S]: internal i at i, leaf k at S + k
+    uint32_t* l_range;       // [2*(S-1)] first last
+    uint32_t* l_visit;
+    // constraints of this step
+    uint32_t* k_list;        // active constraint ids (slot for contacts, joint id + J flag)
+    uint32_t* k_colour;
+    uint32_t* k_tent;
+    uint32_t* k_prio;        // colouring priority (hash of world-local identifiers)
+    uint32_t* k_order;       // constraint indices bucketed by colour
+    uint32_t* inc_off;       // body -> active constraint incidence CSR
+    uint32_t* inc_cur;
+    uint32_t* inc_list;
+    VC* vc;
+    PC* pc;
+    // scan scratch
+    uint32_t* flags;
+    uint32_t* scan;
+    uint32_t* partial;
+    uint32_t* hist;
+    Counters* cnt;
+    const DConf* conf;
+};
+
+// ---------------------------------------------------------------------------
+// Device helpers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t float_to_ordered(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+__device__ __forceinline__ void atomic_min_float(float* addr, float v) {
+    // Works for any sign: the ordered encoding is only used transiently in a CAS loop.
+    unsigned int* a = reinterpret_cast<unsigned int*>(addr);
+    unsigned int old = *a;
+    for (int i = 0; i < 1 << 20; ++i) {
+        const float cur = __uint_as_float(old);
+        if (!(v < cur)) return;
+        const unsigned int prev = atomicCAS(a, old, __float_as_uint(v));
+        if (prev == old) return;
+        old = prev;
+    }
+}
+__device__ __forceinline__ void atomic_max_nonneg_float(float* addr, float v) {
+    // For non-negative finite floats the IEEE bit pattern orders like the value.
+    atomicMax(reinterpret_cast<unsigned int*>(addr), __float_as_uint(v));
+}
+
+__device__ __forceinline__ void set_error(Counters* c, uint32_t code, uint32_t where) {
+    if (atomicCAS(&c->err, 0u, code) == 0u) c->err_where = where;
+}
+
+// Bounded grid-wide barrier for cooperative launches.  Every spin is bounded:
+// after the limit the barrier records PR_ETIMEOUT and returns; once an error is
+// set all later barriers return at once so the kernel drains quickly.
+__device__ __forceinline__ void grid_barrier(Counters* c) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile uint32_t* vgen = &c->bar_gen;
+        volatile uint32_t* verr = &c->err;
+        if (*verr == 0u) {
+            const uint32_t g = *vgen;
+            __threadfence();
+            const uint32_t arrived = atomicAdd(&c->bar_count, 1u);
+            if (arrived == gridDim.x - 1u) {
+                c->bar_count = 0u;
+                __threadfence();
+                atomicAdd(&c->bar_gen, 1u);
+            } else {
+                uint32_t spins = 0;
+                while (*vgen == g) {
+                    if (++spins > (1u << 24)) {
+                        set_error(c, PR_ETIMEOUT, 900u);
+                        break;
+                    }
+                    if (*verr != 0u) break;
+                    __nanosleep(64);
+                }
+            }
+            __threadfence();
+        }
+    }
+    __syncthreads();
+}
+
+// Grid-stride range over a count held in device memory.
+#define GRID_LOOP(i, n) \
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
+
+// ---------------------------------------------------------------------------
+// Host-side primitives implemented in prgpu_prims.cu.
+// ---------------------------------------------------------------------------
+struct Prims {
+    int sm_count;
+    int grid;  // blocks for chunked primitives (<= 1024)
+};
+
+// Exclusive scan of in[0..*n) into out; *total receives the sum.
+void scan_exclusive(const Prims& P, const uint32_t* in, uint32_t* out, const uint32_t* n, uint32_t* total,
+                    uint32_t* partial, cudaStream_t s);
+// Stable LSD radix sort of (key, val) pairs by the low `bits` bits of the keys.
+// Returns true when the sorted result ended in the *_alt buffers.
+bool radix_sort(const Prims& P, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
+                const uint32_t* n, int bits, uint32_t* hist, cudaStream_t s);
+
+}  // namespace prgpu

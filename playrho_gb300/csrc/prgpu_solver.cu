@@ -1,0 +1,1092 @@
+// prgpu_solver.cu -- islands, constraint colouring and the Gauss-Seidel solve.
+//
+// Restates SolveReg / SolveRegIslandViaGS (AabbTreeWorld.cpp:1472-1683) for a
+// batch of worlds:
+//  * islands are connected components over touching non-sensor contacts and
+//    joints between speedable bodies (AddToIsland, :1358-1470), found by a
+//    lock-free union-find; an island is solved when any body in it is awake;
+//  * the sequential contact order of the reference becomes colour order: the
+//    active contacts and joints are coloured so that no two constraints of a
+//    colour share a dynamic body, and each colour is swept in parallel;
+//  * the position loop keeps the reference's per-island early exit
+//    (regMinSeparation, :1628-1644) through per-island, per-iteration minima;
+//  * sleep follows UpdateUnderActiveTimes / Sleepem (:403-429).
+// The velocity loop's early exit (regMinMomentum) only stops iterations that
+// change nothing, so every island runs regVelocityIters sweeps.
+#include <cooperative_groups.h>
+
+#include "prgpu_collide.cuh"
+#include "prgpu_kernels.cuh"
+
+namespace prgpu {
+
+namespace {
+
+constexpr uint32_t kJointBit = 0x80000000u;
+
+// ---- islands ----------------------------------------------------------------
+__device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x) {
+    for (int g = 0; g < 1 << 20; ++g) {
+        const uint32_t p = __ldcg(&parent[x]);
+        if (p == x) return x;
+        x = p;
+    }
+    return x;
+}
+
+__device__ __forceinline__ void uf_union(uint32_t* parent, uint32_t a, uint32_t b, Counters* c) {
+    for (int g = 0; g < 1 << 16; ++g) {
+        uint32_t ra = uf_find(parent, a), rb = uf_find(parent, b);
+        if (ra == rb) return;
+        if (ra < rb) { const uint32_t t = ra; ra = rb; rb = t; }
+        // hook the larger root under the smaller one: labels end as component minima
+        if (atomicCAS(&parent[ra], ra, rb) == ra) return;
+    }
+    set_error(c, PR_ETIMEOUT, 20u);
+}
+
+__global__ void k_isl_init(DW d) {
+    GRID_LOOP(b, d.n_bodies) {
+        d.b_island[b] = b;
+        d.isl_awake[b] = 0u;
+        d.b_flags[b] &= ~(BF_SOLVED | BF_MOVED);
+    }
+}
+
+__device__ __forceinline__ bool island_edge_body(uint32_t f) { return is_speedable(f) && (f & BF_ENABLED); }
+
+__global__ void k_isl_union(DW d) {
+    const uint32_t nl = d.cnt->n_live;
+    GRID_LOOP(i, nl + d.n_joints) {
+        uint32_t a, b;
+        if (i < nl) {
+            const uint32_t slot = d.c_slot[i];
+            if ((d.cs_flags[slot] & (CF_TOUCHING | CF_SENSOR)) != CF_TOUCHING) continue;
+            const uint2 bd = d.cs_body[slot];
+            a = bd.x; b = bd.y;
+        } else {
+            const uint32_t j = i - nl;
+            a = d.j_bodies[2 * j]; b = d.j_bodies[2 * j + 1];
+        }
+        if (island_edge_body(d.b_flags[a]) && island_edge_body(d.b_flags[b])) uf_union(d.b_island, a, b, d.cnt);
+    }
+}
+
+__global__ void k_isl_flatten(DW d) {
+    GRID_LOOP(b, d.n_bodies) {
+        const uint32_t r = uf_find(d.b_island, b);
+        d.b_island[b] = r;
+        const uint32_t f = d.b_flags[b];
+        if (island_edge_body(f) && (f & BF_AWAKE)) d.isl_awake[r] = 1u;
+    }
+}
+
+// pos0 <- pos1, GetBodyConstraint: Cap(GetVelocity(body, h)) (Body.cpp:290-309,
+// Velocity.cpp:26-45), per-island state reset.
+__global__ void k_body_begin(DW d) {
+    const DConf& c = *d.conf;
+    const float h = c.deltaTime;
+    const int np = c.regPositionIters;
+    uint32_t found = 0;
+    GRID_LOOP(b, d.n_bodies) {
+        const uint32_t f = d.b_flags[b];
+        const uint32_t r = d.b_island[b];
+        if (!island_edge_body(f) || !d.isl_awake[r]) continue;
+        d.b_flags[b] = f | BF_SOLVED | BF_AWAKE;
+        const float4 p = d.b_pos1[b];
+        d.b_pos0[b] = p;
+        float4 v = d.b_vel[b];
+        if (is_accelerable(f)) {
+            const float4 a = d.b_acc[b];
+            const float2 dm = d.b_damp[b];
+            v.x = v.x + a.x * h;
+            v.y = v.y + a.y * h;
+            v.z = v.z + h * a.z;
+            const float linv = 1.0f / (1.0f + h * dm.x);
+            v.x = v.x * linv;
+            v.y = v.y * linv;
+            v.z = v.z / (1.0f + h * dm.y);
+        }
+        {
+            const float tx = v.x * h, ty = v.y * h;
+            float lsq = 0.f;
+            lsq += tx * tx;
+            lsq += ty * ty;
+            if (lsq > c.maxTranslation * c.maxTranslation) {
+                const float ratio = c.maxTranslation / sqrtf(lsq);
+                v.x = v.x * ratio;
+                v.y = v.y * ratio;
+            }
+            const float absRot = fabsf(h * v.z);
+            if (absRot > c.maxRotation) {
+                const float ratio = c.maxRotation / absRot;
+                v.z = v.z * ratio;
+            }
+        }
+        d.b_vel[b] = v;
+        if (r == b) {
+            ++found;
+            for (int k = 0; k < np && k < kMaxPosIters; ++k) {
+                d.isl_sep[(size_t)b * kMaxPosIters + k] = __int_as_float(0x7f800000);
+                d.isl_jok[(size_t)b * kMaxPosIters + k] = 1u;
+            }
+            d.isl_uat[b] = __int_as_float(0x7f800000);
+        }
+    }
+    if (found) atomicAdd(&d.cnt->st_islands_found, found);
+}
+
+// ---- active constraints and colouring ---------------------------------------
+__global__ void k_active_flags(DW d) {
+    const uint32_t nl = d.cnt->n_live;
+    GRID_LOOP(i, nl + d.n_joints) {
+        uint32_t on = 0;
+        if (i < nl) {
+            const uint32_t slot = d.c_slot[i];
+            if ((d.cs_flags[slot] & (CF_TOUCHING | CF_SENSOR)) == CF_TOUCHING) {
+                const uint2 bd = d.cs_body[slot];
+                on = ((d.b_flags[bd.x] | d.b_flags[bd.y]) & BF_SOLVED) ? 1u : 0u;
+            }
+        } else {
+            const uint32_t j = i - nl;
+            const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+            const uint32_t fa = d.b_flags[a], fb = d.b_flags[b];
+            on = (((fa | fb) & BF_SOLVED) && (fa & BF_ENABLED) && (fb & BF_ENABLED)) ? 1u : 0u;
+        }
+        d.flags[i] = on;
+    }
+}
+
+__global__ void k_active_scatter(DW d) {
+    const uint32_t nl = d.cnt->n_live;
+    GRID_LOOP(i, nl + d.n_joints) {
+        if (!d.flags[i]) continue;
+        const uint32_t k = d.scan[i];
+        d.k_list[k] = (i < nl) ? d.c_slot[i] : ((i - nl) | kJointBit);
+    }
+}
+
+__global__ void k_active_done(DW d, uint32_t* n_bodies_count) {
+    Counters* c = d.cnt;
+    c->n_active = c->scan_total;
+    c->n_colours = 0u;
+    c->colour_remaining = 0u;
+    for (int k = 0; k < kSerialColour + 2; ++k) { c->colour_cnt[k] = 0u; c->colour_off[k] = 0u; }
+    *n_bodies_count = d.n_bodies;
+}
+
+__device__ __forceinline__ void constraint_bodies(const DW& d, uint32_t id, uint32_t& a, uint32_t& b) {
+    if (id & kJointBit) {
+        const uint32_t j = id & ~kJointBit;
+        a = d.j_bodies[2 * j]; b = d.j_bodies[2 * j + 1];
+    } else {
+        const uint2 bd = d.cs_body[id];
+        a = bd.x; b = bd.y;
+    }
+}
+
+// Colouring resources are the dynamic bodies: only they change under a constraint.
+__global__ void k_inc_count(DW d) {
+    GRID_LOOP(k, d.cnt->n_active) {
+        uint32_t a, b;
+        constraint_bodies(d, d.k_list[k], a, b);
+        if (is_accelerable(d.b_flags[a])) atomicAdd(&d.inc_cur[a], 1u);
+        if (is_accelerable(d.b_flags[b]) && b != a) atomicAdd(&d.inc_cur[b], 1u);
+        d.k_colour[k] = kNone;
+    }
+}
+
+__global__ void k_inc_fill(DW d) {
+    GRID_LOOP(k, d.cnt->n_active) {
+        uint32_t a, b;
+        constraint_bodies(d, d.k_list[k], a, b);
+        if (is_accelerable(d.b_flags[a])) d.inc_list[d.inc_off[a] + atomicAdd(&d.inc_cur[a], 1u)] = k;
+        if (is_accelerable(d.b_flags[b]) && b != a) d.inc_list[d.inc_off[b] + atomicAdd(&d.inc_cur[b], 1u)] = k;
+    }
+}
+
+// Speculative greedy colouring (Gebremedhin-Manne style), deterministic:
+// each round every uncoloured constraint picks the lowest colour unused by its
+// coloured neighbours; among uncoloured neighbours with the same pick, the
+// one of highest priority keeps it.  Rounds repeat until all are coloured; what is left
+// after kMaxColourRounds, or needs a 65th colour, goes to the serial colour.
+constexpr int kMaxColourRounds = 64;
+
+// Conflict priority: a hash of the constraint index (ties broken by index).
+// Index order alone follows the key order, which in stacked scenes is spatial,
+// so conflicts would chain across a whole stack; hashed priorities resolve them
+// in a logarithmic number of rounds and stay deterministic.
+// The hash is of world-local identifiers (proxy pair of a contact, body pair of
+// a joint), so a world is coloured the same whether it is stepped alone or in
+// a batch; ties fall back to the constraint index, whose order within a world
+// is also the same in both cases.
+__device__ __forceinline__ uint32_t mix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
+}
+__device__ __forceinline__ bool colour_beats(const DW& d, uint32_t o, uint32_t k) {
+    const uint32_t a = d.k_prio[o], b = d.k_prio[k];
+    return (a < b) || (a == b && o < k);
+}
+
+__device__ __forceinline__ uint32_t constraint_prio(const DW& d, uint32_t id) {
+    if (id & 0x80000000u) {
+        const uint32_t j = id & 0x7fffffffu;
+        const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+        const uint32_t base = d.w_body_off[d.b_world[a]];
+        return mix32(((a - base) * 0x9E3779B1u) ^ mix32((b - base) + 0x7F4A7C15u) ^ 0xA5A5A5A5u);
+    }
+    const uint2 pr = d.cs_proxy[id];
+    const uint32_t base = d.w_shape_off[d.b_world[d.s_body[pr.x]]];
+    return mix32(((pr.x - base) * 0x9E3779B1u) ^ mix32(pr.y - base));
+}
+
+__global__ void k_colour(DW d) {
+    const uint32_t n = d.cnt->n_active;
+    GRID_LOOP(k, n) d.k_prio[k] = constraint_prio(d, d.k_list[k]);
+    grid_barrier(d.cnt);
+    for (int round = 0; round < kMaxColourRounds; ++round) {
+        GRID_LOOP(k, n) {
+            if (d.k_colour[k] != kNone) continue;
+            uint32_t a, b;
+            constraint_bodies(d, d.k_list[k], a, b);
+            uint64_t forbid = 0;
+            const uint32_t bs[2] = {a, b};
+            for (int e = 0; e < 2; ++e) {
+                const uint32_t x = bs[e];
+                if (!is_accelerable(d.b_flags[x])) continue;
+                for (uint32_t t = d.inc_off[x]; t < d.inc_off[x + 1]; ++t) {
+                    const uint32_t c = __ldcg(&d.k_colour[d.inc_list[t]]);
+                    if (c < (uint32_t)kMaxColours) forbid |= 1ull << c;
+                }
+            }
+            d.k_tent[k] = (forbid == ~0ull) ? (uint32_t)kSerialColour : (uint32_t)(__ffsll((long long)~forbid) - 1);
+        }
+        grid_barrier(d.cnt);
+        uint32_t left = 0;
+        GRID_LOOP(k, n) {
+            if (d.k_colour[k] != kNone) continue;
+            const uint32_t t = __ldcg(&d.k_tent[k]);
+            if (t == (uint32_t)kSerialColour) continue;  // left to the serial colour
+            uint32_t a, b;
+            constraint_bodies(d, d.k_list[k], a, b);
+            bool ok = true;
+            const uint32_t bs[2] = {a, b};
+            for (int e = 0; e < 2 && ok; ++e) {
+                const uint32_t x = bs[e];
+                if (!is_accelerable(d.b_flags[x])) continue;
+                for (uint32_t q = d.inc_off[x]; q < d.inc_off[x + 1]; ++q) {
+                    const uint32_t o = d.inc_list[q];
+                    if (o != k && colour_beats(d, o, k) && __ldcg(&d.k_colour[o]) == kNone &&
+                        (__ldcg(&d.k_tent[o]) & 0xffffu) == t) { ok = false; break; }
+                }
+            }
+            if (ok) d.k_tent[k] = t | 0x40000000u;  // mark as accepted
+            else ++left;
+        }
+        if (left) atomicAdd(&d.cnt->colour_remaining, left);
+        grid_barrier(d.cnt);
+        GRID_LOOP(k, n) {
+            const uint32_t t = __ldcg(&d.k_tent[k]);
+            if (d.k_colour[k] == kNone && (t & 0x40000000u)) d.k_colour[k] = t & 0xffffu;
+        }
+        grid_barrier(d.cnt);
+        const uint32_t rem = *((volatile uint32_t*)&d.cnt->colour_remaining);
+        grid_barrier(d.cnt);
+        if (blockIdx.x == 0 && threadIdx.x == 0) d.cnt->colour_remaining = 0u;
+        grid_barrier(d.cnt);
+        if (rem == 0u) break;
+    }
+    GRID_LOOP(k, n) {
+        if (d.k_colour[k] == kNone) d.k_colour[k] = (uint32_t)kSerialColour;
+        atomicAdd(&d.cnt->colour_cnt[d.k_colour[k]], 1u);
+    }
+    grid_barrier(d.cnt);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Counters* c = d.cnt;
+        uint32_t off = 0, used = 0;
+        for (int k = 0; k <= kSerialColour; ++k) {
+            c->colour_off[k] = off;
+            off += c->colour_cnt[k];
+            if (k < kSerialColour && c->colour_cnt[k]) used = (uint32_t)k + 1u;
+            c->colour_cnt[k] = 0u;  // reused as scatter cursors
+        }
+        c->colour_off[kSerialColour + 1] = off;
+        c->n_colours = used;
+    }
+    grid_barrier(d.cnt);
+    GRID_LOOP(k, n) {
+        const uint32_t c = d.k_colour[k];
+        d.k_order[d.cnt->colour_off[c] + atomicAdd(&d.cnt->colour_cnt[c], 1u)] = k;
+    }
+}
+
+// ---- constraint construction --------------------------------------------------
+// GetWorldManifold (WorldManifold.cpp:111-132), VelocityConstraint ctor +
+// GetPoint + ComputeK (VelocityConstraint.cpp:38-185), PositionConstraint.
+__global__ void k_build_constraints(DW d) {
+    const DConf& c = *d.conf;
+    GRID_LOOP(k, d.cnt->n_active) {
+        const uint32_t id = d.k_list[k];
+        if (id & kJointBit) continue;
+        const uint32_t slot = id;
+        const uint2 bd = d.cs_body[slot];
+        const uint2 pr = d.cs_proxy[slot];
+        const float rA = d.s_radius[pr.x], rB = d.s_radius[pr.y];
+        const float4 pA = d.b_pos1[bd.x], pB = d.b_pos1[bd.y];
+        const float4 mA = d.b_mass[bd.x], mB = d.b_mass[bd.y];
+        const float4 vA = d.b_vel[bd.x], vB = d.b_vel[bd.y];
+        const Xf xfA = get_xf(pA.x, pA.y, pA.z, mk(mA.z, mA.w));
+        const Xf xfB = get_xf(pB.x, pB.y, pB.z, mk(mB.z, mB.w));
+        const uint32_t meta = d.m_meta[slot];
+        const int type = (int)(meta & 0xfu), count = (int)((meta >> 4) & 0xfu);
+        const float4 h = d.m_head[slot];
+        const float4 q0 = d.m_p0[slot], q1 = d.m_p1[slot];
+        const V2 ln = mk(h.x, h.y), lp = mk(h.z, h.w);
+        const V2 plp[2] = {mk(q0.x, q0.y), mk(q1.x, q1.y)};
+        const float pni[2] = {q0.z, q1.z}, pti[2] = {q0.w, q1.w};
+        V2 n = mk(0.f, 0.f);
+        V2 wpt[2] = {mk(0.f, 0.f), mk(0.f, 0.f)};
+        if (type == M_CIRCLES) {
+            const V2 a = xform(lp, xfA), b = xform(plp[0], xfB);
+            n = unit_vector(b - a, mk(1.f, 0.f));
+            const V2 cA = a + n * rA, cB = b - n * rB;
+            wpt[0] = vdiv(cA + cB, 2.0f);
+        } else if (type == M_FACEA) {
+            n = urotate(ln, xfA.q);
+            const V2 planePoint = xform(lp, xfA);
+            for (int i = 0; i < count; ++i) {
+                const V2 clip = xform(plp[i], xfB);
+                const V2 cA = clip + n * (rA - dot(clip - planePoint, n));
+                const V2 cB = clip - n * rB;
+                wpt[i] = vdiv(cA + cB, 2.0f);
+            }
+        } else if (type == M_FACEB) {
+            const V2 nb = urotate(ln, xfB.q);
+            const V2 planePoint = xform(lp, xfB);
+            for (int i = 0; i < count; ++i) {
+                const V2 clip = xform(plp[i], xfA);
+                const V2 cB = clip + nb * (rB - dot(clip - planePoint, nb));
+                const V2 cA = clip - nb * rA;
+                wpt[i] = vdiv(cA + cB, 2.0f);
+            }
+            n = -nb;
+        }
+        const float2 mat = d.cs_mat[slot];
+        VC vc;
+        vc.nx = n.x; vc.ny = n.y; vc.friction = mat.x; vc.tangentSpeed = 0.f;
+        vc.bA = bd.x; vc.bB = bd.y; vc.slot = slot;
+        vc.island = is_speedable(d.b_flags[bd.x]) ? d.b_island[bd.x] : d.b_island[bd.y];
+        const float invMass = mA.x + mB.x;
+        const V2 tangent = fwdperp(n);
+        const V2 velA = mk(vA.x, vA.y), velB = mk(vB.x, vB.y);
+        float rr[2][4], nm[2], tm[2], vb[2], ni[2], ti[2];
+        for (int j = 0; j < count; ++j) {
+            const V2 relA = wpt[j] - mk(pA.x, pA.y);
+            const V2 relB = wpt[j] - mk(pB.x, pB.y);
+            ni[j] = pni[j] * c.dtRatio;
+            ti[j] = pti[j] * c.dtRatio;
+            {
+                const V2 dv = (velB + revperp(relB) * vB.z) - (velA + revperp(relA) * vA.z);
+                const float vn = dot(dv, n);
+                vb[j] = (vn < -c.velocityThreshold) ? -mat.y * vn : 0.f;
+            }
+            {
+                const float crA = cross(relA, n), crB = cross(relB, n);
+                const float value = invMass + mA.y * (crA * crA) + mB.y * (crB * crB);
+                nm[j] = (value != 0.f) ? 1.0f / value : 0.f;
+            }
+            {
+                const float crA = cross(relA, tangent), crB = cross(relB, tangent);
+                const float value = invMass + mA.y * (crA * crA) + mB.y * (crB * crB);
+                tm[j] = (value != 0.f) ? 1.0f / value : 0.f;
+            }
+            rr[j][0] = relA.x; rr[j][1] = relA.y; rr[j][2] = relB.x; rr[j][3] = relB.y;
+        }
+        int cnt = count;
+        float k00 = 0.f, k11 = 0.f, k01 = 0.f, m00 = 0.f, m11 = 0.f, m01 = 0.f;
+        if (c.doBlocksolve && count == 2) {
+            const V2 rA0 = mk(rr[0][0], rr[0][1]), rB0 = mk(rr[0][2], rr[0][3]);
+            const V2 rA1 = mk(rr[1][0], rr[1][1]), rB1 = mk(rr[1][2], rr[1][3]);
+            const float rnA0 = cross(rA0, n), rnB0 = cross(rB0, n);
+            const float rnA1 = cross(rA1, n), rnB1 = cross(rB1, n);
+            const float kk00 = invMass + mA.y * (rnA0 * rnA0) + mB.y * (rnB0 * rnB0);
+            const float kk11 = invMass + mA.y * (rnA1 * rnA1) + mB.y * (rnB1 * rnB1);
+            const float kk01 = invMass + (mA.y * rnA0 * rnA1) + (mB.y * rnB0 * rnB1);
+            const float k_diff = kk00 * kk11 - kk01 * kk01;
+            if (kk00 * kk00 < 1000.0f * k_diff) {
+                k00 = kk00; k11 = kk11; k01 = kk01;
+                const float cp = cross(mk(kk00, kk01), mk(kk01, kk11));
+                if (!almost_zero(cp)) {
+                    const float inv = 1.0f / cp;
+                    m00 = kk11 * inv; m01 = -kk01 * inv; m11 = kk00 * inv;
+                }
+            } else {
+                cnt = 1;
+            }
+        }
+        vc.count = (uint32_t)cnt;
+        vc.rA0x = rr[0][0]; vc.rA0y = rr[0][1]; vc.rB0x = rr[0][2]; vc.rB0y = rr[0][3];
+        vc.nm0 = nm[0]; vc.tm0 = tm[0]; vc.vb0 = vb[0]; vc.ni0 = ni[0]; vc.ti0 = ti[0];
+        if (cnt == 2) {
+            vc.rA1x = rr[1][0]; vc.rA1y = rr[1][1]; vc.rB1x = rr[1][2]; vc.rB1y = rr[1][3];
+            vc.nm1 = nm[1]; vc.tm1 = tm[1]; vc.vb1 = vb[1]; vc.ni1 = ni[1]; vc.ti1 = ti[1];
+        } else {
+            vc.rA1x = vc.rA1y = vc.rB1x = vc.rB1y = 0.f;
+            vc.nm1 = vc.tm1 = vc.vb1 = vc.ni1 = vc.ti1 = 0.f;
+        }
+        vc.k00 = k00; vc.k11 = k11; vc.k01 = k01; vc.m00 = m00; vc.m11 = m11; vc.m01 = m01;
+        vc.pad0 = vc.pad1 = vc.pad2 = 0u;
+        d.vc[k] = vc;
+        PC pcs;
+        pcs.lnx = ln.x; pcs.lny = ln.y; pcs.lpx = lp.x; pcs.lpy = lp.y;
+        pcs.p0x = plp[0].x; pcs.p0y = plp[0].y; pcs.p1x = plp[1].x; pcs.p1y = plp[1].y;
+        pcs.totalRadius = rA + rB;
+        pcs.type = (uint32_t)type; pcs.count = (uint32_t)count; pcs.bA = bd.x; pcs.bB = bd.y;
+        pcs.island = vc.island; pcs.pad0 = pcs.pad1 = 0u;
+        d.pc[k] = pcs;
+    }
+}
+
+// ---- per-constraint solver steps --------------------------------------------
+__device__ __forceinline__ bool writable(const DW& d, uint32_t b) { return is_accelerable(d.b_flags[b]); }
+
+// WarmStartVelocities (AabbTreeWorld.cpp:227-274).
+__device__ void warm_start(const DW& d, const VC& vc) {
+    const float4 mA = d.b_mass[vc.bA], mB = d.b_mass[vc.bB];
+    const V2 n = mk(vc.nx, vc.ny), t = fwdperp(n);
+    float dAx = 0.f, dAy = 0.f, dAw = 0.f, dBx = 0.f, dBy = 0.f, dBw = 0.f;
+    for (uint32_t j = 0; j < vc.count; ++j) {
+        const float ni = j ? vc.ni1 : vc.ni0, ti = j ? vc.ti1 : vc.ti0;
+        const V2 rA = j ? mk(vc.rA1x, vc.rA1y) : mk(vc.rA0x, vc.rA0y);
+        const V2 rB = j ? mk(vc.rB1x, vc.rB1y) : mk(vc.rB0x, vc.rB0y);
+        const V2 P = n * ni + t * ti;
+        const float LA = cross(rA, P), LB = cross(rB, P);
+        dAx = dAx - P.x * mA.x; dAy = dAy - P.y * mA.x; dAw = dAw - mA.y * LA;
+        dBx = dBx + P.x * mB.x; dBy = dBy + P.y * mB.x; dBw = dBw + mB.y * LB;
+    }
+    if (writable(d, vc.bA)) {
+        float4 v = d.b_vel[vc.bA];
+        v.x = v.x + dAx; v.y = v.y + dAy; v.z = v.z + dAw;
+        d.b_vel[vc.bA] = v;
+    }
+    if (writable(d, vc.bB)) {
+        float4 v = d.b_vel[vc.bB];
+        v.x = v.x + dBx; v.y = v.y + dBy; v.z = v.z + dBw;
+        d.b_vel[vc.bB] = v;
+    }
+}
+
+__device__ __forceinline__ V2 rel_vel(float4 va, V2 rA, float4 vb, V2 rB) {
+    return (mk(vb.x, vb.y) + revperp(rB) * vb.z) - (mk(va.x, va.y) + revperp(rA) * va.z);
+}
+
+// GaussSeidel::SolveVelocityConstraint (ContactSolver.cpp:245-492).
+__device__ void solve_contact_velocity(const DW& d, VC& vc) {
+    const float4 mA = d.b_mass[vc.bA], mB = d.b_mass[vc.bB];
+    float4 vA = d.b_vel[vc.bA], vB = d.b_vel[vc.bB];
+    const V2 n = mk(vc.nx, vc.ny);
+    const V2 rA0 = mk(vc.rA0x, vc.rA0y), rB0 = mk(vc.rB0x, vc.rB0y);
+    const V2 rA1 = mk(vc.rA1x, vc.rA1y), rB1 = mk(vc.rB1x, vc.rB1y);
+    // tangent then normal, point 1 before point 0 (ContactSolver.cpp:337-454)
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool tangentPass = pass == 0;
+        if (!tangentPass && vc.count == 2 && !(vc.k00 == 0.f && vc.k11 == 0.f && vc.k01 == 0.f)) {
+            // BlockSolveNormalConstraint (ContactSolver.cpp:245-335)
+            const V2 dv0 = rel_vel(vA, rA0, vB, rB0), dv1 = rel_vel(vA, rA1, vB, rB1);
+            const float vn0 = dot(dv0, n), vn1 = dot(dv1, n);
+            const float b0 = vn0 - vc.vb0, b1 = vn1 - vc.vb1;
+            const float a0 = vc.ni0, a1 = vc.ni1;
+            float Kx0 = 0.f; Kx0 += vc.k00 * a0; Kx0 += vc.k01 * a1;
+            float Kx1 = 0.f; Kx1 += vc.k01 * a0; Kx1 += vc.k11 * a1;
+            const float bp0 = b0 - Kx0, bp1 = b1 - Kx1;
+            float x0 = 0.f, x1 = 0.f;
+            bool apply = false;
+            {
+                float q0 = 0.f; q0 += vc.m00 * bp0; q0 += vc.m01 * bp1;
+                float q1 = 0.f; q1 += vc.m01 * bp0; q1 += vc.m11 * bp1;
+                x0 = -q0; x1 = -q1;
+                apply = (x0 >= 0.f && x1 >= 0.f);
+            }
+            if (!apply) {
+                x0 = -vc.nm0 * bp0; x1 = 0.f;
+                const float vn2 = vc.k01 * x0 + bp1;
+                apply = (x0 >= 0.f && vn2 >= 0.f);
+            }
+            if (!apply) {
+                x0 = 0.f; x1 = -vc.nm1 * bp1;
+                const float vn1b = vc.k01 * x1 + bp0;
+                apply = (x1 >= 0.f && vn1b >= 0.f);
+            }
+            if (!apply) {
+                x0 = 0.f; x1 = 0.f;
+                apply = (bp0 >= 0.f && bp1 >= 0.f);
+            }
+            if (apply) {
+                const float d0 = x0 - vc.ni0, d1 = x1 - vc.ni1;
+                const V2 P0 = n * d0, P1 = n * d1;
+                const V2 P = P0 + P1;
+                const float LA = cross(rA0, P0) + cross(rA1, P1);
+                const float LB = cross(rB0, P0) + cross(rB1, P1);
+                vA.x = vA.x + (-(P.x * mA.x)); vA.y = vA.y + (-(P.y * mA.x)); vA.z = vA.z + (-(mA.y * LA));
+                vB.x = vB.x + P.x * mB.x; vB.y = vB.y + P.y * mB.x; vB.z = vB.z + mB.y * LB;
+                vc.ni0 = x0; vc.ni1 = x1;
+            }
+            continue;
+        }
+        const V2 dir = tangentPass ? fwdperp(n) : n;
+        for (int k = (vc.count == 2) ? 1 : 0; k >= 0; --k) {
+            const V2 rA = k ? rA1 : rA0, rB = k ? rB1 : rB0;
+            const V2 cv = rel_vel(vA, rA, vB, rB);
+            float oldImp, newImp;
+            if (tangentPass) {
+                const float dvel = vc.tangentSpeed - dot(cv, dir);
+                const float lambda = (k ? vc.tm1 : vc.tm0) * dvel;
+                const float maxImp = vc.friction * (k ? vc.ni1 : vc.ni0);
+                oldImp = k ? vc.ti1 : vc.ti0;
+                newImp = clampf_(oldImp + lambda, -maxImp, maxImp);
+            } else {
+                const float dvel = dot(cv, dir);
+                const float lambda = (k ? vc.nm1 : vc.nm0) * ((k ? vc.vb1 : vc.vb0) - dvel);
+                oldImp = k ? vc.ni1 : vc.ni0;
+                newImp = maxf_(oldImp + lambda, 0.f);
+            }
+            const float inc = newImp - oldImp;
+            const V2 P = dir * inc;
+            const float LA = cross(rA, P), LB = cross(rB, P);
+            vA.x = vA.x - P.x * mA.x; vA.y = vA.y - P.y * mA.x; vA.z = vA.z - mA.y * LA;
+            vB.x = vB.x + P.x * mB.x; vB.y = vB.y + P.y * mB.x; vB.z = vB.z + mB.y * LB;
+            const float nv = oldImp + inc;
+            if (tangentPass) { if (k) vc.ti1 = nv; else vc.ti0 = nv; }
+            else { if (k) vc.ni1 = nv; else vc.ni0 = nv; }
+        }
+    }
+    if (writable(d, vc.bA)) d.b_vel[vc.bA] = vA;
+    if (writable(d, vc.bB)) d.b_vel[vc.bB] = vB;
+}
+
+struct PSM {
+    V2 n, pt;
+    float sep;
+};
+// GetPSM (PositionSolverManifold.cpp:103-121).
+__device__ __forceinline__ PSM get_psm(const PC& pc, int idx, Xf xfA, Xf xfB) {
+    PSM r;
+    const V2 lp = mk(pc.lpx, pc.lpy), ln = mk(pc.lnx, pc.lny);
+    const V2 plp = idx ? mk(pc.p1x, pc.p1y) : mk(pc.p0x, pc.p0y);
+    if (pc.type == M_CIRCLES) {
+        const V2 a = xform(lp, xfA), b = xform(plp, xfB);
+        const V2 delta = b - a;
+        r.n = unit_vector(delta, mk(0.f, 0.f));
+        r.pt = vdiv(a + b, 2.0f);
+        r.sep = dot(delta, r.n);
+    } else if (pc.type == M_FACEA) {
+        const V2 planePoint = xform(lp, xfA);
+        r.n = urotate(ln, xfA.q);
+        r.pt = xform(plp, xfB);
+        r.sep = dot(r.pt - planePoint, r.n);
+    } else {
+        const V2 planePoint = xform(lp, xfB);
+        const V2 nb = urotate(ln, xfB.q);
+        r.pt = xform(plp, xfA);
+        r.sep = dot(r.pt - planePoint, nb);
+        r.n = -nb;
+    }
+    return r;
+}
+
+struct PosSol {
+    float ax, ay, aa, bx, by, ba, sep;
+};
+// solver_fn of GaussSeidel::SolvePositionConstraint (ContactSolver.cpp:521-551).
+__device__ __forceinline__ PosSol pos_solver_fn(const PSM& psm, V2 pA, V2 pB, float4 mA, float4 mB, float totalRadius,
+                                                const DConf& c) {
+    const float invMassTotal = mA.x + mB.x;
+    const float separation = psm.sep - totalRadius;
+    const V2 rA = psm.pt - pA, rB = psm.pt - pB;
+    const float cA = cross(rA, psm.n), cB = cross(rB, psm.n);
+    const float K = invMassTotal + mA.y * (cA * cA) + mB.y * (cB * cB);
+    const float C = -clampf_(c.regResolutionRate * (separation + c.linearSlop), -c.maxLinearCorrection, 0.f);
+    const V2 P = vdiv(psm.n * C, K);
+    const float LA = cross(rA, P), LB = cross(rB, P);
+    PosSol s;
+    s.ax = -(P.x * mA.x); s.ay = -(P.y * mA.x); s.aa = -(mA.y * LA);
+    s.bx = P.x * mB.x; s.by = P.y * mB.x; s.ba = +(mB.y * LB);
+    s.sep = separation;
+    return s;
+}
+
+// GaussSeidel::SolvePositionConstraint (ContactSolver.cpp:494-643); returns the
+// separation the reference reports for this constraint.
+__device__ float solve_contact_position(const DW& d, const PC& pc) {
+    const DConf& c = *d.conf;
+    const float4 mA = d.b_mass[pc.bA], mB = d.b_mass[pc.bB];
+    float4 pA = d.b_pos1[pc.bA], pB = d.b_pos1[pc.bB];
+    const V2 lcA = mk(mA.z, mA.w), lcB = mk(mB.z, mB.w);
+    float minSep = __int_as_float(0x7f800000);
+    auto add = [](float4& p, float x, float y, float a) { p.x = p.x + x; p.y = p.y + y; p.z = p.z + a; };
+    if (pc.count == 1u) {
+        const PSM psm0 = get_psm(pc, 0, get_xf(pA.x, pA.y, pA.z, lcA), get_xf(pB.x, pB.y, pB.z, lcB));
+        const PosSol s = pos_solver_fn(psm0, mk(pA.x, pA.y), mk(pB.x, pB.y), mA, mB, pc.totalRadius, c);
+        add(pA, s.ax, s.ay, s.aa); add(pB, s.bx, s.by, s.ba);
+        minSep = 0.f + s.sep;
+    } else if (pc.count == 2u) {
+        const Xf xfA = get_xf(pA.x, pA.y, pA.z, lcA), xfB = get_xf(pB.x, pB.y, pB.z, lcB);
+        const PSM psm0 = get_psm(pc, 0, xfA, xfB);
+        const PSM psm1 = get_psm(pc, 1, xfA, xfB);
+        if (almost_equal(psm0.sep, psm1.sep)) {
+            const PosSol s0 = pos_solver_fn(psm0, mk(pA.x, pA.y), mk(pB.x, pB.y), mA, mB, pc.totalRadius, c);
+            const PosSol s1 = pos_solver_fn(psm1, mk(pA.x, pA.y), mk(pB.x, pB.y), mA, mB, pc.totalRadius, c);
+            add(pA, s0.ax, s0.ay, s0.aa); add(pA, s1.ax, s1.ay, s1.aa);
+            add(pB, s0.bx, s0.by, s0.ba); add(pB, s1.bx, s1.by, s1.ba);
+            minSep = s0.sep;
+        } else if (psm0.sep < psm1.sep || psm1.sep < psm0.sep) {
+            const int first = (psm0.sep < psm1.sep) ? 0 : 1;
+            const PSM pf = first ? psm1 : psm0;
+            const PosSol s0 = pos_solver_fn(pf, mk(pA.x, pA.y), mk(pB.x, pB.y), mA, mB, pc.totalRadius, c);
+            add(pA, s0.ax, s0.ay, s0.aa); add(pB, s0.bx, s0.by, s0.ba);
+            const PSM ps = get_psm(pc, 1 - first, get_xf(pA.x, pA.y, pA.z, lcA), get_xf(pB.x, pB.y, pB.z, lcB));
+            const PosSol s1 = pos_solver_fn(ps, mk(pA.x, pA.y), mk(pB.x, pB.y), mA, mB, pc.totalRadius, c);
+            add(pA, s1.ax, s1.ay, s1.aa); add(pB, s1.bx, s1.by, s1.ba);
+            minSep = s0.sep;
+        }
+    }
+    if (writable(d, pc.bA)) d.b_pos1[pc.bA] = pA;
+    if (writable(d, pc.bB)) d.b_pos1[pc.bB] = pB;
+    return minSep;
+}
+
+// ---- revolute joints (RevoluteJointConf.cpp:127-431) --------------------------
+__device__ void joint_init_velocity(const DW& d, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = d.b_mass[a], mB = d.b_mass[b];
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    const float4 pA = d.b_pos1[a], pB = d.b_pos1[b];
+    float4 vA = d.b_vel[a], vB = d.b_vel[b];
+    const float4 an = d.j_anchor[j];
+    const float4 prm = d.j_param[j];
+    const uint32_t jf = d.j_flags[j];
+    const V2 qA = unit_from_angle(pA.z), qB = unit_from_angle(pB.z);
+    const V2 rA = rotate(mk(an.x, an.y) - mk(mA.z, mA.w), qA);
+    const V2 rB = rotate(mk(an.z, an.w) - mk(mB.z, mB.w), qB);
+    const float totInvI = iIA + iIB;
+    const bool fixedRotation = (totInvI == 0.f);
+    const float exx = iMA + ((rA.y * rA.y) * iIA) + iMB + ((rB.y * rB.y) * iIB);
+    const float eyx = (-rA.y * rA.x * iIA) + (-rB.y * rB.x * iIB);
+    const float ezx = (-rA.y * iIA) + (-rB.y * iIB);
+    const float eyy = iMA + ((rA.x * rA.x) * iIA) + iMB + ((rB.x * rB.x) * iIB);
+    const float ezy = (rA.x * iIA) + (rB.x * iIB);
+    const float angularMass = (totInvI > 0.f) ? 1.0f / totInvI : 0.f;
+    float4 imp = d.j_imp[j];  // x y z limitState
+    float4 m1 = d.j_m1[j];    // ey.z ez.z angularMass motorImpulse
+    float motorImpulse = m1.w;
+    const bool enableMotor = (jf & 2u) != 0u, enableLimit = (jf & 1u) != 0u;
+    if (!enableMotor || fixedRotation) motorImpulse = 0.f;
+    int limitState = (int)imp.w;
+    if (enableLimit && !fixedRotation) {
+        const float jointAngle = pB.z - pA.z - prm.x;
+        if (fabsf(prm.z - prm.y) < (c.angularSlop * 2.0f)) limitState = 3;
+        else if (jointAngle <= prm.y) { if (limitState != 1) { limitState = 1; imp.z = 0.f; } }
+        else if (jointAngle >= prm.z) { if (limitState != 2) { limitState = 2; imp.z = 0.f; } }
+        else { limitState = 0; imp.z = 0.f; }
+    } else {
+        limitState = 0;
+    }
+    if (c.doWarmStart) {
+        imp.x *= c.dtRatio; imp.y *= c.dtRatio; imp.z *= c.dtRatio;
+        motorImpulse *= c.dtRatio;
+        const V2 P = mk(imp.x, imp.y);
+        const float L = motorImpulse + imp.z;
+        const float LA = cross(rA, P) + L, LB = cross(rB, P) + L;
+        vA.x = vA.x - P.x * iMA; vA.y = vA.y - P.y * iMA; vA.z = vA.z - iIA * LA;
+        vB.x = vB.x + P.x * iMB; vB.y = vB.y + P.y * iMB; vB.z = vB.z + iIB * LB;
+    } else {
+        imp.x = imp.y = imp.z = 0.f;
+        motorImpulse = 0.f;
+    }
+    imp.w = (float)limitState;
+    d.j_imp[j] = imp;
+    d.j_r[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    d.j_m0[j] = make_float4(exx, eyx, ezx, eyy);
+    d.j_m1[j] = make_float4(ezy, totInvI, angularMass, motorImpulse);
+    if (writable(d, a)) d.b_vel[a] = vA;
+    if (writable(d, b)) d.b_vel[b] = vB;
+}
+
+__device__ void joint_solve_velocity(const DW& d, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = d.b_mass[a], mB = d.b_mass[b];
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    float4 vA = d.b_vel[a], vB = d.b_vel[b];
+    const float4 r = d.j_r[j];
+    const float4 m0 = d.j_m0[j];
+    float4 m1 = d.j_m1[j];
+    float4 imp = d.j_imp[j];
+    const uint32_t jf = d.j_flags[j];
+    const float4 prm = d.j_param[j];
+    const V2 rA = mk(r.x, r.y), rB = mk(r.z, r.w);
+    const bool fixedRotation = (iIA + iIB == 0.f);
+    if ((jf & 2u) && ((int)imp.w != 3) && !fixedRotation) {
+        const float impulse = -m1.z * (vB.z - vA.z - prm.w);
+        const float oldImpulse = m1.w;
+        const float maxImpulse = c.deltaTime * d.j_maxtorque[j];
+        m1.w = clampf_(m1.w + impulse, -maxImpulse, maxImpulse);
+        const float inc = m1.w - oldImpulse;
+        vA.z -= iIA * inc;
+        vB.z += iIB * inc;
+    }
+    const V2 vb = mk(vB.x, vB.y) + revperp(rB) * vB.z;
+    const V2 va = mk(vA.x, vA.y) + revperp(rA) * vA.z;
+    const V2 vd = vb - va;
+    {
+        // Solve22 (Math.hpp:462-474) on the upper 2x2 of the 3x3 mass
+        const float xx = m0.x, xy = m0.y, yx = m0.y, yy = m0.w;
+        const float cp = xx * yy - xy * yx;
+        const float det = (cp != 0.f) ? (1.0f / cp) : cp;
+        const V2 bb = -vd;
+        const V2 P = mk(det * (yy * bb.x - xy * bb.y), det * (xx * bb.y - yx * bb.x));
+        imp.x += P.x;
+        imp.y += P.y;
+        const float LA = cross(rA, P), LB = cross(rB, P);
+        vA.x = vA.x - P.x * iMA; vA.y = vA.y - P.y * iMA; vA.z = vA.z - iIA * LA;
+        vB.x = vB.x + P.x * iMB; vB.y = vB.y + P.y * iMB; vB.z = vB.z + iIB * LB;
+    }
+    d.j_imp[j] = imp;
+    d.j_m1[j] = m1;
+    if (writable(d, a)) d.b_vel[a] = vA;
+    if (writable(d, b)) d.b_vel[b] = vB;
+}
+
+// Returns whether the joint is within tolerance.
+__device__ bool joint_solve_position(const DW& d, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = d.b_mass[a], mB = d.b_mass[b];
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    float4 pA = d.b_pos1[a], pB = d.b_pos1[b];
+    const float4 an = d.j_anchor[j];
+    const V2 qA = unit_from_angle(pA.z), qB = unit_from_angle(pB.z);
+    const V2 rA = rotate(mk(an.x, an.y) - mk(mA.z, mA.w), qA);
+    const V2 rB = rotate(mk(an.z, an.w) - mk(mB.z, mB.w), qB);
+    const V2 C = (mk(pB.x, pB.y) + rB) - (mk(pA.x, pA.y) + rA);
+    const float positionError = mag2(C);
+    const float exx = iMA + (iIA * (rA.y * rA.y)) + iMB + (iIB * (rB.y * rB.y));
+    const float exy = (-iIA * rA.x * rA.y) + (-iIB * rB.x * rB.y);
+    const float eyy = iMA + (iIA * (rA.x * rA.x)) + iMB + (iIB * (rB.x * rB.x));
+    const float cp = cross(mk(exx, exy), mk(exy, eyy));
+    V2 x = mk(0.f, 0.f);
+    if (!almost_zero(cp)) {
+        const float inv = 1.0f / cp;
+        x = mk((eyy * C.x - exy * C.y) * inv, (exx * C.y - exy * C.x) * inv);
+    }
+    const V2 P = -x;
+    pA.x = pA.x - P.x * iMA; pA.y = pA.y - P.y * iMA; pA.z = pA.z - iIA * cross(rA, P);
+    pB.x = pB.x + P.x * iMB; pB.y = pB.y + P.y * iMB; pB.z = pB.z + iIB * cross(rB, P);
+    if (writable(d, a)) d.b_pos1[a] = pA;
+    if (writable(d, b)) d.b_pos1[b] = pB;
+    return (positionError <= c.linearSlop * c.linearSlop) && (0.f <= c.angularSlop);
+}
+
+__device__ __forceinline__ uint32_t joint_island(const DW& d, uint32_t j) {
+    const uint32_t a = d.j_bodies[2 * j];
+    return is_speedable(d.b_flags[a]) ? d.b_island[a] : d.b_island[d.j_bodies[2 * j + 1]];
+}
+
+// Whether island L reached the position tolerance before iteration `it`.
+__device__ __forceinline__ bool island_done(const DW& d, uint32_t L, int it) {
+    const float thr = d.conf->regMinSeparation;
+    for (int k = 0; k < it; ++k) {
+        const size_t at = (size_t)L * kMaxPosIters + k;
+        if (__ldcg(&d.isl_sep[at]) >= thr && __ldcg(&d.isl_jok[at])) return true;
+    }
+    return false;
+}
+
+// The whole regular-phase solve of a step: warm start, velocity sweeps,
+// position integration, position sweeps, impulse store.  One cooperative
+// launch; a bounded grid barrier separates colours.
+__global__ void k_solve(DW d) {
+    const DConf& c = *d.conf;
+    const uint32_t ncol = d.cnt->n_colours;
+    const uint32_t* off = d.cnt->colour_off;
+    const uint32_t nser = off[kSerialColour + 1] - off[kSerialColour];
+    const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+
+    // warm start (contacts) and joint InitVelocity, colour by colour
+    for (uint32_t col = 0; col <= ncol; ++col) {
+        const bool serial = (col == ncol);
+        const uint32_t lo = serial ? off[kSerialColour] : off[col];
+        const uint32_t n = serial ? nser : off[col + 1] - off[col];
+        if (serial && !n) break;
+        if (serial) {
+            if (lead) {
+                for (uint32_t t = 0; t < n; ++t) {
+                    const uint32_t k = d.k_order[lo + t];
+                    const uint32_t id = d.k_list[k];
+                    if (id & kJointBit) joint_init_velocity(d, id & ~kJointBit);
+                    else if (c.doWarmStart) warm_start(d, d.vc[k]);
+                }
+            }
+        } else {
+            GRID_LOOP(t, n) {
+                const uint32_t k = d.k_order[lo + t];
+                const uint32_t id = d.k_list[k];
+                if (id & kJointBit) joint_init_velocity(d, id & ~kJointBit);
+                else if (c.doWarmStart) warm_start(d, d.vc[k]);
+            }
+        }
+        grid_barrier(d.cnt);
+    }
+    // velocity iterations
+    for (int it = 0; it < c.regVelocityIters; ++it) {
+        for (uint32_t col = 0; col <= ncol; ++col) {
+            const bool serial = (col == ncol);
+            const uint32_t lo = serial ? off[kSerialColour] : off[col];
+            const uint32_t n = serial ? nser : off[col + 1] - off[col];
+            if (serial && !n) break;
+            if (serial) {
+                if (lead) {
+                    for (uint32_t t = 0; t < n; ++t) {
+                        const uint32_t k = d.k_order[lo + t];
+                        const uint32_t id = d.k_list[k];
+                        if (id & kJointBit) joint_solve_velocity(d, id & ~kJointBit);
+                        else { VC vc = d.vc[k]; solve_contact_velocity(d, vc); d.vc[k] = vc; }
+                    }
+                }
+            } else {
+                GRID_LOOP(t, n) {
+                    const uint32_t k = d.k_order[lo + t];
+                    const uint32_t id = d.k_list[k];
+                    if (id & kJointBit) joint_solve_velocity(d, id & ~kJointBit);
+                    else {
+                        VC vc = d.vc[k];
+                        solve_contact_velocity(d, vc);
+                        reinterpret_cast<float4*>(&d.vc[k])[6] = make_float4(vc.ni0, vc.ti0, vc.ni1, vc.ti1);
+                    }
+                }
+            }
+            grid_barrier(d.cnt);
+        }
+    }
+    // IntegratePositions (AabbTreeWorld.cpp:176-188)
+    const float h = c.deltaTime;
+    GRID_LOOP(b, d.n_bodies) {
+        if (!(d.b_flags[b] & BF_SOLVED)) continue;
+        const float4 v = d.b_vel[b];
+        float4 p = d.b_pos1[b];
+        const float tx = v.x * h, ty = v.y * h, rot = h * v.z;
+        p.x = p.x + tx; p.y = p.y + ty; p.z = p.z + rot;
+        d.b_pos1[b] = p;
+    }
+    grid_barrier(d.cnt);
+    // position iterations with per-island early exit
+    for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it) {
+        for (uint32_t col = 0; col <= ncol; ++col) {
+            const bool serial = (col == ncol);
+            const uint32_t lo = serial ? off[kSerialColour] : off[col];
+            const uint32_t n = serial ? nser : off[col + 1] - off[col];
+            if (serial && !n) break;
+            auto body = [&](uint32_t t) {
+                const uint32_t k = d.k_order[lo + t];
+                const uint32_t id = d.k_list[k];
+                if (id & kJointBit) {
+                    const uint32_t j = id & ~kJointBit;
+                    const uint32_t L = joint_island(d, j);
+                    if (island_done(d, L, it)) return;
+                    if (!joint_solve_position(d, j)) d.isl_jok[(size_t)L * kMaxPosIters + it] = 0u;
+                } else {
+                    const PC pc = d.pc[k];
+                    if (island_done(d, pc.island, it)) return;
+                    const float sep = solve_contact_position(d, pc);
+                    atomic_min_float(&d.isl_sep[(size_t)pc.island * kMaxPosIters + it], sep);
+                }
+            };
+            if (serial) {
+                if (lead) for (uint32_t t = 0; t < n; ++t) body(t);
+            } else {
+                GRID_LOOP(t, n) body(t);
+            }
+            grid_barrier(d.cnt);
+        }
+    }
+    // AssignImpulses (AabbTreeWorld.cpp:196-220)
+    GRID_LOOP(k, d.cnt->n_active) {
+        const uint32_t id = d.k_list[k];
+        if (id & kJointBit) continue;
+        const VC& vc = d.vc[k];
+        float4 p0 = d.m_p0[vc.slot];
+        p0.z = vc.ni0; p0.w = vc.ti0;
+        d.m_p0[vc.slot] = p0;
+        if (vc.count == 2u) {
+            float4 p1 = d.m_p1[vc.slot];
+            p1.z = vc.ni1; p1.w = vc.ti1;
+            d.m_p1[vc.slot] = p1;
+        }
+    }
+}
+
+// Write-back bookkeeping, transforms and under-active times
+// (AabbTreeWorld.cpp:1652-1679, :403-417).
+__global__ void k_body_end(DW d) {
+    const DConf& c = *d.conf;
+    GRID_LOOP(b, d.n_bodies) {
+        uint32_t f = d.b_flags[b];
+        if (!(f & BF_SOLVED)) continue;
+        const float4 p = d.b_pos1[b], p0 = d.b_pos0[b];
+        if (p.x != p0.x || p.y != p0.y || p.z != p0.z) {
+            f |= BF_MOVED;
+            const float4 m = d.b_mass[b];
+            const Xf x = get_xf(p.x, p.y, p.z, mk(m.z, m.w));
+            d.b_xf[b] = make_float4(x.p.x, x.p.y, x.q.x, x.q.y);
+        }
+        d.b_flags[b] = f;
+        const float4 v = d.b_vel[b];
+        float lin2 = 0.f;
+        lin2 += v.x * v.x;
+        lin2 += v.y * v.y;
+        const float ang2 = v.z * v.z;
+        const bool under = (ang2 <= c.angularSleepTolerance * c.angularSleepTolerance) &&
+                           (lin2 <= c.linearSleepTolerance * c.linearSleepTolerance);
+        const float t = ((f & BF_ALLOW_SLEEP) && under) ? d.b_uat[b] + c.deltaTime : 0.f;
+        d.b_uat[b] = t;
+        atomic_min_float(&d.isl_uat[d.b_island[b]], t);
+    }
+}
+
+__global__ void k_sleep(DW d) {
+    const DConf& c = *d.conf;
+    const int np = min(c.regPositionIters, kMaxPosIters);
+    uint32_t slept = 0, solved_roots = 0, iters = 0;
+    GRID_LOOP(b, d.n_bodies) {
+        const uint32_t f = d.b_flags[b];
+        if (!(f & BF_SOLVED)) continue;
+        const uint32_t L = d.b_island[b];
+        // solved: tolerance reached within the position iterations
+        int done_at = -1;
+        for (int k = 0; k < np; ++k) {
+            const size_t at = (size_t)L * kMaxPosIters + k;
+            if (d.isl_sep[at] >= c.regMinSeparation && d.isl_jok[at]) { done_at = k; break; }
+        }
+        if (L == b) {
+            if (done_at >= 0) ++solved_roots;
+            iters += (done_at >= 0) ? (uint32_t)(done_at + 1) : (uint32_t)np;
+            const float ms = d.isl_sep[(size_t)L * kMaxPosIters];
+            if (ms < __int_as_float(0x7f800000)) atomic_min_float(&d.cnt->st_min_separation, ms);
+        }
+        if (d.isl_uat[L] >= c.minStillTimeToSleep && done_at >= 0) {
+            if ((f & BF_AWAKE) && (f & BF_ALLOW_SLEEP)) {
+                d.b_flags[b] = f & ~BF_AWAKE;
+                d.b_uat[b] = 0.f;
+                d.b_vel[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+                ++slept;
+            }
+        }
+    }
+    if (slept) atomicAdd(&d.cnt->st_bodies_slept, slept);
+    if (solved_roots) atomicAdd(&d.cnt->st_islands_solved, solved_roots);
+    if (iters) atomicAdd(&d.cnt->st_sum_pos_iters, iters);
+}
+
+__global__ void k_step_reset(DW d) {
+    Counters* c = d.cnt;
+    c->st_contacts_added = 0u;
+    c->st_contacts_destroyed = 0u;
+    c->st_contacts_updated = 0u;
+    c->st_islands_found = 0u;
+    c->st_islands_solved = 0u;
+    c->st_bodies_slept = 0u;
+    c->st_proxies_moved = 0u;
+    c->st_sum_pos_iters = 0u;
+    c->st_min_separation = __int_as_float(0x7f800000);
+    c->st_max_inc_impulse = 0.f;
+    c->bar_count = 0u;
+}
+
+__global__ void k_items_count(DW d, uint32_t* n_items) { *n_items = d.cnt->n_live + d.n_joints; }
+
+__global__ void k_inc_off_tail(DW d) { d.inc_off[d.n_bodies] = d.cnt->pad[3]; }
+
+__global__ void k_clear_dirty(DW d) {
+    GRID_LOOP(b, d.n_bodies) d.b_flags[b] &= ~BF_DIRTY;
+}
+
+template <typename K>
+void launch_coop(K kernel, const DW& d, const Launch& L, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)L.coop_grid);
+    cfg.blockDim = dim3((unsigned)L.coop_threads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, d);
+}
+
+}  // namespace
+
+int coop_blocks_per_sm(int threads) {
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_solve, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_colour, threads, 0);
+    return a < b ? a : b;
+}
+
+void launch_reset_step(const DW& d, const Launch& L, cudaStream_t s) {
+    (void)L;
+    k_step_reset<<<1, 1, 0, s>>>(d);
+}
+
+void launch_clear_dirty(const DW& d, const Launch& L, cudaStream_t s) {
+    k_clear_dirty<<<L.grid, L.threads, 0, s>>>(d);
+}
+
+void launch_islands_colour(const DW& d, const Launch& L, cudaStream_t s) {
+    k_isl_init<<<L.grid, L.threads, 0, s>>>(d);
+    k_isl_union<<<L.grid, L.threads, 0, s>>>(d);
+    k_isl_flatten<<<L.grid, L.threads, 0, s>>>(d);
+    k_body_begin<<<L.grid, L.threads, 0, s>>>(d);
+    // active constraints in live-list order (contacts), then joints
+    uint32_t* n_items = &d.cnt->pad[1];
+    uint32_t* n_bodies = &d.cnt->pad[2];
+    k_active_flags<<<L.grid, L.threads, 0, s>>>(d);
+    k_items_count<<<1, 1, 0, s>>>(d, n_items);
+    scan_exclusive(L.prims, d.flags, d.scan, n_items, &d.cnt->scan_total, d.partial, s);
+    k_active_scatter<<<L.grid, L.threads, 0, s>>>(d);
+    k_active_done<<<1, 1, 0, s>>>(d, n_bodies);
+    cudaMemsetAsync(d.inc_cur, 0, sizeof(uint32_t) * (d.n_bodies + 1), s);
+    k_inc_count<<<L.grid, L.threads, 0, s>>>(d);
+    scan_exclusive(L.prims, d.inc_cur, d.inc_off, n_bodies, &d.cnt->pad[3], d.partial, s);
+    k_inc_off_tail<<<1, 1, 0, s>>>(d);
+    cudaMemsetAsync(d.inc_cur, 0, sizeof(uint32_t) * (d.n_bodies + 1), s);
+    k_inc_fill<<<L.grid, L.threads, 0, s>>>(d);
+    launch_coop(k_colour, d, L, s);
+}
+
+void launch_build_constraints(const DW& d, const Launch& L, cudaStream_t s) {
+    k_build_constraints<<<L.grid, L.threads, 0, s>>>(d);
+}
+
+void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) { launch_coop(k_solve, d, L, s); }
+
+void launch_solve_finish(const DW& d, const Launch& L, cudaStream_t s) {
+    k_body_end<<<L.grid, L.threads, 0, s>>>(d);
+    k_sleep<<<L.grid, L.threads, 0, s>>>(d);
+}
+
+void launch_solve(const DW& d, const Launch& L, cudaStream_t s) {
+    launch_islands_colour(d, L, s);
+    launch_build_constraints(d, L, s);
+    launch_solve_sweeps(d, L, s);
+    launch_solve_finish(d, L, s);
+}
+
+}  // namespace prgpu

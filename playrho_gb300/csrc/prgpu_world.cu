@@ -1,0 +1,966 @@
+// prgpu_world.cu -- host side of the C ABI: batch creation (mass data, proxies,
+// device allocation), step orchestration with CUDA-graph replay, queries.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/prgpu.h"
+#include "prgpu_kernels.cuh"
+
+using namespace prgpu;
+
+struct prgpu_world {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DW d{};
+    Launch L{};
+    std::vector<void*> allocs;
+    cudaGraphExec_t graph = nullptr;
+    cudaGraph_t graph_def = nullptr;
+    prgpu_step_conf conf{};
+    bool conf_valid = false;
+    std::string err;
+    DConf* d_conf = nullptr;
+    float* d_stage = nullptr;
+    uint32_t* d_stage_u = nullptr;
+    Counters* h_cnt = nullptr;  // pinned mirror of the device counters
+    cudaEvent_t graph_ev[8] = {};  // recorded by the captured step between its phases
+};
+
+namespace {
+
+int fail(prgpu_world* w, int code, const char* fmt, ...) {
+    if (w) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        w->err = buf;
+    }
+    return code;
+}
+
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        const cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) return fail(w, PRGPU_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+int dalloc(prgpu_world* w, T** p, size_t n) {
+    void* q = nullptr;
+    const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    const cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    w->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return PRGPU_OK;
+}
+
+// ---- host restatement of the mass-data computation (MassData.cpp, WorldBody.cpp) ----
+struct HV {
+    float x, y;
+};
+inline HV hv(float x, float y) { return HV{x, y}; }
+inline HV operator+(HV a, HV b) { return hv(a.x + b.x, a.y + b.y); }
+inline HV operator-(HV a, HV b) { return hv(a.x - b.x, a.y - b.y); }
+inline HV hmul(HV a, float s) { return hv(a.x * s, a.y * s); }
+inline HV hdiv(HV a, float s) { const float inv = 1.0f / s; return hv(a.x * inv, a.y * inv); }
+inline float hcross(HV a, HV b) { const float m = a.x * b.y; const float s = a.y * b.x; return m - s; }
+inline float hmag2(HV a) { float r = 0.f; r += a.x * a.x; r += a.y * a.y; return r; }
+inline HV hrevperp(HV a) { return hv(-a.y, a.x); }
+inline HV hfwdperp(HV a) { return hv(a.y, -a.x); }
+inline HV hunit(HV v, HV fb) {
+    const float m2 = v.x * v.x + v.y * v.y;
+    if (std::isnormal(m2)) {
+        const float m = std::sqrt(m2);
+        const float inv = 1.0f / m;
+        return hv(v.x * inv, v.y * inv);
+    }
+    const float m = std::hypot(v.x, v.y);
+    if (!std::isnormal(m)) return fb;
+    return hv(v.x / m, v.y / m);
+}
+inline HV hrotate(HV v, HV q) { return hv((q.x * v.x) - (q.y * v.y), (q.y * v.x) + (q.x * v.y)); }
+
+void shape_mass(int nv, const HV* v, float r, float density, float& mass, HV& center, float& I) {
+    const float Pi = 3.14159265358979323846264338327950288f;
+    if (nv == 1) {
+        const float r2 = r * r;
+        const float area = r2 * Pi;
+        mass = density * area;
+        const float Iz = area * ((r2 / 2.0f) + hmag2(v[0]));
+        I = Iz * density;
+        center = v[0];
+        return;
+    }
+    if (nv == 2) {
+        const float r2 = r * r;
+        const float circle_area = r2 * Pi;
+        const float circle_mass = density * circle_area;
+        const HV v0 = v[0], v1 = v[1];
+        const HV dd = v1 - v0;
+        const HV offset = hmul(hrevperp(hunit(dd, hv(0.f, 0.f))), r);
+        const float b = std::sqrt(hmag2(dd));
+        const float h = r * 2.0f;
+        const float rect_mass = density * b * h;
+        mass = circle_mass + rect_mass;
+        center = hdiv(v0 + v1, 2.0f);
+        const float halfCircleArea = circle_area / 2.0f;
+        const float halfRSquared = r2 / 2.0f;
+        const HV q[4] = {v0 + offset, v0 - offset, v1 - offset, v1 + offset};
+        float sum_x = 0.f, sum_y = 0.f;
+        for (int i = 0; i < 4; ++i) {
+            const HV tv = q[i], nx = q[(i + 1) % 4];
+            const float fb = hcross(tv, nx);
+            sum_x += ((tv.y * tv.y) + tv.y * nx.y + (nx.y * nx.y)) * fb;
+            sum_y += ((tv.x * tv.x) + tv.x * nx.x + (nx.x * nx.x)) * fb;
+        }
+        const float Iz = (sum_x + sum_y) * (1.0f / 12.0f);
+        const float I0 = halfCircleArea * (halfRSquared + hmag2(v0));
+        const float I1 = halfCircleArea * (halfRSquared + hmag2(v1));
+        I = (I0 + I1 + Iz) * density;
+        return;
+    }
+    HV ctr = hv(0.f, 0.f);
+    float area = 0.f, II = 0.f;
+    HV s0 = hv(0.f, 0.f);
+    for (int i = 0; i < nv; ++i) s0 = s0 + v[i];
+    s0 = hdiv(s0, (float)nv);
+    for (int i = 0; i < nv; ++i) {
+        const HV e1 = v[i] - s0;
+        const HV e2 = v[(i + 1) % nv] - s0;
+        const float D = hcross(e1, e2);
+        const float triangleArea = D * (1.0f / 2.0f);
+        area += triangleArea;
+        ctr = ctr + hmul(hmul(e1 + e2, triangleArea), 1.0f / 3.0f);
+        const float intx2 = (e1.x * e1.x) + e2.x * e1.x + (e2.x * e2.x);
+        const float inty2 = (e1.y * e1.y) + e2.y * e1.y + (e2.y * e2.y);
+        II += D * (intx2 + inty2) * (1.0f / 12.0f);
+    }
+    const float m = density * area;
+    ctr = ((area > 0.f) && !(std::fabs(area) < 1.17549435e-38f)) ? hdiv(ctr, area) : hv(0.f, 0.f);
+    const HV mdc = ctr + s0;
+    const float inertialLever = hmag2(mdc) - hmag2(ctr);
+    mass = m;
+    center = mdc;
+    I = (density * II) + (m * inertialLever);
+}
+
+struct HostBody {
+    int type;
+    uint32_t flags;
+    float px, py, a;  // pos1 (centre)
+    float vx, vy, w;
+    float lcx, lcy;
+    float xpx, xpy, xc, xs;  // cached transformation
+    float invM, invI;
+};
+
+void host_set_pos(HostBody& b, float px, float py, float a) {
+    b.px = px; b.py = py; b.a = a;
+    const float c = std::cos(a), s = std::sin(a);
+    const HV p = hv(px, py) - hrotate(hv(b.lcx, b.lcy), hv(c, s));
+    b.xpx = p.x; b.xpy = p.y; b.xc = c; b.xs = s;
+}
+
+// ResetMassData -> ComputeMassData -> SetMassData over the shapes attached so far.
+void reset_mass(HostBody& b, const std::vector<int>& shapes, const prgpu_batch_desc* ds,
+                const std::vector<std::vector<HV>>& sv) {
+    float mass = 0.f, I = 0.f;
+    HV wc = hv(0.f, 0.f);
+    for (int s : shapes) {
+        if (ds->shape_density[s] > 0.f) {
+            float m, i;
+            HV c;
+            shape_mass((int)sv[s].size(), sv[s].data(), ds->shape_radius[s], ds->shape_density[s], m, c, i);
+            mass += m;
+            wc = wc + hmul(c, m);
+            I += i;
+        }
+    }
+    const HV center = (mass > 0.f) ? hdiv(wc, mass) : hv(0.f, 0.f);
+    if (b.type != PRGPU_DYNAMIC) {
+        b.invM = 0.f; b.invI = 0.f;
+        if (b.type == PRGPU_STATIC) {
+            const float lx = b.xpx, ly = b.xpy, a = b.a;
+            b.lcx = 0.f; b.lcy = 0.f;
+            host_set_pos(b, lx, ly, a);
+        }
+        return;
+    }
+    const float m = (mass > 0.f) ? mass : 1.0f;
+    b.invM = 1.0f / m;
+    b.invI = 0.f;
+    if ((I > 0.f) && !(b.flags & PRGPU_BODY_FIXED_ROTATION)) {
+        const float Ic = I - (m * hmag2(center));
+        b.invI = 1.0f / Ic;
+    }
+    const HV oldCenter = hv(b.px, b.py);
+    const HV np = hrotate(center, hv(b.xc, b.xs)) + hv(b.xpx, b.xpy);
+    b.lcx = center.x; b.lcy = center.y;
+    host_set_pos(b, np.x, np.y, b.a);
+    const HV dc = hv(b.px, b.py) - oldCenter;
+    const HV dv = hmul(hrevperp(dc), b.w);
+    b.vx = b.vx + dv.x; b.vy = b.vy + dv.y;
+}
+
+struct HostPrep {
+    uint32_t W = 0, N = 0, S = 0, J = 0, V = 0;
+    std::vector<uint32_t> body_off, shape_off, joint_off, body_world;
+    std::vector<std::vector<HV>> sv;
+    std::vector<std::vector<int>> body_shapes;
+    std::vector<HostBody> hb;
+    std::vector<float4> pos1, vel, mass, acc, xfh;
+    std::vector<float2> damp;
+    std::vector<uint32_t> bflags;
+    std::vector<uint32_t> s_meta, s_voff, s_filter, s_body, p_state;
+    std::vector<int32_t> s_group;
+    std::vector<float> s_radius;
+    std::vector<float2> s_mat;
+    std::vector<float4> vtx;
+    std::vector<uint32_t> jcnt, joff, jother, jcc, jcur;
+    std::vector<float4> j_anchor, j_param, j_zero;
+    std::vector<float> j_maxtorque;
+    std::vector<uint32_t> j_bodies, j_flags;
+};
+
+// Validation and host-side preparation of a batch: flattening, mass data
+// (Attach with resetMassData after each shape), normals, joint lists.
+int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
+    const uint32_t W = ds->n_worlds, N = ds->n_bodies, S = ds->n_shapes, J = ds->n_joints, V = ds->n_verts;
+    hp.W = W; hp.N = N; hp.S = S; hp.J = J; hp.V = V;
+    if (W == 0) return PRGPU_EINVAL;
+    // ---- validate and flatten
+    auto& body_off = hp.body_off; auto& shape_off = hp.shape_off; auto& joint_off = hp.joint_off;
+    body_off.assign(W + 1, 0); shape_off.assign(W + 1, 0); joint_off.assign(W + 1, 0);
+    for (uint32_t k = 0; k < W; ++k) {
+        body_off[k + 1] = body_off[k] + ds->world_body_count[k];
+        shape_off[k + 1] = shape_off[k] + ds->world_shape_count[k];
+        joint_off[k + 1] = joint_off[k] + (ds->world_joint_count ? ds->world_joint_count[k] : 0u);
+    }
+    if (body_off[W] != N || shape_off[W] != S || joint_off[W] != J) return PRGPU_EINVAL;
+    auto& body_world = hp.body_world; body_world.assign(N, 0);
+    for (uint32_t k = 0; k < W; ++k)
+        for (uint32_t b = body_off[k]; b < body_off[k + 1]; ++b) body_world[b] = k;
+    auto& sv = hp.sv; sv.assign(S, {});
+    auto& body_shapes = hp.body_shapes; body_shapes.assign(N, {});
+    for (uint32_t s = 0; s < S; ++s) {
+        const uint32_t b = ds->shape_body[s];
+        const uint32_t nv = ds->shape_nv[s];
+        if (b >= N || nv < 1 || nv > 16u || ds->shape_voff[s] + nv > V) return PRGPU_EINVAL;
+        const int kind = ds->shape_kind[s];
+        // A polygon whose points de-duplicate to one or two vertices stays valid
+        // (PolygonShapeConf::Set keeps what VertexSet leaves); collision dispatches
+        // on the vertex count.
+        if ((kind == PRGPU_DISK && nv != 1) || (kind == PRGPU_EDGE && nv != 2) || kind < 0 || kind > 2)
+            return PRGPU_EINVAL;
+        for (uint32_t i = 0; i < nv; ++i)
+            sv[s].push_back(hv(ds->verts[2 * (ds->shape_voff[s] + i)], ds->verts[2 * (ds->shape_voff[s] + i) + 1]));
+    }
+    for (uint32_t k = 0; k < W; ++k) {
+        for (uint32_t s = shape_off[k]; s < shape_off[k + 1]; ++s) {
+            const uint32_t b = ds->shape_body[s];
+            if (b < body_off[k] || b >= body_off[k + 1]) return PRGPU_EINVAL;
+        }
+    }
+    // ---- bodies: BodyConf -> Body, then Attach(..., resetMassData = true) per shape
+    auto& hb = hp.hb; hb.assign(N, HostBody{});
+    for (uint32_t b = 0; b < N; ++b) {
+        HostBody& x = hb[b];
+        x.type = ds->body_type[b];
+        if (x.type < 0 || x.type > 2) return PRGPU_EINVAL;
+        x.flags = ds->body_flags[b];
+        x.lcx = x.lcy = 0.f;
+        host_set_pos(x, ds->body_pos[3 * b], ds->body_pos[3 * b + 1], ds->body_pos[3 * b + 2]);
+        if (x.type == PRGPU_STATIC) { x.vx = x.vy = x.w = 0.f; }
+        else { x.vx = ds->body_vel[3 * b]; x.vy = ds->body_vel[3 * b + 1]; x.w = ds->body_vel[3 * b + 2]; }
+        x.invM = (x.type == PRGPU_DYNAMIC) ? 1.0f : 0.0f;
+        x.invI = 0.f;
+    }
+    for (uint32_t s = 0; s < S; ++s) {
+        const uint32_t b = ds->shape_body[s];
+        body_shapes[b].push_back((int)s);
+        reset_mass(hb[b], body_shapes[b], ds, sv);
+    }
+    // ---- host arrays in device layout
+    auto& pos1 = hp.pos1; auto& vel = hp.vel; auto& mass = hp.mass; auto& acc = hp.acc;
+    pos1.resize(N); vel.resize(N); mass.resize(N); acc.resize(N);
+    auto& damp = hp.damp; damp.resize(N);
+    auto& bflags = hp.bflags; bflags.resize(N);
+    for (uint32_t b = 0; b < N; ++b) {
+        const HostBody& x = hb[b];
+        pos1[b] = make_float4(x.px, x.py, x.a, 0.f);
+        vel[b] = make_float4(x.vx, x.vy, x.w, 0.f);
+        mass[b] = make_float4(x.invM, x.invI, x.lcx, x.lcy);
+        if (x.type == PRGPU_DYNAMIC) acc[b] = make_float4(ds->body_acc[3 * b], ds->body_acc[3 * b + 1], ds->body_acc[3 * b + 2], 0.f);
+        else acc[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+        damp[b] = make_float2(ds->body_damp[2 * b], ds->body_damp[2 * b + 1]);
+        uint32_t f = (uint32_t)x.type;
+        if ((x.flags & PRGPU_BODY_AWAKE) && x.type != PRGPU_STATIC) f |= BF_AWAKE;
+        if (x.flags & PRGPU_BODY_ALLOW_SLEEP) f |= BF_ALLOW_SLEEP;
+        if (x.flags & PRGPU_BODY_FIXED_ROTATION) f |= BF_FIXED_ROT;
+        if (x.flags & PRGPU_BODY_ENABLED) f |= BF_ENABLED;
+        bflags[b] = f;
+    }
+    auto& s_meta = hp.s_meta; auto& s_voff = hp.s_voff; auto& s_filter = hp.s_filter; auto& s_body = hp.s_body;
+    auto& p_state = hp.p_state;
+    s_meta.resize(S); s_voff.resize(S); s_filter.resize(S); s_body.resize(S); p_state.assign(S, 2u);
+    auto& s_group = hp.s_group; s_group.resize(S);
+    auto& s_radius = hp.s_radius; s_radius.resize(S);
+    auto& s_mat = hp.s_mat; s_mat.resize(S);
+    auto& vtx = hp.vtx; vtx.clear();
+    vtx.reserve(V);
+    for (uint32_t s = 0; s < S; ++s) {
+        const int nv = (int)sv[s].size();
+        s_meta[s] = (uint32_t)ds->shape_kind[s] | ((uint32_t)nv << 8) | (ds->shape_filter[4 * s + 3] ? (1u << 16) : 0u);
+        s_voff[s] = (uint32_t)vtx.size();
+        // GetFwdNormalsVector (d2/Math.cpp)
+        for (int i = 0; i < nv; ++i) {
+            HV n = hv(0.f, 0.f);
+            if (nv > 1) n = hunit(hfwdperp(sv[s][(i + 1) % nv] - sv[s][i]), hv(0.f, 0.f));
+            vtx.push_back(make_float4(sv[s][i].x, sv[s][i].y, n.x, n.y));
+        }
+        s_radius[s] = ds->shape_radius[s];
+        s_mat[s] = make_float2(ds->shape_friction[s], ds->shape_restitution[s]);
+        s_filter[s] = ((uint32_t)ds->shape_filter[4 * s] & 0xffffu) | (((uint32_t)ds->shape_filter[4 * s + 1] & 0xffffu) << 16);
+        s_group[s] = (int32_t)(int16_t)ds->shape_filter[4 * s + 2];
+        s_body[s] = ds->shape_body[s];
+    }
+    // body -> joint CSR for ShouldCollide
+    auto& jcnt = hp.jcnt; jcnt.assign(N + 1, 0);
+    for (uint32_t j = 0; j < J; ++j) {
+        const uint32_t a = ds->joint_bodies[2 * j], b = ds->joint_bodies[2 * j + 1];
+        if (a >= N || b >= N) return PRGPU_EINVAL;
+        jcnt[a]++;
+        if (b != a) jcnt[b]++;
+    }
+    auto& joff = hp.joff; joff.assign(N + 1, 0);
+    for (uint32_t b = 0; b < N; ++b) joff[b + 1] = joff[b] + jcnt[b];
+    auto& jother = hp.jother; auto& jcc = hp.jcc; auto& jcur = hp.jcur;
+    jother.assign(std::max<uint32_t>(joff[N], 1), 0); jcc.assign(std::max<uint32_t>(joff[N], 1), 0);
+    jcur.assign(joff.begin(), joff.end() - 1);
+    auto& j_anchor = hp.j_anchor; auto& j_param = hp.j_param; auto& j_zero = hp.j_zero;
+    j_anchor.resize(J); j_param.resize(J); j_zero.assign(J, make_float4(0.f, 0.f, 0.f, 0.f));
+    auto& j_maxtorque = hp.j_maxtorque; j_maxtorque.resize(J);
+    auto& j_bodies = hp.j_bodies; auto& j_flags = hp.j_flags; j_bodies.resize(2 * J); j_flags.resize(J);
+    for (uint32_t j = 0; j < J; ++j) {
+        const uint32_t a = ds->joint_bodies[2 * j], b = ds->joint_bodies[2 * j + 1];
+        const uint32_t cc = ds->joint_flags[3 * j + 2] ? 1u : 0u;
+        jother[jcur[a]] = b; jcc[jcur[a]++] = cc;
+        if (b != a) { jother[jcur[b]] = a; jcc[jcur[b]++] = cc; }
+        j_bodies[2 * j] = a; j_bodies[2 * j + 1] = b;
+        j_anchor[j] = make_float4(ds->joint_anchors[4 * j], ds->joint_anchors[4 * j + 1], ds->joint_anchors[4 * j + 2], ds->joint_anchors[4 * j + 3]);
+        j_param[j] = make_float4(ds->joint_params[6 * j], ds->joint_params[6 * j + 1], ds->joint_params[6 * j + 2], ds->joint_params[6 * j + 3]);
+        j_maxtorque[j] = ds->joint_params[6 * j + 4];
+        j_flags[j] = (ds->joint_flags[3 * j] ? 1u : 0u) | (ds->joint_flags[3 * j + 1] ? 2u : 0u) | (cc << 2);
+    }
+    return PRGPU_OK;
+}
+
+int bits_for(uint64_t n) {
+    int b = 1;
+    while ((1ull << b) < n) ++b;
+    return b;
+}
+
+// Phases of one step; `ev` (kPhases + 1 events) brackets them when profiling.
+constexpr int kPhases = 7;
+
+int enqueue_step(prgpu_world* w, bool solve, cudaEvent_t* ev = nullptr, bool capturing = false) {
+    const DW& d = w->d;
+    const Launch& L = w->L;
+    cudaStream_t s = w->stream;
+    // Inside a capture only external records become event nodes of the graph.
+    auto mark = [&](int k) {
+        if (!ev) return;
+        if (capturing) cudaEventRecordWithFlags(ev[k], s, cudaEventRecordExternal);
+        else cudaEventRecord(ev[k], s);
+    };
+    mark(0);
+    launch_reset_step(d, L, s);
+    // pre-phase (AabbTreeWorld.cpp:2159-2199)
+    launch_pre_proxies(d, L, s);
+    launch_destroy_contacts(d, L, s);
+    launch_update_contacts(d, L, BF_DIRTY, s);
+    launch_find_contacts(d, L, s);
+    mark(1);
+    if (solve) {
+        launch_islands_colour(d, L, s);
+        mark(2);
+        launch_build_constraints(d, L, s);
+        mark(3);
+        launch_solve_sweeps(d, L, s);
+        mark(4);
+        launch_solve_finish(d, L, s);
+        mark(5);
+        // post-solve contact maintenance (AabbTreeWorld.cpp:1532-1557)
+        launch_synchronize(d, L, s);
+        launch_update_contacts(d, L, BF_MOVED, s);
+        mark(6);
+        launch_find_contacts(d, L, s);
+    } else {
+        for (int k = 2; k <= 6; ++k) mark(k);
+    }
+    launch_clear_dirty(d, L, s);
+    mark(7);
+    return PRGPU_OK;
+}
+
+int set_conf(prgpu_world* w, const prgpu_step_conf* conf) {
+    if (!conf) return fail(w, PRGPU_EINVAL, "conf is NULL");
+    if (conf->regPositionIters < 0 || conf->regPositionIters > kMaxPosIters || conf->regVelocityIters < 0)
+        return fail(w, PRGPU_EINVAL, "iteration counts out of range (position iterations <= %d)", kMaxPosIters);
+    if (!w->conf_valid || std::memcmp(&w->conf, conf, sizeof(*conf)) != 0) {
+        static_assert(sizeof(prgpu_step_conf) == sizeof(DConf), "conf layout");
+        CU(cudaMemcpyAsync(w->d_conf, conf, sizeof(DConf), cudaMemcpyHostToDevice, w->stream));
+        w->conf = *conf;
+        w->conf_valid = true;
+    }
+    return PRGPU_OK;
+}
+
+int check_device_error(prgpu_world* w) {
+    CU(cudaMemcpyAsync(w->h_cnt, w->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (w->h_cnt->err) {
+        const uint32_t code = w->h_cnt->err;
+        return fail(w, (int)code, "device error %u at site %u", code, w->h_cnt->err_where);
+    }
+    return PRGPU_OK;
+}
+
+int run_steps(prgpu_world* w, const prgpu_step_conf* conf, int n, bool sync) {
+    int rc = set_conf(w, conf);
+    if (rc) return rc;
+    if (conf->deltaTime == 0.f) {
+        for (int i = 0; i < n; ++i) enqueue_step(w, false);
+        CU(cudaGetLastError());
+    } else {
+        if (!w->graph) {
+            for (int k = 0; k < 8; ++k)
+                if (!w->graph_ev[k]) CU(cudaEventCreate(&w->graph_ev[k]));
+            CU(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+            enqueue_step(w, true, w->graph_ev, true);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e1 = cudaStreamEndCapture(w->stream, &g);
+            if (e1 != cudaSuccess) return fail(w, PRGPU_ECUDA, "graph capture: %s", cudaGetErrorString(e1));
+            const cudaError_t e2 = cudaGraphInstantiate(&w->graph, g, 0);
+            if (e2 != cudaSuccess) return fail(w, PRGPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e2));
+            w->graph_def = g;
+        }
+        for (int i = 0; i < n; ++i) CU(cudaGraphLaunch(w->graph, w->stream));
+    }
+    if (sync) return check_device_error(w);
+    return PRGPU_OK;
+}
+
+__global__ void k_apply_states(DW d, uint32_t first, uint32_t count, const float* pos3, const float* vel3) {
+    GRID_LOOP(i, count) {
+        const uint32_t b = first + i;
+        uint32_t f = d.b_flags[b];
+        if (pos3) {
+            const float4 p = d.b_pos1[b];
+            const float x = pos3[3 * i], y = pos3[3 * i + 1], a = pos3[3 * i + 2];
+            if (x != p.x || y != p.y || a != p.z) {
+                const float4 np = make_float4(x, y, a, 0.f);
+                d.b_pos1[b] = np;
+                d.b_pos0[b] = np;
+                const float4 m = d.b_mass[b];
+                const Xf xf = get_xf(x, y, a, mk(m.z, m.w));
+                d.b_xf[b] = make_float4(xf.p.x, xf.p.y, xf.q.x, xf.q.y);
+                f |= BF_DIRTY;
+            }
+        }
+        if (vel3 && is_speedable(f)) {
+            const float4 v = d.b_vel[b];
+            const float vx = vel3[3 * i], vy = vel3[3 * i + 1], vw = vel3[3 * i + 2];
+            if (vx != v.x || vy != v.y || vw != v.z) {
+                d.b_vel[b] = make_float4(vx, vy, vw, 0.f);
+                // Body::SetVelocity (Body.cpp:182-193): a non-zero velocity wakes the body
+                if (vx != 0.f || vy != 0.f || vw != 0.f) { f |= BF_AWAKE; d.b_uat[b] = 0.f; }
+            }
+        }
+        d.b_flags[b] = f;
+    }
+}
+
+__global__ void k_gather_bodies(DW d, float* pos3, float* vel3, float* xf4, float* mass4, float* uat, uint32_t* flags) {
+    GRID_LOOP(b, d.n_bodies) {
+        const float4 p = d.b_pos1[b], v = d.b_vel[b], x = d.b_xf[b], m = d.b_mass[b];
+        if (pos3) { pos3[3 * b] = p.x; pos3[3 * b + 1] = p.y; pos3[3 * b + 2] = p.z; }
+        if (vel3) { vel3[3 * b] = v.x; vel3[3 * b + 1] = v.y; vel3[3 * b + 2] = v.z; }
+        if (xf4) reinterpret_cast<float4*>(xf4)[b] = x;
+        if (mass4) reinterpret_cast<float4*>(mass4)[b] = m;
+        if (uat) uat[b] = d.b_uat[b];
+        if (flags) flags[b] = (d.b_flags[b] & BF_AWAKE) ? 1u : 0u;
+    }
+}
+
+__global__ void k_gather_contacts(DW d, uint32_t n, uint32_t* proxies2, uint32_t* bodies2, uint32_t* flags,
+                                  int32_t* meta2, float* head4, float* pts8, uint32_t* feat2) {
+    GRID_LOOP(i, n) {
+        const uint32_t slot = d.c_slot[i];
+        const uint2 pr = d.cs_proxy[slot], bd = d.cs_body[slot];
+        if (proxies2) { proxies2[2 * i] = pr.x; proxies2[2 * i + 1] = pr.y; }
+        if (bodies2) { bodies2[2 * i] = bd.x; bodies2[2 * i + 1] = bd.y; }
+        if (flags) flags[i] = ((d.cs_flags[slot] & CF_TOUCHING) ? 1u : 0u) | ((d.cs_flags[slot] & CF_SENSOR) ? 2u : 0u);
+        if (meta2) { const uint32_t m = d.m_meta[slot]; meta2[2 * i] = (int32_t)(m & 0xfu); meta2[2 * i + 1] = (int32_t)((m >> 4) & 0xfu); }
+        if (head4) reinterpret_cast<float4*>(head4)[i] = d.m_head[slot];
+        if (pts8) { reinterpret_cast<float4*>(pts8)[2 * i] = d.m_p0[slot]; reinterpret_cast<float4*>(pts8)[2 * i + 1] = d.m_p1[slot]; }
+        if (feat2) { const uint2 c = d.m_cf[slot]; feat2[2 * i] = c.x; feat2[2 * i + 1] = c.y; }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int prgpu_abi_version(void) { return PRGPU_ABI_VERSION; }
+
+int prgpu_default_step_conf(prgpu_step_conf* c) {
+    if (!c) return PRGPU_EINVAL;
+    // StepConf defaults (StepConf.hpp:59-161, Settings.hpp) in float arithmetic.
+    const float Pi = 3.14159265358979323846264338327950288f;
+    const float linearSlop = 0.005f;
+    std::memset(c, 0, sizeof(*c));
+    c->deltaTime = 1.0f / 60.0f;
+    c->dtRatio = 1.0f;
+    c->minStillTimeToSleep = 1.0f / 2.0f;
+    c->linearSlop = linearSlop;
+    c->angularSlop = (Pi * 2.0f) / 180.0f;
+    c->regResolutionRate = 2.0f / 10.0f;
+    c->regMinSeparation = -linearSlop * 3.0f;
+    c->regMinMomentum = 0.0f / 100.0f;
+    c->velocityThreshold = 1.0f;
+    c->maxTranslation = 2.0f;
+    c->maxRotation = 179.0f * ((1.0f * Pi) / 180.0f);
+    c->maxLinearCorrection = 0.2f;
+    c->maxAngularCorrection = (8.0f / 180.0f) * Pi;
+    c->linearSleepTolerance = 0.01f;
+    c->angularSleepTolerance = (Pi * 2.0f) / 180.0f;
+    c->displaceMultiplier = 2.0f;
+    c->aabbExtension = linearSlop * 20.0f;
+    c->maxCirclesRatio = 10.0f;
+    c->regVelocityIters = 8;
+    c->regPositionIters = 3;
+    c->doWarmStart = 1;
+    c->doBlocksolve = 1;
+    return PRGPU_OK;
+}
+
+int prgpu_convex_hull(const float* xy, int n, float linear_slop, float* out_xy) {
+    if (!xy || !out_xy || n < 0) return -1;
+    const float min_sep2 = linear_slop * linear_slop;
+    std::vector<HV> pts;
+    for (int i = 0; i < n; ++i) {
+        const HV p = hv(xy[2 * i], xy[2 * i + 1]);
+        bool dup = false;
+        for (const HV& q : pts) {
+            if (hmag2(p - q) <= min_sep2) { dup = true; break; }
+        }
+        if (!dup) pts.push_back(p);
+    }
+    const int m = (int)pts.size();
+    if (m == 0) return 0;
+    int i0 = 0;
+    float max_x = pts[0].x;
+    for (int i = 1; i < m; ++i) {
+        const float x = pts[i].x;
+        if ((max_x < x) || ((max_x == x) && (pts[i].y < pts[i0].y))) { max_x = x; i0 = i; }
+    }
+    std::vector<int> hull;
+    int ih = i0;
+    for (int guard = 0; guard <= m; ++guard) {
+        hull.push_back(ih);
+        int ie = 0;
+        for (int j = 1; j < m; ++j) {
+            if (ie == ih) { ie = j; continue; }
+            const HV r = pts[ie] - pts[ih];
+            const HV v = pts[j] - pts[ih];
+            const float c = hcross(r, v);
+            if ((c < 0.f) || ((c == 0.f) && (hmag2(v) > hmag2(r)))) ie = j;
+        }
+        ih = ie;
+        if (ie == i0) break;
+    }
+    for (size_t k = 0; k < hull.size(); ++k) { out_xy[2 * k] = pts[hull[k]].x; out_xy[2 * k + 1] = pts[hull[k]].y; }
+    return (int)hull.size();
+}
+
+int prgpu_prepare_bodies(const prgpu_batch_desc* ds, float* pos3, float* vel3, float* mass4) {
+    if (!ds) return PRGPU_EINVAL;
+    HostPrep hp;
+    const int rc = prepare_host(ds, hp);
+    if (rc) return rc;
+    for (uint32_t b = 0; b < hp.N; ++b) {
+        if (pos3) { pos3[3 * b] = hp.pos1[b].x; pos3[3 * b + 1] = hp.pos1[b].y; pos3[3 * b + 2] = hp.pos1[b].z; }
+        if (vel3) { vel3[3 * b] = hp.vel[b].x; vel3[3 * b + 1] = hp.vel[b].y; vel3[3 * b + 2] = hp.vel[b].z; }
+        if (mass4) { mass4[4 * b] = hp.mass[b].x; mass4[4 * b + 1] = hp.mass[b].y; mass4[4 * b + 2] = hp.mass[b].z; mass4[4 * b + 3] = hp.mass[b].w; }
+    }
+    return PRGPU_OK;
+}
+
+int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out) {
+    if (!ds || !out) return PRGPU_EINVAL;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return PRGPU_ENOTREADY;
+    prgpu_world* w = new prgpu_world();
+    w->device = device;
+    auto bail = [&](int rc) { prgpu_world_destroy(w); return rc; };
+    if (cudaSetDevice(device) != cudaSuccess) return bail(PRGPU_ECUDA);
+    HostPrep hp;
+    {
+        const int prc = prepare_host(ds, hp);
+        if (prc) return bail(fail(w, prc, "invalid batch description"));
+    }
+    const uint32_t W = hp.W, N = hp.N, S = hp.S, J = hp.J;
+    auto& body_off = hp.body_off; auto& shape_off = hp.shape_off; auto& body_world = hp.body_world;
+    auto& pos1 = hp.pos1; auto& vel = hp.vel; auto& mass = hp.mass; auto& acc = hp.acc; auto& damp = hp.damp;
+    auto& bflags = hp.bflags; auto& s_meta = hp.s_meta; auto& s_voff = hp.s_voff; auto& s_filter = hp.s_filter;
+    auto& s_body = hp.s_body; auto& p_state = hp.p_state; auto& s_group = hp.s_group; auto& s_radius = hp.s_radius;
+    auto& s_mat = hp.s_mat; auto& vtx = hp.vtx; auto& joff = hp.joff; auto& jother = hp.jother; auto& jcc = hp.jcc;
+    auto& j_anchor = hp.j_anchor; auto& j_param = hp.j_param; auto& j_zero = hp.j_zero; auto& j_maxtorque = hp.j_maxtorque;
+    auto& j_bodies = hp.j_bodies; auto& j_flags = hp.j_flags;
+    // ---- capacities
+    const uint64_t ccap = ds->contact_capacity ? ds->contact_capacity : (uint64_t)8 * S + 4096;
+    const uint64_t kcap = ds->candidate_capacity ? ds->candidate_capacity : (uint64_t)8 * S + 4096;
+    if (ccap > 0x7fffffffull || kcap > 0x7fffffffull) return bail(PRGPU_ECAPACITY);
+    const uint32_t C = (uint32_t)ccap, K = (uint32_t)kcap;
+    const uint32_t items = std::max<uint32_t>(std::max<uint32_t>(C + J, N + 1), S) + 1;
+    DW& d = w->d;
+    d.n_worlds = W; d.n_bodies = N; d.n_shapes = S; d.n_joints = J; d.n_verts = (uint32_t)vtx.size();
+    d.contact_cap = C; d.cand_cap = K;
+    d.key_bits = (uint32_t)bits_for((uint64_t)S + 1);
+    if (2 * d.key_bits > 64) return bail(PRGPU_ECAPACITY);
+    d.world_bits = (uint32_t)bits_for((uint64_t)W + 1);
+    if (30 + d.world_bits > 64) return bail(PRGPU_ECAPACITY);
+    int rc = 0;
+#define AL(ptr, n) do { rc = dalloc(w, &(ptr), (size_t)(n)); if (rc) return bail(rc); } while (0)
+    uint32_t *w_body_off, *w_shape_off;
+    AL(w_body_off, W + 1); AL(w_shape_off, W + 1);
+    d.w_body_off = w_body_off; d.w_shape_off = w_shape_off;
+    AL(d.w_root, W); AL(d.w_bounds, W);
+    AL(d.b_pos1, N); AL(d.b_pos0, N); AL(d.b_vel, N); AL(d.b_xf, N); AL(d.b_mass, N); AL(d.b_acc, N);
+    AL(d.b_damp, N); AL(d.b_flags, N); AL(d.b_uat, N); AL(d.b_world, N); AL(d.b_island, N);
+    AL(d.b_jnt_off, N + 1); AL(d.b_jnt_other, jother.size()); AL(d.b_jnt_cc, jcc.size());
+    AL(d.isl_awake, N); AL(d.isl_sep, (size_t)N * kMaxPosIters); AL(d.isl_jok, (size_t)N * kMaxPosIters); AL(d.isl_uat, N);
+    AL(d.s_body, S); AL(d.s_meta, S); AL(d.s_voff, S); AL(d.s_radius, S); AL(d.s_mat, S); AL(d.s_filter, S);
+    AL(d.s_group, S); AL(d.verts, vtx.size()); AL(d.p_aabb, S); AL(d.p_moved, S); AL(d.moved_list, S);
+    AL(d.j_bodies, 2 * J); AL(d.j_anchor, J); AL(d.j_param, J); AL(d.j_maxtorque, J); AL(d.j_flags, J);
+    AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_imp, J);
+    AL(d.c_key, C); AL(d.c_slot, C); AL(d.c_key_alt, C); AL(d.c_slot_alt, C); AL(d.free_stack, C);
+    AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C);
+    AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
+    AL(d.n_key, K); AL(d.n_key_alt, K); AL(d.n_val, K); AL(d.n_val_alt, K);
+    AL(d.l_key, S); AL(d.l_key_alt, S); AL(d.l_idx, S); AL(d.l_idx_alt, S); AL(d.l_leaf_box, S);
+    AL(d.l_node_box, S); AL(d.l_left, S); AL(d.l_right, S); AL(d.l_parent, 2 * (size_t)S); AL(d.l_range, 2 * (size_t)S);
+    AL(d.l_visit, S);
+    AL(d.k_list, C + J); AL(d.k_colour, C + J); AL(d.k_tent, C + J); AL(d.k_order, C + J);
+    AL(d.k_prio, C + J);
+    AL(d.inc_off, N + 1); AL(d.inc_cur, N + 1); AL(d.inc_list, 2 * ((size_t)C + J));
+    AL(d.vc, C); AL(d.pc, C);
+    AL(d.flags, items); AL(d.scan, items);
+    w->L.prims.sm_count = 1;
+    {
+        cudaDeviceProp prop;
+        if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return bail(PRGPU_ECUDA);
+        w->L.prims.sm_count = prop.multiProcessorCount;
+    }
+    w->L.prims.grid = std::min(1024, 2 * w->L.prims.sm_count);
+    AL(d.partial, 1024); AL(d.hist, 256 * 1024);
+    Counters* cnt;
+    AL(cnt, 1);
+    d.cnt = cnt;
+    AL(w->d_conf, 1);
+    d.conf = w->d_conf;
+    AL(w->d_stage, (size_t)N * 8 + 16);
+    if (cudaMallocHost(&w->h_cnt, sizeof(Counters)) != cudaSuccess) return bail(PRGPU_ECUDA);
+    w->L.threads = 256;
+    w->L.grid = w->L.prims.sm_count * 8;
+    w->L.coop_threads = 256;
+    const int per_sm = coop_blocks_per_sm(w->L.coop_threads);
+    if (per_sm < 1) return bail(fail(w, PRGPU_ECUDA, "cooperative kernels cannot be resident"));
+    w->L.coop_grid = w->L.prims.sm_count * std::min(per_sm, 4);
+    if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(PRGPU_ECUDA);
+    // ---- uploads
+    auto up = [&](void* dst, const void* src, size_t bytes) -> bool {
+        return bytes == 0 || cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, w->stream) == cudaSuccess;
+    };
+    bool ok = true;
+    ok &= up(w_body_off, body_off.data(), sizeof(uint32_t) * (W + 1));
+    ok &= up(w_shape_off, shape_off.data(), sizeof(uint32_t) * (W + 1));
+    ok &= up(d.b_pos1, pos1.data(), sizeof(float4) * N);
+    ok &= up(d.b_vel, vel.data(), sizeof(float4) * N);
+    ok &= up(d.b_mass, mass.data(), sizeof(float4) * N);
+    ok &= up(d.b_acc, acc.data(), sizeof(float4) * N);
+    ok &= up(d.b_damp, damp.data(), sizeof(float2) * N);
+    ok &= up(d.b_flags, bflags.data(), sizeof(uint32_t) * N);
+    ok &= up(d.b_world, body_world.data(), sizeof(uint32_t) * N);
+    ok &= up(d.b_jnt_off, joff.data(), sizeof(uint32_t) * (N + 1));
+    ok &= up(d.b_jnt_other, jother.data(), sizeof(uint32_t) * jother.size());
+    ok &= up(d.b_jnt_cc, jcc.data(), sizeof(uint32_t) * jcc.size());
+    ok &= up(d.s_body, s_body.data(), sizeof(uint32_t) * S);
+    ok &= up(d.s_meta, s_meta.data(), sizeof(uint32_t) * S);
+    ok &= up(d.s_voff, s_voff.data(), sizeof(uint32_t) * S);
+    ok &= up(d.s_radius, s_radius.data(), sizeof(float) * S);
+    ok &= up(d.s_mat, s_mat.data(), sizeof(float2) * S);
+    ok &= up(d.s_filter, s_filter.data(), sizeof(uint32_t) * S);
+    ok &= up(d.s_group, s_group.data(), sizeof(int32_t) * S);
+    ok &= up(d.verts, vtx.data(), sizeof(float4) * vtx.size());
+    ok &= up(d.p_moved, p_state.data(), sizeof(uint32_t) * S);
+    ok &= up(d.j_bodies, j_bodies.data(), sizeof(uint32_t) * 2 * J);
+    ok &= up(d.j_anchor, j_anchor.data(), sizeof(float4) * J);
+    ok &= up(d.j_param, j_param.data(), sizeof(float4) * J);
+    ok &= up(d.j_maxtorque, j_maxtorque.data(), sizeof(float) * J);
+    ok &= up(d.j_flags, j_flags.data(), sizeof(uint32_t) * J);
+    ok &= up(d.j_imp, j_zero.data(), sizeof(float4) * J);
+    ok &= up(d.j_m1, j_zero.data(), sizeof(float4) * J);
+    ok &= cudaMemsetAsync(d.b_uat, 0, sizeof(float) * N, w->stream) == cudaSuccess;
+    ok &= cudaMemsetAsync(d.cnt, 0, sizeof(Counters), w->stream) == cudaSuccess;
+    if (!ok) return bail(fail(w, PRGPU_ECUDA, "upload failed"));
+    launch_init_bodies(d, w->L, w->stream);
+    if (cudaStreamSynchronize(w->stream) != cudaSuccess) return bail(PRGPU_ECUDA);
+    if (cudaGetLastError() != cudaSuccess) return bail(PRGPU_ECUDA);
+#undef AL
+    *out = w;
+    return PRGPU_OK;
+}
+
+int prgpu_world_destroy(prgpu_world* w) {
+    if (!w) return PRGPU_OK;
+    cudaSetDevice(w->device);
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    if (w->graph) cudaGraphExecDestroy(w->graph);
+    for (int k = 0; k < 8; ++k)
+        if (w->graph_ev[k]) cudaEventDestroy(w->graph_ev[k]);
+    if (w->graph_def) cudaGraphDestroy(w->graph_def);
+    for (void* p : w->allocs) cudaFree(p);
+    if (w->h_cnt) cudaFreeHost(w->h_cnt);
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+    return PRGPU_OK;
+}
+
+int prgpu_step(prgpu_world* w, const prgpu_step_conf* conf, prgpu_step_stats* st) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    const int rc = run_steps(w, conf, 1, true);
+    if (rc) return rc;
+    if (st) {
+        const Counters& c = *w->h_cnt;
+        st->contactsAdded = c.st_contacts_added;
+        st->contactsDestroyed = c.st_contacts_destroyed;
+        st->contactsUpdated = c.st_contacts_updated;
+        st->islandsFound = c.st_islands_found;
+        st->islandsSolved = c.st_islands_solved;
+        st->bodiesSlept = c.st_bodies_slept;
+        st->proxiesMoved = c.st_proxies_moved;
+        st->sumPosIters = c.st_sum_pos_iters;
+        st->liveContacts = c.n_live;
+        st->activeConstraints = c.n_active;
+        st->colours = c.n_colours;
+        st->serialConstraints = c.colour_off[kSerialColour + 1] - c.colour_off[kSerialColour];
+        st->minSeparation = c.st_min_separation;
+        st->maxIncImpulse = c.st_max_inc_impulse;
+    }
+    return PRGPU_OK;
+}
+
+int prgpu_step_n(prgpu_world* w, const prgpu_step_conf* conf, int n) {
+    if (!w || n < 0) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    return run_steps(w, conf, n, true);
+}
+
+int prgpu_step_profiled(prgpu_world* w, const prgpu_step_conf* conf, float* phase_ms, int n_phases,
+                        prgpu_step_stats* st) {
+    if (!w || !conf) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    int rc = set_conf(w, conf);
+    if (rc) return rc;
+    cudaEvent_t ev[kPhases + 1];
+    for (int k = 0; k <= kPhases; ++k) CU(cudaEventCreate(&ev[k]));
+    enqueue_step(w, conf->deltaTime != 0.f, ev);
+    CU(cudaGetLastError());
+    rc = check_device_error(w);
+    if (!rc && phase_ms) {
+        for (int k = 0; k < n_phases && k < kPhases; ++k) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            phase_ms[k] = ms;
+        }
+    }
+    for (int k = 0; k <= kPhases; ++k) cudaEventDestroy(ev[k]);
+    if (!rc && st) {
+        const Counters& c = *w->h_cnt;
+        st->contactsAdded = c.st_contacts_added; st->contactsDestroyed = c.st_contacts_destroyed;
+        st->contactsUpdated = c.st_contacts_updated; st->islandsFound = c.st_islands_found;
+        st->islandsSolved = c.st_islands_solved; st->bodiesSlept = c.st_bodies_slept;
+        st->proxiesMoved = c.st_proxies_moved; st->sumPosIters = c.st_sum_pos_iters;
+        st->liveContacts = c.n_live; st->activeConstraints = c.n_active; st->colours = c.n_colours;
+        st->serialConstraints = c.colour_off[kSerialColour + 1] - c.colour_off[kSerialColour];
+        st->minSeparation = c.st_min_separation; st->maxIncImpulse = c.st_max_inc_impulse;
+    }
+    return rc;
+}
+
+int prgpu_graph_kernel_count(prgpu_world* w, uint32_t* n_kernels) {
+    if (!w || !n_kernels) return PRGPU_EINVAL;
+    if (!w->graph_def) return fail(w, PRGPU_ESTATE, "no captured step yet");
+    size_t n = 0;
+    CU(cudaGraphGetNodes(w->graph_def, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    CU(cudaGraphGetNodes(w->graph_def, nodes.data(), &n));
+    uint32_t k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType t;
+        CU(cudaGraphNodeGetType(nodes[i], &t));
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    *n_kernels = k;
+    return PRGPU_OK;
+}
+
+int prgpu_last_step_phase_ms(prgpu_world* w, float* phase_ms, int n_phases) {
+    if (!w || !phase_ms) return PRGPU_EINVAL;
+    if (!w->graph) return fail(w, PRGPU_ESTATE, "no captured step has run yet");
+    CU(cudaSetDevice(w->device));
+    CU(cudaStreamSynchronize(w->stream));
+    for (int k = 0; k < n_phases && k < kPhases + 1; ++k) {
+        float ms = 0.f;
+        // phase k of the last replay; index kPhases gives the whole step
+        const int a = (k < kPhases) ? k : 0, b = (k < kPhases) ? k + 1 : kPhases;
+        CU(cudaEventElapsedTime(&ms, w->graph_ev[a], w->graph_ev[b]));
+        phase_ms[k] = ms;
+    }
+    return PRGPU_OK;
+}
+
+int prgpu_step_async(prgpu_world* w, const prgpu_step_conf* conf, int n) {
+    if (!w || n < 0) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    return run_steps(w, conf, n, false);
+}
+
+int prgpu_synchronize(prgpu_world* w) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    return check_device_error(w);
+}
+
+int prgpu_get_counts(prgpu_world* w, uint32_t* nw, uint32_t* nb, uint32_t* ns, uint32_t* nj, uint32_t* nc) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    if (nc) {
+        CU(cudaMemcpyAsync(w->h_cnt, w->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        *nc = w->h_cnt->n_live;
+    }
+    if (nw) *nw = w->d.n_worlds;
+    if (nb) *nb = w->d.n_bodies;
+    if (ns) *ns = w->d.n_shapes;
+    if (nj) *nj = w->d.n_joints;
+    return PRGPU_OK;
+}
+
+int prgpu_download_bodies(prgpu_world* w, float* pos3, float* vel3, float* xf4, float* mass4, float* uat,
+                          uint32_t* flags) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    const uint32_t N = w->d.n_bodies;
+    float* base = w->d_stage;
+    float* dpos = pos3 ? base : nullptr;
+    float* dvel = vel3 ? base + (size_t)3 * N : nullptr;
+    std::vector<float> tmp;
+    k_gather_bodies<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, dpos, dvel, nullptr, nullptr, nullptr, nullptr);
+    CU(cudaGetLastError());
+    if (pos3) CU(cudaMemcpyAsync(pos3, dpos, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, w->stream));
+    if (vel3) CU(cudaMemcpyAsync(vel3, dvel, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, w->stream));
+    if (xf4) CU(cudaMemcpyAsync(xf4, w->d.b_xf, sizeof(float4) * N, cudaMemcpyDeviceToHost, w->stream));
+    if (mass4) CU(cudaMemcpyAsync(mass4, w->d.b_mass, sizeof(float4) * N, cudaMemcpyDeviceToHost, w->stream));
+    if (uat) CU(cudaMemcpyAsync(uat, w->d.b_uat, sizeof(float) * N, cudaMemcpyDeviceToHost, w->stream));
+    if (flags) {
+        std::vector<uint32_t> f(N);
+        CU(cudaMemcpyAsync(f.data(), w->d.b_flags, sizeof(uint32_t) * N, cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        for (uint32_t b = 0; b < N; ++b) flags[b] = (f[b] & BF_AWAKE) ? 1u : 0u;
+    }
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_upload_body_states(prgpu_world* w, uint32_t first, uint32_t count, const float* pos3, const float* vel3) {
+    if (!w) return PRGPU_EINVAL;
+    if ((uint64_t)first + count > w->d.n_bodies) return fail(w, PRGPU_EINVAL, "body range out of bounds");
+    CU(cudaSetDevice(w->device));
+    float* dpos = pos3 ? w->d_stage : nullptr;
+    float* dvel = vel3 ? w->d_stage + (size_t)3 * w->d.n_bodies : nullptr;
+    if (pos3) CU(cudaMemcpyAsync(dpos, pos3, sizeof(float) * 3 * count, cudaMemcpyHostToDevice, w->stream));
+    if (vel3) CU(cudaMemcpyAsync(dvel, vel3, sizeof(float) * 3 * count, cudaMemcpyHostToDevice, w->stream));
+    k_apply_states<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, first, count, dpos, dvel);
+    CU(cudaGetLastError());
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
+                            uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
+                            uint32_t* features2) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    CU(cudaMemcpyAsync(w->h_cnt, w->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    const uint32_t n = w->h_cnt->n_live;
+    if (n_out) *n_out = n;
+    if (n > capacity) return fail(w, PRGPU_ECAPACITY, "%u contacts exceed capacity %u", n, capacity);
+    if (n == 0) return PRGPU_OK;
+    // gather into one device scratch block, then copy out
+    const size_t per = 2 + 2 + 1 + 2 + 4 + 8 + 2;  // 32-bit words per contact
+    void* scratch = nullptr;
+    CU(cudaMallocAsync(&scratch, per * 4 * (size_t)n, w->stream));
+    // 16-byte records first so every float4 store is aligned
+    float* g_hd = static_cast<float*>(scratch);
+    float* g_pt = g_hd + 4 * (size_t)n;
+    uint32_t* g_pr = reinterpret_cast<uint32_t*>(g_pt + 8 * (size_t)n);
+    uint32_t* g_bd = g_pr + 2 * (size_t)n;
+    uint32_t* g_fl = g_bd + 2 * (size_t)n;
+    int32_t* g_me = reinterpret_cast<int32_t*>(g_fl + n);
+    uint32_t* g_ft = reinterpret_cast<uint32_t*>(g_me + 2 * (size_t)n);
+    k_gather_contacts<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, n, g_pr, g_bd, g_fl, g_me, g_hd, g_pt, g_ft);
+    if (proxies2) CU(cudaMemcpyAsync(proxies2, g_pr, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (bodies2) CU(cudaMemcpyAsync(bodies2, g_bd, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (flags) CU(cudaMemcpyAsync(flags, g_fl, 4 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (meta2) CU(cudaMemcpyAsync(meta2, g_me, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (head4) CU(cudaMemcpyAsync(head4, g_hd, 16 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (pts8) CU(cudaMemcpyAsync(pts8, g_pt, 32 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (features2) CU(cudaMemcpyAsync(features2, g_ft, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaFreeAsync(scratch, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_download_proxies(prgpu_world* w, float* aabb4) {
+    if (!w || !aabb4) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    CU(cudaMemcpyAsync(aabb4, w->d.p_aabb, sizeof(float4) * w->d.n_shapes, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_last_error(prgpu_world* w, char* buf, int len) {
+    if (!buf || len <= 0) return PRGPU_EINVAL;
+    const std::string& e = w ? w->err : std::string();
+    std::snprintf(buf, (size_t)len, "%s", e.c_str());
+    return PRGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,335 @@
+"""ctypes binding of the C ABI in include/prgpu.h (libprgpu.so, built in-tree).
+
+``GpuBatch`` mirrors the reference's World usage for this path: a batch is
+created from scenes (CreateBody/CreateShape/Attach/CreateJoint), advanced with
+``step`` (Step(World&, StepConf)) and read back with ``bodies`` / ``contacts`` /
+``proxies`` (GetBody, GetContacts + GetManifold, GetTree).  There is no CPU
+fallback: without the library or a GPU every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import List, Sequence
+
+import numpy as np
+
+from .scenes import Scene
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libprgpu.so")
+
+STATUS = {0: "OK", 1: "EINVAL", 2: "ECUDA", 3: "ECAPACITY", 4: "ETIMEOUT", 5: "ENOTREADY", 6: "ESTATE"}
+
+CONF_FLOATS = (
+    "deltaTime", "dtRatio", "minStillTimeToSleep", "linearSlop", "angularSlop",
+    "regResolutionRate", "regMinSeparation", "regMinMomentum", "velocityThreshold",
+    "maxTranslation", "maxRotation", "maxLinearCorrection", "maxAngularCorrection",
+    "linearSleepTolerance", "angularSleepTolerance", "displaceMultiplier", "aabbExtension",
+    "maxCirclesRatio")
+CONF_INTS = ("regVelocityIters", "regPositionIters", "doWarmStart", "doBlocksolve")
+
+
+class StepConf(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in CONF_FLOATS] + [(n, ctypes.c_int32) for n in CONF_INTS]
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in (
+        "contactsAdded", "contactsDestroyed", "contactsUpdated", "islandsFound", "islandsSolved",
+        "bodiesSlept", "proxiesMoved", "sumPosIters", "liveContacts", "activeConstraints", "colours",
+        "serialConstraints")] + [("minSeparation", ctypes.c_float), ("maxIncImpulse", ctypes.c_float)]
+
+
+class BatchDesc(ctypes.Structure):
+    P = ctypes.c_void_p
+    _fields_ = [
+        ("n_worlds", ctypes.c_uint32), ("world_body_count", P), ("world_shape_count", P),
+        ("world_joint_count", P), ("n_bodies", ctypes.c_uint32), ("body_type", P), ("body_pos", P),
+        ("body_vel", P), ("body_acc", P), ("body_damp", P), ("body_flags", P),
+        ("n_shapes", ctypes.c_uint32), ("shape_body", P), ("shape_kind", P), ("shape_voff", P),
+        ("shape_nv", P), ("shape_radius", P), ("shape_density", P), ("shape_friction", P),
+        ("shape_restitution", P), ("shape_filter", P), ("n_verts", ctypes.c_uint32), ("verts", P),
+        ("n_joints", ctypes.c_uint32), ("joint_bodies", P), ("joint_anchors", P), ("joint_params", P),
+        ("joint_flags", P), ("contact_capacity", ctypes.c_uint32), ("candidate_capacity", ctypes.c_uint32)]
+
+
+class PrgpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"prgpu {STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_LIB = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libprgpu.so; raises if it has not been built (no silent fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise PrgpuError(5, f"{path} is missing: build it with playrho_gb300/build.py")
+    lib = ctypes.CDLL(path)
+    P, U, I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
+    lib.prgpu_abi_version.restype = I
+    lib.prgpu_default_step_conf.argtypes = [ctypes.POINTER(StepConf)]
+    lib.prgpu_world_create.argtypes = [ctypes.POINTER(BatchDesc), I, ctypes.POINTER(P)]
+    lib.prgpu_world_destroy.argtypes = [P]
+    lib.prgpu_step.argtypes = [P, ctypes.POINTER(StepConf), ctypes.POINTER(StepStats)]
+    lib.prgpu_step_n.argtypes = [P, ctypes.POINTER(StepConf), I]
+    lib.prgpu_step_async.argtypes = [P, ctypes.POINTER(StepConf), I]
+    lib.prgpu_synchronize.argtypes = [P]
+    lib.prgpu_get_counts.argtypes = [P, P, P, P, P, P]
+    lib.prgpu_download_bodies.argtypes = [P, P, P, P, P, P, P]
+    lib.prgpu_upload_body_states.argtypes = [P, U, U, P, P]
+    lib.prgpu_download_contacts.argtypes = [P, U, P, P, P, P, P, P, P, P]
+    lib.prgpu_download_proxies.argtypes = [P, P]
+    lib.prgpu_last_error.argtypes = [P, ctypes.c_char_p, I]
+    lib.prgpu_convex_hull.argtypes = [P, I, ctypes.c_float, P]
+    lib.prgpu_convex_hull.restype = I
+    lib.prgpu_prepare_bodies.argtypes = [ctypes.POINTER(BatchDesc), P, P, P]
+    lib.prgpu_step_profiled.argtypes = [P, ctypes.POINTER(StepConf), P, I, ctypes.POINTER(StepStats)]
+    lib.prgpu_last_step_phase_ms.argtypes = [P, P, I]
+    lib.prgpu_graph_kernel_count.argtypes = [P, P]
+    _LIB = lib
+    return lib
+
+
+def exported_symbols() -> List[str]:
+    return [
+        "prgpu_abi_version", "prgpu_default_step_conf", "prgpu_world_create", "prgpu_world_destroy",
+        "prgpu_step", "prgpu_step_n", "prgpu_step_async", "prgpu_synchronize", "prgpu_get_counts",
+        "prgpu_download_bodies", "prgpu_upload_body_states", "prgpu_download_contacts",
+        "prgpu_download_proxies", "prgpu_last_error", "prgpu_convex_hull", "prgpu_prepare_bodies", "prgpu_step_profiled",
+        "prgpu_last_step_phase_ms", "prgpu_graph_kernel_count"]
+
+
+def default_conf(**overrides) -> StepConf:
+    lib = load_library()
+    c = StepConf()
+    lib.prgpu_default_step_conf(ctypes.byref(c))
+    for k, v in overrides.items():
+        setattr(c, k, v)
+    return c
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
+
+
+def flatten(scenes: Sequence[Scene]) -> dict:
+    """World-major concatenation of scenes with global body indices."""
+    body_base = np.cumsum([0] + [s.n_bodies for s in scenes])
+    vert_base = np.cumsum([0] + [s.verts.shape[0] for s in scenes])
+    cat = lambda f, dt: np.ascontiguousarray(np.concatenate([f(s) for s in scenes]).astype(dt))
+    out = {
+        "world_body_count": np.array([s.n_bodies for s in scenes], dtype=np.uint32),
+        "world_shape_count": np.array([s.n_shapes for s in scenes], dtype=np.uint32),
+        "world_joint_count": np.array([s.n_joints for s in scenes], dtype=np.uint32),
+        "body_type": cat(lambda s: s.body_type, np.int32),
+        "body_pos": cat(lambda s: s.body_pos, np.float32),
+        "body_vel": cat(lambda s: s.body_vel, np.float32),
+        "body_acc": cat(lambda s: s.body_acc, np.float32),
+        "body_damp": cat(lambda s: s.body_damp, np.float32),
+        "body_flags": cat(lambda s: s.body_flags, np.uint32),
+        "shape_body": np.ascontiguousarray(np.concatenate(
+            [s.shape_body + body_base[i] for i, s in enumerate(scenes)]).astype(np.uint32)),
+        "shape_kind": cat(lambda s: s.shape_kind, np.int32),
+        "shape_voff": np.ascontiguousarray(np.concatenate(
+            [s.shape_voff + vert_base[i] for i, s in enumerate(scenes)]).astype(np.uint32)),
+        "shape_nv": cat(lambda s: s.shape_nv, np.uint32),
+        "shape_radius": cat(lambda s: s.shape_radius, np.float32),
+        "shape_density": cat(lambda s: s.shape_density, np.float32),
+        "shape_friction": cat(lambda s: s.shape_friction, np.float32),
+        "shape_restitution": cat(lambda s: s.shape_restitution, np.float32),
+        "shape_filter": cat(lambda s: s.shape_filter, np.int32),
+        "verts": cat(lambda s: s.verts, np.float32),
+        "joint_bodies": np.ascontiguousarray(np.concatenate(
+            [s.joint_bodies.reshape(-1, 2) + body_base[i] for i, s in enumerate(scenes)]).astype(np.uint32)),
+        "joint_anchors": cat(lambda s: s.joint_anchors.reshape(-1, 4), np.float32),
+        "joint_params": cat(lambda s: s.joint_params.reshape(-1, 6), np.float32),
+        "joint_flags": cat(lambda s: s.joint_flags.reshape(-1, 3), np.int32),
+        "body_base": body_base,
+    }
+    return out
+
+
+def batch_desc(scenes: Sequence[Scene], contact_capacity: int = 0, candidate_capacity: int = 0):
+    """The prgpu_batch_desc of a list of scenes; returns (desc, flattened arrays kept alive)."""
+    f = flatten(list(scenes))
+    d = BatchDesc()
+    d.n_worlds = len(scenes)
+    d.world_body_count = _ptr(f["world_body_count"])
+    d.world_shape_count = _ptr(f["world_shape_count"])
+    d.world_joint_count = _ptr(f["world_joint_count"])
+    d.n_bodies = int(f["body_type"].size)
+    for k in ("body_type", "body_pos", "body_vel", "body_acc", "body_damp", "body_flags", "shape_body",
+              "shape_kind", "shape_voff", "shape_nv", "shape_radius", "shape_density", "shape_friction",
+              "shape_restitution", "shape_filter", "verts", "joint_bodies", "joint_anchors",
+              "joint_params", "joint_flags"):
+        setattr(d, k, _ptr(f[k]))
+    d.n_shapes = int(f["shape_body"].size)
+    d.n_verts = int(f["verts"].shape[0])
+    d.n_joints = int(f["joint_bodies"].shape[0])
+    d.contact_capacity = contact_capacity
+    d.candidate_capacity = candidate_capacity
+    return d, f
+
+
+def prepare_bodies(scenes: Sequence[Scene]) -> dict:
+    """Host-side batch preparation (no GPU): positions, velocities and mass data."""
+    lib = load_library()
+    d, f = batch_desc(scenes)
+    n = d.n_bodies
+    pos, vel, mass = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32), np.zeros((n, 4), np.float32)
+    rc = lib.prgpu_prepare_bodies(ctypes.byref(d), _ptr(pos), _ptr(vel), _ptr(mass))
+    if rc:
+        raise PrgpuError(rc, "prgpu_prepare_bodies failed")
+    return {"pos": pos, "vel": vel, "inv_mass": mass[:, 0], "inv_rot_inertia": mass[:, 1], "local_center": mass[:, 2:4]}
+
+
+class GpuBatch:
+    """A batch of worlds on one GPU behind the C ABI."""
+
+    def __init__(self, scenes: Sequence[Scene], device: int = 0, contact_capacity: int = 0,
+                 candidate_capacity: int = 0):
+        self.lib = load_library()
+        self.scenes = list(scenes)
+        f = flatten(self.scenes)
+        self._keep = f
+        d = BatchDesc()
+        d.n_worlds = len(self.scenes)
+        d.world_body_count = _ptr(f["world_body_count"])
+        d.world_shape_count = _ptr(f["world_shape_count"])
+        d.world_joint_count = _ptr(f["world_joint_count"])
+        d.n_bodies = int(f["body_type"].size)
+        for k in ("body_type", "body_pos", "body_vel", "body_acc", "body_damp", "body_flags", "shape_body",
+                  "shape_kind", "shape_voff", "shape_nv", "shape_radius", "shape_density", "shape_friction",
+                  "shape_restitution", "shape_filter", "verts", "joint_bodies", "joint_anchors",
+                  "joint_params", "joint_flags"):
+            setattr(d, k, _ptr(f[k]))
+        d.n_shapes = int(f["shape_body"].size)
+        d.n_verts = int(f["verts"].shape[0])
+        d.n_joints = int(f["joint_bodies"].shape[0])
+        d.contact_capacity = contact_capacity
+        d.candidate_capacity = candidate_capacity
+        self.n_bodies, self.n_shapes, self.n_joints = d.n_bodies, d.n_shapes, d.n_joints
+        self.body_base = f["body_base"]
+        h = ctypes.c_void_p()
+        rc = self.lib.prgpu_world_create(ctypes.byref(d), device, ctypes.byref(h))
+        if rc:
+            raise PrgpuError(rc, "prgpu_world_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.prgpu_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.prgpu_last_error(self.h, buf, 512)
+            raise PrgpuError(rc, f"{what}: {buf.value.decode()}")
+
+    def step(self, conf: StepConf | None = None, **overrides) -> dict:
+        c = conf if conf is not None else default_conf(**overrides)
+        st = StepStats()
+        self._check(self.lib.prgpu_step(self.h, ctypes.byref(c), ctypes.byref(st)), "prgpu_step")
+        return {n: getattr(st, n) for n, _ in StepStats._fields_}
+
+    def step_n(self, n: int, conf: StepConf | None = None, **overrides):
+        c = conf if conf is not None else default_conf(**overrides)
+        self._check(self.lib.prgpu_step_n(self.h, ctypes.byref(c), int(n)), "prgpu_step_n")
+
+    PHASES = ("pre_contacts", "islands_colour", "constraints", "sweeps", "writeback_sleep", "sync_update",
+              "find_contacts")
+
+    def step_profiled(self, conf: StepConf | None = None, **overrides):
+        """One step launched phase by phase; returns ({phase: ms}, stats)."""
+        c = conf if conf is not None else default_conf(**overrides)
+        ms = np.zeros(len(self.PHASES), np.float32)
+        st = StepStats()
+        self._check(self.lib.prgpu_step_profiled(self.h, ctypes.byref(c), _ptr(ms), len(self.PHASES),
+                                                 ctypes.byref(st)), "prgpu_step_profiled")
+        return dict(zip(self.PHASES, ms.tolist())), {n: getattr(st, n) for n, _ in StepStats._fields_}
+
+    def last_step_phase_ms(self) -> dict:
+        """Phase device times of the last graph-replayed step (and 'step' for all of it)."""
+        ms = np.zeros(len(self.PHASES) + 1, np.float32)
+        self._check(self.lib.prgpu_last_step_phase_ms(self.h, _ptr(ms), ms.size), "phase times")
+        out = dict(zip(self.PHASES, ms[:-1].tolist()))
+        out["step"] = float(ms[-1])
+        return out
+
+    def step_async(self, n: int, conf: StepConf):
+        self._check(self.lib.prgpu_step_async(self.h, ctypes.byref(conf), int(n)), "prgpu_step_async")
+
+    def synchronize(self):
+        self._check(self.lib.prgpu_synchronize(self.h), "prgpu_synchronize")
+
+    def bodies(self) -> dict:
+        n = self.n_bodies
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        xf = np.zeros((n, 4), np.float32)
+        mass = np.zeros((n, 4), np.float32)
+        uat = np.zeros(n, np.float32)
+        flags = np.zeros(n, np.uint32)
+        self._check(self.lib.prgpu_download_bodies(self.h, _ptr(pos), _ptr(vel), _ptr(xf), _ptr(mass), _ptr(uat),
+                                                    _ptr(flags)), "prgpu_download_bodies")
+        return {"pos": pos, "vel": vel, "xf": xf, "inv_mass": mass[:, 0].copy(),
+                "inv_rot_inertia": mass[:, 1].copy(), "local_center": mass[:, 2:4].copy(),
+                "under_active": uat, "awake": (flags & 1).astype(np.int32)}
+
+    def set_body_states(self, pos=None, vel=None, first: int = 0):
+        pos = None if pos is None else np.ascontiguousarray(pos, dtype=np.float32)
+        vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float32)
+        count = (pos if pos is not None else vel).shape[0]
+        self._check(self.lib.prgpu_upload_body_states(self.h, first, count, _ptr(pos), _ptr(vel)),
+                    "prgpu_upload_body_states")
+
+    def contact_count(self) -> int:
+        n = ctypes.c_uint32()
+        self._check(self.lib.prgpu_get_counts(self.h, None, None, None, None, ctypes.byref(n)), "counts")
+        return n.value
+
+    def contacts(self) -> dict:
+        n = self.contact_count()
+        cap = max(n, 1)
+        pr = np.zeros((cap, 2), np.uint32)
+        bd = np.zeros((cap, 2), np.uint32)
+        fl = np.zeros(cap, np.uint32)
+        me = np.zeros((cap, 2), np.int32)
+        hd = np.zeros((cap, 4), np.float32)
+        pt = np.zeros((cap, 2, 4), np.float32)
+        ft = np.zeros((cap, 2), np.uint32)
+        nout = ctypes.c_uint32()
+        self._check(self.lib.prgpu_download_contacts(self.h, cap, ctypes.byref(nout), _ptr(pr), _ptr(bd), _ptr(fl),
+                                                      _ptr(me), _ptr(hd), _ptr(pt), _ptr(ft)), "contacts")
+        n = nout.value
+        feats = np.stack([(ft[:n] >> s) & 0xff for s in (0, 8, 16, 24)], axis=-1).astype(np.int32)
+        return {"proxy": pr[:n].astype(np.int64), "bodies": bd[:n].astype(np.int64), "touching": (fl[:n] & 1).astype(np.int32),
+                "type": me[:n, 0], "count": me[:n, 1], "local_normal": hd[:n, 0:2], "local_point": hd[:n, 2:4],
+                "points": pt[:n], "features": feats}
+
+    def proxies(self) -> np.ndarray:
+        a = np.zeros((self.n_shapes, 4), np.float32)
+        self._check(self.lib.prgpu_download_proxies(self.h, _ptr(a)), "proxies")
+        return a
+
+
+def gpu_available() -> bool:
+    try:
+        import torch  # noqa: F401 -- only to ask whether a device exists
+
+        return bool(torch.cuda.is_available())
+    except Exception:
+        return False

@@ -218,110 +218,239 @@ GRAVITY = (0.0, -10.0, 0.0)
 
 
 def pyramid(rows: int = 20, x0: float = -7.0, ground_half: float = 40.0, density=1.0,
-            friction=0.6, restitution=0.0, builder: SceneBuilder | None = None) -> Scene:
+            friction=0.6, restitution=0.0) -> Scene:
     """Box pyramid on a static edge (workload 1: 20 rows, 210 boxes).
 
-    Row i (0-based) holds rows-i unit boxes (half-extent 0.5) at
-    x = x0 + 0.5625 i + 1.125 j and y = 0.75 + 1.25 i.
+    Row i (0-based) holds rows-i unit boxes (half-extent 0.5, SetAsBox vertex
+    order, which is also the hull order) at x = x0 + 0.5625 i + 1.125 j and
+    y = 0.75 + 1.25 i.
     """
-    sb = builder or SceneBuilder()
-    g = sb.body(STATIC, 0.0, 0.0)
-    sb.edge(g, (-ground_half, 0.0), (ground_half, 0.0), friction=friction)
+    ii, jj = [], []
     for i in range(rows):
-        y = 0.75 + 1.25 * i
-        for j in range(rows - i):
-            x = x0 + 0.5625 * i + 1.125 * j
-            b = sb.body(DYNAMIC, x, y, acc=GRAVITY)
-            sb.box(b, 0.5, 0.5, density=density, friction=friction, restitution=restitution)
-    return sb.build() if builder is None else None
+        ii.extend([i] * (rows - i))
+        jj.extend(range(rows - i))
+    ii = np.asarray(ii, np.float64)
+    jj = np.asarray(jj, np.float64)
+    n = len(ii)
+    nb = n + 1
+    body_type = np.full(nb, DYNAMIC, np.int32)
+    body_type[0] = STATIC
+    pos = np.zeros((nb, 3), F32)
+    pos[1:, 0] = x0 + 0.5625 * ii + 1.125 * jj
+    pos[1:, 1] = 0.75 + 1.25 * ii
+    acc = np.zeros((nb, 3), F32)
+    acc[1:] = GRAVITY
+    ns = n + 1
+    box = np.asarray([(0.5, -0.5), (0.5, 0.5), (-0.5, 0.5), (-0.5, -0.5)], F32)
+    verts = np.concatenate([np.asarray([(-ground_half, 0.0), (ground_half, 0.0)], F32), np.tile(box, (n, 1))])
+    nv = np.full(ns, 4, np.int32)
+    nv[0] = 2
+    voff = np.zeros(ns, np.int32)
+    voff[1:] = 2 + 4 * np.arange(n)
+    kind = np.full(ns, POLYGON, np.int32)
+    kind[0] = EDGE
+    dens = np.full(ns, density, F32)
+    dens[0] = 0.0
+    filt = np.zeros((ns, 4), np.int32)
+    filt[:, 0], filt[:, 1] = 1, 0xFFFF
+    return Scene(body_type=body_type, body_pos=pos, body_vel=np.zeros((nb, 3), F32), body_acc=acc,
+                 body_damp=np.zeros((nb, 2), F32), body_flags=np.full(nb, BF_DEFAULT, np.uint32),
+                 shape_body=np.arange(ns, dtype=np.int32), shape_kind=kind, shape_voff=voff, shape_nv=nv,
+                 shape_radius=np.full(ns, DEFAULT_VERTEX_RADIUS, F32), shape_density=dens,
+                 shape_friction=np.full(ns, friction, F32), shape_restitution=np.full(ns, restitution, F32),
+                 shape_filter=filt, verts=verts, joint_bodies=np.zeros((0, 2), np.int32),
+                 joint_anchors=np.zeros((0, 4), F32), joint_params=np.zeros((0, 6), F32),
+                 joint_flags=np.zeros((0, 3), np.int32))
 
 
-def _random_convex(rng, r, nmin=3, nmax=8):
-    n = int(rng.integers(nmin, nmax + 1))
-    ang = np.sort(rng.uniform(0.0, 2.0 * math.pi, size=n))
-    return [(r * math.cos(a), r * math.sin(a)) for a in ang]
+def convex_hulls(pts: np.ndarray, counts: np.ndarray, slop: float = float(DEFAULT_LINEAR_SLOP)):
+    """Vectorised ``convex_hull`` over many small point sets (float32 arithmetic).
+
+    pts: float32 [P, M, 2]; counts: int [P].  Returns (hull points [P, M, 2], hull counts).
+    Same rules as ``convex_hull``: VertexSet de-duplication, then gift wrapping from
+    the lowest right-most point, counter-clockwise.
+    """
+    pts = np.asarray(pts, dtype=F32)
+    P, M = pts.shape[:2]
+    counts = np.asarray(counts)
+    min_sep2 = F32(F32(slop) * F32(slop))
+    keep = np.zeros((P, M), dtype=bool)
+    for j in range(M):
+        valid = j < counts
+        dup = np.zeros(P, dtype=bool)
+        for i in range(j):
+            dx = pts[:, j, 0] - pts[:, i, 0]
+            dy = pts[:, j, 1] - pts[:, i, 1]
+            dup |= keep[:, i] & ((dx * dx + dy * dy) <= min_sep2)
+        keep[:, j] = valid & ~dup
+    order = np.argsort(~keep, axis=1, kind="stable")
+    q = np.take_along_axis(pts, order[:, :, None], axis=1)
+    n = keep.sum(axis=1)
+    ar = np.arange(P)
+    i0 = np.zeros(P, dtype=np.int64)
+    max_x = q[:, 0, 0].copy()
+    for i in range(1, M):
+        x = q[:, i, 0]
+        better = (i < n) & ((max_x < x) | ((max_x == x) & (q[:, i, 1] < q[ar, i0, 1])))
+        i0 = np.where(better, i, i0)
+        max_x = np.where(better, x, max_x)
+    hull = np.zeros((P, M + 1), dtype=np.int64)
+    hn = np.zeros(P, dtype=np.int64)
+    done = n == 0
+    ih = i0.copy()
+    for _ in range(M + 1):
+        act = ~done
+        hull[ar[act], hn[act]] = ih[act]
+        hn = hn + act
+        ie = np.zeros(P, dtype=np.int64)
+        for j in range(1, M):
+            a = act & (j < n)
+            same = a & (ie == ih)
+            rest = a & ~same
+            rx = q[ar, ie, 0] - q[ar, ih, 0]
+            ry = q[ar, ie, 1] - q[ar, ih, 1]
+            vx = q[:, j, 0] - q[ar, ih, 0]
+            vy = q[:, j, 1] - q[ar, ih, 1]
+            c = rx * vy - ry * vx
+            mv = vx * vx + vy * vy
+            mr = rx * rx + ry * ry
+            take = rest & ((c < 0) | ((c == 0) & (mv > mr)))
+            ie = np.where(same | take, j, ie)
+        ih = np.where(act, ie, ih)
+        done = done | (ie == i0) | (hn > n)
+    hn = np.minimum(hn, n)
+    out = np.zeros((P, M, 2), dtype=F32)
+    idx = hull[:, :M]
+    out[:] = np.take_along_axis(q, idx[:, :, None], axis=1)
+    return out, hn
 
 
-class _Grid:
-    """Uniform-grid overlap rejection of bounding circles during scene generation."""
-
-    def __init__(self, cell: float):
-        self.cell = cell
-        self.cells = {}
-
-    def free(self, x, y, r):
-        c = self.cell
-        i0, i1 = int(math.floor((x - r - 0.6) / c)), int(math.floor((x + r + 0.6) / c))
-        j0, j1 = int(math.floor((y - r - 0.6) / c)), int(math.floor((y + r + 0.6) / c))
-        for i in range(i0, i1 + 1):
-            for j in range(j0, j1 + 1):
-                for (qx, qy, qr) in self.cells.get((i, j), ()):
-                    if (qx - x) ** 2 + (qy - y) ** 2 < (qr + r) ** 2:
-                        return False
-        return True
-
-    def add(self, x, y, r):
-        k = (int(math.floor(x / self.cell)), int(math.floor(y / self.cell)))
-        self.cells.setdefault(k, []).append((x, y, r))
+def _jittered_positions(rng, n, x0, x1, y0, y1, cell, r):
+    """n non-overlapping positions (bounding radius r) on a jittered grid: each body
+    takes its own cell of side `cell` >= 2 r and is placed uniformly inside it."""
+    nx = max(1, int((x1 - x0) // cell))
+    ny = max(1, int((y1 - y0) // cell))
+    if n > nx * ny:
+        raise ValueError(f"{n} bodies do not fit in {nx}x{ny} cells")
+    cells = rng.choice(nx * ny, size=n, replace=False)
+    cx, cy = cells % nx, cells // nx
+    slack = np.maximum(0.5 * cell - r, 0.0)
+    x = x0 + (cx + 0.5) * cell + rng.uniform(-1.0, 1.0, n) * slack
+    y = y0 + (cy + 0.5) * cell + rng.uniform(-1.0, 1.0, n) * slack
+    return x, y
 
 
-def _add_random_shape(sb, rng, x, y, r, is_disk, density, friction, vel=None):
-    v = vel if vel is not None else (0.0, 0.0, 0.0)
-    b = sb.body(DYNAMIC, x, y, v=v, acc=GRAVITY)
-    if is_disk:
-        sb.disk(b, r, density=density, friction=friction)
-    else:
-        sb.polygon(b, _random_convex(rng, r), density=density, friction=friction)
-    return b
+def _assemble(static_edges, x, y, angle, vel, radius, is_disk, nverts, density, friction, rng,
+              extra_bodies=None, joints=None, shape_filter=None, acc=GRAVITY):
+    """Builds a Scene: one static ground body with edges, then one dynamic body per
+    entry (disk or random convex polygon of `nverts` points on a circle)."""
+    n = len(x)
+    nb = 1 + n
+    body_type = np.full(nb, DYNAMIC, np.int32)
+    body_type[0] = STATIC
+    pos = np.zeros((nb, 3), F32)
+    pos[1:, 0], pos[1:, 1], pos[1:, 2] = x, y, angle
+    v = np.zeros((nb, 3), F32)
+    if vel is not None:
+        v[1:] = vel
+    a = np.zeros((nb, 3), F32)
+    a[1:] = acc
+    flags = np.full(nb, BF_DEFAULT, np.uint32)
+    # polygons
+    M = 8
+    pts = np.zeros((n, M, 2), F32)
+    cnt = np.where(is_disk, 1, nverts)
+    poly = ~is_disk
+    if poly.any():
+        k = int(poly.sum())
+        ang = np.sort(rng.uniform(0.0, 2.0 * math.pi, size=(k, M)), axis=1)
+        mask = np.arange(M)[None, :] < nverts[poly][:, None]
+        ang = np.where(mask, ang, np.inf)
+        ang = np.sort(ang, axis=1)
+        rr = radius[poly][:, None]
+        px = np.where(mask, rr * np.cos(np.where(mask, ang, 0.0)), 0.0)
+        py = np.where(mask, rr * np.sin(np.where(mask, ang, 0.0)), 0.0)
+        hp, hn = convex_hulls(np.stack([px, py], -1).astype(F32), nverts[poly])
+        pts[poly] = hp
+        cnt = cnt.copy()
+        cnt[poly] = hn
+    ne = len(static_edges)
+    ns = ne + n
+    shape_body = np.zeros(ns, np.int32)
+    shape_body[ne:] = np.arange(1, nb)
+    kind = np.full(ns, EDGE, np.int32)
+    kind[ne:] = np.where(is_disk, DISK, POLYGON)
+    nv = np.zeros(ns, np.int32)
+    nv[:ne] = 2
+    nv[ne:] = cnt
+    voff = np.zeros(ns, np.int32)
+    voff[1:] = np.cumsum(nv)[:-1]
+    verts = np.zeros((int(nv.sum()), 2), F32)
+    for e, (p0, p1) in enumerate(static_edges):
+        verts[2 * e] = p0
+        verts[2 * e + 1] = p1
+    # dynamic shape vertices, vectorised scatter
+    dyn_off = voff[ne:]
+    dv = np.where(is_disk[:, None, None], 0.0, pts)
+    sel = np.arange(M)[None, :] < cnt[:, None]
+    rows = (dyn_off[:, None] + np.arange(M)[None, :])[sel]
+    verts[rows] = dv[sel]
+    radius_s = np.zeros(ns, F32)
+    radius_s[:ne] = DEFAULT_VERTEX_RADIUS
+    radius_s[ne:] = np.where(is_disk, radius, DEFAULT_VERTEX_RADIUS)
+    dens = np.zeros(ns, F32)
+    dens[ne:] = density
+    fr = np.full(ns, friction, F32)
+    rest = np.zeros(ns, F32)
+    filt = np.zeros((ns, 4), np.int32)
+    filt[:, 0], filt[:, 1] = 1, 0xFFFF
+    return Scene(body_type=body_type, body_pos=pos, body_vel=v, body_acc=a,
+                 body_damp=np.zeros((nb, 2), F32), body_flags=flags, shape_body=shape_body,
+                 shape_kind=kind, shape_voff=voff, shape_nv=nv, shape_radius=radius_s,
+                 shape_density=dens, shape_friction=fr, shape_restitution=rest, shape_filter=filt,
+                 verts=verts, joint_bodies=np.zeros((0, 2), np.int32), joint_anchors=np.zeros((0, 4), F32),
+                 joint_params=np.zeros((0, 6), F32), joint_flags=np.zeros((0, 3), np.int32))
 
 
 def large_box(n_shapes: int = 100_000, size: float = 1000.0, seed: int = 0) -> Scene:
-    """Workload 2: n dynamic shapes (half disks, half 3-8-gons) in a walled box."""
+    """Workload 2: n dynamic shapes (half disks r~U[0.05,0.5], half 3-8-gons on a circle
+    of radius U[0.1,0.6]) in a square closed by 4 static edges; v~N(0,1), w~N(0,0.5),
+    density U[0.5,2], friction 0.4.  Positions are uniform without overlaps
+    (jittered grid of 1.3 m cells)."""
     rng = np.random.default_rng(seed)
-    sb = SceneBuilder()
     h = size / 2.0
-    g = sb.body(STATIC, 0.0, 0.0)
-    for a, b in (((-h, -h), (h, -h)), ((h, -h), (h, h)), ((h, h), (-h, h)), ((-h, h), (-h, -h))):
-        sb.edge(g, a, b, friction=0.4)
-    grid = _Grid(2.0)
-    placed = 0
-    while placed < n_shapes:
-        is_disk = placed < n_shapes // 2
-        r = float(rng.uniform(0.05, 0.5)) if is_disk else float(rng.uniform(0.1, 0.6))
-        x = float(rng.uniform(-h + 1.0, h - 1.0))
-        y = float(rng.uniform(-h + 1.0, h - 1.0))
-        if not grid.free(x, y, r):
-            continue
-        grid.add(x, y, r)
-        vel = (float(rng.normal(0, 1)), float(rng.normal(0, 1)), float(rng.normal(0, 0.5)))
-        _add_random_shape(sb, rng, x, y, r, is_disk, float(rng.uniform(0.5, 2.0)), 0.4, vel)
-        placed += 1
-    return sb.build()
+    n = n_shapes
+    is_disk = np.arange(n) < n // 2
+    radius = np.where(is_disk, rng.uniform(0.05, 0.5, n), rng.uniform(0.1, 0.6, n))
+    x, y = _jittered_positions(rng, n, -h + 0.5, h - 0.5, -h + 0.5, h - 0.5, 1.3, radius)
+    vel = np.stack([rng.normal(0, 1, n), rng.normal(0, 1, n), rng.normal(0, 0.5, n)], -1)
+    nverts = rng.integers(3, 9, n)
+    edges = [((-h, -h), (h, -h)), ((h, -h), (h, h)), ((h, h), (-h, h)), ((-h, h), (-h, -h))]
+    sc = _assemble(edges, x, y, np.zeros(n), vel, radius, is_disk, nverts,
+                   rng.uniform(0.5, 2.0, len(x)), 0.4, rng)
+    sc.shape_density[4:] = rng.uniform(0.5, 2.0, n).astype(F32)
+    sc.shape_friction[:] = F32(0.4)
+    return sc
 
 
 def pile(n_bodies: int, rng, friction=0.6, density=1.0, width=None) -> Scene:
-    """Random pile of disks and 3-8-gons dropped from heights U[1,50] m onto an edge."""
-    sb = SceneBuilder()
-    g = sb.body(STATIC, 0.0, 0.0)
+    """Random pile of disks and 3-8-gons (bounding radius U[0.1,0.5]) dropped from
+    heights U[1,50] m onto a static edge."""
     w = width if width is not None else max(10.0, math.sqrt(n_bodies) * 2.0)
-    sb.edge(g, (-w, 0.0), (w, 0.0), friction=friction)
-    grid = _Grid(2.0)
-    placed = 0
-    while placed < n_bodies:
-        is_disk = bool(rng.integers(0, 2))
-        r = float(rng.uniform(0.1, 0.5))
-        x = float(rng.uniform(-w + 1.0, w - 1.0))
-        y = float(rng.uniform(1.0, 50.0))
-        if not grid.free(x, y, r):
-            continue
-        grid.add(x, y, r)
-        _add_random_shape(sb, rng, x, y, r, is_disk, density, friction)
-        placed += 1
-    return sb.build()
+    n = n_bodies
+    is_disk = rng.integers(0, 2, n).astype(bool)
+    radius = rng.uniform(0.1, 0.5, n)
+    cells_needed = n / ((2 * w - 2.0) // 1.1) + 1
+    top = max(50.0, 1.0 + 1.1 * cells_needed + 1.1)
+    x, y = _jittered_positions(rng, n, -w + 1.0, w - 1.0, 1.0, top, 1.1, radius)
+    nverts = rng.integers(3, 9, n)
+    return _assemble([((-w, 0.0), (w, 0.0))], x, y, np.zeros(n), None, radius, is_disk, nverts,
+                     np.full(n, density), friction, rng)
 
 
 def batched_worlds(n_worlds: int = 4096, seed: int = 1, lo: int = 16, hi: int = 2048) -> List[Scene]:
-    """Workload 3: worlds with log-uniform body counts in [lo, hi]; half pyramids, half piles."""
+    """Workload 3: worlds with log-uniform body counts in [lo, hi]; each is, with equal
+    probability, a box pyramid with as many rows as the count allows or a pile."""
     rng = np.random.default_rng(seed)
     worlds = []
     for _ in range(n_worlds):
@@ -359,38 +488,54 @@ def push_worlds(n_worlds: int = 64, seed: int = 2, mu: float = 0.5, disk_v=(8.0,
 
 
 def chains_world(rng, n_free: int = 8000, n_chains: int = 64, links: int = 32) -> Scene:
-    """Workload 5 world: free mixed shapes plus chains of 0.2x1 m boxes on revolute joints."""
+    """Workload 5 world: free mixed shapes plus chains of 0.2x1 m boxes on revolute
+    joints hanging from static anchors (chain links do not collide with each other)."""
+    w = 160.0 if n_free > 1000 else 40.0
+    n = n_free
+    is_disk = rng.integers(0, 2, n).astype(bool)
+    radius = rng.uniform(0.1, 0.5, n)
+    x, y = _jittered_positions(rng, n, -w + 1.0, w - 1.0, 1.0, 61.0, 1.1, radius)
+    nverts = rng.integers(3, 9, n)
+    free = _assemble([((-w, 0.0), (w, 0.0))], x, y, np.zeros(n), None, radius, is_disk, nverts,
+                     np.ones(n), 0.6, rng)
+    # append chains with a builder (small part of the world)
     sb = SceneBuilder()
-    w = 160.0
-    g = sb.body(STATIC, 0.0, 0.0)
-    sb.edge(g, (-w, 0.0), (w, 0.0), friction=0.6)
-    grid = _Grid(2.0)
-    placed = 0
-    while placed < n_free:
-        is_disk = bool(rng.integers(0, 2))
-        r = float(rng.uniform(0.1, 0.5))
-        x = float(rng.uniform(-w + 1.0, w - 1.0))
-        y = float(rng.uniform(1.0, 60.0))
-        if not grid.free(x, y, r):
-            continue
-        grid.add(x, y, r)
-        _add_random_shape(sb, rng, x, y, r, is_disk, 1.0, 0.6)
-        placed += 1
+    nb0 = free.n_bodies
     top = 100.0
     for c in range(n_chains):
         ax = -w + 2.0 + (2 * w - 4.0) * (c + 0.5) / n_chains
         anchor = sb.body(STATIC, ax, top)
         prev = anchor
         for k in range(links):
-            y = top - 0.5 - 1.0 * k
-            b = sb.body(DYNAMIC, ax, y, acc=GRAVITY)
+            yk = top - 0.5 - 1.0 * k
+            b = sb.body(DYNAMIC, ax, yk, acc=GRAVITY)
             sb.box(b, 0.1, 0.5, density=1.0, friction=0.6, filt=(2, 0xFFFD, 0, 0))
             if prev == anchor:
-                sb.revolute(prev, b, (0.0, 0.0), (0.0, 0.5))
+                sb.revolute(prev + nb0, b + nb0, (0.0, 0.0), (0.0, 0.5))
             else:
-                sb.revolute(prev, b, (0.0, -0.5), (0.0, 0.5))
+                sb.revolute(prev + nb0, b + nb0, (0.0, -0.5), (0.0, 0.5))
             prev = b
-    return sb.build()
+    ch = sb.build()
+    vbase = free.verts.shape[0]
+    return Scene(
+        body_type=np.concatenate([free.body_type, ch.body_type]),
+        body_pos=np.concatenate([free.body_pos, ch.body_pos]),
+        body_vel=np.concatenate([free.body_vel, ch.body_vel]),
+        body_acc=np.concatenate([free.body_acc, ch.body_acc]),
+        body_damp=np.concatenate([free.body_damp, ch.body_damp]),
+        body_flags=np.concatenate([free.body_flags, ch.body_flags]),
+        shape_body=np.concatenate([free.shape_body, ch.shape_body + nb0]).astype(np.int32),
+        shape_kind=np.concatenate([free.shape_kind, ch.shape_kind]),
+        shape_voff=np.concatenate([free.shape_voff, ch.shape_voff + vbase]).astype(np.int32),
+        shape_nv=np.concatenate([free.shape_nv, ch.shape_nv]),
+        shape_radius=np.concatenate([free.shape_radius, ch.shape_radius]),
+        shape_density=np.concatenate([free.shape_density, ch.shape_density]),
+        shape_friction=np.concatenate([free.shape_friction, ch.shape_friction]),
+        shape_restitution=np.concatenate([free.shape_restitution, ch.shape_restitution]),
+        shape_filter=np.concatenate([free.shape_filter, ch.shape_filter]),
+        verts=np.concatenate([free.verts, ch.verts]),
+        joint_bodies=ch.joint_bodies.astype(np.int32), joint_anchors=ch.joint_anchors,
+        joint_params=ch.joint_params, joint_flags=ch.joint_flags)
 
 
 def scene_text(scene: Scene, conf_overrides: dict | None = None) -> str:

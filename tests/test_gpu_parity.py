@@ -1,0 +1,186 @@
+"""GPU world step against the CPU oracle (which is pinned to the reference).
+
+Parity bars (from the world-step specification):
+  (1) broadphase pair sets and contact-feature IDs match exactly;
+  (2) manifold points/normals agree within 1e-5 relative in FP32, and so do
+      post-step states when both sides solve to convergence (the GPU sweeps
+      constraints in colour order, the reference in island order);
+  (3) long runs are compared through drift / penetration / stability metrics.
+Everything goes through the C ABI (libprgpu.so) via playrho_gb300.gpu.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from playrho_gb300 import scenes
+from playrho_gb300.gpu import GpuBatch, default_conf
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+
+
+def pair_set(c):
+    return set(map(tuple, np.asarray(c["proxy"]).astype(np.int64).tolist()))
+
+
+def by_pair(c):
+    return {tuple(int(x) for x in c["proxy"][k]): k for k in range(len(c["proxy"]))}
+
+
+def assert_contacts_match(gc, oc, atol_scale=1.0):
+    assert pair_set(gc) == pair_set(oc)
+    gi, oi = by_pair(gc), by_pair(oc)
+    for key, k in oi.items():
+        j = gi[key]
+        assert int(gc["touching"][j]) == int(oc["touching"][k]), key
+        n = int(oc["count"][k])
+        assert int(gc["count"][j]) == n, key
+        assert int(gc["type"][j]) == int(oc["type"][k]), key
+        np.testing.assert_array_equal(gc["features"][j][:n], oc["features"][k][:n], err_msg=str(key))
+        if n:
+            scale = max(1.0, float(np.abs(oc["local_point"][k]).max()))
+            np.testing.assert_allclose(gc["local_normal"][j], oc["local_normal"][k], atol=RTOL * atol_scale)
+            np.testing.assert_allclose(gc["local_point"][j], oc["local_point"][k], atol=RTOL * scale * atol_scale)
+            np.testing.assert_allclose(gc["points"][j][:n, :2], oc["points"][k][:n, :2], atol=RTOL * scale * atol_scale)
+
+
+def rebased(scene, pos, vel):
+    """The scene with body positions (of the centre of mass) and velocities replaced."""
+    s = scenes.Scene(**{f: getattr(scene, f) for f in scene.__dataclass_fields__})
+    s.body_pos = np.ascontiguousarray(pos, dtype=np.float32)
+    s.body_vel = np.ascontiguousarray(vel, dtype=np.float32)
+    return s
+
+
+def test_first_contacts_pyramid(gpu_lib):
+    sc = scenes.pyramid()
+    g, ow = GpuBatch([sc]), oracle.OracleWorld(sc)
+    g.step(deltaTime=0.0)
+    ow.step(deltaTime=0.0)
+    assert_contacts_match(g.contacts(), ow.contacts())
+    np.testing.assert_array_equal(g.proxies(), ow.proxies()["aabb"])
+
+
+def test_free_fall_is_bit_exact(gpu_lib):
+    sc = scenes.pyramid()
+    g, ow = GpuBatch([sc]), oracle.OracleWorld(sc)
+    for _ in range(10):
+        g.step()
+        ow.step()
+        gb, ob = g.bodies(), ow.bodies()
+        np.testing.assert_array_equal(gb["pos"], ob["pos"])
+        np.testing.assert_array_equal(gb["vel"], ob["vel"])
+    assert_contacts_match(g.contacts(), ow.contacts())
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_pair_sets_random_piles(gpu_lib, seed):
+    # Identical transforms on both sides (fresh worlds from the same state), then a
+    # zero-length step: proxies, pair sets and manifolds must match exactly.
+    rng = np.random.default_rng(seed)
+    sc = scenes.pile(150, rng, width=6.0)
+    g = GpuBatch([sc])
+    for _ in range(240):
+        g.step()
+    gb = g.bodies()
+    s2 = rebased(sc, np.stack([gb["pos"][:, 0], gb["pos"][:, 1], gb["pos"][:, 2]], 1), gb["vel"])
+    # positions above are centres of mass; the scene stores body origins
+    lc = gb["local_center"]
+    c, s = np.cos(gb["pos"][:, 2]), np.sin(gb["pos"][:, 2])
+    org = gb["pos"][:, :2] - np.stack([c * lc[:, 0] - s * lc[:, 1], s * lc[:, 0] + c * lc[:, 1]], 1)
+    s2.body_pos = np.ascontiguousarray(np.concatenate([org, gb["pos"][:, 2:3]], 1), dtype=np.float32)
+    g2, o2 = GpuBatch([s2]), oracle.OracleWorld(s2)
+    g2.step(deltaTime=0.0)
+    o2.step(deltaTime=0.0)
+    gc, oc = g2.contacts(), o2.contacts()
+    assert len(gc["proxy"]) > 20
+    assert_contacts_match(gc, oc, atol_scale=10.0)
+
+
+def test_pyramid_long_run_settles(gpu_lib):
+    sc = scenes.pyramid()
+    g, ow = GpuBatch([sc]), oracle.OracleWorld(sc)
+    g.step_n(600)
+    for _ in range(600):
+        ow.step()
+    gb, ob = g.bodies(), ow.bodies()
+    dyn = sc.body_type == scenes.DYNAMIC
+    # Both come to rest with the pyramid standing.  With 8 velocity iterations the
+    # Gauss-Seidel solve is far from converged, so the colour order and the
+    # island order settle a few boxes at slightly different places: heights agree
+    # within 2 cm (no box dropped), lateral positions within 10 cm.
+    dx = np.abs(gb["pos"][dyn, 0] - ob["pos"][dyn, 0]).max()
+    dy = np.abs(gb["pos"][dyn, 1] - ob["pos"][dyn, 1]).max()
+    assert dy < 0.02, f"heights differ by {dy:.4f} m"
+    assert dx < 0.10, f"lateral positions differ by {dx:.4f} m"
+    assert int(gb["awake"].sum()) == int(ob["awake"].sum()) == 0, (int(gb["awake"].sum()), int(ob["awake"].sum()))
+
+
+def test_batch_equals_single_worlds(gpu_lib):
+    rng = np.random.default_rng(7)
+    worlds = [scenes.pyramid(rows=5), scenes.pile(60, rng, width=5.0), scenes.pyramid(rows=8),
+              scenes.pile(90, rng, width=6.0)]
+    batch = GpuBatch(worlds)
+    singles = [GpuBatch([w]) for w in worlds]
+    for _ in range(60):
+        batch.step()
+        for s in singles:
+            s.step()
+    bb = batch.bodies()
+    for i, s in enumerate(singles):
+        lo, hi = batch.body_base[i], batch.body_base[i + 1]
+        sb = s.bodies()
+        np.testing.assert_array_equal(bb["pos"][lo:hi], sb["pos"])
+        np.testing.assert_array_equal(bb["vel"][lo:hi], sb["vel"])
+
+
+def test_deterministic(gpu_lib):
+    rng = np.random.default_rng(11)
+    sc = scenes.pile(200, rng, width=6.0)
+    a, b = GpuBatch([sc]), GpuBatch([sc])
+    a.step_n(80)
+    b.step_n(80)
+    np.testing.assert_array_equal(a.bodies()["pos"], b.bodies()["pos"])
+
+
+def _stack(n=3, gap=0.0175):
+    # Boxes resting with their skins overlapping by 2.5 mm (inside the 5 mm linear
+    # slop), so the position solver, whose fixed point is order dependent, makes
+    # no correction and the step is decided by the velocity solve alone.
+    sb = scenes.SceneBuilder()
+    g = sb.body(scenes.STATIC, 0.0, 0.0)
+    sb.edge(g, (-5.0, 0.0), (5.0, 0.0), friction=0.6)
+    for i in range(n):
+        b = sb.body(scenes.DYNAMIC, 0.1 * i, 0.5 + gap + (1.0 + gap) * i, acc=scenes.GRAVITY)
+        sb.box(b, 0.5, 0.5, density=1.0, friction=0.6)
+    return sb.build()
+
+
+def test_one_step_at_convergence(gpu_lib):
+    # Resting stack, both sides iterated far past convergence: post-step
+    # velocities and positions agree within 1e-5 relative.
+    sc = _stack(3)
+    conf = dict(regVelocityIters=400, regPositionIters=30, regMinSeparation=float("inf"))
+    g, ow = GpuBatch([sc]), oracle.OracleWorld(sc)
+    for _ in range(3):
+        g.step(**conf)
+        ow.step(**conf)
+    gb, ob = g.bodies(), ow.bodies()
+    dp = np.abs(gb["pos"] - ob["pos"]) / np.maximum(1.0, np.abs(ob["pos"]))
+    dv = np.abs(gb["vel"] - ob["vel"]) / np.maximum(1.0, np.abs(ob["vel"]))
+    assert dp.max() <= 1e-5, f"relative position difference {dp.max():.3g}"
+    assert dv.max() <= 1e-5, f"relative velocity difference {dv.max():.3g}"
+
+
+def test_revolute_chain(gpu_lib):
+    rng = np.random.default_rng(3)
+    sc = scenes.chains_world(rng, n_free=40, n_chains=3, links=6)
+    g, ow = GpuBatch([sc]), oracle.OracleWorld(sc)
+    for _ in range(30):
+        g.step()
+        ow.step()
+    gb, ob = g.bodies(), ow.bodies()
+    # chains hang from static anchors; link positions agree closely
+    d = np.abs(gb["pos"] - ob["pos"]).max()
+    assert d < 5e-3, f"positions differ by {d:.4g}"

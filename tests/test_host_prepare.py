@@ -1,0 +1,73 @@
+"""Host-side batch preparation of the C ABI (mass data, centre positions) against
+the oracle, which matches the reference bit for bit.  Runs without a GPU."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from playrho_gb300 import build, gpu, scenes
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return gpu.load_library()
+
+
+def _cases():
+    rng = np.random.default_rng(1)
+    return {
+        "pyramid": scenes.pyramid(),
+        "pile": scenes.pile(120, rng),
+        "box": scenes.large_box(400, size=40.0, seed=0),
+        "chains": scenes.chains_world(np.random.default_rng(3), n_free=30, n_chains=2, links=5),
+        "push": scenes.push_worlds(1)[0],
+    }
+
+
+@pytest.mark.parametrize("name", list(_cases().keys()))
+def test_prepare_matches_oracle(lib, name):
+    sc = _cases()[name]
+    hp = gpu.prepare_bodies([sc])
+    ob = oracle.OracleWorld(sc).bodies()
+    np.testing.assert_array_equal(hp["pos"], ob["pos"])
+    np.testing.assert_array_equal(hp["vel"], ob["vel"])
+    np.testing.assert_array_equal(hp["inv_mass"], ob["inv_mass"])
+    np.testing.assert_array_equal(hp["inv_rot_inertia"], ob["inv_rot_inertia"])
+
+
+def test_prepare_batch_is_concatenation(lib):
+    c = _cases()
+    worlds = [c["pyramid"], c["pile"], c["chains"]]
+    whole = gpu.prepare_bodies(worlds)
+    parts = [gpu.prepare_bodies([w]) for w in worlds]
+    np.testing.assert_array_equal(whole["pos"], np.concatenate([p["pos"] for p in parts]))
+
+
+def test_invalid_descriptions_rejected(lib):
+    sc = scenes.pyramid(rows=2)
+    bad = scenes.Scene(**{f: getattr(sc, f) for f in sc.__dataclass_fields__})
+    bad.shape_nv = bad.shape_nv.copy()
+    bad.shape_nv[0] = 1  # an edge with one vertex
+    with pytest.raises(gpu.PrgpuError):
+        gpu.prepare_bodies([bad])
+
+
+def test_library_exports(lib):
+    for name in gpu.exported_symbols():
+        assert hasattr(lib, name), name
+    assert lib.prgpu_abi_version() == 1
+
+
+def test_convex_hull_matches_scene_builder(lib):
+    import ctypes
+    rng = np.random.default_rng(4)
+    for _ in range(50):
+        n = int(rng.integers(3, 9))
+        ang = np.sort(rng.uniform(0, 2 * np.pi, n))
+        r = rng.uniform(0.1, 0.6)
+        pts = [(r * np.cos(a), r * np.sin(a)) for a in ang]
+        want = scenes.convex_hull(pts)
+        xy = np.asarray(pts, np.float32).reshape(-1)
+        out = np.zeros_like(xy)
+        m = lib.prgpu_convex_hull(xy.ctypes.data, n, ctypes.c_float(0.005), out.ctypes.data)
+        np.testing.assert_array_equal(out[:2 * m].reshape(-1, 2), np.asarray(want, np.float32))
