@@ -161,6 +161,23 @@ int prgpu_upload_body_states(prgpu_world* w, uint32_t first, uint32_t count, con
 int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
                             uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
                             uint32_t* features2);
+/* prgpu_download_contacts for callers that must not allocate device memory once
+ * running (a real-time loop that forbids allocation in its steady state, or a
+ * process whose device memory is held by another framework's caching allocator,
+ * where a new allocation fails or stalls).  It has no counterpart in the
+ * reference; it exists for those callers only.  Same arguments and results as
+ * prgpu_download_contacts, but the device gather goes through one fixed array
+ * of at most 65,536 contacts (84 bytes each, 5.5 MB) that the library declares
+ * in device memory: every GPU that loads the library holds that array until the
+ * process exits, and no cudaMalloc, cudaFree or allocating library routine is
+ * called.  More live contacts than that limit returns PRGPU_ECAPACITY with a
+ * message.  The first call on a device looks up the array's device address
+ * (with that device current), so make it before any stream capture.  All calls
+ * share the one array and it keeps the last call's contents: calls whose work
+ * overlaps on the GPU (several handles or threads at once) race on it. */
+int prgpu_download_contacts_noalloc(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
+                                    uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
+                                    uint32_t* features2);
 /* Fat (tree) AABB of every proxy: minx miny maxx maxy. */
 int prgpu_download_proxies(prgpu_world* w, float* aabb4);
 /* Runs the host-side part of prgpu_world_create (validation, mass data as

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <mutex>
 
 #include "../../include/prgpu.h"
 #include "prgpu_kernels.cuh"
@@ -944,6 +945,79 @@ int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, 
     if (pts8) CU(cudaMemcpyAsync(pts8, g_pt, 32 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     if (features2) CU(cudaMemcpyAsync(features2, g_ft, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaFreeAsync(scratch, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+// ---- contact download without device allocation ---------------------------
+// Some callers must not allocate device memory once they are running: a
+// real-time control or rendering loop that forbids allocation in its steady
+// state, or a process whose device memory is held by another framework's
+// caching allocator, where a new cudaMalloc/cudaMallocAsync can fail or stall.
+// For them prgpu_download_contacts_noalloc gathers into a fixed array in device
+// memory that exists from the moment the library is loaded (every GPU that
+// loads the library holds it until the process exits).
+constexpr uint32_t kNoAllocMaxContacts = 65536;
+constexpr size_t kNoAllocWords = 21;  // head 4 + points 8 + proxies 2 + bodies 2 + flags 1 + meta 2 + features 2
+static __device__ __align__(256) uint32_t g_noalloc_contacts[kNoAllocMaxContacts * kNoAllocWords];
+
+namespace {
+// Device address of g_noalloc_contacts per device.  In host code the array's
+// name is only a host-side stand-in, so the address is looked up once per
+// device, with that device current, and passed to the gather kernel.
+std::mutex g_noalloc_mutex;
+uint32_t* g_noalloc_ptr[64] = {};
+
+int noalloc_scratch(prgpu_world* w, uint32_t** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (w->device < 0 || w->device >= 64) return fail(w, PRGPU_EINVAL, "device ordinal out of range");
+    if (!g_noalloc_ptr[w->device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_contacts);
+        if (e != cudaSuccess || !p)
+            return fail(w, PRGPU_ECUDA, "cudaGetSymbolAddress(g_noalloc_contacts): %s", cudaGetErrorString(e));
+        g_noalloc_ptr[w->device] = static_cast<uint32_t*>(p);
+    }
+    *out = g_noalloc_ptr[w->device];
+    return PRGPU_OK;
+}
+}  // namespace
+
+int prgpu_download_contacts_noalloc(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
+                                    uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
+                                    uint32_t* features2) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    uint32_t* scratch = nullptr;
+    int rc = noalloc_scratch(w, &scratch);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(w->h_cnt, w->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    const uint32_t n = w->h_cnt->n_live;
+    if (n_out) *n_out = n;
+    if (n > capacity) return fail(w, PRGPU_ECAPACITY, "%u contacts exceed capacity %u", n, capacity);
+    if (n > kNoAllocMaxContacts)
+        return fail(w, PRGPU_ECAPACITY,
+                    "%u contacts exceed the %u that prgpu_download_contacts_noalloc can stage; "
+                    "use prgpu_download_contacts", n, kNoAllocMaxContacts);
+    if (n == 0) return PRGPU_OK;
+    // The gather writes every word of the n records, so nothing needs clearing.
+    float* g_hd = reinterpret_cast<float*>(scratch);
+    float* g_pt = g_hd + 4 * (size_t)n;
+    uint32_t* g_pr = reinterpret_cast<uint32_t*>(g_pt + 8 * (size_t)n);
+    uint32_t* g_bd = g_pr + 2 * (size_t)n;
+    uint32_t* g_fl = g_bd + 2 * (size_t)n;
+    int32_t* g_me = reinterpret_cast<int32_t*>(g_fl + n);
+    uint32_t* g_ft = reinterpret_cast<uint32_t*>(g_me + 2 * (size_t)n);
+    k_gather_contacts<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, n, g_pr, g_bd, g_fl, g_me, g_hd, g_pt, g_ft);
+    CU(cudaGetLastError());
+    if (proxies2) CU(cudaMemcpyAsync(proxies2, g_pr, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (bodies2) CU(cudaMemcpyAsync(bodies2, g_bd, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (flags) CU(cudaMemcpyAsync(flags, g_fl, 4 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (meta2) CU(cudaMemcpyAsync(meta2, g_me, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (head4) CU(cudaMemcpyAsync(head4, g_hd, 16 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (pts8) CU(cudaMemcpyAsync(pts8, g_pt, 32 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (features2) CU(cudaMemcpyAsync(features2, g_ft, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaStreamSynchronize(w->stream));
     return PRGPU_OK;
 }
