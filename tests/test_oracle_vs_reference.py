@@ -1,0 +1,43 @@
+"""The CPU oracle against the PlayRho reference compiled from source, on scenes
+not in the committed fixtures.  Skipped where the reference sources are absent."""
+import numpy as np
+import pytest
+
+from oracle import oracle, refdriver
+from playrho_gb300 import scenes
+
+pytestmark = pytest.mark.skipif(not refdriver.available(), reason="reference sources not present")
+
+
+def _compare(scene, steps, double=False):
+    dumps = refdriver.run(scenes.scene_text(scene), steps, double=double)
+    ow = oracle.OracleWorld(scene, double=double)
+    for n, d in zip(steps, dumps):
+        for _ in range(n):
+            ow.step()
+        b = ow.bodies()
+        np.testing.assert_array_equal(b["pos"], d["bodies"]["pos"])
+        np.testing.assert_array_equal(b["vel"], d["bodies"]["vel"])
+        c = ow.contacts()
+        np.testing.assert_array_equal(c["proxy"], d["contacts"]["proxy"])
+        np.testing.assert_array_equal(c["count"], d["contacts"]["count"])
+        for k in range(len(c["count"])):
+            m = int(c["count"][k])
+            np.testing.assert_array_equal(c["features"][k][:m], d["contacts"]["features"][k][:m])
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_piles(seed):
+    _compare(scenes.pile(250, np.random.default_rng(seed)), [1, 60, 120])
+
+
+def test_small_pyramid_f64():
+    _compare(scenes.pyramid(rows=8), [1, 100, 200], double=True)
+
+
+def test_spinning_box():
+    _compare(scenes.large_box(800, size=40.0, seed=4), [1, 40])
+
+
+def test_chains():
+    _compare(scenes.chains_world(np.random.default_rng(9), n_free=60, n_chains=3, links=6), [1, 80])
