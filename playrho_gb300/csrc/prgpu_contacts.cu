@@ -293,7 +293,7 @@ __device__ __forceinline__ uint32_t part1by1(uint32_t x) {
 }
 
 __global__ void k_lbvh_bounds_reset(DW d) {
-    if (!d.cnt->need_find) return;
+    if (!d.cnt->need_find || !d.cnt->lbvh_rebuild) return;
     GRID_LOOP(w, d.n_worlds) {
         const uint32_t inf = float_to_ordered(__int_as_float(0x7f800000));
         const uint32_t ninf = float_to_ordered(-__int_as_float(0x7f800000));
@@ -304,7 +304,7 @@ __global__ void k_lbvh_bounds_reset(DW d) {
 }
 
 __global__ void k_lbvh_bounds(DW d) {
-    if (!d.cnt->need_find) return;
+    if (!d.cnt->need_find || !d.cnt->lbvh_rebuild) return;
     GRID_LOOP(p, d.n_shapes) {
         const float4 a = d.p_aabb[p];
         const float cx = 0.5f * (a.x + a.z), cy = 0.5f * (a.y + a.w);
@@ -318,7 +318,7 @@ __global__ void k_lbvh_bounds(DW d) {
 }
 
 __global__ void k_lbvh_morton(DW d) {
-    if (!d.cnt->need_find) return;
+    if (!d.cnt->need_find || !d.cnt->lbvh_rebuild) return;
     GRID_LOOP(p, d.n_shapes) {
         const float4 a = d.p_aabb[p];
         const float cx = 0.5f * (a.x + a.z), cy = 0.5f * (a.y + a.w);
@@ -346,7 +346,7 @@ __device__ __forceinline__ int lb_delta(const uint64_t* __restrict__ keys, int n
 
 // Karras (2012) radix-tree construction over the sorted keys.
 __global__ void k_lbvh_internal(DW d) {
-    if (!d.cnt->need_find) return;
+    if (!d.cnt->need_find || !d.cnt->lbvh_rebuild) return;
     const int n = (int)d.n_shapes;
     const uint64_t* keys = d.l_key;
     GRID_LOOP(ui, (uint32_t)(n - 1)) {
@@ -385,7 +385,10 @@ __global__ void k_lbvh_internal(DW d) {
 
 __global__ void k_lbvh_leaves(DW d) {
     if (!d.cnt->need_find) return;
-    GRID_LOOP(k, d.n_shapes) d.l_leaf_box[k] = d.p_aabb[d.l_idx[k]];
+    GRID_LOOP(k, d.n_shapes) {
+        d.l_leaf_box[k] = d.p_aabb[d.l_idx[k]];
+        if (k + 1 < d.n_shapes) d.l_visit[k] = 0u;  // refit counters (internal nodes)
+    }
 }
 
 // Bottom-up refit: the second child to arrive at a node computes its box.
@@ -410,7 +413,7 @@ __global__ void k_lbvh_refit(DW d) {
 
 // Root of each world's subtree: the highest node whose leaves all belong to it.
 __global__ void k_lbvh_roots(DW d) {
-    if (!d.cnt->need_find) return;
+    if (!d.cnt->need_find || !d.cnt->lbvh_rebuild) return;
     const uint32_t n = d.n_shapes;
     GRID_LOOP(i, n) {
         // leaf i: a world with a single proxy has that leaf as its root
@@ -539,6 +542,7 @@ __global__ void k_new_contacts(DW d) {
         d.cs_flags[slot] = flags;
         const float2 ma = d.s_mat[pa], mb = d.s_mat[pb];
         d.cs_mat[slot] = make_float2(sqrtf(ma.x * mb.x), (ma.y > mb.y) ? ma.y : mb.y);
+        d.cs_colour[slot] = kNone;
         store_manifold(d, slot, man_empty());
         if (!sensor) {
             if (is_speedable(fa)) atomicOr(&d.b_flags[ba], BF_AWAKE);
@@ -595,7 +599,24 @@ __global__ void k_copy_u64u32(const uint64_t* ka, const uint32_t* va, uint64_t* 
     }
 }
 
-__global__ void k_set_lbvh_count(DW d, uint32_t* n_out) { *n_out = d.cnt->need_find ? d.n_shapes : 0u; }
+// The tree is rebuilt from fresh Morton codes every kRebuildEvery searches and
+// refitted in between: a refitted tree's node boxes still contain their leaves,
+// so queries return exactly the same pairs, only the traversal may visit more
+// nodes as bodies drift from their Morton order.
+constexpr uint32_t kRebuildEvery = 8;
+
+__global__ void k_set_lbvh_count(DW d, uint32_t* n_out) {
+    Counters* c = d.cnt;
+    if (!c->need_find) {
+        c->lbvh_rebuild = 0u;
+        *n_out = 0u;
+        return;
+    }
+    const bool rebuild = (c->lbvh_age == 0u) || (c->lbvh_age >= kRebuildEvery);
+    c->lbvh_rebuild = rebuild ? 1u : 0u;
+    c->lbvh_age = rebuild ? 1u : c->lbvh_age + 1u;
+    *n_out = rebuild ? d.n_shapes : 0u;
+}
 
 // Initial transforms from positions (device sin/cos), pos0 = pos1.
 __global__ void k_init_bodies(DW d) {

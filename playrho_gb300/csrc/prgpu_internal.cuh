@@ -112,6 +112,8 @@ struct Counters {
     float st_max_inc_impulse;
     uint32_t scan_total;
     uint32_t pad[7];
+    uint32_t lbvh_age;        // searches since the tree was last rebuilt (0: no tree yet)
+    uint32_t lbvh_rebuild;    // this search rebuilds the tree (else refits it)
 };
 
 // Solver / step configuration in device memory (mirrors prgpu_step_conf).
@@ -185,6 +187,8 @@ struct DW {
     uint2* cs_body;
     uint32_t* cs_flags;
     float2* cs_mat;          // friction restitution
+    uint32_t* cs_colour;     // colour the contact had in the last step (first choice next step)
+    uint32_t* j_colour;      // same for joints
     float4* m_head;          // ln.xy lp.xy
     float4* m_p0;            // lp.xy ni ti
     float4* m_p1;

@@ -245,61 +245,78 @@ __device__ __forceinline__ uint32_t constraint_prio(const DW& d, uint32_t id) {
     return mix32(((pr.x - base) * 0x9E3779B1u) ^ mix32(pr.y - base));
 }
 
+__device__ __forceinline__ uint32_t colour_hint(const DW& d, uint32_t id) {
+    return (id & kJointBit) ? d.j_colour[id & ~kJointBit] : d.cs_colour[id];
+}
+
+// Two grid barriers per round.  Phase T: every uncoloured constraint picks a
+// tentative colour from its neighbours' committed colours (in the first round
+// the colour it had last step, if still free); constraints coloured earlier
+// mark their tentative slot as settled.  Phase C: a constraint keeps its pick
+// unless an uncoloured neighbour of higher priority picked the same colour, and
+// commits it at once (phase C reads only tentative picks, never commits).
 __global__ void k_colour(DW d) {
+    constexpr uint32_t kSettled = 0xffffffffu;
     const uint32_t n = d.cnt->n_active;
-    GRID_LOOP(k, n) d.k_prio[k] = constraint_prio(d, d.k_list[k]);
+    uint32_t* rem = &d.cnt->pad[4];  // triple-buffered per-round counters
+    GRID_LOOP(k, n) {
+        d.k_prio[k] = constraint_prio(d, d.k_list[k]);
+        d.k_tent[k] = kSettled;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) { rem[0] = 0u; rem[1] = 0u; rem[2] = 0u; }
     grid_barrier(d.cnt);
     for (int round = 0; round < kMaxColourRounds; ++round) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) rem[(round + 1) % 3] = 0u;
         GRID_LOOP(k, n) {
-            if (d.k_colour[k] != kNone) continue;
+            const uint32_t ck = d.k_colour[k];
+            if (ck != kNone) {
+                if (d.k_tent[k] != kSettled) d.k_tent[k] = kSettled;
+                continue;
+            }
             uint32_t a, b;
-            constraint_bodies(d, d.k_list[k], a, b);
+            const uint32_t id = d.k_list[k];
+            constraint_bodies(d, id, a, b);
             uint64_t forbid = 0;
             const uint32_t bs[2] = {a, b};
             for (int e = 0; e < 2; ++e) {
                 const uint32_t x = bs[e];
-                if (!is_accelerable(d.b_flags[x])) continue;
+                if (!is_accelerable(d.b_flags[x]) || (e == 1 && b == a)) continue;
                 for (uint32_t t = d.inc_off[x]; t < d.inc_off[x + 1]; ++t) {
                     const uint32_t c = __ldcg(&d.k_colour[d.inc_list[t]]);
                     if (c < (uint32_t)kMaxColours) forbid |= 1ull << c;
                 }
             }
-            d.k_tent[k] = (forbid == ~0ull) ? (uint32_t)kSerialColour : (uint32_t)(__ffsll((long long)~forbid) - 1);
+            uint32_t t;
+            const uint32_t hint = (round == 0) ? colour_hint(d, id) : kNone;
+            if (hint < (uint32_t)kMaxColours && !((forbid >> hint) & 1ull)) t = hint;
+            else if (forbid == ~0ull) t = (uint32_t)kSerialColour;
+            else t = (uint32_t)(__ffsll((long long)~forbid) - 1);
+            if (t == (uint32_t)kSerialColour) { d.k_colour[k] = t; d.k_tent[k] = kSettled; }
+            else d.k_tent[k] = t;
         }
         grid_barrier(d.cnt);
         uint32_t left = 0;
         GRID_LOOP(k, n) {
             if (d.k_colour[k] != kNone) continue;
             const uint32_t t = __ldcg(&d.k_tent[k]);
-            if (t == (uint32_t)kSerialColour) continue;  // left to the serial colour
             uint32_t a, b;
             constraint_bodies(d, d.k_list[k], a, b);
             bool ok = true;
             const uint32_t bs[2] = {a, b};
             for (int e = 0; e < 2 && ok; ++e) {
                 const uint32_t x = bs[e];
-                if (!is_accelerable(d.b_flags[x])) continue;
+                if (!is_accelerable(d.b_flags[x]) || (e == 1 && b == a)) continue;
                 for (uint32_t q = d.inc_off[x]; q < d.inc_off[x + 1]; ++q) {
                     const uint32_t o = d.inc_list[q];
-                    if (o != k && colour_beats(d, o, k) && __ldcg(&d.k_colour[o]) == kNone &&
-                        (__ldcg(&d.k_tent[o]) & 0xffffu) == t) { ok = false; break; }
+                    if (o != k && __ldcg(&d.k_tent[o]) == t && colour_beats(d, o, k)) { ok = false; break; }
                 }
             }
-            if (ok) d.k_tent[k] = t | 0x40000000u;  // mark as accepted
+            if (ok) d.k_colour[k] = t;
             else ++left;
         }
-        if (left) atomicAdd(&d.cnt->colour_remaining, left);
+        if (left) atomicAdd(&rem[round % 3], left);
         grid_barrier(d.cnt);
-        GRID_LOOP(k, n) {
-            const uint32_t t = __ldcg(&d.k_tent[k]);
-            if (d.k_colour[k] == kNone && (t & 0x40000000u)) d.k_colour[k] = t & 0xffffu;
-        }
-        grid_barrier(d.cnt);
-        const uint32_t rem = *((volatile uint32_t*)&d.cnt->colour_remaining);
-        grid_barrier(d.cnt);
-        if (blockIdx.x == 0 && threadIdx.x == 0) d.cnt->colour_remaining = 0u;
-        grid_barrier(d.cnt);
-        if (rem == 0u) break;
+        if (*((volatile uint32_t*)&rem[round % 3]) == 0u) break;
     }
     GRID_LOOP(k, n) {
         if (d.k_colour[k] == kNone) d.k_colour[k] = (uint32_t)kSerialColour;
@@ -322,6 +339,11 @@ __global__ void k_colour(DW d) {
     GRID_LOOP(k, n) {
         const uint32_t c = d.k_colour[k];
         d.k_order[d.cnt->colour_off[c] + atomicAdd(&d.cnt->colour_cnt[c], 1u)] = k;
+        // remembered as next step's first choice
+        const uint32_t id = d.k_list[k];
+        const uint32_t keep = (c < (uint32_t)kMaxColours) ? c : kNone;
+        if (id & kJointBit) d.j_colour[id & ~kJointBit] = keep;
+        else d.cs_colour[id] = keep;
     }
 }
 

@@ -660,6 +660,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_imp, J);
     AL(d.c_key, C); AL(d.c_slot, C); AL(d.c_key_alt, C); AL(d.c_slot_alt, C); AL(d.free_stack, C);
     AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C);
+    AL(d.cs_colour, C); AL(d.j_colour, J);
     AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
     AL(d.n_key, K); AL(d.n_key_alt, K); AL(d.n_val, K); AL(d.n_val_alt, K);
     AL(d.l_key, S); AL(d.l_key_alt, S); AL(d.l_idx, S); AL(d.l_idx_alt, S); AL(d.l_leaf_box, S);
@@ -727,6 +728,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ok &= up(d.j_m1, j_zero.data(), sizeof(float4) * J);
     ok &= cudaMemsetAsync(d.b_uat, 0, sizeof(float) * N, w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.cnt, 0, sizeof(Counters), w->stream) == cudaSuccess;
+    ok &= cudaMemsetAsync(d.j_colour, 0xff, sizeof(uint32_t) * std::max<uint32_t>(J, 1), w->stream) == cudaSuccess;
     if (!ok) return bail(fail(w, PRGPU_ECUDA, "upload failed"));
     launch_init_bodies(d, w->L, w->stream);
     if (cudaStreamSynchronize(w->stream) != cudaSuccess) return bail(PRGPU_ECUDA);
