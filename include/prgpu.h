@@ -140,6 +140,15 @@ int prgpu_step_profiled(prgpu_world* w, const prgpu_step_conf* conf, float* phas
 int prgpu_last_step_phase_ms(prgpu_world* w, float* phase_ms, int n_phases);
 /* Number of kernel launches in one captured step. */
 int prgpu_graph_kernel_count(prgpu_world* w, uint32_t* n_kernels);
+/* How the colour sweeps of the regular solve are scheduled.  GRID: one
+ * cooperative launch over the whole batch, a grid barrier between colours.
+ * PER_WORLD: one CTA per world, worlds taken from a queue largest first, a
+ * block barrier between colours.  AUTO: PER_WORLD for batches of 64 worlds or
+ * more.  Both give the same results bit for bit.  No reference counterpart
+ * (the reference solves island by island on one thread). */
+enum { PRGPU_SWEEPS_AUTO = 0, PRGPU_SWEEPS_GRID = 1, PRGPU_SWEEPS_PER_WORLD = 2 };
+int prgpu_set_sweep_mode(prgpu_world* w, int mode);
+int prgpu_get_sweep_mode(prgpu_world* w, int* mode);
 /* Enqueues n steps on the handle's stream and returns at once. */
 int prgpu_step_async(prgpu_world* w, const prgpu_step_conf* conf, int n);
 int prgpu_synchronize(prgpu_world* w);

@@ -54,6 +54,7 @@ PR_HD bool is_accelerable(uint32_t f) { return (f & BF_TYPE_MASK) == 2u; }
 constexpr int kMaxColours = 64;      // colours 0..63 solved in parallel
 constexpr int kSerialColour = 64;    // leftover constraints solved by one thread
 constexpr int kMaxPosIters = 32;
+constexpr int kColStride = kSerialColour + 2;  // per-world colour table row
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr uint32_t kNone = 0xffffffffu;
 
@@ -112,6 +113,7 @@ struct Counters {
     float st_max_inc_impulse;
     uint32_t scan_total;
     uint32_t pad[7];
+    uint32_t world_queue;     // next entry of w_order for the per-world sweep kernel
     uint32_t lbvh_age;        // searches since the tree was last rebuilt (0: no tree yet)
     uint32_t lbvh_rebuild;    // this search rebuilds the tree (else refits it)
 };
@@ -134,6 +136,9 @@ struct DW {
     const uint32_t* w_body_off;
     const uint32_t* w_shape_off;
     uint32_t* w_root;        // LBVH root of each world (internal index or leaf | kLeafBit)
+    const uint32_t* w_order; // worlds by decreasing body count (work order of per-world sweeps)
+    uint32_t* w_coloff;      // [n_worlds * kColStride] constraint offsets per (world, colour)
+    uint32_t* w_colcnt;      // same shape: counts, then scatter cursors
     float4* w_bounds;        // centroid bounds for Morton codes (ordered-int encoded)
     // bodies
     float4* b_pos1;          // cx cy angle -

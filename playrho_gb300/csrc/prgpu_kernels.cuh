@@ -12,6 +12,8 @@ struct Launch {
     int grid;          // grid of element-wise (grid-stride) kernels
     int coop_grid;     // grid of the cooperative colouring / solver kernels
     int coop_threads;
+    bool per_world;    // sweeps run one CTA per world (batches of many worlds)
+    int world_grid;    // persistent CTAs of the per-world sweep kernel
 };
 
 // contacts / broadphase (prgpu_contacts.cu)
@@ -30,5 +32,6 @@ void launch_solve_finish(const DW& d, const Launch& L, cudaStream_t s);
 void launch_reset_step(const DW& d, const Launch& L, cudaStream_t s);
 void launch_clear_dirty(const DW& d, const Launch& L, cudaStream_t s);
 int coop_blocks_per_sm(int threads);
+int world_blocks_per_sm();
 
 }  // namespace prgpu

@@ -830,6 +830,18 @@ __device__ __forceinline__ bool island_done(const DW& d, uint32_t L, int it) {
     return false;
 }
 
+// Puts the serial colour's constraints in ascending index order, so their
+// one-thread Gauss-Seidel order does not depend on scatter atomics.  The
+// serial colour holds the few constraints the colouring gave up on.
+__device__ void sort_serial(uint32_t* a, uint32_t n) {
+    for (uint32_t i = 1; i < n; ++i) {
+        const uint32_t v = a[i];
+        uint32_t j = i;
+        while (j > 0 && a[j - 1] > v) { a[j] = a[j - 1]; --j; }
+        a[j] = v;
+    }
+}
+
 // The whole regular-phase solve of a step: warm start, velocity sweeps,
 // position integration, position sweeps, impulse store.  One cooperative
 // launch; a bounded grid barrier separates colours.
@@ -839,6 +851,7 @@ __global__ void k_solve(DW d) {
     const uint32_t* off = d.cnt->colour_off;
     const uint32_t nser = off[kSerialColour + 1] - off[kSerialColour];
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+    if (lead && nser) sort_serial(d.k_order + off[kSerialColour], nser);
 
     // warm start (contacts) and joint InitVelocity, colour by colour
     for (uint32_t col = 0; col <= ncol; ++col) {
@@ -949,6 +962,176 @@ __global__ void k_solve(DW d) {
             float4 p1 = d.m_p1[vc.slot];
             p1.z = vc.ni1; p1.w = vc.ti1;
             d.m_p1[vc.slot] = p1;
+        }
+    }
+}
+
+// ---- one CTA per world ---------------------------------------------------------
+// For batches of many worlds the colour sweeps run one world per CTA, so the
+// step between two colours is a __syncthreads instead of a grid barrier.  The
+// active constraints are first bucketed by (world, colour).
+__device__ __forceinline__ uint32_t constraint_world(const DW& d, uint32_t id) {
+    uint32_t a, b;
+    constraint_bodies(d, id, a, b);
+    return d.b_world[a];
+}
+
+__global__ void k_wbucket_count(DW d) {
+    GRID_LOOP(k, d.cnt->n_active) {
+        const uint32_t w = constraint_world(d, d.k_list[k]);
+        atomicAdd(&d.w_colcnt[(size_t)w * kColStride + d.k_colour[k]], 1u);
+    }
+}
+
+// One block: exclusive offsets of every (world, colour) bucket, world-major.
+__global__ void k_wbucket_offsets(DW d) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    if (threadIdx.x == 0) s_carry = 0u;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t w0 = 0; w0 < d.n_worlds; w0 += blockDim.x) {
+        const uint32_t w = w0 + threadIdx.x;
+        uint32_t tot = 0;
+        if (w < d.n_worlds)
+            for (int c = 0; c <= kSerialColour; ++c) tot += d.w_colcnt[(size_t)w * kColStride + c];
+        uint32_t x = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += t;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t v = (lane < (int)(blockDim.x >> 5)) ? s_warp[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += t;
+            }
+            if (lane < (int)(blockDim.x >> 5)) s_warp[lane] = v;
+        }
+        __syncthreads();
+        const uint32_t base = s_carry + x - tot + ((warp > 0) ? s_warp[warp - 1] : 0u);
+        if (w < d.n_worlds) {
+            uint32_t run = base;
+            for (int c = 0; c <= kSerialColour; ++c) {
+                const size_t at = (size_t)w * kColStride + c;
+                const uint32_t n = d.w_colcnt[at];
+                d.w_coloff[at] = run;
+                d.w_colcnt[at] = 0u;  // becomes the scatter cursor
+                run += n;
+            }
+            d.w_coloff[(size_t)w * kColStride + kSerialColour + 1] = run;
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) s_carry = base + tot;
+        __syncthreads();
+    }
+}
+
+__global__ void k_wbucket_scatter(DW d) {
+    GRID_LOOP(k, d.cnt->n_active) {
+        const uint32_t w = constraint_world(d, d.k_list[k]);
+        const size_t at = (size_t)w * kColStride + d.k_colour[k];
+        d.k_order[d.w_coloff[at] + atomicAdd(&d.w_colcnt[at], 1u)] = k;
+    }
+}
+
+// All sweeps of one world in one CTA; CTAs take worlds from a queue, largest
+// first.  Same per-constraint steps as k_solve, same order of colours.
+__global__ void __launch_bounds__(256) k_solve_world(DW d) {
+    const DConf& c = *d.conf;
+    __shared__ uint32_t s_w;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_w = atomicAdd(&d.cnt->world_queue, 1u);
+        __syncthreads();
+        const uint32_t qi = s_w;
+        if (qi >= d.n_worlds) return;
+        const uint32_t w = d.w_order[qi];
+        const uint32_t* off = d.w_coloff + (size_t)w * kColStride;
+        if (threadIdx.x == 0 && off[kSerialColour + 1] > off[kSerialColour])
+            sort_serial(d.k_order + off[kSerialColour], off[kSerialColour + 1] - off[kSerialColour]);
+        // Runs f(k) over colour col of this world, then synchronises the CTA.
+        auto sweep = [&](int col, auto&& f) {
+            const uint32_t lo = off[col], hi = off[col + 1];
+            if (lo == hi) return;
+            if (col == kSerialColour) {
+                if (threadIdx.x == 0)
+                    for (uint32_t t = lo; t < hi; ++t) f(d.k_order[t]);
+            } else {
+                for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) f(d.k_order[t]);
+            }
+            __syncthreads();
+        };
+        // warm start and joint InitVelocity
+        for (int col = 0; col <= kSerialColour; ++col) {
+            sweep(col, [&](uint32_t k) {
+                const uint32_t id = d.k_list[k];
+                if (id & kJointBit) joint_init_velocity(d, id & ~kJointBit);
+                else if (c.doWarmStart) warm_start(d, d.vc[k]);
+            });
+        }
+        // velocity iterations
+        for (int it = 0; it < c.regVelocityIters; ++it) {
+            for (int col = 0; col <= kSerialColour; ++col) {
+                sweep(col, [&](uint32_t k) {
+                    const uint32_t id = d.k_list[k];
+                    if (id & kJointBit) {
+                        joint_solve_velocity(d, id & ~kJointBit);
+                    } else {
+                        VC vc = d.vc[k];
+                        solve_contact_velocity(d, vc);
+                        reinterpret_cast<float4*>(&d.vc[k])[6] = make_float4(vc.ni0, vc.ti0, vc.ni1, vc.ti1);
+                    }
+                });
+            }
+        }
+        // IntegratePositions (AabbTreeWorld.cpp:176-188) for this world's bodies
+        const float h = c.deltaTime;
+        for (uint32_t b = d.w_body_off[w] + threadIdx.x; b < d.w_body_off[w + 1]; b += blockDim.x) {
+            if (!(d.b_flags[b] & BF_SOLVED)) continue;
+            const float4 v = d.b_vel[b];
+            float4 p = d.b_pos1[b];
+            const float tx = v.x * h, ty = v.y * h, rot = h * v.z;
+            p.x = p.x + tx; p.y = p.y + ty; p.z = p.z + rot;
+            d.b_pos1[b] = p;
+        }
+        __syncthreads();
+        // position iterations with the per-island early exit
+        for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it) {
+            for (int col = 0; col <= kSerialColour; ++col) {
+                sweep(col, [&](uint32_t k) {
+                    const uint32_t id = d.k_list[k];
+                    if (id & kJointBit) {
+                        const uint32_t j = id & ~kJointBit;
+                        const uint32_t L = joint_island(d, j);
+                        if (island_done(d, L, it)) return;
+                        if (!joint_solve_position(d, j)) d.isl_jok[(size_t)L * kMaxPosIters + it] = 0u;
+                    } else {
+                        const PC pc = d.pc[k];
+                        if (island_done(d, pc.island, it)) return;
+                        const float sep = solve_contact_position(d, pc);
+                        atomic_min_float(&d.isl_sep[(size_t)pc.island * kMaxPosIters + it], sep);
+                    }
+                });
+            }
+        }
+        // AssignImpulses (AabbTreeWorld.cpp:196-220)
+        for (uint32_t t = off[0] + threadIdx.x; t < off[kSerialColour + 1]; t += blockDim.x) {
+            const uint32_t k = d.k_order[t];
+            if (d.k_list[k] & kJointBit) continue;
+            const VC& vc = d.vc[k];
+            float4 p0 = d.m_p0[vc.slot];
+            p0.z = vc.ni0; p0.w = vc.ti0;
+            d.m_p0[vc.slot] = p0;
+            if (vc.count == 2u) {
+                float4 p1 = d.m_p1[vc.slot];
+                p1.z = vc.ni1; p1.w = vc.ti1;
+                d.m_p1[vc.slot] = p1;
+            }
         }
     }
 }
@@ -1097,7 +1280,24 @@ void launch_build_constraints(const DW& d, const Launch& L, cudaStream_t s) {
     k_build_constraints<<<L.grid, L.threads, 0, s>>>(d);
 }
 
-void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) { launch_coop(k_solve, d, L, s); }
+void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) {
+    if (!L.per_world) {
+        launch_coop(k_solve, d, L, s);
+        return;
+    }
+    cudaMemsetAsync(d.w_colcnt, 0, sizeof(uint32_t) * (size_t)d.n_worlds * kColStride, s);
+    cudaMemsetAsync(&d.cnt->world_queue, 0, sizeof(uint32_t), s);
+    k_wbucket_count<<<L.grid, L.threads, 0, s>>>(d);
+    k_wbucket_offsets<<<1, 1024, 0, s>>>(d);
+    k_wbucket_scatter<<<L.grid, L.threads, 0, s>>>(d);
+    k_solve_world<<<L.world_grid, 256, 0, s>>>(d);
+}
+
+int world_blocks_per_sm() {
+    int a = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_solve_world, 256, 0);
+    return a;
+}
 
 void launch_solve_finish(const DW& d, const Launch& L, cudaStream_t s) {
     k_body_end<<<L.grid, L.threads, 0, s>>>(d);

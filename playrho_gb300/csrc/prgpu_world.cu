@@ -374,6 +374,8 @@ int bits_for(uint64_t n) {
 
 // Phases of one step; `ev` (kPhases + 1 events) brackets them when profiling.
 constexpr int kPhases = 7;
+// Batches of at least this many worlds sweep one world per CTA by default.
+constexpr uint32_t kPerWorldMinWorlds = 64;
 
 int enqueue_step(prgpu_world* w, bool solve, cudaEvent_t* ev = nullptr, bool capturing = false) {
     const DW& d = w->d;
@@ -650,6 +652,9 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(w_body_off, W + 1); AL(w_shape_off, W + 1);
     d.w_body_off = w_body_off; d.w_shape_off = w_shape_off;
     AL(d.w_root, W); AL(d.w_bounds, W);
+    uint32_t* w_order;
+    AL(w_order, W); d.w_order = w_order;
+    AL(d.w_coloff, (size_t)W * kColStride); AL(d.w_colcnt, (size_t)W * kColStride);
     AL(d.b_pos1, N); AL(d.b_pos0, N); AL(d.b_vel, N); AL(d.b_xf, N); AL(d.b_mass, N); AL(d.b_acc, N);
     AL(d.b_damp, N); AL(d.b_flags, N); AL(d.b_uat, N); AL(d.b_world, N); AL(d.b_island, N);
     AL(d.b_jnt_off, N + 1); AL(d.b_jnt_other, jother.size()); AL(d.b_jnt_cc, jcc.size());
@@ -692,6 +697,19 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     const int per_sm = coop_blocks_per_sm(w->L.coop_threads);
     if (per_sm < 1) return bail(fail(w, PRGPU_ECUDA, "cooperative kernels cannot be resident"));
     w->L.coop_grid = w->L.prims.sm_count * std::min(per_sm, 4);
+    {
+        const int wps = world_blocks_per_sm();
+        if (wps < 1) return bail(fail(w, PRGPU_ECUDA, "per-world sweep kernel cannot be resident"));
+        w->L.world_grid = w->L.prims.sm_count * wps;
+        w->L.per_world = W >= kPerWorldMinWorlds;
+    }
+    // worlds by decreasing body count, ties by index: the per-world sweeps
+    // start the longest worlds first
+    std::vector<uint32_t> order(W);
+    for (uint32_t i = 0; i < W; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        return body_off[a + 1] - body_off[a] > body_off[b + 1] - body_off[b];
+    });
     if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(PRGPU_ECUDA);
     // ---- uploads
     auto up = [&](void* dst, const void* src, size_t bytes) -> bool {
@@ -700,6 +718,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     bool ok = true;
     ok &= up(w_body_off, body_off.data(), sizeof(uint32_t) * (W + 1));
     ok &= up(w_shape_off, shape_off.data(), sizeof(uint32_t) * (W + 1));
+    ok &= up(w_order, order.data(), sizeof(uint32_t) * W);
     ok &= up(d.b_pos1, pos1.data(), sizeof(float4) * N);
     ok &= up(d.b_vel, vel.data(), sizeof(float4) * N);
     ok &= up(d.b_mass, mass.data(), sizeof(float4) * N);
@@ -845,6 +864,27 @@ int prgpu_last_step_phase_ms(prgpu_world* w, float* phase_ms, int n_phases) {
         CU(cudaEventElapsedTime(&ms, w->graph_ev[a], w->graph_ev[b]));
         phase_ms[k] = ms;
     }
+    return PRGPU_OK;
+}
+
+int prgpu_set_sweep_mode(prgpu_world* w, int mode) {
+    if (!w) return PRGPU_EINVAL;
+    if (mode < PRGPU_SWEEPS_AUTO || mode > PRGPU_SWEEPS_PER_WORLD) return fail(w, PRGPU_EINVAL, "unknown sweep mode %d", mode);
+    const bool per_world = (mode == PRGPU_SWEEPS_AUTO) ? (w->d.n_worlds >= kPerWorldMinWorlds)
+                                                         : (mode == PRGPU_SWEEPS_PER_WORLD);
+    if (per_world == w->L.per_world) return PRGPU_OK;
+    CU(cudaSetDevice(w->device));
+    CU(cudaStreamSynchronize(w->stream));
+    // the captured step holds the old launches: capture again on the next step
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->graph_def) { cudaGraphDestroy(w->graph_def); w->graph_def = nullptr; }
+    w->L.per_world = per_world;
+    return PRGPU_OK;
+}
+
+int prgpu_get_sweep_mode(prgpu_world* w, int* mode) {
+    if (!w || !mode) return PRGPU_EINVAL;
+    *mode = w->L.per_world ? PRGPU_SWEEPS_PER_WORLD : PRGPU_SWEEPS_GRID;
     return PRGPU_OK;
 }
 

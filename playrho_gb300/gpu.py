@@ -92,6 +92,8 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_step_profiled.argtypes = [P, ctypes.POINTER(StepConf), P, I, ctypes.POINTER(StepStats)]
     lib.prgpu_last_step_phase_ms.argtypes = [P, P, I]
     lib.prgpu_graph_kernel_count.argtypes = [P, P]
+    lib.prgpu_set_sweep_mode.argtypes = [P, I]
+    lib.prgpu_get_sweep_mode.argtypes = [P, P]
     _LIB = lib
     return lib
 
@@ -102,7 +104,7 @@ def exported_symbols() -> List[str]:
         "prgpu_step", "prgpu_step_n", "prgpu_step_async", "prgpu_synchronize", "prgpu_get_counts",
         "prgpu_download_bodies", "prgpu_upload_body_states", "prgpu_download_contacts",
         "prgpu_download_proxies", "prgpu_last_error", "prgpu_convex_hull", "prgpu_prepare_bodies", "prgpu_step_profiled",
-        "prgpu_last_step_phase_ms", "prgpu_graph_kernel_count"]
+        "prgpu_last_step_phase_ms", "prgpu_graph_kernel_count", "prgpu_set_sweep_mode", "prgpu_get_sweep_mode"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -268,6 +270,18 @@ class GpuBatch:
         out = dict(zip(self.PHASES, ms[:-1].tolist()))
         out["step"] = float(ms[-1])
         return out
+
+    SWEEP_MODES = {"auto": 0, "grid": 1, "per_world": 2}
+
+    def set_sweep_mode(self, mode: str):
+        """'grid' (one cooperative launch, grid barrier per colour), 'per_world'
+        (one CTA per world) or 'auto'."""
+        self._check(self.lib.prgpu_set_sweep_mode(self.h, self.SWEEP_MODES[mode]), "prgpu_set_sweep_mode")
+
+    def sweep_mode(self) -> str:
+        m = ctypes.c_int(0)
+        self._check(self.lib.prgpu_get_sweep_mode(self.h, ctypes.byref(m)), "prgpu_get_sweep_mode")
+        return {v: k for k, v in self.SWEEP_MODES.items()}[m.value]
 
     def step_async(self, n: int, conf: StepConf):
         self._check(self.lib.prgpu_step_async(self.h, ctypes.byref(conf), int(n)), "prgpu_step_async")
