@@ -256,6 +256,11 @@ def run_ours(args, rank, world_size, local, dist):
     # then W warm-up steps.  The first step creates every proxy and contact, as
     # the reference's does.
     batch.step_n(args.settle, conf)
+    schedule = None
+    if args.sweeps == "auto":
+        # the autotuner times each candidate sweep schedule on the settled batch
+        # (those steps advance it, like settling steps) and keeps the fastest
+        schedule = batch.autotune(2, conf)
     for _ in range(max(3, args.warmup)):
         batch.step_n(1, conf)
     barrier(dist)
@@ -282,6 +287,7 @@ def run_ours(args, rank, world_size, local, dist):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "kernels_only": True,
                               "ms_per_step": statistics.mean(step_ms), "sweeps": batch.sweep_mode(),
+                              "warp_world_max_bodies": batch.warp_world_max_bodies(), "autotune": schedule,
                               "phase_ms": {k: statistics.mean(p[k] for p in phases) for k in phases[0]}}))
         return
     # e2e through the C ABI with host buffers (pinned), copies inside the timed region
@@ -344,7 +350,9 @@ def run_ours(args, rank, world_size, local, dist):
                    "settle_steps": args.settle,
                    "l2": "working set > 129 MB L2 (no flush needed)",
                    "live_contacts": st["liveContacts"], "active_constraints": st["activeConstraints"],
-                   "colours": st["colours"], "serial_constraints": st["serialConstraints"]},
+                   "colours": st["colours"], "serial_constraints": st["serialConstraints"],
+                   "schedule": {"sweeps": batch.sweep_mode(), "warp_world_max_bodies": batch.warp_world_max_bodies(),
+                                "autotuned": schedule is not None}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic,
                      "kernel": ("k_solve_world (Gauss-Seidel colour sweeps, one CTA per world)"

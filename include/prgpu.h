@@ -149,6 +149,22 @@ int prgpu_graph_kernel_count(prgpu_world* w, uint32_t* n_kernels);
 enum { PRGPU_SWEEPS_AUTO = 0, PRGPU_SWEEPS_GRID = 1, PRGPU_SWEEPS_PER_WORLD = 2 };
 int prgpu_set_sweep_mode(prgpu_world* w, int mode);
 int prgpu_get_sweep_mode(prgpu_world* w, int* mode);
+/* In PER_WORLD mode, worlds of at most this many bodies are swept by one warp
+ * (eight worlds at a time per CTA), larger ones by a whole CTA.  Default 256. */
+int prgpu_set_warp_world_max_bodies(prgpu_world* w, uint32_t max_bodies);
+int prgpu_get_warp_world_max_bodies(prgpu_world* w, uint32_t* max_bodies);
+/* A sweep schedule and its measured device time per step. */
+typedef struct prgpu_schedule {
+    int32_t sweep_mode;               /* PRGPU_SWEEPS_GRID or PRGPU_SWEEPS_PER_WORLD */
+    uint32_t warp_world_max_bodies;
+    float step_ms;
+} prgpu_schedule;
+/* Autotuner: times every candidate schedule over steps_per_candidate steps
+ * (after one untimed step that captures it) and keeps the fastest.  The
+ * schedules give identical results, so the only effect on the simulation is
+ * that the world advances (1 + steps_per_candidate) steps per candidate, as
+ * with prgpu_step_n.  No reference counterpart. */
+int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_candidate, prgpu_schedule* best);
 /* Enqueues n steps on the handle's stream and returns at once. */
 int prgpu_step_async(prgpu_world* w, const prgpu_step_conf* conf, int n);
 int prgpu_synchronize(prgpu_world* w);

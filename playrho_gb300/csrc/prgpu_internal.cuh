@@ -54,7 +54,7 @@ PR_HD bool is_accelerable(uint32_t f) { return (f & BF_TYPE_MASK) == 2u; }
 constexpr int kMaxColours = 64;      // colours 0..63 solved in parallel
 constexpr int kSerialColour = 64;    // leftover constraints solved by one thread
 constexpr int kMaxPosIters = 32;
-constexpr int kColStride = kSerialColour + 2;  // per-world colour table row
+constexpr int kColStride = kSerialColour + 2;  // colour table of one world: offsets 0..65
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr uint32_t kNone = 0xffffffffu;
 
@@ -137,8 +137,9 @@ struct DW {
     const uint32_t* w_shape_off;
     uint32_t* w_root;        // LBVH root of each world (internal index or leaf | kLeafBit)
     const uint32_t* w_order; // worlds by decreasing body count (work order of per-world sweeps)
-    uint32_t* w_coloff;      // [n_worlds * kColStride] constraint offsets per (world, colour)
-    uint32_t* w_colcnt;      // same shape: counts, then scatter cursors
+    uint32_t* w_kc;          // [n_worlds + 1] first active contact (index into k_list) of each world
+    uint32_t* w_kj;          // [n_worlds + 1] first active joint of each world
+    uint32_t n_world_big;    // leading entries of w_order swept by a whole CTA (the rest by a warp)
     float4* w_bounds;        // centroid bounds for Morton codes (ordered-int encoded)
     // bodies
     float4* b_pos1;          // cx cy angle -
@@ -221,7 +222,8 @@ struct DW {
     uint32_t* k_colour;
     uint32_t* k_tent;
     uint32_t* k_prio;        // colouring priority (hash of world-local identifiers)
-    uint32_t* k_order;       // constraint indices bucketed by colour
+    uint32_t* k_order;       // constraint indices bucketed by colour (the sweep order)
+    uint32_t* t_id;          // constraint id (k_list entry) at each sweep position; vc/pc share its indexing
     uint32_t* inc_off;       // body -> active constraint incidence CSR
     uint32_t* inc_cur;
     uint32_t* inc_list;

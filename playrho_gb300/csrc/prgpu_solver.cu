@@ -169,6 +169,8 @@ __global__ void k_active_scatter(DW d) {
 __global__ void k_active_done(DW d, uint32_t* n_bodies_count) {
     Counters* c = d.cnt;
     c->n_active = c->scan_total;
+    const uint32_t nl = c->n_live;
+    c->n_active_c = nl ? d.scan[nl - 1] + d.flags[nl - 1] : 0u;
     c->n_colours = 0u;
     c->colour_remaining = 0u;
     for (int k = 0; k < kSerialColour + 2; ++k) { c->colour_cnt[k] = 0u; c->colour_off[k] = 0u; }
@@ -249,71 +251,93 @@ __device__ __forceinline__ uint32_t colour_hint(const DW& d, uint32_t id) {
     return (id & kJointBit) ? d.j_colour[id & ~kJointBit] : d.cs_colour[id];
 }
 
-// Two grid barriers per round.  Phase T: every uncoloured constraint picks a
-// tentative colour from its neighbours' committed colours (in the first round
-// the colour it had last step, if still free); constraints coloured earlier
-// mark their tentative slot as settled.  Phase C: a constraint keeps its pick
-// unless an uncoloured neighbour of higher priority picked the same colour, and
-// commits it at once (phase C reads only tentative picks, never commits).
+// Puts the serial colour's constraints in ascending index order, so their
+// one-thread Gauss-Seidel order does not depend on scatter atomics.  The
+// serial colour holds the few constraints the colouring gave up on.
+__device__ void sort_serial(uint32_t* a, uint32_t n) {
+    for (uint32_t i = 1; i < n; ++i) {
+        const uint32_t v = a[i];
+        uint32_t j = i;
+        while (j > 0 && a[j - 1] > v) { a[j] = a[j - 1]; --j; }
+        a[j] = v;
+    }
+}
+
+// Two barriers per round.  Phase T (colour_pick): every uncoloured constraint
+// picks a tentative colour from its neighbours' committed colours (in the first
+// round the colour it had last step, if still free); constraints coloured
+// earlier mark their tentative slot as settled.  Phase C (colour_keep): a
+// constraint keeps its pick unless an uncoloured neighbour of higher priority
+// picked the same colour, and commits it at once (phase C reads only tentative
+// picks, never commits).  Each round depends only on the previous one, so the
+// colouring is the same whether a world is coloured by the whole grid (k_colour)
+// or by one CTA or warp of its own (k_world_solve).
+constexpr uint32_t kSettled = 0xffffffffu;
+
+__device__ __forceinline__ void colour_init(const DW& d, uint32_t k) {
+    d.k_prio[k] = constraint_prio(d, d.k_list[k]);
+    d.k_tent[k] = kSettled;
+}
+
+__device__ __forceinline__ void colour_pick(const DW& d, uint32_t k, int round) {
+    const uint32_t ck = d.k_colour[k];
+    if (ck != kNone) {
+        if (d.k_tent[k] != kSettled) d.k_tent[k] = kSettled;
+        return;
+    }
+    uint32_t a, b;
+    const uint32_t id = d.k_list[k];
+    constraint_bodies(d, id, a, b);
+    uint64_t forbid = 0;
+    const uint32_t bs[2] = {a, b};
+    for (int e = 0; e < 2; ++e) {
+        const uint32_t x = bs[e];
+        if (!is_accelerable(d.b_flags[x]) || (e == 1 && b == a)) continue;
+        for (uint32_t t = d.inc_off[x]; t < d.inc_off[x + 1]; ++t) {
+            const uint32_t c = __ldcg(&d.k_colour[d.inc_list[t]]);
+            if (c < (uint32_t)kMaxColours) forbid |= 1ull << c;
+        }
+    }
+    uint32_t t;
+    const uint32_t hint = (round == 0) ? colour_hint(d, id) : kNone;
+    if (hint < (uint32_t)kMaxColours && !((forbid >> hint) & 1ull)) t = hint;
+    else if (forbid == ~0ull) t = (uint32_t)kSerialColour;
+    else t = (uint32_t)(__ffsll((long long)~forbid) - 1);
+    if (t == (uint32_t)kSerialColour) { d.k_colour[k] = t; d.k_tent[k] = kSettled; }
+    else d.k_tent[k] = t;
+}
+
+// Returns whether k is still uncoloured after this round.
+__device__ __forceinline__ bool colour_keep(const DW& d, uint32_t k) {
+    if (d.k_colour[k] != kNone) return false;
+    const uint32_t t = __ldcg(&d.k_tent[k]);
+    uint32_t a, b;
+    constraint_bodies(d, d.k_list[k], a, b);
+    const uint32_t bs[2] = {a, b};
+    for (int e = 0; e < 2; ++e) {
+        const uint32_t x = bs[e];
+        if (!is_accelerable(d.b_flags[x]) || (e == 1 && b == a)) continue;
+        for (uint32_t q = d.inc_off[x]; q < d.inc_off[x + 1]; ++q) {
+            const uint32_t o = d.inc_list[q];
+            if (o != k && __ldcg(&d.k_tent[o]) == t && colour_beats(d, o, k)) return true;
+        }
+    }
+    d.k_colour[k] = t;
+    return false;
+}
+
 __global__ void k_colour(DW d) {
-    constexpr uint32_t kSettled = 0xffffffffu;
     const uint32_t n = d.cnt->n_active;
     uint32_t* rem = &d.cnt->pad[4];  // triple-buffered per-round counters
-    GRID_LOOP(k, n) {
-        d.k_prio[k] = constraint_prio(d, d.k_list[k]);
-        d.k_tent[k] = kSettled;
-    }
+    GRID_LOOP(k, n) colour_init(d, k);
     if (blockIdx.x == 0 && threadIdx.x == 0) { rem[0] = 0u; rem[1] = 0u; rem[2] = 0u; }
     grid_barrier(d.cnt);
     for (int round = 0; round < kMaxColourRounds; ++round) {
         if (blockIdx.x == 0 && threadIdx.x == 0) rem[(round + 1) % 3] = 0u;
-        GRID_LOOP(k, n) {
-            const uint32_t ck = d.k_colour[k];
-            if (ck != kNone) {
-                if (d.k_tent[k] != kSettled) d.k_tent[k] = kSettled;
-                continue;
-            }
-            uint32_t a, b;
-            const uint32_t id = d.k_list[k];
-            constraint_bodies(d, id, a, b);
-            uint64_t forbid = 0;
-            const uint32_t bs[2] = {a, b};
-            for (int e = 0; e < 2; ++e) {
-                const uint32_t x = bs[e];
-                if (!is_accelerable(d.b_flags[x]) || (e == 1 && b == a)) continue;
-                for (uint32_t t = d.inc_off[x]; t < d.inc_off[x + 1]; ++t) {
-                    const uint32_t c = __ldcg(&d.k_colour[d.inc_list[t]]);
-                    if (c < (uint32_t)kMaxColours) forbid |= 1ull << c;
-                }
-            }
-            uint32_t t;
-            const uint32_t hint = (round == 0) ? colour_hint(d, id) : kNone;
-            if (hint < (uint32_t)kMaxColours && !((forbid >> hint) & 1ull)) t = hint;
-            else if (forbid == ~0ull) t = (uint32_t)kSerialColour;
-            else t = (uint32_t)(__ffsll((long long)~forbid) - 1);
-            if (t == (uint32_t)kSerialColour) { d.k_colour[k] = t; d.k_tent[k] = kSettled; }
-            else d.k_tent[k] = t;
-        }
+        GRID_LOOP(k, n) colour_pick(d, k, round);
         grid_barrier(d.cnt);
         uint32_t left = 0;
-        GRID_LOOP(k, n) {
-            if (d.k_colour[k] != kNone) continue;
-            const uint32_t t = __ldcg(&d.k_tent[k]);
-            uint32_t a, b;
-            constraint_bodies(d, d.k_list[k], a, b);
-            bool ok = true;
-            const uint32_t bs[2] = {a, b};
-            for (int e = 0; e < 2 && ok; ++e) {
-                const uint32_t x = bs[e];
-                if (!is_accelerable(d.b_flags[x]) || (e == 1 && b == a)) continue;
-                for (uint32_t q = d.inc_off[x]; q < d.inc_off[x + 1]; ++q) {
-                    const uint32_t o = d.inc_list[q];
-                    if (o != k && __ldcg(&d.k_tent[o]) == t && colour_beats(d, o, k)) { ok = false; break; }
-                }
-            }
-            if (ok) d.k_colour[k] = t;
-            else ++left;
-        }
+        GRID_LOOP(k, n) left += colour_keep(d, k) ? 1u : 0u;
         if (left) atomicAdd(&rem[round % 3], left);
         grid_barrier(d.cnt);
         if (*((volatile uint32_t*)&rem[round % 3]) == 0u) break;
@@ -345,16 +369,23 @@ __global__ void k_colour(DW d) {
         if (id & kJointBit) d.j_colour[id & ~kJointBit] = keep;
         else d.cs_colour[id] = keep;
     }
+    grid_barrier(d.cnt);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint32_t lo = d.cnt->colour_off[kSerialColour], hi = d.cnt->colour_off[kSerialColour + 1];
+        if (hi > lo) sort_serial(d.k_order + lo, hi - lo);
+    }
 }
 
 // ---- constraint construction --------------------------------------------------
 // GetWorldManifold (WorldManifold.cpp:111-132), VelocityConstraint ctor +
 // GetPoint + ComputeK (VelocityConstraint.cpp:38-185), PositionConstraint.
-__global__ void k_build_constraints(DW d) {
+// Builds the constraint at sweep position t (vc[t], pc[t]) for constraint k.
+__device__ void build_constraint(const DW& d, uint32_t t, uint32_t k) {
     const DConf& c = *d.conf;
-    GRID_LOOP(k, d.cnt->n_active) {
+    {
         const uint32_t id = d.k_list[k];
-        if (id & kJointBit) continue;
+        d.t_id[t] = id;
+        if (id & kJointBit) return;
         const uint32_t slot = id;
         const uint2 bd = d.cs_body[slot];
         const uint2 pr = d.cs_proxy[slot];
@@ -463,15 +494,20 @@ __global__ void k_build_constraints(DW d) {
         }
         vc.k00 = k00; vc.k11 = k11; vc.k01 = k01; vc.m00 = m00; vc.m11 = m11; vc.m01 = m01;
         vc.pad0 = vc.pad1 = vc.pad2 = 0u;
-        d.vc[k] = vc;
+        d.vc[t] = vc;
         PC pcs;
         pcs.lnx = ln.x; pcs.lny = ln.y; pcs.lpx = lp.x; pcs.lpy = lp.y;
         pcs.p0x = plp[0].x; pcs.p0y = plp[0].y; pcs.p1x = plp[1].x; pcs.p1y = plp[1].y;
         pcs.totalRadius = rA + rB;
         pcs.type = (uint32_t)type; pcs.count = (uint32_t)count; pcs.bA = bd.x; pcs.bB = bd.y;
         pcs.island = vc.island; pcs.pad0 = pcs.pad1 = 0u;
-        d.pc[k] = pcs;
+        d.pc[t] = pcs;
     }
+}
+
+// Constraints are stored in sweep order: position t of k_order.
+__global__ void k_build_constraints(DW d) {
+    GRID_LOOP(t, d.cnt->n_active) build_constraint(d, t, d.k_order[t]);
 }
 
 // ---- per-constraint solver steps --------------------------------------------
@@ -830,309 +866,252 @@ __device__ __forceinline__ bool island_done(const DW& d, uint32_t L, int it) {
     return false;
 }
 
-// Puts the serial colour's constraints in ascending index order, so their
-// one-thread Gauss-Seidel order does not depend on scatter atomics.  The
-// serial colour holds the few constraints the colouring gave up on.
-__device__ void sort_serial(uint32_t* a, uint32_t n) {
-    for (uint32_t i = 1; i < n; ++i) {
-        const uint32_t v = a[i];
-        uint32_t j = i;
-        while (j > 0 && a[j - 1] > v) { a[j] = a[j - 1]; --j; }
-        a[j] = v;
+// ---- per-constraint sweep steps (t = position in sweep order) -------------------
+__device__ __forceinline__ void sweep_warm(const DW& d, uint32_t t) {
+    const uint32_t id = d.t_id[t];
+    if (id & kJointBit) joint_init_velocity(d, id & ~kJointBit);
+    else if (d.conf->doWarmStart) warm_start(d, d.vc[t]);
+}
+
+__device__ __forceinline__ void sweep_velocity(const DW& d, uint32_t t) {
+    const uint32_t id = d.t_id[t];
+    if (id & kJointBit) {
+        joint_solve_velocity(d, id & ~kJointBit);
+    } else {
+        VC vc = d.vc[t];
+        solve_contact_velocity(d, vc);
+        reinterpret_cast<float4*>(&d.vc[t])[6] = make_float4(vc.ni0, vc.ti0, vc.ni1, vc.ti1);
     }
 }
 
-// The whole regular-phase solve of a step: warm start, velocity sweeps,
-// position integration, position sweeps, impulse store.  One cooperative
-// launch; a bounded grid barrier separates colours.
+__device__ __forceinline__ void sweep_position(const DW& d, uint32_t t, int it) {
+    const uint32_t id = d.t_id[t];
+    if (id & kJointBit) {
+        const uint32_t j = id & ~kJointBit;
+        const uint32_t L = joint_island(d, j);
+        if (island_done(d, L, it)) return;
+        if (!joint_solve_position(d, j)) d.isl_jok[(size_t)L * kMaxPosIters + it] = 0u;
+    } else {
+        const PC pc = d.pc[t];
+        if (island_done(d, pc.island, it)) return;
+        const float sep = solve_contact_position(d, pc);
+        atomic_min_float(&d.isl_sep[(size_t)pc.island * kMaxPosIters + it], sep);
+    }
+}
+
+// AssignImpulses (AabbTreeWorld.cpp:196-220)
+__device__ __forceinline__ void store_impulses(const DW& d, uint32_t t) {
+    if (d.t_id[t] & kJointBit) return;
+    const VC& vc = d.vc[t];
+    float4 p0 = d.m_p0[vc.slot];
+    p0.z = vc.ni0; p0.w = vc.ti0;
+    d.m_p0[vc.slot] = p0;
+    if (vc.count == 2u) {
+        float4 p1 = d.m_p1[vc.slot];
+        p1.z = vc.ni1; p1.w = vc.ti1;
+        d.m_p1[vc.slot] = p1;
+    }
+}
+
+// IntegratePositions (AabbTreeWorld.cpp:176-188)
+__device__ __forceinline__ void integrate_body(const DW& d, uint32_t b) {
+    if (!(d.b_flags[b] & BF_SOLVED)) return;
+    const float h = d.conf->deltaTime;
+    const float4 v = d.b_vel[b];
+    float4 p = d.b_pos1[b];
+    const float tx = v.x * h, ty = v.y * h, rot = h * v.z;
+    p.x = p.x + tx; p.y = p.y + ty; p.z = p.z + rot;
+    d.b_pos1[b] = p;
+}
+
+// The whole regular-phase solve of a step over the batch: warm start, velocity
+// sweeps, position integration, position sweeps, impulse store.  One
+// cooperative launch; a bounded grid barrier separates colours; the serial
+// colour runs on one thread.
 __global__ void k_solve(DW d) {
     const DConf& c = *d.conf;
-    const uint32_t ncol = d.cnt->n_colours;
     const uint32_t* off = d.cnt->colour_off;
-    const uint32_t nser = off[kSerialColour + 1] - off[kSerialColour];
+    const uint32_t ncol = d.cnt->n_colours;
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
-    if (lead && nser) sort_serial(d.k_order + off[kSerialColour], nser);
-
-    // warm start (contacts) and joint InitVelocity, colour by colour
-    for (uint32_t col = 0; col <= ncol; ++col) {
+    auto sweep = [&](uint32_t col, auto&& f) {
         const bool serial = (col == ncol);
         const uint32_t lo = serial ? off[kSerialColour] : off[col];
-        const uint32_t n = serial ? nser : off[col + 1] - off[col];
-        if (serial && !n) break;
+        const uint32_t hi = serial ? off[kSerialColour + 1] : off[col + 1];
+        if (lo == hi) return;
         if (serial) {
-            if (lead) {
-                for (uint32_t t = 0; t < n; ++t) {
-                    const uint32_t k = d.k_order[lo + t];
-                    const uint32_t id = d.k_list[k];
-                    if (id & kJointBit) joint_init_velocity(d, id & ~kJointBit);
-                    else if (c.doWarmStart) warm_start(d, d.vc[k]);
-                }
-            }
+            if (lead) for (uint32_t t = lo; t < hi; ++t) f(t);
         } else {
-            GRID_LOOP(t, n) {
-                const uint32_t k = d.k_order[lo + t];
-                const uint32_t id = d.k_list[k];
-                if (id & kJointBit) joint_init_velocity(d, id & ~kJointBit);
-                else if (c.doWarmStart) warm_start(d, d.vc[k]);
-            }
+            GRID_LOOP(i, hi - lo) f(lo + i);
         }
         grid_barrier(d.cnt);
-    }
-    // velocity iterations
-    for (int it = 0; it < c.regVelocityIters; ++it) {
-        for (uint32_t col = 0; col <= ncol; ++col) {
-            const bool serial = (col == ncol);
-            const uint32_t lo = serial ? off[kSerialColour] : off[col];
-            const uint32_t n = serial ? nser : off[col + 1] - off[col];
-            if (serial && !n) break;
-            if (serial) {
-                if (lead) {
-                    for (uint32_t t = 0; t < n; ++t) {
-                        const uint32_t k = d.k_order[lo + t];
-                        const uint32_t id = d.k_list[k];
-                        if (id & kJointBit) joint_solve_velocity(d, id & ~kJointBit);
-                        else { VC vc = d.vc[k]; solve_contact_velocity(d, vc); d.vc[k] = vc; }
-                    }
-                }
-            } else {
-                GRID_LOOP(t, n) {
-                    const uint32_t k = d.k_order[lo + t];
-                    const uint32_t id = d.k_list[k];
-                    if (id & kJointBit) joint_solve_velocity(d, id & ~kJointBit);
-                    else {
-                        VC vc = d.vc[k];
-                        solve_contact_velocity(d, vc);
-                        reinterpret_cast<float4*>(&d.vc[k])[6] = make_float4(vc.ni0, vc.ti0, vc.ni1, vc.ti1);
-                    }
-                }
-            }
-            grid_barrier(d.cnt);
-        }
-    }
-    // IntegratePositions (AabbTreeWorld.cpp:176-188)
-    const float h = c.deltaTime;
-    GRID_LOOP(b, d.n_bodies) {
-        if (!(d.b_flags[b] & BF_SOLVED)) continue;
-        const float4 v = d.b_vel[b];
-        float4 p = d.b_pos1[b];
-        const float tx = v.x * h, ty = v.y * h, rot = h * v.z;
-        p.x = p.x + tx; p.y = p.y + ty; p.z = p.z + rot;
-        d.b_pos1[b] = p;
-    }
+    };
+    for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_warm(d, t); });
+    for (int it = 0; it < c.regVelocityIters; ++it)
+        for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, t); });
+    GRID_LOOP(b, d.n_bodies) integrate_body(d, b);
     grid_barrier(d.cnt);
-    // position iterations with per-island early exit
-    for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it) {
-        for (uint32_t col = 0; col <= ncol; ++col) {
-            const bool serial = (col == ncol);
-            const uint32_t lo = serial ? off[kSerialColour] : off[col];
-            const uint32_t n = serial ? nser : off[col + 1] - off[col];
-            if (serial && !n) break;
-            auto body = [&](uint32_t t) {
-                const uint32_t k = d.k_order[lo + t];
-                const uint32_t id = d.k_list[k];
-                if (id & kJointBit) {
-                    const uint32_t j = id & ~kJointBit;
-                    const uint32_t L = joint_island(d, j);
-                    if (island_done(d, L, it)) return;
-                    if (!joint_solve_position(d, j)) d.isl_jok[(size_t)L * kMaxPosIters + it] = 0u;
-                } else {
-                    const PC pc = d.pc[k];
-                    if (island_done(d, pc.island, it)) return;
-                    const float sep = solve_contact_position(d, pc);
-                    atomic_min_float(&d.isl_sep[(size_t)pc.island * kMaxPosIters + it], sep);
-                }
-            };
-            if (serial) {
-                if (lead) for (uint32_t t = 0; t < n; ++t) body(t);
-            } else {
-                GRID_LOOP(t, n) body(t);
-            }
-            grid_barrier(d.cnt);
-        }
-    }
-    // AssignImpulses (AabbTreeWorld.cpp:196-220)
-    GRID_LOOP(k, d.cnt->n_active) {
-        const uint32_t id = d.k_list[k];
-        if (id & kJointBit) continue;
-        const VC& vc = d.vc[k];
-        float4 p0 = d.m_p0[vc.slot];
-        p0.z = vc.ni0; p0.w = vc.ti0;
-        d.m_p0[vc.slot] = p0;
-        if (vc.count == 2u) {
-            float4 p1 = d.m_p1[vc.slot];
-            p1.z = vc.ni1; p1.w = vc.ti1;
-            d.m_p1[vc.slot] = p1;
-        }
-    }
+    for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it)
+        for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_position(d, t, it); });
+    GRID_LOOP(t, d.cnt->n_active) store_impulses(d, t);
 }
 
-// ---- one CTA per world ---------------------------------------------------------
-// For batches of many worlds the colour sweeps run one world per CTA, so the
-// step between two colours is a __syncthreads instead of a grid barrier.  The
-// active constraints are first bucketed by (world, colour).
+// ---- one group of threads per world --------------------------------------------
+// For batches of many worlds, a CTA (large worlds) or a warp (small ones) does
+// all of one world's solve: colouring (the same rounds as k_colour, with group
+// barriers), bucketing by colour, constraint construction and the sweeps, with
+// a group barrier between two colours instead of a grid barrier.
+//
+// The active constraint lists are world-major (contact keys sort by proxy, and
+// proxies are numbered world by world; joints likewise), so world w owns the
+// contacts k in [w_kc[w], w_kc[w+1]) and the joints k in [w_kj[w], w_kj[w+1]).
 __device__ __forceinline__ uint32_t constraint_world(const DW& d, uint32_t id) {
     uint32_t a, b;
     constraint_bodies(d, id, a, b);
     return d.b_world[a];
 }
 
-__global__ void k_wbucket_count(DW d) {
-    GRID_LOOP(k, d.cnt->n_active) {
-        const uint32_t w = constraint_world(d, d.k_list[k]);
-        atomicAdd(&d.w_colcnt[(size_t)w * kColStride + d.k_colour[k]], 1u);
+__global__ void k_world_ranges(DW d) {
+    const uint32_t nc = d.cnt->n_active_c, na = d.cnt->n_active;
+    GRID_LOOP(w, d.n_worlds + 1) {
+        uint32_t lo = 0, hi = nc;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (constraint_world(d, d.k_list[mid]) < w) lo = mid + 1; else hi = mid;
+        }
+        d.w_kc[w] = lo;
+        lo = nc; hi = na;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (constraint_world(d, d.k_list[mid]) < w) lo = mid + 1; else hi = mid;
+        }
+        d.w_kj[w] = lo;
     }
 }
 
-// One block: exclusive offsets of every (world, colour) bucket, world-major.
-__global__ void k_wbucket_offsets(DW d) {
-    __shared__ uint32_t s_warp[32];
-    __shared__ uint32_t s_carry;
-    if (threadIdx.x == 0) s_carry = 0u;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (uint32_t w0 = 0; w0 < d.n_worlds; w0 += blockDim.x) {
-        const uint32_t w = w0 + threadIdx.x;
-        uint32_t tot = 0;
-        if (w < d.n_worlds)
-            for (int c = 0; c <= kSerialColour; ++c) tot += d.w_colcnt[(size_t)w * kColStride + c];
-        uint32_t x = tot;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += t;
-        }
-        if (lane == 31) s_warp[warp] = x;
-        __syncthreads();
-        if (warp == 0) {
-            uint32_t v = (lane < (int)(blockDim.x >> 5)) ? s_warp[lane] : 0u;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
-                if (lane >= o) v += t;
-            }
-            if (lane < (int)(blockDim.x >> 5)) s_warp[lane] = v;
-        }
-        __syncthreads();
-        const uint32_t base = s_carry + x - tot + ((warp > 0) ? s_warp[warp - 1] : 0u);
-        if (w < d.n_worlds) {
-            uint32_t run = base;
-            for (int c = 0; c <= kSerialColour; ++c) {
-                const size_t at = (size_t)w * kColStride + c;
-                const uint32_t n = d.w_colcnt[at];
-                d.w_coloff[at] = run;
-                d.w_colcnt[at] = 0u;  // becomes the scatter cursor
-                run += n;
-            }
-            d.w_coloff[(size_t)w * kColStride + kSerialColour + 1] = run;
-        }
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) s_carry = base + tot;
-        __syncthreads();
+struct BlockGroup {
+    __device__ __forceinline__ static void sync() { __syncthreads(); }
+    __device__ __forceinline__ static bool any(bool p) { return __syncthreads_or(p) != 0; }
+};
+struct WarpGroup {
+    __device__ __forceinline__ static void sync() { __syncwarp(); }
+    __device__ __forceinline__ static bool any(bool p) {
+        __syncwarp();
+        return __any_sync(0xffffffffu, p) != 0;
     }
-}
+};
 
-__global__ void k_wbucket_scatter(DW d) {
-    GRID_LOOP(k, d.cnt->n_active) {
-        const uint32_t w = constraint_world(d, d.k_list[k]);
-        const size_t at = (size_t)w * kColStride + d.k_colour[k];
-        d.k_order[d.w_coloff[at] + atomicAdd(&d.w_colcnt[at], 1u)] = k;
-    }
-}
-
-// All sweeps of one world in one CTA; CTAs take worlds from a queue, largest
-// first.  Same per-constraint steps as k_solve, same order of colours.
-__global__ void __launch_bounds__(256) k_solve_world(DW d) {
+// col_cnt / col_off: kColStride words of shared memory owned by the group.
+template <class G>
+__device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t size, uint32_t* col_cnt,
+                            uint32_t* col_off) {
     const DConf& c = *d.conf;
+    const uint32_t c0 = d.w_kc[w], c1 = d.w_kc[w + 1], j0 = d.w_kj[w], j1 = d.w_kj[w + 1];
+    const uint32_t ncw = c1 - c0, n = ncw + (j1 - j0);
+    const uint32_t base = c0 + (j0 - d.cnt->n_active_c);  // this world's segment of sweep order
+    auto kof = [&](uint32_t i) { return (i < ncw) ? c0 + i : j0 + (i - ncw); };
+    if (n) {
+        // colouring
+        for (uint32_t i = rank; i < n; i += size) colour_init(d, kof(i));
+        for (uint32_t i = rank; i < (uint32_t)kColStride; i += size) col_cnt[i] = 0u;
+        G::sync();
+        for (int round = 0; round < kMaxColourRounds; ++round) {
+            for (uint32_t i = rank; i < n; i += size) colour_pick(d, kof(i), round);
+            G::sync();
+            bool left = false;
+            for (uint32_t i = rank; i < n; i += size) left |= colour_keep(d, kof(i));
+            if (!G::any(left)) break;
+        }
+        // buckets by colour; what is left goes to the serial colour
+        for (uint32_t i = rank; i < n; i += size) {
+            const uint32_t k = kof(i);
+            uint32_t col = d.k_colour[k];
+            if (col == kNone) { col = (uint32_t)kSerialColour; d.k_colour[k] = col; }
+            atomicAdd(&col_cnt[col], 1u);
+        }
+        G::sync();
+        if (rank == 0) {
+            uint32_t o = 0, used = 0;
+            for (int k = 0; k <= kSerialColour; ++k) {
+                col_off[k] = o;
+                o += col_cnt[k];
+                if (k < kSerialColour && col_cnt[k]) used = (uint32_t)k + 1u;
+                col_cnt[k] = 0u;
+            }
+            col_off[kSerialColour + 1] = o;
+            if (used) atomicMax(&d.cnt->n_colours, used);
+            const uint32_t nser = o - col_off[kSerialColour];
+            if (nser) atomicAdd(&d.cnt->colour_off[kSerialColour + 1], nser);
+        }
+        G::sync();
+        for (uint32_t i = rank; i < n; i += size) {
+            const uint32_t k = kof(i);
+            const uint32_t col = d.k_colour[k];
+            d.k_order[base + col_off[col] + atomicAdd(&col_cnt[col], 1u)] = k;
+            // remembered as next step's first choice
+            const uint32_t id = d.k_list[k];
+            const uint32_t keep = (col < (uint32_t)kMaxColours) ? col : kNone;
+            if (id & kJointBit) d.j_colour[id & ~kJointBit] = keep;
+            else d.cs_colour[id] = keep;
+        }
+        G::sync();
+        if (rank == 0 && col_off[kSerialColour + 1] > col_off[kSerialColour])
+            sort_serial(d.k_order + base + col_off[kSerialColour], col_off[kSerialColour + 1] - col_off[kSerialColour]);
+        G::sync();
+        for (uint32_t t = base + rank; t < base + n; t += size) build_constraint(d, t, d.k_order[t]);
+        G::sync();
+    }
+    // Runs f(t) over colour col of this world, then synchronises the group.
+    auto sweep = [&](int col, auto&& f) {
+        const uint32_t lo = base + col_off[col], hi = base + col_off[col + 1];
+        if (lo == hi) return;
+        if (col == kSerialColour) {
+            if (rank == 0) for (uint32_t t = lo; t < hi; ++t) f(t);
+        } else {
+            for (uint32_t t = lo + rank; t < hi; t += size) f(t);
+        }
+        G::sync();
+    };
+    if (n) {
+        for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_warm(d, t); });
+        for (int it = 0; it < c.regVelocityIters; ++it)
+            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, t); });
+    }
+    for (uint32_t b = d.w_body_off[w] + rank; b < d.w_body_off[w + 1]; b += size) integrate_body(d, b);
+    G::sync();
+    if (n) {
+        for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it)
+            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_position(d, t, it); });
+        for (uint32_t t = base + rank; t < base + n; t += size) store_impulses(d, t);
+    }
+    G::sync();  // the group's shared words are reused by its next world
+}
+
+// Persistent CTAs take worlds from a queue ordered by decreasing body count.
+// The first n_world_big entries are solved by a whole CTA each; once a CTA
+// meets a smaller world, each of its warps takes worlds on its own.
+__global__ void __launch_bounds__(256) k_world_solve(DW d) {
     __shared__ uint32_t s_w;
+    __shared__ uint32_t s_col[8][2][kColStride];
+    uint32_t qi;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_w = atomicAdd(&d.cnt->world_queue, 1u);
         __syncthreads();
-        const uint32_t qi = s_w;
+        qi = s_w;
         if (qi >= d.n_worlds) return;
-        const uint32_t w = d.w_order[qi];
-        const uint32_t* off = d.w_coloff + (size_t)w * kColStride;
-        if (threadIdx.x == 0 && off[kSerialColour + 1] > off[kSerialColour])
-            sort_serial(d.k_order + off[kSerialColour], off[kSerialColour + 1] - off[kSerialColour]);
-        // Runs f(k) over colour col of this world, then synchronises the CTA.
-        auto sweep = [&](int col, auto&& f) {
-            const uint32_t lo = off[col], hi = off[col + 1];
-            if (lo == hi) return;
-            if (col == kSerialColour) {
-                if (threadIdx.x == 0)
-                    for (uint32_t t = lo; t < hi; ++t) f(d.k_order[t]);
-            } else {
-                for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) f(d.k_order[t]);
-            }
-            __syncthreads();
-        };
-        // warm start and joint InitVelocity
-        for (int col = 0; col <= kSerialColour; ++col) {
-            sweep(col, [&](uint32_t k) {
-                const uint32_t id = d.k_list[k];
-                if (id & kJointBit) joint_init_velocity(d, id & ~kJointBit);
-                else if (c.doWarmStart) warm_start(d, d.vc[k]);
-            });
-        }
-        // velocity iterations
-        for (int it = 0; it < c.regVelocityIters; ++it) {
-            for (int col = 0; col <= kSerialColour; ++col) {
-                sweep(col, [&](uint32_t k) {
-                    const uint32_t id = d.k_list[k];
-                    if (id & kJointBit) {
-                        joint_solve_velocity(d, id & ~kJointBit);
-                    } else {
-                        VC vc = d.vc[k];
-                        solve_contact_velocity(d, vc);
-                        reinterpret_cast<float4*>(&d.vc[k])[6] = make_float4(vc.ni0, vc.ti0, vc.ni1, vc.ti1);
-                    }
-                });
-            }
-        }
-        // IntegratePositions (AabbTreeWorld.cpp:176-188) for this world's bodies
-        const float h = c.deltaTime;
-        for (uint32_t b = d.w_body_off[w] + threadIdx.x; b < d.w_body_off[w + 1]; b += blockDim.x) {
-            if (!(d.b_flags[b] & BF_SOLVED)) continue;
-            const float4 v = d.b_vel[b];
-            float4 p = d.b_pos1[b];
-            const float tx = v.x * h, ty = v.y * h, rot = h * v.z;
-            p.x = p.x + tx; p.y = p.y + ty; p.z = p.z + rot;
-            d.b_pos1[b] = p;
-        }
-        __syncthreads();
-        // position iterations with the per-island early exit
-        for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it) {
-            for (int col = 0; col <= kSerialColour; ++col) {
-                sweep(col, [&](uint32_t k) {
-                    const uint32_t id = d.k_list[k];
-                    if (id & kJointBit) {
-                        const uint32_t j = id & ~kJointBit;
-                        const uint32_t L = joint_island(d, j);
-                        if (island_done(d, L, it)) return;
-                        if (!joint_solve_position(d, j)) d.isl_jok[(size_t)L * kMaxPosIters + it] = 0u;
-                    } else {
-                        const PC pc = d.pc[k];
-                        if (island_done(d, pc.island, it)) return;
-                        const float sep = solve_contact_position(d, pc);
-                        atomic_min_float(&d.isl_sep[(size_t)pc.island * kMaxPosIters + it], sep);
-                    }
-                });
-            }
-        }
-        // AssignImpulses (AabbTreeWorld.cpp:196-220)
-        for (uint32_t t = off[0] + threadIdx.x; t < off[kSerialColour + 1]; t += blockDim.x) {
-            const uint32_t k = d.k_order[t];
-            if (d.k_list[k] & kJointBit) continue;
-            const VC& vc = d.vc[k];
-            float4 p0 = d.m_p0[vc.slot];
-            p0.z = vc.ni0; p0.w = vc.ti0;
-            d.m_p0[vc.slot] = p0;
-            if (vc.count == 2u) {
-                float4 p1 = d.m_p1[vc.slot];
-                p1.z = vc.ni1; p1.w = vc.ti1;
-                d.m_p1[vc.slot] = p1;
-            }
-        }
+        if (qi >= d.n_world_big) break;
+        solve_world<BlockGroup>(d, d.w_order[qi], threadIdx.x, blockDim.x, s_col[0][0], s_col[0][1]);
+    }
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    auto next = [&]() {
+        uint32_t x = 0u;
+        if (lane == 0) x = atomicAdd(&d.cnt->world_queue, 1u);
+        return __shfl_sync(0xffffffffu, x, 0);
+    };
+    if (warp != 0) qi = next();  // warp 0 keeps the entry the CTA took
+    while (qi < d.n_worlds) {
+        solve_world<WarpGroup>(d, d.w_order[qi], lane, 32u, s_col[warp][0], s_col[warp][1]);
+        qi = next();
     }
 }
 
@@ -1273,11 +1252,13 @@ void launch_islands_colour(const DW& d, const Launch& L, cudaStream_t s) {
     k_inc_off_tail<<<1, 1, 0, s>>>(d);
     cudaMemsetAsync(d.inc_cur, 0, sizeof(uint32_t) * (d.n_bodies + 1), s);
     k_inc_fill<<<L.grid, L.threads, 0, s>>>(d);
-    launch_coop(k_colour, d, L, s);
+    if (L.per_world) k_world_ranges<<<L.grid, L.threads, 0, s>>>(d);
+    else launch_coop(k_colour, d, L, s);
 }
 
 void launch_build_constraints(const DW& d, const Launch& L, cudaStream_t s) {
-    k_build_constraints<<<L.grid, L.threads, 0, s>>>(d);
+    // per world, k_world_solve builds the constraints once it has coloured them
+    if (!L.per_world) k_build_constraints<<<L.grid, L.threads, 0, s>>>(d);
 }
 
 void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) {
@@ -1285,17 +1266,13 @@ void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) {
         launch_coop(k_solve, d, L, s);
         return;
     }
-    cudaMemsetAsync(d.w_colcnt, 0, sizeof(uint32_t) * (size_t)d.n_worlds * kColStride, s);
     cudaMemsetAsync(&d.cnt->world_queue, 0, sizeof(uint32_t), s);
-    k_wbucket_count<<<L.grid, L.threads, 0, s>>>(d);
-    k_wbucket_offsets<<<1, 1024, 0, s>>>(d);
-    k_wbucket_scatter<<<L.grid, L.threads, 0, s>>>(d);
-    k_solve_world<<<L.world_grid, 256, 0, s>>>(d);
+    k_world_solve<<<L.world_grid, 256, 0, s>>>(d);
 }
 
 int world_blocks_per_sm() {
     int a = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_solve_world, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_world_solve, 256, 0);
     return a;
 }
 

@@ -32,6 +32,8 @@ struct prgpu_world {
     uint32_t* d_stage_u = nullptr;
     Counters* h_cnt = nullptr;  // pinned mirror of the device counters
     cudaEvent_t graph_ev[8] = {};  // recorded by the captured step between its phases
+    std::vector<uint32_t> order_nb;  // body counts of the worlds in work-queue order
+    uint32_t warp_world_max = 0;     // worlds of at most this many bodies are swept by one warp
 };
 
 namespace {
@@ -376,6 +378,23 @@ int bits_for(uint64_t n) {
 constexpr int kPhases = 7;
 // Batches of at least this many worlds sweep one world per CTA by default.
 constexpr uint32_t kPerWorldMinWorlds = 64;
+// Worlds of at most this many bodies are swept by one warp by default.
+constexpr uint32_t kWarpWorldMaxBodies = 256;
+
+uint32_t count_big_worlds(const prgpu_world* w) {
+    uint32_t n = 0;
+    while (n < w->order_nb.size() && w->order_nb[n] > w->warp_world_max) ++n;
+    return n;
+}
+
+// Drops the captured step so that the next step captures the new launches.
+int drop_graph(prgpu_world* w) {
+    CU(cudaSetDevice(w->device));
+    CU(cudaStreamSynchronize(w->stream));
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->graph_def) { cudaGraphDestroy(w->graph_def); w->graph_def = nullptr; }
+    return PRGPU_OK;
+}
 
 int enqueue_step(prgpu_world* w, bool solve, cudaEvent_t* ev = nullptr, bool capturing = false) {
     const DW& d = w->d;
@@ -654,7 +673,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.w_root, W); AL(d.w_bounds, W);
     uint32_t* w_order;
     AL(w_order, W); d.w_order = w_order;
-    AL(d.w_coloff, (size_t)W * kColStride); AL(d.w_colcnt, (size_t)W * kColStride);
+    AL(d.w_kc, W + 1); AL(d.w_kj, W + 1);
     AL(d.b_pos1, N); AL(d.b_pos0, N); AL(d.b_vel, N); AL(d.b_xf, N); AL(d.b_mass, N); AL(d.b_acc, N);
     AL(d.b_damp, N); AL(d.b_flags, N); AL(d.b_uat, N); AL(d.b_world, N); AL(d.b_island, N);
     AL(d.b_jnt_off, N + 1); AL(d.b_jnt_other, jother.size()); AL(d.b_jnt_cc, jcc.size());
@@ -672,6 +691,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.l_node_box, S); AL(d.l_left, S); AL(d.l_right, S); AL(d.l_parent, 2 * (size_t)S); AL(d.l_range, 2 * (size_t)S);
     AL(d.l_visit, S);
     AL(d.k_list, C + J); AL(d.k_colour, C + J); AL(d.k_tent, C + J); AL(d.k_order, C + J);
+    AL(d.t_id, C + J);
     AL(d.k_prio, C + J);
     AL(d.inc_off, N + 1); AL(d.inc_cur, N + 1); AL(d.inc_list, 2 * ((size_t)C + J));
     AL(d.vc, C); AL(d.pc, C);
@@ -710,6 +730,10 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
         return body_off[a + 1] - body_off[a] > body_off[b + 1] - body_off[b];
     });
+    w->order_nb.resize(W);
+    for (uint32_t i = 0; i < W; ++i) w->order_nb[i] = body_off[order[i] + 1] - body_off[order[i]];
+    w->warp_world_max = kWarpWorldMaxBodies;
+    d.n_world_big = count_big_worlds(w);
     if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(PRGPU_ECUDA);
     // ---- uploads
     auto up = [&](void* dst, const void* src, size_t bytes) -> bool {
@@ -873,12 +897,66 @@ int prgpu_set_sweep_mode(prgpu_world* w, int mode) {
     const bool per_world = (mode == PRGPU_SWEEPS_AUTO) ? (w->d.n_worlds >= kPerWorldMinWorlds)
                                                          : (mode == PRGPU_SWEEPS_PER_WORLD);
     if (per_world == w->L.per_world) return PRGPU_OK;
-    CU(cudaSetDevice(w->device));
-    CU(cudaStreamSynchronize(w->stream));
-    // the captured step holds the old launches: capture again on the next step
-    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
-    if (w->graph_def) { cudaGraphDestroy(w->graph_def); w->graph_def = nullptr; }
+    const int rc = drop_graph(w);
+    if (rc) return rc;
     w->L.per_world = per_world;
+    return PRGPU_OK;
+}
+
+int prgpu_set_warp_world_max_bodies(prgpu_world* w, uint32_t max_bodies) {
+    if (!w) return PRGPU_EINVAL;
+    if (max_bodies == w->warp_world_max) return PRGPU_OK;
+    const int rc = drop_graph(w);
+    if (rc) return rc;
+    w->warp_world_max = max_bodies;
+    w->d.n_world_big = count_big_worlds(w);
+    return PRGPU_OK;
+}
+
+int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_candidate, prgpu_schedule* best) {
+    if (!w || !conf || steps_per_candidate < 1) return PRGPU_EINVAL;
+    if (conf->deltaTime == 0.f) return fail(w, PRGPU_EINVAL, "autotune needs a step with deltaTime > 0");
+    CU(cudaSetDevice(w->device));
+    struct Cand { int mode; uint32_t warp_max; };
+    std::vector<Cand> cands = {{PRGPU_SWEEPS_GRID, w->warp_world_max}};
+    if (w->d.n_worlds > 1) {
+        for (uint32_t m : {0u, 64u, 128u, 256u, 512u, 1024u, 0xffffffffu}) cands.push_back({PRGPU_SWEEPS_PER_WORLD, m});
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    float best_ms = 0.f;
+    Cand pick = cands[0];
+    int rc = PRGPU_OK;
+    for (const Cand& cd : cands) {
+        if ((rc = prgpu_set_sweep_mode(w, cd.mode)) != PRGPU_OK) break;
+        if ((rc = prgpu_set_warp_world_max_bodies(w, cd.warp_max)) != PRGPU_OK) break;
+        if ((rc = run_steps(w, conf, 1, true)) != PRGPU_OK) break;  // captures the candidate's step
+        if (cudaEventRecord(e0, w->stream) != cudaSuccess) { rc = PRGPU_ECUDA; break; }
+        if ((rc = run_steps(w, conf, steps_per_candidate, false)) != PRGPU_OK) break;
+        if (cudaEventRecord(e1, w->stream) != cudaSuccess) { rc = PRGPU_ECUDA; break; }
+        if ((rc = check_device_error(w)) != PRGPU_OK) break;
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) { rc = PRGPU_ECUDA; break; }
+        ms /= (float)steps_per_candidate;
+        if (&cd == &cands[0] || ms < best_ms) { best_ms = ms; pick = cd; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = prgpu_set_sweep_mode(w, pick.mode)) != PRGPU_OK) return rc;
+    if ((rc = prgpu_set_warp_world_max_bodies(w, pick.warp_max)) != PRGPU_OK) return rc;
+    if (best) {
+        best->sweep_mode = pick.mode;
+        best->warp_world_max_bodies = pick.warp_max;
+        best->step_ms = best_ms;
+    }
+    return PRGPU_OK;
+}
+
+int prgpu_get_warp_world_max_bodies(prgpu_world* w, uint32_t* max_bodies) {
+    if (!w || !max_bodies) return PRGPU_EINVAL;
+    *max_bodies = w->warp_world_max;
     return PRGPU_OK;
 }
 

@@ -54,6 +54,11 @@ class BatchDesc(ctypes.Structure):
         ("joint_flags", P), ("contact_capacity", ctypes.c_uint32), ("candidate_capacity", ctypes.c_uint32)]
 
 
+class Schedule(ctypes.Structure):
+    _fields_ = [("sweep_mode", ctypes.c_int32), ("warp_world_max_bodies", ctypes.c_uint32),
+                ("step_ms", ctypes.c_float)]
+
+
 class PrgpuError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"prgpu {STATUS.get(code, code)}: {msg}")
@@ -94,6 +99,9 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_graph_kernel_count.argtypes = [P, P]
     lib.prgpu_set_sweep_mode.argtypes = [P, I]
     lib.prgpu_get_sweep_mode.argtypes = [P, P]
+    lib.prgpu_set_warp_world_max_bodies.argtypes = [P, U]
+    lib.prgpu_get_warp_world_max_bodies.argtypes = [P, P]
+    lib.prgpu_autotune.argtypes = [P, ctypes.POINTER(StepConf), I, ctypes.POINTER(Schedule)]
     _LIB = lib
     return lib
 
@@ -104,7 +112,8 @@ def exported_symbols() -> List[str]:
         "prgpu_step", "prgpu_step_n", "prgpu_step_async", "prgpu_synchronize", "prgpu_get_counts",
         "prgpu_download_bodies", "prgpu_upload_body_states", "prgpu_download_contacts",
         "prgpu_download_proxies", "prgpu_last_error", "prgpu_convex_hull", "prgpu_prepare_bodies", "prgpu_step_profiled",
-        "prgpu_last_step_phase_ms", "prgpu_graph_kernel_count", "prgpu_set_sweep_mode", "prgpu_get_sweep_mode"]
+        "prgpu_last_step_phase_ms", "prgpu_graph_kernel_count", "prgpu_set_sweep_mode", "prgpu_get_sweep_mode",
+        "prgpu_set_warp_world_max_bodies", "prgpu_get_warp_world_max_bodies", "prgpu_autotune"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -282,6 +291,25 @@ class GpuBatch:
         m = ctypes.c_int(0)
         self._check(self.lib.prgpu_get_sweep_mode(self.h, ctypes.byref(m)), "prgpu_get_sweep_mode")
         return {v: k for k, v in self.SWEEP_MODES.items()}[m.value]
+
+    def set_warp_world_max_bodies(self, n: int):
+        """Per-world sweeps: worlds of at most n bodies are swept by one warp."""
+        self._check(self.lib.prgpu_set_warp_world_max_bodies(self.h, int(n) & 0xffffffff), "warp world limit")
+
+    def warp_world_max_bodies(self) -> int:
+        m = ctypes.c_uint32(0)
+        self._check(self.lib.prgpu_get_warp_world_max_bodies(self.h, ctypes.byref(m)), "warp world limit")
+        return int(m.value)
+
+    def autotune(self, steps_per_candidate: int = 3, conf: StepConf | None = None) -> dict:
+        """Times the candidate sweep schedules (advancing the world) and keeps the fastest."""
+        c = conf if conf is not None else default_conf()
+        sc = Schedule()
+        self._check(self.lib.prgpu_autotune(self.h, ctypes.byref(c), int(steps_per_candidate), ctypes.byref(sc)),
+                    "prgpu_autotune")
+        inv = {v: k for k, v in self.SWEEP_MODES.items()}
+        return {"sweeps": inv[sc.sweep_mode], "warp_world_max_bodies": int(sc.warp_world_max_bodies),
+                "step_ms": float(sc.step_ms)}
 
     def step_async(self, n: int, conf: StepConf):
         self._check(self.lib.prgpu_step_async(self.h, ctypes.byref(conf), int(n)), "prgpu_step_async")

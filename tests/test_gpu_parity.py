@@ -150,19 +150,41 @@ def test_sweep_modes_agree(gpu_lib):
             worlds.append(scenes.chains_world(rng, n_free=12, n_chains=2, links=6))
         else:
             worlds.append(scenes.pile(8, rng, width=3.0))
-    a = GpuBatch(worlds)
-    b = GpuBatch(worlds)
-    assert a.sweep_mode() == "per_world"  # 72 worlds: the default is one CTA per world
+    a = GpuBatch(worlds)  # per world; worlds of <= 256 bodies by a warp, the rest by a CTA
+    b = GpuBatch(worlds)  # one cooperative grid
+    c = GpuBatch(worlds)  # per world, every world by a whole CTA
+    e = GpuBatch(worlds)  # per world, every world by a warp
+    assert a.sweep_mode() == "per_world"  # 72 worlds: the default is per world
+    assert a.warp_world_max_bodies() == 256
     b.set_sweep_mode("grid")
     assert b.sweep_mode() == "grid"
-    for _ in range(90):
-        a.step()
-        b.step()
-    ba, bb = a.bodies(), b.bodies()
-    np.testing.assert_array_equal(ba["pos"], bb["pos"])
-    np.testing.assert_array_equal(ba["vel"], bb["vel"])
-    ca, cb = a.contacts(), b.contacts()
-    assert pair_set(ca) == pair_set(cb)
+    c.set_warp_world_max_bodies(0)
+    e.set_warp_world_max_bodies(2 ** 32 - 1)
+    for i in range(90):
+        for g in (a, b, c, e):
+            g.step()
+        if i == 40:  # switching schedule mid-run recaptures the step and changes nothing
+            a.set_warp_world_max_bodies(64)
+    ba = a.bodies()
+    for g in (b, c, e):
+        bg = g.bodies()
+        np.testing.assert_array_equal(ba["pos"], bg["pos"])
+        np.testing.assert_array_equal(ba["vel"], bg["vel"])
+        assert pair_set(a.contacts()) == pair_set(g.contacts())
+
+
+def test_autotune_keeps_results(gpu_lib):
+    """The autotuner times schedules on the live batch; the batch ends where
+    plain steps would have taken it."""
+    rng = np.random.default_rng(5)
+    worlds = [scenes.pile(20 + 7 * i, rng, width=4.0) for i in range(80)]
+    a, b = GpuBatch(worlds), GpuBatch(worlds)
+    best = a.autotune(steps_per_candidate=2)
+    assert best["sweeps"] in ("grid", "per_world") and best["step_ms"] > 0
+    n_cand = 1 + 7
+    b.step_n(n_cand * 3)
+    np.testing.assert_array_equal(a.bodies()["pos"], b.bodies()["pos"])
+    np.testing.assert_array_equal(a.bodies()["vel"], b.bodies()["vel"])
 
 
 def test_deterministic(gpu_lib):
