@@ -154,9 +154,16 @@ int prgpu_get_sweep_mode(prgpu_world* w, int* mode);
 int prgpu_set_warp_world_max_bodies(prgpu_world* w, uint32_t max_bodies);
 int prgpu_get_warp_world_max_bodies(prgpu_world* w, uint32_t* max_bodies);
 /* A sweep schedule and its measured device time per step. */
+/* Shared memory (bytes, a multiple of 128) in which the per-world solver
+ * keeps the velocities and positions of the world it sweeps, 44 bytes a body
+ * (a warp gets an eighth); larger worlds are swept in global memory.  0 (the
+ * default) disables staging.  Results do not depend on it. */
+int prgpu_set_stage_bytes(prgpu_world* w, uint32_t bytes);
+int prgpu_get_stage_bytes(prgpu_world* w, uint32_t* bytes);
 typedef struct prgpu_schedule {
     int32_t sweep_mode;               /* PRGPU_SWEEPS_GRID or PRGPU_SWEEPS_PER_WORLD */
     uint32_t warp_world_max_bodies;
+    uint32_t stage_bytes;
     float step_ms;
 } prgpu_schedule;
 /* Autotuner: times every candidate schedule over steps_per_candidate steps

@@ -20,11 +20,16 @@ PR_HD uint32_t cf_pack(unsigned tA, unsigned iA, unsigned tB, unsigned iB) {
 // Flip (ContactFeature.hpp:114-117).
 PR_HD uint32_t cf_flip(uint32_t c) { return ((c >> 16) & 0xffffu) | ((c & 0xffffu) << 16); }
 
+// DistanceProxy (DistanceProxy.hpp) as a view of the shape's vertex records
+// in device memory: vertex xy and outward edge normal zw, count <= kMaxVerts.
+// The collision routines read the vertices where they lie rather than copying
+// them into per-thread (local) memory.
 struct Proxy {
     int count;
     float r;
-    V2 v[kMaxVerts];
-    V2 n[kMaxVerts];
+    const float4* vn;
+    PR_HD V2 vtx(int i) const { const float4 q = vn[i]; return mk(q.x, q.y); }
+    PR_HD V2 nrm(int i) const { const float4 q = vn[i]; return mk(q.z, q.w); }
 };
 
 struct Man {
@@ -98,6 +103,18 @@ PR_HD float min_sep_info(V2 origin, V2 dir, const V2* verts, int n, unsigned& fi
     return minSep;
 }
 
+// The same over a shape's own vertices.
+PR_HD float min_sep_info(V2 origin, V2 dir, const Proxy& p, unsigned& first, unsigned& second) {
+    float minSep = PR_INF;
+    first = kInvalidV; second = kInvalidV;
+    for (int i = 0; i < p.count; ++i) {
+        const float s = dot(dir, p.vtx(i) - origin);
+        if (minSep > s) { minSep = s; first = (unsigned)i; second = kInvalidV; }
+        else if (minSep == s) { second = (unsigned)i; }
+    }
+    return minSep;
+}
+
 struct SepInfo {
     float distance;
     unsigned firstShape, second0, second1;
@@ -108,10 +125,10 @@ PR_HD SepInfo max_sep_4x4(const Proxy& p1, Xf xf1, const Proxy& p2, Xf xf2) {
     SepInfo r; r.distance = -PR_INF; r.firstShape = kInvalidV; r.second0 = kInvalidV; r.second1 = kInvalidV;
     const Xf xf = mult(xf1, xf2);
     V2 verts[4];
-    for (int i = 0; i < 4; ++i) verts[i] = xform(p2.v[i], xf);
+    for (int i = 0; i < 4; ++i) verts[i] = xform(p2.vtx(i), xf);
     for (int i = 0; i < 4; ++i) {
         unsigned f, s;
-        const float d = min_sep_info(p1.v[i], p1.n[i], verts, 4, f, s);
+        const float d = min_sep_info(p1.vtx(i), p1.nrm(i), verts, 4, f, s);
         if (r.distance < d) { r.distance = d; r.second0 = f; r.second1 = s; r.firstShape = (unsigned)i; }
     }
     return r;
@@ -122,10 +139,10 @@ PR_HD SepInfo max_sep(const Proxy& p1, Xf xf1, const Proxy& p2, Xf xf2) {
     SepInfo r; r.distance = -PR_INF; r.firstShape = kInvalidV; r.second0 = kInvalidV; r.second1 = kInvalidV;
     const Xf xf = mult(xf2, xf1);
     for (int i = 0; i < p1.count; ++i) {
-        const V2 origin = xform(p1.v[i], xf);
-        const V2 normal = rotate(p1.n[i], xf.q);
+        const V2 origin = xform(p1.vtx(i), xf);
+        const V2 normal = rotate(p1.nrm(i), xf.q);
         unsigned f, s;
-        const float d = min_sep_info(origin, normal, p2.v, p2.count, f, s);
+        const float d = min_sep_info(origin, normal, p2, f, s);
         if (r.distance < d) { r.distance = d; r.second0 = f; r.second1 = s; r.firstShape = (unsigned)i; }
     }
     return r;
@@ -138,8 +155,8 @@ PR_HD void most_anti_parallel_edge(V2 n0, Xf xf0, const Proxy& s1, Xf xf1, unsig
         const V2 normal = invrotate(rotate(n0, xf0.q), xf1.q);
         const unsigned count = (unsigned)s1.count;
         const unsigned prev = (first == 0u) ? count - 1u : first - 1u;
-        const float prevDot = dot(normal, s1.n[prev]);
-        const float currDot = dot(normal, s1.n[first]);
+        const float prevDot = dot(normal, s1.nrm(prev));
+        const float currDot = dot(normal, s1.nrm(first));
         if (prevDot < currDot) { e0 = prev; e1 = first; }
         else { e0 = first; e1 = (first + 1u) % count; }
         return;
@@ -154,18 +171,18 @@ PR_HD Man manifold_poly(bool flipped, const Proxy& s0, Xf xf0, unsigned idx0, co
     const float r0 = s0.r, r1 = s1.r;
     const float totalRadius = r0 + r1;
     const unsigned idx0Next = (idx0 + 1u) % (unsigned)s0.count;
-    const V2 s0_rel_v0 = s0.v[idx0];
-    const V2 s0_rel_v1 = s0.v[idx0Next];
+    const V2 s0_rel_v0 = s0.vtx(idx0);
+    const V2 s0_rel_v1 = s0.vtx(idx0Next);
     const V2 s0_abs_v0 = xform(s0_rel_v0, xf0);
     const V2 s0_abs_v1 = xform(s0_rel_v1, xf0);
     const float s0_len_edge0 = mag2(s0_rel_v1 - s0_rel_v0);
-    const V2 s0_rel_n0 = s0.n[idx0];
+    const V2 s0_rel_n0 = s0.nrm(idx0);
     const V2 s0_rel_e0_dir = revperp(s0_rel_n0);
     unsigned e1f, e1s;
     most_anti_parallel_edge(s0_rel_n0, xf0, s1, xf1, sec0, sec1, e1f, e1s);
-    const V2 s1_rel_v0 = s1.v[e1f];
+    const V2 s1_rel_v0 = s1.vtx(e1f);
     const V2 s1_abs_v0 = xform(s1_rel_v0, xf1);
-    const V2 s1_rel_v1 = s1.v[e1s];
+    const V2 s1_rel_v1 = s1.vtx(e1s);
     const V2 s1_abs_v1 = xform(s1_rel_v1, xf1);
     {
         const V2 s0_abs_e0_dir = rotate(s0_rel_e0_dir, xf0.q);
@@ -222,16 +239,16 @@ PR_HD Man manifold_circle(bool flipped, float totalRadius, const Proxy& shape, X
     unsigned indexOfMax = 0;
     float maxSeparation = -3.40282347e+38f;
     for (int i = 0; i < vc; ++i) {
-        const float s = dot(shape.n[i], cLocal - shape.v[i]);
+        const float s = dot(shape.nrm(i), cLocal - shape.vtx(i));
         if (s > totalRadius) return man_empty();
         if (maxSeparation < s) { maxSeparation = s; indexOfMax = (unsigned)i; }
     }
     const unsigned indexOfMax2 = (indexOfMax + 1u) % (unsigned)vc;
-    const V2 v1 = shape.v[indexOfMax];
-    const V2 v2 = shape.v[indexOfMax2];
+    const V2 v1 = shape.vtx(indexOfMax);
+    const V2 v2 = shape.vtx(indexOfMax2);
     const uint32_t cfFace = flipped ? cf_pack(CF_VERTEX, 0, CF_FACE, indexOfMax) : cf_pack(CF_FACE, indexOfMax, CF_VERTEX, 0);
     if (maxSeparation < 0.f) {
-        Man m = man_face(flipped ? M_FACEB : M_FACEA, shape.n[indexOfMax], vdiv(v1 + v2, 2.0f));
+        Man m = man_face(flipped ? M_FACEB : M_FACEA, shape.nrm(indexOfMax), vdiv(v1 + v2, 2.0f));
         man_add(m, point, cfFace);
         return m;
     }
@@ -246,8 +263,8 @@ PR_HD Man manifold_circle(bool flipped, float totalRadius, const Proxy& shape, X
         return !flipped ? man_circles(v2, indexOfMax2, point, 0) : man_circles(point, 0, v2, indexOfMax2);
     }
     const V2 faceCenter = vdiv(v1 + v2, 2.0f);
-    if (dot(cLocal - faceCenter, shape.n[indexOfMax]) > totalRadius) return man_empty();
-    Man m = man_face(flipped ? M_FACEB : M_FACEA, shape.n[indexOfMax], faceCenter);
+    if (dot(cLocal - faceCenter, shape.nrm(indexOfMax)) > totalRadius) return man_empty();
+    Man m = man_face(flipped ? M_FACEB : M_FACEA, shape.nrm(indexOfMax), faceCenter);
     man_add(m, point, cfFace);
     return m;
 }
@@ -256,15 +273,15 @@ PR_HD Man manifold_circle(bool flipped, float totalRadius, const Proxy& shape, X
 PR_HD Man collide_shapes(const Proxy& A, Xf xfA, const Proxy& B, Xf xfB, float linearSlop, float maxCirclesRatio) {
     const float totalRadius = A.r + B.r;
     if (A.count == 1 && B.count == 1) {
-        const V2 pA = xform(A.v[0], xfA);
-        const V2 pB = xform(B.v[0], xfB);
+        const V2 pA = xform(A.vtx(0), xfA);
+        const V2 pB = xform(B.vtx(0), xfB);
         const float lenSq = mag2(pB - pA);
         const float totSq = totalRadius * totalRadius;
         if (lenSq > totSq) return man_empty();
-        return man_circles(A.v[0], 0, B.v[0], 0);
+        return man_circles(A.vtx(0), 0, B.vtx(0), 0);
     }
-    if (A.count == 1) return manifold_circle(true, totalRadius, B, xfB, A.v[0], xfA);
-    if (B.count == 1) return manifold_circle(false, totalRadius, A, xfA, B.v[0], xfB);
+    if (A.count == 1) return manifold_circle(true, totalRadius, B, xfB, A.vtx(0), xfA);
+    if (B.count == 1) return manifold_circle(false, totalRadius, A, xfA, B.vtx(0), xfB);
     const bool do4x4 = (A.count == 4) && (B.count == 4);
     const SepInfo sa = do4x4 ? max_sep_4x4(A, xfA, B, xfB) : max_sep(A, xfA, B, xfB);
     if (sa.distance > totalRadius) return man_empty();

@@ -26,13 +26,9 @@ __device__ __forceinline__ void load_proxy(const DW& d, uint32_t p, Proxy& out) 
     const uint32_t meta = d.s_meta[p];
     const int nv = (int)((meta >> 8) & 0xffu);
     const uint32_t voff = d.s_voff[p];
-    out.count = nv;
+    out.count = nv < kMaxVerts ? nv : kMaxVerts;
     out.r = d.s_radius[p];
-    for (int i = 0; i < nv && i < kMaxVerts; ++i) {
-        const float4 v = d.verts[voff + i];
-        out.v[i] = mk(v.x, v.y);
-        out.n[i] = mk(v.z, v.w);
-    }
+    out.vn = d.verts + voff;
 }
 
 __device__ __forceinline__ Xf load_xf(const DW& d, uint32_t b) {

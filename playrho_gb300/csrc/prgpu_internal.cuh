@@ -140,6 +140,7 @@ struct DW {
     uint32_t* w_kc;          // [n_worlds + 1] first active contact (index into k_list) of each world
     uint32_t* w_kj;          // [n_worlds + 1] first active joint of each world
     uint32_t n_world_big;    // leading entries of w_order swept by a whole CTA (the rest by a warp)
+    uint32_t stage_bytes;    // dynamic shared memory of the per-world solver (world body state)
     float4* w_bounds;        // centroid bounds for Morton codes (ordered-int encoded)
     // bodies
     float4* b_pos1;          // cx cy angle -

@@ -32,6 +32,7 @@ void launch_solve_finish(const DW& d, const Launch& L, cudaStream_t s);
 void launch_reset_step(const DW& d, const Launch& L, cudaStream_t s);
 void launch_clear_dirty(const DW& d, const Launch& L, cudaStream_t s);
 int coop_blocks_per_sm(int threads);
-int world_blocks_per_sm();
+// Sets k_world_solve's dynamic shared memory to stage_bytes; returns its CTAs per SM.
+int world_blocks_per_sm(uint32_t stage_bytes);
 
 }  // namespace prgpu

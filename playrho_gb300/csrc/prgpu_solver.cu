@@ -15,6 +15,8 @@
 // change nothing, so every island runs regVelocityIters sweeps.
 #include <cooperative_groups.h>
 
+#include <mutex>
+
 #include "prgpu_collide.cuh"
 #include "prgpu_kernels.cuh"
 
@@ -511,11 +513,11 @@ __global__ void k_build_constraints(DW d) {
 }
 
 // ---- per-constraint solver steps --------------------------------------------
-__device__ __forceinline__ bool writable(const DW& d, uint32_t b) { return is_accelerable(d.b_flags[b]); }
 
 // WarmStartVelocities (AabbTreeWorld.cpp:227-274).
-__device__ void warm_start(const DW& d, const VC& vc) {
-    const float4 mA = d.b_mass[vc.bA], mB = d.b_mass[vc.bB];
+template <class BS>
+__device__ void warm_start(const DW& d, const BS& bs, const VC& vc) {
+    const float4 mA = bs.mass(vc.bA), mB = bs.mass(vc.bB);
     const V2 n = mk(vc.nx, vc.ny), t = fwdperp(n);
     float dAx = 0.f, dAy = 0.f, dAw = 0.f, dBx = 0.f, dBy = 0.f, dBw = 0.f;
     for (uint32_t j = 0; j < vc.count; ++j) {
@@ -527,15 +529,15 @@ __device__ void warm_start(const DW& d, const VC& vc) {
         dAx = dAx - P.x * mA.x; dAy = dAy - P.y * mA.x; dAw = dAw - mA.y * LA;
         dBx = dBx + P.x * mB.x; dBy = dBy + P.y * mB.x; dBw = dBw + mB.y * LB;
     }
-    if (writable(d, vc.bA)) {
-        float4 v = d.b_vel[vc.bA];
+    if (bs.writable(vc.bA)) {
+        float4 v = bs.vel(vc.bA);
         v.x = v.x + dAx; v.y = v.y + dAy; v.z = v.z + dAw;
-        d.b_vel[vc.bA] = v;
+        bs.set_vel(vc.bA, v);
     }
-    if (writable(d, vc.bB)) {
-        float4 v = d.b_vel[vc.bB];
+    if (bs.writable(vc.bB)) {
+        float4 v = bs.vel(vc.bB);
         v.x = v.x + dBx; v.y = v.y + dBy; v.z = v.z + dBw;
-        d.b_vel[vc.bB] = v;
+        bs.set_vel(vc.bB, v);
     }
 }
 
@@ -544,9 +546,10 @@ __device__ __forceinline__ V2 rel_vel(float4 va, V2 rA, float4 vb, V2 rB) {
 }
 
 // GaussSeidel::SolveVelocityConstraint (ContactSolver.cpp:245-492).
-__device__ void solve_contact_velocity(const DW& d, VC& vc) {
-    const float4 mA = d.b_mass[vc.bA], mB = d.b_mass[vc.bB];
-    float4 vA = d.b_vel[vc.bA], vB = d.b_vel[vc.bB];
+template <class BS>
+__device__ void solve_contact_velocity(const DW& d, const BS& bs, VC& vc) {
+    const float4 mA = bs.mass(vc.bA), mB = bs.mass(vc.bB);
+    float4 vA = bs.vel(vc.bA), vB = bs.vel(vc.bB);
     const V2 n = mk(vc.nx, vc.ny);
     const V2 rA0 = mk(vc.rA0x, vc.rA0y), rB0 = mk(vc.rB0x, vc.rB0y);
     const V2 rA1 = mk(vc.rA1x, vc.rA1y), rB1 = mk(vc.rB1x, vc.rB1y);
@@ -623,8 +626,8 @@ __device__ void solve_contact_velocity(const DW& d, VC& vc) {
             else { if (k) vc.ni1 = nv; else vc.ni0 = nv; }
         }
     }
-    if (writable(d, vc.bA)) d.b_vel[vc.bA] = vA;
-    if (writable(d, vc.bB)) d.b_vel[vc.bB] = vB;
+    if (bs.writable(vc.bA)) bs.set_vel(vc.bA, vA);
+    if (bs.writable(vc.bB)) bs.set_vel(vc.bB, vB);
 }
 
 struct PSM {
@@ -680,10 +683,11 @@ __device__ __forceinline__ PosSol pos_solver_fn(const PSM& psm, V2 pA, V2 pB, fl
 
 // GaussSeidel::SolvePositionConstraint (ContactSolver.cpp:494-643); returns the
 // separation the reference reports for this constraint.
-__device__ float solve_contact_position(const DW& d, const PC& pc) {
+template <class BS>
+__device__ float solve_contact_position(const DW& d, const BS& bs, const PC& pc) {
     const DConf& c = *d.conf;
-    const float4 mA = d.b_mass[pc.bA], mB = d.b_mass[pc.bB];
-    float4 pA = d.b_pos1[pc.bA], pB = d.b_pos1[pc.bB];
+    const float4 mA = bs.mass(pc.bA), mB = bs.mass(pc.bB);
+    float4 pA = bs.pos(pc.bA), pB = bs.pos(pc.bB);
     const V2 lcA = mk(mA.z, mA.w), lcB = mk(mB.z, mB.w);
     float minSep = __int_as_float(0x7f800000);
     auto add = [](float4& p, float x, float y, float a) { p.x = p.x + x; p.y = p.y + y; p.z = p.z + a; };
@@ -713,19 +717,20 @@ __device__ float solve_contact_position(const DW& d, const PC& pc) {
             minSep = s0.sep;
         }
     }
-    if (writable(d, pc.bA)) d.b_pos1[pc.bA] = pA;
-    if (writable(d, pc.bB)) d.b_pos1[pc.bB] = pB;
+    if (bs.writable(pc.bA)) bs.set_pos(pc.bA, pA);
+    if (bs.writable(pc.bB)) bs.set_pos(pc.bB, pB);
     return minSep;
 }
 
 // ---- revolute joints (RevoluteJointConf.cpp:127-431) --------------------------
-__device__ void joint_init_velocity(const DW& d, uint32_t j) {
+template <class BS>
+__device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
     const DConf& c = *d.conf;
     const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
-    const float4 mA = d.b_mass[a], mB = d.b_mass[b];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
     const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
-    const float4 pA = d.b_pos1[a], pB = d.b_pos1[b];
-    float4 vA = d.b_vel[a], vB = d.b_vel[b];
+    const float4 pA = bs.pos(a), pB = bs.pos(b);
+    float4 vA = bs.vel(a), vB = bs.vel(b);
     const float4 an = d.j_anchor[j];
     const float4 prm = d.j_param[j];
     const uint32_t jf = d.j_flags[j];
@@ -772,16 +777,17 @@ __device__ void joint_init_velocity(const DW& d, uint32_t j) {
     d.j_r[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
     d.j_m0[j] = make_float4(exx, eyx, ezx, eyy);
     d.j_m1[j] = make_float4(ezy, totInvI, angularMass, motorImpulse);
-    if (writable(d, a)) d.b_vel[a] = vA;
-    if (writable(d, b)) d.b_vel[b] = vB;
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
 }
 
-__device__ void joint_solve_velocity(const DW& d, uint32_t j) {
+template <class BS>
+__device__ void joint_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
     const DConf& c = *d.conf;
     const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
-    const float4 mA = d.b_mass[a], mB = d.b_mass[b];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
     const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
-    float4 vA = d.b_vel[a], vB = d.b_vel[b];
+    float4 vA = bs.vel(a), vB = bs.vel(b);
     const float4 r = d.j_r[j];
     const float4 m0 = d.j_m0[j];
     float4 m1 = d.j_m1[j];
@@ -817,17 +823,18 @@ __device__ void joint_solve_velocity(const DW& d, uint32_t j) {
     }
     d.j_imp[j] = imp;
     d.j_m1[j] = m1;
-    if (writable(d, a)) d.b_vel[a] = vA;
-    if (writable(d, b)) d.b_vel[b] = vB;
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
 }
 
 // Returns whether the joint is within tolerance.
-__device__ bool joint_solve_position(const DW& d, uint32_t j) {
+template <class BS>
+__device__ bool joint_solve_position(const DW& d, const BS& bs, uint32_t j) {
     const DConf& c = *d.conf;
     const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
-    const float4 mA = d.b_mass[a], mB = d.b_mass[b];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
     const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
-    float4 pA = d.b_pos1[a], pB = d.b_pos1[b];
+    float4 pA = bs.pos(a), pB = bs.pos(b);
     const float4 an = d.j_anchor[j];
     const V2 qA = unit_from_angle(pA.z), qB = unit_from_angle(pB.z);
     const V2 rA = rotate(mk(an.x, an.y) - mk(mA.z, mA.w), qA);
@@ -846,8 +853,8 @@ __device__ bool joint_solve_position(const DW& d, uint32_t j) {
     const V2 P = -x;
     pA.x = pA.x - P.x * iMA; pA.y = pA.y - P.y * iMA; pA.z = pA.z - iIA * cross(rA, P);
     pB.x = pB.x + P.x * iMB; pB.y = pB.y + P.y * iMB; pB.z = pB.z + iIB * cross(rB, P);
-    if (writable(d, a)) d.b_pos1[a] = pA;
-    if (writable(d, b)) d.b_pos1[b] = pB;
+    if (bs.writable(a)) bs.set_pos(a, pA);
+    if (bs.writable(b)) bs.set_pos(b, pB);
     return (positionError <= c.linearSlop * c.linearSlop) && (0.f <= c.angularSlop);
 }
 
@@ -856,46 +863,99 @@ __device__ __forceinline__ uint32_t joint_island(const DW& d, uint32_t j) {
     return is_speedable(d.b_flags[a]) ? d.b_island[a] : d.b_island[d.j_bodies[2 * j + 1]];
 }
 
-// Whether island L reached the position tolerance before iteration `it`.
-__device__ __forceinline__ bool island_done(const DW& d, uint32_t L, int it) {
-    const float thr = d.conf->regMinSeparation;
-    for (int k = 0; k < it; ++k) {
-        const size_t at = (size_t)L * kMaxPosIters + k;
-        if (__ldcg(&d.isl_sep[at]) >= thr && __ldcg(&d.isl_jok[at])) return true;
+// ---- body state during the sweeps ---------------------------------------------
+// The sweeps read and write body velocities and positions through one of two
+// accessors.  GlobalBodies works on the batch arrays in HBM (the grid-wide
+// solve, and worlds too large for shared memory).  SharedBodies works on a
+// copy of one world's velocities and positions in the CTA's shared memory,
+// staged in before the sweeps and written back after; inverse masses and flags,
+// which the sweeps only read, stay in global memory behind the L1 cache.
+// Both run the same arithmetic, so results do not depend on the accessor.
+//
+// Per-island position-iteration state (the minimum separation and the joint
+// tolerance of iteration `it`, and whether the island already reached the
+// tolerance) follows the same split.
+struct GlobalBodies {
+    const DW& d;
+    __device__ __forceinline__ float4 vel(uint32_t b) const { return d.b_vel[b]; }
+    __device__ __forceinline__ void set_vel(uint32_t b, float4 v) const { d.b_vel[b] = v; }
+    __device__ __forceinline__ float4 pos(uint32_t b) const { return d.b_pos1[b]; }
+    __device__ __forceinline__ void set_pos(uint32_t b, float4 p) const { d.b_pos1[b] = p; }
+    __device__ __forceinline__ float4 mass(uint32_t b) const { return d.b_mass[b]; }
+    __device__ __forceinline__ bool writable(uint32_t b) const { return is_accelerable(d.b_flags[b]); }
+    // Whether island L reached the position tolerance before iteration `it`.
+    __device__ __forceinline__ bool island_done(uint32_t L, int it) const {
+        const float thr = d.conf->regMinSeparation;
+        for (int k = 0; k < it; ++k) {
+            const size_t at = (size_t)L * kMaxPosIters + k;
+            if (__ldcg(&d.isl_sep[at]) >= thr && __ldcg(&d.isl_jok[at])) return true;
+        }
+        return false;
     }
-    return false;
-}
+    __device__ __forceinline__ void island_sep(uint32_t L, int it, float sep) const {
+        atomic_min_float(&d.isl_sep[(size_t)L * kMaxPosIters + it], sep);
+    }
+    __device__ __forceinline__ void island_joint_fail(uint32_t L, int it) const {
+        d.isl_jok[(size_t)L * kMaxPosIters + it] = 0u;
+    }
+};
+
+// Shared-memory words per staged body: velocity and position (2 x float4),
+// island separation, joint tolerance and done flag.
+constexpr uint32_t kStageBytesPerBody = 44;
+
+struct SharedBodies {
+    const DW& d;
+    uint32_t base;   // first body of the world
+    float4* v;       // [nb] velocities
+    float4* p;       // [nb] positions
+    float* sep;      // [nb] by island root: min separation of the current position iteration
+    uint32_t* jok;   // [nb] by island root: joints within tolerance in the current iteration
+    uint32_t* done;  // [nb] by island root: tolerance reached in an earlier iteration
+    __device__ __forceinline__ float4 vel(uint32_t b) const { return v[b - base]; }
+    __device__ __forceinline__ void set_vel(uint32_t b, float4 x) const { v[b - base] = x; }
+    __device__ __forceinline__ float4 pos(uint32_t b) const { return p[b - base]; }
+    __device__ __forceinline__ void set_pos(uint32_t b, float4 x) const { p[b - base] = x; }
+    __device__ __forceinline__ float4 mass(uint32_t b) const { return __ldg(&d.b_mass[b]); }
+    __device__ __forceinline__ bool writable(uint32_t b) const { return is_accelerable(__ldg(&d.b_flags[b])); }
+    __device__ __forceinline__ bool island_done(uint32_t L, int) const { return done[L - base] != 0u; }
+    __device__ __forceinline__ void island_sep(uint32_t L, int, float s) const { atomic_min_float(&sep[L - base], s); }
+    __device__ __forceinline__ void island_joint_fail(uint32_t L, int) const { jok[L - base] = 0u; }
+};
 
 // ---- per-constraint sweep steps (t = position in sweep order) -------------------
-__device__ __forceinline__ void sweep_warm(const DW& d, uint32_t t) {
+template <class BS>
+__device__ __forceinline__ void sweep_warm(const DW& d, const BS& bs, uint32_t t) {
     const uint32_t id = d.t_id[t];
-    if (id & kJointBit) joint_init_velocity(d, id & ~kJointBit);
-    else if (d.conf->doWarmStart) warm_start(d, d.vc[t]);
+    if (id & kJointBit) joint_init_velocity(d, bs, id & ~kJointBit);
+    else if (d.conf->doWarmStart) warm_start(d, bs, d.vc[t]);
 }
 
-__device__ __forceinline__ void sweep_velocity(const DW& d, uint32_t t) {
+template <class BS>
+__device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32_t t) {
     const uint32_t id = d.t_id[t];
     if (id & kJointBit) {
-        joint_solve_velocity(d, id & ~kJointBit);
+        joint_solve_velocity(d, bs, id & ~kJointBit);
     } else {
         VC vc = d.vc[t];
-        solve_contact_velocity(d, vc);
+        solve_contact_velocity(d, bs, vc);
         reinterpret_cast<float4*>(&d.vc[t])[6] = make_float4(vc.ni0, vc.ti0, vc.ni1, vc.ti1);
     }
 }
 
-__device__ __forceinline__ void sweep_position(const DW& d, uint32_t t, int it) {
+template <class BS>
+__device__ __forceinline__ void sweep_position(const DW& d, const BS& bs, uint32_t t, int it) {
     const uint32_t id = d.t_id[t];
     if (id & kJointBit) {
         const uint32_t j = id & ~kJointBit;
         const uint32_t L = joint_island(d, j);
-        if (island_done(d, L, it)) return;
-        if (!joint_solve_position(d, j)) d.isl_jok[(size_t)L * kMaxPosIters + it] = 0u;
+        if (bs.island_done(L, it)) return;
+        if (!joint_solve_position(d, bs, j)) bs.island_joint_fail(L, it);
     } else {
         const PC pc = d.pc[t];
-        if (island_done(d, pc.island, it)) return;
-        const float sep = solve_contact_position(d, pc);
-        atomic_min_float(&d.isl_sep[(size_t)pc.island * kMaxPosIters + it], sep);
+        if (bs.island_done(pc.island, it)) return;
+        const float sep = solve_contact_position(d, bs, pc);
+        bs.island_sep(pc.island, it, sep);
     }
 }
 
@@ -914,14 +974,15 @@ __device__ __forceinline__ void store_impulses(const DW& d, uint32_t t) {
 }
 
 // IntegratePositions (AabbTreeWorld.cpp:176-188)
-__device__ __forceinline__ void integrate_body(const DW& d, uint32_t b) {
+template <class BS>
+__device__ __forceinline__ void integrate_body(const DW& d, const BS& bs, uint32_t b) {
     if (!(d.b_flags[b] & BF_SOLVED)) return;
     const float h = d.conf->deltaTime;
-    const float4 v = d.b_vel[b];
-    float4 p = d.b_pos1[b];
+    const float4 v = bs.vel(b);
+    float4 p = bs.pos(b);
     const float tx = v.x * h, ty = v.y * h, rot = h * v.z;
     p.x = p.x + tx; p.y = p.y + ty; p.z = p.z + rot;
-    d.b_pos1[b] = p;
+    bs.set_pos(b, p);
 }
 
 // The whole regular-phase solve of a step over the batch: warm start, velocity
@@ -945,13 +1006,14 @@ __global__ void k_solve(DW d) {
         }
         grid_barrier(d.cnt);
     };
-    for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_warm(d, t); });
+    const GlobalBodies bs{d};
+    for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_warm(d, bs, t); });
     for (int it = 0; it < c.regVelocityIters; ++it)
-        for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, t); });
-    GRID_LOOP(b, d.n_bodies) integrate_body(d, b);
+        for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, bs, t); });
+    GRID_LOOP(b, d.n_bodies) integrate_body(d, bs, b);
     grid_barrier(d.cnt);
     for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it)
-        for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_position(d, t, it); });
+        for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_position(d, bs, t, it); });
     GRID_LOOP(t, d.cnt->n_active) store_impulses(d, t);
 }
 
@@ -1000,10 +1062,45 @@ struct WarpGroup {
     }
 };
 
+// The sweeps of one world by one group, over its segment [base, base + n) of
+// sweep order with colour offsets col_off; after_position(it) runs after each
+// position iteration.
+template <class G, class BS, class F>
+__device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uint32_t size, uint32_t base,
+                       uint32_t n, const uint32_t* col_off, F&& after_position) {
+    const DConf& c = *d.conf;
+    // Runs f(t) over colour col of this world, then synchronises the group.
+    auto sweep = [&](int col, auto&& f) {
+        const uint32_t lo = base + col_off[col], hi = base + col_off[col + 1];
+        if (lo == hi) return;
+        if (col == kSerialColour) {
+            if (rank == 0) for (uint32_t t = lo; t < hi; ++t) f(t);
+        } else {
+            for (uint32_t t = lo + rank; t < hi; t += size) f(t);
+        }
+        G::sync();
+    };
+    if (n) {
+        for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_warm(d, bs, t); });
+        for (int it = 0; it < c.regVelocityIters; ++it)
+            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, bs, t); });
+    }
+    for (uint32_t b = d.w_body_off[w] + rank; b < d.w_body_off[w + 1]; b += size) integrate_body(d, bs, b);
+    G::sync();
+    if (n) {
+        for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it) {
+            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_position(d, bs, t, it); });
+            after_position(it);
+        }
+        for (uint32_t t = base + rank; t < base + n; t += size) store_impulses(d, t);
+    }
+    G::sync();
+}
+
 // col_cnt / col_off: kColStride words of shared memory owned by the group.
 template <class G>
 __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t size, uint32_t* col_cnt,
-                            uint32_t* col_off) {
+                            uint32_t* col_off, void* stage, uint32_t stage_cap) {
     const DConf& c = *d.conf;
     const uint32_t c0 = d.w_kc[w], c1 = d.w_kc[w + 1], j0 = d.w_kj[w], j1 = d.w_kj[w + 1];
     const uint32_t ncw = c1 - c0, n = ncw + (j1 - j0);
@@ -1060,28 +1157,46 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
         for (uint32_t t = base + rank; t < base + n; t += size) build_constraint(d, t, d.k_order[t]);
         G::sync();
     }
-    // Runs f(t) over colour col of this world, then synchronises the group.
-    auto sweep = [&](int col, auto&& f) {
-        const uint32_t lo = base + col_off[col], hi = base + col_off[col + 1];
-        if (lo == hi) return;
-        if (col == kSerialColour) {
-            if (rank == 0) for (uint32_t t = lo; t < hi; ++t) f(t);
-        } else {
-            for (uint32_t t = lo + rank; t < hi; t += size) f(t);
+    const uint32_t b0 = d.w_body_off[w], nb = d.w_body_off[w + 1] - b0;
+    if (nb <= stage_cap) {
+        // stage the world's velocities and positions in shared memory
+        float4* sv = reinterpret_cast<float4*>(stage);
+        float4* sp = sv + stage_cap;
+        float* ssep = reinterpret_cast<float*>(sp + stage_cap);
+        uint32_t* sjok = reinterpret_cast<uint32_t*>(ssep + stage_cap);
+        uint32_t* sdone = sjok + stage_cap;
+        for (uint32_t i = rank; i < nb; i += size) {
+            sv[i] = d.b_vel[b0 + i];
+            sp[i] = d.b_pos1[b0 + i];
+            ssep[i] = __int_as_float(0x7f800000);
+            sjok[i] = 1u;
+            sdone[i] = 0u;
         }
         G::sync();
-    };
-    if (n) {
-        for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_warm(d, t); });
-        for (int it = 0; it < c.regVelocityIters; ++it)
-            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, t); });
-    }
-    for (uint32_t b = d.w_body_off[w] + rank; b < d.w_body_off[w + 1]; b += size) integrate_body(d, b);
-    G::sync();
-    if (n) {
-        for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it)
-            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_position(d, t, it); });
-        for (uint32_t t = base + rank; t < base + n; t += size) store_impulses(d, t);
+        const SharedBodies bs{d, b0, sv, sp, ssep, sjok, sdone};
+        // after each position iteration: publish the islands' figures for the
+        // sleep pass, fold them into the early-exit flags and reset them
+        auto island_pass = [&](int it) {
+            const float thr = c.regMinSeparation;
+            for (uint32_t i = rank; i < nb; i += size) {
+                if (d.b_island[b0 + i] != b0 + i || !(d.b_flags[b0 + i] & BF_SOLVED)) continue;
+                const size_t at = (size_t)(b0 + i) * kMaxPosIters + it;
+                d.isl_sep[at] = ssep[i];
+                d.isl_jok[at] = sjok[i];
+                if (ssep[i] >= thr && sjok[i]) sdone[i] = 1u;
+                ssep[i] = __int_as_float(0x7f800000);
+                sjok[i] = 1u;
+            }
+            G::sync();
+        };
+        sweeps<G>(d, bs, w, rank, size, base, n, col_off, island_pass);
+        for (uint32_t i = rank; i < nb; i += size) {
+            d.b_vel[b0 + i] = sv[i];
+            d.b_pos1[b0 + i] = sp[i];
+        }
+    } else {
+        const GlobalBodies bs{d};
+        sweeps<G>(d, bs, w, rank, size, base, n, col_off, [](int) {});
     }
     G::sync();  // the group's shared words are reused by its next world
 }
@@ -1089,7 +1204,8 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
 // Persistent CTAs take worlds from a queue ordered by decreasing body count.
 // The first n_world_big entries are solved by a whole CTA each; once a CTA
 // meets a smaller world, each of its warps takes worlds on its own.
-__global__ void __launch_bounds__(256) k_world_solve(DW d) {
+__global__ void __launch_bounds__(256, 4) k_world_solve(DW d) {
+    extern __shared__ float4 s_stage[];  // d.stage_bytes: body state of the world(s) being solved
     __shared__ uint32_t s_w;
     __shared__ uint32_t s_col[8][2][kColStride];
     uint32_t qi;
@@ -1100,9 +1216,13 @@ __global__ void __launch_bounds__(256) k_world_solve(DW d) {
         qi = s_w;
         if (qi >= d.n_worlds) return;
         if (qi >= d.n_world_big) break;
-        solve_world<BlockGroup>(d, d.w_order[qi], threadIdx.x, blockDim.x, s_col[0][0], s_col[0][1]);
+        solve_world<BlockGroup>(d, d.w_order[qi], threadIdx.x, blockDim.x, s_col[0][0], s_col[0][1], s_stage,
+                                d.stage_bytes / kStageBytesPerBody);
     }
+    // each warp owns an eighth of the staging area
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t part = d.stage_bytes / 8u;
+    void* stage = reinterpret_cast<char*>(s_stage) + (size_t)warp * part;
     auto next = [&]() {
         uint32_t x = 0u;
         if (lane == 0) x = atomicAdd(&d.cnt->world_queue, 1u);
@@ -1110,7 +1230,8 @@ __global__ void __launch_bounds__(256) k_world_solve(DW d) {
     };
     if (warp != 0) qi = next();  // warp 0 keeps the entry the CTA took
     while (qi < d.n_worlds) {
-        solve_world<WarpGroup>(d, d.w_order[qi], lane, 32u, s_col[warp][0], s_col[warp][1]);
+        solve_world<WarpGroup>(d, d.w_order[qi], lane, 32u, s_col[warp][0], s_col[warp][1], stage,
+                               part / kStageBytesPerBody);
         qi = next();
     }
 }
@@ -1267,12 +1388,25 @@ void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) {
         return;
     }
     cudaMemsetAsync(&d.cnt->world_queue, 0, sizeof(uint32_t), s);
-    k_world_solve<<<L.world_grid, 256, 0, s>>>(d);
+    k_world_solve<<<L.world_grid, 256, d.stage_bytes, s>>>(d);
 }
 
-int world_blocks_per_sm() {
+int world_blocks_per_sm(uint32_t stage_bytes) {
+    // The attribute is per function and per process: keep it at the largest
+    // size any batch asked for, so every batch's launches stay valid.
+    static std::mutex mu;
+    static uint32_t set_bytes = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (stage_bytes > set_bytes) {
+            if (cudaFuncSetAttribute(k_world_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes) !=
+                cudaSuccess)
+                return 0;
+            set_bytes = stage_bytes;
+        }
+    }
     int a = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_world_solve, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_world_solve, 256, stage_bytes);
     return a;
 }
 

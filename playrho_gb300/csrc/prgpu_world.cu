@@ -378,6 +378,12 @@ int bits_for(uint64_t n) {
 constexpr int kPhases = 7;
 // Batches of at least this many worlds sweep one world per CTA by default.
 constexpr uint32_t kPerWorldMinWorlds = 64;
+// Shared memory of the per-world solver for staging body state (44 bytes a
+// body; a warp gets an eighth).  0 by default: staging costs CTAs per SM, and
+// the sweeps are bound by latency that staging does not remove; the autotuner
+// tries it.
+constexpr uint32_t kStageBytes = 0u;
+constexpr uint32_t kStageChoices[] = {0u, 1024u * 44u, 2048u * 44u};
 // Worlds of at most this many bodies are swept by one warp by default.
 constexpr uint32_t kWarpWorldMaxBodies = 256;
 
@@ -718,7 +724,10 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     if (per_sm < 1) return bail(fail(w, PRGPU_ECUDA, "cooperative kernels cannot be resident"));
     w->L.coop_grid = w->L.prims.sm_count * std::min(per_sm, 4);
     {
-        const int wps = world_blocks_per_sm();
+        d.stage_bytes = kStageBytes;
+        const int wps = world_blocks_per_sm(d.stage_bytes);
+        if (wps < 1) return bail(fail(w, PRGPU_ECUDA, "per-world sweep kernel cannot be resident"));
+        for (uint32_t sb : kStageChoices) world_blocks_per_sm(sb);  // raise the attribute once
         if (wps < 1) return bail(fail(w, PRGPU_ECUDA, "per-world sweep kernel cannot be resident"));
         w->L.world_grid = w->L.prims.sm_count * wps;
         w->L.per_world = W >= kPerWorldMinWorlds;
@@ -917,10 +926,11 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
     if (!w || !conf || steps_per_candidate < 1) return PRGPU_EINVAL;
     if (conf->deltaTime == 0.f) return fail(w, PRGPU_EINVAL, "autotune needs a step with deltaTime > 0");
     CU(cudaSetDevice(w->device));
-    struct Cand { int mode; uint32_t warp_max; };
-    std::vector<Cand> cands = {{PRGPU_SWEEPS_GRID, w->warp_world_max}};
+    struct Cand { int mode; uint32_t warp_max; uint32_t stage; };
+    std::vector<Cand> cands = {{PRGPU_SWEEPS_GRID, w->warp_world_max, w->d.stage_bytes}};
     if (w->d.n_worlds > 1) {
-        for (uint32_t m : {0u, 64u, 128u, 256u, 512u, 1024u, 0xffffffffu}) cands.push_back({PRGPU_SWEEPS_PER_WORLD, m});
+        for (uint32_t sb : kStageChoices)
+            for (uint32_t m : {0u, 64u, 128u, 256u, 1024u}) cands.push_back({PRGPU_SWEEPS_PER_WORLD, m, sb});
     }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CU(cudaEventCreate(&e0));
@@ -931,6 +941,7 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
     for (const Cand& cd : cands) {
         if ((rc = prgpu_set_sweep_mode(w, cd.mode)) != PRGPU_OK) break;
         if ((rc = prgpu_set_warp_world_max_bodies(w, cd.warp_max)) != PRGPU_OK) break;
+        if ((rc = prgpu_set_stage_bytes(w, cd.stage)) != PRGPU_OK) break;
         if ((rc = run_steps(w, conf, 1, true)) != PRGPU_OK) break;  // captures the candidate's step
         if (cudaEventRecord(e0, w->stream) != cudaSuccess) { rc = PRGPU_ECUDA; break; }
         if ((rc = run_steps(w, conf, steps_per_candidate, false)) != PRGPU_OK) break;
@@ -946,11 +957,33 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
     if (rc) return rc;
     if ((rc = prgpu_set_sweep_mode(w, pick.mode)) != PRGPU_OK) return rc;
     if ((rc = prgpu_set_warp_world_max_bodies(w, pick.warp_max)) != PRGPU_OK) return rc;
+    if ((rc = prgpu_set_stage_bytes(w, pick.stage)) != PRGPU_OK) return rc;
     if (best) {
         best->sweep_mode = pick.mode;
         best->warp_world_max_bodies = pick.warp_max;
+        best->stage_bytes = pick.stage;
         best->step_ms = best_ms;
     }
+    return PRGPU_OK;
+}
+
+int prgpu_set_stage_bytes(prgpu_world* w, uint32_t bytes) {
+    if (!w) return PRGPU_EINVAL;
+    if (bytes % 128u != 0u || bytes > 200u * 1024u) return fail(w, PRGPU_EINVAL, "stage bytes must be a multiple of 128, <= 200 KiB");
+    if (bytes == w->d.stage_bytes) return PRGPU_OK;
+    CU(cudaSetDevice(w->device));
+    const int wps = world_blocks_per_sm(bytes);
+    if (wps < 1) return fail(w, PRGPU_EINVAL, "per-world solver cannot be resident with %u bytes of staging", bytes);
+    const int rc = drop_graph(w);
+    if (rc) return rc;
+    w->d.stage_bytes = bytes;
+    w->L.world_grid = w->L.prims.sm_count * wps;
+    return PRGPU_OK;
+}
+
+int prgpu_get_stage_bytes(prgpu_world* w, uint32_t* bytes) {
+    if (!w || !bytes) return PRGPU_EINVAL;
+    *bytes = w->d.stage_bytes;
     return PRGPU_OK;
 }
 

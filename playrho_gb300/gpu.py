@@ -56,7 +56,7 @@ class BatchDesc(ctypes.Structure):
 
 class Schedule(ctypes.Structure):
     _fields_ = [("sweep_mode", ctypes.c_int32), ("warp_world_max_bodies", ctypes.c_uint32),
-                ("step_ms", ctypes.c_float)]
+                ("stage_bytes", ctypes.c_uint32), ("step_ms", ctypes.c_float)]
 
 
 class PrgpuError(RuntimeError):
@@ -101,6 +101,8 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_get_sweep_mode.argtypes = [P, P]
     lib.prgpu_set_warp_world_max_bodies.argtypes = [P, U]
     lib.prgpu_get_warp_world_max_bodies.argtypes = [P, P]
+    lib.prgpu_set_stage_bytes.argtypes = [P, U]
+    lib.prgpu_get_stage_bytes.argtypes = [P, P]
     lib.prgpu_autotune.argtypes = [P, ctypes.POINTER(StepConf), I, ctypes.POINTER(Schedule)]
     _LIB = lib
     return lib
@@ -113,7 +115,8 @@ def exported_symbols() -> List[str]:
         "prgpu_download_bodies", "prgpu_upload_body_states", "prgpu_download_contacts",
         "prgpu_download_proxies", "prgpu_last_error", "prgpu_convex_hull", "prgpu_prepare_bodies", "prgpu_step_profiled",
         "prgpu_last_step_phase_ms", "prgpu_graph_kernel_count", "prgpu_set_sweep_mode", "prgpu_get_sweep_mode",
-        "prgpu_set_warp_world_max_bodies", "prgpu_get_warp_world_max_bodies", "prgpu_autotune"]
+        "prgpu_set_warp_world_max_bodies", "prgpu_get_warp_world_max_bodies", "prgpu_autotune",
+        "prgpu_set_stage_bytes", "prgpu_get_stage_bytes"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -301,6 +304,15 @@ class GpuBatch:
         self._check(self.lib.prgpu_get_warp_world_max_bodies(self.h, ctypes.byref(m)), "warp world limit")
         return int(m.value)
 
+    def set_stage_bytes(self, n: int):
+        """Shared memory for staging a world's body state in the per-world solver (0: off)."""
+        self._check(self.lib.prgpu_set_stage_bytes(self.h, int(n)), "stage bytes")
+
+    def stage_bytes(self) -> int:
+        m = ctypes.c_uint32(0)
+        self._check(self.lib.prgpu_get_stage_bytes(self.h, ctypes.byref(m)), "stage bytes")
+        return int(m.value)
+
     def autotune(self, steps_per_candidate: int = 3, conf: StepConf | None = None) -> dict:
         """Times the candidate sweep schedules (advancing the world) and keeps the fastest."""
         c = conf if conf is not None else default_conf()
@@ -309,7 +321,7 @@ class GpuBatch:
                     "prgpu_autotune")
         inv = {v: k for k, v in self.SWEEP_MODES.items()}
         return {"sweeps": inv[sc.sweep_mode], "warp_world_max_bodies": int(sc.warp_world_max_bodies),
-                "step_ms": float(sc.step_ms)}
+                "stage_bytes": int(sc.stage_bytes), "step_ms": float(sc.step_ms)}
 
     def step_async(self, n: int, conf: StepConf):
         self._check(self.lib.prgpu_step_async(self.h, ctypes.byref(conf), int(n)), "prgpu_step_async")

@@ -160,13 +160,17 @@ def test_sweep_modes_agree(gpu_lib):
     assert b.sweep_mode() == "grid"
     c.set_warp_world_max_bodies(0)
     e.set_warp_world_max_bodies(2 ** 32 - 1)
+    f = GpuBatch(worlds)  # per world, body state staged in shared memory
+    f.set_stage_bytes(2048 * 44)
+    assert f.stage_bytes() == 2048 * 44
     for i in range(90):
-        for g in (a, b, c, e):
+        for g in (a, b, c, e, f):
             g.step()
         if i == 40:  # switching schedule mid-run recaptures the step and changes nothing
             a.set_warp_world_max_bodies(64)
+            e.set_stage_bytes(1024 * 44)
     ba = a.bodies()
-    for g in (b, c, e):
+    for g in (b, c, e, f):
         bg = g.bodies()
         np.testing.assert_array_equal(ba["pos"], bg["pos"])
         np.testing.assert_array_equal(ba["vel"], bg["vel"])
@@ -181,7 +185,7 @@ def test_autotune_keeps_results(gpu_lib):
     a, b = GpuBatch(worlds), GpuBatch(worlds)
     best = a.autotune(steps_per_candidate=2)
     assert best["sweeps"] in ("grid", "per_world") and best["step_ms"] > 0
-    n_cand = 1 + 7
+    n_cand = 1 + 3 * 5  # the grid, then 3 staging sizes x 5 warp-world limits
     b.step_n(n_cand * 3)
     np.testing.assert_array_equal(a.bodies()["pos"], b.bodies()["pos"])
     np.testing.assert_array_equal(a.bodies()["vel"], b.bodies()["vel"])
