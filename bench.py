@@ -337,10 +337,14 @@ def run_ours(args, rank, world_size, local, dist):
         return
     cpu = None if args.no_cpu_baseline else cpu_baseline_sample(worlds)
     clocks = clk.summary()
+    # DRAM bytes of one solver launch on this workload, from the ncu capture
+    # summarised in profiles/ (a profiler run is never part of the bench)
     traffic = None
     try:
-        with open(os.path.join(ROOT, "profiles", "sweeps_traffic.json")) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch_scaled")
+        with open(os.path.join(ROOT, "profiles", "k_world_solve_1024_full.md")) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch:"):
+                    traffic = float(line.split(":")[1])
     except Exception:
         pass
     out = {
@@ -358,7 +362,7 @@ def run_ours(args, rank, world_size, local, dist):
                                 "autotuned": schedule is not None}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic,
-                     "kernel": ("k_solve_world (Gauss-Seidel colour sweeps, one CTA per world)"
+                     "kernel": ("k_world_solve (per-world colouring, constraint build and Gauss-Seidel sweeps)"
                                 if batch.sweep_mode() == "per_world" else
                                 "k_solve (Gauss-Seidel colour sweeps, cooperative grid)"),
                      "peak_source": peak_kind, "launch_ms": sweeps_ms, "algorithmic_bytes": bytes_sweep},
