@@ -58,8 +58,10 @@ constexpr int kColStride = kSerialColour + 2;  // colour table of one world: off
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr uint32_t kNone = 0xffffffffu;
 
-// Velocity constraint of one contact (VelocityConstraint.hpp), 160 bytes.
-struct __align__(16) VC {
+// Velocity constraint of one contact (VelocityConstraint.hpp) as the solver
+// holds it in registers.  Point-1 and block-solver fields are zero unless
+// count == 2.
+struct VC {
     float nx, ny, friction, tangentSpeed;
     float rA0x, rA0y, rB0x, rB0y;
     float rA1x, rA1y, rB1x, rB1y;
@@ -68,7 +70,16 @@ struct __align__(16) VC {
     float k01, m00, m11, m01;
     float ni0, ti0, ni1, ti1;
     uint32_t bA, bB, count, island;
-    uint32_t slot, pad0, pad1, pad2;
+};
+
+// In memory a velocity constraint is two 64-byte records at its sweep
+// position t: VC0 holds what every contact needs, VC1 the second point and
+// the 2x2 block-solver matrices, read only when count == 2.  A one-point
+// contact so streams 64 bytes a sweep and a two-point one 128.
+//   VC0: nx ny friction tangentSpeed | rA0 rB0 | nm0 tm0 vb0 count | ni0 ti0 bA bB
+//   VC1: rA1 rB1 | nm1 tm1 vb1 k00 | k11 k01 m00 m11 | ni1 ti1 m01 -
+struct __align__(16) VCRec {
+    float4 q[4];
 };
 
 // Position constraint of one contact (PositionConstraint.hpp), 64 bytes.
@@ -228,7 +239,8 @@ struct DW {
     uint32_t* inc_off;       // body -> active constraint incidence CSR
     uint32_t* inc_cur;
     uint32_t* inc_list;
-    VC* vc;
+    VCRec* vc0;              // [contact capacity] velocity constraints in sweep order, first record
+    VCRec* vc1;              // second record (two-point contacts)
     PC* pc;
     // scan scratch
     uint32_t* flags;

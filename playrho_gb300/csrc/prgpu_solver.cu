@@ -381,7 +381,54 @@ __global__ void k_colour(DW d) {
 // ---- constraint construction --------------------------------------------------
 // GetWorldManifold (WorldManifold.cpp:111-132), VelocityConstraint ctor +
 // GetPoint + ComputeK (VelocityConstraint.cpp:38-185), PositionConstraint.
-// Builds the constraint at sweep position t (vc[t], pc[t]) for constraint k.
+// ---- velocity constraint records -------------------------------------------------
+__device__ __forceinline__ void store_vc(const DW& d, uint32_t t, const VC& v) {
+    float4* r0 = d.vc0[t].q;
+    r0[0] = make_float4(v.nx, v.ny, v.friction, v.tangentSpeed);
+    r0[1] = make_float4(v.rA0x, v.rA0y, v.rB0x, v.rB0y);
+    r0[2] = make_float4(v.nm0, v.tm0, v.vb0, __uint_as_float(v.count));
+    r0[3] = make_float4(v.ni0, v.ti0, __uint_as_float(v.bA), __uint_as_float(v.bB));
+    if (v.count == 2u) {
+        float4* r1 = d.vc1[t].q;
+        r1[0] = make_float4(v.rA1x, v.rA1y, v.rB1x, v.rB1y);
+        r1[1] = make_float4(v.nm1, v.tm1, v.vb1, v.k00);
+        r1[2] = make_float4(v.k11, v.k01, v.m00, v.m11);
+        r1[3] = make_float4(v.ni1, v.ti1, v.m01, 0.f);
+    }
+}
+
+__device__ __forceinline__ VC load_vc(const DW& d, uint32_t t) {
+    const float4* r0 = d.vc0[t].q;
+    const float4 a = r0[0], b = r0[1], c = r0[2], e = r0[3];
+    VC v;
+    v.nx = a.x; v.ny = a.y; v.friction = a.z; v.tangentSpeed = a.w;
+    v.rA0x = b.x; v.rA0y = b.y; v.rB0x = b.z; v.rB0y = b.w;
+    v.nm0 = c.x; v.tm0 = c.y; v.vb0 = c.z; v.count = __float_as_uint(c.w);
+    v.ni0 = e.x; v.ti0 = e.y; v.bA = __float_as_uint(e.z); v.bB = __float_as_uint(e.w);
+    v.island = 0u;
+    if (v.count == 2u) {
+        const float4* r1 = d.vc1[t].q;
+        const float4 f = r1[0], g = r1[1], h = r1[2], i = r1[3];
+        v.rA1x = f.x; v.rA1y = f.y; v.rB1x = f.z; v.rB1y = f.w;
+        v.nm1 = g.x; v.tm1 = g.y; v.vb1 = g.z; v.k00 = g.w;
+        v.k11 = h.x; v.k01 = h.y; v.m00 = h.z; v.m11 = h.w;
+        v.ni1 = i.x; v.ti1 = i.y; v.m01 = i.z;
+    } else {
+        v.rA1x = v.rA1y = v.rB1x = v.rB1y = 0.f;
+        v.nm1 = v.tm1 = v.vb1 = 0.f;
+        v.k00 = v.k11 = v.k01 = v.m00 = v.m11 = v.m01 = 0.f;
+        v.ni1 = v.ti1 = 0.f;
+    }
+    return v;
+}
+
+// Writes back the accumulated impulses of the constraint at t.
+__device__ __forceinline__ void store_vc_impulses(const DW& d, uint32_t t, const VC& v) {
+    reinterpret_cast<float2*>(d.vc0[t].q)[6] = make_float2(v.ni0, v.ti0);
+    if (v.count == 2u) reinterpret_cast<float2*>(d.vc1[t].q)[6] = make_float2(v.ni1, v.ti1);
+}
+
+// Builds the constraint at sweep position t (vc0/vc1[t], pc[t]) for constraint k.
 __device__ void build_constraint(const DW& d, uint32_t t, uint32_t k) {
     const DConf& c = *d.conf;
     {
@@ -434,7 +481,7 @@ __device__ void build_constraint(const DW& d, uint32_t t, uint32_t k) {
         const float2 mat = d.cs_mat[slot];
         VC vc;
         vc.nx = n.x; vc.ny = n.y; vc.friction = mat.x; vc.tangentSpeed = 0.f;
-        vc.bA = bd.x; vc.bB = bd.y; vc.slot = slot;
+        vc.bA = bd.x; vc.bB = bd.y;
         vc.island = is_speedable(d.b_flags[bd.x]) ? d.b_island[bd.x] : d.b_island[bd.y];
         const float invMass = mA.x + mB.x;
         const V2 tangent = fwdperp(n);
@@ -495,8 +542,7 @@ __device__ void build_constraint(const DW& d, uint32_t t, uint32_t k) {
             vc.nm1 = vc.tm1 = vc.vb1 = vc.ni1 = vc.ti1 = 0.f;
         }
         vc.k00 = k00; vc.k11 = k11; vc.k01 = k01; vc.m00 = m00; vc.m11 = m11; vc.m01 = m01;
-        vc.pad0 = vc.pad1 = vc.pad2 = 0u;
-        d.vc[t] = vc;
+        store_vc(d, t, vc);
         PC pcs;
         pcs.lnx = ln.x; pcs.lny = ln.y; pcs.lpx = lp.x; pcs.lpy = lp.y;
         pcs.p0x = plp[0].x; pcs.p0y = plp[0].y; pcs.p1x = plp[1].x; pcs.p1y = plp[1].y;
@@ -928,7 +974,7 @@ template <class BS>
 __device__ __forceinline__ void sweep_warm(const DW& d, const BS& bs, uint32_t t) {
     const uint32_t id = d.t_id[t];
     if (id & kJointBit) joint_init_velocity(d, bs, id & ~kJointBit);
-    else if (d.conf->doWarmStart) warm_start(d, bs, d.vc[t]);
+    else if (d.conf->doWarmStart) warm_start(d, bs, load_vc(d, t));
 }
 
 template <class BS>
@@ -937,9 +983,9 @@ __device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32
     if (id & kJointBit) {
         joint_solve_velocity(d, bs, id & ~kJointBit);
     } else {
-        VC vc = d.vc[t];
+        VC vc = load_vc(d, t);
         solve_contact_velocity(d, bs, vc);
-        reinterpret_cast<float4*>(&d.vc[t])[6] = make_float4(vc.ni0, vc.ti0, vc.ni1, vc.ti1);
+        store_vc_impulses(d, t, vc);
     }
 }
 
@@ -961,15 +1007,18 @@ __device__ __forceinline__ void sweep_position(const DW& d, const BS& bs, uint32
 
 // AssignImpulses (AabbTreeWorld.cpp:196-220)
 __device__ __forceinline__ void store_impulses(const DW& d, uint32_t t) {
-    if (d.t_id[t] & kJointBit) return;
-    const VC& vc = d.vc[t];
-    float4 p0 = d.m_p0[vc.slot];
-    p0.z = vc.ni0; p0.w = vc.ti0;
-    d.m_p0[vc.slot] = p0;
-    if (vc.count == 2u) {
-        float4 p1 = d.m_p1[vc.slot];
-        p1.z = vc.ni1; p1.w = vc.ti1;
-        d.m_p1[vc.slot] = p1;
+    const uint32_t slot = d.t_id[t];
+    if (slot & kJointBit) return;
+    const float4 e = d.vc0[t].q[3];
+    const uint32_t count = __float_as_uint(d.vc0[t].q[2].w);
+    float4 p0 = d.m_p0[slot];
+    p0.z = e.x; p0.w = e.y;
+    d.m_p0[slot] = p0;
+    if (count == 2u) {
+        const float4 i = d.vc1[t].q[3];
+        float4 p1 = d.m_p1[slot];
+        p1.z = i.x; p1.w = i.y;
+        d.m_p1[slot] = p1;
     }
 }
 

@@ -700,7 +700,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.t_id, C + J);
     AL(d.k_prio, C + J);
     AL(d.inc_off, N + 1); AL(d.inc_cur, N + 1); AL(d.inc_list, 2 * ((size_t)C + J));
-    AL(d.vc, C); AL(d.pc, C);
+    AL(d.vc0, C); AL(d.vc1, C); AL(d.pc, C);
     AL(d.flags, items); AL(d.scan, items);
     w->L.prims.sm_count = 1;
     {
