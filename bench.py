@@ -47,20 +47,38 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--worlds", type=int, default=4096)
-    p.add_argument("--settle", type=int, default=240,
-                   help="untimed steps that bring the scenes to their contact-rich state")
+    p.add_argument("--settle", type=int, default=None,
+                   help="untimed steps that bring the scenes to their contact-rich state (default per workload)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--sweeps", default="auto", choices=["auto", "grid", "per_world"],
                    help="scheduling of the colour sweeps (auto: one CTA per world for >= 64 worlds)")
     p.add_argument("--kernels-only", action="store_true",
                    help="only the warm-up and timed steps (for a profiler launch list)")
+    p.add_argument("--workload", default="batched", choices=list(WORKLOADS),
+                   help="batched: the headline batch (default); world100k: one world of 100,000 shapes in a "
+                        "1000 m box; chains256: 256 worlds of 8,000 free shapes + 64 revolute chains of 32 links")
     return p.parse_args()
 
 
-def workload(n_worlds):
+# name -> (description, step configuration overrides, default settling steps)
+WORKLOADS = {
+    "batched": ("batched worlds: {n} worlds, log-uniform 16..2048 bodies, pyramids + piles, seed 1", {}, 240),
+    "world100k": ("one world: 100,000 shapes (disks + 3..8-gons) in a 1000 m box, seed 0", {}, 60),
+    "chains256": ("{n} worlds x (8,000 free shapes + 64 chains x 32 links on revolute joints), seed 3",
+                  {"deltaTime": 1.0 / 120.0, "regVelocityIters": 10, "regPositionIters": 4}, 120),
+}
+
+
+def workload(args):
     from playrho_gb300 import scenes
 
-    return scenes.batched_worlds(n_worlds, seed=1)
+    if args.workload == "world100k":
+        return [scenes.large_box(100_000, 1000.0, seed=0)]
+    if args.workload == "chains256":
+        rng = np.random.default_rng(3)
+        n = args.worlds if args.worlds != 4096 else 256
+        return [scenes.chains_world(rng) for _ in range(n)]
+    return scenes.batched_worlds(args.worlds, seed=1)
 
 
 def dist_setup(args):
@@ -166,20 +184,21 @@ def sweep_bytes(stats, conf, n_bodies_solved):
     return nc * per_contact + n_bodies_solved * 52
 
 
-def cpu_baseline_sample(worlds, seconds=8.0):
+def cpu_baseline_sample(worlds, overrides=None, seconds=8.0):
     """Times the single-threaded oracle on a bounded sample of the workload."""
     from oracle import oracle
 
+    overrides = overrides or {}
     sample = worlds[: max(1, len(worlds) // 16)]
     ows = [oracle.OracleWorld(w) for w in sample]
     for o in ows:
-        o.step()
+        o.step(**overrides)
     nb = sum(int((w.body_type == 2).sum()) for w in sample)
     steps = 0
     t0 = time.perf_counter()
     while True:
         for o in ows:
-            o.step()
+            o.step(**overrides)
         steps += 1
         if time.perf_counter() - t0 > seconds or steps >= 200:
             break
@@ -246,11 +265,14 @@ def run_ours(args, rank, world_size, local, dist):
     from playrho_gb300 import build, gpu
 
     build.build()
-    worlds = workload(args.worlds)
+    worlds = workload(args)
+    desc, overrides, settle = WORKLOADS[args.workload]
+    if args.settle is None:
+        args.settle = settle
     n_dyn = sum(int((w.body_type == 2).sum()) for w in worlds)
     batch = gpu.GpuBatch(worlds, device=local)
     batch.set_sweep_mode(args.sweeps)
-    conf = gpu.default_conf()
+    conf = gpu.default_conf(**overrides)
     # Scene preparation: advance the batch `settle` steps (piles land, pyramids take
     # their load) so the measured steps are the contact-rich middle of the run,
     # then W warm-up steps.  The first step creates every proxy and contact, as
@@ -335,12 +357,14 @@ def run_ours(args, rank, world_size, local, dist):
 
     if rank != 0:
         return
-    cpu = None if args.no_cpu_baseline else cpu_baseline_sample(worlds)
+    cpu = None if args.no_cpu_baseline else cpu_baseline_sample(worlds, overrides)
     clocks = clk.summary()
     # DRAM bytes of one solver launch on this workload, from the ncu capture
     # summarised in profiles/ (a profiler run is never part of the bench)
     traffic = None
     try:
+        if args.workload != "batched" or args.worlds != 4096:
+            raise FileNotFoundError("the capture covers the default batch only")
         with open(os.path.join(ROOT, "profiles", "k_world_solve_1024_full.md")) as f:
             for line in f:
                 if line.startswith("dram_bytes_per_launch:"):
@@ -351,9 +375,10 @@ def run_ours(args, rank, world_size, local, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched worlds: {len(worlds)} worlds, log-uniform 16..2048 bodies, "
-                               f"pyramids + piles, seed 1", "worlds": len(worlds), "dynamic_bodies": n_dyn,
-                   "dt": "1/60", "iterations": "8/3", "parallelism": f"replicas x{world_size}",
+        "config": {"workload": desc.format(n=len(worlds)), "worlds": len(worlds), "dynamic_bodies": n_dyn,
+                   "dt": f"1/{round(1.0 / conf.deltaTime)}",
+                   "iterations": f"{conf.regVelocityIters}/{conf.regPositionIters}",
+                   "parallelism": f"replicas x{world_size}",
                    "settle_steps": args.settle,
                    "l2": "working set > 129 MB L2 (no flush needed)",
                    "live_contacts": st["liveContacts"], "active_constraints": st["activeConstraints"],
