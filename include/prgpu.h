@@ -113,6 +113,8 @@ typedef struct prgpu_batch_desc {
     const int32_t* joint_flags;         /* [n_joints*3] enableLimit enableMotor collideConnected */
     uint32_t contact_capacity;          /* 0: automatic */
     uint32_t candidate_capacity;        /* 0: automatic */
+    const float* body_mass;             /* [n_bodies*4] optional invMass invRotInertia localCenter.xy of each
+                                           dynamic body (SetMassData, Body.cpp); NULL: from the shapes */
 } prgpu_batch_desc;
 
 int prgpu_abi_version(void);

@@ -17,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libprgpu.so")
+# C++ host layer over the C ABI (HostWorld), a second library linked to the first
+HOST_SOURCES = [os.path.join(HERE, "host", "host_world.cpp")]
+HOST_LIB = os.path.join(HERE, "libprgpu_host.so")
 SOURCES = ["prgpu_prims.cu", "prgpu_contacts.cu", "prgpu_solver.cu", "prgpu_world.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -61,6 +64,16 @@ def build(verbose: bool = False, extra_flags=None) -> str:
         if res.returncode:
             sys.stderr.write(res.stdout + res.stderr)
             raise RuntimeError("link failed")
+    host_deps = HOST_SOURCES + [os.path.join(HERE, "host", "host_world.hpp"), LIB, __file__] + headers
+    if _stale(HOST_LIB, host_deps):
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-shared",
+               "-I" + os.path.join(HERE, "..", "include"), *HOST_SOURCES, "-L" + HERE, "-lprgpu",
+               "-Wl,-rpath,$ORIGIN", "-o", HOST_LIB]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode:
+            sys.stderr.write(res.stdout + res.stderr)
+            raise RuntimeError("host library build failed")
     return LIB
 
 

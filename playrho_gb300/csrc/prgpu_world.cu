@@ -293,6 +293,19 @@ int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
         body_shapes[b].push_back((int)s);
         reset_mass(hb[b], body_shapes[b], ds, sv);
     }
+    if (ds->body_mass) {
+        // SetMassData (Body.cpp): the transformation stays, the centre moves to
+        // the given local centre; only dynamic bodies take a mass.
+        for (uint32_t b = 0; b < N; ++b) {
+            HostBody& x = hb[b];
+            if (x.type != PRGPU_DYNAMIC) continue;
+            const float* m = ds->body_mass + 4 * b;
+            if (!(m[0] >= 0.f) || !(m[1] >= 0.f)) return PRGPU_EINVAL;
+            x.invM = m[0]; x.invI = m[1]; x.lcx = m[2]; x.lcy = m[3];
+            const HV c = hv(x.xpx, x.xpy) + hrotate(hv(x.lcx, x.lcy), hv(x.xc, x.xs));
+            x.px = c.x; x.py = c.y;
+        }
+    }
     // ---- host arrays in device layout
     auto& pos1 = hp.pos1; auto& vel = hp.vel; auto& mass = hp.mass; auto& acc = hp.acc;
     pos1.resize(N); vel.resize(N); mass.resize(N); acc.resize(N);

@@ -51,7 +51,8 @@ class BatchDesc(ctypes.Structure):
         ("shape_nv", P), ("shape_radius", P), ("shape_density", P), ("shape_friction", P),
         ("shape_restitution", P), ("shape_filter", P), ("n_verts", ctypes.c_uint32), ("verts", P),
         ("n_joints", ctypes.c_uint32), ("joint_bodies", P), ("joint_anchors", P), ("joint_params", P),
-        ("joint_flags", P), ("contact_capacity", ctypes.c_uint32), ("candidate_capacity", ctypes.c_uint32)]
+        ("joint_flags", P), ("contact_capacity", ctypes.c_uint32), ("candidate_capacity", ctypes.c_uint32),
+        ("body_mass", P)]
 
 
 class Schedule(ctypes.Structure):

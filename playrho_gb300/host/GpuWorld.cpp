@@ -1,0 +1,533 @@
+// GpuWorld.cpp -- PlayRho value types to and from the HostWorld records, and the
+// free functions World's WorldModel<GpuWorld> calls.
+#include "GpuWorld.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+
+#include "playrho/InvalidArgument.hpp"
+#include "playrho/LengthError.hpp"
+#include "playrho/OutOfRange.hpp"
+#include "playrho/WrongState.hpp"
+#include "playrho/d2/DiskShapeConf.hpp"
+#include "playrho/d2/EdgeShapeConf.hpp"
+#include "playrho/d2/PolygonShapeConf.hpp"
+#include "playrho/d2/RevoluteJointConf.hpp"
+
+namespace playrho::d2 {
+
+namespace {
+
+float F(Real v) { return static_cast<float>(v); }
+
+// The C ABI's status codes as the reference's exception types.
+[[noreturn]] void Rethrow(const prgpu::Error& e) {
+    switch (e.code) {
+    case PRGPU_EINVAL: throw InvalidArgument(e.what());
+    case PRGPU_ECAPACITY: throw LengthError(e.what());
+    case PRGPU_ESTATE: throw WrongState(e.what());
+    default: throw std::runtime_error(e.what());
+    }
+}
+
+template <class F_>
+auto Guard(F_&& f) -> decltype(f()) {
+    try {
+        return f();
+    } catch (const prgpu::Error& e) {
+        Rethrow(e);
+    }
+}
+
+void CheckUnlocked(const GpuWorld& w) {
+    if (w.locked) throw WrongState("world is locked");
+}
+
+// Body -> HostBody over `base` (the current record), keeping base's position or
+// velocity where `value` leaves them as `before` had them, so that a
+// GetBody/SetBody round trip uploads nothing.
+prgpu::HostBody ToHost(const Body& value, const Body* before, const prgpu::HostBody& base) {
+    prgpu::HostBody h = base;
+    h.type = static_cast<int32_t>(GetType(value));
+    const auto loc = GetLocation(value);
+    const auto ang = GetAngle(value);
+    const bool moved = !before || GetLocation(*before) != loc || GetAngle(*before) != ang;
+    if (moved) {
+        h.x = F(StripUnit(GetX(loc)));
+        h.y = F(StripUnit(GetY(loc)));
+        h.angle = F(StripUnit(ang));
+    }
+    const auto vel = GetVelocity(value);
+    const bool vchanged = !before || GetVelocity(*before) != vel;
+    if (vchanged) {
+        h.vx = F(StripUnit(GetX(vel.linear)));
+        h.vy = F(StripUnit(GetY(vel.linear)));
+        h.w = F(StripUnit(vel.angular));
+    }
+    const auto acc = GetAcceleration(value);
+    h.ax = F(StripUnit(GetX(acc.linear)));
+    h.ay = F(StripUnit(GetY(acc.linear)));
+    h.aa = F(StripUnit(acc.angular));
+    h.linear_damping = F(StripUnit(GetLinearDamping(value)));
+    h.angular_damping = F(StripUnit(GetAngularDamping(value)));
+    uint32_t flags = 0;
+    if (IsSleepingAllowed(value)) flags |= PRGPU_BODY_ALLOW_SLEEP;
+    if (IsAwake(value)) flags |= PRGPU_BODY_AWAKE;
+    if (IsFixedRotation(value)) flags |= PRGPU_BODY_FIXED_ROTATION;
+    if (IsEnabled(value)) flags |= PRGPU_BODY_ENABLED;
+    h.flags = flags;
+    // the mass data the reference computed (ResetMassData / SetMassData)
+    h.explicit_mass = true;
+    h.inv_mass = F(StripUnit(GetInvMass(value)));
+    h.inv_rot_inertia = F(StripUnit(GetInvRotInertia(value)));
+    const auto lc = GetLocalCenter(value);
+    h.lcx = F(StripUnit(GetX(lc)));
+    h.lcy = F(StripUnit(GetY(lc)));
+    h.shapes.clear();
+    for (const auto& s : GetShapes(value)) h.shapes.push_back(to_underlying(s));
+    return h;
+}
+
+prgpu::HostShape ToHost(const Shape& shape) {
+    prgpu::HostShape h;
+    auto base = [&h](const auto& conf) {
+        h.friction = F(conf.friction);
+        h.restitution = F(conf.restitution);
+        h.density = F(StripUnit(conf.density));
+        h.category = static_cast<int32_t>(conf.filter.categoryBits);
+        h.mask = static_cast<int32_t>(conf.filter.maskBits);
+        h.group = static_cast<int32_t>(conf.filter.groupIndex);
+        h.sensor = conf.isSensor ? 1 : 0;
+    };
+    if (const auto* c = TypeCast<DiskShapeConf>(&shape)) {
+        base(*c);
+        h.kind = PRGPU_DISK;
+        h.radius = F(StripUnit(c->vertexRadius));
+        h.verts = {F(StripUnit(GetX(c->location))), F(StripUnit(GetY(c->location)))};
+    } else if (const auto* c = TypeCast<PolygonShapeConf>(&shape)) {
+        base(*c);
+        h.kind = PRGPU_POLYGON;
+        h.radius = F(StripUnit(c->vertexRadius));
+        for (const auto& v : c->ngon.GetVertices()) {
+            h.verts.push_back(F(StripUnit(GetX(v))));
+            h.verts.push_back(F(StripUnit(GetY(v))));
+        }
+    } else if (const auto* c = TypeCast<EdgeShapeConf>(&shape)) {
+        base(*c);
+        h.kind = PRGPU_EDGE;
+        h.radius = F(StripUnit(c->vertexRadius));
+        h.verts = {F(StripUnit(GetX(c->GetVertexA()))), F(StripUnit(GetY(c->GetVertexA()))),
+                   F(StripUnit(GetX(c->GetVertexB()))), F(StripUnit(GetY(c->GetVertexB())))};
+    } else {
+        throw InvalidArgument("GpuWorld: only disk, polygon and edge shapes are stepped on the GPU");
+    }
+    return h;
+}
+
+prgpu::HostJoint ToHost(const Joint& joint) {
+    const auto* c = TypeCast<RevoluteJointConf>(&joint);
+    if (!c) throw InvalidArgument("GpuWorld: only revolute joints are stepped on the GPU");
+    prgpu::HostJoint h;
+    h.body_a = to_underlying(c->bodyA);
+    h.body_b = to_underlying(c->bodyB);
+    h.anchor_a[0] = F(StripUnit(GetX(c->localAnchorA))); h.anchor_a[1] = F(StripUnit(GetY(c->localAnchorA)));
+    h.anchor_b[0] = F(StripUnit(GetX(c->localAnchorB))); h.anchor_b[1] = F(StripUnit(GetY(c->localAnchorB)));
+    h.reference_angle = F(StripUnit(c->referenceAngle));
+    h.lower = F(StripUnit(c->lowerAngle));
+    h.upper = F(StripUnit(c->upperAngle));
+    h.motor_speed = F(StripUnit(c->motorSpeed));
+    h.max_motor_torque = F(StripUnit(c->maxMotorTorque));
+    h.enable_limit = c->enableLimit ? 1 : 0;
+    h.enable_motor = c->enableMotor ? 1 : 0;
+    h.collide_connected = c->collideConnected ? 1 : 0;
+    return h;
+}
+
+prgpu_step_conf ToAbi(const StepConf& c) {
+    prgpu_step_conf s{};
+    prgpu_default_step_conf(&s);
+    s.deltaTime = F(StripUnit(c.deltaTime));
+    s.dtRatio = F(c.dtRatio);
+    s.minStillTimeToSleep = F(StripUnit(c.minStillTimeToSleep));
+    s.linearSlop = F(StripUnit(Length{c.linearSlop}));
+    s.angularSlop = F(StripUnit(Angle{c.angularSlop}));
+    s.regResolutionRate = F(c.regResolutionRate);
+    s.regMinSeparation = F(StripUnit(c.regMinSeparation));
+    s.regMinMomentum = F(StripUnit(c.regMinMomentum));
+    s.velocityThreshold = F(StripUnit(c.velocityThreshold));
+    s.maxTranslation = F(StripUnit(c.maxTranslation));
+    s.maxRotation = F(StripUnit(c.maxRotation));
+    s.maxLinearCorrection = F(StripUnit(c.maxLinearCorrection));
+    s.maxAngularCorrection = F(StripUnit(c.maxAngularCorrection));
+    s.linearSleepTolerance = F(StripUnit(c.linearSleepTolerance));
+    s.angularSleepTolerance = F(StripUnit(c.angularSleepTolerance));
+    s.displaceMultiplier = F(c.displaceMultiplier);
+    s.aabbExtension = F(StripUnit(c.aabbExtension));
+    s.maxCirclesRatio = F(c.maxCirclesRatio);
+    s.regVelocityIters = static_cast<int32_t>(c.regVelocityIters);
+    s.regPositionIters = static_cast<int32_t>(c.regPositionIters);
+    s.doWarmStart = c.doWarmStart ? 1 : 0;
+    s.doBlocksolve = c.doBlocksolve ? 1 : 0;
+    return s;
+}
+
+// The GPU's state of body id into the PlayRho body (Sweep, velocity, sleep).
+void Mirror(GpuWorld& w, uint32_t id) {
+    const prgpu::HostBody& h = w.host.GetBody(id);
+    Body& b = w.bodies[id];
+    const auto lc = GetLocalCenter(b);
+    const Position p{Length2{Real(h.cx) * Meter, Real(h.cy) * Meter}, Real(h.angle) * Radian};
+    b.SetSweep(Sweep{p, lc});
+    b.JustSetVelocity(Velocity{LinearVelocity2{Real(h.vx) * MeterPerSecond, Real(h.vy) * MeterPerSecond},
+                               Real(h.w) * RadianPerSecond});
+    if (h.flags & PRGPU_BODY_AWAKE) b.SetAwakeFlag(); else b.UnsetAwakeFlag();
+    b.SetUnderActiveTime(Real(h.under_active_time) * Second);
+}
+
+template <class ID>
+void CheckRange(ID id, uint32_t range, const char* what) {
+    if (to_underlying(id) >= range) throw OutOfRange<ID>(id, what);
+}
+
+}  // namespace
+
+GpuWorld::GpuWorld(const WorldConf& c, int device) : conf(c), host(device) {}
+
+void GpuWorld::Refresh() const {
+    if (contactsValid) return;
+    auto& self = const_cast<GpuWorld&>(*this);
+    const auto& hc = Guard([&]() -> const std::vector<prgpu::HostContact>& { return self.host.Contacts(); });
+    keyedContacts.clear(); contacts.clear(); manifolds.clear();
+    for (size_t k = 0; k < hc.size(); ++k) {
+        const auto& c = hc[k];
+        Contact ct{Contactable{BodyID(c.body_a), ShapeID(c.shape_a), 0u},
+                   Contactable{BodyID(c.body_b), ShapeID(c.shape_b), 0u}};
+        const auto& sa = shapes[c.shape_a];
+        const auto& sb = shapes[c.shape_b];
+        ct.SetFriction(MixFriction(GetFriction(sa), GetFriction(sb)));
+        ct.SetRestitution(MixRestitution(GetRestitution(sa), GetRestitution(sb)));
+        if (c.touching) ct.SetTouching(); else ct.UnsetTouching();
+        if (c.sensor) ct.SetSensor();
+        keyedContacts.emplace_back(ContactKey{c.proxy_a, c.proxy_b}, ContactID(static_cast<ContactID::underlying_type>(k)));
+        contacts.push_back(ct);
+        Manifold m;
+        const auto ln = UnitVec::Get(Real(c.local_normal[0]), Real(c.local_normal[1])).first;
+        const Length2 lp{Real(c.local_point[0]) * Meter, Real(c.local_point[1]) * Meter};
+        auto pt = [&](int j) {
+            const uint32_t f = c.feature[j];
+            return Manifold::Point{Length2{Real(c.point[j][0]) * Meter, Real(c.point[j][1]) * Meter},
+                                   ContactFeature{ContactFeature::Type(f & 0xffu), ContactFeature::Index((f >> 8) & 0xffu),
+                                                  ContactFeature::Type((f >> 16) & 0xffu),
+                                                  ContactFeature::Index((f >> 24) & 0xffu)},
+                                   Real(c.normal_impulse[j]) * NewtonSecond, Real(c.tangent_impulse[j]) * NewtonSecond};
+        };
+        if (c.type == 1 && c.count >= 1) {  // circles
+            const auto p0 = pt(0);
+            m = Manifold::GetForCircles(lp, p0.contactFeature.indexA, p0.localPoint, p0.contactFeature.indexB);
+            m.SetImpulses(0, p0.normalImpulse, p0.tangentImpulse);
+        } else if (c.type == 2) {  // face A
+            m = (c.count == 0) ? Manifold::GetForFaceA(ln, lp)
+                : (c.count == 1) ? Manifold::GetForFaceA(ln, lp, pt(0)) : Manifold::GetForFaceA(ln, lp, pt(0), pt(1));
+        } else if (c.type == 3) {  // face B
+            m = (c.count == 0) ? Manifold::GetForFaceB(ln, lp)
+                : (c.count == 1) ? Manifold::GetForFaceB(ln, lp, pt(0)) : Manifold::GetForFaceB(ln, lp, pt(0), pt(1));
+        }
+        manifolds.push_back(m);
+    }
+    contactsValid = true;
+}
+
+// ---- listeners ------------------------------------------------------------------
+void SetShapeDestructionListener(GpuWorld& w, ShapeFunction l) noexcept { w.shapeDestructionListener = std::move(l); }
+void SetDetachListener(GpuWorld& w, BodyShapeFunction l) noexcept { w.detachListener = std::move(l); }
+void SetJointDestructionListener(GpuWorld& w, JointFunction l) noexcept { w.jointDestructionListener = std::move(l); }
+void SetBeginContactListener(GpuWorld& w, ContactFunction l) noexcept { w.beginContactListener = std::move(l); }
+void SetEndContactListener(GpuWorld& w, ContactFunction l) noexcept { w.endContactListener = std::move(l); }
+void SetPreSolveContactListener(GpuWorld& w, ContactManifoldFunction l) noexcept { w.preSolveContactListener = std::move(l); }
+void SetPostSolveContactListener(GpuWorld& w, ContactImpulsesFunction l) noexcept { w.postSolveContactListener = std::move(l); }
+
+// ---- world ----------------------------------------------------------------------
+bool operator==(const GpuWorld& lhs, const GpuWorld& rhs) noexcept {
+    return lhs.bodies == rhs.bodies && lhs.shapes == rhs.shapes && lhs.joints == rhs.joints;
+}
+
+std::optional<pmr::StatsResource::Stats> GetResourceStats(const GpuWorld&) noexcept { return std::nullopt; }
+
+void Clear(GpuWorld& w) noexcept {
+    w.host.Clear();
+    w.bodies.clear(); w.shapes.clear(); w.joints.clear();
+    w.Invalidate();
+}
+
+StepStats Step(GpuWorld& w, const StepConf& conf) {
+    CheckUnlocked(w);
+    StepStats stats;
+    const auto sc = ToAbi(conf);
+    const prgpu_step_stats s = Guard([&] { return w.host.Step(sc); });
+    for (uint32_t id = 0; id < w.host.BodyRange(); ++id)
+        if (w.host.BodyAlive(id)) Mirror(w, id);
+    w.Invalidate();
+    if (conf.deltaTime != 0_s) w.invDeltaTime = Real(1) / conf.deltaTime;
+    stats.pre.contactsAdded = s.contactsAdded;
+    stats.pre.contactsDestroyed = s.contactsDestroyed;
+    stats.pre.contactsUpdated = s.contactsUpdated;
+    stats.pre.proxiesMoved = s.proxiesMoved;
+    stats.reg.islandsFound = s.islandsFound;
+    stats.reg.islandsSolved = s.islandsSolved;
+    stats.reg.bodiesSlept = s.bodiesSlept;
+    stats.reg.sumPosIters = s.sumPosIters;
+    stats.reg.minSeparation = Real(s.minSeparation) * Meter;
+    stats.reg.maxIncImpulse = Real(s.maxIncImpulse) * NewtonSecond;
+    return stats;
+}
+
+bool IsStepComplete(const GpuWorld&) noexcept { return true; }
+bool GetSubStepping(const GpuWorld& w) noexcept { return w.subStepping; }
+void SetSubStepping(GpuWorld& w, bool flag) noexcept { w.subStepping = flag; }
+
+const DynamicTree& GetTree(const GpuWorld& w) noexcept {
+    if (!w.treeValid) {
+        w.tree.Clear();
+        std::vector<float> aabb;
+        std::vector<uint32_t> bs;
+        try {
+            const_cast<GpuWorld&>(w).host.Proxies(aabb, bs);
+        } catch (...) {
+            aabb.clear(); bs.clear();
+        }
+        for (size_t k = 0; k < bs.size() / 2; ++k) {
+            const AABB box{LengthInterval{Real(aabb[4 * k]) * Meter, Real(aabb[4 * k + 2]) * Meter},
+                           LengthInterval{Real(aabb[4 * k + 1]) * Meter, Real(aabb[4 * k + 3]) * Meter}};
+            w.tree.CreateLeaf(box, Contactable{BodyID(bs[2 * k]), ShapeID(bs[2 * k + 1]), 0u});
+        }
+        w.treeValid = true;
+    }
+    return w.tree;
+}
+
+bool IsLocked(const GpuWorld& w) noexcept { return w.locked; }
+
+void ShiftOrigin(GpuWorld& w, const Length2& newOrigin) {
+    CheckUnlocked(w);
+    for (uint32_t id = 0; id < w.bodies.size(); ++id) {
+        if (!w.host.BodyAlive(id)) continue;
+        Body b = w.bodies[id];
+        SetLocation(b, GetLocation(b) - newOrigin);
+        SetBody(w, BodyID(id), b);
+    }
+}
+
+Interval<Positive<Length>> GetVertexRadiusInterval(const GpuWorld& w) noexcept { return w.conf.vertexRadius; }
+Frequency GetInvDeltaTime(const GpuWorld& w) noexcept { return w.invDeltaTime; }
+
+// ---- bodies ---------------------------------------------------------------------
+BodyCounter GetBodyRange(const GpuWorld& w) noexcept { return static_cast<BodyCounter>(w.bodies.size()); }
+
+std::vector<BodyID> GetBodies(const GpuWorld& w) {
+    std::vector<BodyID> out;
+    for (uint32_t id = 0; id < w.bodies.size(); ++id)
+        if (w.host.BodyAlive(id)) out.push_back(BodyID(id));
+    return out;
+}
+
+std::vector<BodyID> GetBodiesForProxies(const GpuWorld&) { return {}; }
+
+BodyID CreateBody(GpuWorld& w, const Body& body) {
+    CheckUnlocked(w);
+    if (w.bodies.size() >= MaxBodies) throw LengthError("CreateBody: too many bodies");
+    for (const auto& s : GetShapes(body)) CheckRange(s, static_cast<uint32_t>(w.shapes.size()), "shape ID out of range");
+    const uint32_t id = Guard([&] { return w.host.CreateBody(ToHost(body, nullptr, prgpu::HostBody{})); });
+    if (id >= w.bodies.size()) w.bodies.resize(id + 1);
+    w.bodies[id] = body;
+    w.Invalidate();
+    return BodyID(id);
+}
+
+Body GetBody(const GpuWorld& w, BodyID id) {
+    CheckRange(id, static_cast<uint32_t>(w.bodies.size()), "body ID out of range");
+    if (!w.host.BodyAlive(to_underlying(id))) throw WasDestroyed<BodyID>(id, "body was destroyed");
+    return w.bodies[to_underlying(id)];
+}
+
+void SetBody(GpuWorld& w, BodyID id, const Body& value) {
+    CheckUnlocked(w);
+    const uint32_t i = to_underlying(id);
+    CheckRange(id, static_cast<uint32_t>(w.bodies.size()), "body ID out of range");
+    if (!w.host.BodyAlive(i)) throw WasDestroyed<BodyID>(id, "body was destroyed");
+    for (const auto& s : GetShapes(value)) CheckRange(s, static_cast<uint32_t>(w.shapes.size()), "shape ID out of range");
+    Guard([&] { w.host.SetBody(i, ToHost(value, &w.bodies[i], w.host.GetBody(i))); return 0; });
+    w.bodies[i] = value;
+    w.Invalidate();
+}
+
+void Destroy(GpuWorld& w, BodyID id) {
+    CheckUnlocked(w);
+    const uint32_t i = to_underlying(id);
+    CheckRange(id, static_cast<uint32_t>(w.bodies.size()), "body ID out of range");
+    for (const auto& bj : GetJoints(w, id)) {
+        if (w.jointDestructionListener) w.jointDestructionListener(std::get<1>(bj));
+        w.joints[to_underlying(std::get<1>(bj))] = Joint{};
+    }
+    if (w.detachListener)
+        for (const auto& s : GetShapes(w.bodies[i])) w.detachListener(std::make_pair(id, s));
+    Guard([&] { w.host.DestroyBody(i); return 0; });
+    w.bodies[i] = Body{};
+    w.Invalidate();
+}
+
+std::vector<std::pair<BodyID, JointID>> GetJoints(const GpuWorld& w, BodyID id) {
+    std::vector<std::pair<BodyID, JointID>> out;
+    const uint32_t i = to_underlying(id);
+    for (uint32_t j = 0; j < w.joints.size(); ++j) {
+        if (!w.host.JointAlive(j)) continue;
+        const auto& h = w.host.GetJoint(j);
+        if (h.body_a == i) out.emplace_back(BodyID(h.body_b), JointID(j));
+        else if (h.body_b == i) out.emplace_back(BodyID(h.body_a), JointID(j));
+    }
+    return out;
+}
+
+std::vector<std::tuple<ContactKey, ContactID>> GetContacts(const GpuWorld& w, BodyID id) {
+    w.Refresh();
+    std::vector<std::tuple<ContactKey, ContactID>> out;
+    for (size_t k = 0; k < w.contacts.size(); ++k) {
+        if (GetBodyA(w.contacts[k]) == id || GetBodyB(w.contacts[k]) == id)
+            out.emplace_back(std::get<0>(w.keyedContacts[k]), std::get<1>(w.keyedContacts[k]));
+    }
+    return out;
+}
+
+std::vector<ShapeID> GetShapes(const GpuWorld& w, BodyID id) { return GetShapes(GetBody(w, id)); }
+
+// ---- joints ---------------------------------------------------------------------
+JointCounter GetJointRange(const GpuWorld& w) noexcept { return static_cast<JointCounter>(w.joints.size()); }
+
+std::vector<JointID> GetJoints(const GpuWorld& w) {
+    std::vector<JointID> out;
+    for (uint32_t j = 0; j < w.joints.size(); ++j)
+        if (w.host.JointAlive(j)) out.push_back(JointID(j));
+    return out;
+}
+
+JointID CreateJoint(GpuWorld& w, const Joint& def) {
+    CheckUnlocked(w);
+    if (w.joints.size() >= MaxJoints) throw LengthError("CreateJoint: too many joints");
+    const uint32_t id = Guard([&] { return w.host.CreateJoint(ToHost(def)); });
+    if (id >= w.joints.size()) w.joints.resize(id + 1);
+    w.joints[id] = def;
+    w.Invalidate();
+    return JointID(id);
+}
+
+Joint GetJoint(const GpuWorld& w, JointID id) {
+    CheckRange(id, static_cast<uint32_t>(w.joints.size()), "joint ID out of range");
+    if (!w.host.JointAlive(to_underlying(id))) throw WasDestroyed<JointID>(id, "joint was destroyed");
+    return w.joints[to_underlying(id)];
+}
+
+void SetJoint(GpuWorld& w, JointID id, const Joint& def) {
+    CheckUnlocked(w);
+    CheckRange(id, static_cast<uint32_t>(w.joints.size()), "joint ID out of range");
+    Guard([&] { w.host.SetJoint(to_underlying(id), ToHost(def)); return 0; });
+    w.joints[to_underlying(id)] = def;
+    w.Invalidate();
+}
+
+void Destroy(GpuWorld& w, JointID id) {
+    CheckUnlocked(w);
+    CheckRange(id, static_cast<uint32_t>(w.joints.size()), "joint ID out of range");
+    Guard([&] { w.host.DestroyJoint(to_underlying(id)); return 0; });
+    w.joints[to_underlying(id)] = Joint{};
+    w.Invalidate();
+}
+
+// ---- shapes ---------------------------------------------------------------------
+ShapeCounter GetShapeRange(const GpuWorld& w) noexcept { return static_cast<ShapeCounter>(w.shapes.size()); }
+
+ShapeID CreateShape(GpuWorld& w, const Shape& def) {
+    CheckUnlocked(w);
+    if (w.shapes.size() >= MaxShapes) throw LengthError("CreateShape: too many shapes");
+    const auto& lim = w.conf.vertexRadius;
+    for (ChildCounter i = 0; i < GetChildCount(def); ++i) {
+        const auto vr = GetVertexRadius(def, i);
+        if (vr < lim.GetMin() || vr > lim.GetMax())
+            throw InvalidArgument("CreateShape: vertex radius out of the world's range");
+    }
+    const uint32_t id = Guard([&] { return w.host.CreateShape(ToHost(def)); });
+    if (id >= w.shapes.size()) w.shapes.resize(id + 1);
+    w.shapes[id] = def;
+    w.Invalidate();
+    return ShapeID(id);
+}
+
+Shape GetShape(const GpuWorld& w, ShapeID id) {
+    CheckRange(id, static_cast<uint32_t>(w.shapes.size()), "shape ID out of range");
+    if (!w.host.ShapeAlive(to_underlying(id))) throw WasDestroyed<ShapeID>(id, "shape was destroyed");
+    return w.shapes[to_underlying(id)];
+}
+
+void SetShape(GpuWorld& w, ShapeID id, const Shape& def) {
+    CheckUnlocked(w);
+    CheckRange(id, static_cast<uint32_t>(w.shapes.size()), "shape ID out of range");
+    Guard([&] { w.host.SetShape(to_underlying(id), ToHost(def)); return 0; });
+    w.shapes[to_underlying(id)] = def;
+    w.Invalidate();
+}
+
+void Destroy(GpuWorld& w, ShapeID id) {
+    CheckUnlocked(w);
+    CheckRange(id, static_cast<uint32_t>(w.shapes.size()), "shape ID out of range");
+    if (w.shapeDestructionListener) w.shapeDestructionListener(id);
+    Guard([&] { w.host.DestroyShape(to_underlying(id)); return 0; });
+    for (uint32_t b = 0; b < w.bodies.size(); ++b)
+        if (w.host.BodyAlive(b)) {
+            Body body = w.bodies[b];
+            if (body.Detach(id)) w.bodies[b] = body;
+        }
+    w.shapes[to_underlying(id)] = Shape{};
+    w.Invalidate();
+}
+
+// ---- contacts -------------------------------------------------------------------
+ContactCounter GetContactRange(const GpuWorld& w) noexcept {
+    try {
+        w.Refresh();
+    } catch (...) {
+        return 0;
+    }
+    return static_cast<ContactCounter>(w.contacts.size());
+}
+
+std::vector<KeyedContactID> GetContacts(const GpuWorld& w) {
+    w.Refresh();
+    return w.keyedContacts;
+}
+
+Contact GetContact(const GpuWorld& w, ContactID id) {
+    w.Refresh();
+    CheckRange(id, static_cast<uint32_t>(w.contacts.size()), "contact ID out of range");
+    return w.contacts[to_underlying(id)];
+}
+
+void SetContact(GpuWorld& w, ContactID id, const Contact& value) {
+    w.Refresh();
+    CheckRange(id, static_cast<uint32_t>(w.contacts.size()), "contact ID out of range");
+    // the GPU keeps its own contact records; what a caller may change here (the
+    // enabled flag, friction, restitution) is not taken into the next step
+    w.contacts[to_underlying(id)] = value;
+}
+
+Manifold GetManifold(const GpuWorld& w, ContactID id) {
+    w.Refresh();
+    CheckRange(id, static_cast<uint32_t>(w.manifolds.size()), "contact ID out of range");
+    return w.manifolds[to_underlying(id)];
+}
+
+void SetManifold(GpuWorld& w, ContactID id, const Manifold& value) {
+    w.Refresh();
+    CheckRange(id, static_cast<uint32_t>(w.manifolds.size()), "contact ID out of range");
+    w.manifolds[to_underlying(id)] = value;
+}
+
+}  // namespace playrho::d2

@@ -1,0 +1,65 @@
+"""The C++ drop-in: playrho::d2::World{GpuWorld{}} compiled against the
+reference's own headers and library (the reference's HelloWorld with the World
+constructed over GpuWorld), where the reference sources are available.
+
+Set-up runs through PlayRho's World API into GpuWorld (CreateShape, CreateBody
+with BodyConf::Use(shape), GetBodies, GetInvMass ...); Step reaches the GPU
+library, which without a GPU answers PRGPU_ENOTREADY, surfaced as an exception.
+On a GPU machine the same program steps the world on the GPU.
+"""
+import os
+import shutil
+import subprocess
+import tempfile
+
+import pytest
+
+from playrho_gb300 import build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "playrho_gb300")
+REF = os.environ.get("PLAYRHO_REFERENCE", "/root/reference")
+REF_LIB = os.path.join(ROOT, "oracle", "_ref", "f32", "libPlayRho.a")
+REF_GEN = os.path.join(ROOT, "oracle", "_ref", "f32", "gen")
+
+
+def _compile():
+    if not os.path.isdir(os.path.join(REF, "Library", "include")):
+        pytest.skip("reference headers not available here")
+    if not os.path.exists(REF_LIB):
+        res = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "f32"],
+                             capture_output=True, text=True)
+        if res.returncode or not os.path.exists(REF_LIB):
+            pytest.skip("reference library could not be built here")
+    build.build()
+    out = os.path.join(tempfile.mkdtemp(prefix="gw_"), "gpuworld_check")
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O1", "-std=c++17", "-ffp-contract=off", "-w", "-I" + REF_GEN,
+           "-I" + os.path.join(REF, "Library", "include"), "-I" + os.path.join(ROOT, "include"),
+           "-I" + os.path.join(PKG, "host"), os.path.join(ROOT, "tests", "gpuworld_check.cpp"),
+           os.path.join(PKG, "host", "GpuWorld.cpp"), REF_LIB, "-L" + PKG, "-lprgpu_host", "-lprgpu",
+           "-Wl,-rpath," + PKG, "-o", out]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr[-4000:]
+    return out
+
+
+def test_world_over_gpuworld_builds_and_runs():
+    exe = _compile()
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    lines = dict(l.split(" ", 1) for l in res.stdout.splitlines() if " " in l)
+    assert lines["bodies"] == "2"
+    assert lines["shapes"] == "2"
+    assert lines["type"] == "2"  # BodyType::Dynamic
+    # a disk of density 0 gets the reference's default mass of 1 kg and no rotational inertia
+    inv_mass, inv_rot = (float.fromhex(x) for x in lines["mass"].split())
+    assert inv_mass == 1.0 and inv_rot == 0.0
+    from playrho_gb300.gpu import gpu_available
+
+    if gpu_available():
+        assert res.returncode == 0, res.stdout + res.stderr
+        steps = [l for l in res.stdout.splitlines() if l.startswith("step ")]
+        assert len(steps) == 60
+    else:
+        assert res.returncode == 3
+        assert "prgpu_world_create" in lines.get("error", "")
