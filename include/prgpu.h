@@ -174,6 +174,38 @@ typedef struct prgpu_schedule {
  * that the world advances (1 + steps_per_candidate) steps per candidate, as
  * with prgpu_step_n.  No reference counterpart. */
 int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_candidate, prgpu_schedule* best);
+/* StepAdjoint: gradients of a loss of the state after a window of steps with
+ * respect to the state before it and to the shapes' friction.  No reference
+ * counterpart.  The derivative is that of the step with its discrete decisions
+ * frozen as the forward pass took them (contact set, clamps, block-solver cases,
+ * island early exits, sleep) and each manifold's local geometry held constant
+ * within a step.  Batches with joints are rejected (PRGPU_EINVAL).
+ *   prgpu_adjoint_begin     opens a window; the state is checkpointed every
+ *                           checkpoint_every steps (device copies of the whole batch)
+ *   prgpu_adjoint_forward   n steps with one StepConf, as prgpu_step_n
+ *   prgpu_adjoint_backward  from d(loss)/d(final state) -- positions x y angle of
+ *                           each body's centre of mass and velocities, [n_bodies*3],
+ *                           either may be NULL -- to d(loss)/d(state at the window's
+ *                           start) and d(loss)/d(friction of each shape) [n_shapes];
+ *                           each segment is re-run from its checkpoint to record it,
+ *                           then walked backwards; the batch is left at the window's end
+ *   prgpu_adjoint_tangent   the FP64 forward-mode derivative along the same window
+ *                           (tangents of the start state and friction in, of the
+ *                           final state out), for dot-product tests of the adjoint
+ *   prgpu_adjoint_info      steps in the window, recorded steps whose constraint
+ *                           set-up the differentiable restatement did not reproduce
+ *                           bit for bit (0 expected), local tapes that overflowed
+ *   prgpu_adjoint_end       closes the window and frees its memory
+ * Host calls that change bodies (prgpu_upload_body_states) inside a window are
+ * not recorded and make the gradients meaningless. */
+int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every);
+int prgpu_adjoint_forward(prgpu_world* w, const prgpu_step_conf* conf, int n_steps);
+int prgpu_adjoint_backward(prgpu_world* w, const float* dl_dpos3, const float* dl_dvel3, float* dl_dpos3_start,
+                           float* dl_dvel3_start, float* dl_dfriction);
+int prgpu_adjoint_tangent(prgpu_world* w, const double* dpos3_start, const double* dvel3_start, const double* dfriction,
+                          double* dpos3_end, double* dvel3_end);
+int prgpu_adjoint_info(prgpu_world* w, int* steps, uint32_t* replay_mismatches, uint32_t* tape_overflows);
+int prgpu_adjoint_end(prgpu_world* w);
 /* Enqueues n steps on the handle's stream and returns at once. */
 int prgpu_step_async(prgpu_world* w, const prgpu_step_conf* conf, int n);
 int prgpu_synchronize(prgpu_world* w);

@@ -302,13 +302,17 @@ PR_HD Man collide_shapes(const Proxy& A, Xf xfA, const Proxy& B, Xf xfB, float l
 
 // Warm-start transfer of AabbTreeWorld::Update (AabbTreeWorld.cpp:2644-2678):
 // impulses follow matching contact features, else the nearest old point.
-PR_HD void transfer_impulses(Man& nm, const Man& old) {
+// src (optional) receives, for each new point, the old point its impulses came
+// from (-1: none).
+PR_HD void transfer_impulses(Man& nm, const Man& old, int* src = nullptr) {
     bool found[2] = {false, nm.count < 2};
+    int from[2] = {-1, -1};
     for (int i = 0; i < nm.count; ++i) {
         for (int j = 0; j < old.count; ++j) {
             if (nm.cf[i] == old.cf[j]) {
                 found[i] = true;
                 nm.ni[i] = old.ni[j]; nm.ti[i] = old.ti[j];
+                from[i] = j;
                 break;
             }
         }
@@ -318,10 +322,11 @@ PR_HD void transfer_impulses(Man& nm, const Man& old) {
             float least = PR_INF;
             for (int j = 0; j < old.count; ++j) {
                 const float sq = mag2(old.plp[j] - nm.plp[i]);
-                if (least > sq) { least = sq; nm.ni[i] = old.ni[j]; nm.ti[i] = old.ti[j]; }
+                if (least > sq) { least = sq; nm.ni[i] = old.ni[j]; nm.ti[i] = old.ti[j]; from[i] = j; }
             }
         }
     }
+    if (src) { src[0] = from[0]; src[1] = from[1]; }
 }
 
 }  // namespace prgpu

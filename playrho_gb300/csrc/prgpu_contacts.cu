@@ -190,11 +190,13 @@ __device__ __forceinline__ void store_manifold(const DW& d, uint32_t slot, const
 }
 
 // AabbTreeWorld::Update (AabbTreeWorld.cpp:2587-2721) without listeners.
-__device__ void update_contact(const DW& d, uint32_t slot) {
+// src2 (optional): where the new manifold's points took their impulses from.
+__device__ void update_contact(const DW& d, uint32_t slot, int8_t* src2 = nullptr) {
     const uint2 pr = d.cs_proxy[slot];
     const uint2 bd = d.cs_body[slot];
     uint32_t flags = d.cs_flags[slot];
     bool touching = false;
+    int src[2] = {-1, -1};
     if (flags & CF_SENSOR) {
         store_manifold(d, slot, man_empty());
     } else {
@@ -204,9 +206,10 @@ __device__ void update_contact(const DW& d, uint32_t slot) {
         const Man old = load_manifold(d, slot);
         Man nm = collide_shapes(A, load_xf(d, bd.x), B, load_xf(d, bd.y), d.conf->linearSlop, d.conf->maxCirclesRatio);
         touching = nm.count > 0;
-        transfer_impulses(nm, old);
+        transfer_impulses(nm, old, src);
         store_manifold(d, slot, nm);
     }
+    if (src2) { src2[0] = (int8_t)src[0]; src2[1] = (int8_t)src[1]; }
     flags &= ~CF_NEEDS_UPDATE;
     flags = touching ? (flags | CF_TOUCHING) : (flags & ~CF_TOUCHING);
     d.cs_flags[slot] = flags;
@@ -214,13 +217,15 @@ __device__ void update_contact(const DW& d, uint32_t slot) {
 
 __global__ void k_update_contacts(DW d, uint32_t body_mask) {
     uint32_t updated = 0;
+    // the post-solve pass of a recorded step notes each update's impulse sources
+    int8_t* rec = (d.tape && body_mask == BF_MOVED) ? d.tape->src : nullptr;
     GRID_LOOP(i, d.cnt->n_live) {
         const uint32_t slot = d.c_slot[i];
         const uint2 bd = d.cs_body[slot];
         const bool need = (d.cs_flags[slot] & CF_NEEDS_UPDATE) || (d.b_flags[bd.x] & body_mask) ||
                           (d.b_flags[bd.y] & body_mask);
         if (need) {
-            update_contact(d, slot);
+            update_contact(d, slot, rec ? rec + 2 * (size_t)slot : nullptr);
             ++updated;
         }
     }
@@ -545,6 +550,7 @@ __global__ void k_new_contacts(DW d) {
             if (is_speedable(fb)) atomicOr(&d.b_flags[bb], BF_AWAKE);
         }
         update_contact(d, slot);
+        if (d.tape) d.tape->created[slot] = 1u;  // starts without impulses
         d.n_val[i] = slot;
     }
 }

@@ -91,6 +91,29 @@ struct __align__(16) PC {
     uint32_t bB, island, pad0, pad1;
 };
 
+// What one recorded step keeps for the adjoint and tangent passes (device
+// arrays; K = constraint capacity, C = contact slots, N = bodies).
+struct StepTape {
+    float4* p0;        // [N] centre of mass x y angle at the start of the solve
+    float4* v0;        // [N] velocity at the start of the solve (before k_body_begin)
+    uint32_t* flags;   // [N] body flags after k_body_begin (BF_SOLVED: solved this step)
+    uint8_t* slept;    // [N] put to sleep (velocity zeroed) by this step
+    uint32_t* t_id;    // [K] constraint id at each sweep position (contact slot)
+    PC* pc;            // [K] position constraint (local manifold, bodies, island)
+    float4* cinfo;     // [K] vertex radius A, B, friction, restitution
+    uint2* prox;       // [K] the contact's two proxies (shapes)
+    float4* imp0;      // [K] impulses as built (ni0 ti0 ni1 ti1), before warm start
+    float4* warm;      // [K*2] velocities of A and B before warm start
+    float4* vel;       // [iv*K*3] velocities of A, B and impulses before each velocity solve
+    float4* pos;       // [ip*K*2] positions of A and B before each position solve (A.w: 1 if solved)
+    int8_t* src;       // [C*2] after the post-solve update: old point each new point took its
+                       //       impulses from (-1 none; -2 slot not updated)
+    uint8_t* created;  // [C] slot created by this step's post-solve contact search
+    uint32_t* hdr;     // [kSerialColour + 2 + 4] colour offsets, n_colours, n_active, replay mismatches
+    int iv, ip;        // velocity and position iterations recorded
+    uint32_t kcap;
+};
+
 // Device counters and small per-step state.
 struct Counters {
     uint32_t n_live;          // live contacts (sorted key list length)
@@ -152,6 +175,7 @@ struct DW {
     uint32_t* w_kj;          // [n_worlds + 1] first active joint of each world
     uint32_t n_world_big;    // leading entries of w_order swept by a whole CTA (the rest by a warp)
     uint32_t stage_bytes;    // dynamic shared memory of the per-world solver (world body state)
+    StepTape* tape;          // recording for the adjoint (device struct), else null
     float4* w_bounds;        // centroid bounds for Morton codes (ordered-int encoded)
     // bodies
     float4* b_pos1;          // cx cy angle -

@@ -32,6 +32,42 @@ void launch_solve_finish(const DW& d, const Launch& L, cudaStream_t s);
 void launch_reset_step(const DW& d, const Launch& L, cudaStream_t s);
 void launch_clear_dirty(const DW& d, const Launch& L, cudaStream_t s);
 int coop_blocks_per_sm(int threads);
+// recording for the adjoint (prgpu_adjoint.cu)
+void launch_tape_body_start(const DW& d, const Launch& L, cudaStream_t s);
+void launch_tape_body_flags(const DW& d, const Launch& L, cudaStream_t s);
+void launch_tape_constraints(const DW& d, const Launch& L, cudaStream_t s);
+
+// adjoint and tangent passes over recorded steps (prgpu_adjoint.cu)
+struct AdjState {
+    float4* pbar;     // [N] d(loss)/d(centre x, y, angle)
+    float4* vbar;     // [N] d(loss)/d(velocity)
+    float4* vibar;    // [N] through the velocity bias: d(loss)/d(velocity at the start of the solve)
+    float4* vi;       // [N] velocity at the start of the solve (recomputed)
+    float4* lbar;     // [K] d(loss)/d(impulses ni0 ti0 ni1 ti1) of each constraint
+    float* gbar;      // [K * kGeomWords] d(loss)/d(geometry)
+    float* gval;      // [K * kGeomWords] geometry values
+    float4* mbar;     // [C] d(loss)/d(stored manifold impulses) per slot
+    float4* mtmp;     // [C]
+    float* fbar;      // [S] d(loss)/d(shape friction)
+    uint32_t* err;    // tape overflow count
+};
+
+struct TanState {
+    double* pdot;   // [N*3]
+    double* vdot;   // [N*3]
+    double* vidot;  // [N*3] at the start of the solve
+    double* ldot;   // [K*4]
+    double* gdot;   // [K*kGeomWords]
+    double* mdot;   // [C*4]
+    double* mtmp;   // [C*4]
+    const double* fdot;  // [S] tangent of shape friction
+};
+
+int adj_grid(int sm_count);
+cudaError_t launch_adj_step(const DW& d, const StepTape* tp, const AdjState& a, uint32_t n_slots, int grid,
+                            cudaStream_t s);
+cudaError_t launch_tan_step(const DW& d, const StepTape* tp, const TanState& t, float* gval, uint32_t n_slots,
+                            int grid, cudaStream_t s);
 // Sets k_world_solve's dynamic shared memory to stage_bytes; returns its CTAs per SM.
 int world_blocks_per_sm(uint32_t stage_bytes);
 

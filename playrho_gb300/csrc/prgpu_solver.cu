@@ -970,20 +970,36 @@ struct SharedBodies {
 };
 
 // ---- per-constraint sweep steps (t = position in sweep order) -------------------
+// When the step is recorded for the adjoint (d.tape), each contact step also
+// writes the body state (and impulses) it starts from.
 template <class BS>
 __device__ __forceinline__ void sweep_warm(const DW& d, const BS& bs, uint32_t t) {
     const uint32_t id = d.t_id[t];
-    if (id & kJointBit) joint_init_velocity(d, bs, id & ~kJointBit);
-    else if (d.conf->doWarmStart) warm_start(d, bs, load_vc(d, t));
+    if (id & kJointBit) {
+        joint_init_velocity(d, bs, id & ~kJointBit);
+    } else if (d.conf->doWarmStart) {
+        const VC vc = load_vc(d, t);
+        if (d.tape) {
+            d.tape->warm[2 * (size_t)t] = bs.vel(vc.bA);
+            d.tape->warm[2 * (size_t)t + 1] = bs.vel(vc.bB);
+        }
+        warm_start(d, bs, vc);
+    }
 }
 
 template <class BS>
-__device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32_t t) {
+__device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32_t t, int it) {
     const uint32_t id = d.t_id[t];
     if (id & kJointBit) {
         joint_solve_velocity(d, bs, id & ~kJointBit);
     } else {
         VC vc = load_vc(d, t);
+        if (d.tape) {
+            float4* r = d.tape->vel + 3 * ((size_t)it * d.tape->kcap + t);
+            r[0] = bs.vel(vc.bA);
+            r[1] = bs.vel(vc.bB);
+            r[2] = make_float4(vc.ni0, vc.ti0, vc.ni1, vc.ti1);
+        }
         solve_contact_velocity(d, bs, vc);
         store_vc_impulses(d, t, vc);
     }
@@ -999,7 +1015,15 @@ __device__ __forceinline__ void sweep_position(const DW& d, const BS& bs, uint32
         if (!joint_solve_position(d, bs, j)) bs.island_joint_fail(L, it);
     } else {
         const PC pc = d.pc[t];
-        if (bs.island_done(pc.island, it)) return;
+        const bool done = bs.island_done(pc.island, it);
+        if (d.tape) {
+            float4* r = d.tape->pos + 2 * ((size_t)it * d.tape->kcap + t);
+            float4 a = bs.pos(pc.bA);
+            a.w = done ? 0.f : 1.f;
+            r[0] = a;
+            r[1] = bs.pos(pc.bB);
+        }
+        if (done) return;
         const float sep = solve_contact_position(d, bs, pc);
         bs.island_sep(pc.island, it, sep);
     }
@@ -1058,7 +1082,7 @@ __global__ void k_solve(DW d) {
     const GlobalBodies bs{d};
     for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_warm(d, bs, t); });
     for (int it = 0; it < c.regVelocityIters; ++it)
-        for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, bs, t); });
+        for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, bs, t, it); });
     GRID_LOOP(b, d.n_bodies) integrate_body(d, bs, b);
     grid_barrier(d.cnt);
     for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it)
@@ -1132,7 +1156,7 @@ __device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uin
     if (n) {
         for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_warm(d, bs, t); });
         for (int it = 0; it < c.regVelocityIters; ++it)
-            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, bs, t); });
+            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, bs, t, it); });
     }
     for (uint32_t b = d.w_body_off[w] + rank; b < d.w_body_off[w + 1]; b += size) integrate_body(d, bs, b);
     G::sync();
@@ -1338,6 +1362,7 @@ __global__ void k_sleep(DW d) {
                 d.b_flags[b] = f & ~BF_AWAKE;
                 d.b_uat[b] = 0.f;
                 d.b_vel[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (d.tape) d.tape->slept[b] = 1u;
                 ++slept;
             }
         }
@@ -1407,7 +1432,9 @@ void launch_islands_colour(const DW& d, const Launch& L, cudaStream_t s) {
     k_isl_init<<<L.grid, L.threads, 0, s>>>(d);
     k_isl_union<<<L.grid, L.threads, 0, s>>>(d);
     k_isl_flatten<<<L.grid, L.threads, 0, s>>>(d);
+    if (d.tape) launch_tape_body_start(d, L, s);
     k_body_begin<<<L.grid, L.threads, 0, s>>>(d);
+    if (d.tape) launch_tape_body_flags(d, L, s);
     // active constraints in live-list order (contacts), then joints
     uint32_t* n_items = &d.cnt->pad[1];
     uint32_t* n_bodies = &d.cnt->pad[2];
@@ -1429,6 +1456,7 @@ void launch_islands_colour(const DW& d, const Launch& L, cudaStream_t s) {
 void launch_build_constraints(const DW& d, const Launch& L, cudaStream_t s) {
     // per world, k_world_solve builds the constraints once it has coloured them
     if (!L.per_world) k_build_constraints<<<L.grid, L.threads, 0, s>>>(d);
+    if (d.tape) launch_tape_constraints(d, L, s);  // recording runs the grid-wide solve
 }
 
 void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) {

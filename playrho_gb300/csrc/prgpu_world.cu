@@ -22,6 +22,7 @@ struct prgpu_world {
     DW d{};
     Launch L{};
     std::vector<void*> allocs;
+    std::vector<size_t> alloc_bytes;
     cudaGraphExec_t graph = nullptr;
     cudaGraph_t graph_def = nullptr;
     prgpu_step_conf conf{};
@@ -33,6 +34,7 @@ struct prgpu_world {
     Counters* h_cnt = nullptr;  // pinned mirror of the device counters
     cudaEvent_t graph_ev[8] = {};  // recorded by the captured step between its phases
     std::vector<uint32_t> order_nb;  // body counts of the worlds in work-queue order
+    struct AdjWindow* adj = nullptr;  // open StepAdjoint window, if any
     uint32_t warp_world_max = 0;     // worlds of at most this many bodies are swept by one warp
 };
 
@@ -63,6 +65,7 @@ int dalloc(prgpu_world* w, T** p, size_t n) {
     const cudaError_t e = cudaMalloc(&q, bytes);
     if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
     w->allocs.push_back(q);
+    w->alloc_bytes.push_back(bytes);
     *p = static_cast<T*>(q);
     return PRGPU_OK;
 }
@@ -803,10 +806,13 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     return PRGPU_OK;
 }
 
+void adjoint_close(prgpu_world* w);
+
 int prgpu_world_destroy(prgpu_world* w) {
     if (!w) return PRGPU_OK;
     cudaSetDevice(w->device);
     if (w->stream) cudaStreamSynchronize(w->stream);
+    adjoint_close(w);
     if (w->graph) cudaGraphExecDestroy(w->graph);
     for (int k = 0; k < 8; ++k)
         if (w->graph_ev[k]) cudaEventDestroy(w->graph_ev[k]);
@@ -1200,6 +1206,336 @@ int prgpu_last_error(prgpu_world* w, char* buf, int len) {
     if (!buf || len <= 0) return PRGPU_EINVAL;
     const std::string& e = w ? w->err : std::string();
     std::snprintf(buf, (size_t)len, "%s", e.c_str());
+    return PRGPU_OK;
+}
+
+// ---- StepAdjoint ---------------------------------------------------------------------
+// A window of recorded steps: snapshots of the whole device state every k steps,
+// the tapes of one segment at a time, and the adjoint and tangent state.
+struct AdjWindow {
+    int every = 1;
+    int steps = 0;
+    prgpu_step_conf conf{};
+    bool conf_set = false;
+    std::vector<void*> snaps;       // device copies of every allocation, one per checkpoint
+    void* end_state = nullptr;
+    size_t snap_bytes = 0;
+    std::vector<StepTape> tapes;    // host copies of the device structs
+    StepTape* d_tapes = nullptr;
+    std::vector<void*> mem;         // tape, adjoint and tangent arrays
+    AdjState adj{};
+    TanState tan{};
+    double* fdot = nullptr;
+    float* tgval = nullptr;
+    uint32_t kcap = 0, ccap = 0;
+    int grid = 0;
+    uint32_t mismatches = 0, overflows = 0;
+};
+
+static int adj_alloc(prgpu_world* w, AdjWindow* a, void** p, size_t bytes) {
+    *p = nullptr;
+    const cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "adjoint cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    a->mem.push_back(*p);
+    return PRGPU_OK;
+}
+
+void adjoint_close(prgpu_world* w) {
+    if (!w || !w->adj) return;
+    AdjWindow* a = w->adj;
+    for (void* p : a->snaps) cudaFree(p);
+    if (a->end_state) cudaFree(a->end_state);
+    for (void* p : a->mem) cudaFree(p);
+    delete a;
+    w->adj = nullptr;
+    w->d.tape = nullptr;
+}
+
+static int snap_copy(prgpu_world* w, void* buf, bool save) {
+    size_t off = 0;
+    for (size_t i = 0; i < w->allocs.size(); ++i) {
+        char* b = static_cast<char*>(buf) + off;
+        const cudaError_t e = save ? cudaMemcpyAsync(b, w->allocs[i], w->alloc_bytes[i], cudaMemcpyDeviceToDevice, w->stream)
+                                   : cudaMemcpyAsync(w->allocs[i], b, w->alloc_bytes[i], cudaMemcpyDeviceToDevice, w->stream);
+        if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "snapshot copy: %s", cudaGetErrorString(e));
+        off += (w->alloc_bytes[i] + 255) & ~(size_t)255;
+    }
+    return PRGPU_OK;
+}
+
+static size_t snap_size(const prgpu_world* w) {
+    size_t t = 0;
+    for (size_t b : w->alloc_bytes) t += (b + 255) & ~(size_t)255;
+    return t;
+}
+
+// Re-runs the steps [first, first + n) of the window from their checkpoint
+// with recording on, one tape per step (grid-wide solve, same results).
+// Counts words that differ between two device arrays.
+__global__ void k_count_diff(const uint32_t* a, const uint32_t* b, size_t n, uint32_t* out) {
+    uint32_t c = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        c += (a[i] != b[i]) ? 1u : 0u;
+    if (c) atomicAdd(out, c);
+}
+
+// Byte offset of a world allocation inside a snapshot.
+static size_t snap_offset(const prgpu_world* w, const void* p) {
+    size_t off = 0;
+    for (size_t i = 0; i < w->allocs.size(); ++i) {
+        if (w->allocs[i] == p) return off;
+        off += (w->alloc_bytes[i] + 255) & ~(size_t)255;
+    }
+    return (size_t)-1;
+}
+
+// Whether the live positions and velocities equal those in snapshot `snap`
+// (a re-recorded segment must end where the forward pass went on from).
+static int check_against(prgpu_world* w, const void* snap, uint32_t* differ) {
+    AdjWindow* a = w->adj;
+    CU(cudaMemsetAsync(a->adj.err + 1, 0, sizeof(uint32_t), w->stream));
+    const size_t N4 = 4 * (size_t)w->d.n_bodies;
+    for (const void* p : {(const void*)w->d.b_pos1, (const void*)w->d.b_vel}) {
+        const size_t off = snap_offset(w, p);
+        if (off == (size_t)-1) return fail(w, PRGPU_ESTATE, "snapshot layout");
+        k_count_diff<<<64, 256, 0, w->stream>>>(static_cast<const uint32_t*>(p),
+                                                reinterpret_cast<const uint32_t*>(static_cast<const char*>(snap) + off),
+                                                N4, a->adj.err + 1);
+    }
+    CU(cudaMemcpyAsync(differ, a->adj.err + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+static int record_segment(prgpu_world* w, int seg, int n) {
+    AdjWindow* a = w->adj;
+    int rc = snap_copy(w, a->snaps[seg], false);
+    if (rc) return rc;
+    // the checkpoint holds the configuration of the step before it: upload the window's
+    w->conf_valid = false;
+    rc = set_conf(w, &a->conf);
+    if (rc) return rc;
+    const bool per_world = w->L.per_world;
+    w->L.per_world = false;
+    for (int i = 0; i < n; ++i) {
+        const StepTape& t = a->tapes[i];
+        cudaMemsetAsync(t.src, 0xfe, 2 * (size_t)a->ccap, w->stream);
+        cudaMemsetAsync(t.created, 0, a->ccap, w->stream);
+        cudaMemsetAsync(t.hdr, 0, sizeof(uint32_t) * (kSerialColour + 6), w->stream);
+        w->d.tape = a->d_tapes + i;
+        enqueue_step(w, true);
+        w->d.tape = nullptr;
+    }
+    w->L.per_world = per_world;
+    CU(cudaGetLastError());
+    // replay mismatches of the differentiable restatement
+    for (int i = 0; i < n; ++i) {
+        uint32_t bad = 0;
+        CU(cudaMemcpyAsync(&bad, a->tapes[i].hdr + kSerialColour + 5, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        a->mismatches += bad;
+    }
+    rc = check_device_error(w);
+    if (rc) return rc;
+    // the segment must end where the forward pass continued from
+    const void* next = (size_t)(seg + 1) < a->snaps.size() ? a->snaps[seg + 1] : a->end_state;
+    uint32_t differ = 0;
+    if (next && (rc = check_against(w, next, &differ))) return rc;
+    a->mismatches += differ;
+    return PRGPU_OK;
+}
+
+int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every) {
+    if (!w || checkpoint_every < 1) return PRGPU_EINVAL;
+    if (w->adj) return fail(w, PRGPU_ESTATE, "an adjoint window is already open");
+    if (w->d.n_joints) return fail(w, PRGPU_EINVAL, "adjoint: joints are not part of the differentiated step");
+    CU(cudaSetDevice(w->device));
+    AdjWindow* a = new AdjWindow();
+    a->every = checkpoint_every;
+    a->kcap = w->d.contact_cap + w->d.n_joints;
+    a->ccap = w->d.contact_cap;
+    a->snap_bytes = snap_size(w);
+    a->grid = adj_grid(w->L.prims.sm_count);
+    w->adj = a;
+    if (a->grid < 1) { adjoint_close(w); return fail(w, PRGPU_ECUDA, "adjoint kernels cannot be resident"); }
+    const uint32_t N = w->d.n_bodies, K = a->kcap, C = a->ccap, S = w->d.n_shapes;
+    int rc = 0;
+#define AA(ptr, bytes) do { void* q_; rc = adj_alloc(w, a, &q_, (bytes)); if (rc) { adjoint_close(w); return rc; } \
+                            ptr = reinterpret_cast<decltype(ptr)>(q_); } while (0)
+    AA(a->adj.pbar, sizeof(float4) * N); AA(a->adj.vbar, sizeof(float4) * N); AA(a->adj.vibar, sizeof(float4) * N);
+    AA(a->adj.vi, sizeof(float4) * N); AA(a->adj.lbar, sizeof(float4) * K);
+    AA(a->adj.gbar, sizeof(float) * 24 * (size_t)K); AA(a->adj.gval, sizeof(float) * 24 * (size_t)K);
+    AA(a->adj.mbar, sizeof(float4) * C); AA(a->adj.mtmp, sizeof(float4) * C); AA(a->adj.fbar, sizeof(float) * S);
+    AA(a->adj.err, sizeof(uint32_t) * 2);
+    AA(a->tan.pdot, sizeof(double) * 3 * N); AA(a->tan.vdot, sizeof(double) * 3 * N);
+    AA(a->tan.vidot, sizeof(double) * 3 * N); AA(a->tan.ldot, sizeof(double) * 4 * (size_t)K);
+    AA(a->tan.gdot, sizeof(double) * 24 * (size_t)K); AA(a->tan.mdot, sizeof(double) * 4 * (size_t)C);
+    AA(a->tan.mtmp, sizeof(double) * 4 * (size_t)C); AA(a->fdot, sizeof(double) * S);
+    a->tan.fdot = a->fdot;
+    AA(a->tgval, sizeof(float) * 24 * (size_t)K);
+    return PRGPU_OK;
+}
+
+static int ensure_tapes(prgpu_world* w) {
+    AdjWindow* a = w->adj;
+    if (!a->tapes.empty()) return PRGPU_OK;
+    const uint32_t N = w->d.n_bodies, K = a->kcap, C = a->ccap;
+    const int iv = std::max(0, a->conf.regVelocityIters), ip = std::min(std::max(0, a->conf.regPositionIters), kMaxPosIters);
+    a->tapes.resize(a->every);
+    int rc = 0;
+    for (int i = 0; i < a->every; ++i) {
+        StepTape& t = a->tapes[i];
+        t.iv = iv; t.ip = ip; t.kcap = K;
+        AA(t.p0, sizeof(float4) * N); AA(t.v0, sizeof(float4) * N); AA(t.flags, sizeof(uint32_t) * N);
+        AA(t.slept, N); AA(t.t_id, sizeof(uint32_t) * K); AA(t.pc, sizeof(PC) * K); AA(t.cinfo, sizeof(float4) * K);
+        AA(t.prox, sizeof(uint2) * K); AA(t.imp0, sizeof(float4) * K); AA(t.warm, sizeof(float4) * 2 * (size_t)K);
+        AA(t.vel, sizeof(float4) * 3 * (size_t)K * std::max(iv, 1));
+        AA(t.pos, sizeof(float4) * 2 * (size_t)K * std::max(ip, 1));
+        AA(t.src, 2 * (size_t)C); AA(t.created, C); AA(t.hdr, sizeof(uint32_t) * (kSerialColour + 6));
+    }
+    AA(a->d_tapes, sizeof(StepTape) * a->every);
+    CU(cudaMemcpyAsync(a->d_tapes, a->tapes.data(), sizeof(StepTape) * a->every, cudaMemcpyHostToDevice, w->stream));
+#undef AA
+    return PRGPU_OK;
+}
+
+int prgpu_adjoint_forward(prgpu_world* w, const prgpu_step_conf* conf, int n_steps) {
+    if (!w || !conf || n_steps < 0) return PRGPU_EINVAL;
+    AdjWindow* a = w->adj;
+    if (!a) return fail(w, PRGPU_ESTATE, "no adjoint window is open");
+    if (conf->deltaTime == 0.f) return fail(w, PRGPU_EINVAL, "adjoint steps need deltaTime > 0");
+    if (a->conf_set && std::memcmp(&a->conf, conf, sizeof(*conf)) != 0)
+        return fail(w, PRGPU_EINVAL, "one step configuration per adjoint window");
+    a->conf = *conf;
+    a->conf_set = true;
+    CU(cudaSetDevice(w->device));
+    int rc = ensure_tapes(w);
+    if (rc) return rc;
+    for (int i = 0; i < n_steps; ++i) {
+        if (a->steps % a->every == 0) {
+            void* buf = nullptr;
+            if (cudaMalloc(&buf, a->snap_bytes) != cudaSuccess) return fail(w, PRGPU_ECUDA, "checkpoint allocation");
+            a->snaps.push_back(buf);
+            if ((rc = snap_copy(w, buf, true))) return rc;
+        }
+        if ((rc = run_steps(w, conf, 1, false))) return rc;
+        ++a->steps;
+    }
+    return check_device_error(w);
+}
+
+int prgpu_adjoint_backward(prgpu_world* w, const float* dl_dpos3, const float* dl_dvel3, float* dl_dpos3_start,
+                           float* dl_dvel3_start, float* dl_dfriction) {
+    if (!w) return PRGPU_EINVAL;
+    AdjWindow* a = w->adj;
+    if (!a) return fail(w, PRGPU_ESTATE, "no adjoint window is open");
+    if (a->steps == 0) return fail(w, PRGPU_ESTATE, "the adjoint window has no steps");
+    CU(cudaSetDevice(w->device));
+    const uint32_t N = w->d.n_bodies, S = w->d.n_shapes;
+    int rc = 0;
+    if (!a->end_state && cudaMalloc(&a->end_state, a->snap_bytes) != cudaSuccess)
+        return fail(w, PRGPU_ECUDA, "end-state allocation");
+    if ((rc = snap_copy(w, a->end_state, true))) return rc;
+    std::vector<float4> h(N);
+    for (uint32_t b = 0; b < N; ++b)
+        h[b] = make_float4(dl_dpos3 ? dl_dpos3[3 * b] : 0.f, dl_dpos3 ? dl_dpos3[3 * b + 1] : 0.f,
+                           dl_dpos3 ? dl_dpos3[3 * b + 2] : 0.f, 0.f);
+    CU(cudaMemcpyAsync(a->adj.pbar, h.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    for (uint32_t b = 0; b < N; ++b)
+        h[b] = make_float4(dl_dvel3 ? dl_dvel3[3 * b] : 0.f, dl_dvel3 ? dl_dvel3[3 * b + 1] : 0.f,
+                           dl_dvel3 ? dl_dvel3[3 * b + 2] : 0.f, 0.f);
+    CU(cudaMemcpyAsync(a->adj.vbar, h.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemsetAsync(a->adj.mbar, 0, sizeof(float4) * a->ccap, w->stream));
+    CU(cudaMemsetAsync(a->adj.fbar, 0, sizeof(float) * std::max<uint32_t>(S, 1), w->stream));
+    CU(cudaMemsetAsync(a->adj.err, 0, sizeof(uint32_t), w->stream));
+    const int nseg = (a->steps + a->every - 1) / a->every;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int first = seg * a->every, n = std::min(a->every, a->steps - first);
+        if ((rc = record_segment(w, seg, n))) return rc;
+        for (int i = n - 1; i >= 0; --i) {
+            const cudaError_t e = launch_adj_step(w->d, a->d_tapes + i, a->adj, a->ccap, a->grid, w->stream);
+            if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "adjoint step: %s", cudaGetErrorString(e));
+        }
+        if ((rc = check_device_error(w))) return rc;
+    }
+    if ((rc = snap_copy(w, a->end_state, false))) return rc;
+    uint32_t err = 0;
+    CU(cudaMemcpyAsync(&err, a->adj.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    std::vector<float4> hp(N), hv(N);
+    std::vector<uint32_t> fl(N);
+    CU(cudaMemcpyAsync(hp.data(), a->adj.pbar, sizeof(float4) * N, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaMemcpyAsync(hv.data(), a->adj.vbar, sizeof(float4) * N, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaMemcpyAsync(fl.data(), w->d.b_flags, sizeof(uint32_t) * N, cudaMemcpyDeviceToHost, w->stream));
+    if (dl_dfriction) CU(cudaMemcpyAsync(dl_dfriction, a->adj.fbar, sizeof(float) * S, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    a->overflows += err;
+    for (uint32_t b = 0; b < N; ++b) {
+        // only dynamic bodies' states are differentiated
+        const bool dyn = is_accelerable(fl[b]);
+        if (dl_dpos3_start) {
+            dl_dpos3_start[3 * b] = dyn ? hp[b].x : 0.f; dl_dpos3_start[3 * b + 1] = dyn ? hp[b].y : 0.f;
+            dl_dpos3_start[3 * b + 2] = dyn ? hp[b].z : 0.f;
+        }
+        if (dl_dvel3_start) {
+            dl_dvel3_start[3 * b] = dyn ? hv[b].x : 0.f; dl_dvel3_start[3 * b + 1] = dyn ? hv[b].y : 0.f;
+            dl_dvel3_start[3 * b + 2] = dyn ? hv[b].z : 0.f;
+        }
+    }
+    if (err) return fail(w, PRGPU_ECAPACITY, "adjoint: %u local derivative tapes overflowed", err);
+    return PRGPU_OK;
+}
+
+int prgpu_adjoint_tangent(prgpu_world* w, const double* dpos3_start, const double* dvel3_start, const double* dfriction,
+                          double* dpos3_end, double* dvel3_end) {
+    if (!w) return PRGPU_EINVAL;
+    AdjWindow* a = w->adj;
+    if (!a) return fail(w, PRGPU_ESTATE, "no adjoint window is open");
+    if (a->steps == 0) return fail(w, PRGPU_ESTATE, "the adjoint window has no steps");
+    CU(cudaSetDevice(w->device));
+    const uint32_t N = w->d.n_bodies, S = w->d.n_shapes;
+    int rc = 0;
+    if (!a->end_state && cudaMalloc(&a->end_state, a->snap_bytes) != cudaSuccess)
+        return fail(w, PRGPU_ECUDA, "end-state allocation");
+    if ((rc = snap_copy(w, a->end_state, true))) return rc;
+    std::vector<double> z(3 * (size_t)N, 0.0), zf(std::max<uint32_t>(S, 1), 0.0);
+    CU(cudaMemcpyAsync(a->tan.pdot, dpos3_start ? dpos3_start : z.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(a->tan.vdot, dvel3_start ? dvel3_start : z.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(a->fdot, dfriction ? dfriction : zf.data(), sizeof(double) * S, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemsetAsync(a->tan.mdot, 0, sizeof(double) * 4 * a->ccap, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    const int nseg = (a->steps + a->every - 1) / a->every;
+    for (int seg = 0; seg < nseg; ++seg) {
+        const int first = seg * a->every, n = std::min(a->every, a->steps - first);
+        if ((rc = record_segment(w, seg, n))) return rc;
+        for (int i = 0; i < n; ++i) {
+            const cudaError_t e = launch_tan_step(w->d, a->d_tapes + i, a->tan, a->tgval, a->ccap, a->grid, w->stream);
+            if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "tangent step: %s", cudaGetErrorString(e));
+        }
+        if ((rc = check_device_error(w))) return rc;
+    }
+    if ((rc = snap_copy(w, a->end_state, false))) return rc;
+    if (dpos3_end) CU(cudaMemcpyAsync(dpos3_end, a->tan.pdot, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, w->stream));
+    if (dvel3_end) CU(cudaMemcpyAsync(dvel3_end, a->tan.vdot, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_adjoint_info(prgpu_world* w, int* steps, uint32_t* replay_mismatches, uint32_t* tape_overflows) {
+    if (!w) return PRGPU_EINVAL;
+    if (!w->adj) return fail(w, PRGPU_ESTATE, "no adjoint window is open");
+    if (steps) *steps = w->adj->steps;
+    if (replay_mismatches) *replay_mismatches = w->adj->mismatches;
+    if (tape_overflows) *tape_overflows = w->adj->overflows;
+    return PRGPU_OK;
+}
+
+int prgpu_adjoint_end(prgpu_world* w) {
+    if (!w) return PRGPU_EINVAL;
+    if (!w->adj) return fail(w, PRGPU_ESTATE, "no adjoint window is open");
+    cudaSetDevice(w->device);
+    cudaStreamSynchronize(w->stream);
+    adjoint_close(w);
     return PRGPU_OK;
 }
 

@@ -104,6 +104,12 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_get_warp_world_max_bodies.argtypes = [P, P]
     lib.prgpu_set_stage_bytes.argtypes = [P, U]
     lib.prgpu_get_stage_bytes.argtypes = [P, P]
+    lib.prgpu_adjoint_begin.argtypes = [P, I]
+    lib.prgpu_adjoint_forward.argtypes = [P, ctypes.POINTER(StepConf), I]
+    lib.prgpu_adjoint_backward.argtypes = [P, P, P, P, P, P]
+    lib.prgpu_adjoint_tangent.argtypes = [P, P, P, P, P, P]
+    lib.prgpu_adjoint_info.argtypes = [P, P, P, P]
+    lib.prgpu_adjoint_end.argtypes = [P]
     lib.prgpu_autotune.argtypes = [P, ctypes.POINTER(StepConf), I, ctypes.POINTER(Schedule)]
     _LIB = lib
     return lib
@@ -117,7 +123,8 @@ def exported_symbols() -> List[str]:
         "prgpu_download_proxies", "prgpu_last_error", "prgpu_convex_hull", "prgpu_prepare_bodies", "prgpu_step_profiled",
         "prgpu_last_step_phase_ms", "prgpu_graph_kernel_count", "prgpu_set_sweep_mode", "prgpu_get_sweep_mode",
         "prgpu_set_warp_world_max_bodies", "prgpu_get_warp_world_max_bodies", "prgpu_autotune",
-        "prgpu_set_stage_bytes", "prgpu_get_stage_bytes"]
+        "prgpu_set_stage_bytes", "prgpu_get_stage_bytes", "prgpu_adjoint_begin", "prgpu_adjoint_forward",
+        "prgpu_adjoint_backward", "prgpu_adjoint_tangent", "prgpu_adjoint_info", "prgpu_adjoint_end"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -323,6 +330,46 @@ class GpuBatch:
         inv = {v: k for k, v in self.SWEEP_MODES.items()}
         return {"sweeps": inv[sc.sweep_mode], "warp_world_max_bodies": int(sc.warp_world_max_bodies),
                 "stage_bytes": int(sc.stage_bytes), "step_ms": float(sc.step_ms)}
+
+    # ---- StepAdjoint ----
+    def adjoint_begin(self, checkpoint_every: int = 16):
+        """Opens a window of differentiated steps, checkpointed every k steps."""
+        self._check(self.lib.prgpu_adjoint_begin(self.h, int(checkpoint_every)), "prgpu_adjoint_begin")
+
+    def adjoint_forward(self, n: int, conf: StepConf | None = None, **overrides):
+        c = conf if conf is not None else default_conf(**overrides)
+        self._check(self.lib.prgpu_adjoint_forward(self.h, ctypes.byref(c), int(n)), "prgpu_adjoint_forward")
+
+    def adjoint_backward(self, dl_dpos=None, dl_dvel=None) -> dict:
+        """d(loss)/d(start state) and d(loss)/d(shape friction) from d(loss)/d(final
+        centre-of-mass positions x y angle) and d(loss)/d(final velocities)."""
+        n = self.n_bodies
+        f32 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(n, 3)
+        gp, gv = f32(dl_dpos), f32(dl_dvel)
+        op, ov = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+        of = np.zeros(self.n_shapes, np.float32)
+        self._check(self.lib.prgpu_adjoint_backward(self.h, _ptr(gp), _ptr(gv), _ptr(op), _ptr(ov), _ptr(of)),
+                    "prgpu_adjoint_backward")
+        return {"pos": op, "vel": ov, "friction": of}
+
+    def adjoint_tangent(self, dpos=None, dvel=None, dfriction=None) -> dict:
+        """FP64 forward-mode derivative of the window's final state."""
+        n = self.n_bodies
+        f64 = lambda a, m: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(m)
+        ip, iv, iff = f64(dpos, (n, 3)), f64(dvel, (n, 3)), f64(dfriction, (self.n_shapes,))
+        op, ov = np.zeros((n, 3), np.float64), np.zeros((n, 3), np.float64)
+        self._check(self.lib.prgpu_adjoint_tangent(self.h, _ptr(ip), _ptr(iv), _ptr(iff), _ptr(op), _ptr(ov)),
+                    "prgpu_adjoint_tangent")
+        return {"pos": op, "vel": ov}
+
+    def adjoint_info(self) -> dict:
+        st, mm, ov = ctypes.c_int(), ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self.lib.prgpu_adjoint_info(self.h, ctypes.byref(st), ctypes.byref(mm), ctypes.byref(ov)),
+                    "prgpu_adjoint_info")
+        return {"steps": st.value, "replay_mismatches": mm.value, "tape_overflows": ov.value}
+
+    def adjoint_end(self):
+        self._check(self.lib.prgpu_adjoint_end(self.h), "prgpu_adjoint_end")
 
     def step_async(self, n: int, conf: StepConf):
         self._check(self.lib.prgpu_step_async(self.h, ctypes.byref(conf), int(n)), "prgpu_step_async")

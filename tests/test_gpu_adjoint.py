@@ -1,0 +1,109 @@
+"""StepAdjoint: the reverse pass against the FP64 tangent (dot-product test),
+against finite differences, and the differentiable restatement against the
+forward kernels (replay, bit for bit).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from playrho_gb300 import scenes
+from playrho_gb300.gpu import GpuBatch, default_conf
+
+pytestmark = pytest.mark.gpu
+
+
+def dynamic_mask(batch_scenes):
+    return np.concatenate([s.body_type == scenes.DYNAMIC for s in batch_scenes])
+
+
+def test_dot_product_and_replay(gpu_lib):
+    """<ybar, J xdot> (FP64 tangent) equals <J^T ybar, xdot> (adjoint) over a
+    window of 12 steps with checkpoints every 4, on pushed boxes in contact."""
+    worlds = scenes.push_worlds(6, seed=2)
+    g = GpuBatch(worlds)
+    conf = default_conf(minStillTimeToSleep=1e9)  # keep every body awake in the window
+    g.step_n(40, conf)  # boxes land; the disk meets the first ones
+    g.adjoint_begin(4)
+    g.adjoint_forward(12, conf)
+    info = g.adjoint_info()
+    rng = np.random.default_rng(0)
+    dyn = dynamic_mask(worlds)
+    n, s = g.n_bodies, g.n_shapes
+    ybar_p = rng.standard_normal((n, 3)) * dyn[:, None]
+    ybar_v = rng.standard_normal((n, 3)) * dyn[:, None]
+    xdot_p = rng.standard_normal((n, 3)) * dyn[:, None] * 1e-2
+    xdot_v = rng.standard_normal((n, 3)) * dyn[:, None] * 1e-1
+    xdot_f = rng.standard_normal(s) * 1e-2
+    adj = g.adjoint_backward(ybar_p, ybar_v)
+    tan = g.adjoint_tangent(xdot_p, xdot_v, xdot_f)
+    info = g.adjoint_info()
+    assert info["steps"] == 12
+    assert info["replay_mismatches"] == 0, info
+    assert info["tape_overflows"] == 0, info
+    lhs = float((ybar_p * tan["pos"]).sum() + (ybar_v * tan["vel"]).sum())
+    rhs = float((adj["pos"].astype(np.float64) * xdot_p).sum() + (adj["vel"].astype(np.float64) * xdot_v).sum() +
+                (adj["friction"].astype(np.float64) * xdot_f).sum())
+    scale = max(abs(lhs), abs(rhs), 1e-12)
+    print(f"\ndot-product test: <ybar, J xdot> = {lhs:.9e}, <J^T ybar, xdot> = {rhs:.9e}, "
+          f"rel diff {abs(lhs - rhs) / scale:.2e}")
+    assert abs(lhs - rhs) <= 1e-4 * scale
+    # the window leaves the batch where the forward steps left it
+    b = g.bodies()
+    g.adjoint_end()
+    g2 = GpuBatch(worlds)
+    g2.step_n(52, conf)
+    np.testing.assert_array_equal(b["pos"], g2.bodies()["pos"])
+
+
+def _fd_scene():
+    """A disk pushing three boxes along the ground (no stacking)."""
+    sb = scenes.SceneBuilder()
+    gnd = sb.body(scenes.STATIC, 0.0, 0.0)
+    sb.edge(gnd, (-20.0, 0.0), (40.0, 0.0), friction=0.5)
+    d = sb.body(scenes.DYNAMIC, 0.0, 0.5, v=(6.0, 0.0, 0.0), acc=scenes.GRAVITY)
+    sb.disk(d, 0.5, density=1.0, friction=0.5)
+    for x in (2.0, 3.2, 4.4):
+        b = sb.body(scenes.DYNAMIC, x, 0.5, acc=scenes.GRAVITY)
+        sb.box(b, 0.5, 0.5, density=1.0, friction=0.5)
+    return sb.build()
+
+
+def test_gradient_against_finite_differences_of_the_fp64_oracle(gpu_lib):
+    """d(mean box x after 30 steps)/d(disk's initial velocity and position),
+    adjoint on the GPU against central differences of the FP64 oracle (the
+    reference's step in double).  Both solve to convergence (200 velocity and
+    30 position iterations), so the Gauss-Seidel order does not matter."""
+    sc = _fd_scene()
+    steps = 30
+    over = dict(regVelocityIters=200, regPositionIters=30, minStillTimeToSleep=1e9, regMinSeparation=-1e-9)
+    conf = default_conf(**over)
+    boxes = [2, 3, 4]
+    g = GpuBatch([sc])
+    g.step(deltaTime=0.0)
+    g.adjoint_begin(10)
+    g.adjoint_forward(steps, conf)
+    ybar = np.zeros((sc.n_bodies, 3))
+    ybar[boxes, 0] = 1.0 / len(boxes)
+    adj = g.adjoint_backward(ybar, None)
+    info = g.adjoint_info()
+    assert info["replay_mismatches"] == 0 and info["tape_overflows"] == 0, info
+
+    def loss(dvx=0.0, dx=0.0):
+        s2 = scenes.Scene(**{f: getattr(sc, f) for f in sc.__dataclass_fields__})
+        s2.body_vel = sc.body_vel.astype(np.float64).copy()
+        s2.body_pos = sc.body_pos.astype(np.float64).copy()
+        s2.body_vel[1, 0] += dvx
+        s2.body_pos[1, 0] += dx
+        o = oracle.OracleWorld(s2, double=True)
+        o.step(deltaTime=0.0)
+        for _ in range(steps):
+            o.step(**over)
+        return float(o.bodies()["pos"][boxes, 0].mean())
+
+    h = 1e-4
+    fd_v = (loss(dvx=h) - loss(dvx=-h)) / (2 * h)
+    fd_x = (loss(dx=h) - loss(dx=-h)) / (2 * h)
+    ad_v, ad_x = float(adj["vel"][1, 0]), float(adj["pos"][1, 0])
+    print(f"\nd(mean box x)/d(disk vx): adjoint {ad_v:.6f} fd {fd_v:.6f}; d/d(disk x): adjoint {ad_x:.6f} fd {fd_x:.6f}")
+    assert abs(ad_v - fd_v) <= 1e-3 * max(abs(fd_v), 1e-3) + 1e-4
+    assert abs(ad_x - fd_x) <= 1e-3 * max(abs(fd_x), 1e-3) + 1e-4
