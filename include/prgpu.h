@@ -206,6 +206,9 @@ int prgpu_adjoint_tangent(prgpu_world* w, const double* dpos3_start, const doubl
                           double* dpos3_end, double* dvel3_end);
 int prgpu_adjoint_info(prgpu_world* w, int* steps, uint32_t* replay_mismatches, uint32_t* tape_overflows);
 int prgpu_adjoint_end(prgpu_world* w);
+/* Host time (ms) of the window's forward steps and of the last backward pass's
+ * recording (segments re-run from their checkpoints) and reverse kernels. */
+int prgpu_adjoint_profile(prgpu_world* w, double* forward_ms, double* record_ms, double* reverse_ms);
 /* Enqueues n steps on the handle's stream and returns at once. */
 int prgpu_step_async(prgpu_world* w, const prgpu_step_conf* conf, int n);
 int prgpu_synchronize(prgpu_world* w);

@@ -22,28 +22,50 @@ namespace prgpu {
 namespace diff {
 
 // ---- scalar types ---------------------------------------------------------------
-constexpr int kTapeNodes = 400;
+constexpr int kTapeNodes = 320;
+constexpr int kTapeLanes = 32;               // tapes of one warp, interleaved
+constexpr int kTapeBytes = kTapeNodes * 16;  // shared memory of one thread's tape
 
-// Per-thread tape: node k = a local result with up to two parents and the
-// partial derivative with respect to each.
+// Per-thread tape in shared memory: node k = a local result with up to two
+// parents and the partial derivative with respect to each.  The 32 tapes of a
+// warp are interleaved word by word (node k of lane l at word k*32 + l of each
+// array), so lanes that push or walk their tapes in step hit 32 different banks.
 struct Tape {
-    double pa[kTapeNodes], pb[kTapeNodes], adj[kTapeNodes];
-    int16_t ia[kTapeNodes], ib[kTapeNodes];
+    float* pa;
+    float* pb;
+    float* adj;
+    uint32_t* ix;  // parents: low half a, high half b (int16, -1 = none)
     int n;
     bool overflow;
+    // carves lane's tape out of the warp's 32 * kTapeBytes of shared memory
+    __device__ void init(void* mem, uint32_t lane) {
+        float* f = static_cast<float*>(mem);
+        pa = f + lane;
+        pb = pa + kTapeNodes * kTapeLanes;
+        adj = pb + kTapeNodes * kTapeLanes;
+        ix = reinterpret_cast<uint32_t*>(adj + kTapeNodes * kTapeLanes);
+        n = 0; overflow = false;
+    }
     __device__ void reset() { n = 0; overflow = false; }
-    __device__ int push(int a, double da, int b, double db) {
+    __device__ int push(int a, float da, int b, float db) {
         if (n >= kTapeNodes) { overflow = true; return -1; }
-        ia[n] = (int16_t)a; pa[n] = da; ib[n] = (int16_t)b; pb[n] = db; adj[n] = 0.0;
+        const int o = n * kTapeLanes;
+        ix[o] = (uint32_t)(uint16_t)(int16_t)a | ((uint32_t)(uint16_t)(int16_t)b << 16);
+        pa[o] = da; pb[o] = db; adj[o] = 0.f;
         return n++;
     }
+    __device__ float& grad(int k) { return adj[k * kTapeLanes]; }
+    __device__ float grad(int k) const { return adj[k * kTapeLanes]; }
     // adjoints of every node from those seeded on the outputs
     __device__ void backward() {
         for (int k = n - 1; k >= 0; --k) {
-            const double g = adj[k];
-            if (g == 0.0) continue;
-            if (ia[k] >= 0) adj[ia[k]] += pa[k] * g;
-            if (ib[k] >= 0) adj[ib[k]] += pb[k] * g;
+            const int o = k * kTapeLanes;
+            const float g = adj[o];
+            if (g == 0.f) continue;
+            const uint32_t w = ix[o];
+            const int a = (int16_t)(w & 0xffffu), b = (int16_t)(w >> 16);
+            if (a >= 0) adj[a * kTapeLanes] += pa[o] * g;
+            if (b >= 0) adj[b * kTapeLanes] += pb[o] * g;
         }
     }
 };
@@ -69,37 +91,38 @@ template <> __device__ __forceinline__ float C<float>(float c) { return c; }
 template <> __device__ __forceinline__ AD C<AD>(float c) { return AD{c, -1, nullptr}; }
 template <> __device__ __forceinline__ Tan C<Tan>(float c) { return Tan{c, 0.0}; }
 
-__device__ __forceinline__ AD rec(float v, const AD& a, double da, const AD& b, double db) {
+__device__ __forceinline__ AD rec(float v, const AD& a, float da, const AD& b, float db) {
     Tape* t = a.t ? a.t : b.t;
     if (!t || (a.i < 0 && b.i < 0)) return AD{v, -1, t};
     return AD{v, t->push(a.i, da, b.i, db), t};
 }
-__device__ __forceinline__ AD rec1(float v, const AD& a, double da) {
+__device__ __forceinline__ AD rec1(float v, const AD& a, float da) {
     if (!a.t || a.i < 0) return AD{v, -1, a.t};
-    return AD{v, a.t->push(a.i, da, -1, 0.0), a.t};
+    return AD{v, a.t->push(a.i, da, -1, 0.f), a.t};
 }
 
-__device__ __forceinline__ AD operator+(const AD& a, const AD& b) { return rec(a.v + b.v, a, 1.0, b, 1.0); }
-__device__ __forceinline__ AD operator-(const AD& a, const AD& b) { return rec(a.v - b.v, a, 1.0, b, -1.0); }
-__device__ __forceinline__ AD operator*(const AD& a, const AD& b) { return rec(a.v * b.v, a, (double)b.v, b, (double)a.v); }
+// partial derivatives in float: the tape stores them in float
+__device__ __forceinline__ AD operator+(const AD& a, const AD& b) { return rec(a.v + b.v, a, 1.f, b, 1.f); }
+__device__ __forceinline__ AD operator-(const AD& a, const AD& b) { return rec(a.v - b.v, a, 1.f, b, -1.f); }
+__device__ __forceinline__ AD operator*(const AD& a, const AD& b) { return rec(a.v * b.v, a, b.v, b, a.v); }
 __device__ __forceinline__ AD operator/(const AD& a, const AD& b) {
-    const double bv = b.v;
-    return rec(a.v / b.v, a, 1.0 / bv, b, -(double)a.v / (bv * bv));
+    const float q = a.v / b.v, r = 1.f / b.v;
+    return rec(q, a, r, b, -q * r);
 }
-__device__ __forceinline__ AD operator-(const AD& a) { return rec1(-a.v, a, -1.0); }
+__device__ __forceinline__ AD operator-(const AD& a) { return rec1(-a.v, a, -1.f); }
 __device__ __forceinline__ AD sqrt_(const AD& a) {
     const float r = sqrtf(a.v);
-    return rec1(r, a, 0.5 / (double)r);
+    return rec1(r, a, 0.5f / r);
 }
 __device__ __forceinline__ AD hypot_(const AD& a, const AD& b) {
     const float h = hypotf(a.v, b.v);
-    return rec(h, a, (double)a.v / h, b, (double)b.v / h);
+    return rec(h, a, a.v / h, b, b.v / h);
 }
 __device__ __forceinline__ void sincos_(const AD& a, AD& s, AD& c) {
     float sv, cv;
     sincosf(a.v, &sv, &cv);
-    s = rec1(sv, a, (double)cv);
-    c = rec1(cv, a, -(double)sv);
+    s = rec1(sv, a, cv);
+    c = rec1(cv, a, -sv);
 }
 
 __device__ __forceinline__ Tan operator+(const Tan& a, const Tan& b) { return Tan{a.v + b.v, a.d + b.d}; }
@@ -441,6 +464,280 @@ __device__ void solve_velocity_t(const ContactK& k, const Geom<T>& g, Pair3<T>& 
     if (k.writableB) { vel.bx = vBx; vel.by = vBy; vel.bz = vBw; }
 }
 
+// ---- reverse of solve_velocity_t, written out ----------------------------------------
+// The velocity solve is the innermost loop of the adjoint (every velocity
+// iteration of every contact), so its vector-Jacobian product is written by hand
+// rather than taped: the forward is recomputed from its inputs, keeping the
+// state before each of its (at most four) sub-steps and the branch each took,
+// and the sub-steps are then reversed in the opposite order.  Checked against
+// the FP64 tangent (solve_velocity_t<Tan>) by the dot-product test.
+struct GeomBar {
+    float n[2];
+    float rA[2][2], rB[2][2];
+    float nm[2], tm[2], vb[2];
+    float k00, k11, k01, m00, m11, m01, mu;
+};
+
+struct VelSub {
+    float vA[3], vB[3];  // state before the sub-step
+    float im[4];         // ni0 ti0 ni1 ti1 before the sub-step
+    int kind;            // 0 tangent, 1 normal, 2 block
+    int j;               // point (sequential sub-steps)
+    int branch;          // clamp taken (sequential) or block case (0: none applied)
+};
+
+// relative velocity at (rA, rB) and its reverse
+__device__ __forceinline__ void relvel_f(const float* vA, const float* vB, const float* rA, const float* rB, float* cv) {
+    cv[0] = (vB[0] + (-rB[1]) * vB[2]) - (vA[0] + (-rA[1]) * vA[2]);
+    cv[1] = (vB[1] + rB[0] * vB[2]) - (vA[1] + rA[0] * vA[2]);
+}
+__device__ __forceinline__ void relvel_bar(const float* vA, const float* vB, const float* rA, const float* rB,
+                                           const float* cb, float* vbA, float* vbB, float* rbA, float* rbB) {
+    vbB[0] += cb[0]; vbB[1] += cb[1]; vbB[2] += cb[0] * (-rB[1]) + cb[1] * rB[0];
+    rbB[0] += cb[1] * vB[2]; rbB[1] -= cb[0] * vB[2];
+    vbA[0] -= cb[0]; vbA[1] -= cb[1]; vbA[2] -= cb[0] * (-rA[1]) + cb[1] * rA[0];
+    rbA[0] -= cb[1] * vA[2]; rbA[1] += cb[0] * vA[2];
+}
+
+// vbA/vbB/ib on entry: adjoints of the solve's outputs (vbA/vbB zero for bodies the
+// solve does not store); on exit: adjoints of its inputs.  gb accumulates.
+__device__ inline void solve_velocity_vjp(const ContactK& k, const Geom<float>& g, const Pair3<float>& vin, const Imp<float>& iin,
+                                   float* vbA, float* vbB, float* ib, GeomBar& gb) {
+    const float mAx = k.mA.x, mAy = k.mA.y, mBx = k.mB.x, mBy = k.mB.y;
+    const float n[2] = {val(g.n.x), val(g.n.y)};
+    const float t[2] = {n[1], -n[0]};
+    float rA[2][2], rB[2][2];
+    for (int j = 0; j < 2; ++j) {
+        rA[j][0] = g.rA[j].x; rA[j][1] = g.rA[j].y; rB[j][0] = g.rB[j].x; rB[j][1] = g.rB[j].y;
+    }
+    // forward, keeping the sub-steps
+    VelSub sub[4];
+    int ns = 0;
+    float vA[3] = {vin.ax, vin.ay, vin.az}, vB[3] = {vin.bx, vin.by, vin.bz};
+    float im[4] = {iin.ni0, iin.ti0, iin.ni1, iin.ti1};
+    auto save = [&](int kind, int j) -> VelSub& {
+        VelSub& s = sub[ns++];
+        for (int q = 0; q < 3; ++q) { s.vA[q] = vA[q]; s.vB[q] = vB[q]; }
+        for (int q = 0; q < 4; ++q) s.im[q] = im[q];
+        s.kind = kind; s.j = j; s.branch = 0;
+        return s;
+    };
+    auto apply_P = [&](const float* P, float LA, float LB) {
+        vA[0] = vA[0] - P[0] * mAx; vA[1] = vA[1] - P[1] * mAx; vA[2] = vA[2] - mAy * LA;
+        vB[0] = vB[0] + P[0] * mBx; vB[1] = vB[1] + P[1] * mBx; vB[2] = vB[2] + mBy * LB;
+    };
+    const bool block = g.cnt == 2 && !(g.k00 == 0.f && g.k11 == 0.f && g.k01 == 0.f);
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool tangentPass = pass == 0;
+        if (!tangentPass && block) {
+            VelSub& s = save(2, 0);
+            float dv0[2], dv1[2];
+            relvel_f(vA, vB, rA[0], rB[0], dv0);
+            relvel_f(vA, vB, rA[1], rB[1], dv1);
+            float vn0 = 0.f; vn0 += dv0[0] * n[0]; vn0 += dv0[1] * n[1];
+            float vn1 = 0.f; vn1 += dv1[0] * n[0]; vn1 += dv1[1] * n[1];
+            const float b0 = vn0 - g.vb[0], b1 = vn1 - g.vb[1];
+            const float a0 = im[0], a1 = im[2];
+            float Kx0 = 0.f; Kx0 += g.k00 * a0; Kx0 += g.k01 * a1;
+            float Kx1 = 0.f; Kx1 += g.k01 * a0; Kx1 += g.k11 * a1;
+            const float bp0 = b0 - Kx0, bp1 = b1 - Kx1;
+            float x0, x1;
+            int cs = 0;
+            {
+                float q0 = 0.f; q0 += g.m00 * bp0; q0 += g.m01 * bp1;
+                float q1 = 0.f; q1 += g.m01 * bp0; q1 += g.m11 * bp1;
+                x0 = -q0; x1 = -q1;
+                if (x0 >= 0.f && x1 >= 0.f) cs = 1;
+            }
+            if (!cs) {
+                x0 = -g.nm[0] * bp0; x1 = 0.f;
+                const float vn2 = g.k01 * x0 + bp1;
+                if (x0 >= 0.f && vn2 >= 0.f) cs = 2;
+            }
+            if (!cs) {
+                x0 = 0.f; x1 = -g.nm[1] * bp1;
+                const float vn1b = g.k01 * x1 + bp0;
+                if (x1 >= 0.f && vn1b >= 0.f) cs = 3;
+            }
+            if (!cs) {
+                x0 = 0.f; x1 = 0.f;
+                if (bp0 >= 0.f && bp1 >= 0.f) cs = 4;
+            }
+            s.branch = cs;
+            if (cs) {
+                const float d0 = x0 - im[0], d1 = x1 - im[2];
+                const float P0[2] = {n[0] * d0, n[1] * d0}, P1[2] = {n[0] * d1, n[1] * d1};
+                const float P[2] = {P0[0] + P1[0], P0[1] + P1[1]};
+                const float LA = (rA[0][0] * P0[1] - rA[0][1] * P0[0]) + (rA[1][0] * P1[1] - rA[1][1] * P1[0]);
+                const float LB = (rB[0][0] * P0[1] - rB[0][1] * P0[0]) + (rB[1][0] * P1[1] - rB[1][1] * P1[0]);
+                vA[0] = vA[0] + (-(P[0] * mAx)); vA[1] = vA[1] + (-(P[1] * mAx)); vA[2] = vA[2] + (-(mAy * LA));
+                vB[0] = vB[0] + P[0] * mBx; vB[1] = vB[1] + P[1] * mBx; vB[2] = vB[2] + mBy * LB;
+                im[0] = x0; im[2] = x1;
+            }
+            continue;
+        }
+        const float* dir = tangentPass ? t : n;
+        for (int j = (g.cnt == 2) ? 1 : 0; j >= 0; --j) {
+            VelSub& s = save(tangentPass ? 0 : 1, j);
+            float cv[2];
+            relvel_f(vA, vB, rA[j], rB[j], cv);
+            float dd = 0.f; dd += cv[0] * dir[0]; dd += cv[1] * dir[1];
+            float oldImp, newImp;
+            if (tangentPass) {
+                const float dvel = 0.f - dd;
+                const float lambda = g.tm[j] * dvel;
+                const float maxImp = g.mu * im[2 * j];
+                oldImp = im[2 * j + 1];
+                const float sv = oldImp + lambda;
+                if (sv < -maxImp) { newImp = -maxImp; s.branch = 1; }
+                else if (maxImp < sv) { newImp = maxImp; s.branch = 2; }
+                else { newImp = sv; s.branch = 0; }
+            } else {
+                const float lambda = g.nm[j] * (g.vb[j] - dd);
+                oldImp = im[2 * j];
+                const float sv = oldImp + lambda;
+                if (sv < 0.f) { newImp = 0.f; s.branch = 1; } else { newImp = sv; s.branch = 0; }
+            }
+            const float inc = newImp - oldImp;
+            const float P[2] = {dir[0] * inc, dir[1] * inc};
+            const float LA = rA[j][0] * P[1] - rA[j][1] * P[0], LB = rB[j][0] * P[1] - rB[j][1] * P[0];
+            apply_P(P, LA, LB);
+            if (tangentPass) im[2 * j + 1] = oldImp + inc; else im[2 * j] = oldImp + inc;
+        }
+    }
+    // reverse
+    float nb[2] = {0.f, 0.f};
+    for (int q = ns - 1; q >= 0; --q) {
+        const VelSub& s = sub[q];
+        if (s.kind == 2) {
+            if (!s.branch) continue;
+            // recompute the block step's values from its inputs
+            float dv0[2], dv1[2];
+            relvel_f(s.vA, s.vB, rA[0], rB[0], dv0);
+            relvel_f(s.vA, s.vB, rA[1], rB[1], dv1);
+            float vn0 = 0.f; vn0 += dv0[0] * n[0]; vn0 += dv0[1] * n[1];
+            float vn1 = 0.f; vn1 += dv1[0] * n[0]; vn1 += dv1[1] * n[1];
+            const float b0 = vn0 - g.vb[0], b1 = vn1 - g.vb[1];
+            const float a0 = s.im[0], a1 = s.im[2];
+            float Kx0 = 0.f; Kx0 += g.k00 * a0; Kx0 += g.k01 * a1;
+            float Kx1 = 0.f; Kx1 += g.k01 * a0; Kx1 += g.k11 * a1;
+            const float bp0 = b0 - Kx0, bp1 = b1 - Kx1;
+            float x0 = 0.f, x1 = 0.f;
+            if (s.branch == 1) {
+                float q0 = 0.f; q0 += g.m00 * bp0; q0 += g.m01 * bp1;
+                float q1 = 0.f; q1 += g.m01 * bp0; q1 += g.m11 * bp1;
+                x0 = -q0; x1 = -q1;
+            } else if (s.branch == 2) {
+                x0 = -g.nm[0] * bp0;
+            } else if (s.branch == 3) {
+                x1 = -g.nm[1] * bp1;
+            }
+            const float d0 = x0 - a0, d1 = x1 - a1;
+            const float P0[2] = {n[0] * d0, n[1] * d0}, P1[2] = {n[0] * d1, n[1] * d1};
+            // velocities
+            float Pb[2] = {-mAx * vbA[0] + mBx * vbB[0], -mAx * vbA[1] + mBx * vbB[1]};
+            const float LAb = -mAy * vbA[2], LBb = mBy * vbB[2];
+            float P0b[2] = {Pb[0], Pb[1]}, P1b[2] = {Pb[0], Pb[1]};
+            gb.rA[0][0] += LAb * P0[1]; gb.rA[0][1] -= LAb * P0[0]; P0b[0] -= LAb * rA[0][1]; P0b[1] += LAb * rA[0][0];
+            gb.rA[1][0] += LAb * P1[1]; gb.rA[1][1] -= LAb * P1[0]; P1b[0] -= LAb * rA[1][1]; P1b[1] += LAb * rA[1][0];
+            gb.rB[0][0] += LBb * P0[1]; gb.rB[0][1] -= LBb * P0[0]; P0b[0] -= LBb * rB[0][1]; P0b[1] += LBb * rB[0][0];
+            gb.rB[1][0] += LBb * P1[1]; gb.rB[1][1] -= LBb * P1[0]; P1b[0] -= LBb * rB[1][1]; P1b[1] += LBb * rB[1][0];
+            nb[0] += d0 * P0b[0] + d1 * P1b[0];
+            nb[1] += d0 * P0b[1] + d1 * P1b[1];
+            const float d0b = n[0] * P0b[0] + n[1] * P0b[1];
+            const float d1b = n[0] * P1b[0] + n[1] * P1b[1];
+            const float x0b = ib[0] + d0b, x1b = ib[2] + d1b;
+            float a0b = -d0b, a1b = -d1b;
+            float bp0b = 0.f, bp1b = 0.f;
+            if (s.branch == 1) {
+                const float q0b = -x0b, q1b = -x1b;
+                gb.m00 += q0b * bp0; gb.m01 += q0b * bp1 + q1b * bp0; gb.m11 += q1b * bp1;
+                bp0b = q0b * g.m00 + q1b * g.m01;
+                bp1b = q0b * g.m01 + q1b * g.m11;
+            } else if (s.branch == 2) {
+                gb.nm[0] -= x0b * bp0;
+                bp0b = -x0b * g.nm[0];
+            } else if (s.branch == 3) {
+                gb.nm[1] -= x1b * bp1;
+                bp1b = -x1b * g.nm[1];
+            }
+            const float Kx0b = -bp0b, Kx1b = -bp1b;
+            gb.k00 += Kx0b * a0; gb.k01 += Kx0b * a1 + Kx1b * a0; gb.k11 += Kx1b * a1;
+            a0b += Kx0b * g.k00 + Kx1b * g.k01;
+            a1b += Kx0b * g.k01 + Kx1b * g.k11;
+            const float vn0b = bp0b, vn1b = bp1b;
+            gb.vb[0] -= bp0b; gb.vb[1] -= bp1b;
+            const float dv0b[2] = {vn0b * n[0], vn0b * n[1]}, dv1b[2] = {vn1b * n[0], vn1b * n[1]};
+            nb[0] += vn0b * dv0[0] + vn1b * dv1[0];
+            nb[1] += vn0b * dv0[1] + vn1b * dv1[1];
+            relvel_bar(s.vA, s.vB, rA[0], rB[0], dv0b, vbA, vbB, gb.rA[0], gb.rB[0]);
+            relvel_bar(s.vA, s.vB, rA[1], rB[1], dv1b, vbA, vbB, gb.rA[1], gb.rB[1]);
+            ib[0] = a0b; ib[2] = a1b;
+            continue;
+        }
+        const bool tangentPass = s.kind == 0;
+        const int j = s.j;
+        const float* dir = tangentPass ? t : n;
+        float cv[2];
+        relvel_f(s.vA, s.vB, rA[j], rB[j], cv);
+        float dd = 0.f; dd += cv[0] * dir[0]; dd += cv[1] * dir[1];
+        const int ci = tangentPass ? 2 * j + 1 : 2 * j;  // impulse this sub-step updates
+        const float oldImp = s.im[ci];
+        float newImp, lambda, maxImp = 0.f;
+        if (tangentPass) {
+            lambda = g.tm[j] * (0.f - dd);
+            maxImp = g.mu * s.im[2 * j];
+            newImp = (s.branch == 1) ? -maxImp : (s.branch == 2) ? maxImp : oldImp + lambda;
+        } else {
+            lambda = g.nm[j] * (g.vb[j] - dd);
+            newImp = (s.branch == 1) ? 0.f : oldImp + lambda;
+        }
+        const float inc = newImp - oldImp;
+        const float P[2] = {dir[0] * inc, dir[1] * inc};
+        // velocities
+        float Pb[2] = {-mAx * vbA[0] + mBx * vbB[0], -mAx * vbA[1] + mBx * vbB[1]};
+        const float LAb = -mAy * vbA[2], LBb = mBy * vbB[2];
+        gb.rA[j][0] += LAb * P[1]; gb.rA[j][1] -= LAb * P[0]; Pb[0] -= LAb * rA[j][1]; Pb[1] += LAb * rA[j][0];
+        gb.rB[j][0] += LBb * P[1]; gb.rB[j][1] -= LBb * P[0]; Pb[0] -= LBb * rB[j][1]; Pb[1] += LBb * rB[j][0];
+        float dirb[2] = {inc * Pb[0], inc * Pb[1]};
+        float incb = dir[0] * Pb[0] + dir[1] * Pb[1];
+        // the stored impulse is old + inc
+        incb += ib[ci];
+        float oldb = ib[ci];
+        const float newb = incb;
+        oldb -= incb;
+        float sb = 0.f, maxb = 0.f;
+        if (tangentPass) {
+            if (s.branch == 1) maxb = -newb; else if (s.branch == 2) maxb = newb; else sb = newb;
+        } else {
+            sb = (s.branch == 1) ? 0.f : newb;
+        }
+        oldb += sb;
+        const float lamb = sb;
+        float cvb[2];
+        if (tangentPass) {
+            gb.mu += maxb * s.im[2 * j];
+            ib[2 * j] += maxb * g.mu;
+            gb.tm[j] += lamb * (0.f - dd);
+            const float dvelb = lamb * g.tm[j];  // dvel = 0 - dd
+            cvb[0] = -dvelb * dir[0]; cvb[1] = -dvelb * dir[1];
+            dirb[0] -= dvelb * cv[0]; dirb[1] -= dvelb * cv[1];
+        } else {
+            gb.nm[j] += lamb * (g.vb[j] - dd);
+            gb.vb[j] += lamb * g.nm[j];
+            const float ddb = -lamb * g.nm[j];
+            cvb[0] = ddb * dir[0]; cvb[1] = ddb * dir[1];
+            dirb[0] += ddb * cv[0]; dirb[1] += ddb * cv[1];
+        }
+        ib[ci] = oldb;
+        relvel_bar(s.vA, s.vB, rA[j], rB[j], cvb, vbA, vbB, gb.rA[j], gb.rB[j]);
+        if (tangentPass) { nb[0] -= dirb[1]; nb[1] += dirb[0]; }
+        else { nb[0] += dirb[0]; nb[1] += dirb[1]; }
+        (void)lambda;
+    }
+    gb.n[0] += nb[0]; gb.n[1] += nb[1];
+}
+
 // GetPSM (PositionSolverManifold.cpp:103-121)
 template <class T>
 struct PSMt {
@@ -530,6 +827,140 @@ __device__ void solve_position_t(const ContactK& k, const DConf& c, Pair3<T>& po
     }
     if (k.writableA) { pos.ax = pAx; pos.ay = pAy; pos.az = pAz; }
     if (k.writableB) { pos.bx = pBx; pos.by = pBy; pos.bz = pBz; }
+}
+
+// ---- hand-written reverse of the position solver -----------------------------------
+// q̄ += (d rotate(v, q) / dq)^T ō for a constant v (rotatet and urotatet alike).
+__device__ __forceinline__ void rot_qbar(float vx, float vy, float ox, float oy, float& qx, float& qy) {
+    qx += ox * vx + oy * vy;
+    qy += oy * vx - ox * vy;
+}
+
+// Adjoints of one body's transformation (p = position - rotate(lc, q), q = (cos a,
+// sin a)) turned into adjoints of its position (x, y, angle).
+__device__ __forceinline__ void xf_bar_to_pos(float pbx, float pby, float qbx, float qby, float lcx, float lcy,
+                                              float s, float c, float* out) {
+    out[0] += pbx;
+    out[1] += pby;
+    rot_qbar(lcx, lcy, -pbx, -pby, qbx, qby);
+    out[2] += qbx * -s + qby * c;
+}
+
+// Reverse of one point of GaussSeidel::SolvePositionConstraint: given the body
+// positions p the point starts from and the adjoints sb of its increments s(p),
+// adds (ds/dp)^T sb to pb.  Forward values are recomputed in the forward's order.
+__device__ inline void pos_point_vjp(const ContactK& k, const DConf& c, int idx, const float* p, const float* sb,
+                                     float* pb) {
+    // forward: transformations, the point's manifold and the solver function
+    float sA, cA, sB, cB;
+    sincosf(p[2], &sA, &cA);
+    sincosf(p[5], &sB, &cB);
+    const XfT<float> xfA = get_xft(p[0], p[1], p[2], k.mA.z, k.mA.w);
+    const XfT<float> xfB = get_xft(p[3], p[4], p[5], k.mB.z, k.mB.w);
+    const PSMt<float> psm = get_psmt(k, idx, xfA, xfB);
+    const float invMassTotal = k.mA.x + k.mB.x;
+    const float separation = psm.sep - (k.rA + k.rB);
+    const float rAx = psm.pt.x - p[0], rAy = psm.pt.y - p[1];
+    const float rBx = psm.pt.x - p[3], rBy = psm.pt.y - p[4];
+    const float crA = rAx * psm.n.y - rAy * psm.n.x, crB = rBx * psm.n.y - rBy * psm.n.x;
+    const float K = invMassTotal + k.mA.y * (crA * crA) + k.mB.y * (crB * crB);
+    const float x = c.regResolutionRate * (separation + c.linearSlop);
+    const bool active = !(x < -c.maxLinearCorrection) && !(0.f < x);
+    const float Cv = -clampt(x, -c.maxLinearCorrection, 0.f);
+    const float nCx = psm.n.x * Cv, nCy = psm.n.y * Cv;
+    const float invK = 1.0f / K;
+    const float Px = nCx * invK, Py = nCy * invK;
+    // reverse of the solver function
+    float Pbx = -k.mA.x * sb[0] + k.mB.x * sb[3];
+    float Pby = -k.mA.x * sb[1] + k.mB.x * sb[4];
+    const float LAb = -k.mA.y * sb[2], LBb = k.mB.y * sb[5];
+    float rAbx = LAb * Py, rAby = -LAb * Px, rBbx = LBb * Py, rBby = -LBb * Px;
+    Pbx += -LAb * rAy - LBb * rBy;
+    Pby += LAb * rAx + LBb * rBx;
+    const float nCbx = Pbx * invK, nCby = Pby * invK;
+    const float invKb = Pbx * nCx + Pby * nCy;
+    const float Kb = -invKb * invK * invK;
+    float nbx = nCbx * Cv, nby = nCby * Cv;
+    const float Cb = nCbx * psm.n.x + nCby * psm.n.y;
+    const float sepb = active ? -Cb * c.regResolutionRate : 0.f;
+    const float crAb = Kb * 2.f * k.mA.y * crA, crBb = Kb * 2.f * k.mB.y * crB;
+    rAbx += crAb * psm.n.y; rAby -= crAb * psm.n.x;
+    rBbx += crBb * psm.n.y; rBby -= crBb * psm.n.x;
+    nbx += -crAb * rAy - crBb * rBy;
+    nby += crAb * rAx + crBb * rBx;
+    const float ptbx = rAbx + rBbx, ptby = rAby + rBby;
+    pb[0] -= rAbx; pb[1] -= rAby; pb[3] -= rBbx; pb[4] -= rBby;
+    // reverse of the manifold point (GetPSM) onto both transformations
+    float xApx = 0.f, xApy = 0.f, qAx = 0.f, qAy = 0.f, xBpx = 0.f, xBpy = 0.f, qBx = 0.f, qBy = 0.f;
+    const float plx = idx ? k.p1x : k.p0x, ply = idx ? k.p1y : k.p0y;
+    if (k.type == M_CIRCLES) {
+        const V<float> a = xformt(cv<float>(k.lpx, k.lpy), xfA), b = xformt(cv<float>(plx, ply), xfB);
+        const float dx = b.x - a.x, dy = b.y - a.y;
+        const float m2 = dx * dx + dy * dy;
+        float dbx = sepb * psm.n.x, dby = sepb * psm.n.y;
+        const float ntx = nbx + sepb * dx, nty = nby + sepb * dy;
+        const float m = is_normal_f(m2) ? sqrtf(m2) : hypotf(dx, dy);
+        if (is_normal_f(m)) {  // n = delta / |delta|; otherwise n is the constant fallback
+            const float dn = ntx * psm.n.x + nty * psm.n.y;
+            dbx += (ntx - psm.n.x * dn) / m;
+            dby += (nty - psm.n.y * dn) / m;
+        }
+        const float abx = 0.5f * ptbx - dbx, aby = 0.5f * ptby - dby;
+        const float bbx = 0.5f * ptbx + dbx, bby = 0.5f * ptby + dby;
+        xApx += abx; xApy += aby; rot_qbar(k.lpx, k.lpy, abx, aby, qAx, qAy);
+        xBpx += bbx; xBpy += bby; rot_qbar(plx, ply, bbx, bby, qBx, qBy);
+    } else if (k.type == M_FACEA) {
+        const V<float> pp = xformt(cv<float>(k.lpx, k.lpy), xfA);
+        const float dx = psm.pt.x - pp.x, dy = psm.pt.y - pp.y;
+        const float dbx = sepb * psm.n.x, dby = sepb * psm.n.y;
+        const float ntx = nbx + sepb * dx, nty = nby + sepb * dy;
+        const float ptx = ptbx + dbx, pty = ptby + dby;
+        xApx -= dbx; xApy -= dby; rot_qbar(k.lpx, k.lpy, -dbx, -dby, qAx, qAy);
+        rot_qbar(k.lnx, k.lny, ntx, nty, qAx, qAy);
+        xBpx += ptx; xBpy += pty; rot_qbar(plx, ply, ptx, pty, qBx, qBy);
+    } else {
+        const V<float> pp = xformt(cv<float>(k.lpx, k.lpy), xfB);
+        const float dx = psm.pt.x - pp.x, dy = psm.pt.y - pp.y;
+        // n = -nb
+        const float nbn_x = -psm.n.x, nbn_y = -psm.n.y;
+        const float dbx = sepb * nbn_x, dby = sepb * nbn_y;
+        const float ntx = -nbx + sepb * dx, nty = -nby + sepb * dy;
+        const float ptx = ptbx + dbx, pty = ptby + dby;
+        xBpx -= dbx; xBpy -= dby; rot_qbar(k.lpx, k.lpy, -dbx, -dby, qBx, qBy);
+        rot_qbar(k.lnx, k.lny, ntx, nty, qBx, qBy);
+        xApx += ptx; xApy += pty; rot_qbar(plx, ply, ptx, pty, qAx, qAy);
+    }
+    xf_bar_to_pos(xApx, xApy, qAx, qAy, k.mA.z, k.mA.w, sA, cA, pb);
+    xf_bar_to_pos(xBpx, xBpy, qBx, qBy, k.mB.z, k.mB.w, sB, cB, pb + 3);
+}
+
+// Reverse of solve_position_t in float: yb = adjoints of the output positions
+// (zero for a body the solve does not store); pb = adjoints of the inputs.
+__device__ inline void solve_position_vjp(const ContactK& k, const DConf& c, const float* p, const float* yb, float* pb) {
+    for (int i = 0; i < 6; ++i) pb[i] = yb[i];
+    if (k.count == 1u) {
+        pos_point_vjp(k, c, 0, p, yb, pb);
+    } else if (k.count == 2u) {
+        const XfT<float> xfA = get_xft(p[0], p[1], p[2], k.mA.z, k.mA.w), xfB = get_xft(p[3], p[4], p[5], k.mB.z, k.mB.w);
+        const float sep0 = get_psmt(k, 0, xfA, xfB).sep, sep1 = get_psmt(k, 1, xfA, xfB).sep;
+        if (almost_equal(sep0, sep1)) {
+            pos_point_vjp(k, c, 0, p, yb, pb);
+            pos_point_vjp(k, c, 1, p, yb, pb);
+        } else if (sep0 < sep1 || sep1 < sep0) {
+            // p1 = p + s_first(p); p2 = p1 + s_second(p1)
+            const int first = (sep0 < sep1) ? 0 : 1;
+            Pair3<float> q{p[0], p[1], p[2], p[3], p[4], p[5]};
+            const PSMt<float> pf = get_psmt(k, first, xfA, xfB);
+            float s0[6], sp;
+            pos_solver_fnt(pf, V<float>{q.ax, q.ay}, V<float>{q.bx, q.by}, k, c, s0, sp);
+            const float p1[6] = {q.ax + s0[0], q.ay + s0[1], q.az + s0[2], q.bx + s0[3], q.by + s0[4], q.bz + s0[5]};
+            float b1[6];
+            for (int i = 0; i < 6; ++i) b1[i] = yb[i];
+            pos_point_vjp(k, c, 1 - first, p1, yb, b1);
+            for (int i = 0; i < 6; ++i) pb[i] = b1[i];
+            pos_point_vjp(k, c, first, p, b1, pb);
+        }
+    }
 }
 
 // Body velocity at the start of the solve (k_body_begin): acceleration,

@@ -110,6 +110,8 @@ struct StepTape {
                        //       impulses from (-1 none; -2 slot not updated)
     uint8_t* created;  // [C] slot created by this step's post-solve contact search
     uint32_t* hdr;     // [kSerialColour + 2 + 4] colour offsets, n_colours, n_active, replay mismatches
+    uint32_t* wseg;    // [W*2] first sweep position and constraint count of each world
+    uint32_t* wcol;    // [W*kColStride] colour offsets of each world (relative to its first position)
     int iv, ip;        // velocity and position iterations recorded
     uint32_t kcap;
 };

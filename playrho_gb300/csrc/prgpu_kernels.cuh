@@ -63,11 +63,11 @@ struct TanState {
     const double* fdot;  // [S] tangent of shape friction
 };
 
-int adj_grid(int sm_count);
-cudaError_t launch_adj_step(const DW& d, const StepTape* tp, const AdjState& a, uint32_t n_slots, int grid,
-                            cudaStream_t s);
+// sets the shared-memory attribute of the adjoint kernel; returns its blocks per SM
+int adj_setup();
+cudaError_t launch_adj_step(const DW& d, const StepTape* tp, const AdjState& a, uint32_t n_slots, cudaStream_t s);
 cudaError_t launch_tan_step(const DW& d, const StepTape* tp, const TanState& t, float* gval, uint32_t n_slots,
-                            int grid, cudaStream_t s);
+                            cudaStream_t s);
 // Sets k_world_solve's dynamic shared memory to stage_bytes; returns its CTAs per SM.
 int world_blocks_per_sm(uint32_t stage_bytes);
 

@@ -19,6 +19,7 @@
 
 #include "prgpu_collide.cuh"
 #include "prgpu_kernels.cuh"
+#include "prgpu_tape.cuh"
 
 namespace prgpu {
 
@@ -1230,6 +1231,10 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
         for (uint32_t t = base + rank; t < base + n; t += size) build_constraint(d, t, d.k_order[t]);
         G::sync();
     }
+    if (d.tape) {  // recorded for the adjoint
+        for (uint32_t t = base + rank; t < base + n; t += size) tape_constraint(d, t);
+        tape_world(d, w, base, n, col_off, rank, size);
+    }
     const uint32_t b0 = d.w_body_off[w], nb = d.w_body_off[w + 1] - b0;
     if (nb <= stage_cap) {
         // stage the world's velocities and positions in shared memory
@@ -1456,7 +1461,7 @@ void launch_islands_colour(const DW& d, const Launch& L, cudaStream_t s) {
 void launch_build_constraints(const DW& d, const Launch& L, cudaStream_t s) {
     // per world, k_world_solve builds the constraints once it has coloured them
     if (!L.per_world) k_build_constraints<<<L.grid, L.threads, 0, s>>>(d);
-    if (d.tape) launch_tape_constraints(d, L, s);  // recording runs the grid-wide solve
+    if (d.tape && !L.per_world) launch_tape_constraints(d, L, s);  // per world, k_world_solve records
 }
 
 void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) {

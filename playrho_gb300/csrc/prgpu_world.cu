@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -37,6 +38,8 @@ struct prgpu_world {
     struct AdjWindow* adj = nullptr;  // open StepAdjoint window, if any
     uint32_t warp_world_max = 0;     // worlds of at most this many bodies are swept by one warp
 };
+
+extern "C" void adjoint_drop_graphs(prgpu_world* w);
 
 namespace {
 
@@ -413,6 +416,7 @@ uint32_t count_big_worlds(const prgpu_world* w) {
 int drop_graph(prgpu_world* w) {
     CU(cudaSetDevice(w->device));
     CU(cudaStreamSynchronize(w->stream));
+    adjoint_drop_graphs(w);
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->graph_def) { cudaGraphDestroy(w->graph_def); w->graph_def = nullptr; }
     return PRGPU_OK;
@@ -1230,7 +1234,15 @@ struct AdjWindow {
     uint32_t kcap = 0, ccap = 0;
     int grid = 0;
     uint32_t mismatches = 0, overflows = 0;
+    double forward_ms = 0, record_ms = 0, reverse_ms = 0;  // host time of the phases of the last passes
+    std::vector<cudaGraphExec_t> rec_graphs;  // recorded step into tape i, captured once per window
 };
+
+void adjoint_drop_graphs(prgpu_world* w) {
+    if (!w || !w->adj) return;
+    for (cudaGraphExec_t& g : w->adj->rec_graphs)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
 
 static int adj_alloc(prgpu_world* w, AdjWindow* a, void** p, size_t bytes) {
     *p = nullptr;
@@ -1243,6 +1255,8 @@ static int adj_alloc(prgpu_world* w, AdjWindow* a, void** p, size_t bytes) {
 void adjoint_close(prgpu_world* w) {
     if (!w || !w->adj) return;
     AdjWindow* a = w->adj;
+    cudaStreamSynchronize(w->stream);
+    adjoint_drop_graphs(w);
     for (void* p : a->snaps) cudaFree(p);
     if (a->end_state) cudaFree(a->end_state);
     for (void* p : a->mem) cudaFree(p);
@@ -1307,6 +1321,34 @@ static int check_against(prgpu_world* w, const void* snap, uint32_t* differ) {
     return PRGPU_OK;
 }
 
+// Captures one recorded step into tape i: the tape's per-step words reset, then
+// the regular step with d.tape set, in the per-world sweep layout that the
+// adjoint and tangent kernels follow.
+static int capture_record_step(prgpu_world* w, int i) {
+    AdjWindow* a = w->adj;
+    const StepTape& t = a->tapes[i];
+    const bool per_world = w->L.per_world;
+    CU(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(t.src, 0xfe, 2 * (size_t)a->ccap, w->stream);
+    cudaMemsetAsync(t.created, 0, a->ccap, w->stream);
+    cudaMemsetAsync(t.hdr, 0, sizeof(uint32_t) * (kSerialColour + 6), w->stream);
+    w->L.per_world = true;
+    w->d.tape = a->d_tapes + i;
+    enqueue_step(w, true, nullptr, true);
+    w->d.tape = nullptr;
+    w->L.per_world = per_world;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e1 = cudaStreamEndCapture(w->stream, &g);
+    if (e1 != cudaSuccess) return fail(w, PRGPU_ECUDA, "record capture: %s", cudaGetErrorString(e1));
+    const cudaError_t e2 = cudaGraphInstantiate(&a->rec_graphs[i], g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) {
+        a->rec_graphs[i] = nullptr;
+        return fail(w, PRGPU_ECUDA, "record instantiate: %s", cudaGetErrorString(e2));
+    }
+    return PRGPU_OK;
+}
+
 static int record_segment(prgpu_world* w, int seg, int n) {
     AdjWindow* a = w->adj;
     int rc = snap_copy(w, a->snaps[seg], false);
@@ -1315,26 +1357,17 @@ static int record_segment(prgpu_world* w, int seg, int n) {
     w->conf_valid = false;
     rc = set_conf(w, &a->conf);
     if (rc) return rc;
-    const bool per_world = w->L.per_world;
-    w->L.per_world = false;
+    a->rec_graphs.resize(a->every, nullptr);
     for (int i = 0; i < n; ++i) {
-        const StepTape& t = a->tapes[i];
-        cudaMemsetAsync(t.src, 0xfe, 2 * (size_t)a->ccap, w->stream);
-        cudaMemsetAsync(t.created, 0, a->ccap, w->stream);
-        cudaMemsetAsync(t.hdr, 0, sizeof(uint32_t) * (kSerialColour + 6), w->stream);
-        w->d.tape = a->d_tapes + i;
-        enqueue_step(w, true);
-        w->d.tape = nullptr;
+        if (!a->rec_graphs[i] && (rc = capture_record_step(w, i))) return rc;
+        CU(cudaGraphLaunch(a->rec_graphs[i], w->stream));
     }
-    w->L.per_world = per_world;
-    CU(cudaGetLastError());
     // replay mismatches of the differentiable restatement
-    for (int i = 0; i < n; ++i) {
-        uint32_t bad = 0;
-        CU(cudaMemcpyAsync(&bad, a->tapes[i].hdr + kSerialColour + 5, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
-        CU(cudaStreamSynchronize(w->stream));
-        a->mismatches += bad;
-    }
+    std::vector<uint32_t> bad(n, 0);
+    for (int i = 0; i < n; ++i)
+        CU(cudaMemcpyAsync(&bad[i], a->tapes[i].hdr + kSerialColour + 5, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    for (int i = 0; i < n; ++i) a->mismatches += bad[i];
     rc = check_device_error(w);
     if (rc) return rc;
     // the segment must end where the forward pass continued from
@@ -1355,7 +1388,7 @@ int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every) {
     a->kcap = w->d.contact_cap + w->d.n_joints;
     a->ccap = w->d.contact_cap;
     a->snap_bytes = snap_size(w);
-    a->grid = adj_grid(w->L.prims.sm_count);
+    a->grid = adj_setup();
     w->adj = a;
     if (a->grid < 1) { adjoint_close(w); return fail(w, PRGPU_ECUDA, "adjoint kernels cannot be resident"); }
     const uint32_t N = w->d.n_bodies, K = a->kcap, C = a->ccap, S = w->d.n_shapes;
@@ -1392,6 +1425,8 @@ static int ensure_tapes(prgpu_world* w) {
         AA(t.vel, sizeof(float4) * 3 * (size_t)K * std::max(iv, 1));
         AA(t.pos, sizeof(float4) * 2 * (size_t)K * std::max(ip, 1));
         AA(t.src, 2 * (size_t)C); AA(t.created, C); AA(t.hdr, sizeof(uint32_t) * (kSerialColour + 6));
+        AA(t.wseg, sizeof(uint32_t) * 2 * (size_t)w->d.n_worlds);
+        AA(t.wcol, sizeof(uint32_t) * kColStride * (size_t)w->d.n_worlds);
     }
     AA(a->d_tapes, sizeof(StepTape) * a->every);
     CU(cudaMemcpyAsync(a->d_tapes, a->tapes.data(), sizeof(StepTape) * a->every, cudaMemcpyHostToDevice, w->stream));
@@ -1411,6 +1446,7 @@ int prgpu_adjoint_forward(prgpu_world* w, const prgpu_step_conf* conf, int n_ste
     CU(cudaSetDevice(w->device));
     int rc = ensure_tapes(w);
     if (rc) return rc;
+    const auto t0 = std::chrono::steady_clock::now();
     for (int i = 0; i < n_steps; ++i) {
         if (a->steps % a->every == 0) {
             void* buf = nullptr;
@@ -1421,7 +1457,18 @@ int prgpu_adjoint_forward(prgpu_world* w, const prgpu_step_conf* conf, int n_ste
         if ((rc = run_steps(w, conf, 1, false))) return rc;
         ++a->steps;
     }
-    return check_device_error(w);
+    rc = check_device_error(w);
+    a->forward_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int prgpu_adjoint_profile(prgpu_world* w, double* forward_ms, double* record_ms, double* reverse_ms) {
+    if (!w) return PRGPU_EINVAL;
+    if (!w->adj) return fail(w, PRGPU_ESTATE, "no adjoint window is open");
+    if (forward_ms) *forward_ms = w->adj->forward_ms;
+    if (record_ms) *record_ms = w->adj->record_ms;
+    if (reverse_ms) *reverse_ms = w->adj->reverse_ms;
+    return PRGPU_OK;
 }
 
 int prgpu_adjoint_backward(prgpu_world* w, const float* dl_dpos3, const float* dl_dvel3, float* dl_dpos3_start,
@@ -1450,14 +1497,21 @@ int prgpu_adjoint_backward(prgpu_world* w, const float* dl_dpos3, const float* d
     CU(cudaMemsetAsync(a->adj.fbar, 0, sizeof(float) * std::max<uint32_t>(S, 1), w->stream));
     CU(cudaMemsetAsync(a->adj.err, 0, sizeof(uint32_t), w->stream));
     const int nseg = (a->steps + a->every - 1) / a->every;
+    using clk = std::chrono::steady_clock;
+    a->record_ms = a->reverse_ms = 0;
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int first = seg * a->every, n = std::min(a->every, a->steps - first);
+        const auto t0 = clk::now();
         if ((rc = record_segment(w, seg, n))) return rc;
+        const auto t1 = clk::now();
         for (int i = n - 1; i >= 0; --i) {
-            const cudaError_t e = launch_adj_step(w->d, a->d_tapes + i, a->adj, a->ccap, a->grid, w->stream);
+            const cudaError_t e = launch_adj_step(w->d, a->d_tapes + i, a->adj, a->ccap, w->stream);
             if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "adjoint step: %s", cudaGetErrorString(e));
         }
         if ((rc = check_device_error(w))) return rc;
+        const auto t2 = clk::now();
+        a->record_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        a->reverse_ms += std::chrono::duration<double, std::milli>(t2 - t1).count();
     }
     if ((rc = snap_copy(w, a->end_state, false))) return rc;
     uint32_t err = 0;
@@ -1509,7 +1563,7 @@ int prgpu_adjoint_tangent(prgpu_world* w, const double* dpos3_start, const doubl
         const int first = seg * a->every, n = std::min(a->every, a->steps - first);
         if ((rc = record_segment(w, seg, n))) return rc;
         for (int i = 0; i < n; ++i) {
-            const cudaError_t e = launch_tan_step(w->d, a->d_tapes + i, a->tan, a->tgval, a->ccap, a->grid, w->stream);
+            const cudaError_t e = launch_tan_step(w->d, a->d_tapes + i, a->tan, a->tgval, a->ccap, w->stream);
             if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "tangent step: %s", cudaGetErrorString(e));
         }
         if ((rc = check_device_error(w))) return rc;

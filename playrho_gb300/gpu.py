@@ -110,6 +110,7 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_adjoint_tangent.argtypes = [P, P, P, P, P, P]
     lib.prgpu_adjoint_info.argtypes = [P, P, P, P]
     lib.prgpu_adjoint_end.argtypes = [P]
+    lib.prgpu_adjoint_profile.argtypes = [P, P, P, P]
     lib.prgpu_autotune.argtypes = [P, ctypes.POINTER(StepConf), I, ctypes.POINTER(Schedule)]
     _LIB = lib
     return lib
@@ -124,7 +125,8 @@ def exported_symbols() -> List[str]:
         "prgpu_last_step_phase_ms", "prgpu_graph_kernel_count", "prgpu_set_sweep_mode", "prgpu_get_sweep_mode",
         "prgpu_set_warp_world_max_bodies", "prgpu_get_warp_world_max_bodies", "prgpu_autotune",
         "prgpu_set_stage_bytes", "prgpu_get_stage_bytes", "prgpu_adjoint_begin", "prgpu_adjoint_forward",
-        "prgpu_adjoint_backward", "prgpu_adjoint_tangent", "prgpu_adjoint_info", "prgpu_adjoint_end"]
+        "prgpu_adjoint_backward", "prgpu_adjoint_tangent", "prgpu_adjoint_info", "prgpu_adjoint_end",
+        "prgpu_adjoint_profile"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -367,6 +369,12 @@ class GpuBatch:
         self._check(self.lib.prgpu_adjoint_info(self.h, ctypes.byref(st), ctypes.byref(mm), ctypes.byref(ov)),
                     "prgpu_adjoint_info")
         return {"steps": st.value, "replay_mismatches": mm.value, "tape_overflows": ov.value}
+
+    def adjoint_profile(self) -> dict:
+        f, r, v = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.prgpu_adjoint_profile(self.h, ctypes.byref(f), ctypes.byref(r), ctypes.byref(v)),
+                    "prgpu_adjoint_profile")
+        return {"forward_ms": f.value, "record_ms": r.value, "reverse_ms": v.value}
 
     def adjoint_end(self):
         self._check(self.lib.prgpu_adjoint_end(self.h), "prgpu_adjoint_end")
