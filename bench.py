@@ -403,6 +403,9 @@ def run_ours(args, rank, world_size, local, dist):
     out["gpu_launches"] = launches_per_step(batch) * args.steps
     if args.workload == "batched" and not args.no_adjoint:
         out["adjoint"] = adjoint_bench(local)
+    if args.workload == "chains256" and not args.no_adjoint:
+        batch.close()
+        out["adjoint"] = adjoint_window_bench(worlds, conf, local, args.settle)
     print(json.dumps(out), flush=True)
 
 
@@ -427,6 +430,14 @@ def adjoint_bench(device, n_worlds=64, steps=240, every=16):
     fwd.step_n(steps, conf)
     t_fwd = time.perf_counter() - t0
     fwd.close()
+    # a warm-up window on another batch of the same worlds leaves the window's
+    # device memory (checkpoints, tapes, adjoint state) cached for the timed one
+    wu = gpu.GpuBatch(worlds, device=device)
+    wu.adjoint_begin(every)
+    wu.adjoint_forward(steps, conf)
+    wu.adjoint_backward(np.zeros((wu.n_bodies, 3)), None)
+    wu.adjoint_end()
+    wu.close()
     g = gpu.GpuBatch(worlds, device=device)
     t0 = time.perf_counter()
     g.adjoint_begin(every)
@@ -446,14 +457,70 @@ def adjoint_bench(device, n_worlds=64, steps=240, every=16):
     prof = g.adjoint_profile()
     g.adjoint_end()
     g.close()
+    back_ms = prof["record_ms"] + prof["reverse_ms"]
     return {"metric": "adjoint grad body-steps/s", "value": n_dyn * steps / t_adj, "unit": "body-steps/s",
-            "cost_vs_forward": t_adj / t_fwd, "forward_ms": t_fwd * 1e3, "adjoint_ms": t_adj * 1e3,
+            # the gradient's own cost (recomputing each segment with its tape, then the
+            # reverse pass) and the whole differentiated run (plus the checkpointed
+            # forward pass that gives the loss), both over the plain forward steps
+            "cost_vs_forward": back_ms / (t_fwd * 1e3), "total_vs_forward": t_adj / t_fwd,
+            "forward_ms": t_fwd * 1e3, "adjoint_ms": t_adj * 1e3,
             "workload": f"{n_worlds} worlds x (disk + 32 boxes + ground), seed 2, {steps} steps, "
                         f"checkpoint every {every}, loss |mean box centre - target|^2",
             "loss": loss, "grad_norm": float(np.linalg.norm(grads["vel"])),
             "replay_mismatches": info["replay_mismatches"], "tape_overflows": info["tape_overflows"],
             "phases_ms": prof,
-            "dtype": "f32 forward, f64 local derivatives", "timing": "host clock around synchronous calls"}
+            "dtype": "f32 forward, f32 local derivatives", "timing": "host clock around synchronous calls"}
+
+
+def adjoint_window_bench(worlds, conf, device, settle, window=64, every=8):
+    """StepAdjoint over a window of the chains workload (revolute joints
+    included): loss = sum over worlds of the mean x of the chains' last links,
+    a window of 64 steps with checkpoints every 8.  Two batches of the same
+    worlds advance in lockstep (the step is deterministic): one times the plain
+    forward steps of the window, the other differentiates the same window."""
+    from playrho_gb300 import gpu
+
+    n_dyn = sum(int((w.body_type == 2).sum()) for w in worlds)
+    adj = gpu.GpuBatch(worlds, device=device)
+    plain = gpu.GpuBatch(worlds, device=device)
+    for b in (adj, plain):
+        b.step_n(settle, conf)
+    # warm-up window (the plain twin steps along): leaves the window's device
+    # memory cached for the timed one
+    adj.adjoint_begin(every)
+    adj.adjoint_forward(window, conf)
+    adj.adjoint_backward(np.zeros((adj.n_bodies, 3)), None)
+    adj.adjoint_end()
+    plain.step_n(window, conf)
+    t0 = time.perf_counter()
+    plain.step_n(window, conf)
+    t_fwd = time.perf_counter() - t0
+    plain.close()
+    t0 = time.perf_counter()
+    adj.adjoint_begin(every)
+    adj.adjoint_forward(window, conf)
+    ybar = np.zeros((adj.n_bodies, 3))
+    for k, w in enumerate(worlds):
+        jb = np.asarray(w.joint_bodies).reshape(-1, 2)
+        tips = sorted(set(jb[:, 1].tolist()) - set(jb[:, 0].tolist()))
+        ybar[int(adj.body_base[k]) + np.asarray(tips, dtype=np.int64), 0] = 1.0 / max(1, len(tips))
+    grads = adj.adjoint_backward(ybar, None)
+    t_adj = time.perf_counter() - t0
+    info = adj.adjoint_info()
+    prof = adj.adjoint_profile()
+    adj.adjoint_end()
+    adj.adjoint_trim()
+    adj.close()
+    back_ms = prof["record_ms"] + prof["reverse_ms"]
+    return {"metric": "adjoint grad body-steps/s", "value": n_dyn * window / t_adj, "unit": "body-steps/s",
+            "cost_vs_forward": back_ms / (t_fwd * 1e3), "total_vs_forward": t_adj / t_fwd,
+            "forward_ms": t_fwd * 1e3, "adjoint_ms": t_adj * 1e3,
+            "workload": f"{len(worlds)} chain worlds (revolute joints) after {settle + window} steps, window "
+                        f"{window} steps, checkpoint every {every}, loss = mean x of the chains' last links",
+            "grad_norm": float(np.linalg.norm(grads["vel"])),
+            "replay_mismatches": info["replay_mismatches"], "tape_overflows": info["tape_overflows"],
+            "phases_ms": prof, "dtype": "f32 forward, f32 local derivatives",
+            "timing": "host clock around synchronous calls"}
 
 
 def nvtx_ranges():

@@ -179,7 +179,8 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
  * counterpart.  The derivative is that of the step with its discrete decisions
  * frozen as the forward pass took them (contact set, clamps, block-solver cases,
  * island early exits, sleep) and each manifold's local geometry held constant
- * within a step.  Batches with joints are rejected (PRGPU_EINVAL).
+ * within a step.  Revolute joints take part through their point rows; joints with
+ * a limit or a motor are rejected (PRGPU_EINVAL).
  *   prgpu_adjoint_begin     opens a window; the state is checkpointed every
  *                           checkpoint_every steps (device copies of the whole batch)
  *   prgpu_adjoint_forward   n steps with one StepConf, as prgpu_step_n
@@ -195,7 +196,9 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
  *   prgpu_adjoint_info      steps in the window, recorded steps whose constraint
  *                           set-up the differentiable restatement did not reproduce
  *                           bit for bit (0 expected), local tapes that overflowed
- *   prgpu_adjoint_end       closes the window and frees its memory
+ *   prgpu_adjoint_end       closes the window; its device memory stays cached
+ *                           for the next window of the same sizes
+ *   prgpu_adjoint_trim      frees the cached memory of closed windows
  * Host calls that change bodies (prgpu_upload_body_states) inside a window are
  * not recorded and make the gradients meaningless. */
 int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every);
@@ -206,6 +209,7 @@ int prgpu_adjoint_tangent(prgpu_world* w, const double* dpos3_start, const doubl
                           double* dpos3_end, double* dvel3_end);
 int prgpu_adjoint_info(prgpu_world* w, int* steps, uint32_t* replay_mismatches, uint32_t* tape_overflows);
 int prgpu_adjoint_end(prgpu_world* w);
+int prgpu_adjoint_trim(void);
 /* Host time (ms) of the window's forward steps and of the last backward pass's
  * recording (segments re-run from their checkpoints) and reverse kernels. */
 int prgpu_adjoint_profile(prgpu_world* w, double* forward_ms, double* record_ms, double* reverse_ms);

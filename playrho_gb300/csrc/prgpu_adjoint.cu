@@ -2,27 +2,29 @@
 // steps, and the FP64 forward-mode tangent of the same window.
 //
 // A recorded step (d.tape set) runs the ordinary solver kernels, which also
-// write what each contact step starts from (prgpu_solver.cu sweep_*), the body
-// state at the start of the solve, each world's sweep layout, the impulse
+// write what each constraint step starts from (prgpu_solver.cu sweep_*), the
+// body state at the start of the solve, each world's sweep layout, the impulse
 // sources of the post-solve contact update and the slots created
-// (prgpu_tape.cuh).  From that record, one warp per world:
+// (prgpu_tape.cuh).  From that record the step is walked backwards, turning
+// adjoints of its outputs into adjoints of its inputs (body positions and
+// velocities, stored contact and joint impulses, shape friction):
 //
-//  * k_adj_world walks the step backwards -- sleep, impulse store, the position
-//    iterations colour by colour in reverse, position integration, the velocity
-//    iterations in reverse, warm start, the constraint set-up and the velocity
-//    integration -- turning adjoints of the step's outputs into adjoints of its
-//    inputs (body positions and velocities, stored contact impulses, shape
-//    friction).  The vector-Jacobian products of the iterated pieces, the
-//    velocity and position solves, are written out (solve_velocity_vjp,
-//    solve_position_vjp); the others, run once per contact and step, come from a
-//    per-thread tape of partial derivatives in shared memory (prgpu_diff.cuh).
-//  * k_tan_world walks it forwards with FP64 tangents (Tan), the tangent kernel
-//    a dot-product test checks the adjoint against.
+//  * k_adj_transfer, k_adj_prep: the post-solve contact update, sleep and the
+//    impulse store, backwards; the constraints' geometry values;
+//  * k_adj_sweeps, one block per world: the position iterations colour by
+//    colour in reverse, position integration, the velocity iterations in
+//    reverse (a block barrier separates two colours);
+//  * k_adj_local, every constraint at once: warm start and constraint set-up;
+//  * k_adj_bodies, every body: the velocity integration at the step's start.
 //
-// Worlds are independent, so a warp barrier separates two colours.  Both passes
-// take the forward's branches as recorded (contact set, clamps, block cases,
-// island early exits, sleep), and the manifold's local geometry as constant
-// within a step; joints are not part of the differentiated step.
+// Every local vector-Jacobian product is written out by hand (prgpu_diff.cuh,
+// *_vjp), in float.  k_tan_world walks the same record forwards with FP64
+// tangents (Tan) from the templated restatement of each piece: the tangent
+// kernel the dot-product test checks the adjoint against.
+//
+// Both passes take the forward's branches as recorded (contact set, clamps,
+// block cases, island early exits, sleep), and each manifold's local geometry
+// as constant within a step.  Revolute joints enter through their point rows.
 #include <algorithm>
 
 #include "prgpu_kernels.cuh"
@@ -30,9 +32,7 @@
 
 namespace prgpu {
 
-using diff::AD;
 using diff::Tan;
-using diff::Tape;
 
 // ---- recording --------------------------------------------------------------------
 __global__ void k_tape_body_start(DW d) {
@@ -65,28 +65,6 @@ void launch_tape_constraints(const DW& d, const Launch& L, cudaStream_t s) {
 }
 
 // ---- helpers ------------------------------------------------------------------------
-__device__ __forceinline__ AD leaf(Tape& tp, float v) { return AD{v, tp.push(-1, 0.f, -1, 0.f), &tp}; }
-__device__ __forceinline__ void seed(Tape& tp, const AD& x, float g) {
-    if (x.i >= 0 && g != 0.f) tp.grad(x.i) += g;
-}
-__device__ __forceinline__ float gadj(const Tape& tp, int i) { return tp.grad(i); }
-
-__device__ diff::Geom<AD> geom_leaves(Tape& tp, const float* gv) {
-    diff::Geom<AD> g;
-    g.n = {leaf(tp, gv[0]), leaf(tp, gv[1])};
-    for (int j = 0; j < 2; ++j) {
-        g.rA[j] = {leaf(tp, gv[2 + 4 * j]), leaf(tp, gv[3 + 4 * j])};
-        g.rB[j] = {leaf(tp, gv[4 + 4 * j]), leaf(tp, gv[5 + 4 * j])};
-    }
-    g.nm[0] = leaf(tp, gv[10]); g.tm[0] = leaf(tp, gv[11]); g.nm[1] = leaf(tp, gv[12]); g.tm[1] = leaf(tp, gv[13]);
-    g.vb[0] = leaf(tp, gv[14]); g.vb[1] = leaf(tp, gv[15]);
-    g.k00 = leaf(tp, gv[16]); g.k11 = leaf(tp, gv[17]); g.k01 = leaf(tp, gv[18]);
-    g.m00 = leaf(tp, gv[19]); g.m11 = leaf(tp, gv[20]); g.m01 = leaf(tp, gv[21]);
-    g.mu = leaf(tp, gv[22]);
-    g.cnt = __float_as_int(gv[23]);
-    return g;
-}
-
 // One colour of world w's recorded sweeps, forwards or backwards, by one warp;
 // the serial colour (the leftovers) runs on lane 0 in sweep order.
 template <class F>
@@ -103,6 +81,66 @@ __device__ __forceinline__ void world_pass(uint32_t base, const uint32_t* off, i
         for (uint32_t t = lo + lane; t < hi; t += 32u) f(t);
     }
     __syncwarp();
+}
+
+// One colour of world w's recorded sweeps, backwards, by a block; the serial
+// colour (the leftovers) runs on thread 0 in reverse sweep order.
+template <class F>
+__device__ __forceinline__ void block_pass(uint32_t base, const uint32_t* off, int col, F&& f) {
+    const uint32_t lo = base + off[col], hi = base + off[col + 1];
+    if (lo == hi) return;
+    if (col == kSerialColour) {
+        if (threadIdx.x == 0)
+            for (uint32_t t = hi; t-- > lo;) f(t);
+    } else {
+        for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) f(t);
+    }
+    __syncthreads();
+}
+
+// Recorded constraints of the step: the worlds' segments of sweep order are
+// contiguous, so they are the positions [0, T).
+__device__ __forceinline__ uint32_t recorded_constraints(const DW& d, const StepTape* tp) {
+    const uint32_t w = d.n_worlds - 1u;
+    return tp->wseg[2 * w] + tp->wseg[2 * w + 1];
+}
+
+// ---- joints ---------------------------------------------------------------------------
+__device__ void adj_joint_position(const DW& d, const StepTape* tp, const AdjState& a, uint32_t t, uint32_t j, int it) {
+    const float4* r = tp->pos + 2 * ((size_t)it * tp->kcap + t);
+    if (r[0].w == 0.f) return;  // island already within tolerance
+    const uint32_t A = d.j_bodies[2 * j], B = d.j_bodies[2 * j + 1];
+    const diff::JointK k = joint_k(d, j);
+    const float p[6] = {r[0].x, r[0].y, r[0].z, r[1].x, r[1].y, r[1].z};
+    float yb[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, pb[6];
+    if (k.writableA) { const float4 g = a.pbar[A]; yb[0] = g.x; yb[1] = g.y; yb[2] = g.z; }
+    if (k.writableB) { const float4 g = a.pbar[B]; yb[3] = g.x; yb[4] = g.y; yb[5] = g.z; }
+    diff::joint_position_vjp(k, p, yb, pb);
+    if (k.writableA) a.pbar[A] = make_float4(pb[0], pb[1], pb[2], 0.f);
+    if (k.writableB) a.pbar[B] = make_float4(pb[3], pb[4], pb[5], 0.f);
+}
+
+__device__ void adj_joint_velocity(const DW& d, const StepTape* tp, const AdjState& a, uint32_t t, uint32_t j, int it) {
+    const float4* r = tp->vel + 3 * ((size_t)it * tp->kcap + t);
+    const uint32_t A = d.j_bodies[2 * j], B = d.j_bodies[2 * j + 1];
+    const diff::JointK k = joint_k(d, j);
+    const float* gv = a.gval + (size_t)t * kGeomWords;
+    diff::JGeom<float> g;
+    g.rA = {gv[0], gv[1]}; g.rB = {gv[2], gv[3]};
+    g.exx = gv[4]; g.eyx = gv[5]; g.eyy = gv[6];
+    const diff::Pair3<float> v{r[0].x, r[0].y, r[0].z, r[1].x, r[1].y, r[1].z};
+    float vbA[3] = {0.f, 0.f, 0.f}, vbB[3] = {0.f, 0.f, 0.f};
+    if (k.writableA) { const float4 q = a.vbar[A]; vbA[0] = q.x; vbA[1] = q.y; vbA[2] = q.z; }
+    if (k.writableB) { const float4 q = a.vbar[B]; vbB[0] = q.x; vbB[1] = q.y; vbB[2] = q.z; }
+    const float4 l = a.lbar[t];
+    float ib[2] = {l.x, l.y};
+    float gb[diff::kJointGeomWords] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    diff::joint_velocity_vjp(k, g, v, vbA, vbB, ib, gb);
+    if (k.writableA) a.vbar[A] = make_float4(vbA[0], vbA[1], vbA[2], 0.f);
+    if (k.writableB) a.vbar[B] = make_float4(vbB[0], vbB[1], vbB[2], 0.f);
+    a.lbar[t] = make_float4(ib[0], ib[1], 0.f, 0.f);
+    float* gbar = a.gbar + (size_t)t * kGeomWords;
+    for (int q = 0; q < diff::kJointGeomWords; ++q) gbar[q] += gb[q];
 }
 
 // ---- adjoint ------------------------------------------------------------------------
@@ -124,26 +162,11 @@ __global__ void k_adj_transfer(DW d, const StepTape* tp, AdjState a, uint32_t n_
     }
 }
 
-__global__ void __launch_bounds__(32) k_adj_world(DW d, const StepTape* tp, AdjState a) {
-    extern __shared__ float4 s_tapes[];  // the warp's 32 tapes
-    Tape tap;
-    tap.init(s_tapes, threadIdx.x);
-    const DConf& c = *d.conf;
-    const float h = c.deltaTime;
-    const uint32_t w = blockIdx.x, lane = threadIdx.x;
-    const uint32_t b0 = d.w_body_off[w], b1 = d.w_body_off[w + 1];
-    const uint32_t base = tp->wseg[2 * w], n = tp->wseg[2 * w + 1];
-    // the world's colour table, and the highest parallel colour in use
-    __shared__ uint32_t off[kColStride];
-    for (uint32_t q = lane; q < (uint32_t)kColStride; q += 32u) off[q] = tp->wcol[(size_t)w * kColStride + q];
-    __syncwarp();
-    int top = 0;
-    for (int q = 0; q < kMaxColours; ++q)
-        if (off[q + 1] > off[q]) top = q + 1;
-    // colours in reverse sweep order: the serial one, then top-1 .. 0
-    auto prev_col = [&](int col) { return col == kSerialColour ? top - 1 : col - 1; };
-    // sleep zeroed these velocities; the stored impulses were the final ones
-    for (uint32_t b = b0 + lane; b < b1; b += 32u) {
+// The step's end, backwards: sleep zeroed the slept bodies' velocities; the
+// stored impulses were the iterations' final ones.  Also the constraints'
+// geometry values, which the sweeps' products need.
+__global__ void k_adj_prep(DW d, const StepTape* tp, AdjState a) {
+    GRID_LOOP(b, d.n_bodies) {
         if (tp->slept[b]) a.vbar[b] = make_float4(0.f, 0.f, 0.f, 0.f);
         a.vibar[b] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (tp->flags[b] & BF_SOLVED) {
@@ -154,24 +177,53 @@ __global__ void __launch_bounds__(32) k_adj_world(DW d, const StepTape* tp, AdjS
             a.vi[b] = tp->v0[b];
         }
     }
-    for (uint32_t t = base + lane; t < base + n; t += 32u) {
+    const uint32_t T = recorded_constraints(d, tp);
+    GRID_LOOP(t, T) {
         const uint32_t slot = tp->t_id[t];
         float* gb = a.gbar + (size_t)t * kGeomWords;
         for (int q = 0; q < kGeomWords; ++q) gb[q] = 0.f;
-        if (slot & 0x80000000u) continue;
+        if (slot & 0x80000000u) {  // joint: its stored impulse and its geometry
+            const uint32_t j = slot & 0x7fffffffu;
+            a.lbar[t] = a.jbar[j];
+            a.jbar[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+            const diff::JGeom<float> g =
+                diff::joint_geom_t(joint_k(d, j), tp->p0[d.j_bodies[2 * j]].z, tp->p0[d.j_bodies[2 * j + 1]].z);
+            diff::pack_jgeom(g, a.gval + (size_t)t * kGeomWords);
+            continue;
+        }
         a.lbar[t] = a.mbar[slot];
         a.mbar[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
         const PC& pc = tp->pc[t];
         const diff::Geom<float> g = replay_geom(d, tp, t, contact_k(d, pc, tp->cinfo[t]), tp->cinfo[t].z);
         pack_geom(g, a.gval + (size_t)t * kGeomWords);
     }
-    __syncwarp();
+}
+
+// The iterated part of world w's solve, backwards, by one block: the position
+// iterations colour by colour in reverse, position integration, then the
+// velocity iterations in reverse.  A block barrier separates two colours.
+__global__ void __launch_bounds__(kAdjSweepMaxThreads) k_adj_sweeps(DW d, const StepTape* tp, AdjState a) {
+    const DConf& c = *d.conf;
+    const float h = c.deltaTime;
+    const uint32_t w = blockIdx.x;
+    const uint32_t b0 = d.w_body_off[w], b1 = d.w_body_off[w + 1];
+    const uint32_t base = tp->wseg[2 * w], n = tp->wseg[2 * w + 1];
+    // the world's colour table, and the highest parallel colour in use
+    __shared__ uint32_t off[kColStride];
+    for (uint32_t q = threadIdx.x; q < (uint32_t)kColStride; q += blockDim.x)
+        off[q] = tp->wcol[(size_t)w * kColStride + q];
+    __syncthreads();
+    int top = 0;
+    for (int q = 0; q < kMaxColours; ++q)
+        if (off[q + 1] > off[q]) top = q + 1;
+    // colours in reverse sweep order: the serial one, then top-1 .. 0
+    auto prev_col = [&](int col) { return col == kSerialColour ? top - 1 : col - 1; };
     if (n) {
-        // position iterations, last first, colours in reverse
         for (int it = tp->ip - 1; it >= 0; --it) {
             for (int col = kSerialColour; col >= 0; col = prev_col(col)) {
-                world_pass(base, off, col, true, lane, [&](uint32_t t) {
-                    if (tp->t_id[t] & 0x80000000u) return;
+                block_pass(base, off, col, [&](uint32_t t) {
+                    const uint32_t id = tp->t_id[t];
+                    if (id & 0x80000000u) { adj_joint_position(d, tp, a, t, id & 0x7fffffffu, it); return; }
                     const float4* r = tp->pos + 2 * ((size_t)it * tp->kcap + t);
                     if (r[0].w == 0.f) return;  // island already within tolerance
                     const PC& pc = tp->pc[t];
@@ -190,20 +242,20 @@ __global__ void __launch_bounds__(32) k_adj_world(DW d, const StepTape* tp, AdjS
         }
     }
     // position integration p1 = p0 + h v
-    for (uint32_t b = b0 + lane; b < b1; b += 32u) {
+    for (uint32_t b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
         if (!(tp->flags[b] & BF_SOLVED)) continue;
         const float4 pb = a.pbar[b];
         float4 vb = a.vbar[b];
         vb.x += h * pb.x; vb.y += h * pb.y; vb.z += h * pb.z;
         a.vbar[b] = vb;
     }
-    __syncwarp();
+    __syncthreads();
     if (n) {
-        // velocity iterations, last first, colours in reverse
         for (int it = tp->iv - 1; it >= 0; --it) {
             for (int col = kSerialColour; col >= 0; col = prev_col(col)) {
-                world_pass(base, off, col, true, lane, [&](uint32_t t) {
-                    if (tp->t_id[t] & 0x80000000u) return;
+                block_pass(base, off, col, [&](uint32_t t) {
+                    const uint32_t id = tp->t_id[t];
+                    if (id & 0x80000000u) { adj_joint_velocity(d, tp, a, t, id & 0x7fffffffu, it); return; }
                     const float4* r = tp->vel + 3 * ((size_t)it * tp->kcap + t);
                     const PC& pc = tp->pc[t];
                     const diff::ContactK k = contact_k(d, pc, tp->cinfo[t]);
@@ -233,99 +285,94 @@ __global__ void __launch_bounds__(32) k_adj_world(DW d, const StepTape* tp, AdjS
                 });
             }
         }
-        // warm start
-        for (int col = kSerialColour; col >= 0; col = prev_col(col)) {
-            world_pass(base, off, col, true, lane, [&](uint32_t t) {
-                const uint32_t slot = tp->t_id[t];
-                if (slot & 0x80000000u) return;
-                const PC& pc = tp->pc[t];
-                float4 li = a.lbar[t];  // adjoint of the impulses the first iteration started from
-                if (c.doWarmStart) {
-                    const float4* r = tp->warm + 2 * (size_t)t;
-                    const diff::ContactK k = contact_k(d, pc, tp->cinfo[t]);
-                    const float4 i0 = tp->imp0[t];
-                    tap.reset();
-                    diff::Pair3<AD> v{leaf(tap, r[0].x), leaf(tap, r[0].y), leaf(tap, r[0].z),
-                                      leaf(tap, r[1].x), leaf(tap, r[1].y), leaf(tap, r[1].z)};
-                    const diff::Imp<AD> im{leaf(tap, i0.x), leaf(tap, i0.y), leaf(tap, i0.z), leaf(tap, i0.w)};
-                    const diff::Geom<AD> g = geom_leaves(tap, a.gval + (size_t)t * kGeomWords);
-                    diff::warm_start_t(k, g, v, im);
-                    const float4 ga = a.vbar[pc.bA], gb = a.vbar[pc.bB];
-                    if (k.writableA) { seed(tap, v.ax, ga.x); seed(tap, v.ay, ga.y); seed(tap, v.az, ga.z); }
-                    if (k.writableB) { seed(tap, v.bx, gb.x); seed(tap, v.by, gb.y); seed(tap, v.bz, gb.z); }
-                    tap.backward();
-                    if (tap.overflow) atomicAdd(a.err, 1u);
-                    if (k.writableA) a.vbar[pc.bA] = make_float4(gadj(tap, 0), gadj(tap, 1), gadj(tap, 2), 0.f);
-                    if (k.writableB) a.vbar[pc.bB] = make_float4(gadj(tap, 3), gadj(tap, 4), gadj(tap, 5), 0.f);
-                    li.x += gadj(tap, 6); li.y += gadj(tap, 7); li.z += gadj(tap, 8); li.w += gadj(tap, 9);
-                    float* gbar = a.gbar + (size_t)t * kGeomWords;
-                    for (int q = 0; q < kGeomWords - 1; ++q) gbar[q] += gadj(tap, 10 + q);
-                }
-                // VelocityConstraint's impulses are the stored ones times dtRatio
-                float4 m = a.mbar[slot];
-                m.x += li.x * c.dtRatio; m.y += li.y * c.dtRatio; m.z += li.z * c.dtRatio; m.w += li.w * c.dtRatio;
-                a.mbar[slot] = m;
-            });
+    }
+}
+
+// Warm start and constraint set-up, backwards, for every recorded constraint at
+// once: the warm start's velocity change does not depend on the velocities, and
+// the set-up reads the state at the start of the solve, so neither pass has an
+// order.
+__global__ void k_adj_local(DW d, const StepTape* tp, AdjState a) {
+    const DConf& c = *d.conf;
+    const uint32_t T = recorded_constraints(d, tp);
+    GRID_LOOP(t, T) {
+        const uint32_t slot = tp->t_id[t];
+        float* gbar = a.gbar + (size_t)t * kGeomWords;
+        const float* gv = a.gval + (size_t)t * kGeomWords;
+        if (slot & 0x80000000u) {  // joint
+            const uint32_t j = slot & 0x7fffffffu;
+            const uint32_t A = d.j_bodies[2 * j], B = d.j_bodies[2 * j + 1];
+            const diff::JointK k = joint_k(d, j);
+            if (c.doWarmStart) {  // else the impulses restart from zero; velocities untouched
+                diff::JGeom<float> g;
+                g.rA = {gv[0], gv[1]}; g.rB = {gv[2], gv[3]};
+                g.exx = gv[4]; g.eyx = gv[5]; g.eyy = gv[6];
+                const float4 i0 = tp->imp0[t], l = a.lbar[t];
+                float vbA[3] = {0.f, 0.f, 0.f}, vbB[3] = {0.f, 0.f, 0.f};
+                if (k.writableA) { const float4 q = a.vbar[A]; vbA[0] = q.x; vbA[1] = q.y; vbA[2] = q.z; }
+                if (k.writableB) { const float4 q = a.vbar[B]; vbB[0] = q.x; vbB[1] = q.y; vbB[2] = q.z; }
+                const float lb[2] = {l.x, l.y};
+                float ib[2];
+                diff::joint_warm_vjp(k, g, c.dtRatio, i0.x, i0.y, vbA, vbB, lb, ib, gbar);
+                a.jbar[j] = make_float4(ib[0], ib[1], 0.f, 0.f);
+            }
+            float aAb, aBb;
+            diff::joint_geom_vjp(k, tp->p0[A].z, tp->p0[B].z, gbar, &aAb, &aBb);
+            if (k.writableA) atomicAdd(&a.pbar[A].z, aAb);
+            if (k.writableB) atomicAdd(&a.pbar[B].z, aBb);
+            continue;
         }
+        const PC& pc = tp->pc[t];
+        const float4 ci = tp->cinfo[t];
+        const diff::ContactK k = contact_k(d, pc, ci);
+        float4 li = a.lbar[t];  // adjoint of the impulses the first iteration started from
+        if (c.doWarmStart) {
+            const float4 i0 = tp->imp0[t];
+            const diff::Imp<float> im{i0.x, i0.y, i0.z, i0.w};
+            float vbA[3] = {0.f, 0.f, 0.f}, vbB[3] = {0.f, 0.f, 0.f};
+            if (k.writableA) { const float4 q = a.vbar[pc.bA]; vbA[0] = q.x; vbA[1] = q.y; vbA[2] = q.z; }
+            if (k.writableB) { const float4 q = a.vbar[pc.bB]; vbB[0] = q.x; vbB[1] = q.y; vbB[2] = q.z; }
+            float ib[4] = {0.f, 0.f, 0.f, 0.f};
+            diff::warm_start_vjp(k, unpack_geom(gv), im, vbA, vbB, ib, gbar);
+            li.x += ib[0]; li.y += ib[1]; li.z += ib[2]; li.w += ib[3];
+        }
+        // VelocityConstraint's impulses are the stored ones times dtRatio
+        float4 m = a.mbar[slot];
+        m.x += li.x * c.dtRatio; m.y += li.y * c.dtRatio; m.z += li.z * c.dtRatio; m.w += li.w * c.dtRatio;
+        a.mbar[slot] = m;
         // constraint set-up: geometry from the positions and velocities at the
         // start of the solve and the contact's friction
-        for (uint32_t t = base + lane; t < base + n; t += 32u) {
-            const uint32_t slot = tp->t_id[t];
-            if (slot & 0x80000000u) continue;
-            const PC& pc = tp->pc[t];
-            const float4 ci = tp->cinfo[t];
-            const diff::ContactK k = contact_k(d, pc, ci);
-            const float4 pa = tp->p0[pc.bA], pb = tp->p0[pc.bB], va = a.vi[pc.bA], vb = a.vi[pc.bB];
-            tap.reset();
-            const diff::Pair3<AD> p{leaf(tap, pa.x), leaf(tap, pa.y), leaf(tap, pa.z), leaf(tap, pb.x), leaf(tap, pb.y),
-                                    leaf(tap, pb.z)};
-            const diff::Pair3<AD> v{leaf(tap, va.x), leaf(tap, va.y), leaf(tap, va.z), leaf(tap, vb.x), leaf(tap, vb.y),
-                                    leaf(tap, vb.z)};
-            const AD mu = leaf(tap, ci.z);
-            const diff::Geom<AD> g = diff::build_geom(k, p, v, mu, c);
-            const float* gb = a.gbar + (size_t)t * kGeomWords;
-            seed(tap, g.n.x, gb[0]); seed(tap, g.n.y, gb[1]);
-            for (int j = 0; j < 2; ++j) {
-                seed(tap, g.rA[j].x, gb[2 + 4 * j]); seed(tap, g.rA[j].y, gb[3 + 4 * j]);
-                seed(tap, g.rB[j].x, gb[4 + 4 * j]); seed(tap, g.rB[j].y, gb[5 + 4 * j]);
-            }
-            seed(tap, g.nm[0], gb[10]); seed(tap, g.tm[0], gb[11]); seed(tap, g.nm[1], gb[12]); seed(tap, g.tm[1], gb[13]);
-            seed(tap, g.vb[0], gb[14]); seed(tap, g.vb[1], gb[15]);
-            seed(tap, g.k00, gb[16]); seed(tap, g.k11, gb[17]); seed(tap, g.k01, gb[18]);
-            seed(tap, g.m00, gb[19]); seed(tap, g.m11, gb[20]); seed(tap, g.m01, gb[21]);
-            seed(tap, g.mu, gb[22]);
-            tap.backward();
-            if (tap.overflow) atomicAdd(a.err, 1u);
-            atomicAdd(&a.pbar[pc.bA].x, gadj(tap, 0)); atomicAdd(&a.pbar[pc.bA].y, gadj(tap, 1));
-            atomicAdd(&a.pbar[pc.bA].z, gadj(tap, 2));
-            atomicAdd(&a.pbar[pc.bB].x, gadj(tap, 3)); atomicAdd(&a.pbar[pc.bB].y, gadj(tap, 4));
-            atomicAdd(&a.pbar[pc.bB].z, gadj(tap, 5));
-            atomicAdd(&a.vibar[pc.bA].x, gadj(tap, 6)); atomicAdd(&a.vibar[pc.bA].y, gadj(tap, 7));
-            atomicAdd(&a.vibar[pc.bA].z, gadj(tap, 8));
-            atomicAdd(&a.vibar[pc.bB].x, gadj(tap, 9)); atomicAdd(&a.vibar[pc.bB].y, gadj(tap, 10));
-            atomicAdd(&a.vibar[pc.bB].z, gadj(tap, 11));
-            // MixFriction: sqrt(fA fB)
-            const float mub = gadj(tap, 12);
-            if (mub != 0.f && ci.z > 0.f) {
-                const uint2 pr = tp->prox[t];
-                const float fa = d.s_mat[pr.x].x, fb = d.s_mat[pr.y].x;
-                atomicAdd(&a.fbar[pr.x], mub * fb / (2.0f * ci.z));
-                atomicAdd(&a.fbar[pr.y], mub * fa / (2.0f * ci.z));
-            }
+        const float4 pa = tp->p0[pc.bA], pb = tp->p0[pc.bB], va = a.vi[pc.bA], vb = a.vi[pc.bB];
+        const diff::Pair3<float> p{pa.x, pa.y, pa.z, pb.x, pb.y, pb.z};
+        const diff::Pair3<float> v{va.x, va.y, va.z, vb.x, vb.y, vb.z};
+        float pbar[6], vbar[6], mub;
+        diff::build_geom_vjp(k, p, v, ci.z, c, gbar, pbar, vbar, &mub);
+        atomicAdd(&a.pbar[pc.bA].x, pbar[0]); atomicAdd(&a.pbar[pc.bA].y, pbar[1]); atomicAdd(&a.pbar[pc.bA].z, pbar[2]);
+        atomicAdd(&a.pbar[pc.bB].x, pbar[3]); atomicAdd(&a.pbar[pc.bB].y, pbar[4]); atomicAdd(&a.pbar[pc.bB].z, pbar[5]);
+        atomicAdd(&a.vibar[pc.bA].x, vbar[0]); atomicAdd(&a.vibar[pc.bA].y, vbar[1]);
+        atomicAdd(&a.vibar[pc.bA].z, vbar[2]);
+        atomicAdd(&a.vibar[pc.bB].x, vbar[3]); atomicAdd(&a.vibar[pc.bB].y, vbar[4]);
+        atomicAdd(&a.vibar[pc.bB].z, vbar[5]);
+        // MixFriction: sqrt(fA fB)
+        if (mub != 0.f && ci.z > 0.f) {
+            const uint2 pr = tp->prox[t];
+            const float fa = d.s_mat[pr.x].x, fb = d.s_mat[pr.y].x;
+            atomicAdd(&a.fbar[pr.x], mub * fb / (2.0f * ci.z));
+            atomicAdd(&a.fbar[pr.y], mub * fa / (2.0f * ci.z));
         }
-        __syncwarp();
     }
-    // velocity at the start of the solve from the velocity the step started with
-    for (uint32_t b = b0 + lane; b < b1; b += 32u) {
+}
+
+// velocity at the start of the solve from the velocity the step started with
+__global__ void k_adj_bodies(DW d, const StepTape* tp, AdjState a) {
+    GRID_LOOP(b, d.n_bodies) {
         if (!(tp->flags[b] & BF_SOLVED)) continue;
         const float4 v0 = tp->v0[b];
         const float4 g1 = a.vbar[b], g2 = a.vibar[b];
-        tap.reset();
-        AD vx = leaf(tap, v0.x), vy = leaf(tap, v0.y), vw = leaf(tap, v0.z);
-        start_velocity(d, b, vx, vy, vw);
-        seed(tap, vx, g1.x + g2.x); seed(tap, vy, g1.y + g2.y); seed(tap, vw, g1.z + g2.z);
-        tap.backward();
-        a.vbar[b] = make_float4(gadj(tap, 0), gadj(tap, 1), gadj(tap, 2), 0.f);
+        float bar[3] = {g1.x + g2.x, g1.y + g2.y, g1.z + g2.z};
+        diff::integrate_velocity_vjp(is_accelerable(d.b_flags[b]), d.b_acc[b], d.b_damp[b], *d.conf, v0.x, v0.y, v0.z,
+                                     bar);
+        a.vbar[b] = make_float4(bar[0], bar[1], bar[2], 0.f);
     }
 }
 
@@ -343,6 +390,14 @@ __device__ diff::Geom<Tan> geom_tan(const float* gv, const double* gd) {
     g.k00 = T(16); g.k11 = T(17); g.k01 = T(18); g.m00 = T(19); g.m11 = T(20); g.m01 = T(21);
     g.mu = T(22);
     g.cnt = __float_as_int(gv[23]);
+    return g;
+}
+
+__device__ __forceinline__ diff::JGeom<Tan> jgeom_tan(const float* gv, const double* gd) {
+    diff::JGeom<Tan> g;
+    g.rA = {Tan{gv[0], gd[0]}, Tan{gv[1], gd[1]}};
+    g.rB = {Tan{gv[2], gd[2]}, Tan{gv[3], gd[3]}};
+    g.exx = Tan{gv[4], gd[4]}; g.eyx = Tan{gv[5], gd[5]}; g.eyy = Tan{gv[6], gd[6]};
     return g;
 }
 
@@ -384,7 +439,21 @@ __global__ void __launch_bounds__(32) k_tan_world(DW d, const StepTape* tp, TanS
     // constraint geometry and its tangent; the iterations start from the stored impulses
     for (uint32_t t = base + lane; t < base + n; t += 32u) {
         const uint32_t slot = tp->t_id[t];
-        if (slot & 0x80000000u) continue;
+        if (slot & 0x80000000u) {  // joint: geometry from the angles; the stored impulse
+            const uint32_t j = slot & 0x7fffffffu;
+            const uint32_t A = d.j_bodies[2 * j], B = d.j_bodies[2 * j + 1];
+            const diff::JGeom<Tan> g = diff::joint_geom_t(joint_k(d, j), Tan{tp->p0[A].z, s.pdot[3 * (size_t)A + 2]},
+                                                          Tan{tp->p0[B].z, s.pdot[3 * (size_t)B + 2]});
+            diff::pack_jgeom(g, gval + (size_t)t * kGeomWords);
+            double* gd = s.gdot + (size_t)t * kGeomWords;
+            gd[0] = g.rA.x.d; gd[1] = g.rA.y.d; gd[2] = g.rB.x.d; gd[3] = g.rB.y.d;
+            gd[4] = g.exx.d; gd[5] = g.eyx.d; gd[6] = g.eyy.d;
+            double* l = s.ldot + 4 * (size_t)t;
+            l[0] = c.doWarmStart ? s.jdot[2 * (size_t)j] : 0.0;
+            l[1] = c.doWarmStart ? s.jdot[2 * (size_t)j + 1] : 0.0;
+            l[2] = l[3] = 0.0;
+            continue;
+        }
         const PC& pc = tp->pc[t];
         const float4 ci = tp->cinfo[t];
         const diff::ContactK k = contact_k(d, pc, ci);
@@ -432,14 +501,33 @@ __global__ void __launch_bounds__(32) k_tan_world(DW d, const StepTape* tp, TanS
         const double* b3 = basev + 3 * (size_t)B;
         return diff::Pair3<Tan>{{ra.x, a3[0]}, {ra.y, a3[1]}, {ra.z, a3[2]}, {rb.x, b3[0]}, {rb.y, b3[1]}, {rb.z, b3[2]}};
     };
-    auto store_pair = [&](const diff::ContactK& k, uint32_t A, uint32_t B, const diff::Pair3<Tan>& v, double* basev) {
+    auto store_pair = [&](const auto& k, uint32_t A, uint32_t B, const diff::Pair3<Tan>& v, double* basev) {
         if (k.writableA) { double* a3 = basev + 3 * (size_t)A; a3[0] = v.ax.d; a3[1] = v.ay.d; a3[2] = v.az.d; }
         if (k.writableB) { double* b3 = basev + 3 * (size_t)B; b3[0] = v.bx.d; b3[1] = v.by.d; b3[2] = v.bz.d; }
+    };
+    auto joint_step = [&](uint32_t t, uint32_t j, const float4* r, bool position, bool warm) {
+        const uint32_t A = d.j_bodies[2 * j], B = d.j_bodies[2 * j + 1];
+        const diff::JointK k = joint_k(d, j);
+        double* basev = position ? s.pdot : s.vdot;
+        diff::Pair3<Tan> v = body_pair(A, B, r[0], r[1], basev);
+        if (position) {
+            diff::joint_position_t(k, v);
+        } else {
+            double* l = s.ldot + 4 * (size_t)t;
+            const float4 i = warm ? tp->imp0[t] : r[2];
+            Tan ix{i.x, l[0]}, iy{i.y, l[1]};
+            const diff::JGeom<Tan> g = jgeom_tan(gval + (size_t)t * kGeomWords, s.gdot + (size_t)t * kGeomWords);
+            if (warm) diff::joint_warm_t(k, g, c.dtRatio, v, ix, iy);
+            else diff::joint_velocity_t(k, g, v, ix, iy);
+            l[0] = ix.d; l[1] = iy.d;
+        }
+        store_pair(k, A, B, v, basev);
     };
     if (n && c.doWarmStart) {
         for (int col = 0; col <= kSerialColour; ++col) {
             world_pass(base, off, col, false, lane, [&](uint32_t t) {
-                if (tp->t_id[t] & 0x80000000u) return;
+                const uint32_t id = tp->t_id[t];
+                if (id & 0x80000000u) { joint_step(t, id & 0x7fffffffu, tp->warm + 2 * (size_t)t, false, true); return; }
                 const PC& pc = tp->pc[t];
                 const diff::ContactK k = contact_k(d, pc, tp->cinfo[t]);
                 const float4* r = tp->warm + 2 * (size_t)t;
@@ -456,10 +544,11 @@ __global__ void __launch_bounds__(32) k_tan_world(DW d, const StepTape* tp, TanS
         for (int it = 0; it < tp->iv; ++it) {
             for (int col = 0; col <= kSerialColour; ++col) {
                 world_pass(base, off, col, false, lane, [&](uint32_t t) {
-                    if (tp->t_id[t] & 0x80000000u) return;
+                    const float4* r = tp->vel + 3 * ((size_t)it * tp->kcap + t);
+                    const uint32_t id = tp->t_id[t];
+                    if (id & 0x80000000u) { joint_step(t, id & 0x7fffffffu, r, false, false); return; }
                     const PC& pc = tp->pc[t];
                     const diff::ContactK k = contact_k(d, pc, tp->cinfo[t]);
-                    const float4* r = tp->vel + 3 * ((size_t)it * tp->kcap + t);
                     diff::Pair3<Tan> v = body_pair(pc.bA, pc.bB, r[0], r[1], s.vdot);
                     double* l = s.ldot + 4 * (size_t)t;
                     diff::Imp<Tan> im{{r[2].x, l[0]}, {r[2].y, l[1]}, {r[2].z, l[2]}, {r[2].w, l[3]}};
@@ -482,9 +571,10 @@ __global__ void __launch_bounds__(32) k_tan_world(DW d, const StepTape* tp, TanS
         for (int it = 0; it < tp->ip; ++it) {
             for (int col = 0; col <= kSerialColour; ++col) {
                 world_pass(base, off, col, false, lane, [&](uint32_t t) {
-                    if (tp->t_id[t] & 0x80000000u) return;
                     const float4* r = tp->pos + 2 * ((size_t)it * tp->kcap + t);
                     if (r[0].w == 0.f) return;
+                    const uint32_t id = tp->t_id[t];
+                    if (id & 0x80000000u) { joint_step(t, id & 0x7fffffffu, r, true, false); return; }
                     const PC& pc = tp->pc[t];
                     const diff::ContactK k = contact_k(d, pc, tp->cinfo[t]);
                     diff::Pair3<Tan> p = body_pair(pc.bA, pc.bB, r[0], r[1], s.pdot);
@@ -497,8 +587,13 @@ __global__ void __launch_bounds__(32) k_tan_world(DW d, const StepTape* tp, TanS
     // stored impulses; slept bodies stop
     for (uint32_t t = base + lane; t < base + n; t += 32u) {
         const uint32_t slot = tp->t_id[t];
-        if (slot & 0x80000000u) continue;
         const double* l = s.ldot + 4 * (size_t)t;
+        if (slot & 0x80000000u) {
+            const uint32_t j = slot & 0x7fffffffu;
+            s.jdot[2 * (size_t)j] = l[0];
+            s.jdot[2 * (size_t)j + 1] = l[1];
+            continue;
+        }
         double* m = s.mdot + 4 * (size_t)slot;
         for (int q = 0; q < 4; ++q) m[q] = l[q];
     }
@@ -510,18 +605,20 @@ __global__ void __launch_bounds__(32) k_tan_world(DW d, const StepTape* tp, TanS
 }
 
 // ---- launchers ------------------------------------------------------------------------
-int adj_setup() {
-    const int bytes = 32 * diff::kTapeBytes;
-    if (cudaFuncSetAttribute(k_adj_world, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return 0;
-    int a = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_adj_world, 32, bytes);
-    return a;
+uint32_t adj_parallel_grid() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return 0;
+    return (uint32_t)sms * 8u;
 }
 
 cudaError_t launch_adj_step(const DW& d, const StepTape* tp, const AdjState& a, uint32_t n_slots, cudaStream_t s) {
-    k_adj_transfer<<<256, 256, 0, s>>>(d, tp, a, n_slots);
+    k_adj_transfer<<<a.grid, 256, 0, s>>>(d, tp, a, n_slots);
     cudaMemcpyAsync(a.mbar, a.mtmp, sizeof(float4) * n_slots, cudaMemcpyDeviceToDevice, s);
-    k_adj_world<<<d.n_worlds, 32, 32 * diff::kTapeBytes, s>>>(d, tp, a);
+    k_adj_prep<<<a.grid, 256, 0, s>>>(d, tp, a);
+    k_adj_sweeps<<<d.n_worlds, a.sweep_threads, 0, s>>>(d, tp, a);
+    k_adj_local<<<a.grid, 256, 0, s>>>(d, tp, a);
+    k_adj_bodies<<<a.grid, 256, 0, s>>>(d, tp, a);
     return cudaGetLastError();
 }
 

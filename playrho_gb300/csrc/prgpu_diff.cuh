@@ -5,10 +5,10 @@
 // operation order of the forward kernels (prgpu_solver.cu), so that
 //   T = float  recomputes the forward's values bit for bit (a replay check),
 //   T = Tan    carries an FP64 tangent along the forward's float values
-//              (forward-mode: the tangent kernel),
-//   T = AD     records a per-thread tape of local partial derivatives that a
-//              reverse sweep turns into a vector-Jacobian product (reverse-mode:
-//              the adjoint kernels).
+//              (forward-mode: the tangent kernel).
+// The reverse mode is written out by hand for each piece (*_vjp, in float): the
+// adjoint kernels' local vector-Jacobian products, which the dot-product test
+// checks against the tangent.
 // Branches (clamps, block-solver cases, the position solver's point order,
 // conditioning of K, vb's restitution threshold) are taken on the float values,
 // so they are those of the forward pass: the derivative is that of the forward
@@ -22,60 +22,6 @@ namespace prgpu {
 namespace diff {
 
 // ---- scalar types ---------------------------------------------------------------
-constexpr int kTapeNodes = 320;
-constexpr int kTapeLanes = 32;               // tapes of one warp, interleaved
-constexpr int kTapeBytes = kTapeNodes * 16;  // shared memory of one thread's tape
-
-// Per-thread tape in shared memory: node k = a local result with up to two
-// parents and the partial derivative with respect to each.  The 32 tapes of a
-// warp are interleaved word by word (node k of lane l at word k*32 + l of each
-// array), so lanes that push or walk their tapes in step hit 32 different banks.
-struct Tape {
-    float* pa;
-    float* pb;
-    float* adj;
-    uint32_t* ix;  // parents: low half a, high half b (int16, -1 = none)
-    int n;
-    bool overflow;
-    // carves lane's tape out of the warp's 32 * kTapeBytes of shared memory
-    __device__ void init(void* mem, uint32_t lane) {
-        float* f = static_cast<float*>(mem);
-        pa = f + lane;
-        pb = pa + kTapeNodes * kTapeLanes;
-        adj = pb + kTapeNodes * kTapeLanes;
-        ix = reinterpret_cast<uint32_t*>(adj + kTapeNodes * kTapeLanes);
-        n = 0; overflow = false;
-    }
-    __device__ void reset() { n = 0; overflow = false; }
-    __device__ int push(int a, float da, int b, float db) {
-        if (n >= kTapeNodes) { overflow = true; return -1; }
-        const int o = n * kTapeLanes;
-        ix[o] = (uint32_t)(uint16_t)(int16_t)a | ((uint32_t)(uint16_t)(int16_t)b << 16);
-        pa[o] = da; pb[o] = db; adj[o] = 0.f;
-        return n++;
-    }
-    __device__ float& grad(int k) { return adj[k * kTapeLanes]; }
-    __device__ float grad(int k) const { return adj[k * kTapeLanes]; }
-    // adjoints of every node from those seeded on the outputs
-    __device__ void backward() {
-        for (int k = n - 1; k >= 0; --k) {
-            const int o = k * kTapeLanes;
-            const float g = adj[o];
-            if (g == 0.f) continue;
-            const uint32_t w = ix[o];
-            const int a = (int16_t)(w & 0xffffu), b = (int16_t)(w >> 16);
-            if (a >= 0) adj[a * kTapeLanes] += pa[o] * g;
-            if (b >= 0) adj[b * kTapeLanes] += pb[o] * g;
-        }
-    }
-};
-
-struct AD {
-    float v;
-    int i;     // tape node, -1 for a constant
-    Tape* t;
-};
-
 // value (float) with an FP64 tangent
 struct Tan {
     float v;
@@ -83,47 +29,11 @@ struct Tan {
 };
 
 __device__ __forceinline__ float val(float x) { return x; }
-__device__ __forceinline__ float val(const AD& x) { return x.v; }
 __device__ __forceinline__ float val(const Tan& x) { return x.v; }
 
 template <class T> __device__ __forceinline__ T C(float c);
 template <> __device__ __forceinline__ float C<float>(float c) { return c; }
-template <> __device__ __forceinline__ AD C<AD>(float c) { return AD{c, -1, nullptr}; }
 template <> __device__ __forceinline__ Tan C<Tan>(float c) { return Tan{c, 0.0}; }
-
-__device__ __forceinline__ AD rec(float v, const AD& a, float da, const AD& b, float db) {
-    Tape* t = a.t ? a.t : b.t;
-    if (!t || (a.i < 0 && b.i < 0)) return AD{v, -1, t};
-    return AD{v, t->push(a.i, da, b.i, db), t};
-}
-__device__ __forceinline__ AD rec1(float v, const AD& a, float da) {
-    if (!a.t || a.i < 0) return AD{v, -1, a.t};
-    return AD{v, a.t->push(a.i, da, -1, 0.f), a.t};
-}
-
-// partial derivatives in float: the tape stores them in float
-__device__ __forceinline__ AD operator+(const AD& a, const AD& b) { return rec(a.v + b.v, a, 1.f, b, 1.f); }
-__device__ __forceinline__ AD operator-(const AD& a, const AD& b) { return rec(a.v - b.v, a, 1.f, b, -1.f); }
-__device__ __forceinline__ AD operator*(const AD& a, const AD& b) { return rec(a.v * b.v, a, b.v, b, a.v); }
-__device__ __forceinline__ AD operator/(const AD& a, const AD& b) {
-    const float q = a.v / b.v, r = 1.f / b.v;
-    return rec(q, a, r, b, -q * r);
-}
-__device__ __forceinline__ AD operator-(const AD& a) { return rec1(-a.v, a, -1.f); }
-__device__ __forceinline__ AD sqrt_(const AD& a) {
-    const float r = sqrtf(a.v);
-    return rec1(r, a, 0.5f / r);
-}
-__device__ __forceinline__ AD hypot_(const AD& a, const AD& b) {
-    const float h = hypotf(a.v, b.v);
-    return rec(h, a, a.v / h, b, b.v / h);
-}
-__device__ __forceinline__ void sincos_(const AD& a, AD& s, AD& c) {
-    float sv, cv;
-    sincosf(a.v, &sv, &cv);
-    s = rec1(sv, a, cv);
-    c = rec1(cv, a, -sv);
-}
 
 __device__ __forceinline__ Tan operator+(const Tan& a, const Tan& b) { return Tan{a.v + b.v, a.d + b.d}; }
 __device__ __forceinline__ Tan operator-(const Tan& a, const Tan& b) { return Tan{a.v - b.v, a.d - b.d}; }
@@ -963,6 +873,402 @@ __device__ inline void solve_position_vjp(const ContactK& k, const DConf& c, con
     }
 }
 
+// ---- revolute joints (RevoluteJointConf.cpp:127-431), point rows only ---------------
+// The differentiated step takes joints without motor and limit: the angular
+// impulse then stays zero and only the 2-row point constraint acts.
+struct JointK {
+    float4 mA, mB;  // invM invI lcx lcy of both bodies
+    float4 an;      // local anchors on A (x, y) and B (z, w)
+    uint32_t writableA, writableB;
+};
+
+// InitVelocity's geometry (RevoluteJointConf.cpp:127-186): world anchors relative
+// to the centres and the upper 2x2 of the mass matrix.
+template <class T>
+struct JGeom {
+    V<T> rA, rB;
+    T exx, eyx, eyy;
+};
+constexpr int kJointGeomWords = 7;
+
+template <class T>
+__device__ JGeom<T> joint_geom_t(const JointK& k, const T& angA, const T& angB) {
+    T sA, cA, sB, cB;
+    sincos_(angA, sA, cA);
+    sincos_(angB, sB, cB);
+    JGeom<T> g;
+    g.rA = rotatet(cv<T>(k.an.x - k.mA.z, k.an.y - k.mA.w), V<T>{cA, sA});
+    g.rB = rotatet(cv<T>(k.an.z - k.mB.z, k.an.w - k.mB.w), V<T>{cB, sB});
+    const float iMA = k.mA.x, iIA = k.mA.y, iMB = k.mB.x, iIB = k.mB.y;
+    g.exx = iMA + ((g.rA.y * g.rA.y) * iIA) + iMB + ((g.rB.y * g.rB.y) * iIB);
+    g.eyx = (-g.rA.y * g.rA.x * iIA) + (-g.rB.y * g.rB.x * iIB);
+    g.eyy = iMA + ((g.rA.x * g.rA.x) * iIA) + iMB + ((g.rB.x * g.rB.x) * iIB);
+    return g;
+}
+
+// Warm start of InitVelocity: the stored impulse (ix, iy) scaled by dtRatio is
+// applied to both bodies and becomes the impulse the iterations start from.
+template <class T>
+__device__ void joint_warm_t(const JointK& k, const JGeom<T>& g, float dtRatio, Pair3<T>& v, T& ix, T& iy) {
+    ix = ix * dtRatio;
+    iy = iy * dtRatio;
+    const V<T> P{ix, iy};
+    const T LA = crosst(g.rA, P), LB = crosst(g.rB, P);
+    const float iMA = k.mA.x, iIA = k.mA.y, iMB = k.mB.x, iIB = k.mB.y;
+    v.ax = v.ax - P.x * iMA; v.ay = v.ay - P.y * iMA; v.az = v.az - iIA * LA;
+    v.bx = v.bx + P.x * iMB; v.by = v.by + P.y * iMB; v.bz = v.bz + iIB * LB;
+}
+
+// SolveVelocity's point rows (RevoluteJointConf.cpp:228-331): Solve22 on the
+// upper 2x2 of the mass matrix.
+template <class T>
+__device__ void joint_velocity_t(const JointK& k, const JGeom<T>& g, Pair3<T>& v, T& ix, T& iy) {
+    const V<T> vb{v.bx + (-g.rB.y) * v.bz, v.by + g.rB.x * v.bz};
+    const V<T> va{v.ax + (-g.rA.y) * v.az, v.ay + g.rA.x * v.az};
+    const V<T> vd = sub(vb, va);
+    const T cp = g.exx * g.eyy - g.eyx * g.eyx;
+    const T det = (val(cp) != 0.f) ? (1.0f / cp) : cp;
+    const V<T> bb = neg(vd);
+    const V<T> P{det * (g.eyy * bb.x - g.eyx * bb.y), det * (g.exx * bb.y - g.eyx * bb.x)};
+    ix = ix + P.x;
+    iy = iy + P.y;
+    const T LA = crosst(g.rA, P), LB = crosst(g.rB, P);
+    const float iMA = k.mA.x, iIA = k.mA.y, iMB = k.mB.x, iIB = k.mB.y;
+    v.ax = v.ax - P.x * iMA; v.ay = v.ay - P.y * iMA; v.az = v.az - iIA * LA;
+    v.bx = v.bx + P.x * iMB; v.by = v.by + P.y * iMB; v.bz = v.bz + iIB * LB;
+}
+
+// SolvePosition's point rows (RevoluteJointConf.cpp:333-431); updates the
+// positions of writable bodies.
+template <class T>
+__device__ void joint_position_t(const JointK& k, Pair3<T>& p) {
+    const JGeom<T> g = joint_geom_t(k, p.az, p.bz);
+    const V<T> Cp = sub(add(V<T>{p.bx, p.by}, g.rB), add(V<T>{p.ax, p.ay}, g.rA));
+    const float iMA = k.mA.x, iIA = k.mA.y, iMB = k.mB.x, iIB = k.mB.y;
+    const T exx = iMA + (iIA * (g.rA.y * g.rA.y)) + iMB + (iIB * (g.rB.y * g.rB.y));
+    const T exy = (-iIA * g.rA.x * g.rA.y) + (-iIB * g.rB.x * g.rB.y);
+    const T eyy = iMA + (iIA * (g.rA.x * g.rA.x)) + iMB + (iIB * (g.rB.x * g.rB.x));
+    const T cp = crosst(V<T>{exx, exy}, V<T>{exy, eyy});
+    V<T> x{C<T>(0.f), C<T>(0.f)};
+    if (!almost_zero(val(cp))) {
+        const T inv = 1.0f / cp;
+        x = V<T>{(eyy * Cp.x - exy * Cp.y) * inv, (exx * Cp.y - exy * Cp.x) * inv};
+    }
+    const V<T> P = neg(x);
+    const T nax = p.ax - P.x * iMA, nay = p.ay - P.y * iMA, naz = p.az - iIA * crosst(g.rA, P);
+    const T nbx = p.bx + P.x * iMB, nby = p.by + P.y * iMB, nbz = p.bz + iIB * crosst(g.rB, P);
+    if (k.writableA) { p.ax = nax; p.ay = nay; p.az = naz; }
+    if (k.writableB) { p.bx = nbx; p.by = nby; p.bz = nbz; }
+}
+
+// Reverse of joint_velocity_t in float.  vbA/vbB/ib on entry: adjoints of the
+// outputs (vbA/vbB zero for bodies the solve does not store); on exit: adjoints
+// of the inputs.  gb[0..6] (rA rB exx eyx eyy) accumulates.
+__device__ inline void joint_velocity_vjp(const JointK& k, const JGeom<float>& g, const Pair3<float>& v, float* vbA,
+                                          float* vbB, float* ib, float* gb) {
+    const float iMA = k.mA.x, iIA = k.mA.y, iMB = k.mB.x, iIB = k.mB.y;
+    const float vbx = v.bx + (-g.rB.y) * v.bz, vby = v.by + g.rB.x * v.bz;
+    const float vax = v.ax + (-g.rA.y) * v.az, vay = v.ay + g.rA.x * v.az;
+    const float bbx = -(vbx - vax), bby = -(vby - vay);
+    const float cp = g.exx * g.eyy - g.eyx * g.eyx;
+    const float det = (cp != 0.f) ? (1.0f / cp) : cp;
+    const float ux = g.eyy * bbx - g.eyx * bby, uy = g.exx * bby - g.eyx * bbx;
+    const float Px = det * ux, Py = det * uy;
+    float Pbx = -iMA * vbA[0] + iMB * vbB[0] + ib[0];
+    float Pby = -iMA * vbA[1] + iMB * vbB[1] + ib[1];
+    const float LAb = -iIA * vbA[2], LBb = iIB * vbB[2];
+    float rAbx = LAb * Py, rAby = -LAb * Px, rBbx = LBb * Py, rBby = -LBb * Px;
+    Pbx += -LAb * g.rA.y - LBb * g.rB.y;
+    Pby += LAb * g.rA.x + LBb * g.rB.x;
+    const float ubx = det * Pbx, uby = det * Pby;
+    const float detb = Pbx * ux + Pby * uy;
+    const float cpb = (cp != 0.f) ? -detb * det * det : detb;
+    gb[4] += cpb * g.eyy + uby * bby;
+    gb[6] += cpb * g.exx + ubx * bbx;
+    gb[5] += -2.f * cpb * g.eyx - ubx * bby - uby * bbx;
+    const float bbbx = g.eyy * ubx - g.eyx * uby, bbby = g.exx * uby - g.eyx * ubx;
+    // vd = vb - va = -bb
+    const float vbbx = -bbbx, vbby = -bbby;
+    vbB[0] += vbbx; vbB[1] += vbby; vbB[2] += -vbbx * g.rB.y + vbby * g.rB.x;
+    rBby += -vbbx * v.bz; rBbx += vbby * v.bz;
+    vbA[0] -= vbbx; vbA[1] -= vbby; vbA[2] -= -vbbx * g.rA.y + vbby * g.rA.x;
+    rAby -= -vbbx * v.az; rAbx -= vbby * v.az;
+    gb[0] += rAbx; gb[1] += rAby; gb[2] += rBbx; gb[3] += rBby;
+}
+
+// Reverse of joint_position_t in float: yb = adjoints of the output positions
+// (zero for a body the solve does not store); pb = adjoints of the inputs.
+__device__ inline void joint_position_vjp(const JointK& k, const float* p, const float* yb, float* pb) {
+    const float iMA = k.mA.x, iIA = k.mA.y, iMB = k.mB.x, iIB = k.mB.y;
+    for (int i = 0; i < 6; ++i) pb[i] = yb[i];
+    float sA, cA, sB, cB;
+    sincosf(p[2], &sA, &cA);
+    sincosf(p[5], &sB, &cB);
+    const JGeom<float> g = joint_geom_t(k, p[2], p[5]);
+    const float lAx = k.an.x - k.mA.z, lAy = k.an.y - k.mA.w, lBx = k.an.z - k.mB.z, lBy = k.an.w - k.mB.w;
+    const float Cx = (p[3] + g.rB.x) - (p[0] + g.rA.x), Cy = (p[4] + g.rB.y) - (p[1] + g.rA.y);
+    const float exx = iMA + (iIA * (g.rA.y * g.rA.y)) + iMB + (iIB * (g.rB.y * g.rB.y));
+    const float exy = (-iIA * g.rA.x * g.rA.y) + (-iIB * g.rB.x * g.rB.y);
+    const float eyy = iMA + (iIA * (g.rA.x * g.rA.x)) + iMB + (iIB * (g.rB.x * g.rB.x));
+    const float cp = exx * eyy - exy * exy;
+    const bool solved = !almost_zero(cp);
+    const float inv = solved ? 1.0f / cp : 0.f;
+    const float ux = eyy * Cx - exy * Cy, uy = exx * Cy - exy * Cx;
+    const float Px = solved ? -(ux * inv) : 0.f, Py = solved ? -(uy * inv) : 0.f;
+    float Pbx = -iMA * yb[0] + iMB * yb[3], Pby = -iMA * yb[1] + iMB * yb[4];
+    const float cAb = -iIA * yb[2], cBb = iIB * yb[5];
+    float rAbx = cAb * Py, rAby = -cAb * Px, rBbx = cBb * Py, rBby = -cBb * Px;
+    Pbx += -cAb * g.rA.y - cBb * g.rB.y;
+    Pby += cAb * g.rA.x + cBb * g.rB.x;
+    float Cbx = 0.f, Cby = 0.f, exxb = 0.f, exyb = 0.f, eyyb = 0.f;
+    if (solved) {
+        const float xbx = -Pbx, xby = -Pby;
+        const float invb = xbx * ux + xby * uy;
+        const float ubx = inv * xbx, uby = inv * xby;
+        Cbx = eyy * ubx - exy * uby;
+        Cby = exx * uby - exy * ubx;
+        eyyb += ubx * Cx; exxb += uby * Cy; exyb += -ubx * Cy - uby * Cx;
+        const float cpb = -invb * inv * inv;
+        exxb += cpb * eyy; eyyb += cpb * exx; exyb += -2.f * cpb * exy;
+    }
+    rAby += 2.f * iIA * g.rA.y * exxb; rBby += 2.f * iIB * g.rB.y * exxb;
+    rAbx += -iIA * g.rA.y * exyb; rAby += -iIA * g.rA.x * exyb;
+    rBbx += -iIB * g.rB.y * exyb; rBby += -iIB * g.rB.x * exyb;
+    rAbx += 2.f * iIA * g.rA.x * eyyb; rBbx += 2.f * iIB * g.rB.x * eyyb;
+    pb[3] += Cbx; pb[4] += Cby; rBbx += Cbx; rBby += Cby;
+    pb[0] -= Cbx; pb[1] -= Cby; rAbx -= Cbx; rAby -= Cby;
+    float qAx = 0.f, qAy = 0.f, qBx = 0.f, qBy = 0.f;
+    rot_qbar(lAx, lAy, rAbx, rAby, qAx, qAy);
+    rot_qbar(lBx, lBy, rBbx, rBby, qBx, qBy);
+    pb[2] += qAx * -sA + qAy * cA;
+    pb[5] += qBx * -sB + qBy * cB;
+}
+
+// ---- hand-written reverse of the once-per-step pieces -------------------------------
+// Geometry adjoints in the packed order of pack_geom: n rA0 rB0 rA1 rB1 nm0 tm0 nm1
+// tm1 vb0 vb1 k00 k11 k01 m00 m11 m01 mu.
+enum : int { GB_N = 0, GB_RA0 = 2, GB_RB0 = 4, GB_RA1 = 6, GB_RB1 = 8, GB_NM = 10, GB_VB = 14, GB_K00 = 16,
+             GB_K11 = 17, GB_K01 = 18, GB_M00 = 19, GB_M11 = 20, GB_M01 = 21, GB_MU = 22 };
+
+__device__ __forceinline__ int gb_ra(int j) { return j ? GB_RA1 : GB_RA0; }
+__device__ __forceinline__ int gb_rb(int j) { return j ? GB_RB1 : GB_RB0; }
+
+// Reverse of warm_start_t: the velocity change does not depend on the
+// velocities, whose adjoints vbA/vbB (zero for bodies not stored) pass through;
+// adds the impulses' adjoints to ib and the geometry's to gb (packed order).
+__device__ inline void warm_start_vjp(const ContactK& k, const Geom<float>& g, const Imp<float>& im, const float* vbA,
+                                      const float* vbB, float* ib, float* gb) {
+    const float nx = g.n.x, ny = g.n.y, tx = ny, ty = -nx;
+    float nbx = 0.f, nby = 0.f, tbx = 0.f, tby = 0.f;
+    for (int j = 0; j < g.cnt; ++j) {
+        const float ni = j ? im.ni1 : im.ni0, ti = j ? im.ti1 : im.ti0;
+        const float Px = nx * ni + tx * ti, Py = ny * ni + ty * ti;
+        float Pbx = -k.mA.x * vbA[0] + k.mB.x * vbB[0];
+        float Pby = -k.mA.x * vbA[1] + k.mB.x * vbB[1];
+        const float LAb = -k.mA.y * vbA[2], LBb = k.mB.y * vbB[2];
+        const V<float> rA = g.rA[j], rB = g.rB[j];
+        gb[gb_ra(j)] += LAb * Py; gb[gb_ra(j) + 1] += -LAb * Px;
+        gb[gb_rb(j)] += LBb * Py; gb[gb_rb(j) + 1] += -LBb * Px;
+        Pbx += -LAb * rA.y - LBb * rB.y;
+        Pby += LAb * rA.x + LBb * rB.x;
+        ib[2 * j] += Pbx * nx + Pby * ny;
+        ib[2 * j + 1] += Pbx * tx + Pby * ty;
+        nbx += Pbx * ni; nby += Pby * ni;
+        tbx += Pbx * ti; tby += Pby * ti;
+    }
+    // t = (n.y, -n.x)
+    gb[GB_N] += nbx - tby;
+    gb[GB_N + 1] += nby + tbx;
+}
+
+// Reverse of build_geom in float: from the geometry's adjoints gb (packed order)
+// to the adjoints of the positions (pb) and velocities (vb) it was built from
+// (x y angle of A then B) and of the friction (*mub).
+__device__ inline void build_geom_vjp(const ContactK& k, const Pair3<float>& p, const Pair3<float>& v, float mu,
+                                      const DConf& c, const float* gb, float* pb, float* vb, float* mub) {
+    for (int i = 0; i < 6; ++i) pb[i] = vb[i] = 0.f;
+    *mub = gb[GB_MU];
+    // forward values
+    float sA, cA, sB, cB;
+    sincosf(p.az, &sA, &cA);
+    sincosf(p.bz, &sB, &cB);
+    const XfT<float> xfA = get_xft(p.ax, p.ay, p.az, k.mA.z, k.mA.w);
+    const XfT<float> xfB = get_xft(p.bx, p.by, p.bz, k.mB.z, k.mB.w);
+    const Geom<float> g = build_geom(k, p, v, mu, c);
+    const V<float> ln = cv<float>(k.lnx, k.lny), lp = cv<float>(k.lpx, k.lpy);
+    const V<float> plp[2] = {cv<float>(k.p0x, k.p0y), cv<float>(k.p1x, k.p1y)};
+    const float iA = k.mA.y, iB = k.mB.y;
+    const V<float> n = g.n, t = fwdperpt(n);
+    // the points kept (g.cnt of them): rA = world point - centre of A, rB likewise
+    const V<float>* relA = g.rA;
+    const V<float>* relB = g.rB;
+    // reverse
+    float nbx = gb[GB_N], nby = gb[GB_N + 1], tbx = 0.f, tby = 0.f;
+    V<float> rAb[2] = {{0.f, 0.f}, {0.f, 0.f}}, rBb[2] = {{0.f, 0.f}, {0.f, 0.f}};
+    for (int j = 0; j < g.cnt; ++j) {
+        rAb[j] = V<float>{gb[gb_ra(j)], gb[gb_ra(j) + 1]};
+        rBb[j] = V<float>{gb[gb_rb(j)], gb[gb_rb(j) + 1]};
+    }
+    auto cross_bar = [&](const V<float>& r, const V<float>& q, float cb, V<float>& rb, float& qbx, float& qby) {
+        // cross(r, q) = r.x q.y - r.y q.x
+        rb.x += cb * q.y; rb.y -= cb * q.x;
+        qbx -= cb * r.y; qby += cb * r.x;
+    };
+    if (c.doBlocksolve && g.cnt == 2 && !(g.k00 == 0.f && g.k11 == 0.f && g.k01 == 0.f)) {
+        const float rnA0 = crosst(relA[0], n), rnB0 = crosst(relB[0], n);
+        const float rnA1 = crosst(relA[1], n), rnB1 = crosst(relB[1], n);
+        const float kk00 = g.k00, kk11 = g.k11, kk01 = g.k01;
+        float k00b = gb[GB_K00], k11b = gb[GB_K11], k01b = gb[GB_K01];
+        const float cp = crosst(V<float>{kk00, kk01}, V<float>{kk01, kk11});
+        if (!almost_zero(cp)) {
+            const float inv = 1.0f / cp;
+            const float invb = gb[GB_M00] * kk11 - gb[GB_M01] * kk01 + gb[GB_M11] * kk00;
+            k11b += gb[GB_M00] * inv; k01b -= gb[GB_M01] * inv; k00b += gb[GB_M11] * inv;
+            const float cpb = -invb * inv * inv;
+            k00b += cpb * kk11; k11b += cpb * kk00; k01b -= 2.f * cpb * kk01;
+        }
+        const float rnA0b = k00b * 2.f * iA * rnA0 + k01b * iA * rnA1;
+        const float rnA1b = k11b * 2.f * iA * rnA1 + k01b * iA * rnA0;
+        const float rnB0b = k00b * 2.f * iB * rnB0 + k01b * iB * rnB1;
+        const float rnB1b = k11b * 2.f * iB * rnB1 + k01b * iB * rnB0;
+        cross_bar(relA[0], n, rnA0b, rAb[0], nbx, nby);
+        cross_bar(relB[0], n, rnB0b, rBb[0], nbx, nby);
+        cross_bar(relA[1], n, rnA1b, rAb[1], nbx, nby);
+        cross_bar(relB[1], n, rnB1b, rBb[1], nbx, nby);
+    }
+    V<float> wptb[2] = {{0.f, 0.f}, {0.f, 0.f}};
+    for (int j = 0; j < g.cnt; ++j) {
+        const V<float> ra = relA[j], rb = relB[j];
+        // velocity bias
+        const V<float> dv = rel_velt(v.ax, v.ay, v.az, ra, v.bx, v.by, v.bz, rb);
+        const float vn = dott(dv, n);
+        if (vn < -c.velocityThreshold) {
+            const float vnb = -k.restitution * gb[GB_VB + j];
+            const float dvbx = vnb * n.x, dvby = vnb * n.y;
+            nbx += vnb * dv.x; nby += vnb * dv.y;
+            vb[3] += dvbx; vb[4] += dvby; vb[5] += -dvbx * rb.y + dvby * rb.x;
+            rBb[j].x += dvby * v.bz; rBb[j].y -= dvbx * v.bz;
+            vb[0] -= dvbx; vb[1] -= dvby; vb[2] -= -dvbx * ra.y + dvby * ra.x;
+            rAb[j].x -= dvby * v.az; rAb[j].y += dvbx * v.az;
+        }
+        // normal and tangent mass
+        const float nm = g.nm[j], tm = g.tm[j];
+        if (nm != 0.f) {
+            const float valb = -gb[GB_NM + 2 * j] * nm * nm;
+            const float crA = crosst(ra, n), crB = crosst(rb, n);
+            cross_bar(ra, n, valb * 2.f * iA * crA, rAb[j], nbx, nby);
+            cross_bar(rb, n, valb * 2.f * iB * crB, rBb[j], nbx, nby);
+        }
+        if (tm != 0.f) {
+            const float valb = -gb[GB_NM + 2 * j + 1] * tm * tm;
+            const float crA = crosst(ra, t), crB = crosst(rb, t);
+            cross_bar(ra, t, valb * 2.f * iA * crA, rAb[j], tbx, tby);
+            cross_bar(rb, t, valb * 2.f * iB * crB, rBb[j], tbx, tby);
+        }
+    }
+    // relA = wpt - pA, relB = wpt - pB (points that conditioning dropped carry none)
+    for (int j = 0; j < g.cnt; ++j) {
+        wptb[j] = add(rAb[j], rBb[j]);
+        pb[0] -= rAb[j].x; pb[1] -= rAb[j].y;
+        pb[3] -= rBb[j].x; pb[4] -= rBb[j].y;
+    }
+    // t = fwdperp(n) = (n.y, -n.x)
+    nbx += -tby;
+    nby += tbx;
+    // world manifold onto the two transformations
+    float xApx = 0.f, xApy = 0.f, qAx = 0.f, qAy = 0.f, xBpx = 0.f, xBpy = 0.f, qBx = 0.f, qBy = 0.f;
+    if (k.type == M_CIRCLES) {
+        const V<float> a = xformt(lp, xfA), b = xformt(plp[0], xfB);
+        const float dx = b.x - a.x, dy = b.y - a.y;
+        // wpt = (a + n rA + b - n rB) / 2
+        const float hx = 0.5f * wptb[0].x, hy = 0.5f * wptb[0].y;
+        float abx = hx, aby = hy, bbx = hx, bby = hy;
+        nbx += hx * (k.rA - k.rB); nby += hy * (k.rA - k.rB);
+        const float m2 = dx * dx + dy * dy;
+        const float m = is_normal_f(m2) ? sqrtf(m2) : hypotf(dx, dy);
+        if (is_normal_f(m)) {
+            const float dn = nbx * n.x + nby * n.y;
+            const float dbx = (nbx - n.x * dn) / m, dby = (nby - n.y * dn) / m;
+            abx -= dbx; aby -= dby; bbx += dbx; bby += dby;
+        }
+        xApx += abx; xApy += aby; rot_qbar(lp.x, lp.y, abx, aby, qAx, qAy);
+        xBpx += bbx; xBpy += bby; rot_qbar(plp[0].x, plp[0].y, bbx, bby, qBx, qBy);
+    } else if (k.type == M_FACEA || k.type == M_FACEB) {
+        const bool fa = k.type == M_FACEA;
+        // reference side r (the face), incident side i (the clipped points)
+        const V<float> nn = fa ? n : neg(n);
+        float nnbx = fa ? nbx : -nbx, nnby = fa ? nby : -nby;
+        const XfT<float>& xr = fa ? xfA : xfB;
+        const XfT<float>& xi = fa ? xfB : xfA;
+        const V<float> pp = xformt(lp, xr);
+        const float rr = fa ? k.rA : k.rB, ri = fa ? k.rB : k.rA;
+        float ppbx = 0.f, ppby = 0.f, xipx = 0.f, xipy = 0.f, qix = 0.f, qiy = 0.f;
+        for (int i = 0; i < g.cnt; ++i) {
+            const V<float> clip = xformt(plp[i], xi);
+            const float ex = clip.x - pp.x, ey = clip.y - pp.y;
+            const float s = rr - (ex * nn.x + ey * nn.y);
+            // wpt = (clip + nn s + clip - nn ri) / 2
+            const float hx = 0.5f * wptb[i].x, hy = 0.5f * wptb[i].y;
+            float clbx = 2.f * hx, clby = 2.f * hy;
+            nnbx += hx * (s - ri); nnby += hy * (s - ri);
+            const float sb = hx * nn.x + hy * nn.y;
+            // s = rr - dot(clip - pp, nn)
+            clbx -= sb * nn.x; clby -= sb * nn.y;
+            ppbx += sb * nn.x; ppby += sb * nn.y;
+            nnbx -= sb * ex; nnby -= sb * ey;
+            xipx += clbx; xipy += clby; rot_qbar(plp[i].x, plp[i].y, clbx, clby, qix, qiy);
+        }
+        float xrpx = ppbx, xrpy = ppby, qrx = 0.f, qry = 0.f;
+        rot_qbar(lp.x, lp.y, ppbx, ppby, qrx, qry);
+        rot_qbar(ln.x, ln.y, nnbx, nnby, qrx, qry);  // nn = urotate(ln, q of the face's body)
+        if (fa) { xApx = xrpx; xApy = xrpy; qAx = qrx; qAy = qry; xBpx = xipx; xBpy = xipy; qBx = qix; qBy = qiy; }
+        else { xBpx = xrpx; xBpy = xrpy; qBx = qrx; qBy = qry; xApx = xipx; xApy = xipy; qAx = qix; qAy = qiy; }
+    }
+    xf_bar_to_pos(xApx, xApy, qAx, qAy, k.mA.z, k.mA.w, sA, cA, pb);
+    xf_bar_to_pos(xBpx, xBpy, qBx, qBy, k.mB.z, k.mB.w, sB, cB, pb + 3);
+}
+
+// Reverse of joint_warm_t: velocity adjoints pass through; ib gets the stored
+// impulse's adjoint, gb[0..3] (rA rB) accumulates.
+__device__ inline void joint_warm_vjp(const JointK& k, const JGeom<float>& g, float dtRatio, float ix, float iy,
+                                      const float* vbA, const float* vbB, const float* lb, float* ib, float* gb) {
+    const float Px = ix * dtRatio, Py = iy * dtRatio;
+    float Pbx = -k.mA.x * vbA[0] + k.mB.x * vbB[0] + lb[0];
+    float Pby = -k.mA.x * vbA[1] + k.mB.x * vbB[1] + lb[1];
+    const float LAb = -k.mA.y * vbA[2], LBb = k.mB.y * vbB[2];
+    gb[0] += LAb * Py; gb[1] -= LAb * Px; gb[2] += LBb * Py; gb[3] -= LBb * Px;
+    Pbx += -LAb * g.rA.y - LBb * g.rB.y;
+    Pby += LAb * g.rA.x + LBb * g.rB.x;
+    ib[0] = Pbx * dtRatio;
+    ib[1] = Pby * dtRatio;
+}
+
+// Reverse of joint_geom_t: adjoints of the two angles from gb[0..6].
+__device__ inline void joint_geom_vjp(const JointK& k, float angA, float angB, const float* gb, float* aAb, float* aBb) {
+    const JGeom<float> g = joint_geom_t(k, angA, angB);
+    const float iA = k.mA.y, iB = k.mB.y;
+    float rAbx = gb[0], rAby = gb[1], rBbx = gb[2], rBby = gb[3];
+    const float exxb = gb[4], eyxb = gb[5], eyyb = gb[6];
+    rAby += exxb * 2.f * iA * g.rA.y; rBby += exxb * 2.f * iB * g.rB.y;
+    rAbx += -eyxb * iA * g.rA.y; rAby += -eyxb * iA * g.rA.x;
+    rBbx += -eyxb * iB * g.rB.y; rBby += -eyxb * iB * g.rB.x;
+    rAbx += eyyb * 2.f * iA * g.rA.x; rBbx += eyyb * 2.f * iB * g.rB.x;
+    float sA, cA, sB, cB;
+    sincosf(angA, &sA, &cA);
+    sincosf(angB, &sB, &cB);
+    float qAx = 0.f, qAy = 0.f, qBx = 0.f, qBy = 0.f;
+    rot_qbar(k.an.x - k.mA.z, k.an.y - k.mA.w, rAbx, rAby, qAx, qAy);
+    rot_qbar(k.an.z - k.mB.z, k.an.w - k.mB.w, rBbx, rBby, qBx, qBy);
+    *aAb = qAx * -sA + qAy * cA;
+    *aBb = qBx * -sB + qBy * cB;
+}
+
+template <class T>
+__device__ __forceinline__ void pack_jgeom(const JGeom<T>& g, float* out) {
+    out[0] = val(g.rA.x); out[1] = val(g.rA.y); out[2] = val(g.rB.x); out[3] = val(g.rB.y);
+    out[4] = val(g.exx); out[5] = val(g.eyx); out[6] = val(g.eyy);
+}
+
 // Body velocity at the start of the solve (k_body_begin): acceleration,
 // damping, then the translation and rotation caps.
 template <class T>
@@ -991,6 +1297,41 @@ __device__ void integrate_velocity_t(bool accelerable, float4 a, float2 dm, cons
         // |h w| is clamped to maxRotation: the result keeps w's sign only
         const T ratio = C<T>(c.maxRotation / absRot);
         vw = C<T>(val(vw) * val(ratio));
+    }
+}
+
+// Reverse of integrate_velocity_t in float: b holds the adjoints of the output
+// velocity on entry and of the input velocity on exit (the rotation cap holds
+// |h w| at a constant).
+__device__ inline void integrate_velocity_vjp(bool accelerable, float4 a, float2 dm, const DConf& c, float vx, float vy,
+                                              float vw, float* b) {
+    const float h = c.deltaTime;
+    float linv = 1.0f;
+    if (accelerable) {
+        vx = vx + a.x * h;
+        vy = vy + a.y * h;
+        vw = vw + h * a.z;
+        linv = 1.0f / (1.0f + h * dm.x);
+        vx = vx * linv;
+        vy = vy * linv;
+        vw = vw / (1.0f + h * dm.y);
+    }
+    const float tx = vx * h, ty = vy * h;
+    float lsq = 0.f;
+    lsq = lsq + tx * tx;
+    lsq = lsq + ty * ty;
+    if (lsq > c.maxTranslation * c.maxTranslation) {
+        // out = u maxT / |h u|
+        const float ratio = c.maxTranslation / sqrtf(lsq);
+        const float kb = -ratio * h * h / lsq * (b[0] * vx + b[1] * vy);
+        b[0] = ratio * b[0] + kb * vx;
+        b[1] = ratio * b[1] + kb * vy;
+    }
+    if (fabsf(h * vw) > c.maxRotation) b[2] = 0.f;
+    if (accelerable) {
+        b[0] *= linv;
+        b[1] *= linv;
+        b[2] = b[2] / (1.0f + h * dm.y);
     }
 }
 

@@ -49,8 +49,13 @@ struct AdjState {
     float4* mbar;     // [C] d(loss)/d(stored manifold impulses) per slot
     float4* mtmp;     // [C]
     float* fbar;      // [S] d(loss)/d(shape friction)
+    float4* jbar;     // [J] d(loss)/d(stored joint impulse x y)
     uint32_t* err;    // tape overflow count
+    uint32_t grid;           // blocks of the parallel passes
+    uint32_t sweep_threads;  // threads of the per-world sweep block
 };
+
+constexpr uint32_t kAdjSweepMaxThreads = 512;
 
 struct TanState {
     double* pdot;   // [N*3]
@@ -61,10 +66,11 @@ struct TanState {
     double* mdot;   // [C*4]
     double* mtmp;   // [C*4]
     const double* fdot;  // [S] tangent of shape friction
+    double* jdot;   // [J*2] tangent of the stored joint impulses
 };
 
-// sets the shared-memory attribute of the adjoint kernel; returns its blocks per SM
-int adj_setup();
+// blocks of the adjoint's parallel passes on this device (0: no device)
+uint32_t adj_parallel_grid();
 cudaError_t launch_adj_step(const DW& d, const StepTape* tp, const AdjState& a, uint32_t n_slots, cudaStream_t s);
 cudaError_t launch_tan_step(const DW& d, const StepTape* tp, const TanState& t, float* gval, uint32_t n_slots,
                             cudaStream_t s);

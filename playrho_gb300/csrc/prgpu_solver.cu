@@ -977,7 +977,10 @@ template <class BS>
 __device__ __forceinline__ void sweep_warm(const DW& d, const BS& bs, uint32_t t) {
     const uint32_t id = d.t_id[t];
     if (id & kJointBit) {
-        joint_init_velocity(d, bs, id & ~kJointBit);
+        const uint32_t j = id & ~kJointBit;
+        if (d.tape) tape_joint_warm(d, t, j, bs.vel(d.j_bodies[2 * j]), bs.vel(d.j_bodies[2 * j + 1]));
+        joint_init_velocity(d, bs, j);
+        if (d.tape) tape_joint_check(d, j);
     } else if (d.conf->doWarmStart) {
         const VC vc = load_vc(d, t);
         if (d.tape) {
@@ -992,7 +995,15 @@ template <class BS>
 __device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32_t t, int it) {
     const uint32_t id = d.t_id[t];
     if (id & kJointBit) {
-        joint_solve_velocity(d, bs, id & ~kJointBit);
+        const uint32_t j = id & ~kJointBit;
+        if (d.tape) {
+            float4* r = d.tape->vel + 3 * ((size_t)it * d.tape->kcap + t);
+            r[0] = bs.vel(d.j_bodies[2 * j]);
+            r[1] = bs.vel(d.j_bodies[2 * j + 1]);
+            const float4 i = d.j_imp[j];
+            r[2] = make_float4(i.x, i.y, 0.f, 0.f);
+        }
+        joint_solve_velocity(d, bs, j);
     } else {
         VC vc = load_vc(d, t);
         if (d.tape) {
@@ -1012,7 +1023,15 @@ __device__ __forceinline__ void sweep_position(const DW& d, const BS& bs, uint32
     if (id & kJointBit) {
         const uint32_t j = id & ~kJointBit;
         const uint32_t L = joint_island(d, j);
-        if (bs.island_done(L, it)) return;
+        const bool done = bs.island_done(L, it);
+        if (d.tape) {
+            float4* r = d.tape->pos + 2 * ((size_t)it * d.tape->kcap + t);
+            float4 a = bs.pos(d.j_bodies[2 * j]);
+            a.w = done ? 0.f : 1.f;
+            r[0] = a;
+            r[1] = bs.pos(d.j_bodies[2 * j + 1]);
+        }
+        if (done) return;
         if (!joint_solve_position(d, bs, j)) bs.island_joint_fail(L, it);
     } else {
         const PC pc = d.pc[t];

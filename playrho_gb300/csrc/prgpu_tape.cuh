@@ -105,6 +105,40 @@ static __device__ __noinline__ bool tape_constraint(const DW& d, uint32_t t) {
     return same;
 }
 
+// ---- joints (revolute, point rows) ------------------------------------------------
+__device__ __forceinline__ diff::JointK joint_k(const DW& d, uint32_t j) {
+    diff::JointK k;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    k.mA = d.b_mass[a];
+    k.mB = d.b_mass[b];
+    k.an = d.j_anchor[j];
+    k.writableA = is_accelerable(d.b_flags[a]) ? 1u : 0u;
+    k.writableB = is_accelerable(d.b_flags[b]) ? 1u : 0u;
+    return k;
+}
+
+// What a joint's warm start starts from: both velocities and the stored impulse.
+__device__ __forceinline__ void tape_joint_warm(const DW& d, uint32_t t, uint32_t j, float4 vA, float4 vB) {
+    StepTape* tp = d.tape;
+    tp->warm[2 * (size_t)t] = vA;
+    tp->warm[2 * (size_t)t + 1] = vB;
+    const float4 i = d.j_imp[j];
+    tp->imp0[t] = make_float4(i.x, i.y, 0.f, 0.f);
+}
+
+// After the warm start: the geometry the joint stored must be the one the
+// differentiable restatement computes from the recorded positions, bit for bit.
+static __device__ __noinline__ void tape_joint_check(const DW& d, uint32_t j) {
+    StepTape* tp = d.tape;
+    const diff::JointK k = joint_k(d, j);
+    const diff::JGeom<float> g =
+        diff::joint_geom_t(k, tp->p0[d.j_bodies[2 * j]].z, tp->p0[d.j_bodies[2 * j + 1]].z);
+    const float4 r = d.j_r[j], m0 = d.j_m0[j];
+    const bool same = g.rA.x == r.x && g.rA.y == r.y && g.rB.x == r.z && g.rB.y == r.w && g.exx == m0.x &&
+                      g.eyx == m0.y && g.eyy == m0.w;
+    if (!same) atomicAdd(&tp->hdr[kTapeHdrMismatch], 1u);
+}
+
 // The per-world layout of a recorded step: world w's constraints are the sweep
 // positions [wseg[2w], wseg[2w] + wseg[2w+1]) with colour offsets wcol[w*kColStride..].
 __device__ __forceinline__ void tape_world(const DW& d, uint32_t w, uint32_t base, uint32_t n, const uint32_t* col_off,

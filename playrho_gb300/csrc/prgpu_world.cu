@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -24,6 +26,7 @@ struct prgpu_world {
     Launch L{};
     std::vector<void*> allocs;
     std::vector<size_t> alloc_bytes;
+    std::vector<bool> alloc_scratch;  // rewritten every step before it is read: not checkpointed
     cudaGraphExec_t graph = nullptr;
     cudaGraph_t graph_def = nullptr;
     prgpu_step_conf conf{};
@@ -62,13 +65,14 @@ int fail(prgpu_world* w, int code, const char* fmt, ...) {
     } while (0)
 
 template <typename T>
-int dalloc(prgpu_world* w, T** p, size_t n) {
+int dalloc(prgpu_world* w, T** p, size_t n, bool scratch = false) {
     void* q = nullptr;
     const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
     const cudaError_t e = cudaMalloc(&q, bytes);
     if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
     w->allocs.push_back(q);
     w->alloc_bytes.push_back(bytes);
+    w->alloc_scratch.push_back(scratch);
     *p = static_cast<T*>(q);
     return PRGPU_OK;
 }
@@ -693,6 +697,8 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     if (30 + d.world_bits > 64) return bail(PRGPU_ECAPACITY);
     int rc = 0;
 #define AL(ptr, n) do { rc = dalloc(w, &(ptr), (size_t)(n)); if (rc) return bail(rc); } while (0)
+    // per-step scratch: every step writes it before reading it
+#define ALS(ptr, n) do { rc = dalloc(w, &(ptr), (size_t)(n), true); if (rc) return bail(rc); } while (0)
     uint32_t *w_body_off, *w_shape_off;
     AL(w_body_off, W + 1); AL(w_shape_off, W + 1);
     d.w_body_off = w_body_off; d.w_shape_off = w_shape_off;
@@ -703,25 +709,25 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.b_pos1, N); AL(d.b_pos0, N); AL(d.b_vel, N); AL(d.b_xf, N); AL(d.b_mass, N); AL(d.b_acc, N);
     AL(d.b_damp, N); AL(d.b_flags, N); AL(d.b_uat, N); AL(d.b_world, N); AL(d.b_island, N);
     AL(d.b_jnt_off, N + 1); AL(d.b_jnt_other, jother.size()); AL(d.b_jnt_cc, jcc.size());
-    AL(d.isl_awake, N); AL(d.isl_sep, (size_t)N * kMaxPosIters); AL(d.isl_jok, (size_t)N * kMaxPosIters); AL(d.isl_uat, N);
+    AL(d.isl_awake, N); ALS(d.isl_sep, (size_t)N * kMaxPosIters); ALS(d.isl_jok, (size_t)N * kMaxPosIters); AL(d.isl_uat, N);
     AL(d.s_body, S); AL(d.s_meta, S); AL(d.s_voff, S); AL(d.s_radius, S); AL(d.s_mat, S); AL(d.s_filter, S);
     AL(d.s_group, S); AL(d.verts, vtx.size()); AL(d.p_aabb, S); AL(d.p_moved, S); AL(d.moved_list, S);
     AL(d.j_bodies, 2 * J); AL(d.j_anchor, J); AL(d.j_param, J); AL(d.j_maxtorque, J); AL(d.j_flags, J);
     AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_imp, J);
-    AL(d.c_key, C); AL(d.c_slot, C); AL(d.c_key_alt, C); AL(d.c_slot_alt, C); AL(d.free_stack, C);
+    AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
     AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C);
     AL(d.cs_colour, C); AL(d.j_colour, J);
     AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
-    AL(d.n_key, K); AL(d.n_key_alt, K); AL(d.n_val, K); AL(d.n_val_alt, K);
+    ALS(d.n_key, K); ALS(d.n_key_alt, K); ALS(d.n_val, K); ALS(d.n_val_alt, K);
     AL(d.l_key, S); AL(d.l_key_alt, S); AL(d.l_idx, S); AL(d.l_idx_alt, S); AL(d.l_leaf_box, S);
     AL(d.l_node_box, S); AL(d.l_left, S); AL(d.l_right, S); AL(d.l_parent, 2 * (size_t)S); AL(d.l_range, 2 * (size_t)S);
     AL(d.l_visit, S);
-    AL(d.k_list, C + J); AL(d.k_colour, C + J); AL(d.k_tent, C + J); AL(d.k_order, C + J);
-    AL(d.t_id, C + J);
-    AL(d.k_prio, C + J);
-    AL(d.inc_off, N + 1); AL(d.inc_cur, N + 1); AL(d.inc_list, 2 * ((size_t)C + J));
-    AL(d.vc0, C); AL(d.vc1, C); AL(d.pc, C);
-    AL(d.flags, items); AL(d.scan, items);
+    ALS(d.k_list, C + J); ALS(d.k_colour, C + J); ALS(d.k_tent, C + J); ALS(d.k_order, C + J);
+    ALS(d.t_id, C + J);
+    ALS(d.k_prio, C + J);
+    AL(d.inc_off, N + 1); AL(d.inc_cur, N + 1); ALS(d.inc_list, 2 * ((size_t)C + J));
+    ALS(d.vc0, C); ALS(d.vc1, C); ALS(d.pc, C);
+    ALS(d.flags, items); ALS(d.scan, items);
     w->L.prims.sm_count = 1;
     {
         cudaDeviceProp prop;
@@ -1226,7 +1232,7 @@ struct AdjWindow {
     size_t snap_bytes = 0;
     std::vector<StepTape> tapes;    // host copies of the device structs
     StepTape* d_tapes = nullptr;
-    std::vector<void*> mem;         // tape, adjoint and tangent arrays
+    std::vector<std::pair<void*, size_t>> mem;  // tape, adjoint and tangent arrays
     AdjState adj{};
     TanState tan{};
     double* fdot = nullptr;
@@ -1244,11 +1250,38 @@ void adjoint_drop_graphs(prgpu_world* w) {
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
 }
 
+// Device memory of closed adjoint windows, (device, size) -> buffer, kept for the
+// next window of the same shape (a window allocates its checkpoints, tapes and
+// adjoint state up front; re-mapping gigabytes every window would cost more than
+// the window's steps).  prgpu_adjoint_trim frees it.
+static std::mutex g_adj_cache_mu;
+static std::multimap<std::pair<int, size_t>, void*> g_adj_cache;
+
+static void adj_give(const prgpu_world* w, void* p, size_t bytes) {
+    std::lock_guard<std::mutex> lk(g_adj_cache_mu);
+    g_adj_cache.emplace(std::make_pair(w->device, bytes), p);
+}
+
+// A buffer of exactly `bytes` from the cache, else a new one.
+static cudaError_t adj_take(prgpu_world* w, void** p, size_t bytes) {
+    {
+        std::lock_guard<std::mutex> lk(g_adj_cache_mu);
+        auto it = g_adj_cache.find(std::make_pair(w->device, bytes));
+        if (it != g_adj_cache.end()) {
+            *p = it->second;
+            g_adj_cache.erase(it);
+            return cudaSuccess;
+        }
+    }
+    return cudaMalloc(p, bytes);
+}
+
 static int adj_alloc(prgpu_world* w, AdjWindow* a, void** p, size_t bytes) {
     *p = nullptr;
-    const cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+    bytes = std::max<size_t>(bytes, 16);
+    const cudaError_t e = adj_take(w, p, bytes);
     if (e != cudaSuccess) return fail(w, PRGPU_ECUDA, "adjoint cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
-    a->mem.push_back(*p);
+    a->mem.push_back({*p, bytes});
     return PRGPU_OK;
 }
 
@@ -1257,9 +1290,9 @@ void adjoint_close(prgpu_world* w) {
     AdjWindow* a = w->adj;
     cudaStreamSynchronize(w->stream);
     adjoint_drop_graphs(w);
-    for (void* p : a->snaps) cudaFree(p);
-    if (a->end_state) cudaFree(a->end_state);
-    for (void* p : a->mem) cudaFree(p);
+    for (void* p : a->snaps) adj_give(w, p, a->snap_bytes);
+    if (a->end_state) adj_give(w, a->end_state, a->snap_bytes);
+    for (const auto& m : a->mem) adj_give(w, m.first, m.second);
     delete a;
     w->adj = nullptr;
     w->d.tape = nullptr;
@@ -1268,6 +1301,7 @@ void adjoint_close(prgpu_world* w) {
 static int snap_copy(prgpu_world* w, void* buf, bool save) {
     size_t off = 0;
     for (size_t i = 0; i < w->allocs.size(); ++i) {
+        if (w->alloc_scratch[i]) continue;
         char* b = static_cast<char*>(buf) + off;
         const cudaError_t e = save ? cudaMemcpyAsync(b, w->allocs[i], w->alloc_bytes[i], cudaMemcpyDeviceToDevice, w->stream)
                                    : cudaMemcpyAsync(w->allocs[i], b, w->alloc_bytes[i], cudaMemcpyDeviceToDevice, w->stream);
@@ -1279,7 +1313,8 @@ static int snap_copy(prgpu_world* w, void* buf, bool save) {
 
 static size_t snap_size(const prgpu_world* w) {
     size_t t = 0;
-    for (size_t b : w->alloc_bytes) t += (b + 255) & ~(size_t)255;
+    for (size_t i = 0; i < w->allocs.size(); ++i)
+        if (!w->alloc_scratch[i]) t += (w->alloc_bytes[i] + 255) & ~(size_t)255;
     return t;
 }
 
@@ -1297,6 +1332,7 @@ __global__ void k_count_diff(const uint32_t* a, const uint32_t* b, size_t n, uin
 static size_t snap_offset(const prgpu_world* w, const void* p) {
     size_t off = 0;
     for (size_t i = 0; i < w->allocs.size(); ++i) {
+        if (w->alloc_scratch[i]) continue;
         if (w->allocs[i] == p) return off;
         off += (w->alloc_bytes[i] + 255) & ~(size_t)255;
     }
@@ -1381,16 +1417,21 @@ static int record_segment(prgpu_world* w, int seg, int n) {
 int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every) {
     if (!w || checkpoint_every < 1) return PRGPU_EINVAL;
     if (w->adj) return fail(w, PRGPU_ESTATE, "an adjoint window is already open");
-    if (w->d.n_joints) return fail(w, PRGPU_EINVAL, "adjoint: joints are not part of the differentiated step");
     CU(cudaSetDevice(w->device));
+    if (w->d.n_joints) {  // the differentiated joint is the revolute point constraint
+        std::vector<uint32_t> jf(w->d.n_joints);
+        CU(cudaMemcpy(jf.data(), w->d.j_flags, sizeof(uint32_t) * jf.size(), cudaMemcpyDeviceToHost));
+        for (uint32_t f : jf)
+            if (f & 3u) return fail(w, PRGPU_EINVAL, "adjoint: joints with a limit or a motor are not differentiated");
+    }
     AdjWindow* a = new AdjWindow();
     a->every = checkpoint_every;
     a->kcap = w->d.contact_cap + w->d.n_joints;
     a->ccap = w->d.contact_cap;
     a->snap_bytes = snap_size(w);
-    a->grid = adj_setup();
+    a->grid = (int)adj_parallel_grid();
     w->adj = a;
-    if (a->grid < 1) { adjoint_close(w); return fail(w, PRGPU_ECUDA, "adjoint kernels cannot be resident"); }
+    if (a->grid < 1) { adjoint_close(w); return fail(w, PRGPU_ECUDA, "adjoint: no device"); }
     const uint32_t N = w->d.n_bodies, K = a->kcap, C = a->ccap, S = w->d.n_shapes;
     int rc = 0;
 #define AA(ptr, bytes) do { void* q_; rc = adj_alloc(w, a, &q_, (bytes)); if (rc) { adjoint_close(w); return rc; } \
@@ -1400,6 +1441,12 @@ int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every) {
     AA(a->adj.gbar, sizeof(float) * 24 * (size_t)K); AA(a->adj.gval, sizeof(float) * 24 * (size_t)K);
     AA(a->adj.mbar, sizeof(float4) * C); AA(a->adj.mtmp, sizeof(float4) * C); AA(a->adj.fbar, sizeof(float) * S);
     AA(a->adj.err, sizeof(uint32_t) * 2);
+    AA(a->adj.jbar, sizeof(float4) * std::max<uint32_t>(w->d.n_joints, 1));
+    a->adj.grid = (uint32_t)a->grid;
+    // one block per world in the reverse sweeps; larger worlds get larger blocks
+    const uint32_t most = w->order_nb.empty() ? 0u : *std::max_element(w->order_nb.begin(), w->order_nb.end());
+    a->adj.sweep_threads = most > 4096u ? kAdjSweepMaxThreads : 128u;
+    AA(a->tan.jdot, sizeof(double) * 2 * std::max<uint32_t>(w->d.n_joints, 1));
     AA(a->tan.pdot, sizeof(double) * 3 * N); AA(a->tan.vdot, sizeof(double) * 3 * N);
     AA(a->tan.vidot, sizeof(double) * 3 * N); AA(a->tan.ldot, sizeof(double) * 4 * (size_t)K);
     AA(a->tan.gdot, sizeof(double) * 24 * (size_t)K); AA(a->tan.mdot, sizeof(double) * 4 * (size_t)C);
@@ -1450,7 +1497,7 @@ int prgpu_adjoint_forward(prgpu_world* w, const prgpu_step_conf* conf, int n_ste
     for (int i = 0; i < n_steps; ++i) {
         if (a->steps % a->every == 0) {
             void* buf = nullptr;
-            if (cudaMalloc(&buf, a->snap_bytes) != cudaSuccess) return fail(w, PRGPU_ECUDA, "checkpoint allocation");
+            if (adj_take(w, &buf, a->snap_bytes) != cudaSuccess) return fail(w, PRGPU_ECUDA, "checkpoint allocation");
             a->snaps.push_back(buf);
             if ((rc = snap_copy(w, buf, true))) return rc;
         }
@@ -1480,7 +1527,7 @@ int prgpu_adjoint_backward(prgpu_world* w, const float* dl_dpos3, const float* d
     CU(cudaSetDevice(w->device));
     const uint32_t N = w->d.n_bodies, S = w->d.n_shapes;
     int rc = 0;
-    if (!a->end_state && cudaMalloc(&a->end_state, a->snap_bytes) != cudaSuccess)
+    if (!a->end_state && adj_take(w, &a->end_state, a->snap_bytes) != cudaSuccess)
         return fail(w, PRGPU_ECUDA, "end-state allocation");
     if ((rc = snap_copy(w, a->end_state, true))) return rc;
     std::vector<float4> h(N);
@@ -1494,6 +1541,7 @@ int prgpu_adjoint_backward(prgpu_world* w, const float* dl_dpos3, const float* d
                            dl_dvel3 ? dl_dvel3[3 * b + 2] : 0.f, 0.f);
     CU(cudaMemcpyAsync(a->adj.vbar, h.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, w->stream));
     CU(cudaMemsetAsync(a->adj.mbar, 0, sizeof(float4) * a->ccap, w->stream));
+    CU(cudaMemsetAsync(a->adj.jbar, 0, sizeof(float4) * std::max<uint32_t>(w->d.n_joints, 1), w->stream));
     CU(cudaMemsetAsync(a->adj.fbar, 0, sizeof(float) * std::max<uint32_t>(S, 1), w->stream));
     CU(cudaMemsetAsync(a->adj.err, 0, sizeof(uint32_t), w->stream));
     const int nseg = (a->steps + a->every - 1) / a->every;
@@ -1549,7 +1597,7 @@ int prgpu_adjoint_tangent(prgpu_world* w, const double* dpos3_start, const doubl
     CU(cudaSetDevice(w->device));
     const uint32_t N = w->d.n_bodies, S = w->d.n_shapes;
     int rc = 0;
-    if (!a->end_state && cudaMalloc(&a->end_state, a->snap_bytes) != cudaSuccess)
+    if (!a->end_state && adj_take(w, &a->end_state, a->snap_bytes) != cudaSuccess)
         return fail(w, PRGPU_ECUDA, "end-state allocation");
     if ((rc = snap_copy(w, a->end_state, true))) return rc;
     std::vector<double> z(3 * (size_t)N, 0.0), zf(std::max<uint32_t>(S, 1), 0.0);
@@ -1557,6 +1605,7 @@ int prgpu_adjoint_tangent(prgpu_world* w, const double* dpos3_start, const doubl
     CU(cudaMemcpyAsync(a->tan.vdot, dvel3_start ? dvel3_start : z.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice, w->stream));
     CU(cudaMemcpyAsync(a->fdot, dfriction ? dfriction : zf.data(), sizeof(double) * S, cudaMemcpyHostToDevice, w->stream));
     CU(cudaMemsetAsync(a->tan.mdot, 0, sizeof(double) * 4 * a->ccap, w->stream));
+    CU(cudaMemsetAsync(a->tan.jdot, 0, sizeof(double) * 2 * std::max<uint32_t>(w->d.n_joints, 1), w->stream));
     CU(cudaStreamSynchronize(w->stream));
     const int nseg = (a->steps + a->every - 1) / a->every;
     for (int seg = 0; seg < nseg; ++seg) {
@@ -1581,6 +1630,19 @@ int prgpu_adjoint_info(prgpu_world* w, int* steps, uint32_t* replay_mismatches, 
     if (steps) *steps = w->adj->steps;
     if (replay_mismatches) *replay_mismatches = w->adj->mismatches;
     if (tape_overflows) *tape_overflows = w->adj->overflows;
+    return PRGPU_OK;
+}
+
+int prgpu_adjoint_trim(void) {
+    std::lock_guard<std::mutex> lk(g_adj_cache_mu);
+    int dev = -1;
+    cudaGetDevice(&dev);
+    for (const auto& m : g_adj_cache) {
+        cudaSetDevice(m.first.first);
+        cudaFree(m.second);
+    }
+    g_adj_cache.clear();
+    if (dev >= 0) cudaSetDevice(dev);
     return PRGPU_OK;
 }
 

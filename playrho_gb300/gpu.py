@@ -111,6 +111,7 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_adjoint_info.argtypes = [P, P, P, P]
     lib.prgpu_adjoint_end.argtypes = [P]
     lib.prgpu_adjoint_profile.argtypes = [P, P, P, P]
+    lib.prgpu_adjoint_trim.argtypes = []
     lib.prgpu_autotune.argtypes = [P, ctypes.POINTER(StepConf), I, ctypes.POINTER(Schedule)]
     _LIB = lib
     return lib
@@ -126,7 +127,7 @@ def exported_symbols() -> List[str]:
         "prgpu_set_warp_world_max_bodies", "prgpu_get_warp_world_max_bodies", "prgpu_autotune",
         "prgpu_set_stage_bytes", "prgpu_get_stage_bytes", "prgpu_adjoint_begin", "prgpu_adjoint_forward",
         "prgpu_adjoint_backward", "prgpu_adjoint_tangent", "prgpu_adjoint_info", "prgpu_adjoint_end",
-        "prgpu_adjoint_profile"]
+        "prgpu_adjoint_profile", "prgpu_adjoint_trim"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -378,6 +379,10 @@ class GpuBatch:
 
     def adjoint_end(self):
         self._check(self.lib.prgpu_adjoint_end(self.h), "prgpu_adjoint_end")
+
+    def adjoint_trim(self):
+        """Frees the device memory that closed adjoint windows left cached."""
+        self._check(self.lib.prgpu_adjoint_trim(), "prgpu_adjoint_trim")
 
     def step_async(self, n: int, conf: StepConf):
         self._check(self.lib.prgpu_step_async(self.h, ctypes.byref(conf), int(n)), "prgpu_step_async")

@@ -107,3 +107,99 @@ def test_gradient_against_finite_differences_of_the_fp64_oracle(gpu_lib):
     print(f"\nd(mean box x)/d(disk vx): adjoint {ad_v:.6f} fd {fd_v:.6f}; d/d(disk x): adjoint {ad_x:.6f} fd {fd_x:.6f}")
     assert abs(ad_v - fd_v) <= 1e-3 * max(abs(fd_v), 1e-3) + 1e-4
     assert abs(ad_x - fd_x) <= 1e-3 * max(abs(fd_x), 1e-3) + 1e-4
+
+
+def _chain_scene(n_links=6, disk_vx=6.0, x0=0.0):
+    """A chain of 0.2 x 1 m boxes on revolute joints hanging from a static anchor,
+    struck by a disk rolling along the ground."""
+    sb = scenes.SceneBuilder()
+    gnd = sb.body(scenes.STATIC, 0.0, 0.0)
+    sb.edge(gnd, (-20.0, 0.0), (40.0, 0.0), friction=0.5)
+    top = float(n_links) + 0.6  # the tip link reaches down to 0.6 m, into the disk's path
+    anchor = sb.body(scenes.STATIC, x0 + 2.5, top)
+    d = sb.body(scenes.DYNAMIC, x0, 0.5, v=(disk_vx, 0.0, 0.0), acc=scenes.GRAVITY)
+    sb.disk(d, 0.5, density=1.0, friction=0.5)
+    prev = anchor
+    for k in range(n_links):
+        b = sb.body(scenes.DYNAMIC, x0 + 2.5, top - 0.5 - 1.0 * k, acc=scenes.GRAVITY)
+        sb.box(b, 0.1, 0.5, density=1.0, friction=0.5, filt=(2, 0xFFFD, 0, 0))
+        sb.revolute(prev, b, (0.0, 0.0) if prev == anchor else (0.0, -0.5), (0.0, 0.5))
+        prev = b
+    return sb.build()
+
+
+def test_joint_dot_product_and_replay(gpu_lib):
+    """The dot-product test on worlds whose disks strike hanging chains: revolute
+    joints' warm start, velocity and position rows and stored impulses, in the
+    adjoint and in the tangent, and the joint geometry replayed bit for bit."""
+    worlds = [_chain_scene(n_links=4 + k, disk_vx=5.0 + k) for k in range(4)]
+    g = GpuBatch(worlds)
+    conf = default_conf(minStillTimeToSleep=1e9)
+    g.step_n(25, conf)  # the disks reach the chains
+    g.adjoint_begin(4)
+    g.adjoint_forward(12, conf)
+    rng = np.random.default_rng(1)
+    dyn = dynamic_mask(worlds)
+    n, s = g.n_bodies, g.n_shapes
+    ybar_p = rng.standard_normal((n, 3)) * dyn[:, None]
+    ybar_v = rng.standard_normal((n, 3)) * dyn[:, None]
+    xdot_p = rng.standard_normal((n, 3)) * dyn[:, None] * 1e-2
+    xdot_v = rng.standard_normal((n, 3)) * dyn[:, None] * 1e-1
+    xdot_f = rng.standard_normal(s) * 1e-2
+    adj = g.adjoint_backward(ybar_p, ybar_v)
+    tan = g.adjoint_tangent(xdot_p, xdot_v, xdot_f)
+    info = g.adjoint_info()
+    assert info["replay_mismatches"] == 0, info
+    assert info["tape_overflows"] == 0, info
+    lhs = float((ybar_p * tan["pos"]).sum() + (ybar_v * tan["vel"]).sum())
+    rhs = float((adj["pos"].astype(np.float64) * xdot_p).sum() + (adj["vel"].astype(np.float64) * xdot_v).sum() +
+                (adj["friction"].astype(np.float64) * xdot_f).sum())
+    scale = max(abs(lhs), abs(rhs), 1e-12)
+    print(f"\njoint dot-product test: <ybar, J xdot> = {lhs:.9e}, <J^T ybar, xdot> = {rhs:.9e}, "
+          f"rel diff {abs(lhs - rhs) / scale:.2e}")
+    assert abs(lhs - rhs) <= 1e-4 * scale
+    g.adjoint_end()
+
+
+def test_joint_gradient_against_finite_differences_of_the_fp64_oracle(gpu_lib):
+    """d(chain tip x after 40 steps)/d(disk's initial vx and x): the disk strikes
+    the chain's tip, so the gradient runs through the contact and back up the
+    joints.  Adjoint on the GPU against central differences of the FP64 oracle,
+    both solved to convergence.  (Perturbing a link's own state instead shows the
+    colour-order difference of the position iterations, which do not converge
+    in 30 iterations: the GPU forward's own finite difference then agrees with
+    the adjoint, not with the oracle's.)"""
+    sc = _chain_scene(n_links=4, disk_vx=6.0)
+    steps = 40
+    over = dict(regVelocityIters=200, regPositionIters=30, minStillTimeToSleep=1e9, regMinSeparation=-1e-9)
+    conf = default_conf(**over)
+    tip, disk = sc.n_bodies - 1, 2
+    g = GpuBatch([sc])
+    g.step(deltaTime=0.0)
+    g.adjoint_begin(10)
+    g.adjoint_forward(steps, conf)
+    ybar = np.zeros((sc.n_bodies, 3))
+    ybar[tip, 0] = 1.0
+    adj = g.adjoint_backward(ybar, None)
+    info = g.adjoint_info()
+    assert info["replay_mismatches"] == 0 and info["tape_overflows"] == 0, info
+
+    def loss(dvx=0.0, dx=0.0):
+        s2 = scenes.Scene(**{f: getattr(sc, f) for f in sc.__dataclass_fields__})
+        s2.body_vel = sc.body_vel.astype(np.float64).copy()
+        s2.body_pos = sc.body_pos.astype(np.float64).copy()
+        s2.body_vel[disk, 0] += dvx
+        s2.body_pos[disk, 0] += dx
+        o = oracle.OracleWorld(s2, double=True)
+        o.step(deltaTime=0.0)
+        for _ in range(steps):
+            o.step(**over)
+        return float(o.bodies()["pos"][tip, 0])
+
+    h = 1e-4
+    fd_v = (loss(dvx=h) - loss(dvx=-h)) / (2 * h)
+    fd_x = (loss(dx=h) - loss(dx=-h)) / (2 * h)
+    ad_v, ad_x = float(adj["vel"][disk, 0]), float(adj["pos"][disk, 0])
+    print(f"\nd(tip x)/d(disk vx): adjoint {ad_v:.6f} fd {fd_v:.6f}; d/d(disk x): adjoint {ad_x:.6f} fd {fd_x:.6f}")
+    assert abs(ad_v - fd_v) <= 1e-3 * max(abs(fd_v), 1e-3) + 1e-4
+    assert abs(ad_x - fd_x) <= 1e-3 * max(abs(fd_x), 1e-3) + 1e-4
