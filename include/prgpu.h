@@ -195,7 +195,9 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
  *                           final state out), for dot-product tests of the adjoint
  *   prgpu_adjoint_info      steps in the window, recorded steps whose constraint
  *                           set-up the differentiable restatement did not reproduce
- *                           bit for bit (0 expected), local tapes that overflowed
+ *                           bit for bit, or whose re-run did not end where the
+ *                           forward went on (0 expected), and a count kept at 0
+ *                           (the reverse pass keeps no bounded local tapes)
  *   prgpu_adjoint_end       closes the window; its device memory stays cached
  *                           for the next window of the same sizes
  *   prgpu_adjoint_trim      frees the cached memory of closed windows
