@@ -970,6 +970,9 @@ struct SharedBodies {
     __device__ __forceinline__ void island_joint_fail(uint32_t L, int) const { jok[L - base] = 0u; }
 };
 
+// Non-binding prefetch of the line holding p into L1.
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
 // ---- per-constraint sweep steps (t = position in sweep order) -------------------
 // When the step is recorded for the adjoint (d.tape), each contact step also
 // writes the body state (and impulses) it starts from.
@@ -1162,6 +1165,22 @@ template <class G, class BS, class F>
 __device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uint32_t size, uint32_t base,
                        uint32_t n, const uint32_t* col_off, F&& after_position) {
     const DConf& c = *d.conf;
+    // parallel colours in use: 0 .. top-1 (then the serial colour, often empty)
+    int top = 0;
+    for (int q = 0; q < kMaxColours; ++q)
+        if (col_off[q + 1] > col_off[q]) top = q + 1;
+    const bool serial = col_off[kSerialColour + 1] > col_off[kSerialColour];
+    // The colour after col in sweep order (the first one again after the last).
+    auto next_col = [&](int col) { return (col + 1 < top) ? col + 1 : 0; };
+    // Starts the loads of colour col's records for this thread (the constraint
+    // ids and the records at `rec`, `stride` bytes apart), so that they arrive
+    // while the current colour is solved.
+    auto prefetch = [&](int col, const void* rec, size_t stride) {
+        for (uint32_t t = base + col_off[col] + rank; t < base + col_off[col + 1]; t += size) {
+            prefetch_l1(d.t_id + t);
+            prefetch_l1(static_cast<const char*>(rec) + (size_t)t * stride);
+        }
+    };
     // Runs f(t) over colour col of this world, then synchronises the group.
     auto sweep = [&](int col, auto&& f) {
         const uint32_t lo = base + col_off[col], hi = base + col_off[col + 1];
@@ -1173,16 +1192,24 @@ __device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uin
         }
         G::sync();
     };
+    // One pass over the world's colours; each parallel colour first prefetches the next.
+    auto pass = [&](const void* rec, size_t stride, auto&& f) {
+        for (int col = 0; col < top; ++col) {
+            if (top > 1) prefetch(next_col(col), rec, stride);
+            sweep(col, f);
+        }
+        if (serial) sweep(kSerialColour, f);
+    };
     if (n) {
-        for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_warm(d, bs, t); });
+        pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_warm(d, bs, t); });
         for (int it = 0; it < c.regVelocityIters; ++it)
-            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_velocity(d, bs, t, it); });
+            pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_velocity(d, bs, t, it); });
     }
     for (uint32_t b = d.w_body_off[w] + rank; b < d.w_body_off[w + 1]; b += size) integrate_body(d, bs, b);
     G::sync();
     if (n) {
         for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it) {
-            for (int col = 0; col <= kSerialColour; ++col) sweep(col, [&](uint32_t t) { sweep_position(d, bs, t, it); });
+            pass(d.pc, sizeof(PC), [&](uint32_t t) { sweep_position(d, bs, t, it); });
             after_position(it);
         }
         for (uint32_t t = base + rank; t < base + n; t += size) store_impulses(d, t);
