@@ -21,10 +21,22 @@ CONF_REAL_FIELDS = (
     "linearSleepTolerance", "angularSleepTolerance", "displaceMultiplier", "aabbExtension",
     "maxCirclesRatio")
 CONF_INT_FIELDS = ("regVelocityIters", "regPositionIters", "doWarmStart", "doBlocksolve")
+CONF_TOI_REAL_FIELDS = ("toiResolutionRate", "toiMinSeparation", "toiMinMomentum", "targetDepth", "tolerance")
+CONF_TOI_INT_FIELDS = ("toiVelocityIters", "toiPositionIters", "maxToiRootIters", "maxToiIters",
+                       "maxDistanceIters", "maxSubSteps", "doToi")
 STATS_INT_FIELDS = (
     "preProxiesCreated", "preProxiesMoved", "preContactsDestroyed", "preContactsAdded",
     "preContactsUpdated", "regIslandsFound", "regIslandsSolved", "regContactsAdded",
     "regContactsUpdated", "regProxiesMoved", "regBodiesSlept", "regSumPosIters", "regSumVelIters")
+TOI_STATS_INT_FIELDS = (
+    "toiIslandsFound", "toiIslandsSolved", "toiContactsFound", "toiContactsAtMaxSubSteps",
+    "toiContactsUpdatedToi", "toiContactsUpdatedTouching", "toiContactsSkippedTouching", "toiContactsAdded",
+    "toiProxiesMoved", "toiSumPosIters", "toiSumVelIters", "toiMaxDistIters", "toiMaxToiIters",
+    "toiMaxRootIters")
+# ToiOutput::State (ToiOutput.hpp) as the oracle numbers it
+TOI_STATES = ("unknown", "overlapped", "touching", "separated", "maxRootIters", "nextAfter", "maxToiIters",
+              "belowMinTarget", "maxDistIters", "targetDepthExceedsTotalRadius", "minTargetSquaredOverflow",
+              "maxTargetSquaredOverflow", "notFinite")
 
 
 def build() -> None:
@@ -46,11 +58,14 @@ def _lib(double: bool):
     real = ctypes.c_double if double else ctypes.c_float
 
     class Conf(ctypes.Structure):
-        _fields_ = [(n, real) for n in CONF_REAL_FIELDS] + [(n, ctypes.c_int) for n in CONF_INT_FIELDS]
+        _fields_ = ([(n, real) for n in CONF_REAL_FIELDS] + [(n, ctypes.c_int) for n in CONF_INT_FIELDS]
+                    + [(n, real) for n in CONF_TOI_REAL_FIELDS] + [(n, ctypes.c_int) for n in CONF_TOI_INT_FIELDS])
 
     class Stats(ctypes.Structure):
-        _fields_ = [(n, ctypes.c_int) for n in STATS_INT_FIELDS] + [
-            ("regMinSeparation", real), ("regMaxIncImpulse", real)]
+        _fields_ = ([(n, ctypes.c_int) for n in STATS_INT_FIELDS]
+                    + [("regMinSeparation", real), ("regMaxIncImpulse", real)]
+                    + [(n, ctypes.c_int) for n in TOI_STATS_INT_FIELDS]
+                    + [("toiMinSeparation", real), ("toiMaxIncImpulse", real)])
 
     P = ctypes.c_void_p
     lib.or_world_create.restype = P
@@ -79,6 +94,13 @@ def _lib(double: bool):
     lib.or_collide.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, real, ctypes.c_void_p,
                                ctypes.c_int, ctypes.c_int, ctypes.c_void_p, real, ctypes.c_void_p,
                                real, real, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.or_time_of_impact.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, real, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, real,
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Conf), ctypes.c_void_p]
+    lib.or_time_of_impact.restype = real
+    lib.or_distance.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, real, ctypes.c_void_p,
+                                ctypes.c_int, ctypes.c_int, ctypes.c_void_p, real, ctypes.c_void_p,
+                                ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     _LIBS[key] = (lib, real, Conf, Stats)
     return _LIBS[key]
 
@@ -87,7 +109,7 @@ def default_conf(double: bool = False) -> dict:
     lib, real, Conf, _ = _lib(double)
     c = Conf()
     lib.or_default_conf(ctypes.byref(c))
-    return {n: getattr(c, n) for n in CONF_REAL_FIELDS + CONF_INT_FIELDS}
+    return {n: getattr(c, n) for n, _ in Conf._fields_}
 
 
 class OracleWorld:
@@ -192,3 +214,36 @@ def collide(kind_a, verts_a, r_a, xf_a, kind_b, verts_b, r_b, xf_b, linear_slop=
                    tc.ctypes.data, ft.ctypes.data, fo.ctypes.data)
     return {"type": int(tc[0]), "count": int(tc[1]), "features": ft.reshape(2, 4),
             "local_normal": fo[0:2], "local_point": fo[2:4], "points": fo[4:8].reshape(2, 2)}
+
+
+def time_of_impact(verts_a, r_a, sweep_a, lc_a, verts_b, r_b, sweep_b, lc_b, double=False, **conf):
+    """Stand-alone GetToiViaSat of the oracle: sweeps are (pos0 xy angle, pos1 xy angle,
+    alpha0); returns (time, state name, toi iterations, max distance iterations,
+    max root iterations)."""
+    lib, real, Conf, _ = _lib(double)
+    npr = np.float64 if double else np.float32
+    c = Conf()
+    lib.or_default_conf(ctypes.byref(c))
+    for k, v in conf.items():
+        setattr(c, k, v)
+    arr = lambda x: np.ascontiguousarray(np.asarray(x, dtype=npr).reshape(-1))
+    va, vb, sa, sb, la, lb = (arr(x) for x in (verts_a, verts_b, sweep_a, sweep_b, lc_a, lc_b))
+    io = np.zeros(4, dtype=np.int32)
+    t = lib.or_time_of_impact(0, va.size // 2, va.ctypes.data, r_a, sa.ctypes.data, la.ctypes.data,
+                              0, vb.size // 2, vb.ctypes.data, r_b, sb.ctypes.data, lb.ctypes.data,
+                              ctypes.byref(c), io.ctypes.data)
+    return float(t), TOI_STATES[int(io[0])], int(io[1]), int(io[2]), int(io[3])
+
+
+def distance(verts_a, r_a, xf_a, verts_b, r_b, xf_b, max_iters=20, double=False):
+    """Stand-alone GJK Distance of the oracle from an empty cache: (state, iterations,
+    simplex size, witness point A, witness point B)."""
+    lib, real, _, _ = _lib(double)
+    npr = np.float64 if double else np.float32
+    arr = lambda x: np.ascontiguousarray(np.asarray(x, dtype=npr).reshape(-1))
+    va, vb, xa, xb = (arr(x) for x in (verts_a, verts_b, xf_a, xf_b))
+    io = np.zeros(3, dtype=np.int32)
+    fo = np.zeros(4, dtype=npr)
+    lib.or_distance(0, va.size // 2, va.ctypes.data, r_a, xa.ctypes.data, 0, vb.size // 2, vb.ctypes.data, r_b,
+                    xb.ctypes.data, max_iters, io.ctypes.data, fo.ctypes.data)
+    return int(io[0]), int(io[1]), int(io[2]), fo[0:2].copy(), fo[2:4].copy()

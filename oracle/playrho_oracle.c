@@ -10,8 +10,9 @@
  * Scope: disks, convex polygons and edges (one child per shape), revolute
  * joints, contact persistence with fattened/displaced proxy AABBs, island
  * discovery by depth-first search, sequential-impulse Gauss-Seidel velocity
- * solve with the 2-point block solver, NGS position solve, sleep.  TOI
- * (StepConf::doToi) is not restated: the callers run with doToi = false.
+ * solve with the 2-point block solver, NGS position solve, sleep, and the TOI
+ * phase (StepConf::doToi): GJK distance, conservative advancement by separating
+ * axes, and the sequential sub-stepping of time-of-impact events.
  */
 #include "playrho_oracle.h"
 
@@ -158,7 +159,7 @@ typedef struct { int type; v2 ln; v2 lp; int count; mpt p[2]; } manifold;
 
 typedef struct { int count; v2 v[OR_MAXV]; v2 n[OR_MAXV]; real r; } dproxy;
 
-enum { BF_AWAKE = 1u, BF_ALLOW_SLEEP = 2u, BF_FIXED_ROT = 4u, BF_ENABLED = 8u };
+enum { BF_AWAKE = 1u, BF_ALLOW_SLEEP = 2u, BF_FIXED_ROT = 4u, BF_ENABLED = 8u, BF_BULLET = 16u };
 typedef struct {
     int type;
     unsigned flags;
@@ -168,6 +169,8 @@ typedef struct {
     pos_t vel;
     v2 la;
     real aa, ldamp, adamp, invM, invI, uat;
+    real alpha0;  /* Sweep::alpha0: only non-zero inside the TOI phase */
+    int islanded; /* m_islanded.bodies entry of the TOI phase */
     ivec shapes, proxies;
     ivec ckeys, cids; /* body contact list: (key, contactID), insertion order */
     ivec jids, jother; /* body joint list: (jointID, other body) */
@@ -208,6 +211,8 @@ typedef struct {
     int touching, sensor, needsUpdate, impenetrable;
     real friction, restitution, tangentSpeed;
     manifold m;
+    real toi;                      /* Contact::m_toi, valid when toiValid (e_toiFlag) */
+    int toiValid, toiCount, islanded;
 } contact_t;
 
 struct or_world {
@@ -239,7 +244,8 @@ static inline uint64_t make_key(int a, int b) {
 
 static inline int is_speedable(const body_t* b) { return b->type != OR_STATIC; }
 static inline int is_accelerable(const body_t* b) { return b->type == OR_DYNAMIC; }
-static inline int is_impenetrable(const body_t* b) { return b->type != OR_DYNAMIC; }
+/* Body::GetFlags (Body.cpp:32-66): static and kinematic bodies, and bullets. */
+static inline int is_impenetrable(const body_t* b) { return b->type != OR_DYNAMIC || (b->flags & BF_BULLET); }
 
 /* Body::SetAwake (Body.cpp:161-169). */
 static void body_set_awake(body_t* b) {
@@ -291,6 +297,7 @@ int or_add_body(or_world* w, int type, real px, real py, real angle, real vx, re
     if (flags & OR_BF_ALLOW_SLEEP) b->flags |= BF_ALLOW_SLEEP;
     if (flags & OR_BF_FIXED_ROTATION) b->flags |= BF_FIXED_ROT;
     if (flags & OR_BF_ENABLED) b->flags |= BF_ENABLED;
+    if (flags & OR_BF_BULLET) b->flags |= BF_BULLET;
     if ((flags & OR_BF_AWAKE) && type != OR_STATIC) b->flags |= BF_AWAKE;
     b->lc = V(R(0), R(0));
     b->pos0.lin = V(px, py); b->pos0.ang = angle;
@@ -1590,6 +1597,33 @@ typedef struct {
     ivec bodies, contacts, joints;
 } island_t;
 
+/* GetBodyConstraint (BodyConstraint.hpp:157-167): position 1 and
+ * Cap(GetVelocity(body, h)) (Body.cpp:290-309, Velocity.cpp:26-45). */
+static void make_bc(bc_t* bc, const body_t* b, real h, const or_stepconf* conf) {
+    bc->invM = b->invM; bc->invI = b->invI; bc->lc = b->lc; bc->pos = b->pos1;
+    pos_t v = b->vel;
+    if (is_accelerable(b)) {
+        v.lin = vadd(v.lin, vmul(b->la, h));
+        v.ang = v.ang + h * b->aa;
+        v.lin = vdiv(v.lin, R(1) + h * b->ldamp);
+        v.ang = v.ang / (R(1) + h * b->adamp);
+    }
+    {
+        const v2 translation = vmul(v.lin, h);
+        const real lsq = mag2(translation);
+        if (lsq > conf->maxTranslation * conf->maxTranslation) {
+            const real ratio = conf->maxTranslation / RSQRT(lsq);
+            v.lin = vmul(v.lin, ratio);
+        }
+        const real absRot = fabs(h * v.ang);
+        if (absRot > conf->maxRotation) {
+            const real ratio = conf->maxRotation / absRot;
+            v.ang = v.ang * ratio;
+        }
+    }
+    bc->vel = v;
+}
+
 static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc_t* bcs,
                          or_stepstats* st) {
     const real h = conf->deltaTime;
@@ -1598,34 +1632,9 @@ static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc
         body_t* b = &w->b[isl->bodies.a[i]];
         b->pos0 = b->pos1;
     }
-    /* GetBodyConstraints -> GetBodyConstraint: Cap(GetVelocity(body, h)) (Body.cpp:290-309,
-     * Velocity.cpp:26-45). */
     for (int i = 0; i < isl->bodies.n; ++i) {
         const int id = (int)isl->bodies.a[i];
-        const body_t* b = &w->b[id];
-        bc_t* bc = &bcs[id];
-        bc->invM = b->invM; bc->invI = b->invI; bc->lc = b->lc; bc->pos = b->pos1;
-        pos_t v = b->vel;
-        if (is_accelerable(b)) {
-            v.lin = vadd(v.lin, vmul(b->la, h));
-            v.ang = v.ang + h * b->aa;
-            v.lin = vdiv(v.lin, R(1) + h * b->ldamp);
-            v.ang = v.ang / (R(1) + h * b->adamp);
-        }
-        {
-            const v2 translation = vmul(v.lin, h);
-            const real lsq = mag2(translation);
-            if (lsq > conf->maxTranslation * conf->maxTranslation) {
-                const real ratio = conf->maxTranslation / RSQRT(lsq);
-                v.lin = vmul(v.lin, ratio);
-            }
-            const real absRot = fabs(h * v.ang);
-            if (absRot > conf->maxRotation) {
-                const real ratio = conf->maxRotation / absRot;
-                v.ang = v.ang * ratio;
-            }
-        }
-        bc->vel = v;
+        make_bc(&bcs[id], &w->b[id], h, conf);
     }
     const int nc = isl->contacts.n;
     pc_t* pcs = (pc_t*)malloc(sizeof(pc_t) * (size_t)(nc + 1));
@@ -1781,7 +1790,655 @@ static void solve_reg(or_world* w, const or_stepconf* conf, or_stepstats* st) {
     free(ib); free(ic); free(ij); free(bcs); free(stack);
 }
 
-/* Step(AabbTreeWorld&, StepConf) (AabbTreeWorld.cpp:2144-2219), doToi = false. */
+/* ------------------------------------------------------------------------- */
+/* Time of impact: Distance (GJK), separation scenarios, GetToiViaSat, and the */
+/* TOI phase of the step (StepConf::doToi).                                   */
+/* ------------------------------------------------------------------------- */
+/* Position arithmetic (d2/Position.hpp) and GetPosition (d2/Math.cpp:30-60):
+ * pos0 + (pos1 - pos0) * beta. */
+static pos_t plerp(pos_t p0, pos_t p1, real beta) {
+    pos_t d, s;
+    d.lin = vsub(p1.lin, p0.lin); d.ang = p1.ang - p0.ang;
+    s.lin = vmul(d.lin, beta); s.ang = d.ang * beta;
+    return padd(p0, s);
+}
+static inline int pos_ne(pos_t a, pos_t b) {
+    return !(a.lin.x == b.lin.x && a.lin.y == b.lin.y && a.ang == b.ang);
+}
+
+/* Sweep (d2/Sweep.hpp:43-92). */
+typedef struct { pos_t p0, p1; v2 lc; real a0; } sweep_t;
+static sweep_t body_sweep(const body_t* b) { sweep_t s; s.p0 = b->pos0; s.p1 = b->pos1; s.lc = b->lc; s.a0 = b->alpha0; return s; }
+/* Body::SetSweep (Body.hpp:697-702). */
+static void body_set_sweep(body_t* b, sweep_t s) { b->pos0 = s.p0; b->pos1 = s.p1; b->lc = s.lc; b->alpha0 = s.a0; b->xf = get_xf(s.p1, s.lc); }
+/* GetTransformation(sweep, beta) (d2/Math.hpp:251-254). */
+static inline xf_t sweep_xf(const sweep_t* s, real beta) { return get_xf(plerp(s->p0, s->p1, beta), s->lc); }
+/* Advance0 (Sweep.cpp:27-31) on a body (Body.hpp:722-730). */
+static void body_advance0(body_t* b, real alpha) {
+    const real beta = (alpha - b->alpha0) / (R(1) - b->alpha0);
+    b->pos0 = plerp(b->pos0, b->pos1, beta);
+    b->alpha0 = alpha;
+}
+/* Advance (Body.hpp:1004-1009): Advance0 then position 1 = position 0. */
+static void body_advance(body_t* b, real alpha) { body_advance0(b, alpha); body_set_pos1(b, b->pos0); }
+/* GetNormalized(Angle) (Math.cpp:33-91, default branch). */
+static real angle_normalized(real a) {
+    const real Pi = R(3.14159265358979323846264338327950288L);
+    const real twoPi = R(2) * Pi;
+    const real rTwoPi = R(1) / twoPi;
+#ifdef OR_DOUBLE
+    a = a - trunc(a * rTwoPi) * twoPi;
+#else
+    a = a - truncf(a * rTwoPi) * twoPi;
+#endif
+    if (a >= Pi) a -= Pi * R(2);
+    else if (a < -Pi) a += Pi * R(2);
+    return a;
+}
+/* GetNormalized(Sweep) (d2/Math.hpp:160-167). */
+static sweep_t sweep_normalized(sweep_t s) {
+    const real a0 = angle_normalized(s.p0.ang);
+    const real d = s.p0.ang - a0;
+    s.p0.ang = a0;
+    s.p1.ang -= d;
+    return s;
+}
+
+/* SimplexEdge (SimplexEdge.hpp:40-87) and Simplex (Simplex.cpp). */
+typedef struct { v2 pA; int iA; v2 pB; int iB; } sedge;
+typedef struct { int n; sedge e[3]; real c[3]; } simplex_t;
+typedef struct { int n; int ia[3], ib[3]; real metric; } scache; /* Simplex::Cache */
+
+static inline sedge make_sedge(const dproxy* A, xf_t xfA, int ia, const dproxy* B, xf_t xfB, int ib) {
+    sedge e;
+    e.pA = xform(A->v[ia], xfA); e.iA = ia;
+    e.pB = xform(B->v[ib], xfB); e.iB = ib;
+    return e;
+}
+static inline v2 sdelta(const sedge* e) { return vsub(e->pB, e->pA); }
+
+static simplex_t simplex1(sedge s0) { simplex_t r; memset(&r, 0, sizeof(r)); r.n = 1; r.e[0] = s0; r.c[0] = R(1); return r; }
+static simplex_t simplex2(sedge s0, sedge s1, real c0, real c1) {
+    simplex_t r; memset(&r, 0, sizeof(r)); r.n = 2; r.e[0] = s0; r.e[1] = s1; r.c[0] = c0; r.c[1] = c1; return r;
+}
+/* Simplex::Get (Simplex.cpp:55-169). */
+static simplex_t simplex_get(const sedge* s, int n) {
+    if (n == 1) return simplex1(s[0]);
+    if (n == 2) {
+        const v2 w1 = sdelta(&s[0]), w2 = sdelta(&s[1]);
+        const v2 e12 = vsub(w2, w1);
+        const real d12_2 = -dot(w1, e12);
+        if (d12_2 <= R(0)) return simplex1(s[0]);
+        const real d12_1 = dot(w2, e12);
+        if (d12_1 <= R(0)) return simplex1(s[1]);
+        const real inv_sum = R(1) / (d12_1 + d12_2);
+        return simplex2(s[0], s[1], d12_1 * inv_sum, d12_2 * inv_sum);
+    }
+    const v2 w1 = sdelta(&s[0]), w2 = sdelta(&s[1]), w3 = sdelta(&s[2]);
+    const v2 e12 = vsub(w2, w1);
+    const real d12_1 = dot(w2, e12);
+    const real d12_2 = -dot(w1, e12);
+    const v2 e13 = vsub(w3, w1);
+    const real d13_1 = dot(w3, e13);
+    const real d13_2 = -dot(w1, e13);
+    const v2 e23 = vsub(w3, w2);
+    const real d23_1 = dot(w3, e23);
+    const real d23_2 = -dot(w2, e23);
+    if ((d12_2 <= R(0)) && (d13_2 <= R(0))) return simplex1(s[0]);
+    if ((d12_1 <= R(0)) && (d23_2 <= R(0))) return simplex1(s[1]);
+    if ((d13_1 <= R(0)) && (d23_1 <= R(0))) return simplex1(s[2]);
+    const real n123 = cross(e12, e13);
+    const real d123_3 = n123 * cross(w1, w2);
+    if ((d12_1 > R(0)) && (d12_2 > R(0)) && (d123_3 <= R(0))) {
+        const real inv_sum = R(1) / (d12_1 + d12_2);
+        return simplex2(s[0], s[1], d12_1 * inv_sum, d12_2 * inv_sum);
+    }
+    const real d123_2 = n123 * cross(w3, w1);
+    if ((d13_1 > R(0)) && (d13_2 > R(0)) && (d123_2 <= R(0))) {
+        const real inv_sum = R(1) / (d13_1 + d13_2);
+        return simplex2(s[0], s[2], d13_1 * inv_sum, d13_2 * inv_sum);
+    }
+    const real d123_1 = n123 * cross(w2, w3);
+    if ((d23_1 > R(0)) && (d23_2 > R(0)) && (d123_1 <= R(0))) {
+        const real inv_sum = R(1) / (d23_1 + d23_2);
+        return simplex2(s[2], s[1], d23_2 * inv_sum, d23_1 * inv_sum);
+    }
+    const real inv_sum = R(1) / (d123_1 + d123_2 + d123_3);
+    simplex_t r;
+    memset(&r, 0, sizeof(r));
+    r.n = 3; r.e[0] = s[0]; r.e[1] = s[1]; r.e[2] = s[2];
+    r.c[0] = d123_1 * inv_sum; r.c[1] = d123_2 * inv_sum; r.c[2] = d123_3 * inv_sum;
+    return r;
+}
+/* Simplex::CalcMetric (Simplex.cpp:171-192). */
+static real simplex_metric(const sedge* s, int n) {
+    if (n == 2) return RSQRT(mag2(vsub(sdelta(&s[1]), sdelta(&s[0]))));
+    if (n == 3) return cross(vsub(sdelta(&s[1]), sdelta(&s[0])), vsub(sdelta(&s[2]), sdelta(&s[0])));
+    return R(0);
+}
+/* CalcSearchDirection (Simplex.cpp:37-53). */
+static v2 search_direction(const sedge* s, int n) {
+    if (n == 1) return vneg(sdelta(&s[0]));
+    if (n == 2) {
+        const v2 e12 = vsub(sdelta(&s[1]), sdelta(&s[0]));
+        const v2 e0 = sdelta(&s[0]);
+        const real sgn = cross(e12, vneg(e0));
+        return (sgn > R(0)) ? revperp(e12) : fwdperp(e12);
+    }
+    return V(R(0), R(0));
+}
+/* GetSupportIndex (DistanceProxy.hpp:233-249). */
+static int support_index(const dproxy* p, v2 dir) {
+    int index = 255;
+    real maxValue = -RINF;
+    for (int i = 0; i < p->count; ++i) {
+        const real value = dot(p->v[i], dir);
+        if (maxValue < value) { maxValue = value; index = i; }
+    }
+    return index;
+}
+
+enum { DIST_HITMAX = 1, DIST_MAXPOINTS = 2, DIST_UNFIT = 3, DIST_DUPLICATE = 4 };
+typedef struct { simplex_t s; int iters, state; } dist_out;
+/* Distance (Distance.cpp:96-196) with the cache of the previous call. */
+static dist_out gjk_distance(const dproxy* A, xf_t xfA, const dproxy* B, xf_t xfB, const scache* cache,
+                             int maxIters) {
+    int sa[3], sb[3], sn = cache->n;
+    sedge edges[3];
+    int ne = cache->n;
+    for (int k = 0; k < sn; ++k) {
+        sa[k] = cache->ia[k]; sb[k] = cache->ib[k];
+        edges[k] = make_sedge(A, xfA, sa[k], B, xfB, sb[k]);
+    }
+    if (ne > 1) {
+        const real metric1 = cache->metric;
+        const real metric2 = simplex_metric(edges, ne);
+        if ((metric2 < (metric1 / R(2))) || (metric2 > (metric1 * R(2))) || (metric2 < R(0)) || almost_zero(metric2)) ne = 0;
+    }
+    if (ne == 0) {
+        edges[0] = make_sedge(A, xfA, 0, B, xfB, 0);
+        ne = 1;
+        sn = 1; sa[0] = 0; sb[0] = 0;
+    }
+    dist_out out;
+    memset(&out, 0, sizeof(out));
+    out.state = DIST_HITMAX;
+    int iter = 0;
+    while (iter < maxIters) {
+        ++iter;
+        out.s = simplex_get(edges, ne);
+        ne = out.s.n;
+        for (int k = 0; k < ne; ++k) edges[k] = out.s.e[k];
+        if (ne == 3) { out.state = DIST_MAXPOINTS; break; }
+        const v2 d = search_direction(edges, ne);
+        if (almost_zero(mag2(d))) { out.state = DIST_UNFIT; break; }
+        const int ia = support_index(A, invrotate(vneg(d), xfA.q));
+        const int ib = support_index(B, invrotate(d, xfB.q));
+        int dup = 0;
+        for (int k = 0; k < sn; ++k) if (sa[k] == ia && sb[k] == ib) dup = 1;
+        if (dup) { out.state = DIST_DUPLICATE; break; }
+        edges[ne++] = make_sedge(A, xfA, ia, B, xfB, ib);
+        sn = ne;
+        for (int k = 0; k < ne; ++k) { sa[k] = edges[k].iA; sb[k] = edges[k].iB; }
+    }
+    out.iters = iter;
+    return out;
+}
+/* GetWitnessPoints (Distance.cpp:71-94). */
+static void witness_points(const simplex_t* s, v2* pA, v2* pB) {
+    v2 a = V(R(0), R(0)), b = V(R(0), R(0));
+    for (int i = 0; i < s->n; ++i) {
+        a = vadd(a, vmul(s->e[i].pA, s->c[i]));
+        b = vadd(b, vmul(s->e[i].pB, s->c[i]));
+    }
+    *pA = a; *pB = b;
+}
+
+/* SeparationScenario (SeparationScenario.cpp). */
+enum { SEP_POINTS = 0, SEP_FACE_A = 1, SEP_FACE_B = 2 };
+typedef struct { int type; v2 axis; v2 lp; } sepfn;
+typedef struct { real dist; int ia, ib; } lenidx;
+
+static sepfn separation_scenario(const scache* c, const dproxy* A, xf_t xfA, const dproxy* B, xf_t xfB) {
+    sepfn f;
+    memset(&f, 0, sizeof(f));
+    const int type = (c->n < 2) ? SEP_POINTS : ((c->ia[0] == c->ia[1]) ? SEP_FACE_B : SEP_FACE_A);
+    if (type == SEP_FACE_B) {
+        const v2 lB1 = B->v[c->ib[0]], lB2 = B->v[c->ib[1]];
+        const v2 axis = unit_vector(fwdperp(vsub(lB2, lB1)), V(R(0), R(0)));
+        const v2 normal = urotate(axis, xfB.q);
+        const v2 lp = vdiv(vadd(lB1, lB2), R(2));
+        const v2 pB = xform(lp, xfB);
+        const v2 pA = xform(A->v[c->ia[0]], xfA);
+        f.type = SEP_FACE_B; f.lp = lp;
+        f.axis = (dot(vsub(pA, pB), normal) < R(0)) ? vneg(axis) : axis;
+        return f;
+    }
+    if (type == SEP_FACE_A) {
+        const v2 lA1 = A->v[c->ia[0]], lA2 = A->v[c->ia[1]];
+        const v2 axis = unit_vector(fwdperp(vsub(lA2, lA1)), V(R(0), R(0)));
+        const v2 normal = urotate(axis, xfA.q);
+        const v2 lp = vdiv(vadd(lA1, lA2), R(2));
+        const v2 pA = xform(lp, xfA);
+        const v2 pB = xform(B->v[c->ib[0]], xfB);
+        f.type = SEP_FACE_A; f.lp = lp;
+        f.axis = (dot(vsub(pB, pA), normal) < R(0)) ? vneg(axis) : axis;
+        return f;
+    }
+    const v2 pA = xform(A->v[c->ia[0]], xfA);
+    const v2 pB = xform(B->v[c->ib[0]], xfB);
+    f.type = SEP_POINTS;
+    f.axis = unit_vector(vsub(pB, pA), V(R(0), R(0)));
+    return f;
+}
+/* FindMinSeparation (SeparationScenario.cpp:29-77). */
+static lenidx find_min_separation(const sepfn* f, const dproxy* A, xf_t xfA, const dproxy* B, xf_t xfB) {
+    lenidx r;
+    if (f->type == SEP_POINTS) {
+        const v2 dirA = invrotate(f->axis, xfA.q);
+        const v2 dirB = invrotate(vneg(f->axis), xfB.q);
+        r.ia = support_index(A, dirA);
+        r.ib = support_index(B, dirB);
+        const v2 delta = vsub(xform(B->v[r.ib], xfB), xform(A->v[r.ia], xfA));
+        r.dist = dot(delta, f->axis);
+    } else if (f->type == SEP_FACE_A) {
+        const v2 normal = urotate(f->axis, xfA.q);
+        const v2 pA = xform(f->lp, xfA);
+        r.ia = 255;
+        r.ib = support_index(B, invrotate(vneg(normal), xfB.q));
+        const v2 delta = vsub(xform(B->v[r.ib], xfB), pA);
+        r.dist = dot(delta, normal);
+    } else {
+        const v2 normal = urotate(f->axis, xfB.q);
+        r.ia = support_index(A, invrotate(vneg(normal), xfA.q));
+        r.ib = 255;
+        const v2 pB = xform(f->lp, xfB);
+        const v2 delta = vsub(xform(A->v[r.ia], xfA), pB);
+        r.dist = dot(delta, normal);
+    }
+    return r;
+}
+/* Evaluate (SeparationScenario.cpp:79-119). */
+static real sep_evaluate(const sepfn* f, const dproxy* A, xf_t xfA, const dproxy* B, xf_t xfB, int ia, int ib) {
+    if (f->type == SEP_POINTS) {
+        const v2 delta = vsub(xform(B->v[ib], xfB), xform(A->v[ia], xfA));
+        return dot(delta, f->axis);
+    }
+    if (f->type == SEP_FACE_A) {
+        const v2 normal = urotate(f->axis, xfA.q);
+        const v2 pA = xform(f->lp, xfA);
+        const v2 delta = vsub(xform(B->v[ib], xfB), pA);
+        return dot(delta, normal);
+    }
+    const v2 normal = urotate(f->axis, xfB.q);
+    const v2 pB = xform(f->lp, xfB);
+    const v2 delta = vsub(xform(A->v[ia], xfA), pB);
+    return dot(delta, normal);
+}
+
+/* ToiOutput::State (ToiOutput.hpp). */
+enum {
+    TOI_UNKNOWN = 0, TOI_OVERLAPPED, TOI_TOUCHING, TOI_SEPARATED, TOI_MAX_ROOT_ITERS, TOI_NEXT_AFTER,
+    TOI_MAX_TOI_ITERS, TOI_BELOW_MIN_TARGET, TOI_MAX_DIST_ITERS, TOI_TARGET_DEPTH_EXCEEDS_TOTAL_RADIUS,
+    TOI_MIN_TARGET_SQUARED_OVERFLOW, TOI_MAX_TARGET_SQUARED_OVERFLOW, TOI_NOT_FINITE
+};
+typedef struct { real time; int state, toi_iters, max_dist_iters, max_root_iters; } toi_out;
+
+/* GetToiViaSat (TimeOfImpact.cpp:37-253). */
+static toi_out toi_via_sat(const dproxy* A, const sweep_t* sA, const dproxy* B, const sweep_t* sB,
+                           const or_stepconf* conf) {
+    toi_out o;
+    memset(&o, 0, sizeof(o));
+    const real totalRadius = A->r + B->r;
+    if (conf->targetDepth > totalRadius) { o.state = TOI_TARGET_DEPTH_EXCEEDS_TOTAL_RADIUS; return o; }
+    const real target = totalRadius - conf->targetDepth;
+    const real maxTarget = maxr(target + conf->tolerance, R(0));
+    const real minTarget = maxr(target - conf->tolerance, R(0));
+    const real minTargetSquared = minTarget * minTarget;
+    if (!isfinite(minTargetSquared) && isfinite(minTarget)) { o.state = TOI_MIN_TARGET_SQUARED_OVERFLOW; return o; }
+    const real maxTargetSquared = maxTarget * maxTarget;
+    if (!isfinite(maxTargetSquared) && isfinite(maxTarget)) { o.state = TOI_MAX_TARGET_SQUARED_OVERFLOW; return o; }
+    real timeLo = R(0);
+    xf_t loA = sweep_xf(sA, timeLo), loB = sweep_xf(sB, timeLo);
+    scache cache;
+    memset(&cache, 0, sizeof(cache));
+    while (o.toi_iters < conf->maxToiIters) {
+        const dist_out di = gjk_distance(A, loA, B, loB, &cache, conf->maxDistanceIters);
+        ++o.toi_iters;
+        if (di.iters > o.max_dist_iters) o.max_dist_iters = di.iters;
+        if (di.state == DIST_HITMAX) { o.time = timeLo; o.state = TOI_MAX_DIST_ITERS; return o; }
+        /* Simplex::GetCache (Simplex.hpp:156-159) */
+        cache.n = di.s.n;
+        for (int k = 0; k < di.s.n; ++k) { cache.ia[k] = di.s.e[k].iA; cache.ib[k] = di.s.e[k].iB; }
+        cache.metric = simplex_metric(di.s.e, di.s.n);
+        v2 wA, wB;
+        witness_points(&di.s, &wA, &wB);
+        const real distSquared = mag2(vsub(wB, wA));
+        if (distSquared < minTargetSquared) { o.time = timeLo; o.state = TOI_OVERLAPPED; return o; }
+        if (distSquared <= maxTargetSquared) { o.time = timeLo; o.state = TOI_TOUCHING; return o; }
+        const sepfn fcn = separation_scenario(&cache, A, loA, B, loB);
+        real timeHi = R(1); /* conf.timeMax */
+        xf_t hiA = sweep_xf(sA, timeHi), hiB = sweep_xf(sB, timeHi);
+        for (int pb = 0; pb < 254; ++pb) { /* MaxShapeVertices */
+            const lenidx hs = find_min_separation(&fcn, A, hiA, B, hiB);
+            if (hs.dist > maxTarget) { o.time = timeHi; o.state = TOI_SEPARATED; return o; }
+            if (hs.dist >= minTarget) {
+                if (timeHi == timeLo) { o.time = timeHi; o.state = TOI_SEPARATED; return o; }
+                timeLo = timeHi; loA = hiA; loB = hiB;
+                break;
+            }
+            const real loEval = sep_evaluate(&fcn, A, loA, B, loB, hs.ia, hs.ib);
+            if (loEval <= maxTarget) {
+                o.time = timeLo; o.state = (loEval < minTarget) ? TOI_BELOW_MIN_TARGET : TOI_TOUCHING;
+                return o;
+            }
+            real a1 = timeLo, a2 = timeHi, s1 = loEval, s2 = hs.dist;
+            int roots = 0;
+            real t = timeLo;
+            for (;;) {
+                if (roots == conf->maxToiRootIters) {
+                    if (roots > o.max_root_iters) o.max_root_iters = roots;
+                    o.time = t; o.state = TOI_MAX_ROOT_ITERS; return o;
+                }
+                if (RNEXT(a1, a2) >= a2) {
+                    if (roots > o.max_root_iters) o.max_root_iters = roots;
+                    o.time = t; o.state = TOI_NEXT_AFTER; return o;
+                }
+                /* Secant / Bisect (Math.hpp:92-108) */
+                t = (roots & 1) ? (a1 + (target - s1) * (a2 - a1) / (s2 - s1)) : ((a1 + a2) / R(2));
+                ++roots;
+                const xf_t tA = sweep_xf(sA, t), tB = sweep_xf(sB, t);
+                const real sv = sep_evaluate(&fcn, A, tA, B, tB, hs.ia, hs.ib);
+                if (fabs(sv - target) <= conf->tolerance) {
+                    timeHi = t; hiA = tA; hiB = tB;
+                    break;
+                }
+                if (sv > target) { a1 = t; s1 = sv; } else { a2 = t; s2 = sv; }
+            }
+            if (roots > o.max_root_iters) o.max_root_iters = roots;
+        }
+    }
+    o.time = timeLo;
+    o.state = TOI_MAX_TOI_ITERS;
+    return o;
+}
+
+/* AabbTreeWorld::UpdateContactTOIs (AabbTreeWorld.cpp:1685-1750). */
+static void update_contact_tois(or_world* w, const or_stepconf* conf, or_stepstats* st) {
+    for (int i = 0; i < w->wcids.n; ++i) {
+        contact_t* c = &w->c[w->wcids.a[i]];
+        if (c->toiValid) continue;
+        if (c->sensor || !c->impenetrable) continue;
+        if (c->toiCount >= conf->maxSubSteps) { st->toiContactsAtMaxSubSteps++; continue; }
+        body_t* bA = &w->b[c->bA];
+        body_t* bB = &w->b[c->bB];
+        if (!(bA->flags & BF_AWAKE) && !(bB->flags & BF_AWAKE)) continue;
+        const real alpha0 = maxr(bA->alpha0, bB->alpha0);
+        body_advance0(bA, alpha0);
+        body_advance0(bB, alpha0);
+        const sweep_t sA = sweep_normalized(body_sweep(bA));
+        const sweep_t sB = sweep_normalized(body_sweep(bB));
+        const toi_out o = toi_via_sat(&w->s[c->sA].dp, &sA, &w->s[c->sB].dp, &sB, conf);
+        c->toi = (o.state == TOI_TOUCHING) ? minr(alpha0 + (R(1) - alpha0) * o.time, R(1)) : R(1);
+        c->toiValid = 1;
+        if (o.max_dist_iters > st->toiMaxDistIters) st->toiMaxDistIters = o.max_dist_iters;
+        if (o.toi_iters > st->toiMaxToiIters) st->toiMaxToiIters = o.toi_iters;
+        if (o.max_root_iters > st->toiMaxRootIters) st->toiMaxRootIters = o.max_root_iters;
+        st->toiContactsUpdatedToi++;
+    }
+}
+
+/* FlagForUpdating(contacts of a body) (AabbTreeWorld.cpp). */
+static void flag_body_contacts(or_world* w, const body_t* b) {
+    for (int k = 0; k < b->cids.n; ++k) w->c[b->cids.a[k]].needsUpdate = 1;
+}
+
+/* AabbTreeWorld::SolveToiViaGS (AabbTreeWorld.cpp:1957-2059). */
+static void solve_toi_island(or_world* w, const or_stepconf* conf, island_t* isl, or_stepstats* st,
+                             int* posIters, int* velIters) {
+    bc_t* bcs = (bc_t*)calloc((size_t)w->nb + 1, sizeof(bc_t));
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        const int id = (int)isl->bodies.a[i];
+        make_bc(&bcs[id], &w->b[id], R(0), conf);
+    }
+    const int nc = isl->contacts.n;
+    pc_t* pcs = (pc_t*)malloc(sizeof(pc_t) * (size_t)(nc + 1));
+    vc_t* vcs = (vc_t*)malloc(sizeof(vc_t) * (size_t)(nc + 1));
+    for (int i = 0; i < nc; ++i) {
+        const contact_t* c = &w->c[isl->contacts.a[i]];
+        pcs[i].m = &c->m; pcs[i].bA = c->bA; pcs[i].bB = c->bB;
+        pcs[i].totalRadius = w->s[c->sA].dp.r + w->s[c->sB].dp.r;
+    }
+    /* GetToiConstraintSolverConf (ConstraintSolverConf.cpp:37-45) */
+    or_stepconf ps = *conf;
+    ps.regResolutionRate = conf->toiResolutionRate;
+    real minSepAll = RINF;
+    int solved = 0;
+    *posIters = conf->toiPositionIters;
+    for (int it = 0; it < conf->toiPositionIters; ++it) {
+        real minSep = RINF;
+        for (int i = 0; i < nc; ++i) minSep = minr(minSep, solve_pc(&pcs[i], bcs, &ps));
+        minSepAll = minr(minSepAll, minSep);
+        if (minSep >= conf->toiMinSeparation) { *posIters = it + 1; solved = 1; break; }
+    }
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        const int id = (int)isl->bodies.a[i];
+        w->b[id].pos0 = bcs[id].pos; /* SetPosition0: the sweep only */
+    }
+    /* GetToiVelocityConstraintConf (VelocityConstraint.cpp:207-210): dtRatio 0 */
+    or_stepconf vcf = *conf;
+    vcf.dtRatio = R(0);
+    for (int i = 0; i < nc; ++i) {
+        const contact_t* c = &w->c[isl->contacts.a[i]];
+        const bc_t* A = &bcs[c->bA];
+        const bc_t* B = &bcs[c->bB];
+        const real rA = w->s[c->sA].dp.r, rB = w->s[c->sB].dp.r;
+        const wman_t wm = world_manifold(&c->m, get_xf(A->pos, A->lc), rA, get_xf(B->pos, B->lc), rB);
+        make_vc(&vcs[i], c, &wm, bcs, &vcf);
+    }
+    real maxInc = R(0);
+    *velIters = conf->toiVelocityIters;
+    for (int it = 0; it < conf->toiVelocityIters; ++it) {
+        real newInc = R(0);
+        for (int i = 0; i < nc; ++i) newInc = maxr(newInc, solve_vc(&vcs[i], bcs));
+        if (newInc <= conf->toiMinMomentum) { *velIters = it + 1; break; }
+        maxInc = maxr(maxInc, newInc);
+    }
+    const real h = conf->deltaTime;
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        bc_t* bc = &bcs[isl->bodies.a[i]];
+        const v2 tr = vmul(bc->vel.lin, h);
+        const real rot = h * bc->vel.ang;
+        bc->pos.lin = vadd(bc->pos.lin, tr);
+        bc->pos.ang = bc->pos.ang + rot;
+    }
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        const int id = (int)isl->bodies.a[i];
+        body_t* b = &w->b[id];
+        b->vel = bcs[id].vel;
+        if (pos_ne(b->pos1, bcs[id].pos)) {
+            body_set_pos1(b, bcs[id].pos);
+            flag_body_contacts(w, b);
+        }
+    }
+    if (solved) st->toiIslandsSolved++;
+    st->toiMinSeparation = minr(st->toiMinSeparation, minSepAll);
+    st->toiMaxIncImpulse = maxr(st->toiMaxIncImpulse, maxInc);
+    free(pcs); free(vcs); free(bcs);
+}
+
+/* AabbTreeWorld::ProcessContactsForTOI (AabbTreeWorld.cpp:2061-2142). */
+static void process_contacts_for_toi(or_world* w, int id, island_t* isl, real toi, const or_stepconf* conf,
+                                     int* updated, int* skipped) {
+    body_t* body = &w->b[id];
+    const int bodyImpenetrable = is_impenetrable(body);
+    for (int k = 0; k < w->b[id].cids.n; ++k) {
+        const int cid = (int)w->b[id].cids.a[k];
+        contact_t* c = &w->c[cid];
+        if (c->islanded || c->sensor) continue;
+        const int otherId = (c->bA == id) ? c->bB : c->bA;
+        body_t* other = &w->b[otherId];
+        if (!(bodyImpenetrable || is_impenetrable(other))) continue;
+        const int otherIslanded = other->islanded;
+        const sweep_t backup = body_sweep(other);
+        if (!otherIslanded) {
+            body_advance(other, toi);
+            if (pos_ne(other->pos0, backup.p0) || pos_ne(other->pos1, backup.p1)) flag_body_contacts(w, other);
+        }
+        if (c->needsUpdate) { contact_update(w, cid, conf); ++*updated; }
+        else ++*skipped;
+        if (!c->touching) { body_set_sweep(other, backup); continue; }
+        iv_push(&isl->contacts, cid);
+        c->islanded = 1;
+        if (!otherIslanded) {
+            if (is_speedable(other)) other->flags |= BF_AWAKE;
+            iv_push(&isl->bodies, otherId);
+            other->islanded = 1;
+        }
+    }
+}
+
+/* AabbTreeWorld::SolveToi(ContactID, StepConf) (AabbTreeWorld.cpp:1833-1955). */
+static void solve_toi_contact(or_world* w, int cid, const or_stepconf* conf, island_t* isl, or_stepstats* st) {
+    contact_t* c = &w->c[cid];
+    const real toi = c->toi;
+    const int idA = c->bA, idB = c->bB;
+    body_t* bA = &w->b[idA];
+    body_t* bB = &w->b[idB];
+    int updated = 0, skipped = 0;
+    {
+        const sweep_t backupA = body_sweep(bA), backupB = body_sweep(bB);
+        body_advance(bA, toi);
+        if (pos_ne(bA->pos0, backupA.p0) || pos_ne(bA->pos1, backupA.p1)) flag_body_contacts(w, bA);
+        body_advance(bB, toi);
+        if (pos_ne(bB->pos0, backupB.p0) || pos_ne(bB->pos1, backupB.p1)) flag_body_contacts(w, bB);
+        if (c->needsUpdate) { contact_update(w, cid, conf); ++updated; }
+        c->toiValid = 0;
+        c->toiCount++;
+        if (!c->touching) {
+            body_set_sweep(bA, backupA);
+            body_set_sweep(bB, backupB);
+            st->toiContactsUpdatedTouching += updated;
+            st->toiContactsSkippedTouching += updated ? 0 : 1;
+            return;
+        }
+    }
+    if (is_speedable(bA)) bA->flags |= BF_AWAKE;
+    if (is_speedable(bB)) bB->flags |= BF_AWAKE;
+    isl->bodies.n = isl->contacts.n = isl->joints.n = 0;
+    bA->islanded = 1; bB->islanded = 1; c->islanded = 1;
+    iv_push(&isl->bodies, idA);
+    iv_push(&isl->bodies, idB);
+    iv_push(&isl->contacts, cid);
+    if (is_accelerable(bA)) process_contacts_for_toi(w, idA, isl, toi, conf, &updated, &skipped);
+    if (is_accelerable(bB)) process_contacts_for_toi(w, idB, isl, toi, conf, &updated, &skipped);
+    /* RemoveUnspeedablesFromIslanded */
+    for (int i = 0; i < isl->bodies.n; ++i) {
+        body_t* b = &w->b[isl->bodies.a[i]];
+        if (!is_speedable(b)) b->islanded = 0;
+    }
+    or_stepconf sub = *conf;
+    sub.deltaTime = (R(1) - toi) * conf->deltaTime;
+    int posIters = 0, velIters = 0;
+    solve_toi_island(w, &sub, isl, st, &posIters, &velIters);
+    st->toiSumPosIters += posIters;
+    st->toiSumVelIters += velIters;
+    if (posIters > 0 || velIters > 0) st->toiIslandsFound++;
+    st->toiContactsUpdatedTouching += updated;
+    st->toiContactsSkippedTouching += skipped;
+}
+
+/* AabbTreeWorld::SolveToi(StepConf) (AabbTreeWorld.cpp:1752-1831), no sub-stepping. */
+static void solve_toi(or_world* w, const or_stepconf* conf, or_stepstats* st) {
+    island_t isl;
+    memset(&isl, 0, sizeof(isl));
+    for (;;) {
+        update_contact_tois(w, conf, st);
+        /* GetSoonestContact (AabbTreeWorld.cpp:2870-2890) */
+        int next = -1;
+        real minToi = R(1);
+        for (int i = 0; i < w->wcids.n; ++i) {
+            const contact_t* c = &w->c[w->wcids.a[i]];
+            if (c->toiValid && minToi > c->toi) { minToi = c->toi; next = (int)w->wcids.a[i]; }
+        }
+        if (next < 0) {
+            for (int id = 0; id < w->nb; ++id) { w->b[id].alpha0 = R(0); w->b[id].islanded = 0; }
+            for (int i = 0; i < w->wcids.n; ++i) {
+                contact_t* c = &w->c[w->wcids.a[i]];
+                c->toiValid = 0; c->toiCount = 0; c->islanded = 0;
+            }
+            break;
+        }
+        st->toiContactsFound++;
+        if (!w->c[next].islanded) solve_toi_contact(w, next, conf, &isl, st);
+        for (int id = 0; id < w->nb; ++id) {
+            body_t* b = &w->b[id];
+            if (!b->islanded) continue;
+            b->islanded = 0;
+            if (is_accelerable(b)) {
+                st->toiProxiesMoved += synchronize(w, id, conf);
+                for (int k = 0; k < b->cids.n; ++k) {
+                    contact_t* c = &w->c[b->cids.a[k]];
+                    c->toiValid = 0;
+                    c->islanded = 0;
+                }
+            }
+        }
+        st->toiContactsAdded += find_and_add_contacts(w, conf);
+    }
+    {
+        const int upd = update_contacts(w, conf); /* UpdateContacts: updated and skipped counts */
+        st->toiContactsUpdatedTouching += upd;
+        st->toiContactsSkippedTouching += w->wcids.n - upd;
+    }
+    iv_free(&isl.bodies); iv_free(&isl.contacts); iv_free(&isl.joints);
+}
+
+/* Stand-alone entry points for known-answer tests. */
+static void load_dproxy(dproxy* p, int n, const real* xy, real r) {
+    memset(p, 0, sizeof(*p));
+    p->count = n > OR_MAXV ? OR_MAXV : n;
+    p->r = r;
+    for (int i = 0; i < p->count; ++i) p->v[i] = V(xy[2 * i], xy[2 * i + 1]);
+    make_normals(p);
+}
+real or_time_of_impact(int kindA, int nA, const real* xyA, real rA, const real* sweepA7, const real* lcA2,
+                       int kindB, int nB, const real* xyB, real rB, const real* sweepB7, const real* lcB2,
+                       const or_stepconf* conf, int* iout4) {
+    (void)kindA; (void)kindB;
+    dproxy a, b;
+    load_dproxy(&a, nA, xyA, rA);
+    load_dproxy(&b, nB, xyB, rB);
+    sweep_t sa, sb;
+    sa.p0.lin = V(sweepA7[0], sweepA7[1]); sa.p0.ang = sweepA7[2];
+    sa.p1.lin = V(sweepA7[3], sweepA7[4]); sa.p1.ang = sweepA7[5]; sa.a0 = sweepA7[6];
+    sa.lc = V(lcA2[0], lcA2[1]);
+    sb.p0.lin = V(sweepB7[0], sweepB7[1]); sb.p0.ang = sweepB7[2];
+    sb.p1.lin = V(sweepB7[3], sweepB7[4]); sb.p1.ang = sweepB7[5]; sb.a0 = sweepB7[6];
+    sb.lc = V(lcB2[0], lcB2[1]);
+    const toi_out o = toi_via_sat(&a, &sa, &b, &sb, conf);
+    iout4[0] = o.state; iout4[1] = o.toi_iters; iout4[2] = o.max_dist_iters; iout4[3] = o.max_root_iters;
+    return o.time;
+}
+void or_distance(int kindA, int nA, const real* xyA, real rA, const real* xfA4, int kindB, int nB,
+                 const real* xyB, real rB, const real* xfB4, int maxIters, int* iout3, real* fout4) {
+    (void)kindA; (void)kindB;
+    dproxy a, b;
+    load_dproxy(&a, nA, xyA, rA);
+    load_dproxy(&b, nB, xyB, rB);
+    xf_t xa, xb;
+    xa.p = V(xfA4[0], xfA4[1]); xa.q = V(xfA4[2], xfA4[3]);
+    xb.p = V(xfB4[0], xfB4[1]); xb.q = V(xfB4[2], xfB4[3]);
+    scache cache;
+    memset(&cache, 0, sizeof(cache));
+    const dist_out d = gjk_distance(&a, xa, &b, xb, &cache, maxIters);
+    v2 pA, pB;
+    witness_points(&d.s, &pA, &pB);
+    iout3[0] = d.state; iout3[1] = d.iters; iout3[2] = d.s.n;
+    fout4[0] = pA.x; fout4[1] = pA.y; fout4[2] = pB.x; fout4[3] = pB.y;
+}
+
+/* Step(AabbTreeWorld&, StepConf) (AabbTreeWorld.cpp:2144-2219). */
 void or_step(or_world* w, const or_stepconf* conf, or_stepstats* st) {
     or_stepstats local;
     if (!st) st = &local;
@@ -1799,9 +2456,11 @@ void or_step(or_world* w, const or_stepconf* conf, or_stepstats* st) {
     st->preContactsDestroyed = destroy_contacts(w);
     st->preContactsUpdated = update_contacts(w, conf);
     st->preContactsAdded = find_and_add_contacts(w, conf);
+    st->toiMinSeparation = RINF;
     if (conf->deltaTime != R(0)) {
         w->inv_dt0 = R(1) / conf->deltaTime;
         solve_reg(w, conf, st);
+        if (conf->doToi) solve_toi(w, conf, st);
     }
 }
 
@@ -1832,6 +2491,18 @@ void or_default_conf(or_stepconf* c) {
     c->regPositionIters = 3;
     c->doWarmStart = 1;
     c->doBlocksolve = 1;
+    c->toiResolutionRate = R(75) / R(100);
+    c->toiMinSeparation = -linearSlop * R(1.5f);
+    c->toiMinMomentum = R(0) / R(100);
+    c->targetDepth = linearSlop * R(3);
+    c->tolerance = linearSlop / R(4);
+    c->toiVelocityIters = 8;
+    c->toiPositionIters = 20;
+    c->maxToiRootIters = 30;
+    c->maxToiIters = 20;
+    c->maxDistanceIters = 20;
+    c->maxSubSteps = 8;
+    c->doToi = 0; /* the reference's default is true; callers opt in */
 }
 
 /* ------------------------------------------------------------------------- */

@@ -39,9 +39,11 @@ enum {
     OR_BF_AWAKE = 2u,
     OR_BF_FIXED_ROTATION = 4u,
     OR_BF_ENABLED = 8u,
+    OR_BF_BULLET = 16u, /* BodyConf::bullet: the body is impenetrable (TOI against every body) */
 };
 
-/* Mirrors the StepConf fields the regular phase reads (StepConf.hpp:165-340). */
+/* Mirrors the StepConf fields the step reads (StepConf.hpp:165-392): the
+ * regular phase's, then the TOI phase's. */
 typedef struct or_stepconf {
     or_real deltaTime, dtRatio, minStillTimeToSleep, linearSlop, angularSlop;
     or_real regResolutionRate, regMinSeparation, regMinMomentum, velocityThreshold;
@@ -49,6 +51,9 @@ typedef struct or_stepconf {
     or_real linearSleepTolerance, angularSleepTolerance, displaceMultiplier;
     or_real aabbExtension, maxCirclesRatio;
     int regVelocityIters, regPositionIters, doWarmStart, doBlocksolve;
+    or_real toiResolutionRate, toiMinSeparation, toiMinMomentum, targetDepth, tolerance;
+    int toiVelocityIters, toiPositionIters, maxToiRootIters, maxToiIters, maxDistanceIters;
+    int maxSubSteps, doToi;
 } or_stepconf;
 
 /* Subset of StepStats (StepStats.hpp:41-191) the oracle counts. */
@@ -57,6 +62,12 @@ typedef struct or_stepstats {
     int preContactsUpdated, regIslandsFound, regIslandsSolved, regContactsAdded;
     int regContactsUpdated, regProxiesMoved, regBodiesSlept, regSumPosIters, regSumVelIters;
     or_real regMinSeparation, regMaxIncImpulse;
+    /* ToiStepStats (StepStats.hpp:117-151) */
+    int toiIslandsFound, toiIslandsSolved, toiContactsFound, toiContactsAtMaxSubSteps;
+    int toiContactsUpdatedToi, toiContactsUpdatedTouching, toiContactsSkippedTouching;
+    int toiContactsAdded, toiProxiesMoved, toiSumPosIters, toiSumVelIters;
+    int toiMaxDistIters, toiMaxToiIters, toiMaxRootIters;
+    or_real toiMinSeparation, toiMaxIncImpulse;
 } or_stepstats;
 
 typedef struct or_world or_world;
@@ -82,6 +93,7 @@ int or_add_revolute(or_world* w, int bodyA, int bodyB, or_real lax, or_real lay,
                     or_real lower, or_real upper, int enableMotor, or_real motorSpeed,
                     or_real maxMotorTorque, int collideConnected);
 
+/* StepConf defaults, except doToi = 0: callers ask for the TOI phase explicitly. */
 void or_default_conf(or_stepconf* conf);
 void or_step(or_world* w, const or_stepconf* conf, or_stepstats* stats);
 
@@ -112,6 +124,20 @@ void or_collide(int kindA, int nA, const or_real* xyA, or_real rA, const or_real
                 int kindB, int nB, const or_real* xyB, or_real rB, const or_real* xfB4,
                 or_real linearSlop, or_real maxCirclesRatio,
                 int* type_count2, int* feat8, or_real* fout8);
+
+/* Stand-alone GetToiViaSat (TimeOfImpact.cpp:37-253) for two shapes moving over
+ * sweeps sweepN[7] = pos0.x pos0.y pos0.a pos1.x pos1.y pos1.a alpha0 with the
+ * body's local centre lcN[2].  conf supplies targetDepth, tolerance and the
+ * iteration limits.  iout: state toi_iters max_dist_iters max_root_iters;
+ * returns the time (unit interval). */
+or_real or_time_of_impact(int kindA, int nA, const or_real* xyA, or_real rA, const or_real* sweepA7,
+                          const or_real* lcA2, int kindB, int nB, const or_real* xyB, or_real rB,
+                          const or_real* sweepB7, const or_real* lcB2, const or_stepconf* conf, int* iout4);
+/* Stand-alone Distance (Distance.cpp:96-196) from an empty cache: iout: state
+ * iterations simplex-size; fout: witness point A.xy, witness point B.xy. */
+void or_distance(int kindA, int nA, const or_real* xyA, or_real rA, const or_real* xfA4,
+                 int kindB, int nB, const or_real* xyB, or_real rB, const or_real* xfB4,
+                 int maxIters, int* iout3, or_real* fout4);
 
 #ifdef __cplusplus
 }

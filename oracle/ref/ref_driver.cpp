@@ -6,6 +6,7 @@
 // Input (stdin), one record per line:
 //   conf <StepConf field> <value> ...        overrides of StepConf defaults
 //   body type px py angle vx vy av ax ay aa linDamp angDamp flags
+//        (flags: 1 allow sleep, 2 awake, 4 fixed rotation, 8 enabled, 16 bullet)
 //   shape body kind nverts radius density friction restitution cat mask group sensor x0 y0 ...
 //   joint bodyA bodyB lax lay lbx lby refAngle enableLimit lower upper enableMotor
 //         motorSpeed maxMotorTorque collideConnected
@@ -99,6 +100,15 @@ void dump(const World& world, const StepStats& st)
                 unsigned(st.reg.islandsSolved), unsigned(st.reg.contactsAdded),
                 unsigned(st.reg.bodiesSlept), unsigned(st.reg.sumPosIters), unsigned(st.reg.sumVelIters));
     hex(st.reg.minSeparation / 1_m); hex(st.reg.maxIncImpulse / 1_Ns);
+    std::printf("\n");
+    std::printf("toistats %u %u %u %u %u %u %u %u %u %u %u %u %u %u",
+                unsigned(st.toi.islandsFound), unsigned(st.toi.islandsSolved), unsigned(st.toi.contactsFound),
+                unsigned(st.toi.contactsAtMaxSubSteps), unsigned(st.toi.contactsUpdatedToi),
+                unsigned(st.toi.contactsUpdatedTouching), unsigned(st.toi.contactsSkippedTouching),
+                unsigned(st.toi.contactsAdded), unsigned(st.toi.proxiesMoved), unsigned(st.toi.sumPosIters),
+                unsigned(st.toi.sumVelIters), unsigned(st.toi.maxDistIters), unsigned(st.toi.maxToiIters),
+                unsigned(st.toi.maxRootIters));
+    hex(st.toi.minSeparation / 1_m); hex(st.toi.maxIncImpulse / 1_Ns);
     std::printf("\n");
     const auto nb = GetBodyRange(world);
     for (auto i = decltype(nb){0}; i < nb; ++i) {
@@ -201,6 +211,7 @@ int main()
             bc.UseAwake((flags & 2u) != 0);
             bc.UseFixedRotation((flags & 4u) != 0);
             bc.UseEnabled((flags & 8u) != 0);
+            bc.UseBullet((flags & 16u) != 0);
             CreateBody(world, bc);
         }
         else if (tag == "shape") {

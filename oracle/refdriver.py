@@ -26,7 +26,8 @@ def driver_path(double: bool = False) -> str:
 
 def ensure_built(double: bool = False) -> str:
     path = driver_path(double)
-    if not os.path.exists(path):
+    if os.path.isdir(os.path.join(REF_SRC, "Library")) or not os.path.exists(path):
+        # make relinks the driver when oracle/ref/ref_driver.cpp changed
         subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "-j8",
                         "f64" if double else "f32", f"REF={REF_SRC}"], check=True)
     return path
@@ -50,6 +51,8 @@ def run(scene_text: str, steps, double: bool = False, timeout: float = 600.0):
         if t[0] == "stats":
             cur = {"stats": [int(x) for x in t[1:10]] + [_f(x) for x in t[10:12]],
                    "bodies": [], "proxies": [], "contacts": []}
+        elif t[0] == "toistats":
+            cur["toistats"] = [int(x) for x in t[1:15]] + [_f(x) for x in t[15:17]]
         elif t[0] == "body":
             cur["bodies"].append([_f(x) for x in t[2:15]] + [int(t[15])])
         elif t[0] == "proxy":
@@ -83,4 +86,5 @@ def _finish(d, double):
                 "touching": io[:, 10], "type": io[:, 11], "count": io[:, 12], "local_normal": fo[:, 0:2],
                 "local_point": fo[:, 2:4], "points": fo[:, 4:12].reshape(n, 2, 4),
                 "features": ft.reshape(n, 2, 4)}
-    return {"stats": d["stats"], "bodies": bodies, "proxies": proxies, "contacts": contacts}
+    return {"stats": d["stats"], "toistats": d.get("toistats"), "bodies": bodies, "proxies": proxies,
+            "contacts": contacts}

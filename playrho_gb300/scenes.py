@@ -24,8 +24,8 @@ F32 = np.float32
 
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 DISK, POLYGON, EDGE = 0, 1, 2
-# Body flags (BodyConf booleans): allowSleep, awake, fixedRotation, enabled.
-BF_ALLOW_SLEEP, BF_AWAKE, BF_FIXED_ROTATION, BF_ENABLED = 1, 2, 4, 8
+# Body flags (BodyConf booleans): allowSleep, awake, fixedRotation, enabled, bullet.
+BF_ALLOW_SLEEP, BF_AWAKE, BF_FIXED_ROTATION, BF_ENABLED, BF_BULLET = 1, 2, 4, 8, 16
 BF_DEFAULT = BF_ALLOW_SLEEP | BF_AWAKE | BF_ENABLED
 
 DEFAULT_LINEAR_SLOP = F32(0.005)
@@ -446,6 +446,30 @@ def pile(n_bodies: int, rng, friction=0.6, density=1.0, width=None) -> Scene:
     nverts = rng.integers(3, 9, n)
     return _assemble([((-w, 0.0), (w, 0.0))], x, y, np.zeros(n), None, radius, is_disk, nverts,
                      np.full(n, density), friction, rng)
+
+
+def bullets(n_bodies: int, rng, size: float = 20.0, speed=(60.0, 180.0), bullet_frac: float = 0.5,
+            gravity: bool = True) -> Scene:
+    """Fast disks and 3..8-gons (bounding radius U[0.1,0.4]) inside a square of side 2*size
+    closed by 4 static edges, moving in random directions at U[speed] m/s (1..3 m a
+    1/60 s step, more than their own size): without time-of-impact sub-stepping most
+    pass through the walls.  A fraction `bullet_frac` are bullets (BodyConf::bullet),
+    which also sub-step against the other moving bodies."""
+    h = size
+    n = n_bodies
+    is_disk = rng.integers(0, 2, n).astype(bool)
+    radius = rng.uniform(0.1, 0.4, n)
+    x, y = _jittered_positions(rng, n, -h + 1.0, h - 1.0, -h + 1.0, h - 1.0, 1.0, radius)
+    ang = rng.uniform(0.0, 2.0 * math.pi, n)
+    sp = rng.uniform(speed[0], speed[1], n)
+    vel = np.stack([sp * np.cos(ang), sp * np.sin(ang), rng.normal(0.0, 2.0, n)], -1)
+    nverts = rng.integers(3, 9, n)
+    edges = [((-h, -h), (h, -h)), ((h, -h), (h, h)), ((h, h), (-h, h)), ((-h, h), (-h, -h))]
+    sc = _assemble(edges, x, y, rng.uniform(-math.pi, math.pi, n), vel, radius, is_disk, nverts,
+                   np.full(n, 1.0), 0.3, rng, acc=GRAVITY if gravity else (0.0, 0.0, 0.0))
+    bullet = rng.uniform(0.0, 1.0, n) < bullet_frac
+    sc.body_flags[1:][bullet] |= np.uint32(BF_BULLET)
+    return sc
 
 
 def batched_worlds(n_worlds: int = 4096, seed: int = 1, lo: int = 16, hi: int = 2048) -> List[Scene]:

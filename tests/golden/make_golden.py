@@ -7,7 +7,7 @@ FP32 values kept bit-exact.  Needs the reference sources (PLAYRHO_REFERENCE,
 default /root/reference); the fixtures it writes are what the oracle is checked
 against wherever the sources are absent.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names]
 """
 from __future__ import annotations
 
@@ -44,6 +44,9 @@ def cases():
         "chains_seed3": (scenes.chains_world(np.random.default_rng(3), n_free=200, n_chains=4, links=8),
                          [1, 100], {}),
         "helloworld": (helloworld_scene(), list(range(1, 61)), {}),
+        # time-of-impact phase on (StepConf::doToi, the reference's default)
+        "toi_bullets60_seed3": (scenes.bullets(60, np.random.default_rng(3)), [1, 5, 30, 90], {"doToi": 1}),
+        "toi_pile200_seed11": (scenes.pile(200, np.random.default_rng(11)), [1, 60, 180, 300], {"doToi": 1}),
     }
 
 
@@ -52,12 +55,16 @@ def save(name, scene, steps, conf, double=False):
                           double=double)
     out = {f"scene_{k}": v for k, v in dataclasses.asdict(scene).items()}
     out["steps"] = np.asarray(steps, np.int32)
+    for k, v in conf.items():
+        out[f"conf_{k}"] = np.asarray(v)
     for i, d in enumerate(dumps):
         b, c = d["bodies"], d["contacts"]
         out[f"d{i}_pos"] = b["pos"]
         out[f"d{i}_vel"] = b["vel"]
         out[f"d{i}_awake"] = b["awake"]
         out[f"d{i}_stats"] = np.asarray(d["stats"][:9], np.int64)
+        if conf.get("doToi"):
+            out[f"d{i}_toistats"] = np.asarray(d["toistats"][:14], np.int64)
         if name != "helloworld" or i in (0, 29, 59):
             out[f"d{i}_c_proxy"] = c["proxy"]
             out[f"d{i}_c_count"] = c["count"]
@@ -70,11 +77,17 @@ def save(name, scene, steps, conf, double=False):
     print(path, os.path.getsize(path))
 
 
-def main():
+def main(names=None):
+    """Writes every fixture, or only those named on the command line."""
     for name, (scene, steps, conf) in cases().items():
-        save(name, scene, steps, conf)
-    save("pile300_seed5", scenes.pile(300, np.random.default_rng(5)), [1, 100, 300], {}, double=True)
+        if not names or name in names:
+            save(name, scene, steps, conf)
+    if not names or "pile300_seed5_f64" in names:
+        save("pile300_seed5", scenes.pile(300, np.random.default_rng(5)), [1, 100, 300], {}, double=True)
+    if not names or "toi_bullets60_seed3_f64" in names:
+        save("toi_bullets60_seed3", scenes.bullets(60, np.random.default_rng(3)), [1, 30, 90], {"doToi": 1},
+             double=True)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

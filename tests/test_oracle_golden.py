@@ -3,7 +3,8 @@
 Fixtures (tests/golden/ref_*.npz) come from tests/golden/make_golden.py, which
 runs each scene through the reference library compiled from source.  The oracle
 must reproduce them bit for bit: positions, velocities, awake flags, contact
-keys, contact features, manifold points and step statistics.  Runs without the
+keys, contact features, manifold points and step statistics (with the TOI
+phase's statistics for the fixtures that enable it).  Runs without the
 reference sources or a GPU.
 """
 import glob
@@ -29,10 +30,11 @@ def test_oracle_reproduces_reference(path):
     z = np.load(path)
     double = path.endswith("_f64.npz")
     ow = oracle.OracleWorld(load_scene(z), double=double)
+    conf = {k[len("conf_"):]: z[k].item() for k in z.files if k.startswith("conf_")}
     done = 0
     for i, s in enumerate(z["steps"]):
         while done < s:
-            st = ow.step()
+            st = ow.step(**conf)
             done += 1
         b = ow.bodies()
         np.testing.assert_array_equal(b["pos"], z[f"d{i}_pos"], err_msg=f"positions after {s} steps")
@@ -42,6 +44,9 @@ def test_oracle_reproduces_reference(path):
                                "regIslandsSolved", "regContactsAdded", "regBodiesSlept", "regSumPosIters",
                                "regSumVelIters")]
         np.testing.assert_array_equal(got, z[f"d{i}_stats"], err_msg=f"step statistics after {s} steps")
+        if f"d{i}_toistats" in z:
+            toi = [st[k] for k in oracle.TOI_STATS_INT_FIELDS]
+            np.testing.assert_array_equal(toi, z[f"d{i}_toistats"], err_msg=f"TOI statistics after {s} steps")
         if f"d{i}_c_proxy" in z:
             c = ow.contacts()
             np.testing.assert_array_equal(c["proxy"], z[f"d{i}_c_proxy"])

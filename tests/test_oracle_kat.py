@@ -132,3 +132,58 @@ def test_circle_over_right_face_of_triangle():
     assert abs(m["local_normal"][0] - 0.894427) < 2e-4 and abs(m["local_normal"][1] - 0.44721359) < 2e-4
     assert list(m["points"][0]) == [0, 0]
     assert m["features"][0][0] == 1 and m["features"][0][2] == 0 and m["features"][0][3] == 0
+
+
+# ---- GetToiViaSat (UnitTests/TimeOfImpact.cpp).  Disks are one-vertex proxies at
+# the body origin; sweeps are (pos0 x y angle, pos1 x y angle, alpha0).
+def _toi_limits(slop):
+    s = F32(slop)
+    return {"targetDepth": float(s * F32(3)), "tolerance": float(s / F32(4))}
+
+
+def _toi(rA, sA, rB, sB, verts_a=((0.0, 0.0),), verts_b=((0.0, 0.0),), **conf):
+    return oracle.time_of_impact(verts_a, rA, sA, (0.0, 0.0), verts_b, rB, sB, (0.0, 0.0), **conf)
+
+
+def test_toi_overlapped_touching_separated():
+    # TimeOfImpact.Overlapped / Touching / Separated (:157-216)
+    lim = _toi_limits(0.001)
+    t, state, iters, _, _ = _toi(1.0, (0, 0, 0, 0, 0, 0, 0), 1.0, (0, 0, 0, 0, 0, 0, 0), **lim)
+    assert (state, t, iters) == ("overlapped", 0.0, 1)
+    r = float(F32(1.0) + F32(1.5) * F32(0.001))
+    t, state, iters, _, _ = _toi(r, (0, 0, 0, 0, 0, 0, 0), r, (2, 0, 0, 2, 0, 0, 0), **lim)
+    assert (state, t, iters) == ("touching", 0.0, 1)
+    t, state, iters, _, _ = _toi(1.0, (0, 0, 0, 0, 0, 0, 0), 1.0, (4, 0, 0, 4, 0, 0, 0), **lim)
+    assert (state, t, iters) == ("separated", 1.0, 1)
+
+
+def test_toi_circles_collide():
+    # TimeOfImpact.CollideCirclesHorizontally (:218-240) and CollideCirclesVertically (:283-305)
+    lim = _toi_limits(0.001)
+    t, state, iters, _, _ = _toi(1.0, (-2, 0, 0, 0, 0, 0, 0), 1.0, (2, 0, 0, 0, 0, 0, 0), **lim)
+    approx = ((F32(2) - F32(1)) + F32(lim["targetDepth"]) / F32(2)) / F32(2)
+    assert state == "touching" and iters == 2
+    assert abs(t - float(approx)) <= 1e-6
+    t, state, iters, _, _ = _toi(1.0, (0, -20, 0, 0, 20, 0, 0), 1.0, (0, 20, 0, 0, -20, 0, 0), **lim)
+    assert state == "touching" and iters == 2
+    assert abs(t - 0.4750375) <= 1e-6
+
+
+def test_toi_parallel_paths_do_not_collide():
+    # TimeOfImpact.CirclesPassingParSepPathsDontCollide (:307-335)
+    lim = _toi_limits(0.001)
+    t, state, iters, _, _ = _toi(1.0, (-3, 1, 0, 3, 1, 0, 0), 1.0, (3, -1, 0, -3, -1, 0, 0), **lim)
+    assert state == "separated" and iters == 7
+    assert abs(t - 1.0) <= 1e-3
+
+
+def test_toi_edge_circle_touchingly():
+    # TimeOfImpact.CollideEdgeCircleTouchingly (:242-281), float build: 0.576901972
+    conf = {"targetDepth": 0.0149999997, "tolerance": 0.0, "maxToiRootIters": 30, "maxToiIters": 20,
+            "maxDistanceIters": 20}
+    t, state, iters, _, _ = oracle.time_of_impact(
+        ((-40.0, 0.0), (40.0, 0.0)), 0.00999999977, (0, 0, 0, 0, 0, 0, 0), (0.0, 0.0),
+        ((0.0, 0.0),), 0.5, (-0.490861088, 0.49556452, 1.0125972, -0.486600876, 0.494585991, 1.00495279, 0),
+        (0.0, 0.0), **conf)
+    assert state == "touching" and iters == 2
+    assert abs(t - 0.576901972) <= 1e-9

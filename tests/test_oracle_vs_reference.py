@@ -9,12 +9,14 @@ from playrho_gb300 import scenes
 pytestmark = pytest.mark.skipif(not refdriver.available(), reason="reference sources not present")
 
 
-def _compare(scene, steps, double=False):
-    dumps = refdriver.run(scenes.scene_text(scene), steps, double=double)
+def _compare(scene, steps, double=False, **conf):
+    dumps = refdriver.run(scenes.scene_text(scene, conf), steps, double=double)
     ow = oracle.OracleWorld(scene, double=double)
     for n, d in zip(steps, dumps):
         for _ in range(n):
-            ow.step()
+            st = ow.step(**conf)
+        if conf.get("doToi"):
+            assert [st[k] for k in oracle.TOI_STATS_INT_FIELDS] == d["toistats"][:14]
         b = ow.bodies()
         np.testing.assert_array_equal(b["pos"], d["bodies"]["pos"])
         np.testing.assert_array_equal(b["vel"], d["bodies"]["vel"])
@@ -41,3 +43,12 @@ def test_spinning_box():
 
 def test_chains():
     _compare(scenes.chains_world(np.random.default_rng(9), n_free=60, n_chains=3, links=6), [1, 80])
+
+
+@pytest.mark.parametrize("seed", [21, 22])
+def test_toi_bullets(seed):
+    _compare(scenes.bullets(50, np.random.default_rng(seed)), [1, 20, 60], doToi=1)
+
+
+def test_toi_pile_f64():
+    _compare(scenes.pile(120, np.random.default_rng(23)), [1, 100, 150], double=True, doToi=1)
