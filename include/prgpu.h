@@ -23,6 +23,8 @@
  *   prgpu_download_proxies      GetTree(World) leaf AABBs, World.hpp:937
  *   prgpu_convex_hull           PolygonShapeConf::Set -> GetConvexHullAsVector,
  *                               PolygonShapeConf.cpp:120-133, DistanceProxy.cpp:62-105
+ *   prgpu_time_of_impact        GetToiViaSat(proxyA, sweepA, proxyB, sweepB, ToiConf),
+ *                               Library/include/playrho/d2/TimeOfImpact.hpp, TimeOfImpact.cpp:37-253
  */
 #ifndef PRGPU_H
 #define PRGPU_H
@@ -33,7 +35,7 @@
 extern "C" {
 #endif
 
-#define PRGPU_ABI_VERSION 1
+#define PRGPU_ABI_VERSION 2
 
 enum prgpu_status {
     PRGPU_OK = 0,
@@ -52,13 +54,16 @@ enum {
     PRGPU_BODY_ALLOW_SLEEP = 1,
     PRGPU_BODY_AWAKE = 2,
     PRGPU_BODY_FIXED_ROTATION = 4,
-    PRGPU_BODY_ENABLED = 8
+    PRGPU_BODY_ENABLED = 8,
+    PRGPU_BODY_BULLET = 16      /* impenetrable: time-of-impact sub-stepping against every body */
 };
 
 typedef struct prgpu_world prgpu_world;
 
-/* StepConf fields read by the regular phase (StepConf.hpp:165-340).  TOI is not
- * part of this step: callers use the reference's doToi = false behaviour. */
+/* StepConf fields the step reads (StepConf.hpp:165-392): the regular phase's,
+ * then the time-of-impact phase's.  doToi = 1 (the reference's default) runs the
+ * TOI phase after the regular one; sub-stepping (one TOI event per Step) is not
+ * offered: every step resolves all of its events. */
 typedef struct prgpu_step_conf {
     float deltaTime, dtRatio, minStillTimeToSleep, linearSlop, angularSlop;
     float regResolutionRate, regMinSeparation, regMinMomentum, velocityThreshold;
@@ -66,14 +71,23 @@ typedef struct prgpu_step_conf {
     float linearSleepTolerance, angularSleepTolerance, displaceMultiplier;
     float aabbExtension, maxCirclesRatio;
     int32_t regVelocityIters, regPositionIters, doWarmStart, doBlocksolve;
+    float toiResolutionRate, toiMinSeparation, toiMinMomentum, targetDepth, tolerance;
+    int32_t toiVelocityIters, toiPositionIters, maxToiRootIters, maxToiIters, maxDistanceIters;
+    int32_t maxSubSteps, doToi;
 } prgpu_step_conf;
 
-/* Subset of StepStats (StepStats.hpp:41-191), summed over the batch. */
+/* Subset of StepStats (StepStats.hpp:41-191), summed over the batch; the toi*
+ * fields are ToiStepStats (StepStats.hpp:117-151). */
 typedef struct prgpu_step_stats {
     uint32_t contactsAdded, contactsDestroyed, contactsUpdated;
     uint32_t islandsFound, islandsSolved, bodiesSlept, proxiesMoved, sumPosIters;
     uint32_t liveContacts, activeConstraints, colours, serialConstraints;
     float minSeparation, maxIncImpulse;
+    uint32_t toiIslandsFound, toiIslandsSolved, toiContactsFound, toiContactsAtMaxSubSteps;
+    uint32_t toiContactsUpdatedToi, toiContactsUpdatedTouching, toiContactsSkippedTouching;
+    uint32_t toiContactsAdded, toiProxiesMoved, toiSumPosIters, toiSumVelIters;
+    uint32_t toiMaxDistIters, toiMaxToiIters, toiMaxRootIters, toiRounds;
+    float toiMinSeparation, toiMaxIncImpulse;
 } prgpu_step_stats;
 
 /* A batch of worlds in creation order, flattened world-major.  Body indices in
@@ -264,6 +278,21 @@ int prgpu_last_error(prgpu_world* w, char* buf, int len);
 /* Vertex order of PolygonShapeConf::Set (VertexSet de-duplication + gift wrap);
  * returns the hull vertex count written to out_xy (capacity n). */
 int prgpu_convex_hull(const float* xy, int n, float linear_slop, float* out_xy);
+/* GetToiViaSat on the GPU for n pairs of convex shapes moving over sweeps, with
+ * conf's targetDepth, tolerance, maxToiRootIters, maxToiIters and
+ * maxDistanceIters.  Pair i is shapes 2i (A) and 2i+1 (B):
+ *   nverts[2n]       vertex count (disk 1, edge 2, polygon 3..16)
+ *   verts            the shapes' vertices, x y pairs, one shape after another
+ *   radius[2n]       vertex radius
+ *   sweeps[2n*9]     pos0 x y angle, pos1 x y angle, alpha0, localCenter x y
+ * time_out[n] receives the time in [0, 1]; iout4[n*4] receives the ToiOutput
+ * state (0 unknown 1 overlapped 2 touching 3 separated 4 maxRootIters
+ * 5 nextAfter 6 maxToiIters 7 belowMinTarget 8 maxDistIters
+ * 9 targetDepthExceedsTotalRadius 10 minTargetSquaredOverflow
+ * 11 maxTargetSquaredOverflow), TOI iterations, the most distance iterations
+ * and the most root-finder iterations.  Host buffers; runs on `device`. */
+int prgpu_time_of_impact(int device, uint32_t n, const uint32_t* nverts, const float* verts, const float* radius,
+                         const float* sweeps, const prgpu_step_conf* conf, float* time_out, int32_t* iout4);
 
 #ifdef __cplusplus
 }

@@ -14,6 +14,7 @@
 #include <cooperative_groups.h>
 
 #include "prgpu_collide.cuh"
+#include "prgpu_contact_ops.cuh"
 #include "prgpu_kernels.cuh"
 
 namespace cg = cooperative_groups;
@@ -21,97 +22,6 @@ namespace cg = cooperative_groups;
 namespace prgpu {
 
 namespace {
-
-__device__ __forceinline__ void load_proxy(const DW& d, uint32_t p, Proxy& out) {
-    const uint32_t meta = d.s_meta[p];
-    const int nv = (int)((meta >> 8) & 0xffu);
-    const uint32_t voff = d.s_voff[p];
-    out.count = nv < kMaxVerts ? nv : kMaxVerts;
-    out.r = d.s_radius[p];
-    out.vn = d.verts + voff;
-}
-
-__device__ __forceinline__ Xf load_xf(const DW& d, uint32_t b) {
-    const float4 x = d.b_xf[b];
-    Xf t;
-    t.p = mk(x.x, x.y);
-    t.q = mk(x.z, x.w);
-    return t;
-}
-
-__device__ __forceinline__ Xf xf0_of(const DW& d, uint32_t b) {
-    const float4 p0 = d.b_pos0[b];
-    const float4 m = d.b_mass[b];
-    return get_xf(p0.x, p0.y, p0.z, mk(m.z, m.w));
-}
-
-// AABB helpers (AABB.cpp:51-62, Interval.hpp).
-struct Box {
-    float x0, y0, x1, y1;
-};
-__device__ __forceinline__ void box_include(Box& a, V2 p) {
-    a.x0 = (a.x0 < p.x) ? a.x0 : p.x;
-    a.x1 = (p.x < a.x1) ? a.x1 : p.x;
-    a.y0 = (a.y0 < p.y) ? a.y0 : p.y;
-    a.y1 = (p.y < a.y1) ? a.y1 : p.y;
-}
-__device__ __forceinline__ void box_fatten(Box& a, float r) {
-    a.x0 = a.x0 - r; a.x1 = a.x1 + r;
-    a.y0 = a.y0 - r; a.y1 = a.y1 + r;
-}
-__device__ __forceinline__ void box_displace(Box& a, V2 dsp) {
-    if (dsp.x < 0.f) a.x0 += dsp.x; else a.x1 += dsp.x;
-    if (dsp.y < 0.f) a.y0 += dsp.y; else a.y1 += dsp.y;
-}
-__device__ __forceinline__ bool overlap4(float4 a, float4 b) {
-    {
-        const float maxOfMins = (a.x < b.x) ? b.x : a.x;
-        const float minOfMaxs = (b.z < a.z) ? b.z : a.z;
-        if (!(minOfMaxs >= maxOfMins)) return false;
-    }
-    {
-        const float maxOfMins = (a.y < b.y) ? b.y : a.y;
-        const float minOfMaxs = (b.w < a.w) ? b.w : a.w;
-        if (!(minOfMaxs >= maxOfMins)) return false;
-    }
-    return true;
-}
-__device__ __forceinline__ bool contains4(float4 a, Box b) {
-    return a.x <= b.x0 && a.z >= b.x1 && a.y <= b.y0 && a.w >= b.y1;
-}
-// ComputeAABB(proxy, xf0, xf1) reading the shape from global memory.
-__device__ __forceinline__ Box swept_aabb(const DW& d, uint32_t p, Xf x0, Xf x1) {
-    Box a;
-    a.x0 = __int_as_float(0x7f800000); a.y0 = a.x0;
-    a.x1 = -a.x0; a.y1 = -a.x0;
-    const uint32_t meta = d.s_meta[p];
-    const int nv = (int)((meta >> 8) & 0xffu);
-    const uint32_t voff = d.s_voff[p];
-    for (int i = 0; i < nv; ++i) {
-        const float4 v = d.verts[voff + i];
-        const V2 lv = mk(v.x, v.y);
-        box_include(a, xform(lv, x0));
-        box_include(a, xform(lv, x1));
-    }
-    box_fatten(a, d.s_radius[p]);
-    return a;
-}
-
-__device__ __forceinline__ void append_moved(const DW& d, uint32_t p) {
-    cg::coalesced_group g = cg::coalesced_threads();
-    uint32_t base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(&d.cnt->n_moved, g.size());
-    base = g.shfl(base, 0);
-    d.moved_list[base + g.thread_rank()] = p;
-}
-
-// Re-fattens and displaces the swept AABB of proxy p into its tree AABB.
-__device__ __forceinline__ float4 fat_box(const DW& d, Box a, Xf x0, Xf x1) {
-    box_fatten(a, d.conf->aabbExtension);
-    const V2 disp = (x1.p - x0.p) * d.conf->displaceMultiplier;
-    box_displace(a, disp);
-    return make_float4(a.x0, a.y0, a.x1, a.y1);
-}
 
 // Pre-step proxy maintenance: CreateProxies for new shapes and Synchronize of
 // bodies whose state the host changed (AabbTreeWorld.cpp:2159-2182).
@@ -163,56 +73,6 @@ __global__ void k_moved_done(DW d) {
     c->st_proxies_moved += c->n_moved;
     c->need_find = c->n_moved > 0u ? 1u : 0u;
     c->n_new = 0u;
-}
-
-// ---- manifolds in slot storage ---------------------------------------------
-__device__ __forceinline__ Man load_manifold(const DW& d, uint32_t slot) {
-    Man m;
-    const uint32_t meta = d.m_meta[slot];
-    m.type = (int)(meta & 0xfu);
-    m.count = (int)((meta >> 4) & 0xfu);
-    const float4 h = d.m_head[slot];
-    m.ln = mk(h.x, h.y);
-    m.lp = mk(h.z, h.w);
-    const float4 p0 = d.m_p0[slot], p1 = d.m_p1[slot];
-    m.plp[0] = mk(p0.x, p0.y); m.ni[0] = p0.z; m.ti[0] = p0.w;
-    m.plp[1] = mk(p1.x, p1.y); m.ni[1] = p1.z; m.ti[1] = p1.w;
-    const uint2 cf = d.m_cf[slot];
-    m.cf[0] = cf.x; m.cf[1] = cf.y;
-    return m;
-}
-__device__ __forceinline__ void store_manifold(const DW& d, uint32_t slot, const Man& m) {
-    d.m_meta[slot] = (uint32_t)m.type | ((uint32_t)m.count << 4);
-    d.m_head[slot] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
-    d.m_p0[slot] = make_float4(m.plp[0].x, m.plp[0].y, m.ni[0], m.ti[0]);
-    d.m_p1[slot] = make_float4(m.plp[1].x, m.plp[1].y, m.ni[1], m.ti[1]);
-    d.m_cf[slot] = make_uint2(m.cf[0], m.cf[1]);
-}
-
-// AabbTreeWorld::Update (AabbTreeWorld.cpp:2587-2721) without listeners.
-// src2 (optional): where the new manifold's points took their impulses from.
-__device__ void update_contact(const DW& d, uint32_t slot, int8_t* src2 = nullptr) {
-    const uint2 pr = d.cs_proxy[slot];
-    const uint2 bd = d.cs_body[slot];
-    uint32_t flags = d.cs_flags[slot];
-    bool touching = false;
-    int src[2] = {-1, -1};
-    if (flags & CF_SENSOR) {
-        store_manifold(d, slot, man_empty());
-    } else {
-        Proxy A, B;
-        load_proxy(d, pr.x, A);
-        load_proxy(d, pr.y, B);
-        const Man old = load_manifold(d, slot);
-        Man nm = collide_shapes(A, load_xf(d, bd.x), B, load_xf(d, bd.y), d.conf->linearSlop, d.conf->maxCirclesRatio);
-        touching = nm.count > 0;
-        transfer_impulses(nm, old, src);
-        store_manifold(d, slot, nm);
-    }
-    if (src2) { src2[0] = (int8_t)src[0]; src2[1] = (int8_t)src[1]; }
-    flags &= ~CF_NEEDS_UPDATE;
-    flags = touching ? (flags | CF_TOUCHING) : (flags & ~CF_TOUCHING);
-    d.cs_flags[slot] = flags;
 }
 
 __global__ void k_update_contacts(DW d, uint32_t body_mask) {
@@ -521,6 +381,7 @@ __global__ void k_pairs_done(DW d) {
 __global__ void k_new_contacts(DW d) {
     const uint32_t ft = d.cnt->free_top;
     const uint32_t hw = d.cnt->high_water;
+    const uint64_t seq = d.cnt->seq_next;
     const uint32_t kb = d.key_bits;
     const uint64_t mask = (1ull << kb) - 1ull;
     GRID_LOOP(i, d.cnt->n_new) {
@@ -538,12 +399,14 @@ __global__ void k_new_contacts(DW d) {
         d.cs_body[slot] = make_uint2(ba, bb);
         const bool sensor = ((d.s_meta[pa] | d.s_meta[pb]) & (1u << 16)) != 0u;
         uint32_t flags = CF_NEEDS_UPDATE;
-        if (!is_accelerable(fa) || !is_accelerable(fb)) flags |= CF_IMPENETRABLE;
+        if (is_impenetrable(fa) || is_impenetrable(fb)) flags |= CF_IMPENETRABLE;
         if (sensor) flags |= CF_SENSOR;
         d.cs_flags[slot] = flags;
         const float2 ma = d.s_mat[pa], mb = d.s_mat[pb];
         d.cs_mat[slot] = make_float2(sqrtf(ma.x * mb.x), (ma.y > mb.y) ? ma.y : mb.y);
         d.cs_colour[slot] = kNone;
+        // AddContacts appends in key order to the world's and both bodies' contact lists
+        d.cs_seq[slot] = seq + i;
         store_manifold(d, slot, man_empty());
         if (!sensor) {
             if (is_speedable(fa)) atomicOr(&d.b_flags[ba], BF_AWAKE);
@@ -561,6 +424,7 @@ __global__ void k_new_done(DW d) {
     const uint32_t from_stack = min(nn, c->free_top);
     c->free_top -= from_stack;
     c->high_water += nn - from_stack;
+    c->seq_next += nn;
     if (c->high_water > d.contact_cap) { set_error(c, PR_ECAPACITY, 13u); c->high_water = d.contact_cap; }
     c->st_contacts_added += nn;
 }

@@ -34,9 +34,11 @@ enum : uint32_t {
     BF_ALLOW_SLEEP = 1u << 3,
     BF_FIXED_ROT = 1u << 4,
     BF_ENABLED = 1u << 5,
+    BF_BULLET = 1u << 6,      // BodyConf::bullet: impenetrable, sub-stepped against every body
     BF_SOLVED = 1u << 8,      // in an awake island this step
     BF_MOVED = 1u << 9,       // pos1 changed in this step's solve
     BF_DIRTY = 1u << 10,      // state set by the host since the last step
+    BF_TOI_ISL = 1u << 11,    // in the island of the current time-of-impact event
 };
 
 // Contact slot flags.
@@ -45,11 +47,18 @@ enum : uint32_t {
     CF_SENSOR = 2u,
     CF_NEEDS_UPDATE = 4u,
     CF_IMPENETRABLE = 8u,
+    CF_TOI_VALID = 16u,       // cs_toi holds this step's time of impact (Contact::e_toiFlag)
+    CF_TOI_ISL = 32u,         // in the island of the current time-of-impact event
 };
+// Bits 8..15 of the contact flags count the contact's TOI sub-steps this step.
+constexpr uint32_t kToiCountShift = 8u;
+constexpr uint32_t kToiCountMask = 0xffu << kToiCountShift;
 
 PR_HD uint32_t body_type(uint32_t f) { return f & BF_TYPE_MASK; }
 PR_HD bool is_speedable(uint32_t f) { return (f & BF_TYPE_MASK) != 0u; }
 PR_HD bool is_accelerable(uint32_t f) { return (f & BF_TYPE_MASK) == 2u; }
+// Body::GetFlags (Body.cpp:32-66): static and kinematic bodies, and bullets.
+PR_HD bool is_impenetrable(uint32_t f) { return !is_accelerable(f) || (f & BF_BULLET) != 0u; }
 
 constexpr int kMaxColours = 64;      // colours 0..63 solved in parallel
 constexpr int kSerialColour = 64;    // leftover constraints solved by one thread
@@ -152,6 +161,28 @@ struct Counters {
     uint32_t world_queue;     // next entry of w_order for the per-world sweep kernel
     uint32_t lbvh_age;        // searches since the tree was last rebuilt (0: no tree yet)
     uint32_t lbvh_rebuild;    // this search rebuilds the tree (else refits it)
+    // time-of-impact phase
+    uint32_t toi_events;      // worlds that solved an event in the current round
+    uint32_t toi_rounds;      // rounds run this step
+    uint32_t toi_added_base;  // st_contacts_added before the current round's contact search
+    // ToiStepStats counters (StepStats.hpp:117-151)
+    uint32_t st_toi_found;
+    uint32_t st_toi_islands_found;
+    uint32_t st_toi_islands_solved;
+    uint32_t st_toi_sum_pos_iters;
+    uint32_t st_toi_sum_vel_iters;
+    uint32_t st_toi_updated_toi;
+    uint32_t st_toi_at_max_substeps;
+    uint32_t st_toi_updated_touching;
+    uint32_t st_toi_skipped_touching;
+    uint32_t st_toi_contacts_added;
+    uint32_t st_toi_proxies_moved;
+    uint32_t st_toi_max_dist_iters;
+    uint32_t st_toi_max_toi_iters;
+    uint32_t st_toi_max_root_iters;
+    float st_toi_min_separation;
+    float st_toi_max_inc_impulse;
+    uint64_t seq_next;        // creation sequence number of the next new contact
 };
 
 // Solver / step configuration in device memory (mirrors prgpu_step_conf).
@@ -162,6 +193,9 @@ struct DConf {
     float linearSleepTolerance, angularSleepTolerance, displaceMultiplier;
     float aabbExtension, maxCirclesRatio;
     int regVelocityIters, regPositionIters, doWarmStart, doBlocksolve;
+    float toiResolutionRate, toiMinSeparation, toiMinMomentum, targetDepth, tolerance;
+    int toiVelocityIters, toiPositionIters, maxToiRootIters, maxToiIters, maxDistanceIters;
+    int maxSubSteps, doToi;
 };
 
 // All device pointers of one batch.  Passed to kernels by value.
@@ -175,6 +209,7 @@ struct DW {
     const uint32_t* w_order; // worlds by decreasing body count (work order of per-world sweeps)
     uint32_t* w_kc;          // [n_worlds + 1] first active contact (index into k_list) of each world
     uint32_t* w_kj;          // [n_worlds + 1] first active joint of each world
+    uint32_t* w_toi;         // [n_worlds] time-of-impact loop of the world finished this step (1)
     uint32_t n_world_big;    // leading entries of w_order swept by a whole CTA (the rest by a warp)
     uint32_t stage_bytes;    // dynamic shared memory of the per-world solver (world body state)
     StepTape* tape;          // recording for the adjoint (device struct), else null
@@ -189,6 +224,7 @@ struct DW {
     float2* b_damp;
     uint32_t* b_flags;
     float* b_uat;
+    float* b_alpha0;         // Sweep::alpha0 (non-zero only inside the time-of-impact phase)
     uint32_t* b_world;
     uint32_t* b_island;      // union-find parent / island root
     uint32_t* b_jnt_off;     // body -> joints CSR (for joint collision filtering)
@@ -232,6 +268,8 @@ struct DW {
     uint32_t* cs_flags;
     float2* cs_mat;          // friction restitution
     uint32_t* cs_colour;     // colour the contact had in the last step (first choice next step)
+    float* cs_toi;           // time of impact (valid with CF_TOI_VALID)
+    uint64_t* cs_seq;        // creation sequence: orders a world's contacts as its contact list does
     uint32_t* j_colour;      // same for joints
     float4* m_head;          // ln.xy lp.xy
     float4* m_p0;            // lp.xy ni ti

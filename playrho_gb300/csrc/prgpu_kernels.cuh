@@ -32,6 +32,15 @@ void launch_solve_finish(const DW& d, const Launch& L, cudaStream_t s);
 void launch_reset_step(const DW& d, const Launch& L, cudaStream_t s);
 void launch_clear_dirty(const DW& d, const Launch& L, cudaStream_t s);
 int coop_blocks_per_sm(int threads);
+// time-of-impact phase (prgpu_toi.cu): set-up with round 0's times of impact,
+// one event per world per round (with the contact search of the moved proxies),
+// and the final contact update
+void launch_toi_begin(const DW& d, const Launch& L, cudaStream_t s);
+void launch_toi_round(const DW& d, const Launch& L, cudaStream_t s);
+void launch_toi_end(const DW& d, const Launch& L, cudaStream_t s);
+// GetToiViaSat over n pairs of (proxy, sweep) records
+cudaError_t launch_toi_pairs(uint32_t n, const float4* vtx, const uint32_t* meta, const float* sweeps,
+                             const DConf& c, float* time, int32_t* iout, cudaStream_t s);
 // recording for the adjoint (prgpu_adjoint.cu)
 void launch_tape_body_start(const DW& d, const Launch& L, cudaStream_t s);
 void launch_tape_body_flags(const DW& d, const Launch& L, cudaStream_t s);

@@ -1,0 +1,691 @@
+// prgpu_toi.cu -- the time-of-impact phase of the world step (StepConf::doToi).
+//
+// Restates AabbTreeWorld::SolveToi (AabbTreeWorld.cpp:1685-2142) for a batch of
+// worlds.  The reference handles one TOI event at a time per world: compute the
+// time of impact of every impenetrable contact that lacks one, take the soonest,
+// advance its two bodies to that time, gather the touching contacts they have
+// with impenetrable bodies into a small island, re-solve that island for the rest
+// of the step, synchronise the moved proxies, look for new contacts, and repeat.
+// The GPU keeps that per-world sequence exactly and runs the worlds side by side:
+//  * round 0 computes the times of impact of all contacts in parallel, one
+//    thread per contact (every body still has alpha0 = 0, so the order in which
+//    the reference visits them cannot matter);
+//  * each further round is one event per world, solved by one warp per world:
+//    the warp scans the world's contacts (lanes in parallel) to recompute missing
+//    times of impact in contact-list order, to find the soonest event and to walk
+//    a body's contacts in its contact-list order; lane 0 runs the sequential parts
+//    (advancing sweeps, CollideShapes, the island's position and velocity
+//    iterations) with the island held in shared memory;
+//  * between rounds the batch's broadphase (LBVH refit + query + AddContacts)
+//    runs for the proxies the round moved.
+// Contact-list order is the order contacts were created (cs_seq), as the
+// reference appends new contacts to the world's and each body's list.
+#include <cooperative_groups.h>
+
+#include "prgpu_contact_ops.cuh"
+#include "prgpu_csolve.cuh"
+#include "prgpu_kernels.cuh"
+#include "prgpu_toi.cuh"
+
+namespace prgpu {
+
+namespace {
+
+constexpr int kToiWarps = 4;             // worlds solved by one block of the round kernel
+constexpr uint32_t kToiIslandContacts = 48;
+constexpr uint32_t kToiIslandBodies = kToiIslandContacts + 1;
+constexpr unsigned kFull = 0xffffffffu;
+
+// An event's island and its solver state, in one warp's shared memory.
+struct ToiScratch {
+    VC vc[kToiIslandContacts];
+    float4 bp[kToiIslandBodies];   // body constraint position (x, y, angle)
+    float4 bv[kToiIslandBodies];   // body constraint velocity
+    float4 bm[kToiIslandBodies];   // invMass invRotI localCentre
+    uint32_t bf[kToiIslandBodies]; // body flags
+    uint32_t isl_b[kToiIslandBodies];
+    uint32_t isl_c[kToiIslandContacts];
+    uint32_t moved[kToiIslandBodies];  // bodies whose position 1 the solve changed
+    Sweep backup;
+    uint32_t nb, nc, n_moved, updated, skipped;
+};
+
+// Body-state accessor of the shared solver steps over an island (local indices).
+struct ToiBodies {
+    ToiScratch* s;
+    __device__ __forceinline__ float4 vel(uint32_t b) const { return s->bv[b]; }
+    __device__ __forceinline__ void set_vel(uint32_t b, float4 v) const { s->bv[b] = v; }
+    __device__ __forceinline__ float4 pos(uint32_t b) const { return s->bp[b]; }
+    __device__ __forceinline__ void set_pos(uint32_t b, float4 p) const { s->bp[b] = p; }
+    __device__ __forceinline__ float4 mass(uint32_t b) const { return s->bm[b]; }
+    __device__ __forceinline__ bool writable(uint32_t b) const { return is_accelerable(s->bf[b]); }
+};
+
+PR_HD ToiLimits toi_limits(const DConf& c) {
+    ToiLimits L;
+    L.targetDepth = c.targetDepth;
+    L.tolerance = c.tolerance;
+    L.maxRootIters = c.maxToiRootIters;
+    L.maxToiIters = c.maxToiIters;
+    L.maxDistIters = c.maxDistanceIters;
+    return L;
+}
+
+__device__ __forceinline__ uint32_t toi_count(uint32_t f) { return (f & kToiCountMask) >> kToiCountShift; }
+
+__device__ __forceinline__ Sweep body_sweep(const DW& d, uint32_t b) {
+    const float4 p0 = d.b_pos0[b], p1 = d.b_pos1[b], m = d.b_mass[b];
+    Sweep s;
+    s.p0 = mkpos(p0.x, p0.y, p0.z);
+    s.p1 = mkpos(p1.x, p1.y, p1.z);
+    s.lc = mk(m.z, m.w);
+    s.a0 = d.b_alpha0[b];
+    return s;
+}
+// Body::SetSweep (Body.hpp:697-702): the sweep and the cached transformation.
+__device__ __forceinline__ void body_set_sweep(const DW& d, uint32_t b, const Sweep& s) {
+    const float w0 = d.b_pos0[b].w, w1 = d.b_pos1[b].w;
+    d.b_pos0[b] = make_float4(s.p0.x, s.p0.y, s.p0.a, w0);
+    d.b_pos1[b] = make_float4(s.p1.x, s.p1.y, s.p1.a, w1);
+    d.b_alpha0[b] = s.a0;
+    const Xf xf = get_xf(s.p1.x, s.p1.y, s.p1.a, s.lc);
+    d.b_xf[b] = make_float4(xf.p.x, xf.p.y, xf.q.x, xf.q.y);
+}
+// Advance (Body.hpp:1004-1009): Advance0, then position 1 = position 0.  Returns
+// whether either position changed (the test before FlagForUpdating).
+__device__ __forceinline__ bool body_advance(const DW& d, uint32_t b, float alpha, Sweep& backup) {
+    backup = body_sweep(d, b);
+    Sweep s = backup;
+    sweep_advance0(s, alpha);
+    s.p1 = s.p0;
+    body_set_sweep(d, b, s);
+    return pos_ne(s.p0, backup.p0) || pos_ne(s.p1, backup.p1);
+}
+
+// A contact's time of impact (AabbTreeWorld.cpp:1717-1748): both bodies'
+// sweeps are advanced to the later alpha0, then GetToiViaSat on the
+// normalised sweeps.
+__device__ void compute_toi(const DW& d, uint32_t slot, const ToiLimits& L, int& mdist, int& mtoi, int& mroot) {
+    const uint2 bd = d.cs_body[slot];
+    const uint2 pr = d.cs_proxy[slot];
+    Sweep sA = body_sweep(d, bd.x), sB = body_sweep(d, bd.y);
+    const float alpha0 = maxf_(sA.a0, sB.a0);
+    sweep_advance0(sA, alpha0);
+    d.b_pos0[bd.x] = make_float4(sA.p0.x, sA.p0.y, sA.p0.a, d.b_pos0[bd.x].w);
+    d.b_alpha0[bd.x] = alpha0;
+    sweep_advance0(sB, alpha0);
+    d.b_pos0[bd.y] = make_float4(sB.p0.x, sB.p0.y, sB.p0.a, d.b_pos0[bd.y].w);
+    d.b_alpha0[bd.y] = alpha0;
+    Proxy A, B;
+    load_proxy(d, pr.x, A);
+    load_proxy(d, pr.y, B);
+    const ToiOut o = toi_via_sat(A, sweep_normalized(sA), B, sweep_normalized(sB), L);
+    const float toi = (o.state == TOI_TOUCHING) ? minf_(alpha0 + (1.0f - alpha0) * o.time, 1.0f) : 1.0f;
+    d.cs_toi[slot] = toi;
+    d.cs_flags[slot] |= CF_TOI_VALID;
+    mdist = max(mdist, o.max_dist_iters);
+    mtoi = max(mtoi, o.toi_iters);
+    mroot = max(mroot, o.max_root_iters);
+}
+
+// The filter of UpdateContactTOIs (AabbTreeWorld.cpp:1692-1715) for a contact
+// without a time of impact: 1 compute, 2 at the sub-step limit, 0 skip.
+__device__ __forceinline__ int toi_candidate(const DW& d, uint32_t slot, int maxSubSteps) {
+    const uint32_t f = d.cs_flags[slot];
+    if (f & (CF_TOI_VALID | CF_SENSOR)) return 0;
+    if (!(f & CF_IMPENETRABLE)) return 0;
+    if ((int)toi_count(f) >= maxSubSteps) return 2;
+    const uint2 bd = d.cs_body[slot];
+    if (!(d.b_flags[bd.x] & BF_AWAKE) && !(d.b_flags[bd.y] & BF_AWAKE)) return 0;
+    return 1;
+}
+
+__device__ __forceinline__ void toi_iter_stats(const DW& d, int mdist, int mtoi, int mroot) {
+    if (mdist) atomicMax(&d.cnt->st_toi_max_dist_iters, (uint32_t)mdist);
+    if (mtoi) atomicMax(&d.cnt->st_toi_max_toi_iters, (uint32_t)mtoi);
+    if (mroot) atomicMax(&d.cnt->st_toi_max_root_iters, (uint32_t)mroot);
+}
+
+// ---- phase set-up and round 0 -----------------------------------------------
+
+// Every body starts the phase with alpha0 = 0 (ResetBodiesForSolveTOI ended the
+// last one) and no proxy is marked moved.
+__global__ void k_toi_begin(DW d) {
+    GRID_LOOP(b, d.n_bodies) d.b_alpha0[b] = 0.f;
+    GRID_LOOP(p, d.n_shapes) d.p_moved[p] = 0u;
+    GRID_LOOP(w, d.n_worlds) d.w_toi[w] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        d.cnt->n_moved = 0u;
+        d.cnt->toi_rounds = 0u;
+        d.cnt->toi_events = 0u;
+    }
+}
+
+// UpdateContactTOIs of the first loop iteration, one thread per live contact.
+// alpha0 is 0 for every body, so the Advance0 each contact applies to its two
+// bodies is the same idempotent update whichever thread stores it.
+__global__ void k_toi_first(DW d) {
+    const DConf& c = *d.conf;
+    const ToiLimits L = toi_limits(c);
+    uint32_t updated = 0, at_max = 0;
+    int mdist = 0, mtoi = 0, mroot = 0;
+    GRID_LOOP(i, d.cnt->n_live) {
+        const uint32_t slot = d.c_slot[i];
+        const int k = toi_candidate(d, slot, c.maxSubSteps);
+        if (k == 2) ++at_max;
+        if (k != 1) continue;
+        compute_toi(d, slot, L, mdist, mtoi, mroot);
+        ++updated;
+    }
+    if (updated) atomicAdd(&d.cnt->st_toi_updated_toi, updated);
+    if (at_max) atomicAdd(&d.cnt->st_toi_at_max_substeps, at_max);
+    toi_iter_stats(d, mdist, mtoi, mroot);
+}
+
+// ---- one event per world per round --------------------------------------------
+
+__device__ __forceinline__ uint32_t lower_bound_key(const uint64_t* a, uint32_t n, uint64_t key) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// The world's contacts: a contiguous range of the key-sorted live list (keys
+// start with the smaller proxy index and a world's proxies are contiguous).
+struct Seg {
+    uint32_t c0, c1;
+};
+__device__ __forceinline__ Seg world_contacts(const DW& d, uint32_t w) {
+    const uint32_t n = d.cnt->n_live;
+    Seg s;
+    s.c0 = lower_bound_key(d.c_key, n, (uint64_t)d.w_shape_off[w] << d.key_bits);
+    s.c1 = lower_bound_key(d.c_key, n, (uint64_t)d.w_shape_off[w + 1] << d.key_bits);
+    return s;
+}
+
+// The contact of the world with the smallest creation sequence >= lo that
+// passes pred (kNone if there is none); all lanes get the answer.
+template <class Pred>
+__device__ __forceinline__ uint32_t warp_first_in_list(const DW& d, Seg sg, uint64_t lo, uint32_t lane, Pred pred,
+                                                       uint64_t& seq_out) {
+    uint64_t best = ~0ull;
+    uint32_t bslot = kNone;
+    for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
+        const uint32_t slot = d.c_slot[i];
+        const uint64_t q = d.cs_seq[slot];
+        if (q >= lo && q < best && pred(slot)) { best = q; bslot = slot; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t ob = __shfl_xor_sync(kFull, best, o);
+        const uint32_t os = __shfl_xor_sync(kFull, bslot, o);
+        if (ob < best) { best = ob; bslot = os; }
+    }
+    seq_out = best;
+    return bslot;
+}
+
+// FlagForUpdating over the contacts of body b.
+__device__ __forceinline__ void flag_contacts_of(const DW& d, Seg sg, uint32_t b, uint32_t lane) {
+    for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
+        const uint32_t slot = d.c_slot[i];
+        const uint2 bd = d.cs_body[slot];
+        if (bd.x == b || bd.y == b) d.cs_flags[slot] |= CF_NEEDS_UPDATE;
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ uint32_t island_local(const ToiScratch& S, uint32_t b) {
+    for (uint32_t i = 0; i < S.nb; ++i)
+        if (S.isl_b[i] == b) return i;
+    return kNone;
+}
+
+// GetBodyConstraint (BodyConstraint.hpp:157-167) at h: velocity integrated,
+// damped and capped as in the regular phase.
+__device__ __forceinline__ float4 constraint_velocity(const DW& d, uint32_t b, float h) {
+    const DConf& c = *d.conf;
+    const uint32_t f = d.b_flags[b];
+    float4 v = d.b_vel[b];
+    if (is_accelerable(f)) {
+        const float4 a = d.b_acc[b];
+        const float2 dm = d.b_damp[b];
+        v.x = v.x + a.x * h;
+        v.y = v.y + a.y * h;
+        v.z = v.z + h * a.z;
+        const float linv = 1.0f / (1.0f + h * dm.x);
+        v.x = v.x * linv;
+        v.y = v.y * linv;
+        v.z = v.z / (1.0f + h * dm.y);
+    }
+    const float tx = v.x * h, ty = v.y * h;
+    float lsq = 0.f;
+    lsq += tx * tx;
+    lsq += ty * ty;
+    if (lsq > c.maxTranslation * c.maxTranslation) {
+        const float ratio = c.maxTranslation / sqrtf(lsq);
+        v.x = v.x * ratio;
+        v.y = v.y * ratio;
+    }
+    const float absRot = fabsf(h * v.z);
+    if (absRot > c.maxRotation) {
+        const float ratio = c.maxRotation / absRot;
+        v.z = v.z * ratio;
+    }
+    return v;
+}
+
+// SolveToiViaGS (AabbTreeWorld.cpp:1957-2059) on lane 0: position iterations
+// at toiResolutionRate, the leap to the new position 0, velocity iterations
+// without warm starting, integration over the rest of the step.
+__device__ void toi_solve_island(const DW& d, ToiScratch& S, float toi) {
+    const DConf& c = *d.conf;
+    const float h = (1.0f - toi) * c.deltaTime;
+    for (uint32_t i = 0; i < S.nb; ++i) {
+        const uint32_t g = S.isl_b[i];
+        S.bp[i] = d.b_pos1[g];
+        S.bm[i] = d.b_mass[g];
+        S.bf[i] = d.b_flags[g];
+        S.bv[i] = constraint_velocity(d, g, 0.f);
+    }
+    const ToiBodies bs{&S};
+    const float inf = __int_as_float(0x7f800000);
+    float minSepAll = inf;
+    bool solved = false;
+    int posIters = c.toiPositionIters;
+    for (int it = 0; it < c.toiPositionIters; ++it) {
+        float minSep = inf;
+        for (uint32_t k = 0; k < S.nc; ++k) {
+            const uint32_t slot = S.isl_c[k];
+            const uint2 bd = d.cs_body[slot], pr = d.cs_proxy[slot];
+            const uint32_t la = island_local(S, bd.x), lb = island_local(S, bd.y);
+            if (la == kNone || lb == kNone) { set_error(d.cnt, PR_ESTATE, 41u); return; }
+            const PC pc = make_contact_pc(load_manrec(d, slot), d.s_radius[pr.x] + d.s_radius[pr.y], la, lb);
+            minSep = minf_(minSep, solve_contact_position(d, bs, pc, c.toiResolutionRate));
+        }
+        minSepAll = minf_(minSepAll, minSep);
+        if (minSep >= c.toiMinSeparation) { posIters = it + 1; solved = true; break; }
+    }
+    for (uint32_t i = 0; i < S.nb; ++i) {  // SetPosition0: the sweep only
+        const uint32_t g = S.isl_b[i];
+        d.b_pos0[g] = make_float4(S.bp[i].x, S.bp[i].y, S.bp[i].z, d.b_pos0[g].w);
+    }
+    for (uint32_t k = 0; k < S.nc; ++k) {  // GetToiVelocityConstraintConf: dtRatio 0
+        const uint32_t slot = S.isl_c[k];
+        const uint2 bd = d.cs_body[slot], pr = d.cs_proxy[slot];
+        const uint32_t la = island_local(S, bd.x), lb = island_local(S, bd.y);
+        if (la == kNone || lb == kNone) { set_error(d.cnt, PR_ESTATE, 41u); return; }
+        VC vc = make_contact_vc(load_manrec(d, slot), S.bp[la], S.bp[lb], S.bm[la], S.bm[lb], S.bv[la], S.bv[lb],
+                                d.s_radius[pr.x], d.s_radius[pr.y], d.cs_mat[slot], 0.f, c);
+        vc.bA = la; vc.bB = lb;
+        S.vc[k] = vc;
+    }
+    float maxInc = 0.f;
+    int velIters = c.toiVelocityIters;
+    for (int it = 0; it < c.toiVelocityIters; ++it) {
+        float newInc = 0.f;
+        for (uint32_t k = 0; k < S.nc; ++k) newInc = maxf_(newInc, solve_contact_velocity<ToiBodies, true>(d, bs, S.vc[k]));
+        if (newInc <= c.toiMinMomentum) { velIters = it + 1; break; }
+        maxInc = maxf_(maxInc, newInc);
+    }
+    S.n_moved = 0;
+    for (uint32_t i = 0; i < S.nb; ++i) {  // IntegratePositions, then the write-back
+        float4 p = S.bp[i];
+        const float4 v = S.bv[i];
+        const float tx = v.x * h, ty = v.y * h, rot = h * v.z;
+        p.x = p.x + tx; p.y = p.y + ty; p.z = p.z + rot;
+        const uint32_t g = S.isl_b[i];
+        d.b_vel[g] = make_float4(v.x, v.y, v.z, d.b_vel[g].w);
+        const float4 p1 = d.b_pos1[g];
+        if (pos_ne(mkpos(p1.x, p1.y, p1.z), mkpos(p.x, p.y, p.z))) {
+            d.b_pos1[g] = make_float4(p.x, p.y, p.z, p1.w);
+            const Xf xf = get_xf(p.x, p.y, p.z, mk(S.bm[i].z, S.bm[i].w));
+            d.b_xf[g] = make_float4(xf.p.x, xf.p.y, xf.q.x, xf.q.y);
+            S.moved[S.n_moved++] = g;
+        }
+    }
+    Counters* cn = d.cnt;
+    if (solved) atomicAdd(&cn->st_toi_islands_solved, 1u);
+    if (posIters > 0 || velIters > 0) atomicAdd(&cn->st_toi_islands_found, 1u);
+    atomicAdd(&cn->st_toi_sum_pos_iters, (uint32_t)posIters);
+    atomicAdd(&cn->st_toi_sum_vel_iters, (uint32_t)velIters);
+    atomic_min_float(&cn->st_toi_min_separation, minSepAll);
+    atomic_max_nonneg_float(&cn->st_toi_max_inc_impulse, maxInc);
+}
+
+// ProcessContactsForTOI (AabbTreeWorld.cpp:2061-2142) for body x, walking its
+// contacts in its contact-list order.  Returns false on island overflow.
+__device__ bool toi_process_contacts(const DW& d, Seg sg, uint32_t x, float toi, ToiScratch& S, uint32_t lane) {
+    const bool impX = is_impenetrable(d.b_flags[x]);
+    uint64_t lo = 0;
+    for (uint32_t guard = 0; guard <= sg.c1 - sg.c0; ++guard) {  // each pass takes a later contact
+        uint64_t q;
+        const uint32_t slot = warp_first_in_list(d, sg, lo, lane, [&](uint32_t s) {
+            const uint2 bd = d.cs_body[s];
+            return bd.x == x || bd.y == x;
+        }, q);
+        if (slot == kNone) return true;
+        lo = q + 1;
+        // lane 0 decides; 1: go on with the contact, 2: the other body moved
+        uint32_t act = 0, other = 0;
+        if (lane == 0) {
+            const uint32_t f = d.cs_flags[slot];
+            const uint2 bd = d.cs_body[slot];
+            other = (bd.x == x) ? bd.y : bd.x;
+            const uint32_t fo = d.b_flags[other];
+            if (!(f & (CF_TOI_ISL | CF_SENSOR)) && (impX || is_impenetrable(fo))) {
+                act = 1u;
+                if (!(fo & BF_TOI_ISL)) {
+                    if (body_advance(d, other, toi, S.backup)) act |= 2u;
+                } else {
+                    S.backup = body_sweep(d, other);
+                }
+            }
+        }
+        act = __shfl_sync(kFull, act, 0);
+        other = __shfl_sync(kFull, other, 0);
+        if (act & 2u) flag_contacts_of(d, sg, other, lane);
+        uint32_t ok = 1u;
+        if (lane == 0 && (act & 1u)) {
+            uint32_t f = d.cs_flags[slot];
+            if (f & CF_NEEDS_UPDATE) {
+                update_contact(d, slot);
+                ++S.updated;
+                f = d.cs_flags[slot];
+            } else {
+                ++S.skipped;
+            }
+            if (!(f & CF_TOUCHING)) {
+                body_set_sweep(d, other, S.backup);
+            } else if (S.nc >= kToiIslandContacts) {
+                ok = 0u;
+            } else {
+                S.isl_c[S.nc++] = slot;
+                d.cs_flags[slot] = f | CF_TOI_ISL;
+                const uint32_t fo = d.b_flags[other];
+                if (!(fo & BF_TOI_ISL)) {
+                    d.b_flags[other] = fo | BF_TOI_ISL | (is_speedable(fo) ? BF_AWAKE : 0u);
+                    S.isl_b[S.nb++] = other;
+                }
+            }
+        }
+        ok = __shfl_sync(kFull, ok, 0);
+        __syncwarp();
+        if (!ok) return false;
+    }
+    return true;
+}
+
+// SolveToi(ContactID) (AabbTreeWorld.cpp:1833-1955) for the world's soonest
+// contact; returns false if the island overflowed its shared-memory capacity.
+__device__ bool toi_event(const DW& d, Seg sg, uint32_t next, ToiScratch& S, uint32_t lane) {
+    const uint2 bd = d.cs_body[next];
+    const float toi = d.cs_toi[next];
+    Sweep bkA, bkB;
+    uint32_t moved = 0;
+    if (lane == 0) {
+        if (body_advance(d, bd.x, toi, bkA)) moved |= 1u;
+        if (body_advance(d, bd.y, toi, bkB)) moved |= 2u;
+    }
+    moved = __shfl_sync(kFull, moved, 0);
+    if (moved & 1u) flag_contacts_of(d, sg, bd.x, lane);
+    if (moved & 2u) flag_contacts_of(d, sg, bd.y, lane);
+    uint32_t go = 0;
+    if (lane == 0) {
+        uint32_t f = d.cs_flags[next];
+        uint32_t updated = 0;
+        if (f & CF_NEEDS_UPDATE) {
+            update_contact(d, next);
+            updated = 1;
+            f = d.cs_flags[next];
+        }
+        const uint32_t n = min(toi_count(f) + 1u, 255u);
+        f = (f & ~(CF_TOI_VALID | kToiCountMask)) | (n << kToiCountShift);
+        if (!(f & CF_TOUCHING)) {
+            d.cs_flags[next] = f;
+            body_set_sweep(d, bd.x, bkA);
+            body_set_sweep(d, bd.y, bkB);
+            atomicAdd(&d.cnt->st_toi_updated_touching, updated);
+            atomicAdd(&d.cnt->st_toi_skipped_touching, updated ? 0u : 1u);
+        } else {
+            d.cs_flags[next] = f | CF_TOI_ISL;
+            const uint32_t fa = d.b_flags[bd.x], fb = d.b_flags[bd.y];
+            d.b_flags[bd.x] = fa | BF_TOI_ISL | (is_speedable(fa) ? BF_AWAKE : 0u);
+            d.b_flags[bd.y] = fb | BF_TOI_ISL | (is_speedable(fb) ? BF_AWAKE : 0u);
+            S.isl_b[0] = bd.x; S.isl_b[1] = bd.y; S.nb = 2;
+            S.isl_c[0] = next; S.nc = 1;
+            S.updated = updated; S.skipped = 0;
+            go = 1;
+        }
+    }
+    go = __shfl_sync(kFull, go, 0);
+    __syncwarp();
+    if (!go) return true;
+    if (is_accelerable(d.b_flags[bd.x]) && !toi_process_contacts(d, sg, bd.x, toi, S, lane)) return false;
+    if (is_accelerable(d.b_flags[bd.y]) && !toi_process_contacts(d, sg, bd.y, toi, S, lane)) return false;
+    if (lane == 0) {
+        for (uint32_t i = 0; i < S.nb; ++i) {  // RemoveUnspeedablesFromIslanded
+            const uint32_t g = S.isl_b[i];
+            if (!is_speedable(d.b_flags[g])) d.b_flags[g] &= ~BF_TOI_ISL;
+        }
+        toi_solve_island(d, S, toi);
+        atomicAdd(&d.cnt->st_toi_updated_touching, S.updated);
+        atomicAdd(&d.cnt->st_toi_skipped_touching, S.skipped);
+    }
+    __syncwarp();
+    const uint32_t nm = __shfl_sync(kFull, S.n_moved, 0);
+    for (uint32_t i = 0; i < nm; ++i) flag_contacts_of(d, sg, S.moved[i], lane);
+    return true;
+}
+
+// One iteration of the reference's TOI loop (AabbTreeWorld.cpp:1758-1826) for
+// world w: missing times of impact, the soonest event, its island, then the
+// proxies of the islanded bodies.
+__device__ void toi_world_round(const DW& d, uint32_t w, ToiScratch& S, bool first, uint32_t lane) {
+    const DConf& c = *d.conf;
+    const Seg sg = world_contacts(d, w);
+    if (!first) {
+        // UpdateContactTOIs in contact-list order (Advance0 makes the order matter)
+        uint32_t at_max = 0;
+        for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u)
+            if (toi_candidate(d, d.c_slot[i], c.maxSubSteps) == 2) ++at_max;
+        if (at_max) atomicAdd(&d.cnt->st_toi_at_max_substeps, at_max);
+        const ToiLimits L = toi_limits(c);
+        int mdist = 0, mtoi = 0, mroot = 0;
+        uint32_t updated = 0;
+        for (uint32_t guard = 0; guard <= sg.c1 - sg.c0; ++guard) {  // each pass gives one contact a time
+            uint64_t q;
+            const uint32_t slot = warp_first_in_list(d, sg, 0, lane, [&](uint32_t s) {
+                return toi_candidate(d, s, c.maxSubSteps) == 1;
+            }, q);
+            if (slot == kNone) break;
+            if (lane == 0) {
+                compute_toi(d, slot, L, mdist, mtoi, mroot);
+                ++updated;
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            if (updated) atomicAdd(&d.cnt->st_toi_updated_toi, updated);
+            toi_iter_stats(d, mdist, mtoi, mroot);
+        }
+    }
+    // GetSoonestContact (AabbTreeWorld.cpp:2870-2890): the smallest time below 1,
+    // the earliest in the contact list among equal times
+    float best = 1.0f;
+    uint64_t bseq = ~0ull;
+    uint32_t next = kNone;
+    for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
+        const uint32_t slot = d.c_slot[i];
+        if (!(d.cs_flags[slot] & CF_TOI_VALID)) continue;
+        const float t = d.cs_toi[slot];
+        const uint64_t q = d.cs_seq[slot];
+        if (t < best || (t == best && next != kNone && q < bseq)) { best = t; bseq = q; next = slot; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(kFull, best, o);
+        const uint64_t oq = __shfl_xor_sync(kFull, bseq, o);
+        const uint32_t on = __shfl_xor_sync(kFull, next, o);
+        if (on != kNone && (next == kNone || ob < best || (ob == best && oq < bseq))) {
+            best = ob; bseq = oq; next = on;
+        }
+    }
+    if (next == kNone) {
+        // no more events: ResetBodiesForSolveTOI and ResetContactsForSolveTOI
+        for (uint32_t b = d.w_body_off[w] + lane; b < d.w_body_off[w + 1]; b += 32u) d.b_alpha0[b] = 0.f;
+        for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
+            const uint32_t slot = d.c_slot[i];
+            d.cs_flags[slot] &= ~(CF_TOI_VALID | CF_TOI_ISL | kToiCountMask);
+        }
+        if (lane == 0) d.w_toi[w] = 1u;
+        return;
+    }
+    if (lane == 0) {
+        atomicAdd(&d.cnt->st_toi_found, 1u);
+        atomicAdd(&d.cnt->toi_events, 1u);
+    }
+    S.nb = 0;
+    __syncwarp();
+    if (!(d.cs_flags[next] & CF_TOI_ISL)) {
+        if (!toi_event(d, sg, next, S, lane)) {
+            if (lane == 0) set_error(d.cnt, PR_ECAPACITY, 40u);
+            return;
+        }
+    }
+    __syncwarp();
+    // islanded bodies: synchronise the proxies of accelerable ones and forget
+    // their contacts' times of impact and island marks
+    for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
+        const uint32_t slot = d.c_slot[i];
+        const uint2 bd = d.cs_body[slot];
+        const uint32_t fa = d.b_flags[bd.x], fb = d.b_flags[bd.y];
+        if (((fa & BF_TOI_ISL) && is_accelerable(fa)) || ((fb & BF_TOI_ISL) && is_accelerable(fb)))
+            d.cs_flags[slot] &= ~(CF_TOI_VALID | CF_TOI_ISL);
+    }
+    uint32_t moved = 0;
+    for (uint32_t p = d.w_shape_off[w] + lane; p < d.w_shape_off[w + 1]; p += 32u) {
+        const uint32_t b = d.s_body[p];
+        const uint32_t f = d.b_flags[b];
+        if (!(f & BF_TOI_ISL) || !is_accelerable(f)) continue;
+        const Xf x0 = xf0_of(d, b), x1 = load_xf(d, b);
+        const Box a = swept_aabb(d, p, x0, x1);
+        if (!contains4(d.p_aabb[p], a)) {
+            d.p_aabb[p] = fat_box(d, a, x0, x1);
+            d.p_moved[p] = 1u;
+            append_moved(d, p);
+            ++moved;
+        }
+    }
+    if (moved) atomicAdd(&d.cnt->st_toi_proxies_moved, moved);
+    __syncwarp();
+    if (lane == 0)
+        for (uint32_t i = 0; i < S.nb; ++i) d.b_flags[S.isl_b[i]] &= ~BF_TOI_ISL;
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(kToiWarps * 32) k_toi_round(DW d) {
+    __shared__ ToiScratch scratch[kToiWarps];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const bool first = d.cnt->toi_rounds == 1u;
+    if (d.cnt->err) return;
+    for (uint32_t w = blockIdx.x * kToiWarps + wid; w < d.n_worlds; w += gridDim.x * kToiWarps) {
+        if (d.w_toi[w]) continue;
+        toi_world_round(d, w, scratch[wid], first, lane);
+    }
+}
+
+// Before a round: the proxies the last round moved are no longer "moved".
+__global__ void k_toi_clear_moved(DW d) {
+    GRID_LOOP(i, d.cnt->n_moved) d.p_moved[d.moved_list[i]] = 0u;
+}
+__global__ void k_toi_round_reset(DW d) {
+    Counters* c = d.cnt;
+    c->n_moved = 0u;
+    c->toi_events = 0u;
+    c->toi_rounds += 1u;
+}
+__global__ void k_toi_moved_done(DW d) {
+    Counters* c = d.cnt;
+    c->need_find = c->n_moved > 0u ? 1u : 0u;
+    c->n_new = 0u;
+    c->toi_added_base = c->st_contacts_added;
+}
+__global__ void k_toi_added(DW d) {
+    Counters* c = d.cnt;
+    c->st_toi_contacts_added += c->st_contacts_added - c->toi_added_base;
+}
+
+// The final UpdateContacts of SolveToi (AabbTreeWorld.cpp:1827-1829).
+__global__ void k_toi_update_contacts(DW d) {
+    uint32_t updated = 0, skipped = 0;
+    GRID_LOOP(i, d.cnt->n_live) {
+        const uint32_t slot = d.c_slot[i];
+        if (d.cs_flags[slot] & CF_NEEDS_UPDATE) {
+            update_contact(d, slot);
+            ++updated;
+        } else {
+            ++skipped;
+        }
+    }
+    if (updated) atomicAdd(&d.cnt->st_toi_updated_touching, updated);
+    if (skipped) atomicAdd(&d.cnt->st_toi_skipped_touching, skipped);
+}
+
+// ---- GetToiViaSat over a batch of pairs (the C ABI's prgpu_time_of_impact) ----
+__global__ void k_toi_pairs(uint32_t n, const float4* vtx, const uint32_t* meta, const float* sweeps,
+                            ToiLimits L, float* time, int32_t* iout) {
+    GRID_LOOP(i, n) {
+        Proxy P[2];
+        Sweep S[2];
+        for (int k = 0; k < 2; ++k) {
+            const uint32_t m = meta[2 * i + k];  // vertex offset << 8 | count
+            P[k].count = (int)(m & 0xffu);
+            P[k].vn = vtx + (m >> 8);
+            P[k].r = sweeps[(2 * i + k) * 10 + 9];
+            const float* s = sweeps + (2 * i + k) * 10;
+            S[k].p0 = mkpos(s[0], s[1], s[2]);
+            S[k].p1 = mkpos(s[3], s[4], s[5]);
+            S[k].a0 = s[6];
+            S[k].lc = mk(s[7], s[8]);
+        }
+        const ToiOut o = toi_via_sat(P[0], S[0], P[1], S[1], L);
+        time[i] = o.time;
+        iout[4 * i + 0] = o.state;
+        iout[4 * i + 1] = o.toi_iters;
+        iout[4 * i + 2] = o.max_dist_iters;
+        iout[4 * i + 3] = o.max_root_iters;
+    }
+}
+
+}  // namespace
+
+void launch_toi_begin(const DW& d, const Launch& L, cudaStream_t s) {
+    k_toi_begin<<<L.grid, L.threads, 0, s>>>(d);
+    k_toi_first<<<L.grid, L.threads, 0, s>>>(d);
+}
+
+void launch_toi_round(const DW& d, const Launch& L, cudaStream_t s) {
+    k_toi_clear_moved<<<L.grid, L.threads, 0, s>>>(d);
+    k_toi_round_reset<<<1, 1, 0, s>>>(d);
+    const int blocks = (int)std::min<uint32_t>((d.n_worlds + kToiWarps - 1) / kToiWarps, (uint32_t)L.grid);
+    k_toi_round<<<blocks, kToiWarps * 32, 0, s>>>(d);
+    k_toi_moved_done<<<1, 1, 0, s>>>(d);
+    launch_find_contacts(d, L, s);
+    k_toi_added<<<1, 1, 0, s>>>(d);
+}
+
+void launch_toi_end(const DW& d, const Launch& L, cudaStream_t s) {
+    k_toi_update_contacts<<<L.grid, L.threads, 0, s>>>(d);
+}
+
+cudaError_t launch_toi_pairs(uint32_t n, const float4* vtx, const uint32_t* meta, const float* sweeps,
+                             const DConf& c, float* time, int32_t* iout, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const int blocks = (int)std::min<uint32_t>((n + 127) / 128, 4096u);
+    k_toi_pairs<<<blocks, 128, 0, s>>>(n, vtx, meta, sweeps, toi_limits(c), time, iout);
+    return cudaGetLastError();
+}
+
+}  // namespace prgpu

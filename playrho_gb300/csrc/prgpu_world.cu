@@ -40,6 +40,8 @@ struct prgpu_world {
     std::vector<uint32_t> order_nb;  // body counts of the worlds in work-queue order
     struct AdjWindow* adj = nullptr;  // open StepAdjoint window, if any
     uint32_t warp_world_max = 0;     // worlds of at most this many bodies are swept by one warp
+    // time-of-impact phase: set-up, one round, and the final update, each captured once
+    cudaGraphExec_t toi_graph[3] = {};
 };
 
 extern "C" void adjoint_drop_graphs(prgpu_world* w);
@@ -334,6 +336,7 @@ int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
         if (x.flags & PRGPU_BODY_ALLOW_SLEEP) f |= BF_ALLOW_SLEEP;
         if (x.flags & PRGPU_BODY_FIXED_ROTATION) f |= BF_FIXED_ROT;
         if (x.flags & PRGPU_BODY_ENABLED) f |= BF_ENABLED;
+        if (x.flags & PRGPU_BODY_BULLET) f |= BF_BULLET;
         bflags[b] = f;
     }
     auto& s_meta = hp.s_meta; auto& s_voff = hp.s_voff; auto& s_filter = hp.s_filter; auto& s_body = hp.s_body;
@@ -423,6 +426,8 @@ int drop_graph(prgpu_world* w) {
     adjoint_drop_graphs(w);
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->graph_def) { cudaGraphDestroy(w->graph_def); w->graph_def = nullptr; }
+    for (auto& g : w->toi_graph)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     return PRGPU_OK;
 }
 
@@ -470,6 +475,9 @@ int set_conf(prgpu_world* w, const prgpu_step_conf* conf) {
     if (!conf) return fail(w, PRGPU_EINVAL, "conf is NULL");
     if (conf->regPositionIters < 0 || conf->regPositionIters > kMaxPosIters || conf->regVelocityIters < 0)
         return fail(w, PRGPU_EINVAL, "iteration counts out of range (position iterations <= %d)", kMaxPosIters);
+    if (conf->toiPositionIters < 0 || conf->toiVelocityIters < 0 || conf->maxToiRootIters < 0 ||
+        conf->maxToiIters < 0 || conf->maxDistanceIters < 0 || conf->maxSubSteps < 0 || conf->maxSubSteps > 255)
+        return fail(w, PRGPU_EINVAL, "time-of-impact iteration counts out of range (maxSubSteps <= 255)");
     if (!w->conf_valid || std::memcmp(&w->conf, conf, sizeof(*conf)) != 0) {
         static_assert(sizeof(prgpu_step_conf) == sizeof(DConf), "conf layout");
         CU(cudaMemcpyAsync(w->d_conf, conf, sizeof(DConf), cudaMemcpyHostToDevice, w->stream));
@@ -489,26 +497,83 @@ int check_device_error(prgpu_world* w) {
     return PRGPU_OK;
 }
 
+// Captures the launches `fn` enqueues on the world's stream into *g once.
+template <class F>
+int capture_once(prgpu_world* w, cudaGraphExec_t* g, F fn) {
+    if (*g) return PRGPU_OK;
+    CU(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+    fn();
+    cudaGraph_t def = nullptr;
+    const cudaError_t e1 = cudaStreamEndCapture(w->stream, &def);
+    if (e1 != cudaSuccess) return fail(w, PRGPU_ECUDA, "graph capture: %s", cudaGetErrorString(e1));
+    const cudaError_t e2 = cudaGraphInstantiate(g, def, 0);
+    cudaGraphDestroy(def);
+    if (e2 != cudaSuccess) return fail(w, PRGPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e2));
+    return PRGPU_OK;
+}
+
+// Guard on the number of time-of-impact rounds of one step: every event adds a
+// sub-step to one contact and contacts have at most maxSubSteps, so the loop
+// ends long before this.
+constexpr uint32_t kMaxToiRounds = 1u << 17;
+
+// The time-of-impact phase of one step (AabbTreeWorld.cpp:1752-1831): round
+// after round of one event per world until no world has an event left.  The
+// host reads the device counters after each round to decide whether to go on.
+int run_toi_phase(prgpu_world* w) {
+    const DW& d = w->d;
+    const Launch& L = w->L;
+    cudaStream_t s = w->stream;
+    int rc;
+    if ((rc = capture_once(w, &w->toi_graph[0], [&] { launch_toi_begin(d, L, s); }))) return rc;
+    if ((rc = capture_once(w, &w->toi_graph[1], [&] { launch_toi_round(d, L, s); }))) return rc;
+    if ((rc = capture_once(w, &w->toi_graph[2], [&] { launch_toi_end(d, L, s); }))) return rc;
+    CU(cudaGraphLaunch(w->toi_graph[0], s));
+    for (uint32_t r = 0;; ++r) {
+        CU(cudaGraphLaunch(w->toi_graph[1], s));
+        CU(cudaMemcpyAsync(w->h_cnt, d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        if (w->h_cnt->err)
+            return fail(w, (int)w->h_cnt->err, "device error %u at site %u", w->h_cnt->err, w->h_cnt->err_where);
+        if (w->h_cnt->toi_events == 0u) break;
+        if (r >= kMaxToiRounds) return fail(w, PRGPU_ETIMEOUT, "time-of-impact loop did not finish");
+    }
+    CU(cudaGraphLaunch(w->toi_graph[2], s));
+    return PRGPU_OK;
+}
+
+// Launches the captured regular-phase step graph n times (capturing it first).
+int launch_step_graphs(prgpu_world* w, int n) {
+    if (!w->graph) {
+        for (int k = 0; k < 8; ++k)
+            if (!w->graph_ev[k]) CU(cudaEventCreate(&w->graph_ev[k]));
+        CU(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(w, true, w->graph_ev, true);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e1 = cudaStreamEndCapture(w->stream, &g);
+        if (e1 != cudaSuccess) return fail(w, PRGPU_ECUDA, "graph capture: %s", cudaGetErrorString(e1));
+        const cudaError_t e2 = cudaGraphInstantiate(&w->graph, g, 0);
+        if (e2 != cudaSuccess) return fail(w, PRGPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e2));
+        w->graph_def = g;
+    }
+    for (int i = 0; i < n; ++i) CU(cudaGraphLaunch(w->graph, w->stream));
+    return PRGPU_OK;
+}
+
 int run_steps(prgpu_world* w, const prgpu_step_conf* conf, int n, bool sync) {
     int rc = set_conf(w, conf);
     if (rc) return rc;
     if (conf->deltaTime == 0.f) {
         for (int i = 0; i < n; ++i) enqueue_step(w, false);
         CU(cudaGetLastError());
-    } else {
-        if (!w->graph) {
-            for (int k = 0; k < 8; ++k)
-                if (!w->graph_ev[k]) CU(cudaEventCreate(&w->graph_ev[k]));
-            CU(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
-            enqueue_step(w, true, w->graph_ev, true);
-            cudaGraph_t g = nullptr;
-            const cudaError_t e1 = cudaStreamEndCapture(w->stream, &g);
-            if (e1 != cudaSuccess) return fail(w, PRGPU_ECUDA, "graph capture: %s", cudaGetErrorString(e1));
-            const cudaError_t e2 = cudaGraphInstantiate(&w->graph, g, 0);
-            if (e2 != cudaSuccess) return fail(w, PRGPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e2));
-            w->graph_def = g;
+    } else if (conf->doToi) {
+        // the TOI loop reads the device counters between rounds: step by step
+        for (int i = 0; i < n; ++i) {
+            if ((rc = launch_step_graphs(w, 1)) != PRGPU_OK) return rc;
+            if ((rc = run_toi_phase(w)) != PRGPU_OK) return rc;
         }
-        for (int i = 0; i < n; ++i) CU(cudaGraphLaunch(w->graph, w->stream));
+    } else if ((rc = launch_step_graphs(w, n)) != PRGPU_OK) {
+        return rc;
     }
     if (sync) return check_device_error(w);
     return PRGPU_OK;
@@ -605,6 +670,18 @@ int prgpu_default_step_conf(prgpu_step_conf* c) {
     c->regPositionIters = 3;
     c->doWarmStart = 1;
     c->doBlocksolve = 1;
+    c->toiResolutionRate = 75.0f / 100.0f;
+    c->toiMinSeparation = -linearSlop * 1.5f;
+    c->toiMinMomentum = 0.0f / 100.0f;
+    c->targetDepth = linearSlop * 3.0f;
+    c->tolerance = linearSlop / 4.0f;
+    c->toiVelocityIters = 8;
+    c->toiPositionIters = 20;
+    c->maxToiRootIters = 30;
+    c->maxToiIters = 20;
+    c->maxDistanceIters = 20;
+    c->maxSubSteps = 8;
+    c->doToi = 1;
     return PRGPU_OK;
 }
 
@@ -645,6 +722,48 @@ int prgpu_convex_hull(const float* xy, int n, float linear_slop, float* out_xy) 
     }
     for (size_t k = 0; k < hull.size(); ++k) { out_xy[2 * k] = pts[hull[k]].x; out_xy[2 * k + 1] = pts[hull[k]].y; }
     return (int)hull.size();
+}
+
+int prgpu_time_of_impact(int device, uint32_t n, const uint32_t* nverts, const float* verts, const float* radius,
+                         const float* sweeps, const prgpu_step_conf* conf, float* time_out, int32_t* iout4) {
+    if (n == 0) return PRGPU_OK;
+    if (!nverts || !verts || !radius || !sweeps || !conf || !time_out || !iout4) return PRGPU_EINVAL;
+    std::vector<uint32_t> meta(2 * (size_t)n);
+    std::vector<float4> vtx;
+    std::vector<float> sw(2 * (size_t)n * 10);
+    for (size_t k = 0; k < 2 * (size_t)n; ++k) {
+        const uint32_t nv = nverts[k];
+        if (nv < 1 || nv > 16u) return PRGPU_EINVAL;  // the shapes the step supports
+        if (vtx.size() + nv >= (1u << 24)) return PRGPU_ECAPACITY;
+        meta[k] = ((uint32_t)vtx.size() << 8) | nv;
+        for (uint32_t i = 0; i < nv; ++i) {
+            const size_t v = vtx.size();
+            vtx.push_back(make_float4(verts[2 * v], verts[2 * v + 1], 0.f, 0.f));
+        }
+        for (int q = 0; q < 9; ++q) sw[k * 10 + q] = sweeps[k * 9 + q];
+        sw[k * 10 + 9] = radius[k];
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return PRGPU_ECUDA;
+    float4* d_vtx = nullptr;
+    uint32_t* d_meta = nullptr;
+    float *d_sw = nullptr, *d_time = nullptr;
+    int32_t* d_io = nullptr;
+    DConf dc;
+    static_assert(sizeof(prgpu_step_conf) == sizeof(DConf), "conf layout");
+    std::memcpy(&dc, conf, sizeof(dc));
+    cudaError_t e = cudaMalloc(&d_vtx, sizeof(float4) * vtx.size());
+    if (e == cudaSuccess) e = cudaMalloc(&d_meta, sizeof(uint32_t) * meta.size());
+    if (e == cudaSuccess) e = cudaMalloc(&d_sw, sizeof(float) * sw.size());
+    if (e == cudaSuccess) e = cudaMalloc(&d_time, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&d_io, sizeof(int32_t) * 4 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(d_vtx, vtx.data(), sizeof(float4) * vtx.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_meta, meta.data(), sizeof(uint32_t) * meta.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_sw, sw.data(), sizeof(float) * sw.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_toi_pairs(n, d_vtx, d_meta, d_sw, dc, d_time, d_io, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(time_out, d_time, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(iout4, d_io, sizeof(int32_t) * 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(d_vtx); cudaFree(d_meta); cudaFree(d_sw); cudaFree(d_time); cudaFree(d_io);
+    return e == cudaSuccess ? PRGPU_OK : PRGPU_ECUDA;
 }
 
 int prgpu_prepare_bodies(const prgpu_batch_desc* ds, float* pos3, float* vel3, float* mass4) {
@@ -705,9 +824,10 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.w_root, W); AL(d.w_bounds, W);
     uint32_t* w_order;
     AL(w_order, W); d.w_order = w_order;
-    AL(d.w_kc, W + 1); AL(d.w_kj, W + 1);
+    AL(d.w_kc, W + 1); AL(d.w_kj, W + 1); AL(d.w_toi, W);
     AL(d.b_pos1, N); AL(d.b_pos0, N); AL(d.b_vel, N); AL(d.b_xf, N); AL(d.b_mass, N); AL(d.b_acc, N);
     AL(d.b_damp, N); AL(d.b_flags, N); AL(d.b_uat, N); AL(d.b_world, N); AL(d.b_island, N);
+    AL(d.b_alpha0, N);
     AL(d.b_jnt_off, N + 1); AL(d.b_jnt_other, jother.size()); AL(d.b_jnt_cc, jcc.size());
     AL(d.isl_awake, N); ALS(d.isl_sep, (size_t)N * kMaxPosIters); ALS(d.isl_jok, (size_t)N * kMaxPosIters); AL(d.isl_uat, N);
     AL(d.s_body, S); AL(d.s_meta, S); AL(d.s_voff, S); AL(d.s_radius, S); AL(d.s_mat, S); AL(d.s_filter, S);
@@ -716,7 +836,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_imp, J);
     AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
     AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C);
-    AL(d.cs_colour, C); AL(d.j_colour, J);
+    AL(d.cs_colour, C); AL(d.j_colour, J); AL(d.cs_toi, C); AL(d.cs_seq, C);
     AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
     ALS(d.n_key, K); ALS(d.n_key_alt, K); ALS(d.n_val, K); ALS(d.n_val_alt, K);
     AL(d.l_key, S); AL(d.l_key_alt, S); AL(d.l_idx, S); AL(d.l_idx_alt, S); AL(d.l_leaf_box, S);
@@ -805,6 +925,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ok &= up(d.j_imp, j_zero.data(), sizeof(float4) * J);
     ok &= up(d.j_m1, j_zero.data(), sizeof(float4) * J);
     ok &= cudaMemsetAsync(d.b_uat, 0, sizeof(float) * N, w->stream) == cudaSuccess;
+    ok &= cudaMemsetAsync(d.b_alpha0, 0, sizeof(float) * N, w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.cnt, 0, sizeof(Counters), w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.j_colour, 0xff, sizeof(uint32_t) * std::max<uint32_t>(J, 1), w->stream) == cudaSuccess;
     if (!ok) return bail(fail(w, PRGPU_ECUDA, "upload failed"));
@@ -827,6 +948,8 @@ int prgpu_world_destroy(prgpu_world* w) {
     for (int k = 0; k < 8; ++k)
         if (w->graph_ev[k]) cudaEventDestroy(w->graph_ev[k]);
     if (w->graph_def) cudaGraphDestroy(w->graph_def);
+    for (auto g : w->toi_graph)
+        if (g) cudaGraphExecDestroy(g);
     for (void* p : w->allocs) cudaFree(p);
     if (w->h_cnt) cudaFreeHost(w->h_cnt);
     if (w->stream) cudaStreamDestroy(w->stream);
@@ -834,28 +957,46 @@ int prgpu_world_destroy(prgpu_world* w) {
     return PRGPU_OK;
 }
 
+void fill_stats(const Counters& c, prgpu_step_stats* st) {
+    st->contactsAdded = c.st_contacts_added;
+    st->contactsDestroyed = c.st_contacts_destroyed;
+    st->contactsUpdated = c.st_contacts_updated;
+    st->islandsFound = c.st_islands_found;
+    st->islandsSolved = c.st_islands_solved;
+    st->bodiesSlept = c.st_bodies_slept;
+    st->proxiesMoved = c.st_proxies_moved;
+    st->sumPosIters = c.st_sum_pos_iters;
+    st->liveContacts = c.n_live;
+    st->activeConstraints = c.n_active;
+    st->colours = c.n_colours;
+    st->serialConstraints = c.colour_off[kSerialColour + 1] - c.colour_off[kSerialColour];
+    st->minSeparation = c.st_min_separation;
+    st->maxIncImpulse = c.st_max_inc_impulse;
+    st->toiIslandsFound = c.st_toi_islands_found;
+    st->toiIslandsSolved = c.st_toi_islands_solved;
+    st->toiContactsFound = c.st_toi_found;
+    st->toiContactsAtMaxSubSteps = c.st_toi_at_max_substeps;
+    st->toiContactsUpdatedToi = c.st_toi_updated_toi;
+    st->toiContactsUpdatedTouching = c.st_toi_updated_touching;
+    st->toiContactsSkippedTouching = c.st_toi_skipped_touching;
+    st->toiContactsAdded = c.st_toi_contacts_added;
+    st->toiProxiesMoved = c.st_toi_proxies_moved;
+    st->toiSumPosIters = c.st_toi_sum_pos_iters;
+    st->toiSumVelIters = c.st_toi_sum_vel_iters;
+    st->toiMaxDistIters = c.st_toi_max_dist_iters;
+    st->toiMaxToiIters = c.st_toi_max_toi_iters;
+    st->toiMaxRootIters = c.st_toi_max_root_iters;
+    st->toiRounds = c.toi_rounds;
+    st->toiMinSeparation = c.st_toi_min_separation;
+    st->toiMaxIncImpulse = c.st_toi_max_inc_impulse;
+}
+
 int prgpu_step(prgpu_world* w, const prgpu_step_conf* conf, prgpu_step_stats* st) {
     if (!w) return PRGPU_EINVAL;
     CU(cudaSetDevice(w->device));
     const int rc = run_steps(w, conf, 1, true);
     if (rc) return rc;
-    if (st) {
-        const Counters& c = *w->h_cnt;
-        st->contactsAdded = c.st_contacts_added;
-        st->contactsDestroyed = c.st_contacts_destroyed;
-        st->contactsUpdated = c.st_contacts_updated;
-        st->islandsFound = c.st_islands_found;
-        st->islandsSolved = c.st_islands_solved;
-        st->bodiesSlept = c.st_bodies_slept;
-        st->proxiesMoved = c.st_proxies_moved;
-        st->sumPosIters = c.st_sum_pos_iters;
-        st->liveContacts = c.n_live;
-        st->activeConstraints = c.n_active;
-        st->colours = c.n_colours;
-        st->serialConstraints = c.colour_off[kSerialColour + 1] - c.colour_off[kSerialColour];
-        st->minSeparation = c.st_min_separation;
-        st->maxIncImpulse = c.st_max_inc_impulse;
-    }
+    if (st) fill_stats(*w->h_cnt, st);
     return PRGPU_OK;
 }
 
@@ -875,6 +1016,10 @@ int prgpu_step_profiled(prgpu_world* w, const prgpu_step_conf* conf, float* phas
     for (int k = 0; k <= kPhases; ++k) CU(cudaEventCreate(&ev[k]));
     enqueue_step(w, conf->deltaTime != 0.f, ev);
     CU(cudaGetLastError());
+    if (conf->deltaTime != 0.f && conf->doToi && (rc = run_toi_phase(w)) != PRGPU_OK) {
+        for (int k = 0; k <= kPhases; ++k) cudaEventDestroy(ev[k]);
+        return rc;
+    }
     rc = check_device_error(w);
     if (!rc && phase_ms) {
         for (int k = 0; k < n_phases && k < kPhases; ++k) {
@@ -884,16 +1029,7 @@ int prgpu_step_profiled(prgpu_world* w, const prgpu_step_conf* conf, float* phas
         }
     }
     for (int k = 0; k <= kPhases; ++k) cudaEventDestroy(ev[k]);
-    if (!rc && st) {
-        const Counters& c = *w->h_cnt;
-        st->contactsAdded = c.st_contacts_added; st->contactsDestroyed = c.st_contacts_destroyed;
-        st->contactsUpdated = c.st_contacts_updated; st->islandsFound = c.st_islands_found;
-        st->islandsSolved = c.st_islands_solved; st->bodiesSlept = c.st_bodies_slept;
-        st->proxiesMoved = c.st_proxies_moved; st->sumPosIters = c.st_sum_pos_iters;
-        st->liveContacts = c.n_live; st->activeConstraints = c.n_active; st->colours = c.n_colours;
-        st->serialConstraints = c.colour_off[kSerialColour + 1] - c.colour_off[kSerialColour];
-        st->minSeparation = c.st_min_separation; st->maxIncImpulse = c.st_max_inc_impulse;
-    }
+    if (!rc && st) fill_stats(*w->h_cnt, st);
     return rc;
 }
 
@@ -1486,6 +1622,7 @@ int prgpu_adjoint_forward(prgpu_world* w, const prgpu_step_conf* conf, int n_ste
     AdjWindow* a = w->adj;
     if (!a) return fail(w, PRGPU_ESTATE, "no adjoint window is open");
     if (conf->deltaTime == 0.f) return fail(w, PRGPU_EINVAL, "adjoint steps need deltaTime > 0");
+    if (conf->doToi) return fail(w, PRGPU_EINVAL, "the adjoint differentiates the regular phase: doToi must be 0");
     if (a->conf_set && std::memcmp(&a->conf, conf, sizeof(*conf)) != 0)
         return fail(w, PRGPU_EINVAL, "one step configuration per adjoint window");
     a->conf = *conf;

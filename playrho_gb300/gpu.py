@@ -28,17 +28,31 @@ CONF_FLOATS = (
     "linearSleepTolerance", "angularSleepTolerance", "displaceMultiplier", "aabbExtension",
     "maxCirclesRatio")
 CONF_INTS = ("regVelocityIters", "regPositionIters", "doWarmStart", "doBlocksolve")
+CONF_TOI_FLOATS = ("toiResolutionRate", "toiMinSeparation", "toiMinMomentum", "targetDepth", "tolerance")
+CONF_TOI_INTS = ("toiVelocityIters", "toiPositionIters", "maxToiRootIters", "maxToiIters", "maxDistanceIters",
+                 "maxSubSteps", "doToi")
+TOI_STATS = ("toiIslandsFound", "toiIslandsSolved", "toiContactsFound", "toiContactsAtMaxSubSteps",
+             "toiContactsUpdatedToi", "toiContactsUpdatedTouching", "toiContactsSkippedTouching",
+             "toiContactsAdded", "toiProxiesMoved", "toiSumPosIters", "toiSumVelIters", "toiMaxDistIters",
+             "toiMaxToiIters", "toiMaxRootIters", "toiRounds")
+# ToiOutput::State as prgpu_time_of_impact reports it
+TOI_STATES = ("unknown", "overlapped", "touching", "separated", "maxRootIters", "nextAfter", "maxToiIters",
+              "belowMinTarget", "maxDistIters", "targetDepthExceedsTotalRadius", "minTargetSquaredOverflow",
+              "maxTargetSquaredOverflow")
 
 
 class StepConf(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_float) for n in CONF_FLOATS] + [(n, ctypes.c_int32) for n in CONF_INTS]
+    _fields_ = ([(n, ctypes.c_float) for n in CONF_FLOATS] + [(n, ctypes.c_int32) for n in CONF_INTS]
+                + [(n, ctypes.c_float) for n in CONF_TOI_FLOATS] + [(n, ctypes.c_int32) for n in CONF_TOI_INTS])
 
 
 class StepStats(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_uint32) for n in (
+    _fields_ = ([(n, ctypes.c_uint32) for n in (
         "contactsAdded", "contactsDestroyed", "contactsUpdated", "islandsFound", "islandsSolved",
         "bodiesSlept", "proxiesMoved", "sumPosIters", "liveContacts", "activeConstraints", "colours",
         "serialConstraints")] + [("minSeparation", ctypes.c_float), ("maxIncImpulse", ctypes.c_float)]
+        + [(n, ctypes.c_uint32) for n in TOI_STATS]
+        + [("toiMinSeparation", ctypes.c_float), ("toiMaxIncImpulse", ctypes.c_float)])
 
 
 class BatchDesc(ctypes.Structure):
@@ -113,6 +127,7 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_adjoint_profile.argtypes = [P, P, P, P]
     lib.prgpu_adjoint_trim.argtypes = []
     lib.prgpu_autotune.argtypes = [P, ctypes.POINTER(StepConf), I, ctypes.POINTER(Schedule)]
+    lib.prgpu_time_of_impact.argtypes = [I, U, P, P, P, P, ctypes.POINTER(StepConf), P, P]
     _LIB = lib
     return lib
 
@@ -127,16 +142,49 @@ def exported_symbols() -> List[str]:
         "prgpu_set_warp_world_max_bodies", "prgpu_get_warp_world_max_bodies", "prgpu_autotune",
         "prgpu_set_stage_bytes", "prgpu_get_stage_bytes", "prgpu_adjoint_begin", "prgpu_adjoint_forward",
         "prgpu_adjoint_backward", "prgpu_adjoint_tangent", "prgpu_adjoint_info", "prgpu_adjoint_end",
-        "prgpu_adjoint_profile", "prgpu_adjoint_trim"]
+        "prgpu_adjoint_profile", "prgpu_adjoint_trim", "prgpu_time_of_impact"]
 
 
 def default_conf(**overrides) -> StepConf:
+    """StepConf defaults (prgpu_default_step_conf) with the time-of-impact phase
+    off unless asked for (doToi=1, the reference's own default): the regular
+    phase alone is what the batch workloads and most parity checks run."""
     lib = load_library()
     c = StepConf()
     lib.prgpu_default_step_conf(ctypes.byref(c))
+    c.doToi = 0
     for k, v in overrides.items():
         setattr(c, k, v)
     return c
+
+
+def time_of_impact(pairs, device: int = 0, **conf):
+    """GetToiViaSat on the GPU for a list of pairs ((verts_a, radius_a, sweep_a),
+    (verts_b, radius_b, sweep_b)); a sweep is pos0 x y angle, pos1 x y angle,
+    alpha0, local centre x y.  Returns (times, states, toi iterations, max
+    distance iterations, max root iterations) as numpy arrays."""
+    lib = load_library()
+    nv, verts, rad, sw = [], [], [], []
+    for pair in pairs:
+        for v, r, s in pair:
+            v = np.asarray(v, np.float32).reshape(-1, 2)
+            nv.append(len(v))
+            verts.append(v)
+            rad.append(r)
+            sw.append(np.asarray(s, np.float32).reshape(9))
+    n = len(pairs)
+    nv = np.asarray(nv, np.uint32)
+    verts = np.ascontiguousarray(np.concatenate(verts) if verts else np.zeros((0, 2), np.float32))
+    rad = np.asarray(rad, np.float32)
+    sw = np.ascontiguousarray(np.stack(sw) if sw else np.zeros((0, 9), np.float32))
+    t = np.zeros(n, np.float32)
+    io = np.zeros((n, 4), np.int32)
+    c = default_conf(**conf)
+    rc = lib.prgpu_time_of_impact(device, n, nv.ctypes.data, verts.ctypes.data, rad.ctypes.data, sw.ctypes.data,
+                                  ctypes.byref(c), t.ctypes.data, io.ctypes.data)
+    if rc:
+        raise PrgpuError(rc, "prgpu_time_of_impact failed")
+    return t, io[:, 0], io[:, 1], io[:, 2], io[:, 3]
 
 
 def _ptr(a: np.ndarray):

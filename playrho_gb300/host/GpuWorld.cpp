@@ -76,6 +76,7 @@ prgpu::HostBody ToHost(const Body& value, const Body* before, const prgpu::HostB
     if (IsAwake(value)) flags |= PRGPU_BODY_AWAKE;
     if (IsFixedRotation(value)) flags |= PRGPU_BODY_FIXED_ROTATION;
     if (IsEnabled(value)) flags |= PRGPU_BODY_ENABLED;
+    if (IsImpenetrable(value) && GetType(value) == BodyType::Dynamic) flags |= PRGPU_BODY_BULLET;
     h.flags = flags;
     // the mass data the reference computed (ResetMassData / SetMassData)
     h.explicit_mass = true;
@@ -169,6 +170,18 @@ prgpu_step_conf ToAbi(const StepConf& c) {
     s.regPositionIters = static_cast<int32_t>(c.regPositionIters);
     s.doWarmStart = c.doWarmStart ? 1 : 0;
     s.doBlocksolve = c.doBlocksolve ? 1 : 0;
+    s.toiResolutionRate = F(c.toiResolutionRate);
+    s.toiMinSeparation = F(StripUnit(c.toiMinSeparation));
+    s.toiMinMomentum = F(StripUnit(c.toiMinMomentum));
+    s.targetDepth = F(StripUnit(Length{c.targetDepth}));
+    s.tolerance = F(StripUnit(Length{c.tolerance}));
+    s.toiVelocityIters = static_cast<int32_t>(c.toiVelocityIters);
+    s.toiPositionIters = static_cast<int32_t>(c.toiPositionIters);
+    s.maxToiRootIters = static_cast<int32_t>(c.maxToiRootIters);
+    s.maxToiIters = static_cast<int32_t>(c.maxToiIters);
+    s.maxDistanceIters = static_cast<int32_t>(c.maxDistanceIters);
+    s.maxSubSteps = static_cast<int32_t>(c.maxSubSteps);
+    s.doToi = c.doToi ? 1 : 0;
     return s;
 }
 
@@ -279,6 +292,22 @@ StepStats Step(GpuWorld& w, const StepConf& conf) {
     stats.reg.sumPosIters = s.sumPosIters;
     stats.reg.minSeparation = Real(s.minSeparation) * Meter;
     stats.reg.maxIncImpulse = Real(s.maxIncImpulse) * NewtonSecond;
+    stats.toi.islandsFound = s.toiIslandsFound;
+    stats.toi.islandsSolved = s.toiIslandsSolved;
+    stats.toi.contactsFound = s.toiContactsFound;
+    stats.toi.contactsAtMaxSubSteps = s.toiContactsAtMaxSubSteps;
+    stats.toi.contactsUpdatedToi = s.toiContactsUpdatedToi;
+    stats.toi.contactsUpdatedTouching = s.toiContactsUpdatedTouching;
+    stats.toi.contactsSkippedTouching = s.toiContactsSkippedTouching;
+    stats.toi.contactsAdded = s.toiContactsAdded;
+    stats.toi.proxiesMoved = s.toiProxiesMoved;
+    stats.toi.sumPosIters = s.toiSumPosIters;
+    stats.toi.sumVelIters = s.toiSumVelIters;
+    stats.toi.maxDistIters = static_cast<ToiStepStats::dist_iter_type>(s.toiMaxDistIters);
+    stats.toi.maxToiIters = static_cast<ToiStepStats::toi_iter_type>(s.toiMaxToiIters);
+    stats.toi.maxRootIters = static_cast<ToiStepStats::root_iter_type>(s.toiMaxRootIters);
+    stats.toi.minSeparation = Real(s.toiMinSeparation) * Meter;
+    stats.toi.maxIncImpulse = Real(s.toiMaxIncImpulse) * NewtonSecond;
     return stats;
 }
 

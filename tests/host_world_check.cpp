@@ -29,6 +29,7 @@ int main() {
     std::vector<uint32_t> body_ids;
     prgpu_step_conf conf;
     prgpu_default_step_conf(&conf);
+    conf.doToi = 0;  // compared with the batch API's regular-phase steps
     std::string line;
     try {
         while (std::getline(std::cin, line)) {

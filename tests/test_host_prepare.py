@@ -53,9 +53,14 @@ def test_invalid_descriptions_rejected(lib):
 
 
 def test_library_exports(lib):
-    for name in gpu.exported_symbols():
+    import os
+    import re
+    header = os.path.join(os.path.dirname(__file__), "..", "include", "prgpu.h")
+    declared = set(re.findall(r"^int (prgpu_\w+)\(", open(header).read(), re.M))
+    assert declared >= set(gpu.exported_symbols())
+    for name in sorted(declared):
         assert hasattr(lib, name), name
-    assert lib.prgpu_abi_version() == 1
+    assert lib.prgpu_abi_version() == 2
 
 
 def test_convex_hull_matches_scene_builder(lib):

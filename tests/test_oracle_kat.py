@@ -50,10 +50,10 @@ def test_gravitational_body_movement():
 
 
 # ---- HelloWorld/ExpectedOutput.txt: x, y, angle of the falling disk after each
-# of 60 default steps.  Lines 47-50 are where the disk lands; there the reference
-# runs its time-of-impact sub-stepping (StepConf::doToi defaults to true), which
-# this step does not restate, so those four lines are checked against the
-# reference's own doToi = false run (tests/golden/ref_helloworld.npz) instead.
+# of 60 default steps.  Lines 47-50 are where the disk lands and the reference's
+# time-of-impact sub-stepping (StepConf::doToi, on by default) acts: with doToi
+# every line must match; without it those four lines differ (they are checked
+# against the reference's own doToi = false run, tests/golden/ref_helloworld.npz).
 HELLO_Y = ("4.00 3.99 3.98 3.97 3.96 3.94 3.92 3.90 3.88 3.85 3.82 3.79 3.75 3.71 3.67 3.63 3.58 3.53 3.48 "
            "3.43 3.37 3.31 3.25 3.18 3.12 3.04 2.97 2.89 2.82 2.73 2.65 2.56 2.47 2.38 2.28 2.19 2.09 1.98 "
            "1.88 1.77 1.66 1.54 1.42 1.30 1.18 1.06 1.00 1.00 1.00 1.00 1.00 1.00 1.00 1.00 1.00 1.00 1.00 "
@@ -61,7 +61,8 @@ HELLO_Y = ("4.00 3.99 3.98 3.97 3.96 3.94 3.92 3.90 3.88 3.85 3.82 3.79 3.75 3.7
 TOI_LINES = {46, 47, 48, 49}
 
 
-def test_helloworld_trajectory():
+@pytest.mark.parametrize("do_toi", [0, 1])
+def test_helloworld_trajectory(do_toi):
     sb = scenes.SceneBuilder()
     g = sb.body(scenes.STATIC, 0.0, -10.0)
     sb.box(g, 50.0, 10.0)
@@ -69,10 +70,10 @@ def test_helloworld_trajectory():
     sb.disk(b, 1.0)
     ow = oracle.OracleWorld(sb.build())
     for i in range(60):
-        ow.step()
+        ow.step(doToi=do_toi)
         xf = ow.bodies()["xf"][1]
         line = f"{xf[0]:5.2f}{xf[1]:5.2f}{math.atan2(xf[3], xf[2]):5.2f}"
-        if i not in TOI_LINES:
+        if do_toi or i not in TOI_LINES:
             assert line == f" 0.00{float(HELLO_Y[i]):5.2f} 0.00", (i, line)
 
 
