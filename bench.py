@@ -51,13 +51,17 @@ def parse():
                    help="untimed steps that bring the scenes to their contact-rich state (default per workload)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-adjoint", action="store_true", help="skip the StepAdjoint measurement")
+    p.add_argument("--no-toi", action="store_true", help="skip the time-of-impact (doToi) measurement")
+    p.add_argument("--toi", action="store_true",
+                   help="run the workload's timed steps with the time-of-impact phase on (doToi = 1)")
     p.add_argument("--sweeps", default="auto", choices=["auto", "grid", "per_world"],
                    help="scheduling of the colour sweeps (auto: one CTA per world for >= 64 worlds)")
     p.add_argument("--kernels-only", action="store_true",
                    help="only the warm-up and timed steps (for a profiler launch list)")
     p.add_argument("--workload", default="batched", choices=list(WORKLOADS),
                    help="batched: the headline batch (default); world100k: one world of 100,000 shapes in a "
-                        "1000 m box; chains256: 256 worlds of 8,000 free shapes + 64 revolute chains of 32 links")
+                        "1000 m box; chains256: 256 worlds of 8,000 free shapes + 64 revolute chains of 32 links; "
+                        "bullets1024: 1024 worlds of 40 fast shapes in closed boxes with the time-of-impact phase")
     return p.parse_args()
 
 
@@ -67,6 +71,8 @@ WORKLOADS = {
     "world100k": ("one world: 100,000 shapes (disks + 3..8-gons) in a 1000 m box, seed 0", {}, 60),
     "chains256": ("{n} worlds x (8,000 free shapes + 64 chains x 32 links on revolute joints), seed 3",
                   {"deltaTime": 1.0 / 120.0, "regVelocityIters": 10, "regPositionIters": 4}, 120),
+    "bullets1024": ("{n} worlds x 40 fast disks and 3..8-gons (60..180 m/s, half bullets) in a closed 30 m box, "
+                    "seed 9, time-of-impact phase on", {"doToi": 1}, 3),
 }
 
 
@@ -79,6 +85,10 @@ def workload(args):
         rng = np.random.default_rng(3)
         n = args.worlds if args.worlds != 4096 else 256
         return [scenes.chains_world(rng) for _ in range(n)]
+    if args.workload == "bullets1024":
+        rng = np.random.default_rng(9)
+        n = args.worlds if args.worlds != 4096 else 1024
+        return [scenes.bullets(40, rng, size=15.0) for _ in range(n)]
     return scenes.batched_worlds(args.worlds, seed=1)
 
 
@@ -268,6 +278,9 @@ def run_ours(args, rank, world_size, local, dist):
     build.build()
     worlds = workload(args)
     desc, overrides, settle = WORKLOADS[args.workload]
+    if args.toi:
+        overrides = dict(overrides, doToi=1)
+        desc += ", time-of-impact phase on"
     if args.settle is None:
         args.settle = settle
     n_dyn = sum(int((w.body_type == 2).sum()) for w in worlds)
@@ -292,8 +305,17 @@ def run_ours(args, rank, world_size, local, dist):
     with Clocks(local) as clk:
         nvtx[0]("timed")  # a profiler can select the timed steps by this range
         for _ in range(args.steps):
-            batch.step_async(1, conf)
-            ph = batch.last_step_phase_ms()
+            if conf.doToi:
+                # the TOI loop syncs with the host between rounds: host clock over the whole step
+                t = time.perf_counter()
+                batch.step_n(1, conf)
+                ms = (time.perf_counter() - t) * 1e3
+                ph = batch.last_step_phase_ms()
+                ph["toi"] = ms - ph["step"]
+                ph["step"] = ms
+            else:
+                batch.step_async(1, conf)
+                ph = batch.last_step_phase_ms()
             phases.append(ph)
             step_ms.append(ph["step"])
         batch.synchronize()
@@ -401,12 +423,79 @@ def run_ours(args, rank, world_size, local, dist):
         "clocks": clocks,
     }
     out["gpu_launches"] = launches_per_step(batch) * args.steps
+    if args.workload == "batched" and not args.no_toi:
+        out["toi"] = toi_bench(batch, overrides, local, n_dyn)
     if args.workload == "batched" and not args.no_adjoint:
         out["adjoint"] = adjoint_bench(local)
     if args.workload == "chains256" and not args.no_adjoint:
         batch.close()
         out["adjoint"] = adjoint_window_bench(worlds, conf, local, args.settle)
     print(json.dumps(out), flush=True)
+
+
+def _timed_steps(batch, conf, steps):
+    """Host-clock seconds of `steps` synchronous steps and their statistics."""
+    stats = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        stats.append(batch.step(conf))
+    return time.perf_counter() - t0, stats
+
+
+def toi_bench(batch, overrides, device, n_dyn, steps=10, n_bullet_worlds=1024, bullet_steps=20):
+    """The step with the time-of-impact phase on (StepConf::doToi, the reference's
+    default).  (1) The settled headline batch: body-steps/s with and without the
+    TOI phase, its rounds and events per step.  (2) A TOI-heavy batch: 1024 worlds
+    of 40 fast disks and polygons (60-180 m/s, half of them bullets) in closed
+    15 m boxes, with the single-threaded CPU oracle on a sample of it beside it.
+    Host clock around synchronous prgpu_step calls (the TOI loop reads the device
+    counters between rounds, so these steps are not graph replays)."""
+    from playrho_gb300 import gpu, scenes
+
+    off = gpu.default_conf(**overrides)
+    on = gpu.default_conf(**overrides, doToi=1)
+    for c in (on, off):
+        _timed_steps(batch, c, 2)
+    t_on, st_on = _timed_steps(batch, on, steps)
+    t_off, _ = _timed_steps(batch, off, steps)
+    rounds = [s["toiRounds"] for s in st_on]
+    headline = {
+        "value": n_dyn * steps / t_on, "unit": UNIT, "ms_per_step": t_on / steps * 1e3,
+        "without_toi_ms_per_step": t_off / steps * 1e3,
+        "toi_rounds_per_step": statistics.mean(rounds), "toi_events_per_step":
+            statistics.mean(s["toiContactsFound"] for s in st_on),
+        "toi_computed_per_step": statistics.mean(s["toiContactsUpdatedToi"] for s in st_on)}
+    rng = np.random.default_rng(9)
+    worlds = [scenes.bullets(40, rng, size=15.0) for _ in range(n_bullet_worlds)]
+    nb = sum(int((w.body_type == 2).sum()) for w in worlds)
+    g = gpu.GpuBatch(worlds, device=device)
+    _timed_steps(g, on, 3)
+    t_b, st_b = _timed_steps(g, on, bullet_steps)
+    g.close()
+    from oracle import oracle
+
+    sample = worlds[:16]
+    ows = [oracle.OracleWorld(w) for w in sample]
+    for o in ows:
+        for _ in range(3):
+            o.step(doToi=1)
+    nbs = sum(int((w.body_type == 2).sum()) for w in sample)
+    t0 = time.perf_counter()
+    for _ in range(bullet_steps):
+        for o in ows:
+            o.step(doToi=1)
+    t_cpu = time.perf_counter() - t0
+    bullets = {
+        "value": nb * bullet_steps / t_b, "unit": UNIT, "ms_per_step": t_b / bullet_steps * 1e3,
+        "workload": f"{n_bullet_worlds} worlds x 40 fast disks and 3..8-gons (60..180 m/s, half bullets) in a "
+                    f"closed 30 m box, seed 9, steps 4..{3 + bullet_steps}",
+        "toi_rounds_per_step": statistics.mean(s["toiRounds"] for s in st_b),
+        "toi_events_per_step": statistics.mean(s["toiContactsFound"] for s in st_b),
+        "toi_computed_per_step": statistics.mean(s["toiContactsUpdatedToi"] for s in st_b),
+        "cpu_baseline": {"value": nbs * bullet_steps / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"16 of {n_bullet_worlds} worlds, {bullet_steps} steps with doToi, oracle FP32"}}
+    return {"headline_batch": headline, "bullets": bullets,
+            "timing": "host clock around synchronous steps (the TOI loop syncs between rounds)"}
 
 
 def adjoint_bench(device, n_worlds=64, steps=240, every=16):

@@ -36,9 +36,26 @@ constexpr uint32_t kToiIslandContacts = 48;
 constexpr uint32_t kToiIslandBodies = kToiIslandContacts + 1;
 constexpr unsigned kFull = 0xffffffffu;
 
-// An event's island and its solver state, in one warp's shared memory.
+constexpr uint32_t kToiBatch = 64;       // contacts gathered and ordered at once by a warp
+
+// Contacts whose times of impact a warp computes together: their sweeps are
+// recorded in contact-list order (the Advance0 of each contact sees the ones
+// before it), then the lanes run GetToiViaSat on them side by side.
+struct ToiBatch {
+    uint32_t slot[kToiBatch];
+    uint64_t seq[kToiBatch];
+    Sweep sA[kToiBatch], sB[kToiBatch];
+    float alpha0[kToiBatch];
+};
+
+// An event's island and its solver state, in one warp's shared memory.  The
+// velocity constraints are built only after the contacts have been gathered and
+// the missing times of impact computed, so they share their memory with those.
 struct ToiScratch {
-    VC vc[kToiIslandContacts];
+    union {
+        VC vc[kToiIslandContacts];
+        ToiBatch batch;
+    };
     float4 bp[kToiIslandBodies];   // body constraint position (x, y, angle)
     float4 bv[kToiIslandBodies];   // body constraint velocity
     float4 bm[kToiIslandBodies];   // invMass invRotI localCentre
@@ -227,6 +244,116 @@ __device__ __forceinline__ uint32_t warp_first_in_list(const DW& d, Seg sg, uint
     return bslot;
 }
 
+// Gathers the world's contacts that pass pred into (slot, seq) ordered by
+// creation sequence, i.e. in contact-list order.  Returns how many pass; only the
+// first kToiBatch are stored, so a larger count means the list is incomplete.
+template <class Pred>
+__device__ uint32_t warp_gather_in_list_order(const DW& d, Seg sg, uint32_t lane, Pred pred, uint32_t* slots,
+                                              uint64_t* seqs) {
+    uint32_t n = 0;
+    for (uint32_t base = sg.c0; base < sg.c1; base += 32u) {
+        const uint32_t i = base + lane;
+        uint32_t slot = kNone;
+        bool take = false;
+        if (i < sg.c1) {
+            slot = d.c_slot[i];
+            take = pred(slot);
+        }
+        const unsigned m = __ballot_sync(kFull, take);
+        if (take) {
+            const uint32_t at = n + (uint32_t)__popc(m & ((1u << lane) - 1u));
+            if (at < kToiBatch) { slots[at] = slot; seqs[at] = d.cs_seq[slot]; }
+        }
+        n += (uint32_t)__popc(m);
+    }
+    __syncwarp();
+    // rank sort by sequence (sequences are unique): each lane places two entries
+    const uint32_t k = min(n, kToiBatch);
+    uint32_t ms[2] = {kNone, kNone}, rk[2] = {0, 0};
+    uint64_t mq[2] = {0, 0};
+    for (int e = 0; e < 2; ++e) {
+        const uint32_t j = lane + 32u * (uint32_t)e;
+        if (j < k) {
+            ms[e] = slots[j]; mq[e] = seqs[j];
+            for (uint32_t o = 0; o < k; ++o) rk[e] += (seqs[o] < mq[e]) ? 1u : 0u;
+        }
+    }
+    __syncwarp();
+    for (int e = 0; e < 2; ++e)
+        if (ms[e] != kNone) { slots[rk[e]] = ms[e]; seqs[rk[e]] = mq[e]; }
+    __syncwarp();
+    return n;
+}
+
+// UpdateContactTOIs (AabbTreeWorld.cpp:1685-1750) for the world's contacts
+// without a time of impact, in contact-list order: lane 0 advances the sweeps
+// (cheap and order-dependent), then every lane computes times of impact.  Up
+// to kToiBatch such contacts are gathered at once (the usual case after an
+// event); beyond that lane 0 takes them one by one.
+__device__ void toi_update_world(const DW& d, Seg sg, ToiScratch& S, uint32_t lane) {
+    const DConf& c = *d.conf;
+    const ToiLimits L = toi_limits(c);
+    uint32_t at_max = 0;
+    for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u)
+        if (toi_candidate(d, d.c_slot[i], c.maxSubSteps) == 2) ++at_max;
+    if (at_max) atomicAdd(&d.cnt->st_toi_at_max_substeps, at_max);
+    int mdist = 0, mtoi = 0, mroot = 0;
+    uint32_t updated = 0;
+    ToiBatch& B = S.batch;
+    auto missing = [&](uint32_t s) { return toi_candidate(d, s, c.maxSubSteps) == 1; };
+    const uint32_t n = warp_gather_in_list_order(d, sg, lane, missing, B.slot, B.seq);
+    if (n > kToiBatch) {
+        // more than one gather holds: one contact per scan, in list order, on lane 0
+        for (uint32_t guard = 0; guard <= sg.c1 - sg.c0; ++guard) {
+            uint64_t q;
+            const uint32_t slot = warp_first_in_list(d, sg, 0, lane, missing, q);
+            if (slot == kNone) break;
+            if (lane == 0) {
+                compute_toi(d, slot, L, mdist, mtoi, mroot);
+                ++updated;
+            }
+            __syncwarp();
+        }
+    } else if (n > 0) {
+        const uint32_t k = n;
+        if (lane == 0) {
+            for (uint32_t j = 0; j < k; ++j) {
+                const uint2 bd = d.cs_body[B.slot[j]];
+                Sweep sA = body_sweep(d, bd.x), sB = body_sweep(d, bd.y);
+                const float alpha0 = maxf_(sA.a0, sB.a0);
+                sweep_advance0(sA, alpha0);
+                d.b_pos0[bd.x] = make_float4(sA.p0.x, sA.p0.y, sA.p0.a, d.b_pos0[bd.x].w);
+                d.b_alpha0[bd.x] = alpha0;
+                sweep_advance0(sB, alpha0);
+                d.b_pos0[bd.y] = make_float4(sB.p0.x, sB.p0.y, sB.p0.a, d.b_pos0[bd.y].w);
+                d.b_alpha0[bd.y] = alpha0;
+                B.sA[j] = sweep_normalized(sA);
+                B.sB[j] = sweep_normalized(sB);
+                B.alpha0[j] = alpha0;
+            }
+        }
+        __syncwarp();
+        for (uint32_t j = lane; j < k; j += 32u) {
+            const uint32_t slot = B.slot[j];
+            const uint2 pr = d.cs_proxy[slot];
+            Proxy PA, PB;
+            load_proxy(d, pr.x, PA);
+            load_proxy(d, pr.y, PB);
+            const ToiOut o = toi_via_sat(PA, B.sA[j], PB, B.sB[j], L);
+            const float a0 = B.alpha0[j];
+            d.cs_toi[slot] = (o.state == TOI_TOUCHING) ? minf_(a0 + (1.0f - a0) * o.time, 1.0f) : 1.0f;
+            d.cs_flags[slot] |= CF_TOI_VALID;
+            mdist = max(mdist, o.max_dist_iters);
+            mtoi = max(mtoi, o.toi_iters);
+            mroot = max(mroot, o.max_root_iters);
+            ++updated;
+        }
+        __syncwarp();
+    }
+    if (updated) atomicAdd(&d.cnt->st_toi_updated_toi, updated);
+    toi_iter_stats(d, mdist, mtoi, mroot);
+}
+
 // FlagForUpdating over the contacts of body b.
 __device__ __forceinline__ void flag_contacts_of(const DW& d, Seg sg, uint32_t b, uint32_t lane) {
     for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
@@ -355,65 +482,81 @@ __device__ void toi_solve_island(const DW& d, ToiScratch& S, float toi) {
     atomic_max_nonneg_float(&cn->st_toi_max_inc_impulse, maxInc);
 }
 
+// One contact of ProcessContactsForTOI (AabbTreeWorld.cpp:2084-2137) for body
+// x.  Returns false on island overflow.
+__device__ bool toi_process_contact(const DW& d, Seg sg, uint32_t x, bool impX, uint32_t slot, float toi,
+                                    ToiScratch& S, uint32_t lane) {
+    // lane 0 decides; 1: go on with the contact, 2: the other body moved
+    uint32_t act = 0, other = 0;
+    if (lane == 0) {
+        const uint32_t f = d.cs_flags[slot];
+        const uint2 bd = d.cs_body[slot];
+        other = (bd.x == x) ? bd.y : bd.x;
+        const uint32_t fo = d.b_flags[other];
+        if (!(f & (CF_TOI_ISL | CF_SENSOR)) && (impX || is_impenetrable(fo))) {
+            act = 1u;
+            if (!(fo & BF_TOI_ISL)) {
+                if (body_advance(d, other, toi, S.backup)) act |= 2u;
+            } else {
+                S.backup = body_sweep(d, other);
+            }
+        }
+    }
+    act = __shfl_sync(kFull, act, 0);
+    other = __shfl_sync(kFull, other, 0);
+    if (act & 2u) flag_contacts_of(d, sg, other, lane);
+    uint32_t ok = 1u;
+    if (lane == 0 && (act & 1u)) {
+        uint32_t f = d.cs_flags[slot];
+        if (f & CF_NEEDS_UPDATE) {
+            update_contact(d, slot);
+            ++S.updated;
+            f = d.cs_flags[slot];
+        } else {
+            ++S.skipped;
+        }
+        if (!(f & CF_TOUCHING)) {
+            body_set_sweep(d, other, S.backup);
+        } else if (S.nc >= kToiIslandContacts) {
+            ok = 0u;
+        } else {
+            S.isl_c[S.nc++] = slot;
+            d.cs_flags[slot] = f | CF_TOI_ISL;
+            const uint32_t fo = d.b_flags[other];
+            if (!(fo & BF_TOI_ISL)) {
+                d.b_flags[other] = fo | BF_TOI_ISL | (is_speedable(fo) ? BF_AWAKE : 0u);
+                S.isl_b[S.nb++] = other;
+            }
+        }
+    }
+    ok = __shfl_sync(kFull, ok, 0);
+    __syncwarp();
+    return ok != 0u;
+}
+
 // ProcessContactsForTOI (AabbTreeWorld.cpp:2061-2142) for body x, walking its
 // contacts in its contact-list order.  Returns false on island overflow.
 __device__ bool toi_process_contacts(const DW& d, Seg sg, uint32_t x, float toi, ToiScratch& S, uint32_t lane) {
     const bool impX = is_impenetrable(d.b_flags[x]);
+    auto touches_x = [&](uint32_t s) {
+        const uint2 bd = d.cs_body[s];
+        return bd.x == x || bd.y == x;
+    };
+    // the body's list, gathered once (the island solve reuses this memory later)
+    const uint32_t n = warp_gather_in_list_order(d, sg, lane, touches_x, S.batch.slot, S.batch.seq);
+    if (n <= kToiBatch) {
+        for (uint32_t j = 0; j < n; ++j)
+            if (!toi_process_contact(d, sg, x, impX, S.batch.slot[j], toi, S, lane)) return false;
+        return true;
+    }
+    // more contacts than one gather holds: take them one scan at a time
     uint64_t lo = 0;
     for (uint32_t guard = 0; guard <= sg.c1 - sg.c0; ++guard) {  // each pass takes a later contact
         uint64_t q;
-        const uint32_t slot = warp_first_in_list(d, sg, lo, lane, [&](uint32_t s) {
-            const uint2 bd = d.cs_body[s];
-            return bd.x == x || bd.y == x;
-        }, q);
+        const uint32_t slot = warp_first_in_list(d, sg, lo, lane, touches_x, q);
         if (slot == kNone) return true;
         lo = q + 1;
-        // lane 0 decides; 1: go on with the contact, 2: the other body moved
-        uint32_t act = 0, other = 0;
-        if (lane == 0) {
-            const uint32_t f = d.cs_flags[slot];
-            const uint2 bd = d.cs_body[slot];
-            other = (bd.x == x) ? bd.y : bd.x;
-            const uint32_t fo = d.b_flags[other];
-            if (!(f & (CF_TOI_ISL | CF_SENSOR)) && (impX || is_impenetrable(fo))) {
-                act = 1u;
-                if (!(fo & BF_TOI_ISL)) {
-                    if (body_advance(d, other, toi, S.backup)) act |= 2u;
-                } else {
-                    S.backup = body_sweep(d, other);
-                }
-            }
-        }
-        act = __shfl_sync(kFull, act, 0);
-        other = __shfl_sync(kFull, other, 0);
-        if (act & 2u) flag_contacts_of(d, sg, other, lane);
-        uint32_t ok = 1u;
-        if (lane == 0 && (act & 1u)) {
-            uint32_t f = d.cs_flags[slot];
-            if (f & CF_NEEDS_UPDATE) {
-                update_contact(d, slot);
-                ++S.updated;
-                f = d.cs_flags[slot];
-            } else {
-                ++S.skipped;
-            }
-            if (!(f & CF_TOUCHING)) {
-                body_set_sweep(d, other, S.backup);
-            } else if (S.nc >= kToiIslandContacts) {
-                ok = 0u;
-            } else {
-                S.isl_c[S.nc++] = slot;
-                d.cs_flags[slot] = f | CF_TOI_ISL;
-                const uint32_t fo = d.b_flags[other];
-                if (!(fo & BF_TOI_ISL)) {
-                    d.b_flags[other] = fo | BF_TOI_ISL | (is_speedable(fo) ? BF_AWAKE : 0u);
-                    S.isl_b[S.nb++] = other;
-                }
-            }
-        }
-        ok = __shfl_sync(kFull, ok, 0);
-        __syncwarp();
-        if (!ok) return false;
+        if (!toi_process_contact(d, sg, x, impX, slot, toi, S, lane)) return false;
     }
     return true;
 }
@@ -484,34 +627,8 @@ __device__ bool toi_event(const DW& d, Seg sg, uint32_t next, ToiScratch& S, uin
 // world w: missing times of impact, the soonest event, its island, then the
 // proxies of the islanded bodies.
 __device__ void toi_world_round(const DW& d, uint32_t w, ToiScratch& S, bool first, uint32_t lane) {
-    const DConf& c = *d.conf;
     const Seg sg = world_contacts(d, w);
-    if (!first) {
-        // UpdateContactTOIs in contact-list order (Advance0 makes the order matter)
-        uint32_t at_max = 0;
-        for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u)
-            if (toi_candidate(d, d.c_slot[i], c.maxSubSteps) == 2) ++at_max;
-        if (at_max) atomicAdd(&d.cnt->st_toi_at_max_substeps, at_max);
-        const ToiLimits L = toi_limits(c);
-        int mdist = 0, mtoi = 0, mroot = 0;
-        uint32_t updated = 0;
-        for (uint32_t guard = 0; guard <= sg.c1 - sg.c0; ++guard) {  // each pass gives one contact a time
-            uint64_t q;
-            const uint32_t slot = warp_first_in_list(d, sg, 0, lane, [&](uint32_t s) {
-                return toi_candidate(d, s, c.maxSubSteps) == 1;
-            }, q);
-            if (slot == kNone) break;
-            if (lane == 0) {
-                compute_toi(d, slot, L, mdist, mtoi, mroot);
-                ++updated;
-            }
-            __syncwarp();
-        }
-        if (lane == 0) {
-            if (updated) atomicAdd(&d.cnt->st_toi_updated_toi, updated);
-            toi_iter_stats(d, mdist, mtoi, mroot);
-        }
-    }
+    if (!first) toi_update_world(d, sg, S, lane);
     // GetSoonestContact (AabbTreeWorld.cpp:2870-2890): the smallest time below 1,
     // the earliest in the contact list among equal times
     float best = 1.0f;
