@@ -165,6 +165,10 @@ struct Counters {
     uint32_t toi_events;      // worlds that solved an event in the current round
     uint32_t toi_rounds;      // rounds run this step
     uint32_t toi_added_base;  // st_contacts_added before the current round's contact search
+    uint32_t toi_rebuild;     // rebuild the impenetrable list before the next round
+    uint32_t toi_scan_n;      // entries the list's compaction scans
+    uint32_t toi_imp_total;
+    uint32_t n_imp;           // impenetrable contacts listed
     // ToiStepStats counters (StepStats.hpp:117-151)
     uint32_t st_toi_found;
     uint32_t st_toi_islands_found;
@@ -210,6 +214,7 @@ struct DW {
     uint32_t* w_kc;          // [n_worlds + 1] first active contact (index into k_list) of each world
     uint32_t* w_kj;          // [n_worlds + 1] first active joint of each world
     uint32_t* w_toi;         // [n_worlds] time-of-impact loop of the world finished this step (1)
+    uint32_t* w_toi_ep;      // [n_worlds] the world's epoch counter in the TOI phase
     uint32_t n_world_big;    // leading entries of w_order swept by a whole CTA (the rest by a warp)
     uint32_t stage_bytes;    // dynamic shared memory of the per-world solver (world body state)
     StepTape* tape;          // recording for the adjoint (device struct), else null
@@ -225,6 +230,10 @@ struct DW {
     uint32_t* b_flags;
     float* b_uat;
     float* b_alpha0;         // Sweep::alpha0 (non-zero only inside the time-of-impact phase)
+    uint32_t* b_toi_ep;      // TOI phase: epoch of the body's last position change (0: none)
+    uint32_t* b_toi_rst;     // TOI phase: epoch at which its contacts' times of impact were voided
+    const uint32_t* b_shape_off;  // body -> shapes CSR
+    const uint32_t* b_shapes;
     uint32_t* b_world;
     uint32_t* b_island;      // union-find parent / island root
     uint32_t* b_jnt_off;     // body -> joints CSR (for joint collision filtering)
@@ -270,6 +279,10 @@ struct DW {
     uint32_t* cs_colour;     // colour the contact had in the last step (first choice next step)
     float* cs_toi;           // time of impact (valid with CF_TOI_VALID)
     uint64_t* cs_seq;        // creation sequence: orders a world's contacts as its contact list does
+    uint32_t* cs_toi_ep;     // TOI phase: epoch of the contact's last Update
+    uint32_t* cs_toi_at;     // TOI phase: epoch at which its time of impact was computed
+    uint64_t* t_key;         // TOI phase: key-sorted list of the impenetrable contacts
+    uint32_t* t_slot;
     uint32_t* j_colour;      // same for joints
     float4* m_head;          // ln.xy lp.xy
     float4* m_p0;            // lp.xy ni ti

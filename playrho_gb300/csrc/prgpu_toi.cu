@@ -11,15 +11,24 @@
 //    thread per contact (every body still has alpha0 = 0, so the order in which
 //    the reference visits them cannot matter);
 //  * each further round is one event per world, solved by one warp per world:
-//    the warp scans the world's contacts (lanes in parallel) to recompute missing
-//    times of impact in contact-list order, to find the soonest event and to walk
-//    a body's contacts in its contact-list order; lane 0 runs the sequential parts
+//    the lanes gather the world's contacts that need a time of impact (in
+//    contact-list order) and compute them side by side, find the soonest event,
+//    and gather the event bodies' contacts; lane 0 runs the sequential parts
 //    (advancing sweeps, CollideShapes, the island's position and velocity
 //    iterations) with the island held in shared memory;
 //  * between rounds the batch's broadphase (LBVH refit + query + AddContacts)
 //    runs for the proxies the round moved.
 // Contact-list order is the order contacts were created (cs_seq), as the
 // reference appends new contacts to the world's and each body's list.
+//
+// Scans stay short: only impenetrable contacts (one body static, kinematic or a
+// bullet) can have a time of impact, so the phase keeps a key-sorted list of
+// them (rebuilt when a round adds contacts) and scans a world's slice of it.
+// The reference's per-contact flags that the phase raises on every contact of a
+// body (FlagForUpdating, ResetBodyContactsForSolveTOI) become per-body epochs of
+// a per-world counter: a contact needs an update when one of its bodies moved
+// after its last update, and its time of impact is void when one of its bodies
+// was reset after it was computed.
 #include <cooperative_groups.h>
 
 #include "prgpu_contact_ops.cuh"
@@ -34,9 +43,8 @@ namespace {
 constexpr int kToiWarps = 4;             // worlds solved by one block of the round kernel
 constexpr uint32_t kToiIslandContacts = 48;
 constexpr uint32_t kToiIslandBodies = kToiIslandContacts + 1;
-constexpr unsigned kFull = 0xffffffffu;
-
 constexpr uint32_t kToiBatch = 64;       // contacts gathered and ordered at once by a warp
+constexpr unsigned kFull = 0xffffffffu;
 
 // Contacts whose times of impact a warp computes together: their sweeps are
 // recorded in contact-list order (the Advance0 of each contact sees the ones
@@ -62,9 +70,8 @@ struct ToiScratch {
     uint32_t bf[kToiIslandBodies]; // body flags
     uint32_t isl_b[kToiIslandBodies];
     uint32_t isl_c[kToiIslandContacts];
-    uint32_t moved[kToiIslandBodies];  // bodies whose position 1 the solve changed
     Sweep backup;
-    uint32_t nb, nc, n_moved, updated, skipped;
+    uint32_t nb, nc, updated, skipped, ep;
 };
 
 // Body-state accessor of the shared solver steps over an island (local indices).
@@ -88,7 +95,35 @@ PR_HD ToiLimits toi_limits(const DConf& c) {
     return L;
 }
 
+// One out-of-line copy each of the two largest routines the phase calls from
+// several places, to keep the round kernel's code small.
+__device__ __noinline__ ToiOut toi_of(const Proxy& A, const Sweep& sA, const Proxy& B, const Sweep& sB,
+                                      const ToiLimits& L) {
+    return toi_via_sat(A, sA, B, sB, L);
+}
+// Update (AabbTreeWorld.cpp:2587-2721) inside the phase; stamps the contact
+// with the world's current epoch.
+__device__ __noinline__ void toi_update(const DW& d, uint32_t slot, uint32_t ep) {
+    update_contact(d, slot);
+    d.cs_toi_ep[slot] = ep;
+}
+
 __device__ __forceinline__ uint32_t toi_count(uint32_t f) { return (f & kToiCountMask) >> kToiCountShift; }
+
+// NeedsUpdating: flagged, or a body moved since the contact's last update.
+__device__ __forceinline__ bool toi_needs_update(const DW& d, uint32_t slot) {
+    if (d.cs_flags[slot] & CF_NEEDS_UPDATE) return true;
+    const uint2 bd = d.cs_body[slot];
+    const uint32_t e = d.cs_toi_ep[slot];
+    return d.b_toi_ep[bd.x] > e || d.b_toi_ep[bd.y] > e;
+}
+// HasValidToi: computed, and neither body reset since.
+__device__ __forceinline__ bool toi_valid(const DW& d, uint32_t slot) {
+    if (!(d.cs_flags[slot] & CF_TOI_VALID)) return false;
+    const uint2 bd = d.cs_body[slot];
+    const uint32_t at = d.cs_toi_at[slot];
+    return at >= d.b_toi_rst[bd.x] && at >= d.b_toi_rst[bd.y];
+}
 
 __device__ __forceinline__ Sweep body_sweep(const DW& d, uint32_t b) {
     const float4 p0 = d.b_pos0[b], p1 = d.b_pos1[b], m = d.b_mass[b];
@@ -108,23 +143,21 @@ __device__ __forceinline__ void body_set_sweep(const DW& d, uint32_t b, const Sw
     const Xf xf = get_xf(s.p1.x, s.p1.y, s.p1.a, s.lc);
     d.b_xf[b] = make_float4(xf.p.x, xf.p.y, xf.q.x, xf.q.y);
 }
-// Advance (Body.hpp:1004-1009): Advance0, then position 1 = position 0.  Returns
-// whether either position changed (the test before FlagForUpdating).
-__device__ __forceinline__ bool body_advance(const DW& d, uint32_t b, float alpha, Sweep& backup) {
+// Advance (Body.hpp:1004-1009): Advance0, then position 1 = position 0.  When
+// either position changed, every contact of the body needs an update
+// (FlagForUpdating): the body takes a new epoch.
+__device__ __forceinline__ void body_advance(const DW& d, uint32_t b, float alpha, Sweep& backup, uint32_t& ep) {
     backup = body_sweep(d, b);
     Sweep s = backup;
     sweep_advance0(s, alpha);
     s.p1 = s.p0;
     body_set_sweep(d, b, s);
-    return pos_ne(s.p0, backup.p0) || pos_ne(s.p1, backup.p1);
+    if (pos_ne(s.p0, backup.p0) || pos_ne(s.p1, backup.p1)) d.b_toi_ep[b] = ++ep;
 }
 
-// A contact's time of impact (AabbTreeWorld.cpp:1717-1748): both bodies'
-// sweeps are advanced to the later alpha0, then GetToiViaSat on the
-// normalised sweeps.
-__device__ void compute_toi(const DW& d, uint32_t slot, const ToiLimits& L, int& mdist, int& mtoi, int& mroot) {
-    const uint2 bd = d.cs_body[slot];
-    const uint2 pr = d.cs_proxy[slot];
+// Both bodies' sweeps advanced to the later alpha0 (AabbTreeWorld.cpp:1717-1723);
+// the normalised sweeps GetToiViaSat is given.
+__device__ __forceinline__ float advance_pair(const DW& d, uint2 bd, Sweep& nA, Sweep& nB) {
     Sweep sA = body_sweep(d, bd.x), sB = body_sweep(d, bd.y);
     const float alpha0 = maxf_(sA.a0, sB.a0);
     sweep_advance0(sA, alpha0);
@@ -133,12 +166,21 @@ __device__ void compute_toi(const DW& d, uint32_t slot, const ToiLimits& L, int&
     sweep_advance0(sB, alpha0);
     d.b_pos0[bd.y] = make_float4(sB.p0.x, sB.p0.y, sB.p0.a, d.b_pos0[bd.y].w);
     d.b_alpha0[bd.y] = alpha0;
+    nA = sweep_normalized(sA);
+    nB = sweep_normalized(sB);
+    return alpha0;
+}
+
+// The time of impact of a contact from its advanced sweeps (:1725-1748).
+__device__ __forceinline__ void store_toi(const DW& d, uint32_t slot, const Sweep& sA, const Sweep& sB, float alpha0,
+                                          uint32_t ep, const ToiLimits& L, int& mdist, int& mtoi, int& mroot) {
+    const uint2 pr = d.cs_proxy[slot];
     Proxy A, B;
     load_proxy(d, pr.x, A);
     load_proxy(d, pr.y, B);
-    const ToiOut o = toi_via_sat(A, sweep_normalized(sA), B, sweep_normalized(sB), L);
-    const float toi = (o.state == TOI_TOUCHING) ? minf_(alpha0 + (1.0f - alpha0) * o.time, 1.0f) : 1.0f;
-    d.cs_toi[slot] = toi;
+    const ToiOut o = toi_of(A, sA, B, sB, L);
+    d.cs_toi[slot] = (o.state == TOI_TOUCHING) ? minf_(alpha0 + (1.0f - alpha0) * o.time, 1.0f) : 1.0f;
+    d.cs_toi_at[slot] = ep;
     d.cs_flags[slot] |= CF_TOI_VALID;
     mdist = max(mdist, o.max_dist_iters);
     mtoi = max(mtoi, o.toi_iters);
@@ -146,11 +188,11 @@ __device__ void compute_toi(const DW& d, uint32_t slot, const ToiLimits& L, int&
 }
 
 // The filter of UpdateContactTOIs (AabbTreeWorld.cpp:1692-1715) for a contact
-// without a time of impact: 1 compute, 2 at the sub-step limit, 0 skip.
+// of the impenetrable list: 1 compute, 2 at the sub-step limit, 0 skip.
 __device__ __forceinline__ int toi_candidate(const DW& d, uint32_t slot, int maxSubSteps) {
     const uint32_t f = d.cs_flags[slot];
-    if (f & (CF_TOI_VALID | CF_SENSOR)) return 0;
-    if (!(f & CF_IMPENETRABLE)) return 0;
+    if ((f & CF_SENSOR) || !(f & CF_IMPENETRABLE)) return 0;
+    if (toi_valid(d, slot)) return 0;
     if ((int)toi_count(f) >= maxSubSteps) return 2;
     const uint2 bd = d.cs_body[slot];
     if (!(d.b_flags[bd.x] & BF_AWAKE) && !(d.b_flags[bd.y] & BF_AWAKE)) return 0;
@@ -163,35 +205,76 @@ __device__ __forceinline__ void toi_iter_stats(const DW& d, int mdist, int mtoi,
     if (mroot) atomicMax(&d.cnt->st_toi_max_root_iters, (uint32_t)mroot);
 }
 
-// ---- phase set-up and round 0 -----------------------------------------------
+// ---- phase set-up, the impenetrable list and round 0 -----------------------------
 
 // Every body starts the phase with alpha0 = 0 (ResetBodiesForSolveTOI ended the
-// last one) and no proxy is marked moved.
+// last one), no epochs, no proxy marked moved; every world at epoch 1.
 __global__ void k_toi_begin(DW d) {
-    GRID_LOOP(b, d.n_bodies) d.b_alpha0[b] = 0.f;
+    GRID_LOOP(b, d.n_bodies) {
+        d.b_alpha0[b] = 0.f;
+        d.b_toi_ep[b] = 0u;
+        d.b_toi_rst[b] = 0u;
+    }
+    GRID_LOOP(s, d.contact_cap) {
+        d.cs_toi_ep[s] = 0u;
+        d.cs_toi_at[s] = 0u;
+    }
     GRID_LOOP(p, d.n_shapes) d.p_moved[p] = 0u;
-    GRID_LOOP(w, d.n_worlds) d.w_toi[w] = 0u;
+    GRID_LOOP(w, d.n_worlds) {
+        d.w_toi[w] = 0u;
+        d.w_toi_ep[w] = 1u;
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         d.cnt->n_moved = 0u;
         d.cnt->toi_rounds = 0u;
         d.cnt->toi_events = 0u;
+        d.cnt->toi_rebuild = 1u;
     }
 }
 
-// UpdateContactTOIs of the first loop iteration, one thread per live contact.
-// alpha0 is 0 for every body, so the Advance0 each contact applies to its two
-// bodies is the same idempotent update whichever thread stores it.
+// The impenetrable list: live contacts with an impenetrable body, key-sorted
+// (a stable compaction of the live list), rebuilt when contacts were added.
+__global__ void k_toi_list_flags(DW d) {
+    Counters* c = d.cnt;
+    const bool rebuild = c->toi_rebuild != 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) c->toi_scan_n = rebuild ? c->n_live : 0u;
+    if (!rebuild) return;
+    GRID_LOOP(i, c->n_live) {
+        const uint32_t f = d.cs_flags[d.c_slot[i]];
+        d.flags[i] = ((f & CF_IMPENETRABLE) && !(f & CF_SENSOR)) ? 1u : 0u;
+    }
+}
+__global__ void k_toi_list_scatter(DW d) {
+    if (!d.cnt->toi_rebuild) return;
+    GRID_LOOP(i, d.cnt->n_live) {
+        if (d.flags[i]) {
+            d.t_key[d.scan[i]] = d.c_key[i];
+            d.t_slot[d.scan[i]] = d.c_slot[i];
+        }
+    }
+}
+__global__ void k_toi_list_done(DW d) {
+    Counters* c = d.cnt;
+    if (c->toi_rebuild) c->n_imp = c->toi_imp_total;
+    c->toi_rebuild = 0u;
+}
+
+// UpdateContactTOIs of the first loop iteration, one thread per impenetrable
+// contact.  alpha0 is 0 for every body, so the Advance0 each contact applies to
+// its two bodies is the same idempotent update whichever thread stores it.
 __global__ void k_toi_first(DW d) {
     const DConf& c = *d.conf;
     const ToiLimits L = toi_limits(c);
     uint32_t updated = 0, at_max = 0;
     int mdist = 0, mtoi = 0, mroot = 0;
-    GRID_LOOP(i, d.cnt->n_live) {
-        const uint32_t slot = d.c_slot[i];
+    GRID_LOOP(i, d.cnt->n_imp) {
+        const uint32_t slot = d.t_slot[i];
         const int k = toi_candidate(d, slot, c.maxSubSteps);
         if (k == 2) ++at_max;
         if (k != 1) continue;
-        compute_toi(d, slot, L, mdist, mtoi, mroot);
+        Sweep sA, sB;
+        const float alpha0 = advance_pair(d, d.cs_body[slot], sA, sB);
+        store_toi(d, slot, sA, sB, alpha0, 1u, L, mdist, mtoi, mroot);
         ++updated;
     }
     if (updated) atomicAdd(&d.cnt->st_toi_updated_toi, updated);
@@ -210,20 +293,22 @@ __device__ __forceinline__ uint32_t lower_bound_key(const uint64_t* a, uint32_t 
     return lo;
 }
 
-// The world's contacts: a contiguous range of the key-sorted live list (keys
-// start with the smaller proxy index and a world's proxies are contiguous).
+// A world's slice of a key-sorted contact list (keys start with the smaller
+// proxy index and a world's proxies are contiguous).
 struct Seg {
+    const uint32_t* slots;
     uint32_t c0, c1;
 };
-__device__ __forceinline__ Seg world_contacts(const DW& d, uint32_t w) {
-    const uint32_t n = d.cnt->n_live;
+__device__ __forceinline__ Seg world_slice(const DW& d, uint32_t w, const uint64_t* keys, const uint32_t* slots,
+                                           uint32_t n) {
     Seg s;
-    s.c0 = lower_bound_key(d.c_key, n, (uint64_t)d.w_shape_off[w] << d.key_bits);
-    s.c1 = lower_bound_key(d.c_key, n, (uint64_t)d.w_shape_off[w + 1] << d.key_bits);
+    s.slots = slots;
+    s.c0 = lower_bound_key(keys, n, (uint64_t)d.w_shape_off[w] << d.key_bits);
+    s.c1 = lower_bound_key(keys, n, (uint64_t)d.w_shape_off[w + 1] << d.key_bits);
     return s;
 }
 
-// The contact of the world with the smallest creation sequence >= lo that
+// The contact of the slice with the smallest creation sequence >= lo that
 // passes pred (kNone if there is none); all lanes get the answer.
 template <class Pred>
 __device__ __forceinline__ uint32_t warp_first_in_list(const DW& d, Seg sg, uint64_t lo, uint32_t lane, Pred pred,
@@ -231,7 +316,7 @@ __device__ __forceinline__ uint32_t warp_first_in_list(const DW& d, Seg sg, uint
     uint64_t best = ~0ull;
     uint32_t bslot = kNone;
     for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
-        const uint32_t slot = d.c_slot[i];
+        const uint32_t slot = sg.slots[i];
         const uint64_t q = d.cs_seq[slot];
         if (q >= lo && q < best && pred(slot)) { best = q; bslot = slot; }
     }
@@ -244,7 +329,7 @@ __device__ __forceinline__ uint32_t warp_first_in_list(const DW& d, Seg sg, uint
     return bslot;
 }
 
-// Gathers the world's contacts that pass pred into (slot, seq) ordered by
+// Gathers the slice's contacts that pass pred into (slot, seq) ordered by
 // creation sequence, i.e. in contact-list order.  Returns how many pass; only the
 // first kToiBatch are stored, so a larger count means the list is incomplete.
 template <class Pred>
@@ -256,7 +341,7 @@ __device__ uint32_t warp_gather_in_list_order(const DW& d, Seg sg, uint32_t lane
         uint32_t slot = kNone;
         bool take = false;
         if (i < sg.c1) {
-            slot = d.c_slot[i];
+            slot = sg.slots[i];
             take = pred(slot);
         }
         const unsigned m = __ballot_sync(kFull, take);
@@ -290,78 +375,44 @@ __device__ uint32_t warp_gather_in_list_order(const DW& d, Seg sg, uint32_t lane
 // (cheap and order-dependent), then every lane computes times of impact.  Up
 // to kToiBatch such contacts are gathered at once (the usual case after an
 // event); beyond that lane 0 takes them one by one.
-__device__ void toi_update_world(const DW& d, Seg sg, ToiScratch& S, uint32_t lane) {
+__device__ void toi_update_world(const DW& d, Seg imp, ToiScratch& S, uint32_t lane) {
     const DConf& c = *d.conf;
     const ToiLimits L = toi_limits(c);
     uint32_t at_max = 0;
-    for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u)
-        if (toi_candidate(d, d.c_slot[i], c.maxSubSteps) == 2) ++at_max;
+    for (uint32_t i = imp.c0 + lane; i < imp.c1; i += 32u)
+        if (toi_candidate(d, imp.slots[i], c.maxSubSteps) == 2) ++at_max;
     if (at_max) atomicAdd(&d.cnt->st_toi_at_max_substeps, at_max);
     int mdist = 0, mtoi = 0, mroot = 0;
     uint32_t updated = 0;
     ToiBatch& B = S.batch;
+    const uint32_t ep = S.ep;
     auto missing = [&](uint32_t s) { return toi_candidate(d, s, c.maxSubSteps) == 1; };
-    const uint32_t n = warp_gather_in_list_order(d, sg, lane, missing, B.slot, B.seq);
+    const uint32_t n = warp_gather_in_list_order(d, imp, lane, missing, B.slot, B.seq);
     if (n > kToiBatch) {
-        // more than one gather holds: one contact per scan, in list order, on lane 0
-        for (uint32_t guard = 0; guard <= sg.c1 - sg.c0; ++guard) {
+        for (uint32_t guard = 0; guard <= imp.c1 - imp.c0; ++guard) {  // each pass gives one contact a time
             uint64_t q;
-            const uint32_t slot = warp_first_in_list(d, sg, 0, lane, missing, q);
+            const uint32_t slot = warp_first_in_list(d, imp, 0, lane, missing, q);
             if (slot == kNone) break;
             if (lane == 0) {
-                compute_toi(d, slot, L, mdist, mtoi, mroot);
+                Sweep sA, sB;
+                const float alpha0 = advance_pair(d, d.cs_body[slot], sA, sB);
+                store_toi(d, slot, sA, sB, alpha0, ep, L, mdist, mtoi, mroot);
                 ++updated;
             }
             __syncwarp();
         }
     } else if (n > 0) {
-        const uint32_t k = n;
-        if (lane == 0) {
-            for (uint32_t j = 0; j < k; ++j) {
-                const uint2 bd = d.cs_body[B.slot[j]];
-                Sweep sA = body_sweep(d, bd.x), sB = body_sweep(d, bd.y);
-                const float alpha0 = maxf_(sA.a0, sB.a0);
-                sweep_advance0(sA, alpha0);
-                d.b_pos0[bd.x] = make_float4(sA.p0.x, sA.p0.y, sA.p0.a, d.b_pos0[bd.x].w);
-                d.b_alpha0[bd.x] = alpha0;
-                sweep_advance0(sB, alpha0);
-                d.b_pos0[bd.y] = make_float4(sB.p0.x, sB.p0.y, sB.p0.a, d.b_pos0[bd.y].w);
-                d.b_alpha0[bd.y] = alpha0;
-                B.sA[j] = sweep_normalized(sA);
-                B.sB[j] = sweep_normalized(sB);
-                B.alpha0[j] = alpha0;
-            }
-        }
+        if (lane == 0)
+            for (uint32_t j = 0; j < n; ++j) B.alpha0[j] = advance_pair(d, d.cs_body[B.slot[j]], B.sA[j], B.sB[j]);
         __syncwarp();
-        for (uint32_t j = lane; j < k; j += 32u) {
-            const uint32_t slot = B.slot[j];
-            const uint2 pr = d.cs_proxy[slot];
-            Proxy PA, PB;
-            load_proxy(d, pr.x, PA);
-            load_proxy(d, pr.y, PB);
-            const ToiOut o = toi_via_sat(PA, B.sA[j], PB, B.sB[j], L);
-            const float a0 = B.alpha0[j];
-            d.cs_toi[slot] = (o.state == TOI_TOUCHING) ? minf_(a0 + (1.0f - a0) * o.time, 1.0f) : 1.0f;
-            d.cs_flags[slot] |= CF_TOI_VALID;
-            mdist = max(mdist, o.max_dist_iters);
-            mtoi = max(mtoi, o.toi_iters);
-            mroot = max(mroot, o.max_root_iters);
+        for (uint32_t j = lane; j < n; j += 32u) {
+            store_toi(d, B.slot[j], B.sA[j], B.sB[j], B.alpha0[j], ep, L, mdist, mtoi, mroot);
             ++updated;
         }
         __syncwarp();
     }
     if (updated) atomicAdd(&d.cnt->st_toi_updated_toi, updated);
     toi_iter_stats(d, mdist, mtoi, mroot);
-}
-
-// FlagForUpdating over the contacts of body b.
-__device__ __forceinline__ void flag_contacts_of(const DW& d, Seg sg, uint32_t b, uint32_t lane) {
-    for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
-        const uint32_t slot = d.c_slot[i];
-        const uint2 bd = d.cs_body[slot];
-        if (bd.x == b || bd.y == b) d.cs_flags[slot] |= CF_NEEDS_UPDATE;
-    }
-    __syncwarp();
 }
 
 __device__ __forceinline__ uint32_t island_local(const ToiScratch& S, uint32_t b) {
@@ -457,7 +508,6 @@ __device__ void toi_solve_island(const DW& d, ToiScratch& S, float toi) {
         if (newInc <= c.toiMinMomentum) { velIters = it + 1; break; }
         maxInc = maxf_(maxInc, newInc);
     }
-    S.n_moved = 0;
     for (uint32_t i = 0; i < S.nb; ++i) {  // IntegratePositions, then the write-back
         float4 p = S.bp[i];
         const float4 v = S.bv[i];
@@ -470,7 +520,7 @@ __device__ void toi_solve_island(const DW& d, ToiScratch& S, float toi) {
             d.b_pos1[g] = make_float4(p.x, p.y, p.z, p1.w);
             const Xf xf = get_xf(p.x, p.y, p.z, mk(S.bm[i].z, S.bm[i].w));
             d.b_xf[g] = make_float4(xf.p.x, xf.p.y, xf.q.x, xf.q.y);
-            S.moved[S.n_moved++] = g;
+            d.b_toi_ep[g] = ++S.ep;  // FlagForUpdating of its contacts
         }
     }
     Counters* cn = d.cnt;
@@ -483,107 +533,90 @@ __device__ void toi_solve_island(const DW& d, ToiScratch& S, float toi) {
 }
 
 // One contact of ProcessContactsForTOI (AabbTreeWorld.cpp:2084-2137) for body
-// x.  Returns false on island overflow.
-__device__ bool toi_process_contact(const DW& d, Seg sg, uint32_t x, bool impX, uint32_t slot, float toi,
-                                    ToiScratch& S, uint32_t lane) {
-    // lane 0 decides; 1: go on with the contact, 2: the other body moved
-    uint32_t act = 0, other = 0;
-    if (lane == 0) {
-        const uint32_t f = d.cs_flags[slot];
-        const uint2 bd = d.cs_body[slot];
-        other = (bd.x == x) ? bd.y : bd.x;
-        const uint32_t fo = d.b_flags[other];
-        if (!(f & (CF_TOI_ISL | CF_SENSOR)) && (impX || is_impenetrable(fo))) {
-            act = 1u;
-            if (!(fo & BF_TOI_ISL)) {
-                if (body_advance(d, other, toi, S.backup)) act |= 2u;
-            } else {
-                S.backup = body_sweep(d, other);
-            }
-        }
+// x, on lane 0.  Returns false on island overflow.
+__device__ bool toi_process_contact(const DW& d, uint32_t x, bool impX, uint32_t slot, float toi, ToiScratch& S) {
+    const uint32_t f0 = d.cs_flags[slot];
+    const uint2 bd = d.cs_body[slot];
+    const uint32_t other = (bd.x == x) ? bd.y : bd.x;
+    const uint32_t fo = d.b_flags[other];
+    if ((f0 & (CF_TOI_ISL | CF_SENSOR)) || !(impX || is_impenetrable(fo))) return true;
+    const bool otherIslanded = (fo & BF_TOI_ISL) != 0u;
+    if (!otherIslanded) body_advance(d, other, toi, S.backup, S.ep);
+    else S.backup = body_sweep(d, other);
+    if (toi_needs_update(d, slot)) {
+        toi_update(d, slot, S.ep);
+        ++S.updated;
+    } else {
+        ++S.skipped;
     }
-    act = __shfl_sync(kFull, act, 0);
-    other = __shfl_sync(kFull, other, 0);
-    if (act & 2u) flag_contacts_of(d, sg, other, lane);
-    uint32_t ok = 1u;
-    if (lane == 0 && (act & 1u)) {
-        uint32_t f = d.cs_flags[slot];
-        if (f & CF_NEEDS_UPDATE) {
-            update_contact(d, slot);
-            ++S.updated;
-            f = d.cs_flags[slot];
-        } else {
-            ++S.skipped;
-        }
-        if (!(f & CF_TOUCHING)) {
-            body_set_sweep(d, other, S.backup);
-        } else if (S.nc >= kToiIslandContacts) {
-            ok = 0u;
-        } else {
-            S.isl_c[S.nc++] = slot;
-            d.cs_flags[slot] = f | CF_TOI_ISL;
-            const uint32_t fo = d.b_flags[other];
-            if (!(fo & BF_TOI_ISL)) {
-                d.b_flags[other] = fo | BF_TOI_ISL | (is_speedable(fo) ? BF_AWAKE : 0u);
-                S.isl_b[S.nb++] = other;
-            }
-        }
+    const uint32_t f = d.cs_flags[slot];
+    if (!(f & CF_TOUCHING)) {
+        body_set_sweep(d, other, S.backup);
+        return true;
     }
-    ok = __shfl_sync(kFull, ok, 0);
-    __syncwarp();
-    return ok != 0u;
+    if (S.nc >= kToiIslandContacts) return false;
+    S.isl_c[S.nc++] = slot;
+    d.cs_flags[slot] = f | CF_TOI_ISL;
+    if (!otherIslanded) {
+        d.b_flags[other] = fo | BF_TOI_ISL | (is_speedable(fo) ? BF_AWAKE : 0u);
+        S.isl_b[S.nb++] = other;
+    }
+    return true;
 }
 
 // ProcessContactsForTOI (AabbTreeWorld.cpp:2061-2142) for body x, walking its
-// contacts in its contact-list order.  Returns false on island overflow.
-__device__ bool toi_process_contacts(const DW& d, Seg sg, uint32_t x, float toi, ToiScratch& S, uint32_t lane) {
+// contacts in its contact-list order.  Only contacts with an impenetrable body
+// take part unless x is itself impenetrable (a bullet), so a non-bullet walks
+// the impenetrable list and a bullet all of its world's contacts.  Returns false
+// on island overflow.
+__device__ bool toi_process_contacts(const DW& d, Seg all, Seg imp, uint32_t x, float toi, ToiScratch& S,
+                                     uint32_t lane) {
     const bool impX = is_impenetrable(d.b_flags[x]);
+    const Seg sg = impX ? all : imp;
     auto touches_x = [&](uint32_t s) {
         const uint2 bd = d.cs_body[s];
         return bd.x == x || bd.y == x;
     };
     // the body's list, gathered once (the island solve reuses this memory later)
     const uint32_t n = warp_gather_in_list_order(d, sg, lane, touches_x, S.batch.slot, S.batch.seq);
+    uint32_t ok = 1u;
     if (n <= kToiBatch) {
-        for (uint32_t j = 0; j < n; ++j)
-            if (!toi_process_contact(d, sg, x, impX, S.batch.slot[j], toi, S, lane)) return false;
-        return true;
+        if (lane == 0)
+            for (uint32_t j = 0; j < n && ok; ++j) ok = toi_process_contact(d, x, impX, S.batch.slot[j], toi, S);
+        ok = __shfl_sync(kFull, ok, 0);
+        __syncwarp();
+        return ok != 0u;
     }
     // more contacts than one gather holds: take them one scan at a time
     uint64_t lo = 0;
-    for (uint32_t guard = 0; guard <= sg.c1 - sg.c0; ++guard) {  // each pass takes a later contact
+    for (uint32_t guard = 0; guard <= sg.c1 - sg.c0 && ok; ++guard) {  // each pass takes a later contact
         uint64_t q;
         const uint32_t slot = warp_first_in_list(d, sg, lo, lane, touches_x, q);
-        if (slot == kNone) return true;
+        if (slot == kNone) break;
         lo = q + 1;
-        if (!toi_process_contact(d, sg, x, impX, slot, toi, S, lane)) return false;
+        if (lane == 0) ok = toi_process_contact(d, x, impX, slot, toi, S);
+        ok = __shfl_sync(kFull, ok, 0);
+        __syncwarp();
     }
-    return true;
+    return ok != 0u;
 }
 
 // SolveToi(ContactID) (AabbTreeWorld.cpp:1833-1955) for the world's soonest
 // contact; returns false if the island overflowed its shared-memory capacity.
-__device__ bool toi_event(const DW& d, Seg sg, uint32_t next, ToiScratch& S, uint32_t lane) {
+__device__ bool toi_event(const DW& d, Seg all, Seg imp, uint32_t next, ToiScratch& S, uint32_t lane) {
     const uint2 bd = d.cs_body[next];
     const float toi = d.cs_toi[next];
-    Sweep bkA, bkB;
-    uint32_t moved = 0;
-    if (lane == 0) {
-        if (body_advance(d, bd.x, toi, bkA)) moved |= 1u;
-        if (body_advance(d, bd.y, toi, bkB)) moved |= 2u;
-    }
-    moved = __shfl_sync(kFull, moved, 0);
-    if (moved & 1u) flag_contacts_of(d, sg, bd.x, lane);
-    if (moved & 2u) flag_contacts_of(d, sg, bd.y, lane);
     uint32_t go = 0;
     if (lane == 0) {
-        uint32_t f = d.cs_flags[next];
+        Sweep bkA, bkB;
+        body_advance(d, bd.x, toi, bkA, S.ep);
+        body_advance(d, bd.y, toi, bkB, S.ep);
         uint32_t updated = 0;
-        if (f & CF_NEEDS_UPDATE) {
-            update_contact(d, next);
+        if (toi_needs_update(d, next)) {
+            toi_update(d, next, S.ep);
             updated = 1;
-            f = d.cs_flags[next];
         }
+        uint32_t f = d.cs_flags[next];
         const uint32_t n = min(toi_count(f) + 1u, 255u);
         f = (f & ~(CF_TOI_VALID | kToiCountMask)) | (n << kToiCountShift);
         if (!(f & CF_TOUCHING)) {
@@ -606,8 +639,8 @@ __device__ bool toi_event(const DW& d, Seg sg, uint32_t next, ToiScratch& S, uin
     go = __shfl_sync(kFull, go, 0);
     __syncwarp();
     if (!go) return true;
-    if (is_accelerable(d.b_flags[bd.x]) && !toi_process_contacts(d, sg, bd.x, toi, S, lane)) return false;
-    if (is_accelerable(d.b_flags[bd.y]) && !toi_process_contacts(d, sg, bd.y, toi, S, lane)) return false;
+    if (is_accelerable(d.b_flags[bd.x]) && !toi_process_contacts(d, all, imp, bd.x, toi, S, lane)) return false;
+    if (is_accelerable(d.b_flags[bd.y]) && !toi_process_contacts(d, all, imp, bd.y, toi, S, lane)) return false;
     if (lane == 0) {
         for (uint32_t i = 0; i < S.nb; ++i) {  // RemoveUnspeedablesFromIslanded
             const uint32_t g = S.isl_b[i];
@@ -618,25 +651,44 @@ __device__ bool toi_event(const DW& d, Seg sg, uint32_t next, ToiScratch& S, uin
         atomicAdd(&d.cnt->st_toi_skipped_touching, S.skipped);
     }
     __syncwarp();
-    const uint32_t nm = __shfl_sync(kFull, S.n_moved, 0);
-    for (uint32_t i = 0; i < nm; ++i) flag_contacts_of(d, sg, S.moved[i], lane);
     return true;
+}
+
+// Synchronize (AabbTreeWorld.cpp:2564-2585) of the proxies of body b, as the
+// TOI loop does for each accelerable islanded body (:1805-1812).
+__device__ __forceinline__ uint32_t toi_sync_body(const DW& d, uint32_t b) {
+    uint32_t moved = 0;
+    for (uint32_t k = d.b_shape_off[b]; k < d.b_shape_off[b + 1]; ++k) {
+        const uint32_t p = d.b_shapes[k];
+        const Xf x0 = xf0_of(d, b), x1 = load_xf(d, b);
+        const Box a = swept_aabb(d, p, x0, x1);
+        if (!contains4(d.p_aabb[p], a)) {
+            d.p_aabb[p] = fat_box(d, a, x0, x1);
+            d.p_moved[p] = 1u;
+            const uint32_t at = atomicAdd(&d.cnt->n_moved, 1u);
+            d.moved_list[at] = p;
+            ++moved;
+        }
+    }
+    return moved;
 }
 
 // One iteration of the reference's TOI loop (AabbTreeWorld.cpp:1758-1826) for
 // world w: missing times of impact, the soonest event, its island, then the
-// proxies of the islanded bodies.
+// islanded bodies' proxies and contacts.
 __device__ void toi_world_round(const DW& d, uint32_t w, ToiScratch& S, bool first, uint32_t lane) {
-    const Seg sg = world_contacts(d, w);
-    if (!first) toi_update_world(d, sg, S, lane);
+    const Seg imp = world_slice(d, w, d.t_key, d.t_slot, d.cnt->n_imp);
+    if (lane == 0) { S.ep = d.w_toi_ep[w]; S.nb = 0; S.nc = 0; }
+    __syncwarp();
+    if (!first) toi_update_world(d, imp, S, lane);
     // GetSoonestContact (AabbTreeWorld.cpp:2870-2890): the smallest time below 1,
     // the earliest in the contact list among equal times
     float best = 1.0f;
     uint64_t bseq = ~0ull;
     uint32_t next = kNone;
-    for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
-        const uint32_t slot = d.c_slot[i];
-        if (!(d.cs_flags[slot] & CF_TOI_VALID)) continue;
+    for (uint32_t i = imp.c0 + lane; i < imp.c1; i += 32u) {
+        const uint32_t slot = imp.slots[i];
+        if (!toi_valid(d, slot)) continue;
         const float t = d.cs_toi[slot];
         const uint64_t q = d.cs_seq[slot];
         if (t < best || (t == best && next != kNone && q < bseq)) { best = t; bseq = q; next = slot; }
@@ -651,11 +703,10 @@ __device__ void toi_world_round(const DW& d, uint32_t w, ToiScratch& S, bool fir
     }
     if (next == kNone) {
         // no more events: ResetBodiesForSolveTOI and ResetContactsForSolveTOI
+        // (only impenetrable contacts carry TOI bits; the epochs restart next phase)
         for (uint32_t b = d.w_body_off[w] + lane; b < d.w_body_off[w + 1]; b += 32u) d.b_alpha0[b] = 0.f;
-        for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
-            const uint32_t slot = d.c_slot[i];
-            d.cs_flags[slot] &= ~(CF_TOI_VALID | CF_TOI_ISL | kToiCountMask);
-        }
+        for (uint32_t i = imp.c0 + lane; i < imp.c1; i += 32u)
+            d.cs_flags[imp.slots[i]] &= ~(CF_TOI_VALID | CF_TOI_ISL | kToiCountMask);
         if (lane == 0) d.w_toi[w] = 1u;
         return;
     }
@@ -663,42 +714,33 @@ __device__ void toi_world_round(const DW& d, uint32_t w, ToiScratch& S, bool fir
         atomicAdd(&d.cnt->st_toi_found, 1u);
         atomicAdd(&d.cnt->toi_events, 1u);
     }
-    S.nb = 0;
-    __syncwarp();
     if (!(d.cs_flags[next] & CF_TOI_ISL)) {
-        if (!toi_event(d, sg, next, S, lane)) {
+        const Seg all = world_slice(d, w, d.c_key, d.c_slot, d.cnt->n_live);
+        if (!toi_event(d, all, imp, next, S, lane)) {
             if (lane == 0) set_error(d.cnt, PR_ECAPACITY, 40u);
             return;
         }
     }
-    __syncwarp();
-    // islanded bodies: synchronise the proxies of accelerable ones and forget
-    // their contacts' times of impact and island marks
-    for (uint32_t i = sg.c0 + lane; i < sg.c1; i += 32u) {
-        const uint32_t slot = d.c_slot[i];
-        const uint2 bd = d.cs_body[slot];
-        const uint32_t fa = d.b_flags[bd.x], fb = d.b_flags[bd.y];
-        if (((fa & BF_TOI_ISL) && is_accelerable(fa)) || ((fb & BF_TOI_ISL) && is_accelerable(fb)))
-            d.cs_flags[slot] &= ~(CF_TOI_VALID | CF_TOI_ISL);
-    }
+    // the islanded bodies: accelerable ones synchronise their proxies and void
+    // their contacts' times of impact (one new epoch for all); the event's
+    // contacts leave the island
     uint32_t moved = 0;
-    for (uint32_t p = d.w_shape_off[w] + lane; p < d.w_shape_off[w + 1]; p += 32u) {
-        const uint32_t b = d.s_body[p];
-        const uint32_t f = d.b_flags[b];
-        if (!(f & BF_TOI_ISL) || !is_accelerable(f)) continue;
-        const Xf x0 = xf0_of(d, b), x1 = load_xf(d, b);
-        const Box a = swept_aabb(d, p, x0, x1);
-        if (!contains4(d.p_aabb[p], a)) {
-            d.p_aabb[p] = fat_box(d, a, x0, x1);
-            d.p_moved[p] = 1u;
-            append_moved(d, p);
-            ++moved;
+    const uint32_t rst = S.ep + 1u;
+    for (uint32_t i = lane; i < S.nb; i += 32u) {
+        const uint32_t g = S.isl_b[i];
+        const uint32_t f = d.b_flags[g];
+        if ((f & BF_TOI_ISL) && is_accelerable(f)) {
+            moved += toi_sync_body(d, g);
+            d.b_toi_rst[g] = rst;
         }
     }
     if (moved) atomicAdd(&d.cnt->st_toi_proxies_moved, moved);
     __syncwarp();
-    if (lane == 0)
+    if (lane == 0) {
+        for (uint32_t i = 0; i < S.nc; ++i) d.cs_flags[S.isl_c[i]] &= ~CF_TOI_ISL;
         for (uint32_t i = 0; i < S.nb; ++i) d.b_flags[S.isl_b[i]] &= ~BF_TOI_ISL;
+        d.w_toi_ep[w] = rst;
+    }
     __syncwarp();
 }
 
@@ -729,9 +771,13 @@ __global__ void k_toi_moved_done(DW d) {
     c->n_new = 0u;
     c->toi_added_base = c->st_contacts_added;
 }
+// Contacts the round's search added; when there are any, the impenetrable list
+// is rebuilt before the next round.
 __global__ void k_toi_added(DW d) {
     Counters* c = d.cnt;
-    c->st_toi_contacts_added += c->st_contacts_added - c->toi_added_base;
+    const uint32_t added = c->st_contacts_added - c->toi_added_base;
+    c->st_toi_contacts_added += added;
+    c->toi_rebuild = added ? 1u : 0u;
 }
 
 // The final UpdateContacts of SolveToi (AabbTreeWorld.cpp:1827-1829).
@@ -739,7 +785,7 @@ __global__ void k_toi_update_contacts(DW d) {
     uint32_t updated = 0, skipped = 0;
     GRID_LOOP(i, d.cnt->n_live) {
         const uint32_t slot = d.c_slot[i];
-        if (d.cs_flags[slot] & CF_NEEDS_UPDATE) {
+        if (toi_needs_update(d, slot)) {
             update_contact(d, slot);
             ++updated;
         } else {
@@ -776,10 +822,19 @@ __global__ void k_toi_pairs(uint32_t n, const float4* vtx, const uint32_t* meta,
     }
 }
 
+// The impenetrable list, rebuilt when toi_rebuild is set.
+void launch_toi_list(const DW& d, const Launch& L, cudaStream_t s) {
+    k_toi_list_flags<<<L.grid, L.threads, 0, s>>>(d);
+    scan_exclusive(L.prims, d.flags, d.scan, &d.cnt->toi_scan_n, &d.cnt->toi_imp_total, d.partial, s);
+    k_toi_list_scatter<<<L.grid, L.threads, 0, s>>>(d);
+    k_toi_list_done<<<1, 1, 0, s>>>(d);
+}
+
 }  // namespace
 
 void launch_toi_begin(const DW& d, const Launch& L, cudaStream_t s) {
     k_toi_begin<<<L.grid, L.threads, 0, s>>>(d);
+    launch_toi_list(d, L, s);
     k_toi_first<<<L.grid, L.threads, 0, s>>>(d);
 }
 
@@ -791,6 +846,7 @@ void launch_toi_round(const DW& d, const Launch& L, cudaStream_t s) {
     k_toi_moved_done<<<1, 1, 0, s>>>(d);
     launch_find_contacts(d, L, s);
     k_toi_added<<<1, 1, 0, s>>>(d);
+    launch_toi_list(d, L, s);
 }
 
 void launch_toi_end(const DW& d, const Launch& L, cudaStream_t s) {

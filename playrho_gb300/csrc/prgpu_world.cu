@@ -824,10 +824,14 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.w_root, W); AL(d.w_bounds, W);
     uint32_t* w_order;
     AL(w_order, W); d.w_order = w_order;
-    AL(d.w_kc, W + 1); AL(d.w_kj, W + 1); AL(d.w_toi, W);
+    AL(d.w_kc, W + 1); AL(d.w_kj, W + 1); ALS(d.w_toi, W); ALS(d.w_toi_ep, W);
     AL(d.b_pos1, N); AL(d.b_pos0, N); AL(d.b_vel, N); AL(d.b_xf, N); AL(d.b_mass, N); AL(d.b_acc, N);
     AL(d.b_damp, N); AL(d.b_flags, N); AL(d.b_uat, N); AL(d.b_world, N); AL(d.b_island, N);
-    AL(d.b_alpha0, N);
+    // the TOI phase's own state: reset when the phase starts
+    ALS(d.b_alpha0, N); ALS(d.b_toi_ep, N); ALS(d.b_toi_rst, N);
+    uint32_t *b_shape_off, *b_shapes;
+    AL(b_shape_off, N + 1); AL(b_shapes, S);
+    d.b_shape_off = b_shape_off; d.b_shapes = b_shapes;
     AL(d.b_jnt_off, N + 1); AL(d.b_jnt_other, jother.size()); AL(d.b_jnt_cc, jcc.size());
     AL(d.isl_awake, N); ALS(d.isl_sep, (size_t)N * kMaxPosIters); ALS(d.isl_jok, (size_t)N * kMaxPosIters); AL(d.isl_uat, N);
     AL(d.s_body, S); AL(d.s_meta, S); AL(d.s_voff, S); AL(d.s_radius, S); AL(d.s_mat, S); AL(d.s_filter, S);
@@ -836,7 +840,8 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_imp, J);
     AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
     AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C);
-    AL(d.cs_colour, C); AL(d.j_colour, J); AL(d.cs_toi, C); AL(d.cs_seq, C);
+    AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C);
+    ALS(d.cs_toi_ep, C); ALS(d.cs_toi_at, C); ALS(d.t_key, C); ALS(d.t_slot, C);
     AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
     ALS(d.n_key, K); ALS(d.n_key_alt, K); ALS(d.n_val, K); ALS(d.n_val_alt, K);
     AL(d.l_key, S); AL(d.l_key_alt, S); AL(d.l_idx, S); AL(d.l_idx_alt, S); AL(d.l_leaf_box, S);
@@ -909,6 +914,16 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ok &= up(d.b_jnt_other, jother.data(), sizeof(uint32_t) * jother.size());
     ok &= up(d.b_jnt_cc, jcc.data(), sizeof(uint32_t) * jcc.size());
     ok &= up(d.s_body, s_body.data(), sizeof(uint32_t) * S);
+    // body -> shapes, in shape order
+    std::vector<uint32_t> bs_off(N + 1, 0u), bs_idx(S);
+    for (uint32_t p = 0; p < S; ++p) ++bs_off[s_body[p] + 1];
+    for (uint32_t b = 0; b < N; ++b) bs_off[b + 1] += bs_off[b];
+    {
+        std::vector<uint32_t> cur(bs_off.begin(), bs_off.end() - 1);
+        for (uint32_t p = 0; p < S; ++p) bs_idx[cur[s_body[p]]++] = p;
+    }
+    ok &= up(b_shape_off, bs_off.data(), sizeof(uint32_t) * (N + 1));
+    ok &= up(b_shapes, bs_idx.data(), sizeof(uint32_t) * S);
     ok &= up(d.s_meta, s_meta.data(), sizeof(uint32_t) * S);
     ok &= up(d.s_voff, s_voff.data(), sizeof(uint32_t) * S);
     ok &= up(d.s_radius, s_radius.data(), sizeof(float) * S);
