@@ -195,6 +195,12 @@ typedef struct {
     real angularMass, motorImpulse;
     real imp[3];
     int limitState;
+    /* the other joint types: kind, parameters (OR_JOINT_* layouts) and solver state */
+    int type;
+    real extra[8];
+    v2 u, linErr;
+    real jmass, invGamma, bias, length, angErr;
+    real lm[2][2];
 } joint_t;
 enum { LS_INACTIVE = 0, LS_LOWER = 1, LS_UPPER = 2, LS_EQUAL = 3 };
 
@@ -484,6 +490,18 @@ void or_reset_mass(or_world* w, int body) {
     const v2 newCenter = b->pos1.lin;
     const v2 dc = vsub(newCenter, oldCenter);
     b->vel.lin = vadd(b->vel.lin, vmul(revperp(dc), b->vel.ang));
+}
+
+/* CreateJoint of the other joint types: anchors, collideConnected and the
+ * type's parameters (the OR_JOINT_* layouts in playrho_oracle.h). */
+int or_add_joint(or_world* w, int type, int bodyA, int bodyB, real lax, real lay, real lbx, real lby,
+                 int collideConnected, const real* extra8) {
+    const int jid = or_add_revolute(w, bodyA, bodyB, lax, lay, lbx, lby, R(0), 0, R(0), R(0), 0, R(0), R(0),
+                                    collideConnected);
+    joint_t* j = &w->j[jid];
+    j->type = type;
+    for (int k = 0; k < 8; ++k) j->extra[k] = extra8 ? extra8[k] : R(0);
+    return jid;
 }
 
 int or_add_revolute(or_world* w, int bodyA, int bodyB, real lax, real lay, real lbx, real lby,
@@ -1597,6 +1615,523 @@ typedef struct {
     ivec bodies, contacts, joints;
 } island_t;
 
+/* ------------------------------------------------------------------------- */
+/* Other joint types (DistanceJointConf.cpp, RopeJointConf.cpp,               */
+/* WeldJointConf.cpp, FrictionJointConf.cpp, MotorJointConf.cpp).             */
+/* ------------------------------------------------------------------------- */
+/* Position / Velocity operator!= (Position.hpp, Velocity.hpp). */
+static inline int pos_ne(pos_t a, pos_t b) {
+    return !(a.lin.x == b.lin.x && a.lin.y == b.lin.y && a.ang == b.ang);
+}
+/* UnitVec::Get(x, y) (UnitVec.hpp:175-235): the direction and the magnitude. */
+static v2 unit_len(v2 v, real* len) {
+    const real m2 = v.x * v.x + v.y * v.y;
+    if (isnormal(m2)) {
+        const real m = RSQRT(m2);
+        const real inv = R(1) / m;
+        *len = m;
+        return V(v.x * inv, v.y * inv);
+    }
+    const real m = RHYPOT(v.x, v.y);
+    if (!isnormal(m)) { *len = R(0); return V(R(0), R(0)); }
+    *len = m;
+    return V(v.x / m, v.y / m);
+}
+/* Velocity / Position -= {invMass * P, invRotI * L} and += (Velocity.hpp, Position.hpp). */
+static inline void sub_imp(pos_t* p, real iM, v2 P, real iI, real L) {
+    p->lin = vsub(p->lin, vmul(P, iM)); p->ang = p->ang - iI * L;
+}
+static inline void add_imp(pos_t* p, real iM, v2 P, real iI, real L) {
+    p->lin = vadd(p->lin, vmul(P, iM)); p->ang = p->ang + iI * L;
+}
+/* linear velocity + GetRevPerpendicular(r) * angular velocity */
+static inline v2 point_vel(pos_t v, v2 r) { return vadd(v.lin, vmul(revperp(r), v.ang)); }
+/* Matrix * vector, each row accumulated from zero (Vector.hpp:455-470); m[b][a]. */
+static inline v2 mat22_mul(real m[2][2], v2 v) {
+    real x = R(0); x += m[0][0] * v.x; x += m[0][1] * v.y;
+    real y = R(0); y += m[1][0] * v.x; y += m[1][1] * v.y;
+    return V(x, y);
+}
+/* Invert(Matrix22) (Math.hpp:430-442). */
+static void mat22_invert(real k[2][2], real out[2][2]) {
+    const real cp = cross(V(k[0][0], k[0][1]), V(k[1][0], k[1][1]));
+    if (!almost_zero(cp)) {
+        const real inv = R(1) / cp;
+        out[0][0] = k[1][1] * inv; out[0][1] = -k[0][1] * inv;
+        out[1][0] = -k[1][0] * inv; out[1][1] = k[0][0] * inv;
+    } else {
+        out[0][0] = out[0][1] = out[1][0] = out[1][1] = R(0);
+    }
+}
+/* Vec3 Dot and Cross (Math.hpp:320-333, :397-409). */
+static inline real dot3(const real* a, const real* b) { real r = R(0); r += a[0] * b[0]; r += a[1] * b[1]; r += a[2] * b[2]; return r; }
+static inline void cross3(const real* a, const real* b, real* o) {
+    const real x = a[1] * b[2] - a[2] * b[1], y = a[2] * b[0] - a[0] * b[2], z = a[0] * b[1] - a[1] * b[0];
+    o[0] = x; o[1] = y; o[2] = z;
+}
+/* Solve33 / Solve22 / GetInverse22 / GetSymInverse33 (Math.hpp:447-512); K[i] is the i-th Vec3. */
+static void solve33(real K[3][3], const real* b, real* o) {
+    real c[3];
+    cross3(K[1], K[2], c);
+    const real dp = dot3(K[0], c);
+    const real det = (dp != R(0)) ? (R(1) / dp) : dp;
+    real t[3];
+    const real x = det * dot3(b, c);
+    cross3(b, K[2], t);
+    const real y = det * dot3(K[0], t);
+    cross3(K[1], b, t);
+    const real z = det * dot3(K[0], t);
+    o[0] = x; o[1] = y; o[2] = z;
+}
+static v2 solve22k(real K[3][3], v2 b) {
+    const real xx = K[0][0], xy = K[1][0], yx = K[0][1], yy = K[1][1];
+    const real cp = xx * yy - xy * yx;
+    const real det = (cp != R(0)) ? (R(1) / cp) : cp;
+    return V(det * (yy * b.x - xy * b.y), det * (xx * b.y - yx * b.x));
+}
+static void inverse22(real K[3][3], real o[3][3]) {
+    const real a = K[0][0], b = K[1][0], c = K[0][1], d = K[1][1];
+    real det = (a * d) - (b * c);
+    if (det != R(0)) det = R(1) / det;
+    o[0][0] = det * d; o[0][1] = -det * c; o[0][2] = R(0);
+    o[1][0] = -det * b; o[1][1] = det * a; o[1][2] = R(0);
+    o[2][0] = R(0); o[2][1] = R(0); o[2][2] = R(0);
+}
+static void sym_inverse33(real K[3][3], real o[3][3]) {
+    real c[3];
+    cross3(K[1], K[2], c);
+    const real invDet = dot3(K[0], c);
+    const real det = (invDet != R(0)) ? (R(1) / invDet) : invDet;
+    const real a11 = K[0][0], a12 = K[1][0], a13 = K[2][0], a22 = K[1][1], a23 = K[2][1], a33 = K[2][2];
+    const real ex_y = det * (a13 * a23 - a12 * a33);
+    const real ey_z = det * (a13 * a12 - a11 * a23);
+    const real ex_z = det * (a12 * a23 - a13 * a22);
+    o[0][0] = det * (a22 * a33 - a23 * a23); o[0][1] = ex_y; o[0][2] = ex_z;
+    o[1][0] = ex_y; o[1][1] = det * (a11 * a33 - a13 * a13); o[1][2] = ey_z;
+    o[2][0] = ex_z; o[2][1] = ey_z; o[2][2] = det * (a11 * a22 - a12 * a12);
+}
+/* GetMat33 of the weld joint (WeldJointConf.cpp:36-62). */
+static void weld_k(real iMA, v2 rA, real iIA, real iMB, v2 rB, real iIB, real K[3][3]) {
+    const real exx = iMA + (rA.y * rA.y) * iIA + iMB + (rB.y * rB.y) * iIB;
+    const real eyx = -rA.y * rA.x * iIA + -rB.y * rB.x * iIB;
+    const real ezx = -rA.y * iIA + -rB.y * iIB;
+    const real eyy = iMA + (rA.x * rA.x) * iIA + iMB + (rB.x * rB.x) * iIB;
+    const real ezy = rA.x * iIA + rB.x * iIB;
+    const real ezz = iIA + iIB;
+    K[0][0] = exx; K[1][0] = eyx; K[2][0] = ezx;
+    K[0][1] = eyx; K[1][1] = eyy; K[2][1] = ezy;
+    K[0][2] = ezx; K[1][2] = ezy; K[2][2] = ezz;
+}
+static inline v2 anchor_r(v2 la, const bc_t* b) { return rotate(vsub(la, b->lc), unit_from_angle(b->pos.ang)); }
+
+/* DistanceJointConf InitVelocity / SolveVelocity / SolvePosition (DistanceJointConf.cpp:79-247). */
+static void dj_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    j->rA = anchor_r(j->laA, A);
+    j->rB = anchor_r(j->laB, B);
+    real length;
+    j->u = unit_len(vsub(vadd(B->pos.lin, j->rB), vadd(A->pos.lin, j->rA)), &length);
+    const real crAu = cross(j->rA, j->u), crBu = cross(j->rB, j->u);
+    real invMass = A->invM + A->invI * (crAu * crAu) + B->invM + B->invI * (crBu * crBu);
+    j->jmass = (invMass != R(0)) ? R(1) / invMass : R(0);
+    const real frequency = j->extra[1], dampingRatio = j->extra[2];
+    if (frequency > R(0)) {
+        const real Pi = R(3.14159265358979323846264338327950288L);
+        const real C = length - j->extra[0];
+        const real omega = R(2) * Pi * frequency;
+        const real d = R(2) * j->jmass * dampingRatio * omega;
+        const real k = j->jmass * (omega * omega);
+        const real h = conf->deltaTime;
+        const real gamma = h * (d + h * k);
+        j->invGamma = (gamma != R(0)) ? R(1) / gamma : R(0);
+        j->bias = C * h * k * j->invGamma;
+        invMass += j->invGamma;
+        j->jmass = (invMass != R(0)) ? R(1) / invMass : R(0);
+    } else {
+        j->invGamma = R(0);
+        j->bias = R(0);
+    }
+    if (conf->doWarmStart) {
+        j->imp[0] *= conf->dtRatio;
+        const v2 P = vmul(j->u, j->imp[0]);
+        sub_imp(&vA, A->invM, P, A->invI, cross(j->rA, P));
+        add_imp(&vB, B->invM, P, B->invI, cross(j->rB, P));
+    } else {
+        j->imp[0] = R(0);
+    }
+    A->vel = vA; B->vel = vB;
+}
+static int dj_solve_velocity(joint_t* j, bc_t* bcs) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const real Cdot = dot(j->u, vsub(point_vel(vB, j->rB), point_vel(vA, j->rA)));
+    const real impulse = -j->jmass * (Cdot + j->bias + j->invGamma * j->imp[0]);
+    j->imp[0] += impulse;
+    const v2 P = vmul(j->u, impulse);
+    sub_imp(&vA, A->invM, P, A->invI, cross(j->rA, P));
+    add_imp(&vB, B->invM, P, B->invI, cross(j->rB, P));
+    A->vel = vA; B->vel = vB;
+    return impulse == R(0);
+}
+static int dj_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    if (j->extra[1] > R(0)) return 1;
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t pA = A->pos, pB = B->pos;
+    const v2 rA = anchor_r(j->laA, A), rB = anchor_r(j->laB, B);
+    real length;
+    const v2 u = unit_len(vsub(vadd(pB.lin, rB), vadd(pA.lin, rA)), &length);
+    const real C = clampr(length - j->extra[0], -conf->maxLinearCorrection, conf->maxLinearCorrection);
+    const real impulse = -j->jmass * C;
+    const v2 P = vmul(u, impulse);
+    sub_imp(&pA, A->invM, P, A->invI, cross(rA, P));
+    add_imp(&pB, B->invM, P, B->invI, cross(rB, P));
+    A->pos = pA; B->pos = pB;
+    return fabs(C) < conf->linearSlop;
+}
+
+/* RopeJointConf InitVelocity / SolveVelocity / SolvePosition (RopeJointConf.cpp:78-214). */
+static void rope_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    j->rA = anchor_r(j->laA, A);
+    j->rB = anchor_r(j->laB, B);
+    const v2 uv = unit_len(vsub(vadd(B->pos.lin, j->rB), vadd(A->pos.lin, j->rA)), &j->length);
+    const real C = j->length - j->extra[0];
+    j->limitState = (C > R(0)) ? LS_UPPER : LS_INACTIVE;
+    if (j->length > conf->linearSlop) {
+        j->u = uv;
+    } else {
+        j->u = V(R(0), R(0));
+        j->jmass = R(0);
+        j->imp[0] = R(0);
+        return;
+    }
+    const real crA = cross(j->rA, j->u), crB = cross(j->rB, j->u);
+    const real invMass = A->invM + B->invM + A->invI * (crA * crA) + B->invI * (crB * crB);
+    j->jmass = (invMass != R(0)) ? R(1) / invMass : R(0);
+    if (conf->doWarmStart) {
+        j->imp[0] *= conf->dtRatio;
+        const v2 P = vmul(j->u, j->imp[0]);
+        sub_imp(&vA, A->invM, P, A->invI, cross(j->rA, P));
+        add_imp(&vB, B->invM, P, B->invI, cross(j->rB, P));
+    } else {
+        j->imp[0] = R(0);
+    }
+    A->vel = vA; B->vel = vB;
+}
+static int rope_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const v2 vpA = point_vel(vA, j->rA), vpB = point_vel(vB, j->rB);
+    const real C = j->length - j->extra[0];
+    const real inv_h = (conf->deltaTime != R(0)) ? R(1) / conf->deltaTime : R(0);
+    const real Cdot = dot(j->u, vsub(vpB, vpA)) + ((C < R(0)) ? inv_h * C : R(0));
+    real local = -j->jmass * Cdot;
+    const real old = j->imp[0];
+    j->imp[0] = minr(R(0), j->imp[0] + local);
+    local = j->imp[0] - old;
+    const v2 P = vmul(j->u, local);
+    sub_imp(&vA, A->invM, P, A->invI, cross(j->rA, P));
+    add_imp(&vB, B->invM, P, B->invI, cross(j->rB, P));
+    A->vel = vA; B->vel = vB;
+    return local == R(0);
+}
+static int rope_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t pA = A->pos, pB = B->pos;
+    const v2 rA = anchor_r(j->laA, A), rB = anchor_r(j->laB, B);
+    real length;
+    const v2 uv = unit_len(vsub(vadd(pB.lin, rB), vadd(pA.lin, rA)), &length);
+    const real C = clampr(length - j->extra[0], R(0), conf->maxLinearCorrection);
+    const real local = -j->jmass * C;
+    const v2 P = vmul(uv, local);
+    sub_imp(&pA, A->invM, P, A->invI, cross(rA, P));
+    add_imp(&pB, B->invM, P, B->invI, cross(rB, P));
+    A->pos = pA; B->pos = pB;
+    return (length - j->extra[0]) < conf->linearSlop;
+}
+
+/* WeldJointConf InitVelocity / SolveVelocity / SolvePosition (WeldJointConf.cpp:133-376). */
+static void weld_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    j->rA = anchor_r(j->laA, A);
+    j->rB = anchor_r(j->laB, B);
+    real K[3][3];
+    weld_k(iMA, j->rA, iIA, iMB, j->rB, iIB, K);
+    const real frequency = j->extra[1], dampingRatio = j->extra[2];
+    if (frequency > R(0)) {
+        inverse22(K, j->mass);
+        real invRotInertia = iIA + iIB;
+        const real rotInertia = (invRotInertia > R(0)) ? R(1) / invRotInertia : R(0);
+        const real C = B->pos.ang - A->pos.ang - j->extra[0];
+        const real Pi = R(3.14159265358979323846264338327950288L);
+        const real omega = R(2) * Pi * frequency;
+        const real d = R(2) * rotInertia * dampingRatio * omega;
+        const real k = rotInertia * omega * omega;
+        const real h = conf->deltaTime;
+        const real invGamma = h * (d + h * k);
+        j->invGamma = (invGamma != R(0)) ? R(1) / invGamma : R(0); /* the joint's gamma */
+        j->bias = C * h * k * j->invGamma;
+        invRotInertia += j->invGamma;
+        j->mass[2][2] = (invRotInertia != R(0)) ? R(1) / invRotInertia : R(0);
+    } else if (K[2][2] == R(0)) {
+        inverse22(K, j->mass);
+        j->invGamma = R(0);
+        j->bias = R(0);
+    } else {
+        sym_inverse33(K, j->mass);
+        j->invGamma = R(0);
+        j->bias = R(0);
+    }
+    if (conf->doWarmStart) {
+        j->imp[0] *= conf->dtRatio; j->imp[1] *= conf->dtRatio; j->imp[2] *= conf->dtRatio;
+        const v2 P = V(j->imp[0], j->imp[1]);
+        const real L = j->imp[2];
+        sub_imp(&vA, iMA, P, iIA, L + cross(j->rA, P));
+        add_imp(&vB, iMB, P, iIB, L + cross(j->rB, P));
+    } else {
+        j->imp[0] = j->imp[1] = j->imp[2] = R(0);
+    }
+    A->vel = vA; B->vel = vB;
+}
+static int weld_solve_velocity(joint_t* j, bc_t* bcs) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    const pos_t oA = A->vel, oB = B->vel;
+    pos_t vA = oA, vB = oB;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    if (j->extra[1] > R(0)) {
+        const real Cdot2 = vB.ang - vA.ang;
+        const real gamma = j->invGamma * j->imp[2];
+        const real impulse2 = -j->mass[2][2] * (Cdot2 + j->bias + gamma);
+        j->imp[2] += impulse2;
+        vA.ang -= iIA * impulse2;
+        vB.ang += iIB * impulse2;
+        const v2 Cdot1 = vsub(point_vel(vB, j->rB), point_vel(vA, j->rA));
+        /* Transform(Vec2, Mat33) (Math.hpp:522-527) */
+        const v2 t = V(j->mass[0][0] * Cdot1.x + j->mass[1][0] * Cdot1.y,
+                       j->mass[0][1] * Cdot1.x + j->mass[1][1] * Cdot1.y);
+        const v2 impulse1 = vneg(t);
+        j->imp[0] += impulse1.x;
+        j->imp[1] += impulse1.y;
+        const v2 P = impulse1;
+        sub_imp(&vA, iMA, P, iIA, cross(j->rA, P));
+        add_imp(&vB, iMB, P, iIB, cross(j->rB, P));
+    } else {
+        const v2 Cdot1 = vsub(point_vel(vB, j->rB), point_vel(vA, j->rA));
+        const real Cdot2 = vB.ang - vA.ang;
+        const real Cdot[3] = {Cdot1.x, Cdot1.y, Cdot2};
+        real imp3[3];
+        for (int b = 0; b < 3; ++b) imp3[b] = -dot3(j->mass[b], Cdot); /* -(mass * Cdot) */
+        j->imp[0] += imp3[0]; j->imp[1] += imp3[1]; j->imp[2] += imp3[2];
+        const v2 P = V(imp3[0], imp3[1]);
+        const real L = imp3[2];
+        sub_imp(&vA, iMA, P, iIA, L + cross(j->rA, P));
+        add_imp(&vB, iMB, P, iIB, L + cross(j->rB, P));
+    }
+    const int changed = pos_ne(vA, oA) || pos_ne(vB, oB);
+    if (changed) { A->vel = vA; B->vel = vB; }
+    return !changed;
+}
+static int weld_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t pA = A->pos, pB = B->pos;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const v2 rA = anchor_r(j->laA, A), rB = anchor_r(j->laB, B);
+    real positionError, angularError;
+    real K[3][3];
+    weld_k(iMA, rA, iIA, iMB, rB, iIB, K);
+    const v2 C1 = vsub(vadd(pB.lin, rB), vadd(pA.lin, rA));
+    if (j->extra[1] > R(0)) {
+        positionError = RSQRT(mag2(C1));
+        angularError = R(0);
+        const v2 P = vneg(solve22k(K, C1));
+        sub_imp(&pA, iMA, P, iIA, cross(rA, P));
+        add_imp(&pB, iMB, P, iIB, cross(rB, P));
+    } else {
+        const real C2 = pB.ang - pA.ang - j->extra[0];
+        positionError = RSQRT(mag2(C1));
+        angularError = fabs(C2);
+        const real C[3] = {C1.x, C1.y, C2};
+        real imp3[3];
+        if (K[2][2] > R(0)) {
+            real s[3];
+            solve33(K, C, s);
+            imp3[0] = -s[0]; imp3[1] = -s[1]; imp3[2] = -s[2];
+        } else {
+            const v2 i2 = vneg(solve22k(K, C1));
+            imp3[0] = i2.x; imp3[1] = i2.y; imp3[2] = R(0);
+        }
+        const v2 P = V(imp3[0], imp3[1]);
+        const real L = imp3[2];
+        sub_imp(&pA, iMA, P, iIA, L + cross(rA, P));
+        add_imp(&pB, iMB, P, iIB, L + cross(rB, P));
+    }
+    A->pos = pA; B->pos = pB;
+    return (positionError <= conf->linearSlop) && (angularError <= conf->angularSlop);
+}
+
+/* FrictionJointConf (FrictionJointConf.cpp:90-239) and MotorJointConf
+ * (MotorJointConf.cpp:89-235): a 2x2 linear and a scalar angular friction. */
+static void fm_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf, int motor) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    if (motor) {
+        j->rA = rotate(vsub(V(j->extra[0], j->extra[1]), A->lc), unit_from_angle(A->pos.ang));
+        j->rB = rotate(vneg(B->lc), unit_from_angle(B->pos.ang));
+    } else {
+        j->rA = anchor_r(j->laA, A);
+        j->rB = anchor_r(j->laB, B);
+    }
+    const v2 rA = j->rA, rB = j->rB;
+    real K[2][2];
+    if (motor) {
+        K[0][0] = iMA + iMB + iIA * (rA.y * rA.y) + iIB * (rB.y * rB.y);
+        K[0][1] = -iIA * rA.x * rA.y + -iIB * rB.x * rB.y;
+        K[1][1] = iMA + iMB + iIA * (rA.x * rA.x) + iIB * (rB.x * rB.x);
+    } else {
+        K[0][0] = iMA + iIA * (rA.y * rA.y) + iMB + iIB * (rB.y * rB.y);
+        K[0][1] = -iIA * rA.x * rA.y + -iIB * rB.x * rB.y;
+        K[1][1] = iMA + iIA * (rA.x * rA.x) + iMB + iIB * (rB.x * rB.x);
+    }
+    K[1][0] = K[0][1];
+    mat22_invert(K, j->lm);
+    const real invRotInertia = iIA + iIB;
+    j->angularMass = (invRotInertia > R(0)) ? R(1) / invRotInertia : R(0);
+    if (motor) {
+        j->linErr = vsub(vadd(B->pos.lin, rB), vadd(A->pos.lin, rA));
+        j->angErr = (B->pos.ang - A->pos.ang) - j->extra[2];
+    }
+    if (conf->doWarmStart) {
+        j->imp[0] *= conf->dtRatio; j->imp[1] *= conf->dtRatio; j->imp[2] *= conf->dtRatio;
+        const v2 P = V(j->imp[0], j->imp[1]);
+        sub_imp(&vA, iMA, P, iIA, cross(rA, P) + j->imp[2]);
+        add_imp(&vB, iMB, P, iIB, cross(rB, P) + j->imp[2]);
+    } else {
+        j->imp[0] = j->imp[1] = j->imp[2] = R(0);
+    }
+    A->vel = vA; B->vel = vB;
+}
+/* The linear impulse, clamped to h * maxForce in magnitude. */
+static v2 clamp_linear(joint_t* j, v2 impulse, real maxImpulse) {
+    const v2 old = V(j->imp[0], j->imp[1]);
+    v2 li = vadd(old, impulse);
+    if (mag2(li) > maxImpulse * maxImpulse) li = vmul(unit_vector(li, V(R(0), R(0))), maxImpulse);
+    j->imp[0] = li.x; j->imp[1] = li.y;
+    return vsub(li, old);
+}
+static int friction_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const real iIA = A->invI, iIB = B->invI;
+    const real h = conf->deltaTime;
+    const real maxForce = j->extra[0], maxTorque = j->extra[1];
+    int solved = 1;
+    {
+        const real angularImpulse = -j->angularMass * (vB.ang - vA.ang);
+        const real old = j->imp[2];
+        const real maxAng = h * maxTorque;
+        j->imp[2] = clampr(j->imp[2] + angularImpulse, -maxAng, maxAng);
+        const real inc = j->imp[2] - old;
+        if (inc != R(0)) solved = 0;
+        vA.ang -= iIA * inc;
+        vB.ang += iIB * inc;
+    }
+    {
+        const v2 impulse = vneg(mat22_mul(j->lm, vsub(point_vel(vB, j->rB), point_vel(vA, j->rA))));
+        const v2 inc = clamp_linear(j, impulse, h * maxForce);
+        const real angA = cross(j->rA, inc), angB = cross(j->rB, inc);
+        if (inc.x != R(0) || inc.y != R(0)) solved = 0;
+        sub_imp(&vA, A->invM, inc, iIA, angA);
+        add_imp(&vB, B->invM, inc, iIB, angB);
+    }
+    A->vel = vA; B->vel = vB;
+    return solved;
+}
+static int motor_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const real h = conf->deltaTime;
+    const real inv_h = (h != R(0)) ? R(1) / h : R(0);
+    const real maxForce = j->extra[3], maxTorque = j->extra[4], cf = j->extra[5];
+    int solved = 1;
+    {
+        const real Cdot = (vB.ang - vA.ang) + inv_h * cf * j->angErr;
+        const real angularImpulse = -j->angularMass * Cdot;
+        const real old = j->imp[2];
+        const real maxAng = h * maxTorque;
+        const real nw = clampr(old + angularImpulse, -maxAng, maxAng);
+        j->imp[2] = nw;
+        const real inc = nw - old;
+        if (inc != R(0)) {
+            sub_imp(&vA, R(0), V(R(0), R(0)), iIA, inc);
+            add_imp(&vB, R(0), V(R(0), R(0)), iIB, inc);
+            solved = 0;
+        }
+    }
+    {
+        const v2 Cdot = vadd(vsub(point_vel(vB, j->rB), point_vel(vA, j->rA)), vmul(j->linErr, inv_h * cf));
+        const v2 impulse = vneg(mat22_mul(j->lm, Cdot));
+        const v2 inc = clamp_linear(j, impulse, h * maxForce);
+        const real angA = cross(j->rA, inc), angB = cross(j->rB, inc);
+        if (inc.x != R(0) || inc.y != R(0) || angA != R(0) || angB != R(0)) {
+            sub_imp(&vA, iMA, inc, iIA, angA);
+            add_imp(&vB, iMB, inc, iIB, angB);
+            solved = 0;
+        }
+    }
+    if (solved) return 1;
+    A->vel = vA; B->vel = vB;
+    return 0;
+}
+
+/* Joint dispatch (JointConf visitors, Joint.cpp). */
+static void joint_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    switch (j->type) {
+    case OR_JOINT_DISTANCE: dj_init_velocity(j, bcs, conf); break;
+    case OR_JOINT_ROPE: rope_init_velocity(j, bcs, conf); break;
+    case OR_JOINT_WELD: weld_init_velocity(j, bcs, conf); break;
+    case OR_JOINT_FRICTION: fm_init_velocity(j, bcs, conf, 0); break;
+    case OR_JOINT_MOTOR: fm_init_velocity(j, bcs, conf, 1); break;
+    default: rj_init_velocity(j, bcs, conf); break;
+    }
+}
+static int joint_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    switch (j->type) {
+    case OR_JOINT_DISTANCE: return dj_solve_velocity(j, bcs);
+    case OR_JOINT_ROPE: return rope_solve_velocity(j, bcs, conf);
+    case OR_JOINT_WELD: return weld_solve_velocity(j, bcs);
+    case OR_JOINT_FRICTION: return friction_solve_velocity(j, bcs, conf);
+    case OR_JOINT_MOTOR: return motor_solve_velocity(j, bcs, conf);
+    default: return rj_solve_velocity(j, bcs, conf);
+    }
+}
+static int joint_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    switch (j->type) {
+    case OR_JOINT_DISTANCE: return dj_solve_position(j, bcs, conf);
+    case OR_JOINT_ROPE: return rope_solve_position(j, bcs, conf);
+    case OR_JOINT_WELD: return weld_solve_position(j, bcs, conf);
+    case OR_JOINT_FRICTION: case OR_JOINT_MOTOR: return 1;
+    default: return rj_solve_position(j, bcs, conf);
+    }
+}
+
 /* GetBodyConstraint (BodyConstraint.hpp:157-167): position 1 and
  * Cap(GetVelocity(body, h)) (Body.cpp:290-309, Velocity.cpp:26-45). */
 static void make_bc(bc_t* bc, const body_t* b, real h, const or_stepconf* conf) {
@@ -1656,13 +2191,13 @@ static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc
     if (conf->doWarmStart) {
         for (int i = 0; i < nc; ++i) warm_start(&vcs[i], bcs);
     }
-    for (int i = 0; i < isl->joints.n; ++i) rj_init_velocity(&w->j[isl->joints.a[i]], bcs, conf);
+    for (int i = 0; i < isl->joints.n; ++i) joint_init_velocity(&w->j[isl->joints.a[i]], bcs, conf);
 
     int velIters = conf->regVelocityIters;
     real maxInc = R(0);
     for (int it = 0; it < conf->regVelocityIters; ++it) {
         int jointsOkay = 1;
-        for (int i = 0; i < isl->joints.n; ++i) jointsOkay &= rj_solve_velocity(&w->j[isl->joints.a[i]], bcs, conf);
+        for (int i = 0; i < isl->joints.n; ++i) jointsOkay &= joint_solve_velocity(&w->j[isl->joints.a[i]], bcs, conf);
         real newInc = R(0);
         for (int i = 0; i < nc; ++i) newInc = maxr(newInc, solve_vc(&vcs[i], bcs));
         maxInc = maxr(maxInc, newInc);
@@ -1684,7 +2219,7 @@ static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc
         minSepIsland = minr(minSepIsland, minSep);
         const int contactsOkay = (minSep >= conf->regMinSeparation);
         int jointsOkay = 1;
-        for (int i = 0; i < isl->joints.n; ++i) jointsOkay &= rj_solve_position(&w->j[isl->joints.a[i]], bcs, conf);
+        for (int i = 0; i < isl->joints.n; ++i) jointsOkay &= joint_solve_position(&w->j[isl->joints.a[i]], bcs, conf);
         if (contactsOkay && jointsOkay) { posIters = it + 1; solved = 1; break; }
     }
     /* AssignImpulses (:196-220) */
@@ -1801,9 +2336,6 @@ static pos_t plerp(pos_t p0, pos_t p1, real beta) {
     d.lin = vsub(p1.lin, p0.lin); d.ang = p1.ang - p0.ang;
     s.lin = vmul(d.lin, beta); s.ang = d.ang * beta;
     return padd(p0, s);
-}
-static inline int pos_ne(pos_t a, pos_t b) {
-    return !(a.lin.x == b.lin.x && a.lin.y == b.lin.y && a.ang == b.ang);
 }
 
 /* Sweep (d2/Sweep.hpp:43-92). */

@@ -94,6 +94,18 @@ int or_add_revolute(or_world* w, int bodyA, int bodyB, or_real lax, or_real lay,
                     or_real maxMotorTorque, int collideConnected);
 
 /* StepConf defaults, except doToi = 0: callers ask for the TOI phase explicitly. */
+/* Joint kinds of or_add_joint and their parameters extra8[]:
+ *   OR_JOINT_DISTANCE  length frequency dampingRatio      (DistanceJointConf)
+ *   OR_JOINT_ROPE      maxLength                          (RopeJointConf)
+ *   OR_JOINT_WELD      referenceAngle frequency dampingRatio (WeldJointConf)
+ *   OR_JOINT_FRICTION  maxForce maxTorque                 (FrictionJointConf)
+ *   OR_JOINT_MOTOR     linearOffset.x .y angularOffset maxForce maxTorque
+ *                      correctionFactor (no anchors)      (MotorJointConf) */
+enum { OR_JOINT_REVOLUTE = 0, OR_JOINT_DISTANCE = 1, OR_JOINT_ROPE = 2, OR_JOINT_WELD = 3,
+       OR_JOINT_FRICTION = 4, OR_JOINT_MOTOR = 5 };
+int or_add_joint(or_world* w, int type, int bodyA, int bodyB, or_real lax, or_real lay, or_real lbx,
+                 or_real lby, int collideConnected, const or_real* extra8);
+
 void or_default_conf(or_stepconf* conf);
 void or_step(or_world* w, const or_stepconf* conf, or_stepstats* stats);
 

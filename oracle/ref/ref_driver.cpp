@@ -23,6 +23,11 @@
 #include <playrho/d2/EdgeShapeConf.hpp>
 #include <playrho/d2/PolygonShapeConf.hpp>
 #include <playrho/d2/RevoluteJointConf.hpp>
+#include <playrho/d2/DistanceJointConf.hpp>
+#include <playrho/d2/RopeJointConf.hpp>
+#include <playrho/d2/WeldJointConf.hpp>
+#include <playrho/d2/FrictionJointConf.hpp>
+#include <playrho/d2/MotorJointConf.hpp>
 #include <playrho/d2/Joint.hpp>
 #include <playrho/d2/DynamicTree.hpp>
 #include <playrho/StepConf.hpp>
@@ -272,6 +277,43 @@ int main()
             j.maxMotorTorque = rd(in) * 1_Nm;
             in >> en; j.collideConnected = en != 0;
             CreateJoint(world, Joint{j});
+        }
+        else if (tag == "jointx") {
+            // jointx kind bodyA bodyB lax lay lbx lby collideConnected e0..e7
+            int kind = 0, a = 0, b = 0; in >> kind >> a >> b;
+            const auto lax = rd(in), lay = rd(in), lbx = rd(in), lby = rd(in);
+            int cc = 0; in >> cc;
+            Real e[8];
+            for (auto& x : e) x = rd(in);
+            const auto bA = BodyID(static_cast<BodyID::underlying_type>(a));
+            const auto bB = BodyID(static_cast<BodyID::underlying_type>(b));
+            const auto laA = Length2{lax * 1_m, lay * 1_m}, laB = Length2{lbx * 1_m, lby * 1_m};
+            if (kind == 1) {
+                auto j = DistanceJointConf{bA, bB, laA, laB, e[0] * 1_m};
+                j.frequency = e[1] * 1_Hz; j.dampingRatio = e[2]; j.collideConnected = cc != 0;
+                CreateJoint(world, Joint{j});
+            } else if (kind == 2) {
+                auto j = RopeJointConf{bA, bB};
+                j.localAnchorA = laA; j.localAnchorB = laB; j.maxLength = e[0] * 1_m; j.collideConnected = cc != 0;
+                CreateJoint(world, Joint{j});
+            } else if (kind == 3) {
+                auto j = WeldJointConf{};
+                j.bodyA = bA; j.bodyB = bB; j.localAnchorA = laA; j.localAnchorB = laB;
+                j.referenceAngle = e[0] * 1_rad; j.frequency = e[1] * 1_Hz; j.dampingRatio = e[2];
+                j.collideConnected = cc != 0;
+                CreateJoint(world, Joint{j});
+            } else if (kind == 4) {
+                auto j = FrictionJointConf{};
+                j.bodyA = bA; j.bodyB = bB; j.localAnchorA = laA; j.localAnchorB = laB;
+                j.maxForce = e[0] * 1_N; j.maxTorque = e[1] * 1_Nm; j.collideConnected = cc != 0;
+                CreateJoint(world, Joint{j});
+            } else if (kind == 5) {
+                auto j = MotorJointConf{};
+                j.bodyA = bA; j.bodyB = bB; j.linearOffset = Length2{e[0] * 1_m, e[1] * 1_m};
+                j.angularOffset = e[2] * 1_rad; j.maxForce = e[3] * 1_N; j.maxTorque = e[4] * 1_Nm;
+                j.correctionFactor = e[5]; j.collideConnected = cc != 0;
+                CreateJoint(world, Joint{j});
+            }
         }
         else if (tag == "step") {
             int n = 0; in >> n;

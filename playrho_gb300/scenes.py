@@ -24,6 +24,16 @@ F32 = np.float32
 
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 DISK, POLYGON, EDGE = 0, 1, 2
+# Joint kinds (the reference's JointConf types) and their parameters in joint_extra.
+JOINT_REVOLUTE, JOINT_DISTANCE, JOINT_ROPE, JOINT_WELD, JOINT_FRICTION, JOINT_MOTOR = 0, 1, 2, 3, 4, 5
+JOINT_PARAMS = {
+    JOINT_DISTANCE: ("length", "frequency", "damping_ratio"),
+    JOINT_ROPE: ("max_length",),
+    JOINT_WELD: ("reference_angle", "frequency", "damping_ratio"),
+    JOINT_FRICTION: ("max_force", "max_torque"),
+    JOINT_MOTOR: ("linear_offset_x", "linear_offset_y", "angular_offset", "max_force", "max_torque",
+                  "correction_factor"),
+}
 # Body flags (BodyConf booleans): allowSleep, awake, fixedRotation, enabled, bullet.
 BF_ALLOW_SLEEP, BF_AWAKE, BF_FIXED_ROTATION, BF_ENABLED, BF_BULLET = 1, 2, 4, 8, 16
 BF_DEFAULT = BF_ALLOW_SLEEP | BF_AWAKE | BF_ENABLED
@@ -34,7 +44,7 @@ DEFAULT_VERTEX_RADIUS = F32(DEFAULT_LINEAR_SLOP * F32(2))  # PolygonShapeConf.hp
 
 @dataclasses.dataclass
 class Scene:
-    """One world: bodies, shapes (one child each) and revolute joints."""
+    """One world: bodies, shapes (one child each) and joints."""
 
     body_type: np.ndarray      # int32 [B]
     body_pos: np.ndarray       # float32 [B,3] x, y, angle
@@ -56,6 +66,16 @@ class Scene:
     joint_anchors: np.ndarray  # float32 [J,4] localAnchorA.xy localAnchorB.xy
     joint_params: np.ndarray   # float32 [J,6] refAngle lower upper motorSpeed maxMotorTorque pad
     joint_flags: np.ndarray    # int32 [J,3] enableLimit enableMotor collideConnected
+    # joint kind (JOINT_*) and the other kinds' parameters (layouts at JOINT_PARAMS)
+    joint_type: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))
+    joint_extra: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 8), np.float32))
+
+    def __post_init__(self):
+        nj = int(np.asarray(self.joint_bodies).reshape(-1, 2).shape[0])
+        if len(self.joint_type) != nj:
+            self.joint_type = np.zeros(nj, np.int32)
+        if len(self.joint_extra) != nj:
+            self.joint_extra = np.zeros((nj, 8), np.float32)
 
     @property
     def n_bodies(self) -> int:
@@ -97,6 +117,8 @@ class SceneBuilder:
         self.j_anchor: List[tuple] = []
         self.j_params: List[tuple] = []
         self.j_flags: List[tuple] = []
+        self.j_type: List[int] = []
+        self.j_extra: List[tuple] = []
 
     def body(self, btype, x, y, angle=0.0, v=(0.0, 0.0, 0.0), acc=(0.0, 0.0, 0.0),
              damp=(0.0, 0.0), flags=BF_DEFAULT) -> int:
@@ -147,6 +169,25 @@ class SceneBuilder:
         speed, torque = motor if motor else (0.0, 0.0)
         self.j_params.append((ref_angle, lower, upper, speed, torque, 0.0))
         self.j_flags.append((1 if limit else 0, 1 if motor else 0, 1 if collide_connected else 0))
+        self.j_type.append(JOINT_REVOLUTE)
+        self.j_extra.append((0.0,) * 8)
+        return len(self.j_bodies) - 1
+
+    def joint(self, kind, a, b, anchor_a=(0.0, 0.0), anchor_b=(0.0, 0.0), collide_connected=False, **params):
+        """A joint of another kind (JOINT_*) with its parameters by name (JOINT_PARAMS)."""
+        names = JOINT_PARAMS[kind]
+        unknown = set(params) - set(names)
+        if unknown:
+            raise ValueError(f"unknown parameters {sorted(unknown)} for joint kind {kind}")
+        extra = [float(params.get(n, 0.0)) for n in names] + [0.0] * (8 - len(names))
+        if kind == JOINT_MOTOR and "correction_factor" not in params:
+            extra[5] = 0.2  # MotorJointConf::correctionFactor default
+        self.j_bodies.append((a, b))
+        self.j_anchor.append((anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1]))
+        self.j_params.append((0.0,) * 6)
+        self.j_flags.append((0, 0, 1 if collide_connected else 0))
+        self.j_type.append(int(kind))
+        self.j_extra.append(tuple(extra))
         return len(self.j_bodies) - 1
 
     def build(self) -> Scene:
@@ -161,7 +202,8 @@ class SceneBuilder:
             shape_density=f(self.s_density, 0), shape_friction=f(self.s_friction, 0),
             shape_restitution=f(self.s_rest, 0), shape_filter=i(self.s_filter, 4),
             verts=f(self.verts, 2), joint_bodies=i(self.j_bodies, 2), joint_anchors=f(self.j_anchor, 4),
-            joint_params=f(self.j_params, 6), joint_flags=i(self.j_flags, 3))
+            joint_params=f(self.j_params, 6), joint_flags=i(self.j_flags, 3),
+            joint_type=np.asarray(self.j_type, np.int32), joint_extra=f(self.j_extra, 8))
 
 
 def convex_hull(points) -> list:
@@ -472,6 +514,50 @@ def bullets(n_bodies: int, rng, size: float = 20.0, speed=(60.0, 180.0), bullet_
     return sc
 
 
+def joint_zoo(rng, per_kind: int = 4, kinds=None, n_disks: int = 12, gravity: bool = True) -> Scene:
+    """Mechanisms of every joint kind side by side above a ground edge: a static
+    anchor holding a dynamic box by a distance (stiff and soft), rope, weld (rigid
+    and soft), friction or motor joint, with disks dropped on them."""
+    kinds = list(kinds) if kinds is not None else [JOINT_DISTANCE, JOINT_ROPE, JOINT_WELD, JOINT_FRICTION,
+                                                     JOINT_MOTOR]
+    acc = GRAVITY if gravity else (0.0, 0.0, 0.0)
+    sb = SceneBuilder()
+    g = sb.body(STATIC, 0.0, 0.0)
+    width = 3.0 * per_kind * len(kinds)
+    sb.edge(g, (-width, 0.0), (width, 0.0))
+    x = -width / 2.0
+    for kind in kinds:
+        for k in range(per_kind):
+            x += 3.0
+            anchor = sb.body(STATIC, x, 8.0)
+            hx, hy = float(rng.uniform(0.2, 0.6)), float(rng.uniform(0.2, 0.6))
+            by = 8.0 - float(rng.uniform(1.0, 3.0))
+            b = sb.body(DYNAMIC, x + float(rng.uniform(-1.5, 1.5)), by, angle=float(rng.uniform(-1, 1)),
+                        v=(float(rng.normal(0, 2)), float(rng.normal(0, 2)), float(rng.normal(0, 1))), acc=acc)
+            sb.box(b, hx, hy, density=1.0, friction=0.5)
+            soft = k % 2 == 1
+            if kind == JOINT_DISTANCE:
+                sb.joint(kind, anchor, b, (0.0, 0.0), (hx * 0.5, 0.0), length=float(rng.uniform(1.0, 3.0)),
+                         frequency=2.0 if soft else 0.0, damping_ratio=0.3 if soft else 0.0)
+            elif kind == JOINT_ROPE:
+                sb.joint(kind, anchor, b, (0.0, 0.0), (0.0, hy * 0.5), max_length=float(rng.uniform(1.5, 3.0)))
+            elif kind == JOINT_WELD:
+                sb.joint(kind, anchor, b, (0.0, -1.0), (0.0, hy), reference_angle=float(rng.uniform(-0.3, 0.3)),
+                         frequency=3.0 if soft else 0.0, damping_ratio=0.5 if soft else 0.0)
+            elif kind == JOINT_FRICTION:
+                sb.joint(kind, anchor, b, (0.0, 0.0), (0.0, 0.0), max_force=float(rng.uniform(1.0, 20.0)),
+                         max_torque=float(rng.uniform(0.5, 5.0)))
+            elif kind == JOINT_MOTOR:
+                sb.joint(kind, anchor, b, linear_offset_x=float(rng.uniform(-1, 1)),
+                         linear_offset_y=float(rng.uniform(-3, -1)), angular_offset=float(rng.uniform(-1, 1)),
+                         max_force=float(rng.uniform(20.0, 200.0)), max_torque=float(rng.uniform(5.0, 50.0)),
+                         correction_factor=0.3)
+    for _ in range(n_disks):
+        d = sb.body(DYNAMIC, float(rng.uniform(-width / 2, width / 2)), float(rng.uniform(10.0, 16.0)), acc=acc)
+        sb.disk(d, float(rng.uniform(0.2, 0.5)), density=1.0, friction=0.3)
+    return sb.build()
+
+
 def batched_worlds(n_worlds: int = 4096, seed: int = 1, lo: int = 16, hi: int = 2048) -> List[Scene]:
     """Workload 3: worlds with log-uniform body counts in [lo, hi]; each is, with equal
     probability, a box pyramid with as many rows as the count allows or a pile."""
@@ -585,6 +671,11 @@ def scene_text(scene: Scene, conf_overrides: dict | None = None) -> str:
         an = scene.joint_anchors[j]
         pr = scene.joint_params[j]
         fl = scene.joint_flags[j]
+        kind = int(scene.joint_type[j])
+        if kind != JOINT_REVOLUTE:
+            out.append("jointx %d %d %d %s %d %s" % (kind, a, b, " ".join(hx(x) for x in an), fl[2],
+                                                     " ".join(hx(x) for x in scene.joint_extra[j])))
+            continue
         out.append("joint %d %d %s %d %s %s %d %s %s %d" % (
             a, b, " ".join(hx(x) for x in (*an, pr[0])), fl[0], hx(pr[1]), hx(pr[2]), fl[1],
             hx(pr[3]), hx(pr[4]), fl[2]))

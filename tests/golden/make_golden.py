@@ -47,6 +47,8 @@ def cases():
         # time-of-impact phase on (StepConf::doToi, the reference's default)
         "toi_bullets60_seed3": (scenes.bullets(60, np.random.default_rng(3)), [1, 5, 30, 90], {"doToi": 1}),
         "toi_pile200_seed11": (scenes.pile(200, np.random.default_rng(11)), [1, 60, 180, 300], {"doToi": 1}),
+        # distance, rope, weld, friction and motor joints side by side
+        "joint_zoo_seed7": (scenes.joint_zoo(np.random.default_rng(7)), [1, 60, 180], {}),
     }
 
 
