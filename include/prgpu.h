@@ -120,7 +120,7 @@ typedef struct prgpu_batch_desc {
     const int32_t* shape_filter;        /* [n_shapes*4] category mask group sensor */
     uint32_t n_verts;
     const float* verts;                 /* [n_verts*2] */
-    uint32_t n_joints;                  /* revolute joints */
+    uint32_t n_joints;                  /* joints (kinds in joint_type) */
     const uint32_t* joint_bodies;       /* [n_joints*2] */
     const float* joint_anchors;         /* [n_joints*4] localAnchorA.xy localAnchorB.xy */
     const float* joint_params;          /* [n_joints*6] refAngle lower upper motorSpeed maxMotorTorque - */
@@ -129,7 +129,23 @@ typedef struct prgpu_batch_desc {
     uint32_t candidate_capacity;        /* 0: automatic */
     const float* body_mass;             /* [n_bodies*4] optional invMass invRotInertia localCenter.xy of each
                                            dynamic body (SetMassData, Body.cpp); NULL: from the shapes */
+    const int32_t* joint_type;          /* [n_joints] PRGPU_JOINT_*; NULL: every joint is revolute */
+    const float* joint_extra;           /* [n_joints*8] parameters of the other kinds (below) */
 } prgpu_batch_desc;
+
+/* Joint kinds and their joint_extra parameters (the reference's JointConf types;
+ * joint_anchors are localAnchorA.xy localAnchorB.xy, joint_flags[2] collideConnected):
+ *   REVOLUTE   RevoluteJointConf: joint_params, joint_flags (extra unused)
+ *   DISTANCE   DistanceJointConf: length frequency dampingRatio
+ *   ROPE       RopeJointConf:     maxLength
+ *   WELD       WeldJointConf:     referenceAngle frequency dampingRatio
+ *   FRICTION   FrictionJointConf: maxForce maxTorque
+ *   MOTOR      MotorJointConf:    linearOffset.x linearOffset.y angularOffset maxForce maxTorque
+ *                                 correctionFactor (anchors unused) */
+enum prgpu_joint_kind {
+    PRGPU_JOINT_REVOLUTE = 0, PRGPU_JOINT_DISTANCE = 1, PRGPU_JOINT_ROPE = 2, PRGPU_JOINT_WELD = 3,
+    PRGPU_JOINT_FRICTION = 4, PRGPU_JOINT_MOTOR = 5
+};
 
 int prgpu_abi_version(void);
 int prgpu_default_step_conf(prgpu_step_conf* out);

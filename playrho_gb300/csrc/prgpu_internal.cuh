@@ -261,7 +261,8 @@ struct DW {
     float4* j_anchor;        // laA.xy laB.xy
     float4* j_param;         // ref lower upper motorSpeed
     float* j_maxtorque;
-    uint32_t* j_flags;       // enableLimit | enableMotor << 1 | collideConnected << 2
+    uint32_t* j_flags;       // enableLimit | enableMotor << 1 | collideConnected << 2 | kind << 8
+    const float4* j_extra;   // [2J] the other kinds' parameters (PRGPU_JOINT_* layouts)
     float4* j_r;             // rA.xy rB.xy
     float4* j_m0;            // mass ex.x ex.y ex.z ey.y
     float4* j_m1;            // ey.z ez.z angularMass motorImpulse

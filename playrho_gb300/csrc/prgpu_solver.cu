@@ -460,7 +460,7 @@ __global__ void k_build_constraints(DW d) {
 
 // ---- revolute joints (RevoluteJointConf.cpp:127-431) --------------------------
 template <class BS>
-__device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
+__device__ void revolute_init_velocity(const DW& d, const BS& bs, uint32_t j) {
     const DConf& c = *d.conf;
     const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
     const float4 mA = bs.mass(a), mB = bs.mass(b);
@@ -518,7 +518,7 @@ __device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
 }
 
 template <class BS>
-__device__ void joint_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
+__device__ void revolute_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
     const DConf& c = *d.conf;
     const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
     const float4 mA = bs.mass(a), mB = bs.mass(b);
@@ -565,7 +565,7 @@ __device__ void joint_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
 
 // Returns whether the joint is within tolerance.
 template <class BS>
-__device__ bool joint_solve_position(const DW& d, const BS& bs, uint32_t j) {
+__device__ bool revolute_solve_position(const DW& d, const BS& bs, uint32_t j) {
     const DConf& c = *d.conf;
     const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
     const float4 mA = bs.mass(a), mB = bs.mass(b);
@@ -592,6 +592,491 @@ __device__ bool joint_solve_position(const DW& d, const BS& bs, uint32_t j) {
     if (bs.writable(a)) bs.set_pos(a, pA);
     if (bs.writable(b)) bs.set_pos(b, pB);
     return (positionError <= c.linearSlop * c.linearSlop) && (0.f <= c.angularSlop);
+}
+
+// ---- the other joint kinds (DistanceJointConf.cpp, RopeJointConf.cpp,
+// WeldJointConf.cpp, FrictionJointConf.cpp, MotorJointConf.cpp) ----------------
+// Solver state in j_m0 / j_m1 / j_imp by kind:
+//   distance, rope: m0 = u.x u.y mass invGamma, m1 = bias length - -, imp.x
+//   weld:           m0 = mass00 mass01 mass02 mass11, m1 = mass12 mass22 gamma bias, imp.xyz
+//   friction:       m0 = linearMass00 01 11 angularMass, imp = linear xy, angular z
+//   motor:          friction's, and m1 = linearError xy, angularError
+enum : uint32_t { JK_REVOLUTE = 0, JK_DISTANCE = 1, JK_ROPE = 2, JK_WELD = 3, JK_FRICTION = 4, JK_MOTOR = 5 };
+__device__ __forceinline__ uint32_t joint_kind(const DW& d, uint32_t j) { return (d.j_flags[j] >> 8) & 0xffu; }
+
+// UnitVec::Get(x, y) (UnitVec.hpp:175-235): direction and magnitude.
+__device__ __forceinline__ V2 unit_len(V2 v, float& len) {
+    const float m2 = v.x * v.x + v.y * v.y;
+    if (is_normal_f(m2)) {
+        const float m = sqrtf(m2);
+        const float inv = 1.0f / m;
+        len = m;
+        return mk(v.x * inv, v.y * inv);
+    }
+    const float m = hypotf(v.x, v.y);
+    if (!is_normal_f(m)) { len = 0.f; return mk(0.f, 0.f); }
+    len = m;
+    return mk(v.x / m, v.y / m);
+}
+// Velocity / Position -= and += {invMass * P, invRotI * L}.
+__device__ __forceinline__ void sub_imp(float4& s, float iM, V2 P, float iI, float L) {
+    s.x = s.x - P.x * iM; s.y = s.y - P.y * iM; s.z = s.z - iI * L;
+}
+__device__ __forceinline__ void add_imp(float4& s, float iM, V2 P, float iI, float L) {
+    s.x = s.x + P.x * iM; s.y = s.y + P.y * iM; s.z = s.z + iI * L;
+}
+__device__ __forceinline__ V2 point_vel(float4 v, V2 r) { return mk(v.x, v.y) + revperp(r) * v.z; }
+__device__ __forceinline__ V2 anchor_r(V2 la, float4 m, float angle) {
+    return rotate(la - mk(m.z, m.w), unit_from_angle(angle));
+}
+// Matrix * vector, rows accumulated from zero (Vector.hpp:455-470), for a
+// symmetric 2x2 (a b; b c).
+__device__ __forceinline__ V2 sym22_mul(float a, float b, float c, V2 v) {
+    float x = 0.f; x += a * v.x; x += b * v.y;
+    float y = 0.f; y += b * v.x; y += c * v.y;
+    return mk(x, y);
+}
+__device__ __forceinline__ float dot3(const float* a, const float* b) {
+    float r = 0.f; r += a[0] * b[0]; r += a[1] * b[1]; r += a[2] * b[2]; return r;
+}
+__device__ __forceinline__ void cross3(const float* a, const float* b, float* o) {
+    const float x = a[1] * b[2] - a[2] * b[1], y = a[2] * b[0] - a[0] * b[2], z = a[0] * b[1] - a[1] * b[0];
+    o[0] = x; o[1] = y; o[2] = z;
+}
+// GetMat33 of the weld joint (WeldJointConf.cpp:36-62); K[i] is the i-th Vec3.
+__device__ __forceinline__ void weld_k(float iMA, V2 rA, float iIA, float iMB, V2 rB, float iIB, float K[3][3]) {
+    const float exx = iMA + (rA.y * rA.y) * iIA + iMB + (rB.y * rB.y) * iIB;
+    const float eyx = -rA.y * rA.x * iIA + -rB.y * rB.x * iIB;
+    const float ezx = -rA.y * iIA + -rB.y * iIB;
+    const float eyy = iMA + (rA.x * rA.x) * iIA + iMB + (rB.x * rB.x) * iIB;
+    const float ezy = rA.x * iIA + rB.x * iIB;
+    const float ezz = iIA + iIB;
+    K[0][0] = exx; K[1][0] = eyx; K[2][0] = ezx;
+    K[0][1] = eyx; K[1][1] = eyy; K[2][1] = ezy;
+    K[0][2] = ezx; K[1][2] = ezy; K[2][2] = ezz;
+}
+// Solve22 / Solve33 (Math.hpp:447-475).
+__device__ __forceinline__ V2 solve22k(const float K[3][3], V2 b) {
+    const float xx = K[0][0], xy = K[1][0], yx = K[0][1], yy = K[1][1];
+    const float cp = xx * yy - xy * yx;
+    const float det = (cp != 0.f) ? (1.0f / cp) : cp;
+    return mk(det * (yy * b.x - xy * b.y), det * (xx * b.y - yx * b.x));
+}
+__device__ __forceinline__ void solve33(const float K[3][3], const float* b, float* o) {
+    float c[3], t[3];
+    cross3(K[1], K[2], c);
+    const float dp = dot3(K[0], c);
+    const float det = (dp != 0.f) ? (1.0f / dp) : dp;
+    const float x = det * dot3(b, c);
+    cross3(b, K[2], t);
+    const float y = det * dot3(K[0], t);
+    cross3(K[1], b, t);
+    const float z = det * dot3(K[0], t);
+    o[0] = x; o[1] = y; o[2] = z;
+}
+
+template <class BS>
+__device__ void distance_init_velocity(const DW& d, const BS& bs, uint32_t j, bool rope) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float4 pA = bs.pos(a), pB = bs.pos(b);
+    float4 vA = bs.vel(a), vB = bs.vel(b);
+    const float4 an = d.j_anchor[j], e = d.j_extra[2 * j];
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    float length;
+    V2 u = unit_len((mk(pB.x, pB.y) + rB) - (mk(pA.x, pA.y) + rA), length);
+    float4 imp = d.j_imp[j];
+    float jmass = 0.f, invGamma = 0.f, bias = 0.f;
+    bool warm = c.doWarmStart != 0;
+    if (rope) {
+        // RopeJointConf InitVelocity (RopeJointConf.cpp:78-131)
+        if (!(length > c.linearSlop)) {
+            u = mk(0.f, 0.f);
+            imp.x = 0.f;
+            warm = false;
+        } else {
+            const float crA = cross(rA, u), crB = cross(rB, u);
+            const float invMass = mA.x + mB.x + mA.y * (crA * crA) + mB.y * (crB * crB);
+            jmass = (invMass != 0.f) ? 1.0f / invMass : 0.f;
+        }
+    } else {
+        // DistanceJointConf InitVelocity (DistanceJointConf.cpp:79-146)
+        const float crAu = cross(rA, u), crBu = cross(rB, u);
+        float invMass = mA.x + mA.y * (crAu * crAu) + mB.x + mB.y * (crBu * crBu);
+        jmass = (invMass != 0.f) ? 1.0f / invMass : 0.f;
+        if (e.y > 0.f) {
+            const float Pi = 3.14159265358979323846264338327950288f;
+            const float C = length - e.x;
+            const float omega = 2.0f * Pi * e.y;
+            const float dd = 2.0f * jmass * e.z * omega;
+            const float k = jmass * (omega * omega);
+            const float h = c.deltaTime;
+            const float gamma = h * (dd + h * k);
+            invGamma = (gamma != 0.f) ? 1.0f / gamma : 0.f;
+            bias = C * h * k * invGamma;
+            invMass += invGamma;
+            jmass = (invMass != 0.f) ? 1.0f / invMass : 0.f;
+        }
+    }
+    if (warm) {
+        imp.x *= c.dtRatio;
+        const V2 P = u * imp.x;
+        sub_imp(vA, mA.x, P, mA.y, cross(rA, P));
+        add_imp(vB, mB.x, P, mB.y, cross(rB, P));
+    } else if (!rope || length > c.linearSlop) {
+        imp.x = 0.f;
+    }
+    d.j_imp[j] = imp;
+    d.j_r[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    d.j_m0[j] = make_float4(u.x, u.y, jmass, invGamma);
+    d.j_m1[j] = make_float4(bias, length, 0.f, 0.f);
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ void distance_solve_velocity(const DW& d, const BS& bs, uint32_t j, bool rope) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    float4 vA = bs.vel(a), vB = bs.vel(b);
+    const float4 r = d.j_r[j], m0 = d.j_m0[j], m1 = d.j_m1[j];
+    float4 imp = d.j_imp[j];
+    const V2 rA = mk(r.x, r.y), rB = mk(r.z, r.w), u = mk(m0.x, m0.y);
+    V2 P;
+    if (rope) {
+        // RopeJointConf SolveVelocity (RopeJointConf.cpp:133-171)
+        const float C = m1.y - d.j_extra[2 * j].x;
+        const float inv_h = (c.deltaTime != 0.f) ? 1.0f / c.deltaTime : 0.f;
+        const float Cdot = dot(u, point_vel(vB, rB) - point_vel(vA, rA)) + ((C < 0.f) ? inv_h * C : 0.f);
+        float local = -m0.z * Cdot;
+        const float old = imp.x;
+        imp.x = minf_(0.f, imp.x + local);
+        local = imp.x - old;
+        P = u * local;
+    } else {
+        // DistanceJointConf SolveVelocity (DistanceJointConf.cpp:148-182)
+        const float Cdot = dot(u, point_vel(vB, rB) - point_vel(vA, rA));
+        const float impulse = -m0.z * (Cdot + m1.x + m0.w * imp.x);
+        imp.x += impulse;
+        P = u * impulse;
+    }
+    sub_imp(vA, mA.x, P, mA.y, cross(rA, P));
+    add_imp(vB, mB.x, P, mB.y, cross(rB, P));
+    d.j_imp[j] = imp;
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ bool distance_solve_position(const DW& d, const BS& bs, uint32_t j, bool rope) {
+    const DConf& c = *d.conf;
+    const float4 e = d.j_extra[2 * j];
+    if (!rope && e.y > 0.f) return true;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    float4 pA = bs.pos(a), pB = bs.pos(b);
+    const float4 an = d.j_anchor[j];
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    float length;
+    const V2 u = unit_len((mk(pB.x, pB.y) + rB) - (mk(pA.x, pA.y) + rA), length);
+    const float C = rope ? clampf_(length - e.x, 0.f, c.maxLinearCorrection)
+                         : clampf_(length - e.x, -c.maxLinearCorrection, c.maxLinearCorrection);
+    const float impulse = -d.j_m0[j].z * C;
+    const V2 P = u * impulse;
+    sub_imp(pA, mA.x, P, mA.y, cross(rA, P));
+    add_imp(pB, mB.x, P, mB.y, cross(rB, P));
+    if (bs.writable(a)) bs.set_pos(a, pA);
+    if (bs.writable(b)) bs.set_pos(b, pB);
+    return rope ? ((length - e.x) < c.linearSlop) : (fabsf(C) < c.linearSlop);
+}
+
+// WeldJointConf (WeldJointConf.cpp:133-376).
+template <class BS>
+__device__ void weld_init_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    const float4 pA = bs.pos(a), pB = bs.pos(b);
+    float4 vA = bs.vel(a), vB = bs.vel(b);
+    const float4 an = d.j_anchor[j], e = d.j_extra[2 * j];
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    float K[3][3];
+    weld_k(iMA, rA, iIA, iMB, rB, iIB, K);
+    float m00, m01, m02 = 0.f, m11, m12 = 0.f, m22 = 0.f, gamma = 0.f, bias = 0.f;
+    if (e.y > 0.f || K[2][2] == 0.f) {
+        // GetInverse22 (Math.hpp:478-490)
+        const float aa = K[0][0], bb = K[1][0], cc = K[0][1], dd = K[1][1];
+        float det = (aa * dd) - (bb * cc);
+        if (det != 0.f) det = 1.0f / det;
+        m00 = det * dd; m01 = -det * cc; m11 = det * aa;
+        if (e.y > 0.f) {
+            float invRotInertia = iIA + iIB;
+            const float rotInertia = (invRotInertia > 0.f) ? 1.0f / invRotInertia : 0.f;
+            const float C = pB.z - pA.z - e.x;
+            const float Pi = 3.14159265358979323846264338327950288f;
+            const float omega = 2.0f * Pi * e.y;
+            const float damp = 2.0f * rotInertia * e.z * omega;
+            const float k = rotInertia * omega * omega;
+            const float h = c.deltaTime;
+            const float invGamma = h * (damp + h * k);
+            gamma = (invGamma != 0.f) ? 1.0f / invGamma : 0.f;
+            bias = C * h * k * gamma;
+            invRotInertia += gamma;
+            m22 = (invRotInertia != 0.f) ? 1.0f / invRotInertia : 0.f;
+        }
+    } else {
+        // GetSymInverse33 (Math.hpp:493-512)
+        float cr[3];
+        cross3(K[1], K[2], cr);
+        const float invDet = dot3(K[0], cr);
+        const float det = (invDet != 0.f) ? (1.0f / invDet) : invDet;
+        const float a11 = K[0][0], a12 = K[1][0], a13 = K[2][0], a22 = K[1][1], a23 = K[2][1], a33 = K[2][2];
+        m01 = det * (a13 * a23 - a12 * a33);
+        m12 = det * (a13 * a12 - a11 * a23);
+        m02 = det * (a12 * a23 - a13 * a22);
+        m00 = det * (a22 * a33 - a23 * a23);
+        m11 = det * (a11 * a33 - a13 * a13);
+        m22 = det * (a11 * a22 - a12 * a12);
+    }
+    float4 imp = d.j_imp[j];
+    if (c.doWarmStart) {
+        imp.x *= c.dtRatio; imp.y *= c.dtRatio; imp.z *= c.dtRatio;
+        const V2 P = mk(imp.x, imp.y);
+        const float L = imp.z;
+        sub_imp(vA, iMA, P, iIA, L + cross(rA, P));
+        add_imp(vB, iMB, P, iIB, L + cross(rB, P));
+    } else {
+        imp.x = imp.y = imp.z = 0.f;
+    }
+    d.j_imp[j] = imp;
+    d.j_r[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    d.j_m0[j] = make_float4(m00, m01, m02, m11);
+    d.j_m1[j] = make_float4(m12, m22, gamma, bias);
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ void weld_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    const float4 oA = bs.vel(a), oB = bs.vel(b);
+    float4 vA = oA, vB = oB;
+    const float4 r = d.j_r[j], m0 = d.j_m0[j], m1 = d.j_m1[j];
+    const V2 rA = mk(r.x, r.y), rB = mk(r.z, r.w);
+    float4 imp = d.j_imp[j];
+    if (d.j_extra[2 * j].y > 0.f) {
+        const float Cdot2 = vB.z - vA.z;
+        const float gamma = m1.z * imp.z;
+        const float impulse2 = -m1.y * (Cdot2 + m1.w + gamma);
+        imp.z += impulse2;
+        vA.z -= iIA * impulse2;
+        vB.z += iIB * impulse2;
+        const V2 Cdot1 = point_vel(vB, rB) - point_vel(vA, rA);
+        // Transform(Vec2, Mat33) (Math.hpp:522-527)
+        const V2 impulse1 = -mk(m0.x * Cdot1.x + m0.y * Cdot1.y, m0.y * Cdot1.x + m0.w * Cdot1.y);
+        imp.x += impulse1.x;
+        imp.y += impulse1.y;
+        sub_imp(vA, iMA, impulse1, iIA, cross(rA, impulse1));
+        add_imp(vB, iMB, impulse1, iIB, cross(rB, impulse1));
+    } else {
+        const V2 Cdot1 = point_vel(vB, rB) - point_vel(vA, rA);
+        const float Cdot[3] = {Cdot1.x, Cdot1.y, vB.z - vA.z};
+        const float row0[3] = {m0.x, m0.y, m0.z}, row1[3] = {m0.y, m0.w, m1.x}, row2[3] = {m0.z, m1.x, m1.y};
+        const float ix = -dot3(row0, Cdot), iy = -dot3(row1, Cdot), iz = -dot3(row2, Cdot);
+        imp.x += ix; imp.y += iy; imp.z += iz;
+        const V2 P = mk(ix, iy);
+        sub_imp(vA, iMA, P, iIA, iz + cross(rA, P));
+        add_imp(vB, iMB, P, iIB, iz + cross(rB, P));
+    }
+    d.j_imp[j] = imp;
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ bool weld_solve_position(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    float4 pA = bs.pos(a), pB = bs.pos(b);
+    const float4 an = d.j_anchor[j], e = d.j_extra[2 * j];
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    float K[3][3];
+    weld_k(iMA, rA, iIA, iMB, rB, iIB, K);
+    const V2 C1 = (mk(pB.x, pB.y) + rB) - (mk(pA.x, pA.y) + rA);
+    const float positionError = sqrtf(mag2(C1));
+    float angularError = 0.f;
+    if (e.y > 0.f) {
+        const V2 P = -solve22k(K, C1);
+        sub_imp(pA, iMA, P, iIA, cross(rA, P));
+        add_imp(pB, iMB, P, iIB, cross(rB, P));
+    } else {
+        const float C2 = pB.z - pA.z - e.x;
+        angularError = fabsf(C2);
+        const float Cv[3] = {C1.x, C1.y, C2};
+        float im[3];
+        if (K[2][2] > 0.f) {
+            float s[3];
+            solve33(K, Cv, s);
+            im[0] = -s[0]; im[1] = -s[1]; im[2] = -s[2];
+        } else {
+            const V2 i2 = -solve22k(K, C1);
+            im[0] = i2.x; im[1] = i2.y; im[2] = 0.f;
+        }
+        const V2 P = mk(im[0], im[1]);
+        sub_imp(pA, iMA, P, iIA, im[2] + cross(rA, P));
+        add_imp(pB, iMB, P, iIB, im[2] + cross(rB, P));
+    }
+    if (bs.writable(a)) bs.set_pos(a, pA);
+    if (bs.writable(b)) bs.set_pos(b, pB);
+    return (positionError <= c.linearSlop) && (angularError <= c.angularSlop);
+}
+
+// FrictionJointConf (FrictionJointConf.cpp:90-239) and MotorJointConf
+// (MotorJointConf.cpp:89-235).
+template <class BS>
+__device__ void friction_init_velocity(const DW& d, const BS& bs, uint32_t j, bool motor) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    const float4 pA = bs.pos(a), pB = bs.pos(b);
+    float4 vA = bs.vel(a), vB = bs.vel(b);
+    const float4 an = d.j_anchor[j], e = d.j_extra[2 * j];
+    V2 rA, rB;
+    if (motor) {
+        rA = rotate(mk(e.x, e.y) - mk(mA.z, mA.w), unit_from_angle(pA.z));
+        rB = rotate(-mk(mB.z, mB.w), unit_from_angle(pB.z));
+    } else {
+        rA = anchor_r(mk(an.x, an.y), mA, pA.z);
+        rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    }
+    float exx, exy, eyy;
+    if (motor) {
+        exx = iMA + iMB + iIA * (rA.y * rA.y) + iIB * (rB.y * rB.y);
+        eyy = iMA + iMB + iIA * (rA.x * rA.x) + iIB * (rB.x * rB.x);
+    } else {
+        exx = iMA + iIA * (rA.y * rA.y) + iMB + iIB * (rB.y * rB.y);
+        eyy = iMA + iIA * (rA.x * rA.x) + iMB + iIB * (rB.x * rB.x);
+    }
+    exy = -iIA * rA.x * rA.y + -iIB * rB.x * rB.y;
+    // Invert(Matrix22) (Math.hpp:430-442)
+    float l00 = 0.f, l01 = 0.f, l11 = 0.f;
+    {
+        const float cp = cross(mk(exx, exy), mk(exy, eyy));
+        if (!almost_zero(cp)) {
+            const float inv = 1.0f / cp;
+            l00 = eyy * inv; l01 = -exy * inv; l11 = exx * inv;
+        }
+    }
+    const float invRotInertia = iIA + iIB;
+    const float angularMass = (invRotInertia > 0.f) ? 1.0f / invRotInertia : 0.f;
+    float4 imp = d.j_imp[j];
+    if (c.doWarmStart) {
+        imp.x *= c.dtRatio; imp.y *= c.dtRatio; imp.z *= c.dtRatio;
+        const V2 P = mk(imp.x, imp.y);
+        sub_imp(vA, iMA, P, iIA, cross(rA, P) + imp.z);
+        add_imp(vB, iMB, P, iIB, cross(rB, P) + imp.z);
+    } else {
+        imp.x = imp.y = imp.z = 0.f;
+    }
+    d.j_imp[j] = imp;
+    d.j_r[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    d.j_m0[j] = make_float4(l00, l01, l11, angularMass);
+    if (motor) {
+        const V2 le = (mk(pB.x, pB.y) + rB) - (mk(pA.x, pA.y) + rA);
+        d.j_m1[j] = make_float4(le.x, le.y, (pB.z - pA.z) - e.z, 0.f);
+    }
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ void friction_solve_velocity(const DW& d, const BS& bs, uint32_t j, bool motor) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    float4 vA = bs.vel(a), vB = bs.vel(b);
+    const float4 r = d.j_r[j], m0 = d.j_m0[j], e0 = d.j_extra[2 * j], e1 = d.j_extra[2 * j + 1];
+    const V2 rA = mk(r.x, r.y), rB = mk(r.z, r.w);
+    float4 imp = d.j_imp[j];
+    const float h = c.deltaTime;
+    const float inv_h = (h != 0.f) ? 1.0f / h : 0.f;
+    const float maxForce = motor ? e0.w : e0.x, maxTorque = motor ? e1.x : e0.y, cf = e1.y;
+    const float4 err = motor ? d.j_m1[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    {
+        const float Cdot = motor ? (vB.z - vA.z) + inv_h * cf * err.z : (vB.z - vA.z);
+        const float angularImpulse = -m0.w * Cdot;
+        const float old = imp.z;
+        const float maxAng = h * maxTorque;
+        imp.z = clampf_(old + angularImpulse, -maxAng, maxAng);
+        const float inc = imp.z - old;
+        if (!motor || inc != 0.f) {
+            vA.z -= iIA * inc;
+            vB.z += iIB * inc;
+        }
+    }
+    {
+        V2 Cdot = point_vel(vB, rB) - point_vel(vA, rA);
+        if (motor) Cdot = Cdot + mk(err.x, err.y) * (inv_h * cf);
+        const V2 impulse = -sym22_mul(m0.x, m0.y, m0.z, Cdot);
+        const V2 old = mk(imp.x, imp.y);
+        V2 li = old + impulse;
+        const float maxImpulse = h * maxForce;
+        if (mag2(li) > maxImpulse * maxImpulse) li = unit_vector(li, mk(0.f, 0.f)) * maxImpulse;
+        imp.x = li.x; imp.y = li.y;
+        const V2 inc = li - old;
+        const float angA = cross(rA, inc), angB = cross(rB, inc);
+        if (!motor || inc.x != 0.f || inc.y != 0.f || angA != 0.f || angB != 0.f) {
+            sub_imp(vA, iMA, inc, iIA, angA);
+            add_imp(vB, iMB, inc, iIB, angB);
+        }
+    }
+    d.j_imp[j] = imp;
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+// Joint dispatch on the kind (the JointConf visitors of Joint.cpp).
+template <class BS>
+__device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
+    switch (joint_kind(d, j)) {
+    case JK_DISTANCE: distance_init_velocity(d, bs, j, false); break;
+    case JK_ROPE: distance_init_velocity(d, bs, j, true); break;
+    case JK_WELD: weld_init_velocity(d, bs, j); break;
+    case JK_FRICTION: friction_init_velocity(d, bs, j, false); break;
+    case JK_MOTOR: friction_init_velocity(d, bs, j, true); break;
+    default: revolute_init_velocity(d, bs, j); break;
+    }
+}
+template <class BS>
+__device__ void joint_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
+    switch (joint_kind(d, j)) {
+    case JK_DISTANCE: distance_solve_velocity(d, bs, j, false); break;
+    case JK_ROPE: distance_solve_velocity(d, bs, j, true); break;
+    case JK_WELD: weld_solve_velocity(d, bs, j); break;
+    case JK_FRICTION: friction_solve_velocity(d, bs, j, false); break;
+    case JK_MOTOR: friction_solve_velocity(d, bs, j, true); break;
+    default: revolute_solve_velocity(d, bs, j); break;
+    }
+}
+// Returns whether the joint is within tolerance.
+template <class BS>
+__device__ bool joint_solve_position(const DW& d, const BS& bs, uint32_t j) {
+    switch (joint_kind(d, j)) {
+    case JK_DISTANCE: return distance_solve_position(d, bs, j, false);
+    case JK_ROPE: return distance_solve_position(d, bs, j, true);
+    case JK_WELD: return weld_solve_position(d, bs, j);
+    case JK_FRICTION: case JK_MOTOR: return true;
+    default: return revolute_solve_position(d, bs, j);
+    }
 }
 
 __device__ __forceinline__ uint32_t joint_island(const DW& d, uint32_t j) {

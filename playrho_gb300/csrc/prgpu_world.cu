@@ -242,7 +242,7 @@ struct HostPrep {
     std::vector<float2> s_mat;
     std::vector<float4> vtx;
     std::vector<uint32_t> jcnt, joff, jother, jcc, jcur;
-    std::vector<float4> j_anchor, j_param, j_zero;
+    std::vector<float4> j_anchor, j_param, j_zero, j_extra;
     std::vector<float> j_maxtorque;
     std::vector<uint32_t> j_bodies, j_flags;
 };
@@ -380,6 +380,7 @@ int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
     j_anchor.resize(J); j_param.resize(J); j_zero.assign(J, make_float4(0.f, 0.f, 0.f, 0.f));
     auto& j_maxtorque = hp.j_maxtorque; j_maxtorque.resize(J);
     auto& j_bodies = hp.j_bodies; auto& j_flags = hp.j_flags; j_bodies.resize(2 * J); j_flags.resize(J);
+    hp.j_extra.assign(2 * (size_t)J, make_float4(0.f, 0.f, 0.f, 0.f));
     for (uint32_t j = 0; j < J; ++j) {
         const uint32_t a = ds->joint_bodies[2 * j], b = ds->joint_bodies[2 * j + 1];
         const uint32_t cc = ds->joint_flags[3 * j + 2] ? 1u : 0u;
@@ -389,7 +390,13 @@ int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
         j_anchor[j] = make_float4(ds->joint_anchors[4 * j], ds->joint_anchors[4 * j + 1], ds->joint_anchors[4 * j + 2], ds->joint_anchors[4 * j + 3]);
         j_param[j] = make_float4(ds->joint_params[6 * j], ds->joint_params[6 * j + 1], ds->joint_params[6 * j + 2], ds->joint_params[6 * j + 3]);
         j_maxtorque[j] = ds->joint_params[6 * j + 4];
-        j_flags[j] = (ds->joint_flags[3 * j] ? 1u : 0u) | (ds->joint_flags[3 * j + 1] ? 2u : 0u) | (cc << 2);
+        const int32_t kind = ds->joint_type ? ds->joint_type[j] : PRGPU_JOINT_REVOLUTE;
+        if (kind < PRGPU_JOINT_REVOLUTE || kind > PRGPU_JOINT_MOTOR) return PRGPU_EINVAL;
+        j_flags[j] = (ds->joint_flags[3 * j] ? 1u : 0u) | (ds->joint_flags[3 * j + 1] ? 2u : 0u) | (cc << 2) |
+                     ((uint32_t)kind << 8);
+        const float* e = ds->joint_extra ? ds->joint_extra + 8 * (size_t)j : nullptr;
+        hp.j_extra[2 * j] = e ? make_float4(e[0], e[1], e[2], e[3]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        hp.j_extra[2 * j + 1] = e ? make_float4(e[4], e[5], e[6], e[7]) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     return PRGPU_OK;
 }
@@ -837,6 +844,9 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.s_body, S); AL(d.s_meta, S); AL(d.s_voff, S); AL(d.s_radius, S); AL(d.s_mat, S); AL(d.s_filter, S);
     AL(d.s_group, S); AL(d.verts, vtx.size()); AL(d.p_aabb, S); AL(d.p_moved, S); AL(d.moved_list, S);
     AL(d.j_bodies, 2 * J); AL(d.j_anchor, J); AL(d.j_param, J); AL(d.j_maxtorque, J); AL(d.j_flags, J);
+    float4* j_extra_d;
+    AL(j_extra_d, 2 * (size_t)J);
+    d.j_extra = j_extra_d;
     AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_imp, J);
     AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
     AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C);
@@ -935,6 +945,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ok &= up(d.j_bodies, j_bodies.data(), sizeof(uint32_t) * 2 * J);
     ok &= up(d.j_anchor, j_anchor.data(), sizeof(float4) * J);
     ok &= up(d.j_param, j_param.data(), sizeof(float4) * J);
+    ok &= up(j_extra_d, hp.j_extra.data(), sizeof(float4) * 2 * J);
     ok &= up(d.j_maxtorque, j_maxtorque.data(), sizeof(float) * J);
     ok &= up(d.j_flags, j_flags.data(), sizeof(uint32_t) * J);
     ok &= up(d.j_imp, j_zero.data(), sizeof(float4) * J);
@@ -1573,7 +1584,8 @@ int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every) {
         std::vector<uint32_t> jf(w->d.n_joints);
         CU(cudaMemcpy(jf.data(), w->d.j_flags, sizeof(uint32_t) * jf.size(), cudaMemcpyDeviceToHost));
         for (uint32_t f : jf)
-            if (f & 3u) return fail(w, PRGPU_EINVAL, "adjoint: joints with a limit or a motor are not differentiated");
+            if ((f & 3u) || (f >> 8))
+                return fail(w, PRGPU_EINVAL, "adjoint: only revolute joints without a limit or a motor are differentiated");
     }
     AdjWindow* a = new AdjWindow();
     a->every = checkpoint_every;

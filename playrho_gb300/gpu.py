@@ -66,7 +66,7 @@ class BatchDesc(ctypes.Structure):
         ("shape_restitution", P), ("shape_filter", P), ("n_verts", ctypes.c_uint32), ("verts", P),
         ("n_joints", ctypes.c_uint32), ("joint_bodies", P), ("joint_anchors", P), ("joint_params", P),
         ("joint_flags", P), ("contact_capacity", ctypes.c_uint32), ("candidate_capacity", ctypes.c_uint32),
-        ("body_mass", P)]
+        ("body_mass", P), ("joint_type", P), ("joint_extra", P)]
 
 
 class Schedule(ctypes.Structure):
@@ -223,6 +223,8 @@ def flatten(scenes: Sequence[Scene]) -> dict:
         "joint_anchors": cat(lambda s: s.joint_anchors.reshape(-1, 4), np.float32),
         "joint_params": cat(lambda s: s.joint_params.reshape(-1, 6), np.float32),
         "joint_flags": cat(lambda s: s.joint_flags.reshape(-1, 3), np.int32),
+        "joint_type": cat(lambda s: s.joint_type.reshape(-1), np.int32),
+        "joint_extra": cat(lambda s: s.joint_extra.reshape(-1, 8), np.float32),
         "body_base": body_base,
     }
     return out
@@ -240,7 +242,7 @@ def batch_desc(scenes: Sequence[Scene], contact_capacity: int = 0, candidate_cap
     for k in ("body_type", "body_pos", "body_vel", "body_acc", "body_damp", "body_flags", "shape_body",
               "shape_kind", "shape_voff", "shape_nv", "shape_radius", "shape_density", "shape_friction",
               "shape_restitution", "shape_filter", "verts", "joint_bodies", "joint_anchors",
-              "joint_params", "joint_flags"):
+              "joint_params", "joint_flags", "joint_type", "joint_extra"):
         setattr(d, k, _ptr(f[k]))
     d.n_shapes = int(f["shape_body"].size)
     d.n_verts = int(f["verts"].shape[0])
@@ -280,7 +282,7 @@ class GpuBatch:
         for k in ("body_type", "body_pos", "body_vel", "body_acc", "body_damp", "body_flags", "shape_body",
                   "shape_kind", "shape_voff", "shape_nv", "shape_radius", "shape_density", "shape_friction",
                   "shape_restitution", "shape_filter", "verts", "joint_bodies", "joint_anchors",
-                  "joint_params", "joint_flags"):
+                  "joint_params", "joint_flags", "joint_type", "joint_extra"):
             setattr(d, k, _ptr(f[k]))
         d.n_shapes = int(f["shape_body"].size)
         d.n_verts = int(f["verts"].shape[0])

@@ -1,0 +1,101 @@
+"""The GPU step with distance, rope, weld, friction and motor joints against the
+CPU oracle (whose joints are pinned bit for bit to the reference:
+tests/test_oracle_vs_reference.py, tests/golden/ref_joint_zoo_seed7.npz).
+
+The GPU differs from the oracle only in sin/cos, so a mechanism alone in its
+world follows the oracle to within float rounding growth; joints keep their
+constraints (rope and distance lengths, weld angles); a batch gives each world
+the bits it has alone; the adjoint refuses joint kinds it does not
+differentiate.  Everything goes through the C ABI.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from playrho_gb300 import scenes
+from playrho_gb300.gpu import GpuBatch, PrgpuError
+
+pytestmark = pytest.mark.gpu
+
+KINDS = {"distance": scenes.JOINT_DISTANCE, "rope": scenes.JOINT_ROPE, "weld": scenes.JOINT_WELD,
+         "friction": scenes.JOINT_FRICTION, "motor": scenes.JOINT_MOTOR}
+
+
+def single_mechanisms(kind, n, seed):
+    rng = np.random.default_rng(seed)
+    return [scenes.joint_zoo(rng, per_kind=2, kinds=[kind], n_disks=0) for _ in range(n)]
+
+
+@pytest.mark.parametrize("name", sorted(KINDS))
+def test_joint_kind_matches_oracle(gpu_lib, name):
+    worlds = single_mechanisms(KINDS[name], 6, 50 + KINDS[name])
+    g = GpuBatch(worlds)
+    ows = [oracle.OracleWorld(w) for w in worlds]
+    for step in range(60):
+        g.step()
+        for ow in ows:
+            ow.step()
+        if step in (0, 59):
+            gb = g.bodies()
+            for i, ow in enumerate(ows):
+                base, n = int(g.body_base[i]), worlds[i].n_bodies
+                ob = ow.bodies()
+                # one step: within 1e-5 relative; 60 steps: rounding growth of sin/cos only
+                tol = 1e-5 if step == 0 else 2e-3
+                np.testing.assert_allclose(gb["pos"][base:base + n], ob["pos"], rtol=tol, atol=tol,
+                                           err_msg=f"{name} world {i} step {step}")
+                np.testing.assert_allclose(gb["vel"][base:base + n], ob["vel"], rtol=tol, atol=10 * tol,
+                                           err_msg=f"{name} world {i} step {step}")
+
+
+def _anchor_distance(g, w, base, j):
+    a, b = (int(x) for x in w.joint_bodies[j])
+    xf = g.bodies()["xf"]
+
+    def world_point(body, local):
+        c, s = xf[base + body, 2], xf[base + body, 3]
+        return xf[base + body, :2] + np.array([c * local[0] - s * local[1], s * local[0] + c * local[1]])
+
+    an = w.joint_anchors[j]
+    return float(np.linalg.norm(world_point(b, an[2:4]) - world_point(a, an[0:2])))
+
+
+def test_joint_constraints_hold(gpu_lib):
+    worlds = [scenes.joint_zoo(np.random.default_rng(70 + k), per_kind=3, n_disks=8) for k in range(4)]
+    g = GpuBatch(worlds)
+    g.step_n(120, None)
+    tol = 0.1  # the position solver's corrections under impacts, in metres / radians
+    for i, w in enumerate(worlds):
+        base = int(g.body_base[i])
+        pos = g.bodies()["pos"]
+        for j in range(w.n_joints):
+            kind = int(w.joint_type[j])
+            if kind == scenes.JOINT_ROPE:
+                assert _anchor_distance(g, w, base, j) <= float(w.joint_extra[j][0]) + tol
+            elif kind == scenes.JOINT_DISTANCE and w.joint_extra[j][1] == 0.0:
+                assert abs(_anchor_distance(g, w, base, j) - float(w.joint_extra[j][0])) <= tol
+            elif kind == scenes.JOINT_WELD and w.joint_extra[j][1] == 0.0:
+                a, b = (int(x) for x in w.joint_bodies[j])
+                rel = pos[base + b, 2] - pos[base + a, 2] - float(w.joint_extra[j][0])
+                assert abs(rel) <= tol
+                assert _anchor_distance(g, w, base, j) <= tol
+
+
+def test_joint_batch_equals_single_worlds(gpu_lib):
+    worlds = [scenes.joint_zoo(np.random.default_rng(90 + k), per_kind=2, n_disks=6) for k in range(4)]
+    g = GpuBatch(worlds)
+    singles = [GpuBatch([w]) for w in worlds]
+    g.step_n(80, None)
+    for s in singles:
+        s.step_n(80, None)
+    gb = g.bodies()
+    for i, s in enumerate(singles):
+        base, n = int(g.body_base[i]), worlds[i].n_bodies
+        np.testing.assert_array_equal(gb["pos"][base:base + n], s.bodies()["pos"])
+        np.testing.assert_array_equal(gb["vel"][base:base + n], s.bodies()["vel"])
+
+
+def test_adjoint_rejects_other_joint_kinds(gpu_lib):
+    g = GpuBatch(single_mechanisms(scenes.JOINT_WELD, 1, 3))
+    with pytest.raises(PrgpuError):
+        g.adjoint_begin(4)
