@@ -13,7 +13,12 @@
 #include "playrho/d2/DiskShapeConf.hpp"
 #include "playrho/d2/EdgeShapeConf.hpp"
 #include "playrho/d2/PolygonShapeConf.hpp"
+#include "playrho/d2/DistanceJointConf.hpp"
+#include "playrho/d2/FrictionJointConf.hpp"
+#include "playrho/d2/MotorJointConf.hpp"
 #include "playrho/d2/RevoluteJointConf.hpp"
+#include "playrho/d2/RopeJointConf.hpp"
+#include "playrho/d2/WeldJointConf.hpp"
 
 namespace playrho::d2 {
 
@@ -126,22 +131,64 @@ prgpu::HostShape ToHost(const Shape& shape) {
     return h;
 }
 
+// The joint kinds the GPU steps, with their parameters in HostJoint::extra in the
+// order prgpu.h gives (DistanceJointConf.hpp:102-116, RopeJointConf.hpp:89-95,
+// WeldJointConf.hpp:104-119, FrictionJointConf.hpp:97-106, MotorJointConf.hpp:114-129).
 prgpu::HostJoint ToHost(const Joint& joint) {
-    const auto* c = TypeCast<RevoluteJointConf>(&joint);
-    if (!c) throw InvalidArgument("GpuWorld: only revolute joints are stepped on the GPU");
     prgpu::HostJoint h;
-    h.body_a = to_underlying(c->bodyA);
-    h.body_b = to_underlying(c->bodyB);
-    h.anchor_a[0] = F(StripUnit(GetX(c->localAnchorA))); h.anchor_a[1] = F(StripUnit(GetY(c->localAnchorA)));
-    h.anchor_b[0] = F(StripUnit(GetX(c->localAnchorB))); h.anchor_b[1] = F(StripUnit(GetY(c->localAnchorB)));
-    h.reference_angle = F(StripUnit(c->referenceAngle));
-    h.lower = F(StripUnit(c->lowerAngle));
-    h.upper = F(StripUnit(c->upperAngle));
-    h.motor_speed = F(StripUnit(c->motorSpeed));
-    h.max_motor_torque = F(StripUnit(c->maxMotorTorque));
-    h.enable_limit = c->enableLimit ? 1 : 0;
-    h.enable_motor = c->enableMotor ? 1 : 0;
-    h.collide_connected = c->collideConnected ? 1 : 0;
+    const auto common = [&h](const auto& c) {
+        h.body_a = to_underlying(c.bodyA);
+        h.body_b = to_underlying(c.bodyB);
+        h.collide_connected = c.collideConnected ? 1 : 0;
+    };
+    const auto anchors = [&h](const auto& c) {
+        h.anchor_a[0] = F(StripUnit(GetX(c.localAnchorA))); h.anchor_a[1] = F(StripUnit(GetY(c.localAnchorA)));
+        h.anchor_b[0] = F(StripUnit(GetX(c.localAnchorB))); h.anchor_b[1] = F(StripUnit(GetY(c.localAnchorB)));
+    };
+    if (const auto* c = TypeCast<RevoluteJointConf>(&joint)) {
+        common(*c); anchors(*c);
+        h.kind = PRGPU_JOINT_REVOLUTE;
+        h.reference_angle = F(StripUnit(c->referenceAngle));
+        h.lower = F(StripUnit(c->lowerAngle));
+        h.upper = F(StripUnit(c->upperAngle));
+        h.motor_speed = F(StripUnit(c->motorSpeed));
+        h.max_motor_torque = F(StripUnit(c->maxMotorTorque));
+        h.enable_limit = c->enableLimit ? 1 : 0;
+        h.enable_motor = c->enableMotor ? 1 : 0;
+    } else if (const auto* c = TypeCast<DistanceJointConf>(&joint)) {
+        common(*c); anchors(*c);
+        h.kind = PRGPU_JOINT_DISTANCE;
+        h.extra[0] = F(StripUnit(c->length));
+        h.extra[1] = F(StripUnit(Frequency{c->frequency}));
+        h.extra[2] = F(c->dampingRatio);
+    } else if (const auto* c = TypeCast<RopeJointConf>(&joint)) {
+        common(*c); anchors(*c);
+        h.kind = PRGPU_JOINT_ROPE;
+        h.extra[0] = F(StripUnit(c->maxLength));
+    } else if (const auto* c = TypeCast<WeldJointConf>(&joint)) {
+        common(*c); anchors(*c);
+        h.kind = PRGPU_JOINT_WELD;
+        h.extra[0] = F(StripUnit(c->referenceAngle));
+        h.extra[1] = F(StripUnit(Frequency{c->frequency}));
+        h.extra[2] = F(c->dampingRatio);
+    } else if (const auto* c = TypeCast<FrictionJointConf>(&joint)) {
+        common(*c); anchors(*c);
+        h.kind = PRGPU_JOINT_FRICTION;
+        h.extra[0] = F(StripUnit(Force{c->maxForce}));
+        h.extra[1] = F(StripUnit(Torque{c->maxTorque}));
+    } else if (const auto* c = TypeCast<MotorJointConf>(&joint)) {
+        common(*c);
+        h.kind = PRGPU_JOINT_MOTOR;
+        h.extra[0] = F(StripUnit(GetX(c->linearOffset)));
+        h.extra[1] = F(StripUnit(GetY(c->linearOffset)));
+        h.extra[2] = F(StripUnit(c->angularOffset));
+        h.extra[3] = F(StripUnit(Force{c->maxForce}));
+        h.extra[4] = F(StripUnit(Torque{c->maxTorque}));
+        h.extra[5] = F(c->correctionFactor);
+    } else {
+        throw InvalidArgument("GpuWorld: only revolute, distance, rope, weld, friction and motor joints are "
+                              "stepped on the GPU");
+    }
     return h;
 }
 

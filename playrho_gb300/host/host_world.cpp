@@ -233,8 +233,8 @@ void HostWorld::Build() {
     }
     const uint32_t S = (uint32_t)s_body.size();
     std::vector<uint32_t> j_bodies;
-    std::vector<float> j_anchor, j_param;
-    std::vector<int32_t> j_flags;
+    std::vector<float> j_anchor, j_param, j_extra;
+    std::vector<int32_t> j_flags, j_type;
     for (uint32_t j = 0; j < joints_.size(); ++j) {
         if (!joint_live_[j]) continue;
         const HostJoint& x = joints_[j];
@@ -242,6 +242,8 @@ void HostWorld::Build() {
         j_anchor.insert(j_anchor.end(), {x.anchor_a[0], x.anchor_a[1], x.anchor_b[0], x.anchor_b[1]});
         j_param.insert(j_param.end(), {x.reference_angle, x.lower, x.upper, x.motor_speed, x.max_motor_torque, 0.f});
         j_flags.insert(j_flags.end(), {x.enable_limit, x.enable_motor, x.collide_connected});
+        j_type.push_back(x.kind);
+        j_extra.insert(j_extra.end(), x.extra, x.extra + 8);
     }
     const uint32_t J = (uint32_t)j_bodies.size() / 2;
     prgpu_batch_desc d{};
@@ -254,7 +256,7 @@ void HostWorld::Build() {
     d.shape_friction = s_friction.data(); d.shape_restitution = s_restitution.data(); d.shape_filter = s_filter.data();
     d.n_verts = (uint32_t)(verts.size() / 2); d.verts = verts.data();
     d.n_joints = J; d.joint_bodies = j_bodies.data(); d.joint_anchors = j_anchor.data(); d.joint_params = j_param.data();
-    d.joint_flags = j_flags.data();
+    d.joint_flags = j_flags.data(); d.joint_type = j_type.data(); d.joint_extra = j_extra.data();
     std::vector<float> mass4;
     if (any_mass) {
         // mass data from the shapes, then the bodies that set their own

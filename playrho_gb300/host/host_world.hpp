@@ -56,10 +56,12 @@ struct HostShape {
 
 // RevoluteJointConf (RevoluteJointConf.hpp): bodies, local anchors, limits, motor.
 struct HostJoint {
+    int32_t kind = PRGPU_JOINT_REVOLUTE;                         // prgpu_joint_kind
     uint32_t body_a = 0, body_b = 0;
     float anchor_a[2] = {0.f, 0.f}, anchor_b[2] = {0.f, 0.f};
     float reference_angle = 0.f, lower = 0.f, upper = 0.f, motor_speed = 0.f, max_motor_torque = 0.f;
     int32_t enable_limit = 0, enable_motor = 0, collide_connected = 0;
+    float extra[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // the other kinds' parameters (prgpu.h)
 };
 
 // A live contact after the last step (Contact.hpp + Manifold.hpp).

@@ -1,11 +1,14 @@
-// gpuworld_check.cpp -- the reference's HelloWorld program with two changes:
-// the World is constructed over GpuWorld, and the step configuration turns off
-// TOI (the GPU step is the regular phase).  Everything else goes through
+// gpuworld_check.cpp -- the reference's HelloWorld program with one change:
+// the World is constructed over GpuWorld.  Everything else goes through
 // PlayRho's own World API (CreateShape, CreateBody with BodyConf::Use(shape),
-// Step, GetTransformation, ...).
+// Step with the default StepConf, GetTransformation, ...).  Then one joint of
+// each kind the GPU steps is made through CreateJoint on a second world and the
+// joint GpuWorld hands to the GPU side is printed.
 //
 // Prints, one per line:
 //   bodies N / shapes N / mass <invMass> <invRotI> / type T     after set-up
+//   joint <kind> <collide> <anchorA.x> <anchorB.y> <extra0..5>  per joint kind
+//   joint_rejected <what>                                       for a kind the GPU does not step
 //   step <i> <x> <y> <angle>                                    per step (needs a GPU)
 //   error <what>                                                when stepping fails
 #include <cstdio>
@@ -14,6 +17,52 @@
 #include "playrho/d2/BasicAPI.hpp"
 
 #include "GpuWorld.hpp"
+
+namespace {
+
+void CheckJoints() {
+    using namespace playrho;
+    using namespace playrho::d2;
+    auto world = World{GpuWorld{}};
+    const auto disk = CreateShape(world, DiskShapeConf{}.UseRadius(0.5_m));
+    const auto a = CreateBody(world, BodyConf{}.Use(BodyType::Dynamic).Use(disk).UseLocation(Length2{0_m, 0_m}));
+    const auto b = CreateBody(world, BodyConf{}.Use(BodyType::Dynamic).Use(disk).UseLocation(Length2{2_m, 0_m}));
+    const auto anchorA = Length2{0.25_m, 0_m};
+    const auto anchorB = Length2{-0.25_m, 0.5_m};
+    auto distance = DistanceJointConf{a, b};
+    distance.localAnchorA = anchorA; distance.localAnchorB = anchorB;
+    distance.length = 1.5_m; distance.frequency = 4_Hz; distance.dampingRatio = 0.5f;
+    auto rope = RopeJointConf{a, b};
+    rope.localAnchorA = anchorA; rope.localAnchorB = anchorB; rope.maxLength = 2.5_m;
+    rope.collideConnected = true;
+    auto weld = WeldJointConf{a, b};
+    weld.localAnchorA = anchorA; weld.localAnchorB = anchorB;
+    weld.referenceAngle = 0.25_rad; weld.frequency = 2_Hz; weld.dampingRatio = 0.75f;
+    auto friction = FrictionJointConf{a, b};
+    friction.localAnchorA = anchorA; friction.localAnchorB = anchorB;
+    friction.maxForce = 3_N; friction.maxTorque = 1.5_Nm;
+    auto motor = MotorJointConf{a, b};
+    motor.linearOffset = Length2{1_m, -0.5_m}; motor.angularOffset = 0.125_rad;
+    motor.maxForce = 10_N; motor.maxTorque = 5_Nm; motor.correctionFactor = 0.25f;
+    auto revolute = RevoluteJointConf{a, b};
+    revolute.localAnchorA = anchorA; revolute.localAnchorB = anchorB;
+    for (const auto& def : {Joint{revolute}, Joint{distance}, Joint{rope}, Joint{weld}, Joint{friction},
+                            Joint{motor}}) {
+        const auto id = CreateJoint(world, def);
+        const auto& h = TypeCast<const GpuWorld&>(world).host.GetJoint(to_underlying(id));
+        std::printf("joint %d %d %a %a", h.kind, h.collide_connected, static_cast<double>(h.anchor_a[0]),
+                    static_cast<double>(h.anchor_b[1]));
+        for (auto k = 0; k < 6; ++k) std::printf(" %a", static_cast<double>(h.extra[k]));
+        std::printf("\n");
+    }
+    try {
+        CreateJoint(world, Joint{PrismaticJointConf{a, b}});
+    } catch (const InvalidArgument& e) {
+        std::printf("joint_rejected %s\n", e.what());
+    }
+}
+
+} // namespace
 
 int main() {
     using namespace playrho;
@@ -38,8 +87,8 @@ int main() {
     std::printf("mass %a %a\n", static_cast<double>(StripUnit(GetInvMass(world, ball))),
                 static_cast<double>(StripUnit(GetInvRotInertia(world, ball))));
     std::printf("type %d\n", static_cast<int>(GetType(world, ball)));
-    auto conf = StepConf{};
-    conf.doToi = false;
+    CheckJoints();
+    const auto conf = StepConf{};
     try {
         for (auto i = 0; i < maxSteps; ++i) {
             Step(world, conf);

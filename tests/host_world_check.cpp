@@ -1,7 +1,7 @@
 // host_world_check.cpp -- drives prgpu::HostWorld (the C++ host layer) the way
 // a PlayRho program drives a World: CreateBody, CreateShape + attach, CreateJoint,
 // Step, GetBody, SetBody.  Reads a scene in the reference driver's text form on
-// stdin (body / shape / joint lines, hexadecimal floats), then commands:
+// stdin (body / shape / joint / jointx lines, hexadecimal floats), then commands:
 //   step N                 N steps with the default StepConf
 //   teleport B x y         SetBody of body B with a new location (velocities kept)
 //   destroy_body B         Destroy(BodyID)
@@ -73,6 +73,17 @@ int main() {
                 j.anchor_b[0] = hexf(an[2]); j.anchor_b[1] = hexf(an[3]);
                 j.reference_angle = hexf(ref); j.lower = hexf(lo); j.upper = hexf(up);
                 j.motor_speed = hexf(ms); j.max_motor_torque = hexf(mt);
+                world.CreateJoint(j);
+            } else if (cmd == "jointx") {
+                HostJoint j;
+                uint32_t a, b;
+                std::string an[4], e[8];
+                in >> j.kind >> a >> b >> an[0] >> an[1] >> an[2] >> an[3] >> j.collide_connected;
+                for (auto& x : e) in >> x;
+                j.body_a = body_ids.at(a); j.body_b = body_ids.at(b);
+                j.anchor_a[0] = hexf(an[0]); j.anchor_a[1] = hexf(an[1]);
+                j.anchor_b[0] = hexf(an[2]); j.anchor_b[1] = hexf(an[3]);
+                for (int k = 0; k < 8; ++k) j.extra[k] = hexf(e[k]);
                 world.CreateJoint(j);
             } else if (cmd == "step") {
                 int n = 0;

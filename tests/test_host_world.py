@@ -71,13 +71,17 @@ def _shapes_by_body(sc):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["pile", "chains"])
+@pytest.mark.parametrize("kind", ["pile", "chains", "joint_zoo"])
 def test_host_world_steps_like_the_batch(checker, gpu_lib, kind):
     from playrho_gb300.gpu import GpuBatch
 
     rng = np.random.default_rng(21)
-    sc = scenes.pile(120, rng, width=5.0) if kind == "pile" else scenes.chains_world(rng, n_free=60, n_chains=3,
-                                                                                      links=6)
+    if kind == "pile":
+        sc = scenes.pile(120, rng, width=5.0)
+    elif kind == "chains":
+        sc = scenes.chains_world(rng, n_free=60, n_chains=3, links=6)
+    else:
+        sc = scenes.joint_zoo(rng, per_kind=2, n_disks=10)
     assert _shapes_by_body(sc)  # proxies in the same order on both paths
     res = run(checker, scenes.scene_text(sc) + "step 90\ndump\n")
     assert res.returncode == 0, res.stderr
