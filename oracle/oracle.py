@@ -82,6 +82,7 @@ def _lib(double: bool):
     lib.or_add_joint.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int] + [real] * 4 + [ctypes.c_int,
                                                                                            ctypes.c_void_p]
     lib.or_add_joint.restype = ctypes.c_int
+    lib.or_joint_enable.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.or_default_conf.argtypes = [ctypes.POINTER(Conf)]
     lib.or_step.argtypes = [P, ctypes.POINTER(Conf), ctypes.POINTER(Stats)]
     lib.or_body_count.argtypes = [P]
@@ -144,7 +145,9 @@ class OracleWorld:
             kind = int(scene.joint_type[j])
             if kind != 0:
                 ex = np.ascontiguousarray(scene.joint_extra[j], dtype=self.np_real)
-                lib.or_add_joint(h, kind, int(a), int(b), *(float(x) for x in an), int(fl[2]), ex.ctypes.data)
+                jid = lib.or_add_joint(h, kind, int(a), int(b), *(float(x) for x in an), int(fl[2]),
+                                       ex.ctypes.data)
+                lib.or_joint_enable(h, jid, int(fl[0]), int(fl[1]))
                 continue
             lib.or_add_revolute(h, int(a), int(b), *(float(x) for x in an), float(pr[0]), int(fl[0]),
                                 float(pr[1]), float(pr[2]), int(fl[1]), float(pr[3]), float(pr[4]),

@@ -201,6 +201,10 @@ typedef struct {
     v2 u, linErr;
     real jmass, invGamma, bias, length, angErr;
     real lm[2][2];
+    /* prismatic (axis perp a1 a2 s1 s2), wheel (ax=axis ay=perp sAx=a1 sBx=a2
+     * sAy=s1 sBy=s2), pulley (uA=u uB=u2) and target (C=linErr) state */
+    v2 axis, perp, u2;
+    real a1, a2, s1, s2, springMass, gamma, springImp, angImp;
 } joint_t;
 enum { LS_INACTIVE = 0, LS_LOWER = 1, LS_UPPER = 2, LS_EQUAL = 3 };
 
@@ -492,6 +496,8 @@ void or_reset_mass(or_world* w, int body) {
     b->vel.lin = vadd(b->vel.lin, vmul(revperp(dc), b->vel.ang));
 }
 
+static v2 unit_len(v2 v, real* len);
+
 /* CreateJoint of the other joint types: anchors, collideConnected and the
  * type's parameters (the OR_JOINT_* layouts in playrho_oracle.h). */
 int or_add_joint(or_world* w, int type, int bodyA, int bodyB, real lax, real lay, real lbx, real lby,
@@ -501,7 +507,19 @@ int or_add_joint(or_world* w, int type, int bodyA, int bodyB, real lax, real lay
     joint_t* j = &w->j[jid];
     j->type = type;
     for (int k = 0; k < 8; ++k) j->extra[k] = extra8 ? extra8[k] : R(0);
+    if (type == OR_JOINT_PRISMATIC || type == OR_JOINT_WHEEL) {
+        /* localXAxisA is the UnitVec::Get of the given axis (UnitVec.hpp:175-235) */
+        real len;
+        const v2 ax = unit_len(V(j->extra[0], j->extra[1]), &len);
+        j->extra[0] = ax.x; j->extra[1] = ax.y;
+    }
     return jid;
+}
+
+/* enableLimit / enableMotor of a prismatic (both) or wheel (enableMotor) joint. */
+void or_joint_enable(or_world* w, int jid, int enableLimit, int enableMotor) {
+    w->j[jid].enableLimit = enableLimit;
+    w->j[jid].enableMotor = enableMotor;
 }
 
 int or_add_revolute(or_world* w, int bodyA, int bodyB, real lax, real lay, real lbx, real lby,
@@ -2101,6 +2119,496 @@ static int motor_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) 
     return 0;
 }
 
+/* Solve(Matrix22, Vector2) (Math.hpp:412-425): rows k[0], k[1]. */
+static v2 solve22m(real k[2][2], v2 b) {
+    const real cp = cross(V(k[0][0], k[0][1]), V(k[1][0], k[1][1]));
+    if (!almost_zero(cp)) {
+        const real inverse = R(1) / cp;
+        return V((k[1][1] * b.x - k[1][0] * b.y) * inverse, (k[0][0] * b.y - k[0][1] * b.x) * inverse);
+    }
+    return V(R(0), R(0));
+}
+/* std::max / std::min as the reference calls them: (a < b) ? b : a and (b < a) ? b : a. */
+static inline real stdmax(real a, real b) { return (a < b) ? b : a; }
+static inline real stdmin(real a, real b) { return (b < a) ? b : a; }
+/* Velocity / Position -= and += {invMass * P, invRotI * L} with the scaling first (Velocity.hpp). */
+
+/* PrismaticJointConf InitVelocity / SolveVelocity / SolvePosition
+ * (PrismaticJointConf.cpp:95-449); extra = localXAxisA.xy referenceAngle
+ * lowerTranslation upperTranslation motorSpeed maxMotorForce. */
+static void pj_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const v2 qA = unit_from_angle(A->pos.ang);
+    const v2 rA = anchor_r(j->laA, A), rB = anchor_r(j->laB, B);
+    const v2 d = vsub(vadd(vsub(B->pos.lin, A->pos.lin), rB), rA);
+    const v2 xaxis = V(j->extra[0], j->extra[1]);
+    j->axis = urotate(xaxis, qA);
+    j->a1 = cross(vadd(d, rA), j->axis);
+    j->a2 = cross(rB, j->axis);
+    const real invRotMassA = iIA * (j->a1 * j->a1);
+    const real invRotMassB = iIB * (j->a2 * j->a2);
+    const real totalInvMass = iMA + iMB + invRotMassA + invRotMassB;
+    j->jmass = (totalInvMass > R(0)) ? R(1) / totalInvMass : R(0);
+    {
+        j->perp = urotate(revperp(xaxis), qA);
+        j->s1 = cross(vadd(d, rA), j->perp);
+        j->s2 = cross(rB, j->perp);
+        const real invRotMassA2 = iIA * (j->s1 * j->s1);
+        const real invRotMassB2 = iIB * (j->s2 * j->s2);
+        const real k11 = iMA + iMB + invRotMassA2 + invRotMassB2;
+        const real k12 = iIA * j->s1 + iIB * j->s2;
+        const real k13 = iIA * j->s1 * j->a1 + iIB * j->s2 * j->a2;
+        const real totalInvRotInertia = iIA + iIB;
+        const real k22 = (totalInvRotInertia == R(0)) ? R(1) : totalInvRotInertia;
+        const real k23 = iIA * j->a1 + iIB * j->a2;
+        const real k33 = totalInvMass;
+        j->mass[0][0] = k11; j->mass[0][1] = k12; j->mass[0][2] = k13;
+        j->mass[1][0] = k12; j->mass[1][1] = k22; j->mass[1][2] = k23;
+        j->mass[2][0] = k13; j->mass[2][1] = k23; j->mass[2][2] = k33;
+    }
+    const real lower = j->extra[3], upper = j->extra[4];
+    if (j->enableLimit) {
+        const real jointTranslation = dot(j->axis, d);
+        if (fabs(upper - lower) < (conf->linearSlop * R(2))) {
+            j->limitState = LS_EQUAL;
+        } else if (jointTranslation <= lower) {
+            if (j->limitState != LS_LOWER) { j->limitState = LS_LOWER; j->imp[2] = R(0); }
+        } else if (jointTranslation >= upper) {
+            if (j->limitState != LS_UPPER) { j->limitState = LS_UPPER; j->imp[2] = R(0); }
+        } else {
+            j->limitState = LS_INACTIVE;
+            j->imp[2] = R(0);
+        }
+    } else {
+        j->limitState = LS_INACTIVE;
+        j->imp[2] = R(0);
+    }
+    if (!j->enableMotor) j->motorImpulse = R(0);
+    if (conf->doWarmStart) {
+        j->imp[0] *= conf->dtRatio; j->imp[1] *= conf->dtRatio; j->imp[2] *= conf->dtRatio;
+        j->motorImpulse *= conf->dtRatio;
+        const v2 Px = vmul(j->perp, j->imp[0]);
+        const real Pxs1 = j->imp[0] * j->s1;
+        const real Pxs2 = j->imp[0] * j->s2;
+        const real PzLength = j->motorImpulse + j->imp[2];
+        const v2 Pz = vmul(j->axis, PzLength);
+        const v2 P = vadd(Px, Pz);
+        const real L = j->imp[1];
+        const real LA = L + (Pxs1 + PzLength * j->a1);
+        const real LB = L + (Pxs2 + PzLength * j->a2);
+        sub_imp(&vA, iMA, P, iIA, LA);
+        add_imp(&vB, iMB, P, iIB, LB);
+    } else {
+        j->imp[0] = j->imp[1] = j->imp[2] = R(0);
+        j->motorImpulse = R(0);
+    }
+    A->vel = vA; B->vel = vB;
+}
+static int pj_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    const pos_t oldA = A->vel, oldB = B->vel;
+    pos_t vA = oldA, vB = oldB;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    if (j->enableMotor && j->limitState != LS_EQUAL) {
+        const real vDot = dot(j->axis, vsub(vB.lin, vA.lin));
+        const real Cdot = vDot + (j->a2 * vB.ang - j->a1 * vA.ang);
+        real impulse = j->jmass * (j->extra[5] - Cdot);
+        const real oldImpulse = j->motorImpulse;
+        const real maxImpulse = conf->deltaTime * j->extra[6];
+        j->motorImpulse = clampr(j->motorImpulse + impulse, -maxImpulse, maxImpulse);
+        impulse = j->motorImpulse - oldImpulse;
+        const v2 P = vmul(j->axis, impulse);
+        const real LA = impulse * j->a1, LB = impulse * j->a2;
+        sub_imp(&vA, iMA, P, iIA, LA);
+        add_imp(&vB, iMB, P, iIB, LB);
+    }
+    const v2 velDelta = vsub(vB.lin, vA.lin);
+    const real sRotSpeed = j->s2 * vB.ang - j->s1 * vA.ang;
+    const v2 Cdot1 = V(dot(j->perp, velDelta) + sRotSpeed, vB.ang - vA.ang);
+    if (j->enableLimit && j->limitState != LS_INACTIVE) {
+        const real deltaDot = dot(j->axis, velDelta);
+        const real aRotSpeed = j->a2 * vB.ang - j->a1 * vA.ang;
+        const real Cdot2 = deltaDot + aRotSpeed;
+        const real negCdot[3] = {-Cdot1.x, -Cdot1.y, -Cdot2};
+        const real f1[3] = {j->imp[0], j->imp[1], j->imp[2]};
+        real add[3];
+        solve33(j->mass, negCdot, add);
+        j->imp[0] += add[0]; j->imp[1] += add[1]; j->imp[2] += add[2];
+        if (j->limitState == LS_LOWER) j->imp[2] = stdmax(j->imp[2], R(0));
+        else if (j->limitState == LS_UPPER) j->imp[2] = stdmin(j->imp[2], R(0));
+        const real dz = j->imp[2] - f1[2];
+        const v2 b = V(-Cdot1.x - dz * j->mass[2][0], -Cdot1.y - dz * j->mass[2][1]);
+        const v2 s22 = solve22k(j->mass, b);
+        const v2 f2r = V(s22.x + f1[0], s22.y + f1[1]);
+        j->imp[0] = f2r.x; j->imp[1] = f2r.y;
+        const real df[3] = {j->imp[0] - f1[0], j->imp[1] - f1[1], j->imp[2] - f1[2]};
+        const v2 P = vadd(vmul(j->perp, df[0]), vmul(j->axis, df[2]));
+        const real LA = df[0] * j->s1 + df[1] + df[2] * j->a1;
+        const real LB = df[0] * j->s2 + df[1] + df[2] * j->a2;
+        sub_imp(&vA, iMA, P, iIA, LA);
+        add_imp(&vB, iMB, P, iIB, LB);
+    } else {
+        const v2 df = solve22k(j->mass, vneg(Cdot1));
+        j->imp[0] += df.x; j->imp[1] += df.y;
+        const v2 P = vmul(j->perp, df.x);
+        const real LA = df.x * j->s1 + df.y;
+        const real LB = df.x * j->s2 + df.y;
+        sub_imp(&vA, iMA, P, iIA, LA);
+        add_imp(&vB, iMB, P, iIB, LB);
+    }
+    if (pos_ne(vA, oldA) || pos_ne(vB, oldB)) {
+        A->vel = vA; B->vel = vB;
+        return 0;
+    }
+    return 1;
+}
+static int pj_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t pA = A->pos, pB = B->pos;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const v2 qA = unit_from_angle(pA.ang);
+    const v2 rA = anchor_r(j->laA, A), rB = anchor_r(j->laB, B);
+    const v2 d = vsub(vadd(pB.lin, rB), vadd(pA.lin, rA));
+    const v2 xaxis = V(j->extra[0], j->extra[1]);
+    const v2 axis = urotate(xaxis, qA);
+    const real a1 = cross(vadd(d, rA), axis), a2 = cross(rB, axis);
+    const v2 perp = urotate(revperp(xaxis), qA);
+    const real s1 = cross(vadd(d, rA), perp), s2 = cross(rB, perp);
+    const v2 C1 = V(dot(perp, d), pB.ang - pA.ang - j->extra[2]);
+    real linearError = fabs(C1.x);
+    const real angularError = fabs(C1.y);
+    int active = 0;
+    real C2 = R(0);
+    const real lower = j->extra[3], upper = j->extra[4];
+    if (j->enableLimit) {
+        const real translation = dot(axis, d);
+        if (fabs(upper - lower) < (R(2) * conf->linearSlop)) {
+            C2 = clampr(translation, -conf->maxLinearCorrection, conf->maxLinearCorrection);
+            linearError = stdmax(linearError, fabs(translation));
+            active = 1;
+        } else if (translation <= lower) {
+            C2 = clampr(translation - lower + conf->linearSlop, -conf->maxLinearCorrection, R(0));
+            linearError = stdmax(linearError, lower - translation);
+            active = 1;
+        } else if (translation >= upper) {
+            C2 = clampr(translation - upper - conf->linearSlop, R(0), conf->maxLinearCorrection);
+            linearError = stdmax(linearError, translation - upper);
+            active = 1;
+        }
+    }
+    real impulse[3];
+    if (active) {
+        const real k11 = iMA + iIA * (s1 * s1) + iMB + iIB * (s2 * s2);
+        const real k12 = iIA * s1 + iIB * s2;
+        const real k13 = iIA * s1 * a1 + iIB * s2 * a2;
+        real k22 = iIA + iIB;
+        if (k22 == R(0)) k22 = R(1);
+        const real k23 = iIA * a1 + iIB * a2;
+        const real k33 = iMA + iIA * (a1 * a1) + iMB + iIB * (a2 * a2);
+        real K[3][3] = {{k11, k12, k13}, {k12, k22, k23}, {k13, k23, k33}};
+        const real negC[3] = {-C1.x, -C1.y, -C2};
+        solve33(K, negC, impulse);
+    } else {
+        const real k11 = iMA + iIA * s1 * s1 + iMB + iIB * s2 * s2;
+        const real k12 = iIA * s1 + iIB * s2;
+        real k22 = iIA + iIB;
+        if (k22 == R(0)) k22 = R(1);
+        real K[2][2] = {{k11, k12}, {k12, k22}};
+        const v2 i1 = solve22m(K, vneg(C1));
+        impulse[0] = i1.x; impulse[1] = i1.y; impulse[2] = R(0);
+    }
+    const v2 P = vadd(vmul(perp, impulse[0]), vmul(axis, impulse[2]));
+    const real LA = impulse[0] * s1 + impulse[1] + impulse[2] * a1;
+    const real LB = impulse[0] * s2 + impulse[1] + impulse[2] * a2;
+    sub_imp(&pA, iMA, P, iIA, LA);
+    add_imp(&pB, iMB, P, iIB, LB);
+    A->pos = pA; B->pos = pB;
+    return (linearError <= conf->linearSlop) && (angularError <= conf->angularSlop);
+}
+
+/* WheelJointConf InitVelocity / SolveVelocity / SolvePosition
+ * (WheelJointConf.cpp:80-311); extra = localXAxisA.xy motorSpeed maxMotorTorque
+ * frequency dampingRatio. */
+static void wj_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const v2 qA = unit_from_angle(A->pos.ang);
+    const v2 rA = anchor_r(j->laA, A), rB = anchor_r(j->laB, B);
+    const v2 dd = vsub(vadd(B->pos.lin, rB), vadd(A->pos.lin, rA));
+    const v2 xaxis = V(j->extra[0], j->extra[1]);
+    {
+        j->perp = urotate(revperp(xaxis), qA);  /* ay */
+        j->s1 = cross(vadd(dd, rA), j->perp);   /* sAy */
+        j->s2 = cross(rB, j->perp);             /* sBy */
+        const real invRotMassA = iIA * (j->s1 * j->s1);
+        const real invRotMassB = iIB * (j->s2 * j->s2);
+        const real invMass = iMA + iMB + invRotMassA + invRotMassB;
+        j->jmass = (invMass > R(0)) ? R(1) / invMass : R(0);
+    }
+    j->springMass = R(0);
+    j->bias = R(0);
+    j->gamma = R(0);
+    const real frequency = j->extra[4], dampingRatio = j->extra[5];
+    if (frequency > R(0)) {
+        j->axis = urotate(xaxis, qA);           /* ax */
+        j->a1 = cross(vadd(dd, rA), j->axis);   /* sAx */
+        j->a2 = cross(rB, j->axis);             /* sBx */
+        const real invRotMassA = iIA * (j->a1 * j->a1);
+        const real invRotMassB = iIB * (j->a2 * j->a2);
+        const real invMass = iMA + iMB + invRotMassA + invRotMassB;
+        if (invMass > R(0)) {
+            j->springMass = R(1) / invMass;
+            const real C = dot(dd, j->axis);
+            const real Pi = R(3.14159265358979323846264338327950288L);
+            const real omega = R(2) * Pi * frequency;
+            const real d = R(2) * j->springMass * dampingRatio * omega;
+            const real k = j->springMass * omega * omega;
+            const real h = conf->deltaTime;
+            const real invGamma = h * (d + h * k);
+            j->gamma = (invGamma > R(0)) ? R(1) / invGamma : R(0);
+            j->bias = C * h * k * j->gamma;
+            const real totalInvMass = invMass + j->gamma;
+            j->springMass = (totalInvMass > R(0)) ? R(1) / totalInvMass : R(0);
+        }
+    } else {
+        j->springImp = R(0);
+        j->axis = V(R(0), R(0));
+        j->a1 = R(0);
+        j->a2 = R(0);
+    }
+    if (j->enableMotor) {
+        const real invRotInertia = iIA + iIB;
+        j->angularMass = (invRotInertia > R(0)) ? R(1) / invRotInertia : R(0);
+    } else {
+        j->angularMass = R(0);
+        j->angImp = R(0);
+    }
+    if (conf->doWarmStart) {
+        j->imp[0] *= conf->dtRatio;
+        j->springImp *= conf->dtRatio;
+        j->angImp *= conf->dtRatio;
+        const v2 P = vadd(vmul(j->perp, j->imp[0]), vmul(j->axis, j->springImp));
+        const real LA = (j->imp[0] * j->s1 + j->springImp * j->a1) + j->angImp;
+        const real LB = (j->imp[0] * j->s2 + j->springImp * j->a2) + j->angImp;
+        sub_imp(&vA, iMA, P, iIA, LA);
+        add_imp(&vB, iMB, P, iIB, LB);
+    } else {
+        j->imp[0] = R(0);
+        j->springImp = R(0);
+        j->angImp = R(0);
+    }
+    A->vel = vA; B->vel = vB;
+}
+static int wj_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    const pos_t oldA = A->vel, oldB = B->vel;
+    pos_t vA = oldA, vB = oldB;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    {
+        const real d = dot(j->axis, vsub(vB.lin, vA.lin));
+        const real Cdot = d + j->a2 * vB.ang - j->a1 * vA.ang;
+        const real impulse = -j->springMass * (Cdot + j->bias + j->gamma * j->springImp);
+        j->springImp += impulse;
+        const v2 P = vmul(j->axis, impulse);
+        const real LA = impulse * j->a1, LB = impulse * j->a2;
+        sub_imp(&vA, iMA, P, iIA, LA);
+        add_imp(&vB, iMB, P, iIB, LB);
+    }
+    {
+        const real Cdot = vB.ang - vA.ang - j->extra[2];
+        real impulse = -j->angularMass * Cdot;
+        const real oldImpulse = j->angImp;
+        const real maxImpulse = conf->deltaTime * j->extra[3];
+        j->angImp = clampr(j->angImp + impulse, -maxImpulse, maxImpulse);
+        impulse = j->angImp - oldImpulse;
+        vA.ang -= iIA * impulse;
+        vB.ang += iIB * impulse;
+    }
+    {
+        const real d = dot(j->perp, vsub(vB.lin, vA.lin));
+        const real Cdot = d + j->s2 * vB.ang - j->s1 * vA.ang;
+        const real impulse = -j->jmass * Cdot;
+        j->imp[0] += impulse;
+        const v2 P = vmul(j->perp, impulse);
+        const real LA = impulse * j->s1, LB = impulse * j->s2;
+        sub_imp(&vA, iMA, P, iIA, LA);
+        add_imp(&vB, iMB, P, iIB, LB);
+    }
+    if (pos_ne(vA, oldA) || pos_ne(vB, oldB)) {
+        A->vel = vA; B->vel = vB;
+        return 0;
+    }
+    return 1;
+}
+static int wj_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t pA = A->pos, pB = B->pos;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const v2 qA = unit_from_angle(pA.ang);
+    const v2 rA = anchor_r(j->laA, A), rB = anchor_r(j->laB, B);
+    const v2 d = vadd(vsub(pB.lin, pA.lin), vsub(rB, rA));
+    const v2 ay = urotate(revperp(V(j->extra[0], j->extra[1])), qA);
+    const real sAy = cross(vadd(d, rA), ay);
+    const real sBy = cross(rB, ay);
+    const real C = dot(d, ay);
+    /* the effective mass uses sAy and sBy as InitVelocity left them */
+    const real invRotMassA = iIA * (j->s1 * j->s1);
+    const real invRotMassB = iIB * (j->s2 * j->s2);
+    const real k = iMA + iMB + invRotMassA + invRotMassB;
+    const real impulse = (k != R(0)) ? -(C / k) : R(0);
+    const v2 P = vmul(ay, impulse);
+    const real LA = impulse * sAy, LB = impulse * sBy;
+    sub_imp(&pA, iMA, P, iIA, LA);
+    add_imp(&pB, iMB, P, iIB, LB);
+    A->pos = pA; B->pos = pB;
+    return fabs(C) <= conf->linearSlop;
+}
+
+/* PulleyJointConf InitVelocity / SolveVelocity / SolvePosition
+ * (PulleyJointConf.cpp:93-241); extra = groundAnchorA.xy groundAnchorB.xy
+ * lengthA lengthB ratio. */
+static void pu_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const real ratio = j->extra[6];
+    j->rA = anchor_r(j->laA, A);
+    j->rB = anchor_r(j->laB, B);
+    const v2 pulleyAxisA = vsub(vadd(A->pos.lin, j->rA), V(j->extra[0], j->extra[1]));
+    const v2 pulleyAxisB = vsub(vadd(B->pos.lin, j->rB), V(j->extra[2], j->extra[3]));
+    j->u = unit_vector(pulleyAxisA, V(R(0), R(0)));
+    j->u2 = unit_vector(pulleyAxisB, V(R(0), R(0)));
+    const real ruA = cross(j->rA, j->u);
+    const real ruB = cross(j->rB, j->u2);
+    const real totInvMassA = iMA + (iIA * (ruA * ruA));
+    const real totInvMassB = iMB + (iIB * (ruB * ruB));
+    const real totalInvMass = totInvMassA + ratio * ratio * totInvMassB;
+    j->jmass = (totalInvMass > R(0)) ? R(1) / totalInvMass : R(0);
+    if (conf->doWarmStart) {
+        j->imp[0] *= conf->dtRatio;
+        const v2 PA = vmul(j->u, -(j->imp[0]));
+        const v2 PB = vmul(j->u2, (-ratio * j->imp[0]));
+        add_imp(&vA, iMA, PA, iIA, cross(j->rA, PA));
+        add_imp(&vB, iMB, PB, iIB, cross(j->rB, PB));
+    } else {
+        j->imp[0] = R(0);
+    }
+    A->vel = vA; B->vel = vB;
+}
+static int pu_solve_velocity(joint_t* j, bc_t* bcs) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t vA = A->vel, vB = B->vel;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const real ratio = j->extra[6];
+    const v2 vpA = point_vel(vA, j->rA);
+    const v2 vpB = point_vel(vB, j->rB);
+    const real Cdot = -dot(j->u, vpA) - ratio * dot(j->u2, vpB);
+    const real impulse = -j->jmass * Cdot;
+    j->imp[0] += impulse;
+    const v2 PA = vmul(j->u, -impulse);
+    const v2 PB = vmul(j->u2, -ratio * impulse);
+    add_imp(&vA, iMA, PA, iIA, cross(j->rA, PA));
+    add_imp(&vB, iMB, PB, iIB, cross(j->rB, PB));
+    A->vel = vA; B->vel = vB;
+    return impulse == R(0);
+}
+static int pu_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    pos_t pA = A->pos, pB = B->pos;
+    const real iMA = A->invM, iIA = A->invI, iMB = B->invM, iIB = B->invI;
+    const real ratio = j->extra[6];
+    const v2 rA = anchor_r(j->laA, A), rB = anchor_r(j->laB, B);
+    real lengthA, lengthB;
+    const v2 uA = unit_len(vsub(vadd(pA.lin, rA), V(j->extra[0], j->extra[1])), &lengthA);
+    const v2 uB = unit_len(vsub(vadd(pB.lin, rB), V(j->extra[2], j->extra[3])), &lengthB);
+    const real ruA = cross(rA, uA);
+    const real ruB = cross(rB, uB);
+    const real totalInvMassA = iMA + iIA * (ruA * ruA);
+    const real totalInvMassB = iMB + iIB * (ruB * ruB);
+    const real totalInvMass = totalInvMassA + (ratio * ratio) * totalInvMassB;
+    const real mass = (totalInvMass > R(0)) ? R(1) / totalInvMass : R(0);
+    const real srcLengthRatio = j->extra[4] + ratio * j->extra[5];
+    const real dstLengthRatio = lengthA + ratio * lengthB;
+    const real C = srcLengthRatio - dstLengthRatio;
+    const real linearError = fabs(C);
+    const real impulse = -mass * C;
+    const v2 PA = vmul(uA, -impulse);
+    const v2 PB = vmul(uB, -ratio * impulse);
+    add_imp(&pA, iMA, PA, iIA, cross(rA, PA));
+    add_imp(&pB, iMB, PB, iIB, cross(rB, PB));
+    A->pos = pA; B->pos = pB;
+    return linearError < conf->linearSlop;
+}
+
+/* TargetJointConf InitVelocity / SolveVelocity (TargetJointConf.cpp:51-184);
+ * the joint has only body B (bA == bB here); extra = target.xy maxForce
+ * frequency dampingRatio. */
+static void tj_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* B = &bcs[j->bB];
+    const pos_t posB = B->pos;
+    pos_t vB = B->vel;
+    const v2 qB = unit_from_angle(posB.ang);
+    const real iM = B->invM, iI = B->invI;
+    const real mass = (iM != R(0)) ? (R(1) / iM) : R(0);
+    const real Pi = R(3.14159265358979323846264338327950288L);
+    const real omega = R(2) * Pi * j->extra[3];
+    const real d = R(2) * mass * j->extra[4] * omega;
+    const real k = mass * (omega * omega);
+    const real h = conf->deltaTime;
+    const real tmp = d + h * k;
+    const real invGamma = h * tmp;
+    j->gamma = (invGamma != R(0)) ? R(1) / invGamma : R(0);
+    const real beta = h * k * j->gamma;
+    j->rB = rotate(vsub(j->laB, B->lc), qB);
+    {
+        /* GetEffectiveMassMatrix (TargetJointConf.cpp:51-72) */
+        const real exx = iM + (iI * (j->rB.y * j->rB.y)) + j->gamma;
+        const real exy = -iI * j->rB.x * j->rB.y;
+        const real eyy = iM + (iI * (j->rB.x * j->rB.x)) + j->gamma;
+        real K[2][2] = {{exx, exy}, {exy, eyy}};
+        mat22_invert(K, j->lm);
+    }
+    j->linErr = vmul(vsub(vadd(posB.lin, j->rB), V(j->extra[0], j->extra[1])), beta);
+    const real DampingAmount = R(0.98f);
+    vB.ang *= DampingAmount;
+    if (conf->doWarmStart) {
+        j->imp[0] *= conf->dtRatio; j->imp[1] *= conf->dtRatio;
+        const v2 P = V(j->imp[0], j->imp[1]);
+        add_imp(&vB, iM, P, iI, cross(j->rB, P));
+    } else {
+        j->imp[0] = j->imp[1] = R(0);
+    }
+    B->vel = vB;
+}
+static int tj_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* B = &bcs[j->bB];
+    pos_t vB = B->vel;
+    const v2 Cdot = point_vel(vB, j->rB);
+    const v2 ev = vadd(Cdot, vadd(j->linErr, vmul(V(j->imp[0], j->imp[1]), j->gamma)));
+    const v2 oldImpulse = V(j->imp[0], j->imp[1]);
+    const v2 addImpulse = mat22_mul(j->lm, vneg(ev));
+    v2 impulse = vadd(oldImpulse, addImpulse);
+    const real maxImpulse = conf->deltaTime * j->extra[2];
+    if (mag2(impulse) > maxImpulse * maxImpulse) impulse = vmul(unit_vector(impulse, V(R(0), R(0))), maxImpulse);
+    j->imp[0] = impulse.x; j->imp[1] = impulse.y;
+    const v2 inc = vsub(impulse, oldImpulse);
+    add_imp(&vB, B->invM, inc, B->invI, cross(j->rB, inc));
+    B->vel = vB;
+    return inc.x == R(0) && inc.y == R(0);
+}
+
 /* Joint dispatch (JointConf visitors, Joint.cpp). */
 static void joint_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
     switch (j->type) {
@@ -2109,6 +2617,10 @@ static void joint_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) 
     case OR_JOINT_WELD: weld_init_velocity(j, bcs, conf); break;
     case OR_JOINT_FRICTION: fm_init_velocity(j, bcs, conf, 0); break;
     case OR_JOINT_MOTOR: fm_init_velocity(j, bcs, conf, 1); break;
+    case OR_JOINT_PRISMATIC: pj_init_velocity(j, bcs, conf); break;
+    case OR_JOINT_WHEEL: wj_init_velocity(j, bcs, conf); break;
+    case OR_JOINT_PULLEY: pu_init_velocity(j, bcs, conf); break;
+    case OR_JOINT_TARGET: tj_init_velocity(j, bcs, conf); break;
     default: rj_init_velocity(j, bcs, conf); break;
     }
 }
@@ -2119,6 +2631,10 @@ static int joint_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) 
     case OR_JOINT_WELD: return weld_solve_velocity(j, bcs);
     case OR_JOINT_FRICTION: return friction_solve_velocity(j, bcs, conf);
     case OR_JOINT_MOTOR: return motor_solve_velocity(j, bcs, conf);
+    case OR_JOINT_PRISMATIC: return pj_solve_velocity(j, bcs, conf);
+    case OR_JOINT_WHEEL: return wj_solve_velocity(j, bcs, conf);
+    case OR_JOINT_PULLEY: return pu_solve_velocity(j, bcs);
+    case OR_JOINT_TARGET: return tj_solve_velocity(j, bcs, conf);
     default: return rj_solve_velocity(j, bcs, conf);
     }
 }
@@ -2127,7 +2643,10 @@ static int joint_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* 
     case OR_JOINT_DISTANCE: return dj_solve_position(j, bcs, conf);
     case OR_JOINT_ROPE: return rope_solve_position(j, bcs, conf);
     case OR_JOINT_WELD: return weld_solve_position(j, bcs, conf);
-    case OR_JOINT_FRICTION: case OR_JOINT_MOTOR: return 1;
+    case OR_JOINT_FRICTION: case OR_JOINT_MOTOR: case OR_JOINT_TARGET: return 1;
+    case OR_JOINT_PRISMATIC: return pj_solve_position(j, bcs, conf);
+    case OR_JOINT_WHEEL: return wj_solve_position(j, bcs, conf);
+    case OR_JOINT_PULLEY: return pu_solve_position(j, bcs, conf);
     default: return rj_solve_position(j, bcs, conf);
     }
 }

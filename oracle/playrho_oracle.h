@@ -100,11 +100,23 @@ int or_add_revolute(or_world* w, int bodyA, int bodyB, or_real lax, or_real lay,
  *   OR_JOINT_WELD      referenceAngle frequency dampingRatio (WeldJointConf)
  *   OR_JOINT_FRICTION  maxForce maxTorque                 (FrictionJointConf)
  *   OR_JOINT_MOTOR     linearOffset.x .y angularOffset maxForce maxTorque
- *                      correctionFactor (no anchors)      (MotorJointConf) */
+ *                      correctionFactor (no anchors)      (MotorJointConf)
+ *   OR_JOINT_PRISMATIC localXAxisA.x .y referenceAngle lowerTranslation
+ *                      upperTranslation motorSpeed maxMotorForce (PrismaticJointConf)
+ *   OR_JOINT_WHEEL     localXAxisA.x .y motorSpeed maxMotorTorque frequency
+ *                      dampingRatio                       (WheelJointConf)
+ *   OR_JOINT_PULLEY    groundAnchorA.x .y groundAnchorB.x .y lengthA lengthB ratio
+ *                                                         (PulleyJointConf)
+ *   OR_JOINT_TARGET    target.x .y maxForce frequency dampingRatio; bodyA == bodyB
+ *                      stands for the reference's invalid body A (TargetJointConf)
+ * The axis of a prismatic or wheel joint is normalised as UnitVec::Get does;
+ * or_joint_enable sets their enableLimit / enableMotor. */
 enum { OR_JOINT_REVOLUTE = 0, OR_JOINT_DISTANCE = 1, OR_JOINT_ROPE = 2, OR_JOINT_WELD = 3,
-       OR_JOINT_FRICTION = 4, OR_JOINT_MOTOR = 5 };
+       OR_JOINT_FRICTION = 4, OR_JOINT_MOTOR = 5, OR_JOINT_PRISMATIC = 6, OR_JOINT_WHEEL = 7,
+       OR_JOINT_PULLEY = 8, OR_JOINT_TARGET = 9 };
 int or_add_joint(or_world* w, int type, int bodyA, int bodyB, or_real lax, or_real lay, or_real lbx,
                  or_real lby, int collideConnected, const or_real* extra8);
+void or_joint_enable(or_world* w, int jid, int enableLimit, int enableMotor);
 
 void or_default_conf(or_stepconf* conf);
 void or_step(or_world* w, const or_stepconf* conf, or_stepstats* stats);

@@ -28,6 +28,10 @@
 #include <playrho/d2/WeldJointConf.hpp>
 #include <playrho/d2/FrictionJointConf.hpp>
 #include <playrho/d2/MotorJointConf.hpp>
+#include <playrho/d2/PrismaticJointConf.hpp>
+#include <playrho/d2/WheelJointConf.hpp>
+#include <playrho/d2/PulleyJointConf.hpp>
+#include <playrho/d2/TargetJointConf.hpp>
 #include <playrho/d2/Joint.hpp>
 #include <playrho/d2/DynamicTree.hpp>
 #include <playrho/StepConf.hpp>
@@ -279,10 +283,10 @@ int main()
             CreateJoint(world, Joint{j});
         }
         else if (tag == "jointx") {
-            // jointx kind bodyA bodyB lax lay lbx lby collideConnected e0..e7
+            // jointx kind bodyA bodyB lax lay lbx lby collideConnected enableLimit enableMotor e0..e7
             int kind = 0, a = 0, b = 0; in >> kind >> a >> b;
             const auto lax = rd(in), lay = rd(in), lbx = rd(in), lby = rd(in);
-            int cc = 0; in >> cc;
+            int cc = 0, el = 0, em = 0; in >> cc >> el >> em;
             Real e[8];
             for (auto& x : e) x = rd(in);
             const auto bA = BodyID(static_cast<BodyID::underlying_type>(a));
@@ -312,6 +316,31 @@ int main()
                 j.bodyA = bA; j.bodyB = bB; j.linearOffset = Length2{e[0] * 1_m, e[1] * 1_m};
                 j.angularOffset = e[2] * 1_rad; j.maxForce = e[3] * 1_N; j.maxTorque = e[4] * 1_Nm;
                 j.correctionFactor = e[5]; j.collideConnected = cc != 0;
+                CreateJoint(world, Joint{j});
+            } else if (kind == 6) {
+                const auto axis = std::get<UnitVec>(UnitVec::Get(e[0], e[1]));
+                auto j = PrismaticJointConf{bA, bB, laA, laB, axis, e[2] * 1_rad};
+                j.enableLimit = el != 0; j.lowerTranslation = e[3] * 1_m; j.upperTranslation = e[4] * 1_m;
+                j.enableMotor = em != 0; j.motorSpeed = e[5] * 1_rad / 1_s; j.maxMotorForce = e[6] * 1_N;
+                j.collideConnected = cc != 0;
+                CreateJoint(world, Joint{j});
+            } else if (kind == 7) {
+                const auto axis = std::get<UnitVec>(UnitVec::Get(e[0], e[1]));
+                auto j = WheelJointConf{bA, bB, laA, laB, axis};
+                j.enableMotor = em != 0; j.motorSpeed = e[2] * 1_rad / 1_s; j.maxMotorTorque = e[3] * 1_Nm;
+                j.frequency = e[4] * 1_Hz; j.dampingRatio = e[5]; j.collideConnected = cc != 0;
+                CreateJoint(world, Joint{j});
+            } else if (kind == 8) {
+                auto j = PulleyJointConf{bA, bB, Length2{e[0] * 1_m, e[1] * 1_m}, Length2{e[2] * 1_m, e[3] * 1_m},
+                                         laA, laB, e[4] * 1_m, e[5] * 1_m};
+                j.ratio = e[6]; j.collideConnected = cc != 0;
+                CreateJoint(world, Joint{j});
+            } else if (kind == 9) {
+                // the target joint has body B only (its body A is InvalidBodyID)
+                auto j = TargetJointConf{bB};
+                j.localAnchorB = laB; j.target = Length2{e[0] * 1_m, e[1] * 1_m};
+                j.maxForce = e[2] * 1_N; j.frequency = e[3] * 1_Hz; j.dampingRatio = e[4];
+                j.collideConnected = cc != 0;
                 CreateJoint(world, Joint{j});
             }
         }

@@ -26,6 +26,7 @@ STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 DISK, POLYGON, EDGE = 0, 1, 2
 # Joint kinds (the reference's JointConf types) and their parameters in joint_extra.
 JOINT_REVOLUTE, JOINT_DISTANCE, JOINT_ROPE, JOINT_WELD, JOINT_FRICTION, JOINT_MOTOR = 0, 1, 2, 3, 4, 5
+JOINT_PRISMATIC, JOINT_WHEEL, JOINT_PULLEY, JOINT_TARGET = 6, 7, 8, 9
 JOINT_PARAMS = {
     JOINT_DISTANCE: ("length", "frequency", "damping_ratio"),
     JOINT_ROPE: ("max_length",),
@@ -33,6 +34,18 @@ JOINT_PARAMS = {
     JOINT_FRICTION: ("max_force", "max_torque"),
     JOINT_MOTOR: ("linear_offset_x", "linear_offset_y", "angular_offset", "max_force", "max_torque",
                   "correction_factor"),
+    JOINT_PRISMATIC: ("axis_x", "axis_y", "reference_angle", "lower", "upper", "motor_speed", "max_motor_force"),
+    JOINT_WHEEL: ("axis_x", "axis_y", "motor_speed", "max_motor_torque", "frequency", "damping_ratio"),
+    JOINT_PULLEY: ("ground_a_x", "ground_a_y", "ground_b_x", "ground_b_y", "length_a", "length_b", "ratio"),
+    JOINT_TARGET: ("target_x", "target_y", "max_force", "frequency", "damping_ratio"),
+}
+# Parameter defaults of the reference's JointConf types where they are not zero.
+JOINT_DEFAULTS = {
+    JOINT_MOTOR: {"correction_factor": 0.2},                               # MotorJointConf.hpp
+    JOINT_PRISMATIC: {"axis_x": 1.0},                                      # UnitVec::GetRight()
+    JOINT_WHEEL: {"axis_x": 1.0, "frequency": 2.0, "damping_ratio": 0.7},  # WheelJointConf.hpp:76-79
+    JOINT_PULLEY: {"ratio": 1.0},                                          # PulleyJointConf.hpp:126
+    JOINT_TARGET: {"frequency": 5.0, "damping_ratio": 0.7},                # TargetJointConf.hpp:63-69
 }
 # Body flags (BodyConf booleans): allowSleep, awake, fixedRotation, enabled, bullet.
 BF_ALLOW_SLEEP, BF_AWAKE, BF_FIXED_ROTATION, BF_ENABLED, BF_BULLET = 1, 2, 4, 8, 16
@@ -173,19 +186,23 @@ class SceneBuilder:
         self.j_extra.append((0.0,) * 8)
         return len(self.j_bodies) - 1
 
-    def joint(self, kind, a, b, anchor_a=(0.0, 0.0), anchor_b=(0.0, 0.0), collide_connected=False, **params):
-        """A joint of another kind (JOINT_*) with its parameters by name (JOINT_PARAMS)."""
+    def joint(self, kind, a, b, anchor_a=(0.0, 0.0), anchor_b=(0.0, 0.0), collide_connected=False,
+              enable_limit=False, enable_motor=False, **params):
+        """A joint of another kind (JOINT_*) with its parameters by name (JOINT_PARAMS);
+        enable_limit / enable_motor for prismatic and wheel joints.  A target joint
+        has body b only: pass a=None (it is stored as a == b)."""
         names = JOINT_PARAMS[kind]
         unknown = set(params) - set(names)
         if unknown:
             raise ValueError(f"unknown parameters {sorted(unknown)} for joint kind {kind}")
-        extra = [float(params.get(n, 0.0)) for n in names] + [0.0] * (8 - len(names))
-        if kind == JOINT_MOTOR and "correction_factor" not in params:
-            extra[5] = 0.2  # MotorJointConf::correctionFactor default
+        defaults = JOINT_DEFAULTS.get(kind, {})
+        extra = [float(params.get(n, defaults.get(n, 0.0))) for n in names] + [0.0] * (8 - len(names))
+        if kind == JOINT_TARGET:
+            a = b
         self.j_bodies.append((a, b))
         self.j_anchor.append((anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1]))
         self.j_params.append((0.0,) * 6)
-        self.j_flags.append((0, 0, 1 if collide_connected else 0))
+        self.j_flags.append((1 if enable_limit else 0, 1 if enable_motor else 0, 1 if collide_connected else 0))
         self.j_type.append(int(kind))
         self.j_extra.append(tuple(extra))
         return len(self.j_bodies) - 1
@@ -517,9 +534,12 @@ def bullets(n_bodies: int, rng, size: float = 20.0, speed=(60.0, 180.0), bullet_
 def joint_zoo(rng, per_kind: int = 4, kinds=None, n_disks: int = 12, gravity: bool = True) -> Scene:
     """Mechanisms of every joint kind side by side above a ground edge: a static
     anchor holding a dynamic box by a distance (stiff and soft), rope, weld (rigid
-    and soft), friction or motor joint, with disks dropped on them."""
+    and soft), friction, motor or prismatic joint (limit, motor or both), a wheel
+    on a suspension (sprung or rigid, motor on or off), two boxes on a pulley and
+    a box pulled to a target point, with disks dropped on them."""
     kinds = list(kinds) if kinds is not None else [JOINT_DISTANCE, JOINT_ROPE, JOINT_WELD, JOINT_FRICTION,
-                                                     JOINT_MOTOR]
+                                                     JOINT_MOTOR, JOINT_PRISMATIC, JOINT_WHEEL, JOINT_PULLEY,
+                                                     JOINT_TARGET]
     acc = GRAVITY if gravity else (0.0, 0.0, 0.0)
     sb = SceneBuilder()
     g = sb.body(STATIC, 0.0, 0.0)
@@ -532,10 +552,16 @@ def joint_zoo(rng, per_kind: int = 4, kinds=None, n_disks: int = 12, gravity: bo
             anchor = sb.body(STATIC, x, 8.0)
             hx, hy = float(rng.uniform(0.2, 0.6)), float(rng.uniform(0.2, 0.6))
             by = 8.0 - float(rng.uniform(1.0, 3.0))
-            b = sb.body(DYNAMIC, x + float(rng.uniform(-1.5, 1.5)), by, angle=float(rng.uniform(-1, 1)),
+            bx, ba = x + float(rng.uniform(-1.5, 1.5)), float(rng.uniform(-1, 1))
+            if kind == JOINT_PULLEY:
+                bx, ba = x - 1.0, 0.5 * ba
+            b = sb.body(DYNAMIC, bx, by, angle=ba,
                         v=(float(rng.normal(0, 2)), float(rng.normal(0, 2)), float(rng.normal(0, 1))), acc=acc)
-            sb.box(b, hx, hy, density=1.0, friction=0.5)
             soft = k % 2 == 1
+            if kind == JOINT_WHEEL:
+                sb.disk(b, hx, density=1.0, friction=0.5)
+            else:
+                sb.box(b, hx, hy, density=1.0, friction=0.5)
             if kind == JOINT_DISTANCE:
                 sb.joint(kind, anchor, b, (0.0, 0.0), (hx * 0.5, 0.0), length=float(rng.uniform(1.0, 3.0)),
                          frequency=2.0 if soft else 0.0, damping_ratio=0.3 if soft else 0.0)
@@ -552,6 +578,31 @@ def joint_zoo(rng, per_kind: int = 4, kinds=None, n_disks: int = 12, gravity: bo
                          linear_offset_y=float(rng.uniform(-3, -1)), angular_offset=float(rng.uniform(-1, 1)),
                          max_force=float(rng.uniform(20.0, 200.0)), max_torque=float(rng.uniform(5.0, 50.0)),
                          correction_factor=0.3)
+            elif kind == JOINT_PRISMATIC:
+                t = float(rng.uniform(0.0, math.pi))
+                sb.joint(kind, anchor, b, (bx - x, by - 8.0), (0.0, 0.0), enable_limit=k % 3 != 1,
+                         enable_motor=k % 3 != 0, axis_x=math.cos(t), axis_y=math.sin(t), reference_angle=ba,
+                         lower=-1.0, upper=float(rng.uniform(0.5, 1.5)), motor_speed=float(rng.uniform(-2, 2)),
+                         max_motor_force=float(rng.uniform(10.0, 100.0)))
+            elif kind == JOINT_WHEEL:
+                sb.joint(kind, anchor, b, (bx - x, by - 8.0), (0.0, 0.0), enable_motor=soft,
+                         axis_x=float(rng.uniform(-0.3, 0.3)), axis_y=1.0, motor_speed=float(rng.uniform(-5, 5)),
+                         max_motor_torque=float(rng.uniform(1.0, 10.0)), frequency=0.0 if k % 3 == 2 else 4.0,
+                         damping_ratio=0.7)
+            elif kind == JOINT_PULLEY:
+                b2y = 8.0 - float(rng.uniform(1.0, 3.0))
+                b2 = sb.body(DYNAMIC, x + 1.0, b2y, acc=acc)
+                sb.box(b2, hy, hx, density=1.0, friction=0.5)
+                ga, gb = (x - 1.0, 10.0), (x + 1.0, 10.0)
+                wa = (bx - math.sin(ba) * hy, by + math.cos(ba) * hy)  # body b's anchor (0, hy) in the world
+                sb.joint(kind, b, b2, (0.0, hy), (0.0, hx), collide_connected=True, ground_a_x=ga[0],
+                         ground_a_y=ga[1], ground_b_x=gb[0], ground_b_y=gb[1],
+                         length_a=math.hypot(wa[0] - ga[0], wa[1] - ga[1]), length_b=10.0 - (b2y + hx),
+                         ratio=1.5 if soft else 1.0)
+            elif kind == JOINT_TARGET:
+                sb.joint(kind, None, b, anchor_b=(0.5 * hx, 0.0), target_x=x + float(rng.uniform(-1, 1)),
+                         target_y=float(rng.uniform(4.0, 7.0)), max_force=float(rng.uniform(20.0, 200.0)),
+                         frequency=5.0 if soft else 2.0, damping_ratio=0.7)
     for _ in range(n_disks):
         d = sb.body(DYNAMIC, float(rng.uniform(-width / 2, width / 2)), float(rng.uniform(10.0, 16.0)), acc=acc)
         sb.disk(d, float(rng.uniform(0.2, 0.5)), density=1.0, friction=0.3)
@@ -673,8 +724,8 @@ def scene_text(scene: Scene, conf_overrides: dict | None = None) -> str:
         fl = scene.joint_flags[j]
         kind = int(scene.joint_type[j])
         if kind != JOINT_REVOLUTE:
-            out.append("jointx %d %d %d %s %d %s" % (kind, a, b, " ".join(hx(x) for x in an), fl[2],
-                                                     " ".join(hx(x) for x in scene.joint_extra[j])))
+            out.append("jointx %d %d %d %s %d %d %d %s" % (kind, a, b, " ".join(hx(x) for x in an), fl[2], fl[0],
+                                                           fl[1], " ".join(hx(x) for x in scene.joint_extra[j])))
             continue
         out.append("joint %d %d %s %d %s %s %d %s %s %d" % (
             a, b, " ".join(hx(x) for x in (*an, pr[0])), fl[0], hx(pr[1]), hx(pr[2]), fl[1],

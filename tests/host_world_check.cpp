@@ -78,7 +78,8 @@ int main() {
                 HostJoint j;
                 uint32_t a, b;
                 std::string an[4], e[8];
-                in >> j.kind >> a >> b >> an[0] >> an[1] >> an[2] >> an[3] >> j.collide_connected;
+                in >> j.kind >> a >> b >> an[0] >> an[1] >> an[2] >> an[3] >> j.collide_connected >> j.enable_limit >>
+                    j.enable_motor;
                 for (auto& x : e) in >> x;
                 j.body_a = body_ids.at(a); j.body_b = body_ids.at(b);
                 j.anchor_a[0] = hexf(an[0]); j.anchor_a[1] = hexf(an[1]);

@@ -54,9 +54,10 @@ def test_toi_pile_f64():
     _compare(scenes.pile(120, np.random.default_rng(23)), [1, 100, 150], double=True, doToi=1)
 
 
-@pytest.mark.parametrize("kind", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("kind", [1, 2, 3, 4, 5, 6, 7, 8, 9])
 def test_joint_kinds(kind):
-    # distance, rope, weld, friction and motor joints (stiff and soft), with contacts
+    # distance, rope, weld, friction, motor, prismatic, wheel, pulley and target joints
+    # (stiff and soft, limits and motors on and off), with contacts
     _compare(scenes.joint_zoo(np.random.default_rng(30 + kind), per_kind=4, kinds=[kind], n_disks=6), [1, 30, 120])
 
 
