@@ -141,10 +141,21 @@ typedef struct prgpu_batch_desc {
  *   WELD       WeldJointConf:     referenceAngle frequency dampingRatio
  *   FRICTION   FrictionJointConf: maxForce maxTorque
  *   MOTOR      MotorJointConf:    linearOffset.x linearOffset.y angularOffset maxForce maxTorque
- *                                 correctionFactor (anchors unused) */
+ *                                 correctionFactor (anchors unused)
+ *   PRISMATIC  PrismaticJointConf: localXAxisA.x .y referenceAngle lowerTranslation
+ *                                 upperTranslation motorSpeed maxMotorForce; joint_flags[0]
+ *                                 enableLimit, joint_flags[1] enableMotor
+ *   WHEEL      WheelJointConf:    localXAxisA.x .y motorSpeed maxMotorTorque frequency
+ *                                 dampingRatio; joint_flags[1] enableMotor
+ *   PULLEY     PulleyJointConf:   groundAnchorA.x .y groundAnchorB.x .y lengthA lengthB ratio
+ *   TARGET     TargetJointConf:   target.x .y maxForce frequency dampingRatio; the joint has
+ *                                 body B only: joint_bodies gives it twice (localAnchorA unused)
+ * The axis of a prismatic or wheel joint is normalised as UnitVec::Get does.
+ * GearJointConf (four bodies, two other joints) is not stepped. */
 enum prgpu_joint_kind {
     PRGPU_JOINT_REVOLUTE = 0, PRGPU_JOINT_DISTANCE = 1, PRGPU_JOINT_ROPE = 2, PRGPU_JOINT_WELD = 3,
-    PRGPU_JOINT_FRICTION = 4, PRGPU_JOINT_MOTOR = 5
+    PRGPU_JOINT_FRICTION = 4, PRGPU_JOINT_MOTOR = 5, PRGPU_JOINT_PRISMATIC = 6, PRGPU_JOINT_WHEEL = 7,
+    PRGPU_JOINT_PULLEY = 8, PRGPU_JOINT_TARGET = 9
 };
 
 int prgpu_abi_version(void);

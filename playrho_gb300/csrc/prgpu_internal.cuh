@@ -266,6 +266,7 @@ struct DW {
     float4* j_r;             // rA.xy rB.xy
     float4* j_m0;            // mass ex.x ex.y ex.z ey.y
     float4* j_m1;            // ey.z ez.z angularMass motorImpulse
+    float4* j_m2;            // the other kinds' further solver state
     float4* j_imp;           // impulse xyz, limitState
     // contacts (slot storage)
     uint64_t* c_key;         // sorted live keys

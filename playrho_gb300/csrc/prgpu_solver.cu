@@ -601,7 +601,14 @@ __device__ bool revolute_solve_position(const DW& d, const BS& bs, uint32_t j) {
 //   weld:           m0 = mass00 mass01 mass02 mass11, m1 = mass12 mass22 gamma bias, imp.xyz
 //   friction:       m0 = linearMass00 01 11 angularMass, imp = linear xy, angular z
 //   motor:          friction's, and m1 = linearError xy, angularError
-enum : uint32_t { JK_REVOLUTE = 0, JK_DISTANCE = 1, JK_ROPE = 2, JK_WELD = 3, JK_FRICTION = 4, JK_MOTOR = 5 };
+//   prismatic:      r = axis perp, m0 = a1 a2 s1 s2, m1 = K11 K12 K13 K22,
+//                   m2 = K23 K33 motorMass motorImpulse, imp.xyz, limitState
+//   wheel:          r = ax ay, m0 = sAx sBx sAy sBy, m1 = mass springMass bias gamma,
+//                   m2.x = angularMass, imp = impulse springImpulse angularImpulse
+//   pulley:         r = rA rB, m0 = uA uB, m1.x = mass, imp.x
+//   target:         r.zw = rB, m0 = mass22 (00 01 11) gamma, m1.xy = C, imp.xy
+enum : uint32_t { JK_REVOLUTE = 0, JK_DISTANCE = 1, JK_ROPE = 2, JK_WELD = 3, JK_FRICTION = 4, JK_MOTOR = 5,
+                  JK_PRISMATIC = 6, JK_WHEEL = 7, JK_PULLEY = 8, JK_TARGET = 9 };
 __device__ __forceinline__ uint32_t joint_kind(const DW& d, uint32_t j) { return (d.j_flags[j] >> 8) & 0xffu; }
 
 // UnitVec::Get(x, y) (UnitVec.hpp:175-235): direction and magnitude.
@@ -1044,6 +1051,534 @@ __device__ void friction_solve_velocity(const DW& d, const BS& bs, uint32_t j, b
     if (bs.writable(b)) bs.set_vel(b, vB);
 }
 
+// Whether a velocity or position changed (Velocity / Position operator!=).
+__device__ __forceinline__ bool state_ne(float4 a, float4 b) { return !(a.x == b.x && a.y == b.y && a.z == b.z); }
+
+// PrismaticJointConf (PrismaticJointConf.cpp:95-449); extra = localXAxisA.xy
+// referenceAngle lowerTranslation upperTranslation motorSpeed maxMotorForce.
+template <class BS>
+__device__ void prismatic_init_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    const float4 pA = bs.pos(a), pB = bs.pos(b);
+    float4 vA = bs.vel(a), vB = bs.vel(b);
+    const float4 an = d.j_anchor[j], e0 = d.j_extra[2 * j], e1 = d.j_extra[2 * j + 1];
+    const uint32_t jf = d.j_flags[j];
+    const V2 qA = unit_from_angle(pA.z);
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    const V2 dd = ((mk(pB.x, pB.y) - mk(pA.x, pA.y)) + rB) - rA;
+    const V2 xaxis = mk(e0.x, e0.y);
+    const V2 axis = urotate(xaxis, qA);
+    const float a1 = cross(dd + rA, axis), a2 = cross(rB, axis);
+    const float invRotMassA = iIA * (a1 * a1), invRotMassB = iIB * (a2 * a2);
+    const float totalInvMass = iMA + iMB + invRotMassA + invRotMassB;
+    const float motorMass = (totalInvMass > 0.f) ? 1.0f / totalInvMass : 0.f;
+    const V2 perp = urotate(revperp(xaxis), qA);
+    const float s1 = cross(dd + rA, perp), s2 = cross(rB, perp);
+    const float invRotMassA2 = iIA * (s1 * s1), invRotMassB2 = iIB * (s2 * s2);
+    const float k11 = iMA + iMB + invRotMassA2 + invRotMassB2;
+    const float k12 = iIA * s1 + iIB * s2;
+    const float k13 = iIA * s1 * a1 + iIB * s2 * a2;
+    const float totalInvRotInertia = iIA + iIB;
+    const float k22 = (totalInvRotInertia == 0.f) ? 1.0f : totalInvRotInertia;
+    const float k23 = iIA * a1 + iIB * a2;
+    const float k33 = totalInvMass;
+    float4 imp = d.j_imp[j];
+    float motorImpulse = d.j_m2[j].w;
+    int limitState = (int)imp.w;
+    const float lower = e0.w, upper = e1.x;
+    if (jf & 1u) {
+        const float jointTranslation = dot(axis, dd);
+        if (fabsf(upper - lower) < (c.linearSlop * 2.0f)) limitState = 3;
+        else if (jointTranslation <= lower) { if (limitState != 1) { limitState = 1; imp.z = 0.f; } }
+        else if (jointTranslation >= upper) { if (limitState != 2) { limitState = 2; imp.z = 0.f; } }
+        else { limitState = 0; imp.z = 0.f; }
+    } else {
+        limitState = 0;
+        imp.z = 0.f;
+    }
+    if (!(jf & 2u)) motorImpulse = 0.f;
+    if (c.doWarmStart) {
+        imp.x *= c.dtRatio; imp.y *= c.dtRatio; imp.z *= c.dtRatio;
+        motorImpulse *= c.dtRatio;
+        const V2 Px = perp * imp.x;
+        const float Pxs1 = imp.x * s1, Pxs2 = imp.x * s2;
+        const float PzLength = motorImpulse + imp.z;
+        const V2 P = Px + axis * PzLength;
+        const float L = imp.y;
+        const float LA = L + (Pxs1 + PzLength * a1);
+        const float LB = L + (Pxs2 + PzLength * a2);
+        sub_imp(vA, iMA, P, iIA, LA);
+        add_imp(vB, iMB, P, iIB, LB);
+    } else {
+        imp.x = imp.y = imp.z = 0.f;
+        motorImpulse = 0.f;
+    }
+    imp.w = (float)limitState;
+    d.j_imp[j] = imp;
+    d.j_r[j] = make_float4(axis.x, axis.y, perp.x, perp.y);
+    d.j_m0[j] = make_float4(a1, a2, s1, s2);
+    d.j_m1[j] = make_float4(k11, k12, k13, k22);
+    d.j_m2[j] = make_float4(k23, k33, motorMass, motorImpulse);
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ void prismatic_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    const float4 oldA = bs.vel(a), oldB = bs.vel(b);
+    float4 vA = oldA, vB = oldB;
+    const float4 r = d.j_r[j], m0 = d.j_m0[j], m1 = d.j_m1[j], e1 = d.j_extra[2 * j + 1];
+    float4 m2 = d.j_m2[j];
+    float4 imp = d.j_imp[j];
+    const uint32_t jf = d.j_flags[j];
+    const int limitState = (int)imp.w;
+    const V2 axis = mk(r.x, r.y), perp = mk(r.z, r.w);
+    const float a1 = m0.x, a2 = m0.y, s1 = m0.z, s2 = m0.w;
+    if ((jf & 2u) && limitState != 3) {
+        const float vDot = dot(axis, mk(vB.x, vB.y) - mk(vA.x, vA.y));
+        const float Cdot = vDot + (a2 * vB.z - a1 * vA.z);
+        float impulse = m2.z * (e1.y - Cdot);
+        const float oldImpulse = m2.w;
+        const float maxImpulse = c.deltaTime * e1.z;
+        m2.w = clampf_(m2.w + impulse, -maxImpulse, maxImpulse);
+        impulse = m2.w - oldImpulse;
+        const V2 P = axis * impulse;
+        sub_imp(vA, iMA, P, iIA, impulse * a1);
+        add_imp(vB, iMB, P, iIB, impulse * a2);
+        d.j_m2[j] = m2;
+    }
+    float K[3][3] = {{m1.x, m1.y, m1.z}, {m1.y, m1.w, m2.x}, {m1.z, m2.x, m2.y}};
+    const V2 velDelta = mk(vB.x, vB.y) - mk(vA.x, vA.y);
+    const float sRotSpeed = s2 * vB.z - s1 * vA.z;
+    const V2 Cdot1 = mk(dot(perp, velDelta) + sRotSpeed, vB.z - vA.z);
+    if ((jf & 1u) && limitState != 0) {
+        const float deltaDot = dot(axis, velDelta);
+        const float aRotSpeed = a2 * vB.z - a1 * vA.z;
+        const float Cdot2 = deltaDot + aRotSpeed;
+        const float negCdot[3] = {-Cdot1.x, -Cdot1.y, -Cdot2};
+        const float4 f1 = imp;
+        float add[3];
+        solve33(K, negCdot, add);
+        imp.x += add[0]; imp.y += add[1]; imp.z += add[2];
+        if (limitState == 1) imp.z = maxf_(imp.z, 0.f);
+        else if (limitState == 2) imp.z = minf_(imp.z, 0.f);
+        const float dz = imp.z - f1.z;
+        const V2 bb = mk(-Cdot1.x - dz * K[2][0], -Cdot1.y - dz * K[2][1]);
+        const V2 s22 = solve22k(K, bb);
+        imp.x = s22.x + f1.x; imp.y = s22.y + f1.y;
+        const float dx = imp.x - f1.x, dy = imp.y - f1.y, dzz = imp.z - f1.z;
+        const V2 P = perp * dx + axis * dzz;
+        const float LA = dx * s1 + dy + dzz * a1;
+        const float LB = dx * s2 + dy + dzz * a2;
+        sub_imp(vA, iMA, P, iIA, LA);
+        add_imp(vB, iMB, P, iIB, LB);
+    } else {
+        const V2 df = solve22k(K, -Cdot1);
+        imp.x += df.x; imp.y += df.y;
+        const V2 P = perp * df.x;
+        sub_imp(vA, iMA, P, iIA, df.x * s1 + df.y);
+        add_imp(vB, iMB, P, iIB, df.x * s2 + df.y);
+    }
+    d.j_imp[j] = imp;
+    if (state_ne(vA, oldA) || state_ne(vB, oldB)) {
+        if (bs.writable(a)) bs.set_vel(a, vA);
+        if (bs.writable(b)) bs.set_vel(b, vB);
+    }
+}
+
+template <class BS>
+__device__ bool prismatic_solve_position(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    float4 pA = bs.pos(a), pB = bs.pos(b);
+    const float4 an = d.j_anchor[j], e0 = d.j_extra[2 * j], e1 = d.j_extra[2 * j + 1];
+    const V2 qA = unit_from_angle(pA.z);
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    const V2 dd = (mk(pB.x, pB.y) + rB) - (mk(pA.x, pA.y) + rA);
+    const V2 xaxis = mk(e0.x, e0.y);
+    const V2 axis = urotate(xaxis, qA);
+    const float a1 = cross(dd + rA, axis), a2 = cross(rB, axis);
+    const V2 perp = urotate(revperp(xaxis), qA);
+    const float s1 = cross(dd + rA, perp), s2 = cross(rB, perp);
+    const V2 C1 = mk(dot(perp, dd), pB.z - pA.z - e0.z);
+    float linearError = fabsf(C1.x);
+    const float angularError = fabsf(C1.y);
+    bool active = false;
+    float C2 = 0.f;
+    const float lower = e0.w, upper = e1.x;
+    if (d.j_flags[j] & 1u) {
+        const float translation = dot(axis, dd);
+        if (fabsf(upper - lower) < (2.0f * c.linearSlop)) {
+            C2 = clampf_(translation, -c.maxLinearCorrection, c.maxLinearCorrection);
+            linearError = maxf_(linearError, fabsf(translation));
+            active = true;
+        } else if (translation <= lower) {
+            C2 = clampf_(translation - lower + c.linearSlop, -c.maxLinearCorrection, 0.f);
+            linearError = maxf_(linearError, lower - translation);
+            active = true;
+        } else if (translation >= upper) {
+            C2 = clampf_(translation - upper - c.linearSlop, 0.f, c.maxLinearCorrection);
+            linearError = maxf_(linearError, translation - upper);
+            active = true;
+        }
+    }
+    float impulse[3];
+    if (active) {
+        const float k11 = iMA + iIA * (s1 * s1) + iMB + iIB * (s2 * s2);
+        const float k12 = iIA * s1 + iIB * s2;
+        const float k13 = iIA * s1 * a1 + iIB * s2 * a2;
+        float k22 = iIA + iIB;
+        if (k22 == 0.f) k22 = 1.0f;
+        const float k23 = iIA * a1 + iIB * a2;
+        const float k33 = iMA + iIA * (a1 * a1) + iMB + iIB * (a2 * a2);
+        const float K[3][3] = {{k11, k12, k13}, {k12, k22, k23}, {k13, k23, k33}};
+        const float negC[3] = {-C1.x, -C1.y, -C2};
+        solve33(K, negC, impulse);
+    } else {
+        const float k11 = iMA + iIA * s1 * s1 + iMB + iIB * s2 * s2;
+        const float k12 = iIA * s1 + iIB * s2;
+        float k22 = iIA + iIB;
+        if (k22 == 0.f) k22 = 1.0f;
+        // Solve(Matrix22, Vector2) (Math.hpp:412-425)
+        const V2 bneg = -C1;
+        const float cp = cross(mk(k11, k12), mk(k12, k22));
+        impulse[0] = impulse[1] = impulse[2] = 0.f;
+        if (!almost_zero(cp)) {
+            const float inverse = 1.0f / cp;
+            impulse[0] = (k22 * bneg.x - k12 * bneg.y) * inverse;
+            impulse[1] = (k11 * bneg.y - k12 * bneg.x) * inverse;
+        }
+    }
+    const V2 P = perp * impulse[0] + axis * impulse[2];
+    const float LA = impulse[0] * s1 + impulse[1] + impulse[2] * a1;
+    const float LB = impulse[0] * s2 + impulse[1] + impulse[2] * a2;
+    sub_imp(pA, iMA, P, iIA, LA);
+    add_imp(pB, iMB, P, iIB, LB);
+    if (bs.writable(a)) bs.set_pos(a, pA);
+    if (bs.writable(b)) bs.set_pos(b, pB);
+    return (linearError <= c.linearSlop) && (angularError <= c.angularSlop);
+}
+
+// WheelJointConf (WheelJointConf.cpp:80-311); extra = localXAxisA.xy motorSpeed
+// maxMotorTorque frequency dampingRatio.
+template <class BS>
+__device__ void wheel_init_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    const float4 pA = bs.pos(a), pB = bs.pos(b);
+    float4 vA = bs.vel(a), vB = bs.vel(b);
+    const float4 an = d.j_anchor[j], e0 = d.j_extra[2 * j], e1 = d.j_extra[2 * j + 1];
+    const V2 qA = unit_from_angle(pA.z);
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    const V2 dd = (mk(pB.x, pB.y) + rB) - (mk(pA.x, pA.y) + rA);
+    const V2 xaxis = mk(e0.x, e0.y);
+    const V2 ay = urotate(revperp(xaxis), qA);
+    const float sAy = cross(dd + rA, ay), sBy = cross(rB, ay);
+    float mass;
+    {
+        const float invMass = iMA + iMB + iIA * (sAy * sAy) + iIB * (sBy * sBy);
+        mass = (invMass > 0.f) ? 1.0f / invMass : 0.f;
+    }
+    float4 imp = d.j_imp[j];  // impulse springImpulse angularImpulse
+    float springMass = 0.f, bias = 0.f, gamma = 0.f;
+    V2 ax = mk(0.f, 0.f);
+    float sAx = 0.f, sBx = 0.f;
+    const float frequency = e1.x, dampingRatio = e1.y;
+    if (frequency > 0.f) {
+        ax = urotate(xaxis, qA);
+        sAx = cross(dd + rA, ax);
+        sBx = cross(rB, ax);
+        const float invMass = iMA + iMB + iIA * (sAx * sAx) + iIB * (sBx * sBx);
+        if (invMass > 0.f) {
+            springMass = 1.0f / invMass;
+            const float C = dot(dd, ax);
+            const float Pi = 3.14159265358979323846264338327950288f;
+            const float omega = 2.0f * Pi * frequency;
+            const float dc = 2.0f * springMass * dampingRatio * omega;
+            const float k = springMass * omega * omega;
+            const float h = c.deltaTime;
+            const float invGamma = h * (dc + h * k);
+            gamma = (invGamma > 0.f) ? 1.0f / invGamma : 0.f;
+            bias = C * h * k * gamma;
+            const float totalInvMass = invMass + gamma;
+            springMass = (totalInvMass > 0.f) ? 1.0f / totalInvMass : 0.f;
+        }
+    } else {
+        imp.y = 0.f;
+    }
+    float angularMass = 0.f;
+    if (d.j_flags[j] & 2u) {
+        const float invRotInertia = iIA + iIB;
+        angularMass = (invRotInertia > 0.f) ? 1.0f / invRotInertia : 0.f;
+    } else {
+        imp.z = 0.f;
+    }
+    if (c.doWarmStart) {
+        imp.x *= c.dtRatio; imp.y *= c.dtRatio; imp.z *= c.dtRatio;
+        const V2 P = ay * imp.x + ax * imp.y;
+        const float LA = (imp.x * sAy + imp.y * sAx) + imp.z;
+        const float LB = (imp.x * sBy + imp.y * sBx) + imp.z;
+        sub_imp(vA, iMA, P, iIA, LA);
+        add_imp(vB, iMB, P, iIB, LB);
+    } else {
+        imp.x = imp.y = imp.z = 0.f;
+    }
+    d.j_imp[j] = imp;
+    d.j_r[j] = make_float4(ax.x, ax.y, ay.x, ay.y);
+    d.j_m0[j] = make_float4(sAx, sBx, sAy, sBy);
+    d.j_m1[j] = make_float4(mass, springMass, bias, gamma);
+    d.j_m2[j] = make_float4(angularMass, 0.f, 0.f, 0.f);
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ void wheel_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    const float4 oldA = bs.vel(a), oldB = bs.vel(b);
+    float4 vA = oldA, vB = oldB;
+    const float4 r = d.j_r[j], m0 = d.j_m0[j], m1 = d.j_m1[j], e0 = d.j_extra[2 * j];
+    const float angularMass = d.j_m2[j].x;
+    float4 imp = d.j_imp[j];
+    const V2 ax = mk(r.x, r.y), ay = mk(r.z, r.w);
+    const float sAx = m0.x, sBx = m0.y, sAy = m0.z, sBy = m0.w;
+    {
+        const float dv = dot(ax, mk(vB.x, vB.y) - mk(vA.x, vA.y));
+        const float Cdot = dv + sBx * vB.z - sAx * vA.z;
+        const float impulse = -m1.y * (Cdot + m1.z + m1.w * imp.y);
+        imp.y += impulse;
+        const V2 P = ax * impulse;
+        sub_imp(vA, iMA, P, iIA, impulse * sAx);
+        add_imp(vB, iMB, P, iIB, impulse * sBx);
+    }
+    {
+        const float Cdot = vB.z - vA.z - e0.z;
+        float impulse = -angularMass * Cdot;
+        const float oldImpulse = imp.z;
+        const float maxImpulse = c.deltaTime * e0.w;
+        imp.z = clampf_(imp.z + impulse, -maxImpulse, maxImpulse);
+        impulse = imp.z - oldImpulse;
+        vA.z -= iIA * impulse;
+        vB.z += iIB * impulse;
+    }
+    {
+        const float dv = dot(ay, mk(vB.x, vB.y) - mk(vA.x, vA.y));
+        const float Cdot = dv + sBy * vB.z - sAy * vA.z;
+        const float impulse = -m1.x * Cdot;
+        imp.x += impulse;
+        const V2 P = ay * impulse;
+        sub_imp(vA, iMA, P, iIA, impulse * sAy);
+        add_imp(vB, iMB, P, iIB, impulse * sBy);
+    }
+    d.j_imp[j] = imp;
+    if (state_ne(vA, oldA) || state_ne(vB, oldB)) {
+        if (bs.writable(a)) bs.set_vel(a, vA);
+        if (bs.writable(b)) bs.set_vel(b, vB);
+    }
+}
+
+template <class BS>
+__device__ bool wheel_solve_position(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    float4 pA = bs.pos(a), pB = bs.pos(b);
+    const float4 an = d.j_anchor[j], e0 = d.j_extra[2 * j], m0 = d.j_m0[j];
+    const V2 qA = unit_from_angle(pA.z);
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    const V2 dd = (mk(pB.x, pB.y) - mk(pA.x, pA.y)) + (rB - rA);
+    const V2 ay = urotate(revperp(mk(e0.x, e0.y)), qA);
+    const float sAy = cross(dd + rA, ay), sBy = cross(rB, ay);
+    const float C = dot(dd, ay);
+    // the effective mass uses sAy and sBy as InitVelocity left them
+    const float k = iMA + iMB + iIA * (m0.z * m0.z) + iIB * (m0.w * m0.w);
+    const float impulse = (k != 0.f) ? -(C / k) : 0.f;
+    const V2 P = ay * impulse;
+    sub_imp(pA, iMA, P, iIA, impulse * sAy);
+    add_imp(pB, iMB, P, iIB, impulse * sBy);
+    if (bs.writable(a)) bs.set_pos(a, pA);
+    if (bs.writable(b)) bs.set_pos(b, pB);
+    return fabsf(C) <= c.linearSlop;
+}
+
+// PulleyJointConf (PulleyJointConf.cpp:93-241); extra = groundAnchorA.xy
+// groundAnchorB.xy lengthA lengthB ratio.
+template <class BS>
+__device__ void pulley_init_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    const float4 pA = bs.pos(a), pB = bs.pos(b);
+    float4 vA = bs.vel(a), vB = bs.vel(b);
+    const float4 an = d.j_anchor[j], e0 = d.j_extra[2 * j], e1 = d.j_extra[2 * j + 1];
+    const float ratio = e1.z;
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    const V2 uA = unit_vector((mk(pA.x, pA.y) + rA) - mk(e0.x, e0.y), mk(0.f, 0.f));
+    const V2 uB = unit_vector((mk(pB.x, pB.y) + rB) - mk(e0.z, e0.w), mk(0.f, 0.f));
+    const float ruA = cross(rA, uA), ruB = cross(rB, uB);
+    const float totInvMassA = iMA + (iIA * (ruA * ruA));
+    const float totInvMassB = iMB + (iIB * (ruB * ruB));
+    const float totalInvMass = totInvMassA + ratio * ratio * totInvMassB;
+    const float mass = (totalInvMass > 0.f) ? 1.0f / totalInvMass : 0.f;
+    float4 imp = d.j_imp[j];
+    if (c.doWarmStart) {
+        imp.x *= c.dtRatio;
+        const V2 PA = uA * (-imp.x);
+        const V2 PB = uB * (-ratio * imp.x);
+        add_imp(vA, iMA, PA, iIA, cross(rA, PA));
+        add_imp(vB, iMB, PB, iIB, cross(rB, PB));
+    } else {
+        imp.x = 0.f;
+    }
+    d.j_imp[j] = imp;
+    d.j_r[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    d.j_m0[j] = make_float4(uA.x, uA.y, uB.x, uB.y);
+    d.j_m1[j] = make_float4(mass, 0.f, 0.f, 0.f);
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ void pulley_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    float4 vA = bs.vel(a), vB = bs.vel(b);
+    const float4 r = d.j_r[j], m0 = d.j_m0[j];
+    const float ratio = d.j_extra[2 * j + 1].z;
+    float4 imp = d.j_imp[j];
+    const V2 rA = mk(r.x, r.y), rB = mk(r.z, r.w), uA = mk(m0.x, m0.y), uB = mk(m0.z, m0.w);
+    const float Cdot = -dot(uA, point_vel(vA, rA)) - ratio * dot(uB, point_vel(vB, rB));
+    const float impulse = -d.j_m1[j].x * Cdot;
+    imp.x += impulse;
+    const V2 PA = uA * (-impulse);
+    const V2 PB = uB * (-ratio * impulse);
+    add_imp(vA, mA.x, PA, mA.y, cross(rA, PA));
+    add_imp(vB, mB.x, PB, mB.y, cross(rB, PB));
+    d.j_imp[j] = imp;
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ bool pulley_solve_position(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b);
+    const float iMA = mA.x, iIA = mA.y, iMB = mB.x, iIB = mB.y;
+    float4 pA = bs.pos(a), pB = bs.pos(b);
+    const float4 an = d.j_anchor[j], e0 = d.j_extra[2 * j], e1 = d.j_extra[2 * j + 1];
+    const float ratio = e1.z;
+    const V2 rA = anchor_r(mk(an.x, an.y), mA, pA.z), rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    float lengthA, lengthB;
+    const V2 uA = unit_len((mk(pA.x, pA.y) + rA) - mk(e0.x, e0.y), lengthA);
+    const V2 uB = unit_len((mk(pB.x, pB.y) + rB) - mk(e0.z, e0.w), lengthB);
+    const float ruA = cross(rA, uA), ruB = cross(rB, uB);
+    const float totalInvMassA = iMA + iIA * (ruA * ruA);
+    const float totalInvMassB = iMB + iIB * (ruB * ruB);
+    const float totalInvMass = totalInvMassA + (ratio * ratio) * totalInvMassB;
+    const float mass = (totalInvMass > 0.f) ? 1.0f / totalInvMass : 0.f;
+    const float srcLengthRatio = e1.x + ratio * e1.y;
+    const float dstLengthRatio = lengthA + ratio * lengthB;
+    const float C = srcLengthRatio - dstLengthRatio;
+    const float impulse = -mass * C;
+    const V2 PA = uA * (-impulse);
+    const V2 PB = uB * (-ratio * impulse);
+    add_imp(pA, iMA, PA, iIA, cross(rA, PA));
+    add_imp(pB, iMB, PB, iIB, cross(rB, PB));
+    if (bs.writable(a)) bs.set_pos(a, pA);
+    if (bs.writable(b)) bs.set_pos(b, pB);
+    return fabsf(C) < c.linearSlop;
+}
+
+// TargetJointConf (TargetJointConf.cpp:51-184): body B only (body A is the same
+// index and untouched); extra = target.xy maxForce frequency dampingRatio.
+template <class BS>
+__device__ void target_init_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t b = d.j_bodies[2 * j + 1];
+    const float4 mB = bs.mass(b);
+    const float iM = mB.x, iI = mB.y;
+    const float4 pB = bs.pos(b);
+    float4 vB = bs.vel(b);
+    const float4 an = d.j_anchor[j], e0 = d.j_extra[2 * j], e1 = d.j_extra[2 * j + 1];
+    const float mass = (iM != 0.f) ? (1.0f / iM) : 0.f;
+    const float Pi = 3.14159265358979323846264338327950288f;
+    const float omega = 2.0f * Pi * e0.w;
+    const float dc = 2.0f * mass * e1.x * omega;
+    const float k = mass * (omega * omega);
+    const float h = c.deltaTime;
+    const float tmp = dc + h * k;
+    const float invGamma = h * tmp;
+    const float gamma = (invGamma != 0.f) ? 1.0f / invGamma : 0.f;
+    const float beta = h * k * gamma;
+    const V2 rB = anchor_r(mk(an.z, an.w), mB, pB.z);
+    // GetEffectiveMassMatrix (TargetJointConf.cpp:51-72), then Invert(Matrix22)
+    const float exx = iM + (iI * (rB.y * rB.y)) + gamma;
+    const float exy = -iI * rB.x * rB.y;
+    const float eyy = iM + (iI * (rB.x * rB.x)) + gamma;
+    float l00 = 0.f, l01 = 0.f, l11 = 0.f;
+    {
+        const float cp = cross(mk(exx, exy), mk(exy, eyy));
+        if (!almost_zero(cp)) {
+            const float inv = 1.0f / cp;
+            l00 = eyy * inv; l01 = -exy * inv; l11 = exx * inv;
+        }
+    }
+    const V2 C = ((mk(pB.x, pB.y) + rB) - mk(e0.x, e0.y)) * beta;
+    vB.z *= 0.98f;
+    float4 imp = d.j_imp[j];
+    if (c.doWarmStart) {
+        imp.x *= c.dtRatio; imp.y *= c.dtRatio;
+        const V2 P = mk(imp.x, imp.y);
+        add_imp(vB, iM, P, iI, cross(rB, P));
+    } else {
+        imp.x = imp.y = 0.f;
+    }
+    d.j_imp[j] = imp;
+    d.j_r[j] = make_float4(0.f, 0.f, rB.x, rB.y);
+    d.j_m0[j] = make_float4(l00, l01, l11, gamma);
+    d.j_m1[j] = make_float4(C.x, C.y, 0.f, 0.f);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
+template <class BS>
+__device__ void target_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const uint32_t b = d.j_bodies[2 * j + 1];
+    const float4 mB = bs.mass(b);
+    float4 vB = bs.vel(b);
+    const float4 r = d.j_r[j], m0 = d.j_m0[j], m1 = d.j_m1[j];
+    float4 imp = d.j_imp[j];
+    const V2 rB = mk(r.z, r.w);
+    const V2 oldImpulse = mk(imp.x, imp.y);
+    const V2 ev = point_vel(vB, rB) + (mk(m1.x, m1.y) + oldImpulse * m0.w);
+    const V2 add = sym22_mul(m0.x, m0.y, m0.z, -ev);
+    V2 impulse = oldImpulse + add;
+    const float maxImpulse = c.deltaTime * d.j_extra[2 * j].z;
+    if (mag2(impulse) > maxImpulse * maxImpulse) impulse = unit_vector(impulse, mk(0.f, 0.f)) * maxImpulse;
+    imp.x = impulse.x; imp.y = impulse.y;
+    const V2 inc = impulse - oldImpulse;
+    add_imp(vB, mB.x, inc, mB.y, cross(rB, inc));
+    d.j_imp[j] = imp;
+    if (bs.writable(b)) bs.set_vel(b, vB);
+}
+
 // Joint dispatch on the kind (the JointConf visitors of Joint.cpp).
 template <class BS>
 __device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
@@ -1053,6 +1588,10 @@ __device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
     case JK_WELD: weld_init_velocity(d, bs, j); break;
     case JK_FRICTION: friction_init_velocity(d, bs, j, false); break;
     case JK_MOTOR: friction_init_velocity(d, bs, j, true); break;
+    case JK_PRISMATIC: prismatic_init_velocity(d, bs, j); break;
+    case JK_WHEEL: wheel_init_velocity(d, bs, j); break;
+    case JK_PULLEY: pulley_init_velocity(d, bs, j); break;
+    case JK_TARGET: target_init_velocity(d, bs, j); break;
     default: revolute_init_velocity(d, bs, j); break;
     }
 }
@@ -1064,6 +1603,10 @@ __device__ void joint_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
     case JK_WELD: weld_solve_velocity(d, bs, j); break;
     case JK_FRICTION: friction_solve_velocity(d, bs, j, false); break;
     case JK_MOTOR: friction_solve_velocity(d, bs, j, true); break;
+    case JK_PRISMATIC: prismatic_solve_velocity(d, bs, j); break;
+    case JK_WHEEL: wheel_solve_velocity(d, bs, j); break;
+    case JK_PULLEY: pulley_solve_velocity(d, bs, j); break;
+    case JK_TARGET: target_solve_velocity(d, bs, j); break;
     default: revolute_solve_velocity(d, bs, j); break;
     }
 }
@@ -1074,7 +1617,10 @@ __device__ bool joint_solve_position(const DW& d, const BS& bs, uint32_t j) {
     case JK_DISTANCE: return distance_solve_position(d, bs, j, false);
     case JK_ROPE: return distance_solve_position(d, bs, j, true);
     case JK_WELD: return weld_solve_position(d, bs, j);
-    case JK_FRICTION: case JK_MOTOR: return true;
+    case JK_FRICTION: case JK_MOTOR: case JK_TARGET: return true;
+    case JK_PRISMATIC: return prismatic_solve_position(d, bs, j);
+    case JK_WHEEL: return wheel_solve_position(d, bs, j);
+    case JK_PULLEY: return pulley_solve_position(d, bs, j);
     default: return revolute_solve_position(d, bs, j);
     }
 }

@@ -391,12 +391,18 @@ int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
         j_param[j] = make_float4(ds->joint_params[6 * j], ds->joint_params[6 * j + 1], ds->joint_params[6 * j + 2], ds->joint_params[6 * j + 3]);
         j_maxtorque[j] = ds->joint_params[6 * j + 4];
         const int32_t kind = ds->joint_type ? ds->joint_type[j] : PRGPU_JOINT_REVOLUTE;
-        if (kind < PRGPU_JOINT_REVOLUTE || kind > PRGPU_JOINT_MOTOR) return PRGPU_EINVAL;
+        if (kind < PRGPU_JOINT_REVOLUTE || kind > PRGPU_JOINT_TARGET) return PRGPU_EINVAL;
+        if (kind == PRGPU_JOINT_TARGET && a != b) return PRGPU_EINVAL;
         j_flags[j] = (ds->joint_flags[3 * j] ? 1u : 0u) | (ds->joint_flags[3 * j + 1] ? 2u : 0u) | (cc << 2) |
                      ((uint32_t)kind << 8);
         const float* e = ds->joint_extra ? ds->joint_extra + 8 * (size_t)j : nullptr;
         hp.j_extra[2 * j] = e ? make_float4(e[0], e[1], e[2], e[3]) : make_float4(0.f, 0.f, 0.f, 0.f);
         hp.j_extra[2 * j + 1] = e ? make_float4(e[4], e[5], e[6], e[7]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (kind == PRGPU_JOINT_PRISMATIC || kind == PRGPU_JOINT_WHEEL) {
+            // localXAxisA = UnitVec::Get(axis) (UnitVec.hpp:175-235)
+            const V2 ax = unit_vector(mk(hp.j_extra[2 * j].x, hp.j_extra[2 * j].y), mk(0.f, 0.f));
+            hp.j_extra[2 * j].x = ax.x; hp.j_extra[2 * j].y = ax.y;
+        }
     }
     return PRGPU_OK;
 }
@@ -847,7 +853,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     float4* j_extra_d;
     AL(j_extra_d, 2 * (size_t)J);
     d.j_extra = j_extra_d;
-    AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_imp, J);
+    AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_m2, J); AL(d.j_imp, J);
     AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
     AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C);
     AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C);
@@ -950,6 +956,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ok &= up(d.j_flags, j_flags.data(), sizeof(uint32_t) * J);
     ok &= up(d.j_imp, j_zero.data(), sizeof(float4) * J);
     ok &= up(d.j_m1, j_zero.data(), sizeof(float4) * J);
+    ok &= up(d.j_m2, j_zero.data(), sizeof(float4) * J);
     ok &= cudaMemsetAsync(d.b_uat, 0, sizeof(float) * N, w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.b_alpha0, 0, sizeof(float) * N, w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.cnt, 0, sizeof(Counters), w->stream) == cudaSuccess;

@@ -16,9 +16,13 @@
 #include "playrho/d2/DistanceJointConf.hpp"
 #include "playrho/d2/FrictionJointConf.hpp"
 #include "playrho/d2/MotorJointConf.hpp"
+#include "playrho/d2/PrismaticJointConf.hpp"
+#include "playrho/d2/PulleyJointConf.hpp"
 #include "playrho/d2/RevoluteJointConf.hpp"
 #include "playrho/d2/RopeJointConf.hpp"
+#include "playrho/d2/TargetJointConf.hpp"
 #include "playrho/d2/WeldJointConf.hpp"
+#include "playrho/d2/WheelJointConf.hpp"
 
 namespace playrho::d2 {
 
@@ -133,7 +137,9 @@ prgpu::HostShape ToHost(const Shape& shape) {
 
 // The joint kinds the GPU steps, with their parameters in HostJoint::extra in the
 // order prgpu.h gives (DistanceJointConf.hpp:102-116, RopeJointConf.hpp:89-95,
-// WeldJointConf.hpp:104-119, FrictionJointConf.hpp:97-106, MotorJointConf.hpp:114-129).
+// WeldJointConf.hpp:104-119, FrictionJointConf.hpp:97-106, MotorJointConf.hpp:114-129,
+// PrismaticJointConf.hpp:131-159, WheelJointConf.hpp:132-150, PulleyJointConf.hpp:100-126,
+// TargetJointConf.hpp:119-140).
 prgpu::HostJoint ToHost(const Joint& joint) {
     prgpu::HostJoint h;
     const auto common = [&h](const auto& c) {
@@ -185,9 +191,50 @@ prgpu::HostJoint ToHost(const Joint& joint) {
         h.extra[3] = F(StripUnit(Force{c->maxForce}));
         h.extra[4] = F(StripUnit(Torque{c->maxTorque}));
         h.extra[5] = F(c->correctionFactor);
+    } else if (const auto* c = TypeCast<PrismaticJointConf>(&joint)) {
+        common(*c); anchors(*c);
+        h.kind = PRGPU_JOINT_PRISMATIC;
+        h.extra[0] = F(GetX(c->localXAxisA));
+        h.extra[1] = F(GetY(c->localXAxisA));
+        h.extra[2] = F(StripUnit(c->referenceAngle));
+        h.extra[3] = F(StripUnit(c->lowerTranslation));
+        h.extra[4] = F(StripUnit(c->upperTranslation));
+        h.extra[5] = F(StripUnit(c->motorSpeed));
+        h.extra[6] = F(StripUnit(c->maxMotorForce));
+        h.enable_limit = c->enableLimit ? 1 : 0;
+        h.enable_motor = c->enableMotor ? 1 : 0;
+    } else if (const auto* c = TypeCast<WheelJointConf>(&joint)) {
+        common(*c); anchors(*c);
+        h.kind = PRGPU_JOINT_WHEEL;
+        h.extra[0] = F(GetX(c->localXAxisA));
+        h.extra[1] = F(GetY(c->localXAxisA));
+        h.extra[2] = F(StripUnit(c->motorSpeed));
+        h.extra[3] = F(StripUnit(c->maxMotorTorque));
+        h.extra[4] = F(StripUnit(Frequency{c->frequency}));
+        h.extra[5] = F(c->dampingRatio);
+        h.enable_motor = c->enableMotor ? 1 : 0;
+    } else if (const auto* c = TypeCast<PulleyJointConf>(&joint)) {
+        common(*c); anchors(*c);
+        h.kind = PRGPU_JOINT_PULLEY;
+        h.extra[0] = F(StripUnit(GetX(c->groundAnchorA))); h.extra[1] = F(StripUnit(GetY(c->groundAnchorA)));
+        h.extra[2] = F(StripUnit(GetX(c->groundAnchorB))); h.extra[3] = F(StripUnit(GetY(c->groundAnchorB)));
+        h.extra[4] = F(StripUnit(c->lengthA));
+        h.extra[5] = F(StripUnit(c->lengthB));
+        h.extra[6] = F(c->ratio);
+    } else if (const auto* c = TypeCast<TargetJointConf>(&joint)) {
+        // body B only: the GPU side holds it as both bodies (its body A is InvalidBodyID)
+        if (c->bodyB == InvalidBodyID) throw InvalidArgument("GpuWorld: target joint without body B");
+        h.body_a = h.body_b = to_underlying(c->bodyB);
+        h.collide_connected = c->collideConnected ? 1 : 0;
+        h.anchor_b[0] = F(StripUnit(GetX(c->localAnchorB))); h.anchor_b[1] = F(StripUnit(GetY(c->localAnchorB)));
+        h.kind = PRGPU_JOINT_TARGET;
+        h.extra[0] = F(StripUnit(GetX(c->target))); h.extra[1] = F(StripUnit(GetY(c->target)));
+        h.extra[2] = F(StripUnit(Force{c->maxForce}));
+        h.extra[3] = F(StripUnit(Frequency{c->frequency}));
+        h.extra[4] = F(Real{c->dampingRatio});
     } else {
-        throw InvalidArgument("GpuWorld: only revolute, distance, rope, weld, friction and motor joints are "
-                              "stepped on the GPU");
+        throw InvalidArgument("GpuWorld: only revolute, distance, rope, weld, friction, motor, prismatic, wheel, "
+                              "pulley and target joints are stepped on the GPU");
     }
     return h;
 }
@@ -458,8 +505,13 @@ std::vector<std::pair<BodyID, JointID>> GetJoints(const GpuWorld& w, BodyID id) 
     for (uint32_t j = 0; j < w.joints.size(); ++j) {
         if (!w.host.JointAlive(j)) continue;
         const auto& h = w.host.GetJoint(j);
-        if (h.body_a == i) out.emplace_back(BodyID(h.body_b), JointID(j));
-        else if (h.body_b == i) out.emplace_back(BodyID(h.body_a), JointID(j));
+        if (h.kind == PRGPU_JOINT_TARGET) {
+            if (h.body_b == i) out.emplace_back(InvalidBodyID, JointID(j));
+        } else if (h.body_a == i) {
+            out.emplace_back(BodyID(h.body_b), JointID(j));
+        } else if (h.body_b == i) {
+            out.emplace_back(BodyID(h.body_a), JointID(j));
+        }
     }
     return out;
 }

@@ -7,7 +7,8 @@
 //
 // Prints, one per line:
 //   bodies N / shapes N / mass <invMass> <invRotI> / type T     after set-up
-//   joint <kind> <collide> <anchorA.x> <anchorB.y> <extra0..5>  per joint kind
+//   joint <kind> <collide> <anchorA.x> <anchorB.y> <extra0..6> <limit> <motor> <bodyA> <bodyB>
+//                                                               per joint kind
 //   joint_rejected <what>                                       for a kind the GPU does not step
 //   step <i> <x> <y> <angle>                                    per step (needs a GPU)
 //   error <what>                                                when stepping fails
@@ -15,6 +16,11 @@
 #include <exception>
 
 #include "playrho/d2/BasicAPI.hpp"
+#include "playrho/d2/GearJointConf.hpp"
+#include "playrho/d2/PrismaticJointConf.hpp"
+#include "playrho/d2/PulleyJointConf.hpp"
+#include "playrho/d2/TargetJointConf.hpp"
+#include "playrho/d2/WheelJointConf.hpp"
 
 #include "GpuWorld.hpp"
 
@@ -46,17 +52,29 @@ void CheckJoints() {
     motor.maxForce = 10_N; motor.maxTorque = 5_Nm; motor.correctionFactor = 0.25f;
     auto revolute = RevoluteJointConf{a, b};
     revolute.localAnchorA = anchorA; revolute.localAnchorB = anchorB;
+    auto prismatic = PrismaticJointConf{a, b, anchorA, anchorB, UnitVec::GetUp(), 0.5_rad};
+    prismatic.enableLimit = true; prismatic.lowerTranslation = -1_m; prismatic.upperTranslation = 2_m;
+    prismatic.enableMotor = true; prismatic.motorSpeed = 3_rad / 1_s; prismatic.maxMotorForce = 7_N;
+    auto wheel = WheelJointConf{a, b, anchorA, anchorB, UnitVec::GetUp()};
+    wheel.enableMotor = true; wheel.motorSpeed = -2_rad / 1_s; wheel.maxMotorTorque = 6_Nm;
+    wheel.frequency = 4_Hz; wheel.dampingRatio = 0.5f;
+    auto pulley = PulleyJointConf{a, b, Length2{-1_m, 5_m}, Length2{2_m, 5_m}, anchorA, anchorB, 4_m, 3_m};
+    pulley.ratio = 1.5f;
+    auto target = TargetJointConf{b};
+    target.localAnchorB = anchorB; target.target = Length2{3_m, 4_m}; target.maxForce = 9_N;
+    target.frequency = 3_Hz; target.dampingRatio = 0.25f;
     for (const auto& def : {Joint{revolute}, Joint{distance}, Joint{rope}, Joint{weld}, Joint{friction},
-                            Joint{motor}}) {
+                            Joint{motor}, Joint{prismatic}, Joint{wheel}, Joint{pulley}, Joint{target}}) {
         const auto id = CreateJoint(world, def);
         const auto& h = TypeCast<const GpuWorld&>(world).host.GetJoint(to_underlying(id));
         std::printf("joint %d %d %a %a", h.kind, h.collide_connected, static_cast<double>(h.anchor_a[0]),
                     static_cast<double>(h.anchor_b[1]));
-        for (auto k = 0; k < 6; ++k) std::printf(" %a", static_cast<double>(h.extra[k]));
+        for (auto k = 0; k < 7; ++k) std::printf(" %a", static_cast<double>(h.extra[k]));
+        std::printf(" %d %d %u %u", h.enable_limit, h.enable_motor, h.body_a, h.body_b);
         std::printf("\n");
     }
     try {
-        CreateJoint(world, Joint{PrismaticJointConf{a, b}});
+        CreateJoint(world, Joint{GearJointConf{}});
     } catch (const InvalidArgument& e) {
         std::printf("joint_rejected %s\n", e.what());
     }

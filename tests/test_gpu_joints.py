@@ -1,10 +1,12 @@
-"""The GPU step with distance, rope, weld, friction and motor joints against the
-CPU oracle (whose joints are pinned bit for bit to the reference:
+"""The GPU step with distance, rope, weld, friction, motor, prismatic, wheel,
+pulley and target joints against the CPU oracle (whose joints are pinned bit for
+bit to the reference:
 tests/test_oracle_vs_reference.py, tests/golden/ref_joint_zoo_seed7.npz).
 
 The GPU differs from the oracle only in sin/cos, so a mechanism alone in its
 world follows the oracle to within float rounding growth; joints keep their
-constraints (rope and distance lengths, weld angles); a batch gives each world
+constraints (rope and distance lengths, weld angles, prismatic and wheel axes and
+limits, pulley lengths); a batch gives each world
 the bits it has alone; the adjoint refuses joint kinds it does not
 differentiate.  Everything goes through the C ABI.
 """
@@ -18,7 +20,8 @@ from playrho_gb300.gpu import GpuBatch, PrgpuError
 pytestmark = pytest.mark.gpu
 
 KINDS = {"distance": scenes.JOINT_DISTANCE, "rope": scenes.JOINT_ROPE, "weld": scenes.JOINT_WELD,
-         "friction": scenes.JOINT_FRICTION, "motor": scenes.JOINT_MOTOR}
+         "friction": scenes.JOINT_FRICTION, "motor": scenes.JOINT_MOTOR, "prismatic": scenes.JOINT_PRISMATIC,
+         "wheel": scenes.JOINT_WHEEL, "pulley": scenes.JOINT_PULLEY, "target": scenes.JOINT_TARGET}
 
 
 def single_mechanisms(kind, n, seed):
@@ -48,16 +51,31 @@ def test_joint_kind_matches_oracle(gpu_lib, name):
                                            err_msg=f"{name} world {i} step {step}")
 
 
-def _anchor_distance(g, w, base, j):
-    a, b = (int(x) for x in w.joint_bodies[j])
+def _world_point(g, base, body, local):
     xf = g.bodies()["xf"]
+    c, s = xf[base + body, 2], xf[base + body, 3]
+    return xf[base + body, :2] + np.array([c * local[0] - s * local[1], s * local[0] + c * local[1]])
 
-    def world_point(body, local):
-        c, s = xf[base + body, 2], xf[base + body, 3]
-        return xf[base + body, :2] + np.array([c * local[0] - s * local[1], s * local[0] + c * local[1]])
 
+def _anchor_delta(g, w, base, j):
+    a, b = (int(x) for x in w.joint_bodies[j])
     an = w.joint_anchors[j]
-    return float(np.linalg.norm(world_point(b, an[2:4]) - world_point(a, an[0:2])))
+    return _world_point(g, base, b, an[2:4]) - _world_point(g, base, a, an[0:2])
+
+
+def _anchor_distance(g, w, base, j):
+    return float(np.linalg.norm(_anchor_delta(g, w, base, j)))
+
+
+def _axis(g, w, base, j):
+    """The joint's axis and its perpendicular in the world (localXAxisA rotated by body A)."""
+    a = int(w.joint_bodies[j][0])
+    e = w.joint_extra[j]
+    ax = np.array([e[0], e[1]], dtype=np.float64) / np.hypot(e[0], e[1])
+    xf = g.bodies()["xf"]
+    c, s = xf[base + a, 2], xf[base + a, 3]
+    axis = np.array([c * ax[0] - s * ax[1], s * ax[0] + c * ax[1]])
+    return axis, np.array([-axis[1], axis[0]])
 
 
 def test_joint_constraints_hold(gpu_lib):
@@ -79,6 +97,19 @@ def test_joint_constraints_hold(gpu_lib):
                 rel = pos[base + b, 2] - pos[base + a, 2] - float(w.joint_extra[j][0])
                 assert abs(rel) <= tol
                 assert _anchor_distance(g, w, base, j) <= tol
+            elif kind in (scenes.JOINT_PRISMATIC, scenes.JOINT_WHEEL):
+                axis, perp = _axis(g, w, base, j)
+                dv = _anchor_delta(g, w, base, j)
+                assert abs(float(dv @ perp)) <= tol
+                if kind == scenes.JOINT_PRISMATIC and w.joint_flags[j][0]:
+                    e = w.joint_extra[j]
+                    assert float(e[3]) - tol <= float(dv @ axis) <= float(e[4]) + tol
+            elif kind == scenes.JOINT_PULLEY:
+                a, b = (int(x) for x in w.joint_bodies[j])
+                e, an = w.joint_extra[j], w.joint_anchors[j]
+                la = np.linalg.norm(_world_point(g, base, a, an[0:2]) - e[0:2])
+                lb = np.linalg.norm(_world_point(g, base, b, an[2:4]) - e[2:4])
+                assert abs((la + e[6] * lb) - (e[4] + e[6] * e[5])) <= tol
 
 
 def test_joint_batch_equals_single_worlds(gpu_lib):

@@ -56,15 +56,21 @@ def test_world_over_gpuworld_builds_and_runs():
     assert inv_mass == 1.0 and inv_rot == 0.0
     # one joint of each kind reaches the GPU side with its kind and parameters
     joints = [l.split()[1:] for l in res.stdout.splitlines() if l.startswith("joint ")]
-    assert [int(j[0]) for j in joints] == [0, 1, 2, 3, 4, 5]  # prgpu_joint_kind order
-    extra = {int(j[0]): [float.fromhex(x) for x in j[4:]] for j in joints}
+    assert [int(j[0]) for j in joints] == list(range(10))  # prgpu_joint_kind order
+    extra = {int(j[0]): [float.fromhex(x) for x in j[4:11]] for j in joints}
+    flags = {int(j[0]): [int(x) for x in j[11:15]] for j in joints}
     assert all(float.fromhex(j[2]) == 0.25 and float.fromhex(j[3]) == 0.5 for j in joints[:5])
     assert int(joints[2][1]) == 1 and int(joints[1][1]) == 0  # collideConnected
     assert extra[1][:3] == [1.5, 4.0, 0.5]
     assert extra[2][:1] == [2.5]
     assert extra[3][:3] == [0.25, 2.0, 0.75]
     assert extra[4][:2] == [3.0, 1.5]
-    assert extra[5] == [1.0, -0.5, 0.125, 10.0, 5.0, 0.25]
+    assert extra[5][:6] == [1.0, -0.5, 0.125, 10.0, 5.0, 0.25]
+    assert extra[6] == [0.0, 1.0, 0.5, -1.0, 2.0, 3.0, 7.0] and flags[6][:2] == [1, 1]
+    assert extra[7][:6] == [0.0, 1.0, -2.0, 6.0, 4.0, 0.5] and flags[7][:2] == [0, 1]
+    assert extra[8] == [-1.0, 5.0, 2.0, 5.0, 4.0, 3.0, 1.5] and int(joints[8][1]) == 1  # pulley collides
+    assert extra[9][:5] == [3.0, 4.0, 9.0, 3.0, 0.25]
+    assert flags[9][2] == flags[9][3] == flags[0][3]  # the target joint holds body B only
     assert any(l.startswith("joint_rejected ") for l in res.stdout.splitlines())
     from playrho_gb300.gpu import gpu_available
 
