@@ -543,12 +543,14 @@ def joint_zoo(rng, per_kind: int = 4, kinds=None, n_disks: int = 12, gravity: bo
     acc = GRAVITY if gravity else (0.0, 0.0, 0.0)
     sb = SceneBuilder()
     g = sb.body(STATIC, 0.0, 0.0)
-    width = 3.0 * per_kind * len(kinds)
+    # a pulley's two boxes take more room than one box
+    spacing = {kind: 4.0 if kind == JOINT_PULLEY else 3.0 for kind in kinds}
+    width = per_kind * sum(spacing.values())
     sb.edge(g, (-width, 0.0), (width, 0.0))
     x = -width / 2.0
     for kind in kinds:
         for k in range(per_kind):
-            x += 3.0
+            x += spacing[kind]
             anchor = sb.body(STATIC, x, 8.0)
             hx, hy = float(rng.uniform(0.2, 0.6)), float(rng.uniform(0.2, 0.6))
             by = 8.0 - float(rng.uniform(1.0, 3.0))
