@@ -277,6 +277,13 @@ int prgpu_upload_body_states(prgpu_world* w, uint32_t first, uint32_t count, con
 int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
                             uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
                             uint32_t* features2);
+/* The creation sequence number of each live contact, in the order of
+ * prgpu_download_contacts.  Sorting a world's contacts by it gives the order of the
+ * reference's contact list (AabbTreeWorld::m_contacts), the order in which Step
+ * updates contacts and calls the BeginContact / EndContact listeners
+ * (AabbTreeWorld.cpp:2333-2415, 2703-2714); a contact destroyed and created again
+ * gets a new number. */
+int prgpu_download_contact_seq(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint64_t* seq);
 /* prgpu_download_contacts for callers that must not allocate device memory once
  * running (a real-time loop that forbids allocation in its steady state, or a
  * process whose device memory is held by another framework's caching allocator,

@@ -83,6 +83,8 @@ def _lib(double: bool):
                                                                                            ctypes.c_void_p]
     lib.or_add_joint.restype = ctypes.c_int
     lib.or_joint_enable.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.or_events.argtypes = [P, ctypes.c_void_p, ctypes.c_int]
+    lib.or_events.restype = ctypes.c_int
     lib.or_default_conf.argtypes = [ctypes.POINTER(Conf)]
     lib.or_step.argtypes = [P, ctypes.POINTER(Conf), ctypes.POINTER(Stats)]
     lib.or_body_count.argtypes = [P]
@@ -187,6 +189,14 @@ class OracleWorld:
 
     def set_body_state(self, i, pos, vel):
         self.lib.or_set_body_state(self.h, int(i), *(float(x) for x in (*pos, *vel)))
+
+    def events(self) -> list:
+        """BeginContact (1) / EndContact (2) listener calls of the last step, in call
+        order, as (kind, lower shape ID, higher shape ID)."""
+        n = self.lib.or_events(self.h, None, 0)
+        buf = np.zeros(max(3 * n, 3), np.int32)
+        self.lib.or_events(self.h, buf.ctypes.data, n)
+        return [tuple(int(x) for x in buf[3 * i:3 * i + 3]) for i in range(n)]
 
     def contacts(self) -> dict:
         n = self.lib.or_contact_count(self.h)

@@ -237,7 +237,16 @@ struct or_world {
     ivec bodiesForSync;
     ivec proxiesForContacts;
     real inv_dt0;
+    ivec events;            /* the last step's contact listener calls: (kind, shape, shape) */
 };
+
+/* A BeginContact (1) or EndContact (2) listener call, with the contact's shapes
+ * in ascending order (AabbTreeWorld.cpp:2249-2253, 2703-2714). */
+static void record_event(or_world* w, int kind, const contact_t* c) {
+    iv_push(&w->events, kind);
+    iv_push(&w->events, c->sA < c->sB ? c->sA : c->sB);
+    iv_push(&w->events, c->sA < c->sB ? c->sB : c->sA);
+}
 
 #define GROW(ptr, n, cap, T)                                                   \
     do {                                                                       \
@@ -293,6 +302,7 @@ void or_world_destroy(or_world* w) {
     free(w->b); free(w->s); free(w->j); free(w->p); free(w->c);
     iv_free(&w->cfree); iv_free(&w->wkeys); iv_free(&w->wcids);
     iv_free(&w->fixturesForProxies); iv_free(&w->bodiesForSync); iv_free(&w->proxiesForContacts);
+    iv_free(&w->events);
     free(w);
 }
 
@@ -902,6 +912,8 @@ static void contact_update(or_world* w, int cid, const or_stepconf* conf) {
         c->m = nm;
     }
     c->needsUpdate = 0;
+    if (!c->touching && newTouching) record_event(w, 1, c);
+    else if (c->touching && !newTouching) record_event(w, 2, c);
     c->touching = newTouching;
 }
 
@@ -914,6 +926,7 @@ static void contact_destroy(or_world* w, int cid) {
     if (k >= 0) { iv_erase_at(&bA->cids, k); iv_erase_at(&bA->ckeys, k); }
     k = kv_find(&bB->cids, cid);
     if (k >= 0) { iv_erase_at(&bB->cids, k); iv_erase_at(&bB->ckeys, k); }
+    if (c->touching) record_event(w, 2, c);
     if (c->m.count > 0 && !c->sensor) { body_set_awake(bA); body_set_awake(bB); }
     c->alive = 0;
     iv_push(&w->cfree, cid);
@@ -3494,6 +3507,7 @@ void or_step(or_world* w, const or_stepconf* conf, or_stepstats* st) {
     or_stepstats local;
     if (!st) st = &local;
     memset(st, 0, sizeof(*st));
+    w->events.n = 0;
     st->regMinSeparation = RINF;
     for (int i = 0; i < w->fixturesForProxies.n; ++i) {
         const int body = (int)(w->fixturesForProxies.a[i] >> 32);
@@ -3597,4 +3611,13 @@ int or_proxy_count(const or_world* w) { return w->np; }
 void or_get_proxy(const or_world* w, int p, int* bsc, real* aabb) {
     bsc[0] = w->p[p].body; bsc[1] = w->p[p].shape; bsc[2] = w->p[p].child;
     memcpy(aabb, w->p[p].aabb, 4 * sizeof(real));
+}
+
+/* The contact listener calls of the last or_step: up to cap (kind, shape,
+ * shape) triples into out; returns how many there were. */
+int or_events(const or_world* w, int* out, int cap) {
+    const int n = w->events.n / 3;
+    for (int i = 0; i < n && i < cap; ++i)
+        for (int k = 0; k < 3; ++k) out[3 * i + k] = (int)w->events.a[3 * i + k];
+    return n;
 }

@@ -120,6 +120,9 @@ void or_joint_enable(or_world* w, int jid, int enableLimit, int enableMotor);
 
 void or_default_conf(or_stepconf* conf);
 void or_step(or_world* w, const or_stepconf* conf, or_stepstats* stats);
+/* BeginContact (kind 1) and EndContact (kind 2) listener calls of the last
+ * or_step, in call order, as (kind, lower shape ID, higher shape ID) triples. */
+int or_events(const or_world* w, int* out, int cap);
 
 /* Body queries. */
 int or_body_count(const or_world* w);

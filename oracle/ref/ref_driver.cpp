@@ -186,6 +186,14 @@ void dump(const World& world, const StepStats& st)
 int main()
 {
     auto world = World{};
+    // BeginContact / EndContact calls as "ev kind lowerShape higherShape" lines
+    const auto event = [&world](int kind, ContactID id) {
+        const auto& c = GetContact(world, id);
+        const auto a = to_underlying(GetShapeA(c)), b = to_underlying(GetShapeB(c));
+        std::printf("ev %d %u %u\n", kind, static_cast<unsigned>(a < b ? a : b), static_cast<unsigned>(a < b ? b : a));
+    };
+    SetBeginContactListener(world, [event](ContactID id) { event(1, id); });
+    SetEndContactListener(world, [event](ContactID id) { event(2, id); });
     auto conf = StepConf{};
     conf.doToi = false;
     auto stats = StepStats{};

@@ -43,14 +43,17 @@ def run(scene_text: str, steps, double: bool = False, timeout: float = 600.0):
     seq = [steps] if isinstance(steps, int) else list(steps)
     cmd = scene_text + "".join(f"step {n}\ndump\n" for n in seq)
     res = subprocess.run([path], input=cmd, capture_output=True, text=True, timeout=timeout, check=True)
-    dumps, cur = [], None
+    dumps, cur, events = [], None, []
     for line in res.stdout.splitlines():
         t = line.split()
         if not t:
             continue
-        if t[0] == "stats":
+        if t[0] == "ev":
+            events.append(tuple(int(x) for x in t[1:4]))
+        elif t[0] == "stats":
             cur = {"stats": [int(x) for x in t[1:10]] + [_f(x) for x in t[10:12]],
-                   "bodies": [], "proxies": [], "contacts": []}
+                   "bodies": [], "proxies": [], "contacts": [], "events": events}
+            events = []
         elif t[0] == "toistats":
             cur["toistats"] = [int(x) for x in t[1:15]] + [_f(x) for x in t[15:17]]
         elif t[0] == "body":
@@ -87,4 +90,4 @@ def _finish(d, double):
                 "local_point": fo[:, 2:4], "points": fo[:, 4:12].reshape(n, 2, 4),
                 "features": ft.reshape(n, 2, 4)}
     return {"stats": d["stats"], "toistats": d.get("toistats"), "bodies": bodies, "proxies": proxies,
-            "contacts": contacts}
+            "contacts": contacts, "events": d["events"]}

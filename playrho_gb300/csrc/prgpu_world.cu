@@ -649,6 +649,10 @@ __global__ void k_gather_contacts(DW d, uint32_t n, uint32_t* proxies2, uint32_t
     }
 }
 
+__global__ void k_gather_seq(DW d, uint32_t n, uint64_t* seq) {
+    GRID_LOOP(i, n) seq[i] = d.cs_seq[d.c_slot[i]];
+}
+
 }  // namespace
 
 extern "C" {
@@ -1296,6 +1300,24 @@ int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, 
     if (pts8) CU(cudaMemcpyAsync(pts8, g_pt, 32 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     if (features2) CU(cudaMemcpyAsync(features2, g_ft, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaFreeAsync(scratch, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_download_contact_seq(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint64_t* seq) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    CU(cudaMemcpyAsync(w->h_cnt, w->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    const uint32_t n = w->h_cnt->n_live;
+    if (n_out) *n_out = n;
+    if (n > capacity) return fail(w, PRGPU_ECAPACITY, "%u contacts exceed capacity %u", n, capacity);
+    if (n == 0 || !seq) return PRGPU_OK;
+    uint64_t* g = nullptr;
+    CU(cudaMallocAsync(reinterpret_cast<void**>(&g), 8 * (size_t)n, w->stream));
+    k_gather_seq<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, n, g);
+    CU(cudaMemcpyAsync(seq, g, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaFreeAsync(g, w->stream));
     CU(cudaStreamSynchronize(w->stream));
     return PRGPU_OK;
 }

@@ -104,6 +104,7 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_download_bodies.argtypes = [P, P, P, P, P, P, P]
     lib.prgpu_upload_body_states.argtypes = [P, U, U, P, P]
     lib.prgpu_download_contacts.argtypes = [P, U, P, P, P, P, P, P, P, P]
+    lib.prgpu_download_contact_seq.argtypes = [P, U, P, P]
     lib.prgpu_download_proxies.argtypes = [P, P]
     lib.prgpu_last_error.argtypes = [P, ctypes.c_char_p, I]
     lib.prgpu_convex_hull.argtypes = [P, I, ctypes.c_float, P]
@@ -291,6 +292,7 @@ class GpuBatch:
         d.candidate_capacity = candidate_capacity
         self.n_bodies, self.n_shapes, self.n_joints = d.n_bodies, d.n_shapes, d.n_joints
         self.body_base = f["body_base"]
+        self.shape_base = np.cumsum([0] + [sc.n_shapes for sc in scenes])
         h = ctypes.c_void_p()
         rc = self.lib.prgpu_world_create(ctypes.byref(d), device, ctypes.byref(h))
         if rc:
@@ -485,10 +487,69 @@ class GpuBatch:
                 "type": me[:n, 0], "count": me[:n, 1], "local_normal": hd[:n, 0:2], "local_point": hd[:n, 2:4],
                 "points": pt[:n], "features": feats}
 
+    def contact_seq(self) -> np.ndarray:
+        """Creation sequence numbers of the live contacts, in the order of contacts()."""
+        n = self.contact_count()
+        seq = np.zeros(max(n, 1), np.uint64)
+        nout = ctypes.c_uint32()
+        self._check(self.lib.prgpu_download_contact_seq(self.h, seq.size, ctypes.byref(nout), _ptr(seq)), "seq")
+        return seq[:nout.value]
+
     def proxies(self) -> np.ndarray:
         a = np.zeros((self.n_shapes, 4), np.float32)
         self._check(self.lib.prgpu_download_proxies(self.h, _ptr(a)), "proxies")
         return a
+
+
+class ContactEvents:
+    """BeginContact / EndContact listener calls of each world, replayed after every
+    step from two consecutive contact snapshots of a batch.
+
+    The calls of a step come in the reference's order: first EndContact for each
+    touching contact the step destroyed, in contact-list order (DestroyContacts, then
+    InternalDestroy, AabbTreeWorld.cpp:2245-2331).  Then BeginContact / EndContact for
+    each contact whose touching state changed, in contact-list order (UpdateContacts and
+    Update, :2333-2415, 2703-2714).  The contact-list order is the creation order.
+    A contact that the step created touches only if it was created at the start of the
+    step, for shapes added since the last step, and was updated in that step.  Contacts
+    found after the solve are not updated until the next step.  With the time-of-impact
+    phase on, a contact that the phase makes
+    touch and separate within one step shows only its net change.  An event is (kind,
+    lower shape ID, higher shape ID) with world-local shape IDs; kind 1 is begin and 2
+    is end."""
+
+    def __init__(self, batch: "GpuBatch"):
+        self.batch = batch
+        self.prev = self._snapshot()
+
+    def _snapshot(self) -> dict:
+        c = self.batch.contacts()
+        seq = self.batch.contact_seq()
+        sb = np.asarray(self.batch.shape_base, dtype=np.int64)
+        world = np.searchsorted(sb, c["proxy"][:, 0], side="right") - 1
+        lo = c["proxy"].min(axis=1) - sb[world]
+        hi = c["proxy"].max(axis=1) - sb[world]
+        return {int(q): (int(w), int(a), int(b), int(t)) for q, w, a, b, t in
+                zip(seq, world, lo, hi, c["touching"])}
+
+    def step(self, conf=None) -> list:
+        """One batch step; returns each world's listener calls of that step."""
+        self.batch.step(conf)
+        cur = self._snapshot()
+        events = [[] for _ in range(len(self.batch.shape_base) - 1)]
+        for q in sorted(self.prev):
+            w, a, b, t = self.prev[q]
+            if q not in cur and t:
+                events[w].append((2, a, b))
+        for q in sorted(cur):
+            w, a, b, t = cur[q]
+            if q in self.prev:
+                if self.prev[q][3] != t:
+                    events[w].append((1 if t else 2, a, b))
+            elif t:
+                events[w].append((1, a, b))
+        self.prev = cur
+        return events
 
 
 def gpu_available() -> bool:

@@ -63,3 +63,28 @@ def test_joint_kinds(kind):
 
 def test_joint_zoo_f64():
     _compare(scenes.joint_zoo(np.random.default_rng(36)), [1, 80], double=True)
+
+
+def _compare_events(scene, steps, double=False, **conf):
+    """The oracle's BeginContact / EndContact calls equal the reference listeners'."""
+    dumps = refdriver.run(scenes.scene_text(scene, conf), steps, double=double)
+    ow = oracle.OracleWorld(scene, double=double)
+    total = 0
+    for n, d in zip(steps, dumps):
+        evs = []
+        for _ in range(n):
+            ow.step(**conf)
+            evs += ow.events()
+        assert evs == d["events"]
+        total += len(evs)
+    return total
+
+
+@pytest.mark.parametrize("seed", [41, 42])
+def test_contact_events_piles(seed):
+    assert _compare_events(scenes.pile(150, np.random.default_rng(seed)), [1, 40, 100]) > 0
+
+
+def test_contact_events_bullets_with_toi():
+    assert _compare_events(scenes.bullets(40, np.random.default_rng(43)), [1, 20, 40], doToi=1) > 0
+
