@@ -277,6 +277,13 @@ int prgpu_upload_body_states(prgpu_world* w, uint32_t first, uint32_t count, con
 int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
                             uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
                             uint32_t* features2);
+/* Query(tree, aabb, callback) over one world's broadphase tree (DynamicTree.cpp:673-710):
+ * the world-local shape IDs whose fat AABB overlaps `aabb` (minx miny maxx maxy), by
+ * TestOverlap, in ascending order (the reference visits them in tree order).  Valid
+ * after the first step, which creates the proxies; more than `capacity` overlaps
+ * returns PRGPU_ECAPACITY with *n_out set. */
+int prgpu_query_aabb(prgpu_world* w, uint32_t world, const float* aabb4, uint32_t capacity, uint32_t* n_out,
+                     uint32_t* shapes);
 /* The creation sequence number of each live contact, in the order of
  * prgpu_download_contacts.  Sorting a world's contacts by it gives the order of the
  * reference's contact list (AabbTreeWorld::m_contacts), the order in which Step

@@ -649,6 +649,20 @@ __global__ void k_gather_contacts(DW d, uint32_t n, uint32_t* proxies2, uint32_t
     }
 }
 
+// TestOverlap(leaf fat AABB, query AABB) (AABB.hpp, as DynamicTree::Query calls it)
+// for every proxy of one world; the overlapping ones are appended to out.
+__global__ void k_query_aabb(DW d, uint32_t first, uint32_t n, float4 q, uint32_t cap, uint32_t* out,
+                             uint32_t* count) {
+    GRID_LOOP(i, n) {
+        const float4 a = d.p_aabb[first + i];
+        const float maxOfMinsX = (a.x < q.x) ? q.x : a.x, minOfMaxsX = (q.z < a.z) ? q.z : a.z;
+        const float maxOfMinsY = (a.y < q.y) ? q.y : a.y, minOfMaxsY = (q.w < a.w) ? q.w : a.w;
+        if (!(minOfMaxsX >= maxOfMinsX) || !(minOfMaxsY >= maxOfMinsY)) continue;
+        const uint32_t k = atomicAdd(count, 1u);
+        if (k < cap) out[k] = i;
+    }
+}
+
 __global__ void k_gather_seq(DW d, uint32_t n, uint64_t* seq) {
     GRID_LOOP(i, n) seq[i] = d.cs_seq[d.c_slot[i]];
 }
@@ -1301,6 +1315,37 @@ int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, 
     if (features2) CU(cudaMemcpyAsync(features2, g_ft, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaFreeAsync(scratch, w->stream));
     CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_query_aabb(prgpu_world* w, uint32_t world, const float* aabb4, uint32_t capacity, uint32_t* n_out,
+                     uint32_t* shapes) {
+    if (!w || !aabb4) return PRGPU_EINVAL;
+    if (world >= w->d.n_worlds) return fail(w, PRGPU_EINVAL, "world %u out of range", world);
+    CU(cudaSetDevice(w->device));
+    uint32_t off[2] = {0u, 0u};
+    CU(cudaMemcpyAsync(off, w->d.w_shape_off + world, sizeof(off), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    const uint32_t n = off[1] - off[0];
+    if (n_out) *n_out = 0;
+    if (n == 0) return PRGPU_OK;
+    uint32_t* g = nullptr;
+    CU(cudaMallocAsync(reinterpret_cast<void**>(&g), 4 * ((size_t)n + 1), w->stream));
+    CU(cudaMemsetAsync(g, 0, 4, w->stream));
+    const float4 q = make_float4(aabb4[0], aabb4[1], aabb4[2], aabb4[3]);
+    k_query_aabb<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, off[0], n, q, n, g + 1, g);
+    uint32_t found = 0;
+    CU(cudaMemcpyAsync(&found, g, 4, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (n_out) *n_out = found;
+    if (found > capacity) {
+        CU(cudaFreeAsync(g, w->stream));
+        return fail(w, PRGPU_ECAPACITY, "%u overlaps exceed capacity %u", found, capacity);
+    }
+    if (found && shapes) CU(cudaMemcpyAsync(shapes, g + 1, 4 * (size_t)found, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaFreeAsync(g, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (shapes) std::sort(shapes, shapes + found);
     return PRGPU_OK;
 }
 

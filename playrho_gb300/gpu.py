@@ -105,6 +105,7 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_upload_body_states.argtypes = [P, U, U, P, P]
     lib.prgpu_download_contacts.argtypes = [P, U, P, P, P, P, P, P, P, P]
     lib.prgpu_download_contact_seq.argtypes = [P, U, P, P]
+    lib.prgpu_query_aabb.argtypes = [P, U, P, U, P, P]
     lib.prgpu_download_proxies.argtypes = [P, P]
     lib.prgpu_last_error.argtypes = [P, ctypes.c_char_p, I]
     lib.prgpu_convex_hull.argtypes = [P, I, ctypes.c_float, P]
@@ -486,6 +487,15 @@ class GpuBatch:
         return {"proxy": pr[:n].astype(np.int64), "bodies": bd[:n].astype(np.int64), "touching": (fl[:n] & 1).astype(np.int32),
                 "type": me[:n, 0], "count": me[:n, 1], "local_normal": hd[:n, 0:2], "local_point": hd[:n, 2:4],
                 "points": pt[:n], "features": feats}
+
+    def query_aabb(self, world: int, aabb) -> np.ndarray:
+        """World-local shape IDs whose fat AABB overlaps aabb (minx, miny, maxx, maxy)."""
+        q = np.ascontiguousarray(aabb, dtype=np.float32)
+        cap = int(self.shape_base[world + 1] - self.shape_base[world])
+        out = np.zeros(max(cap, 1), np.uint32)
+        nout = ctypes.c_uint32()
+        self._check(self.lib.prgpu_query_aabb(self.h, world, _ptr(q), cap, ctypes.byref(nout), _ptr(out)), "query")
+        return out[:nout.value].astype(np.int64)
 
     def contact_seq(self) -> np.ndarray:
         """Creation sequence numbers of the live contacts, in the order of contacts()."""
