@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define PRGPU_ABI_VERSION 2
+#define PRGPU_ABI_VERSION 3
 
 enum prgpu_status {
     PRGPU_OK = 0,
@@ -88,6 +88,7 @@ typedef struct prgpu_step_stats {
     uint32_t toiContactsAdded, toiProxiesMoved, toiSumPosIters, toiSumVelIters;
     uint32_t toiMaxDistIters, toiMaxToiIters, toiMaxRootIters, toiRounds;
     float toiMinSeparation, toiMaxIncImpulse;
+    uint32_t bodiesSolved;  /* dynamic bodies of the awake islands the step advanced (body-steps) */
 } prgpu_step_stats;
 
 /* A batch of worlds in creation order, flattened world-major.  Body indices in
@@ -256,9 +257,17 @@ int prgpu_adjoint_trim(void);
 /* Host time (ms) of the window's forward steps and of the last backward pass's
  * recording (segments re-run from their checkpoints) and reverse kernels. */
 int prgpu_adjoint_profile(prgpu_world* w, double* forward_ms, double* record_ms, double* reverse_ms);
-/* Enqueues n steps on the handle's stream and returns at once. */
+/* Enqueues n steps on the handle's stream and returns at once.  A device error
+ * raised by an earlier step (capacity overflow, a bounded wait that gave up) is
+ * returned by the next prgpu_step_async once that step has finished, and by
+ * prgpu_synchronize, which waits for all of them. */
 int prgpu_step_async(prgpu_world* w, const prgpu_step_conf* conf, int n);
 int prgpu_synchronize(prgpu_world* w);
+/* Body-steps since the handle was created: the dynamic bodies of awake islands
+ * summed over every step the device ran (sleeping and static bodies are not
+ * counted).  Waits for the handle's work.  No reference counterpart (the
+ * throughput unit of the batched step). */
+int prgpu_get_body_steps(prgpu_world* w, uint64_t* total);
 int prgpu_get_counts(prgpu_world* w, uint32_t* n_worlds, uint32_t* n_bodies, uint32_t* n_shapes,
                      uint32_t* n_joints, uint32_t* n_contacts);
 /* Body state; any pointer may be NULL.  flags: bit0 awake.  mass: invM invI lcx lcy. */
@@ -308,8 +317,20 @@ int prgpu_download_contact_seq(prgpu_world* w, uint32_t capacity, uint32_t* n_ou
 int prgpu_download_contacts_noalloc(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
                                     uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
                                     uint32_t* features2);
-/* Fat (tree) AABB of every proxy: minx miny maxx maxy. */
+/* Fat (tree) AABB of every proxy: minx miny maxx maxy.  A shape without a proxy
+ * (its body was created disabled, AabbTreeWorld.cpp:1040) reports an empty box
+ * (min +inf, max -inf). */
 int prgpu_download_proxies(prgpu_world* w, float* aabb4);
+/* The order in which the last step's regular-phase solve swept its constraints
+ * (warm start, velocity and position iterations all follow it), world by world:
+ * items3[3t..3t+2] = (0, shape A, shape B) for the contact of two shapes (global
+ * shape indices, lower first) or (1, joint, 0) for a joint (global joint index).
+ * No reference counterpart: the reference solves each island in its own order
+ * (ContactSolver.cpp, AabbTreeWorld.cpp:1563-1683); this order is a valid
+ * Gauss-Seidel order of the same constraints (graph colours), reported so that
+ * parity checks can replay it.  Valid after a step without the time-of-impact
+ * phase, until the next step. */
+int prgpu_download_sweep_order(prgpu_world* w, uint32_t capacity, uint32_t* n_out, int32_t* items3);
 /* Runs the host-side part of prgpu_world_create (validation, mass data as
  * Attach(..., resetMassData = true) leaves it) without a GPU: centre-of-mass
  * positions, velocities and invM invI lcx lcy of every body.  Any output may be NULL. */

@@ -91,6 +91,8 @@ def _lib(double: bool):
     lib.or_body_count.restype = ctypes.c_int
     lib.or_get_body.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     lib.or_set_body_state.argtypes = [P, ctypes.c_int] + [real] * 6
+    lib.or_set_body_xf.argtypes = [P, ctypes.c_int] + [real] * 4
+    lib.or_set_solve_order.argtypes = [P, ctypes.c_int, ctypes.c_void_p]
     lib.or_contact_count.argtypes = [P]
     lib.or_contact_count.restype = ctypes.c_int
     lib.or_get_contact.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
@@ -189,6 +191,19 @@ class OracleWorld:
 
     def set_body_state(self, i, pos, vel):
         self.lib.or_set_body_state(self.h, int(i), *(float(x) for x in (*pos, *vel)))
+
+    def set_body_xf(self, xf4):
+        """Gives every body the transformation (p.x, p.y, cos, sin) in xf4 [n, 4]
+        (identical transforms on both sides of a parity check)."""
+        for i, x in enumerate(np.asarray(xf4)):
+            self.lib.or_set_body_xf(self.h, int(i), *(float(v) for v in x))
+
+    def set_solve_order(self, items):
+        """Solve constraints in the order of ``items`` [n, 3] from the next step on:
+        (0, shape A, shape B) for a contact, (1, joint, 0) for a joint; None or an
+        empty list restores the reference's order."""
+        a = np.ascontiguousarray(np.asarray(items if items is not None else [], dtype=np.int32).reshape(-1, 3))
+        self.lib.or_set_solve_order(self.h, int(a.shape[0]), a.ctypes.data if a.size else None)
 
     def events(self) -> list:
         """BeginContact (1) / EndContact (2) listener calls of the last step, in call

@@ -238,6 +238,11 @@ struct or_world {
     ivec proxiesForContacts;
     real inv_dt0;
     ivec events;            /* the last step's contact listener calls: (kind, shape, shape) */
+    /* or_set_solve_order: ranks of contacts (by shape pair) and joints for the
+     * next step's island solves; empty: the reference's order */
+    ivec order_ckeys;       /* (shape min << 32 | shape max), sorted */
+    ivec order_crank;       /* rank of order_ckeys[i] */
+    ivec order_jrank;       /* rank of joint j, or -1 */
 };
 
 /* A BeginContact (1) or EndContact (2) listener call, with the contact's shapes
@@ -303,6 +308,7 @@ void or_world_destroy(or_world* w) {
     iv_free(&w->cfree); iv_free(&w->wkeys); iv_free(&w->wcids);
     iv_free(&w->fixturesForProxies); iv_free(&w->bodiesForSync); iv_free(&w->proxiesForContacts);
     iv_free(&w->events);
+    iv_free(&w->order_ckeys); iv_free(&w->order_crank); iv_free(&w->order_jrank);
     free(w);
 }
 
@@ -369,10 +375,10 @@ int or_add_shape(or_world* w, int body, int kind, int nverts, const real* xy, re
     s->density = density; s->friction = friction; s->restitution = restitution;
     s->cat = categoryBits; s->mask = maskBits; s->group = groupIndex; s->sensor = sensor;
     const int sid = w->ns++;
-    /* CreateBody / Attach queue the fixture for proxy creation in the next Step
-     * (AabbTreeWorld.cpp:1041). */
+    /* CreateBody / Attach queue the fixture for proxy creation in the next Step,
+     * for an enabled body only (AabbTreeWorld.cpp:1040-1041, :1302). */
     iv_push(&w->b[body].shapes, sid);
-    iv_push(&w->fixturesForProxies, ((int64_t)body << 32) | (int64_t)sid);
+    if (w->b[body].flags & BF_ENABLED) iv_push(&w->fixturesForProxies, ((int64_t)body << 32) | (int64_t)sid);
     return sid;
 }
 
@@ -1099,10 +1105,20 @@ static int find_and_add_contacts(or_world* w, const or_stepconf* conf) {
     return added;
 }
 
+/* GetTransform0(sweep) (Sweep.hpp).  The body's transformation is always
+ * GetTransform1(sweep) (Body::SetSweep / SetPosition1), so when pos0 equals pos1
+ * the stored transformation is that same value; taking it keeps a transformation
+ * set by or_set_body_xf (identical transforms injected on both sides of a
+ * parity check). */
+static xf_t xf0_of(const body_t* b) {
+    if (b->pos0.lin.x == b->pos1.lin.x && b->pos0.lin.y == b->pos1.lin.y && b->pos0.ang == b->pos1.ang) return b->xf;
+    return get_xf(b->pos0, b->lc);
+}
+
 /* CreateProxies (AabbTreeWorld.cpp:557-579). */
 static void create_proxies(or_world* w, int body, int shape, const or_stepconf* conf) {
     body_t* b = &w->b[body];
-    const xf_t x0 = get_xf(b->pos0, b->lc);
+    const xf_t x0 = xf0_of(b);
     const xf_t x1 = b->xf;
     const v2 disp = vmul(vsub(x1.p, x0.p), conf->displaceMultiplier);
     GROW(w->p, w->np, w->capp, proxy_t);
@@ -1119,7 +1135,7 @@ static void create_proxies(or_world* w, int body, int shape, const or_stepconf* 
 /* AabbTreeWorld::Synchronize (AabbTreeWorld.cpp:2564-2585). */
 static int synchronize(or_world* w, int body, const or_stepconf* conf) {
     body_t* b = &w->b[body];
-    const xf_t x0 = get_xf(b->pos0, b->lc);
+    const xf_t x0 = xf0_of(b);
     const xf_t x1 = b->xf;
     const v2 disp = vmul(vsub(x1.p, x0.p), conf->displaceMultiplier);
     int n = 0;
@@ -2691,6 +2707,43 @@ static void make_bc(bc_t* bc, const body_t* b, real h, const or_stepconf* conf) 
     bc->vel = v;
 }
 
+/* Island constraint order set by or_set_solve_order (test infrastructure). */
+typedef struct { int64_t rank; int joint, idx; } ord_item;
+static int cmp_ord(const void* a, const void* b) {
+    const ord_item* x = (const ord_item*)a;
+    const ord_item* y = (const ord_item*)b;
+    if (x->rank != y->rank) return (x->rank < y->rank) ? -1 : 1;
+    if (x->joint != y->joint) return x->joint - y->joint;
+    return x->idx - y->idx;
+}
+static int64_t contact_rank(const or_world* w, const contact_t* c) {
+    const int a = c->sA < c->sB ? c->sA : c->sB, b = c->sA < c->sB ? c->sB : c->sA;
+    const int64_t key = ((int64_t)a << 32) | (int64_t)b;
+    int lo = 0, hi = w->order_ckeys.n;
+    while (lo < hi) {
+        const int mid = (lo + hi) / 2;
+        if (w->order_ckeys.a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    if (lo < w->order_ckeys.n && w->order_ckeys.a[lo] == key) return w->order_crank.a[lo];
+    return INT64_MAX / 2; /* not listed: after every listed constraint, in island order */
+}
+static ord_item* island_order(const or_world* w, const island_t* isl) {
+    const int nc = isl->contacts.n, nj = isl->joints.n;
+    ord_item* o = (ord_item*)malloc(sizeof(ord_item) * (size_t)(nc + nj + 1));
+    for (int i = 0; i < nc; ++i) {
+        o[i].rank = contact_rank(w, &w->c[isl->contacts.a[i]]);
+        o[i].joint = 0; o[i].idx = i;
+    }
+    for (int i = 0; i < nj; ++i) {
+        const int jid = (int)isl->joints.a[i];
+        const int64_t r = (jid < w->order_jrank.n) ? w->order_jrank.a[jid] : -1;
+        o[nc + i].rank = (r >= 0) ? r : INT64_MAX / 2;
+        o[nc + i].joint = 1; o[nc + i].idx = i;
+    }
+    qsort(o, (size_t)(nc + nj), sizeof(ord_item), cmp_ord);
+    return o;
+}
+
 static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc_t* bcs,
                          or_stepstats* st) {
     const real h = conf->deltaTime;
@@ -2720,18 +2773,37 @@ static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc
         const wman_t wm = world_manifold(&c->m, xfA, rA, xfB, rB);
         make_vc(&vcs[i], c, &wm, bcs, conf);
     }
-    if (conf->doWarmStart) {
-        for (int i = 0; i < nc; ++i) warm_start(&vcs[i], bcs);
+    /* With a solve order set (or_set_solve_order), every pass visits the island's
+     * contacts and joints interleaved in that order instead of the reference's
+     * (contacts in island order, joints before contacts in each iteration). */
+    const int nj = isl->joints.n;
+    ord_item* ord = (w->order_crank.n || w->order_jrank.n) ? island_order(w, isl) : NULL;
+    if (ord) {
+        for (int q = 0; q < nc + nj; ++q) {
+            if (ord[q].joint) joint_init_velocity(&w->j[isl->joints.a[ord[q].idx]], bcs, conf);
+            else if (conf->doWarmStart) warm_start(&vcs[ord[q].idx], bcs);
+        }
+    } else {
+        if (conf->doWarmStart) {
+            for (int i = 0; i < nc; ++i) warm_start(&vcs[i], bcs);
+        }
+        for (int i = 0; i < nj; ++i) joint_init_velocity(&w->j[isl->joints.a[i]], bcs, conf);
     }
-    for (int i = 0; i < isl->joints.n; ++i) joint_init_velocity(&w->j[isl->joints.a[i]], bcs, conf);
 
     int velIters = conf->regVelocityIters;
     real maxInc = R(0);
     for (int it = 0; it < conf->regVelocityIters; ++it) {
         int jointsOkay = 1;
-        for (int i = 0; i < isl->joints.n; ++i) jointsOkay &= joint_solve_velocity(&w->j[isl->joints.a[i]], bcs, conf);
         real newInc = R(0);
-        for (int i = 0; i < nc; ++i) newInc = maxr(newInc, solve_vc(&vcs[i], bcs));
+        if (ord) {
+            for (int q = 0; q < nc + nj; ++q) {
+                if (ord[q].joint) jointsOkay &= joint_solve_velocity(&w->j[isl->joints.a[ord[q].idx]], bcs, conf);
+                else newInc = maxr(newInc, solve_vc(&vcs[ord[q].idx], bcs));
+            }
+        } else {
+            for (int i = 0; i < nj; ++i) jointsOkay &= joint_solve_velocity(&w->j[isl->joints.a[i]], bcs, conf);
+            for (int i = 0; i < nc; ++i) newInc = maxr(newInc, solve_vc(&vcs[i], bcs));
+        }
         maxInc = maxr(maxInc, newInc);
         if (jointsOkay && (newInc <= conf->regMinMomentum)) { velIters = it + 1; break; }
     }
@@ -2747,13 +2819,23 @@ static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc
     real minSepIsland = RINF;
     for (int it = 0; it < conf->regPositionIters; ++it) {
         real minSep = RINF;
-        for (int i = 0; i < nc; ++i) minSep = minr(minSep, solve_pc(&pcs[i], bcs, conf));
+        int jointsOkay = 1;
+        if (ord) {
+            for (int q = 0; q < nc + nj; ++q) {
+                if (ord[q].joint) jointsOkay &= joint_solve_position(&w->j[isl->joints.a[ord[q].idx]], bcs, conf);
+                else minSep = minr(minSep, solve_pc(&pcs[ord[q].idx], bcs, conf));
+            }
+        } else {
+            for (int i = 0; i < nc; ++i) minSep = minr(minSep, solve_pc(&pcs[i], bcs, conf));
+        }
         minSepIsland = minr(minSepIsland, minSep);
         const int contactsOkay = (minSep >= conf->regMinSeparation);
-        int jointsOkay = 1;
-        for (int i = 0; i < isl->joints.n; ++i) jointsOkay &= joint_solve_position(&w->j[isl->joints.a[i]], bcs, conf);
+        if (!ord) {
+            for (int i = 0; i < nj; ++i) jointsOkay &= joint_solve_position(&w->j[isl->joints.a[i]], bcs, conf);
+        }
         if (contactsOkay && jointsOkay) { posIters = it + 1; solved = 1; break; }
     }
+    free(ord);
     /* AssignImpulses (:196-220) */
     for (int i = 0; i < nc; ++i) {
         contact_t* c = &w->c[isl->contacts.a[i]];
@@ -3592,6 +3674,41 @@ void or_set_body_state(or_world* w, int id, real px, real py, real angle, real v
     b->vel.lin = V(vx, vy); b->vel.ang = av;
     for (int k = 0; k < b->cids.n; ++k) w->c[b->cids.a[k]].needsUpdate = 1;
     iv_push(&w->bodiesForSync, id);
+}
+static int cmp_i64pair(const void* a, const void* b) {
+    const int64_t* x = (const int64_t*)a;
+    const int64_t* y = (const int64_t*)b;
+    return (x[0] < y[0]) ? -1 : (x[0] > y[0]) ? 1 : 0;
+}
+void or_set_solve_order(or_world* w, int n, const int* items3) {
+    w->order_ckeys.n = w->order_crank.n = w->order_jrank.n = 0;
+    if (n <= 0) return;
+    int64_t* pairs = (int64_t*)malloc(sizeof(int64_t) * 2 * (size_t)n);
+    int np = 0;
+    for (int i = 0; i < n; ++i) {
+        const int kind = items3[3 * i], a = items3[3 * i + 1], b = items3[3 * i + 2];
+        if (kind == 0) {
+            const int lo = a < b ? a : b, hi = a < b ? b : a;
+            pairs[2 * np] = ((int64_t)lo << 32) | (int64_t)hi;
+            pairs[2 * np + 1] = i;
+            ++np;
+        } else {
+            while (w->order_jrank.n <= a) iv_push(&w->order_jrank, -1);
+            w->order_jrank.a[a] = i;
+        }
+    }
+    qsort(pairs, (size_t)np, 2 * sizeof(int64_t), cmp_i64pair);
+    for (int i = 0; i < np; ++i) {
+        iv_push(&w->order_ckeys, pairs[2 * i]);
+        iv_push(&w->order_crank, pairs[2 * i + 1]);
+    }
+    free(pairs);
+}
+
+void or_set_body_xf(or_world* w, int id, real px, real py, real c, real sn) {
+    body_t* b = &w->b[id];
+    b->xf.p = V(px, py);
+    b->xf.q = V(c, sn);
 }
 int or_contact_count(const or_world* w) { return w->wcids.n; }
 void or_get_contact(const or_world* w, int k, int* io, real* fo, int* feat) {

@@ -132,6 +132,20 @@ void or_get_body(const or_world* w, int body, or_real* out13, int* awake);
 void or_set_body_state(or_world* w, int body, or_real px, or_real py, or_real angle,
                        or_real vx, or_real vy, or_real av);
 void or_get_local_center(const or_world* w, int body, or_real* out2);
+/* Test hook with no reference counterpart: replaces the body's transformation
+ * (p, q = cos sin) without touching its sweep, so that a parity check can give
+ * this world exactly the transformation another implementation computed from the
+ * same angle (the two sides' sin/cos may round differently).  Used on a body at
+ * rest in its sweep (pos0 == pos1) before the first step. */
+void or_set_body_xf(or_world* w, int body, or_real px, or_real py, or_real c, or_real s);
+/* Test hook with no reference counterpart: from the next step on, each island's
+ * warm start, velocity iterations and position iterations visit its contacts and
+ * joints interleaved in the order of items3 (n triples: (0, shape A, shape B) for
+ * the contact of two shapes, (1, joint, 0) for a joint) instead of the
+ * reference's order.  Used to check a solver that sweeps constraints in another
+ * valid Gauss-Seidel order (graph colours) against the same arithmetic in the
+ * same order.  n = 0 restores the reference's order. */
+void or_set_solve_order(or_world* w, int n, const int* items3);
 
 /* Contact queries.  Contacts are reported in the world's container order. */
 int or_contact_count(const or_world* w);

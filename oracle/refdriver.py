@@ -1,8 +1,10 @@
 """Runs scenes through the PlayRho reference compiled from source (oracle/ref).
 
-Available only where the reference sources are present (this container): the
-binaries live in oracle/_ref/ and are built by ``make -C oracle/ref``.  Used to
-check the oracle; never part of the shipped library.
+Available where the reference sources have been staged into oracle/_ref/src
+(``make -C oracle/ref stage PLAYRHO_REFERENCE=<checkout>``; git-ignored, never
+committed): the binaries live in oracle/_ref/ and are built from that copy by
+``make -C oracle/ref``.  Used to check the oracle and as the CPU baseline;
+never part of the shipped library.
 """
 from __future__ import annotations
 
@@ -13,11 +15,15 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-REF_SRC = os.environ.get("PLAYRHO_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_DIR, "src")  # the staged copy of the reference
+
+
+def staged() -> bool:
+    return os.path.isdir(os.path.join(REF_SRC, "Library", "source"))
 
 
 def available(double: bool = False) -> bool:
-    return os.path.exists(driver_path(double)) or os.path.isdir(os.path.join(REF_SRC, "Library"))
+    return os.path.exists(driver_path(double)) or staged()
 
 
 def driver_path(double: bool = False) -> str:
@@ -26,10 +32,19 @@ def driver_path(double: bool = False) -> str:
 
 def ensure_built(double: bool = False) -> str:
     path = driver_path(double)
-    if os.path.isdir(os.path.join(REF_SRC, "Library")) or not os.path.exists(path):
+    if staged() or not os.path.exists(path):
         # make relinks the driver when oracle/ref/ref_driver.cpp changed
-        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "-j8",
-                        "f64" if double else "f32", f"REF={REF_SRC}"], check=True)
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"-j{os.cpu_count() or 8}",
+                        "f64" if double else "f32"], check=True)
+    return path
+
+
+def ensure_bench_built() -> str:
+    """Builds the multi-world timing driver (oracle/ref/ref_bench.cpp)."""
+    path = os.path.join(REF_DIR, "ref_bench_f32")
+    if staged() or not os.path.exists(path):
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"-j{os.cpu_count() or 8}", "bench"],
+                       check=True)
     return path
 
 

@@ -31,7 +31,12 @@ __global__ void k_pre_proxies(DW d) {
         const uint32_t b = d.s_body[p];
         const uint32_t bf = d.b_flags[b];
         uint32_t moved = 0;
-        if (state == 2u) {
+        if (d.s_meta[p] & kShapeNoProxy) {
+            // no proxy: an inverted box, which overlaps nothing and leaves every
+            // union it enters unchanged
+            const float inf = __int_as_float(0x7f800000);
+            d.p_aabb[p] = make_float4(inf, inf, -inf, -inf);
+        } else if (state == 2u) {
             const Xf x0 = xf0_of(d, b), x1 = load_xf(d, b);
             d.p_aabb[p] = fat_box(d, swept_aabb(d, p, x0, x1), x0, x1);
             moved = 1u;
@@ -167,6 +172,7 @@ __global__ void k_lbvh_bounds_reset(DW d) {
 __global__ void k_lbvh_bounds(DW d) {
     if (!d.cnt->need_find || !d.cnt->lbvh_rebuild) return;
     GRID_LOOP(p, d.n_shapes) {
+        if (d.s_meta[p] & kShapeNoProxy) continue;
         const float4 a = d.p_aabb[p];
         const float cx = 0.5f * (a.x + a.z), cy = 0.5f * (a.y + a.w);
         const uint32_t w = d.b_world[d.s_body[p]];
@@ -182,7 +188,9 @@ __global__ void k_lbvh_morton(DW d) {
     if (!d.cnt->need_find || !d.cnt->lbvh_rebuild) return;
     GRID_LOOP(p, d.n_shapes) {
         const float4 a = d.p_aabb[p];
-        const float cx = 0.5f * (a.x + a.z), cy = 0.5f * (a.y + a.w);
+        // a shape without a proxy (inverted box) sorts to its world's corner
+        const bool none = (d.s_meta[p] & kShapeNoProxy) != 0u;
+        const float cx = none ? 0.f : 0.5f * (a.x + a.z), cy = none ? 0.f : 0.5f * (a.y + a.w);
         const uint32_t w = d.b_world[d.s_body[p]];
         const uint32_t* wb = reinterpret_cast<const uint32_t*>(&d.w_bounds[w]);
         const float bx0 = ordered_to_float(wb[0]), by0 = ordered_to_float(wb[1]);
@@ -397,7 +405,7 @@ __global__ void k_new_contacts(DW d) {
         const uint32_t fa = d.b_flags[ba], fb = d.b_flags[bb];
         d.cs_proxy[slot] = make_uint2(pa, pb);
         d.cs_body[slot] = make_uint2(ba, bb);
-        const bool sensor = ((d.s_meta[pa] | d.s_meta[pb]) & (1u << 16)) != 0u;
+        const bool sensor = ((d.s_meta[pa] | d.s_meta[pb]) & kShapeSensor) != 0u;
         uint32_t flags = CF_NEEDS_UPDATE;
         if (is_impenetrable(fa) || is_impenetrable(fb)) flags |= CF_IMPENETRABLE;
         if (sensor) flags |= CF_SENSOR;

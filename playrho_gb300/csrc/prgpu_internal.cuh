@@ -50,6 +50,10 @@ enum : uint32_t {
     CF_TOI_VALID = 16u,       // cs_toi holds this step's time of impact (Contact::e_toiFlag)
     CF_TOI_ISL = 32u,         // in the island of the current time-of-impact event
 };
+// Shape meta word: kind | vertex count << 8 | these bits.
+constexpr uint32_t kShapeSensor = 1u << 16;
+constexpr uint32_t kShapeNoProxy = 1u << 17;  // the shape's body was disabled at creation: no proxy
+
 // Bits 8..15 of the contact flags count the contact's TOI sub-steps this step.
 constexpr uint32_t kToiCountShift = 8u;
 constexpr uint32_t kToiCountMask = 0xffu << kToiCountShift;
@@ -65,6 +69,7 @@ constexpr int kSerialColour = 64;    // leftover constraints solved by one threa
 constexpr int kMaxPosIters = 32;
 constexpr int kColStride = kSerialColour + 2;  // colour table of one world: offsets 0..65
 constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr uint32_t kJointBit = 0x80000000u;  // constraint id of a joint (else a contact slot)
 constexpr uint32_t kNone = 0xffffffffu;
 
 // Velocity constraint of one contact (VelocityConstraint.hpp) as the solver
@@ -187,6 +192,9 @@ struct Counters {
     float st_toi_min_separation;
     float st_toi_max_inc_impulse;
     uint64_t seq_next;        // creation sequence number of the next new contact
+    uint32_t st_bodies_solved;  // dynamic bodies of the awake islands this step (body-steps)
+    uint32_t pad_solved;
+    uint64_t body_steps;      // st_bodies_solved summed over every step since creation
 };
 
 // Solver / step configuration in device memory (mirrors prgpu_step_conf).

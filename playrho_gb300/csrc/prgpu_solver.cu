@@ -26,8 +26,6 @@ namespace prgpu {
 
 namespace {
 
-constexpr uint32_t kJointBit = 0x80000000u;
-
 // ---- islands ----------------------------------------------------------------
 __device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x) {
     for (int g = 0; g < 1 << 20; ++g) {
@@ -91,12 +89,13 @@ __global__ void k_body_begin(DW d) {
     const DConf& c = *d.conf;
     const float h = c.deltaTime;
     const int np = c.regPositionIters;
-    uint32_t found = 0;
+    uint32_t found = 0, solved = 0;
     GRID_LOOP(b, d.n_bodies) {
         const uint32_t f = d.b_flags[b];
         const uint32_t r = d.b_island[b];
         if (!island_edge_body(f) || !d.isl_awake[r]) continue;
         d.b_flags[b] = f | BF_SOLVED | BF_AWAKE;
+        if (is_accelerable(f)) ++solved;
         const float4 p = d.b_pos1[b];
         d.b_pos0[b] = p;
         float4 v = d.b_vel[b];
@@ -138,6 +137,12 @@ __global__ void k_body_begin(DW d) {
         }
     }
     if (found) atomicAdd(&d.cnt->st_islands_found, found);
+    // body-steps: one per dynamic body of an awake island (warp sums, one atomic a warp)
+    solved = __reduce_add_sync(0xffffffffu, solved);
+    if ((threadIdx.x & 31u) == 0u && solved) {
+        atomicAdd(&d.cnt->st_bodies_solved, solved);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&d.cnt->body_steps), (unsigned long long)solved);
+    }
 }
 
 // ---- active constraints and colouring ---------------------------------------
@@ -2155,6 +2160,7 @@ __global__ void k_step_reset(DW d) {
     c->st_sum_pos_iters = 0u;
     c->st_min_separation = __int_as_float(0x7f800000);
     c->st_max_inc_impulse = 0.f;
+    c->st_bodies_solved = 0u;
     c->bar_count = 0u;
     c->st_toi_found = 0u;
     c->st_toi_islands_found = 0u;

@@ -36,6 +36,10 @@ struct prgpu_world {
     float* d_stage = nullptr;
     uint32_t* d_stage_u = nullptr;
     Counters* h_cnt = nullptr;  // pinned mirror of the device counters
+    // pinned copy of the device error word and site, written by every graph-replayed
+    // step as it ends (read by prgpu_step_async without waiting)
+    uint32_t* h_err = nullptr;
+    bool stepped = false;       // a step has run: proxies exist
     cudaEvent_t graph_ev[8] = {};  // recorded by the captured step between its phases
     std::vector<uint32_t> order_nb;  // body counts of the worlds in work-queue order
     struct AdjWindow* adj = nullptr;  // open StepAdjoint window, if any
@@ -349,7 +353,11 @@ int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
     vtx.reserve(V);
     for (uint32_t s = 0; s < S; ++s) {
         const int nv = (int)sv[s].size();
-        s_meta[s] = (uint32_t)ds->shape_kind[s] | ((uint32_t)nv << 8) | (ds->shape_filter[4 * s + 3] ? (1u << 16) : 0u);
+        // CreateBody / Attach queue a proxy only for a shape of an enabled body
+        // (AabbTreeWorld.cpp:1040, :1302): the shapes of a disabled body get none.
+        const bool no_proxy = !(hb[ds->shape_body[s]].flags & PRGPU_BODY_ENABLED);
+        s_meta[s] = (uint32_t)ds->shape_kind[s] | ((uint32_t)nv << 8) | (ds->shape_filter[4 * s + 3] ? kShapeSensor : 0u) |
+                    (no_proxy ? kShapeNoProxy : 0u);
         s_voff[s] = (uint32_t)vtx.size();
         // GetFwdNormalsVector (d2/Math.cpp)
         for (int i = 0; i < nv; ++i) {
@@ -562,6 +570,8 @@ int launch_step_graphs(prgpu_world* w, int n) {
             if (!w->graph_ev[k]) CU(cudaEventCreate(&w->graph_ev[k]));
         CU(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
         enqueue_step(w, true, w->graph_ev, true);
+        // the step's error word, for prgpu_step_async to read without waiting
+        cudaMemcpyAsync(w->h_err, &w->d.cnt->err, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream);
         cudaGraph_t g = nullptr;
         const cudaError_t e1 = cudaStreamEndCapture(w->stream, &g);
         if (e1 != cudaSuccess) return fail(w, PRGPU_ECUDA, "graph capture: %s", cudaGetErrorString(e1));
@@ -576,6 +586,7 @@ int launch_step_graphs(prgpu_world* w, int n) {
 int run_steps(prgpu_world* w, const prgpu_step_conf* conf, int n, bool sync) {
     int rc = set_conf(w, conf);
     if (rc) return rc;
+    if (n > 0) w->stepped = true;
     if (conf->deltaTime == 0.f) {
         for (int i = 0; i < n; ++i) enqueue_step(w, false);
         CU(cudaGetLastError());
@@ -902,6 +913,8 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     d.conf = w->d_conf;
     AL(w->d_stage, (size_t)N * 8 + 16);
     if (cudaMallocHost(&w->h_cnt, sizeof(Counters)) != cudaSuccess) return bail(PRGPU_ECUDA);
+    if (cudaMallocHost(&w->h_err, 2 * sizeof(uint32_t)) != cudaSuccess) return bail(PRGPU_ECUDA);
+    w->h_err[0] = w->h_err[1] = 0u;
     w->L.threads = 256;
     w->L.grid = w->L.prims.sm_count * 8;
     w->L.coop_threads = 256;
@@ -1003,6 +1016,7 @@ int prgpu_world_destroy(prgpu_world* w) {
         if (g) cudaGraphExecDestroy(g);
     for (void* p : w->allocs) cudaFree(p);
     if (w->h_cnt) cudaFreeHost(w->h_cnt);
+    if (w->h_err) cudaFreeHost(w->h_err);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
     return PRGPU_OK;
@@ -1040,6 +1054,7 @@ void fill_stats(const Counters& c, prgpu_step_stats* st) {
     st->toiRounds = c.toi_rounds;
     st->toiMinSeparation = c.st_toi_min_separation;
     st->toiMaxIncImpulse = c.st_toi_max_inc_impulse;
+    st->bodiesSolved = c.st_bodies_solved;
 }
 
 int prgpu_step(prgpu_world* w, const prgpu_step_conf* conf, prgpu_step_stats* st) {
@@ -1063,6 +1078,7 @@ int prgpu_step_profiled(prgpu_world* w, const prgpu_step_conf* conf, float* phas
     CU(cudaSetDevice(w->device));
     int rc = set_conf(w, conf);
     if (rc) return rc;
+    w->stepped = true;
     cudaEvent_t ev[kPhases + 1];
     for (int k = 0; k <= kPhases; ++k) CU(cudaEventCreate(&ev[k]));
     enqueue_step(w, conf->deltaTime != 0.f, ev);
@@ -1218,7 +1234,20 @@ int prgpu_get_sweep_mode(prgpu_world* w, int* mode) {
 int prgpu_step_async(prgpu_world* w, const prgpu_step_conf* conf, int n) {
     if (!w || n < 0) return PRGPU_EINVAL;
     CU(cudaSetDevice(w->device));
+    // an error of a step that has already finished (its graph copied the error
+    // word to pinned memory as it ended) stops the caller before more are queued
+    const volatile uint32_t* he = w->h_err;
+    if (he[0]) return fail(w, (int)he[0], "device error %u at site %u (an earlier step)", he[0], he[1]);
     return run_steps(w, conf, n, false);
+}
+
+int prgpu_get_body_steps(prgpu_world* w, uint64_t* total) {
+    if (!w || !total) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    CU(cudaMemcpyAsync(w->h_cnt, w->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    *total = w->h_cnt->body_steps;
+    return PRGPU_OK;
 }
 
 int prgpu_synchronize(prgpu_world* w) {
@@ -1282,6 +1311,15 @@ int prgpu_upload_body_states(prgpu_world* w, uint32_t first, uint32_t count, con
     return PRGPU_OK;
 }
 
+// Device scratch from cudaMallocAsync, freed on the stream on every return path.
+struct AsyncScratch {
+    void* p = nullptr;
+    cudaStream_t s = nullptr;
+    ~AsyncScratch() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
 int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
                             uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
                             uint32_t* features2) {
@@ -1295,10 +1333,10 @@ int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, 
     if (n == 0) return PRGPU_OK;
     // gather into one device scratch block, then copy out
     const size_t per = 2 + 2 + 1 + 2 + 4 + 8 + 2;  // 32-bit words per contact
-    void* scratch = nullptr;
-    CU(cudaMallocAsync(&scratch, per * 4 * (size_t)n, w->stream));
+    AsyncScratch scratch{nullptr, w->stream};
+    CU(cudaMallocAsync(&scratch.p, per * 4 * (size_t)n, w->stream));
     // 16-byte records first so every float4 store is aligned
-    float* g_hd = static_cast<float*>(scratch);
+    float* g_hd = static_cast<float*>(scratch.p);
     float* g_pt = g_hd + 4 * (size_t)n;
     uint32_t* g_pr = reinterpret_cast<uint32_t*>(g_pt + 8 * (size_t)n);
     uint32_t* g_bd = g_pr + 2 * (size_t)n;
@@ -1306,6 +1344,7 @@ int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, 
     int32_t* g_me = reinterpret_cast<int32_t*>(g_fl + n);
     uint32_t* g_ft = reinterpret_cast<uint32_t*>(g_me + 2 * (size_t)n);
     k_gather_contacts<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, n, g_pr, g_bd, g_fl, g_me, g_hd, g_pt, g_ft);
+    CU(cudaGetLastError());
     if (proxies2) CU(cudaMemcpyAsync(proxies2, g_pr, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     if (bodies2) CU(cudaMemcpyAsync(bodies2, g_bd, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     if (flags) CU(cudaMemcpyAsync(flags, g_fl, 4 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
@@ -1313,7 +1352,8 @@ int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, 
     if (head4) CU(cudaMemcpyAsync(head4, g_hd, 16 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     if (pts8) CU(cudaMemcpyAsync(pts8, g_pt, 32 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     if (features2) CU(cudaMemcpyAsync(features2, g_ft, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
-    CU(cudaFreeAsync(scratch, w->stream));
+    CU(cudaFreeAsync(scratch.p, w->stream));
+    scratch.p = nullptr;
     CU(cudaStreamSynchronize(w->stream));
     return PRGPU_OK;
 }
@@ -1328,22 +1368,23 @@ int prgpu_query_aabb(prgpu_world* w, uint32_t world, const float* aabb4, uint32_
     CU(cudaStreamSynchronize(w->stream));
     const uint32_t n = off[1] - off[0];
     if (n_out) *n_out = 0;
-    if (n == 0) return PRGPU_OK;
-    uint32_t* g = nullptr;
-    CU(cudaMallocAsync(reinterpret_cast<void**>(&g), 4 * ((size_t)n + 1), w->stream));
+    // The first step creates the proxies; before it the tree is empty (no overlaps).
+    if (n == 0 || !w->stepped) return PRGPU_OK;
+    AsyncScratch scratch{nullptr, w->stream};
+    CU(cudaMallocAsync(&scratch.p, 4 * ((size_t)n + 1), w->stream));
+    uint32_t* g = static_cast<uint32_t*>(scratch.p);
     CU(cudaMemsetAsync(g, 0, 4, w->stream));
     const float4 q = make_float4(aabb4[0], aabb4[1], aabb4[2], aabb4[3]);
     k_query_aabb<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, off[0], n, q, n, g + 1, g);
+    CU(cudaGetLastError());
     uint32_t found = 0;
     CU(cudaMemcpyAsync(&found, g, 4, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaStreamSynchronize(w->stream));
     if (n_out) *n_out = found;
-    if (found > capacity) {
-        CU(cudaFreeAsync(g, w->stream));
-        return fail(w, PRGPU_ECAPACITY, "%u overlaps exceed capacity %u", found, capacity);
-    }
+    if (found > capacity) return fail(w, PRGPU_ECAPACITY, "%u overlaps exceed capacity %u", found, capacity);
     if (found && shapes) CU(cudaMemcpyAsync(shapes, g + 1, 4 * (size_t)found, cudaMemcpyDeviceToHost, w->stream));
-    CU(cudaFreeAsync(g, w->stream));
+    CU(cudaFreeAsync(scratch.p, w->stream));
+    scratch.p = nullptr;
     CU(cudaStreamSynchronize(w->stream));
     if (shapes) std::sort(shapes, shapes + found);
     return PRGPU_OK;
@@ -1358,11 +1399,48 @@ int prgpu_download_contact_seq(prgpu_world* w, uint32_t capacity, uint32_t* n_ou
     if (n_out) *n_out = n;
     if (n > capacity) return fail(w, PRGPU_ECAPACITY, "%u contacts exceed capacity %u", n, capacity);
     if (n == 0 || !seq) return PRGPU_OK;
-    uint64_t* g = nullptr;
-    CU(cudaMallocAsync(reinterpret_cast<void**>(&g), 8 * (size_t)n, w->stream));
+    AsyncScratch scratch{nullptr, w->stream};
+    CU(cudaMallocAsync(&scratch.p, 8 * (size_t)n, w->stream));
+    uint64_t* g = static_cast<uint64_t*>(scratch.p);
     k_gather_seq<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, n, g);
+    CU(cudaGetLastError());
     CU(cudaMemcpyAsync(seq, g, 8 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
-    CU(cudaFreeAsync(g, w->stream));
+    CU(cudaFreeAsync(scratch.p, w->stream));
+    scratch.p = nullptr;
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+__global__ void k_gather_sweep_order(DW d, uint32_t n, int32_t* items3) {
+    GRID_LOOP(t, n) {
+        const uint32_t id = d.t_id[t];
+        int32_t* o = items3 + 3 * (size_t)t;
+        if (id & kJointBit) {
+            o[0] = 1; o[1] = (int32_t)(id & ~kJointBit); o[2] = 0;
+        } else {
+            const uint2 pr = d.cs_proxy[id];
+            o[0] = 0; o[1] = (int32_t)min(pr.x, pr.y); o[2] = (int32_t)max(pr.x, pr.y);
+        }
+    }
+}
+
+int prgpu_download_sweep_order(prgpu_world* w, uint32_t capacity, uint32_t* n_out, int32_t* items3) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    CU(cudaMemcpyAsync(w->h_cnt, w->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    const uint32_t n = w->stepped ? w->h_cnt->n_active : 0u;
+    if (n_out) *n_out = n;
+    if (n > capacity) return fail(w, PRGPU_ECAPACITY, "%u constraints exceed capacity %u", n, capacity);
+    if (n == 0 || !items3) return PRGPU_OK;
+    AsyncScratch scratch{nullptr, w->stream};
+    CU(cudaMallocAsync(&scratch.p, 12 * (size_t)n, w->stream));
+    int32_t* g = static_cast<int32_t*>(scratch.p);
+    k_gather_sweep_order<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, n, g);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(items3, g, 12 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaFreeAsync(scratch.p, w->stream));
+    scratch.p = nullptr;
     CU(cudaStreamSynchronize(w->stream));
     return PRGPU_OK;
 }

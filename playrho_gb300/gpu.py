@@ -52,7 +52,8 @@ class StepStats(ctypes.Structure):
         "bodiesSlept", "proxiesMoved", "sumPosIters", "liveContacts", "activeConstraints", "colours",
         "serialConstraints")] + [("minSeparation", ctypes.c_float), ("maxIncImpulse", ctypes.c_float)]
         + [(n, ctypes.c_uint32) for n in TOI_STATS]
-        + [("toiMinSeparation", ctypes.c_float), ("toiMaxIncImpulse", ctypes.c_float)])
+        + [("toiMinSeparation", ctypes.c_float), ("toiMaxIncImpulse", ctypes.c_float)]
+        + [("bodiesSolved", ctypes.c_uint32)])
 
 
 class BatchDesc(ctypes.Structure):
@@ -130,11 +131,15 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_adjoint_trim.argtypes = []
     lib.prgpu_autotune.argtypes = [P, ctypes.POINTER(StepConf), I, ctypes.POINTER(Schedule)]
     lib.prgpu_time_of_impact.argtypes = [I, U, P, P, P, P, ctypes.POINTER(StepConf), P, P]
+    lib.prgpu_get_body_steps.argtypes = [P, P]
+    lib.prgpu_download_sweep_order.argtypes = [P, U, P, P]
+    lib.prgpu_download_contacts_noalloc.argtypes = [P, U, P, P, P, P, P, P, P, P]
     _LIB = lib
     return lib
 
 
 def exported_symbols() -> List[str]:
+    """The entry points this binding uses (each one declared in include/prgpu.h)."""
     return [
         "prgpu_abi_version", "prgpu_default_step_conf", "prgpu_world_create", "prgpu_world_destroy",
         "prgpu_step", "prgpu_step_n", "prgpu_step_async", "prgpu_synchronize", "prgpu_get_counts",
@@ -144,7 +149,9 @@ def exported_symbols() -> List[str]:
         "prgpu_set_warp_world_max_bodies", "prgpu_get_warp_world_max_bodies", "prgpu_autotune",
         "prgpu_set_stage_bytes", "prgpu_get_stage_bytes", "prgpu_adjoint_begin", "prgpu_adjoint_forward",
         "prgpu_adjoint_backward", "prgpu_adjoint_tangent", "prgpu_adjoint_info", "prgpu_adjoint_end",
-        "prgpu_adjoint_profile", "prgpu_adjoint_trim", "prgpu_time_of_impact"]
+        "prgpu_adjoint_profile", "prgpu_adjoint_trim", "prgpu_time_of_impact", "prgpu_get_body_steps",
+        "prgpu_download_sweep_order", "prgpu_download_contacts_noalloc", "prgpu_download_contact_seq",
+        "prgpu_query_aabb"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -504,6 +511,21 @@ class GpuBatch:
         nout = ctypes.c_uint32()
         self._check(self.lib.prgpu_download_contact_seq(self.h, seq.size, ctypes.byref(nout), _ptr(seq)), "seq")
         return seq[:nout.value]
+
+    def body_steps(self) -> int:
+        """Dynamic bodies of awake islands summed over every step run so far."""
+        n = ctypes.c_uint64()
+        self._check(self.lib.prgpu_get_body_steps(self.h, ctypes.byref(n)), "prgpu_get_body_steps")
+        return int(n.value)
+
+    def sweep_order(self) -> np.ndarray:
+        """The last step's constraint sweep order: rows (0, shape A, shape B) for
+        contacts and (1, joint, 0) for joints, global indices."""
+        n = ctypes.c_uint32()
+        self._check(self.lib.prgpu_download_sweep_order(self.h, 0, ctypes.byref(n), None), "sweep order")
+        out = np.zeros((max(n.value, 1), 3), np.int32)
+        self._check(self.lib.prgpu_download_sweep_order(self.h, n.value, ctypes.byref(n), _ptr(out)), "sweep order")
+        return out[:n.value]
 
     def proxies(self) -> np.ndarray:
         a = np.zeros((self.n_shapes, 4), np.float32)

@@ -3,9 +3,10 @@
 Runs each scene through the reference compiled from source (oracle/ref, built
 with `make -C oracle/ref`) and stores, per fixture, the scene arrays and the
 reference's bodies, contacts and step statistics after the listed steps, with
-FP32 values kept bit-exact.  Needs the reference sources (PLAYRHO_REFERENCE,
-default /root/reference); the fixtures it writes are what the oracle is checked
-against wherever the sources are absent.
+FP32 values kept bit-exact.  Needs the reference sources staged into
+oracle/_ref/src (``make -C oracle/ref stage PLAYRHO_REFERENCE=<checkout>``);
+the fixtures it writes are what the oracle is checked against wherever the
+sources are absent.
 
     python tests/golden/make_golden.py [fixture names]
 """

@@ -11,6 +11,7 @@ Everything goes through the C ABI (libprgpu.so) via playrho_gb300.gpu.
 import numpy as np
 import pytest
 
+import parity_util as pu
 from oracle import oracle
 from playrho_gb300 import scenes
 from playrho_gb300.gpu import GpuBatch, default_conf
@@ -74,28 +75,112 @@ def test_free_fall_is_bit_exact(gpu_lib):
     assert_contacts_match(g.contacts(), ow.contacts())
 
 
+def _contacts_from_identical_transforms(batch, worlds, indices, min_contacts=1):
+    """Rebases worlds `indices` of a stepped batch onto fresh GPU and oracle worlds
+    with identical transforms (the oracle takes the GPU's), runs one zero-length
+    step on both (proxies, pair search and the first manifold update, as the
+    reference's first Step does) and compares every world's contacts."""
+    sample = pu.rebased_worlds(batch, worlds, indices)
+    g2 = GpuBatch(sample)
+    ows = pu.oracle_worlds_with_gpu_transforms(g2, sample)
+    g2.step(deltaTime=0.0)
+    for o in ows:
+        o.step(deltaTime=0.0)
+    per = pu.split_contacts(g2.contacts(), g2.shape_base)
+    gc = g2.contacts()
+    total = 0
+    for k, o in enumerate(ows):
+        pu.assert_world_contacts_match(gc, per[k], o.contacts(), what=f"world {indices[k]}")
+        total += len(per[k])
+    assert total >= min_contacts
+    return total
+
+
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_pair_sets_random_piles(gpu_lib, seed):
-    # Identical transforms on both sides (fresh worlds from the same state), then a
-    # zero-length step: proxies, pair sets and manifolds must match exactly.
+    # A settled pile rebased onto fresh worlds with identical transforms, then a
+    # zero-length step: pair sets and features exact, manifolds within 1e-5.
     rng = np.random.default_rng(seed)
     sc = scenes.pile(150, rng, width=6.0)
     g = GpuBatch([sc])
-    for _ in range(240):
+    g.step_n(240)
+    _contacts_from_identical_transforms(g, [sc], [0], min_contacts=20)
+
+
+def test_headline_batch_sample_matches_oracle(gpu_lib):
+    """The benchmark's batch (4096 worlds, log-uniform 16..2048 bodies, pyramids
+    and piles, seed 1) after its 240 settling steps: 64 of its worlds (every 64th,
+    so small and large, pyramids and piles) rebased onto identical transforms give
+    the oracle's pair sets, features and manifolds."""
+    worlds = scenes.batched_worlds(4096, seed=1)
+    g = GpuBatch(worlds)
+    g.step_n(240)
+    idx = list(range(0, 4096, 64))
+    n = _contacts_from_identical_transforms(g, worlds, idx, min_contacts=5000)
+    assert n >= 5000
+
+
+def crop(scene, keep):
+    """The bodies of `scene` with keep[body] true, with their shapes (no joints)."""
+    keep = np.asarray(keep, bool)
+    new_id = np.cumsum(keep) - 1
+    sk = keep[scene.shape_body]
+    sb = scenes.SceneBuilder()
+    for b in np.flatnonzero(keep):
+        sb.body(int(scene.body_type[b]), *(float(x) for x in scene.body_pos[b]), v=tuple(scene.body_vel[b]),
+                acc=tuple(scene.body_acc[b]), damp=tuple(scene.body_damp[b]), flags=int(scene.body_flags[b]))
+    for s in np.flatnonzero(sk):
+        vo, nv = int(scene.shape_voff[s]), int(scene.shape_nv[s])
+        sb._shape(int(new_id[scene.shape_body[s]]), int(scene.shape_kind[s]),
+                  [tuple(v) for v in scene.verts[vo:vo + nv]], float(scene.shape_radius[s]),
+                  float(scene.shape_density[s]), float(scene.shape_friction[s]),
+                  float(scene.shape_restitution[s]), tuple(int(x) for x in scene.shape_filter[s]))
+    return sb.build()
+
+
+def test_large_world_crop_matches_oracle(gpu_lib):
+    """The 100,000-shape box (1000 m, seed 0) after 60 steps, cropped to the
+    bodies left of x = +100 m (60 % of the box: below the reference's 65,534-body
+    limit) with the four walls, rebased onto identical transforms: pair sets,
+    features and manifolds as the oracle's."""
+    sc = scenes.large_box(100_000, 1000.0, seed=0)
+    g = GpuBatch([sc])
+    g.step_n(60)
+    b = g.bodies()
+    moved = pu.rebased(sc, b["pos"], b["vel"], b["local_center"])
+    keep = (moved.body_type == scenes.STATIC) | (moved.body_pos[:, 0] < 100.0)
+    cropped = crop(moved, keep)
+    assert 50_000 < cropped.n_bodies <= 65_534
+    g2 = GpuBatch([cropped])
+    _contacts_from_identical_transforms(g2, [cropped], [0], min_contacts=500)
+
+
+def test_disabled_body_has_no_proxy(gpu_lib):
+    """A body created disabled gets no proxies (AabbTreeWorld.cpp:1040): it has no
+    contacts although it overlaps others, and queries do not find its shapes."""
+    sb = scenes.SceneBuilder()
+    gnd = sb.body(scenes.STATIC, 0.0, 0.0)
+    sb.edge(gnd, (-10.0, 0.0), (10.0, 0.0))
+    a = sb.body(scenes.DYNAMIC, 0.0, 0.49, acc=scenes.GRAVITY)
+    sb.box(a, 0.5, 0.5, density=1.0)
+    off = sb.body(scenes.DYNAMIC, 0.3, 0.9, acc=scenes.GRAVITY,
+                  flags=scenes.BF_ALLOW_SLEEP | scenes.BF_AWAKE)  # not enabled
+    sb.disk(off, 0.5, density=1.0)
+    c = sb.body(scenes.DYNAMIC, 2.0, 0.45, acc=scenes.GRAVITY)
+    sb.disk(c, 0.5, density=1.0)
+    sc = sb.build()
+    g, ow = GpuBatch([sc]), oracle.OracleWorld(sc)
+    assert len(g.query_aabb(0, (-20.0, -20.0, 20.0, 20.0))) == 0  # before the first step: no proxies
+    for _ in range(3):
         g.step()
-    gb = g.bodies()
-    s2 = rebased(sc, np.stack([gb["pos"][:, 0], gb["pos"][:, 1], gb["pos"][:, 2]], 1), gb["vel"])
-    # positions above are centres of mass; the scene stores body origins
-    lc = gb["local_center"]
-    c, s = np.cos(gb["pos"][:, 2]), np.sin(gb["pos"][:, 2])
-    org = gb["pos"][:, :2] - np.stack([c * lc[:, 0] - s * lc[:, 1], s * lc[:, 0] + c * lc[:, 1]], 1)
-    s2.body_pos = np.ascontiguousarray(np.concatenate([org, gb["pos"][:, 2:3]], 1), dtype=np.float32)
-    g2, o2 = GpuBatch([s2]), oracle.OracleWorld(s2)
-    g2.step(deltaTime=0.0)
-    o2.step(deltaTime=0.0)
-    gc, oc = g2.contacts(), o2.contacts()
-    assert len(gc["proxy"]) > 20
-    assert_contacts_match(gc, oc, atol_scale=10.0)
+        ow.step()
+    gc, oc = g.contacts(), ow.contacts()
+    per = pu.split_contacts(gc, g.shape_base)
+    pu.assert_world_contacts_match(gc, per[0], oc, what="disabled body")
+    assert all(2 not in key for key in per[0])  # shape 2 belongs to the disabled body
+    found = set(g.query_aabb(0, (-20.0, -20.0, 20.0, 20.0)).tolist())
+    assert found == {0, 1, 3}
+    np.testing.assert_array_equal(g.bodies()["pos"][off], ow.bodies()["pos"][off])
 
 
 def test_pyramid_long_run_settles(gpu_lib):

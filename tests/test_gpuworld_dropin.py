@@ -18,7 +18,7 @@ from playrho_gb300 import build
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "playrho_gb300")
-REF = os.environ.get("PLAYRHO_REFERENCE", "/root/reference")
+REF = os.path.join(ROOT, "oracle", "_ref", "src")  # the staged reference (oracle/ref/Makefile stage)
 REF_LIB = os.path.join(ROOT, "oracle", "_ref", "f32", "libPlayRho.a")
 REF_GEN = os.path.join(ROOT, "oracle", "_ref", "f32", "gen")
 

@@ -45,6 +45,15 @@ def test_chains():
     _compare(scenes.chains_world(np.random.default_rng(9), n_free=60, n_chains=3, links=6), [1, 80])
 
 
+def test_disabled_bodies_have_no_proxies():
+    # every fifth body of a pile is created disabled: the reference gives its shapes
+    # no proxies (AabbTreeWorld.cpp:1040), so the proxy ranks, the contacts and the
+    # steps follow without them
+    sc = scenes.pile(120, np.random.default_rng(13))
+    sc.body_flags[1::5] &= ~np.uint32(scenes.BF_ENABLED)
+    _compare(sc, [1, 40, 90])
+
+
 @pytest.mark.parametrize("seed", [21, 22])
 def test_toi_bullets(seed):
     _compare(scenes.bullets(50, np.random.default_rng(seed)), [1, 20, 60], doToi=1)
