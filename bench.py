@@ -4,6 +4,11 @@ Default workload: 4096 independent worlds (body counts log-uniform in [16, 2048]
 half box pyramids, half piles of disks and 3-8-gons, seed 1; ~1.6 M bodies)
 advanced together in one CUDA-graph step (dt 1/60, 8/3 iterations, float32).
 
+A body-step is one awake dynamic body advanced one step (the device counts the
+dynamic bodies of awake islands; sleeping bodies are not counted).  Every arm
+runs the same untimed steps first (settling, autotuning, warm-up), so all of
+them time the same state of the simulation.
+
   value : body-steps/s of the batched step, inputs resident in HBM, device time
           from CUDA events the captured step graph records around its phases
   e2e   : the same metric through the C ABI with host buffers: every step
@@ -11,13 +16,14 @@ advanced together in one CUDA-graph step (dt 1/60, 8/3 iterations, float32).
           back, all inside the host-timed region
   roofline : the Gauss-Seidel sweep kernel (the dominant phase), algorithmic
           bytes per launch over its live CUDA-event duration vs measured HBM peak
-  cpu_baseline : the CPU oracle (a restatement of the reference step, pinned bit
-          for bit to the reference) on one host core, on a bounded sample
+  cpu_baseline : the reference's own step (its library built from the staged
+          sources; the oracle port where they are absent) on one host core, on
+          every 64th world
 
-``--impl reference`` times the reference's CPU step on the host's cores (the
-oracle port, one process per core) on the same workload and prints the same
-metric.  Multi-GPU (torchrun): each rank advances its own copy of the batch
-(worlds are independent; no collective on the data path), scaling "weak".
+``--impl reference`` times the reference's CPU step on all host cores (one
+process per core, every world of the workload) and prints the same metric.
+Multi-GPU (torchrun): each rank advances its own copy of the batch (worlds are
+independent; no collective on the data path), scaling "weak".
 """
 from __future__ import annotations
 
@@ -195,79 +201,148 @@ def sweep_bytes(stats, conf, n_bodies_solved):
     return nc * per_contact + n_bodies_solved * 52
 
 
-def cpu_baseline_sample(worlds, overrides=None, seconds=8.0):
-    """Times the single-threaded oracle on a bounded sample of the workload."""
-    from oracle import oracle
-
-    overrides = overrides or {}
-    sample = worlds[: max(1, len(worlds) // 16)]
-    ows = [oracle.OracleWorld(w) for w in sample]
-    for o in ows:
-        o.step(**overrides)
-    nb = sum(int((w.body_type == 2).sum()) for w in sample)
-    steps = 0
-    t0 = time.perf_counter()
-    while True:
-        for o in ows:
-            o.step(**overrides)
-        steps += 1
-        if time.perf_counter() - t0 > seconds or steps >= 200:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": nb * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{len(sample)} of {len(worlds)} worlds ({nb} dynamic bodies), {steps} steps after 1 warm-up, "
-                      f"{dt:.1f} s, oracle FP32 (bit-exact restatement of the reference step)"}
+# prgpu_autotune times 16 candidate schedules (the grid-wide one, then 3 staging
+# sizes x 5 warp-world limits), each over one capturing step plus the steps asked
+# for; those steps advance the batch like any other.
+AUTOTUNE_CANDIDATES = 16
+AUTOTUNE_STEPS = 2
 
 
-def _ref_worker(args):
-    """Process-pool worker: builds its share of worlds in the oracle and steps them."""
-    idx, n_worlds, steps, warmup = args
+def steps_before_timing(args) -> int:
+    """Steps every arm runs on the workload before its timed steps: the settling
+    steps, the autotuner's steps and the warm-up steps, so that all arms time the
+    same state of the simulation."""
+    tune = AUTOTUNE_CANDIDATES * (1 + AUTOTUNE_STEPS) if args.sweeps == "auto" else 0
+    return args.settle + tune + max(3, args.warmup)
+
+
+def balanced_shares(worlds, parts):
+    """Splits world indices into `parts` shares of about equal body counts
+    (largest world first into the lightest share)."""
+    order = sorted(range(len(worlds)), key=lambda i: -worlds[i].n_bodies)
+    shares = [[] for _ in range(parts)]
+    load = [0] * parts
+    for i in order:
+        k = load.index(min(load))
+        shares[k].append(i)
+        load[k] += worlds[i].n_bodies
+    return [sorted(s) for s in shares if s]
+
+
+def _port_worker(idx, workload_args, pre, steps, overrides, barrier, out):
+    """Oracle-port process: builds its share of the workload's worlds, runs the
+    untimed steps, waits for the other processes, then times its steps."""
     sys.path.insert(0, ROOT)
     from oracle import oracle
-    from playrho_gb300 import scenes
 
-    worlds = scenes.batched_worlds(n_worlds, seed=1)
-    mine = [worlds[i] for i in idx]
-    ows = [oracle.OracleWorld(w) for w in mine]
-    for _ in range(warmup):
-        for o in ows:
-            o.step()
-    nb = sum(int((w.body_type == 2).sum()) for w in mine)
-    t0 = time.perf_counter()
+    worlds = workload(workload_args)
+    mine = [(oracle.OracleWorld(worlds[i]), worlds[i].body_type == 2) for i in idx]
+    for _ in range(pre):
+        for o, _dyn in mine:
+            o.step(**overrides)
+    barrier.wait()
+    seconds, body_steps = 0.0, 0
     for _ in range(steps):
-        for o in ows:
-            o.step()
-    return nb, time.perf_counter() - t0
+        for o, dyn in mine:
+            body_steps += int(((o.bodies()["awake"] != 0) & dyn).sum())
+            t0 = time.perf_counter()
+            o.step(**overrides)
+            seconds += time.perf_counter() - t0
+    out.put((seconds, body_steps))
+
+
+def cpu_step_runs(args, worlds, idx_shares, pre, steps, overrides):
+    """Times the reference's CPU step on shares of the workload, one process per
+    share, all processes starting their timed steps together.  Uses the
+    reference's own library (oracle/_ref/ref_bench_f32, built from the staged
+    reference sources) where it can be built, else the oracle port.  Returns
+    (kind, [(seconds, awake body-steps), ...])."""
+    from oracle import refdriver
+
+    if refdriver.staged():
+        try:
+            exe = refdriver.ensure_bench_built()
+        except Exception as e:  # the reference does not build on this host: use the port
+            print(f"reference bench driver not built ({e}); timing the oracle port", file=sys.stderr)
+            exe = None
+        if exe:
+            from playrho_gb300 import scenes
+
+            conf = "".join(f"conf {k} {float(v)!r}\n" for k, v in overrides.items())
+            procs = []
+            for share in idx_shares:
+                p = subprocess.Popen([exe], stdin=subprocess.PIPE, stdout=subprocess.PIPE, text=True)
+                text = "".join("world\n" + scenes.scene_text(worlds[i]) for i in share)
+                p.stdin.write(text + conf + f"run {pre}\nready\n")
+                p.stdin.flush()
+                procs.append(p)
+            for p in procs:
+                line = p.stdout.readline().split()
+                if not line or line[0] != "ready":
+                    raise RuntimeError("reference bench driver failed")
+            for p in procs:
+                p.stdin.write(f"go\ntime {steps}\n")
+                p.stdin.flush()
+            res = []
+            for p in procs:
+                r = p.stdout.readline().split()
+                p.stdin.close()
+                p.wait()
+                res.append((float(r[1]), int(r[2])))
+            return "reference", res
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(len(idx_shares))
+    q = ctx.Queue()
+    wargs = argparse.Namespace(**{k: getattr(args, k) for k in ("workload", "worlds")})
+    procs = [ctx.Process(target=_port_worker, args=(s, wargs, pre, steps, overrides, barrier, q)) for s in idx_shares]
+    for p in procs:
+        p.start()
+    res = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+    return "port", res
+
+
+def cpu_sample_desc(kind, n_worlds, n_sample, procs, pre, steps):
+    what = ("the reference's library (Step over each world)" if kind == "reference"
+            else "the oracle port (bit-exact restatement of the reference step), the reference sources being absent")
+    return (f"{n_sample} of {n_worlds} worlds on {procs} process{'es' if procs > 1 else ''}, {steps} timed steps "
+            f"after {pre} untimed ones (the GPU arm's settling, autotuning and warm-up steps), {what}; "
+            f"body-steps = awake dynamic bodies before each step")
 
 
 def run_reference(args, rank):
-    """The reference's CPU step on all host cores (oracle port), same workload and metric."""
-    import multiprocessing as mp
-
+    """The reference's CPU step on the host's cores: the same worlds, the same
+    untimed steps before timing, the same metric (awake body-steps/s).  Under
+    torchrun only rank 0 runs it."""
     if rank != 0:
         return
+    desc, overrides, settle = WORKLOADS[args.workload]
+    if args.settle is None:
+        args.settle = settle
+    if args.toi:
+        overrides = dict(overrides, doToi=1)
+    worlds = workload(args)
+    pre = steps_before_timing(args)
     cores = os.cpu_count() or 1
-    n_worlds = args.worlds
-    # one bounded sample per process: a slice of the worlds, `steps` steps each
-    per = max(1, min(n_worlds // cores, 64))
-    idx_all = list(range(n_worlds))
-    shares = [idx_all[c::cores][:per] for c in range(cores)]
-    steps = max(1, min(args.steps, 5))
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_ref_worker, [(s, n_worlds, steps, min(args.warmup, 1)) for s in shares])
-    nb = sum(r[0] for r in res)
-    tmax = max(r[1] for r in res)
-    value = nb * steps / tmax
+    shares = balanced_shares(worlds, cores)
+    kind, res = cpu_step_runs(args, worlds, shares, pre, args.steps, overrides)
+    tmax = max(r[0] for r in res)
+    body_steps = sum(r[1] for r in res)
+    value = body_steps / tmax
     out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-           "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": tmax / steps * 1e3,
+           "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": tmax / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic",
-           "config": {"workload": f"batched worlds: {n_worlds} worlds, log-uniform 16..2048 bodies, seed 1",
-                      "sample": f"{sum(len(s) for s in shares)} worlds on {cores} processes"},
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": f"{sum(len(s) for s in shares)} of {n_worlds} worlds, {steps} steps, "
-                                      f"one oracle process per core (reference sources are not on this host)"},
+           "config": {"workload": desc.format(n=len(worlds)), "worlds": len(worlds),
+                      "dynamic_bodies": sum(w.n_dynamic() for w in worlds),
+                      "awake_body_steps_per_step": body_steps / args.steps,
+                      "steps_before_timing": pre, "processes": len(shares)},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": len(shares), "kind": kind,
+                            "sample": cpu_sample_desc(kind, len(worlds), len(worlds), len(shares), pre,
+                                                      args.steps)},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -296,12 +371,13 @@ def run_ours(args, rank, world_size, local, dist):
     if args.sweeps == "auto":
         # the autotuner times each candidate sweep schedule on the settled batch
         # (those steps advance it, like settling steps) and keeps the fastest
-        schedule = batch.autotune(2, conf)
+        schedule = batch.autotune(AUTOTUNE_STEPS, conf)
     for _ in range(max(3, args.warmup)):
         batch.step_n(1, conf)
     barrier(dist)
     step_ms, phases = [], []
     nvtx = nvtx_ranges()
+    body_steps0 = batch.body_steps()
     with Clocks(local) as clk:
         nvtx[0]("timed")  # a profiler can select the timed steps by this range
         for _ in range(args.steps):
@@ -321,12 +397,15 @@ def run_ours(args, rank, world_size, local, dist):
         batch.synchronize()
         nvtx[1]()
     barrier(dist)
+    # body-steps: the dynamic bodies of awake islands in each timed step, counted
+    # on the device (sleeping bodies are not counted)
+    timed_body_steps = batch.body_steps() - body_steps0
     total_s = max_over_ranks(dist, sum(step_ms) / 1e3)
-    value = world_size * n_dyn * args.steps / total_s
+    value = world_size * timed_body_steps / total_s
     # statistics of one more step (outside the timed region) for the roofline bytes
     _, st = batch.step_profiled(conf)
     sweeps_ms = statistics.mean(p["sweeps"] for p in phases)
-    n_solved = n_dyn  # every dynamic body of an awake island is integrated
+    n_solved = st["bodiesSolved"]  # bodies integrated by the sweep kernel in that step
     bytes_sweep = sweep_bytes(st, conf, n_solved)
     peak, peak_kind = measured_peaks()
     achieved = bytes_sweep / (sweeps_ms / 1e3) / 1e9
@@ -353,34 +432,55 @@ def run_ours(args, rank, world_size, local, dist):
     pp, vp = ctypes.c_void_p(pos_h.data_ptr()), ctypes.c_void_p(vel_h.data_ptr())
     e2e_steps = max(3, args.steps // 2)
     barrier(dist)
+    e2e_bs0 = batch.body_steps()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         batch._check(lib.prgpu_upload_body_states(batch.h, 0, nb, pp, vp), "upload")
         batch._check(lib.prgpu_step_n(batch.h, ctypes.byref(conf), 1), "step")
         batch._check(lib.prgpu_download_bodies(batch.h, pp, vp, None, None, None, None), "download")
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
-    e2e_value = world_size * n_dyn * e2e_steps / e2e_s
+    e2e_value = world_size * (batch.body_steps() - e2e_bs0) / e2e_s
 
-    # the plain single-world GPU step on a sample of the same worlds (one world per call)
+    # The plain single-world GPU step on a sample of the same worlds in the same
+    # state (one world per handle and per call): each sampled world is rebuilt from
+    # the batch's current bodies (positions, velocities, sleep), then 3 untimed
+    # steps find its contacts again and restore warm starting before 10 timed ones.
     plain = None
     if rank == 0:
-        sample = worlds[:: max(1, len(worlds) // 48)][:48]
-        singles = [gpu.GpuBatch([w], device=local) for w in sample]
+        from playrho_gb300 import scenes
+
+        every = max(1, len(worlds) // 48)
+        idx = list(range(0, len(worlds), every))[:48]
+        bnow = batch.bodies()
+        singles = []
+        for i in idx:
+            lo, hi = int(batch.body_base[i]), int(batch.body_base[i + 1])
+            singles.append(gpu.GpuBatch([scenes.rebase(worlds[i], bnow["pos"][lo:hi], bnow["vel"][lo:hi],
+                                                       bnow["local_center"][lo:hi], bnow["awake"][lo:hi])],
+                                        device=local))
         for s in singles:
             s.step_n(3, conf)
-        nsb = sum(int((w.body_type == 2).sum()) for w in sample)
+        bs0 = sum(s.body_steps() for s in singles)
         t0 = time.perf_counter()
         for _ in range(10):
             for s in singles:
                 s.step_n(1, conf)
         plain_dt = time.perf_counter() - t0
-        plain = nsb * 10 / plain_dt
+        plain = (sum(s.body_steps() for s in singles) - bs0) / plain_dt
         for s in singles:
             s.close()
 
     if rank != 0:
         return
-    cpu = None if args.no_cpu_baseline else cpu_baseline_sample(worlds, overrides)
+    cpu = None
+    if not args.no_cpu_baseline:
+        # the reference's step on one core, on every 64th world of the workload, after
+        # the same untimed steps as the timed region of this arm
+        sample = list(range(0, len(worlds), 64 if len(worlds) >= 256 else max(1, len(worlds) // 4)))
+        pre = steps_before_timing(args)
+        kind, res = cpu_step_runs(args, worlds, [sample], pre, args.steps, overrides)
+        cpu = {"value": res[0][1] / res[0][0], "unit": UNIT, "cores": 1, "kind": kind,
+               "sample": cpu_sample_desc(kind, len(worlds), len(sample), 1, pre, args.steps)}
     clocks = clk.summary()
     # DRAM bytes of one solver launch on this workload, from the ncu capture
     # summarised in profiles/ (a profiler run is never part of the bench)
@@ -399,10 +499,13 @@ def run_ours(args, rank, world_size, local, dist):
         "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc.format(n=len(worlds)), "worlds": len(worlds), "dynamic_bodies": n_dyn,
+                   "awake_bodies": timed_body_steps / args.steps,
+                   "asleep_bodies": n_dyn - timed_body_steps / args.steps,
+                   "body_step": "one awake dynamic body advanced one step (sleeping bodies not counted)",
                    "dt": f"1/{round(1.0 / conf.deltaTime)}",
                    "iterations": f"{conf.regVelocityIters}/{conf.regPositionIters}",
                    "parallelism": f"replicas x{world_size}",
-                   "settle_steps": args.settle,
+                   "settle_steps": args.settle, "steps_before_timing": steps_before_timing(args),
                    "l2": "working set > 129 MB L2 (no flush needed)",
                    "live_contacts": st["liveContacts"], "active_constraints": st["activeConstraints"],
                    "colours": st["colours"], "serial_constraints": st["serialConstraints"],
@@ -424,7 +527,7 @@ def run_ours(args, rank, world_size, local, dist):
     }
     out["gpu_launches"] = launches_per_step(batch) * args.steps
     if args.workload == "batched" and not args.no_toi:
-        out["toi"] = toi_bench(batch, overrides, local, n_dyn)
+        out["toi"] = toi_bench(args, batch, overrides, local)
     if args.workload == "batched" and not args.no_adjoint:
         out["adjoint"] = adjoint_bench(local)
     if args.workload == "chains256" and not args.no_adjoint:
@@ -442,58 +545,52 @@ def _timed_steps(batch, conf, steps):
     return time.perf_counter() - t0, stats
 
 
-def toi_bench(batch, overrides, device, n_dyn, steps=10, n_bullet_worlds=1024, bullet_steps=20):
+def toi_bench(args, batch, overrides, device, steps=10, n_bullet_worlds=1024, bullet_steps=20):
     """The step with the time-of-impact phase on (StepConf::doToi, the reference's
     default).  (1) The settled headline batch: body-steps/s with and without the
     TOI phase, its rounds and events per step.  (2) A TOI-heavy batch: 1024 worlds
     of 40 fast disks and polygons (60-180 m/s, half of them bullets) in closed
-    15 m boxes, with the single-threaded CPU oracle on a sample of it beside it.
+    15 m boxes, with the reference's step on one core on a sample of it beside it.
     Host clock around synchronous prgpu_step calls (the TOI loop reads the device
-    counters between rounds, so these steps are not graph replays)."""
+    counters between rounds, so these steps are not graph replays).  Body-steps
+    count awake dynamic bodies."""
     from playrho_gb300 import gpu, scenes
 
     off = gpu.default_conf(**overrides)
     on = gpu.default_conf(**overrides, doToi=1)
     for c in (on, off):
         _timed_steps(batch, c, 2)
+    bs0 = batch.body_steps()
     t_on, st_on = _timed_steps(batch, on, steps)
+    bs_on = batch.body_steps() - bs0
     t_off, _ = _timed_steps(batch, off, steps)
     rounds = [s["toiRounds"] for s in st_on]
     headline = {
-        "value": n_dyn * steps / t_on, "unit": UNIT, "ms_per_step": t_on / steps * 1e3,
+        "value": bs_on / t_on, "unit": UNIT, "ms_per_step": t_on / steps * 1e3,
         "without_toi_ms_per_step": t_off / steps * 1e3,
         "toi_rounds_per_step": statistics.mean(rounds), "toi_events_per_step":
             statistics.mean(s["toiContactsFound"] for s in st_on),
         "toi_computed_per_step": statistics.mean(s["toiContactsUpdatedToi"] for s in st_on)}
     rng = np.random.default_rng(9)
     worlds = [scenes.bullets(40, rng, size=15.0) for _ in range(n_bullet_worlds)]
-    nb = sum(int((w.body_type == 2).sum()) for w in worlds)
     g = gpu.GpuBatch(worlds, device=device)
     _timed_steps(g, on, 3)
+    bs0 = g.body_steps()
     t_b, st_b = _timed_steps(g, on, bullet_steps)
+    bs_b = g.body_steps() - bs0
     g.close()
-    from oracle import oracle
-
-    sample = worlds[:16]
-    ows = [oracle.OracleWorld(w) for w in sample]
-    for o in ows:
-        for _ in range(3):
-            o.step(doToi=1)
-    nbs = sum(int((w.body_type == 2).sum()) for w in sample)
-    t0 = time.perf_counter()
-    for _ in range(bullet_steps):
-        for o in ows:
-            o.step(doToi=1)
-    t_cpu = time.perf_counter() - t0
+    targs = argparse.Namespace(workload="bullets1024", worlds=n_bullet_worlds)
+    kind, res = cpu_step_runs(targs, worlds, [list(range(16))], 3, bullet_steps, {"doToi": 1})
     bullets = {
-        "value": nb * bullet_steps / t_b, "unit": UNIT, "ms_per_step": t_b / bullet_steps * 1e3,
+        "value": bs_b / t_b, "unit": UNIT, "ms_per_step": t_b / bullet_steps * 1e3,
         "workload": f"{n_bullet_worlds} worlds x 40 fast disks and 3..8-gons (60..180 m/s, half bullets) in a "
                     f"closed 30 m box, seed 9, steps 4..{3 + bullet_steps}",
         "toi_rounds_per_step": statistics.mean(s["toiRounds"] for s in st_b),
         "toi_events_per_step": statistics.mean(s["toiContactsFound"] for s in st_b),
         "toi_computed_per_step": statistics.mean(s["toiContactsUpdatedToi"] for s in st_b),
-        "cpu_baseline": {"value": nbs * bullet_steps / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"16 of {n_bullet_worlds} worlds, {bullet_steps} steps with doToi, oracle FP32"}}
+        "cpu_baseline": {"value": res[0][1] / res[0][0], "unit": UNIT, "cores": 1, "kind": kind,
+                         "sample": cpu_sample_desc(kind, n_bullet_worlds, 16, 1, 3, bullet_steps)
+                         + ", time-of-impact phase on"}}
     return {"headline_batch": headline, "bullets": bullets,
             "timing": "host clock around synchronous steps (the TOI loop syncs between rounds)"}
 

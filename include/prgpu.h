@@ -329,7 +329,7 @@ int prgpu_download_proxies(prgpu_world* w, float* aabb4);
  * (ContactSolver.cpp, AabbTreeWorld.cpp:1563-1683); this order is a valid
  * Gauss-Seidel order of the same constraints (graph colours), reported so that
  * parity checks can replay it.  Valid after a step without the time-of-impact
- * phase, until the next step. */
+ * phase, until the next step.  With items3 NULL only *n_out is set. */
 int prgpu_download_sweep_order(prgpu_world* w, uint32_t capacity, uint32_t* n_out, int32_t* items3);
 /* Runs the host-side part of prgpu_world_create (validation, mass data as
  * Attach(..., resetMassData = true) leaves it) without a GPU: centre-of-mass

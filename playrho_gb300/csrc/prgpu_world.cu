@@ -1431,8 +1431,8 @@ int prgpu_download_sweep_order(prgpu_world* w, uint32_t capacity, uint32_t* n_ou
     CU(cudaStreamSynchronize(w->stream));
     const uint32_t n = w->stepped ? w->h_cnt->n_active : 0u;
     if (n_out) *n_out = n;
+    if (n == 0 || !items3) return PRGPU_OK;  // a count-only call
     if (n > capacity) return fail(w, PRGPU_ECAPACITY, "%u constraints exceed capacity %u", n, capacity);
-    if (n == 0 || !items3) return PRGPU_OK;
     AsyncScratch scratch{nullptr, w->stream};
     CU(cudaMallocAsync(&scratch.p, 12 * (size_t)n, w->stream));
     int32_t* g = static_cast<int32_t*>(scratch.p);

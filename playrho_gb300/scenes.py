@@ -492,6 +492,26 @@ def large_box(n_shapes: int = 100_000, size: float = 1000.0, seed: int = 0) -> S
     return sc
 
 
+def rebase(scene: Scene, pos_com, vel, local_center, awake=None) -> Scene:
+    """The scene with each body moved to a state read back from a world: centre of
+    mass position (x y angle), velocity and, when given, whether it is awake.  The
+    scene stores body origins, so the local centre is rotated back out; a sleeping
+    body is created asleep (BodyConf::awake false)."""
+    s = Scene(**{f: getattr(scene, f) for f in scene.__dataclass_fields__})
+    pos_com = np.asarray(pos_com, np.float64)
+    lc = np.asarray(local_center, np.float64)
+    c, sn = np.cos(pos_com[:, 2]), np.sin(pos_com[:, 2])
+    org = pos_com[:, :2] - np.stack([c * lc[:, 0] - sn * lc[:, 1], sn * lc[:, 0] + c * lc[:, 1]], 1)
+    s.body_pos = np.ascontiguousarray(np.concatenate([org, pos_com[:, 2:3]], 1), dtype=F32)
+    s.body_vel = np.ascontiguousarray(vel, dtype=F32)
+    if awake is not None:
+        flags = s.body_flags.copy()
+        asleep = (np.asarray(awake) == 0) & (s.body_type != STATIC)
+        flags[asleep] &= ~np.uint32(BF_AWAKE)
+        s.body_flags = flags
+    return s
+
+
 def pile(n_bodies: int, rng, friction=0.6, density=1.0, width=None) -> Scene:
     """Random pile of disks and 3-8-gons (bounding radius U[0.1,0.5]) dropped from
     heights U[1,50] m onto a static edge."""

@@ -12,14 +12,8 @@ RTOL = 1e-5
 
 def rebased(scene, pos_com, vel, lc):
     """The scene with each body moved to a centre-of-mass position pos_com (x y
-    angle) and velocity; the scene stores body origins, so the local centre lc is
-    rotated back out."""
-    s = scenes.Scene(**{f: getattr(scene, f) for f in scene.__dataclass_fields__})
-    c, sn = np.cos(pos_com[:, 2]), np.sin(pos_com[:, 2])
-    org = pos_com[:, :2] - np.stack([c * lc[:, 0] - sn * lc[:, 1], sn * lc[:, 0] + c * lc[:, 1]], 1)
-    s.body_pos = np.ascontiguousarray(np.concatenate([org, pos_com[:, 2:3]], 1), dtype=np.float32)
-    s.body_vel = np.ascontiguousarray(vel, dtype=np.float32)
-    return s
+    angle) and velocity (scenes.rebase)."""
+    return scenes.rebase(scene, pos_com, vel, lc)
 
 
 def rebased_worlds(batch, scenes_, indices):

@@ -203,3 +203,112 @@ def test_joint_gradient_against_finite_differences_of_the_fp64_oracle(gpu_lib):
     print(f"\nd(tip x)/d(disk vx): adjoint {ad_v:.6f} fd {fd_v:.6f}; d/d(disk x): adjoint {ad_x:.6f} fd {fd_x:.6f}")
     assert abs(ad_v - fd_v) <= 1e-3 * max(abs(fd_v), 1e-3) + 1e-4
     assert abs(ad_x - fd_x) <= 1e-3 * max(abs(fd_x), 1e-3) + 1e-4
+
+
+# ---- the differentiable workload: 64 pushing worlds, checkpoint every 16 -------
+PUSH_CONF = dict(regVelocityIters=200, regPositionIters=30, minStillTimeToSleep=1e9, regMinSeparation=-1e-9)
+
+
+def _push_targets(n):
+    rng = np.random.default_rng(2)
+    return np.stack([rng.uniform(10, 30, n), rng.uniform(0, 2, n)], 1)
+
+
+def _push_loss(pos, targets, k):
+    m = np.asarray(pos, np.float64)[2:34, :2].mean(0)  # ground, disk, then the 32 boxes
+    return float(((m - targets[k]) ** 2).sum())
+
+
+@pytest.mark.parametrize("steps", [60, 240])
+def test_push_workload_gradients_against_fp64_finite_differences(gpu_lib, steps):
+    """The differentiable workload: 64 worlds (a disk pushing 32 boxes on a ground,
+    all with friction mu, seed 2), checkpoint every 16 steps, loss = squared
+    distance of each world's mean box centre from its target in [10,30]x[0,2].
+    d(loss)/d(disk initial velocity x, y) and d(loss)/d(mu) from StepAdjoint on
+    the whole batch, against central differences (h = 1e-4) of the FP64 oracle.
+
+    mu is every shape's friction, so MixFriction (sqrt(f1 f2), Contact.hpp:57)
+    gives mu for every contact and d(loss)/d(mu) is the sum of the adjoint's
+    d(loss)/d(shape friction) over the world's shapes.
+
+    Solved to convergence (200 velocity, 30 position iterations, no sleep), and
+    the FP64 oracle replays, step by step, the Gauss-Seidel order the GPU swept
+    (prgpu_download_sweep_order): the position solver's result depends on the
+    order (its fixed points are not unique), and over hundreds of steps that
+    difference would otherwise dominate.
+
+    The loss is only piecewise smooth: contacts begin and end, and friction
+    switches between sticking and sliding, at parameter values that a 1e-4 step
+    can straddle; across such a point no derivative exists and a central
+    difference means nothing.  So every 4th world is checked (16 of 64), and a
+    (world, parameter) pair counts where the central differences at h and h/2
+    agree within 1e-4 (the loss is smooth there); every pair that counts must
+    agree with the adjoint within 1e-3 relative.  Over 60 steps most pairs are
+    smooth; over 240 only a few are (none for mu), hence two windows."""
+    worlds = scenes.push_worlds(64, seed=2)
+    targets = _push_targets(64)
+    conf = default_conf(**PUSH_CONF)
+    # the forward's sweep order, step by step (the step is deterministic: the
+    # adjoint's own forward takes the same path)
+    rec = GpuBatch(worlds)
+    orders = []
+    sb = np.asarray(rec.shape_base, np.int64)
+    for _ in range(steps):
+        rec.step(conf)
+        o = rec.sweep_order().astype(np.int64)
+        w = np.searchsorted(sb, o[:, 1], side="right") - 1
+        loc = o.copy()
+        loc[:, 1] -= sb[w]
+        loc[:, 2] -= sb[w]
+        orders.append([loc[w == k] for k in range(len(worlds))])
+    g = GpuBatch(worlds)
+    g.adjoint_begin(16)
+    g.adjoint_forward(steps, conf)
+    b = g.bodies()
+    np.testing.assert_array_equal(b["pos"], rec.bodies()["pos"])
+    ybar = np.zeros((g.n_bodies, 3))
+    for k in range(len(worlds)):
+        lo = int(g.body_base[k])
+        m = b["pos"][lo + 2:lo + 34, :2].astype(np.float64).mean(0)
+        ybar[lo + 2:lo + 34, :2] = 2.0 * (m - targets[k]) / 32.0
+    adj = g.adjoint_backward(ybar, None)
+    info = g.adjoint_info()
+    assert info["replay_mismatches"] == 0 and info["tape_overflows"] == 0, info
+    g.adjoint_end()
+
+    def loss(k, dvx=0.0, dvy=0.0, dmu=0.0):
+        sc = worlds[k]
+        s2 = scenes.Scene(**{f: getattr(sc, f) for f in sc.__dataclass_fields__})
+        s2.body_vel = sc.body_vel.astype(np.float64).copy()
+        s2.body_vel[1, 0] += dvx
+        s2.body_vel[1, 1] += dvy
+        s2.shape_friction = sc.shape_friction.astype(np.float64) + dmu
+        o = oracle.OracleWorld(s2, double=True)
+        for s in range(steps):
+            o.set_solve_order(orders[s][k])
+            o.step(**PUSH_CONF)
+        return _push_loss(o.bodies()["pos"], targets, k)
+
+    h = 1e-4
+    checked, report = {"vx": 0, "vy": 0, "mu": 0}, []
+    for k in range(0, 64, 4):
+        lo, hi = int(g.body_base[k]), int(g.shape_base[k])
+        ad = {"vx": float(adj["vel"][lo + 1, 0]), "vy": float(adj["vel"][lo + 1, 1]),
+              "mu": float(adj["friction"][hi:int(g.shape_base[k + 1])].astype(np.float64).sum())}
+        for name, kw in (("vx", "dvx"), ("vy", "dvy"), ("mu", "dmu")):
+            fd = (loss(k, **{kw: h}) - loss(k, **{kw: -h})) / (2 * h)
+            fd2 = (loss(k, **{kw: h / 2}) - loss(k, **{kw: -h / 2})) / h
+            if abs(fd - fd2) > 1e-4 * max(abs(fd), 1e-3):
+                continue  # not smooth at this point: no derivative to compare
+            checked[name] += 1
+            rel = abs(ad[name] - fd) / max(abs(fd), 1e-3)
+            report.append((k, name, ad[name], fd, rel))
+    print(f"\n{steps} steps, smooth pairs checked {checked}")
+    for k, name, a, f, r in report:
+        print(f"  world {k:2d} d/d{name}: adjoint {a:.6g} fd {f:.6g} rel {r:.1e}")
+    bad = [r for r in report if r[4] > 1e-3]
+    assert not bad, bad
+    if steps == 60:
+        assert checked["vx"] >= 8 and checked["vy"] >= 8 and checked["mu"] >= 4, checked
+    else:
+        assert checked["vx"] + checked["vy"] >= 4, checked

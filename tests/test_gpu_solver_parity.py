@@ -10,12 +10,14 @@ checks are:
     is the same computation, so the GPU equals the oracle in the reference's own
     order within 1e-5 relative, positions and velocities, at the default 8/3
     iterations and at 400/30;
-  * coupled contacts (stacks, piles, a chain struck by disks): the oracle replays
-    the GPU's sweep order (prgpu_download_sweep_order) and the two agree within
-    1e-5 relative, positions and velocities, step after step.  That checks the
-    arithmetic of every solver piece on coupled constraints;
+  * coupled contacts (stacks, piles, a jointed bridge struck by bodies): the
+    oracle replays the GPU's sweep order (prgpu_download_sweep_order) and the two
+    agree within 1e-5 relative, positions and velocities, after one step from an
+    identical state (contacts found and solved) and after the next, warm-started
+    step.  That checks the arithmetic of every solver piece on coupled constraints;
   * at velocity convergence (4000 iterations) the velocities no longer depend on
-    the order: the GPU equals the oracle in the reference's order within 1e-5.
+    the order: one step from an identical state gives the GPU the oracle's
+    velocities (reference order) within 1e-5.
     Positions after the position iterations do depend on the order even then (the
     position solver's fixed points are not unique: any state with every
     separation above -linearSlop is one), so they are checked by the replay above.
@@ -169,7 +171,10 @@ def test_coupled_contacts_in_the_gpu_sweep_order(gpu_lib, scene, conf):
         o = pu.oracle_worlds_with_gpu_transforms(g, [sc])[0]
     else:
         g, o = GpuBatch([sc]), oracle.OracleWorld(sc)
-    steps = 4
+    # The first step finds the contacts and solves them (no warm start: they are
+    # new); the second warm-starts from the first's impulses.  Later steps would
+    # carry the first steps' sin/cos rounding forward, so the check stops there.
+    steps = 2
     touched, minsep = 0, 0.0
     for k in range(steps):
         st = g.step(**CONFS[conf])
@@ -190,8 +195,11 @@ def test_velocities_at_convergence_reference_order(gpu_lib, scene):
     sc = stacks(n=4) if scene == "stacks" else packed_pile()
     conf = dict(regVelocityIters=4000, regPositionIters=30, regMinSeparation=float("inf"))
     g, o = GpuBatch([sc]), oracle.OracleWorld(sc)
-    for _ in range(2):  # the contacts are created at the end of the first step
-        g.step(**conf)
-        o.step(**conf)
+    # one step from the identical initial state: the first step creates the
+    # proxies, finds the contacts and solves them (a second step would start from
+    # positions that the order-dependent position iterations left differently)
+    st = g.step(**conf)
+    o.step(**conf)
+    assert st["activeConstraints"] >= 10
     dv = pu.rel_err(g.bodies()["vel"], o.bodies()["vel"])
     assert dv <= pu.RTOL, f"velocities at convergence differ by {dv:.3g}"

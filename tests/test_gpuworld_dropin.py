@@ -5,7 +5,9 @@ constructed over GpuWorld), where the reference sources are available.
 Set-up runs through PlayRho's World API into GpuWorld (CreateShape, CreateBody
 with BodyConf::Use(shape), GetBodies, GetInvMass ...); Step reaches the GPU
 library, which without a GPU answers PRGPU_ENOTREADY, surfaced as an exception.
-On a GPU machine the same program steps the world on the GPU.
+On a GPU machine (the -m gpu test) the same program steps the world on the GPU.
+The reference's headers and library come from the staged copy of its sources
+(oracle/_ref/src, oracle/ref/Makefile), built on the machine that runs the test.
 """
 import os
 import shutil
@@ -23,12 +25,17 @@ REF_LIB = os.path.join(ROOT, "oracle", "_ref", "f32", "libPlayRho.a")
 REF_GEN = os.path.join(ROOT, "oracle", "_ref", "f32", "gen")
 
 
+_EXE = []
+
+
 def _compile():
+    if _EXE:
+        return _EXE[0]
     if not os.path.isdir(os.path.join(REF, "Library", "include")):
-        pytest.skip("reference headers not available here")
+        pytest.skip("reference sources not staged here (make -C oracle/ref stage)")
     if not os.path.exists(REF_LIB):
-        res = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "f32"],
-                             capture_output=True, text=True)
+        res = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"-j{os.cpu_count() or 8}",
+                              "f32"], capture_output=True, text=True)
         if res.returncode or not os.path.exists(REF_LIB):
             pytest.skip("reference library could not be built here")
     build.build()
@@ -41,6 +48,7 @@ def _compile():
            "-Wl,-rpath," + PKG, "-o", out]
     res = subprocess.run(cmd, capture_output=True, text=True)
     assert res.returncode == 0, res.stderr[-4000:]
+    _EXE.append(out)
     return out
 
 
@@ -74,10 +82,31 @@ def test_world_over_gpuworld_builds_and_runs():
     assert any(l.startswith("joint_rejected ") for l in res.stdout.splitlines())
     from playrho_gb300.gpu import gpu_available
 
-    if gpu_available():
-        assert res.returncode == 0, res.stdout + res.stderr
-        steps = [l for l in res.stdout.splitlines() if l.startswith("step ")]
-        assert len(steps) == 60
-    else:
+    if not gpu_available():
         assert res.returncode == 3
         assert "prgpu_world_create" in lines.get("error", "")
+
+
+@pytest.mark.gpu
+def test_helloworld_over_gpuworld_steps_on_the_gpu(gpu_lib):
+    """The reference's HelloWorld with World{GpuWorld{}} (default StepConf, so the
+    time-of-impact phase is on): its 60 printed lines equal the reference's
+    HelloWorld/ExpectedOutput.txt, and the disk's location after every step equals,
+    bit for bit, the reference's own run of the same scene (tests/golden)."""
+    import numpy as np
+
+    exe = _compile()
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stdout + res.stderr
+    steps = [l.split()[1:] for l in res.stdout.splitlines() if l.startswith("step ")]
+    assert len(steps) == 60
+    xya = [[float.fromhex(v) for v in s[1:]] for s in steps]
+    # HelloWorld prints each value with std::setw(5) and 2 fixed decimals
+    printed = ["".join("%5.2f" % v for v in row) for row in xya]
+    with open(os.path.join(REF, "HelloWorld", "ExpectedOutput.txt")) as f:
+        expected = [l.rstrip("\n") for l in f if l.strip()]
+    assert printed == expected[:60]
+    gold = np.load(os.path.join(ROOT, "tests", "golden", "ref_helloworld.npz"))
+    for i in range(60):
+        ref = gold[f"d{i}_pos"][1]
+        assert np.float32(xya[i][0]) == ref[0] and np.float32(xya[i][1]) == ref[1], (i, xya[i], ref)
