@@ -190,9 +190,22 @@ def test_coupled_contacts_in_the_gpu_sweep_order(gpu_lib, scene, conf):
         assert minsep < -0.02  # the position solver had penetration to correct
 
 
-@pytest.mark.parametrize("scene", ["stacks", "packed_pile"])
+def frictionless_pile():
+    sc = packed_pile()
+    sc.shape_friction[:] = 0.0
+    return sc
+
+
+@pytest.mark.parametrize("scene", ["stacks", "frictionless_pile"])
 def test_velocities_at_convergence_reference_order(gpu_lib, scene):
-    sc = stacks(n=4) if scene == "stacks" else packed_pile()
+    """Where the velocity problem has one solution, the Gauss-Seidel order stops
+    mattering at convergence.  Stacks of boxes (two-point manifolds, block
+    solver, friction) and a packed frictionless pile have one; the packed pile
+    with friction does not: its statically indeterminate friction impulses leave
+    the velocities order dependent at any iteration count (0.19 m/s between two
+    orders of the oracle itself after 20,000 iterations), so it is checked only
+    in the replayed order above."""
+    sc = stacks(n=4) if scene == "stacks" else frictionless_pile()
     conf = dict(regVelocityIters=4000, regPositionIters=30, regMinSeparation=float("inf"))
     g, o = GpuBatch([sc]), oracle.OracleWorld(sc)
     # one step from the identical initial state: the first step creates the

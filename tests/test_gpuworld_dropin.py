@@ -92,8 +92,12 @@ def test_helloworld_over_gpuworld_steps_on_the_gpu(gpu_lib):
     """The reference's HelloWorld with World{GpuWorld{}} (default StepConf, so the
     time-of-impact phase is on): its 60 printed lines equal the reference's
     HelloWorld/ExpectedOutput.txt, and the disk's location after every step equals,
-    bit for bit, the reference's own run of the same scene (tests/golden)."""
+    bit for bit, the oracle's (pinned to the reference with the time-of-impact
+    phase on) on the same scene."""
     import numpy as np
+
+    from oracle import oracle
+    from playrho_gb300 import scenes
 
     exe = _compile()
     res = subprocess.run([exe], capture_output=True, text=True, timeout=300)
@@ -106,7 +110,15 @@ def test_helloworld_over_gpuworld_steps_on_the_gpu(gpu_lib):
     with open(os.path.join(REF, "HelloWorld", "ExpectedOutput.txt")) as f:
         expected = [l.rstrip("\n") for l in f if l.strip()]
     assert printed == expected[:60]
-    gold = np.load(os.path.join(ROOT, "tests", "golden", "ref_helloworld.npz"))
+    # HelloWorld/HelloWorld.cpp: a 50x10 half-extent ground box at (0,-10), a 1 m
+    # disk dropped from (0,4) with EarthlyGravity (-9.8f)
+    sb = scenes.SceneBuilder()
+    g = sb.body(scenes.STATIC, 0.0, -10.0)
+    sb.box(g, 50.0, 10.0)
+    b = sb.body(scenes.DYNAMIC, 0.0, 4.0, acc=(0.0, float(np.float32(-9.8)), 0.0))
+    sb.disk(b, 1.0)
+    ow = oracle.OracleWorld(sb.build())
     for i in range(60):
-        ref = gold[f"d{i}_pos"][1]
+        ow.step(doToi=1)
+        ref = ow.bodies()["xf"][1]
         assert np.float32(xya[i][0]) == ref[0] and np.float32(xya[i][1]) == ref[1], (i, xya[i], ref)
