@@ -151,12 +151,19 @@ typedef struct prgpu_batch_desc {
  *   PULLEY     PulleyJointConf:   groundAnchorA.x .y groundAnchorB.x .y lengthA lengthB ratio
  *   TARGET     TargetJointConf:   target.x .y maxForce frequency dampingRatio; the joint has
  *                                 body B only: joint_bodies gives it twice (localAnchorA unused)
- * The axis of a prismatic or wheel joint is normalised as UnitVec::Get does.
- * GearJointConf (four bodies, two other joints) is not stepped. */
+ *   GEAR       GearJointConf:     joint1 joint2 ratio [constant use-constant]: couples two
+ *                                 earlier revolute or prismatic joints of the same world
+ *                                 (global joint indices) as GetGearJointConf(world, joint1,
+ *                                 joint2, ratio) does (GearJointConf.cpp:66-160); joint_bodies
+ *                                 are joint1's and joint2's second bodies (A, B), their first
+ *                                 bodies (C, D) take part too.  The constant is the joints'
+ *                                 coordinates at creation unless extra[4] != 0, which gives it
+ *                                 in extra[3] (a GearJointConf made earlier).
+ * The axis of a prismatic or wheel joint is normalised as UnitVec::Get does. */
 enum prgpu_joint_kind {
     PRGPU_JOINT_REVOLUTE = 0, PRGPU_JOINT_DISTANCE = 1, PRGPU_JOINT_ROPE = 2, PRGPU_JOINT_WELD = 3,
     PRGPU_JOINT_FRICTION = 4, PRGPU_JOINT_MOTOR = 5, PRGPU_JOINT_PRISMATIC = 6, PRGPU_JOINT_WHEEL = 7,
-    PRGPU_JOINT_PULLEY = 8, PRGPU_JOINT_TARGET = 9
+    PRGPU_JOINT_PULLEY = 8, PRGPU_JOINT_TARGET = 9, PRGPU_JOINT_GEAR = 10
 };
 
 int prgpu_abi_version(void);
@@ -317,6 +324,28 @@ int prgpu_download_contact_seq(prgpu_world* w, uint32_t capacity, uint32_t* n_ou
 int prgpu_download_contacts_noalloc(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* proxies2,
                                     uint32_t* bodies2, uint32_t* flags, int32_t* meta2, float* head4, float* pts8,
                                     uint32_t* features2);
+/* Contact identities and the contact fields a caller may change, for every live
+ * contact in the order of prgpu_download_contacts:
+ *   slots[i]   the contact's slot: its ContactID, stable for the contact's life and
+ *              reused after it is destroyed, as the reference's ObjectPool reuses IDs
+ *              (AabbTreeWorld.cpp:2423-2547 AddContacts, :2290-2331 DestroyContacts)
+ *   mat4[4i..] friction, restitution, tangent speed, enabled (1 or 0) (Contact.hpp)
+ * Either array may be NULL. */
+int prgpu_download_contact_state(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* slots, float* mat4);
+/* SetContact(World&, ContactID, Contact) (AabbTreeWorld.cpp:2797-2832) for the
+ * fields the step reads: a disabled contact stays out of the islands and the
+ * solver (AabbTreeWorld.cpp:1433) and out of the time-of-impact phase
+ * (:1696, :2106) until it is enabled again; friction, restitution and tangent
+ * speed are used from the next step's velocity constraints (:321-357).
+ * PRGPU_EINVAL if the slot holds no live contact. */
+int prgpu_set_contact(prgpu_world* w, uint32_t slot, int enabled, float friction, float restitution,
+                      float tangent_speed);
+/* SetManifold(World&, ContactID, Manifold) (AabbTreeWorld.cpp:2834-2848): the
+ * manifold's type and point count must stay (else PRGPU_EINVAL); head4 = local
+ * normal xy, local point xy; pts8 = per point local xy, normal and tangent impulse.
+ * The contact features are kept. */
+int prgpu_set_manifold(prgpu_world* w, uint32_t slot, int32_t type, int32_t count, const float* head4,
+                       const float* pts8);
 /* Fat (tree) AABB of every proxy: minx miny maxx maxy.  A shape without a proxy
  * (its body was created disabled, AabbTreeWorld.cpp:1040) reports an empty box
  * (min +inf, max -inf). */

@@ -83,6 +83,8 @@ def _lib(double: bool):
                                                                                            ctypes.c_void_p]
     lib.or_add_joint.restype = ctypes.c_int
     lib.or_joint_enable.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.or_add_gear.argtypes = [P, ctypes.c_int, ctypes.c_int, real]
+    lib.or_add_gear.restype = ctypes.c_int
     lib.or_events.argtypes = [P, ctypes.c_void_p, ctypes.c_int]
     lib.or_events.restype = ctypes.c_int
     lib.or_default_conf.argtypes = [ctypes.POINTER(Conf)]
@@ -147,6 +149,10 @@ class OracleWorld:
             a, b = scene.joint_bodies[j]
             an, pr, fl = scene.joint_anchors[j], scene.joint_params[j], scene.joint_flags[j]
             kind = int(scene.joint_type[j])
+            if kind == 10:  # gear: the two joints it couples and the ratio
+                ex = scene.joint_extra[j]
+                lib.or_add_gear(h, int(ex[0]), int(ex[1]), float(ex[2]))
+                continue
             if kind != 0:
                 ex = np.ascontiguousarray(scene.joint_extra[j], dtype=self.np_real)
                 jid = lib.or_add_joint(h, kind, int(a), int(b), *(float(x) for x in an), int(fl[2]),

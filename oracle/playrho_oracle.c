@@ -205,6 +205,13 @@ typedef struct {
      * sAy=s1 sBy=s2), pulley (uA=u uB=u2) and target (C=linErr) state */
     v2 axis, perp, u2;
     real a1, a2, s1, s2, springMass, gamma, springImp, angImp;
+    /* gear joint (GearJointConf.hpp): bodies C and D, the kind of each coupled
+     * joint (0 revolute, 1 prismatic) with its data, ratio, constant, solver state */
+    int bC, bD, gAC, gBD;
+    real gRefAC, gRefBD, ratio, constant;
+    v2 gLaAC, gLbAC, gAxAC, gLaBD, gLbBD, gAxBD;
+    v2 JvAC, JvBD;
+    real JwA, JwB, JwC, JwD, gmass, gimp;
 } joint_t;
 enum { LS_INACTIVE = 0, LS_LOWER = 1, LS_UPPER = 2, LS_EQUAL = 3 };
 
@@ -533,6 +540,46 @@ int or_add_joint(or_world* w, int type, int bodyA, int bodyB, real lax, real lay
 }
 
 /* enableLimit / enableMotor of a prismatic (both) or wheel (enableMotor) joint. */
+/* GetGearJointConf(world, id1, id2, ratio) (GearJointConf.cpp:66-160): body A/B
+ * are the second bodies of the two joints, C/D their first bodies; the constant
+ * is the joints' coordinates now, so that the gear holds the current pose. */
+int or_add_gear(or_world* w, int joint1, int joint2, real ratio) {
+    const joint_t j1 = w->j[joint1], j2 = w->j[joint2];
+    const int A = j1.bB, B = j2.bB, C = j1.bA, D = j2.bA;
+    const int jid = or_add_revolute(w, A, B, R(0), R(0), R(0), R(0), R(0), 0, R(0), R(0), 0, R(0), R(0), 0);
+    joint_t* j = &w->j[jid];
+    j->type = OR_JOINT_GEAR;
+    j->bC = C; j->bD = D;
+    real scalar1 = R(0), scalar2 = R(0);
+    if (j1.type == OR_JOINT_PRISMATIC) {
+        j->gAC = 1;
+        j->gLaAC = j1.laA; j->gLbAC = j1.laB; j->gAxAC = V(j1.extra[0], j1.extra[1]);
+        const xf_t xfA = w->b[A].xf, xfC = w->b[C].xf;
+        const v2 pC = j1.laA;
+        const v2 pA = invrotate(vadd(rotate(j1.laB, xfA.q), vsub(xfA.p, xfC.p)), xfC.q);
+        scalar1 = dot(vsub(pA, pC), j->gAxAC);
+    } else {
+        j->gAC = 0;
+        j->gRefAC = j1.refAngle;
+        scalar1 = (w->b[A].pos1.ang - w->b[C].pos1.ang) - j1.refAngle;
+    }
+    if (j2.type == OR_JOINT_PRISMATIC) {
+        j->gBD = 1;
+        j->gLaBD = j2.laA; j->gLbBD = j2.laB; j->gAxBD = V(j2.extra[0], j2.extra[1]);
+        const xf_t xfB = w->b[B].xf, xfD = w->b[D].xf;
+        const v2 pD = j2.laA;
+        const v2 pB = invrotate(vadd(rotate(j2.laB, xfB.q), vsub(xfB.p, xfD.p)), xfD.q);
+        scalar2 = dot(vsub(pB, pD), j->gAxBD);
+    } else {
+        j->gBD = 0;
+        j->gRefBD = j2.refAngle;
+        scalar2 = (w->b[B].pos1.ang - w->b[D].pos1.ang) - j2.refAngle;
+    }
+    j->ratio = ratio;
+    j->constant = scalar1 + ratio * scalar2;
+    return jid;
+}
+
 void or_joint_enable(or_world* w, int jid, int enableLimit, int enableMotor) {
     w->j[jid].enableLimit = enableLimit;
     w->j[jid].enableMotor = enableMotor;
@@ -2639,6 +2686,161 @@ static int tj_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
 }
 
 /* Joint dispatch (JointConf visitors, Joint.cpp). */
+/* GearJointConf InitVelocity / SolveVelocity / SolvePosition
+ * (GearJointConf.cpp:170-261, :263-300, :302-474). */
+static void gear_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    bc_t* C = &bcs[j->bC];
+    bc_t* D = &bcs[j->bD];
+    pos_t velA = A->vel, velB = B->vel, velC = C->vel, velD = D->vel;
+    real invMass = R(0);
+    if (j->gAC == 1) {
+        const v2 qA = unit_from_angle(A->pos.ang), qC = unit_from_angle(C->pos.ang);
+        const v2 u = rotate(j->gAxAC, qC);
+        const v2 rC = rotate(vsub(j->gLaAC, C->lc), qC);
+        const v2 rA = rotate(vsub(j->gLbAC, A->lc), qA);
+        j->JvAC = vmul(u, R(1));
+        j->JwC = cross(rC, u);
+        j->JwA = cross(rA, u);
+        const real invRotMassC = C->invI * (j->JwC * j->JwC);
+        const real invRotMassA = A->invI * (j->JwA * j->JwA);
+        const real invLinMass = ((C->invM + A->invM) + invRotMassC) + invRotMassA;
+        invMass += invLinMass;
+    } else {
+        j->JvAC = V(R(0), R(0));
+        j->JwA = R(1);
+        j->JwC = R(1);
+        invMass += A->invI + C->invI;
+    }
+    if (j->gBD == 1) {
+        const v2 qB = unit_from_angle(B->pos.ang), qD = unit_from_angle(D->pos.ang);
+        const v2 u = rotate(j->gAxBD, qD);
+        const v2 rD = rotate(vsub(j->gLaBD, D->lc), qD);
+        const v2 rB = rotate(vsub(j->gLbBD, B->lc), qB);
+        j->JvBD = vmul(u, j->ratio);
+        j->JwD = j->ratio * cross(rD, u);
+        j->JwB = j->ratio * cross(rB, u);
+        const real invRotMassD = D->invI * (j->JwD * j->JwD);
+        const real invRotMassB = B->invI * (j->JwB * j->JwB);
+        const real invLinMass = ((j->ratio * j->ratio) * (D->invM + B->invM) + invRotMassD) + invRotMassB;
+        invMass += invLinMass;
+    } else {
+        j->JvBD = V(R(0), R(0));
+        j->JwB = j->ratio;
+        j->JwD = j->ratio;
+        invMass += (j->ratio * j->ratio) * (B->invI + D->invI);
+    }
+    j->gmass = (invMass > R(0)) ? R(1) / invMass : R(0);
+    if (conf->doWarmStart) {
+        const real imp = j->gimp;
+        velA.lin = vadd(velA.lin, vmul(j->JvAC, A->invM * imp)); velA.ang = velA.ang + (A->invI * imp) * j->JwA;
+        velB.lin = vadd(velB.lin, vmul(j->JvBD, B->invM * imp)); velB.ang = velB.ang + (B->invI * imp) * j->JwB;
+        velC.lin = vsub(velC.lin, vmul(j->JvAC, C->invM * imp)); velC.ang = velC.ang - (C->invI * imp) * j->JwC;
+        velD.lin = vsub(velD.lin, vmul(j->JvBD, D->invM * imp)); velD.ang = velD.ang - (D->invI * imp) * j->JwD;
+    } else {
+        j->gimp = R(0);
+    }
+    A->vel = velA; B->vel = velB; C->vel = velC; D->vel = velD;
+}
+
+static int gear_solve_velocity(joint_t* j, bc_t* bcs) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    bc_t* C = &bcs[j->bC];
+    bc_t* D = &bcs[j->bD];
+    pos_t velA = A->vel, velB = B->vel, velC = C->vel, velD = D->vel;
+    const real acDot = dot(j->JvAC, vsub(velA.lin, velC.lin));
+    const real bdDot = dot(j->JvBD, vsub(velB.lin, velD.lin));
+    const real Cdot = ((acDot + bdDot) + (j->JwA * velA.ang - j->JwC * velC.ang)) + (j->JwB * velB.ang - j->JwD * velD.ang);
+    const real impulse = -j->gmass * Cdot;
+    j->gimp += impulse;
+    velA.lin = vadd(velA.lin, vmul(j->JvAC, A->invM * impulse)); velA.ang = velA.ang + (A->invI * impulse) * j->JwA;
+    velB.lin = vadd(velB.lin, vmul(j->JvBD, B->invM * impulse)); velB.ang = velB.ang + (B->invI * impulse) * j->JwB;
+    velC.lin = vsub(velC.lin, vmul(j->JvAC, C->invM * impulse)); velC.ang = velC.ang - (C->invI * impulse) * j->JwC;
+    velD.lin = vsub(velD.lin, vmul(j->JvBD, D->invM * impulse)); velD.ang = velD.ang - (D->invI * impulse) * j->JwD;
+    A->vel = velA; B->vel = velB; C->vel = velC; D->vel = velD;
+    return impulse == R(0);
+}
+
+/* Cap(Position, ConstraintSolverConf) (d2/Math.cpp:63-71). */
+static pos_t cap_position(pos_t p, const or_stepconf* conf) {
+    const real lsq = mag2(p.lin);
+    if (lsq > conf->maxLinearCorrection * conf->maxLinearCorrection) p.lin = vmul(p.lin, conf->maxLinearCorrection / RSQRT(lsq));
+    p.ang = clampr(p.ang, -conf->maxAngularCorrection, conf->maxAngularCorrection);
+    return p;
+}
+
+static int gear_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* conf) {
+    bc_t* A = &bcs[j->bA];
+    bc_t* B = &bcs[j->bB];
+    bc_t* C = &bcs[j->bC];
+    bc_t* D = &bcs[j->bD];
+    const pos_t posA = A->pos, posB = B->pos, posC = C->pos, posD = D->pos;
+    if (!isfinite(j->constant)) return 1;
+    v2 JvAC = V(R(0), R(0)), JvBD = V(R(0), R(0));
+    real JwA = R(0), JwB = R(0), JwC = R(0), JwD = R(0), coordA = R(0), coordB = R(0), invMass = R(0);
+    if (j->gAC == 1) {
+        const v2 qA = unit_from_angle(posA.ang), qC = unit_from_angle(posC.ang);
+        const v2 u = rotate(j->gAxAC, qC);
+        const v2 rC = rotate(vsub(j->gLaAC, C->lc), qC);
+        const v2 rA = rotate(vsub(j->gLbAC, A->lc), qA);
+        JvAC = vmul(u, R(1));
+        JwC = cross(rC, u);
+        JwA = cross(rA, u);
+        const real invLinMass = C->invM + A->invM;
+        const real invRotMassC = C->invI * (JwC * JwC);
+        const real invRotMassA = A->invI * (JwA * JwA);
+        invMass += (invLinMass + invRotMassC) + invRotMassA;
+        const v2 pC = vsub(j->gLaAC, C->lc);
+        const v2 pA = invrotate(vadd(rA, vsub(posA.lin, posC.lin)), qC);
+        coordA = dot(vsub(pA, pC), j->gAxAC);
+    } else {
+        JwA = R(1);
+        JwC = R(1);
+        invMass += A->invI + C->invI;
+        coordA = (posA.ang - posC.ang) - j->gRefAC;
+    }
+    if (j->gBD == 1) {
+        const v2 qB = unit_from_angle(posB.ang), qD = unit_from_angle(posD.ang);
+        const v2 u = rotate(j->gAxBD, qD);
+        const v2 rD = rotate(vsub(j->gLaBD, D->lc), qD);
+        const v2 rB = rotate(vsub(j->gLbBD, B->lc), qB);
+        JvBD = vmul(u, j->ratio);
+        JwD = j->ratio * cross(rD, u);
+        JwB = j->ratio * cross(rB, u);
+        const real invLinMass = (j->ratio * j->ratio) * (D->invM + B->invM);
+        const real invRotMassD = D->invI * (JwD * JwD);
+        const real invRotMassB = B->invI * (JwB * JwB);
+        invMass += (invLinMass + invRotMassD) + invRotMassB;
+        const v2 pD = vsub(j->gLaBD, D->lc);
+        const v2 pB = invrotate(vadd(rB, vsub(posB.lin, posD.lin)), qD);
+        coordB = dot(vsub(pB, pD), j->gAxBD);
+    } else {
+        JwB = j->ratio;
+        JwD = j->ratio;
+        invMass += (j->ratio * j->ratio) * (B->invI + D->invI);
+        coordB = (posB.ang - posD.ang) - j->gRefBD;
+    }
+    const real Cv = ((coordA + j->ratio * coordB) - j->constant) * conf->regResolutionRate;
+    const real impulse = (invMass > R(0)) ? -Cv / invMass : R(0);
+    pos_t dA, dB, dC, dD;
+    dA.lin = vmul(JvAC, A->invM * impulse); dA.ang = (A->invI * impulse) * JwA;
+    dC.lin = vmul(JvAC, C->invM * impulse); dC.ang = (C->invI * impulse) * JwC;
+    dB.lin = vmul(JvBD, B->invM * impulse); dB.ang = (B->invI * impulse) * JwB;
+    dD.lin = vmul(JvBD, D->invM * impulse); dD.ang = (D->invI * impulse) * JwD;
+    dA = cap_position(dA, conf); dC = cap_position(dC, conf);
+    dB = cap_position(dB, conf); dD = cap_position(dD, conf);
+    A->pos.lin = vadd(posA.lin, dA.lin); A->pos.ang = posA.ang + dA.ang;
+    B->pos.lin = vadd(posB.lin, dB.lin); B->pos.ang = posB.ang + dB.ang;
+    C->pos.lin = vsub(posC.lin, dC.lin); C->pos.ang = posC.ang - dC.ang;
+    D->pos.lin = vsub(posD.lin, dD.lin); D->pos.ang = posD.ang - dD.ang;
+    real lin = R(0), ang = R(0);
+    lin = maxr(lin, mag2(dA.lin)); lin = maxr(lin, mag2(dB.lin)); lin = maxr(lin, mag2(dC.lin)); lin = maxr(lin, mag2(dD.lin));
+    ang = maxr(ang, fabs(dA.ang)); ang = maxr(ang, fabs(dB.ang)); ang = maxr(ang, fabs(dC.ang)); ang = maxr(ang, fabs(dD.ang));
+    return (lin <= conf->linearSlop * conf->linearSlop) && (ang <= conf->angularSlop);
+}
+
 static void joint_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) {
     switch (j->type) {
     case OR_JOINT_DISTANCE: dj_init_velocity(j, bcs, conf); break;
@@ -2650,6 +2852,7 @@ static void joint_init_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) 
     case OR_JOINT_WHEEL: wj_init_velocity(j, bcs, conf); break;
     case OR_JOINT_PULLEY: pu_init_velocity(j, bcs, conf); break;
     case OR_JOINT_TARGET: tj_init_velocity(j, bcs, conf); break;
+    case OR_JOINT_GEAR: gear_init_velocity(j, bcs, conf); break;
     default: rj_init_velocity(j, bcs, conf); break;
     }
 }
@@ -2664,6 +2867,7 @@ static int joint_solve_velocity(joint_t* j, bc_t* bcs, const or_stepconf* conf) 
     case OR_JOINT_WHEEL: return wj_solve_velocity(j, bcs, conf);
     case OR_JOINT_PULLEY: return pu_solve_velocity(j, bcs);
     case OR_JOINT_TARGET: return tj_solve_velocity(j, bcs, conf);
+    case OR_JOINT_GEAR: return gear_solve_velocity(j, bcs);
     default: return rj_solve_velocity(j, bcs, conf);
     }
 }
@@ -2676,6 +2880,7 @@ static int joint_solve_position(const joint_t* j, bc_t* bcs, const or_stepconf* 
     case OR_JOINT_PRISMATIC: return pj_solve_position(j, bcs, conf);
     case OR_JOINT_WHEEL: return wj_solve_position(j, bcs, conf);
     case OR_JOINT_PULLEY: return pu_solve_position(j, bcs, conf);
+    case OR_JOINT_GEAR: return gear_solve_position(j, bcs, conf);
     default: return rj_solve_position(j, bcs, conf);
     }
 }

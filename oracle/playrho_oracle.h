@@ -113,10 +113,14 @@ int or_add_revolute(or_world* w, int bodyA, int bodyB, or_real lax, or_real lay,
  * or_joint_enable sets their enableLimit / enableMotor. */
 enum { OR_JOINT_REVOLUTE = 0, OR_JOINT_DISTANCE = 1, OR_JOINT_ROPE = 2, OR_JOINT_WELD = 3,
        OR_JOINT_FRICTION = 4, OR_JOINT_MOTOR = 5, OR_JOINT_PRISMATIC = 6, OR_JOINT_WHEEL = 7,
-       OR_JOINT_PULLEY = 8, OR_JOINT_TARGET = 9 };
+       OR_JOINT_PULLEY = 8, OR_JOINT_TARGET = 9, OR_JOINT_GEAR = 10 };
 int or_add_joint(or_world* w, int type, int bodyA, int bodyB, or_real lax, or_real lay, or_real lbx,
                  or_real lby, int collideConnected, const or_real* extra8);
 void or_joint_enable(or_world* w, int jid, int enableLimit, int enableMotor);
+/* GearJointConf from GetGearJointConf(world, joint1, joint2, ratio)
+ * (GearJointConf.cpp:66-160): couples the two joints (revolute or prismatic) so
+ * that coordinate1 + ratio * coordinate2 stays at its value now.  Returns JointID. */
+int or_add_gear(or_world* w, int joint1, int joint2, or_real ratio);
 
 void or_default_conf(or_stepconf* conf);
 void or_step(or_world* w, const or_stepconf* conf, or_stepstats* stats);

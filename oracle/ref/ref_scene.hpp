@@ -28,6 +28,7 @@
 #include <playrho/d2/WheelJointConf.hpp>
 #include <playrho/d2/PulleyJointConf.hpp>
 #include <playrho/d2/TargetJointConf.hpp>
+#include <playrho/d2/GearJointConf.hpp>
 #include <playrho/d2/Joint.hpp>
 #include <playrho/StepConf.hpp>
 
@@ -222,6 +223,11 @@ inline bool ApplyRecord(World& world, StepConf& conf, const std::string& tag, st
                                      laA, laB, e[4] * 1_m, e[5] * 1_m};
             j.ratio = e[6]; j.collideConnected = cc != 0;
             CreateJoint(world, Joint{j});
+        } else if (kind == 10) {
+            // the gear couples two existing joints (e0, e1) with ratio e2
+            const auto j1 = JointID(static_cast<JointID::underlying_type>(e[0]));
+            const auto j2 = JointID(static_cast<JointID::underlying_type>(e[1]));
+            CreateJoint(world, Joint{GetGearJointConf(world, j1, j2, e[2])});
         } else if (kind == 9) {
             // the target joint has body B only (its body A is InvalidBodyID)
             auto j = TargetJointConf{bB};

@@ -406,12 +406,13 @@ __global__ void k_new_contacts(DW d) {
         d.cs_proxy[slot] = make_uint2(pa, pb);
         d.cs_body[slot] = make_uint2(ba, bb);
         const bool sensor = ((d.s_meta[pa] | d.s_meta[pb]) & kShapeSensor) != 0u;
-        uint32_t flags = CF_NEEDS_UPDATE;
+        uint32_t flags = CF_NEEDS_UPDATE | CF_LIVE;
         if (is_impenetrable(fa) || is_impenetrable(fb)) flags |= CF_IMPENETRABLE;
         if (sensor) flags |= CF_SENSOR;
         d.cs_flags[slot] = flags;
         const float2 ma = d.s_mat[pa], mb = d.s_mat[pb];
         d.cs_mat[slot] = make_float2(sqrtf(ma.x * mb.x), (ma.y > mb.y) ? ma.y : mb.y);
+        d.cs_tspeed[slot] = 0.f;
         d.cs_colour[slot] = kNone;
         // AddContacts appends in key order to the world's and both bodies' contact lists
         d.cs_seq[slot] = seq + i;

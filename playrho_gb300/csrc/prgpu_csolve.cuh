@@ -37,7 +37,7 @@ __device__ __forceinline__ ManRec load_manrec(const DW& d, uint32_t slot) {
 // scaled by dtRatio.  Body indices and the island are the caller's to fill in.
 __device__ __forceinline__ VC make_contact_vc(const ManRec& m, float4 pA, float4 pB, float4 mA, float4 mB, float4 vA,
                                               float4 vB, float rA, float rB, float2 mat, float dtRatio,
-                                              const DConf& c) {
+                                              const DConf& c, float tangentSpeed = 0.f) {
     const Xf xfA = get_xf(pA.x, pA.y, pA.z, mk(mA.z, mA.w));
     const Xf xfB = get_xf(pB.x, pB.y, pB.z, mk(mB.z, mB.w));
     const int type = m.type, count = m.count;
@@ -69,7 +69,7 @@ __device__ __forceinline__ VC make_contact_vc(const ManRec& m, float4 pA, float4
         n = -nb;
     }
     VC vc;
-    vc.nx = n.x; vc.ny = n.y; vc.friction = mat.x; vc.tangentSpeed = 0.f;
+    vc.nx = n.x; vc.ny = n.y; vc.friction = mat.x; vc.tangentSpeed = tangentSpeed;
     vc.bA = vc.bB = 0u; vc.island = 0u;
     const float invMass = mA.x + mB.x;
     const V2 tangent = fwdperp(n);

@@ -49,7 +49,12 @@ enum : uint32_t {
     CF_IMPENETRABLE = 8u,
     CF_TOI_VALID = 16u,       // cs_toi holds this step's time of impact (Contact::e_toiFlag)
     CF_TOI_ISL = 32u,         // in the island of the current time-of-impact event
+    CF_DISABLED = 64u,        // Contact::e_enabledFlag unset (SetContact): not solved, not in islands
+    CF_LIVE = 128u,           // the slot holds a live contact
 };
+// A touching, enabled, non-sensor contact: one the islands and the solver take
+// (AddToIsland, AabbTreeWorld.cpp:1433).
+PR_HD bool contact_solvable(uint32_t f) { return (f & (CF_TOUCHING | CF_SENSOR | CF_DISABLED)) == CF_TOUCHING; }
 // Shape meta word: kind | vertex count << 8 | these bits.
 constexpr uint32_t kShapeSensor = 1u << 16;
 constexpr uint32_t kShapeNoProxy = 1u << 17;  // the shape's body was disabled at creation: no proxy
@@ -271,6 +276,10 @@ struct DW {
     float* j_maxtorque;
     uint32_t* j_flags;       // enableLimit | enableMotor << 1 | collideConnected << 2 | kind << 8
     const float4* j_extra;   // [2J] the other kinds' parameters (PRGPU_JOINT_* layouts)
+    // [5J] gear joints: C D typeAC typeBD (bits) | ratio constant refAngleAC refAngleBD |
+    // localAnchorA.xy localAnchorB.xy of AC | localXAxisA.xy of AC, localAnchorA.xy of BD |
+    // localAnchorB.xy localXAxisA.xy of BD
+    const float4* j_gear;
     float4* j_r;             // rA.xy rB.xy
     float4* j_m0;            // mass ex.x ex.y ex.z ey.y
     float4* j_m1;            // ey.z ez.z angularMass motorImpulse
@@ -286,6 +295,7 @@ struct DW {
     uint2* cs_body;
     uint32_t* cs_flags;
     float2* cs_mat;          // friction restitution
+    float* cs_tspeed;        // tangent speed (Contact::GetTangentSpeed; SetContact)
     uint32_t* cs_colour;     // colour the contact had in the last step (first choice next step)
     float* cs_toi;           // time of impact (valid with CF_TOI_VALID)
     uint64_t* cs_seq;        // creation sequence: orders a world's contacts as its contact list does

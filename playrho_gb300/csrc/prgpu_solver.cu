@@ -63,7 +63,7 @@ __global__ void k_isl_union(DW d) {
         uint32_t a, b;
         if (i < nl) {
             const uint32_t slot = d.c_slot[i];
-            if ((d.cs_flags[slot] & (CF_TOUCHING | CF_SENSOR)) != CF_TOUCHING) continue;
+            if (!contact_solvable(d.cs_flags[slot])) continue;
             const uint2 bd = d.cs_body[slot];
             a = bd.x; b = bd.y;
         } else {
@@ -152,7 +152,7 @@ __global__ void k_active_flags(DW d) {
         uint32_t on = 0;
         if (i < nl) {
             const uint32_t slot = d.c_slot[i];
-            if ((d.cs_flags[slot] & (CF_TOUCHING | CF_SENSOR)) == CF_TOUCHING) {
+            if (contact_solvable(d.cs_flags[slot])) {
                 const uint2 bd = d.cs_body[slot];
                 on = ((d.b_flags[bd.x] | d.b_flags[bd.y]) & BF_SOLVED) ? 1u : 0u;
             }
@@ -196,23 +196,44 @@ __device__ __forceinline__ void constraint_bodies(const DW& d, uint32_t id, uint
     }
 }
 
+// Every body a constraint reads and writes: the two of a contact or joint, four
+// of a gear joint (its own A and B, and the coupled joints' C and D), each once.
+__device__ __forceinline__ int constraint_body_set(const DW& d, uint32_t id, uint32_t (&bs)[4]) {
+    uint32_t a, b;
+    constraint_bodies(d, id, a, b);
+    int n = 0;
+    bs[n++] = a;
+    if (b != a) bs[n++] = b;
+    if ((id & kJointBit) && ((d.j_flags[id & ~kJointBit] >> 8) & 0xffu) == 10u) {
+        const float4 g0 = d.j_gear[5 * (id & ~kJointBit)];
+        const uint32_t c = __float_as_uint(g0.x), e = __float_as_uint(g0.y);
+        bool dup = false;
+        for (int i = 0; i < n; ++i) dup |= (bs[i] == c);
+        if (!dup) bs[n++] = c;
+        dup = false;
+        for (int i = 0; i < n; ++i) dup |= (bs[i] == e);
+        if (!dup) bs[n++] = e;
+    }
+    return n;
+}
+
 // Colouring resources are the dynamic bodies: only they change under a constraint.
 __global__ void k_inc_count(DW d) {
     GRID_LOOP(k, d.cnt->n_active) {
-        uint32_t a, b;
-        constraint_bodies(d, d.k_list[k], a, b);
-        if (is_accelerable(d.b_flags[a])) atomicAdd(&d.inc_cur[a], 1u);
-        if (is_accelerable(d.b_flags[b]) && b != a) atomicAdd(&d.inc_cur[b], 1u);
+        uint32_t bs[4];
+        const int n = constraint_body_set(d, d.k_list[k], bs);
+        for (int e = 0; e < n; ++e)
+            if (is_accelerable(d.b_flags[bs[e]])) atomicAdd(&d.inc_cur[bs[e]], 1u);
         d.k_colour[k] = kNone;
     }
 }
 
 __global__ void k_inc_fill(DW d) {
     GRID_LOOP(k, d.cnt->n_active) {
-        uint32_t a, b;
-        constraint_bodies(d, d.k_list[k], a, b);
-        if (is_accelerable(d.b_flags[a])) d.inc_list[d.inc_off[a] + atomicAdd(&d.inc_cur[a], 1u)] = k;
-        if (is_accelerable(d.b_flags[b]) && b != a) d.inc_list[d.inc_off[b] + atomicAdd(&d.inc_cur[b], 1u)] = k;
+        uint32_t bs[4];
+        const int n = constraint_body_set(d, d.k_list[k], bs);
+        for (int e = 0; e < n; ++e)
+            if (is_accelerable(d.b_flags[bs[e]])) d.inc_list[d.inc_off[bs[e]] + atomicAdd(&d.inc_cur[bs[e]], 1u)] = k;
     }
 }
 
@@ -294,14 +315,13 @@ __device__ __forceinline__ void colour_pick(const DW& d, uint32_t k, int round) 
         if (d.k_tent[k] != kSettled) d.k_tent[k] = kSettled;
         return;
     }
-    uint32_t a, b;
     const uint32_t id = d.k_list[k];
-    constraint_bodies(d, id, a, b);
+    uint32_t bs[4];
+    const int nb = constraint_body_set(d, id, bs);
     uint64_t forbid = 0;
-    const uint32_t bs[2] = {a, b};
-    for (int e = 0; e < 2; ++e) {
+    for (int e = 0; e < nb; ++e) {
         const uint32_t x = bs[e];
-        if (!is_accelerable(d.b_flags[x]) || (e == 1 && b == a)) continue;
+        if (!is_accelerable(d.b_flags[x])) continue;
         for (uint32_t t = d.inc_off[x]; t < d.inc_off[x + 1]; ++t) {
             const uint32_t c = __ldcg(&d.k_colour[d.inc_list[t]]);
             if (c < (uint32_t)kMaxColours) forbid |= 1ull << c;
@@ -320,12 +340,11 @@ __device__ __forceinline__ void colour_pick(const DW& d, uint32_t k, int round) 
 __device__ __forceinline__ bool colour_keep(const DW& d, uint32_t k) {
     if (d.k_colour[k] != kNone) return false;
     const uint32_t t = __ldcg(&d.k_tent[k]);
-    uint32_t a, b;
-    constraint_bodies(d, d.k_list[k], a, b);
-    const uint32_t bs[2] = {a, b};
-    for (int e = 0; e < 2; ++e) {
+    uint32_t bs[4];
+    const int nb = constraint_body_set(d, d.k_list[k], bs);
+    for (int e = 0; e < nb; ++e) {
         const uint32_t x = bs[e];
-        if (!is_accelerable(d.b_flags[x]) || (e == 1 && b == a)) continue;
+        if (!is_accelerable(d.b_flags[x])) continue;
         for (uint32_t q = d.inc_off[x]; q < d.inc_off[x + 1]; ++q) {
             const uint32_t o = d.inc_list[q];
             if (o != k && __ldcg(&d.k_tent[o]) == t && colour_beats(d, o, k)) return true;
@@ -447,7 +466,7 @@ __device__ void build_constraint(const DW& d, uint32_t t, uint32_t k) {
     const float rA = d.s_radius[pr.x], rB = d.s_radius[pr.y];
     const ManRec m = load_manrec(d, slot);
     VC vc = make_contact_vc(m, d.b_pos1[bd.x], d.b_pos1[bd.y], d.b_mass[bd.x], d.b_mass[bd.y], d.b_vel[bd.x],
-                            d.b_vel[bd.y], rA, rB, d.cs_mat[slot], c.dtRatio, c);
+                            d.b_vel[bd.y], rA, rB, d.cs_mat[slot], c.dtRatio, c, d.cs_tspeed[slot]);
     vc.bA = bd.x; vc.bB = bd.y;
     vc.island = is_speedable(d.b_flags[bd.x]) ? d.b_island[bd.x] : d.b_island[bd.y];
     store_vc(d, t, vc);
@@ -613,7 +632,7 @@ __device__ bool revolute_solve_position(const DW& d, const BS& bs, uint32_t j) {
 //   pulley:         r = rA rB, m0 = uA uB, m1.x = mass, imp.x
 //   target:         r.zw = rB, m0 = mass22 (00 01 11) gamma, m1.xy = C, imp.xy
 enum : uint32_t { JK_REVOLUTE = 0, JK_DISTANCE = 1, JK_ROPE = 2, JK_WELD = 3, JK_FRICTION = 4, JK_MOTOR = 5,
-                  JK_PRISMATIC = 6, JK_WHEEL = 7, JK_PULLEY = 8, JK_TARGET = 9 };
+                  JK_PRISMATIC = 6, JK_WHEEL = 7, JK_PULLEY = 8, JK_TARGET = 9, JK_GEAR = 10 };
 __device__ __forceinline__ uint32_t joint_kind(const DW& d, uint32_t j) { return (d.j_flags[j] >> 8) & 0xffu; }
 
 // UnitVec::Get(x, y) (UnitVec.hpp:175-235): direction and magnitude.
@@ -1584,6 +1603,206 @@ __device__ void target_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
     if (bs.writable(b)) bs.set_vel(b, vB);
 }
 
+// GearJointConf (GearJointConf.cpp:170-474): bodies A and B (the joint's) and C
+// and D (the coupled joints' first bodies); the coupling of A to C (and of B
+// to D) is through a revolute joint's angle or a prismatic joint's translation.
+// Solver state: JvAC JvBD in j_r, JwA JwB JwC JwD in j_m0, mass in j_m1.x,
+// impulse in j_imp.x.
+struct GearData {
+    uint32_t c, d;
+    bool prisAC, prisBD;
+    float ratio, constant, refAC, refBD;
+    V2 laAC, lbAC, axAC, laBD, lbBD, axBD;
+};
+__device__ __forceinline__ GearData load_gear(const DW& d, uint32_t j) {
+    const float4 g0 = d.j_gear[5 * j], g1 = d.j_gear[5 * j + 1], g2 = d.j_gear[5 * j + 2];
+    const float4 g3 = d.j_gear[5 * j + 3], g4 = d.j_gear[5 * j + 4];
+    GearData g;
+    g.c = __float_as_uint(g0.x); g.d = __float_as_uint(g0.y);
+    g.prisAC = __float_as_uint(g0.z) != 0u; g.prisBD = __float_as_uint(g0.w) != 0u;
+    g.ratio = g1.x; g.constant = g1.y; g.refAC = g1.z; g.refBD = g1.w;
+    g.laAC = mk(g2.x, g2.y); g.lbAC = mk(g2.z, g2.w); g.axAC = mk(g3.x, g3.y);
+    g.laBD = mk(g3.z, g3.w); g.lbBD = mk(g4.x, g4.y); g.axBD = mk(g4.z, g4.w);
+    return g;
+}
+// v += sign * {(iM * imp) * Jv, (iI * imp) * Jw}
+__device__ __forceinline__ void gear_add(float4& v, V2 Jv, float iM, float iI, float Jw, float imp, bool add) {
+    const V2 l = Jv * (iM * imp);
+    const float a = (iI * imp) * Jw;
+    if (add) { v.x = v.x + l.x; v.y = v.y + l.y; v.z = v.z + a; }
+    else { v.x = v.x - l.x; v.y = v.y - l.y; v.z = v.z - a; }
+}
+
+template <class BS>
+__device__ void gear_init_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const GearData g = load_gear(d, j);
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b), mC = bs.mass(g.c), mD = bs.mass(g.d);
+    float4 vA = bs.vel(a), vB = bs.vel(b), vC = bs.vel(g.c), vD = bs.vel(g.d);
+    V2 JvAC = mk(0.f, 0.f), JvBD = mk(0.f, 0.f);
+    float JwA, JwB, JwC, JwD, invMass = 0.f;
+    if (g.prisAC) {
+        const V2 qA = unit_from_angle(bs.pos(a).z), qC = unit_from_angle(bs.pos(g.c).z);
+        const V2 u = rotate(g.axAC, qC);
+        const V2 rC = rotate(g.laAC - mk(mC.z, mC.w), qC);
+        const V2 rA = rotate(g.lbAC - mk(mA.z, mA.w), qA);
+        JvAC = u * 1.0f;
+        JwC = cross(rC, u);
+        JwA = cross(rA, u);
+        const float invRotMassC = mC.y * (JwC * JwC);
+        const float invRotMassA = mA.y * (JwA * JwA);
+        invMass += ((mC.x + mA.x) + invRotMassC) + invRotMassA;
+    } else {
+        JwA = 1.0f; JwC = 1.0f;
+        invMass += mA.y + mC.y;
+    }
+    if (g.prisBD) {
+        const V2 qB = unit_from_angle(bs.pos(b).z), qD = unit_from_angle(bs.pos(g.d).z);
+        const V2 u = rotate(g.axBD, qD);
+        const V2 rD = rotate(g.laBD - mk(mD.z, mD.w), qD);
+        const V2 rB = rotate(g.lbBD - mk(mB.z, mB.w), qB);
+        JvBD = u * g.ratio;
+        JwD = g.ratio * cross(rD, u);
+        JwB = g.ratio * cross(rB, u);
+        const float invRotMassD = mD.y * (JwD * JwD);
+        const float invRotMassB = mB.y * (JwB * JwB);
+        invMass += ((g.ratio * g.ratio) * (mD.x + mB.x) + invRotMassD) + invRotMassB;
+    } else {
+        JwB = g.ratio; JwD = g.ratio;
+        invMass += (g.ratio * g.ratio) * (mB.y + mD.y);
+    }
+    const float mass = (invMass > 0.f) ? 1.0f / invMass : 0.f;
+    float4 imp = d.j_imp[j];
+    if (c.doWarmStart) {
+        gear_add(vA, JvAC, mA.x, mA.y, JwA, imp.x, true);
+        gear_add(vB, JvBD, mB.x, mB.y, JwB, imp.x, true);
+        gear_add(vC, JvAC, mC.x, mC.y, JwC, imp.x, false);
+        gear_add(vD, JvBD, mD.x, mD.y, JwD, imp.x, false);
+    } else {
+        imp.x = 0.f;
+    }
+    d.j_imp[j] = imp;
+    d.j_r[j] = make_float4(JvAC.x, JvAC.y, JvBD.x, JvBD.y);
+    d.j_m0[j] = make_float4(JwA, JwB, JwC, JwD);
+    d.j_m1[j] = make_float4(mass, 0.f, 0.f, 0.f);
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+    if (bs.writable(g.c)) bs.set_vel(g.c, vC);
+    if (bs.writable(g.d)) bs.set_vel(g.d, vD);
+}
+
+template <class BS>
+__device__ void gear_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
+    const float4 g0 = d.j_gear[5 * j];
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const uint32_t cc = __float_as_uint(g0.x), dd = __float_as_uint(g0.y);
+    const float4 mA = bs.mass(a), mB = bs.mass(b), mC = bs.mass(cc), mD = bs.mass(dd);
+    float4 vA = bs.vel(a), vB = bs.vel(b), vC = bs.vel(cc), vD = bs.vel(dd);
+    const float4 r = d.j_r[j], w = d.j_m0[j];
+    const V2 JvAC = mk(r.x, r.y), JvBD = mk(r.z, r.w);
+    const float acDot = dot(JvAC, mk(vA.x, vA.y) - mk(vC.x, vC.y));
+    const float bdDot = dot(JvBD, mk(vB.x, vB.y) - mk(vD.x, vD.y));
+    const float Cdot = ((acDot + bdDot) + (w.x * vA.z - w.z * vC.z)) + (w.y * vB.z - w.w * vD.z);
+    const float impulse = -d.j_m1[j].x * Cdot;
+    float4 imp = d.j_imp[j];
+    imp.x += impulse;
+    gear_add(vA, JvAC, mA.x, mA.y, w.x, impulse, true);
+    gear_add(vB, JvBD, mB.x, mB.y, w.y, impulse, true);
+    gear_add(vC, JvAC, mC.x, mC.y, w.z, impulse, false);
+    gear_add(vD, JvBD, mD.x, mD.y, w.w, impulse, false);
+    d.j_imp[j] = imp;
+    if (bs.writable(a)) bs.set_vel(a, vA);
+    if (bs.writable(b)) bs.set_vel(b, vB);
+    if (bs.writable(cc)) bs.set_vel(cc, vC);
+    if (bs.writable(dd)) bs.set_vel(dd, vD);
+}
+
+// Cap(Position, ConstraintSolverConf) (d2/Math.cpp:63-71).
+__device__ __forceinline__ void cap_position(float& x, float& y, float& a, const DConf& c) {
+    float lsq = 0.f;
+    lsq += x * x;
+    lsq += y * y;
+    if (lsq > c.maxLinearCorrection * c.maxLinearCorrection) {
+        const float s = c.maxLinearCorrection / sqrtf(lsq);
+        x = x * s; y = y * s;
+    }
+    a = (a < -c.maxAngularCorrection) ? -c.maxAngularCorrection : ((c.maxAngularCorrection < a) ? c.maxAngularCorrection : a);
+}
+
+template <class BS>
+__device__ bool gear_solve_position(const DW& d, const BS& bs, uint32_t j) {
+    const DConf& c = *d.conf;
+    const GearData g = load_gear(d, j);
+    const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
+    const float4 mA = bs.mass(a), mB = bs.mass(b), mC = bs.mass(g.c), mD = bs.mass(g.d);
+    const float4 pA = bs.pos(a), pB = bs.pos(b), pC = bs.pos(g.c), pD = bs.pos(g.d);
+    if (!isfinite(g.constant)) return true;
+    V2 JvAC = mk(0.f, 0.f), JvBD = mk(0.f, 0.f);
+    float JwA, JwB, JwC, JwD, coordA, coordB, invMass = 0.f;
+    if (g.prisAC) {
+        const V2 qA = unit_from_angle(pA.z), qC = unit_from_angle(pC.z);
+        const V2 u = rotate(g.axAC, qC);
+        const V2 rC = rotate(g.laAC - mk(mC.z, mC.w), qC);
+        const V2 rA = rotate(g.lbAC - mk(mA.z, mA.w), qA);
+        JvAC = u * 1.0f;
+        JwC = cross(rC, u);
+        JwA = cross(rA, u);
+        const float invLinMass = mC.x + mA.x;
+        const float invRotMassC = mC.y * (JwC * JwC);
+        const float invRotMassA = mA.y * (JwA * JwA);
+        invMass += (invLinMass + invRotMassC) + invRotMassA;
+        const V2 pc = g.laAC - mk(mC.z, mC.w);
+        const V2 pa = invrotate(rA + (mk(pA.x, pA.y) - mk(pC.x, pC.y)), qC);
+        coordA = dot(pa - pc, g.axAC);
+    } else {
+        JwA = 1.0f; JwC = 1.0f;
+        invMass += mA.y + mC.y;
+        coordA = (pA.z - pC.z) - g.refAC;
+    }
+    if (g.prisBD) {
+        const V2 qB = unit_from_angle(pB.z), qD = unit_from_angle(pD.z);
+        const V2 u = rotate(g.axBD, qD);
+        const V2 rD = rotate(g.laBD - mk(mD.z, mD.w), qD);
+        const V2 rB = rotate(g.lbBD - mk(mB.z, mB.w), qB);
+        JvBD = u * g.ratio;
+        JwD = g.ratio * cross(rD, u);
+        JwB = g.ratio * cross(rB, u);
+        const float invLinMass = (g.ratio * g.ratio) * (mD.x + mB.x);
+        const float invRotMassD = mD.y * (JwD * JwD);
+        const float invRotMassB = mB.y * (JwB * JwB);
+        invMass += (invLinMass + invRotMassD) + invRotMassB;
+        const V2 pd = g.laBD - mk(mD.z, mD.w);
+        const V2 pb = invrotate(rB + (mk(pB.x, pB.y) - mk(pD.x, pD.y)), qD);
+        coordB = dot(pb - pd, g.axBD);
+    } else {
+        JwB = g.ratio; JwD = g.ratio;
+        invMass += (g.ratio * g.ratio) * (mB.y + mD.y);
+        coordB = (pB.z - pD.z) - g.refBD;
+    }
+    const float C = ((coordA + g.ratio * coordB) - g.constant) * c.regResolutionRate;
+    const float impulse = (invMass > 0.f) ? -C / invMass : 0.f;
+    float dAx = (mA.x * impulse) * JvAC.x, dAy = (mA.x * impulse) * JvAC.y, dAa = (mA.y * impulse) * JwA;
+    float dCx = (mC.x * impulse) * JvAC.x, dCy = (mC.x * impulse) * JvAC.y, dCa = (mC.y * impulse) * JwC;
+    float dBx = (mB.x * impulse) * JvBD.x, dBy = (mB.x * impulse) * JvBD.y, dBa = (mB.y * impulse) * JwB;
+    float dDx = (mD.x * impulse) * JvBD.x, dDy = (mD.x * impulse) * JvBD.y, dDa = (mD.y * impulse) * JwD;
+    cap_position(dAx, dAy, dAa, c);
+    cap_position(dCx, dCy, dCa, c);
+    cap_position(dBx, dBy, dBa, c);
+    cap_position(dDx, dDy, dDa, c);
+    if (bs.writable(a)) bs.set_pos(a, make_float4(pA.x + dAx, pA.y + dAy, pA.z + dAa, pA.w));
+    if (bs.writable(b)) bs.set_pos(b, make_float4(pB.x + dBx, pB.y + dBy, pB.z + dBa, pB.w));
+    if (bs.writable(g.c)) bs.set_pos(g.c, make_float4(pC.x - dCx, pC.y - dCy, pC.z - dCa, pC.w));
+    if (bs.writable(g.d)) bs.set_pos(g.d, make_float4(pD.x - dDx, pD.y - dDy, pD.z - dDa, pD.w));
+    auto msq = [](float x, float y) { float r = 0.f; r += x * x; r += y * y; return r; };
+    float lin = 0.f, ang = 0.f;
+    lin = maxf_(lin, msq(dAx, dAy)); lin = maxf_(lin, msq(dBx, dBy));
+    lin = maxf_(lin, msq(dCx, dCy)); lin = maxf_(lin, msq(dDx, dDy));
+    ang = maxf_(ang, fabsf(dAa)); ang = maxf_(ang, fabsf(dBa));
+    ang = maxf_(ang, fabsf(dCa)); ang = maxf_(ang, fabsf(dDa));
+    return (lin <= c.linearSlop * c.linearSlop) && (ang <= c.angularSlop);
+}
+
 // Joint dispatch on the kind (the JointConf visitors of Joint.cpp).
 template <class BS>
 __device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
@@ -1597,6 +1816,7 @@ __device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
     case JK_WHEEL: wheel_init_velocity(d, bs, j); break;
     case JK_PULLEY: pulley_init_velocity(d, bs, j); break;
     case JK_TARGET: target_init_velocity(d, bs, j); break;
+    case JK_GEAR: gear_init_velocity(d, bs, j); break;
     default: revolute_init_velocity(d, bs, j); break;
     }
 }
@@ -1612,6 +1832,7 @@ __device__ void joint_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
     case JK_WHEEL: wheel_solve_velocity(d, bs, j); break;
     case JK_PULLEY: pulley_solve_velocity(d, bs, j); break;
     case JK_TARGET: target_solve_velocity(d, bs, j); break;
+    case JK_GEAR: gear_solve_velocity(d, bs, j); break;
     default: revolute_solve_velocity(d, bs, j); break;
     }
 }
@@ -1626,6 +1847,7 @@ __device__ bool joint_solve_position(const DW& d, const BS& bs, uint32_t j) {
     case JK_PRISMATIC: return prismatic_solve_position(d, bs, j);
     case JK_WHEEL: return wheel_solve_position(d, bs, j);
     case JK_PULLEY: return pulley_solve_position(d, bs, j);
+    case JK_GEAR: return gear_solve_position(d, bs, j);
     default: return revolute_solve_position(d, bs, j);
     }
 }

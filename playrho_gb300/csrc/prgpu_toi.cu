@@ -191,7 +191,7 @@ __device__ __forceinline__ void store_toi(const DW& d, uint32_t slot, const Swee
 // of the impenetrable list: 1 compute, 2 at the sub-step limit, 0 skip.
 __device__ __forceinline__ int toi_candidate(const DW& d, uint32_t slot, int maxSubSteps) {
     const uint32_t f = d.cs_flags[slot];
-    if ((f & CF_SENSOR) || !(f & CF_IMPENETRABLE)) return 0;
+    if ((f & (CF_SENSOR | CF_DISABLED)) || !(f & CF_IMPENETRABLE)) return 0;
     if (toi_valid(d, slot)) return 0;
     if ((int)toi_count(f) >= maxSubSteps) return 2;
     const uint2 bd = d.cs_body[slot];
@@ -496,7 +496,7 @@ __device__ void toi_solve_island(const DW& d, ToiScratch& S, float toi) {
         const uint32_t la = island_local(S, bd.x), lb = island_local(S, bd.y);
         if (la == kNone || lb == kNone) { set_error(d.cnt, PR_ESTATE, 41u); return; }
         VC vc = make_contact_vc(load_manrec(d, slot), S.bp[la], S.bp[lb], S.bm[la], S.bm[lb], S.bv[la], S.bv[lb],
-                                d.s_radius[pr.x], d.s_radius[pr.y], d.cs_mat[slot], 0.f, c);
+                                d.s_radius[pr.x], d.s_radius[pr.y], d.cs_mat[slot], 0.f, c, d.cs_tspeed[slot]);
         vc.bA = la; vc.bB = lb;
         S.vc[k] = vc;
     }
@@ -550,7 +550,7 @@ __device__ bool toi_process_contact(const DW& d, uint32_t x, bool impX, uint32_t
         ++S.skipped;
     }
     const uint32_t f = d.cs_flags[slot];
-    if (!(f & CF_TOUCHING)) {
+    if (!(f & CF_TOUCHING) || (f & CF_DISABLED)) {  // not touching, or disabled by SetContact
         body_set_sweep(d, other, S.backup);
         return true;
     }

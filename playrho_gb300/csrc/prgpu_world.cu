@@ -246,7 +246,7 @@ struct HostPrep {
     std::vector<float2> s_mat;
     std::vector<float4> vtx;
     std::vector<uint32_t> jcnt, joff, jother, jcc, jcur;
-    std::vector<float4> j_anchor, j_param, j_zero, j_extra;
+    std::vector<float4> j_anchor, j_param, j_zero, j_extra, j_gear;
     std::vector<float> j_maxtorque;
     std::vector<uint32_t> j_bodies, j_flags;
 };
@@ -399,7 +399,7 @@ int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
         j_param[j] = make_float4(ds->joint_params[6 * j], ds->joint_params[6 * j + 1], ds->joint_params[6 * j + 2], ds->joint_params[6 * j + 3]);
         j_maxtorque[j] = ds->joint_params[6 * j + 4];
         const int32_t kind = ds->joint_type ? ds->joint_type[j] : PRGPU_JOINT_REVOLUTE;
-        if (kind < PRGPU_JOINT_REVOLUTE || kind > PRGPU_JOINT_TARGET) return PRGPU_EINVAL;
+        if (kind < PRGPU_JOINT_REVOLUTE || kind > PRGPU_JOINT_GEAR) return PRGPU_EINVAL;
         if (kind == PRGPU_JOINT_TARGET && a != b) return PRGPU_EINVAL;
         j_flags[j] = (ds->joint_flags[3 * j] ? 1u : 0u) | (ds->joint_flags[3 * j + 1] ? 2u : 0u) | (cc << 2) |
                      ((uint32_t)kind << 8);
@@ -411,6 +411,58 @@ int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
             const V2 ax = unit_vector(mk(hp.j_extra[2 * j].x, hp.j_extra[2 * j].y), mk(0.f, 0.f));
             hp.j_extra[2 * j].x = ax.x; hp.j_extra[2 * j].y = ax.y;
         }
+    }
+    // Gear joints: GetGearJointConf(world, joint1, joint2, ratio) (GearJointConf.cpp:
+    // 66-160) on the bodies' state at creation; joint_extra = joint1 joint2 ratio
+    // (global indices of two earlier revolute or prismatic joints of the same world).
+    hp.j_gear.assign(5 * (size_t)J, make_float4(0.f, 0.f, 0.f, 0.f));
+    auto body_angle = [&](uint32_t b) { return ds->body_pos[3 * b + 2]; };
+    auto body_xf = [&](uint32_t b) {
+        const float an = ds->body_pos[3 * b + 2];
+        return Xf{mk(ds->body_pos[3 * b], ds->body_pos[3 * b + 1]), mk(std::cos(an), std::sin(an))};
+    };
+    auto bits = [](uint32_t u) { float f; std::memcpy(&f, &u, sizeof f); return f; };
+    for (uint32_t j = 0; j < J; ++j) {
+        if (!ds->joint_type || ds->joint_type[j] != PRGPU_JOINT_GEAR) continue;
+        const float* e = ds->joint_extra ? ds->joint_extra + 8 * (size_t)j : nullptr;
+        if (!e) return PRGPU_EINVAL;
+        const float f1 = e[0], f2 = e[1], ratio = e[2];
+        if (!(f1 >= 0.f && f2 >= 0.f && f1 < (float)j && f2 < (float)j) || f1 != std::floor(f1) || f2 != std::floor(f2))
+            return PRGPU_EINVAL;
+        const uint32_t j1 = (uint32_t)f1, j2 = (uint32_t)f2;
+        const int32_t k1 = ds->joint_type[j1], k2 = ds->joint_type[j2];
+        if ((k1 != PRGPU_JOINT_REVOLUTE && k1 != PRGPU_JOINT_PRISMATIC) ||
+            (k2 != PRGPU_JOINT_REVOLUTE && k2 != PRGPU_JOINT_PRISMATIC))
+            return PRGPU_EINVAL;
+        const uint32_t A = ds->joint_bodies[2 * j1 + 1], B = ds->joint_bodies[2 * j2 + 1];
+        const uint32_t C = ds->joint_bodies[2 * j1], D = ds->joint_bodies[2 * j2];
+        if (ds->joint_bodies[2 * j] != A || ds->joint_bodies[2 * j + 1] != B) return PRGPU_EINVAL;
+        // the coordinate of body X against body Y through joint jj (its data out)
+        auto coupling = [&](uint32_t jj, uint32_t X, uint32_t Y, float& ref, V2& la, V2& lb, V2& ax) -> float {
+            if (ds->joint_type[jj] == PRGPU_JOINT_PRISMATIC) {
+                la = mk(ds->joint_anchors[4 * jj], ds->joint_anchors[4 * jj + 1]);
+                lb = mk(ds->joint_anchors[4 * jj + 2], ds->joint_anchors[4 * jj + 3]);
+                ax = mk(hp.j_extra[2 * jj].x, hp.j_extra[2 * jj].y);
+                const Xf xX = body_xf(X), xY = body_xf(Y);
+                const V2 pX = invrotate(rotate(lb, xX.q) + (xX.p - xY.p), xY.q);
+                return dot(pX - la, ax);
+            }
+            ref = ds->joint_params[6 * jj];
+            return (body_angle(X) - body_angle(Y)) - ref;
+        };
+        float refAC = 0.f, refBD = 0.f;
+        V2 laAC = mk(0.f, 0.f), lbAC = laAC, axAC = laAC, laBD = laAC, lbBD = laAC, axBD = laAC;
+        const float scalar1 = coupling(j1, A, C, refAC, laAC, lbAC, axAC);
+        const float scalar2 = coupling(j2, B, D, refBD, laBD, lbBD, axBD);
+        // e[4] != 0: the caller's constant (a GearJointConf made earlier) instead
+        const float constant = (e[4] != 0.f) ? e[3] : scalar1 + ratio * scalar2;
+        float4* g = &hp.j_gear[5 * (size_t)j];
+        g[0] = make_float4(bits(C), bits(D), bits(k1 == PRGPU_JOINT_PRISMATIC ? 1u : 0u),
+                           bits(k2 == PRGPU_JOINT_PRISMATIC ? 1u : 0u));
+        g[1] = make_float4(ratio, constant, refAC, refBD);
+        g[2] = make_float4(laAC.x, laAC.y, lbAC.x, lbAC.y);
+        g[3] = make_float4(axAC.x, axAC.y, laBD.x, laBD.y);
+        g[4] = make_float4(lbBD.x, lbBD.y, axBD.x, axBD.y);
     }
     return PRGPU_OK;
 }
@@ -678,6 +730,38 @@ __global__ void k_gather_seq(DW d, uint32_t n, uint64_t* seq) {
     GRID_LOOP(i, n) seq[i] = d.cs_seq[d.c_slot[i]];
 }
 
+// Slot and the caller-settable fields of every live contact, in key order.
+__global__ void k_gather_contact_state(DW d, uint32_t n, uint32_t* slots, float4* mat4) {
+    GRID_LOOP(i, n) {
+        const uint32_t slot = d.c_slot[i];
+        slots[i] = slot;
+        const float2 m = d.cs_mat[slot];
+        mat4[i] = make_float4(m.x, m.y, d.cs_tspeed[slot], (d.cs_flags[slot] & CF_DISABLED) ? 0.f : 1.f);
+    }
+}
+
+// SetContact / SetManifold on one slot; status 0 ok, 1 not a live contact,
+// 2 the manifold's type or point count differs.
+__global__ void k_set_contact(DW d, uint32_t slot, int enabled, float friction, float restitution, float tspeed,
+                              uint32_t* status) {
+    const uint32_t f = d.cs_flags[slot];
+    if (!(f & CF_LIVE)) { *status = 1u; return; }
+    d.cs_flags[slot] = enabled ? (f & ~CF_DISABLED) : (f | CF_DISABLED);
+    d.cs_mat[slot] = make_float2(friction, restitution);
+    d.cs_tspeed[slot] = tspeed;
+    *status = 0u;
+}
+__global__ void k_set_manifold(DW d, uint32_t slot, int type, int count, float4 head, float4 p0, float4 p1,
+                               uint32_t* status) {
+    if (!(d.cs_flags[slot] & CF_LIVE)) { *status = 1u; return; }
+    const uint32_t meta = d.m_meta[slot];
+    if ((int)(meta & 0xfu) != type || (int)((meta >> 4) & 0xfu) != count) { *status = 2u; return; }
+    d.m_head[slot] = head;
+    d.m_p0[slot] = p0;
+    d.m_p1[slot] = p1;
+    *status = 0u;
+}
+
 }  // namespace
 
 extern "C" {
@@ -882,9 +966,12 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     float4* j_extra_d;
     AL(j_extra_d, 2 * (size_t)J);
     d.j_extra = j_extra_d;
+    float4* j_gear_d;
+    AL(j_gear_d, 5 * (size_t)J);
+    d.j_gear = j_gear_d;
     AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_m2, J); AL(d.j_imp, J);
     AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
-    AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C);
+    AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C); AL(d.cs_tspeed, C);
     AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C);
     ALS(d.cs_toi_ep, C); ALS(d.cs_toi_at, C); ALS(d.t_key, C); ALS(d.t_slot, C);
     AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
@@ -895,7 +982,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ALS(d.k_list, C + J); ALS(d.k_colour, C + J); ALS(d.k_tent, C + J); ALS(d.k_order, C + J);
     ALS(d.t_id, C + J);
     ALS(d.k_prio, C + J);
-    AL(d.inc_off, N + 1); AL(d.inc_cur, N + 1); ALS(d.inc_list, 2 * ((size_t)C + J));
+    AL(d.inc_off, N + 1); AL(d.inc_cur, N + 1); ALS(d.inc_list, 2 * (size_t)C + 4 * (size_t)J);
     ALS(d.vc0, C); ALS(d.vc1, C); ALS(d.pc, C);
     ALS(d.flags, items); ALS(d.scan, items);
     w->L.prims.sm_count = 1;
@@ -983,6 +1070,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ok &= up(d.j_anchor, j_anchor.data(), sizeof(float4) * J);
     ok &= up(d.j_param, j_param.data(), sizeof(float4) * J);
     ok &= up(j_extra_d, hp.j_extra.data(), sizeof(float4) * 2 * J);
+    ok &= up(j_gear_d, hp.j_gear.data(), sizeof(float4) * 5 * J);
     ok &= up(d.j_maxtorque, j_maxtorque.data(), sizeof(float) * J);
     ok &= up(d.j_flags, j_flags.data(), sizeof(uint32_t) * J);
     ok &= up(d.j_imp, j_zero.data(), sizeof(float4) * J);
@@ -1387,6 +1475,62 @@ int prgpu_query_aabb(prgpu_world* w, uint32_t world, const float* aabb4, uint32_
     scratch.p = nullptr;
     CU(cudaStreamSynchronize(w->stream));
     if (shapes) std::sort(shapes, shapes + found);
+    return PRGPU_OK;
+}
+
+int prgpu_download_contact_state(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* slots, float* mat4) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    CU(cudaMemcpyAsync(w->h_cnt, w->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    const uint32_t n = w->h_cnt->n_live;
+    if (n_out) *n_out = n;
+    if (n == 0 || (!slots && !mat4)) return PRGPU_OK;
+    if (n > capacity) return fail(w, PRGPU_ECAPACITY, "%u contacts exceed capacity %u", n, capacity);
+    AsyncScratch scratch{nullptr, w->stream};
+    CU(cudaMallocAsync(&scratch.p, 20 * (size_t)n, w->stream));
+    float4* g_mat = static_cast<float4*>(scratch.p);
+    uint32_t* g_slot = reinterpret_cast<uint32_t*>(g_mat + n);
+    k_gather_contact_state<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, n, g_slot, g_mat);
+    CU(cudaGetLastError());
+    if (slots) CU(cudaMemcpyAsync(slots, g_slot, 4 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    if (mat4) CU(cudaMemcpyAsync(mat4, g_mat, 16 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaFreeAsync(scratch.p, w->stream));
+    scratch.p = nullptr;
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_set_contact(prgpu_world* w, uint32_t slot, int enabled, float friction, float restitution,
+                      float tangent_speed) {
+    if (!w) return PRGPU_EINVAL;
+    if (slot >= w->d.contact_cap) return fail(w, PRGPU_EINVAL, "contact slot %u out of range", slot);
+    CU(cudaSetDevice(w->device));
+    uint32_t* status = reinterpret_cast<uint32_t*>(w->d_stage);
+    k_set_contact<<<1, 1, 0, w->stream>>>(w->d, slot, enabled, friction, restitution, tangent_speed, status);
+    CU(cudaGetLastError());
+    uint32_t st = 0;
+    CU(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (st) return fail(w, PRGPU_EINVAL, "contact slot %u holds no live contact", slot);
+    return PRGPU_OK;
+}
+
+int prgpu_set_manifold(prgpu_world* w, uint32_t slot, int32_t type, int32_t count, const float* head4,
+                       const float* pts8) {
+    if (!w || !head4 || !pts8) return PRGPU_EINVAL;
+    if (slot >= w->d.contact_cap) return fail(w, PRGPU_EINVAL, "contact slot %u out of range", slot);
+    CU(cudaSetDevice(w->device));
+    uint32_t* status = reinterpret_cast<uint32_t*>(w->d_stage);
+    k_set_manifold<<<1, 1, 0, w->stream>>>(w->d, slot, type, count, make_float4(head4[0], head4[1], head4[2], head4[3]),
+                                           make_float4(pts8[0], pts8[1], pts8[2], pts8[3]),
+                                           make_float4(pts8[4], pts8[5], pts8[6], pts8[7]), status);
+    CU(cudaGetLastError());
+    uint32_t st = 0;
+    CU(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (st == 1u) return fail(w, PRGPU_EINVAL, "contact slot %u holds no live contact", slot);
+    if (st == 2u) return fail(w, PRGPU_EINVAL, "cannot change the manifold's type or point count");
     return PRGPU_OK;
 }
 

@@ -151,7 +151,7 @@ def exported_symbols() -> List[str]:
         "prgpu_adjoint_backward", "prgpu_adjoint_tangent", "prgpu_adjoint_info", "prgpu_adjoint_end",
         "prgpu_adjoint_profile", "prgpu_adjoint_trim", "prgpu_time_of_impact", "prgpu_get_body_steps",
         "prgpu_download_sweep_order", "prgpu_download_contacts_noalloc", "prgpu_download_contact_seq",
-        "prgpu_query_aabb"]
+        "prgpu_query_aabb", "prgpu_download_contact_state", "prgpu_set_contact", "prgpu_set_manifold"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -200,6 +200,18 @@ def _ptr(a: np.ndarray):
     return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
 
 
+def _gear_offsets(scenes: Sequence[Scene], extra: np.ndarray) -> np.ndarray:
+    """Gear joints name their coupled joints by index within the world; the batch
+    takes global indices."""
+    base = 0
+    for s in scenes:
+        t = np.asarray(s.joint_type).reshape(-1)
+        for j in np.flatnonzero(t == 10):
+            extra[base + j, 0:2] += base
+        base += len(t)
+    return extra
+
+
 def flatten(scenes: Sequence[Scene]) -> dict:
     """World-major concatenation of scenes with global body indices."""
     body_base = np.cumsum([0] + [s.n_bodies for s in scenes])
@@ -233,7 +245,7 @@ def flatten(scenes: Sequence[Scene]) -> dict:
         "joint_params": cat(lambda s: s.joint_params.reshape(-1, 6), np.float32),
         "joint_flags": cat(lambda s: s.joint_flags.reshape(-1, 3), np.int32),
         "joint_type": cat(lambda s: s.joint_type.reshape(-1), np.int32),
-        "joint_extra": cat(lambda s: s.joint_extra.reshape(-1, 8), np.float32),
+        "joint_extra": _gear_offsets(scenes, cat(lambda s: s.joint_extra.reshape(-1, 8), np.float32)),
         "body_base": body_base,
     }
     return out

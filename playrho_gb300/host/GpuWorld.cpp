@@ -15,6 +15,7 @@
 #include "playrho/d2/PolygonShapeConf.hpp"
 #include "playrho/d2/DistanceJointConf.hpp"
 #include "playrho/d2/FrictionJointConf.hpp"
+#include "playrho/d2/GearJointConf.hpp"
 #include "playrho/d2/MotorJointConf.hpp"
 #include "playrho/d2/PrismaticJointConf.hpp"
 #include "playrho/d2/PulleyJointConf.hpp"
@@ -233,8 +234,7 @@ prgpu::HostJoint ToHost(const Joint& joint) {
         h.extra[3] = F(StripUnit(Frequency{c->frequency}));
         h.extra[4] = F(Real{c->dampingRatio});
     } else {
-        throw InvalidArgument("GpuWorld: only revolute, distance, rope, weld, friction, motor, prismatic, wheel, "
-                              "pulley and target joints are stepped on the GPU");
+        throw InvalidArgument("GpuWorld: joint type not stepped on the GPU");
     }
     return h;
 }
@@ -305,18 +305,21 @@ void GpuWorld::Refresh() const {
     if (contactsValid) return;
     auto& self = const_cast<GpuWorld&>(*this);
     const auto& hc = Guard([&]() -> const std::vector<prgpu::HostContact>& { return self.host.Contacts(); });
-    keyedContacts.clear(); contacts.clear(); manifolds.clear();
+    keyedContacts.clear(); contacts.clear(); manifolds.clear(); contactSeq.clear(); contactIndex.clear();
     for (size_t k = 0; k < hc.size(); ++k) {
         const auto& c = hc[k];
         Contact ct{Contactable{BodyID(c.body_a), ShapeID(c.shape_a), 0u},
                    Contactable{BodyID(c.body_b), ShapeID(c.shape_b), 0u}};
-        const auto& sa = shapes[c.shape_a];
-        const auto& sb = shapes[c.shape_b];
-        ct.SetFriction(MixFriction(GetFriction(sa), GetFriction(sb)));
-        ct.SetRestitution(MixRestitution(GetRestitution(sa), GetRestitution(sb)));
+        ct.SetFriction(Real(c.friction));
+        ct.SetRestitution(Real(c.restitution));
+        ct.SetTangentSpeed(Real(c.tangent_speed) * MeterPerSecond);
+        if (c.enabled) ct.SetEnabled(); else ct.UnsetEnabled();
         if (c.touching) ct.SetTouching(); else ct.UnsetTouching();
         if (c.sensor) ct.SetSensor();
-        keyedContacts.emplace_back(ContactKey{c.proxy_a, c.proxy_b}, ContactID(static_cast<ContactID::underlying_type>(k)));
+        keyedContacts.emplace_back(ContactKey{c.proxy_a, c.proxy_b}, ContactID(static_cast<ContactID::underlying_type>(c.slot)));
+        if (contactIndex.size() <= c.slot) contactIndex.resize(c.slot + 1, -1);
+        contactIndex[c.slot] = static_cast<int32_t>(k);
+        contactSeq.push_back(c.seq);
         contacts.push_back(ct);
         Manifold m;
         const auto ln = UnitVec::Get(Real(c.local_normal[0]), Real(c.local_normal[1])).first;
@@ -367,14 +370,82 @@ void Clear(GpuWorld& w) noexcept {
     w.Invalidate();
 }
 
+namespace {
+
+// The live contacts by creation number, with what the listeners may ask about.
+std::vector<std::pair<uint32_t, GpuWorld::Snapshot>> TakeSnapshot(const GpuWorld& w) {
+    w.Refresh();
+    std::vector<std::pair<uint32_t, GpuWorld::Snapshot>> out;
+    out.reserve(w.contacts.size());
+    for (size_t k = 0; k < w.contacts.size(); ++k) {
+        out.emplace_back(static_cast<uint32_t>(to_underlying(std::get<ContactID>(w.keyedContacts[k]))),
+                         GpuWorld::Snapshot{w.contactSeq[k], IsTouching(w.contacts[k]), w.contacts[k], w.manifolds[k]});
+    }
+    std::sort(out.begin(), out.end(), [](const auto& a, const auto& b) { return a.second.seq < b.second.seq; });
+    return out;
+}
+
+// BeginContact / EndContact calls of the step just run, from the contacts before
+// and after it, in the reference's order: EndContact for each touching contact
+// the step destroyed (DestroyContacts -> InternalDestroy, AabbTreeWorld.cpp:
+// 2245-2253, 2290-2331), then BeginContact / EndContact for each contact whose
+// touching state changed or that was created touching (Update, :2703-2714);
+// both passes in contact-list (creation) order.
+void CallContactListeners(GpuWorld& w, std::vector<std::pair<uint32_t, GpuWorld::Snapshot>>& before) {
+    auto after = TakeSnapshot(w);
+    std::vector<std::pair<bool, ContactID>> calls;  // (begin?, id)
+    size_t j = 0;
+    for (const auto& e : before) {  // destroyed: in `before`, not in `after`
+        while (j < after.size() && after[j].second.seq < e.second.seq) ++j;
+        const bool alive = j < after.size() && after[j].second.seq == e.second.seq;
+        if (!alive && e.second.touching) calls.emplace_back(false, ContactID(e.first));
+    }
+    size_t i = 0;
+    for (const auto& e : after) {
+        while (i < before.size() && before[i].second.seq < e.second.seq) ++i;
+        const bool existed = i < before.size() && before[i].second.seq == e.second.seq;
+        const bool was = existed && before[i].second.touching;
+        if (e.second.touching != was) calls.emplace_back(e.second.touching, ContactID(e.first));
+    }
+    w.replaying = &before;
+    w.locked = true;
+    try {
+        for (const auto& c : calls) {
+            if (c.first) { if (w.beginContactListener) w.beginContactListener(c.second); }
+            else if (w.endContactListener) w.endContactListener(c.second);
+        }
+    } catch (...) {
+        w.locked = false;
+        w.replaying = nullptr;
+        throw;
+    }
+    w.locked = false;
+    w.replaying = nullptr;
+    before = std::move(after);
+}
+
+}  // namespace
+
 StepStats Step(GpuWorld& w, const StepConf& conf) {
     CheckUnlocked(w);
     StepStats stats;
     const auto sc = ToAbi(conf);
+    const bool listen = static_cast<bool>(w.beginContactListener) || static_cast<bool>(w.endContactListener);
+    // the contacts before the step (kept from the last step while listeners are set)
+    if (listen && !w.listening) {
+        w.previous = w.host.HasGpuBatch() ? TakeSnapshot(w) : decltype(w.previous){};
+        w.listening = true;
+    }
+    if (!listen) {
+        w.previous.clear();
+        w.listening = false;
+    }
+    if (w.host.NeedsRebuild()) w.previous.clear();  // a rebuilt batch finds its contacts anew
     const prgpu_step_stats s = Guard([&] { return w.host.Step(sc); });
     for (uint32_t id = 0; id < w.host.BodyRange(); ++id)
         if (w.host.BodyAlive(id)) Mirror(w, id);
     w.Invalidate();
+    if (listen) CallContactListeners(w, w.previous);
     if (conf.deltaTime != 0_s) w.invDeltaTime = Real(1) / conf.deltaTime;
     stats.pre.contactsAdded = s.contactsAdded;
     stats.pre.contactsDestroyed = s.contactsDestroyed;
@@ -538,10 +609,50 @@ std::vector<JointID> GetJoints(const GpuWorld& w) {
     return out;
 }
 
+namespace {
+
+// A GearJointConf (GearJointConf.hpp) for the GPU: the two joints it couples are
+// found among the world's joints by their bodies (the gear's A and B are their
+// second bodies, C and D their first) and kinds (revolute or prismatic, as the
+// conf's type data say); ratio and constant are the conf's own.
+prgpu::HostJoint GearToHost(const GpuWorld& w, const GearJointConf& c) {
+    auto find = [&](BodyID first, BodyID second, bool prismatic) -> uint32_t {
+        for (uint32_t j = 0; j < w.joints.size(); ++j) {
+            if (!w.host.JointAlive(j)) continue;
+            const auto& h = w.host.GetJoint(j);
+            const bool kindOk = prismatic ? (h.kind == PRGPU_JOINT_PRISMATIC) : (h.kind == PRGPU_JOINT_REVOLUTE);
+            if (kindOk && h.body_a == to_underlying(first) && h.body_b == to_underlying(second)) return j;
+        }
+        throw InvalidArgument("GpuWorld: no revolute or prismatic joint that the gear joint couples");
+    };
+    const bool prisAC = std::holds_alternative<GearJointConf::PrismaticData>(c.typeDataAC);
+    const bool prisBD = std::holds_alternative<GearJointConf::PrismaticData>(c.typeDataBD);
+    if (std::holds_alternative<std::monostate>(c.typeDataAC) || std::holds_alternative<std::monostate>(c.typeDataBD))
+        throw InvalidArgument("GpuWorld: gear joint without coupled joint data");
+    prgpu::HostJoint h;
+    h.kind = PRGPU_JOINT_GEAR;
+    h.body_a = to_underlying(GetBodyA(c));
+    h.body_b = to_underlying(GetBodyB(c));
+    h.collide_connected = c.collideConnected ? 1 : 0;
+    h.extra[0] = static_cast<float>(find(c.bodyC, GetBodyA(c), prisAC));
+    h.extra[1] = static_cast<float>(find(c.bodyD, GetBodyB(c), prisBD));
+    h.extra[2] = F(c.ratio);
+    h.extra[3] = F(c.constant);
+    h.extra[4] = 1.f;  // keep the conf's constant
+    return h;
+}
+
+prgpu::HostJoint ToHost(const GpuWorld& w, const Joint& def) {
+    if (const auto* c = TypeCast<GearJointConf>(&def)) return GearToHost(w, *c);
+    return ToHost(def);
+}
+
+}  // namespace
+
 JointID CreateJoint(GpuWorld& w, const Joint& def) {
     CheckUnlocked(w);
     if (w.joints.size() >= MaxJoints) throw LengthError("CreateJoint: too many joints");
-    const uint32_t id = Guard([&] { return w.host.CreateJoint(ToHost(def)); });
+    const uint32_t id = Guard([&] { return w.host.CreateJoint(ToHost(w, def)); });
     if (id >= w.joints.size()) w.joints.resize(id + 1);
     w.joints[id] = def;
     w.Invalidate();
@@ -557,7 +668,7 @@ Joint GetJoint(const GpuWorld& w, JointID id) {
 void SetJoint(GpuWorld& w, JointID id, const Joint& def) {
     CheckUnlocked(w);
     CheckRange(id, static_cast<uint32_t>(w.joints.size()), "joint ID out of range");
-    Guard([&] { w.host.SetJoint(to_underlying(id), ToHost(def)); return 0; });
+    Guard([&] { w.host.SetJoint(to_underlying(id), ToHost(w, def)); return 0; });
     w.joints[to_underlying(id)] = def;
     w.Invalidate();
 }
@@ -618,13 +729,32 @@ void Destroy(GpuWorld& w, ShapeID id) {
 }
 
 // ---- contacts -------------------------------------------------------------------
+namespace {
+
+// Position of a live contact by ID; -1 with *old set for a contact the last step
+// destroyed, while that step's listeners run (they may still ask about it).
+int32_t ContactAt(const GpuWorld& w, ContactID id, const GpuWorld::Snapshot** old) {
+    w.Refresh();
+    *old = nullptr;
+    const auto slot = to_underlying(id);
+    if (slot < w.contactIndex.size() && w.contactIndex[slot] >= 0) return w.contactIndex[slot];
+    if (w.replaying) {
+        for (const auto& e : *w.replaying)
+            if (e.first == slot) { *old = &e.second; return -1; }
+    }
+    if (slot >= w.contactIndex.size()) throw OutOfRange<ContactID>(id, "contact ID out of range");
+    throw WasDestroyed<ContactID>(id, "contact was destroyed");
+}
+
+}  // namespace
+
 ContactCounter GetContactRange(const GpuWorld& w) noexcept {
     try {
         w.Refresh();
     } catch (...) {
         return 0;
     }
-    return static_cast<ContactCounter>(w.contacts.size());
+    return static_cast<ContactCounter>(w.contactIndex.size());
 }
 
 std::vector<KeyedContactID> GetContacts(const GpuWorld& w) {
@@ -633,29 +763,62 @@ std::vector<KeyedContactID> GetContacts(const GpuWorld& w) {
 }
 
 Contact GetContact(const GpuWorld& w, ContactID id) {
-    w.Refresh();
-    CheckRange(id, static_cast<uint32_t>(w.contacts.size()), "contact ID out of range");
-    return w.contacts[to_underlying(id)];
+    const GpuWorld::Snapshot* old;
+    const auto k = ContactAt(w, id, &old);
+    return old ? old->contact : w.contacts[static_cast<size_t>(k)];
 }
 
+// SetContact (AabbTreeWorld.cpp:2797-2832): the contactables and the sensor
+// state stay; enabled, friction, restitution and tangent speed are taken into
+// the next step.
 void SetContact(GpuWorld& w, ContactID id, const Contact& value) {
-    w.Refresh();
-    CheckRange(id, static_cast<uint32_t>(w.contacts.size()), "contact ID out of range");
-    // the GPU keeps its own contact records; what a caller may change here (the
-    // enabled flag, friction, restitution) is not taken into the next step
-    w.contacts[to_underlying(id)] = value;
+    CheckUnlocked(w);
+    const GpuWorld::Snapshot* old;
+    const auto k = ContactAt(w, id, &old);
+    if (old) throw WasDestroyed<ContactID>(id, "contact was destroyed");
+    const auto& elem = w.contacts[static_cast<size_t>(k)];
+    if (elem.GetContactableA() != value.GetContactableA()) throw InvalidArgument("cannot change contactable A");
+    if (elem.GetContactableB() != value.GetContactableB()) throw InvalidArgument("cannot change contactable B");
+    if (IsSensor(elem) != IsSensor(value))
+        throw InvalidArgument("change shape A or B being a sensor to change sensor state");
+    Guard([&] {
+        w.host.SetContact(to_underlying(id), IsEnabled(value), F(GetFriction(value)), F(GetRestitution(value)),
+                          F(GetTangentSpeed(value) / MeterPerSecond));
+    });
+    w.Invalidate();
 }
 
 Manifold GetManifold(const GpuWorld& w, ContactID id) {
-    w.Refresh();
-    CheckRange(id, static_cast<uint32_t>(w.manifolds.size()), "contact ID out of range");
-    return w.manifolds[to_underlying(id)];
+    const GpuWorld::Snapshot* old;
+    const auto k = ContactAt(w, id, &old);
+    return old ? old->manifold : w.manifolds[static_cast<size_t>(k)];
 }
 
+// SetManifold (AabbTreeWorld.cpp:2834-2848): same type and point count.
 void SetManifold(GpuWorld& w, ContactID id, const Manifold& value) {
-    w.Refresh();
-    CheckRange(id, static_cast<uint32_t>(w.manifolds.size()), "contact ID out of range");
-    w.manifolds[to_underlying(id)] = value;
+    CheckUnlocked(w);
+    const GpuWorld::Snapshot* old;
+    const auto k = ContactAt(w, id, &old);
+    if (old) throw WasDestroyed<ContactID>(id, "contact was destroyed");
+    const auto& m = w.manifolds[static_cast<size_t>(k)];
+    if (m.GetType() != value.GetType()) throw InvalidArgument("cannot change manifold type");
+    if (m.GetPointCount() != value.GetPointCount()) throw InvalidArgument("cannot change manifold point count");
+    float head[4] = {F(GetX(value.GetLocalNormal())), F(GetY(value.GetLocalNormal())),
+                     F(GetX(value.GetLocalPoint()) / Meter), F(GetY(value.GetLocalPoint()) / Meter)};
+    float pts[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (auto j = 0; j < static_cast<int>(value.GetPointCount()); ++j) {
+        const auto p = value.GetPoint(j);
+        pts[4 * j] = F(GetX(p.localPoint) / Meter);
+        pts[4 * j + 1] = F(GetY(p.localPoint) / Meter);
+        pts[4 * j + 2] = F(p.normalImpulse / NewtonSecond);
+        pts[4 * j + 3] = F(p.tangentImpulse / NewtonSecond);
+    }
+    const int type = (value.GetType() == Manifold::e_circles) ? 1 : (value.GetType() == Manifold::e_faceA) ? 2
+                   : (value.GetType() == Manifold::e_faceB) ? 3 : 0;
+    Guard([&] {
+        w.host.SetManifold(to_underlying(id), type, static_cast<int32_t>(value.GetPointCount()), head, pts);
+    });
+    w.Invalidate();
 }
 
 }  // namespace playrho::d2

@@ -14,13 +14,19 @@
 // -- works unchanged, so a program switches by changing the constructor call.
 //
 // What the GPU world does differently, by design of this path:
-//  * the regular phase only (StepConf::doToi is taken as false) and the
-//    revolute joint only (other joint types throw InvalidArgument); disk,
-//    polygon and edge shapes (others throw InvalidArgument);
+//  * disk, polygon and edge shapes (chain and multi shapes throw
+//    InvalidArgument); StepConf::doToi runs the time-of-impact phase, but
+//    sub-stepping (one event per Step) is not offered;
 //  * Gauss-Seidel sweeps visit contacts in colour order, not island order;
-//  * listeners are stored but not called (contact events are not reported);
-//  * contact IDs index the live contacts in ContactKey order and are valid
-//    until the next Step;
+//  * contact IDs are the GPU's contact slots: stable for a contact's life and
+//    reused after it is destroyed, as the reference's pools reuse them;
+//    SetContact (enabled, friction, restitution, tangent speed) and SetManifold
+//    take effect from the next step;
+//  * the BeginContact / EndContact listeners are called from Step after the GPU
+//    step, in the order the reference calls them (EndContact of the touching
+//    contacts the step destroyed, then the contacts whose touching state
+//    changed, each in contact-list order); while they run the world is locked.
+//    The pre-solve and post-solve listeners are stored but not called;
 //  * changing anything but a body's position or velocity between steps
 //    (creating or destroying entities, attaching shapes, changing a body's type,
 //    flags or mass) rebuilds the GPU batch: contacts are found again on the next
@@ -75,9 +81,21 @@ public:
     bool locked = false;
     // caches rebuilt after each step, on first use
     mutable bool contactsValid = false;
-    mutable std::vector<KeyedContactID> keyedContacts;
-    mutable std::vector<Contact> contacts;
+    mutable std::vector<KeyedContactID> keyedContacts;  // live contacts in ContactKey order
+    mutable std::vector<Contact> contacts;               // by position in keyedContacts
     mutable std::vector<Manifold> manifolds;
+    mutable std::vector<uint64_t> contactSeq;            // creation number of each (contact-list order)
+    mutable std::vector<int32_t> contactIndex;           // ContactID (slot) -> position, or -1
+    // contacts after the last step (for the listener calls of the next), by creation number
+    struct Snapshot {
+        uint64_t seq;
+        bool touching;
+        Contact contact;
+        Manifold manifold;
+    };
+    std::vector<std::pair<uint32_t, Snapshot>> previous;
+    bool listening = false;  // `previous` holds the contacts after the last step
+    const std::vector<std::pair<uint32_t, Snapshot>>* replaying = nullptr;  // while listeners run
     mutable bool treeValid = false;
     mutable DynamicTree tree;
 

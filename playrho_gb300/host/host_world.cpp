@@ -1,6 +1,7 @@
 // host_world.cpp -- HostWorld: pools, GPU batch construction and state mirroring.
 #include "host_world.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -235,9 +236,20 @@ void HostWorld::Build() {
     std::vector<uint32_t> j_bodies;
     std::vector<float> j_anchor, j_param, j_extra;
     std::vector<int32_t> j_flags, j_type;
+    // a gear names its coupled joints by ID; the batch takes their batch indices
+    std::vector<uint32_t> joint_gpu(joints_.size(), ~0u);
+    for (uint32_t j = 0, k = 0; j < joints_.size(); ++j)
+        if (joint_live_[j]) joint_gpu[j] = k++;
     for (uint32_t j = 0; j < joints_.size(); ++j) {
         if (!joint_live_[j]) continue;
-        const HostJoint& x = joints_[j];
+        HostJoint x = joints_[j];
+        if (x.kind == PRGPU_JOINT_GEAR) {
+            for (int k = 0; k < 2; ++k) {
+                const auto id = static_cast<uint32_t>(x.extra[k]);
+                if (id >= joints_.size() || !joint_live_[id]) throw Error(PRGPU_EINVAL, "gear joint: coupled joint destroyed");
+                x.extra[k] = static_cast<float>(joint_gpu[id]);
+            }
+        }
         j_bodies.insert(j_bodies.end(), {body_gpu_[x.body_a], body_gpu_[x.body_b]});
         j_anchor.insert(j_anchor.end(), {x.anchor_a[0], x.anchor_a[1], x.anchor_b[0], x.anchor_b[1]});
         j_param.insert(j_param.end(), {x.reference_angle, x.lower, x.upper, x.motor_speed, x.max_motor_torque, 0.f});
@@ -343,9 +355,20 @@ const std::vector<HostContact>& HostWorld::Contacts() {
     uint32_t n = 0;
     Check(prgpu_download_contacts(gpu_, nc, &n, pr.data(), bd.data(), fl.data(), meta.data(), head.data(), pts.data(),
                                   ft.data()), "prgpu_download_contacts");
+    std::vector<uint32_t> slots(n + 1);
+    std::vector<float> mat(4 * (size_t)n + 4);
+    std::vector<uint64_t> seq(n + 1);
+    uint32_t n2 = 0, n3 = 0;
+    Check(prgpu_download_contact_state(gpu_, n, &n2, slots.data(), mat.data()), "prgpu_download_contact_state");
+    Check(prgpu_download_contact_seq(gpu_, n, &n3, seq.data()), "prgpu_download_contact_seq");
+    if (n2 != n || n3 != n) throw Error(PRGPU_ESTATE, "contact downloads disagree");
     contacts_.resize(n);
     for (uint32_t k = 0; k < n; ++k) {
         HostContact& c = contacts_[k];
+        c.slot = slots[k];
+        c.seq = seq[k];
+        c.friction = mat[4 * k]; c.restitution = mat[4 * k + 1]; c.tangent_speed = mat[4 * k + 2];
+        c.enabled = mat[4 * k + 3] != 0.f;
         c.proxy_a = leaf_id(pr[2 * k]); c.proxy_b = leaf_id(pr[2 * k + 1]);
         c.body_a = proxy_body_[pr[2 * k]]; c.shape_a = proxy_shape_[pr[2 * k]];
         c.body_b = proxy_body_[pr[2 * k + 1]]; c.shape_b = proxy_shape_[pr[2 * k + 1]];
@@ -361,6 +384,18 @@ const std::vector<HostContact>& HostWorld::Contacts() {
     }
     contacts_valid_ = true;
     return contacts_;
+}
+
+void HostWorld::SetContact(uint32_t slot, bool enabled, float friction, float restitution, float tangent_speed) {
+    if (!gpu_ || rebuild_) throw Error(PRGPU_EINVAL, "no such contact");
+    Check(prgpu_set_contact(gpu_, slot, enabled ? 1 : 0, friction, restitution, tangent_speed), "prgpu_set_contact");
+    contacts_valid_ = false;
+}
+
+void HostWorld::SetManifold(uint32_t slot, int32_t type, int32_t count, const float head4[4], const float pts8[8]) {
+    if (!gpu_ || rebuild_) throw Error(PRGPU_EINVAL, "no such contact");
+    Check(prgpu_set_manifold(gpu_, slot, type, count, head4, pts8), "prgpu_set_manifold");
+    contacts_valid_ = false;
 }
 
 void HostWorld::Proxies(std::vector<float>& aabb4, std::vector<uint32_t>& body_shape2) {

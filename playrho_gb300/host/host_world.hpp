@@ -61,11 +61,14 @@ struct HostJoint {
     float anchor_a[2] = {0.f, 0.f}, anchor_b[2] = {0.f, 0.f};
     float reference_angle = 0.f, lower = 0.f, upper = 0.f, motor_speed = 0.f, max_motor_torque = 0.f;
     int32_t enable_limit = 0, enable_motor = 0, collide_connected = 0;
-    float extra[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // the other kinds' parameters (prgpu.h)
+    float extra[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // the other kinds' parameters (prgpu.h);
+                                                                 // a gear's coupled joints by joint ID
 };
 
 // A live contact after the last step (Contact.hpp + Manifold.hpp).
 struct HostContact {
+    uint32_t slot = 0;                                           // ContactID: stable for the contact's life
+    uint64_t seq = 0;                                            // creation number (contact-list order)
     uint32_t body_a = 0, body_b = 0, shape_a = 0, shape_b = 0;  // IDs of the host pools
     uint32_t proxy_a = 0, proxy_b = 0;                           // tree leaf IDs (ContactKey)
     bool touching = false, sensor = false;
@@ -74,6 +77,8 @@ struct HostContact {
     float point[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
     float normal_impulse[2] = {0.f, 0.f}, tangent_impulse[2] = {0.f, 0.f};
     uint32_t feature[2] = {0u, 0u};                              // typeA | indexA << 8 | typeB << 16 | indexB << 24
+    float friction = 0.f, restitution = 0.f, tangent_speed = 0.f;
+    bool enabled = true;
 };
 
 // Errors carry the C ABI's status code; the drop-in maps them onto the
@@ -116,10 +121,15 @@ public:
     prgpu_step_stats Step(const prgpu_step_conf& conf);
     // Live contacts after the last step, in ContactKey order.
     const std::vector<HostContact>& Contacts();
+    // SetContact / SetManifold on a live contact's slot (prgpu_set_contact, prgpu_set_manifold).
+    void SetContact(uint32_t slot, bool enabled, float friction, float restitution, float tangent_speed);
+    void SetManifold(uint32_t slot, int32_t type, int32_t count, const float head4[4], const float pts8[8]);
     // Fat AABB (minx miny maxx maxy) and (body, shape) of every proxy, by leaf ID order.
     void Proxies(std::vector<float>& aabb4, std::vector<uint32_t>& body_shape2);
     void Clear();
     bool HasGpuBatch() const { return gpu_ != nullptr; }
+    // The next Step rebuilds the GPU batch (entities changed since the last one).
+    bool NeedsRebuild() const { return gpu_ == nullptr || rebuild_; }
 
 private:
     void Build();         // (re)creates the GPU batch from the pools

@@ -26,7 +26,7 @@ STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 DISK, POLYGON, EDGE = 0, 1, 2
 # Joint kinds (the reference's JointConf types) and their parameters in joint_extra.
 JOINT_REVOLUTE, JOINT_DISTANCE, JOINT_ROPE, JOINT_WELD, JOINT_FRICTION, JOINT_MOTOR = 0, 1, 2, 3, 4, 5
-JOINT_PRISMATIC, JOINT_WHEEL, JOINT_PULLEY, JOINT_TARGET = 6, 7, 8, 9
+JOINT_PRISMATIC, JOINT_WHEEL, JOINT_PULLEY, JOINT_TARGET, JOINT_GEAR = 6, 7, 8, 9, 10
 JOINT_PARAMS = {
     JOINT_DISTANCE: ("length", "frequency", "damping_ratio"),
     JOINT_ROPE: ("max_length",),
@@ -38,6 +38,9 @@ JOINT_PARAMS = {
     JOINT_WHEEL: ("axis_x", "axis_y", "motor_speed", "max_motor_torque", "frequency", "damping_ratio"),
     JOINT_PULLEY: ("ground_a_x", "ground_a_y", "ground_b_x", "ground_b_y", "length_a", "length_b", "ratio"),
     JOINT_TARGET: ("target_x", "target_y", "max_force", "frequency", "damping_ratio"),
+    # the gear's parameters are the two joints it couples (joint indices of the
+    # same scene) and the ratio: GetGearJointConf(world, joint1, joint2, ratio)
+    JOINT_GEAR: ("joint1", "joint2", "ratio"),
 }
 # Parameter defaults of the reference's JointConf types where they are not zero.
 JOINT_DEFAULTS = {
@@ -205,6 +208,19 @@ class SceneBuilder:
         self.j_flags.append((1 if enable_limit else 0, 1 if enable_motor else 0, 1 if collide_connected else 0))
         self.j_type.append(int(kind))
         self.j_extra.append(tuple(extra))
+        return len(self.j_bodies) - 1
+
+    def gear(self, joint1, joint2, ratio=1.0):
+        """A gear joint coupling two earlier revolute or prismatic joints
+        (GetGearJointConf, GearJointConf.cpp:66-160): its bodies A and B are the
+        joints' second bodies (C and D, their first bodies, are implied)."""
+        a, b = self.j_bodies[joint1][1], self.j_bodies[joint2][1]
+        self.j_bodies.append((a, b))
+        self.j_anchor.append((0.0, 0.0, 0.0, 0.0))
+        self.j_params.append((0.0,) * 6)
+        self.j_flags.append((0, 0, 0))
+        self.j_type.append(JOINT_GEAR)
+        self.j_extra.append((float(joint1), float(joint2), float(ratio)) + (0.0,) * 5)
         return len(self.j_bodies) - 1
 
     def build(self) -> Scene:
@@ -628,6 +644,43 @@ def joint_zoo(rng, per_kind: int = 4, kinds=None, n_disks: int = 12, gravity: bo
     for _ in range(n_disks):
         d = sb.body(DYNAMIC, float(rng.uniform(-width / 2, width / 2)), float(rng.uniform(10.0, 16.0)), acc=acc)
         sb.disk(d, float(rng.uniform(0.2, 0.5)), density=1.0, friction=0.3)
+    return sb.build()
+
+
+def gear_scene(rng, pairs: int = 3, n_disks: int = 10, gravity: bool = True) -> Scene:
+    """Gear trains above a ground edge: pairs of wheels on revolute joints to
+    static anchors coupled by gears of ratio 1..3 (one wheel driven by a motor),
+    and racks on prismatic joints coupled to a pinion's revolute joint, with
+    disks dropped onto them."""
+    acc = GRAVITY if gravity else (0.0, 0.0, 0.0)
+    sb = SceneBuilder()
+    g = sb.body(STATIC, 0.0, 0.0)
+    width = 8.0 * pairs
+    sb.edge(g, (-width, 0.0), (width, 0.0))
+    x = -width / 2.0
+    for k in range(pairs):
+        x += 5.0
+        r1, r2 = float(rng.uniform(0.5, 1.0)), float(rng.uniform(0.3, 0.8))
+        a1, a2 = sb.body(STATIC, x, 6.0), sb.body(STATIC, x + r1 + r2 + 0.2, 6.0)
+        w1 = sb.body(DYNAMIC, x, 6.0, v=(0.0, 0.0, float(rng.normal(0, 2))), acc=acc)
+        sb.disk(w1, r1, density=1.0, friction=0.5)
+        w2 = sb.body(DYNAMIC, x + r1 + r2 + 0.2, 6.0, acc=acc)
+        sb.polygon(w2, [(r2 * math.cos(t), r2 * math.sin(t)) for t in np.linspace(0, 2 * math.pi, 7)[:-1]],
+                   density=1.0, friction=0.5)
+        j1 = sb.revolute(a1, w1, (0.0, 0.0), (0.0, 0.0), motor=(float(rng.uniform(-3, 3)), 50.0) if k == 0 else None)
+        j2 = sb.revolute(a2, w2, (0.0, 0.0), (0.0, 0.0))
+        sb.gear(j1, j2, ratio=float(rng.uniform(1.0, 3.0)))
+        # rack and pinion: a box sliding on a horizontal prismatic joint under the
+        # first wheel, coupled to the wheel's rotation
+        rb = sb.body(DYNAMIC, x, 3.0, acc=acc)
+        sb.box(rb, 1.2, 0.2, density=1.0, friction=0.5)
+        ra = sb.body(STATIC, x, 3.0)
+        jr = sb.joint(JOINT_PRISMATIC, ra, rb, (0.0, 0.0), (0.0, 0.0), axis_x=1.0, axis_y=0.0,
+                      enable_limit=True, lower=-2.0, upper=2.0)
+        sb.gear(j1, jr, ratio=float(rng.uniform(-2.0, -0.5)))
+    for _ in range(n_disks):
+        d = sb.body(DYNAMIC, float(rng.uniform(-width / 2, width / 2)), float(rng.uniform(8.0, 12.0)), acc=acc)
+        sb.disk(d, float(rng.uniform(0.2, 0.4)), density=1.0, friction=0.3)
     return sb.build()
 
 

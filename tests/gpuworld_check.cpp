@@ -14,6 +14,7 @@
 //   error <what>                                                when stepping fails
 #include <cstdio>
 #include <exception>
+#include <optional>
 
 #include "playrho/d2/BasicAPI.hpp"
 #include "playrho/d2/GearJointConf.hpp"
@@ -73,10 +74,75 @@ void CheckJoints() {
         std::printf(" %d %d %u %u", h.enable_limit, h.enable_motor, h.body_a, h.body_b);
         std::printf("\n");
     }
+    // a gear coupling the revolute joint (ID 0) and the prismatic one (ID 6), made
+    // by the reference's own GetGearJointConf: GpuWorld finds the two joints
+    const auto gear = CreateJoint(world, Joint{GetGearJointConf(world, JointID(0), JointID(6), 2.0f)});
+    const auto& gh = TypeCast<const GpuWorld&>(world).host.GetJoint(to_underlying(gear));
+    std::printf("gear %d %g %g %g %d\n", gh.kind, double(gh.extra[0]), double(gh.extra[1]), double(gh.extra[2]),
+                int(gh.extra[4]));
     try {
         CreateJoint(world, Joint{GearJointConf{}});
     } catch (const InvalidArgument& e) {
         std::printf("joint_rejected %s\n", e.what());
+    }
+}
+
+// The same calls on a world of either kind: a box and a disk dropped on a ground
+// box, the BeginContact / EndContact listeners recording (step, begin?, lower
+// shape, higher shape), the box-ground contact's ID followed through the run,
+// and SetContact on it: a tangent speed of 2 m/s with friction 0.8 from step 20
+// (a conveyor belt), disabled from step 45 (the box sinks through the ground).
+// Prints "<tag> event ...", "<tag> id ..." and "<tag> pos ..." lines.
+void Conveyor(playrho::d2::World& world, const char* tag) {
+    using namespace playrho;
+    using namespace playrho::d2;
+    const auto ground = CreateShape(world, PolygonShapeConf{}.SetAsBox(20_m, 1_m));
+    CreateBody(world, BodyConf{}.Use(ground).UseLocation(Length2{0_m, -1_m}));
+    const auto boxShape = CreateShape(world, PolygonShapeConf{}.SetAsBox(0.5_m, 0.5_m).UseDensity(1_kgpm2).UseFriction(0.5f));
+    const auto box = CreateBody(world, BodyConf{}.Use(BodyType::Dynamic).Use(boxShape)
+                                           .UseLocation(Length2{0_m, 0.75_m}).UseLinearAcceleration(EarthlyGravity));
+    const auto diskShape = CreateShape(world, DiskShapeConf{}.UseRadius(0.4_m).UseDensity(1_kgpm2));
+    CreateBody(world, BodyConf{}.Use(BodyType::Dynamic).Use(diskShape).UseLocation(Length2{3_m, 1.5_m})
+                          .UseLinearAcceleration(EarthlyGravity));
+    auto step = 0;
+    auto event = [&world, &step, tag](const char* kind, ContactID id) {
+        const auto& c = GetContact(world, id);
+        const auto a = to_underlying(GetShapeA(c)), b = to_underlying(GetShapeB(c));
+        std::printf("%s event %d %s %u %u\n", tag, step, kind, unsigned(a < b ? a : b), unsigned(a < b ? b : a));
+    };
+    SetBeginContactListener(world, [event](ContactID id) { event("begin", id); });
+    SetEndContactListener(world, [event](ContactID id) { event("end", id); });
+    auto conf = StepConf{};
+    auto boxContact = std::optional<ContactID>{};
+    for (step = 1; step <= 60; ++step) {
+        Step(world, conf);
+        for (const auto& kc : GetContacts(world)) {
+            const auto id = std::get<ContactID>(kc);
+            const auto& c = GetContact(world, id);
+            if ((GetBodyA(c) == box || GetBodyB(c) == box) && IsTouching(c) && !boxContact) {
+                boxContact = id;
+                std::printf("%s id %d\n", tag, step);
+            }
+        }
+        if (boxContact) {
+            // the ID stays the contact's own while it lives
+            const auto& c = GetContact(world, *boxContact);
+            if (GetBodyA(c) != box && GetBodyB(c) != box) std::printf("%s id_changed %d\n", tag, step);
+            if (step == 20) {
+                auto m = GetContact(world, *boxContact);
+                m.SetTangentSpeed(2_mps);
+                m.SetFriction(0.8f);
+                SetContact(world, *boxContact, m);
+            }
+            if (step == 45) {
+                auto m = GetContact(world, *boxContact);
+                m.UnsetEnabled();
+                SetContact(world, *boxContact, m);
+            }
+        }
+        const auto xf = GetTransformation(world, box);
+        std::printf("%s pos %d %a %a %a\n", tag, step, double(StripUnit(GetX(xf.p))), double(StripUnit(GetY(xf.p))),
+                    double(StripUnit(GetAngle(xf.q))));
     }
 }
 
@@ -106,6 +172,10 @@ int main() {
                 static_cast<double>(StripUnit(GetInvRotInertia(world, ball))));
     std::printf("type %d\n", static_cast<int>(GetType(world, ball)));
     CheckJoints();
+    {
+        auto ref = World{};
+        Conveyor(ref, "ref");
+    }
     const auto conf = StepConf{};
     try {
         for (auto i = 0; i < maxSteps; ++i) {
@@ -116,6 +186,8 @@ int main() {
             std::printf("step %d %a %a %a\n", i, static_cast<double>(StripUnit(GetX(location))),
                         static_cast<double>(StripUnit(GetY(location))), static_cast<double>(StripUnit(angle)));
         }
+        auto gpu = World{GpuWorld{}};
+        Conveyor(gpu, "gpu");
     } catch (const std::exception& e) {
         std::printf("error %s\n", e.what());
         return 3;

@@ -130,3 +130,59 @@ def test_adjoint_rejects_other_joint_kinds(gpu_lib):
     g = GpuBatch(single_mechanisms(scenes.JOINT_WELD, 1, 3))
     with pytest.raises(PrgpuError):
         g.adjoint_begin(4)
+
+
+def _gear_coordinates(g, w, base):
+    """Each gear's coordinate1 + ratio * coordinate2 (revolute: the angle of B
+    against A less the reference angle; prismatic: the translation along the
+    axis) from the GPU's bodies, as GearJointConf.cpp:66-160 defines it."""
+    b = g.bodies()
+    out = []
+    for j in np.flatnonzero(np.asarray(w.joint_type) == scenes.JOINT_GEAR):
+        j1, j2, ratio = int(w.joint_extra[j][0]), int(w.joint_extra[j][1]), float(w.joint_extra[j][2])
+        coords = []
+        for jj in (j1, j2):
+            a, bb = (int(x) for x in w.joint_bodies[jj])
+            if int(w.joint_type[jj]) == scenes.JOINT_PRISMATIC:
+                e = w.joint_extra[jj]
+                ax = np.array([e[0], e[1]], np.float64) / np.hypot(e[0], e[1])
+                xa, xb = b["xf"][base + a], b["xf"][base + bb]
+                d = (xb[:2] + np.array([xb[2] * w.joint_anchors[jj][2] - xb[3] * w.joint_anchors[jj][3],
+                                        xb[3] * w.joint_anchors[jj][2] + xb[2] * w.joint_anchors[jj][3]])) - xa[:2]
+                c, s = xa[2], xa[3]
+                local = np.array([c * d[0] + s * d[1], c * d[1] - s * d[0]]) - w.joint_anchors[jj][:2]
+                coords.append(float(local @ ax))
+            else:
+                coords.append(float(b["pos"][base + bb, 2] - b["pos"][base + a, 2] - w.joint_params[jj][0]))
+        out.append(coords[0] + ratio * coords[1])
+    return np.array(out)
+
+
+def test_gear_joint_matches_oracle(gpu_lib):
+    """Gear joints (GearJointConf: revolute-revolute gear trains, one driven by a
+    motor, and rack-and-pinion couplings with a prismatic joint) are 4-body
+    constraint rows, coloured over all four bodies: the GPU follows the oracle
+    (pinned bit for bit to the reference) within 1e-5 after one step and within
+    sin/cos rounding growth after 120, and every gear keeps its coordinate
+    combination at its value at creation."""
+    worlds = [scenes.gear_scene(np.random.default_rng(60 + k)) for k in range(4)]
+    g = GpuBatch(worlds)
+    ows = [oracle.OracleWorld(w) for w in worlds]
+    start = [_gear_coordinates(g, w, int(g.body_base[i])) for i, w in enumerate(worlds)]
+    for step in range(120):
+        g.step()
+        for ow in ows:
+            ow.step()
+        if step in (0, 119):
+            gb = g.bodies()
+            for i, ow in enumerate(ows):
+                base, n = int(g.body_base[i]), worlds[i].n_bodies
+                ob = ow.bodies()
+                tol = 1e-5 if step == 0 else 2e-3
+                np.testing.assert_allclose(gb["pos"][base:base + n], ob["pos"], rtol=tol, atol=tol,
+                                           err_msg=f"gear world {i} step {step}")
+                np.testing.assert_allclose(gb["vel"][base:base + n], ob["vel"], rtol=tol, atol=10 * tol,
+                                           err_msg=f"gear world {i} step {step}")
+    for i, w in enumerate(worlds):
+        now = _gear_coordinates(g, w, int(g.body_base[i]))
+        assert np.abs(now - start[i]).max() < 2e-2, (i, now, start[i])

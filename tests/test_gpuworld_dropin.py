@@ -79,7 +79,8 @@ def test_world_over_gpuworld_builds_and_runs():
     assert extra[8] == [-1.0, 5.0, 2.0, 5.0, 4.0, 3.0, 1.5] and int(joints[8][1]) == 1  # pulley collides
     assert extra[9][:5] == [3.0, 4.0, 9.0, 3.0, 0.25]
     assert flags[9][2] == flags[9][3] == flags[0][3]  # the target joint holds body B only
-    assert any(l.startswith("joint_rejected ") for l in res.stdout.splitlines())
+    assert any(l.startswith("joint_rejected ") for l in res.stdout.splitlines())  # a gear without joints
+    assert lines["gear"] == "10 0 6 2 1"  # GetGearJointConf's gear reaches the GPU side with its joints
     from playrho_gb300.gpu import gpu_available
 
     if not gpu_available():
@@ -122,3 +123,20 @@ def test_helloworld_over_gpuworld_steps_on_the_gpu(gpu_lib):
         ow.step(doToi=1)
         ref = ow.bodies()["xf"][1]
         assert np.float32(xya[i][0]) == ref[0] and np.float32(xya[i][1]) == ref[1], (i, xya[i], ref)
+
+    # The same program runs one scenario through the reference's own World{} and
+    # through World{GpuWorld{}} with identical calls: listener calls, the step at
+    # which the box's contact appears (and that its ID keeps naming it), and the
+    # box's path with SetContact's tangent speed, friction and disabling.
+    def lines(tag, kind):
+        return [l.split()[2:] for l in res.stdout.splitlines() if l.startswith(f"{tag} {kind} ")]
+
+    assert lines("gpu", "event") == lines("ref", "event") and len(lines("ref", "event")) >= 2
+    assert lines("gpu", "id") == lines("ref", "id") and not lines("gpu", "id_changed")
+    gp, rp = lines("gpu", "pos"), lines("ref", "pos")
+    assert len(gp) == len(rp) == 60
+    for g, r in zip(gp, rp):
+        gv, rv = [float.fromhex(x) for x in g[1:]], [float.fromhex(x) for x in r[1:]]
+        assert np.allclose(gv, rv, rtol=0, atol=1e-5), (g[0], gv, rv)
+    assert float.fromhex(rp[43][1]) > 0.5  # the conveyor moved the box
+    assert float.fromhex(rp[59][2]) < 0.3  # once disabled, the contact no longer holds it

@@ -97,3 +97,10 @@ def test_contact_events_piles(seed):
 def test_contact_events_bullets_with_toi():
     assert _compare_events(scenes.bullets(40, np.random.default_rng(43)), [1, 20, 40], doToi=1) > 0
 
+
+
+@pytest.mark.parametrize("double", [False, True])
+def test_gear_joints(double):
+    # gear trains (revolute-revolute, one on a motor) and rack-and-pinion gears
+    # (revolute-prismatic) with disks falling on them
+    _compare(scenes.gear_scene(np.random.default_rng(61)), [1, 60, 120], double=double)
