@@ -27,6 +27,7 @@
 // as constant within a step.  Revolute joints enter through their point rows.
 #include <algorithm>
 
+#include "prgpu_contact_ops.cuh"
 #include "prgpu_kernels.cuh"
 #include "prgpu_tape.cuh"
 
@@ -103,6 +104,112 @@ __device__ __forceinline__ void block_pass(uint32_t base, const uint32_t* off, i
 __device__ __forceinline__ uint32_t recorded_constraints(const DW& d, const StepTape* tp) {
     const uint32_t w = d.n_worlds - 1u;
     return tp->wseg[2 * w] + tp->wseg[2 * w + 1];
+}
+
+// ---- manifold points that move with the bodies ----------------------------------------
+// A point that ClipSegmentToLine (Manifold.cpp:61-102) made lies where the
+// incident edge meets a side plane of the reference face, so its coordinates in
+// the incident shape's frame depend on both bodies' positions at the collision,
+// which are the positions the step starts from.  The rest of every manifold's
+// local geometry (shape vertices, face normals, face centres) is constant.
+
+// The clipped point in the incident shape's frame: the incident edge a-b (in its
+// frame, transformation xi) meets the plane through the reference vertex vs with
+// normal -e (side 0) or +e (side 1), e being the reference edge direction in
+// its frame (transformation xr).
+template <class T>
+__device__ diff::V<T> clip_point_t(V2 a, V2 b, V2 vs, V2 e, bool side1, const diff::XfT<T>& xr,
+                                   const diff::XfT<T>& xi) {
+    using namespace diff;
+    const V<T> A = xformt(cv<T>(a.x, a.y), xi), B = xformt(cv<T>(b.x, b.y), xi);
+    const V<T> E = rotatet(cv<T>(e.x, e.y), xr.q);
+    const V<T> N = side1 ? E : neg(E);
+    const T off = dott(N, xformt(cv<T>(vs.x, vs.y), xr));
+    const T da = dott(N, A) - off, db = dott(N, B) - off;
+    const T f = da / (da - db);
+    const V<T> D = sub(add(A, scale(sub(B, A), f)), xi.p);
+    return V<T>{xi.q.x * D.x + xi.q.y * D.y, xi.q.x * D.y - xi.q.y * D.x};
+}
+
+struct MovingPoints {
+    int n;              // clipped points (0: the contact's local geometry is constant)
+    int idx[2];         // their index in the manifold
+    bool side1[2];
+    V2 vs[2];           // the side plane's reference vertex
+    V2 a, b, e;         // incident edge, reference edge direction (own frames)
+    bool flipped;       // the reference face is shape B's
+};
+
+// The contact's clipped points, found by colliding its shapes again at the
+// recorded step-start positions; that must give back the recorded manifold bit
+// for bit, else a replay mismatch is counted and the points are taken as fixed.
+__device__ MovingPoints moving_points(const DW& d, const StepTape* tp, uint32_t t, const PC& pc) {
+    MovingPoints m;
+    m.n = 0;
+    if (pc.type == M_CIRCLES) return m;
+    const uint2 pr = tp->prox[t];
+    Proxy A, B;
+    load_proxy(d, pr.x, A);
+    load_proxy(d, pr.y, B);
+    if (A.count < 2 || B.count < 2) return m;  // a disk's manifold is fixed in both frames
+    const float4 pa = tp->p0[pc.bA], pb = tp->p0[pc.bB];
+    const float4 ma = d.b_mass[pc.bA], mb = d.b_mass[pc.bB];
+    const Xf xfA = get_xf(pa.x, pa.y, pa.z, mk(ma.z, ma.w)), xfB = get_xf(pb.x, pb.y, pb.z, mk(mb.z, mb.w));
+    PolyPick pick;
+    const Man man = collide_shapes(A, xfA, B, xfB, d.conf->linearSlop, d.conf->maxCirclesRatio, &pick);
+    bool same = (uint32_t)man.type == pc.type && (uint32_t)man.count == pc.count && man.ln.x == pc.lnx &&
+                man.ln.y == pc.lny && man.lp.x == pc.lpx && man.lp.y == pc.lpy && man.plp[0].x == pc.p0x &&
+                man.plp[0].y == pc.p0y;
+    if (same && man.count == 2) same = man.plp[1].x == pc.p1x && man.plp[1].y == pc.p1y;
+    if (!same) {
+        atomicAdd(&tp->hdr[kTapeHdrMismatch], 1u);
+        return m;
+    }
+    const Proxy& s0 = pick.flipped ? B : A;
+    const Proxy& s1 = pick.flipped ? A : B;
+    for (int i = 0; i < man.count; ++i) {
+        const uint32_t c = pick.flipped ? cf_flip(man.cf[i]) : man.cf[i];
+        if ((c & 0xffu) != CF_VERTEX || ((c >> 16) & 0xffu) != CF_FACE) continue;  // a shape vertex
+        const unsigned side = (c >> 8) & 0xffu;
+        m.idx[m.n] = i;
+        m.side1[m.n] = side != pick.idx0;
+        m.vs[m.n] = s0.vtx(side);
+        ++m.n;
+    }
+    m.a = s1.vtx(pick.e1f);
+    m.b = s1.vtx(pick.e1s);
+    m.e = revperp(s0.nrm(pick.idx0));
+    m.flipped = pick.flipped != 0u;
+    return m;
+}
+
+// Tangents of the local points (p0x p0y p1x p1y) for tangents dA, dB of the
+// step-start positions (x y angle) of bodies A and B.
+__device__ void moving_points_tan(const DW& d, const StepTape* tp, const PC& pc, const MovingPoints& m,
+                                  const double* dA, const double* dB, double* out) {
+    out[0] = out[1] = out[2] = out[3] = 0.0;
+    const float4 pa = tp->p0[pc.bA], pb = tp->p0[pc.bB];
+    const float4 ma = d.b_mass[pc.bA], mb = d.b_mass[pc.bB];
+    const diff::XfT<Tan> xfA = diff::get_xft(Tan{pa.x, dA[0]}, Tan{pa.y, dA[1]}, Tan{pa.z, dA[2]}, ma.z, ma.w);
+    const diff::XfT<Tan> xfB = diff::get_xft(Tan{pb.x, dB[0]}, Tan{pb.y, dB[1]}, Tan{pb.z, dB[2]}, mb.z, mb.w);
+    for (int k = 0; k < m.n; ++k) {
+        const diff::V<Tan> q = m.flipped ? clip_point_t(m.a, m.b, m.vs[k], m.e, m.side1[k], xfB, xfA)
+                                         : clip_point_t(m.a, m.b, m.vs[k], m.e, m.side1[k], xfA, xfB);
+        out[2 * m.idx[k]] = q.x.d;
+        out[2 * m.idx[k] + 1] = q.y.d;
+    }
+}
+
+// Reverse: pb (x y angle of A, then B) += J^T lb, J the local points' Jacobian,
+// one column per position coordinate.
+__device__ void moving_points_vjp(const DW& d, const StepTape* tp, const PC& pc, const MovingPoints& m,
+                                  const float* lb, float* pb) {
+    for (int q = 0; q < 6; ++q) {
+        double u[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, col[4];
+        u[q] = 1.0;
+        moving_points_tan(d, tp, pc, m, u, u + 3, col);
+        pb[q] += (float)(col[0] * lb[0] + col[1] * lb[1] + col[2] * lb[2] + col[3] * lb[3]);
+    }
 }
 
 // ---- joints ---------------------------------------------------------------------------
@@ -232,7 +339,7 @@ __global__ void __launch_bounds__(kAdjSweepMaxThreads) k_adj_sweeps(DW d, const 
                     float yb[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, pb[6];
                     if (k.writableA) { const float4 g = a.pbar[pc.bA]; yb[0] = g.x; yb[1] = g.y; yb[2] = g.z; }
                     if (k.writableB) { const float4 g = a.pbar[pc.bB]; yb[3] = g.x; yb[4] = g.y; yb[5] = g.z; }
-                    diff::solve_position_vjp(k, c, p, yb, pb);
+                    diff::solve_position_vjp(k, c, p, yb, pb, a.gbar + (size_t)t * kGeomWords + kLocalPts);
                     // bodies that are not dynamic are not differentiated (and can be
                     // shared within a colour)
                     if (k.writableA) a.pbar[pc.bA] = make_float4(pb[0], pb[1], pb[2], 0.f);
@@ -346,7 +453,10 @@ __global__ void k_adj_local(DW d, const StepTape* tp, AdjState a) {
         const diff::Pair3<float> p{pa.x, pa.y, pa.z, pb.x, pb.y, pb.z};
         const diff::Pair3<float> v{va.x, va.y, va.z, vb.x, vb.y, vb.z};
         float pbar[6], vbar[6], mub;
-        diff::build_geom_vjp(k, p, v, ci.z, c, gbar, pbar, vbar, &mub);
+        diff::build_geom_vjp(k, p, v, ci.z, c, gbar, pbar, vbar, &mub, gbar + kLocalPts);
+        // clipped manifold points moved with the positions the step started from
+        const MovingPoints mp = moving_points(d, tp, t, pc);
+        if (mp.n) moving_points_vjp(d, tp, pc, mp, gbar + kLocalPts, pbar);
         atomicAdd(&a.pbar[pc.bA].x, pbar[0]); atomicAdd(&a.pbar[pc.bA].y, pbar[1]); atomicAdd(&a.pbar[pc.bA].z, pbar[2]);
         atomicAdd(&a.pbar[pc.bB].x, pbar[3]); atomicAdd(&a.pbar[pc.bB].y, pbar[4]); atomicAdd(&a.pbar[pc.bB].z, pbar[5]);
         atomicAdd(&a.vibar[pc.bA].x, vbar[0]); atomicAdd(&a.vibar[pc.bA].y, vbar[1]);
@@ -456,7 +566,7 @@ __global__ void __launch_bounds__(32) k_tan_world(DW d, const StepTape* tp, TanS
         }
         const PC& pc = tp->pc[t];
         const float4 ci = tp->cinfo[t];
-        const diff::ContactK k = contact_k(d, pc, ci);
+        diff::ContactK k = contact_k(d, pc, ci);
         const float4 pa = tp->p0[pc.bA], pb = tp->p0[pc.bB];
         float vax = tp->v0[pc.bA].x, vay = tp->v0[pc.bA].y, vaw = tp->v0[pc.bA].z;
         float vbx = tp->v0[pc.bB].x, vby = tp->v0[pc.bB].y, vbw = tp->v0[pc.bB].z;
@@ -472,11 +582,14 @@ __global__ void __launch_bounds__(32) k_tan_world(DW d, const StepTape* tp, TanS
             const float fa = d.s_mat[pr.x].x, fb = d.s_mat[pr.y].x;
             mud = (fb * s.fdot[pr.x] + fa * s.fdot[pr.y]) / (2.0 * ci.z);
         }
+        double* gd = s.gdot + (size_t)t * kGeomWords;
+        const MovingPoints mp = moving_points(d, tp, t, pc);
+        if (mp.n) moving_points_tan(d, tp, pc, mp, dpa, dpb, k.dp);
+        for (int q = 0; q < 4; ++q) gd[kLocalPts + q] = k.dp[q];
         const diff::Pair3<Tan> p{{pa.x, dpa[0]}, {pa.y, dpa[1]}, {pa.z, dpa[2]}, {pb.x, dpb[0]}, {pb.y, dpb[1]}, {pb.z, dpb[2]}};
         const diff::Pair3<Tan> v{{vax, dva[0]}, {vay, dva[1]}, {vaw, dva[2]}, {vbx, dvb[0]}, {vby, dvb[1]}, {vbw, dvb[2]}};
         const diff::Geom<Tan> g = diff::build_geom(k, p, v, Tan{ci.z, mud}, c);
         pack_geom(g, gval + (size_t)t * kGeomWords);
-        double* gd = s.gdot + (size_t)t * kGeomWords;
         gd[0] = g.n.x.d; gd[1] = g.n.y.d;
         for (int j = 0; j < 2; ++j) {
             gd[2 + 4 * j] = g.rA[j].x.d; gd[3 + 4 * j] = g.rA[j].y.d;
@@ -576,7 +689,9 @@ __global__ void __launch_bounds__(32) k_tan_world(DW d, const StepTape* tp, TanS
                     const uint32_t id = tp->t_id[t];
                     if (id & 0x80000000u) { joint_step(t, id & 0x7fffffffu, r, true, false); return; }
                     const PC& pc = tp->pc[t];
-                    const diff::ContactK k = contact_k(d, pc, tp->cinfo[t]);
+                    diff::ContactK k = contact_k(d, pc, tp->cinfo[t]);
+                    const double* gd = s.gdot + (size_t)t * kGeomWords + kLocalPts;
+                    k.dp[0] = gd[0]; k.dp[1] = gd[1]; k.dp[2] = gd[2]; k.dp[3] = gd[3];
                     diff::Pair3<Tan> p = body_pair(pc.bA, pc.bB, r[0], r[1], s.pdot);
                     diff::solve_position_t(k, c, p);
                     store_pair(k, pc.bA, pc.bB, p, s.pdot);

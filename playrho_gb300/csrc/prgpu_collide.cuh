@@ -165,9 +165,16 @@ PR_HD void most_anti_parallel_edge(V2 n0, Xf xf0, const Proxy& s1, Xf xf1, unsig
     else { e0 = second; e1 = first; }
 }
 
+// The features a polygon-polygon manifold was built from: the reference face
+// idx0 of s0 (shape B of the contact when flipped) and the incident edge
+// (e1f, e1s) of s1.  The adjoint differentiates the clipped points through them.
+struct PolyPick {
+    unsigned flipped, idx0, e1f, e1s;
+};
+
 // GetManifold for two polygons (Manifold.cpp:162-291).
 PR_HD Man manifold_poly(bool flipped, const Proxy& s0, Xf xf0, unsigned idx0, const Proxy& s1, Xf xf1,
-                        unsigned sec0, unsigned sec1, float maxCirclesRatio) {
+                        unsigned sec0, unsigned sec1, float maxCirclesRatio, PolyPick* pick = nullptr) {
     const float r0 = s0.r, r1 = s1.r;
     const float totalRadius = r0 + r1;
     const unsigned idx0Next = (idx0 + 1u) % (unsigned)s0.count;
@@ -180,6 +187,7 @@ PR_HD Man manifold_poly(bool flipped, const Proxy& s0, Xf xf0, unsigned idx0, co
     const V2 s0_rel_e0_dir = revperp(s0_rel_n0);
     unsigned e1f, e1s;
     most_anti_parallel_edge(s0_rel_n0, xf0, s1, xf1, sec0, sec1, e1f, e1s);
+    if (pick) { pick->flipped = flipped ? 1u : 0u; pick->idx0 = idx0; pick->e1f = e1f; pick->e1s = e1s; }
     const V2 s1_rel_v0 = s1.vtx(e1f);
     const V2 s1_abs_v0 = xform(s1_rel_v0, xf1);
     const V2 s1_rel_v1 = s1.vtx(e1s);
@@ -270,7 +278,8 @@ PR_HD Man manifold_circle(bool flipped, float totalRadius, const Proxy& shape, X
 }
 
 // CollideShapes (Manifold.cpp:393-438).
-PR_HD Man collide_shapes(const Proxy& A, Xf xfA, const Proxy& B, Xf xfB, float linearSlop, float maxCirclesRatio) {
+PR_HD Man collide_shapes(const Proxy& A, Xf xfA, const Proxy& B, Xf xfB, float linearSlop, float maxCirclesRatio,
+                         PolyPick* pick = nullptr) {
     const float totalRadius = A.r + B.r;
     if (A.count == 1 && B.count == 1) {
         const V2 pA = xform(A.vtx(0), xfA);
@@ -296,8 +305,8 @@ PR_HD Man collide_shapes(const Proxy& A, Xf xfA, const Proxy& B, Xf xfB, float l
         return man_empty();
     const float k_tol = linearSlop / 10.0f;
     return (sb.distance > (sa.distance + k_tol))
-               ? manifold_poly(true, B, xfB, sb.firstShape, A, xfA, sb.second0, sb.second1, maxCirclesRatio)
-               : manifold_poly(false, A, xfA, sa.firstShape, B, xfB, sa.second0, sa.second1, maxCirclesRatio);
+               ? manifold_poly(true, B, xfB, sb.firstShape, A, xfA, sb.second0, sb.second1, maxCirclesRatio, pick)
+               : manifold_poly(false, A, xfA, sa.firstShape, B, xfB, sa.second0, sa.second1, maxCirclesRatio, pick);
 }
 
 // Warm-start transfer of AabbTreeWorld::Update (AabbTreeWorld.cpp:2644-2678):

@@ -416,6 +416,7 @@ __global__ void k_new_contacts(DW d) {
         d.cs_colour[slot] = kNone;
         // AddContacts appends in key order to the world's and both bodies' contact lists
         d.cs_seq[slot] = seq + i;
+        d.cs_prio[slot] = contact_prio(d, pa, pb);
         store_manifold(d, slot, man_empty());
         if (!sensor) {
             if (is_speedable(fa)) atomicOr(&d.b_flags[ba], BF_AWAKE);

@@ -148,7 +148,13 @@ struct ContactK {
     uint32_t type, count; // manifold type and point count (before conditioning)
     float lnx, lny, lpx, lpy, p0x, p0y, p1x, p1y;  // local manifold
     uint32_t writableA, writableB;
+    double dp[4];         // tangents of p0x p0y p1x p1y (the tangent pass; zero elsewhere)
 };
+
+// A manifold point coordinate as T: its float value, with its tangent under Tan.
+template <class T> __device__ __forceinline__ T kpt(float v, double d);
+template <> __device__ __forceinline__ float kpt<float>(float v, double) { return v; }
+template <> __device__ __forceinline__ Tan kpt<Tan>(float v, double d) { return Tan{v, d}; }
 
 // Velocity-constraint geometry (the values VelocityConstraint holds).
 template <class T>
@@ -175,7 +181,8 @@ __device__ Geom<T> build_geom(const ContactK& k, const Pair3<T>& p, const Pair3<
     const XfT<T> xfA = get_xft(p.ax, p.ay, p.az, k.mA.z, k.mA.w);
     const XfT<T> xfB = get_xft(p.bx, p.by, p.bz, k.mB.z, k.mB.w);
     const V<T> ln = cv<T>(k.lnx, k.lny), lp = cv<T>(k.lpx, k.lpy);
-    const V<T> plp[2] = {cv<T>(k.p0x, k.p0y), cv<T>(k.p1x, k.p1y)};
+    const V<T> plp[2] = {V<T>{kpt<T>(k.p0x, k.dp[0]), kpt<T>(k.p0y, k.dp[1])},
+                         V<T>{kpt<T>(k.p1x, k.dp[2]), kpt<T>(k.p1y, k.dp[3])}};
     const int count = (int)k.count;
     V<T> n = cv<T>(0.f, 0.f);
     V<T> wpt[2] = {cv<T>(0.f, 0.f), cv<T>(0.f, 0.f)};
@@ -658,7 +665,8 @@ template <class T>
 __device__ PSMt<T> get_psmt(const ContactK& k, int idx, const XfT<T>& xfA, const XfT<T>& xfB) {
     PSMt<T> r;
     const V<T> lp = cv<T>(k.lpx, k.lpy), ln = cv<T>(k.lnx, k.lny);
-    const V<T> plp = idx ? cv<T>(k.p1x, k.p1y) : cv<T>(k.p0x, k.p0y);
+    const V<T> plp = idx ? V<T>{kpt<T>(k.p1x, k.dp[2]), kpt<T>(k.p1y, k.dp[3])}
+                         : V<T>{kpt<T>(k.p0x, k.dp[0]), kpt<T>(k.p0y, k.dp[1])};
     if (k.type == M_CIRCLES) {
         const V<T> a = xformt(lp, xfA), b = xformt(plp, xfB);
         const V<T> delta = sub(b, a);
@@ -756,11 +764,19 @@ __device__ __forceinline__ void xf_bar_to_pos(float pbx, float pby, float qbx, f
     out[2] += qbx * -s + qby * c;
 }
 
+// Reverse of v = rotate(l, q) onto l, for a constant q: l̄ += rotate^T(v̄, q).
+__device__ __forceinline__ void rot_lbar(float qx, float qy, float vbx, float vby, float* lb) {
+    lb[0] += qx * vbx + qy * vby;
+    lb[1] += qx * vby - qy * vbx;
+}
+
 // Reverse of one point of GaussSeidel::SolvePositionConstraint: given the body
 // positions p the point starts from and the adjoints sb of its increments s(p),
-// adds (ds/dp)^T sb to pb.  Forward values are recomputed in the forward's order.
+// adds (ds/dp)^T sb to pb, and the adjoint of the manifold point's local
+// coordinates to lb[2 idx], lb[2 idx + 1].  Forward values are recomputed in the
+// forward's order.
 __device__ inline void pos_point_vjp(const ContactK& k, const DConf& c, int idx, const float* p, const float* sb,
-                                     float* pb) {
+                                     float* pb, float* lb) {
     // forward: transformations, the point's manifold and the solver function
     float sA, cA, sB, cB;
     sincosf(p[2], &sA, &cA);
@@ -828,6 +844,7 @@ __device__ inline void pos_point_vjp(const ContactK& k, const DConf& c, int idx,
         xApx -= dbx; xApy -= dby; rot_qbar(k.lpx, k.lpy, -dbx, -dby, qAx, qAy);
         rot_qbar(k.lnx, k.lny, ntx, nty, qAx, qAy);
         xBpx += ptx; xBpy += pty; rot_qbar(plx, ply, ptx, pty, qBx, qBy);
+        rot_lbar(xfB.q.x, xfB.q.y, ptx, pty, lb + 2 * idx);
     } else {
         const V<float> pp = xformt(cv<float>(k.lpx, k.lpy), xfB);
         const float dx = psm.pt.x - pp.x, dy = psm.pt.y - pp.y;
@@ -839,23 +856,26 @@ __device__ inline void pos_point_vjp(const ContactK& k, const DConf& c, int idx,
         xBpx -= dbx; xBpy -= dby; rot_qbar(k.lpx, k.lpy, -dbx, -dby, qBx, qBy);
         rot_qbar(k.lnx, k.lny, ntx, nty, qBx, qBy);
         xApx += ptx; xApy += pty; rot_qbar(plx, ply, ptx, pty, qAx, qAy);
+        rot_lbar(xfA.q.x, xfA.q.y, ptx, pty, lb + 2 * idx);
     }
     xf_bar_to_pos(xApx, xApy, qAx, qAy, k.mA.z, k.mA.w, sA, cA, pb);
     xf_bar_to_pos(xBpx, xBpy, qBx, qBy, k.mB.z, k.mB.w, sB, cB, pb + 3);
 }
 
 // Reverse of solve_position_t in float: yb = adjoints of the output positions
-// (zero for a body the solve does not store); pb = adjoints of the inputs.
-__device__ inline void solve_position_vjp(const ContactK& k, const DConf& c, const float* p, const float* yb, float* pb) {
+// (zero for a body the solve does not store); pb = adjoints of the inputs; lb
+// (p0x p0y p1x p1y) accumulates the adjoints of the manifold's local points.
+__device__ inline void solve_position_vjp(const ContactK& k, const DConf& c, const float* p, const float* yb, float* pb,
+                                          float* lb) {
     for (int i = 0; i < 6; ++i) pb[i] = yb[i];
     if (k.count == 1u) {
-        pos_point_vjp(k, c, 0, p, yb, pb);
+        pos_point_vjp(k, c, 0, p, yb, pb, lb);
     } else if (k.count == 2u) {
         const XfT<float> xfA = get_xft(p[0], p[1], p[2], k.mA.z, k.mA.w), xfB = get_xft(p[3], p[4], p[5], k.mB.z, k.mB.w);
         const float sep0 = get_psmt(k, 0, xfA, xfB).sep, sep1 = get_psmt(k, 1, xfA, xfB).sep;
         if (almost_equal(sep0, sep1)) {
-            pos_point_vjp(k, c, 0, p, yb, pb);
-            pos_point_vjp(k, c, 1, p, yb, pb);
+            pos_point_vjp(k, c, 0, p, yb, pb, lb);
+            pos_point_vjp(k, c, 1, p, yb, pb, lb);
         } else if (sep0 < sep1 || sep1 < sep0) {
             // p1 = p + s_first(p); p2 = p1 + s_second(p1)
             const int first = (sep0 < sep1) ? 0 : 1;
@@ -866,9 +886,9 @@ __device__ inline void solve_position_vjp(const ContactK& k, const DConf& c, con
             const float p1[6] = {q.ax + s0[0], q.ay + s0[1], q.az + s0[2], q.bx + s0[3], q.by + s0[4], q.bz + s0[5]};
             float b1[6];
             for (int i = 0; i < 6; ++i) b1[i] = yb[i];
-            pos_point_vjp(k, c, 1 - first, p1, yb, b1);
+            pos_point_vjp(k, c, 1 - first, p1, yb, b1, lb);
             for (int i = 0; i < 6; ++i) pb[i] = b1[i];
-            pos_point_vjp(k, c, first, p, b1, pb);
+            pos_point_vjp(k, c, first, p, b1, pb, lb);
         }
     }
 }
@@ -1083,9 +1103,10 @@ __device__ inline void warm_start_vjp(const ContactK& k, const Geom<float>& g, c
 
 // Reverse of build_geom in float: from the geometry's adjoints gb (packed order)
 // to the adjoints of the positions (pb) and velocities (vb) it was built from
-// (x y angle of A then B) and of the friction (*mub).
+// (x y angle of A then B) and of the friction (*mub); lb (p0x p0y p1x p1y)
+// accumulates the adjoints of the manifold's local points.
 __device__ inline void build_geom_vjp(const ContactK& k, const Pair3<float>& p, const Pair3<float>& v, float mu,
-                                      const DConf& c, const float* gb, float* pb, float* vb, float* mub) {
+                                      const DConf& c, const float* gb, float* pb, float* vb, float* mub, float* lb) {
     for (int i = 0; i < 6; ++i) pb[i] = vb[i] = 0.f;
     *mub = gb[GB_MU];
     // forward values
@@ -1217,6 +1238,7 @@ __device__ inline void build_geom_vjp(const ContactK& k, const Pair3<float>& p, 
             ppbx += sb * nn.x; ppby += sb * nn.y;
             nnbx -= sb * ex; nnby -= sb * ey;
             xipx += clbx; xipy += clby; rot_qbar(plp[i].x, plp[i].y, clbx, clby, qix, qiy);
+            rot_lbar(xi.q.x, xi.q.y, clbx, clby, lb + 2 * i);
         }
         float xrpx = ppbx, xrpy = ppby, qrx = 0.f, qry = 0.f;
         rot_qbar(lp.x, lp.y, ppbx, ppby, qrx, qry);

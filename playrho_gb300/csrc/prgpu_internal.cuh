@@ -299,6 +299,7 @@ struct DW {
     uint32_t* cs_colour;     // colour the contact had in the last step (first choice next step)
     float* cs_toi;           // time of impact (valid with CF_TOI_VALID)
     uint64_t* cs_seq;        // creation sequence: orders a world's contacts as its contact list does
+    uint32_t* cs_prio;       // colouring priority (a hash of the world-local proxy pair), set at creation
     uint32_t* cs_toi_ep;     // TOI phase: epoch of the contact's last Update
     uint32_t* cs_toi_at;     // TOI phase: epoch at which its time of impact was computed
     uint64_t* t_key;         // TOI phase: key-sorted list of the impenetrable contacts
@@ -373,6 +374,22 @@ __device__ __forceinline__ void atomic_min_float(float* addr, float v) {
 __device__ __forceinline__ void atomic_max_nonneg_float(float* addr, float v) {
     // For non-negative finite floats the IEEE bit pattern orders like the value.
     atomicMax(reinterpret_cast<unsigned int*>(addr), __float_as_uint(v));
+}
+
+// Colouring priorities hash world-local identifiers, so that a world is
+// coloured the same whether it is stepped alone or in a batch.
+__device__ __forceinline__ uint32_t prio_mix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
+}
+// The priority of the contact of proxies pa < pb (global indices).
+__device__ __forceinline__ uint32_t contact_prio(const DW& d, uint32_t pa, uint32_t pb) {
+    const uint32_t base = d.w_shape_off[d.b_world[d.s_body[pa]]];
+    return prio_mix32(((pa - base) * 0x9E3779B1u) ^ prio_mix32(pb - base));
 }
 
 __device__ __forceinline__ void set_error(Counters* c, uint32_t code, uint32_t where) {

@@ -65,6 +65,7 @@ struct AdjState {
 };
 
 constexpr uint32_t kAdjSweepMaxThreads = 512;
+constexpr int kAdjGeomWords = 28;  // words per recorded constraint in gbar, gval and gdot
 
 struct TanState {
     double* pdot;   // [N*3]

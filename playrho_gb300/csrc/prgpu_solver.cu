@@ -252,14 +252,6 @@ constexpr int kMaxColourRounds = 64;
 // a joint), so a world is coloured the same whether it is stepped alone or in
 // a batch; ties fall back to the constraint index, whose order within a world
 // is also the same in both cases.
-__device__ __forceinline__ uint32_t mix32(uint32_t h) {
-    h ^= h >> 16;
-    h *= 0x85EBCA6Bu;
-    h ^= h >> 13;
-    h *= 0xC2B2AE35u;
-    h ^= h >> 16;
-    return h;
-}
 __device__ __forceinline__ bool colour_beats(const DW& d, uint32_t o, uint32_t k) {
     const uint32_t a = d.k_prio[o], b = d.k_prio[k];
     return (a < b) || (a == b && o < k);
@@ -270,11 +262,9 @@ __device__ __forceinline__ uint32_t constraint_prio(const DW& d, uint32_t id) {
         const uint32_t j = id & 0x7fffffffu;
         const uint32_t a = d.j_bodies[2 * j], b = d.j_bodies[2 * j + 1];
         const uint32_t base = d.w_body_off[d.b_world[a]];
-        return mix32(((a - base) * 0x9E3779B1u) ^ mix32((b - base) + 0x7F4A7C15u) ^ 0xA5A5A5A5u);
+        return prio_mix32(((a - base) * 0x9E3779B1u) ^ prio_mix32((b - base) + 0x7F4A7C15u) ^ 0xA5A5A5A5u);
     }
-    const uint2 pr = d.cs_proxy[id];
-    const uint32_t base = d.w_shape_off[d.b_world[d.s_body[pr.x]]];
-    return mix32(((pr.x - base) * 0x9E3779B1u) ^ mix32(pr.y - base));
+    return d.cs_prio[id];  // contact_prio of the slot's proxy pair, kept since its creation
 }
 
 __device__ __forceinline__ uint32_t colour_hint(const DW& d, uint32_t id) {
@@ -317,7 +307,9 @@ __device__ __forceinline__ void colour_pick(const DW& d, uint32_t k, int round) 
     }
     const uint32_t id = d.k_list[k];
     uint32_t bs[4];
-    const int nb = constraint_body_set(d, id, bs);
+    // In round 0 no constraint is committed yet (k_inc_count cleared them all),
+    // so no colour is forbidden and the neighbours need not be read.
+    const int nb = (round == 0) ? 0 : constraint_body_set(d, id, bs);
     uint64_t forbid = 0;
     for (int e = 0; e < nb; ++e) {
         const uint32_t x = bs[e];

@@ -4,10 +4,15 @@
 #pragma once
 
 #include "prgpu_diff.cuh"
+#include "prgpu_kernels.cuh"
 
 namespace prgpu {
 
-constexpr int kGeomWords = 24;  // n rA0 rB0 rA1 rB1 nm0 tm0 nm1 tm1 vb0 vb1 k00 k11 k01 m00 m11 m01 mu cnt
+// n rA0 rB0 rA1 rB1 nm0 tm0 nm1 tm1 vb0 vb1 k00 k11 k01 m00 m11 m01 mu cnt, then
+// the manifold's local points p0 p1 (words kLocalPts..+3: their adjoints in gbar,
+// their tangents in gdot)
+constexpr int kGeomWords = kAdjGeomWords;
+constexpr int kLocalPts = 24;
 constexpr int kTapeHdrMismatch = kSerialColour + 5;  // hdr word counting replay mismatches
 
 __device__ __forceinline__ diff::ContactK contact_k(const DW& d, const PC& pc, float4 ci) {
@@ -20,6 +25,7 @@ __device__ __forceinline__ diff::ContactK contact_k(const DW& d, const PC& pc, f
     k.p0x = pc.p0x; k.p0y = pc.p0y; k.p1x = pc.p1x; k.p1y = pc.p1y;
     k.writableA = is_accelerable(d.b_flags[pc.bA]) ? 1u : 0u;
     k.writableB = is_accelerable(d.b_flags[pc.bB]) ? 1u : 0u;
+    k.dp[0] = k.dp[1] = k.dp[2] = k.dp[3] = 0.0;
     return k;
 }
 

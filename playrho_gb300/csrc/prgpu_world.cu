@@ -972,7 +972,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_m2, J); AL(d.j_imp, J);
     AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
     AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C); AL(d.cs_tspeed, C);
-    AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C);
+    AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C); AL(d.cs_prio, C);
     ALS(d.cs_toi_ep, C); ALS(d.cs_toi_at, C); ALS(d.t_key, C); ALS(d.t_slot, C);
     AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
     ALS(d.n_key, K); ALS(d.n_key_alt, K); ALS(d.n_val, K); ALS(d.n_val_alt, K);
@@ -1897,7 +1897,7 @@ int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every) {
                             ptr = reinterpret_cast<decltype(ptr)>(q_); } while (0)
     AA(a->adj.pbar, sizeof(float4) * N); AA(a->adj.vbar, sizeof(float4) * N); AA(a->adj.vibar, sizeof(float4) * N);
     AA(a->adj.vi, sizeof(float4) * N); AA(a->adj.lbar, sizeof(float4) * K);
-    AA(a->adj.gbar, sizeof(float) * 24 * (size_t)K); AA(a->adj.gval, sizeof(float) * 24 * (size_t)K);
+    AA(a->adj.gbar, sizeof(float) * kAdjGeomWords * (size_t)K); AA(a->adj.gval, sizeof(float) * kAdjGeomWords * (size_t)K);
     AA(a->adj.mbar, sizeof(float4) * C); AA(a->adj.mtmp, sizeof(float4) * C); AA(a->adj.fbar, sizeof(float) * S);
     AA(a->adj.err, sizeof(uint32_t) * 2);
     AA(a->adj.jbar, sizeof(float4) * std::max<uint32_t>(w->d.n_joints, 1));
@@ -1908,10 +1908,10 @@ int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every) {
     AA(a->tan.jdot, sizeof(double) * 2 * std::max<uint32_t>(w->d.n_joints, 1));
     AA(a->tan.pdot, sizeof(double) * 3 * N); AA(a->tan.vdot, sizeof(double) * 3 * N);
     AA(a->tan.vidot, sizeof(double) * 3 * N); AA(a->tan.ldot, sizeof(double) * 4 * (size_t)K);
-    AA(a->tan.gdot, sizeof(double) * 24 * (size_t)K); AA(a->tan.mdot, sizeof(double) * 4 * (size_t)C);
+    AA(a->tan.gdot, sizeof(double) * kAdjGeomWords * (size_t)K); AA(a->tan.mdot, sizeof(double) * 4 * (size_t)C);
     AA(a->tan.mtmp, sizeof(double) * 4 * (size_t)C); AA(a->fdot, sizeof(double) * S);
     a->tan.fdot = a->fdot;
-    AA(a->tgval, sizeof(float) * 24 * (size_t)K);
+    AA(a->tgval, sizeof(float) * kAdjGeomWords * (size_t)K);
     return PRGPU_OK;
 }
 
