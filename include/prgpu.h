@@ -295,11 +295,34 @@ int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, 
                             uint32_t* features2);
 /* Query(tree, aabb, callback) over one world's broadphase tree (DynamicTree.cpp:673-710):
  * the world-local shape IDs whose fat AABB overlaps `aabb` (minx miny maxx maxy), by
- * TestOverlap, in ascending order (the reference visits them in tree order).  Valid
- * after the first step, which creates the proxies; more than `capacity` overlaps
- * returns PRGPU_ECAPACITY with *n_out set. */
+ * TestOverlap, in ascending order (the reference visits them in tree order).  The
+ * walk runs on the world's subtree of the step's LBVH.  Valid after the first step,
+ * which creates the proxies; more than `capacity` overlaps returns PRGPU_ECAPACITY
+ * with *n_out set. */
 int prgpu_query_aabb(prgpu_world* w, uint32_t world, const float* aabb4, uint32_t capacity, uint32_t* n_out,
                      uint32_t* shapes);
+/* n queries at once, one thread per query: query k takes worlds[k] and
+ * aabb4[4k..4k+3]; counts[k] = its number of overlaps and shapes[k*capacity ..]
+ * its first min(counts[k], capacity) shape IDs, ascending.  shapes may be NULL
+ * (counts only); PRGPU_ECAPACITY if a query has more than capacity overlaps. */
+int prgpu_query_aabbs(prgpu_world* w, uint32_t n, const uint32_t* worlds, const float* aabb4, uint32_t capacity,
+                      uint32_t* counts, uint32_t* shapes);
+/* RayCast(World, RayCastInput, callback) (RayCastOutput.cpp:241-337) with a
+ * callback that answers RayCastOpcode::ClipRay to every hit, for n rays at once:
+ * ray k in worlds[k] from p1 to p2 up to maxFraction (rays5[5k..] = p1x p1y p2x
+ * p2y maxFraction).  shapes[k] = the world-local shape of its nearest hit (-1:
+ * none; ties go to the lower shape ID, where the reference's answer depends on
+ * its tree order) and hits5[5k..] = fraction, point x y (p1 + (p2 - p1) *
+ * fraction), normal x y, as the shape RayCast (RayCastOutput.cpp:41-233)
+ * computes them.  Valid after the first step. */
+int prgpu_raycast(prgpu_world* w, uint32_t n, const uint32_t* worlds, const float* rays5, int32_t* shapes,
+                  float* hits5);
+/* The same ray with a callback that answers RayCastOpcode::ResetRay: every shape
+ * the ray hits, ascending by shape ID, with hits5 as above; *n_out = their
+ * number; PRGPU_ECAPACITY if more than capacity (shapes and hits5 may be NULL to
+ * count). */
+int prgpu_raycast_all(prgpu_world* w, uint32_t world, const float* ray5, uint32_t capacity, uint32_t* n_out,
+                      int32_t* shapes, float* hits5);
 /* The creation sequence number of each live contact, in the order of
  * prgpu_download_contacts.  Sorting a world's contacts by it gives the order of the
  * reference's contact list (AabbTreeWorld::m_contacts), the order in which Step
@@ -332,6 +355,28 @@ int prgpu_download_contacts_noalloc(prgpu_world* w, uint32_t capacity, uint32_t*
  *   mat4[4i..] friction, restitution, tangent speed, enabled (1 or 0) (Contact.hpp)
  * Either array may be NULL. */
 int prgpu_download_contact_state(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* slots, float* mat4);
+/* Records for the PreSolveContact / PostSolveContact listeners
+ * (ContactManifoldFunction, ContactImpulsesFunction; called by the reference at
+ * AabbTreeWorld.cpp:2716-2720 and :1669-1672).  Enabling keeps, for every contact
+ * the regular phase solves, its velocity constraint's impulses and its island's
+ * iteration argument; it allocates 24 bytes per contact slot on first use and
+ * re-captures the step.  Off by default. */
+int prgpu_set_solve_records(prgpu_world* w, int enabled);
+/* The live contacts the last step updated (AabbTreeWorld::Update) or solved, in no
+ * particular order (*n_out of them; with every array NULL only *n_out is set):
+ *   slots[i]     the contact's slot
+ *   info[i]      bits 0-2: phases that updated it (1: the step's pre-phase,
+ *                UpdateContacts and AddContacts, :2186-2198; 2: the regular phase's
+ *                post-solve pass, :1549-1557; 4: the time-of-impact phase);
+ *                bit 3: solved by the regular phase (needs prgpu_set_solve_records);
+ *                bits 4-7: its velocity constraint's point count; bits 8-15: the
+ *                iteration argument (the position iteration at which the island
+ *                reached tolerance, else 255 = StepConf::InvalidIteration)
+ *   imp4[4i..]   the solved normal and tangent impulses of points 0 and 1
+ *                (GetContactImpulses, ContactImpulsesList.cpp:28-38)
+ * PRGPU_ECAPACITY (with *n_out set) if there are more than capacity records. */
+int prgpu_download_solve_records(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* slots, uint32_t* info,
+                                 float* imp4);
 /* SetContact(World&, ContactID, Contact) (AabbTreeWorld.cpp:2797-2832) for the
  * fields the step reads: a disabled contact stays out of the islands and the
  * solver (AabbTreeWorld.cpp:1433) and out of the time-of-impact phase

@@ -87,6 +87,10 @@ def _lib(double: bool):
     lib.or_add_gear.restype = ctypes.c_int
     lib.or_events.argtypes = [P, ctypes.c_void_p, ctypes.c_int]
     lib.or_events.restype = ctypes.c_int
+    lib.or_solve_calls.argtypes = [P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    lib.or_solve_calls.restype = ctypes.c_int
+    lib.or_raycast.argtypes = [P, real, real, real, real, real, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.or_raycast.restype = ctypes.c_int
     lib.or_default_conf.argtypes = [ctypes.POINTER(Conf)]
     lib.or_step.argtypes = [P, ctypes.POINTER(Conf), ctypes.POINTER(Stats)]
     lib.or_body_count.argtypes = [P]
@@ -218,6 +222,29 @@ class OracleWorld:
         buf = np.zeros(max(3 * n, 3), np.int32)
         self.lib.or_events(self.h, buf.ctypes.data, n)
         return [tuple(int(x) for x in buf[3 * i:3 * i + 3]) for i in range(n)]
+
+    def solve_calls(self) -> list:
+        """PreSolveContact (3) / PostSolveContact (4) listener calls of the last step,
+        in call order, as (kind, lower shape ID, higher shape ID, point count,
+        iteration, ni0, ti0, ni1, ti1): preSolve's manifold before the update (the
+        iteration is 0), postSolve's velocity-constraint impulses and its
+        iteration argument (255: not solved)."""
+        n = self.lib.or_solve_calls(self.h, None, None, 0)
+        ints = np.zeros(max(5 * n, 5), np.int32)
+        imp = np.zeros(max(4 * n, 4), np.float64)
+        self.lib.or_solve_calls(self.h, ints.ctypes.data, imp.ctypes.data, n)
+        return [tuple(int(x) for x in ints[5 * i:5 * i + 5]) + tuple(float(x) for x in imp[4 * i:4 * i + 4])
+                for i in range(n)]
+
+    def raycast(self, p1, p2, max_fraction=1.0) -> list:
+        """RayCast of the world with a callback that answers ResetRay: every shape
+        hit, in shape order, as (shape, fraction, point x, point y, normal x, normal y)."""
+        n = self.lib.or_raycast(self.h, *(float(v) for v in (p1[0], p1[1], p2[0], p2[1], max_fraction)), 0, None, None)
+        shapes = np.zeros(max(n, 1), np.int32)
+        hits = np.zeros((max(n, 1), 5), self.np_real)
+        self.lib.or_raycast(self.h, *(float(v) for v in (p1[0], p1[1], p2[0], p2[1], max_fraction)), n,
+                            shapes.ctypes.data, hits.ctypes.data)
+        return [(int(shapes[k]),) + tuple(hits[k]) for k in range(n)]
 
     def contacts(self) -> dict:
         n = self.lib.or_contact_count(self.h)

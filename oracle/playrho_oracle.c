@@ -245,6 +245,7 @@ struct or_world {
     ivec proxiesForContacts;
     real inv_dt0;
     ivec events;            /* the last step's contact listener calls: (kind, shape, shape) */
+    ivec solve_calls;       /* the last step's preSolve / postSolve calls, 9 words each */
     /* or_set_solve_order: ranks of contacts (by shape pair) and joints for the
      * next step's island solves; empty: the reference's order */
     ivec order_ckeys;       /* (shape min << 32 | shape max), sorted */
@@ -258,6 +259,29 @@ static void record_event(or_world* w, int kind, const contact_t* c) {
     iv_push(&w->events, kind);
     iv_push(&w->events, c->sA < c->sB ? c->sA : c->sB);
     iv_push(&w->events, c->sA < c->sB ? c->sB : c->sA);
+}
+
+/* A PreSolveContact (kind 3: the manifold before the update, AabbTreeWorld.cpp:
+ * 2716-2720) or PostSolveContact (kind 4: the velocity constraint's impulses,
+ * GetContactImpulses, ContactImpulsesList.cpp:28-38, and the iteration argument,
+ * AabbTreeWorld.cpp:196-205) listener call: kind, shapes in ascending order,
+ * point count, iteration, then the two points' normal and tangent impulses as
+ * the bits of doubles. */
+static void record_solve_call(or_world* w, int kind, const contact_t* c, int count, int iter, const real* ni,
+                              const real* ti) {
+    iv_push(&w->solve_calls, kind);
+    iv_push(&w->solve_calls, c->sA < c->sB ? c->sA : c->sB);
+    iv_push(&w->solve_calls, c->sA < c->sB ? c->sB : c->sA);
+    iv_push(&w->solve_calls, count);
+    iv_push(&w->solve_calls, iter);
+    for (int k = 0; k < 2; ++k) {
+        const double v[2] = {k < count ? (double)ni[k] : 0.0, k < count ? (double)ti[k] : 0.0};
+        for (int q = 0; q < 2; ++q) {
+            int64_t bits;
+            memcpy(&bits, &v[q], sizeof bits);
+            iv_push(&w->solve_calls, bits);
+        }
+    }
 }
 
 #define GROW(ptr, n, cap, T)                                                   \
@@ -315,6 +339,7 @@ void or_world_destroy(or_world* w) {
     iv_free(&w->cfree); iv_free(&w->wkeys); iv_free(&w->wcids);
     iv_free(&w->fixturesForProxies); iv_free(&w->bodiesForSync); iv_free(&w->proxiesForContacts);
     iv_free(&w->events);
+    iv_free(&w->solve_calls);
     iv_free(&w->order_ckeys); iv_free(&w->order_crank); iv_free(&w->order_jrank);
     free(w);
 }
@@ -925,6 +950,8 @@ static int kv_find(const ivec* ids, int64_t id) {
     return -1;
 }
 
+static int sensor_touching(const dproxy* A, xf_t xfA, const dproxy* B, xf_t xfB, int maxIters);
+
 /* AabbTreeWorld::Update(ContactID) (AabbTreeWorld.cpp:2587-2721). */
 static void contact_update(or_world* w, int cid, const or_stepconf* conf) {
     contact_t* c = &w->c[cid];
@@ -935,8 +962,8 @@ static void contact_update(or_world* w, int cid, const or_stepconf* conf) {
     const shape_t* sB = &w->s[c->sB];
     int newTouching;
     if (c->sensor) {
-        /* sensors: TestOverlap via GJK is not restated; configs use no sensors */
-        newTouching = 0;
+        /* TestOverlap (:2622-2625); sensors make no manifold (:2634) */
+        newTouching = sensor_touching(&sA->dp, bA->xf, &sB->dp, bB->xf, conf->maxDistanceIters);
         c->m = man_empty();
     } else {
         manifold nm = collide_shapes(&sA->dp, bA->xf, &sB->dp, bB->xf, conf->linearSlop, conf->maxCirclesRatio);
@@ -968,6 +995,10 @@ static void contact_update(or_world* w, int cid, const or_stepconf* conf) {
     if (!c->touching && newTouching) record_event(w, 1, c);
     else if (c->touching && !newTouching) record_event(w, 2, c);
     c->touching = newTouching;
+    if (!c->sensor && newTouching) {
+        const real ni[2] = {old.p[0].ni, old.p[1].ni}, ti[2] = {old.p[0].ti, old.p[1].ti};
+        record_solve_call(w, 3, c, old.count, 0, ni, ti);
+    }
 }
 
 /* InternalDestroy(ContactID) (AabbTreeWorld.cpp:2245-2279). */
@@ -3046,6 +3077,8 @@ static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc
         contact_t* c = &w->c[isl->contacts.a[i]];
         for (int k = 0; k < vcs[i].count; ++k) { c->m.p[k].ni = vcs[i].p[k].ni; c->m.p[k].ti = vcs[i].p[k].ti; }
     }
+    /* Report to PostSolveContact after the write-back (:1669-1672) */
+    const int post_iter = solved ? posIters - 1 : 255;  /* StepConf::InvalidIteration */
     /* write back (:1652-1664) */
     for (int i = 0; i < isl->bodies.n; ++i) {
         const int id = (int)isl->bodies.a[i];
@@ -3056,6 +3089,10 @@ static void solve_island(or_world* w, const or_stepconf* conf, island_t* isl, bc
             body_set_pos1(b, bc->pos);
             for (int k = 0; k < b->cids.n; ++k) w->c[b->cids.a[k]].needsUpdate = 1;
         }
+    }
+    for (int i = 0; i < nc; ++i) {
+        const real ni[2] = {vcs[i].p[0].ni, vcs[i].p[1].ni}, ti[2] = {vcs[i].p[0].ti, vcs[i].p[1].ti};
+        record_solve_call(w, 4, &w->c[isl->contacts.a[i]], vcs[i].count, post_iter, ni, ti);
     }
     /* UpdateUnderActiveTimes + Sleepem (:403-429) */
     real minUat = RINF;
@@ -3345,6 +3382,20 @@ static void witness_points(const simplex_t* s, v2* pA, v2* pB) {
     *pA = a; *pB = b;
 }
 
+/* TestOverlap (Distance.cpp:205-216) >= 0: GJK Distance from an empty cache
+ * (GetDistanceConf(StepConf), DistanceConf.cpp:36-41), then the total vertex
+ * radius squared less the squared distance of the witness points. */
+static int sensor_touching(const dproxy* A, xf_t xfA, const dproxy* B, xf_t xfB, int maxIters) {
+    scache cache;
+    memset(&cache, 0, sizeof(cache));
+    const dist_out di = gjk_distance(A, xfA, B, xfB, &cache, maxIters);
+    v2 pa, pb;
+    witness_points(&di.s, &pa, &pb);
+    const real d2 = mag2(vsub(pb, pa));
+    const real tr = A->r + B->r;
+    return (tr * tr - d2) >= R(0);
+}
+
 /* SeparationScenario (SeparationScenario.cpp). */
 enum { SEP_POINTS = 0, SEP_FACE_A = 1, SEP_FACE_B = 2 };
 typedef struct { int type; v2 axis; v2 lp; } sepfn;
@@ -3612,6 +3663,11 @@ static void solve_toi_island(or_world* w, const or_stepconf* conf, island_t* isl
             flag_body_contacts(w, b);
         }
     }
+    /* Report to PostSolveContact (AabbTreeWorld.cpp:2053-2055) */
+    for (int i = 0; i < nc; ++i) {
+        const real ni[2] = {vcs[i].p[0].ni, vcs[i].p[1].ni}, ti[2] = {vcs[i].p[0].ti, vcs[i].p[1].ti};
+        record_solve_call(w, 4, &w->c[isl->contacts.a[i]], vcs[i].count, *posIters, ni, ti);
+    }
     if (solved) st->toiIslandsSolved++;
     st->toiMinSeparation = minr(st->toiMinSeparation, minSepAll);
     st->toiMaxIncImpulse = maxr(st->toiMaxIncImpulse, maxInc);
@@ -3795,6 +3851,7 @@ void or_step(or_world* w, const or_stepconf* conf, or_stepstats* st) {
     if (!st) st = &local;
     memset(st, 0, sizeof(*st));
     w->events.n = 0;
+    w->solve_calls.n = 0;
     st->regMinSeparation = RINF;
     for (int i = 0; i < w->fixturesForProxies.n; ++i) {
         const int body = (int)(w->fixturesForProxies.a[i] >> 32);
@@ -3933,6 +3990,105 @@ int or_proxy_count(const or_world* w) { return w->np; }
 void or_get_proxy(const or_world* w, int p, int* bsc, real* aabb) {
     bsc[0] = w->p[p].body; bsc[1] = w->p[p].shape; bsc[2] = w->p[p].child;
     memcpy(aabb, w->p[p].aabb, 4 * sizeof(real));
+}
+
+/* RayCast(radius, location, input) (RayCastOutput.cpp:41-71). */
+static int ray_circle(real radius, v2 loc, v2 p1, v2 p2, real maxF, real* frac, v2* normal) {
+    const v2 s = vsub(p1, loc);
+    const real b = mag2(s) - radius * radius;
+    const v2 seg = vsub(p2, p1);
+    const real c = dot(s, seg);
+    const real rr = mag2(seg);
+    const real sigma = (c * c) - rr * b;
+    if ((sigma < R(0)) || almost_zero(rr)) return 0;
+    const real a = -(c + RSQRT(sigma));
+    const real f = a / rr;
+    if ((f >= R(0)) && (f <= maxF)) {
+        *frac = f;
+        *normal = unit_vector(vadd(s, vmul(seg, f)), V(R(0), R(0)));
+        return 1;
+    }
+    return 0;
+}
+
+/* RayCast(DistanceProxy, input, transform) (RayCastOutput.cpp:132-233). */
+static int ray_proxy(const dproxy* P, xf_t xf, v2 p1, v2 p2, real maxF, real* frac, v2* normal) {
+    const real radius = P->r;
+    v2 v0 = P->v[0];
+    if (P->count == 1) return ray_circle(radius, xform(v0, xf), p1, p2, maxF, frac, normal);
+    const v2 r0 = invxform(p1, xf), r1 = invxform(p2, xf);
+    const v2 ray = vsub(r1, r0);
+    real minT = RNEXT(maxF, R(2));
+    v2 found = V(R(0), R(0));
+    for (int i = 0; i < P->count; ++i) {
+        real cf;
+        v2 cn;
+        if (ray_circle(radius, v0, r0, r1, maxF, &cf, &cn) && (minT > cf)) { minT = cf; found = cn; }
+        const v2 v1 = P->v[(i + 1) % P->count];
+        const v2 edge = vsub(v1, v0);
+        const real rxe = cross(ray, edge);
+        if (!almost_zero(rxe)) {
+            const v2 n = P->n[i];
+            const v2 q = vsub(vadd(v0, vmul(n, radius)), r0);
+            const real inv = R(1) / rxe;
+            const real t = cross(q, edge) * inv;
+            const real u = cross(q, ray) * inv;
+            if ((t >= R(0)) && (t <= R(1)) && (u >= R(0)) && (u <= R(1)) && (minT > t)) { minT = t; found = n; }
+        }
+        v0 = v1;
+    }
+    if (minT <= maxF) {
+        *frac = minT;
+        *normal = rotate(found, xf.q);
+        return 1;
+    }
+    return 0;
+}
+
+/* RayCast(World, input, callback) (RayCastOutput.cpp:301-337) with a callback
+ * that answers ResetRay: every shape with a proxy that the ray hits.  Up to cap
+ * hits in shape order into shapes and hit5 (fraction, point = p1 + (p2 - p1) *
+ * fraction, normal); returns how many there were.  The tree walk only prunes:
+ * a shape the ray hits lies inside its fat AABB. */
+int or_raycast(const or_world* w, real p1x, real p1y, real p2x, real p2y, real maxF, int cap, int* shapes,
+               real* hit5) {
+    const v2 p1 = V(p1x, p1y), p2 = V(p2x, p2y);
+    int n = 0;
+    for (int p = 0; p < w->np; ++p) {
+        const int s = w->p[p].shape;
+        real f;
+        v2 nrm;
+        if (!ray_proxy(&w->s[s].dp, w->b[w->p[p].body].xf, p1, p2, maxF, &f, &nrm)) continue;
+        if (n < cap) {
+            /* insertion in shape order */
+            int k = n;
+            while (k > 0 && shapes[k - 1] > s) {
+                shapes[k] = shapes[k - 1];
+                for (int q = 0; q < 5; ++q) hit5[5 * k + q] = hit5[5 * (k - 1) + q];
+                --k;
+            }
+            const v2 pt = vadd(p1, vmul(vsub(p2, p1), f));
+            shapes[k] = s;
+            hit5[5 * k] = f; hit5[5 * k + 1] = pt.x; hit5[5 * k + 2] = pt.y;
+            hit5[5 * k + 3] = nrm.x; hit5[5 * k + 4] = nrm.y;
+        }
+        ++n;
+    }
+    return n;
+}
+
+/* The PreSolveContact / PostSolveContact calls of the last or_step, in call
+ * order: up to cap records of 5 ints (kind 3 or 4, lower shape, higher shape,
+ * point count, iteration) into ints and 4 doubles (normal and tangent impulse
+ * of both points) into imp; returns how many calls there were. */
+int or_solve_calls(const or_world* w, int* ints, double* imp, int cap) {
+    const int n = w->solve_calls.n / 9;
+    for (int i = 0; i < n && i < cap; ++i) {
+        const int64_t* r = w->solve_calls.a + 9 * i;
+        for (int k = 0; k < 5; ++k) ints[5 * i + k] = (int)r[k];
+        for (int k = 0; k < 4; ++k) memcpy(&imp[4 * i + k], &r[5 + k], sizeof(double));
+    }
+    return n;
 }
 
 /* The contact listener calls of the last or_step: up to cap (kind, shape,

@@ -127,6 +127,14 @@ void or_step(or_world* w, const or_stepconf* conf, or_stepstats* stats);
 /* BeginContact (kind 1) and EndContact (kind 2) listener calls of the last
  * or_step, in call order, as (kind, lower shape ID, higher shape ID) triples. */
 int or_events(const or_world* w, int* out, int cap);
+/* PreSolveContact (kind 3) / PostSolveContact (kind 4) calls of the last step:
+ * per call 5 ints (kind, lower shape, higher shape, point count, iteration) and
+ * 4 doubles (normal and tangent impulse of points 0 and 1). */
+int or_solve_calls(const or_world* w, int* ints, double* imp, int cap);
+/* Every shape the ray p1 -> p2 (up to maxF) hits, in shape order: shapes[k] and
+ * hit5[5k..] = fraction, point xy, normal xy; returns the number of hits. */
+int or_raycast(const or_world* w, or_real p1x, or_real p1y, or_real p2x, or_real p2y, or_real maxF, int cap,
+               int* shapes, or_real* hit5);
 
 /* Body queries. */
 int or_body_count(const or_world* w);

@@ -12,10 +12,12 @@
 //         motorSpeed maxMotorTorque collideConnected
 //   step N            (runs N steps; may repeat)
 //   dump              (prints bodies, contacts and proxies)
+//   ray x1 y1 x2 y2 maxFraction   (prints every shape the ray hits)
 //   defaults          (prints the StepConf defaults)
 #include "ref_scene.hpp"
 
 #include <playrho/d2/DynamicTree.hpp>
+#include <playrho/d2/RayCastOutput.hpp>
 
 #include <algorithm>
 #include <cstdio>
@@ -139,6 +141,35 @@ int main()
     };
     SetBeginContactListener(world, [event](ContactID id) { event(1, id); });
     SetEndContactListener(world, [event](ContactID id) { event(2, id); });
+    // PreSolveContact / PostSolveContact calls as "solve kind lowerShape higherShape
+    // count iteration ni0 ti0 ni1 ti1" lines (kind 3: the manifold before the
+    // update; kind 4: the solved impulses and the iteration argument)
+    const auto solveCall = [&world](int kind, ContactID id, int count, unsigned iter, const double* imp) {
+        const auto& c = GetContact(world, id);
+        const auto a = to_underlying(GetShapeA(c)), b = to_underlying(GetShapeB(c));
+        std::printf("solve %d %u %u %d %u", kind, static_cast<unsigned>(a < b ? a : b),
+                    static_cast<unsigned>(a < b ? b : a), count, iter);
+        for (int k = 0; k < 4; ++k) hex(imp[k]);
+        std::printf("\n");
+    };
+    SetPreSolveContactListener(world, [solveCall](ContactID id, const Manifold& old) {
+        double imp[4] = {0, 0, 0, 0};
+        const auto n = int(old.GetPointCount());
+        for (int k = 0; k < n; ++k) {
+            imp[2 * k] = double(old.GetPoint(k).normalImpulse / 1_Ns);
+            imp[2 * k + 1] = double(old.GetPoint(k).tangentImpulse / 1_Ns);
+        }
+        solveCall(3, id, n, 0u, imp);
+    });
+    SetPostSolveContactListener(world, [solveCall](ContactID id, const ContactImpulsesList& ci, unsigned iter) {
+        double imp[4] = {0, 0, 0, 0};
+        const auto n = int(ci.GetCount());
+        for (int k = 0; k < n; ++k) {
+            imp[2 * k] = double(ci.GetEntryNormal(k) / 1_Ns);
+            imp[2 * k + 1] = double(ci.GetEntryTanget(k) / 1_Ns);
+        }
+        solveCall(4, id, n, iter, imp);
+    });
     auto conf = StepConf{};
     conf.doToi = false;
     auto stats = StepStats{};
@@ -155,6 +186,25 @@ int main()
         else if (tag == "step") {
             int n = 0; in >> n;
             for (int i = 0; i < n; ++i) stats = Step(world, conf);
+        }
+        else if (tag == "ray") {
+            // RayCast(World, RayCastInput, callback) answering ResetRay: every hit as
+            // "rayhit shape point.x point.y normal.x normal.y", then "rayend"
+            double x1, y1, x2, y2, f;
+            in >> x1 >> y1 >> x2 >> y2 >> f;
+            auto input = RayCastInput{};
+            input.p1 = Length2{Real(x1) * Meter, Real(y1) * Meter};
+            input.p2 = Length2{Real(x2) * Meter, Real(y2) * Meter};
+            input.maxFraction = UnitInterval<Real>(Real(f));
+            RayCast(world, input, [](BodyID, ShapeID shape, ChildCounter, const Length2& pt, const UnitVec& n) {
+                std::printf("rayhit %u", static_cast<unsigned>(to_underlying(shape)));
+                hex(double(StripUnit(GetX(pt)))); hex(double(StripUnit(GetY(pt))));
+                hex(double(GetX(n))); hex(double(GetY(n)));
+                std::printf("\n");
+                return RayCastOpcode::ResetRay;
+            });
+            std::printf("rayend\n");
+            std::fflush(stdout);
         }
         else if (tag == "dump") {
             dump(world, stats);

@@ -58,17 +58,19 @@ def run(scene_text: str, steps, double: bool = False, timeout: float = 600.0):
     seq = [steps] if isinstance(steps, int) else list(steps)
     cmd = scene_text + "".join(f"step {n}\ndump\n" for n in seq)
     res = subprocess.run([path], input=cmd, capture_output=True, text=True, timeout=timeout, check=True)
-    dumps, cur, events = [], None, []
+    dumps, cur, events, calls = [], None, [], []
     for line in res.stdout.splitlines():
         t = line.split()
         if not t:
             continue
         if t[0] == "ev":
             events.append(tuple(int(x) for x in t[1:4]))
+        elif t[0] == "solve":
+            calls.append(tuple(int(x) for x in t[1:6]) + tuple(_f(x) for x in t[6:10]))
         elif t[0] == "stats":
             cur = {"stats": [int(x) for x in t[1:10]] + [_f(x) for x in t[10:12]],
-                   "bodies": [], "proxies": [], "contacts": [], "events": events}
-            events = []
+                   "bodies": [], "proxies": [], "contacts": [], "events": events, "solve_calls": calls}
+            events, calls = [], []
         elif t[0] == "toistats":
             cur["toistats"] = [int(x) for x in t[1:15]] + [_f(x) for x in t[15:17]]
         elif t[0] == "body":
@@ -83,6 +85,28 @@ def run(scene_text: str, steps, double: bool = False, timeout: float = 600.0):
         elif t[0] == "end":
             dumps.append(_finish(cur, double))
     return dumps
+
+
+def run_rays(scene_text: str, steps: int, rays, double: bool = False, timeout: float = 600.0):
+    """Steps the scene ``steps`` times, then casts each ray (x1, y1, x2, y2,
+    maxFraction) through RayCast(World, ...) with a callback answering ResetRay;
+    returns per ray the list of hits (shape, point x, point y, normal x, normal y)
+    in the reference's tree order."""
+    path = ensure_built(double)
+    cmd = scene_text + f"step {int(steps)}\n" + "".join("ray " + " ".join(repr(float(v)) for v in r) + "\n"
+                                                        for r in rays)
+    res = subprocess.run([path], input=cmd, capture_output=True, text=True, timeout=timeout, check=True)
+    out, cur = [], []
+    for line in res.stdout.splitlines():
+        t = line.split()
+        if not t:
+            continue
+        if t[0] == "rayhit":
+            cur.append((int(t[1]),) + tuple(_f(x) for x in t[2:6]))
+        elif t[0] == "rayend":
+            out.append(cur)
+            cur = []
+    return out
 
 
 def _finish(d, double):
@@ -105,4 +129,4 @@ def _finish(d, double):
                 "local_point": fo[:, 2:4], "points": fo[:, 4:12].reshape(n, 2, 4),
                 "features": ft.reshape(n, 2, 4)}
     return {"stats": d["stats"], "toistats": d.get("toistats"), "bodies": bodies, "proxies": proxies,
-            "contacts": contacts, "events": d["events"]}
+            "contacts": contacts, "events": d["events"], "solve_calls": d["solve_calls"]}

@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libprgpu.so")
 # C++ host layer over the C ABI (HostWorld), a second library linked to the first
 HOST_SOURCES = [os.path.join(HERE, "host", "host_world.cpp")]
 HOST_LIB = os.path.join(HERE, "libprgpu_host.so")
-SOURCES = ["prgpu_prims.cu", "prgpu_contacts.cu", "prgpu_solver.cu", "prgpu_toi.cu", "prgpu_world.cu",
+SOURCES = ["prgpu_prims.cu", "prgpu_contacts.cu", "prgpu_solver.cu", "prgpu_toi.cu", "prgpu_world.cu", "prgpu_query.cu",
            "prgpu_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",

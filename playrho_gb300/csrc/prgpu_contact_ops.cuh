@@ -7,6 +7,7 @@
 #include <cooperative_groups.h>
 
 #include "prgpu_collide.cuh"
+#include "prgpu_toi.cuh"
 #include "prgpu_internal.cuh"
 
 namespace prgpu {
@@ -126,6 +127,24 @@ __device__ __forceinline__ void store_manifold(const DW& d, uint32_t slot, const
     d.m_cf[slot] = make_uint2(m.cf[0], m.cf[1]);
 }
 
+// A sensor contact's touching state: TestOverlap (Distance.cpp:205-216) >= 0,
+// i.e. GJK Distance from an empty cache with StepConf::maxDistanceIters
+// (GetDistanceConf, DistanceConf.cpp:36-41), then the total vertex radius squared
+// less the squared distance of the witness points.
+static __device__ __noinline__ bool sensor_touching(const DW& d, uint2 pr, uint2 bd) {
+    Proxy A, B;
+    load_proxy(d, pr.x, A);
+    load_proxy(d, pr.y, B);
+    SCache cache;
+    cache.n = 0;
+    cache.metric = 0.f;
+    const DistOut di = gjk_distance(A, load_xf(d, bd.x), B, load_xf(d, bd.y), cache, d.conf->maxDistanceIters);
+    V2 wa, wb;
+    witness_points(di.s, wa, wb);
+    const float tr = A.r + B.r;
+    return (tr * tr - mag2(wb - wa)) >= 0.f;
+}
+
 // AabbTreeWorld::Update (AabbTreeWorld.cpp:2587-2721) without listeners.
 // src2 (optional): where the new manifold's points took their impulses from.
 static __device__ void update_contact(const DW& d, uint32_t slot, int8_t* src2 = nullptr) {
@@ -135,6 +154,7 @@ static __device__ void update_contact(const DW& d, uint32_t slot, int8_t* src2 =
     bool touching = false;
     int src[2] = {-1, -1};
     if (flags & CF_SENSOR) {
+        touching = sensor_touching(d, pr, bd);  // sensors make no manifold (:2634)
         store_manifold(d, slot, man_empty());
     } else {
         Proxy A, B;
@@ -150,6 +170,9 @@ static __device__ void update_contact(const DW& d, uint32_t slot, int8_t* src2 =
     flags &= ~CF_NEEDS_UPDATE;
     flags = touching ? (flags | CF_TOUCHING) : (flags & ~CF_TOUCHING);
     d.cs_flags[slot] = flags;
+    // which phases of this step updated the contact (the listener replay)
+    const uint32_t tag = d.cnt->step_no << 3, old = d.cs_upd[slot];
+    d.cs_upd[slot] = (((old & ~7u) == tag) ? old : tag) | d.cnt->upd_phase;
 }
 
 }  // namespace prgpu

@@ -417,6 +417,8 @@ __global__ void k_new_contacts(DW d) {
         // AddContacts appends in key order to the world's and both bodies' contact lists
         d.cs_seq[slot] = seq + i;
         d.cs_prio[slot] = contact_prio(d, pa, pb);
+        d.cs_upd[slot] = 0u;
+        if (d.cs_post_tag) d.cs_post_tag[slot] = make_uint2(0u, 0u);
         store_manifold(d, slot, man_empty());
         if (!sensor) {
             if (is_speedable(fa)) atomicOr(&d.b_flags[ba], BF_AWAKE);
@@ -530,6 +532,10 @@ void launch_destroy_contacts(const DW& d, const Launch& L, cudaStream_t s) {
     k_destroy_done<<<1, 1, 0, s>>>(d);
     k_copy_live<<<L.grid, L.threads, 0, s>>>(d);
 }
+
+__global__ void k_set_upd_phase(DW d, uint32_t phase) { d.cnt->upd_phase = phase; }
+
+void launch_set_upd_phase(const DW& d, uint32_t phase, cudaStream_t s) { k_set_upd_phase<<<1, 1, 0, s>>>(d, phase); }
 
 void launch_update_contacts(const DW& d, const Launch& L, uint32_t body_mask, cudaStream_t s) {
     k_update_contacts<<<L.grid, L.threads, 0, s>>>(d, body_mask);

@@ -52,6 +52,11 @@ enum : uint32_t {
     CF_DISABLED = 64u,        // Contact::e_enabledFlag unset (SetContact): not solved, not in islands
     CF_LIVE = 128u,           // the slot holds a live contact
 };
+// Phases of a step in which contacts are updated (AabbTreeWorld::Update): the
+// pre-phase (UpdateContacts and AddContacts of Step), the regular phase's
+// post-solve pass (SolveReg) and the time-of-impact phase.
+enum : uint32_t { kUpdPre = 1u, kUpdPost = 2u, kUpdToi = 4u };
+
 // A touching, enabled, non-sensor contact: one the islands and the solver take
 // (AddToIsland, AabbTreeWorld.cpp:1433).
 PR_HD bool contact_solvable(uint32_t f) { return (f & (CF_TOUCHING | CF_SENSOR | CF_DISABLED)) == CF_TOUCHING; }
@@ -155,6 +160,8 @@ struct Counters {
     uint32_t bar_count;
     uint32_t bar_gen;
     uint32_t need_find;
+    uint32_t step_no;         // steps begun (tags the contact updates and solve records of a step)
+    uint32_t upd_phase;       // phase bit the contact updates are tagged with (kUpd*)
     // StepStats counters (StepStats.hpp)
     uint32_t st_contacts_added;
     uint32_t st_contacts_destroyed;
@@ -296,6 +303,9 @@ struct DW {
     uint32_t* cs_flags;
     float2* cs_mat;          // friction restitution
     float* cs_tspeed;        // tangent speed (Contact::GetTangentSpeed; SetContact)
+    uint32_t* cs_upd;        // (step_no << 3) | phases of that step in which the contact was updated
+    float4* cs_post;         // solve records (while listening): impulses ni0 ti0 ni1 ti1 of the
+    uint2* cs_post_tag;      //   velocity constraint; (step_no, count | iteration << 8); null: off
     uint32_t* cs_colour;     // colour the contact had in the last step (first choice next step)
     float* cs_toi;           // time of impact (valid with CF_TOI_VALID)
     uint64_t* cs_seq;        // creation sequence: orders a world's contacts as its contact list does

@@ -20,6 +20,15 @@ struct Launch {
 void launch_pre_proxies(const DW& d, const Launch& L, cudaStream_t s);
 void launch_destroy_contacts(const DW& d, const Launch& L, cudaStream_t s);
 void launch_update_contacts(const DW& d, const Launch& L, uint32_t body_mask, cudaStream_t s);
+void launch_set_upd_phase(const DW& d, uint32_t phase, cudaStream_t s);
+void launch_post_record(const DW& d, const Launch& L, cudaStream_t s);
+// spatial queries over the step's LBVH (prgpu_query.cu)
+void launch_query_boxes(const DW& d, const Launch& L, uint32_t n, const uint32_t* worlds, const float4* boxes,
+                        uint32_t cap, uint32_t* counts, uint32_t* out, uint32_t* status, cudaStream_t s);
+void launch_ray_nearest(const DW& d, const Launch& L, uint32_t n, const uint32_t* worlds, const float* rays5,
+                        int32_t* shape_out, float* hit5, uint32_t* status, cudaStream_t s);
+void launch_ray_all(const DW& d, uint32_t w, const float* ray5, uint32_t cap, uint32_t* count, int32_t* shapes,
+                    float* hit5, uint32_t* status, cudaStream_t s);
 void launch_find_contacts(const DW& d, const Launch& L, cudaStream_t s);
 void launch_synchronize(const DW& d, const Launch& L, cudaStream_t s);
 void launch_init_bodies(const DW& d, const Launch& L, cudaStream_t s);

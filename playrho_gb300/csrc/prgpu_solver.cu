@@ -2008,6 +2008,32 @@ __device__ __forceinline__ void store_impulses(const DW& d, uint32_t t) {
     }
 }
 
+// Solve records for the PostSolveContact replay (Report, AabbTreeWorld.cpp:
+// 196-205, called at :1669-1672): each solved contact's velocity-constraint
+// impulses (GetContactImpulses: the points left after conditioning) and the
+// iteration argument of its island: the position iteration that reached the
+// tolerance, else StepConf::InvalidIteration (255).
+__global__ void k_post_record(DW d) {
+    const DConf& c = *d.conf;
+    const int np = min(c.regPositionIters, kMaxPosIters);
+    const uint32_t step = d.cnt->step_no;
+    GRID_LOOP(t, d.cnt->n_active) {
+        const uint32_t slot = d.t_id[t];
+        if (slot & kJointBit) continue;
+        const float4 e = d.vc0[t].q[3];
+        const uint32_t count = __float_as_uint(d.vc0[t].q[2].w);
+        const float4 i = (count == 2u) ? d.vc1[t].q[3] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint32_t L = d.pc[t].island;
+        uint32_t iter = 255u;
+        for (int k = 0; k < np; ++k) {
+            const size_t at = (size_t)L * kMaxPosIters + k;
+            if (d.isl_sep[at] >= c.regMinSeparation && d.isl_jok[at]) { iter = (uint32_t)k; break; }
+        }
+        d.cs_post[slot] = make_float4(e.x, e.y, i.x, i.y);
+        d.cs_post_tag[slot] = make_uint2(step, count | (iter << 8));
+    }
+}
+
 // IntegratePositions (AabbTreeWorld.cpp:176-188)
 template <class BS>
 __device__ __forceinline__ void integrate_body(const DW& d, const BS& bs, uint32_t b) {
@@ -2364,6 +2390,8 @@ __global__ void k_sleep(DW d) {
 
 __global__ void k_step_reset(DW d) {
     Counters* c = d.cnt;
+    c->step_no += 1u;
+    c->upd_phase = kUpdPre;
     c->st_contacts_added = 0u;
     c->st_contacts_destroyed = 0u;
     c->st_contacts_updated = 0u;
@@ -2494,6 +2522,8 @@ int world_blocks_per_sm(uint32_t stage_bytes) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_world_solve, 256, stage_bytes);
     return a;
 }
+
+void launch_post_record(const DW& d, const Launch& L, cudaStream_t s) { k_post_record<<<L.grid, L.threads, 0, s>>>(d); }
 
 void launch_solve_finish(const DW& d, const Launch& L, cudaStream_t s) {
     k_body_end<<<L.grid, L.threads, 0, s>>>(d);

@@ -833,6 +833,7 @@ void launch_toi_list(const DW& d, const Launch& L, cudaStream_t s) {
 }  // namespace
 
 void launch_toi_begin(const DW& d, const Launch& L, cudaStream_t s) {
+    launch_set_upd_phase(d, kUpdToi, s);
     k_toi_begin<<<L.grid, L.threads, 0, s>>>(d);
     launch_toi_list(d, L, s);
     k_toi_first<<<L.grid, L.threads, 0, s>>>(d);

@@ -39,6 +39,8 @@ struct prgpu_world {
     // pinned copy of the device error word and site, written by every graph-replayed
     // step as it ends (read by prgpu_step_async without waiting)
     uint32_t* h_err = nullptr;
+    float4* post_imp = nullptr;  // solve records (prgpu_set_solve_records), allocated on first use
+    uint2* post_tag = nullptr;
     bool stepped = false;       // a step has run: proxies exist
     cudaEvent_t graph_ev[8] = {};  // recorded by the captured step between its phases
     std::vector<uint32_t> order_nb;  // body counts of the worlds in work-queue order
@@ -530,8 +532,10 @@ int enqueue_step(prgpu_world* w, bool solve, cudaEvent_t* ev = nullptr, bool cap
         launch_solve_sweeps(d, L, s);
         mark(4);
         launch_solve_finish(d, L, s);
+        if (d.cs_post_tag) launch_post_record(d, L, s);
         mark(5);
         // post-solve contact maintenance (AabbTreeWorld.cpp:1532-1557)
+        launch_set_upd_phase(d, kUpdPost, s);
         launch_synchronize(d, L, s);
         launch_update_contacts(d, L, BF_MOVED, s);
         mark(6);
@@ -712,20 +716,6 @@ __global__ void k_gather_contacts(DW d, uint32_t n, uint32_t* proxies2, uint32_t
     }
 }
 
-// TestOverlap(leaf fat AABB, query AABB) (AABB.hpp, as DynamicTree::Query calls it)
-// for every proxy of one world; the overlapping ones are appended to out.
-__global__ void k_query_aabb(DW d, uint32_t first, uint32_t n, float4 q, uint32_t cap, uint32_t* out,
-                             uint32_t* count) {
-    GRID_LOOP(i, n) {
-        const float4 a = d.p_aabb[first + i];
-        const float maxOfMinsX = (a.x < q.x) ? q.x : a.x, minOfMaxsX = (q.z < a.z) ? q.z : a.z;
-        const float maxOfMinsY = (a.y < q.y) ? q.y : a.y, minOfMaxsY = (q.w < a.w) ? q.w : a.w;
-        if (!(minOfMaxsX >= maxOfMinsX) || !(minOfMaxsY >= maxOfMinsY)) continue;
-        const uint32_t k = atomicAdd(count, 1u);
-        if (k < cap) out[k] = i;
-    }
-}
-
 __global__ void k_gather_seq(DW d, uint32_t n, uint64_t* seq) {
     GRID_LOOP(i, n) seq[i] = d.cs_seq[d.c_slot[i]];
 }
@@ -737,6 +727,28 @@ __global__ void k_gather_contact_state(DW d, uint32_t n, uint32_t* slots, float4
         slots[i] = slot;
         const float2 m = d.cs_mat[slot];
         mat4[i] = make_float4(m.x, m.y, d.cs_tspeed[slot], (d.cs_flags[slot] & CF_DISABLED) ? 0.f : 1.f);
+    }
+}
+
+// The live contacts that the last step updated or solved: slot, then the
+// phases that updated it (kUpd* bits), bit 3 if it was solved with its point
+// count at bits 4-7 and the iteration argument at bits 8-15, and the solved
+// impulses.  n_rec counts the records; nothing is written past cap.
+__global__ void k_gather_solve_records(DW d, uint32_t n, uint32_t cap, uint32_t* n_rec, uint32_t* slots,
+                                       uint32_t* info, float4* imp) {
+    const uint32_t step = d.cnt->step_no;
+    GRID_LOOP(i, n) {
+        const uint32_t slot = d.c_slot[i];
+        const uint32_t upd = d.cs_upd[slot];
+        const uint32_t phases = ((upd >> 3) == step) ? (upd & 7u) : 0u;
+        const uint2 tag = d.cs_post_tag ? d.cs_post_tag[slot] : make_uint2(0u, 0u);
+        const bool posted = d.cs_post_tag && tag.x == step;
+        if (!phases && !posted) continue;
+        const uint32_t k = atomicAdd(n_rec, 1u);
+        if (k >= cap) continue;
+        slots[k] = slot;
+        info[k] = phases | (posted ? 8u | ((tag.y & 0xffu) << 4) | (((tag.y >> 8) & 0xffu) << 8) : 0u);
+        imp[k] = posted ? d.cs_post[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
@@ -972,7 +984,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_m2, J); AL(d.j_imp, J);
     AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
     AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C); AL(d.cs_tspeed, C);
-    AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C); AL(d.cs_prio, C);
+    AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C); AL(d.cs_prio, C); AL(d.cs_upd, C);
     ALS(d.cs_toi_ep, C); ALS(d.cs_toi_at, C); ALS(d.t_key, C); ALS(d.t_slot, C);
     AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
     ALS(d.n_key, K); ALS(d.n_key_alt, K); ALS(d.n_val, K); ALS(d.n_val_alt, K);
@@ -1079,6 +1091,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ok &= cudaMemsetAsync(d.b_uat, 0, sizeof(float) * N, w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.b_alpha0, 0, sizeof(float) * N, w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.cnt, 0, sizeof(Counters), w->stream) == cudaSuccess;
+    ok &= cudaMemsetAsync(d.cs_upd, 0, sizeof(uint32_t) * std::max<uint32_t>(C, 1), w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.j_colour, 0xff, sizeof(uint32_t) * std::max<uint32_t>(J, 1), w->stream) == cudaSuccess;
     if (!ok) return bail(fail(w, PRGPU_ECUDA, "upload failed"));
     launch_init_bodies(d, w->L, w->stream);
@@ -1103,6 +1116,8 @@ int prgpu_world_destroy(prgpu_world* w) {
     for (auto g : w->toi_graph)
         if (g) cudaGraphExecDestroy(g);
     for (void* p : w->allocs) cudaFree(p);
+    if (w->post_imp) cudaFree(w->post_imp);
+    if (w->post_tag) cudaFree(w->post_tag);
     if (w->h_cnt) cudaFreeHost(w->h_cnt);
     if (w->h_err) cudaFreeHost(w->h_err);
     if (w->stream) cudaStreamDestroy(w->stream);
@@ -1446,35 +1461,138 @@ int prgpu_download_contacts(prgpu_world* w, uint32_t capacity, uint32_t* n_out, 
     return PRGPU_OK;
 }
 
-int prgpu_query_aabb(prgpu_world* w, uint32_t world, const float* aabb4, uint32_t capacity, uint32_t* n_out,
-                     uint32_t* shapes) {
-    if (!w || !aabb4) return PRGPU_EINVAL;
-    if (world >= w->d.n_worlds) return fail(w, PRGPU_EINVAL, "world %u out of range", world);
+int prgpu_query_aabbs(prgpu_world* w, uint32_t n, const uint32_t* worlds, const float* aabb4, uint32_t capacity,
+                      uint32_t* counts, uint32_t* shapes) {
+    if (!w || (n && (!worlds || !aabb4 || !counts))) return PRGPU_EINVAL;
+    for (uint32_t k = 0; k < n; ++k)
+        if (worlds[k] >= w->d.n_worlds) return fail(w, PRGPU_EINVAL, "world %u out of range", worlds[k]);
     CU(cudaSetDevice(w->device));
-    uint32_t off[2] = {0u, 0u};
-    CU(cudaMemcpyAsync(off, w->d.w_shape_off + world, sizeof(off), cudaMemcpyDeviceToHost, w->stream));
-    CU(cudaStreamSynchronize(w->stream));
-    const uint32_t n = off[1] - off[0];
-    if (n_out) *n_out = 0;
     // The first step creates the proxies; before it the tree is empty (no overlaps).
-    if (n == 0 || !w->stepped) return PRGPU_OK;
+    if (n == 0 || !w->stepped) {
+        for (uint32_t k = 0; k < n; ++k) counts[k] = 0;
+        return PRGPU_OK;
+    }
+    const size_t cap = shapes ? capacity : 0;
     AsyncScratch scratch{nullptr, w->stream};
-    CU(cudaMallocAsync(&scratch.p, 4 * ((size_t)n + 1), w->stream));
-    uint32_t* g = static_cast<uint32_t*>(scratch.p);
-    CU(cudaMemsetAsync(g, 0, 4, w->stream));
-    const float4 q = make_float4(aabb4[0], aabb4[1], aabb4[2], aabb4[3]);
-    k_query_aabb<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, off[0], n, q, n, g + 1, g);
+    CU(cudaMallocAsync(&scratch.p, 16 * (size_t)n + 4 * (size_t)n * (2 + cap) + 16, w->stream));
+    float4* g_box = static_cast<float4*>(scratch.p);
+    uint32_t* g_world = reinterpret_cast<uint32_t*>(g_box + n);
+    uint32_t* g_count = g_world + n;
+    uint32_t* g_status = g_count + n;
+    uint32_t* g_out = g_status + 1;
+    CU(cudaMemcpyAsync(g_box, aabb4, 16 * (size_t)n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(g_world, worlds, 4 * (size_t)n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemsetAsync(g_status, 0, 4, w->stream));
+    launch_query_boxes(w->d, w->L, n, g_world, g_box, (uint32_t)cap, g_count, g_out, g_status, w->stream);
     CU(cudaGetLastError());
-    uint32_t found = 0;
-    CU(cudaMemcpyAsync(&found, g, 4, cudaMemcpyDeviceToHost, w->stream));
-    CU(cudaStreamSynchronize(w->stream));
-    if (n_out) *n_out = found;
-    if (found > capacity) return fail(w, PRGPU_ECAPACITY, "%u overlaps exceed capacity %u", found, capacity);
-    if (found && shapes) CU(cudaMemcpyAsync(shapes, g + 1, 4 * (size_t)found, cudaMemcpyDeviceToHost, w->stream));
+    uint32_t status = 0;
+    CU(cudaMemcpyAsync(counts, g_count, 4 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaMemcpyAsync(&status, g_status, 4, cudaMemcpyDeviceToHost, w->stream));
+    if (cap) CU(cudaMemcpyAsync(shapes, g_out, 4 * (size_t)n * cap, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaFreeAsync(scratch.p, w->stream));
     scratch.p = nullptr;
     CU(cudaStreamSynchronize(w->stream));
-    if (shapes) std::sort(shapes, shapes + found);
+    if (status) return fail(w, PRGPU_ESTATE, "tree walk deeper than its stack");
+    bool over = false;
+    for (uint32_t k = 0; k < n; ++k) {
+        if (counts[k] > cap) { over = over || shapes != nullptr; continue; }
+        if (cap) std::sort(shapes + (size_t)k * cap, shapes + (size_t)k * cap + counts[k]);
+    }
+    if (over) return fail(w, PRGPU_ECAPACITY, "overlaps exceed capacity %u", capacity);
+    return PRGPU_OK;
+}
+
+int prgpu_query_aabb(prgpu_world* w, uint32_t world, const float* aabb4, uint32_t capacity, uint32_t* n_out,
+                     uint32_t* shapes) {
+    if (!w || !aabb4) return PRGPU_EINVAL;
+    uint32_t count = 0;
+    const int rc = prgpu_query_aabbs(w, 1, &world, aabb4, capacity, &count, shapes);
+    if (n_out) *n_out = count;
+    return rc;
+}
+
+int prgpu_raycast(prgpu_world* w, uint32_t n, const uint32_t* worlds, const float* rays5, int32_t* shapes,
+                  float* hits5) {
+    if (!w || (n && (!worlds || !rays5 || !shapes || !hits5))) return PRGPU_EINVAL;
+    for (uint32_t k = 0; k < n; ++k)
+        if (worlds[k] >= w->d.n_worlds) return fail(w, PRGPU_EINVAL, "world %u out of range", worlds[k]);
+    CU(cudaSetDevice(w->device));
+    if (n == 0) return PRGPU_OK;
+    if (!w->stepped) {
+        for (uint32_t k = 0; k < n; ++k) {
+            shapes[k] = -1;
+            for (int q = 0; q < 5; ++q) hits5[5 * (size_t)k + q] = 0.f;
+        }
+        return PRGPU_OK;
+    }
+    AsyncScratch scratch{nullptr, w->stream};
+    CU(cudaMallocAsync(&scratch.p, 48 * (size_t)n + 16, w->stream));
+    float* g_ray = static_cast<float*>(scratch.p);
+    float* g_hit = g_ray + 5 * (size_t)n;
+    uint32_t* g_world = reinterpret_cast<uint32_t*>(g_hit + 5 * (size_t)n);
+    int32_t* g_shape = reinterpret_cast<int32_t*>(g_world + n);
+    uint32_t* g_status = reinterpret_cast<uint32_t*>(g_shape + n);
+    CU(cudaMemcpyAsync(g_ray, rays5, 20 * (size_t)n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(g_world, worlds, 4 * (size_t)n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemsetAsync(g_status, 0, 4, w->stream));
+    launch_ray_nearest(w->d, w->L, n, g_world, g_ray, g_shape, g_hit, g_status, w->stream);
+    CU(cudaGetLastError());
+    uint32_t status = 0;
+    CU(cudaMemcpyAsync(shapes, g_shape, 4 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaMemcpyAsync(hits5, g_hit, 20 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaMemcpyAsync(&status, g_status, 4, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaFreeAsync(scratch.p, w->stream));
+    scratch.p = nullptr;
+    CU(cudaStreamSynchronize(w->stream));
+    if (status) return fail(w, PRGPU_ESTATE, "tree walk deeper than its stack");
+    return PRGPU_OK;
+}
+
+int prgpu_raycast_all(prgpu_world* w, uint32_t world, const float* ray5, uint32_t capacity, uint32_t* n_out,
+                      int32_t* shapes, float* hits5) {
+    if (!w || !ray5 || !n_out) return PRGPU_EINVAL;
+    if (world >= w->d.n_worlds) return fail(w, PRGPU_EINVAL, "world %u out of range", world);
+    CU(cudaSetDevice(w->device));
+    *n_out = 0;
+    if (!w->stepped) return PRGPU_OK;
+    const size_t cap = (shapes && hits5) ? capacity : 0;
+    AsyncScratch scratch{nullptr, w->stream};
+    CU(cudaMallocAsync(&scratch.p, 24 * cap + 16, w->stream));
+    float* g_hit = static_cast<float*>(scratch.p);
+    int32_t* g_shape = reinterpret_cast<int32_t*>(g_hit + 5 * cap);
+    uint32_t* g_count = reinterpret_cast<uint32_t*>(g_shape + cap);
+    uint32_t* g_status = g_count + 1;
+    CU(cudaMemsetAsync(g_status, 0, 4, w->stream));
+    launch_ray_all(w->d, world, ray5, (uint32_t)cap, g_count, g_shape, g_hit, g_status, w->stream);
+    CU(cudaGetLastError());
+    uint32_t cs[2] = {0u, 0u};
+    CU(cudaMemcpyAsync(cs, g_count, 8, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    const uint32_t found = cs[0];
+    *n_out = found;
+    if (cs[1]) {
+        CU(cudaFreeAsync(scratch.p, w->stream));
+        scratch.p = nullptr;
+        return fail(w, PRGPU_ESTATE, "tree walk deeper than its stack");
+    }
+    const size_t m = std::min<size_t>(found, cap);
+    if (m) {
+        CU(cudaMemcpyAsync(shapes, g_shape, 4 * m, cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaMemcpyAsync(hits5, g_hit, 20 * m, cudaMemcpyDeviceToHost, w->stream));
+    }
+    CU(cudaFreeAsync(scratch.p, w->stream));
+    scratch.p = nullptr;
+    CU(cudaStreamSynchronize(w->stream));
+    if (found > cap && cap) return fail(w, PRGPU_ECAPACITY, "%u hits exceed capacity %u", found, capacity);
+    // in shape order (the reference reports them in tree order)
+    std::vector<std::pair<int32_t, uint32_t>> order(m);
+    for (size_t k = 0; k < m; ++k) order[k] = {shapes[k], (uint32_t)k};
+    std::sort(order.begin(), order.end());
+    std::vector<float> h(hits5, hits5 + 5 * m);
+    for (size_t k = 0; k < m; ++k) {
+        shapes[k] = order[k].first;
+        for (int q = 0; q < 5; ++q) hits5[5 * k + q] = h[5 * (size_t)order[k].second + q];
+    }
     return PRGPU_OK;
 }
 
@@ -1495,6 +1613,62 @@ int prgpu_download_contact_state(prgpu_world* w, uint32_t capacity, uint32_t* n_
     CU(cudaGetLastError());
     if (slots) CU(cudaMemcpyAsync(slots, g_slot, 4 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     if (mat4) CU(cudaMemcpyAsync(mat4, g_mat, 16 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaFreeAsync(scratch.p, w->stream));
+    scratch.p = nullptr;
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_set_solve_records(prgpu_world* w, int enabled) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    const bool on = enabled != 0;
+    if (on == (w->d.cs_post_tag != nullptr)) return PRGPU_OK;
+    int rc = drop_graph(w);
+    if (rc) return rc;
+    if (on) {
+        const size_t C = std::max<uint32_t>(w->d.contact_cap, 1);
+        if (!w->post_imp) {
+            CU(cudaMalloc(&w->post_imp, sizeof(float4) * C));
+            CU(cudaMalloc(&w->post_tag, sizeof(uint2) * C));
+            CU(cudaMemsetAsync(w->post_tag, 0, sizeof(uint2) * C, w->stream));
+        }
+        w->d.cs_post = w->post_imp;
+        w->d.cs_post_tag = w->post_tag;
+    } else {
+        w->d.cs_post = nullptr;
+        w->d.cs_post_tag = nullptr;
+    }
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_download_solve_records(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* slots, uint32_t* info,
+                                 float* imp4) {
+    if (!w || !n_out) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    CU(cudaMemcpyAsync(w->h_cnt, w->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    const uint32_t n = w->h_cnt->n_live;
+    *n_out = 0;
+    if (n == 0) return PRGPU_OK;
+    AsyncScratch scratch{nullptr, w->stream};
+    CU(cudaMallocAsync(&scratch.p, 28 * (size_t)n + 16, w->stream));
+    float4* g_imp = static_cast<float4*>(scratch.p);
+    uint32_t* g_slot = reinterpret_cast<uint32_t*>(g_imp + n);
+    uint32_t* g_info = g_slot + n;
+    uint32_t* g_n = g_info + n;
+    CU(cudaMemsetAsync(g_n, 0, 4, w->stream));
+    k_gather_solve_records<<<w->L.grid, w->L.threads, 0, w->stream>>>(w->d, n, n, g_n, g_slot, g_info, g_imp);
+    CU(cudaGetLastError());
+    uint32_t m = 0;
+    CU(cudaMemcpyAsync(&m, g_n, 4, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    *n_out = m;
+    if (m > capacity && (slots || info || imp4)) return fail(w, PRGPU_ECAPACITY, "%u records exceed capacity %u", m, capacity);
+    if (slots) CU(cudaMemcpyAsync(slots, g_slot, 4 * (size_t)m, cudaMemcpyDeviceToHost, w->stream));
+    if (info) CU(cudaMemcpyAsync(info, g_info, 4 * (size_t)m, cudaMemcpyDeviceToHost, w->stream));
+    if (imp4) CU(cudaMemcpyAsync(imp4, g_imp, 16 * (size_t)m, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaFreeAsync(scratch.p, w->stream));
     scratch.p = nullptr;
     CU(cudaStreamSynchronize(w->stream));

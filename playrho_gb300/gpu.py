@@ -134,6 +134,12 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_get_body_steps.argtypes = [P, P]
     lib.prgpu_download_sweep_order.argtypes = [P, U, P, P]
     lib.prgpu_download_contacts_noalloc.argtypes = [P, U, P, P, P, P, P, P, P, P]
+    lib.prgpu_download_contact_state.argtypes = [P, U, P, P, P]
+    lib.prgpu_set_solve_records.argtypes = [P, I]
+    lib.prgpu_query_aabbs.argtypes = [P, U, P, P, U, P, P]
+    lib.prgpu_raycast.argtypes = [P, U, P, P, P, P]
+    lib.prgpu_raycast_all.argtypes = [P, U, P, U, P, P, P]
+    lib.prgpu_download_solve_records.argtypes = [P, U, P, P, P, P]
     _LIB = lib
     return lib
 
@@ -151,7 +157,9 @@ def exported_symbols() -> List[str]:
         "prgpu_adjoint_backward", "prgpu_adjoint_tangent", "prgpu_adjoint_info", "prgpu_adjoint_end",
         "prgpu_adjoint_profile", "prgpu_adjoint_trim", "prgpu_time_of_impact", "prgpu_get_body_steps",
         "prgpu_download_sweep_order", "prgpu_download_contacts_noalloc", "prgpu_download_contact_seq",
-        "prgpu_query_aabb", "prgpu_download_contact_state", "prgpu_set_contact", "prgpu_set_manifold"]
+        "prgpu_query_aabb", "prgpu_download_contact_state", "prgpu_set_contact", "prgpu_set_manifold",
+        "prgpu_set_solve_records", "prgpu_download_solve_records", "prgpu_query_aabbs", "prgpu_raycast",
+        "prgpu_raycast_all"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -516,6 +524,41 @@ class GpuBatch:
         self._check(self.lib.prgpu_query_aabb(self.h, world, _ptr(q), cap, ctypes.byref(nout), _ptr(out)), "query")
         return out[:nout.value].astype(np.int64)
 
+    def query_aabbs(self, worlds, boxes, capacity: int = 64):
+        """Many AABB queries at once (prgpu_query_aabbs): per query its overlap count
+        and its world-local shape IDs (ascending)."""
+        w = np.ascontiguousarray(worlds, dtype=np.uint32)
+        q = np.ascontiguousarray(boxes, dtype=np.float32).reshape(-1, 4)
+        n = w.size
+        counts = np.zeros(max(n, 1), np.uint32)
+        out = np.zeros(max(n * capacity, 1), np.uint32)
+        self._check(self.lib.prgpu_query_aabbs(self.h, n, _ptr(w), _ptr(q), capacity, _ptr(counts), _ptr(out)),
+                    "prgpu_query_aabbs")
+        return counts[:n].astype(np.int64), [out[k * capacity:k * capacity + int(counts[k])].astype(np.int64)
+                                             for k in range(n)]
+
+    def raycast(self, worlds, rays):
+        """Nearest hit of each ray (prgpu_raycast): rays [n, 5] = x1 y1 x2 y2 maxFraction;
+        returns shape IDs (-1: none) and hits [n, 5] = fraction, point xy, normal xy."""
+        w = np.ascontiguousarray(worlds, dtype=np.uint32)
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 5)
+        n = w.size
+        shapes = np.zeros(max(n, 1), np.int32)
+        hits = np.zeros((max(n, 1), 5), np.float32)
+        self._check(self.lib.prgpu_raycast(self.h, n, _ptr(w), _ptr(r), _ptr(shapes), _ptr(hits)), "prgpu_raycast")
+        return shapes[:n].astype(np.int64), hits[:n]
+
+    def raycast_all(self, world: int, ray, capacity: int = 256) -> list:
+        """Every shape one ray hits (prgpu_raycast_all), ascending by shape, as
+        (shape, fraction, point x, point y, normal x, normal y)."""
+        r = np.ascontiguousarray(ray, dtype=np.float32).reshape(5)
+        shapes = np.zeros(capacity, np.int32)
+        hits = np.zeros((capacity, 5), np.float32)
+        n = ctypes.c_uint32()
+        self._check(self.lib.prgpu_raycast_all(self.h, int(world), _ptr(r), capacity, ctypes.byref(n), _ptr(shapes),
+                                               _ptr(hits)), "prgpu_raycast_all")
+        return [(int(shapes[k]),) + tuple(hits[k]) for k in range(n.value)]
+
     def contact_seq(self) -> np.ndarray:
         """Creation sequence numbers of the live contacts, in the order of contacts()."""
         n = self.contact_count()
@@ -529,6 +572,37 @@ class GpuBatch:
         n = ctypes.c_uint64()
         self._check(self.lib.prgpu_get_body_steps(self.h, ctypes.byref(n)), "prgpu_get_body_steps")
         return int(n.value)
+
+    def contact_slots(self) -> np.ndarray:
+        """Slot (ContactID) of every live contact, in the order of contacts()."""
+        n = self.contact_count()
+        out = np.zeros(max(n, 1), np.uint32)
+        nout = ctypes.c_uint32()
+        self._check(self.lib.prgpu_download_contact_state(self.h, out.size, ctypes.byref(nout), _ptr(out), None),
+                    "contact state")
+        return out[:nout.value].astype(np.int64)
+
+    def set_solve_records(self, enabled: bool = True):
+        """Keep each solved contact's impulses and iteration argument (postSolve)."""
+        self._check(self.lib.prgpu_set_solve_records(self.h, int(bool(enabled))), "prgpu_set_solve_records")
+
+    def solve_records(self) -> dict:
+        """The live contacts the last step updated or solved: slot, phases (bits:
+        1 pre-phase, 2 post-solve pass, 4 time-of-impact phase), solved (bool),
+        point count, iteration argument, impulses (ni0 ti0 ni1 ti1)."""
+        n = ctypes.c_uint32()
+        self._check(self.lib.prgpu_download_solve_records(self.h, 0, ctypes.byref(n), None, None, None), "records")
+        cap = max(n.value, 1)
+        sl = np.zeros(cap, np.uint32)
+        info = np.zeros(cap, np.uint32)
+        imp = np.zeros((cap, 4), np.float32)
+        self._check(self.lib.prgpu_download_solve_records(self.h, cap, ctypes.byref(n), _ptr(sl), _ptr(info), _ptr(imp)),
+                    "records")
+        m = n.value
+        info = info[:m]
+        return {"slot": sl[:m].astype(np.int64), "phases": (info & 7).astype(np.int32),
+                "solved": (info & 8) != 0, "count": ((info >> 4) & 15).astype(np.int32),
+                "iter": ((info >> 8) & 255).astype(np.int32), "imp": imp[:m]}
 
     def sweep_order(self) -> np.ndarray:
         """The last step's constraint sweep order: rows (0, shape A, shape B) for

@@ -385,34 +385,107 @@ std::vector<std::pair<uint32_t, GpuWorld::Snapshot>> TakeSnapshot(const GpuWorld
     return out;
 }
 
-// BeginContact / EndContact calls of the step just run, from the contacts before
-// and after it, in the reference's order: EndContact for each touching contact
-// the step destroyed (DestroyContacts -> InternalDestroy, AabbTreeWorld.cpp:
-// 2245-2253, 2290-2331), then BeginContact / EndContact for each contact whose
-// touching state changed or that was created touching (Update, :2703-2714);
-// both passes in contact-list (creation) order.
+// The contact listener calls of the step just run, in the reference's order
+// (Step, AabbTreeWorld.cpp:2144-2219), from the contacts before and after it and
+// the GPU's records of which phase updated or solved each contact:
+//  1. EndContact for each touching contact the step destroyed (DestroyContacts ->
+//     InternalDestroy, :2245-2253, :2290-2331);
+//  2. the pre-phase's UpdateContacts and AddContacts (:2186-2198), then
+//  3. PostSolveContact for each contact the regular phase solved (:1669-1672),
+//  4. the post-solve UpdateContacts and AddContacts (:1549-1557), and
+//  5. the time-of-impact phase's updates (:1879, :2098):
+//     for each contact updated in a phase, in contact-list (creation) order, its
+//     BeginContact / EndContact if its touching state changed (attributed to the
+//     last phase that updated it), then PreSolveContact with the manifold before
+//     that update if it touches and is not a sensor (Update, :2703-2720).
+// The manifold before the post-solve update carries the solved impulses
+// (AssignImpulses, :196-220); before a time-of-impact update, the manifold
+// after the step is passed.
 void CallContactListeners(GpuWorld& w, std::vector<std::pair<uint32_t, GpuWorld::Snapshot>>& before) {
     auto after = TakeSnapshot(w);
-    std::vector<std::pair<bool, ContactID>> calls;  // (begin?, id)
+    std::vector<prgpu::HostSolveRecord> recs;
+    if (w.preSolveContactListener || w.postSolveContactListener || w.beginContactListener || w.endContactListener)
+        recs = Guard([&] { return w.host.SolveRecords(); });
+    std::vector<const prgpu::HostSolveRecord*> by_slot;
+    for (const auto& r : recs) {
+        if (r.slot >= by_slot.size()) by_slot.resize(r.slot + 1, nullptr);
+        by_slot[r.slot] = &r;
+    }
+    auto record = [&](uint32_t slot) -> const prgpu::HostSolveRecord* {
+        return slot < by_slot.size() ? by_slot[slot] : nullptr;
+    };
+    // before-step state of each contact in `after` (nullptr: created by this step)
+    std::vector<const GpuWorld::Snapshot*> prior(after.size(), nullptr);
+    {
+        size_t i = 0;
+        for (size_t k = 0; k < after.size(); ++k) {
+            while (i < before.size() && before[i].second.seq < after[k].second.seq) ++i;
+            if (i < before.size() && before[i].second.seq == after[k].second.seq) prior[k] = &before[i].second;
+        }
+    }
+    struct Call {
+        int kind;  // 1 begin, 2 end, 3 pre-solve, 4 post-solve
+        ContactID id;
+        Manifold manifold;
+        ContactImpulsesList impulses;
+        unsigned iter;
+    };
+    std::vector<Call> calls;
     size_t j = 0;
     for (const auto& e : before) {  // destroyed: in `before`, not in `after`
         while (j < after.size() && after[j].second.seq < e.second.seq) ++j;
         const bool alive = j < after.size() && after[j].second.seq == e.second.seq;
-        if (!alive && e.second.touching) calls.emplace_back(false, ContactID(e.first));
+        if (!alive && e.second.touching) calls.push_back(Call{2, ContactID(e.first), {}, {}, 0u});
     }
-    size_t i = 0;
+    auto last_phase = [](uint32_t phases) { return phases & 4u ? 4u : phases & 2u ? 2u : phases & 1u ? 1u : 0u; };
+    auto phase_pass = [&](uint32_t phase) {
+        for (size_t k = 0; k < after.size(); ++k) {
+            const auto& e = after[k];
+            const auto* r = record(e.first);
+            const uint32_t phases = r ? r->phases : 0u;
+            const bool was = prior[k] && prior[k]->touching;
+            const bool changed = e.second.touching != was;
+            // a change without a record (none is expected) is reported with the post-solve pass
+            const bool here = (phases & phase) != 0u;
+            if (changed && (last_phase(phases) == phase || (phases == 0u && phase == 2u)))
+                calls.push_back(Call{e.second.touching ? 1 : 2, ContactID(e.first), {}, {}, 0u});
+            if (!here || !e.second.touching || IsSensor(e.second.contact)) continue;
+            Manifold old;
+            if (phase == 4u) {
+                old = e.second.manifold;
+            } else if (prior[k]) {
+                old = prior[k]->manifold;
+                if (phase == 2u && r && r->solved) {
+                    const auto n = std::min<std::size_t>(old.GetPointCount(), static_cast<std::size_t>(r->count));
+                    for (std::size_t q = 0; q < n; ++q)
+                        old.SetImpulses(q, Real(r->normal_impulse[q]) * NewtonSecond,
+                                        Real(r->tangent_impulse[q]) * NewtonSecond);
+                }
+            }
+            calls.push_back(Call{3, ContactID(e.first), old, {}, 0u});
+        }
+    };
+    phase_pass(1u);
     for (const auto& e : after) {
-        while (i < before.size() && before[i].second.seq < e.second.seq) ++i;
-        const bool existed = i < before.size() && before[i].second.seq == e.second.seq;
-        const bool was = existed && before[i].second.touching;
-        if (e.second.touching != was) calls.emplace_back(e.second.touching, ContactID(e.first));
+        const auto* r = record(e.first);
+        if (!r || !r->solved) continue;
+        ContactImpulsesList imp;
+        for (int q = 0; q < r->count && q < 2; ++q)
+            imp.AddEntry(Real(r->normal_impulse[q]) * NewtonSecond, Real(r->tangent_impulse[q]) * NewtonSecond);
+        calls.push_back(Call{4, ContactID(e.first), {}, imp, r->iter});
     }
+    phase_pass(2u);
+    phase_pass(4u);
     w.replaying = &before;
     w.locked = true;
     try {
         for (const auto& c : calls) {
-            if (c.first) { if (w.beginContactListener) w.beginContactListener(c.second); }
-            else if (w.endContactListener) w.endContactListener(c.second);
+            switch (c.kind) {
+            case 1: if (w.beginContactListener) w.beginContactListener(c.id); break;
+            case 2: if (w.endContactListener) w.endContactListener(c.id); break;
+            case 3: if (w.preSolveContactListener) w.preSolveContactListener(c.id, c.manifold); break;
+            default: if (w.postSolveContactListener) w.postSolveContactListener(c.id, c.impulses, c.iter); break;
+            }
         }
     } catch (...) {
         w.locked = false;
@@ -430,7 +503,10 @@ StepStats Step(GpuWorld& w, const StepConf& conf) {
     CheckUnlocked(w);
     StepStats stats;
     const auto sc = ToAbi(conf);
-    const bool listen = static_cast<bool>(w.beginContactListener) || static_cast<bool>(w.endContactListener);
+    const bool listen = static_cast<bool>(w.beginContactListener) || static_cast<bool>(w.endContactListener) ||
+                        static_cast<bool>(w.preSolveContactListener) || static_cast<bool>(w.postSolveContactListener);
+    w.host.SetSolveRecords(static_cast<bool>(w.postSolveContactListener) ||
+                           static_cast<bool>(w.preSolveContactListener));
     // the contacts before the step (kept from the last step while listeners are set)
     if (listen && !w.listening) {
         w.previous = w.host.HasGpuBatch() ? TakeSnapshot(w) : decltype(w.previous){};

@@ -22,11 +22,15 @@
 //    reused after it is destroyed, as the reference's pools reuse them;
 //    SetContact (enabled, friction, restitution, tangent speed) and SetManifold
 //    take effect from the next step;
-//  * the BeginContact / EndContact listeners are called from Step after the GPU
-//    step, in the order the reference calls them (EndContact of the touching
-//    contacts the step destroyed, then the contacts whose touching state
-//    changed, each in contact-list order); while they run the world is locked.
-//    The pre-solve and post-solve listeners are stored but not called;
+//  * the contact listeners are called from Step after the GPU step, phase by
+//    phase in the order the reference calls them (EndContact of the touching
+//    contacts the step destroyed; BeginContact / EndContact / PreSolveContact of
+//    the contacts the pre-phase updated; PostSolveContact of the solved
+//    contacts; then those of the post-solve and time-of-impact updates), each
+//    phase in contact-list order; while they run the world is locked.  Within
+//    the post-solve calls the order is contact-list order, not island order;
+//    the time-of-impact phase's own PostSolveContact calls are not made, and
+//    its PreSolveContact calls pass the manifold after the step;
 //  * changing anything but a body's position or velocity between steps
 //    (creating or destroying entities, attaching shapes, changing a body's type,
 //    flags or mass) rebuilds the GPU batch: contacts are found again on the next

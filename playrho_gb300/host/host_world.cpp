@@ -284,6 +284,7 @@ void HostWorld::Build() {
     }
     Check(prgpu_world_create(&d, device_, &gpu_), "prgpu_world_create");
     rebuild_ = false;
+    if (solve_records_) Check(prgpu_set_solve_records(gpu_, 1), "prgpu_set_solve_records");
     state_dirty_.assign(bodies_.size(), false);
     lc_.assign(2 * (size_t)N, 0.f);
     std::vector<float> m(4 * (size_t)N), p(3 * (size_t)N);
@@ -384,6 +385,39 @@ const std::vector<HostContact>& HostWorld::Contacts() {
     }
     contacts_valid_ = true;
     return contacts_;
+}
+
+void HostWorld::SetSolveRecords(bool enabled) {
+    if (enabled == solve_records_) return;
+    solve_records_ = enabled;
+    if (gpu_) Check(prgpu_set_solve_records(gpu_, enabled ? 1 : 0), "prgpu_set_solve_records");
+}
+
+std::vector<HostSolveRecord> HostWorld::SolveRecords() {
+    std::vector<HostSolveRecord> out;
+    if (!gpu_) return out;
+    uint32_t n = 0;
+    Check(prgpu_download_solve_records(gpu_, 0, &n, nullptr, nullptr, nullptr), "prgpu_download_solve_records");
+    if (n == 0) return out;
+    std::vector<uint32_t> slots(n), info(n);
+    std::vector<float> imp(4 * (size_t)n);
+    uint32_t m = 0;
+    Check(prgpu_download_solve_records(gpu_, n, &m, slots.data(), info.data(), imp.data()),
+          "prgpu_download_solve_records");
+    out.resize(m);
+    for (uint32_t k = 0; k < m; ++k) {
+        HostSolveRecord& r = out[k];
+        r.slot = slots[k];
+        r.phases = info[k] & 7u;
+        r.solved = (info[k] & 8u) != 0u;
+        r.count = (int32_t)((info[k] >> 4) & 15u);
+        r.iter = (info[k] >> 8) & 255u;
+        for (int j = 0; j < 2; ++j) {
+            r.normal_impulse[j] = imp[4 * k + 2 * j];
+            r.tangent_impulse[j] = imp[4 * k + 2 * j + 1];
+        }
+    }
+    return out;
 }
 
 void HostWorld::SetContact(uint32_t slot, bool enabled, float friction, float restitution, float tangent_speed) {

@@ -81,6 +81,19 @@ struct HostContact {
     bool enabled = true;
 };
 
+// What the last step did to one live contact (prgpu_download_solve_records):
+// the phases that updated it (1 pre-phase, 2 post-solve pass, 4 time-of-impact
+// phase) and, if the regular phase solved it, its velocity constraint's impulses
+// and its island's iteration argument.
+struct HostSolveRecord {
+    uint32_t slot = 0;
+    uint32_t phases = 0;
+    bool solved = false;
+    int32_t count = 0;     // velocity-constraint points
+    uint32_t iter = 255;   // StepConf::InvalidIteration unless the island reached tolerance
+    float normal_impulse[2] = {0.f, 0.f}, tangent_impulse[2] = {0.f, 0.f};
+};
+
 // Errors carry the C ABI's status code; the drop-in maps them onto the
 // reference's exception types.
 struct Error : std::runtime_error {
@@ -124,6 +137,10 @@ public:
     // SetContact / SetManifold on a live contact's slot (prgpu_set_contact, prgpu_set_manifold).
     void SetContact(uint32_t slot, bool enabled, float friction, float restitution, float tangent_speed);
     void SetManifold(uint32_t slot, int32_t type, int32_t count, const float head4[4], const float pts8[8]);
+    // Keep solve records from the next step on (prgpu_set_solve_records), across rebuilds.
+    void SetSolveRecords(bool enabled);
+    // The live contacts the last step updated or solved.
+    std::vector<HostSolveRecord> SolveRecords();
     // Fat AABB (minx miny maxx maxy) and (body, shape) of every proxy, by leaf ID order.
     void Proxies(std::vector<float>& aabb4, std::vector<uint32_t>& body_shape2);
     void Clear();
@@ -154,6 +171,7 @@ private:
     std::vector<bool> state_dirty_;           // body ID -> position/velocity set since the last step
     bool contacts_valid_ = false;
     std::vector<HostContact> contacts_;
+    bool solve_records_ = false;
 };
 
 }  // namespace prgpu

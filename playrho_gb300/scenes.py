@@ -136,6 +136,28 @@ class SceneBuilder:
         self.j_type: List[int] = []
         self.j_extra: List[tuple] = []
 
+    @classmethod
+    def from_scene(cls, sc: "Scene") -> "SceneBuilder":
+        """A builder holding ``sc``'s bodies, shapes and joints (same IDs), to add to."""
+        sb = cls()
+        for b in range(sc.n_bodies):
+            sb.body(int(sc.body_type[b]), *(float(v) for v in sc.body_pos[b]), v=tuple(float(v) for v in sc.body_vel[b]),
+                    acc=tuple(float(v) for v in sc.body_acc[b]), damp=tuple(float(v) for v in sc.body_damp[b]),
+                    flags=int(sc.body_flags[b]))
+        for k in range(sc.n_shapes):
+            o, n = int(sc.shape_voff[k]), int(sc.shape_nv[k])
+            sb._shape(int(sc.shape_body[k]), int(sc.shape_kind[k]), [tuple(v) for v in sc.verts[o:o + n]],
+                      float(sc.shape_radius[k]), float(sc.shape_density[k]), float(sc.shape_friction[k]),
+                      float(sc.shape_restitution[k]), tuple(int(v) for v in sc.shape_filter[k]))
+        for j in range(sc.n_joints):
+            sb.j_bodies.append(tuple(int(v) for v in sc.joint_bodies[j]))
+            sb.j_anchor.append(tuple(float(v) for v in sc.joint_anchors[j]))
+            sb.j_params.append(tuple(float(v) for v in sc.joint_params[j]))
+            sb.j_flags.append(tuple(int(v) for v in sc.joint_flags[j]))
+            sb.j_type.append(int(sc.joint_type[j]))
+            sb.j_extra.append(tuple(float(v) for v in sc.joint_extra[j]))
+        return sb
+
     def body(self, btype, x, y, angle=0.0, v=(0.0, 0.0, 0.0), acc=(0.0, 0.0, 0.0),
              damp=(0.0, 0.0), flags=BF_DEFAULT) -> int:
         self.b_type.append(int(btype))
@@ -645,6 +667,26 @@ def joint_zoo(rng, per_kind: int = 4, kinds=None, n_disks: int = 12, gravity: bo
         d = sb.body(DYNAMIC, float(rng.uniform(-width / 2, width / 2)), float(rng.uniform(10.0, 16.0)), acc=acc)
         sb.disk(d, float(rng.uniform(0.2, 0.5)), density=1.0, friction=0.3)
     return sb.build()
+
+
+def sensor_scene(rng, n_bodies: int = 120) -> Scene:
+    """A pile falling through sensors: static sensor zones (boxes and disks) across
+    the fall, and every fifth falling body a sensor itself.  Sensors make no
+    manifolds and no impulses; their touching state comes from TestOverlap
+    (Distance.cpp:205-216), which is what Begin/EndContact report for them."""
+    sc = pile(n_bodies, rng)
+    sb = SceneBuilder.from_scene(sc)
+    w = max(10.0, math.sqrt(n_bodies) * 2.0)
+    for k in range(6):
+        z = sb.body(STATIC, -w + (k + 0.5) * (2.0 * w / 6.0), 8.0 + 6.0 * (k % 3))
+        if k % 2:
+            sb.disk(z, 1.5, filt=(1, 0xFFFF, 0, 1))
+        else:
+            sb.box(z, 2.0, 0.6, filt=(1, 0xFFFF, 0, 1))
+    out = sb.build()
+    falling = np.flatnonzero(out.body_type[out.shape_body] == DYNAMIC)
+    out.shape_filter[falling[::5], 3] = 1
+    return out
 
 
 def gear_scene(rng, pairs: int = 3, n_disks: int = 10, gravity: bool = True) -> Scene:

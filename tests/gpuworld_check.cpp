@@ -92,8 +92,9 @@ void CheckJoints() {
 // shape, higher shape), the box-ground contact's ID followed through the run,
 // and SetContact on it: a tangent speed of 2 m/s with friction 0.8 from step 20
 // (a conveyor belt), disabled from step 45 (the box sinks through the ground).
-// Prints "<tag> event ...", "<tag> id ..." and "<tag> pos ..." lines.
-void Conveyor(playrho::d2::World& world, const char* tag) {
+// Prints "<tag> event ...", "<tag> call ...", "<tag> pre ...", "<tag> post ...",
+// "<tag> id ..." and "<tag> pos ..." lines; StepConf::doToi as given.
+void Conveyor(playrho::d2::World& world, const char* tag, bool doToi) {
     using namespace playrho;
     using namespace playrho::d2;
     const auto ground = CreateShape(world, PolygonShapeConf{}.SetAsBox(20_m, 1_m));
@@ -109,10 +110,42 @@ void Conveyor(playrho::d2::World& world, const char* tag) {
         const auto& c = GetContact(world, id);
         const auto a = to_underlying(GetShapeA(c)), b = to_underlying(GetShapeB(c));
         std::printf("%s event %d %s %u %u\n", tag, step, kind, unsigned(a < b ? a : b), unsigned(a < b ? b : a));
+        std::printf("%s call %d %s %u %u\n", tag, step, kind, unsigned(a < b ? a : b), unsigned(a < b ? b : a));
     };
     SetBeginContactListener(world, [event](ContactID id) { event("begin", id); });
     SetEndContactListener(world, [event](ContactID id) { event("end", id); });
+    // PreSolveContact / PostSolveContact: "<tag> call <step> <kind> <lower> <higher>"
+    // for the order of all listener calls, and "<tag> pre|post <step> <lower>
+    // <higher> <count> [<iteration>] <ni0 ti0 ni1 ti1>" with their arguments
+    auto shapes = [&world](ContactID id) {
+        const auto& c = GetContact(world, id);
+        const auto a = to_underlying(GetShapeA(c)), b = to_underlying(GetShapeB(c));
+        return std::pair<unsigned, unsigned>(unsigned(a < b ? a : b), unsigned(a < b ? b : a));
+    };
+    SetPreSolveContactListener(world, [&step, tag, shapes](ContactID id, const Manifold& old) {
+        const auto sh = shapes(id);
+        std::printf("%s call %d pre %u %u\n", tag, step, sh.first, sh.second);
+        std::printf("%s pre %d %u %u %d", tag, step, sh.first, sh.second, int(old.GetPointCount()));
+        for (auto k = 0u; k < 2u; ++k) {
+            const bool has = k < old.GetPointCount();
+            std::printf(" %a %a", has ? double(StripUnit(old.GetPoint(k).normalImpulse)) : 0.0,
+                        has ? double(StripUnit(old.GetPoint(k).tangentImpulse)) : 0.0);
+        }
+        std::printf("\n");
+    });
+    SetPostSolveContactListener(world, [&step, tag, shapes](ContactID id, const ContactImpulsesList& imp, unsigned it) {
+        const auto sh = shapes(id);
+        std::printf("%s call %d post %u %u\n", tag, step, sh.first, sh.second);
+        std::printf("%s post %d %u %u %d %u", tag, step, sh.first, sh.second, int(imp.GetCount()), it);
+        for (auto k = 0u; k < 2u; ++k) {
+            const bool has = k < imp.GetCount();
+            std::printf(" %a %a", has ? double(StripUnit(imp.GetEntryNormal(k))) : 0.0,
+                        has ? double(StripUnit(imp.GetEntryTanget(k))) : 0.0);
+        }
+        std::printf("\n");
+    });
     auto conf = StepConf{};
+    conf.doToi = doToi;
     auto boxContact = std::optional<ContactID>{};
     for (step = 1; step <= 60; ++step) {
         Step(world, conf);
@@ -174,7 +207,9 @@ int main() {
     CheckJoints();
     {
         auto ref = World{};
-        Conveyor(ref, "ref");
+        Conveyor(ref, "ref", true);
+        auto ref2 = World{};
+        Conveyor(ref2, "rnt", false);
     }
     const auto conf = StepConf{};
     try {
@@ -187,7 +222,9 @@ int main() {
                         static_cast<double>(StripUnit(GetY(location))), static_cast<double>(StripUnit(angle)));
         }
         auto gpu = World{GpuWorld{}};
-        Conveyor(gpu, "gpu");
+        Conveyor(gpu, "gpu", true);
+        auto gpu2 = World{GpuWorld{}};
+        Conveyor(gpu2, "gnt", false);
     } catch (const std::exception& e) {
         std::printf("error %s\n", e.what());
         return 3;

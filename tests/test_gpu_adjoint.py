@@ -225,35 +225,43 @@ def test_push_workload_gradients_against_fp64_finite_differences(gpu_lib, steps)
     all with friction mu, seed 2), checkpoint every 16 steps, loss = squared
     distance of each world's mean box centre from its target in [10,30]x[0,2].
     d(loss)/d(disk initial velocity x, y) and d(loss)/d(mu) from StepAdjoint on
-    the whole batch, against central differences (h = 1e-4) of the FP64 oracle.
+    the whole batch.
 
     mu is every shape's friction, so MixFriction (sqrt(f1 f2), Contact.hpp:57)
     gives mu for every contact and d(loss)/d(mu) is the sum of the adjoint's
     d(loss)/d(shape friction) over the world's shapes.
 
-    Solved to convergence (200 velocity, 30 position iterations, no sleep), and
-    the FP64 oracle replays, step by step, the Gauss-Seidel order the GPU swept
-    (prgpu_download_sweep_order): the position solver's result depends on the
-    order (its fixed points are not unique), and over hundreds of steps that
-    difference would otherwise dominate.
+    Solved to convergence (200 velocity, 30 position iterations, no sleep).  Two
+    checks:
 
-    The loss is only piecewise smooth: contacts begin and end, and friction
-    switches between sticking and sliding, at parameter values that a 1e-4 step
-    can straddle; across such a point no derivative exists and a central
-    difference means nothing.  So every 4th world is checked (16 of 64), and a
-    (world, parameter) pair counts where the central differences at h and h/2
-    agree within 1e-4 (the loss is smooth there); every pair that counts must
-    agree with the adjoint within 1e-3 relative.  Over 60 steps most pairs are
-    smooth; over 240 only a few are (none for mu), hence two windows."""
+    1. The adjoint (float reverse pass) against the FP64 tangent of the same
+       forward (forward mode along the GPU's own trajectory): every world and
+       parameter.  Over 60 steps within 1e-3; over 240 steps the reverse pass's
+       float rounding grows with the window in a few worlds, so there 90 % of the
+       pairs are held to 1e-3.
+
+    2. Against central differences (h = 1e-4) of the FP64 oracle, which replays
+       step by step the Gauss-Seidel order the GPU swept
+       (prgpu_download_sweep_order): the position solver's fixed points are not
+       unique, and over hundreds of steps the order would otherwise dominate.
+       The loss is only piecewise smooth (contacts begin and end, friction
+       switches between sticking and sliding), and the FP64 trajectory takes its
+       own pieces: it is compared where it takes the GPU's (the same number of
+       touching contacts in every step) and where the central differences at h
+       and h/2 agree within 1e-5 relative.  On a smooth piece they differ by
+       O(h^2) and by the FP64 rounding of the loss over 2h, both below 1e-8
+       here; a larger gap means a piece boundary (a stick-slip switch, say)
+       within h.  Every pair that counts must agree with the adjoint within 1e-3
+       relative; every 4th world is checked (16 of 64)."""
     worlds = scenes.push_worlds(64, seed=2)
     targets = _push_targets(64)
     conf = default_conf(**PUSH_CONF)
-    # the forward's sweep order, step by step (the step is deterministic: the
-    # adjoint's own forward takes the same path)
+    # the forward's sweep order and touching contacts, step by step (the step is
+    # deterministic: the adjoint's own forward takes the same path)
     rec = GpuBatch(worlds)
-    orders = []
+    orders, touching = [], np.zeros((steps, len(worlds)), np.int64)
     sb = np.asarray(rec.shape_base, np.int64)
-    for _ in range(steps):
+    for s in range(steps):
         rec.step(conf)
         o = rec.sweep_order().astype(np.int64)
         w = np.searchsorted(sb, o[:, 1], side="right") - 1
@@ -261,6 +269,9 @@ def test_push_workload_gradients_against_fp64_finite_differences(gpu_lib, steps)
         loc[:, 1] -= sb[w]
         loc[:, 2] -= sb[w]
         orders.append([loc[w == k] for k in range(len(worlds))])
+        c = rec.contacts()
+        cw = np.searchsorted(sb, c["proxy"][:, 0], side="right") - 1
+        touching[s] = np.bincount(cw[c["touching"] != 0], minlength=len(worlds))
     g = GpuBatch(worlds)
     g.adjoint_begin(16)
     g.adjoint_forward(steps, conf)
@@ -274,9 +285,42 @@ def test_push_workload_gradients_against_fp64_finite_differences(gpu_lib, steps)
     adj = g.adjoint_backward(ybar, None)
     info = g.adjoint_info()
     assert info["replay_mismatches"] == 0 and info["tape_overflows"] == 0, info
+    # the same derivatives by the FP64 tangent, all worlds at once
+    tan = {}
+    for name in ("vx", "vy", "mu"):
+        dv, df = np.zeros((g.n_bodies, 3)), np.zeros(g.n_shapes)
+        for k in range(len(worlds)):
+            if name == "mu":
+                df[int(g.shape_base[k]):int(g.shape_base[k + 1])] = 1.0
+            else:
+                dv[int(g.body_base[k]) + 1, 0 if name == "vx" else 1] = 1.0
+        tan[name] = g.adjoint_tangent(None, dv, df)["pos"]
     g.adjoint_end()
 
-    def loss(k, dvx=0.0, dvy=0.0, dmu=0.0):
+    def adjoint(k):
+        lo, hi = int(g.body_base[k]), int(g.shape_base[k])
+        return {"vx": float(adj["vel"][lo + 1, 0]), "vy": float(adj["vel"][lo + 1, 1]),
+                "mu": float(adj["friction"][hi:int(g.shape_base[k + 1])].astype(np.float64).sum())}
+
+    rels, nonfinite = [], []
+    for k in range(len(worlds)):
+        lo, hi = int(g.body_base[k]), int(g.body_base[k + 1])
+        ad = adjoint(k)
+        for name in ("vx", "vy", "mu"):
+            t = float((ybar[lo:hi] * tan[name][lo:hi]).sum())
+            if not (np.isfinite(ad[name]) and np.isfinite(t)):
+                nonfinite.append((k, name, ad[name], t))
+            rels.append(abs(ad[name] - t) / max(abs(t), 1e-3))
+    assert not nonfinite, nonfinite
+    rels = np.asarray(rels)
+    print(f"\n{steps} steps: adjoint vs FP64 tangent, worst rel {rels.max():.1e}, "
+          f"within 1e-3: {np.mean(rels <= 1e-3):.1%}")
+    if steps == 60:
+        assert rels.max() <= 1e-3
+    else:
+        assert np.mean(rels <= 1e-3) >= 0.9
+
+    def run(k, dvx=0.0, dvy=0.0, dmu=0.0, count=None):
         sc = worlds[k]
         s2 = scenes.Scene(**{f: getattr(sc, f) for f in sc.__dataclass_fields__})
         s2.body_vel = sc.body_vel.astype(np.float64).copy()
@@ -287,28 +331,33 @@ def test_push_workload_gradients_against_fp64_finite_differences(gpu_lib, steps)
         for s in range(steps):
             o.set_solve_order(orders[s][k])
             o.step(**PUSH_CONF)
+            if count is not None:
+                count.append(int(o.contacts()["touching"].sum()))
         return _push_loss(o.bodies()["pos"], targets, k)
 
     h = 1e-4
-    checked, report = {"vx": 0, "vy": 0, "mu": 0}, []
+    checked, report, skipped = {"vx": 0, "vy": 0, "mu": 0}, [], []
     for k in range(0, 64, 4):
-        lo, hi = int(g.body_base[k]), int(g.shape_base[k])
-        ad = {"vx": float(adj["vel"][lo + 1, 0]), "vy": float(adj["vel"][lo + 1, 1]),
-              "mu": float(adj["friction"][hi:int(g.shape_base[k + 1])].astype(np.float64).sum())}
+        seq = []
+        run(k, count=seq)
+        if not np.array_equal(seq, touching[:, k]):
+            skipped.append(k)  # the FP64 run takes other pieces: no common derivative
+            continue
+        ad = adjoint(k)
         for name, kw in (("vx", "dvx"), ("vy", "dvy"), ("mu", "dmu")):
-            fd = (loss(k, **{kw: h}) - loss(k, **{kw: -h})) / (2 * h)
-            fd2 = (loss(k, **{kw: h / 2}) - loss(k, **{kw: -h / 2})) / h
-            if abs(fd - fd2) > 1e-4 * max(abs(fd), 1e-3):
+            fd = (run(k, **{kw: h}) - run(k, **{kw: -h})) / (2 * h)
+            fd2 = (run(k, **{kw: h / 2}) - run(k, **{kw: -h / 2})) / h
+            if abs(fd - fd2) > 1e-5 * max(abs(fd), 1e-3):
                 continue  # not smooth at this point: no derivative to compare
             checked[name] += 1
             rel = abs(ad[name] - fd) / max(abs(fd), 1e-3)
             report.append((k, name, ad[name], fd, rel))
-    print(f"\n{steps} steps, smooth pairs checked {checked}")
+    print(f"{steps} steps, smooth pairs checked {checked}; worlds whose FP64 run took other pieces: {skipped}")
     for k, name, a, f, r in report:
         print(f"  world {k:2d} d/d{name}: adjoint {a:.6g} fd {f:.6g} rel {r:.1e}")
     bad = [r for r in report if r[4] > 1e-3]
     assert not bad, bad
     if steps == 60:
-        assert checked["vx"] >= 8 and checked["vy"] >= 8 and checked["mu"] >= 4, checked
+        assert checked["vx"] >= 6 and checked["vy"] >= 6 and checked["mu"] >= 2, checked
     else:
-        assert checked["vx"] + checked["vy"] >= 4, checked
+        assert checked["vx"] + checked["vy"] >= 2, checked

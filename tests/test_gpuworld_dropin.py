@@ -140,3 +140,15 @@ def test_helloworld_over_gpuworld_steps_on_the_gpu(gpu_lib):
         assert np.allclose(gv, rv, rtol=0, atol=1e-5), (g[0], gv, rv)
     assert float.fromhex(rp[43][1]) > 0.5  # the conveyor moved the box
     assert float.fromhex(rp[59][2]) < 0.3  # once disabled, the contact no longer holds it
+    # The scenario again without the time-of-impact phase (whose own listener
+    # calls GpuWorld does not make): every listener call, in order (Begin/End,
+    # PreSolve, PostSolve), and the pre- and post-solve arguments: point counts
+    # and iteration arguments exactly, impulses within 1e-4.
+    assert lines("gnt", "call") == lines("rnt", "call")
+    for kind, head in (("pre", 4), ("post", 5)):
+        gl, rl = lines("gnt", kind), lines("rnt", kind)
+        assert len(gl) == len(rl) > 20, kind
+        for g, r in zip(gl, rl):
+            assert g[:head] == r[:head], (kind, g, r)
+            gv, rv = [float.fromhex(x) for x in g[head:]], [float.fromhex(x) for x in r[head:]]
+            assert np.allclose(gv, rv, rtol=1e-4, atol=1e-4), (kind, g, r)

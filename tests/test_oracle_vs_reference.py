@@ -23,6 +23,7 @@ def _compare(scene, steps, double=False, **conf):
         c = ow.contacts()
         np.testing.assert_array_equal(c["proxy"], d["contacts"]["proxy"])
         np.testing.assert_array_equal(c["count"], d["contacts"]["count"])
+        np.testing.assert_array_equal(c["touching"], d["contacts"]["touching"])
         for k in range(len(c["count"])):
             m = int(c["count"][k])
             np.testing.assert_array_equal(c["features"][k][:m], d["contacts"]["features"][k][:m])
@@ -104,3 +105,76 @@ def test_gear_joints(double):
     # gear trains (revolute-revolute, one on a motor) and rack-and-pinion gears
     # (revolute-prismatic) with disks falling on them
     _compare(scenes.gear_scene(np.random.default_rng(61)), [1, 60, 120], double=double)
+
+
+def _compare_solve_calls(scene, steps, double=False, **conf):
+    """The oracle's PreSolveContact / PostSolveContact calls (contact, point count,
+    iteration argument, impulses) equal the reference listeners', call for call."""
+    dumps = refdriver.run(scenes.scene_text(scene, conf), steps, double=double)
+    ow = oracle.OracleWorld(scene, double=double)
+    kinds = {3: 0, 4: 0}
+    for n, d in zip(steps, dumps):
+        calls = []
+        for _ in range(n):
+            ow.step(**conf)
+            calls += ow.solve_calls()
+        assert calls == d["solve_calls"]
+        for c in calls:
+            kinds[c[0]] += 1
+    return kinds
+
+
+@pytest.mark.parametrize("seed", [44, 45])
+def test_presolve_postsolve_piles(seed):
+    kinds = _compare_solve_calls(scenes.pile(150, np.random.default_rng(seed)), [1, 40, 100])
+    assert kinds[3] > 0 and kinds[4] > 0
+
+
+def test_presolve_postsolve_with_toi_f64():
+    # bullets: the time-of-impact islands report too (AabbTreeWorld.cpp:2053)
+    kinds = _compare_solve_calls(scenes.bullets(40, np.random.default_rng(46)), [1, 20, 40], double=True, doToi=1)
+    assert kinds[3] > 0 and kinds[4] > 0
+
+
+@pytest.mark.parametrize("double", [False, True])
+def test_sensors(double):
+    # sensor zones and sensor bodies: touching by TestOverlap (AabbTreeWorld.cpp:
+    # 2620-2634), no manifolds, Begin/EndContact for them
+    sc = scenes.sensor_scene(np.random.default_rng(47))
+    _compare(sc, [1, 60, 150], double=double)
+    assert _compare_events(sc, [1, 60, 150], double=double) > 0
+    dumps = refdriver.run(scenes.scene_text(sc, {}), [150], double=double)
+    sensor_shapes = set(np.flatnonzero(sc.shape_filter[:, 3]).tolist())
+    ev = [e for e in dumps[0]["events"] if e[1] in sensor_shapes or e[2] in sensor_shapes]
+    assert len(ev) > 0  # sensors did begin or end touching
+
+
+def _rays(rng, n, half):
+    """Rays across a world of half-width `half`: random ends, a few vertical ones
+    and short ones, maxFraction in (0, 1]."""
+    a = np.stack([rng.uniform(-half, half, n), rng.uniform(0.0, 5.0, n)], 1)
+    b = np.stack([rng.uniform(-half, half, n), rng.uniform(-1.0, 5.0, n)], 1)
+    b[: n // 8, 0] = a[: n // 8, 0]  # vertical
+    b[n // 8: n // 4] = a[n // 8: n // 4] + rng.uniform(-0.5, 0.5, (n // 4 - n // 8, 2))  # short
+    f = rng.uniform(0.2, 1.0, n)
+    f[::3] = 1.0
+    return np.concatenate([a, b, f[:, None]], 1)
+
+
+@pytest.mark.parametrize("double", [False, True])
+def test_raycast(double):
+    # RayCast(World, RayCastInput, callback) (RayCastOutput.cpp:301-337) answering
+    # ResetRay: every shape hit, its point and normal, after the pile has settled
+    # into contact; the reference reports them in tree order, the oracle in shape order
+    sc = scenes.pile(150, np.random.default_rng(48))
+    rays = _rays(np.random.default_rng(49), 200, 18.0)
+    ref = refdriver.run_rays(scenes.scene_text(sc, {}), 120, rays, double=double)
+    ow = oracle.OracleWorld(sc, double=double)
+    for _ in range(120):
+        ow.step()
+    hits = 0
+    for r, want in zip(rays, ref):
+        got = ow.raycast(r[0:2], r[2:4], r[4])
+        assert [(g[0], g[2], g[3], g[4], g[5]) for g in got] == sorted(want), r
+        hits += len(got)
+    assert hits > 100
