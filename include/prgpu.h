@@ -355,6 +355,22 @@ int prgpu_download_contacts_noalloc(prgpu_world* w, uint32_t capacity, uint32_t*
  *   mat4[4i..] friction, restitution, tangent speed, enabled (1 or 0) (Contact.hpp)
  * Either array may be NULL. */
 int prgpu_download_contact_state(prgpu_world* w, uint32_t capacity, uint32_t* n_out, uint32_t* slots, float* mat4);
+/* Capacity growth (off by default).  The reference's contact containers grow
+ * without bound; a batch holds contact_capacity contacts and candidate_capacity
+ * new pairs per search, and a step that runs out raises PRGPU_ECAPACITY with its
+ * state already advanced without the contacts it could not hold.  With growth on,
+ * prgpu_step and prgpu_step_n keep the state before each step on the device (one
+ * copy of the batch's persistent arrays), and a step that runs out is undone,
+ * both capacities double (up to 16 times) and the step runs again, with the same
+ * result as with the larger capacities from the start.  prgpu_step_async and
+ * prgpu_step_profiled do not grow.  Not inside an adjoint window. */
+int prgpu_set_capacity_growth(prgpu_world* w, int enabled);
+int prgpu_get_capacities(prgpu_world* w, uint32_t* contacts, uint32_t* candidates);
+/* Spins a grid-wide barrier wait may take before it gives up, records
+ * PRGPU_ETIMEOUT in the device error word and lets the kernel drain (0 restores
+ * the default of 2^24; 1 gives up at the first wait).  For failure tests of the
+ * bounded waits. */
+int prgpu_set_wait_limit(prgpu_world* w, uint32_t spins);
 /* Records for the PreSolveContact / PostSolveContact listeners
  * (ContactManifoldFunction, ContactImpulsesFunction; called by the reference at
  * AabbTreeWorld.cpp:2716-2720 and :1669-1672).  Enabling keeps, for every contact

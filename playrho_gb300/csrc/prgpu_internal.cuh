@@ -161,6 +161,7 @@ struct Counters {
     uint32_t bar_gen;
     uint32_t need_find;
     uint32_t step_no;         // steps begun (tags the contact updates and solve records of a step)
+    uint32_t wait_limit;      // spins a grid-barrier wait may take (0: the default, 2^24)
     uint32_t upd_phase;       // phase bit the contact updates are tagged with (kUpd*)
     // StepStats counters (StepStats.hpp)
     uint32_t st_contacts_added;
@@ -423,9 +424,10 @@ __device__ __forceinline__ void grid_barrier(Counters* c) {
                 __threadfence();
                 atomicAdd(&c->bar_gen, 1u);
             } else {
+                const uint32_t limit = c->wait_limit ? c->wait_limit - 1u : (1u << 24);
                 uint32_t spins = 0;
                 while (*vgen == g) {
-                    if (++spins > (1u << 24)) {
+                    if (spins++ >= limit) {
                         set_error(c, PR_ETIMEOUT, 900u);
                         break;
                     }

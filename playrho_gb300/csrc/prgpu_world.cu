@@ -19,6 +19,12 @@
 
 using namespace prgpu;
 
+// Sizes of a batch's device arrays.
+struct WorldDims {
+    uint32_t W, N, S, J, C, K, V, JO, JC;  // worlds, bodies, shapes, joints, contact and candidate
+                                           // capacity, vertices, joint-partner and collide entries
+};
+
 struct prgpu_world {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -39,6 +45,10 @@ struct prgpu_world {
     // pinned copy of the device error word and site, written by every graph-replayed
     // step as it ends (read by prgpu_step_async without waiting)
     uint32_t* h_err = nullptr;
+    WorldDims dims{};            // sizes the device arrays were allocated with
+    bool grow = false;           // prgpu_set_capacity_growth
+    void* backup = nullptr;      // the state before the step in flight (growth on)
+    size_t backup_bytes = 0;
     float4* post_imp = nullptr;  // solve records (prgpu_set_solve_records), allocated on first use
     uint2* post_tag = nullptr;
     bool stepped = false;       // a step has run: proxies exist
@@ -51,6 +61,12 @@ struct prgpu_world {
 };
 
 extern "C" void adjoint_drop_graphs(prgpu_world* w);
+
+extern "C" {
+static int alloc_world(prgpu_world* w, const WorldDims& z);
+static int snap_copy(prgpu_world* w, void* buf, bool save);
+static size_t snap_size(const prgpu_world* w);
+}
 
 namespace {
 
@@ -639,6 +655,107 @@ int launch_step_graphs(prgpu_world* w, int n) {
     return PRGPU_OK;
 }
 
+// Moves a batch onto arrays of contact capacity C2 and candidate capacity K2:
+// every array that is not per-step scratch is copied by position into its
+// larger counterpart (alloc_world's order), so slots, keys and lists keep their
+// indices and the batch continues exactly as it would have with the larger
+// capacities from the start.
+int grow_world(prgpu_world* w, uint32_t C2, uint32_t K2) {
+    if (w->adj) return fail(w, PRGPU_ESTATE, "capacities cannot grow inside an adjoint window");
+    int rc = drop_graph(w);
+    if (rc) return rc;
+    prgpu_world* n = new prgpu_world();
+    n->device = w->device;
+    n->d = w->d;
+    n->d.contact_cap = C2;
+    n->d.cand_cap = K2;
+    WorldDims z = w->dims;
+    z.C = C2;
+    z.K = K2;
+    rc = alloc_world(n, z);
+    if (rc == PRGPU_OK && n->allocs.size() != w->allocs.size()) rc = PRGPU_ESTATE;
+    for (size_t i = 0; rc == PRGPU_OK && i < w->allocs.size(); ++i) {
+        if (w->alloc_scratch[i]) continue;
+        const size_t b = std::min(w->alloc_bytes[i], n->alloc_bytes[i]);
+        if (cudaMemcpyAsync(n->allocs[i], w->allocs[i], b, cudaMemcpyDeviceToDevice, w->stream) != cudaSuccess)
+            rc = PRGPU_ECUDA;
+    }
+    float4* post_imp = nullptr;
+    uint2* post_tag = nullptr;
+    if (rc == PRGPU_OK && w->post_imp) {
+        const size_t c0 = w->dims.C;
+        if (cudaMalloc(&post_imp, sizeof(float4) * C2) != cudaSuccess ||
+            cudaMalloc(&post_tag, sizeof(uint2) * C2) != cudaSuccess ||
+            cudaMemsetAsync(post_tag, 0, sizeof(uint2) * C2, w->stream) != cudaSuccess ||
+            cudaMemcpyAsync(post_imp, w->post_imp, sizeof(float4) * c0, cudaMemcpyDeviceToDevice, w->stream) != cudaSuccess ||
+            cudaMemcpyAsync(post_tag, w->post_tag, sizeof(uint2) * c0, cudaMemcpyDeviceToDevice, w->stream) != cudaSuccess)
+            rc = PRGPU_ECUDA;
+    }
+    if (rc == PRGPU_OK && cudaStreamSynchronize(w->stream) != cudaSuccess) rc = PRGPU_ECUDA;
+    if (rc != PRGPU_OK) {
+        if (post_imp) cudaFree(post_imp);
+        if (post_tag) cudaFree(post_tag);
+        prgpu_world_destroy(n);
+        return fail(w, rc, "capacity growth to %u contacts failed", C2);
+    }
+    const bool records = w->d.cs_post_tag != nullptr;
+    std::swap(w->allocs, n->allocs);
+    std::swap(w->alloc_bytes, n->alloc_bytes);
+    std::swap(w->alloc_scratch, n->alloc_scratch);
+    std::swap(w->d_conf, n->d_conf);
+    std::swap(w->d_stage, n->d_stage);
+    w->d = n->d;
+    w->dims = z;
+    if (w->post_imp) {
+        std::swap(w->post_imp, post_imp);
+        std::swap(w->post_tag, post_tag);
+        cudaFree(post_imp);
+        cudaFree(post_tag);
+    }
+    w->d.cs_post = records ? w->post_imp : nullptr;
+    w->d.cs_post_tag = records ? w->post_tag : nullptr;
+    if (w->backup) { cudaFree(w->backup); w->backup = nullptr; w->backup_bytes = 0; }
+    prgpu_world_destroy(n);  // the arrays the batch left
+    return PRGPU_OK;
+}
+
+int run_steps(prgpu_world* w, const prgpu_step_conf* conf, int n, bool sync);
+
+// Keeps the state before the step in w->backup (growth on).
+int take_backup(prgpu_world* w) {
+    const size_t bytes = snap_size(w);
+    if (!w->backup || w->backup_bytes != bytes) {
+        if (w->backup) cudaFree(w->backup);
+        w->backup = nullptr;
+        CU(cudaMalloc(&w->backup, bytes));
+        w->backup_bytes = bytes;
+    }
+    return snap_copy(w, w->backup, true);
+}
+
+// Steps one by one; a step that runs out of contact or candidate capacity
+// (PRGPU_ECAPACITY) is undone from the state kept before it, both capacities
+// double, and the step runs again.
+int run_steps_growing(prgpu_world* w, const prgpu_step_conf* conf, int n) {
+    constexpr int kMaxDoublings = 16;
+    for (int i = 0; i < n; ++i) {
+        int rc = take_backup(w);
+        if (rc) return rc;
+        for (int attempt = 0;; ++attempt) {
+            rc = run_steps(w, conf, 1, true);
+            if (rc != PRGPU_ECAPACITY || attempt == kMaxDoublings) break;
+            if ((rc = snap_copy(w, w->backup, false)) != PRGPU_OK) return rc;
+            CU(cudaStreamSynchronize(w->stream));
+            const uint32_t C2 = (uint32_t)std::min<uint64_t>(2ull * w->dims.C, 0x7fffffffull);
+            const uint32_t K2 = (uint32_t)std::min<uint64_t>(2ull * w->dims.K, 0x7fffffffull);
+            if ((rc = grow_world(w, C2, K2)) != PRGPU_OK) return rc;
+            if ((rc = take_backup(w)) != PRGPU_OK) return rc;
+        }
+        if (rc) return rc;
+    }
+    return PRGPU_OK;
+}
+
 int run_steps(prgpu_world* w, const prgpu_step_conf* conf, int n, bool sync) {
     int rc = set_conf(w, conf);
     if (rc) return rc;
@@ -917,6 +1034,70 @@ int prgpu_prepare_bodies(const prgpu_batch_desc* ds, float* pos3, float* vel3, f
     return PRGPU_OK;
 }
 
+// Allocates every device array of a batch (in one fixed order: capacity growth
+// copies a world's arrays onto a larger set by position in that order) and
+// points w->d at them.
+static int alloc_world(prgpu_world* w, const WorldDims& z) {
+    DW& d = w->d;
+    const uint32_t W = z.W, N = z.N, S = z.S, J = z.J, C = z.C, K = z.K;
+    const uint32_t items = std::max<uint32_t>(std::max<uint32_t>(C + J, N + 1), S) + 1;
+    int rc = 0;
+#define AL(ptr, n) do { rc = dalloc(w, &(ptr), (size_t)(n)); if (rc) return rc; } while (0)
+    // per-step scratch: every step writes it before reading it
+#define ALS(ptr, n) do { rc = dalloc(w, &(ptr), (size_t)(n), true); if (rc) return rc; } while (0)
+    AL(d.partial, 1024); AL(d.hist, 256 * 1024);
+    Counters* cnt;
+    AL(cnt, 1);
+    d.cnt = cnt;
+    AL(w->d_conf, 1);
+    d.conf = w->d_conf;
+    AL(w->d_stage, (size_t)N * 8 + 16);
+    uint32_t *w_body_off, *w_shape_off;
+    AL(w_body_off, W + 1); AL(w_shape_off, W + 1);
+    d.w_body_off = w_body_off; d.w_shape_off = w_shape_off;
+    AL(d.w_root, W); AL(d.w_bounds, W);
+    uint32_t* w_order;
+    AL(w_order, W); d.w_order = w_order;
+    AL(d.w_kc, W + 1); AL(d.w_kj, W + 1); ALS(d.w_toi, W); ALS(d.w_toi_ep, W);
+    AL(d.b_pos1, N); AL(d.b_pos0, N); AL(d.b_vel, N); AL(d.b_xf, N); AL(d.b_mass, N); AL(d.b_acc, N);
+    AL(d.b_damp, N); AL(d.b_flags, N); AL(d.b_uat, N); AL(d.b_world, N); AL(d.b_island, N);
+    // the TOI phase's own state: reset when the phase starts
+    ALS(d.b_alpha0, N); ALS(d.b_toi_ep, N); ALS(d.b_toi_rst, N);
+    uint32_t *b_shape_off, *b_shapes;
+    AL(b_shape_off, N + 1); AL(b_shapes, S);
+    d.b_shape_off = b_shape_off; d.b_shapes = b_shapes;
+    AL(d.b_jnt_off, N + 1); AL(d.b_jnt_other, z.JO); AL(d.b_jnt_cc, z.JC);
+    AL(d.isl_awake, N); ALS(d.isl_sep, (size_t)N * kMaxPosIters); ALS(d.isl_jok, (size_t)N * kMaxPosIters); AL(d.isl_uat, N);
+    AL(d.s_body, S); AL(d.s_meta, S); AL(d.s_voff, S); AL(d.s_radius, S); AL(d.s_mat, S); AL(d.s_filter, S);
+    AL(d.s_group, S); AL(d.verts, z.V); AL(d.p_aabb, S); AL(d.p_moved, S); AL(d.moved_list, S);
+    AL(d.j_bodies, 2 * J); AL(d.j_anchor, J); AL(d.j_param, J); AL(d.j_maxtorque, J); AL(d.j_flags, J);
+    float4* j_extra_d;
+    AL(j_extra_d, 2 * (size_t)J);
+    d.j_extra = j_extra_d;
+    float4* j_gear_d;
+    AL(j_gear_d, 5 * (size_t)J);
+    d.j_gear = j_gear_d;
+    AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_m2, J); AL(d.j_imp, J);
+    AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
+    AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C); AL(d.cs_tspeed, C);
+    AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C); AL(d.cs_prio, C); AL(d.cs_upd, C);
+    ALS(d.cs_toi_ep, C); ALS(d.cs_toi_at, C); ALS(d.t_key, C); ALS(d.t_slot, C);
+    AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
+    ALS(d.n_key, K); ALS(d.n_key_alt, K); ALS(d.n_val, K); ALS(d.n_val_alt, K);
+    AL(d.l_key, S); AL(d.l_key_alt, S); AL(d.l_idx, S); AL(d.l_idx_alt, S); AL(d.l_leaf_box, S);
+    AL(d.l_node_box, S); AL(d.l_left, S); AL(d.l_right, S); AL(d.l_parent, 2 * (size_t)S); AL(d.l_range, 2 * (size_t)S);
+    AL(d.l_visit, S);
+    ALS(d.k_list, C + J); ALS(d.k_colour, C + J); ALS(d.k_tent, C + J); ALS(d.k_order, C + J);
+    ALS(d.t_id, C + J);
+    ALS(d.k_prio, C + J);
+    AL(d.inc_off, N + 1); AL(d.inc_cur, N + 1); ALS(d.inc_list, 2 * (size_t)C + 4 * (size_t)J);
+    ALS(d.vc0, C + J); ALS(d.vc1, C + J); ALS(d.pc, C + J);
+    ALS(d.flags, items); ALS(d.scan, items);
+#undef AL
+#undef ALS
+    return PRGPU_OK;
+}
+
 int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out) {
     if (!ds || !out) return PRGPU_EINVAL;
     *out = nullptr;
@@ -944,7 +1125,6 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     const uint64_t kcap = ds->candidate_capacity ? ds->candidate_capacity : (uint64_t)8 * S + 4096;
     if (ccap > 0x7fffffffull || kcap > 0x7fffffffull) return bail(PRGPU_ECAPACITY);
     const uint32_t C = (uint32_t)ccap, K = (uint32_t)kcap;
-    const uint32_t items = std::max<uint32_t>(std::max<uint32_t>(C + J, N + 1), S) + 1;
     DW& d = w->d;
     d.n_worlds = W; d.n_bodies = N; d.n_shapes = S; d.n_joints = J; d.n_verts = (uint32_t)vtx.size();
     d.contact_cap = C; d.cand_cap = K;
@@ -953,50 +1133,20 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     d.world_bits = (uint32_t)bits_for((uint64_t)W + 1);
     if (30 + d.world_bits > 64) return bail(PRGPU_ECAPACITY);
     int rc = 0;
-#define AL(ptr, n) do { rc = dalloc(w, &(ptr), (size_t)(n)); if (rc) return bail(rc); } while (0)
-    // per-step scratch: every step writes it before reading it
-#define ALS(ptr, n) do { rc = dalloc(w, &(ptr), (size_t)(n), true); if (rc) return bail(rc); } while (0)
-    uint32_t *w_body_off, *w_shape_off;
-    AL(w_body_off, W + 1); AL(w_shape_off, W + 1);
-    d.w_body_off = w_body_off; d.w_shape_off = w_shape_off;
-    AL(d.w_root, W); AL(d.w_bounds, W);
-    uint32_t* w_order;
-    AL(w_order, W); d.w_order = w_order;
-    AL(d.w_kc, W + 1); AL(d.w_kj, W + 1); ALS(d.w_toi, W); ALS(d.w_toi_ep, W);
-    AL(d.b_pos1, N); AL(d.b_pos0, N); AL(d.b_vel, N); AL(d.b_xf, N); AL(d.b_mass, N); AL(d.b_acc, N);
-    AL(d.b_damp, N); AL(d.b_flags, N); AL(d.b_uat, N); AL(d.b_world, N); AL(d.b_island, N);
-    // the TOI phase's own state: reset when the phase starts
-    ALS(d.b_alpha0, N); ALS(d.b_toi_ep, N); ALS(d.b_toi_rst, N);
-    uint32_t *b_shape_off, *b_shapes;
-    AL(b_shape_off, N + 1); AL(b_shapes, S);
-    d.b_shape_off = b_shape_off; d.b_shapes = b_shapes;
-    AL(d.b_jnt_off, N + 1); AL(d.b_jnt_other, jother.size()); AL(d.b_jnt_cc, jcc.size());
-    AL(d.isl_awake, N); ALS(d.isl_sep, (size_t)N * kMaxPosIters); ALS(d.isl_jok, (size_t)N * kMaxPosIters); AL(d.isl_uat, N);
-    AL(d.s_body, S); AL(d.s_meta, S); AL(d.s_voff, S); AL(d.s_radius, S); AL(d.s_mat, S); AL(d.s_filter, S);
-    AL(d.s_group, S); AL(d.verts, vtx.size()); AL(d.p_aabb, S); AL(d.p_moved, S); AL(d.moved_list, S);
-    AL(d.j_bodies, 2 * J); AL(d.j_anchor, J); AL(d.j_param, J); AL(d.j_maxtorque, J); AL(d.j_flags, J);
-    float4* j_extra_d;
-    AL(j_extra_d, 2 * (size_t)J);
-    d.j_extra = j_extra_d;
-    float4* j_gear_d;
-    AL(j_gear_d, 5 * (size_t)J);
-    d.j_gear = j_gear_d;
-    AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_m2, J); AL(d.j_imp, J);
-    AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
-    AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C); AL(d.cs_tspeed, C);
-    AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C); AL(d.cs_prio, C); AL(d.cs_upd, C);
-    ALS(d.cs_toi_ep, C); ALS(d.cs_toi_at, C); ALS(d.t_key, C); ALS(d.t_slot, C);
-    AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
-    ALS(d.n_key, K); ALS(d.n_key_alt, K); ALS(d.n_val, K); ALS(d.n_val_alt, K);
-    AL(d.l_key, S); AL(d.l_key_alt, S); AL(d.l_idx, S); AL(d.l_idx_alt, S); AL(d.l_leaf_box, S);
-    AL(d.l_node_box, S); AL(d.l_left, S); AL(d.l_right, S); AL(d.l_parent, 2 * (size_t)S); AL(d.l_range, 2 * (size_t)S);
-    AL(d.l_visit, S);
-    ALS(d.k_list, C + J); ALS(d.k_colour, C + J); ALS(d.k_tent, C + J); ALS(d.k_order, C + J);
-    ALS(d.t_id, C + J);
-    ALS(d.k_prio, C + J);
-    AL(d.inc_off, N + 1); AL(d.inc_cur, N + 1); ALS(d.inc_list, 2 * (size_t)C + 4 * (size_t)J);
-    ALS(d.vc0, C); ALS(d.vc1, C); ALS(d.pc, C);
-    ALS(d.flags, items); ALS(d.scan, items);
+    {
+        WorldDims z;
+        z.W = W; z.N = N; z.S = S; z.J = J; z.C = C; z.K = K; z.V = (uint32_t)vtx.size();
+        z.JO = (uint32_t)jother.size(); z.JC = (uint32_t)jcc.size();
+        w->dims = z;
+        if ((rc = alloc_world(w, z)) != PRGPU_OK) return bail(rc);
+    }
+    uint32_t* w_body_off = const_cast<uint32_t*>(d.w_body_off);
+    uint32_t* w_shape_off = const_cast<uint32_t*>(d.w_shape_off);
+    uint32_t* w_order = const_cast<uint32_t*>(d.w_order);
+    uint32_t* b_shape_off = const_cast<uint32_t*>(d.b_shape_off);
+    uint32_t* b_shapes = const_cast<uint32_t*>(d.b_shapes);
+    float4* j_extra_d = const_cast<float4*>(d.j_extra);
+    float4* j_gear_d = const_cast<float4*>(d.j_gear);
     w->L.prims.sm_count = 1;
     {
         cudaDeviceProp prop;
@@ -1004,13 +1154,6 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
         w->L.prims.sm_count = prop.multiProcessorCount;
     }
     w->L.prims.grid = std::min(1024, 2 * w->L.prims.sm_count);
-    AL(d.partial, 1024); AL(d.hist, 256 * 1024);
-    Counters* cnt;
-    AL(cnt, 1);
-    d.cnt = cnt;
-    AL(w->d_conf, 1);
-    d.conf = w->d_conf;
-    AL(w->d_stage, (size_t)N * 8 + 16);
     if (cudaMallocHost(&w->h_cnt, sizeof(Counters)) != cudaSuccess) return bail(PRGPU_ECUDA);
     if (cudaMallocHost(&w->h_err, 2 * sizeof(uint32_t)) != cudaSuccess) return bail(PRGPU_ECUDA);
     w->h_err[0] = w->h_err[1] = 0u;
@@ -1097,7 +1240,6 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     launch_init_bodies(d, w->L, w->stream);
     if (cudaStreamSynchronize(w->stream) != cudaSuccess) return bail(PRGPU_ECUDA);
     if (cudaGetLastError() != cudaSuccess) return bail(PRGPU_ECUDA);
-#undef AL
     *out = w;
     return PRGPU_OK;
 }
@@ -1118,6 +1260,7 @@ int prgpu_world_destroy(prgpu_world* w) {
     for (void* p : w->allocs) cudaFree(p);
     if (w->post_imp) cudaFree(w->post_imp);
     if (w->post_tag) cudaFree(w->post_tag);
+    if (w->backup) cudaFree(w->backup);
     if (w->h_cnt) cudaFreeHost(w->h_cnt);
     if (w->h_err) cudaFreeHost(w->h_err);
     if (w->stream) cudaStreamDestroy(w->stream);
@@ -1163,7 +1306,7 @@ void fill_stats(const Counters& c, prgpu_step_stats* st) {
 int prgpu_step(prgpu_world* w, const prgpu_step_conf* conf, prgpu_step_stats* st) {
     if (!w) return PRGPU_EINVAL;
     CU(cudaSetDevice(w->device));
-    const int rc = run_steps(w, conf, 1, true);
+    const int rc = w->grow ? run_steps_growing(w, conf, 1) : run_steps(w, conf, 1, true);
     if (rc) return rc;
     if (st) fill_stats(*w->h_cnt, st);
     return PRGPU_OK;
@@ -1172,7 +1315,34 @@ int prgpu_step(prgpu_world* w, const prgpu_step_conf* conf, prgpu_step_stats* st
 int prgpu_step_n(prgpu_world* w, const prgpu_step_conf* conf, int n) {
     if (!w || n < 0) return PRGPU_EINVAL;
     CU(cudaSetDevice(w->device));
-    return run_steps(w, conf, n, true);
+    return w->grow ? run_steps_growing(w, conf, n) : run_steps(w, conf, n, true);
+}
+
+int prgpu_set_capacity_growth(prgpu_world* w, int enabled) {
+    if (!w) return PRGPU_EINVAL;
+    w->grow = enabled != 0;
+    if (!w->grow && w->backup) {
+        CU(cudaSetDevice(w->device));
+        cudaFree(w->backup);
+        w->backup = nullptr;
+        w->backup_bytes = 0;
+    }
+    return PRGPU_OK;
+}
+
+int prgpu_get_capacities(prgpu_world* w, uint32_t* contacts, uint32_t* candidates) {
+    if (!w) return PRGPU_EINVAL;
+    if (contacts) *contacts = w->d.contact_cap;
+    if (candidates) *candidates = w->d.cand_cap;
+    return PRGPU_OK;
+}
+
+int prgpu_set_wait_limit(prgpu_world* w, uint32_t spins) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    CU(cudaMemcpyAsync(&w->d.cnt->wait_limit, &spins, sizeof(spins), cudaMemcpyHostToDevice, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
 }
 
 int prgpu_step_profiled(prgpu_world* w, const prgpu_step_conf* conf, float* phase_ms, int n_phases,

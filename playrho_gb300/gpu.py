@@ -137,6 +137,9 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_download_contact_state.argtypes = [P, U, P, P, P]
     lib.prgpu_set_solve_records.argtypes = [P, I]
     lib.prgpu_query_aabbs.argtypes = [P, U, P, P, U, P, P]
+    lib.prgpu_set_capacity_growth.argtypes = [P, I]
+    lib.prgpu_get_capacities.argtypes = [P, P, P]
+    lib.prgpu_set_wait_limit.argtypes = [P, U]
     lib.prgpu_raycast.argtypes = [P, U, P, P, P, P]
     lib.prgpu_raycast_all.argtypes = [P, U, P, U, P, P, P]
     lib.prgpu_download_solve_records.argtypes = [P, U, P, P, P, P]
@@ -159,7 +162,7 @@ def exported_symbols() -> List[str]:
         "prgpu_download_sweep_order", "prgpu_download_contacts_noalloc", "prgpu_download_contact_seq",
         "prgpu_query_aabb", "prgpu_download_contact_state", "prgpu_set_contact", "prgpu_set_manifold",
         "prgpu_set_solve_records", "prgpu_download_solve_records", "prgpu_query_aabbs", "prgpu_raycast",
-        "prgpu_raycast_all"]
+        "prgpu_raycast_all", "prgpu_set_capacity_growth", "prgpu_get_capacities", "prgpu_set_wait_limit"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -572,6 +575,20 @@ class GpuBatch:
         n = ctypes.c_uint64()
         self._check(self.lib.prgpu_get_body_steps(self.h, ctypes.byref(n)), "prgpu_get_body_steps")
         return int(n.value)
+
+    def set_capacity_growth(self, enabled: bool = True):
+        """Undo a step that runs out of contact or candidate capacity, double both and
+        run it again (prgpu_set_capacity_growth)."""
+        self._check(self.lib.prgpu_set_capacity_growth(self.h, int(bool(enabled))), "prgpu_set_capacity_growth")
+
+    def capacities(self) -> tuple:
+        c, k = ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self.lib.prgpu_get_capacities(self.h, ctypes.byref(c), ctypes.byref(k)), "prgpu_get_capacities")
+        return c.value, k.value
+
+    def set_wait_limit(self, spins: int):
+        """Spins a grid-barrier wait may take before it gives up (0: default)."""
+        self._check(self.lib.prgpu_set_wait_limit(self.h, int(spins)), "prgpu_set_wait_limit")
 
     def contact_slots(self) -> np.ndarray:
         """Slot (ContactID) of every live contact, in the order of contacts()."""

@@ -284,6 +284,8 @@ void HostWorld::Build() {
     }
     Check(prgpu_world_create(&d, device_, &gpu_), "prgpu_world_create");
     rebuild_ = false;
+    // the reference's contact containers grow without bound: so do the batch's
+    Check(prgpu_set_capacity_growth(gpu_, 1), "prgpu_set_capacity_growth");
     if (solve_records_) Check(prgpu_set_solve_records(gpu_, 1), "prgpu_set_solve_records");
     state_dirty_.assign(bodies_.size(), false);
     lc_.assign(2 * (size_t)N, 0.f);
