@@ -25,6 +25,18 @@
  *                               PolygonShapeConf.cpp:120-133, DistanceProxy.cpp:62-105
  *   prgpu_time_of_impact        GetToiViaSat(proxyA, sweepA, proxyB, sweepB, ToiConf),
  *                               Library/include/playrho/d2/TimeOfImpact.hpp, TimeOfImpact.cpp:37-253
+ *   prgpu_query_aabb(s)         Query(GetTree(World), AABB, callback), DynamicTree.cpp:673-710
+ *   prgpu_raycast(_all)         RayCast(World, RayCastInput, callback), RayCastOutput.cpp:301-337
+ *   prgpu_download_contact_seq  the contact-list (creation) order of GetContacts(World)
+ *   prgpu_download_contact_state  ContactID + GetContact (enabled, friction, restitution,
+ *                               tangent speed), AabbTreeWorld.cpp:2797-2832
+ *   prgpu_set_contact           SetContact(World, ContactID, Contact), AabbTreeWorld.cpp:2797-2832
+ *   prgpu_set_manifold          SetManifold(World, ContactID, Manifold), AabbTreeWorld.cpp:2834-2848
+ *   prgpu_set_solve_records,    the arguments of the PreSolveContact / PostSolveContact
+ *   prgpu_download_solve_records  listeners, AabbTreeWorld.cpp:2716-2720, :1669-1672
+ *   prgpu_set_capacity_growth   the unbounded growth of the reference's contact containers
+ * The remaining entry points (schedule, autotuner, StepAdjoint, sweep order, body
+ * steps, wait limit, allocation-free download) have no reference counterpart.
  */
 #ifndef PRGPU_H
 #define PRGPU_H

@@ -135,7 +135,7 @@ def test_adjoint_rejects_other_joint_kinds(gpu_lib):
 def _gear_coordinates(g, w, base):
     """Each gear's coordinate1 + ratio * coordinate2 (revolute: the angle of B
     against A less the reference angle; prismatic: the translation along the
-    axis) from the GPU's bodies, as GearJointConf.cpp:66-160 defines it."""
+    axis) from the GPU's bodies, as GetGearJointConf (GearJointConf.cpp:92-170) defines it."""
     b = g.bodies()
     out = []
     for j in np.flatnonzero(np.asarray(w.joint_type) == scenes.JOINT_GEAR):
