@@ -47,7 +47,7 @@
 extern "C" {
 #endif
 
-#define PRGPU_ABI_VERSION 3
+#define PRGPU_ABI_VERSION 4
 
 enum prgpu_status {
     PRGPU_OK = 0,
@@ -144,6 +144,13 @@ typedef struct prgpu_batch_desc {
                                            dynamic body (SetMassData, Body.cpp); NULL: from the shapes */
     const int32_t* joint_type;          /* [n_joints] PRGPU_JOINT_*; NULL: every joint is revolute */
     const float* joint_extra;           /* [n_joints*8] parameters of the other kinds (below) */
+    const int32_t* shape_owner;         /* [n_shapes] optional (ABI 4): for a child of a multi-child shape
+                                           (ChainShapeConf: its edges; MultiShapeConf: its convex hulls),
+                                           the index of the shape's first child, else -1.  The children
+                                           of one shape are consecutive, on one body, each a shape of the
+                                           batch with its own proxy (child order = proxy order); the mass
+                                           data counts them as the one shape (ChainShapeConf.cpp:113-147,
+                                           MultiShapeConf.cpp:35-57).  NULL: every shape has one child. */
 } prgpu_batch_desc;
 
 /* Joint kinds and their joint_extra parameters (the reference's JointConf types;

@@ -76,6 +76,7 @@ def _lib(double: bool):
                                  real, real, real, real, ctypes.c_uint, ctypes.c_uint, ctypes.c_int, ctypes.c_int]
     lib.or_add_shape.restype = ctypes.c_int
     lib.or_reset_mass.argtypes = [P, ctypes.c_int]
+    lib.or_set_shape_owner.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.or_add_revolute.argtypes = [P, ctypes.c_int, ctypes.c_int] + [real] * 5 + [
         ctypes.c_int, real, real, ctypes.c_int, real, real, ctypes.c_int]
     lib.or_add_revolute.restype = ctypes.c_int
@@ -144,11 +145,15 @@ class OracleWorld:
             xy = np.ascontiguousarray(scene.verts[vo:vo + nv].reshape(-1), dtype=self.np_real)
             f = scene.shape_filter[s]
             b = int(scene.shape_body[s])
-            lib.or_add_shape(h, b, int(scene.shape_kind[s]), nv, xy.ctypes.data,
-                             float(scene.shape_radius[s]), float(scene.shape_density[s]),
-                             float(scene.shape_friction[s]), float(scene.shape_restitution[s]),
-                             int(f[0]), int(f[1]), int(f[2]), int(f[3]))
-            lib.or_reset_mass(h, b)  # Attach(world, body, shape, resetMassData = true)
+            sid = lib.or_add_shape(h, b, int(scene.shape_kind[s]), nv, xy.ctypes.data,
+                                   float(scene.shape_radius[s]), float(scene.shape_density[s]),
+                                   float(scene.shape_friction[s]), float(scene.shape_restitution[s]),
+                                   int(f[0]), int(f[1]), int(f[2]), int(f[3]))
+            own = int(scene.shape_owner[s])
+            if own >= 0:  # a child of a chain (edges) or multi shape (hulls)
+                lib.or_set_shape_owner(h, sid, own, 1 if int(scene.shape_kind[own]) == 2 else 2)
+            if own < 0 or s + 1 == scene.n_shapes or int(scene.shape_owner[s + 1]) != own:
+                lib.or_reset_mass(h, b)  # Attach(world, body, shape, resetMassData = true)
         for j in range(scene.n_joints):
             a, b = scene.joint_bodies[j]
             an, pr, fl = scene.joint_anchors[j], scene.joint_params[j], scene.joint_flags[j]

@@ -182,6 +182,10 @@ typedef struct {
     real density, friction, restitution;
     unsigned cat, mask;
     int group, sensor;
+    /* a child of a multi-child shape (ChainShapeConf: edges, MultiShapeConf: convex
+     * hulls): the index of the shape's first child and the kind (1 chain, 2 multi);
+     * owner -1 for a shape of one child */
+    int owner, okind;
 } shape_t;
 
 typedef struct {
@@ -406,6 +410,7 @@ int or_add_shape(or_world* w, int body, int kind, int nverts, const real* xy, re
     make_normals(&s->dp);
     s->density = density; s->friction = friction; s->restitution = restitution;
     s->cat = categoryBits; s->mask = maskBits; s->group = groupIndex; s->sensor = sensor;
+    s->owner = -1; s->okind = 0;
     const int sid = w->ns++;
     /* CreateBody / Attach queue the fixture for proxy creation in the next Step,
      * for an enabled body only (AabbTreeWorld.cpp:1040-1041, :1302). */
@@ -497,16 +502,61 @@ static void shape_mass(const shape_t* s, real* mass, v2* center, real* I) {
 
 /* ResetMassData -> ComputeMassData (WorldShape.cpp:160-176) -> SetMassData
  * (WorldBody.cpp:365-400). */
+void or_set_shape_owner(or_world* w, int shape, int owner, int kind) {
+    w->s[shape].owner = owner;
+    w->s[shape].okind = kind;
+}
+
+/* GetMassData of a multi-child shape from its children first..first+n-1:
+ * ChainShapeConf::GetMassData (ChainShapeConf.cpp:113-147: the segments' masses,
+ * inertias and mass-weighted centres summed, the centre divided by the summed
+ * segment areas) or GetMassData(MultiShapeConf) (MultiShapeConf.cpp:35-57: the
+ * hulls' masses, inertias and mass-weighted centres summed, the centre divided
+ * by the mass). */
+static void group_mass(const or_world* w, int first, int n, int kind, real* mass, v2* center, real* I) {
+    const real Pi = R(3.14159265358979323846264338327950288L);
+    real m = R(0), Iz = R(0), area = R(0);
+    v2 c = V(R(0), R(0));
+    for (int k = 0; k < n; ++k) {
+        const shape_t* s = &w->s[first + k];
+        real mk, ik;
+        v2 ck;
+        shape_mass(s, &mk, &ck, &ik);
+        m += mk;
+        Iz += ik;
+        if (kind == 1) {
+            c = vadd(c, vmul(ck, mk));
+            const v2 d = vsub(s->dp.v[1], s->dp.v[0]);
+            const real bl = RSQRT(mag2(d));
+            const real h = s->dp.r * R(2);
+            area += bl * h + (s->dp.r * s->dp.r) * Pi;
+        } else {
+            c = vadd(c, vmul(ck, mk));
+        }
+    }
+    if (kind == 1) c = vdiv(c, area);
+    else c = (m > R(0)) ? vdiv(c, m) : V(R(0), R(0));
+    *mass = m; *center = c; *I = Iz;
+}
+
 void or_reset_mass(or_world* w, int body) {
     body_t* b = &w->b[body];
     real mass = R(0), I = R(0);
     v2 wc = V(R(0), R(0));
     for (int k = 0; k < b->shapes.n; ++k) {
-        const shape_t* s = &w->s[b->shapes.a[k]];
+        const int sid = (int)b->shapes.a[k];
+        const shape_t* s = &w->s[sid];
+        if (s->owner >= 0 && s->owner != sid) continue;  /* a later child: counted with the first */
         if (s->density > R(0)) {
             real m, i;
             v2 c;
-            shape_mass(s, &m, &c, &i);
+            if (s->owner == sid) {
+                int n = 1;
+                while (k + n < b->shapes.n && w->s[b->shapes.a[k + n]].owner == sid) ++n;
+                group_mass(w, sid, n, s->okind, &m, &c, &i);
+            } else {
+                shape_mass(s, &m, &c, &i);
+            }
             mass += m;
             wc = vadd(wc, vmul(c, m));
             I += i;

@@ -87,6 +87,10 @@ int or_add_shape(or_world* w, int body, int kind, int nverts, const or_real* xy,
                  unsigned categoryBits, unsigned maskBits, int groupIndex, int sensor);
 /* ResetMassData (WorldBody.cpp:360-400). */
 void or_reset_mass(or_world* w, int body);
+/* Marks shape as a child of the multi-child shape whose first child is owner
+ * (kind 1: ChainShapeConf, its children edges; 2: MultiShapeConf, convex hulls);
+ * the children of one shape are added consecutively, before or_reset_mass. */
+void or_set_shape_owner(or_world* w, int shape, int owner, int kind);
 /* Revolute joint (RevoluteJointConf).  Returns JointID. */
 int or_add_revolute(or_world* w, int bodyA, int bodyB, or_real lax, or_real lay,
                     or_real lbx, or_real lby, or_real refAngle, int enableLimit,

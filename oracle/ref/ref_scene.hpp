@@ -18,6 +18,8 @@
 #include <playrho/d2/DiskShapeConf.hpp>
 #include <playrho/d2/EdgeShapeConf.hpp>
 #include <playrho/d2/PolygonShapeConf.hpp>
+#include <playrho/d2/ChainShapeConf.hpp>
+#include <playrho/d2/MultiShapeConf.hpp>
 #include <playrho/d2/RevoluteJointConf.hpp>
 #include <playrho/d2/DistanceJointConf.hpp>
 #include <playrho/d2/RopeJointConf.hpp>
@@ -147,6 +149,47 @@ inline bool ApplyRecord(World& world, StepConf& conf, const std::string& tag, st
         else {
             auto c = EdgeShapeConf{v.at(0), v.at(1)};
             c.UseVertexRadius(radius * 1_m);
+            c.UseDensity(density * 1_kgpm2).UseFriction(friction).UseRestitution(restitution);
+            c.UseFilter(filter).UseIsSensor(sensor != 0);
+            sid = CreateShape(world, c);
+        }
+        Attach(world, BodyID(static_cast<BodyID::underlying_type>(body)), sid, true);
+    }
+    else if (tag == "chain" || tag == "multi") {
+        // chain body nv radius density friction restitution cat mask group sensor x0 y0 ...
+        // multi body nhulls radius density friction restitution cat mask group sensor
+        //       (nv x0 y0 ...) per hull
+        int body = 0, n = 0;
+        in >> body >> n;
+        auto radius = rd(in);
+        const auto density = rd(in), friction = rd(in), restitution = rd(in);
+        const auto minRadius = GetVertexRadiusInterval(world).GetMin() / 1_m;
+        if (radius < minRadius) radius = static_cast<Real>(minRadius);
+        unsigned cat = 0, mask = 0; int group = 0, sensor = 0;
+        in >> cat >> mask >> group >> sensor;
+        auto filter = Filter{};
+        filter.categoryBits = static_cast<Filter::bits_type>(cat);
+        filter.maskBits = static_cast<Filter::bits_type>(mask);
+        filter.groupIndex = static_cast<Filter::index_type>(group);
+        ShapeID sid;
+        if (tag == "chain") {
+            std::vector<Length2> v;
+            for (int i = 0; i < n; ++i) { const auto x = rd(in); const auto y = rd(in); v.push_back(Length2{x * 1_m, y * 1_m}); }
+            auto c = ChainShapeConf{};
+            c.Set(v);
+            c.vertexRadius = radius * 1_m;
+            c.UseDensity(density * 1_kgpm2).UseFriction(friction).UseRestitution(restitution);
+            c.UseFilter(filter).UseIsSensor(sensor != 0);
+            sid = CreateShape(world, c);
+        }
+        else {
+            auto c = MultiShapeConf{};
+            for (int k = 0; k < n; ++k) {
+                int nv = 0; in >> nv;
+                auto vs = VertexSet{};
+                for (int i = 0; i < nv; ++i) { const auto x = rd(in); const auto y = rd(in); vs.add(Length2{x * 1_m, y * 1_m}); }
+                c.AddConvexHull(vs, radius * 1_m);
+            }
             c.UseDensity(density * 1_kgpm2).UseFriction(friction).UseRestitution(restitution);
             c.UseFilter(filter).UseIsSensor(sensor != 0);
             sid = CreateShape(world, c);

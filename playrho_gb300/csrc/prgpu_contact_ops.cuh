@@ -147,13 +147,17 @@ static __device__ __noinline__ bool sensor_touching(const DW& d, uint2 pr, uint2
 
 // AabbTreeWorld::Update (AabbTreeWorld.cpp:2587-2721) without listeners.
 // src2 (optional): where the new manifold's points took their impulses from.
+// kSensors false: the caller passes no sensor contact, and the GJK of the
+// sensor test stays out of its kernel (its registers would cost the bulk
+// update pass its occupancy).
+template <bool kSensors = true>
 static __device__ void update_contact(const DW& d, uint32_t slot, int8_t* src2 = nullptr) {
     const uint2 pr = d.cs_proxy[slot];
     const uint2 bd = d.cs_body[slot];
     uint32_t flags = d.cs_flags[slot];
     bool touching = false;
     int src[2] = {-1, -1};
-    if (flags & CF_SENSOR) {
+    if (kSensors && (flags & CF_SENSOR)) {
         touching = sensor_touching(d, pr, bd);  // sensors make no manifold (:2634)
         store_manifold(d, slot, man_empty());
     } else {

@@ -87,10 +87,26 @@ __global__ void k_update_contacts(DW d, uint32_t body_mask) {
     GRID_LOOP(i, d.cnt->n_live) {
         const uint32_t slot = d.c_slot[i];
         const uint2 bd = d.cs_body[slot];
-        const bool need = (d.cs_flags[slot] & CF_NEEDS_UPDATE) || (d.b_flags[bd.x] & body_mask) ||
-                          (d.b_flags[bd.y] & body_mask);
-        if (need) {
-            update_contact(d, slot, rec ? rec + 2 * (size_t)slot : nullptr);
+        const uint32_t f = d.cs_flags[slot];
+        const bool need = (f & CF_NEEDS_UPDATE) || (d.b_flags[bd.x] & body_mask) || (d.b_flags[bd.y] & body_mask);
+        if (need && !(f & CF_SENSOR)) {
+            update_contact<false>(d, slot, rec ? rec + 2 * (size_t)slot : nullptr);
+            ++updated;
+        }
+    }
+    if (updated) atomicAdd(&d.cnt->st_contacts_updated, updated);
+}
+
+// The sensor contacts of the same pass (TestOverlap instead of CollideShapes).
+__global__ void k_update_sensors(DW d, uint32_t body_mask) {
+    uint32_t updated = 0;
+    GRID_LOOP(i, d.cnt->n_live) {
+        const uint32_t slot = d.c_slot[i];
+        const uint32_t f = d.cs_flags[slot];
+        if (!(f & CF_SENSOR)) continue;
+        const uint2 bd = d.cs_body[slot];
+        if ((f & CF_NEEDS_UPDATE) || (d.b_flags[bd.x] & body_mask) || (d.b_flags[bd.y] & body_mask)) {
+            update_contact<true>(d, slot);
             ++updated;
         }
     }
@@ -539,6 +555,7 @@ void launch_set_upd_phase(const DW& d, uint32_t phase, cudaStream_t s) { k_set_u
 
 void launch_update_contacts(const DW& d, const Launch& L, uint32_t body_mask, cudaStream_t s) {
     k_update_contacts<<<L.grid, L.threads, 0, s>>>(d, body_mask);
+    k_update_sensors<<<L.grid, L.threads, 0, s>>>(d, body_mask);
 }
 
 void launch_find_contacts(const DW& d, const Launch& L, cudaStream_t s) {

@@ -208,16 +208,56 @@ void host_set_pos(HostBody& b, float px, float py, float a) {
     b.xpx = p.x; b.xpy = p.y; b.xc = c; b.xs = s;
 }
 
+// GetMassData of a multi-child shape from its consecutive children
+// shapes[k0 .. k0+n-1]: ChainShapeConf (edges; ChainShapeConf.cpp:113-147: summed
+// masses, inertias and mass-weighted centres, the centre divided by the summed
+// segment areas) or MultiShapeConf (hulls; MultiShapeConf.cpp:35-57: the centre
+// divided by the mass).
+void group_mass(const std::vector<int>& shapes, size_t k0, size_t n, bool chain, const prgpu_batch_desc* ds,
+                const std::vector<std::vector<HV>>& sv, float& mass, HV& center, float& I) {
+    const float Pi = 3.14159265358979323846f;
+    float m = 0.f, iz = 0.f, area = 0.f;
+    HV c = hv(0.f, 0.f);
+    for (size_t k = k0; k < k0 + n; ++k) {
+        const int s = shapes[k];
+        float mk, ik;
+        HV ck;
+        shape_mass((int)sv[s].size(), sv[s].data(), ds->shape_radius[s], ds->shape_density[s], mk, ck, ik);
+        m += mk;
+        iz += ik;
+        c = c + hmul(ck, mk);
+        if (chain) {
+            const HV d = sv[s][1] - sv[s][0];
+            const float bl = std::sqrt(hmag2(d));
+            const float r = ds->shape_radius[s];
+            const float h = r * 2.0f;
+            area += bl * h + (r * r) * Pi;
+        }
+    }
+    if (chain) c = hdiv(c, area);
+    else c = (m > 0.f) ? hdiv(c, m) : hv(0.f, 0.f);
+    mass = m; center = c; I = iz;
+}
+
 // ResetMassData -> ComputeMassData -> SetMassData over the shapes attached so far.
 void reset_mass(HostBody& b, const std::vector<int>& shapes, const prgpu_batch_desc* ds,
                 const std::vector<std::vector<HV>>& sv) {
     float mass = 0.f, I = 0.f;
     HV wc = hv(0.f, 0.f);
-    for (int s : shapes) {
+    for (size_t k = 0; k < shapes.size(); ++k) {
+        const int s = shapes[k];
+        const int own = ds->shape_owner ? ds->shape_owner[s] : -1;
+        if (own >= 0 && own != s) continue;  // a later child: counted with the first
         if (ds->shape_density[s] > 0.f) {
             float m, i;
             HV c;
-            shape_mass((int)sv[s].size(), sv[s].data(), ds->shape_radius[s], ds->shape_density[s], m, c, i);
+            if (own == s) {
+                size_t n = 1;
+                while (k + n < shapes.size() && ds->shape_owner[shapes[k + n]] == s) ++n;
+                group_mass(shapes, k, n, ds->shape_kind[s] == PRGPU_EDGE, ds, sv, m, c, i);
+            } else {
+                shape_mass((int)sv[s].size(), sv[s].data(), ds->shape_radius[s], ds->shape_density[s], m, c, i);
+            }
             mass += m;
             wc = wc + hmul(c, m);
             I += i;
@@ -325,7 +365,18 @@ int prepare_host(const prgpu_batch_desc* ds, HostPrep& hp) {
     for (uint32_t s = 0; s < S; ++s) {
         const uint32_t b = ds->shape_body[s];
         body_shapes[b].push_back((int)s);
-        reset_mass(hb[b], body_shapes[b], ds, sv);
+        // Attach(..., resetMassData = true) once per shape of the reference: after
+        // the last child of a multi-child shape
+        const int own = ds->shape_owner ? ds->shape_owner[s] : -1;
+        if (own >= 0) {
+            const bool first = own == (int)s;
+            if (own > (int)s || ds->shape_body[own] != b || ds->shape_owner[own] != own ||
+                (!first && ds->shape_owner[s - 1] != own) || ds->shape_kind[s] != ds->shape_kind[own] ||
+                (ds->shape_kind[s] == PRGPU_DISK))
+                return PRGPU_EINVAL;
+        }
+        const bool last = own < 0 || s + 1 == S || ds->shape_owner[s + 1] != own;
+        if (last) reset_mass(hb[b], body_shapes[b], ds, sv);
     }
     if (ds->body_mass) {
         // SetMassData (Body.cpp): the transformation stays, the centre moves to

@@ -67,7 +67,7 @@ class BatchDesc(ctypes.Structure):
         ("shape_restitution", P), ("shape_filter", P), ("n_verts", ctypes.c_uint32), ("verts", P),
         ("n_joints", ctypes.c_uint32), ("joint_bodies", P), ("joint_anchors", P), ("joint_params", P),
         ("joint_flags", P), ("contact_capacity", ctypes.c_uint32), ("candidate_capacity", ctypes.c_uint32),
-        ("body_mass", P), ("joint_type", P), ("joint_extra", P)]
+        ("body_mass", P), ("joint_type", P), ("joint_extra", P), ("shape_owner", P)]
 
 
 class Schedule(ctypes.Structure):
@@ -257,6 +257,11 @@ def flatten(scenes: Sequence[Scene]) -> dict:
         "joint_flags": cat(lambda s: s.joint_flags.reshape(-1, 3), np.int32),
         "joint_type": cat(lambda s: s.joint_type.reshape(-1), np.int32),
         "joint_extra": _gear_offsets(scenes, cat(lambda s: s.joint_extra.reshape(-1, 8), np.float32)),
+        # first child of a multi-child shape as a global shape index (-1 stays -1)
+        "shape_owner": np.ascontiguousarray(np.concatenate(
+            [np.where(s.shape_owner >= 0, s.shape_owner + shape_base_i, -1)
+             for s, shape_base_i in zip(scenes, np.cumsum([0] + [x.n_shapes for x in scenes])[:-1])]
+        ).astype(np.int32)),
         "body_base": body_base,
     }
     return out
@@ -274,7 +279,7 @@ def batch_desc(scenes: Sequence[Scene], contact_capacity: int = 0, candidate_cap
     for k in ("body_type", "body_pos", "body_vel", "body_acc", "body_damp", "body_flags", "shape_body",
               "shape_kind", "shape_voff", "shape_nv", "shape_radius", "shape_density", "shape_friction",
               "shape_restitution", "shape_filter", "verts", "joint_bodies", "joint_anchors",
-              "joint_params", "joint_flags", "joint_type", "joint_extra"):
+              "joint_params", "joint_flags", "joint_type", "joint_extra", "shape_owner"):
         setattr(d, k, _ptr(f[k]))
     d.n_shapes = int(f["shape_body"].size)
     d.n_verts = int(f["verts"].shape[0])
@@ -314,7 +319,7 @@ class GpuBatch:
         for k in ("body_type", "body_pos", "body_vel", "body_acc", "body_damp", "body_flags", "shape_body",
                   "shape_kind", "shape_voff", "shape_nv", "shape_radius", "shape_density", "shape_friction",
                   "shape_restitution", "shape_filter", "verts", "joint_bodies", "joint_anchors",
-                  "joint_params", "joint_flags", "joint_type", "joint_extra"):
+                  "joint_params", "joint_flags", "joint_type", "joint_extra", "shape_owner"):
             setattr(d, k, _ptr(f[k]))
         d.n_shapes = int(f["shape_body"].size)
         d.n_verts = int(f["verts"].shape[0])

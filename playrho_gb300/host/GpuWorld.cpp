@@ -13,6 +13,8 @@
 #include "playrho/d2/DiskShapeConf.hpp"
 #include "playrho/d2/EdgeShapeConf.hpp"
 #include "playrho/d2/PolygonShapeConf.hpp"
+#include "playrho/d2/ChainShapeConf.hpp"
+#include "playrho/d2/MultiShapeConf.hpp"
 #include "playrho/d2/DistanceJointConf.hpp"
 #include "playrho/d2/FrictionJointConf.hpp"
 #include "playrho/d2/GearJointConf.hpp"
@@ -130,8 +132,30 @@ prgpu::HostShape ToHost(const Shape& shape) {
         h.radius = F(StripUnit(c->vertexRadius));
         h.verts = {F(StripUnit(GetX(c->GetVertexA()))), F(StripUnit(GetY(c->GetVertexA()))),
                    F(StripUnit(GetX(c->GetVertexB()))), F(StripUnit(GetY(c->GetVertexB())))};
+    } else if (TypeCast<ChainShapeConf>(&shape) || TypeCast<MultiShapeConf>(&shape)) {
+        // each child (an edge of a chain, a convex hull of a multi shape) becomes a
+        // shape of the batch with its own proxy, as the reference gives each child one
+        const bool chain = TypeCast<ChainShapeConf>(&shape) != nullptr;
+        if (chain) base(*TypeCast<ChainShapeConf>(&shape));
+        else base(*TypeCast<MultiShapeConf>(&shape));
+        h.kind = chain ? PRGPU_EDGE : PRGPU_POLYGON;
+        const auto n = GetChildCount(shape);
+        if (n == 0) throw InvalidArgument("GpuWorld: a shape without children");
+        for (ChildCounter i = 0; i < n; ++i) {
+            const auto child = GetChild(shape, i);
+            const auto nv = child.GetVertexCount();
+            if ((chain && nv != 2) || (!chain && nv < 3))
+                throw InvalidArgument("GpuWorld: chain children must be edges, multi-shape children polygons");
+            h.radius = F(StripUnit(child.GetVertexRadius()));
+            std::vector<float> v;
+            for (auto k = decltype(nv){0}; k < nv; ++k) {
+                v.push_back(F(StripUnit(GetX(child.GetVertex(k)))));
+                v.push_back(F(StripUnit(GetY(child.GetVertex(k)))));
+            }
+            h.children.push_back(std::move(v));
+        }
     } else {
-        throw InvalidArgument("GpuWorld: only disk, polygon and edge shapes are stepped on the GPU");
+        throw InvalidArgument("GpuWorld: only disk, polygon, edge, chain and multi shapes are stepped on the GPU");
     }
     return h;
 }
@@ -308,8 +332,8 @@ void GpuWorld::Refresh() const {
     keyedContacts.clear(); contacts.clear(); manifolds.clear(); contactSeq.clear(); contactIndex.clear();
     for (size_t k = 0; k < hc.size(); ++k) {
         const auto& c = hc[k];
-        Contact ct{Contactable{BodyID(c.body_a), ShapeID(c.shape_a), 0u},
-                   Contactable{BodyID(c.body_b), ShapeID(c.shape_b), 0u}};
+        Contact ct{Contactable{BodyID(c.body_a), ShapeID(c.shape_a), ChildCounter(c.child_a)},
+                   Contactable{BodyID(c.body_b), ShapeID(c.shape_b), ChildCounter(c.child_b)}};
         ct.SetFriction(Real(c.friction));
         ct.SetRestitution(Real(c.restitution));
         ct.SetTangentSpeed(Real(c.tangent_speed) * MeterPerSecond);
@@ -566,10 +590,10 @@ const DynamicTree& GetTree(const GpuWorld& w) noexcept {
         } catch (...) {
             aabb.clear(); bs.clear();
         }
-        for (size_t k = 0; k < bs.size() / 2; ++k) {
+        for (size_t k = 0; k < bs.size() / 3; ++k) {
             const AABB box{LengthInterval{Real(aabb[4 * k]) * Meter, Real(aabb[4 * k + 2]) * Meter},
                            LengthInterval{Real(aabb[4 * k + 1]) * Meter, Real(aabb[4 * k + 3]) * Meter}};
-            w.tree.CreateLeaf(box, Contactable{BodyID(bs[2 * k]), ShapeID(bs[2 * k + 1]), 0u});
+            w.tree.CreateLeaf(box, Contactable{BodyID(bs[3 * k]), ShapeID(bs[3 * k + 1]), ChildCounter(bs[3 * k + 2])});
         }
         w.treeValid = true;
     }

@@ -14,9 +14,10 @@
 // -- works unchanged, so a program switches by changing the constructor call.
 //
 // What the GPU world does differently, by design of this path:
-//  * disk, polygon and edge shapes (chain and multi shapes throw
-//    InvalidArgument); StepConf::doToi runs the time-of-impact phase, but
-//    sub-stepping (one event per Step) is not offered;
+//  * disk, polygon, edge, chain and multi shapes; a chain's edges and a multi
+//    shape's hulls are shapes of the GPU batch, one proxy per child as in the
+//    reference; StepConf::doToi runs the time-of-impact phase, but sub-stepping
+//    (one event per Step) is not offered;
 //  * Gauss-Seidel sweeps visit contacts in colour order, not island order;
 //  * contact IDs are the GPU's contact slots: stable for a contact's life and
 //    reused after it is destroyed, as the reference's pools reuse them;

@@ -211,25 +211,34 @@ void HostWorld::Build() {
         any_mass = any_mass || (b.explicit_mass && b.type == PRGPU_DYNAMIC);
     }
     // proxies: every (body, attached shape), bodies in ID order, shapes in attach order
-    proxy_body_.clear(); proxy_shape_.clear();
+    proxy_body_.clear(); proxy_shape_.clear(); proxy_child_.clear();
     std::vector<uint32_t> s_body, s_voff, s_nv;
-    std::vector<int32_t> s_kind, s_filter;
+    std::vector<int32_t> s_kind, s_filter, s_owner;
+    bool any_children = false;
     std::vector<float> s_radius, s_density, s_friction, s_restitution, verts;
     for (uint32_t i = 0; i < N; ++i) {
         for (uint32_t sid : bodies_[gpu_body_[i]].shapes) {
             const HostShape& s = shapes_[sid];
-            proxy_body_.push_back(gpu_body_[i]);
-            proxy_shape_.push_back(sid);
-            s_body.push_back(i);
-            s_kind.push_back(s.kind);
-            s_voff.push_back((uint32_t)(verts.size() / 2));
-            s_nv.push_back((uint32_t)(s.verts.size() / 2));
-            verts.insert(verts.end(), s.verts.begin(), s.verts.end());
-            s_radius.push_back(s.radius);
-            s_density.push_back(s.density);
-            s_friction.push_back(s.friction);
-            s_restitution.push_back(s.restitution);
-            s_filter.insert(s_filter.end(), {s.category, s.mask, s.group, s.sensor});
+            const size_t nc = s.children.empty() ? 1 : s.children.size();
+            const int32_t first = (int32_t)s_body.size();
+            any_children = any_children || !s.children.empty();
+            for (size_t c = 0; c < nc; ++c) {
+                const std::vector<float>& v = s.children.empty() ? s.verts : s.children[c];
+                proxy_body_.push_back(gpu_body_[i]);
+                proxy_shape_.push_back(sid);
+                proxy_child_.push_back((uint32_t)c);
+                s_body.push_back(i);
+                s_kind.push_back(s.kind);
+                s_owner.push_back(s.children.empty() ? -1 : first);
+                s_voff.push_back((uint32_t)(verts.size() / 2));
+                s_nv.push_back((uint32_t)(v.size() / 2));
+                verts.insert(verts.end(), v.begin(), v.end());
+                s_radius.push_back(s.radius);
+                s_density.push_back(s.density);
+                s_friction.push_back(s.friction);
+                s_restitution.push_back(s.restitution);
+                s_filter.insert(s_filter.end(), {s.category, s.mask, s.group, s.sensor});
+            }
         }
     }
     const uint32_t S = (uint32_t)s_body.size();
@@ -269,6 +278,7 @@ void HostWorld::Build() {
     d.n_verts = (uint32_t)(verts.size() / 2); d.verts = verts.data();
     d.n_joints = J; d.joint_bodies = j_bodies.data(); d.joint_anchors = j_anchor.data(); d.joint_params = j_param.data();
     d.joint_flags = j_flags.data(); d.joint_type = j_type.data(); d.joint_extra = j_extra.data();
+    d.shape_owner = any_children ? s_owner.data() : nullptr;
     std::vector<float> mass4;
     if (any_mass) {
         // mass data from the shapes, then the bodies that set their own
@@ -373,8 +383,9 @@ const std::vector<HostContact>& HostWorld::Contacts() {
         c.friction = mat[4 * k]; c.restitution = mat[4 * k + 1]; c.tangent_speed = mat[4 * k + 2];
         c.enabled = mat[4 * k + 3] != 0.f;
         c.proxy_a = leaf_id(pr[2 * k]); c.proxy_b = leaf_id(pr[2 * k + 1]);
-        c.body_a = proxy_body_[pr[2 * k]]; c.shape_a = proxy_shape_[pr[2 * k]];
+        c.body_a = proxy_body_[pr[2 * k]]; c.shape_a = proxy_shape_[pr[2 * k]]; c.child_a = proxy_child_[pr[2 * k]];
         c.body_b = proxy_body_[pr[2 * k + 1]]; c.shape_b = proxy_shape_[pr[2 * k + 1]];
+        c.child_b = proxy_child_[pr[2 * k + 1]];
         c.touching = (fl[k] & 1u) != 0u; c.sensor = (fl[k] & 2u) != 0u;
         c.type = meta[2 * k]; c.count = meta[2 * k + 1];
         c.local_normal[0] = head[4 * k]; c.local_normal[1] = head[4 * k + 1];
@@ -434,13 +445,20 @@ void HostWorld::SetManifold(uint32_t slot, int32_t type, int32_t count, const fl
     contacts_valid_ = false;
 }
 
-void HostWorld::Proxies(std::vector<float>& aabb4, std::vector<uint32_t>& body_shape2) {
+void HostWorld::Proxies(std::vector<float>& aabb4, std::vector<uint32_t>& body_shape_child3) {
     aabb4.clear();
-    body_shape2.clear();
+    body_shape_child3.clear();
     if (!gpu_) return;
     aabb4.resize(4 * proxy_body_.size());
     Check(prgpu_download_proxies(gpu_, aabb4.data()), "prgpu_download_proxies");
-    for (size_t k = 0; k < proxy_body_.size(); ++k) body_shape2.insert(body_shape2.end(), {proxy_body_[k], proxy_shape_[k]});
+    for (size_t k = 0; k < proxy_body_.size(); ++k)
+        body_shape_child3.insert(body_shape_child3.end(), {proxy_body_[k], proxy_shape_[k], proxy_child_[k]});
+}
+
+uint32_t HostWorld::ProxyOf(uint32_t shape, uint32_t child) const {
+    for (size_t k = 0; k < proxy_shape_.size(); ++k)
+        if (proxy_shape_[k] == shape && proxy_child_[k] == child) return (uint32_t)k;
+    return ~0u;
 }
 
 }  // namespace prgpu

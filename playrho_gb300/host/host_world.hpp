@@ -50,6 +50,10 @@ struct HostBody {
 struct HostShape {
     int32_t kind = PRGPU_DISK;
     std::vector<float> verts;  // x0 y0 x1 y1 ...
+    // a shape of several children (ChainShapeConf: edges, MultiShapeConf: convex
+    // hulls): each child's vertices, kind then being the children's kind; each
+    // child becomes a shape of the batch with its own proxy (prgpu_batch_desc::shape_owner)
+    std::vector<std::vector<float>> children;
     float radius = 0.f, density = 0.f, friction = 0.2f, restitution = 0.f;
     int32_t category = 1, mask = 0xffff, group = 0, sensor = 0;
 };
@@ -70,6 +74,7 @@ struct HostContact {
     uint32_t slot = 0;                                           // ContactID: stable for the contact's life
     uint64_t seq = 0;                                            // creation number (contact-list order)
     uint32_t body_a = 0, body_b = 0, shape_a = 0, shape_b = 0;  // IDs of the host pools
+    uint32_t child_a = 0, child_b = 0;                           // child indices of the shapes
     uint32_t proxy_a = 0, proxy_b = 0;                           // tree leaf IDs (ContactKey)
     bool touching = false, sensor = false;
     int32_t type = 0, count = 0;                                 // Manifold::Type, point count
@@ -141,8 +146,10 @@ public:
     void SetSolveRecords(bool enabled);
     // The live contacts the last step updated or solved.
     std::vector<HostSolveRecord> SolveRecords();
-    // Fat AABB (minx miny maxx maxy) and (body, shape) of every proxy, by leaf ID order.
-    void Proxies(std::vector<float>& aabb4, std::vector<uint32_t>& body_shape2);
+    // Fat AABB (minx miny maxx maxy) and (body, shape, child) of every proxy, by leaf ID order.
+    void Proxies(std::vector<float>& aabb4, std::vector<uint32_t>& body_shape_child3);
+    // The GPU shape (proxy) index of a shape's child, or ~0u (after a step).
+    uint32_t ProxyOf(uint32_t shape, uint32_t child) const;
     void Clear();
     bool HasGpuBatch() const { return gpu_ != nullptr; }
     // The next Step rebuilds the GPU batch (entities changed since the last one).
@@ -166,7 +173,7 @@ private:
     bool rebuild_ = true;
     std::vector<uint32_t> gpu_body_;          // GPU body index -> body ID
     std::vector<uint32_t> body_gpu_;          // body ID -> GPU body index (or ~0)
-    std::vector<uint32_t> proxy_body_, proxy_shape_;  // GPU shape (proxy) index -> IDs
+    std::vector<uint32_t> proxy_body_, proxy_shape_, proxy_child_;  // GPU shape (proxy) index -> IDs
     std::vector<float> lc_;                   // local centre per GPU body (x y)
     std::vector<bool> state_dirty_;           // body ID -> position/velocity set since the last step
     bool contacts_valid_ = false;

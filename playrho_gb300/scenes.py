@@ -85,6 +85,9 @@ class Scene:
     # joint kind (JOINT_*) and the other kinds' parameters (layouts at JOINT_PARAMS)
     joint_type: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))
     joint_extra: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 8), np.float32))
+    # multi-child shapes (ChainShapeConf, MultiShapeConf): each child is a shape here,
+    # with the index of its shape's first child; -1 for a shape of one child
+    shape_owner: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))
 
     def __post_init__(self):
         nj = int(np.asarray(self.joint_bodies).reshape(-1, 2).shape[0])
@@ -92,6 +95,9 @@ class Scene:
             self.joint_type = np.zeros(nj, np.int32)
         if len(self.joint_extra) != nj:
             self.joint_extra = np.zeros((nj, 8), np.float32)
+        ns = int(np.asarray(self.shape_body).shape[0])
+        if len(self.shape_owner) != ns:
+            self.shape_owner = np.full(ns, -1, np.int32)
 
     @property
     def n_bodies(self) -> int:
@@ -135,6 +141,7 @@ class SceneBuilder:
         self.j_flags: List[tuple] = []
         self.j_type: List[int] = []
         self.j_extra: List[tuple] = []
+        self.s_owner: List[int] = []
 
     @classmethod
     def from_scene(cls, sc: "Scene") -> "SceneBuilder":
@@ -149,6 +156,7 @@ class SceneBuilder:
             sb._shape(int(sc.shape_body[k]), int(sc.shape_kind[k]), [tuple(v) for v in sc.verts[o:o + n]],
                       float(sc.shape_radius[k]), float(sc.shape_density[k]), float(sc.shape_friction[k]),
                       float(sc.shape_restitution[k]), tuple(int(v) for v in sc.shape_filter[k]))
+            sb.s_owner[k] = int(sc.shape_owner[k])
         for j in range(sc.n_joints):
             sb.j_bodies.append(tuple(int(v) for v in sc.joint_bodies[j]))
             sb.j_anchor.append(tuple(float(v) for v in sc.joint_anchors[j]))
@@ -179,6 +187,7 @@ class SceneBuilder:
         self.s_friction.append(friction)
         self.s_rest.append(restitution)
         self.s_filter.append(filt)
+        self.s_owner.append(-1)
         return len(self.s_body) - 1
 
     def disk(self, body, radius, loc=(0.0, 0.0), density=0.0, friction=0.2, restitution=0.0,
@@ -198,6 +207,28 @@ class SceneBuilder:
     def edge(self, body, v0, v1, vertex_radius=float(DEFAULT_VERTEX_RADIUS), density=0.0,
              friction=0.2, restitution=0.0, filt=(1, 0xFFFF, 0, 0)):
         return self._shape(body, EDGE, [v0, v1], vertex_radius, density, friction, restitution, filt)
+
+    def chain(self, body, points, vertex_radius=float(DEFAULT_VERTEX_RADIUS), density=0.0, friction=0.2,
+              restitution=0.0, filt=(1, 0xFFFF, 0, 0)) -> int:
+        """ChainShapeConf over `points` (a loop repeats the first point at the end):
+        one edge child per segment, each its own proxy; returns the first child."""
+        first = None
+        for a, b in zip(points[:-1], points[1:]):
+            k = self._shape(body, EDGE, [a, b], vertex_radius, density, friction, restitution, filt)
+            first = k if first is None else first
+            self.s_owner[k] = first
+        return first
+
+    def multi(self, body, hulls, vertex_radius=float(DEFAULT_VERTEX_RADIUS), density=0.0, friction=0.2,
+              restitution=0.0, filt=(1, 0xFFFF, 0, 0)) -> int:
+        """MultiShapeConf with one convex hull child per point set in `hulls`
+        (MultiShapeConf::AddConvexHull); returns the first child."""
+        first = None
+        for pts in hulls:
+            k = self._shape(body, POLYGON, convex_hull(pts), vertex_radius, density, friction, restitution, filt)
+            first = k if first is None else first
+            self.s_owner[k] = first
+        return first
 
     def revolute(self, a, b, anchor_a, anchor_b, ref_angle=0.0, limit=None, motor=None,
                  collide_connected=False):
@@ -258,7 +289,8 @@ class SceneBuilder:
             shape_restitution=f(self.s_rest, 0), shape_filter=i(self.s_filter, 4),
             verts=f(self.verts, 2), joint_bodies=i(self.j_bodies, 2), joint_anchors=f(self.j_anchor, 4),
             joint_params=f(self.j_params, 6), joint_flags=i(self.j_flags, 3),
-            joint_type=np.asarray(self.j_type, np.int32), joint_extra=f(self.j_extra, 8))
+            joint_type=np.asarray(self.j_type, np.int32), joint_extra=f(self.j_extra, 8),
+            shape_owner=np.asarray(self.s_owner, np.int32))
 
 
 def convex_hull(points) -> list:
@@ -669,6 +701,35 @@ def joint_zoo(rng, per_kind: int = 4, kinds=None, n_disks: int = 12, gravity: bo
     return sb.build()
 
 
+def multi_child_scene(rng, n_multi: int = 24, n_disks: int = 24) -> Scene:
+    """Multi-child shapes: a static ChainShapeConf terrain (hills of 40 segments,
+    each segment an edge child with its own proxy) and dynamic bodies each carrying
+    one MultiShapeConf of two or three convex hulls (an L, a T, a dumbbell), with
+    disks, dropped onto it."""
+    sb = SceneBuilder()
+    g = sb.body(STATIC, 0.0, 0.0)
+    xs = np.linspace(-20.0, 20.0, 41)
+    ys = 1.5 * np.sin(xs * 0.35) + 0.4 * np.sin(xs * 1.3) + rng.uniform(-0.2, 0.2, xs.size)
+    sb.chain(g, [(float(x), float(y)) for x, y in zip(xs, ys)], friction=0.6)
+    sb.chain(g, [(-20.0, 12.0), (-20.0, ys[0]), ], friction=0.6)  # walls
+    sb.chain(g, [(20.0, ys[-1]), (20.0, 12.0)], friction=0.6)
+    shapes = [
+        [[(-0.6, -0.2), (0.6, -0.2), (0.6, 0.2), (-0.6, 0.2)], [(-0.6, 0.2), (-0.2, 0.2), (-0.2, 0.9), (-0.6, 0.9)]],
+        [[(-0.7, 0.3), (0.7, 0.3), (0.7, 0.6), (-0.7, 0.6)], [(-0.15, -0.6), (0.15, -0.6), (0.15, 0.3), (-0.15, 0.3)]],
+        [[(-0.8, -0.15), (0.8, -0.15), (0.8, 0.15), (-0.8, 0.15)], [(-1.0, -0.4), (-0.6, -0.4), (-0.6, 0.4), (-1.0, 0.4)],
+         [(0.6, -0.4), (1.0, -0.4), (1.0, 0.4), (0.6, 0.4)]],
+    ]
+    for k in range(n_multi):
+        b = sb.body(DYNAMIC, float(rng.uniform(-17.0, 17.0)), float(4.0 + 1.6 * k % 8 + rng.uniform(0.0, 0.4)),
+                    angle=float(rng.uniform(-math.pi, math.pi)), acc=GRAVITY)
+        sb.multi(b, shapes[k % 3], density=1.0, friction=0.5)
+    for k in range(n_disks):
+        b = sb.body(DYNAMIC, float(rng.uniform(-17.0, 17.0)), float(12.0 + 1.2 * k % 6 + rng.uniform(0.0, 0.4)),
+                    acc=GRAVITY)
+        sb.disk(b, float(rng.uniform(0.2, 0.45)), density=1.0, friction=0.4)
+    return sb.build()
+
+
 def sensor_scene(rng, n_bodies: int = 120) -> Scene:
     """A pile falling through sensors: static sensor zones (boxes and disks) across
     the fall, and every fifth falling body a sensor itself.  Sensors make no
@@ -826,14 +887,33 @@ def scene_text(scene: Scene, conf_overrides: dict | None = None) -> str:
         p, v, a, d = scene.body_pos[i], scene.body_vel[i], scene.body_acc[i], scene.body_damp[i]
         out.append("body %d %s %d" % (scene.body_type[i], " ".join(hx(x) for x in (*p, *v, *a, *d)),
                                        scene.body_flags[i]))
+    owner = scene.shape_owner
     for s in range(scene.n_shapes):
         vo, nv = scene.shape_voff[s], scene.shape_nv[s]
-        vs = " ".join(hx(x) for x in scene.verts[vo:vo + nv].reshape(-1))
         f = scene.shape_filter[s]
+        head = (hx(scene.shape_radius[s]), hx(scene.shape_density[s]), hx(scene.shape_friction[s]),
+                hx(scene.shape_restitution[s]))
+        if owner[s] >= 0:
+            if owner[s] != s:
+                continue  # written with its shape's first child
+            kids = [s]
+            while kids[-1] + 1 < scene.n_shapes and owner[kids[-1] + 1] == s:
+                kids.append(kids[-1] + 1)
+            if scene.shape_kind[s] == EDGE:  # chain: the children's vertices, shared ends once
+                pts = [scene.verts[scene.shape_voff[s]]] + [scene.verts[scene.shape_voff[k] + 1] for k in kids]
+                out.append("chain %d %d %s %s %s %s %d %d %d %d %s" % (
+                    scene.shape_body[s], len(pts), *head, f[0], f[1], f[2], f[3],
+                    " ".join(hx(x) for p in pts for x in p)))
+            else:  # multi: each hull's vertex count and vertices
+                hulls = " ".join("%d %s" % (scene.shape_nv[k], " ".join(
+                    hx(x) for x in scene.verts[scene.shape_voff[k]:scene.shape_voff[k] + scene.shape_nv[k]].reshape(-1)))
+                    for k in kids)
+                out.append("multi %d %d %s %s %s %s %d %d %d %d %s" % (
+                    scene.shape_body[s], len(kids), *head, f[0], f[1], f[2], f[3], hulls))
+            continue
+        vs = " ".join(hx(x) for x in scene.verts[vo:vo + nv].reshape(-1))
         out.append("shape %d %d %d %s %s %s %s %d %d %d %d %s" % (
-            scene.shape_body[s], scene.shape_kind[s], nv, hx(scene.shape_radius[s]),
-            hx(scene.shape_density[s]), hx(scene.shape_friction[s]), hx(scene.shape_restitution[s]),
-            f[0], f[1], f[2], f[3], vs))
+            scene.shape_body[s], scene.shape_kind[s], nv, *head, f[0], f[1], f[2], f[3], vs))
     for j in range(scene.n_joints):
         a, b = scene.joint_bodies[j]
         an = scene.joint_anchors[j]

@@ -17,6 +17,12 @@
 #include <optional>
 
 #include "playrho/d2/BasicAPI.hpp"
+#include "playrho/d2/ChainShapeConf.hpp"
+#include "playrho/d2/MultiShapeConf.hpp"
+
+#include <cmath>
+#include <utility>
+#include <vector>
 #include "playrho/d2/GearJointConf.hpp"
 #include "playrho/d2/PrismaticJointConf.hpp"
 #include "playrho/d2/PulleyJointConf.hpp"
@@ -179,6 +185,74 @@ void Conveyor(playrho::d2::World& world, const char* tag, bool doToi) {
     }
 }
 
+// Multi-child shapes: a ChainShapeConf terrain and two bodies of MultiShapeConf
+// hulls and a disk falling onto it.  Prints "<tag> tcontact <step> <shapeA> <childA>
+// <shapeB> <childB> <touching>" for every contact at a few steps (lower shape first),
+// "<tag> tpos <step> <body> x y angle" every 10 steps and "<tag> tmass <body> invMass
+// invRotInertia" once.
+void Terrain(playrho::d2::World& world, const char* tag) {
+    using namespace playrho;
+    using namespace playrho::d2;
+    auto chain = ChainShapeConf{};
+    std::vector<Length2> pts;
+    for (int i = 0; i <= 20; ++i) {
+        const auto x = Real(-10 + i);
+        pts.push_back(Length2{x * 1_m, Real(0.6) * Real(std::sin(double(x) * 0.7)) * 1_m});
+    }
+    chain.Set(pts);
+    chain.UseFriction(0.6f);
+    const auto ground = CreateShape(world, chain);
+    CreateBody(world, BodyConf{}.Use(ground));
+    auto hull = [](std::initializer_list<Length2> pts) {
+        auto vs = VertexSet{};
+        for (const auto& p : pts) vs.add(p);
+        return vs;
+    };
+    auto l = MultiShapeConf{};
+    l.AddConvexHull(hull({Length2{-0.6_m, -0.2_m}, Length2{0.6_m, -0.2_m}, Length2{0.6_m, 0.2_m},
+                          Length2{-0.6_m, 0.2_m}}));
+    l.AddConvexHull(hull({Length2{-0.6_m, 0.2_m}, Length2{-0.2_m, 0.2_m}, Length2{-0.2_m, 0.9_m},
+                          Length2{-0.6_m, 0.9_m}}));
+    l.UseDensity(1_kgpm2).UseFriction(0.5f);
+    const auto lshape = CreateShape(world, l);
+    std::vector<BodyID> bodies;
+    bodies.push_back(CreateBody(world, BodyConf{}.Use(BodyType::Dynamic).Use(lshape)
+                                           .UseLocation(Length2{-5_m, 3_m}).UseAngle(0.3_rad)
+                                           .UseLinearAcceleration(EarthlyGravity)));
+    bodies.push_back(CreateBody(world, BodyConf{}.Use(BodyType::Dynamic).Use(lshape)
+                                           .UseLocation(Length2{4_m, 2.5_m}).UseAngle(-1.1_rad)
+                                           .UseLinearAcceleration(EarthlyGravity)));
+    const auto disk = CreateShape(world, DiskShapeConf{}.UseRadius(0.35_m).UseDensity(1_kgpm2));
+    bodies.push_back(CreateBody(world, BodyConf{}.Use(BodyType::Dynamic).Use(disk)
+                                           .UseLocation(Length2{0.3_m, 2_m}).UseLinearAcceleration(EarthlyGravity)));
+    for (const auto& b : bodies)
+        std::printf("%s tmass %u %a %a\n", tag, unsigned(to_underlying(b)), double(StripUnit(GetInvMass(world, b))),
+                    double(StripUnit(GetInvRotInertia(world, b))));
+    auto conf = StepConf{};
+    conf.doToi = false;
+    for (auto step = 1; step <= 90; ++step) {
+        Step(world, conf);
+        if (step == 1 || step == 30 || step == 60 || step == 90) {
+            for (const auto& kc : GetContacts(world)) {
+                const auto& c = GetContact(world, std::get<ContactID>(kc));
+                auto a = std::make_pair(unsigned(to_underlying(GetShapeA(c))), unsigned(GetChildIndexA(c)));
+                auto b = std::make_pair(unsigned(to_underlying(GetShapeB(c))), unsigned(GetChildIndexB(c)));
+                if (b < a) std::swap(a, b);
+                std::printf("%s tcontact %d %u %u %u %u %d\n", tag, step, a.first, a.second, b.first, b.second,
+                            IsTouching(c) ? 1 : 0);
+            }
+        }
+        if (step % 10 == 0) {
+            for (const auto& b : bodies) {
+                const auto xf = GetTransformation(world, b);
+                std::printf("%s tpos %d %u %a %a %a\n", tag, step, unsigned(to_underlying(b)),
+                            double(StripUnit(GetX(xf.p))), double(StripUnit(GetY(xf.p))),
+                            double(StripUnit(GetAngle(xf.q))));
+            }
+        }
+    }
+}
+
 } // namespace
 
 int main() {
@@ -210,6 +284,8 @@ int main() {
         Conveyor(ref, "ref", true);
         auto ref2 = World{};
         Conveyor(ref2, "rnt", false);
+        auto ref3 = World{};
+        Terrain(ref3, "ref");
     }
     const auto conf = StepConf{};
     try {
@@ -225,6 +301,8 @@ int main() {
         Conveyor(gpu, "gpu", true);
         auto gpu2 = World{GpuWorld{}};
         Conveyor(gpu2, "gnt", false);
+        auto gpu3 = World{GpuWorld{}};
+        Terrain(gpu3, "gpu");
     } catch (const std::exception& e) {
         std::printf("error %s\n", e.what());
         return 3;

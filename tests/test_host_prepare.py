@@ -21,6 +21,9 @@ def _cases():
         "box": scenes.large_box(400, size=40.0, seed=0),
         "chains": scenes.chains_world(np.random.default_rng(3), n_free=30, n_chains=2, links=5),
         "push": scenes.push_worlds(1)[0],
+        # multi-child shapes: a chain terrain and bodies of MultiShapeConf hulls (one
+        # Attach each, mass data of the whole shape)
+        "multi": scenes.multi_child_scene(np.random.default_rng(5)),
     }
 
 
@@ -52,6 +55,16 @@ def test_invalid_descriptions_rejected(lib):
         gpu.prepare_bodies([bad])
 
 
+def test_multi_child_owner_rules(lib):
+    sc = scenes.multi_child_scene(np.random.default_rng(6))
+    bad = scenes.Scene(**{f: getattr(sc, f) for f in sc.__dataclass_fields__})
+    bad.shape_owner = bad.shape_owner.copy()
+    k = int(np.flatnonzero(bad.shape_owner >= 0)[3])
+    bad.shape_owner[k] = k + 5  # a child before its shape's first child
+    with pytest.raises(gpu.PrgpuError):
+        gpu.prepare_bodies([bad])
+
+
 def test_library_exports(lib):
     import os
     import re
@@ -60,7 +73,7 @@ def test_library_exports(lib):
     assert declared >= set(gpu.exported_symbols())
     for name in sorted(declared):
         assert hasattr(lib, name), name
-    assert lib.prgpu_abi_version() == 3
+    assert lib.prgpu_abi_version() == 4
 
 
 def test_convex_hull_matches_scene_builder(lib):

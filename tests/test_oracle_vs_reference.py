@@ -178,3 +178,11 @@ def test_raycast(double):
         assert [(g[0], g[2], g[3], g[4], g[5]) for g in got] == sorted(want), r
         hits += len(got)
     assert hits > 100
+
+
+@pytest.mark.parametrize("double", [False, True])
+def test_multi_child_shapes(double):
+    # a ChainShapeConf terrain (one proxy per edge child) and bodies of MultiShapeConf
+    # hulls: proxies, contact keys and features per child, mass data of the whole
+    # shape (ChainShapeConf.cpp:113-147, MultiShapeConf.cpp:35-57), states
+    _compare(scenes.multi_child_scene(np.random.default_rng(51)), [1, 60, 150], double=double)
