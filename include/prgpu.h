@@ -35,6 +35,8 @@
  *   prgpu_set_solve_records,    the arguments of the PreSolveContact / PostSolveContact
  *   prgpu_download_solve_records  listeners, AabbTreeWorld.cpp:2716-2720, :1669-1672
  *   prgpu_set_capacity_growth   the unbounded growth of the reference's contact containers
+ *   prgpu_set_sub_stepping,     SetSubStepping(World, bool) / IsStepComplete(World),
+ *   prgpu_get_step_complete     AabbTreeWorld.cpp:1819-1823, :2206-2209
  * The remaining entry points (schedule, autotuner, StepAdjoint, sweep order, body
  * steps, wait limit, allocation-free download) have no reference counterpart.
  */
@@ -385,6 +387,15 @@ int prgpu_download_contact_state(prgpu_world* w, uint32_t capacity, uint32_t* n_
  * prgpu_step_profiled do not grow.  Not inside an adjoint window. */
 int prgpu_set_capacity_growth(prgpu_world* w, int enabled);
 int prgpu_get_capacities(prgpu_world* w, uint32_t* contacts, uint32_t* candidates);
+/* SetSubStepping(World, flag) (AabbTreeWorld.hpp; the TOI loop's break at
+ * AabbTreeWorld.cpp:1819-1823): with it on, each world's time-of-impact phase
+ * stops after one event and the world's step is left incomplete; the next step
+ * skips that world's regular phase (IsStepComplete, :2206-2209) and continues its
+ * time-of-impact phase, until a phase finds no event.  Off by default. */
+int prgpu_set_sub_stepping(prgpu_world* w, int enabled);
+/* IsStepComplete(World) for one world of the batch: 1, or 0 while sub-stepping
+ * left its time-of-impact phase unfinished. */
+int prgpu_get_step_complete(prgpu_world* w, uint32_t world, int* complete);
 /* Spins a grid-wide barrier wait may take before it gives up, records
  * PRGPU_ETIMEOUT in the device error word and lets the kernel drain (0 restores
  * the default of 2^24; 1 gives up at the first wait).  For failure tests of the

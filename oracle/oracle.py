@@ -76,6 +76,9 @@ def _lib(double: bool):
                                  real, real, real, real, ctypes.c_uint, ctypes.c_uint, ctypes.c_int, ctypes.c_int]
     lib.or_add_shape.restype = ctypes.c_int
     lib.or_reset_mass.argtypes = [P, ctypes.c_int]
+    lib.or_set_sub_stepping.argtypes = [P, ctypes.c_int]
+    lib.or_is_step_complete.argtypes = [P]
+    lib.or_is_step_complete.restype = ctypes.c_int
     lib.or_set_shape_owner.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.or_add_revolute.argtypes = [P, ctypes.c_int, ctypes.c_int] + [real] * 5 + [
         ctypes.c_int, real, real, ctypes.c_int, real, real, ctypes.c_int]
@@ -240,6 +243,13 @@ class OracleWorld:
         self.lib.or_solve_calls(self.h, ints.ctypes.data, imp.ctypes.data, n)
         return [tuple(int(x) for x in ints[5 * i:5 * i + 5]) + tuple(float(x) for x in imp[4 * i:4 * i + 4])
                 for i in range(n)]
+
+    def set_sub_stepping(self, flag: bool = True):
+        """SetSubStepping: the time-of-impact phase stops after one event a step."""
+        self.lib.or_set_sub_stepping(self.h, int(bool(flag)))
+
+    def is_step_complete(self) -> bool:
+        return bool(self.lib.or_is_step_complete(self.h))
 
     def raycast(self, p1, p2, max_fraction=1.0) -> list:
         """RayCast of the world with a callback that answers ResetRay: every shape

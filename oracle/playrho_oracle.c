@@ -248,6 +248,8 @@ struct or_world {
     ivec bodiesForSync;
     ivec proxiesForContacts;
     real inv_dt0;
+    int sub_stepping;       /* SetSubStepping: the TOI phase stops after one event */
+    int step_incomplete;    /* !IsStepComplete: the next Step skips the regular phase */
     ivec events;            /* the last step's contact listener calls: (kind, shape, shape) */
     ivec solve_calls;       /* the last step's preSolve / postSolve calls, 9 words each */
     /* or_set_solve_order: ranks of contacts (by shape pair) and joints for the
@@ -3819,6 +3821,8 @@ static void solve_toi(or_world* w, const or_stepconf* conf, or_stepstats* st) {
             if (c->toiValid && minToi > c->toi) { minToi = c->toi; next = (int)w->wcids.a[i]; }
         }
         if (next < 0) {
+            /* e_stepComplete, ResetBodiesForSolveTOI, ResetContactsForSolveTOI (:1770-1777) */
+            w->step_incomplete = 0;
             for (int id = 0; id < w->nb; ++id) { w->b[id].alpha0 = R(0); w->b[id].islanded = 0; }
             for (int i = 0; i < w->wcids.n; ++i) {
                 contact_t* c = &w->c[w->wcids.a[i]];
@@ -3842,6 +3846,10 @@ static void solve_toi(or_world* w, const or_stepconf* conf, or_stepstats* st) {
             }
         }
         st->toiContactsAdded += find_and_add_contacts(w, conf);
+        if (w->sub_stepping) {  /* one event per Step (:1819-1823) */
+            w->step_incomplete = 1;
+            break;
+        }
     }
     {
         const int upd = update_contacts(w, conf); /* UpdateContacts: updated and skipped counts */
@@ -3918,10 +3926,13 @@ void or_step(or_world* w, const or_stepconf* conf, or_stepstats* st) {
     st->toiMinSeparation = RINF;
     if (conf->deltaTime != R(0)) {
         w->inv_dt0 = R(1) / conf->deltaTime;
-        solve_reg(w, conf, st);
+        if (!w->step_incomplete) solve_reg(w, conf, st);  /* IsStepComplete (:2206-2209) */
         if (conf->doToi) solve_toi(w, conf, st);
     }
 }
+
+void or_set_sub_stepping(or_world* w, int flag) { w->sub_stepping = flag != 0; }
+int or_is_step_complete(const or_world* w) { return !w->step_incomplete; }
 
 /* StepConf defaults (StepConf.hpp:59-161, Settings.hpp). */
 void or_default_conf(or_stepconf* c) {

@@ -128,6 +128,9 @@ int or_add_gear(or_world* w, int joint1, int joint2, or_real ratio);
 
 void or_default_conf(or_stepconf* conf);
 void or_step(or_world* w, const or_stepconf* conf, or_stepstats* stats);
+/* SetSubStepping / IsStepComplete (AabbTreeWorld.cpp:1819-1823, :2206-2209). */
+void or_set_sub_stepping(or_world* w, int flag);
+int or_is_step_complete(const or_world* w);
 /* BeginContact (kind 1) and EndContact (kind 2) listener calls of the last
  * or_step, in call order, as (kind, lower shape ID, higher shape ID) triples. */
 int or_events(const or_world* w, int* out, int cap);

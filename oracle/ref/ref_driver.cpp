@@ -13,6 +13,7 @@
 //   step N            (runs N steps; may repeat)
 //   dump              (prints bodies, contacts and proxies)
 //   ray x1 y1 x2 y2 maxFraction   (prints every shape the ray hits)
+//   substep 0|1       (SetSubStepping)
 //   defaults          (prints the StepConf defaults)
 #include "ref_scene.hpp"
 
@@ -50,6 +51,7 @@ void printDefaults()
 
 void dump(const World& world, const StepStats& st)
 {
+    std::printf("complete %d\n", IsStepComplete(world) ? 1 : 0);
     std::printf("stats %u %u %u %u %u %u %u %u %u",
                 unsigned(st.pre.proxiesCreated), unsigned(st.pre.contactsDestroyed),
                 unsigned(st.pre.contactsAdded), unsigned(st.reg.islandsFound),
@@ -186,6 +188,10 @@ int main()
         else if (tag == "step") {
             int n = 0; in >> n;
             for (int i = 0; i < n; ++i) stats = Step(world, conf);
+        }
+        else if (tag == "substep") {
+            int flag = 0; in >> flag;
+            SetSubStepping(world, flag != 0);
         }
         else if (tag == "ray") {
             // RayCast(World, RayCastInput, callback) answering ResetRay: every hit as

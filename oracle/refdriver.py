@@ -58,7 +58,7 @@ def run(scene_text: str, steps, double: bool = False, timeout: float = 600.0):
     seq = [steps] if isinstance(steps, int) else list(steps)
     cmd = scene_text + "".join(f"step {n}\ndump\n" for n in seq)
     res = subprocess.run([path], input=cmd, capture_output=True, text=True, timeout=timeout, check=True)
-    dumps, cur, events, calls = [], None, [], []
+    dumps, cur, events, calls, complete = [], None, [], [], 1
     for line in res.stdout.splitlines():
         t = line.split()
         if not t:
@@ -67,9 +67,12 @@ def run(scene_text: str, steps, double: bool = False, timeout: float = 600.0):
             events.append(tuple(int(x) for x in t[1:4]))
         elif t[0] == "solve":
             calls.append(tuple(int(x) for x in t[1:6]) + tuple(_f(x) for x in t[6:10]))
+        elif t[0] == "complete":
+            complete = int(t[1])
         elif t[0] == "stats":
             cur = {"stats": [int(x) for x in t[1:10]] + [_f(x) for x in t[10:12]],
-                   "bodies": [], "proxies": [], "contacts": [], "events": events, "solve_calls": calls}
+                   "bodies": [], "proxies": [], "contacts": [], "events": events, "solve_calls": calls,
+                   "complete": complete}
             events, calls = [], []
         elif t[0] == "toistats":
             cur["toistats"] = [int(x) for x in t[1:15]] + [_f(x) for x in t[15:17]]
@@ -129,4 +132,4 @@ def _finish(d, double):
                 "local_point": fo[:, 2:4], "points": fo[:, 4:12].reshape(n, 2, 4),
                 "features": ft.reshape(n, 2, 4)}
     return {"stats": d["stats"], "toistats": d.get("toistats"), "bodies": bodies, "proxies": proxies,
-            "contacts": contacts, "events": d["events"], "solve_calls": d["solve_calls"]}
+            "contacts": contacts, "events": d["events"], "solve_calls": d["solve_calls"], "complete": d["complete"]}

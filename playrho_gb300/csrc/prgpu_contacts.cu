@@ -434,6 +434,8 @@ __global__ void k_new_contacts(DW d) {
         d.cs_seq[slot] = seq + i;
         d.cs_prio[slot] = contact_prio(d, pa, pb);
         d.cs_upd[slot] = 0u;
+        d.cs_toi_ep[slot] = 0u;
+        d.cs_toi_at[slot] = 0u;
         if (d.cs_post_tag) d.cs_post_tag[slot] = make_uint2(0u, 0u);
         store_manifold(d, slot, man_empty());
         if (!sensor) {

@@ -162,6 +162,7 @@ struct Counters {
     uint32_t need_find;
     uint32_t step_no;         // steps begun (tags the contact updates and solve records of a step)
     uint32_t wait_limit;      // spins a grid-barrier wait may take (0: the default, 2^24)
+    uint32_t sub_stepping;    // SetSubStepping: the TOI phase stops after one event per world
     uint32_t upd_phase;       // phase bit the contact updates are tagged with (kUpd*)
     // StepStats counters (StepStats.hpp)
     uint32_t st_contacts_added;
@@ -236,6 +237,8 @@ struct DW {
     uint32_t* w_kj;          // [n_worlds + 1] first active joint of each world
     uint32_t* w_toi;         // [n_worlds] time-of-impact loop of the world finished this step (1)
     uint32_t* w_toi_ep;      // [n_worlds] the world's epoch counter in the TOI phase
+    uint32_t* w_incomplete;  // [n_worlds] !IsStepComplete: sub-stepping stopped the world's TOI phase
+                             //   after an event; its next step skips the regular phase
     uint32_t n_world_big;    // leading entries of w_order swept by a whole CTA (the rest by a warp)
     uint32_t stage_bytes;    // dynamic shared memory of the per-world solver (world body state)
     StepTape* tape;          // recording for the adjoint (device struct), else null

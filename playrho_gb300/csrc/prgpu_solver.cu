@@ -94,6 +94,7 @@ __global__ void k_body_begin(DW d) {
         const uint32_t f = d.b_flags[b];
         const uint32_t r = d.b_island[b];
         if (!island_edge_body(f) || !d.isl_awake[r]) continue;
+        if (d.w_incomplete[d.b_world[b]]) continue;  // !IsStepComplete: no SolveReg (AabbTreeWorld.cpp:2206-2209)
         d.b_flags[b] = f | BF_SOLVED | BF_AWAKE;
         if (is_accelerable(f)) ++solved;
         const float4 p = d.b_pos1[b];

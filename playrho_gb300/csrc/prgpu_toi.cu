@@ -209,20 +209,25 @@ __device__ __forceinline__ void toi_iter_stats(const DW& d, int mdist, int mtoi,
 
 // Every body starts the phase with alpha0 = 0 (ResetBodiesForSolveTOI ended the
 // last one), no epochs, no proxy marked moved; every world at epoch 1.
+// A world whose last phase sub-stepping stopped after an event continues that
+// phase: its bodies' alpha0, the epochs and the contacts' times of impact stay.
 __global__ void k_toi_begin(DW d) {
     GRID_LOOP(b, d.n_bodies) {
+        if (d.w_incomplete[d.b_world[b]]) continue;
         d.b_alpha0[b] = 0.f;
         d.b_toi_ep[b] = 0u;
         d.b_toi_rst[b] = 0u;
     }
-    GRID_LOOP(s, d.contact_cap) {
+    GRID_LOOP(i, d.cnt->n_live) {
+        const uint32_t s = d.c_slot[i];
+        if (d.w_incomplete[d.b_world[d.cs_body[s].x]]) continue;
         d.cs_toi_ep[s] = 0u;
         d.cs_toi_at[s] = 0u;
     }
     GRID_LOOP(p, d.n_shapes) d.p_moved[p] = 0u;
     GRID_LOOP(w, d.n_worlds) {
         d.w_toi[w] = 0u;
-        d.w_toi_ep[w] = 1u;
+        if (!d.w_incomplete[w]) d.w_toi_ep[w] = 1u;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         d.cnt->n_moved = 0u;
@@ -269,6 +274,7 @@ __global__ void k_toi_first(DW d) {
     int mdist = 0, mtoi = 0, mroot = 0;
     GRID_LOOP(i, d.cnt->n_imp) {
         const uint32_t slot = d.t_slot[i];
+        if (d.w_incomplete[d.b_world[d.cs_body[slot].x]]) continue;  // its round computes them in list order
         const int k = toi_candidate(d, slot, c.maxSubSteps);
         if (k == 2) ++at_max;
         if (k != 1) continue;
@@ -680,7 +686,8 @@ __device__ void toi_world_round(const DW& d, uint32_t w, ToiScratch& S, bool fir
     const Seg imp = world_slice(d, w, d.t_key, d.t_slot, d.cnt->n_imp);
     if (lane == 0) { S.ep = d.w_toi_ep[w]; S.nb = 0; S.nc = 0; }
     __syncwarp();
-    if (!first) toi_update_world(d, imp, S, lane);
+    // round 0 of a continued phase: its missing times of impact in list order
+    if (!first || d.w_incomplete[w]) toi_update_world(d, imp, S, lane);
     // GetSoonestContact (AabbTreeWorld.cpp:2870-2890): the smallest time below 1,
     // the earliest in the contact list among equal times
     float best = 1.0f;
@@ -707,7 +714,7 @@ __device__ void toi_world_round(const DW& d, uint32_t w, ToiScratch& S, bool fir
         for (uint32_t b = d.w_body_off[w] + lane; b < d.w_body_off[w + 1]; b += 32u) d.b_alpha0[b] = 0.f;
         for (uint32_t i = imp.c0 + lane; i < imp.c1; i += 32u)
             d.cs_flags[imp.slots[i]] &= ~(CF_TOI_VALID | CF_TOI_ISL | kToiCountMask);
-        if (lane == 0) d.w_toi[w] = 1u;
+        if (lane == 0) { d.w_toi[w] = 1u; d.w_incomplete[w] = 0u; }  // e_stepComplete
         return;
     }
     if (lane == 0) {
@@ -740,6 +747,9 @@ __device__ void toi_world_round(const DW& d, uint32_t w, ToiScratch& S, bool fir
         for (uint32_t i = 0; i < S.nc; ++i) d.cs_flags[S.isl_c[i]] &= ~CF_TOI_ISL;
         for (uint32_t i = 0; i < S.nb; ++i) d.b_flags[S.isl_b[i]] &= ~BF_TOI_ISL;
         d.w_toi_ep[w] = rst;
+        // sub-stepping: one event per Step (AabbTreeWorld.cpp:1819-1823); the contact
+        // search after it runs with this round's
+        if (d.cnt->sub_stepping) { d.w_toi[w] = 1u; d.w_incomplete[w] = 1u; }
     }
     __syncwarp();
 }
@@ -787,6 +797,7 @@ __global__ void k_toi_update_contacts(DW d) {
         const uint32_t slot = d.c_slot[i];
         if (toi_needs_update(d, slot)) {
             update_contact(d, slot);
+            d.cs_toi_ep[slot] = d.w_toi_ep[d.b_world[d.cs_body[slot].x]];  // up to date for a continued phase
             ++updated;
         } else {
             ++skipped;

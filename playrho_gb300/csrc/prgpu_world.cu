@@ -1109,11 +1109,12 @@ static int alloc_world(prgpu_world* w, const WorldDims& z) {
     AL(d.w_root, W); AL(d.w_bounds, W);
     uint32_t* w_order;
     AL(w_order, W); d.w_order = w_order;
-    AL(d.w_kc, W + 1); AL(d.w_kj, W + 1); ALS(d.w_toi, W); ALS(d.w_toi_ep, W);
+    // the TOI phase's state persists between steps when sub-stepping stops a phase
+    AL(d.w_kc, W + 1); AL(d.w_kj, W + 1); ALS(d.w_toi, W); AL(d.w_toi_ep, W); AL(d.w_incomplete, W);
     AL(d.b_pos1, N); AL(d.b_pos0, N); AL(d.b_vel, N); AL(d.b_xf, N); AL(d.b_mass, N); AL(d.b_acc, N);
     AL(d.b_damp, N); AL(d.b_flags, N); AL(d.b_uat, N); AL(d.b_world, N); AL(d.b_island, N);
     // the TOI phase's own state: reset when the phase starts
-    ALS(d.b_alpha0, N); ALS(d.b_toi_ep, N); ALS(d.b_toi_rst, N);
+    AL(d.b_alpha0, N); AL(d.b_toi_ep, N); AL(d.b_toi_rst, N);
     uint32_t *b_shape_off, *b_shapes;
     AL(b_shape_off, N + 1); AL(b_shapes, S);
     d.b_shape_off = b_shape_off; d.b_shapes = b_shapes;
@@ -1131,8 +1132,8 @@ static int alloc_world(prgpu_world* w, const WorldDims& z) {
     AL(d.j_r, J); AL(d.j_m0, J); AL(d.j_m1, J); AL(d.j_m2, J); AL(d.j_imp, J);
     AL(d.c_key, C); AL(d.c_slot, C); ALS(d.c_key_alt, C); ALS(d.c_slot_alt, C); AL(d.free_stack, C);
     AL(d.cs_proxy, C); AL(d.cs_body, C); AL(d.cs_flags, C); AL(d.cs_mat, C); AL(d.cs_tspeed, C);
-    AL(d.cs_colour, C); AL(d.j_colour, J); ALS(d.cs_toi, C); AL(d.cs_seq, C); AL(d.cs_prio, C); AL(d.cs_upd, C);
-    ALS(d.cs_toi_ep, C); ALS(d.cs_toi_at, C); ALS(d.t_key, C); ALS(d.t_slot, C);
+    AL(d.cs_colour, C); AL(d.j_colour, J); AL(d.cs_toi, C); AL(d.cs_seq, C); AL(d.cs_prio, C); AL(d.cs_upd, C);
+    AL(d.cs_toi_ep, C); AL(d.cs_toi_at, C); ALS(d.t_key, C); ALS(d.t_slot, C);
     AL(d.m_head, C); AL(d.m_p0, C); AL(d.m_p1, C); AL(d.m_meta, C); AL(d.m_cf, C);
     ALS(d.n_key, K); ALS(d.n_key_alt, K); ALS(d.n_val, K); ALS(d.n_val_alt, K);
     AL(d.l_key, S); AL(d.l_key_alt, S); AL(d.l_idx, S); AL(d.l_idx_alt, S); AL(d.l_leaf_box, S);
@@ -1284,6 +1285,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ok &= up(d.j_m2, j_zero.data(), sizeof(float4) * J);
     ok &= cudaMemsetAsync(d.b_uat, 0, sizeof(float) * N, w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.b_alpha0, 0, sizeof(float) * N, w->stream) == cudaSuccess;
+    ok &= cudaMemsetAsync(d.w_incomplete, 0, sizeof(uint32_t) * W, w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.cnt, 0, sizeof(Counters), w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.cs_upd, 0, sizeof(uint32_t) * std::max<uint32_t>(C, 1), w->stream) == cudaSuccess;
     ok &= cudaMemsetAsync(d.j_colour, 0xff, sizeof(uint32_t) * std::max<uint32_t>(J, 1), w->stream) == cudaSuccess;
@@ -1385,6 +1387,26 @@ int prgpu_get_capacities(prgpu_world* w, uint32_t* contacts, uint32_t* candidate
     if (!w) return PRGPU_EINVAL;
     if (contacts) *contacts = w->d.contact_cap;
     if (candidates) *candidates = w->d.cand_cap;
+    return PRGPU_OK;
+}
+
+int prgpu_set_sub_stepping(prgpu_world* w, int enabled) {
+    if (!w) return PRGPU_EINVAL;
+    CU(cudaSetDevice(w->device));
+    const uint32_t v = enabled ? 1u : 0u;
+    CU(cudaMemcpyAsync(&w->d.cnt->sub_stepping, &v, sizeof(v), cudaMemcpyHostToDevice, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_get_step_complete(prgpu_world* w, uint32_t world, int* complete) {
+    if (!w || !complete) return PRGPU_EINVAL;
+    if (world >= w->d.n_worlds) return fail(w, PRGPU_EINVAL, "world %u out of range", world);
+    CU(cudaSetDevice(w->device));
+    uint32_t v = 0;
+    CU(cudaMemcpyAsync(&v, w->d.w_incomplete + world, sizeof(v), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    *complete = v ? 0 : 1;
     return PRGPU_OK;
 }
 

@@ -140,6 +140,8 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_set_capacity_growth.argtypes = [P, I]
     lib.prgpu_get_capacities.argtypes = [P, P, P]
     lib.prgpu_set_wait_limit.argtypes = [P, U]
+    lib.prgpu_set_sub_stepping.argtypes = [P, I]
+    lib.prgpu_get_step_complete.argtypes = [P, U, P]
     lib.prgpu_raycast.argtypes = [P, U, P, P, P, P]
     lib.prgpu_raycast_all.argtypes = [P, U, P, U, P, P, P]
     lib.prgpu_download_solve_records.argtypes = [P, U, P, P, P, P]
@@ -162,7 +164,8 @@ def exported_symbols() -> List[str]:
         "prgpu_download_sweep_order", "prgpu_download_contacts_noalloc", "prgpu_download_contact_seq",
         "prgpu_query_aabb", "prgpu_download_contact_state", "prgpu_set_contact", "prgpu_set_manifold",
         "prgpu_set_solve_records", "prgpu_download_solve_records", "prgpu_query_aabbs", "prgpu_raycast",
-        "prgpu_raycast_all", "prgpu_set_capacity_growth", "prgpu_get_capacities", "prgpu_set_wait_limit"]
+        "prgpu_raycast_all", "prgpu_set_capacity_growth", "prgpu_get_capacities", "prgpu_set_wait_limit",
+        "prgpu_set_sub_stepping", "prgpu_get_step_complete"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -590,6 +593,16 @@ class GpuBatch:
         c, k = ctypes.c_uint32(), ctypes.c_uint32()
         self._check(self.lib.prgpu_get_capacities(self.h, ctypes.byref(c), ctypes.byref(k)), "prgpu_get_capacities")
         return c.value, k.value
+
+    def set_sub_stepping(self, enabled: bool = True):
+        """SetSubStepping: each world's time-of-impact phase stops after one event."""
+        self._check(self.lib.prgpu_set_sub_stepping(self.h, int(bool(enabled))), "prgpu_set_sub_stepping")
+
+    def step_complete(self, world: int) -> bool:
+        """IsStepComplete of one world."""
+        v = ctypes.c_int()
+        self._check(self.lib.prgpu_get_step_complete(self.h, int(world), ctypes.byref(v)), "prgpu_get_step_complete")
+        return bool(v.value)
 
     def set_wait_limit(self, spins: int):
         """Spins a grid-barrier wait may take before it gives up (0: default)."""

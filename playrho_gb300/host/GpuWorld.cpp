@@ -576,9 +576,21 @@ StepStats Step(GpuWorld& w, const StepConf& conf) {
     return stats;
 }
 
-bool IsStepComplete(const GpuWorld&) noexcept { return true; }
+bool IsStepComplete(const GpuWorld& w) noexcept {
+    try {
+        return const_cast<GpuWorld&>(w).host.StepComplete();
+    } catch (...) {
+        return true;
+    }
+}
 bool GetSubStepping(const GpuWorld& w) noexcept { return w.subStepping; }
-void SetSubStepping(GpuWorld& w, bool flag) noexcept { w.subStepping = flag; }
+void SetSubStepping(GpuWorld& w, bool flag) noexcept {
+    w.subStepping = flag;
+    try {
+        w.host.SetSubStepping(flag);  // also kept for the next batch the host builds
+    } catch (...) {
+    }
+}
 
 const DynamicTree& GetTree(const GpuWorld& w) noexcept {
     if (!w.treeValid) {

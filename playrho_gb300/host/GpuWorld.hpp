@@ -16,8 +16,9 @@
 // What the GPU world does differently, by design of this path:
 //  * disk, polygon, edge, chain and multi shapes; a chain's edges and a multi
 //    shape's hulls are shapes of the GPU batch, one proxy per child as in the
-//    reference; StepConf::doToi runs the time-of-impact phase, but sub-stepping
-//    (one event per Step) is not offered;
+//    reference; StepConf::doToi runs the time-of-impact phase, with sub-stepping
+//    (one event per Step, IsStepComplete) as the reference offers it; a world
+//    rebuilt while its step is incomplete starts complete;
 //  * Gauss-Seidel sweeps visit contacts in colour order, not island order;
 //  * contact IDs are the GPU's contact slots: stable for a contact's life and
 //    reused after it is destroyed, as the reference's pools reuse them;

@@ -116,10 +116,16 @@ void HostWorld::DestroyBody(uint32_t id) {
 
 // ---- shapes ------------------------------------------------------------------
 uint32_t HostWorld::CreateShape(const HostShape& s) {
-    const size_t nv = s.verts.size() / 2;
-    if (s.verts.size() % 2 || nv < 1 || nv > 16 || (s.kind == PRGPU_DISK && nv != 1) ||
-        (s.kind == PRGPU_EDGE && nv != 2) || s.kind < PRGPU_DISK || s.kind > PRGPU_EDGE)
-        throw Error(PRGPU_EINVAL, "CreateShape: unsupported shape (disk, polygon of <= 16 vertices, edge)");
+    auto valid = [&](const std::vector<float>& v) {
+        const size_t nv = v.size() / 2;
+        return !(v.size() % 2 || nv < 1 || nv > 16 || (s.kind == PRGPU_DISK && nv != 1) ||
+                 (s.kind == PRGPU_EDGE && nv != 2) || s.kind < PRGPU_DISK || s.kind > PRGPU_EDGE);
+    };
+    bool ok = s.children.empty() ? valid(s.verts) : s.kind != PRGPU_DISK;
+    for (const auto& c : s.children) ok = ok && valid(c);
+    if (!ok)
+        throw Error(PRGPU_EINVAL, "CreateShape: unsupported shape (disk, polygon of <= 16 vertices, edge, "
+                                  "or children of edges or polygons)");
     const uint32_t id = pool_add(shapes_, shape_live_, shape_free_, s);
     rebuild_ = true;
     return id;
@@ -297,6 +303,7 @@ void HostWorld::Build() {
     // the reference's contact containers grow without bound: so do the batch's
     Check(prgpu_set_capacity_growth(gpu_, 1), "prgpu_set_capacity_growth");
     if (solve_records_) Check(prgpu_set_solve_records(gpu_, 1), "prgpu_set_solve_records");
+    if (sub_stepping_) Check(prgpu_set_sub_stepping(gpu_, 1), "prgpu_set_sub_stepping");
     state_dirty_.assign(bodies_.size(), false);
     lc_.assign(2 * (size_t)N, 0.f);
     std::vector<float> m(4 * (size_t)N), p(3 * (size_t)N);
@@ -398,6 +405,18 @@ const std::vector<HostContact>& HostWorld::Contacts() {
     }
     contacts_valid_ = true;
     return contacts_;
+}
+
+void HostWorld::SetSubStepping(bool enabled) {
+    sub_stepping_ = enabled;
+    if (gpu_) Check(prgpu_set_sub_stepping(gpu_, enabled ? 1 : 0), "prgpu_set_sub_stepping");
+}
+
+bool HostWorld::StepComplete() {
+    if (!gpu_) return true;
+    int complete = 1;
+    Check(prgpu_get_step_complete(gpu_, 0, &complete), "prgpu_get_step_complete");
+    return complete != 0;
 }
 
 void HostWorld::SetSolveRecords(bool enabled) {

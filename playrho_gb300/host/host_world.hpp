@@ -144,6 +144,9 @@ public:
     void SetManifold(uint32_t slot, int32_t type, int32_t count, const float head4[4], const float pts8[8]);
     // Keep solve records from the next step on (prgpu_set_solve_records), across rebuilds.
     void SetSolveRecords(bool enabled);
+    // SetSubStepping / IsStepComplete (prgpu_set_sub_stepping, prgpu_get_step_complete).
+    void SetSubStepping(bool enabled);
+    bool StepComplete();
     // The live contacts the last step updated or solved.
     std::vector<HostSolveRecord> SolveRecords();
     // Fat AABB (minx miny maxx maxy) and (body, shape, child) of every proxy, by leaf ID order.
@@ -179,6 +182,7 @@ private:
     bool contacts_valid_ = false;
     std::vector<HostContact> contacts_;
     bool solve_records_ = false;
+    bool sub_stepping_ = false;
 };
 
 }  // namespace prgpu

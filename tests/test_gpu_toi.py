@@ -225,3 +225,31 @@ def test_batch_equals_single_worlds(gpu_lib):
         base, n = int(g.body_base[i]), worlds[i].n_bodies
         np.testing.assert_array_equal(gb["pos"][base:base + n], s.bodies()["pos"])
         np.testing.assert_array_equal(gb["vel"][base:base + n], s.bodies()["vel"])
+
+
+def test_sub_stepping_bit_exact(gpu_lib):
+    """SetSubStepping: each world's time-of-impact phase stops after one event and
+    its next step skips the regular phase (AabbTreeWorld.cpp:1819-1823,
+    :2206-2209).  Fired disks, 24 worlds in one batch whose steps complete at
+    different times: IsStepComplete and the states equal the oracle's (pinned to
+    the reference with sub-stepping in test_oracle_vs_reference) bit for bit."""
+    rng = np.random.default_rng(17)
+    worlds = [fired_disk(rng) for _ in range(24)]
+    g = GpuBatch(worlds)
+    g.set_sub_stepping(True)
+    ows = [oracle.OracleWorld(w) for w in worlds]
+    for ow in ows:
+        ow.set_sub_stepping(True)
+    incomplete = 0
+    for step in range(30):
+        g.step(doToi=1)
+        for ow in ows:
+            ow.step(doToi=1)
+        gb = g.bodies()
+        for i, ow in enumerate(ows):
+            assert g.step_complete(i) == ow.is_step_complete(), (i, step)
+            incomplete += 0 if ow.is_step_complete() else 1
+            base = int(g.body_base[i])
+            np.testing.assert_array_equal(gb["pos"][base:base + 2], ow.bodies()["pos"], err_msg=f"world {i} step {step}")
+            np.testing.assert_array_equal(gb["vel"][base:base + 2], ow.bodies()["vel"], err_msg=f"world {i} step {step}")
+    assert incomplete > 0

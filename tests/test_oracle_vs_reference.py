@@ -186,3 +186,25 @@ def test_multi_child_shapes(double):
     # hulls: proxies, contact keys and features per child, mass data of the whole
     # shape (ChainShapeConf.cpp:113-147, MultiShapeConf.cpp:35-57), states
     _compare(scenes.multi_child_scene(np.random.default_rng(51)), [1, 60, 150], double=double)
+
+
+@pytest.mark.parametrize("double", [False, True])
+def test_toi_sub_stepping(double):
+    # SetSubStepping: the time-of-impact phase stops after one event a step and the
+    # next Step skips the regular phase until an event loop finds nothing
+    # (AabbTreeWorld.cpp:1819-1823, :2206-2209)
+    sc = scenes.bullets(40, np.random.default_rng(57))
+    steps = [1, 1, 1, 5, 20, 40]
+    dumps = refdriver.run("substep 1\n" + scenes.scene_text(sc, {"doToi": 1}), steps, double=double)
+    ow = oracle.OracleWorld(sc, double=double)
+    ow.set_sub_stepping(True)
+    incomplete = 0
+    for n, d in zip(steps, dumps):
+        for _ in range(n):
+            ow.step(doToi=1)
+        assert int(ow.is_step_complete()) == d["complete"]
+        incomplete += 1 - d["complete"]
+        b = ow.bodies()
+        np.testing.assert_array_equal(b["pos"], d["bodies"]["pos"])
+        np.testing.assert_array_equal(b["vel"], d["bodies"]["vel"])
+    assert incomplete > 0
