@@ -201,10 +201,11 @@ def sweep_bytes(stats, conf, n_bodies_solved):
     return nc * per_contact + n_bodies_solved * 52
 
 
-# prgpu_autotune times 16 candidate schedules (the grid-wide one, then 3 staging
-# sizes x 5 warp-world limits), each over one capturing step plus the steps asked
-# for; those steps advance the batch like any other.
-AUTOTUNE_CANDIDATES = 16
+# prgpu_autotune times 22 candidate schedules (the grid-wide one, 3 staging sizes
+# x 5 warp-world limits, then 2 warp-world limits x 3 group-world limits), each
+# over one capturing step plus the steps asked for; those steps advance the batch
+# like any other.
+AUTOTUNE_CANDIDATES = 22
 AUTOTUNE_STEPS = 2
 
 
@@ -510,7 +511,8 @@ def run_ours(args, rank, world_size, local, dist):
                    "live_contacts": st["liveContacts"], "active_constraints": st["activeConstraints"],
                    "colours": st["colours"], "serial_constraints": st["serialConstraints"],
                    "schedule": {"sweeps": batch.sweep_mode(), "warp_world_max_bodies": batch.warp_world_max_bodies(),
-                                "autotuned": schedule is not None}},
+                                "group_world_max_bodies": batch.group_world_max_bodies(),
+                                "stage_bytes": batch.stage_bytes(), "autotuned": schedule is not None}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic,
                      "kernel": ("k_world_solve (per-world colouring, constraint build and Gauss-Seidel sweeps)"

@@ -49,7 +49,7 @@
 extern "C" {
 #endif
 
-#define PRGPU_ABI_VERSION 4
+#define PRGPU_ABI_VERSION 5
 
 enum prgpu_status {
     PRGPU_OK = 0,
@@ -225,6 +225,12 @@ int prgpu_get_sweep_mode(prgpu_world* w, int* mode);
  * (eight worlds at a time per CTA), larger ones by a whole CTA.  Default 256. */
 int prgpu_set_warp_world_max_bodies(prgpu_world* w, uint32_t max_bodies);
 int prgpu_get_warp_world_max_bodies(prgpu_world* w, uint32_t* max_bodies);
+/* In PER_WORLD mode, worlds larger than the warp limit and of at most this many
+ * bodies are swept by groups of 64 threads (four worlds at a time per CTA, each
+ * group on a named barrier of its own); larger ones by a whole CTA.  0 (the
+ * default): no groups.  Results do not depend on it. */
+int prgpu_set_group_world_max_bodies(prgpu_world* w, uint32_t max_bodies);
+int prgpu_get_group_world_max_bodies(prgpu_world* w, uint32_t* max_bodies);
 /* A sweep schedule and its measured device time per step. */
 /* Shared memory (bytes, a multiple of 128) in which the per-world solver
  * keeps the velocities and positions of the world it sweeps, 44 bytes a body
@@ -237,6 +243,7 @@ typedef struct prgpu_schedule {
     uint32_t warp_world_max_bodies;
     uint32_t stage_bytes;
     float step_ms;
+    uint32_t group_world_max_bodies;  /* ABI 5 */
 } prgpu_schedule;
 /* Autotuner: times every candidate schedule over steps_per_candidate steps
  * (after one untimed step that captures it) and keeps the fastest.  The

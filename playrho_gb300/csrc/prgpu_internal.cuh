@@ -239,7 +239,8 @@ struct DW {
     uint32_t* w_toi_ep;      // [n_worlds] the world's epoch counter in the TOI phase
     uint32_t* w_incomplete;  // [n_worlds] !IsStepComplete: sub-stepping stopped the world's TOI phase
                              //   after an event; its next step skips the regular phase
-    uint32_t n_world_big;    // leading entries of w_order swept by a whole CTA (the rest by a warp)
+    uint32_t n_world_big;    // leading entries of w_order swept by a whole CTA,
+    uint32_t n_world_mid;    //   then up to n_world_mid by groups of kGroupThreads threads (the rest by a warp)
     uint32_t stage_bytes;    // dynamic shared memory of the per-world solver (world body state)
     StepTape* tape;          // recording for the adjoint (device struct), else null
     float4* w_bounds;        // centroid bounds for Morton codes (ordered-int encoded)

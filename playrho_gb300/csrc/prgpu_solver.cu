@@ -2123,6 +2123,26 @@ struct WarpGroup {
         return __any_sync(0xffffffffu, p) != 0;
     }
 };
+// kGroupThreads consecutive threads of a CTA on a named barrier of their own
+// (1 + group index; barrier 0 is __syncthreads'), so that the CTA's groups sweep
+// different worlds and one world's barrier waits overlap another's loads.
+constexpr uint32_t kGroupThreads = 64;
+struct SubGroup {
+    __device__ __forceinline__ static uint32_t bar() { return 1u + threadIdx.x / kGroupThreads; }
+    __device__ __forceinline__ static void sync() {
+        asm volatile("bar.sync %0, %1;" ::"r"(bar()), "n"(kGroupThreads) : "memory");
+    }
+    __device__ __forceinline__ static bool any(bool p) {
+        uint32_t r;
+        asm volatile(
+            "{\n .reg .pred ps, pd;\n setp.ne.u32 ps, %1, 0;\n bar.red.or.pred pd, %2, %3, ps;\n"
+            " selp.u32 %0, 1, 0, pd;\n}"
+            : "=r"(r)
+            : "r"((uint32_t)p), "r"(bar()), "n"(kGroupThreads)
+            : "memory");
+        return r != 0u;
+    }
+};
 
 // The sweeps of one world by one group, over its segment [base, base + n) of
 // sweep order with colour offsets col_off; after_position(it) runs after each
@@ -2293,7 +2313,8 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
 
 // Persistent CTAs take worlds from a queue ordered by decreasing body count.
 // The first n_world_big entries are solved by a whole CTA each; once a CTA
-// meets a smaller world, each of its warps takes worlds on its own.
+// meets a smaller world, each of its groups of kGroupThreads threads takes
+// worlds on its own up to n_world_mid, and then each of its warps.
 __global__ void __launch_bounds__(256, 4) k_world_solve(DW d) {
     extern __shared__ float4 s_stage[];  // d.stage_bytes: body state of the world(s) being solved
     __shared__ uint32_t s_w;
@@ -2309,16 +2330,36 @@ __global__ void __launch_bounds__(256, 4) k_world_solve(DW d) {
         solve_world<BlockGroup>(d, d.w_order[qi], threadIdx.x, blockDim.x, s_col[0][0], s_col[0][1], s_stage,
                                 d.stage_bytes / kStageBytesPerBody);
     }
-    // each warp owns an eighth of the staging area
+    // each warp owns an eighth of the staging area, a group its warps' parts
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t part = d.stage_bytes / 8u;
+    constexpr uint32_t gwarps = kGroupThreads / 32u;
+    const uint32_t grp = threadIdx.x / kGroupThreads, grank = threadIdx.x % kGroupThreads;
+    if (d.n_world_mid > d.n_world_big) {
+        __shared__ uint32_t s_gq[256u / kGroupThreads];
+        auto gnext = [&]() {
+            SubGroup::sync();
+            if (grank == 0) s_gq[grp] = atomicAdd(&d.cnt->world_queue, 1u);
+            SubGroup::sync();
+            return s_gq[grp];
+        };
+        if (grp != 0) qi = gnext();  // group 0 keeps the entry the CTA took
+        void* gstage = reinterpret_cast<char*>(s_stage) + (size_t)(grp * gwarps) * part;
+        while (qi < d.n_world_mid) {
+            solve_world<SubGroup>(d, d.w_order[qi], grank, kGroupThreads, s_col[grp * gwarps][0],
+                                  s_col[grp * gwarps][1], gstage, gwarps * part / kStageBytesPerBody);
+            qi = gnext();
+        }
+        // the group's first warp keeps the group's entry
+    }
     void* stage = reinterpret_cast<char*>(s_stage) + (size_t)warp * part;
     auto next = [&]() {
         uint32_t x = 0u;
         if (lane == 0) x = atomicAdd(&d.cnt->world_queue, 1u);
         return __shfl_sync(0xffffffffu, x, 0);
     };
-    if (warp != 0) qi = next();  // warp 0 keeps the entry the CTA took
+    // warp 0 (of the CTA, or of each group) keeps the entry its CTA or group took
+    if ((d.n_world_mid > d.n_world_big) ? (warp % gwarps != 0) : (warp != 0)) qi = next();
     while (qi < d.n_worlds) {
         solve_world<WarpGroup>(d, d.w_order[qi], lane, 32u, s_col[warp][0], s_col[warp][1], stage,
                                part / kStageBytesPerBody);

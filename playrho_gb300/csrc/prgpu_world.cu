@@ -55,7 +55,8 @@ struct prgpu_world {
     cudaEvent_t graph_ev[8] = {};  // recorded by the captured step between its phases
     std::vector<uint32_t> order_nb;  // body counts of the worlds in work-queue order
     struct AdjWindow* adj = nullptr;  // open StepAdjoint window, if any
-    uint32_t warp_world_max = 0;     // worlds of at most this many bodies are swept by one warp
+    uint32_t warp_world_max = 0;     // worlds of at most this many bodies are swept by one warp,
+    uint32_t group_world_max = 0;    //   of at most this many (if larger) by a group of 64 threads
     // time-of-impact phase: set-up, one round, and the final update, each captured once
     cudaGraphExec_t toi_graph[3] = {};
 };
@@ -554,6 +555,18 @@ constexpr uint32_t kStageBytes = 0u;
 constexpr uint32_t kStageChoices[] = {0u, 1024u * 44u, 2048u * 44u};
 // Worlds of at most this many bodies are swept by one warp by default.
 constexpr uint32_t kWarpWorldMaxBodies = 256;
+
+// Queue entries of worlds above max_bodies (the queue is by decreasing size).
+uint32_t count_worlds_above(const prgpu_world* w, uint32_t max_bodies) {
+    uint32_t n = 0;
+    while (n < w->order_nb.size() && w->order_nb[n] > max_bodies) ++n;
+    return n;
+}
+
+void count_world_classes(prgpu_world* w) {
+    w->d.n_world_mid = count_worlds_above(w, w->warp_world_max);
+    w->d.n_world_big = count_worlds_above(w, std::max(w->warp_world_max, w->group_world_max));
+}
 
 uint32_t count_big_worlds(const prgpu_world* w) {
     uint32_t n = 0;
@@ -1234,7 +1247,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     w->order_nb.resize(W);
     for (uint32_t i = 0; i < W; ++i) w->order_nb[i] = body_off[order[i] + 1] - body_off[order[i]];
     w->warp_world_max = kWarpWorldMaxBodies;
-    d.n_world_big = count_big_worlds(w);
+    count_world_classes(w);
     if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(PRGPU_ECUDA);
     // ---- uploads
     auto up = [&](void* dst, const void* src, size_t bytes) -> bool {
@@ -1496,7 +1509,7 @@ int prgpu_set_warp_world_max_bodies(prgpu_world* w, uint32_t max_bodies) {
     const int rc = drop_graph(w);
     if (rc) return rc;
     w->warp_world_max = max_bodies;
-    w->d.n_world_big = count_big_worlds(w);
+    count_world_classes(w);
     return PRGPU_OK;
 }
 
@@ -1504,11 +1517,14 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
     if (!w || !conf || steps_per_candidate < 1) return PRGPU_EINVAL;
     if (conf->deltaTime == 0.f) return fail(w, PRGPU_EINVAL, "autotune needs a step with deltaTime > 0");
     CU(cudaSetDevice(w->device));
-    struct Cand { int mode; uint32_t warp_max; uint32_t stage; };
-    std::vector<Cand> cands = {{PRGPU_SWEEPS_GRID, w->warp_world_max, w->d.stage_bytes}};
+    struct Cand { int mode; uint32_t warp_max; uint32_t stage; uint32_t group_max; };
+    std::vector<Cand> cands = {{PRGPU_SWEEPS_GRID, w->warp_world_max, w->d.stage_bytes, 0u}};
     if (w->d.n_worlds > 1) {
         for (uint32_t sb : kStageChoices)
-            for (uint32_t m : {0u, 64u, 128u, 256u, 1024u}) cands.push_back({PRGPU_SWEEPS_PER_WORLD, m, sb});
+            for (uint32_t m : {0u, 64u, 128u, 256u, 1024u}) cands.push_back({PRGPU_SWEEPS_PER_WORLD, m, sb, 0u});
+        // worlds up to 256, 512 or 1024 bodies swept by groups of 64 threads
+        for (uint32_t m : {0u, 64u})
+            for (uint32_t g : {256u, 512u, 1024u}) cands.push_back({PRGPU_SWEEPS_PER_WORLD, m, 0u, g});
     }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CU(cudaEventCreate(&e0));
@@ -1519,6 +1535,7 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
     for (const Cand& cd : cands) {
         if ((rc = prgpu_set_sweep_mode(w, cd.mode)) != PRGPU_OK) break;
         if ((rc = prgpu_set_warp_world_max_bodies(w, cd.warp_max)) != PRGPU_OK) break;
+        if ((rc = prgpu_set_group_world_max_bodies(w, cd.group_max)) != PRGPU_OK) break;
         if ((rc = prgpu_set_stage_bytes(w, cd.stage)) != PRGPU_OK) break;
         if ((rc = run_steps(w, conf, 1, true)) != PRGPU_OK) break;  // captures the candidate's step
         if (cudaEventRecord(e0, w->stream) != cudaSuccess) { rc = PRGPU_ECUDA; break; }
@@ -1535,10 +1552,12 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
     if (rc) return rc;
     if ((rc = prgpu_set_sweep_mode(w, pick.mode)) != PRGPU_OK) return rc;
     if ((rc = prgpu_set_warp_world_max_bodies(w, pick.warp_max)) != PRGPU_OK) return rc;
+    if ((rc = prgpu_set_group_world_max_bodies(w, pick.group_max)) != PRGPU_OK) return rc;
     if ((rc = prgpu_set_stage_bytes(w, pick.stage)) != PRGPU_OK) return rc;
     if (best) {
         best->sweep_mode = pick.mode;
         best->warp_world_max_bodies = pick.warp_max;
+        best->group_world_max_bodies = pick.group_max;
         best->stage_bytes = pick.stage;
         best->step_ms = best_ms;
     }
@@ -1562,6 +1581,22 @@ int prgpu_set_stage_bytes(prgpu_world* w, uint32_t bytes) {
 int prgpu_get_stage_bytes(prgpu_world* w, uint32_t* bytes) {
     if (!w || !bytes) return PRGPU_EINVAL;
     *bytes = w->d.stage_bytes;
+    return PRGPU_OK;
+}
+
+int prgpu_set_group_world_max_bodies(prgpu_world* w, uint32_t max_bodies) {
+    if (!w) return PRGPU_EINVAL;
+    if (max_bodies == w->group_world_max) return PRGPU_OK;
+    const int rc = drop_graph(w);
+    if (rc) return rc;
+    w->group_world_max = max_bodies;
+    count_world_classes(w);
+    return PRGPU_OK;
+}
+
+int prgpu_get_group_world_max_bodies(prgpu_world* w, uint32_t* max_bodies) {
+    if (!w || !max_bodies) return PRGPU_EINVAL;
+    *max_bodies = w->group_world_max;
     return PRGPU_OK;
 }
 

@@ -72,7 +72,8 @@ class BatchDesc(ctypes.Structure):
 
 class Schedule(ctypes.Structure):
     _fields_ = [("sweep_mode", ctypes.c_int32), ("warp_world_max_bodies", ctypes.c_uint32),
-                ("stage_bytes", ctypes.c_uint32), ("step_ms", ctypes.c_float)]
+                ("stage_bytes", ctypes.c_uint32), ("step_ms", ctypes.c_float),
+                ("group_world_max_bodies", ctypes.c_uint32)]
 
 
 class PrgpuError(RuntimeError):
@@ -141,6 +142,8 @@ def load_library(path: str = LIB_PATH):
     lib.prgpu_get_capacities.argtypes = [P, P, P]
     lib.prgpu_set_wait_limit.argtypes = [P, U]
     lib.prgpu_set_sub_stepping.argtypes = [P, I]
+    lib.prgpu_set_group_world_max_bodies.argtypes = [P, U]
+    lib.prgpu_get_group_world_max_bodies.argtypes = [P, P]
     lib.prgpu_get_step_complete.argtypes = [P, U, P]
     lib.prgpu_raycast.argtypes = [P, U, P, P, P, P]
     lib.prgpu_raycast_all.argtypes = [P, U, P, U, P, P, P]
@@ -165,7 +168,8 @@ def exported_symbols() -> List[str]:
         "prgpu_query_aabb", "prgpu_download_contact_state", "prgpu_set_contact", "prgpu_set_manifold",
         "prgpu_set_solve_records", "prgpu_download_solve_records", "prgpu_query_aabbs", "prgpu_raycast",
         "prgpu_raycast_all", "prgpu_set_capacity_growth", "prgpu_get_capacities", "prgpu_set_wait_limit",
-        "prgpu_set_sub_stepping", "prgpu_get_step_complete"]
+        "prgpu_set_sub_stepping", "prgpu_get_step_complete", "prgpu_set_group_world_max_bodies",
+        "prgpu_get_group_world_max_bodies"]
 
 
 def default_conf(**overrides) -> StepConf:
@@ -397,6 +401,16 @@ class GpuBatch:
         self._check(self.lib.prgpu_get_sweep_mode(self.h, ctypes.byref(m)), "prgpu_get_sweep_mode")
         return {v: k for k, v in self.SWEEP_MODES.items()}[m.value]
 
+    def set_group_world_max_bodies(self, n: int):
+        """Per-world sweeps: worlds above the warp limit and of at most n bodies are
+        swept by groups of 64 threads (0: no groups)."""
+        self._check(self.lib.prgpu_set_group_world_max_bodies(self.h, int(n) & 0xffffffff), "group world limit")
+
+    def group_world_max_bodies(self) -> int:
+        m = ctypes.c_uint32(0)
+        self._check(self.lib.prgpu_get_group_world_max_bodies(self.h, ctypes.byref(m)), "group world limit")
+        return int(m.value)
+
     def set_warp_world_max_bodies(self, n: int):
         """Per-world sweeps: worlds of at most n bodies are swept by one warp."""
         self._check(self.lib.prgpu_set_warp_world_max_bodies(self.h, int(n) & 0xffffffff), "warp world limit")
@@ -423,7 +437,8 @@ class GpuBatch:
                     "prgpu_autotune")
         inv = {v: k for k, v in self.SWEEP_MODES.items()}
         return {"sweeps": inv[sc.sweep_mode], "warp_world_max_bodies": int(sc.warp_world_max_bodies),
-                "stage_bytes": int(sc.stage_bytes), "step_ms": float(sc.step_ms)}
+                "group_world_max_bodies": int(sc.group_world_max_bodies), "stage_bytes": int(sc.stage_bytes),
+                "step_ms": float(sc.step_ms)}
 
     # ---- StepAdjoint ----
     def adjoint_begin(self, checkpoint_every: int = 16):

@@ -186,10 +186,10 @@ void Conveyor(playrho::d2::World& world, const char* tag, bool doToi) {
 }
 
 // Multi-child shapes: a ChainShapeConf terrain and two bodies of MultiShapeConf
-// hulls and a disk falling onto it.  Prints "<tag> tcontact <step> <shapeA> <childA>
-// <shapeB> <childB> <touching>" for every contact at a few steps (lower shape first),
-// "<tag> tpos <step> <body> x y angle" every 10 steps and "<tag> tmass <body> invMass
-// invRotInertia" once.
+// hulls and a disk falling onto it, 30 steps.  Prints "<tag> tcontact <step>
+// <shapeA> <childA> <shapeB> <childB> <touching>" for every contact at steps 1,
+// 10, 20 and 30 (lower shape first), "<tag> tpos <step> <body> x y angle" every 5
+// steps and "<tag> tmass <body> invMass invRotInertia" once.
 void Terrain(playrho::d2::World& world, const char* tag) {
     using namespace playrho;
     using namespace playrho::d2;
@@ -230,9 +230,9 @@ void Terrain(playrho::d2::World& world, const char* tag) {
                     double(StripUnit(GetInvRotInertia(world, b))));
     auto conf = StepConf{};
     conf.doToi = false;
-    for (auto step = 1; step <= 90; ++step) {
+    for (auto step = 1; step <= 30; ++step) {
         Step(world, conf);
-        if (step == 1 || step == 30 || step == 60 || step == 90) {
+        if (step == 1 || step == 10 || step == 20 || step == 30) {
             for (const auto& kc : GetContacts(world)) {
                 const auto& c = GetContact(world, std::get<ContactID>(kc));
                 auto a = std::make_pair(unsigned(to_underlying(GetShapeA(c))), unsigned(GetChildIndexA(c)));
@@ -242,7 +242,7 @@ void Terrain(playrho::d2::World& world, const char* tag) {
                             IsTouching(c) ? 1 : 0);
             }
         }
-        if (step % 10 == 0) {
+        if (step % 5 == 0 && step <= 30) {
             for (const auto& b : bodies) {
                 const auto xf = GetTransformation(world, b);
                 std::printf("%s tpos %d %u %a %a %a\n", tag, step, unsigned(to_underlying(b)),

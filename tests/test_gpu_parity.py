@@ -248,14 +248,24 @@ def test_sweep_modes_agree(gpu_lib):
     f = GpuBatch(worlds)  # per world, body state staged in shared memory
     f.set_stage_bytes(2048 * 44)
     assert f.stage_bytes() == 2048 * 44
+    h = GpuBatch(worlds)  # per world, every world by a group of 64 threads
+    h.set_warp_world_max_bodies(0)
+    h.set_group_world_max_bodies(1024)
+    assert h.group_world_max_bodies() == 1024
+    k = GpuBatch(worlds)  # warps up to 32 bodies, groups up to 64, CTAs above; staged
+    k.set_warp_world_max_bodies(32)
+    k.set_group_world_max_bodies(64)
+    k.set_stage_bytes(2048 * 44)
     for i in range(90):
-        for g in (a, b, c, e, f):
+        for g in (a, b, c, e, f, h, k):
             g.step()
         if i == 40:  # switching schedule mid-run recaptures the step and changes nothing
             a.set_warp_world_max_bodies(64)
             e.set_stage_bytes(1024 * 44)
+            h.set_group_world_max_bodies(0)
+            a.set_group_world_max_bodies(256)
     ba = a.bodies()
-    for g in (b, c, e, f):
+    for g in (b, c, e, f, h, k):
         bg = g.bodies()
         np.testing.assert_array_equal(ba["pos"], bg["pos"])
         np.testing.assert_array_equal(ba["vel"], bg["vel"])
@@ -270,7 +280,8 @@ def test_autotune_keeps_results(gpu_lib):
     a, b = GpuBatch(worlds), GpuBatch(worlds)
     best = a.autotune(steps_per_candidate=2)
     assert best["sweeps"] in ("grid", "per_world") and best["step_ms"] > 0
-    n_cand = 1 + 3 * 5  # the grid, then 3 staging sizes x 5 warp-world limits
+    assert best["group_world_max_bodies"] in (0, 256, 512, 1024)
+    n_cand = 1 + 3 * 5 + 2 * 3  # the grid, 3 staging sizes x 5 warp-world limits, 2 x 3 group limits
     b.step_n(n_cand * 3)
     np.testing.assert_array_equal(a.bodies()["pos"], b.bodies()["pos"])
     np.testing.assert_array_equal(a.bodies()["vel"], b.bodies()["vel"])

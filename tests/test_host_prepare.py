@@ -73,7 +73,7 @@ def test_library_exports(lib):
     assert declared >= set(gpu.exported_symbols())
     for name in sorted(declared):
         assert hasattr(lib, name), name
-    assert lib.prgpu_abi_version() == 4
+    assert lib.prgpu_abi_version() == 5
 
 
 def test_convex_hull_matches_scene_builder(lib):
