@@ -201,6 +201,35 @@ def sweep_bytes(stats, conf, n_bodies_solved):
     return nc * per_contact + n_bodies_solved * 52
 
 
+def update_bytes(st, worlds) -> float:
+    """Algorithmic bytes of the post-solve contact maintenance phase: k_synchronize
+    (each shape's body and flags, both transforms and its box read, the moved flag
+    written: 60 B; its vertices read for the swept box: 12 + 16 nv B), then
+    k_update_contacts over the contacts of moved bodies (every live contact's flags
+    and body ids read: 12 B; each contact updated reads its proxy ids and old
+    manifold and writes the new manifold, flags and phase tag: 8 + 60 + 60 + 4 + 8
+    = 140 B; each shape's record and vertices read once more: 12 + 16 nv B, and
+    each body's transform and flags: 20 B)."""
+    n_shapes = sum(w.n_shapes for w in worlds)
+    n_verts = sum(int(w.shape_nv.sum()) for w in worlds)
+    n_bodies = sum(w.n_bodies for w in worlds)
+    shape_bytes = 12 * n_shapes + 16 * n_verts
+    return (60 * n_shapes + 2 * shape_bytes + 20 * n_bodies + 12 * st["liveContacts"]
+            + 140 * st["contactsUpdated"])
+
+
+def profile_figure(name: str, key: str):
+    """A figure (`key: value` line) of an ncu summary under profiles/."""
+    try:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
+            for line in f:
+                if line.startswith(key + ":"):
+                    return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 # prgpu_autotune times 22 candidate schedules (the grid-wide one, 3 staging sizes
 # x 5 warp-world limits, then 2 warp-world limits x 3 group-world limits), each
 # over one capturing step plus the steps asked for; those steps advance the batch
@@ -485,16 +514,13 @@ def run_ours(args, rank, world_size, local, dist):
     clocks = clk.summary()
     # DRAM bytes of one solver launch on this workload, from the ncu capture
     # summarised in profiles/ (a profiler run is never part of the bench)
-    traffic = None
-    try:
-        if args.workload != "batched" or args.worlds != 4096:
-            raise FileNotFoundError("the capture covers the default batch only")
-        with open(os.path.join(ROOT, "profiles", "k_world_solve_1024_full.md")) as f:
-            for line in f:
-                if line.startswith("dram_bytes_per_launch:"):
-                    traffic = float(line.split(":")[1])
-    except Exception:
-        pass
+    traffic = upd_traffic = None
+    if args.workload == "batched" and args.worlds == 4096:  # the captures cover the default batch only
+        traffic = profile_figure("k_world_solve_1024_full.md", "dram_bytes_per_launch")
+        upd_traffic = profile_figure("k_update_contacts_4096.md", "dram_bytes_per_phase")
+    upd_ms = statistics.mean(p["sync_update"] for p in phases)
+    bytes_upd = update_bytes(st, worlds)
+    achieved_upd = bytes_upd / (upd_ms / 1e3) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
@@ -519,6 +545,12 @@ def run_ours(args, rank, world_size, local, dist):
                                 if batch.sweep_mode() == "per_world" else
                                 "k_solve (Gauss-Seidel colour sweeps, cooperative grid)"),
                      "peak_source": peak_kind, "launch_ms": sweeps_ms, "algorithmic_bytes": bytes_sweep},
+        "update_roofline": {"bound": "hbm", "achieved": achieved_upd, "peak": peak, "unit": "GB/s",
+                            "frac": achieved_upd / peak, "traffic": upd_traffic,
+                            "kernel": "post-solve contact maintenance (k_synchronize, then k_update_contacts "
+                                      "over the contacts of moved bodies)",
+                            "peak_source": peak_kind, "phase_ms": upd_ms, "algorithmic_bytes": bytes_upd,
+                            "contacts_updated": st["contactsUpdated"]},
         "phase_ms": {k: statistics.mean(p[k] for p in phases) for k in phases[0]},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nb * 24, "d2h_bytes_per_step": nb * 24},

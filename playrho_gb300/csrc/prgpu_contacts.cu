@@ -80,16 +80,19 @@ __global__ void k_moved_done(DW d) {
     c->n_new = 0u;
 }
 
+// Each contact's update touches only its own slot, so the pass walks the slots
+// in ascending order (live ones by their flag) rather than the key-ordered live
+// list: the slot-indexed records are then read and written in coalesced runs.
 __global__ void k_update_contacts(DW d, uint32_t body_mask) {
     uint32_t updated = 0;
     // the post-solve pass of a recorded step notes each update's impulse sources
     int8_t* rec = (d.tape && body_mask == BF_MOVED) ? d.tape->src : nullptr;
-    GRID_LOOP(i, d.cnt->n_live) {
-        const uint32_t slot = d.c_slot[i];
-        const uint2 bd = d.cs_body[slot];
+    GRID_LOOP(slot, d.cnt->high_water) {
         const uint32_t f = d.cs_flags[slot];
+        if ((f & (CF_LIVE | CF_SENSOR)) != CF_LIVE) continue;
+        const uint2 bd = d.cs_body[slot];
         const bool need = (f & CF_NEEDS_UPDATE) || (d.b_flags[bd.x] & body_mask) || (d.b_flags[bd.y] & body_mask);
-        if (need && !(f & CF_SENSOR)) {
+        if (need) {
             update_contact<false>(d, slot, rec ? rec + 2 * (size_t)slot : nullptr);
             ++updated;
         }
@@ -100,10 +103,9 @@ __global__ void k_update_contacts(DW d, uint32_t body_mask) {
 // The sensor contacts of the same pass (TestOverlap instead of CollideShapes).
 __global__ void k_update_sensors(DW d, uint32_t body_mask) {
     uint32_t updated = 0;
-    GRID_LOOP(i, d.cnt->n_live) {
-        const uint32_t slot = d.c_slot[i];
+    GRID_LOOP(slot, d.cnt->high_water) {
         const uint32_t f = d.cs_flags[slot];
-        if (!(f & CF_SENSOR)) continue;
+        if ((f & (CF_LIVE | CF_SENSOR)) != (CF_LIVE | CF_SENSOR)) continue;
         const uint2 bd = d.cs_body[slot];
         if ((f & CF_NEEDS_UPDATE) || (d.b_flags[bd.x] & body_mask) || (d.b_flags[bd.y] & body_mask)) {
             update_contact<true>(d, slot);
@@ -557,7 +559,7 @@ void launch_set_upd_phase(const DW& d, uint32_t phase, cudaStream_t s) { k_set_u
 
 void launch_update_contacts(const DW& d, const Launch& L, uint32_t body_mask, cudaStream_t s) {
     k_update_contacts<<<L.grid, L.threads, 0, s>>>(d, body_mask);
-    k_update_sensors<<<L.grid, L.threads, 0, s>>>(d, body_mask);
+    if (L.sensors) k_update_sensors<<<L.grid, L.threads, 0, s>>>(d, body_mask);
 }
 
 void launch_find_contacts(const DW& d, const Launch& L, cudaStream_t s) {

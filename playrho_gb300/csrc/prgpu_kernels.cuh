@@ -14,6 +14,7 @@ struct Launch {
     int coop_threads;
     bool per_world;    // sweeps run one CTA per world (batches of many worlds)
     int world_grid;    // persistent CTAs of the per-world sweep kernel
+    bool sensors;      // the batch has sensor shapes (their update pass runs)
 };
 
 // contacts / broadphase (prgpu_contacts.cu)

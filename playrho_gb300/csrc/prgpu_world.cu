@@ -1279,6 +1279,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     ok &= up(b_shape_off, bs_off.data(), sizeof(uint32_t) * (N + 1));
     ok &= up(b_shapes, bs_idx.data(), sizeof(uint32_t) * S);
     ok &= up(d.s_meta, s_meta.data(), sizeof(uint32_t) * S);
+    w->L.sensors = std::any_of(s_meta.begin(), s_meta.end(), [](uint32_t m) { return (m & kShapeSensor) != 0u; });
     ok &= up(d.s_voff, s_voff.data(), sizeof(uint32_t) * S);
     ok &= up(d.s_radius, s_radius.data(), sizeof(float) * S);
     ok &= up(d.s_mat, s_mat.data(), sizeof(float2) * S);
