@@ -80,22 +80,85 @@ __global__ void k_moved_done(DW d) {
     c->n_new = 0u;
 }
 
+// Work class of a contact update: its shapes' vertex counts (1 a disk, 2 an
+// edge, up to 8 told apart, in either order) and whether it touched after its
+// last update, which decides whether the narrowphase stops after the
+// separation tests or goes on to clip a manifold.
+constexpr uint32_t kUpdClasses = 128;
+constexpr uint32_t kUpdThreads = 256;
+constexpr uint32_t kUpdPerThread = 4;
+constexpr uint32_t kUpdWindow = kUpdThreads * kUpdPerThread;
+__device__ __forceinline__ uint32_t update_class(const DW& d, uint32_t slot, uint32_t f) {
+    const uint2 pr = d.cs_proxy[slot];
+    const uint32_t na = min(max((d.s_meta[pr.x] >> 8) & 0xffu, 1u), 8u) - 1u;
+    const uint32_t nb = min(max((d.s_meta[pr.y] >> 8) & 0xffu, 1u), 8u) - 1u;
+    return ((f & CF_TOUCHING) ? 64u : 0u) | (min(na, nb) << 3) | max(na, nb);
+}
+
 // Each contact's update touches only its own slot, so the pass walks the slots
 // in ascending order (live ones by their flag) rather than the key-ordered live
-// list: the slot-indexed records are then read and written in coalesced runs.
-__global__ void k_update_contacts(DW d, uint32_t body_mask) {
+// list: the slot-indexed records are then read in coalesced runs.  A block takes
+// a window of kUpdWindow slots at a time, sorts the ones that need an update by
+// work class in shared memory (a counting sort) and deals the sorted list out in
+// runs of 32, so that a warp's lanes run the same narrowphase case, no lane
+// idles on a contact that needs no update, and each warp gets runs from all over
+// the list (the block waits for its slowest warp at the end of each window).
+__global__ void __launch_bounds__(kUpdThreads) k_update_contacts(DW d, uint32_t body_mask) {
+    __shared__ uint32_t s_at[kUpdClasses];            // per class: count, then first position
+    __shared__ uint32_t s_wsum[kUpdClasses / 32u];
+    __shared__ uint32_t s_slot[kUpdWindow];
     uint32_t updated = 0;
     // the post-solve pass of a recorded step notes each update's impulse sources
     int8_t* rec = (d.tape && body_mask == BF_MOVED) ? d.tape->src : nullptr;
-    GRID_LOOP(slot, d.cnt->high_water) {
-        const uint32_t f = d.cs_flags[slot];
-        if ((f & (CF_LIVE | CF_SENSOR)) != CF_LIVE) continue;
-        const uint2 bd = d.cs_body[slot];
-        const bool need = (f & CF_NEEDS_UPDATE) || (d.b_flags[bd.x] & body_mask) || (d.b_flags[bd.y] & body_mask);
-        if (need) {
-            update_contact<false>(d, slot, rec ? rec + 2 * (size_t)slot : nullptr);
+    const uint32_t hw = d.cnt->high_water, t = threadIdx.x, lane = t & 31u;
+    for (uint32_t base = blockIdx.x * kUpdWindow; base < hw; base += gridDim.x * kUpdWindow) {
+        if (t < kUpdClasses) s_at[t] = 0u;
+        __syncthreads();
+        uint32_t pick[kUpdPerThread];  // class << 16 | rank within the class, or kNone
+#pragma unroll
+        for (uint32_t k = 0; k < kUpdPerThread; ++k) {
+            const uint32_t slot = base + k * kUpdThreads + t;
+            pick[k] = kNone;
+            if (slot < hw) {
+                const uint32_t f = d.cs_flags[slot];
+                if ((f & (CF_LIVE | CF_SENSOR)) == CF_LIVE) {
+                    const uint2 bd = d.cs_body[slot];
+                    if ((f & CF_NEEDS_UPDATE) || (d.b_flags[bd.x] & body_mask) || (d.b_flags[bd.y] & body_mask)) {
+                        const uint32_t cls = update_class(d, slot, f);
+                        pick[k] = (cls << 16) | atomicAdd(&s_at[cls], 1u);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // exclusive scan of the class counts: warp scans, then the warps' totals
+        uint32_t cnt = 0u, incl = 0u;
+        if (t < kUpdClasses) {
+            cnt = incl = s_at[t];
+            for (uint32_t o = 1u; o < 32u; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31u) s_wsum[t >> 5] = incl;
+        }
+        __syncthreads();
+        uint32_t total = 0u, before = 0u;
+        for (uint32_t k = 0; k < kUpdClasses / 32u; ++k) {
+            if (k < (t >> 5)) before += s_wsum[k];
+            total += s_wsum[k];
+        }
+        if (t < kUpdClasses) s_at[t] = before + incl - cnt;
+        __syncthreads();
+#pragma unroll
+        for (uint32_t k = 0; k < kUpdPerThread; ++k)
+            if (pick[k] != kNone) s_slot[s_at[pick[k] >> 16] + (pick[k] & 0xffffu)] = base + k * kUpdThreads + t;
+        __syncthreads();
+        for (uint32_t e = t; e < total; e += kUpdThreads) {
+            const uint32_t sl = s_slot[e];
+            update_contact<false>(d, sl, rec ? rec + 2 * (size_t)sl : nullptr);
             ++updated;
         }
+        __syncthreads();  // s_at and s_slot are refilled for the next window
     }
     if (updated) atomicAdd(&d.cnt->st_contacts_updated, updated);
 }
@@ -558,7 +621,7 @@ __global__ void k_set_upd_phase(DW d, uint32_t phase) { d.cnt->upd_phase = phase
 void launch_set_upd_phase(const DW& d, uint32_t phase, cudaStream_t s) { k_set_upd_phase<<<1, 1, 0, s>>>(d, phase); }
 
 void launch_update_contacts(const DW& d, const Launch& L, uint32_t body_mask, cudaStream_t s) {
-    k_update_contacts<<<L.grid, L.threads, 0, s>>>(d, body_mask);
+    k_update_contacts<<<L.grid, kUpdThreads, 0, s>>>(d, body_mask);
     if (L.sensors) k_update_sensors<<<L.grid, L.threads, 0, s>>>(d, body_mask);
 }
 
