@@ -110,6 +110,10 @@ __global__ void __launch_bounds__(kUpdThreads) k_update_contacts(DW d, uint32_t 
     uint32_t updated = 0;
     // the post-solve pass of a recorded step notes each update's impulse sources
     int8_t* rec = (d.tape && body_mask == BF_MOVED) ? d.tape->src : nullptr;
+    // The pre-phase pass updates the contacts of bodies the host changed; a contact
+    // flagged CF_NEEDS_UPDATE at creation is updated there and then, so with no
+    // body changed there is nothing to do.
+    if (body_mask == BF_DIRTY && !d.cnt->dirty_any) return;
     const uint32_t hw = d.cnt->high_water, t = threadIdx.x, lane = t & 31u;
     for (uint32_t base = blockIdx.x * kUpdWindow; base < hw; base += gridDim.x * kUpdWindow) {
         if (t < kUpdClasses) s_at[t] = 0u;
@@ -165,6 +169,7 @@ __global__ void __launch_bounds__(kUpdThreads) k_update_contacts(DW d, uint32_t 
 
 // The sensor contacts of the same pass (TestOverlap instead of CollideShapes).
 __global__ void k_update_sensors(DW d, uint32_t body_mask) {
+    if (body_mask == BF_DIRTY && !d.cnt->dirty_any) return;
     uint32_t updated = 0;
     GRID_LOOP(slot, d.cnt->high_water) {
         const uint32_t f = d.cs_flags[slot];

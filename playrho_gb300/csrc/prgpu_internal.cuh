@@ -164,6 +164,7 @@ struct Counters {
     uint32_t wait_limit;      // spins a grid-barrier wait may take (0: the default, 2^24)
     uint32_t sub_stepping;    // SetSubStepping: the TOI phase stops after one event per world
     uint32_t upd_phase;       // phase bit the contact updates are tagged with (kUpd*)
+    uint32_t dirty_any;       // some body carries BF_DIRTY (host-set state since the last step)
     // StepStats counters (StepStats.hpp)
     uint32_t st_contacts_added;
     uint32_t st_contacts_destroyed;

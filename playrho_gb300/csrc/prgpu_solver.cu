@@ -1915,18 +1915,20 @@ __device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefe
 
 // ---- per-constraint sweep steps (t = position in sweep order) -------------------
 // When the step is recorded for the adjoint (d.tape), each contact step also
-// writes the body state (and impulses) it starts from.
-template <class BS>
+// writes the body state (and impulses) it starts from.  kFull false: the caller
+// guarantees a step without joints or recording, and their code stays out of the
+// kernel (its registers would cost the contact sweeps).
+template <bool kFull = true, class BS>
 __device__ __forceinline__ void sweep_warm(const DW& d, const BS& bs, uint32_t t) {
     const uint32_t id = d.t_id[t];
-    if (id & kJointBit) {
+    if (kFull && (id & kJointBit)) {
         const uint32_t j = id & ~kJointBit;
         if (d.tape) tape_joint_warm(d, t, j, bs.vel(d.j_bodies[2 * j]), bs.vel(d.j_bodies[2 * j + 1]));
         joint_init_velocity(d, bs, j);
         if (d.tape) tape_joint_check(d, j);
     } else if (d.conf->doWarmStart) {
         const VC vc = load_vc(d, t);
-        if (d.tape) {
+        if (kFull && d.tape) {
             d.tape->warm[2 * (size_t)t] = bs.vel(vc.bA);
             d.tape->warm[2 * (size_t)t + 1] = bs.vel(vc.bB);
         }
@@ -1934,10 +1936,10 @@ __device__ __forceinline__ void sweep_warm(const DW& d, const BS& bs, uint32_t t
     }
 }
 
-template <class BS>
+template <bool kFull = true, class BS>
 __device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32_t t, int it) {
     const uint32_t id = d.t_id[t];
-    if (id & kJointBit) {
+    if (kFull && (id & kJointBit)) {
         const uint32_t j = id & ~kJointBit;
         if (d.tape) {
             float4* r = d.tape->vel + 3 * ((size_t)it * d.tape->kcap + t);
@@ -1949,7 +1951,7 @@ __device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32
         joint_solve_velocity(d, bs, j);
     } else {
         VC vc = load_vc(d, t);
-        if (d.tape) {
+        if (kFull && d.tape) {
             float4* r = d.tape->vel + 3 * ((size_t)it * d.tape->kcap + t);
             r[0] = bs.vel(vc.bA);
             r[1] = bs.vel(vc.bB);
@@ -1960,10 +1962,10 @@ __device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32
     }
 }
 
-template <class BS>
+template <bool kFull = true, class BS>
 __device__ __forceinline__ void sweep_position(const DW& d, const BS& bs, uint32_t t, int it) {
     const uint32_t id = d.t_id[t];
-    if (id & kJointBit) {
+    if (kFull && (id & kJointBit)) {
         const uint32_t j = id & ~kJointBit;
         const uint32_t L = joint_island(d, j);
         const bool done = bs.island_done(L, it);
@@ -1979,7 +1981,7 @@ __device__ __forceinline__ void sweep_position(const DW& d, const BS& bs, uint32
     } else {
         const PC pc = d.pc[t];
         const bool done = bs.island_done(pc.island, it);
-        if (d.tape) {
+        if (kFull && d.tape) {
             float4* r = d.tape->pos + 2 * ((size_t)it * d.tape->kcap + t);
             float4 a = bs.pos(pc.bA);
             a.w = done ? 0.f : 1.f;
@@ -2147,7 +2149,7 @@ struct SubGroup {
 // The sweeps of one world by one group, over its segment [base, base + n) of
 // sweep order with colour offsets col_off; after_position(it) runs after each
 // position iteration.
-template <class G, class BS, class F>
+template <bool kFull, class G, class BS, class F>
 __device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uint32_t size, uint32_t base,
                        uint32_t n, const uint32_t* col_off, F&& after_position) {
     const DConf& c = *d.conf;
@@ -2187,15 +2189,15 @@ __device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uin
         if (serial) sweep(kSerialColour, f);
     };
     if (n) {
-        pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_warm(d, bs, t); });
+        pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_warm<kFull>(d, bs, t); });
         for (int it = 0; it < c.regVelocityIters; ++it)
-            pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_velocity(d, bs, t, it); });
+            pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_velocity<kFull>(d, bs, t, it); });
     }
     for (uint32_t b = d.w_body_off[w] + rank; b < d.w_body_off[w + 1]; b += size) integrate_body(d, bs, b);
     G::sync();
     if (n) {
         for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it) {
-            pass(d.pc, sizeof(PC), [&](uint32_t t) { sweep_position(d, bs, t, it); });
+            pass(d.pc, sizeof(PC), [&](uint32_t t) { sweep_position<kFull>(d, bs, t, it); });
             after_position(it);
         }
         for (uint32_t t = base + rank; t < base + n; t += size) store_impulses(d, t);
@@ -2204,7 +2206,7 @@ __device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uin
 }
 
 // col_cnt / col_off: kColStride words of shared memory owned by the group.
-template <class G>
+template <class G, bool kFull>
 __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t size, uint32_t* col_cnt,
                             uint32_t* col_off, void* stage, uint32_t stage_cap) {
     const DConf& c = *d.conf;
@@ -2263,7 +2265,7 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
         for (uint32_t t = base + rank; t < base + n; t += size) build_constraint(d, t, d.k_order[t]);
         G::sync();
     }
-    if (d.tape) {  // recorded for the adjoint
+    if (kFull && d.tape) {  // recorded for the adjoint
         for (uint32_t t = base + rank; t < base + n; t += size) tape_constraint(d, t);
         tape_world(d, w, base, n, col_off, rank, size);
     }
@@ -2299,14 +2301,14 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
             }
             G::sync();
         };
-        sweeps<G>(d, bs, w, rank, size, base, n, col_off, island_pass);
+        sweeps<kFull, G>(d, bs, w, rank, size, base, n, col_off, island_pass);
         for (uint32_t i = rank; i < nb; i += size) {
             d.b_vel[b0 + i] = sv[i];
             d.b_pos1[b0 + i] = sp[i];
         }
     } else {
         const GlobalBodies bs{d};
-        sweeps<G>(d, bs, w, rank, size, base, n, col_off, [](int) {});
+        sweeps<kFull, G>(d, bs, w, rank, size, base, n, col_off, [](int) {});
     }
     G::sync();  // the group's shared words are reused by its next world
 }
@@ -2315,6 +2317,8 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
 // The first n_world_big entries are solved by a whole CTA each; once a CTA
 // meets a smaller world, each of its groups of kGroupThreads threads takes
 // worlds on its own up to n_world_mid, and then each of its warps.
+// kFull false: the instance for steps without joints or recording.
+template <bool kFull>
 __global__ void __launch_bounds__(256, 4) k_world_solve(DW d) {
     extern __shared__ float4 s_stage[];  // d.stage_bytes: body state of the world(s) being solved
     __shared__ uint32_t s_w;
@@ -2327,7 +2331,7 @@ __global__ void __launch_bounds__(256, 4) k_world_solve(DW d) {
         qi = s_w;
         if (qi >= d.n_worlds) return;
         if (qi >= d.n_world_big) break;
-        solve_world<BlockGroup>(d, d.w_order[qi], threadIdx.x, blockDim.x, s_col[0][0], s_col[0][1], s_stage,
+        solve_world<BlockGroup, kFull>(d, d.w_order[qi], threadIdx.x, blockDim.x, s_col[0][0], s_col[0][1], s_stage,
                                 d.stage_bytes / kStageBytesPerBody);
     }
     // each warp owns an eighth of the staging area, a group its warps' parts
@@ -2346,7 +2350,7 @@ __global__ void __launch_bounds__(256, 4) k_world_solve(DW d) {
         if (grp != 0) qi = gnext();  // group 0 keeps the entry the CTA took
         void* gstage = reinterpret_cast<char*>(s_stage) + (size_t)(grp * gwarps) * part;
         while (qi < d.n_world_mid) {
-            solve_world<SubGroup>(d, d.w_order[qi], grank, kGroupThreads, s_col[grp * gwarps][0],
+            solve_world<SubGroup, kFull>(d, d.w_order[qi], grank, kGroupThreads, s_col[grp * gwarps][0],
                                   s_col[grp * gwarps][1], gstage, gwarps * part / kStageBytesPerBody);
             qi = gnext();
         }
@@ -2361,7 +2365,7 @@ __global__ void __launch_bounds__(256, 4) k_world_solve(DW d) {
     // warp 0 (of the CTA, or of each group) keeps the entry its CTA or group took
     if ((d.n_world_mid > d.n_world_big) ? (warp % gwarps != 0) : (warp != 0)) qi = next();
     while (qi < d.n_worlds) {
-        solve_world<WarpGroup>(d, d.w_order[qi], lane, 32u, s_col[warp][0], s_col[warp][1], stage,
+        solve_world<WarpGroup, kFull>(d, d.w_order[qi], lane, 32u, s_col[warp][0], s_col[warp][1], stage,
                                part / kStageBytesPerBody);
         qi = next();
     }
@@ -2470,8 +2474,11 @@ __global__ void k_items_count(DW d, uint32_t* n_items) { *n_items = d.cnt->n_liv
 __global__ void k_inc_off_tail(DW d) { d.inc_off[d.n_bodies] = d.cnt->pad[3]; }
 
 __global__ void k_clear_dirty(DW d) {
+    if (!d.cnt->dirty_any) return;
     GRID_LOOP(b, d.n_bodies) d.b_flags[b] &= ~BF_DIRTY;
 }
+
+__global__ void k_dirty_done(DW d) { d.cnt->dirty_any = 0u; }
 
 template <typename K>
 void launch_coop(K kernel, const DW& d, const Launch& L, cudaStream_t s) {
@@ -2504,6 +2511,7 @@ void launch_reset_step(const DW& d, const Launch& L, cudaStream_t s) {
 
 void launch_clear_dirty(const DW& d, const Launch& L, cudaStream_t s) {
     k_clear_dirty<<<L.grid, L.threads, 0, s>>>(d);
+    k_dirty_done<<<1, 1, 0, s>>>(d);
 }
 
 void launch_islands_colour(const DW& d, const Launch& L, cudaStream_t s) {
@@ -2543,7 +2551,8 @@ void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) {
         return;
     }
     cudaMemsetAsync(&d.cnt->world_queue, 0, sizeof(uint32_t), s);
-    k_world_solve<<<L.world_grid, 256, d.stage_bytes, s>>>(d);
+    if (d.tape || d.n_joints) k_world_solve<true><<<L.world_grid, 256, d.stage_bytes, s>>>(d);
+    else k_world_solve<false><<<L.world_grid, 256, d.stage_bytes, s>>>(d);
 }
 
 int world_blocks_per_sm(uint32_t stage_bytes) {
@@ -2554,15 +2563,18 @@ int world_blocks_per_sm(uint32_t stage_bytes) {
     {
         std::lock_guard<std::mutex> lock(mu);
         if (stage_bytes > set_bytes) {
-            if (cudaFuncSetAttribute(k_world_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes) !=
-                cudaSuccess)
-                return 0;
+            for (auto k : {k_world_solve<true>, k_world_solve<false>})
+                if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes) !=
+                    cudaSuccess)
+                    return 0;
             set_bytes = stage_bytes;
         }
     }
-    int a = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_world_solve, 256, stage_bytes);
-    return a;
+    // both instances have the same launch bounds; the grid is sized for the smaller residency
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_world_solve<true>, 256, stage_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_world_solve<false>, 256, stage_bytes);
+    return a < b ? a : b;
 }
 
 void launch_post_record(const DW& d, const Launch& L, cudaStream_t s) { k_post_record<<<L.grid, L.threads, 0, s>>>(d); }

@@ -855,6 +855,7 @@ __global__ void k_apply_states(DW d, uint32_t first, uint32_t count, const float
                 const Xf xf = get_xf(x, y, a, mk(m.z, m.w));
                 d.b_xf[b] = make_float4(xf.p.x, xf.p.y, xf.q.x, xf.q.y);
                 f |= BF_DIRTY;
+                d.cnt->dirty_any = 1u;
             }
         }
         if (vel3 && is_speedable(f)) {
