@@ -231,10 +231,10 @@ def profile_figure(name: str, key: str):
 
 
 # prgpu_autotune times 22 candidate schedules (the grid-wide one, 3 staging sizes
-# x 5 warp-world limits, then 2 warp-world limits x 3 group-world limits), each
-# over one capturing step plus the steps asked for; those steps advance the batch
-# like any other.
-AUTOTUNE_CANDIDATES = 22
+# x 5 warp-world limits, then 2 warp-world limits x 3 group-world limits), then
+# the 3 fastest once more, each timing over one capturing step plus the steps
+# asked for; those steps advance the batch like any other.
+AUTOTUNE_CANDIDATES = 22 + 3
 AUTOTUNE_STEPS = 2
 
 

@@ -246,10 +246,12 @@ typedef struct prgpu_schedule {
     uint32_t group_world_max_bodies;  /* ABI 5 */
 } prgpu_schedule;
 /* Autotuner: times every candidate schedule over steps_per_candidate steps
- * (after one untimed step that captures it) and keeps the fastest.  The
- * schedules give identical results, so the only effect on the simulation is
- * that the world advances (1 + steps_per_candidate) steps per candidate, as
- * with prgpu_step_n.  No reference counterpart. */
+ * (after one untimed step that captures it), times the 3 fastest once more,
+ * and keeps the fastest (each candidate by its faster timing).  A batch of one
+ * world has 1 candidate, a batch of several 22 (25 timings).  The schedules give
+ * identical results, so the only effect on the simulation is that the world
+ * advances (1 + steps_per_candidate) steps per timing, as with prgpu_step_n.
+ * No reference counterpart. */
 int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_candidate, prgpu_schedule* best);
 /* StepAdjoint: gradients of a loss of the state after a window of steps with
  * respect to the state before it and to the shapes' friction.  No reference
