@@ -1568,11 +1568,11 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    size_t best = 0;
+    size_t fastest = 0;
     for (size_t i = 1; i < cands.size(); ++i)
-        if (ms[i] < ms[best]) best = i;
-    const Cand pick = cands[best];
-    const float best_ms = ms[best];
+        if (ms[i] < ms[fastest]) fastest = i;
+    const Cand pick = cands[fastest];
+    const float best_ms = ms[fastest];
     if ((rc = prgpu_set_sweep_mode(w, pick.mode)) != PRGPU_OK) return rc;
     if ((rc = prgpu_set_warp_world_max_bodies(w, pick.warp_max)) != PRGPU_OK) return rc;
     if ((rc = prgpu_set_group_world_max_bodies(w, pick.group_max)) != PRGPU_OK) return rc;
