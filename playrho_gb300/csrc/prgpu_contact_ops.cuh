@@ -13,12 +13,11 @@
 namespace prgpu {
 
 __device__ __forceinline__ void load_proxy(const DW& d, uint32_t p, Proxy& out) {
-    const uint32_t meta = d.s_meta[p];
-    const int nv = (int)((meta >> 8) & 0xffu);
-    const uint32_t voff = d.s_voff[p];
+    const uint4 rec = d.s_rec[p];
+    const int nv = (int)((rec.x >> 8) & 0xffu);
     out.count = nv < kMaxVerts ? nv : kMaxVerts;
-    out.r = d.s_radius[p];
-    out.vn = d.verts + voff;
+    out.r = __uint_as_float(rec.z);
+    out.vn = d.verts + rec.y;
 }
 
 __device__ __forceinline__ Xf load_xf(const DW& d, uint32_t b) {
@@ -74,16 +73,15 @@ __device__ __forceinline__ Box swept_aabb(const DW& d, uint32_t p, Xf x0, Xf x1)
     Box a;
     a.x0 = __int_as_float(0x7f800000); a.y0 = a.x0;
     a.x1 = -a.x0; a.y1 = -a.x0;
-    const uint32_t meta = d.s_meta[p];
-    const int nv = (int)((meta >> 8) & 0xffu);
-    const uint32_t voff = d.s_voff[p];
+    const uint4 rec = d.s_rec[p];
+    const int nv = (int)((rec.x >> 8) & 0xffu);
     for (int i = 0; i < nv; ++i) {
-        const float4 v = d.verts[voff + i];
+        const float4 v = d.verts[rec.y + i];
         const V2 lv = mk(v.x, v.y);
         box_include(a, xform(lv, x0));
         box_include(a, xform(lv, x1));
     }
-    box_fatten(a, d.s_radius[p]);
+    box_fatten(a, __uint_as_float(rec.z));
     return a;
 }
 

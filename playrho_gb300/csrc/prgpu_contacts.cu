@@ -90,8 +90,8 @@ constexpr uint32_t kUpdPerThread = 4;
 constexpr uint32_t kUpdWindow = kUpdThreads * kUpdPerThread;
 __device__ __forceinline__ uint32_t update_class(const DW& d, uint32_t slot, uint32_t f) {
     const uint2 pr = d.cs_proxy[slot];
-    const uint32_t na = min(max((d.s_meta[pr.x] >> 8) & 0xffu, 1u), 8u) - 1u;
-    const uint32_t nb = min(max((d.s_meta[pr.y] >> 8) & 0xffu, 1u), 8u) - 1u;
+    const uint32_t na = min(max((d.s_rec[pr.x].x >> 8) & 0xffu, 1u), 8u) - 1u;
+    const uint32_t nb = min(max((d.s_rec[pr.y].x >> 8) & 0xffu, 1u), 8u) - 1u;
     return ((f & CF_TOUCHING) ? 64u : 0u) | (min(na, nb) << 3) | max(na, nb);
 }
 

@@ -275,6 +275,7 @@ struct DW {
     uint32_t* s_meta;        // kind | nverts << 8
     uint32_t* s_voff;
     float* s_radius;
+    uint4* s_rec;            // meta, voff, radius (bits), body: the narrowphase's one 16-byte load
     float2* s_mat;           // friction restitution
     uint32_t* s_filter;      // category | mask << 16
     int32_t* s_group;        // group index; bit 30 = sensor

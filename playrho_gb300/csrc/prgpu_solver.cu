@@ -36,9 +36,28 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x) {
     return x;
 }
 
+// The root of x for the unions, halving the path on the way (each node visited
+// is pointed at its grandparent).  Only non-roots are written and a node stays a
+// non-root once hooked, so these plain stores never meet the hooking CAS on a
+// root; every value written is an ancestor in the same set (possibly a stale
+// one), so any interleaving ends with the same sets, and, hooking larger roots
+// under smaller ones, the same roots.  (The flattening pass writes each body's
+// root and must not race with such stores: it uses uf_find.)
+__device__ __forceinline__ uint32_t uf_find_halving(uint32_t* parent, uint32_t x) {
+    for (int g = 0; g < 1 << 20; ++g) {
+        const uint32_t p = __ldcg(&parent[x]);
+        if (p == x) return x;
+        const uint32_t gp = __ldcg(&parent[p]);
+        if (gp == p) return p;
+        __stcg(&parent[x], gp);
+        x = gp;
+    }
+    return x;
+}
+
 __device__ __forceinline__ void uf_union(uint32_t* parent, uint32_t a, uint32_t b, Counters* c) {
     for (int g = 0; g < 1 << 16; ++g) {
-        uint32_t ra = uf_find(parent, a), rb = uf_find(parent, b);
+        uint32_t ra = uf_find_halving(parent, a), rb = uf_find_halving(parent, b);
         if (ra == rb) return;
         if (ra < rb) { const uint32_t t = ra; ra = rb; rb = t; }
         // hook the larger root under the smaller one: labels end as component minima
@@ -57,17 +76,18 @@ __global__ void k_isl_init(DW d) {
 
 __device__ __forceinline__ bool island_edge_body(uint32_t f) { return is_speedable(f) && (f & BF_ENABLED); }
 
+// The contacts are taken by slot (a free slot's flags are 0, never solvable):
+// the union order does not change the components or their labels.
 __global__ void k_isl_union(DW d) {
-    const uint32_t nl = d.cnt->n_live;
-    GRID_LOOP(i, nl + d.n_joints) {
+    const uint32_t hw = d.cnt->high_water;
+    GRID_LOOP(i, hw + d.n_joints) {
         uint32_t a, b;
-        if (i < nl) {
-            const uint32_t slot = d.c_slot[i];
-            if (!contact_solvable(d.cs_flags[slot])) continue;
-            const uint2 bd = d.cs_body[slot];
+        if (i < hw) {
+            if (!contact_solvable(d.cs_flags[i])) continue;
+            const uint2 bd = d.cs_body[i];
             a = bd.x; b = bd.y;
         } else {
-            const uint32_t j = i - nl;
+            const uint32_t j = i - hw;
             a = d.j_bodies[2 * j]; b = d.j_bodies[2 * j + 1];
         }
         if (island_edge_body(d.b_flags[a]) && island_edge_body(d.b_flags[b])) uf_union(d.b_island, a, b, d.cnt);

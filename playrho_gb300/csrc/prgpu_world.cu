@@ -1134,7 +1134,8 @@ static int alloc_world(prgpu_world* w, const WorldDims& z) {
     d.b_shape_off = b_shape_off; d.b_shapes = b_shapes;
     AL(d.b_jnt_off, N + 1); AL(d.b_jnt_other, z.JO); AL(d.b_jnt_cc, z.JC);
     AL(d.isl_awake, N); ALS(d.isl_sep, (size_t)N * kMaxPosIters); ALS(d.isl_jok, (size_t)N * kMaxPosIters); AL(d.isl_uat, N);
-    AL(d.s_body, S); AL(d.s_meta, S); AL(d.s_voff, S); AL(d.s_radius, S); AL(d.s_mat, S); AL(d.s_filter, S);
+    AL(d.s_body, S); AL(d.s_meta, S); AL(d.s_voff, S); AL(d.s_radius, S); AL(d.s_rec, S); AL(d.s_mat, S);
+    AL(d.s_filter, S);
     AL(d.s_group, S); AL(d.verts, z.V); AL(d.p_aabb, S); AL(d.p_moved, S); AL(d.moved_list, S);
     AL(d.j_bodies, 2 * J); AL(d.j_anchor, J); AL(d.j_param, J); AL(d.j_maxtorque, J); AL(d.j_flags, J);
     float4* j_extra_d;
@@ -1283,6 +1284,15 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     w->L.sensors = std::any_of(s_meta.begin(), s_meta.end(), [](uint32_t m) { return (m & kShapeSensor) != 0u; });
     ok &= up(d.s_voff, s_voff.data(), sizeof(uint32_t) * S);
     ok &= up(d.s_radius, s_radius.data(), sizeof(float) * S);
+    {
+        std::vector<uint4> rec(S);
+        for (uint32_t p = 0; p < S; ++p) {
+            uint32_t r;
+            std::memcpy(&r, &s_radius[p], sizeof r);
+            rec[p] = make_uint4(s_meta[p], s_voff[p], r, s_body[p]);
+        }
+        ok &= up(d.s_rec, rec.data(), sizeof(uint4) * S);
+    }
     ok &= up(d.s_mat, s_mat.data(), sizeof(float2) * S);
     ok &= up(d.s_filter, s_filter.data(), sizeof(uint32_t) * S);
     ok &= up(d.s_group, s_group.data(), sizeof(int32_t) * S);
