@@ -340,15 +340,21 @@ __global__ void k_lbvh_internal(DW d) {
 
 __global__ void k_lbvh_leaves(DW d) {
     if (!d.cnt->need_find) return;
+    const bool rebuild = d.cnt->lbvh_rebuild != 0u;
     GRID_LOOP(k, d.n_shapes) {
-        d.l_leaf_box[k] = d.p_aabb[d.l_idx[k]];
-        if (k + 1 < d.n_shapes) d.l_visit[k] = 0u;  // refit counters (internal nodes)
+        const uint32_t p = d.l_idx[k];
+        d.l_leaf_box[k] = d.p_aabb[p];
+        if (rebuild) {
+            d.l_inv[p] = k;
+            if (k + 1 < d.n_shapes) d.l_visit[k] = 0u;  // refit counters (internal nodes)
+        }
     }
 }
 
-// Bottom-up refit: the second child to arrive at a node computes its box.
+// Bottom-up box computation of a rebuilt tree: the second child to arrive at a
+// node computes its box.
 __global__ void k_lbvh_refit(DW d) {
-    if (!d.cnt->need_find) return;
+    if (!d.cnt->need_find || !d.cnt->lbvh_rebuild) return;
     const uint32_t n = d.n_shapes;
     if (n < 2) return;
     GRID_LOOP(k, n) {
@@ -363,6 +369,57 @@ __global__ void k_lbvh_refit(DW d) {
             __threadfence();
             node = d.l_parent[node];
         }
+    }
+}
+
+__device__ __forceinline__ void atomic_min_box(float* a, float v) {
+    // ordered as signed integers when v >= 0, as unsigned (reversed) when v < 0
+    if (v >= 0.f) atomicMin(reinterpret_cast<int*>(a), __float_as_int(v));
+    else atomicMax(reinterpret_cast<unsigned int*>(a), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_box(float* a, float v) {
+    if (v >= 0.f) atomicMax(reinterpret_cast<int*>(a), __float_as_int(v));
+    else atomicMin(reinterpret_cast<unsigned int*>(a), __float_as_uint(v));
+}
+
+// Refit between rebuilds: only the proxies that moved have new boxes, so each
+// moved leaf widens its ancestors (atomic min/max per side) until one already
+// contains its box.  Node boxes then still contain every leaf below them, so a
+// search returns exactly the same pairs as over tight boxes; they only stay as
+// wide as the widest box seen since the rebuild.  An ancestor that contained the
+// box because another leaf widened it is widened above by that leaf's own walk,
+// and boxes are convex, so every ancestor ends up containing every moved leaf.
+__global__ void k_lbvh_expand(DW d) {
+    if (!d.cnt->need_find || d.cnt->lbvh_rebuild) return;
+    const uint32_t n = d.n_shapes;
+    if (n < 2) return;
+    GRID_LOOP(m, d.cnt->n_moved) {
+        const uint32_t p = d.moved_list[m];
+        const float4 b = d.p_aabb[p];
+        uint32_t node = d.l_parent[(n - 1) + d.l_inv[p]];
+        for (int guard = 0; guard < 256 && node != kNone; ++guard) {
+            const float4 nb = __ldcg(&d.l_node_box[node]);
+            if (nb.x <= b.x && nb.y <= b.y && nb.z >= b.z && nb.w >= b.w) break;
+            float* f = reinterpret_cast<float*>(&d.l_node_box[node]);
+            if (b.x < nb.x) atomic_min_box(f + 0, b.x);
+            if (b.y < nb.y) atomic_min_box(f + 1, b.y);
+            if (b.z > nb.z) atomic_max_box(f + 2, b.z);
+            if (b.w > nb.w) atomic_max_box(f + 3, b.w);
+            node = d.l_parent[node];
+        }
+    }
+}
+
+// Row starts of the sorted live list by smaller proxy: c_first[p] is the first
+// entry whose key's smaller proxy is >= p (c_first[S] = n_live), so the live
+// contacts whose smaller proxy is p are the entries [c_first[p], c_first[p+1]).
+__global__ void k_contact_rows(DW d) {
+    if (!d.cnt->need_find) return;
+    const uint32_t nl = d.cnt->n_live, kb = d.key_bits, ns = d.n_shapes;
+    GRID_LOOP(i, nl + 1u) {
+        const uint32_t lo = (i < nl) ? (uint32_t)(d.c_key[i] >> kb) : ns;
+        const uint32_t from = (i > 0u) ? (uint32_t)(d.c_key[i - 1u] >> kb) + 1u : 0u;
+        for (uint32_t p = from; p <= lo && p <= ns; ++p) d.c_first[p] = i;
     }
 }
 
@@ -415,7 +472,6 @@ __device__ __forceinline__ uint32_t lower_bound_u64(const uint64_t* a, uint32_t 
 // FindContacts + the AddContacts filters for every moved proxy; keys of pairs
 // that pass and are not yet contacts are appended to n_key.
 __global__ void __launch_bounds__(128) k_find_pairs(DW d) {
-    const uint32_t n_live = d.cnt->n_live;
     const uint32_t kb = d.key_bits;
     GRID_LOOP(m, d.cnt->n_moved) {
         const uint32_t p = d.moved_list[m];
@@ -443,8 +499,13 @@ __global__ void __launch_bounds__(128) k_find_pairs(DW d) {
                     const uint32_t lo = min(p, q), hi = max(p, q);
                     if (!should_collide(d, lo, hi, d.s_body[lo], d.s_body[hi])) continue;
                     const uint64_t key = ((uint64_t)lo << kb) | (uint64_t)hi;
-                    const uint32_t at = lower_bound_u64(d.c_key, n_live, key);
-                    if (at < n_live && d.c_key[at] == key) continue;
+                    // already a contact: a short scan of lo's row of the live list
+                    bool live = false;
+                    for (uint32_t at = d.c_first[lo], end = d.c_first[lo + 1u]; at < end; ++at) {
+                        const uint64_t k2 = d.c_key[at];
+                        if (k2 >= key) { live = (k2 == key); break; }
+                    }
+                    if (live) continue;
                     cg::coalesced_group g = cg::coalesced_threads();
                     uint32_t base = 0;
                     if (g.thread_rank() == 0) base = atomicAdd(&d.cnt->n_new, g.size());
@@ -643,7 +704,9 @@ void launch_find_contacts(const DW& d, const Launch& L, cudaStream_t s) {
     k_lbvh_internal<<<L.grid, L.threads, 0, s>>>(d);
     k_lbvh_leaves<<<L.grid, L.threads, 0, s>>>(d);
     k_lbvh_refit<<<L.grid, L.threads, 0, s>>>(d);
+    k_lbvh_expand<<<L.grid, L.threads, 0, s>>>(d);
     k_lbvh_roots<<<L.grid, L.threads, 0, s>>>(d);
+    k_contact_rows<<<L.grid, L.threads, 0, s>>>(d);
     // query moved proxies, filter, sort the new keys, create and merge
     k_find_pairs<<<L.grid * 2, 128, 0, s>>>(d);
     k_pairs_done<<<1, 1, 0, s>>>(d);

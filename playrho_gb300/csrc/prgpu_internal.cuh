@@ -344,6 +344,8 @@ struct DW {
     uint32_t* l_parent;      // [2S]: internal i at i, leaf k at S + k
     uint32_t* l_range;       // [2*(S-1)] first last
     uint32_t* l_visit;
+    uint32_t* l_inv;         // [S] leaf of each proxy (written when the tree is rebuilt)
+    uint32_t* c_first;       // [S+1] first live-list entry whose smaller proxy is >= p (each search)
     // constraints of this step
     uint32_t* k_list;        // active constraint ids (slot for contacts, joint id + J flag)
     uint32_t* k_colour;

@@ -1153,7 +1153,7 @@ static int alloc_world(prgpu_world* w, const WorldDims& z) {
     ALS(d.n_key, K); ALS(d.n_key_alt, K); ALS(d.n_val, K); ALS(d.n_val_alt, K);
     AL(d.l_key, S); AL(d.l_key_alt, S); AL(d.l_idx, S); AL(d.l_idx_alt, S); AL(d.l_leaf_box, S);
     AL(d.l_node_box, S); AL(d.l_left, S); AL(d.l_right, S); AL(d.l_parent, 2 * (size_t)S); AL(d.l_range, 2 * (size_t)S);
-    AL(d.l_visit, S);
+    AL(d.l_visit, S); AL(d.l_inv, S); ALS(d.c_first, (size_t)S + 1);
     ALS(d.k_list, C + J); ALS(d.k_colour, C + J); ALS(d.k_tent, C + J); ALS(d.k_order, C + J);
     ALS(d.t_id, C + J);
     ALS(d.k_prio, C + J);
