@@ -12,6 +12,7 @@ namespace prgpu {
 namespace {
 
 constexpr int kScanThreads = 256;
+constexpr uint32_t kScanItems = 8;
 constexpr int kSortThreads = 256;
 constexpr int kRadix = 256;
 
@@ -53,8 +54,18 @@ __global__ void k_scan_reduce(const uint32_t* __restrict__ in, const uint32_t* n
     __shared__ uint32_t s[32];
     uint32_t lo, hi;
     chunk_of(*n_ptr, lo, hi);
-    uint32_t sum = 0;
-    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) sum += in[i];
+    // four independent loads in flight per thread
+    uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    const uint32_t step = blockDim.x;
+    uint32_t i = lo + threadIdx.x;
+    for (; i + 3u * step < hi; i += 4u * step) {
+        s0 += in[i];
+        s1 += in[i + step];
+        s2 += in[i + 2u * step];
+        s3 += in[i + 3u * step];
+    }
+    for (; i < hi; i += step) s0 += in[i];
+    uint32_t sum = (s0 + s1) + (s2 + s3);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
     if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = sum;
@@ -99,13 +110,25 @@ __global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restric
     __shared__ uint32_t s_warp[32];
     uint32_t lo, hi;
     chunk_of(*n_ptr, lo, hi);
+    // kScanItems consecutive elements per thread: one block scan per
+    // kScanItems * blockDim elements
     uint32_t running = partial[blockIdx.x];
-    for (uint32_t base = lo; base < hi; base += blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
-        const uint32_t v = (i < hi) ? in[i] : 0u;
+    for (uint32_t base = lo; base < hi; base += blockDim.x * kScanItems) {
+        const uint32_t i0 = base + threadIdx.x * kScanItems;
+        uint32_t v[kScanItems];
+        uint32_t sum = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < kScanItems; ++j) {
+            v[j] = (i0 + j < hi) ? in[i0 + j] : 0u;
+            sum += v[j];
+        }
         uint32_t tot;
-        const uint32_t incl = block_inclusive_scan(v, s_warp, tot);
-        if (i < hi) out[i] = running + incl - v;
+        uint32_t r = running + block_inclusive_scan(sum, s_warp, tot) - sum;
+#pragma unroll
+        for (uint32_t j = 0; j < kScanItems; ++j) {
+            if (i0 + j < hi) out[i0 + j] = r;
+            r += v[j];
+        }
         running += tot;
     }
 }
