@@ -20,8 +20,12 @@ LIB = os.path.join(HERE, "libprgpu.so")
 # C++ host layer over the C ABI (HostWorld), a second library linked to the first
 HOST_SOURCES = [os.path.join(HERE, "host", "host_world.cpp")]
 HOST_LIB = os.path.join(HERE, "libprgpu_host.so")
-SOURCES = ["prgpu_prims.cu", "prgpu_contacts.cu", "prgpu_solver.cu", "prgpu_toi.cu", "prgpu_world.cu", "prgpu_query.cu",
-           "prgpu_adjoint.cu"]
+# longest compiles first; prgpu_solver_full.cu and prgpu_solver_lean.cu each
+# compile one k_world_solve instance out of prgpu_solver.cu
+SOURCES = ["prgpu_solver_full.cu", "prgpu_solver_lean.cu", "prgpu_solver.cu", "prgpu_adjoint.cu", "prgpu_toi.cu",
+           "prgpu_contacts.cu", "prgpu_world.cu", "prgpu_prims.cu", "prgpu_query.cu"]
+# files that include another .cu
+CU_DEPS = {"prgpu_solver_full.cu": ["prgpu_solver.cu"], "prgpu_solver_lean.cu": ["prgpu_solver.cu"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(HERE, "..", "include")]
@@ -51,7 +55,8 @@ def build(verbose: bool = False, extra_flags=None) -> str:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(o)
-        if _stale(o, [s, __file__] + headers):
+        deps = [s, __file__] + headers + [os.path.join(CSRC, x) for x in CU_DEPS.get(src, [])]
+        if _stale(o, deps):
             jobs.append([nvcc(), *ARCH, *flags, "-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         for cmd, res in zip(jobs, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs)):

@@ -13,6 +13,16 @@
 //  * sleep follows UpdateUnderActiveTimes / Sleepem (:403-429).
 // The velocity loop's early exit (regMinMomentum) only stops iterations that
 // change nothing, so every island runs regVelocityIters sweeps.
+//
+// PRGPU_SOLVER_PART selects what a translation unit compiles, so that the two
+// k_world_solve instances (by far the longest to compile) build in parallel
+// with the rest: 0 (this file) everything but k_world_solve; 1 and 2
+// (prgpu_solver_full.cu, prgpu_solver_lean.cu) k_world_solve<true> and
+// k_world_solve<false> with their launch helpers.
+#ifndef PRGPU_SOLVER_PART
+#define PRGPU_SOLVER_PART 0
+#endif
+
 #include <cooperative_groups.h>
 
 #include <mutex>
@@ -66,6 +76,7 @@ __device__ __forceinline__ void uf_union(uint32_t* parent, uint32_t a, uint32_t 
     set_error(c, PR_ETIMEOUT, 20u);
 }
 
+#if PRGPU_SOLVER_PART == 0
 __global__ void k_isl_init(DW d) {
     GRID_LOOP(b, d.n_bodies) {
         d.b_island[b] = b;
@@ -165,8 +176,10 @@ __global__ void k_body_begin(DW d) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&d.cnt->body_steps), (unsigned long long)solved);
     }
 }
+#endif
 
 // ---- active constraints and colouring ---------------------------------------
+#if PRGPU_SOLVER_PART == 0
 __global__ void k_active_flags(DW d) {
     const uint32_t nl = d.cnt->n_live;
     GRID_LOOP(i, nl + d.n_joints) {
@@ -206,6 +219,7 @@ __global__ void k_active_done(DW d, uint32_t* n_bodies_count) {
     for (int k = 0; k < kSerialColour + 2; ++k) { c->colour_cnt[k] = 0u; c->colour_off[k] = 0u; }
     *n_bodies_count = d.n_bodies;
 }
+#endif
 
 __device__ __forceinline__ void constraint_bodies(const DW& d, uint32_t id, uint32_t& a, uint32_t& b) {
     if (id & kJointBit) {
@@ -238,6 +252,7 @@ __device__ __forceinline__ int constraint_body_set(const DW& d, uint32_t id, uin
     return n;
 }
 
+#if PRGPU_SOLVER_PART == 0
 // Colouring resources are the dynamic bodies: only they change under a constraint.
 __global__ void k_inc_count(DW d) {
     GRID_LOOP(k, d.cnt->n_active) {
@@ -257,6 +272,7 @@ __global__ void k_inc_fill(DW d) {
             if (is_accelerable(d.b_flags[bs[e]])) d.inc_list[d.inc_off[bs[e]] + atomicAdd(&d.inc_cur[bs[e]], 1u)] = k;
     }
 }
+#endif
 
 // Speculative greedy colouring (Gebremedhin-Manne style), deterministic:
 // each round every uncoloured constraint picks the lowest colour unused by its
@@ -367,6 +383,7 @@ __device__ __forceinline__ bool colour_keep(const DW& d, uint32_t k) {
     return false;
 }
 
+#if PRGPU_SOLVER_PART == 0
 __global__ void k_colour(DW d) {
     const uint32_t n = d.cnt->n_active;
     uint32_t* rem = &d.cnt->pad[4];  // triple-buffered per-round counters
@@ -416,6 +433,7 @@ __global__ void k_colour(DW d) {
         if (hi > lo) sort_serial(d.k_order + lo, hi - lo);
     }
 }
+#endif
 
 // ---- constraint construction --------------------------------------------------
 // GetWorldManifold (WorldManifold.cpp:111-132), VelocityConstraint ctor +
@@ -488,10 +506,12 @@ __device__ void build_constraint(const DW& d, uint32_t t, uint32_t k) {
     d.pc[t] = pcs;
 }
 
+#if PRGPU_SOLVER_PART == 0
 // Constraints are stored in sweep order: position t of k_order.
 __global__ void k_build_constraints(DW d) {
     GRID_LOOP(t, d.cnt->n_active) build_constraint(d, t, d.k_order[t]);
 }
+#endif
 
 // Per-constraint solver steps: prgpu_csolve.cuh.
 
@@ -1818,7 +1838,7 @@ __device__ bool gear_solve_position(const DW& d, const BS& bs, uint32_t j) {
 
 // Joint dispatch on the kind (the JointConf visitors of Joint.cpp).
 template <class BS>
-__device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
+__device__ __noinline__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
     switch (joint_kind(d, j)) {
     case JK_DISTANCE: distance_init_velocity(d, bs, j, false); break;
     case JK_ROPE: distance_init_velocity(d, bs, j, true); break;
@@ -1834,7 +1854,7 @@ __device__ void joint_init_velocity(const DW& d, const BS& bs, uint32_t j) {
     }
 }
 template <class BS>
-__device__ void joint_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
+__device__ __noinline__ void joint_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
     switch (joint_kind(d, j)) {
     case JK_DISTANCE: distance_solve_velocity(d, bs, j, false); break;
     case JK_ROPE: distance_solve_velocity(d, bs, j, true); break;
@@ -1851,7 +1871,7 @@ __device__ void joint_solve_velocity(const DW& d, const BS& bs, uint32_t j) {
 }
 // Returns whether the joint is within tolerance.
 template <class BS>
-__device__ bool joint_solve_position(const DW& d, const BS& bs, uint32_t j) {
+__device__ __noinline__ bool joint_solve_position(const DW& d, const BS& bs, uint32_t j) {
     switch (joint_kind(d, j)) {
     case JK_DISTANCE: return distance_solve_position(d, bs, j, false);
     case JK_ROPE: return distance_solve_position(d, bs, j, true);
@@ -2031,6 +2051,7 @@ __device__ __forceinline__ void store_impulses(const DW& d, uint32_t t) {
     }
 }
 
+#if PRGPU_SOLVER_PART == 0
 // Solve records for the PostSolveContact replay (Report, AabbTreeWorld.cpp:
 // 196-205, called at :1669-1672): each solved contact's velocity-constraint
 // impulses (GetContactImpulses: the points left after conditioning) and the
@@ -2056,6 +2077,7 @@ __global__ void k_post_record(DW d) {
         d.cs_post_tag[slot] = make_uint2(step, count | (iter << 8));
     }
 }
+#endif
 
 // IntegratePositions (AabbTreeWorld.cpp:176-188)
 template <class BS>
@@ -2069,6 +2091,7 @@ __device__ __forceinline__ void integrate_body(const DW& d, const BS& bs, uint32
     bs.set_pos(b, p);
 }
 
+#if PRGPU_SOLVER_PART == 0
 // The whole regular-phase solve of a step over the batch: warm start, velocity
 // sweeps, position integration, position sweeps, impulse store.  One
 // cooperative launch; a bounded grid barrier separates colours; the serial
@@ -2100,6 +2123,7 @@ __global__ void k_solve(DW d) {
         for (uint32_t col = 0; col <= ncol; ++col) sweep(col, [&](uint32_t t) { sweep_position(d, bs, t, it); });
     GRID_LOOP(t, d.cnt->n_active) store_impulses(d, t);
 }
+#endif
 
 // ---- one group of threads per world --------------------------------------------
 // For batches of many worlds, a CTA (large worlds) or a warp (small ones) does
@@ -2116,6 +2140,7 @@ __device__ __forceinline__ uint32_t constraint_world(const DW& d, uint32_t id) {
     return d.b_world[a];
 }
 
+#if PRGPU_SOLVER_PART == 0
 __global__ void k_world_ranges(DW d) {
     const uint32_t nc = d.cnt->n_active_c, na = d.cnt->n_active;
     GRID_LOOP(w, d.n_worlds + 1) {
@@ -2133,6 +2158,7 @@ __global__ void k_world_ranges(DW d) {
         d.w_kj[w] = lo;
     }
 }
+#endif
 
 struct BlockGroup {
     __device__ __forceinline__ static void sync() { __syncthreads(); }
@@ -2333,6 +2359,7 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
     G::sync();  // the group's shared words are reused by its next world
 }
 
+#if PRGPU_SOLVER_PART != 0
 // Persistent CTAs take worlds from a queue ordered by decreasing body count.
 // The first n_world_big entries are solved by a whole CTA each; once a CTA
 // meets a smaller world, each of its groups of kGroupThreads threads takes
@@ -2390,7 +2417,9 @@ __global__ void __launch_bounds__(256, 4) k_world_solve(DW d) {
         qi = next();
     }
 }
+#endif
 
+#if PRGPU_SOLVER_PART == 0
 // Write-back bookkeeping, transforms and under-active times
 // (AabbTreeWorld.cpp:1652-1679, :403-417).
 __global__ void k_body_end(DW d) {
@@ -2515,8 +2544,10 @@ void launch_coop(K kernel, const DW& d, const Launch& L, cudaStream_t s) {
     cudaLaunchKernelEx(&cfg, kernel, d);
 }
 
+#endif
 }  // namespace
 
+#if PRGPU_SOLVER_PART == 0
 int coop_blocks_per_sm(int threads) {
     int a = 0, b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_solve, threads, 0);
@@ -2571,8 +2602,8 @@ void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) {
         return;
     }
     cudaMemsetAsync(&d.cnt->world_queue, 0, sizeof(uint32_t), s);
-    if (d.tape || d.n_joints) k_world_solve<true><<<L.world_grid, 256, d.stage_bytes, s>>>(d);
-    else k_world_solve<false><<<L.world_grid, 256, d.stage_bytes, s>>>(d);
+    if (d.tape || d.n_joints) world_solve_full_launch(d, (unsigned)L.world_grid, s);
+    else world_solve_lean_launch(d, (unsigned)L.world_grid, s);
 }
 
 int world_blocks_per_sm(uint32_t stage_bytes) {
@@ -2583,17 +2614,12 @@ int world_blocks_per_sm(uint32_t stage_bytes) {
     {
         std::lock_guard<std::mutex> lock(mu);
         if (stage_bytes > set_bytes) {
-            for (auto k : {k_world_solve<true>, k_world_solve<false>})
-                if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes) !=
-                    cudaSuccess)
-                    return 0;
+            if (!world_solve_full_allow_smem(stage_bytes) || !world_solve_lean_allow_smem(stage_bytes)) return 0;
             set_bytes = stage_bytes;
         }
     }
     // both instances have the same launch bounds; the grid is sized for the smaller residency
-    int a = 0, b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_world_solve<true>, 256, stage_bytes);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_world_solve<false>, 256, stage_bytes);
+    const int a = world_solve_full_blocks_per_sm(stage_bytes), b = world_solve_lean_blocks_per_sm(stage_bytes);
     return a < b ? a : b;
 }
 
@@ -2610,5 +2636,31 @@ void launch_solve(const DW& d, const Launch& L, cudaStream_t s) {
     launch_solve_sweeps(d, L, s);
     launch_solve_finish(d, L, s);
 }
+#else
+// The one k_world_solve instance this translation unit compiles, and its launch
+// helpers (declared in prgpu_kernels.cuh).
+#if PRGPU_SOLVER_PART == 1
+#define PRGPU_WS_FULL true
+#define PRGPU_WS_NAME(x) world_solve_full_##x
+#else
+#define PRGPU_WS_FULL false
+#define PRGPU_WS_NAME(x) world_solve_lean_##x
+#endif
+
+void PRGPU_WS_NAME(launch)(const DW& d, unsigned grid, cudaStream_t s) {
+    k_world_solve<PRGPU_WS_FULL><<<grid, 256, d.stage_bytes, s>>>(d);
+}
+
+bool PRGPU_WS_NAME(allow_smem)(uint32_t stage_bytes) {
+    return cudaFuncSetAttribute(k_world_solve<PRGPU_WS_FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)stage_bytes) == cudaSuccess;
+}
+
+int PRGPU_WS_NAME(blocks_per_sm)(uint32_t stage_bytes) {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_world_solve<PRGPU_WS_FULL>, 256, stage_bytes);
+    return n;
+}
+#endif
 
 }  // namespace prgpu
