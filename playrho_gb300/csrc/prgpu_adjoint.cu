@@ -200,15 +200,53 @@ __device__ void moving_points_tan(const DW& d, const StepTape* tp, const PC& pc,
     }
 }
 
-// Reverse: pb (x y angle of A, then B) += J^T lb, J the local points' Jacobian,
-// one column per position coordinate.
+// Reverse: pb (x y angle of A, then B) += J^T lb, J the local points' Jacobian.
+// In the incident frame the clipped point is a + f (b - a) (clip_point_t with
+// the incident transformation taken out), so only the scalar
+// f = da / (da - db) moves, da and db being the side plane's signed distances
+// N.(Aw - Vw) and N.(Bw - Vw) of the incident edge's world points Aw, Bw, with
+// Vw the plane's world vertex and N = +-R_r e its normal.  The adjoint of f is
+// lb.(b - a); with rp(v) = (-v.y, v.x), d/d(angle) of a rotated vector R v is
+// rp(R v), so:
+//   incident centre  (da_bar + db_bar) N
+//   incident angle   da_bar N.rp(Aw - Pi) + db_bar N.rp(Bw - Pi)
+//   reference centre -(da_bar + db_bar) N
+//   reference angle  da_bar (rp(N).(Aw - Vw) - N.rp(Vw - Pr)) + db_bar (rp(N).(Bw - Vw) - N.rp(Vw - Pr))
+// (Pi, Pr the bodies' centres), in float: one pass instead of a forward-mode
+// evaluation per position coordinate.  moving_points_tan keeps the FP64 form
+// for the tangent that checks this.
 __device__ void moving_points_vjp(const DW& d, const StepTape* tp, const PC& pc, const MovingPoints& m,
                                   const float* lb, float* pb) {
-    for (int q = 0; q < 6; ++q) {
-        double u[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, col[4];
-        u[q] = 1.0;
-        moving_points_tan(d, tp, pc, m, u, u + 3, col);
-        pb[q] += (float)(col[0] * lb[0] + col[1] * lb[1] + col[2] * lb[2] + col[3] * lb[3]);
+    const float4 pa = tp->p0[pc.bA], pbb = tp->p0[pc.bB];
+    const float4 ma = d.b_mass[pc.bA], mb = d.b_mass[pc.bB];
+    const Xf xfA = get_xf(pa.x, pa.y, pa.z, mk(ma.z, ma.w)), xfB = get_xf(pbb.x, pbb.y, pbb.z, mk(mb.z, mb.w));
+    const Xf& xr = m.flipped ? xfB : xfA;
+    const Xf& xi = m.flipped ? xfA : xfB;
+    const V2 Pr = m.flipped ? mk(pbb.x, pbb.y) : mk(pa.x, pa.y);
+    const V2 Pi = m.flipped ? mk(pa.x, pa.y) : mk(pbb.x, pbb.y);
+    float* gr = m.flipped ? pb + 3 : pb;  // reference body's x y angle
+    float* gi = m.flipped ? pb : pb + 3;  // incident body's
+    const V2 Aw = rotate(m.a, xi.q) + xi.p, Bw = rotate(m.b, xi.q) + xi.p;
+    const V2 E = rotate(m.e, xr.q);
+    const V2 ba = m.b - m.a;
+    for (int k = 0; k < m.n; ++k) {
+        const V2 N = m.side1[k] ? E : mk(-E.x, -E.y);
+        const V2 Vw = rotate(m.vs[k], xr.q) + xr.p;
+        const V2 u = Aw - Vw, w = Bw - Vw;
+        const float da = dot(N, u), db = dot(N, w), den = da - db;
+        if (den == 0.f) continue;  // no crossing: ClipSegmentToLine made no point here
+        const int i = m.idx[k];
+        const float fbar = lb[2 * i] * ba.x + lb[2 * i + 1] * ba.y;
+        const float den2 = den * den;
+        const float dab = -fbar * db / den2, dbb = fbar * da / den2;
+        const float s = dab + dbb;
+        const V2 rN = revperp(N), rV = revperp(Vw - Pr);
+        gi[0] += s * N.x;
+        gi[1] += s * N.y;
+        gi[2] += dab * dot(N, revperp(Aw - Pi)) + dbb * dot(N, revperp(Bw - Pi));
+        gr[0] -= s * N.x;
+        gr[1] -= s * N.y;
+        gr[2] += dab * (dot(rN, u) - dot(N, rV)) + dbb * (dot(rN, w) - dot(N, rV));
     }
 }
 
