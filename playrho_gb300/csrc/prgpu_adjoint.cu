@@ -212,41 +212,52 @@ __device__ void moving_points_tan(const DW& d, const StepTape* tp, const PC& pc,
 //   incident angle   da_bar N.rp(Aw - Pi) + db_bar N.rp(Bw - Pi)
 //   reference centre -(da_bar + db_bar) N
 //   reference angle  da_bar (rp(N).(Aw - Vw) - N.rp(Vw - Pr)) + db_bar (rp(N).(Bw - Vw) - N.rp(Vw - Pr))
-// (Pi, Pr the bodies' centres), in float: one pass instead of a forward-mode
-// evaluation per position coordinate.  moving_points_tan keeps the FP64 form
-// for the tangent that checks this.
+// (Pi, Pr the bodies' centres).  One pass instead of a forward-mode evaluation
+// per position coordinate.  The distances are small differences of world
+// coordinates, so the pass runs in FP64 from each body's (float) rotation;
+// moving_points_tan keeps the forward-mode form for the tangent that checks it.
 __device__ void moving_points_vjp(const DW& d, const StepTape* tp, const PC& pc, const MovingPoints& m,
                                   const float* lb, float* pb) {
+    struct D2 { double x, y; };
+    auto sub2 = [](D2 u, D2 v) { return D2{u.x - v.x, u.y - v.y}; };
+    auto dot2 = [](D2 u, D2 v) { return u.x * v.x + u.y * v.y; };
+    auto rp2 = [](D2 u) { return D2{-u.y, u.x}; };
+    // R v + P - R lc: the world point of local point v of a body at centre P
+    auto world = [](V2 v, V2 q, D2 P, V2 lc) {
+        const double x = (double)v.x - lc.x, y = (double)v.y - lc.y;
+        return D2{P.x + (q.x * x - q.y * y), P.y + (q.y * x + q.x * y)};
+    };
     const float4 pa = tp->p0[pc.bA], pbb = tp->p0[pc.bB];
     const float4 ma = d.b_mass[pc.bA], mb = d.b_mass[pc.bB];
-    const Xf xfA = get_xf(pa.x, pa.y, pa.z, mk(ma.z, ma.w)), xfB = get_xf(pbb.x, pbb.y, pbb.z, mk(mb.z, mb.w));
-    const Xf& xr = m.flipped ? xfB : xfA;
-    const Xf& xi = m.flipped ? xfA : xfB;
-    const V2 Pr = m.flipped ? mk(pbb.x, pbb.y) : mk(pa.x, pa.y);
-    const V2 Pi = m.flipped ? mk(pa.x, pa.y) : mk(pbb.x, pbb.y);
+    const float4& pr = m.flipped ? pbb : pa;  // reference body
+    const float4& pi = m.flipped ? pa : pbb;  // incident body
+    const float4& mr = m.flipped ? mb : ma;
+    const float4& mi = m.flipped ? ma : mb;
+    const V2 qr = unit_from_angle(pr.z), qi = unit_from_angle(pi.z);
+    const D2 Pr{pr.x, pr.y}, Pi{pi.x, pi.y};
     float* gr = m.flipped ? pb + 3 : pb;  // reference body's x y angle
     float* gi = m.flipped ? pb : pb + 3;  // incident body's
-    const V2 Aw = rotate(m.a, xi.q) + xi.p, Bw = rotate(m.b, xi.q) + xi.p;
-    const V2 E = rotate(m.e, xr.q);
-    const V2 ba = m.b - m.a;
+    const D2 Aw = world(m.a, qi, Pi, mk(mi.z, mi.w)), Bw = world(m.b, qi, Pi, mk(mi.z, mi.w));
+    const D2 E{(double)qr.x * m.e.x - (double)qr.y * m.e.y, (double)qr.y * m.e.x + (double)qr.x * m.e.y};
+    const D2 ba{(double)m.b.x - m.a.x, (double)m.b.y - m.a.y};
     for (int k = 0; k < m.n; ++k) {
-        const V2 N = m.side1[k] ? E : mk(-E.x, -E.y);
-        const V2 Vw = rotate(m.vs[k], xr.q) + xr.p;
-        const V2 u = Aw - Vw, w = Bw - Vw;
-        const float da = dot(N, u), db = dot(N, w), den = da - db;
-        if (den == 0.f) continue;  // no crossing: ClipSegmentToLine made no point here
+        const D2 N = m.side1[k] ? E : D2{-E.x, -E.y};
+        const D2 Vw = world(m.vs[k], qr, Pr, mk(mr.z, mr.w));
+        const D2 u = sub2(Aw, Vw), w = sub2(Bw, Vw);
+        const double da = dot2(N, u), db = dot2(N, w), den = da - db;
+        if (den == 0.0) continue;  // no crossing: ClipSegmentToLine made no point here
         const int i = m.idx[k];
-        const float fbar = lb[2 * i] * ba.x + lb[2 * i + 1] * ba.y;
-        const float den2 = den * den;
-        const float dab = -fbar * db / den2, dbb = fbar * da / den2;
-        const float s = dab + dbb;
-        const V2 rN = revperp(N), rV = revperp(Vw - Pr);
-        gi[0] += s * N.x;
-        gi[1] += s * N.y;
-        gi[2] += dab * dot(N, revperp(Aw - Pi)) + dbb * dot(N, revperp(Bw - Pi));
-        gr[0] -= s * N.x;
-        gr[1] -= s * N.y;
-        gr[2] += dab * (dot(rN, u) - dot(N, rV)) + dbb * (dot(rN, w) - dot(N, rV));
+        const double fbar = lb[2 * i] * ba.x + lb[2 * i + 1] * ba.y;
+        const double den2 = den * den;
+        const double dab = -fbar * db / den2, dbb = fbar * da / den2;
+        const double s = dab + dbb;
+        const D2 rN = rp2(N), rV = rp2(sub2(Vw, Pr));
+        gi[0] += (float)(s * N.x);
+        gi[1] += (float)(s * N.y);
+        gi[2] += (float)(dab * dot2(N, rp2(sub2(Aw, Pi))) + dbb * dot2(N, rp2(sub2(Bw, Pi))));
+        gr[0] -= (float)(s * N.x);
+        gr[1] -= (float)(s * N.y);
+        gr[2] += (float)(dab * (dot2(rN, u) - dot2(N, rV)) + dbb * (dot2(rN, w) - dot2(N, rV)));
     }
 }
 
