@@ -701,7 +701,7 @@ void launch_find_contacts(const DW& d, const Launch& L, cudaStream_t s) {
     k_lbvh_bounds<<<L.grid, L.threads, 0, s>>>(d);
     k_lbvh_morton<<<L.grid, L.threads, 0, s>>>(d);
     const bool alt = radix_sort(L.prims, d.l_key, d.l_key_alt, d.l_idx, d.l_idx_alt, n_lbvh, 30 + (int)d.world_bits,
-                                d.hist, s);
+                                d.hist, d.cnt, s);
     if (alt) k_copy_u64u32<<<L.grid, L.threads, 0, s>>>(d.l_key_alt, d.l_idx_alt, d.l_key, d.l_idx, n_lbvh);
     k_lbvh_internal<<<L.grid, L.threads, 0, s>>>(d);
     k_lbvh_leaves<<<L.grid, L.threads, 0, s>>>(d);
@@ -713,7 +713,7 @@ void launch_find_contacts(const DW& d, const Launch& L, cudaStream_t s) {
     k_find_pairs<<<L.grid * 2, 128, 0, s>>>(d);
     k_pairs_done<<<1, 1, 0, s>>>(d);
     const bool alt2 = radix_sort(L.prims, d.n_key, d.n_key_alt, d.n_val, d.n_val_alt, &d.cnt->n_new,
-                                 2 * (int)d.key_bits, d.hist, s);
+                                 2 * (int)d.key_bits, d.hist, d.cnt, s);
     if (alt2) k_copy_u64u32<<<L.grid, L.threads, 0, s>>>(d.n_key_alt, d.n_val_alt, d.n_key, d.n_val, &d.cnt->n_new);
     k_new_contacts<<<L.grid, L.threads, 0, s>>>(d);
     k_new_done<<<1, 1, 0, s>>>(d);

@@ -465,8 +465,11 @@ struct Prims {
 void scan_exclusive(const Prims& P, const uint32_t* in, uint32_t* out, const uint32_t* n, uint32_t* total,
                     uint32_t* partial, cudaStream_t s);
 // Stable LSD radix sort of (key, val) pairs by the low `bits` bits of the keys.
-// Returns true when the sorted result ended in the *_alt buffers.
+// Returns true when the sorted result ended in the *_alt buffers.  hist holds
+// kRadix * (radix_coop_grid(P) + 1) words; cnt's grid barrier separates passes.
 bool radix_sort(const Prims& P, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
-                const uint32_t* n, int bits, uint32_t* hist, cudaStream_t s);
+                const uint32_t* n, int bits, uint32_t* hist, Counters* cnt, cudaStream_t s);
+// Blocks of the cooperative sort launch (all resident at once, at most P.grid).
+int radix_coop_grid(const Prims& P);
 
 }  // namespace prgpu

@@ -5,6 +5,8 @@
 // kernels produced.  The grid is fixed (a multiple of the SM count); block b
 // owns the contiguous chunk [b*ceil(n/G), (b+1)*ceil(n/G)), which keeps the
 // sort stable without a global look-back.
+#include <algorithm>
+
 #include "prgpu_internal.cuh"
 
 namespace prgpu {
@@ -134,112 +136,122 @@ __global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restric
 }
 
 // ---- radix sort -----------------------------------------------------------
-// Multi-block path (n > kSmallSort): per pass an upsweep of per-block digit
-// counts, one block that scans each digit's counts across blocks (a warp per
-// digit, coalesced) and the digit totals, and a stable downsweep.  Small inputs
-// (n <= kSmallSort, e.g. the few new contacts of a step) are sorted by a single
-// block in shared memory; the multi-block kernels then return at once.
+// Multi-block path (n > kSmallSort): one cooperative launch runs every pass;
+// per pass each block counts the digits of its chunk, the digit rows of those
+// counts are scanned across blocks (a warp per digit, coalesced) with the digit
+// totals, and each block scatters its chunk stably; a bounded grid barrier
+// separates the three.  Small inputs (n <= kSmallSort, e.g. the few new
+// contacts of a step) are sorted by a single block in shared memory, and the
+// cooperative launch returns at once, as it does for n = 0 (a step that
+// rebuilds no tree): one launch a sort instead of three a pass.
+//
+// Data that other blocks wrote earlier in the launch (the keys and values of
+// the previous pass, the digit counts) is read through L2 (__ldcg): a block's
+// L1 may hold lines of those arrays from before the barrier.
 constexpr uint32_t kSmallSort = 4096;
 
-__global__ void k_radix_upsweep(const uint64_t* __restrict__ keys, const uint32_t* n_ptr, int shift,
-                                uint32_t* hist) {
-    __shared__ uint32_t s_cnt[kRadix];
-    const uint32_t n = *n_ptr;
-    if (n <= kSmallSort) return;
-    for (int d = threadIdx.x; d < kRadix; d += blockDim.x) s_cnt[d] = 0;
-    __syncthreads();
-    uint32_t lo, hi;
-    chunk_of(n, lo, hi);
-    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        const uint32_t d = (uint32_t)(keys[i] >> shift) & 0xffu;
-        atomicAdd(&s_cnt[d], 1u);
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < kRadix; d += blockDim.x) hist[d * gridDim.x + blockIdx.x] = s_cnt[d];
-}
-
-// One block of 1024 threads.  hist[d*g + b] becomes the exclusive offset of
-// block b within digit d; hist[kRadix*g + d] the exclusive offset of digit d.
-__global__ void k_radix_scan(uint32_t* hist, int g, const uint32_t* n_ptr) {
-    __shared__ uint32_t s_tot[kRadix];
-    if (*n_ptr <= kSmallSort) return;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int d = warp; d < kRadix; d += nwarps) {
-        uint32_t run = 0;
-        for (int b0 = 0; b0 < g; b0 += 32) {
-            const int b = b0 + lane;
-            const uint32_t v = (b < g) ? hist[d * g + b] : 0u;
-            uint32_t x = v;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += t;
-            }
-            if (b < g) hist[d * g + b] = run + x - v;
-            run += __shfl_sync(0xffffffffu, x, 31);
-        }
-        if (lane == 0) s_tot[d] = run;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t run = 0;
-        for (int d0 = 0; d0 < kRadix; d0 += 32) {
-            const uint32_t v = s_tot[d0 + lane];
-            uint32_t x = v;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += t;
-            }
-            hist[kRadix * g + d0 + lane] = run + x - v;
-            run += __shfl_sync(0xffffffffu, x, 31);
-        }
-    }
-}
-
-__global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(
-    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
-    uint32_t* __restrict__ vout, const uint32_t* n_ptr, int shift, const uint32_t* __restrict__ hist) {
+__global__ void __launch_bounds__(kSortThreads) k_radix_coop(uint64_t* keys, uint64_t* keys_alt, uint32_t* vals,
+                                                              uint32_t* vals_alt, const uint32_t* n_ptr, int passes,
+                                                              uint32_t* hist, Counters* cnt) {
     constexpr int kWarps = kSortThreads / 32;
+    __shared__ uint32_t s_cnt[kRadix];
     __shared__ uint32_t s_base[kRadix];
     __shared__ uint32_t s_wcnt[kWarps][kRadix];
     const uint32_t n = *n_ptr;
     if (n <= kSmallSort) return;
+    const uint32_t g = gridDim.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int d = threadIdx.x; d < kRadix; d += blockDim.x)
-        s_base[d] = hist[d * gridDim.x + blockIdx.x] + hist[kRadix * gridDim.x + d];
+    const uint32_t lt = (1u << lane) - 1u;
     uint32_t lo, hi;
     chunk_of(n, lo, hi);
-    const uint32_t lt = (1u << lane) - 1u;
-    for (uint32_t base = lo; base < hi; base += blockDim.x) {
-        for (int k = threadIdx.x; k < kWarps * kRadix; k += blockDim.x) (&s_wcnt[0][0])[k] = 0u;
+    const uint64_t* kin = keys;
+    const uint32_t* vin = vals;
+    uint64_t* kout = keys_alt;
+    uint32_t* vout = vals_alt;
+    for (int pass = 0; pass < passes; ++pass) {
+        const int shift = pass * 8;
+        // digit counts of this block's chunk
+        for (int dd = threadIdx.x; dd < kRadix; dd += blockDim.x) s_cnt[dd] = 0u;
         __syncthreads();
-        const uint32_t i = base + threadIdx.x;
-        const bool valid = i < hi;
-        uint64_t key = 0;
-        uint32_t val = 0, d = 0xffffffffu;
-        if (valid) {
-            key = kin[i];
-            val = vin[i];
-            d = (uint32_t)(key >> shift) & 0xffu;
+        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+            atomicAdd(&s_cnt[(uint32_t)(__ldcg(kin + i) >> shift) & 0xffu], 1u);
+        __syncthreads();
+        for (int dd = threadIdx.x; dd < kRadix; dd += blockDim.x) hist[dd * g + blockIdx.x] = s_cnt[dd];
+        grid_barrier(cnt);
+        // hist[d*g + b] becomes block b's exclusive offset within digit d,
+        // hist[kRadix*g + d] digit d's total
+        for (uint32_t dd = blockIdx.x * kWarps + warp; dd < (uint32_t)kRadix; dd += g * kWarps) {
+            uint32_t run = 0;
+            for (uint32_t b0 = 0; b0 < g; b0 += 32) {
+                const uint32_t b = b0 + lane;
+                const uint32_t v = (b < g) ? __ldcg(hist + dd * g + b) : 0u;
+                uint32_t x = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += t;
+                }
+                if (b < g) hist[dd * g + b] = run + x - v;
+                run += __shfl_sync(0xffffffffu, x, 31);
+            }
+            if (lane == 0) hist[kRadix * g + dd] = run;
         }
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
-        const uint32_t rank = __popc(peers & lt);
-        if (valid && rank == 0) s_wcnt[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            uint32_t off = s_base[d] + rank;
-            for (int w = 0; w < warp; ++w) off += s_wcnt[w][d];
-            kout[off] = key;
-            vout[off] = val;
+        grid_barrier(cnt);
+        // this block's base of each digit: the digits before it, then the blocks before it
+        if (warp == 0) {
+            uint32_t run = 0;
+            for (int d0 = 0; d0 < kRadix; d0 += 32) {
+                const uint32_t v = __ldcg(hist + kRadix * g + d0 + lane);
+                uint32_t x = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += t;
+                }
+                s_base[d0 + lane] = run + x - v;
+                run += __shfl_sync(0xffffffffu, x, 31);
+            }
         }
         __syncthreads();
-        for (int dd = threadIdx.x; dd < kRadix; dd += blockDim.x) {
-            uint32_t t = 0;
-            for (int w = 0; w < kWarps; ++w) t += s_wcnt[w][dd];
-            s_base[dd] += t;
+        for (int dd = threadIdx.x; dd < kRadix; dd += blockDim.x) s_base[dd] += __ldcg(hist + dd * g + blockIdx.x);
+        // stable scatter of the chunk: ranks within a warp by match, warps in order
+        for (uint32_t base = lo; base < hi; base += blockDim.x) {
+            for (int k = threadIdx.x; k < kWarps * kRadix; k += blockDim.x) (&s_wcnt[0][0])[k] = 0u;
+            __syncthreads();
+            const uint32_t i = base + threadIdx.x;
+            const bool valid = i < hi;
+            uint64_t key = 0;
+            uint32_t val = 0, d = 0xffffffffu;
+            if (valid) {
+                key = __ldcg(kin + i);
+                val = __ldcg(vin + i);
+                d = (uint32_t)(key >> shift) & 0xffu;
+            }
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            const uint32_t rank = __popc(peers & lt);
+            if (valid && rank == 0) s_wcnt[warp][d] = __popc(peers);
+            __syncthreads();
+            if (valid) {
+                uint32_t off = s_base[d] + rank;
+                for (int w = 0; w < warp; ++w) off += s_wcnt[w][d];
+                kout[off] = key;
+                vout[off] = val;
+            }
+            __syncthreads();
+            for (int dd = threadIdx.x; dd < kRadix; dd += blockDim.x) {
+                uint32_t t = 0;
+                for (int w = 0; w < kWarps; ++w) t += s_wcnt[w][dd];
+                s_base[dd] += t;
+            }
+            __syncthreads();
         }
-        __syncthreads();
+        grid_barrier(cnt);
+        const uint64_t* tk = kout;
+        kout = const_cast<uint64_t*>(kin);
+        kin = tk;
+        const uint32_t* tv = vout;
+        vout = const_cast<uint32_t*>(vin);
+        vin = tv;
     }
 }
 
@@ -318,7 +330,7 @@ void scan_exclusive(const Prims& P, const uint32_t* in, uint32_t* out, const uin
 }
 
 bool radix_sort(const Prims& P, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
-                const uint32_t* n, int bits, uint32_t* hist, cudaStream_t s) {
+                const uint32_t* n, int bits, uint32_t* hist, Counters* cnt, cudaStream_t s) {
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_small_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmem);
@@ -329,19 +341,29 @@ bool radix_sort(const Prims& P, uint64_t* keys, uint64_t* keys_alt, uint32_t* va
     // small inputs: one block, result written straight to where the passes would leave it
     k_small_sort<<<1, kSmallThreads, kSmallSmem, s>>>(keys, vals, alt ? keys_alt : keys, alt ? vals_alt : vals, n,
                                                       passes * 8);
-    uint64_t* kin = keys;
-    uint64_t* kout = keys_alt;
-    uint32_t* vi = vals;
-    uint32_t* vo = vals_alt;
-    for (int pass = 0; pass < passes; ++pass) {
-        const int shift = pass * 8;
-        k_radix_upsweep<<<P.grid, kSortThreads, 0, s>>>(kin, n, shift, hist);
-        k_radix_scan<<<1, 1024, 0, s>>>(hist, P.grid, n);
-        k_radix_downsweep<<<P.grid, kSortThreads, 0, s>>>(kin, vi, kout, vo, n, shift, hist);
-        uint64_t* tk = kin; kin = kout; kout = tk;
-        uint32_t* tv = vi; vi = vo; vo = tv;
-    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)radix_coop_grid(P));
+    cfg.blockDim = dim3((unsigned)kSortThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_radix_coop, keys, keys_alt, vals, vals_alt, n, passes, hist, cnt);
     return alt;
+}
+
+int radix_coop_grid(const Prims& P) {
+    // every block of the cooperative sort must be resident at once
+    static int per_sm = -1;
+    if (per_sm < 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_radix_coop, kSortThreads, 0) != cudaSuccess) b = 1;
+        per_sm = b < 1 ? 1 : b;
+    }
+    return std::min(P.grid, per_sm * P.sm_count);
 }
 
 }  // namespace prgpu

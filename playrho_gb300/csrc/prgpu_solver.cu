@@ -2365,8 +2365,11 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
 // meets a smaller world, each of its groups of kGroupThreads threads takes
 // worlds on its own up to n_world_mid, and then each of its warps.
 // kFull false: the instance for steps without joints or recording.
+#ifndef PRGPU_WORLD_SOLVE_MIN_BLOCKS
+#define PRGPU_WORLD_SOLVE_MIN_BLOCKS 4
+#endif
 template <bool kFull>
-__global__ void __launch_bounds__(256, 4) k_world_solve(DW d) {
+__global__ void __launch_bounds__(256, PRGPU_WORLD_SOLVE_MIN_BLOCKS) k_world_solve(DW d) {
     extern __shared__ float4 s_stage[];  // d.stage_bytes: body state of the world(s) being solved
     __shared__ uint32_t s_w;
     __shared__ uint32_t s_col[8][2][kColStride];

@@ -1110,7 +1110,7 @@ static int alloc_world(prgpu_world* w, const WorldDims& z) {
 #define AL(ptr, n) do { rc = dalloc(w, &(ptr), (size_t)(n)); if (rc) return rc; } while (0)
     // per-step scratch: every step writes it before reading it
 #define ALS(ptr, n) do { rc = dalloc(w, &(ptr), (size_t)(n), true); if (rc) return rc; } while (0)
-    AL(d.partial, 1024); AL(d.hist, 256 * 1024);
+    AL(d.partial, 1024); AL(d.hist, 256 * 1025);  // digit rows of up to 1024 sort blocks, then the digit totals
     Counters* cnt;
     AL(cnt, 1);
     d.cnt = cnt;
@@ -1221,6 +1221,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
         w->L.prims.sm_count = prop.multiProcessorCount;
     }
     w->L.prims.grid = std::min(1024, 2 * w->L.prims.sm_count);
+    (void)radix_coop_grid(w->L.prims);  // occupancy query before any stream capture
     if (cudaMallocHost(&w->h_cnt, sizeof(Counters)) != cudaSuccess) return bail(PRGPU_ECUDA);
     if (cudaMallocHost(&w->h_err, 2 * sizeof(uint32_t)) != cudaSuccess) return bail(PRGPU_ECUDA);
     w->h_err[0] = w->h_err[1] = 0u;
