@@ -20,12 +20,12 @@ LIB = os.path.join(HERE, "libprgpu.so")
 # C++ host layer over the C ABI (HostWorld), a second library linked to the first
 HOST_SOURCES = [os.path.join(HERE, "host", "host_world.cpp")]
 HOST_LIB = os.path.join(HERE, "libprgpu_host.so")
-# longest compiles first; prgpu_solver_full.cu and prgpu_solver_lean.cu each
-# compile one k_world_solve instance out of prgpu_solver.cu
-SOURCES = ["prgpu_solver_full.cu", "prgpu_solver_lean.cu", "prgpu_solver.cu", "prgpu_adjoint.cu", "prgpu_toi.cu",
-           "prgpu_contacts.cu", "prgpu_world.cu", "prgpu_prims.cu", "prgpu_query.cu"]
+# longest compiles first; prgpu_solver_{full,lean,tape}.cu each compile one
+# k_world_solve instance out of prgpu_solver.cu
+SOURCES = ["prgpu_solver_full.cu", "prgpu_solver_lean.cu", "prgpu_solver_tape.cu", "prgpu_solver.cu",
+           "prgpu_adjoint.cu", "prgpu_toi.cu", "prgpu_contacts.cu", "prgpu_world.cu", "prgpu_prims.cu", "prgpu_query.cu"]
 # files that include another .cu
-CU_DEPS = {"prgpu_solver_full.cu": ["prgpu_solver.cu"], "prgpu_solver_lean.cu": ["prgpu_solver.cu"]}
+CU_DEPS = {f: ["prgpu_solver.cu"] for f in ("prgpu_solver_full.cu", "prgpu_solver_lean.cu", "prgpu_solver_tape.cu")}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(HERE, "..", "include")]

@@ -96,14 +96,18 @@ cudaError_t launch_tan_step(const DW& d, const StepTape* tp, const TanState& t, 
                             cudaStream_t s);
 // Sets k_world_solve's dynamic shared memory to stage_bytes; returns its CTAs per SM.
 int world_blocks_per_sm(uint32_t stage_bytes);
-// k_world_solve<true> (joints, recording) and k_world_solve<false>, each in a
-// translation unit of its own: launch on the per-world grid, raise the dynamic
-// shared memory limit (false if refused), CTAs per SM at that staging size.
+// The k_world_solve instances with joint and recording code (full), with
+// neither (lean) and with recording code only (tape), each in a translation
+// unit of its own: launch on the per-world grid, raise the dynamic shared
+// memory limit (false if refused), CTAs per SM at that staging size.
 void world_solve_full_launch(const DW& d, unsigned grid, cudaStream_t s);
 bool world_solve_full_allow_smem(uint32_t stage_bytes);
 int world_solve_full_blocks_per_sm(uint32_t stage_bytes);
 void world_solve_lean_launch(const DW& d, unsigned grid, cudaStream_t s);
 bool world_solve_lean_allow_smem(uint32_t stage_bytes);
 int world_solve_lean_blocks_per_sm(uint32_t stage_bytes);
+void world_solve_tape_launch(const DW& d, unsigned grid, cudaStream_t s);
+bool world_solve_tape_allow_smem(uint32_t stage_bytes);
+int world_solve_tape_blocks_per_sm(uint32_t stage_bytes);
 
 }  // namespace prgpu

@@ -14,17 +14,19 @@
 // The velocity loop's early exit (regMinMomentum) only stops iterations that
 // change nothing, so every island runs regVelocityIters sweeps.
 //
-// PRGPU_SOLVER_PART selects what a translation unit compiles, so that the two
+// PRGPU_SOLVER_PART selects what a translation unit compiles, so that the
 // k_world_solve instances (by far the longest to compile) build in parallel
-// with the rest: 0 (this file) everything but k_world_solve; 1 and 2
-// (prgpu_solver_full.cu, prgpu_solver_lean.cu) k_world_solve<true> and
-// k_world_solve<false> with their launch helpers.
+// with the rest: 0 (this file) everything but k_world_solve; 1, 2 and 3
+// (prgpu_solver_full.cu, prgpu_solver_lean.cu, prgpu_solver_tape.cu) the
+// instance with joint and recording code, the one with neither, and the one
+// that records but has no joint code, each with its launch helpers.
 #ifndef PRGPU_SOLVER_PART
 #define PRGPU_SOLVER_PART 0
 #endif
 
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "prgpu_collide.cuh"
@@ -1955,20 +1957,22 @@ __device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefe
 
 // ---- per-constraint sweep steps (t = position in sweep order) -------------------
 // When the step is recorded for the adjoint (d.tape), each contact step also
-// writes the body state (and impulses) it starts from.  kFull false: the caller
-// guarantees a step without joints or recording, and their code stays out of the
-// kernel (its registers would cost the contact sweeps).
-template <bool kFull = true, class BS>
+// writes the body state (and impulses) it starts from.  kMode says which of the
+// joint code (kModeJoints) and the recording code (kModeTape) the instance
+// carries: the caller guarantees a step needs no more, and the code left out
+// costs the contact sweeps no registers.
+constexpr int kModeJoints = 1, kModeTape = 2, kModeAll = kModeJoints | kModeTape;
+template <int kMode = kModeAll, class BS>
 __device__ __forceinline__ void sweep_warm(const DW& d, const BS& bs, uint32_t t) {
     const uint32_t id = d.t_id[t];
-    if (kFull && (id & kJointBit)) {
+    if ((kMode & kModeJoints) && (id & kJointBit)) {
         const uint32_t j = id & ~kJointBit;
         if (d.tape) tape_joint_warm(d, t, j, bs.vel(d.j_bodies[2 * j]), bs.vel(d.j_bodies[2 * j + 1]));
         joint_init_velocity(d, bs, j);
         if (d.tape) tape_joint_check(d, j);
     } else if (d.conf->doWarmStart) {
         const VC vc = load_vc(d, t);
-        if (kFull && d.tape) {
+        if ((kMode & kModeTape) && d.tape) {
             d.tape->warm[2 * (size_t)t] = bs.vel(vc.bA);
             d.tape->warm[2 * (size_t)t + 1] = bs.vel(vc.bB);
         }
@@ -1976,10 +1980,10 @@ __device__ __forceinline__ void sweep_warm(const DW& d, const BS& bs, uint32_t t
     }
 }
 
-template <bool kFull = true, class BS>
+template <int kMode = kModeAll, class BS>
 __device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32_t t, int it) {
     const uint32_t id = d.t_id[t];
-    if (kFull && (id & kJointBit)) {
+    if ((kMode & kModeJoints) && (id & kJointBit)) {
         const uint32_t j = id & ~kJointBit;
         if (d.tape) {
             float4* r = d.tape->vel + 3 * ((size_t)it * d.tape->kcap + t);
@@ -1991,7 +1995,7 @@ __device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32
         joint_solve_velocity(d, bs, j);
     } else {
         VC vc = load_vc(d, t);
-        if (kFull && d.tape) {
+        if ((kMode & kModeTape) && d.tape) {
             float4* r = d.tape->vel + 3 * ((size_t)it * d.tape->kcap + t);
             r[0] = bs.vel(vc.bA);
             r[1] = bs.vel(vc.bB);
@@ -2002,10 +2006,10 @@ __device__ __forceinline__ void sweep_velocity(const DW& d, const BS& bs, uint32
     }
 }
 
-template <bool kFull = true, class BS>
+template <int kMode = kModeAll, class BS>
 __device__ __forceinline__ void sweep_position(const DW& d, const BS& bs, uint32_t t, int it) {
     const uint32_t id = d.t_id[t];
-    if (kFull && (id & kJointBit)) {
+    if ((kMode & kModeJoints) && (id & kJointBit)) {
         const uint32_t j = id & ~kJointBit;
         const uint32_t L = joint_island(d, j);
         const bool done = bs.island_done(L, it);
@@ -2021,7 +2025,7 @@ __device__ __forceinline__ void sweep_position(const DW& d, const BS& bs, uint32
     } else {
         const PC pc = d.pc[t];
         const bool done = bs.island_done(pc.island, it);
-        if (kFull && d.tape) {
+        if ((kMode & kModeTape) && d.tape) {
             float4* r = d.tape->pos + 2 * ((size_t)it * d.tape->kcap + t);
             float4 a = bs.pos(pc.bA);
             a.w = done ? 0.f : 1.f;
@@ -2195,7 +2199,7 @@ struct SubGroup {
 // The sweeps of one world by one group, over its segment [base, base + n) of
 // sweep order with colour offsets col_off; after_position(it) runs after each
 // position iteration.
-template <bool kFull, class G, class BS, class F>
+template <int kMode, class G, class BS, class F>
 __device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uint32_t size, uint32_t base,
                        uint32_t n, const uint32_t* col_off, F&& after_position) {
     const DConf& c = *d.conf;
@@ -2235,15 +2239,15 @@ __device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uin
         if (serial) sweep(kSerialColour, f);
     };
     if (n) {
-        pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_warm<kFull>(d, bs, t); });
+        pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_warm<kMode>(d, bs, t); });
         for (int it = 0; it < c.regVelocityIters; ++it)
-            pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_velocity<kFull>(d, bs, t, it); });
+            pass(d.vc0, sizeof(VCRec), [&](uint32_t t) { sweep_velocity<kMode>(d, bs, t, it); });
     }
     for (uint32_t b = d.w_body_off[w] + rank; b < d.w_body_off[w + 1]; b += size) integrate_body(d, bs, b);
     G::sync();
     if (n) {
         for (int it = 0; it < c.regPositionIters && it < kMaxPosIters; ++it) {
-            pass(d.pc, sizeof(PC), [&](uint32_t t) { sweep_position<kFull>(d, bs, t, it); });
+            pass(d.pc, sizeof(PC), [&](uint32_t t) { sweep_position<kMode>(d, bs, t, it); });
             after_position(it);
         }
         for (uint32_t t = base + rank; t < base + n; t += size) store_impulses(d, t);
@@ -2252,7 +2256,7 @@ __device__ void sweeps(const DW& d, const BS& bs, uint32_t w, uint32_t rank, uin
 }
 
 // col_cnt / col_off: kColStride words of shared memory owned by the group.
-template <class G, bool kFull>
+template <class G, int kMode>
 __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t size, uint32_t* col_cnt,
                             uint32_t* col_off, void* stage, uint32_t stage_cap) {
     const DConf& c = *d.conf;
@@ -2311,7 +2315,7 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
         for (uint32_t t = base + rank; t < base + n; t += size) build_constraint(d, t, d.k_order[t]);
         G::sync();
     }
-    if (kFull && d.tape) {  // recorded for the adjoint
+    if ((kMode & kModeTape) && d.tape) {  // recorded for the adjoint
         for (uint32_t t = base + rank; t < base + n; t += size) tape_constraint(d, t);
         tape_world(d, w, base, n, col_off, rank, size);
     }
@@ -2347,14 +2351,14 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
             }
             G::sync();
         };
-        sweeps<kFull, G>(d, bs, w, rank, size, base, n, col_off, island_pass);
+        sweeps<kMode, G>(d, bs, w, rank, size, base, n, col_off, island_pass);
         for (uint32_t i = rank; i < nb; i += size) {
             d.b_vel[b0 + i] = sv[i];
             d.b_pos1[b0 + i] = sp[i];
         }
     } else {
         const GlobalBodies bs{d};
-        sweeps<kFull, G>(d, bs, w, rank, size, base, n, col_off, [](int) {});
+        sweeps<kMode, G>(d, bs, w, rank, size, base, n, col_off, [](int) {});
     }
     G::sync();  // the group's shared words are reused by its next world
 }
@@ -2364,11 +2368,11 @@ __device__ void solve_world(const DW& d, uint32_t w, uint32_t rank, uint32_t siz
 // The first n_world_big entries are solved by a whole CTA each; once a CTA
 // meets a smaller world, each of its groups of kGroupThreads threads takes
 // worlds on its own up to n_world_mid, and then each of its warps.
-// kFull false: the instance for steps without joints or recording.
+// kMode: the joint and recording code the instance carries (sweep_warm).
 #ifndef PRGPU_WORLD_SOLVE_MIN_BLOCKS
 #define PRGPU_WORLD_SOLVE_MIN_BLOCKS 4
 #endif
-template <bool kFull>
+template <int kMode>
 __global__ void __launch_bounds__(256, PRGPU_WORLD_SOLVE_MIN_BLOCKS) k_world_solve(DW d) {
     extern __shared__ float4 s_stage[];  // d.stage_bytes: body state of the world(s) being solved
     __shared__ uint32_t s_w;
@@ -2381,7 +2385,7 @@ __global__ void __launch_bounds__(256, PRGPU_WORLD_SOLVE_MIN_BLOCKS) k_world_sol
         qi = s_w;
         if (qi >= d.n_worlds) return;
         if (qi >= d.n_world_big) break;
-        solve_world<BlockGroup, kFull>(d, d.w_order[qi], threadIdx.x, blockDim.x, s_col[0][0], s_col[0][1], s_stage,
+        solve_world<BlockGroup, kMode>(d, d.w_order[qi], threadIdx.x, blockDim.x, s_col[0][0], s_col[0][1], s_stage,
                                 d.stage_bytes / kStageBytesPerBody);
     }
     // each warp owns an eighth of the staging area, a group its warps' parts
@@ -2400,7 +2404,7 @@ __global__ void __launch_bounds__(256, PRGPU_WORLD_SOLVE_MIN_BLOCKS) k_world_sol
         if (grp != 0) qi = gnext();  // group 0 keeps the entry the CTA took
         void* gstage = reinterpret_cast<char*>(s_stage) + (size_t)(grp * gwarps) * part;
         while (qi < d.n_world_mid) {
-            solve_world<SubGroup, kFull>(d, d.w_order[qi], grank, kGroupThreads, s_col[grp * gwarps][0],
+            solve_world<SubGroup, kMode>(d, d.w_order[qi], grank, kGroupThreads, s_col[grp * gwarps][0],
                                   s_col[grp * gwarps][1], gstage, gwarps * part / kStageBytesPerBody);
             qi = gnext();
         }
@@ -2415,7 +2419,7 @@ __global__ void __launch_bounds__(256, PRGPU_WORLD_SOLVE_MIN_BLOCKS) k_world_sol
     // warp 0 (of the CTA, or of each group) keeps the entry its CTA or group took
     if ((d.n_world_mid > d.n_world_big) ? (warp % gwarps != 0) : (warp != 0)) qi = next();
     while (qi < d.n_worlds) {
-        solve_world<WarpGroup, kFull>(d, d.w_order[qi], lane, 32u, s_col[warp][0], s_col[warp][1], stage,
+        solve_world<WarpGroup, kMode>(d, d.w_order[qi], lane, 32u, s_col[warp][0], s_col[warp][1], stage,
                                part / kStageBytesPerBody);
         qi = next();
     }
@@ -2605,7 +2609,8 @@ void launch_solve_sweeps(const DW& d, const Launch& L, cudaStream_t s) {
         return;
     }
     cudaMemsetAsync(&d.cnt->world_queue, 0, sizeof(uint32_t), s);
-    if (d.tape || d.n_joints) world_solve_full_launch(d, (unsigned)L.world_grid, s);
+    if (d.n_joints) world_solve_full_launch(d, (unsigned)L.world_grid, s);
+    else if (d.tape) world_solve_tape_launch(d, (unsigned)L.world_grid, s);
     else world_solve_lean_launch(d, (unsigned)L.world_grid, s);
 }
 
@@ -2617,13 +2622,16 @@ int world_blocks_per_sm(uint32_t stage_bytes) {
     {
         std::lock_guard<std::mutex> lock(mu);
         if (stage_bytes > set_bytes) {
-            if (!world_solve_full_allow_smem(stage_bytes) || !world_solve_lean_allow_smem(stage_bytes)) return 0;
+            if (!world_solve_full_allow_smem(stage_bytes) || !world_solve_lean_allow_smem(stage_bytes) ||
+                !world_solve_tape_allow_smem(stage_bytes))
+                return 0;
             set_bytes = stage_bytes;
         }
     }
     // both instances have the same launch bounds; the grid is sized for the smaller residency
     const int a = world_solve_full_blocks_per_sm(stage_bytes), b = world_solve_lean_blocks_per_sm(stage_bytes);
-    return a < b ? a : b;
+    const int c = world_solve_tape_blocks_per_sm(stage_bytes);
+    return std::min(a, std::min(b, c));
 }
 
 void launch_post_record(const DW& d, const Launch& L, cudaStream_t s) { k_post_record<<<L.grid, L.threads, 0, s>>>(d); }
@@ -2643,25 +2651,28 @@ void launch_solve(const DW& d, const Launch& L, cudaStream_t s) {
 // The one k_world_solve instance this translation unit compiles, and its launch
 // helpers (declared in prgpu_kernels.cuh).
 #if PRGPU_SOLVER_PART == 1
-#define PRGPU_WS_FULL true
+#define PRGPU_WS_MODE kModeAll
 #define PRGPU_WS_NAME(x) world_solve_full_##x
-#else
-#define PRGPU_WS_FULL false
+#elif PRGPU_SOLVER_PART == 2
+#define PRGPU_WS_MODE 0
 #define PRGPU_WS_NAME(x) world_solve_lean_##x
+#else
+#define PRGPU_WS_MODE kModeTape
+#define PRGPU_WS_NAME(x) world_solve_tape_##x
 #endif
 
 void PRGPU_WS_NAME(launch)(const DW& d, unsigned grid, cudaStream_t s) {
-    k_world_solve<PRGPU_WS_FULL><<<grid, 256, d.stage_bytes, s>>>(d);
+    k_world_solve<PRGPU_WS_MODE><<<grid, 256, d.stage_bytes, s>>>(d);
 }
 
 bool PRGPU_WS_NAME(allow_smem)(uint32_t stage_bytes) {
-    return cudaFuncSetAttribute(k_world_solve<PRGPU_WS_FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_world_solve<PRGPU_WS_MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)stage_bytes) == cudaSuccess;
 }
 
 int PRGPU_WS_NAME(blocks_per_sm)(uint32_t stage_bytes) {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_world_solve<PRGPU_WS_FULL>, 256, stage_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_world_solve<PRGPU_WS_MODE>, 256, stage_bytes);
     return n;
 }
 #endif
