@@ -474,8 +474,8 @@ __global__ void k_adj_local(DW d, const StepTape* tp, AdjState a) {
             }
             float aAb, aBb;
             diff::joint_geom_vjp(k, tp->p0[A].z, tp->p0[B].z, gbar, &aAb, &aBb);
-            if (k.writableA) atomicAdd(&a.pbar[A].z, aAb);
-            if (k.writableB) atomicAdd(&a.pbar[B].z, aBb);
+            if (k.writableA) atomicAdd(a.pvacc + 6 * (size_t)A + 2, (double)aAb);
+            if (k.writableB) atomicAdd(a.pvacc + 6 * (size_t)B + 2, (double)aBb);
             continue;
         }
         const PC& pc = tp->pc[t];
@@ -506,12 +506,17 @@ __global__ void k_adj_local(DW d, const StepTape* tp, AdjState a) {
         // clipped manifold points moved with the positions the step started from
         const MovingPoints mp = moving_points(d, tp, t, pc);
         if (mp.n) moving_points_vjp(d, tp, pc, mp, gbar + kLocalPts, pbar);
-        atomicAdd(&a.pbar[pc.bA].x, pbar[0]); atomicAdd(&a.pbar[pc.bA].y, pbar[1]); atomicAdd(&a.pbar[pc.bA].z, pbar[2]);
-        atomicAdd(&a.pbar[pc.bB].x, pbar[3]); atomicAdd(&a.pbar[pc.bB].y, pbar[4]); atomicAdd(&a.pbar[pc.bB].z, pbar[5]);
-        atomicAdd(&a.vibar[pc.bA].x, vbar[0]); atomicAdd(&a.vibar[pc.bA].y, vbar[1]);
-        atomicAdd(&a.vibar[pc.bA].z, vbar[2]);
-        atomicAdd(&a.vibar[pc.bB].x, vbar[3]); atomicAdd(&a.vibar[pc.bB].y, vbar[4]);
-        atomicAdd(&a.vibar[pc.bB].z, vbar[5]);
+        // summed per body in FP64 (k_adj_bodies folds the sums in): the order of
+        // the atomics then leaves the float result unchanged, so the reverse pass
+        // gives the same gradients on every run
+        double* accA = a.pvacc + 6 * (size_t)pc.bA;
+        double* accB = a.pvacc + 6 * (size_t)pc.bB;
+        for (int q = 0; q < 3; ++q) {
+            atomicAdd(accA + q, (double)pbar[q]);
+            atomicAdd(accB + q, (double)pbar[3 + q]);
+            atomicAdd(accA + 3 + q, (double)vbar[q]);
+            atomicAdd(accB + 3 + q, (double)vbar[3 + q]);
+        }
         // MixFriction: sqrt(fA fB)
         if (mub != 0.f && ci.z > 0.f) {
             const uint2 pr = tp->prox[t];
@@ -525,6 +530,16 @@ __global__ void k_adj_local(DW d, const StepTape* tp, AdjState a) {
 // velocity at the start of the solve from the velocity the step started with
 __global__ void k_adj_bodies(DW d, const StepTape* tp, AdjState a) {
     GRID_LOOP(b, d.n_bodies) {
+        // k_adj_local's FP64 sums: position adjoints added to the sweeps', the
+        // start-velocity adjoints as they are; cleared for the next step
+        double* acc = a.pvacc + 6 * (size_t)b;
+        float4 p = a.pbar[b];
+        p.x = (float)((double)p.x + acc[0]);
+        p.y = (float)((double)p.y + acc[1]);
+        p.z = (float)((double)p.z + acc[2]);
+        a.pbar[b] = p;
+        a.vibar[b] = make_float4((float)acc[3], (float)acc[4], (float)acc[5], 0.f);
+        for (int q = 0; q < 6; ++q) acc[q] = 0.0;
         if (!(tp->flags[b] & BF_SOLVED)) continue;
         const float4 v0 = tp->v0[b];
         const float4 g1 = a.vbar[b], g2 = a.vibar[b];
@@ -774,6 +789,24 @@ uint32_t adj_parallel_grid() {
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return 0;
     return (uint32_t)sms * 8u;
+}
+
+uint32_t adj_sweep_threads(uint32_t most, uint32_t n_worlds) {
+    // by the largest world: worlds of up to 256 bodies have a few dozen
+    // constraints a colour (one warp, whose barriers are the cheapest)
+    uint32_t t = most > 4096u ? kAdjSweepMaxThreads : most > 256u ? 128u : 32u;
+    // one block a world: halve the block while that lets every world's block be
+    // resident at once (a second wave of blocks would double the pass)
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return t;
+    auto resident = [&](uint32_t threads) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_adj_sweeps, (int)threads, 0) != cudaSuccess) return 0u;
+        return (uint32_t)b * (uint32_t)sms;
+    };
+    while (t > 128u && resident(t) < n_worlds && resident(t / 2u) >= n_worlds) t /= 2u;
+    return t;
 }
 
 cudaError_t launch_adj_step(const DW& d, const StepTape* tp, const AdjState& a, uint32_t n_slots, cudaStream_t s) {

@@ -62,6 +62,7 @@ struct AdjState {
     float4* vbar;     // [N] d(loss)/d(velocity)
     float4* vibar;    // [N] through the velocity bias: d(loss)/d(velocity at the start of the solve)
     float4* vi;       // [N] velocity at the start of the solve (recomputed)
+    double* pvacc;    // [N*6] k_adj_local's adjoints of each body's position and start velocity, in FP64
     float4* lbar;     // [K] d(loss)/d(impulses ni0 ti0 ni1 ti1) of each constraint
     float* gbar;      // [K * kGeomWords] d(loss)/d(geometry)
     float* gval;      // [K * kGeomWords] geometry values
@@ -91,6 +92,8 @@ struct TanState {
 
 // blocks of the adjoint's parallel passes on this device (0: no device)
 uint32_t adj_parallel_grid();
+// threads of the reverse sweeps' block (one a world), from the largest world's bodies
+uint32_t adj_sweep_threads(uint32_t most, uint32_t n_worlds);
 cudaError_t launch_adj_step(const DW& d, const StepTape* tp, const AdjState& a, uint32_t n_slots, cudaStream_t s);
 cudaError_t launch_tan_step(const DW& d, const StepTape* tp, const TanState& t, float* gval, uint32_t n_slots,
                             cudaStream_t s);

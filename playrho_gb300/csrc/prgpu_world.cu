@@ -2186,6 +2186,9 @@ struct AdjWindow {
     uint32_t mismatches = 0, overflows = 0;
     double forward_ms = 0, record_ms = 0, reverse_ms = 0;  // host time of the phases of the last passes
     std::vector<cudaGraphExec_t> rec_graphs;  // recorded step into tape i, captured once per window
+    // steps [taped_lo, taped_hi) of a segment that the forward pass recorded into
+    // tapes 0.. as it ran them (its last segment); -1: none
+    int taped_lo = -1, taped_hi = -1;
 };
 
 void adjoint_drop_graphs(prgpu_world* w) {
@@ -2329,6 +2332,28 @@ static int capture_record_step(prgpu_world* w, int i) {
     return PRGPU_OK;
 }
 
+// One step recorded into tape i (the window's configuration already uploaded).
+static int record_step(prgpu_world* w, int i) {
+    AdjWindow* a = w->adj;
+    a->rec_graphs.resize(a->every, nullptr);
+    int rc = 0;
+    if (!a->rec_graphs[i] && (rc = capture_record_step(w, i))) return rc;
+    CU(cudaGraphLaunch(a->rec_graphs[i], w->stream));
+    return PRGPU_OK;
+}
+
+// Adds the replay mismatches of the differentiable restatement recorded in
+// tapes 0..n-1, then checks the device error word.
+static int count_tape_mismatches(prgpu_world* w, int n) {
+    AdjWindow* a = w->adj;
+    std::vector<uint32_t> bad(n, 0);
+    for (int i = 0; i < n; ++i)
+        CU(cudaMemcpyAsync(&bad[i], a->tapes[i].hdr + kSerialColour + 5, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    for (int i = 0; i < n; ++i) a->mismatches += bad[i];
+    return check_device_error(w);
+}
+
 static int record_segment(prgpu_world* w, int seg, int n) {
     AdjWindow* a = w->adj;
     int rc = snap_copy(w, a->snaps[seg], false);
@@ -2337,19 +2362,9 @@ static int record_segment(prgpu_world* w, int seg, int n) {
     w->conf_valid = false;
     rc = set_conf(w, &a->conf);
     if (rc) return rc;
-    a->rec_graphs.resize(a->every, nullptr);
-    for (int i = 0; i < n; ++i) {
-        if (!a->rec_graphs[i] && (rc = capture_record_step(w, i))) return rc;
-        CU(cudaGraphLaunch(a->rec_graphs[i], w->stream));
-    }
-    // replay mismatches of the differentiable restatement
-    std::vector<uint32_t> bad(n, 0);
     for (int i = 0; i < n; ++i)
-        CU(cudaMemcpyAsync(&bad[i], a->tapes[i].hdr + kSerialColour + 5, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
-    CU(cudaStreamSynchronize(w->stream));
-    for (int i = 0; i < n; ++i) a->mismatches += bad[i];
-    rc = check_device_error(w);
-    if (rc) return rc;
+        if ((rc = record_step(w, i))) return rc;
+    if ((rc = count_tape_mismatches(w, n))) return rc;
     // the segment must end where the forward pass continued from
     const void* next = (size_t)(seg + 1) < a->snaps.size() ? a->snaps[seg + 1] : a->end_state;
     uint32_t differ = 0;
@@ -2382,17 +2397,15 @@ int prgpu_adjoint_begin(prgpu_world* w, int checkpoint_every) {
 #define AA(ptr, bytes) do { void* q_; rc = adj_alloc(w, a, &q_, (bytes)); if (rc) { adjoint_close(w); return rc; } \
                             ptr = reinterpret_cast<decltype(ptr)>(q_); } while (0)
     AA(a->adj.pbar, sizeof(float4) * N); AA(a->adj.vbar, sizeof(float4) * N); AA(a->adj.vibar, sizeof(float4) * N);
-    AA(a->adj.vi, sizeof(float4) * N); AA(a->adj.lbar, sizeof(float4) * K);
+    AA(a->adj.vi, sizeof(float4) * N); AA(a->adj.lbar, sizeof(float4) * K); AA(a->adj.pvacc, sizeof(double) * 6 * N);
     AA(a->adj.gbar, sizeof(float) * kAdjGeomWords * (size_t)K); AA(a->adj.gval, sizeof(float) * kAdjGeomWords * (size_t)K);
     AA(a->adj.mbar, sizeof(float4) * C); AA(a->adj.mtmp, sizeof(float4) * C); AA(a->adj.fbar, sizeof(float) * S);
     AA(a->adj.err, sizeof(uint32_t) * 2);
     AA(a->adj.jbar, sizeof(float4) * std::max<uint32_t>(w->d.n_joints, 1));
     a->adj.grid = (uint32_t)a->grid;
     // one block per world in the reverse sweeps; larger worlds get larger blocks
-    // (worlds of up to 256 bodies have a few dozen constraints a colour: one warp,
-    // whose barriers are the cheapest)
     const uint32_t most = w->order_nb.empty() ? 0u : *std::max_element(w->order_nb.begin(), w->order_nb.end());
-    a->adj.sweep_threads = most > 4096u ? kAdjSweepMaxThreads : most > 256u ? 128u : 32u;
+    a->adj.sweep_threads = adj_sweep_threads(most, w->d.n_worlds);
     AA(a->tan.jdot, sizeof(double) * 2 * std::max<uint32_t>(w->d.n_joints, 1));
     AA(a->tan.pdot, sizeof(double) * 3 * N); AA(a->tan.vdot, sizeof(double) * 3 * N);
     AA(a->tan.vidot, sizeof(double) * 3 * N); AA(a->tan.ldot, sizeof(double) * 4 * (size_t)K);
@@ -2442,14 +2455,28 @@ int prgpu_adjoint_forward(prgpu_world* w, const prgpu_step_conf* conf, int n_ste
     int rc = ensure_tapes(w);
     if (rc) return rc;
     const auto t0 = std::chrono::steady_clock::now();
+    // the window's last segment as of this call is recorded as it runs, so that
+    // the backward pass (if it comes next) need not run it again
+    const int end = a->steps + n_steps;
+    const int tail_first = end > 0 ? ((end - 1) / a->every) * a->every : 0;
     for (int i = 0; i < n_steps; ++i) {
-        if (a->steps % a->every == 0) {
+        const int s = a->steps, seg_first = s - s % a->every;
+        if (s == seg_first) {
             void* buf = nullptr;
             if (adj_take(w, &buf, a->snap_bytes) != cudaSuccess) return fail(w, PRGPU_ECUDA, "checkpoint allocation");
             a->snaps.push_back(buf);
             if ((rc = snap_copy(w, buf, true))) return rc;
         }
-        if ((rc = run_steps(w, conf, 1, false))) return rc;
+        const bool tape = s >= tail_first && (s == seg_first || (a->taped_lo == seg_first && a->taped_hi == s));
+        if (tape) {
+            if ((rc = set_conf(w, conf))) return rc;
+            w->stepped = true;
+            if ((rc = record_step(w, s - seg_first))) return rc;
+            if (s == seg_first) a->taped_lo = s;
+            a->taped_hi = s + 1;
+        } else if ((rc = run_steps(w, conf, 1, false))) {
+            return rc;
+        }
         ++a->steps;
     }
     rc = check_device_error(w);
@@ -2489,6 +2516,7 @@ int prgpu_adjoint_backward(prgpu_world* w, const float* dl_dpos3, const float* d
                            dl_dvel3 ? dl_dvel3[3 * b + 2] : 0.f, 0.f);
     CU(cudaMemcpyAsync(a->adj.vbar, h.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, w->stream));
     CU(cudaMemsetAsync(a->adj.mbar, 0, sizeof(float4) * a->ccap, w->stream));
+    CU(cudaMemsetAsync(a->adj.pvacc, 0, sizeof(double) * 6 * N, w->stream));
     CU(cudaMemsetAsync(a->adj.jbar, 0, sizeof(float4) * std::max<uint32_t>(w->d.n_joints, 1), w->stream));
     CU(cudaMemsetAsync(a->adj.fbar, 0, sizeof(float) * std::max<uint32_t>(S, 1), w->stream));
     CU(cudaMemsetAsync(a->adj.err, 0, sizeof(uint32_t), w->stream));
@@ -2498,7 +2526,14 @@ int prgpu_adjoint_backward(prgpu_world* w, const float* dl_dpos3, const float* d
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int first = seg * a->every, n = std::min(a->every, a->steps - first);
         const auto t0 = clk::now();
-        if ((rc = record_segment(w, seg, n))) return rc;
+        if (first == a->taped_lo && a->steps == a->taped_hi) {
+            // the forward pass recorded this segment as it ran it; the world is
+            // at the segment's end, as a recomputation would leave it
+            if ((rc = count_tape_mismatches(w, n))) return rc;
+        } else if ((rc = record_segment(w, seg, n))) {
+            return rc;
+        }
+        a->taped_lo = a->taped_hi = -1;  // the tapes now hold other segments
         const auto t1 = clk::now();
         for (int i = n - 1; i >= 0; --i) {
             const cudaError_t e = launch_adj_step(w->d, a->d_tapes + i, a->adj, a->ccap, w->stream);
@@ -2556,6 +2591,7 @@ int prgpu_adjoint_tangent(prgpu_world* w, const double* dpos3_start, const doubl
     CU(cudaMemsetAsync(a->tan.jdot, 0, sizeof(double) * 2 * std::max<uint32_t>(w->d.n_joints, 1), w->stream));
     CU(cudaStreamSynchronize(w->stream));
     const int nseg = (a->steps + a->every - 1) / a->every;
+    a->taped_lo = a->taped_hi = -1;  // the segments below are recorded over the tapes
     for (int seg = 0; seg < nseg; ++seg) {
         const int first = seg * a->every, n = std::min(a->every, a->steps - first);
         if ((rc = record_segment(w, seg, n))) return rc;
