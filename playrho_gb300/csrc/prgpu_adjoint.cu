@@ -358,7 +358,10 @@ __global__ void k_adj_prep(DW d, const StepTape* tp, AdjState a) {
 // The iterated part of world w's solve, backwards, by one block: the position
 // iterations colour by colour in reverse, position integration, then the
 // velocity iterations in reverse.  A block barrier separates two colours.
-__global__ void __launch_bounds__(kAdjSweepMaxThreads) k_adj_sweeps(DW d, const StepTape* tp, AdjState a) {
+// kWide: the instance for blocks of kAdjSweepMaxThreads, held to 64 registers so
+// that two blocks fit on a multiprocessor.
+template <bool kWide>
+__global__ void __launch_bounds__(kAdjSweepMaxThreads, kWide ? 2 : 1) k_adj_sweeps(DW d, const StepTape* tp, AdjState a) {
     const DConf& c = *d.conf;
     const float h = c.deltaTime;
     const uint32_t w = blockIdx.x;
@@ -794,26 +797,24 @@ uint32_t adj_parallel_grid() {
 uint32_t adj_sweep_threads(uint32_t most, uint32_t n_worlds) {
     // by the largest world: worlds of up to 256 bodies have a few dozen
     // constraints a colour (one warp, whose barriers are the cheapest)
-    uint32_t t = most > 4096u ? kAdjSweepMaxThreads : most > 256u ? 128u : 32u;
-    // one block a world: halve the block while that lets every world's block be
-    // resident at once (a second wave of blocks would double the pass)
+    const uint32_t t = most > 4096u ? kAdjSweepMaxThreads : most > 256u ? 128u : 32u;
+    if (t < kAdjSweepMaxThreads) return t;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return t;
-    auto resident = [&](uint32_t threads) {
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_adj_sweeps, (int)threads, 0) != cudaSuccess) return 0u;
-        return (uint32_t)b * (uint32_t)sms;
-    };
-    while (t > 128u && resident(t) < n_worlds && resident(t / 2u) >= n_worlds) t /= 2u;
-    return t;
+    // the wide instance while every world's block is resident at once with it (a
+    // second wave of blocks would double the pass), else half the block
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_adj_sweeps<true>, (int)t, 0) != cudaSuccess) return t;
+    return (uint32_t)b * (uint32_t)sms >= n_worlds ? t : t / 2u;
 }
 
 cudaError_t launch_adj_step(const DW& d, const StepTape* tp, const AdjState& a, uint32_t n_slots, cudaStream_t s) {
     k_adj_transfer<<<a.grid, 256, 0, s>>>(d, tp, a, n_slots);
     cudaMemcpyAsync(a.mbar, a.mtmp, sizeof(float4) * n_slots, cudaMemcpyDeviceToDevice, s);
     k_adj_prep<<<a.grid, 256, 0, s>>>(d, tp, a);
-    k_adj_sweeps<<<d.n_worlds, a.sweep_threads, 0, s>>>(d, tp, a);
+    if (a.sweep_threads == kAdjSweepMaxThreads) k_adj_sweeps<true><<<d.n_worlds, a.sweep_threads, 0, s>>>(d, tp, a);
+    else k_adj_sweeps<false><<<d.n_worlds, a.sweep_threads, 0, s>>>(d, tp, a);
     k_adj_local<<<a.grid, 256, 0, s>>>(d, tp, a);
     k_adj_bodies<<<a.grid, 256, 0, s>>>(d, tp, a);
     return cudaGetLastError();
