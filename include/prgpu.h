@@ -262,13 +262,19 @@ int prgpu_autotune(prgpu_world* w, const prgpu_step_conf* conf, int steps_per_ca
  * a limit or a motor are rejected (PRGPU_EINVAL).
  *   prgpu_adjoint_begin     opens a window; the state is checkpointed every
  *                           checkpoint_every steps (device copies of the whole batch)
- *   prgpu_adjoint_forward   n steps with one StepConf, as prgpu_step_n
+ *   prgpu_adjoint_forward   n steps with one StepConf, as prgpu_step_n; the steps
+ *                           of the window's last segment (as of this call) are
+ *                           recorded as they run
  *   prgpu_adjoint_backward  from d(loss)/d(final state) -- positions x y angle of
  *                           each body's centre of mass and velocities, [n_bodies*3],
  *                           either may be NULL -- to d(loss)/d(state at the window's
  *                           start) and d(loss)/d(friction of each shape) [n_shapes];
- *                           each segment is re-run from its checkpoint to record it,
- *                           then walked backwards; the batch is left at the window's end
+ *                           each segment is re-run from its checkpoint to record it
+ *                           (the last one only if the forward pass did not record
+ *                           it), then walked backwards; the batch is left at the
+ *                           window's end.  The position and velocity gradients are
+ *                           the same on every run (friction gradients are summed
+ *                           with float atomics and may differ in the last bits)
  *   prgpu_adjoint_tangent   the FP64 forward-mode derivative along the same window
  *                           (tangents of the start state and friction in, of the
  *                           final state out), for dot-product tests of the adjoint
@@ -291,8 +297,9 @@ int prgpu_adjoint_tangent(prgpu_world* w, const double* dpos3_start, const doubl
 int prgpu_adjoint_info(prgpu_world* w, int* steps, uint32_t* replay_mismatches, uint32_t* tape_overflows);
 int prgpu_adjoint_end(prgpu_world* w);
 int prgpu_adjoint_trim(void);
-/* Host time (ms) of the window's forward steps and of the last backward pass's
- * recording (segments re-run from their checkpoints) and reverse kernels. */
+/* Host time (ms) of the window's forward steps (the recording of the last
+ * segment included) and of the last backward pass's recording (segments re-run
+ * from their checkpoints) and reverse kernels. */
 int prgpu_adjoint_profile(prgpu_world* w, double* forward_ms, double* record_ms, double* reverse_ms);
 /* Enqueues n steps on the handle's stream and returns at once.  A device error
  * raised by an earlier step (capacity overflow, a bounded wait that gave up) is
