@@ -15,7 +15,10 @@ struct Launch {
     bool per_world;    // sweeps run one CTA per world (batches of many worlds)
     int world_grid;    // persistent CTAs of the per-world sweep kernel
     bool sensors;      // the batch has sensor shapes (their update pass runs)
+    bool isl_big_worlds;  // a world has more bodies than the islands' shared-memory pass holds
 };
+// bodies of the largest world whose islands are found in shared memory
+constexpr uint32_t kIslSmemBodiesMax = 8192;
 
 // contacts / broadphase (prgpu_contacts.cu)
 void launch_pre_proxies(const DW& d, const Launch& L, cudaStream_t s);

@@ -89,16 +89,98 @@ __global__ void k_isl_init(DW d) {
 
 __device__ __forceinline__ bool island_edge_body(uint32_t f) { return is_speedable(f) && (f & BF_ENABLED); }
 
-// The contacts are taken by slot (a free slot's flags are 0, never solvable):
-// the union order does not change the components or their labels.
-__global__ void k_isl_union(DW d) {
-    const uint32_t hw = d.cnt->high_water;
+// The first index of the sorted live list whose key is >= key, by a warp: each
+// round the 32 lanes probe 32 evenly spaced entries and the range shrinks to the
+// gap where the keys cross.
+__device__ __forceinline__ uint32_t live_lower_bound(const uint64_t* keys, uint32_t n, uint64_t key, uint32_t lane) {
+    uint32_t lo = 0, hi = n;  // the answer lies in [lo, hi]
+    while (hi - lo > 32u) {
+        const uint32_t step = (hi - lo) / 32u;
+        const bool less = keys[lo + (lane + 1u) * step - 1u] < key;
+        const uint32_t k = __popc(__ballot_sync(0xffffffffu, less));
+        const uint32_t nhi = (k < 32u) ? lo + (k + 1u) * step - 1u : hi;
+        lo += k * step;
+        hi = nhi;
+    }
+    const bool less = lo + lane < hi && keys[lo + lane] < key;
+    return lo + __popc(__ballot_sync(0xffffffffu, less));
+}
+
+// Union-find in shared memory, with the rules of uf_find_halving / uf_union:
+// only non-roots are rewritten, larger roots are hooked under smaller ones.
+__device__ __forceinline__ uint32_t s_find(volatile uint32_t* p, uint32_t x) {
+    for (int g = 0; g < 1 << 20; ++g) {
+        const uint32_t q = p[x];
+        if (q == x) return x;
+        const uint32_t r = p[q];
+        if (r == q) return q;
+        p[x] = r;
+        x = r;
+    }
+    return x;
+}
+
+__device__ __forceinline__ void s_union(uint32_t* p, uint32_t a, uint32_t b, Counters* c) {
+    for (int g = 0; g < 1 << 16; ++g) {
+        uint32_t ra = s_find(p, a), rb = s_find(p, b);
+        if (ra == rb) return;
+        if (ra < rb) { const uint32_t t = ra; ra = rb; rb = t; }
+        if (atomicCAS(&p[ra], ra, rb) == ra) return;
+    }
+    set_error(c, PR_ETIMEOUT, 21u);
+}
+
+// Islands over contacts, one block a world of at most kIslSmemBodiesMax bodies.
+// The live list is sorted by key and proxies are numbered world by world, so
+// world w's contacts are the entries whose smaller proxy is one of its shapes:
+// one range of the list.  The block unions them in shared memory and writes each
+// body's root; the roots are component minima, as the global union leaves them,
+// so the joints' unions (k_isl_union) and the flattening that follow see the same
+// sets and labels.  Larger worlds are left to k_isl_union.
+
+
+__global__ void __launch_bounds__(256) k_isl_world(DW d) {
+    __shared__ uint32_t s_par[kIslSmemBodiesMax];
+    __shared__ uint32_t s_rng[2];
+    const uint32_t w = blockIdx.x;
+    const uint32_t b0 = d.w_body_off[w], nb = d.w_body_off[w + 1] - b0;
+    if (nb > kIslSmemBodiesMax) return;
+    if (threadIdx.x < 64u) {  // warp 0 finds the world's first entry, warp 1 the next world's
+        const uint32_t lane = threadIdx.x & 31u, which = threadIdx.x >> 5;
+        const uint64_t key = (uint64_t)d.w_shape_off[w + which] << d.key_bits;
+        const uint32_t at = live_lower_bound(d.c_key, d.cnt->n_live, key, lane);
+        if (lane == 0) s_rng[which] = at;
+    }
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) s_par[i] = i;
+    __syncthreads();
+    for (uint32_t i = s_rng[0] + threadIdx.x; i < s_rng[1]; i += blockDim.x) {
+        const uint32_t slot = d.c_slot[i];
+        if (!contact_solvable(d.cs_flags[slot])) continue;
+        const uint2 bd = d.cs_body[slot];
+        if (!(island_edge_body(d.b_flags[bd.x]) && island_edge_body(d.b_flags[bd.y]))) continue;
+        if (bd.x - b0 >= nb || bd.y - b0 >= nb) {  // a contact of another world's bodies: not made
+            set_error(d.cnt, PR_EINVAL, 22u);
+            continue;
+        }
+        s_union(s_par, bd.x - b0, bd.y - b0, d.cnt);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) d.b_island[b0 + i] = b0 + s_find(s_par, i);
+}
+
+// Joints, and (big_worlds) the contacts of worlds above kIslSmemBodiesMax bodies,
+// taken by slot (a free slot's flags are 0, never solvable): the union order
+// does not change the components or their labels.
+__global__ void k_isl_union(DW d, bool big_worlds) {
+    const uint32_t hw = big_worlds ? d.cnt->high_water : 0u;
     GRID_LOOP(i, hw + d.n_joints) {
         uint32_t a, b;
         if (i < hw) {
             if (!contact_solvable(d.cs_flags[i])) continue;
             const uint2 bd = d.cs_body[i];
             a = bd.x; b = bd.y;
+            const uint32_t w = d.b_world[a];
+            if (d.w_body_off[w + 1] - d.w_body_off[w] <= kIslSmemBodiesMax) continue;  // done by k_isl_world
         } else {
             const uint32_t j = i - hw;
             a = d.j_bodies[2 * j]; b = d.j_bodies[2 * j + 1];
@@ -2574,7 +2656,8 @@ void launch_clear_dirty(const DW& d, const Launch& L, cudaStream_t s) {
 
 void launch_islands_colour(const DW& d, const Launch& L, cudaStream_t s) {
     k_isl_init<<<L.grid, L.threads, 0, s>>>(d);
-    k_isl_union<<<L.grid, L.threads, 0, s>>>(d);
+    k_isl_world<<<d.n_worlds, 256, 0, s>>>(d);
+    k_isl_union<<<L.grid, L.threads, 0, s>>>(d, L.isl_big_worlds);
     k_isl_flatten<<<L.grid, L.threads, 0, s>>>(d);
     if (d.tape) launch_tape_body_start(d, L, s);
     k_body_begin<<<L.grid, L.threads, 0, s>>>(d);

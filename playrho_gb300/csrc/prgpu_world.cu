@@ -1249,6 +1249,7 @@ int prgpu_world_create(const prgpu_batch_desc* ds, int device, prgpu_world** out
     });
     w->order_nb.resize(W);
     for (uint32_t i = 0; i < W; ++i) w->order_nb[i] = body_off[order[i] + 1] - body_off[order[i]];
+    w->L.isl_big_worlds = W > 0 && w->order_nb[0] > kIslSmemBodiesMax;
     w->warp_world_max = kWarpWorldMaxBodies;
     count_world_classes(w);
     if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(PRGPU_ECUDA);
