@@ -373,6 +373,10 @@ def run_reference(args, rank):
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": len(shares), "kind": kind,
                             "sample": cpu_sample_desc(kind, len(worlds), len(worlds), len(shares), pre,
                                                       args.steps)},
+           # one core's figure: each process's own rate over its share of the worlds
+           "single_thread": {"value": statistics.mean(r[1] / r[0] for r in res if r[0] > 0), "unit": UNIT,
+                             "cores": 1, "sample": f"mean over the {len(shares)} processes of each one's "
+                                                   "awake body-steps over its own timed steps"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
