@@ -155,6 +155,18 @@ def test_large_world_crop_matches_oracle(gpu_lib):
     _contacts_from_identical_transforms(g2, [cropped], [0], min_contacts=500)
 
 
+def test_chain_worlds_sample_matches_oracle(gpu_lib):
+    """The chains workload's worlds (8,000 free disks and 3..8-gons plus 64 chains
+    of 32 boxes on revolute joints, seed 3, dt 1/120, 10/4 iterations), the first
+    two of its generator after its 120 settling steps, rebased onto identical
+    transforms: pair sets, features and manifolds as the oracle's."""
+    rng = np.random.default_rng(3)
+    worlds = [scenes.chains_world(rng) for _ in range(2)]
+    g = GpuBatch(worlds)
+    g.step_n(120, default_conf(deltaTime=1.0 / 120.0, regVelocityIters=10, regPositionIters=4))
+    _contacts_from_identical_transforms(g, worlds, [0, 1], min_contacts=3000)  # 4075 of them
+
+
 def test_disabled_body_has_no_proxy(gpu_lib):
     """A body created disabled gets no proxies (AabbTreeWorld.cpp:1040): it has no
     contacts although it overlaps others, and queries do not find its shapes."""
